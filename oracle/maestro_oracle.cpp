@@ -1,0 +1,1287 @@
+// Test infrastructure only: CPU oracle of the MAESTROeX scalar-advection stage (3-D,
+// planar geometry, one AMR level).  It restates, function by function, the reference's
+// AdvancePremac -> DensityAdvance -> EnthalpyAdvance call chain so that the GPU library
+// can be checked against it; it is never linked into or called by the product.
+//
+// Parity status: unpinned (see maestro_oracle.h).
+//
+// Build: -O2 -ffp-contract=off (no FMA contraction), no fast-math, so every expression is
+// evaluated in the reference's operation order with IEEE binary64 rounding.
+#include "maestro_oracle.h"
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "mo_fill.hpp"
+#include "mo_ppm.hpp"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace mo {
+
+static thread_local std::string g_err;
+
+struct Stage {
+    mo_params P;
+    Level L;
+    int nspec = 0, nscal = 0, nb = 0, nr = 0;
+    int ng_s = 3, ng_adv = 3;
+    std::vector<BCRec> bcs_s, bcs_u, bcs_f;
+    std::vector<double> rho0_old, rho0_new, rhoh0_old, rhoh0_new, p0_old, p0_new, psi, grav_cell,
+        w0_force, w0, rho0_predicted_edge;
+    MF w0_cart;  // 3 comps, 2 ghosts
+    MF gpi, thermal;
+    PPMCtx pc;
+    double dt = 0, rel_eps = 0;
+
+    // ------------------------------------------------------------------ setup
+    // Maestro::BCSetup (Source/MaestroSetup.cpp:276-500)
+    void BCSetup() {
+        bcs_s.assign(nscal, BCRec{});
+        bcs_u.assign(3, BCRec{});
+        bcs_f.assign(nscal, BCRec{});
+        for (int dir = 0; dir < 3; ++dir) {
+            for (int side = 0; side < 2; ++side) {
+                int pb = side == 0 ? P.phys_bc_lo[dir] : P.phys_bc_hi[dir];
+                auto set = [&](BCRec& r, int v) { (side == 0 ? r.lo : r.hi)[dir] = v; };
+                int u = 0, un = 0, s = 0, spi = 0, f = 0;
+                switch (pb) {
+                    case interior: u = un = s = spi = f = int_dir; break;
+                    case inflow: u = un = ext_dir; s = ext_dir; spi = foextrap; f = foextrap; break;
+                    case outflow: u = un = foextrap; s = foextrap; spi = ext_dir; f = foextrap; break;
+                    case symmetry: u = reflect_even; un = reflect_odd; s = spi = reflect_even; f = reflect_even; break;
+                    case slipwall: u = hoextrap; un = ext_dir; s = hoextrap; spi = foextrap; f = foextrap; break;
+                    case noslipwall: u = un = ext_dir; s = hoextrap; spi = foextrap; f = foextrap; break;
+                    default: throw std::runtime_error("invalid phys_bc");
+                }
+                for (int c = 0; c < 3; ++c) set(bcs_u[c], c == dir ? un : u);
+                for (int c = 0; c < nscal; ++c) set(bcs_s[c], c == Pi ? spi : s);
+                for (int c = 0; c < nscal; ++c) set(bcs_f[c], f);
+            }
+        }
+    }
+
+    // Maestro::Put1dArrayOnCart, planar branch (Source/MaestroFill3dData.cpp:9-93):
+    // valid cells from the 1-D array, then FillPatch of the ghost cells.
+    void Put1dArrayOnCart(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec,
+                          const std::vector<BCRec>* bcs, int bccomp, bool is_vel) {
+        const int outcomp = vec ? 2 : 0;
+        for (int b = 0; b < nb; ++b) {
+            const Arr& a = s0_cart[b];
+            MO_FOR3(L.ba[b]) {
+                const int r = k;
+                a(i, j, k, outcomp) = edge ? 0.5 * (s0[r] + s0[r + 1]) : s0[r];
+            }
+        }
+        if (s0_cart.ng > 0) {
+            int nc = vec ? 3 : 1;
+            FillPatch(L, s0_cart, 0, nc, bccomp, *bcs, is_vel);
+        }
+    }
+
+    // Maestro::CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), one level, one chunk.
+    static void CelltoEdge(const std::vector<double>& c, std::vector<double>& e) {
+        const int nr_lev = (int)c.size();
+        e.assign(nr_lev + 1, 0.0);
+        const int lo = 0, hi = nr_lev;
+        for (int r = lo; r <= hi; ++r) {
+            if (r == 0) {
+                e[r] = c[r];
+            } else if (r == 1 || r == lo) {
+                e[r] = 0.5 * (c[r - 1] + c[r]);
+            } else if (r == nr_lev) {
+                e[r] = c[r - 1];
+            } else if (r == nr_lev - 1 || r == hi) {
+                e[r] = 0.5 * (c[r] + c[r - 1]);
+            } else {
+                double tmp = 7.0 / 12.0 * (c[r] + c[r - 1]) - 1.0 / 12.0 * (c[r + 1] + c[r - 2]);
+                double s0min = mn(c[r], c[r - 1]);
+                double s0max = mx(c[r], c[r - 1]);
+                e[r] = mn(mx(tmp, s0min), s0max);
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------ face ghosts
+    // Maestro::FillUmacGhost (Source/MaestroFillData.cpp:176-453), one level.
+    void FillUmacGhost(MF* um) {
+        const int* dlo = L.dom.lo;
+        const int* dhi = L.dom.hi;
+        for (int b = 0; b < nb; ++b) {
+            const Arr& umac = um[0][b];
+            const Arr& vmac = um[1][b];
+            const Arr& wmac = um[2][b];
+            for (int dd = 0; dd < 3; ++dd) {
+                Box gb = grow(nodal(L.ba[b], dd), 1);
+                const int bclo = P.phys_bc_lo[dd], bchi = P.phys_bc_hi[dd];
+                MO_FOR3(gb) {
+                    const int I = dd == 0 ? i : (dd == 1 ? j : k);
+                    const int di = dd == 0, dj = dd == 1, dk = dd == 2;
+                    // q_n is the face velocity normal to dd, q_t the two tangential ones
+                    const Arr* comp[3] = {&umac, &vmac, &wmac};
+                    const Arr& qn = *comp[dd];
+                    if (I == dlo[dd] - 1) {
+                        switch (bclo) {
+                            case inflow:
+                                for (int c = 0; c < 3; ++c)
+                                    (*comp[c])(i, j, k) = c == dd ? qn(i + di, j + dj, k + dk) : 0.0;
+                                break;
+                            case slipwall:
+                            case noslipwall:
+                                for (int c = 0; c < 3; ++c) (*comp[c])(i, j, k) = 0.0;
+                                break;
+                            case outflow:
+                                for (int c = 0; c < 3; ++c)
+                                    (*comp[c])(i, j, k) = (*comp[c])(i + di, j + dj, k + dk);
+                                break;
+                            case symmetry:
+                                for (int c = 0; c < 3; ++c)
+                                    (*comp[c])(i, j, k) = c == dd ? -qn(i + 2 * di, j + 2 * dj, k + 2 * dk)
+                                                                  : (*comp[c])(i + di, j + dj, k + dk);
+                                break;
+                            default: break;
+                        }
+                    }
+                    if (I == dhi[dd] + 2) {
+                        switch (bchi) {
+                            case inflow:
+                                for (int c = 0; c < 3; ++c) {
+                                    if (c == dd) qn(i, j, k) = qn(i - di, j - dj, k - dk);
+                                    else (*comp[c])(i - di, j - dj, k - dk) = 0.0;
+                                }
+                                break;
+                            case slipwall:
+                            case noslipwall:
+                                for (int c = 0; c < 3; ++c) {
+                                    if (c == dd) qn(i, j, k) = 0.0;
+                                    else (*comp[c])(i - di, j - dj, k - dk) = 0.0;
+                                }
+                                break;
+                            case outflow:
+                                for (int c = 0; c < 3; ++c) {
+                                    if (c == dd) qn(i, j, k) = qn(i - di, j - dj, k - dk);
+                                    else (*comp[c])(i - di, j - dj, k - dk) = (*comp[c])(i - 2 * di, j - 2 * dj, k - 2 * dk);
+                                }
+                                break;
+                            case symmetry:
+                                for (int c = 0; c < 3; ++c) {
+                                    if (c == dd) qn(i, j, k) = -qn(i - 2 * di, j - 2 * dj, k - 2 * dk);
+                                    else (*comp[c])(i - di, j - dj, k - dk) = (*comp[c])(i - 2 * di, j - 2 * dj, k - 2 * dk);
+                                }
+                                break;
+                            default: break;
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    void FillFaceGhosts(MF* um) {
+        for (int d = 0; d < 3; ++d) FillBoundary(L, um[d], 0, 1, um[d].ng);
+        FillUmacGhost(um);
+    }
+
+    // Maestro::Addw0, planar (Source/MaestroFill3dData.cpp:357-462)
+    void Addw0(MF* uedge, double mult) {
+        for (int b = 0; b < nb; ++b) {
+            const Arr& wedge = uedge[2][b];
+            Box zbx = grow(grow(nodal(L.ba[b], 2), 0, 1), 1, 1);
+            MO_FOR3(zbx) { wedge(i, j, k) += mult * w0[k]; }
+        }
+        FillFaceGhosts(uedge);
+    }
+
+    // ------------------------------------------------------------------ MakeUtrans
+    // Maestro::MakeUtrans, 3-D (Source/MaestroMakeUtrans.cpp:6-56, 270-648)
+    void MakeUtrans(MF& utilde, MF& ufull, MF* utrans) {
+        const double dt2 = 0.5 * dt;
+        const int* domlo = L.dom.lo;
+        const int* domhi = L.dom.hi;
+        MF Ip, Im;
+        Ip.define(L.ba, 3, 2);
+        Im.define(L.ba, 3, 2);
+        MF& velsrc = (P.ppm_type == 0) ? utilde : ufull;  // u_mf / v_mf / w_mf copies
+        for (int d = 0; d < 3; ++d) {
+#pragma omp parallel for schedule(dynamic)
+            for (int b = 0; b < nb; ++b) {
+                const Box obx = grow(L.ba[b], 1);
+                const Box xbx = nodal(L.ba[b], d);
+                const Arr& ut = utilde[b];
+                const Arr& uf = ufull[b];
+                const Arr& Ipa = Ip[b];
+                const Arr& Ima = Im[b];
+                const Arr& tr = utrans[d][b];
+                const Arr& w0a = w0_cart[b];
+                if (P.ppm_type == 0) {
+                    Slope_dir(P.slope_order, L.dom, obx, velsrc[b].comp(d), Ipa, 1, bcs_u, d, d);
+                } else {
+                    PPM(pc, obx, ut, velsrc[b].comp(0), velsrc[b].comp(1), velsrc[b].comp(2), Ipa, Ima,
+                        bcs_u[d], false, d);
+                }
+                const int bclo = P.phys_bc_lo[d], bchi = P.phys_bc_hi[d];
+                const int di = d == 0, dj = d == 1, dk = d == 2;
+                MO_FOR3(xbx) {
+                    const int I = d == 0 ? i : (d == 1 ? j : k);
+                    double l = 0.0, r = 0.0;
+                    if (P.ppm_type == 0) {
+                        l = ut(i - di, j - dj, k - dk, d) +
+                            (0.5 - (dt2 / L.dx[d]) * mx(0.0, uf(i - di, j - dj, k - dk, d))) *
+                                Ipa(i - di, j - dj, k - dk, 0);
+                        r = ut(i, j, k, d) - (0.5 + (dt2 / L.dx[d]) * mn(0.0, uf(i, j, k, d))) * Ipa(i, j, k, 0);
+                    } else {
+                        l = Ipa(i - di, j - dj, k - dk, d);
+                        r = Ima(i, j, k, d);
+                    }
+                    if (I == domlo[d]) {
+                        switch (bclo) {
+                            case inflow: l = ut(i - di, j - dj, k - dk, d); r = ut(i - di, j - dj, k - dk, d); break;
+                            case slipwall: case noslipwall: case symmetry: l = 0.0; r = 0.0; break;
+                            case outflow: l = mn(r, 0.0); r = l; break;
+                            default: break;
+                        }
+                    } else if (I == domhi[d] + 1) {
+                        switch (bchi) {
+                            case inflow: l = ut(i + di, j + dj, k + dk, d); r = ut(i + di, j + dj, k + dk, d); break;
+                            case slipwall: case noslipwall: case symmetry: l = 0.0; r = 0.0; break;
+                            case outflow: l = mx(l, 0.0); r = l; break;
+                            default: break;
+                        }
+                    }
+                    if (d < 2) {
+                        bool test = (l <= 0.0 && r >= 0.0) || (fab(l + r) < rel_eps);
+                        double v = 0.5 * (l + r) > 0.0 ? l : r;
+                        tr(i, j, k) = test ? 0.0 : v;
+                    } else {
+                        const double w0c = w0a(i, j, k, 2);
+                        bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fab(l + r + 2.0 * w0c) < rel_eps);
+                        double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+                        tr(i, j, k) = test ? 0.0 : v;
+                    }
+                }
+            }
+        }
+        FillFaceGhosts(utrans);
+    }
+
+    // ------------------------------------------------------------------ MakeVelForce
+    // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-126, 250-259)
+    void MakeVelForce(MF& vel_force, MF* uedge, MF& sold, MF& w0_force_cart) {
+        MF grav_cart, rho0_cart;
+        grav_cart.define(L.ba, 3, 1, -1, 0.0);
+        rho0_cart.define(L.ba, 1, 1, -1, 0.0);
+        Put1dArrayOnCart(rho0_old, rho0_cart, false, false, &bcs_s, Rho, false);
+        Put1dArrayOnCart(grav_cell, grav_cart, false, true, &bcs_f, 0, false);
+        vel_force.setVal(0.0);
+        const int domhi = L.dom.hi[2];
+        for (int b = 0; b < nb; ++b) {
+            const Arr& gpi_arr = gpi[b];
+            const Arr& rho_arr = sold[b];
+            const Arr& wedge = uedge[2][b];
+            const Arr& w0_arr = w0_cart[b];
+            const Arr& w0f = w0_force_cart[b];
+            const Arr& grav = grav_cart[b];
+            const Arr& r0 = rho0_cart[b];
+            const Arr& vf = vel_force[b];
+            MO_FOR3(L.ba[b]) {
+                double rhopert = rho_arr(i, j, k) - r0(i, j, k);
+                if (rho_arr(i, j, k) < (P.buoyancy_cutoff_factor * P.base_cutoff_density)) rhopert = 0.0;
+                for (int dim = 0; dim < 2; ++dim) vf(i, j, k, dim) = -gpi_arr(i, j, k, dim) / rho_arr(i, j, k);
+                vf(i, j, k, 2) = (rhopert * grav(i, j, k, 2) - gpi_arr(i, j, k, 2)) / rho_arr(i, j, k) - w0f(i, j, k, 2);
+                if (k <= -1 || k >= domhi) {
+                } else {
+                    vf(i, j, k, 2) -= (wedge(i, j, k + 1) + wedge(i, j, k)) *
+                                      (w0_arr(i, j, k + 1, 2) - w0_arr(i, j, k, 2)) / (2.0 * L.dx[2]);
+                }
+            }
+        }
+        FillPatch(L, vel_force, 0, 3, 0, bcs_u, true);
+    }
+
+    // ------------------------------------------------------------------ VelPred
+    // Maestro::VelPred, 3-D (Source/MaestroVelPred.cpp:5-292, 735-1915)
+    void VelPred(MF& utilde, MF& ufull, MF* utrans, MF* umac, MF& force) {
+        const double dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt6 = dt / 6.0;
+        const int* domlo = L.dom.lo;
+        const int* domhi = L.dom.hi;
+        const double h[3] = {L.dx[0], L.dx[1], L.dx[2]};
+        // Ipu..Imw: per velocity component c, 3 directional comps, 1 ghost
+        MF Ipc[3], Imc[3];
+        for (int c = 0; c < 3; ++c) {
+            Ipc[c].define(L.ba, 3, 1);
+            Imc[c].define(L.ba, 3, 1);
+        }
+        MF ul[3], ur[3], uimh[3];  // ulx/urx/uimhx ... 3 comps, 1 ghost
+        for (int d = 0; d < 3; ++d) {
+            ul[d].define(L.ba, 3, 1);
+            ur[d].define(L.ba, 3, 1);
+            uimh[d].define(L.ba, 3, 1);
+        }
+        // transverse states q_{d|t} of component c = the third direction: index [c][d]
+        MF qimh[3][3];
+        for (int c = 0; c < 3; ++c)
+            for (int d = 0; d < 3; ++d)
+                if (c != d) qimh[c][d].define(L.ba, 1, 1);
+        MF& velsrc = (P.ppm_type == 0) ? utilde : ufull;
+#pragma omp parallel for schedule(dynamic)
+        for (int b = 0; b < nb; ++b) {
+            const Box obx = grow(L.ba[b], 1);
+            const Arr& ut = utilde[b];
+            const Arr& uf = ufull[b];
+            // PPM / slopes (:205-255)
+            if (P.ppm_type == 0) {
+                Slope_dir(P.slope_order, L.dom, obx, ut, Ipc[0][b], 3, bcs_u, 0, 0);  // slopex -> Ipu
+                Slope_dir(P.slope_order, L.dom, obx, ut, Imc[1][b], 3, bcs_u, 0, 1);  // slopey -> Imv
+                Slope_dir(P.slope_order, L.dom, obx, ut, Imc[2][b], 3, bcs_u, 0, 2);  // slopez -> Imw
+            } else {
+                for (int c = 0; c < 3; ++c)
+                    PPM(pc, obx, ut, velsrc[b].comp(0), velsrc[b].comp(1), velsrc[b].comp(2), Ipc[c][b], Imc[c][b],
+                        bcs_u[c], false, c);
+            }
+            // VelPredInterface (:735-1128)
+            for (int d = 0; d < 3; ++d) {
+                const Box mbx = growLo(obx, d, -1);
+                const int di = d == 0, dj = d == 1, dk = d == 2;
+                const int bclo = P.phys_bc_lo[d], bchi = P.phys_bc_hi[d];
+                const Arr& l = ul[d][b];
+                const Arr& r = ur[d][b];
+                const Arr& im = uimh[d][b];
+                const Arr& tr = utrans[d][b];
+                const Arr& slope = (d == 0) ? Ipc[0][b] : (d == 1 ? Imc[1][b] : Imc[2][b]);
+                MO_FOR3(mbx) {
+                    const int I = d == 0 ? i : (d == 1 ? j : k);
+                    if (P.ppm_type == 0) {
+                        double maxu = 0.5 - dt2 * mx(0.0, uf(i - di, j - dj, k - dk, d)) / h[d];
+                        double minu = 0.5 + dt2 * mn(0.0, uf(i, j, k, d)) / h[d];
+                        for (int n = 0; n < 3; ++n) {
+                            l(i, j, k, n) = ut(i - di, j - dj, k - dk, n) + maxu * slope(i - di, j - dj, k - dk, n);
+                            r(i, j, k, n) = ut(i, j, k, n) - minu * slope(i, j, k, n);
+                        }
+                    } else {
+                        for (int n = 0; n < 3; ++n) {
+                            l(i, j, k, n) = Ipc[n][b](i - di, j - dj, k - dk, d);
+                            r(i, j, k, n) = Imc[n][b](i, j, k, d);
+                        }
+                    }
+                    if (I == domlo[d]) {
+                        switch (bclo) {
+                            case inflow:
+                                for (int n = 0; n < 3; ++n) {
+                                    l(i, j, k, n) = ut(i - di, j - dj, k - dk, n);
+                                    r(i, j, k, n) = ut(i - di, j - dj, k - dk, n);
+                                }
+                                break;
+                            case slipwall:
+                            case symmetry:
+                                for (int n = 0; n < 3; ++n) {
+                                    if (n == d) { l(i, j, k, n) = 0.0; r(i, j, k, n) = 0.0; }
+                                    else l(i, j, k, n) = r(i, j, k, n);
+                                }
+                                break;
+                            case noslipwall:
+                                for (int n = 0; n < 3; ++n) { l(i, j, k, n) = 0.0; r(i, j, k, n) = 0.0; }
+                                break;
+                            case outflow:
+                                r(i, j, k, d) = mn(r(i, j, k, d), 0.0);
+                                for (int n = 0; n < 3; ++n) l(i, j, k, n) = r(i, j, k, n);
+                                break;
+                            default: break;
+                        }
+                    } else if (I == domhi[d] + 1) {
+                        switch (bchi) {
+                            case inflow:
+                                for (int n = 0; n < 3; ++n) {
+                                    l(i, j, k, n) = ut(i, j, k, n);
+                                    r(i, j, k, n) = ut(i, j, k, n);
+                                }
+                                break;
+                            case slipwall:
+                            case symmetry:
+                                for (int n = 0; n < 3; ++n) {
+                                    if (n == d) { l(i, j, k, n) = 0.0; r(i, j, k, n) = 0.0; }
+                                    else r(i, j, k, n) = l(i, j, k, n);
+                                }
+                                break;
+                            case noslipwall:
+                                for (int n = 0; n < 3; ++n) { l(i, j, k, n) = 0.0; r(i, j, k, n) = 0.0; }
+                                break;
+                            case outflow:
+                                l(i, j, k, d) = mx(l(i, j, k, d), 0.0);
+                                for (int n = 0; n < 3; ++n) r(i, j, k, n) = l(i, j, k, n);
+                                break;
+                            default: break;
+                        }
+                    }
+                    for (int n = 0; n < 3; ++n) {
+                        if (n == d) continue;
+                        double v = tr(i, j, k) > 0.0 ? l(i, j, k, n) : r(i, j, k, n);
+                        im(i, j, k, n) = fab(tr(i, j, k)) < rel_eps ? 0.5 * (l(i, j, k, n) + r(i, j, k, n)) : v;
+                    }
+                }
+            }
+            // VelPredTransverse (:1130-1595): component c on faces d, transverse t
+            for (int c = 0; c < 3; ++c)
+                for (int d = 0; d < 3; ++d) {
+                    if (c == d) continue;
+                    const int t = 3 - c - d;
+                    Box imhbox = growHi(grow(L.ba[b], c, 1), d, 1);
+                    const int di = d == 0, dj = d == 1, dk = d == 2;
+                    const int ti = t == 0, tj = t == 1, tk = t == 2;
+                    const int bclo = P.phys_bc_lo[d], bchi = P.phys_bc_hi[d];
+                    const Arr& l = ul[d][b];
+                    const Arr& r = ur[d][b];
+                    const Arr& trt = utrans[t][b];
+                    const Arr& imt = uimh[t][b];
+                    const Arr& trd = utrans[d][b];
+                    const Arr& out = qimh[c][d][b];
+                    MO_FOR3(imhbox) {
+                        const int I = d == 0 ? i : (d == 1 ? j : k);
+                        const int il = i - di, jl = j - dj, kl = k - dk;
+                        double lq = l(i, j, k, c) - (dt6 / h[t]) * (trt(il + ti, jl + tj, kl + tk) + trt(il, jl, kl)) *
+                                                        (imt(il + ti, jl + tj, kl + tk, c) - imt(il, jl, kl, c));
+                        double rq = r(i, j, k, c) - (dt6 / h[t]) * (trt(i + ti, j + tj, k + tk) + trt(i, j, k)) *
+                                                        (imt(i + ti, j + tj, k + tk, c) - imt(i, j, k, c));
+                        if (I == domlo[d]) {
+                            switch (bclo) {
+                                case inflow: lq = ut(il, jl, kl, c); rq = ut(il, jl, kl, c); break;
+                                case slipwall: case symmetry: case outflow: lq = rq; break;
+                                case noslipwall: lq = 0.0; rq = 0.0; break;
+                                default: break;
+                            }
+                        } else if (I == domhi[d] + 1) {
+                            switch (bchi) {
+                                case inflow: lq = ut(i, j, k, c); rq = ut(i, j, k, c); break;
+                                case slipwall: case symmetry: case outflow: rq = lq; break;
+                                case noslipwall: lq = 0.0; rq = 0.0; break;
+                                default: break;
+                            }
+                        }
+                        double v = trd(i, j, k) > 0.0 ? lq : rq;
+                        out(i, j, k) = fab(trd(i, j, k)) < rel_eps ? 0.5 * (lq + rq) : v;
+                    }
+                }
+            // VelPredVelocities (:1597-1915)
+            for (int d = 0; d < 3; ++d) {
+                const Box xbx = nodal(L.ba[b], d);
+                const int di = d == 0, dj = d == 1, dk = d == 2;
+                const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+                const int a1i = t1 == 0, a1j = t1 == 1, a1k = t1 == 2;
+                const int a2i = t2 == 0, a2j = t2 == 1, a2k = t2 == 2;
+                const Arr& l = ul[d][b];
+                const Arr& r = ur[d][b];
+                const Arr& tr1 = utrans[t1][b];
+                const Arr& tr2 = utrans[t2][b];
+                const Arr& q1 = qimh[d][t1][b];  // e.g. uimhyz for d = x
+                const Arr& q2 = qimh[d][t2][b];  // e.g. uimhzy
+                const Arr& f = force[b];
+                const Arr& out = umac[d][b];
+                const Arr& w0a = w0_cart[b];
+                const int bclo = P.phys_bc_lo[d], bchi = P.phys_bc_hi[d];
+                MO_FOR3(xbx) {
+                    const int I = d == 0 ? i : (d == 1 ? j : k);
+                    const int il = i - di, jl = j - dj, kl = k - dk;
+                    double fl = f(il, jl, kl, d);
+                    double fr = f(i, j, k, d);
+                    double ml = l(i, j, k, d) -
+                                (dt4 / h[t1]) * (tr1(il + a1i, jl + a1j, kl + a1k) + tr1(il, jl, kl)) *
+                                    (q1(il + a1i, jl + a1j, kl + a1k) - q1(il, jl, kl)) -
+                                (dt4 / h[t2]) * (tr2(il + a2i, jl + a2j, kl + a2k) + tr2(il, jl, kl)) *
+                                    (q2(il + a2i, jl + a2j, kl + a2k) - q2(il, jl, kl)) +
+                                dt2 * fl;
+                    double mr = r(i, j, k, d) -
+                                (dt4 / h[t1]) * (tr1(i + a1i, j + a1j, k + a1k) + tr1(i, j, k)) *
+                                    (q1(i + a1i, j + a1j, k + a1k) - q1(i, j, k)) -
+                                (dt4 / h[t2]) * (tr2(i + a2i, j + a2j, k + a2k) + tr2(i, j, k)) *
+                                    (q2(i + a2i, j + a2j, k + a2k) - q2(i, j, k)) +
+                                dt2 * fr;
+                    if (d < 2) {
+                        bool test = (ml <= 0.0 && mr >= 0.0) || (fab(ml + mr) < rel_eps);
+                        double v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+                        out(i, j, k) = test ? 0.0 : v;
+                    } else {
+                        const double w0c = w0a(i, j, k, 2);
+                        bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fab(ml + mr + 2.0 * w0c) < rel_eps);
+                        double v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+                        out(i, j, k) = test ? 0.0 : v;
+                    }
+                    if (I == domlo[d]) {
+                        switch (bclo) {
+                            case inflow: out(i, j, k) = ut(il, jl, kl, d); break;
+                            case slipwall: case symmetry: case noslipwall: out(i, j, k) = 0.0; break;
+                            case outflow: out(i, j, k) = mn(mr, 0.0); break;
+                            default: break;
+                        }
+                    } else if (I == domhi[d] + 1) {
+                        switch (bchi) {
+                            case inflow: out(i, j, k) = ut(i, j, k, d); break;
+                            case slipwall: case symmetry: case noslipwall: out(i, j, k) = 0.0; break;
+                            case outflow: out(i, j, k) = mx(ml, 0.0); break;
+                            default: break;
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------ AdvancePremac
+    // Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84)
+    void AdvancePremac(MF& uold, MF& sold, MF* umac, MF& w0_force_cart, MF* utrans, MF& vel_force) {
+        MF utilde, ufull;
+        utilde.define(L.ba, 3, ng_adv, -1, 0.0);
+        for (int b = 0; b < nb; ++b) {
+            MO_FOR3(L.ba[b]) for (int n = 0; n < 3; ++n) utilde[b](i, j, k, n) = uold[b](i, j, k, n);
+        }
+        FillPatch(L, utilde, 0, 3, 0, bcs_u, true);
+        ufull.define(L.ba, 3, ng_adv, -1, 0.0);
+        for (int b = 0; b < nb; ++b) {
+            MO_FOR3(L.ba[b]) for (int n = 0; n < 3; ++n) ufull[b](i, j, k, n) = w0_cart[b](i, j, k, n);
+        }
+        FillPatch(L, ufull, 0, 3, 0, bcs_u, true);
+        for (int b = 0; b < nb; ++b) {
+            MO_FOR3(grow(L.ba[b], ng_adv)) for (int n = 0; n < 3; ++n) ufull[b](i, j, k, n) += utilde[b](i, j, k, n);
+        }
+        for (int d = 0; d < 3; ++d) utrans[d].define(L.ba, 1, 1, d, 0.0);
+        MakeUtrans(utilde, ufull, utrans);
+        vel_force.define(L.ba, 3, 1, -1, 0.0);
+        MakeVelForce(vel_force, utrans, sold, w0_force_cart);
+        Addw0(utrans, 1.0);
+        VelPred(utilde, ufull, utrans, umac, vel_force);
+    }
+
+    // ------------------------------------------------------------------ MakeEdgeScal
+    // Maestro::MakeDivU (Source/MaestroMakeEdgeScalars.cpp:648-660)
+    void MakeDivU(const Box& bx, const Arr& divu, const Arr& u, const Arr& v, const Arr& w) {
+        MO_FOR3(bx) {
+            divu(i, j, k) = u(i + 1, j, k) - u(i, j, k) + v(i, j + 1, k) - v(i, j, k) + w(i, j, k + 1) - w(i, j, k);
+            divu(i, j, k) /= L.dx[0];
+        }
+    }
+
+    // Maestro::MakeEdgeScal, 3-D, is_vel = false (Source/MaestroMakeEdgeScalars.cpp:6-302,
+    // 662-1667).  BC overrides of the is_vel branches are kept for completeness.
+    void MakeEdgeScal(MF& state, MF* sedge, MF* umac, MF& force, const std::vector<BCRec>& bcs, int start_scomp,
+                      int start_bccomp, int num_comp, bool is_conservative) {
+        const bool is_vel = false;
+        const int* domlo = L.dom.lo;
+        const int* domhi = L.dom.hi;
+        const double h[3] = {L.dx[0], L.dx[1], L.dx[2]};
+        MF Ip, Im;
+        Ip.define(L.ba, 3, 1);
+        Im.define(L.ba, 3, 1);
+        MF sl[3], sr[3], simh[3];
+        for (int d = 0; d < 3; ++d) {
+            sl[d].define(L.ba, 1, 1, -1, 0.0);
+            sr[d].define(L.ba, 1, 1, -1, 0.0);
+            simh[d].define(L.ba, 1, 1, -1, 0.0);
+        }
+        MF slopez, divu;
+        slopez.define(L.ba, 1, 1);
+        divu.define(L.ba, 1, 1);
+        MF simh2[3][3];  // simh2[d][t]: d-faces corrected by t (simhxy = [0][1])
+        for (int d = 0; d < 3; ++d)
+            for (int t = 0; t < 3; ++t)
+                if (d != t) simh2[d][t].define(L.ba, 1, 1, -1, 0.0);
+        const double dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt3 = dt / 3.0, dt6 = dt / 6.0;
+
+        for (int scomp = start_scomp; scomp < start_scomp + num_comp; ++scomp) {
+            const int bccomp = start_bccomp + scomp - start_scomp;
+            const int comp = scomp;
+#pragma omp parallel for schedule(dynamic)
+            for (int b = 0; b < nb; ++b) {
+                const Box obx = grow(L.ba[b], 1);
+                if (is_conservative) MakeDivU(obx, divu[b], umac[0][b], umac[1][b], umac[2][b]);
+                if (P.ppm_type == 0) {
+                    Arr sc = state[b].comp(comp);
+                    sc.nc = 1;
+                    std::vector<BCRec> one(1, bcs[bccomp]);
+                    Slope_dir(P.slope_order, L.dom, obx, sc, Ip[b], 1, one, 0, 0);
+                    Slope_dir(P.slope_order, L.dom, obx, sc, Im[b], 1, one, 0, 1);
+                    Slope_dir(P.slope_order, L.dom, obx, sc, slopez[b], 1, one, 0, 2);
+                } else {
+                    PPM(pc, obx, state[b], umac[0][b], umac[1][b], umac[2][b], Ip[b], Im[b], bcs[bccomp], true, comp);
+                }
+            }
+            const int bc_lo[3] = {bcs[bccomp].lo[0], bcs[bccomp].lo[1], bcs[bccomp].lo[2]};
+            const int bc_hi[3] = {bcs[bccomp].hi[0], bcs[bccomp].hi[1], bcs[bccomp].hi[2]};
+#pragma omp parallel for schedule(dynamic)
+            for (int b = 0; b < nb; ++b) {
+                const Box obx = grow(L.ba[b], 1);
+                const Arr& scal = state[b];
+                const Arr* uu[3] = {&umac[0][b], &umac[1][b], &umac[2][b]};
+                // MakeEdgeScalPredictor (:662-863)
+                for (int d = 0; d < 3; ++d) {
+                    const Box mbx = growLo(obx, d, -1);
+                    const int di = d == 0, dj = d == 1, dk = d == 2;
+                    const Arr& l = sl[d][b];
+                    const Arr& r = sr[d][b];
+                    const Arr& sm = simh[d][b];
+                    const Arr& ud = *uu[d];
+                    const Arr& slope = d == 0 ? Ip[b] : (d == 1 ? Im[b] : slopez[b]);
+                    MO_FOR3(mbx) {
+                        const int I = d == 0 ? i : (d == 1 ? j : k);
+                        const int il = i - di, jl = j - dj, kl = k - dk;
+                        if (P.ppm_type == 0) {
+                            l(i, j, k) = scal(il, jl, kl, comp) + 0.5 * (1.0 - dt * ud(i, j, k) / h[d]) * slope(il, jl, kl, 0);
+                            r(i, j, k) = scal(i, j, k, comp) - 0.5 * (1.0 + dt * ud(i, j, k) / h[d]) * slope(i, j, k, 0);
+                        } else {
+                            l(i, j, k) = Ip[b](il, jl, kl, d);
+                            r(i, j, k) = Im[b](i, j, k, d);
+                        }
+                        if (I == domlo[d]) {
+                            int bclo = bc_lo[d];
+                            if (bclo == ext_dir) {
+                                l(i, j, k) = scal(il, jl, kl, comp);
+                                r(i, j, k) = scal(il, jl, kl, comp);
+                            } else if (bclo == foextrap || bclo == hoextrap) {
+                                if (is_vel && comp == d) r(i, j, k) = mn(r(i, j, k), 0.0);
+                                l(i, j, k) = r(i, j, k);
+                            } else if (bclo == reflect_even) {
+                                l(i, j, k) = r(i, j, k);
+                            } else if (bclo == reflect_odd) {
+                                l(i, j, k) = 0.0;
+                                r(i, j, k) = 0.0;
+                            }
+                        } else if (I == domhi[d] + 1) {
+                            int bchi = bc_hi[d];
+                            if (bchi == ext_dir) {
+                                l(i, j, k) = scal(i, j, k, comp);
+                                r(i, j, k) = scal(i, j, k, comp);
+                            } else if (bchi == foextrap || bchi == hoextrap) {
+                                if (is_vel && comp == d) l(i, j, k) = mx(l(i, j, k), 0.0);
+                                r(i, j, k) = l(i, j, k);
+                            } else if (bchi == reflect_even) {
+                                r(i, j, k) = l(i, j, k);
+                            } else if (bchi == reflect_odd) {
+                                l(i, j, k) = 0.0;
+                                r(i, j, k) = 0.0;
+                            }
+                        }
+                        sm(i, j, k) = (ud(i, j, k) > 0.0) ? l(i, j, k) : r(i, j, k);
+                        sm(i, j, k) = (fab(ud(i, j, k)) > 0.0) ? sm(i, j, k) : 0.5 * (l(i, j, k) + r(i, j, k));
+                    }
+                }
+                // MakeEdgeScalTransverse (:865-1359): d-faces corrected by direction t
+                for (int d = 0; d < 3; ++d)
+                    for (int t = 0; t < 3; ++t) {
+                        if (d == t) continue;
+                        const int o = 3 - d - t;
+                        Box imhbox = growHi(grow(L.ba[b], o, 1), d, 1);
+                        const int di = d == 0, dj = d == 1, dk = d == 2;
+                        const int ti = t == 0, tj = t == 1, tk = t == 2;
+                        const Arr& l = sl[d][b];
+                        const Arr& r = sr[d][b];
+                        const Arr& st = simh[t][b];
+                        const Arr& ut = *uu[t];
+                        const Arr& ud = *uu[d];
+                        const Arr& dv = divu[b];
+                        const Arr& out = simh2[d][t][b];
+                        MO_FOR3(imhbox) {
+                            const int I = d == 0 ? i : (d == 1 ? j : k);
+                            const int il = i - di, jl = j - dj, kl = k - dk;
+                            double lq, rq;
+                            if (is_conservative) {
+                                lq = l(i, j, k) -
+                                     (dt3 / h[t]) * (st(il + ti, jl + tj, kl + tk) * ut(il + ti, jl + tj, kl + tk) -
+                                                     st(il, jl, kl) * ut(il, jl, kl)) -
+                                     dt3 * scal(il, jl, kl, comp) * dv(il, jl, kl) +
+                                     (dt3 / h[t]) * scal(il, jl, kl, comp) *
+                                         (ut(il + ti, jl + tj, kl + tk) - ut(il, jl, kl));
+                                rq = r(i, j, k) -
+                                     (dt3 / h[t]) * (st(i + ti, j + tj, k + tk) * ut(i + ti, j + tj, k + tk) -
+                                                     st(i, j, k) * ut(i, j, k)) -
+                                     dt3 * scal(i, j, k, comp) * dv(i, j, k) +
+                                     (dt3 / h[t]) * scal(i, j, k, comp) * (ut(i + ti, j + tj, k + tk) - ut(i, j, k));
+                            } else {
+                                lq = l(i, j, k) - (dt6 / h[t]) * (ut(il + ti, jl + tj, kl + tk) + ut(il, jl, kl)) *
+                                                      (st(il + ti, jl + tj, kl + tk) - st(il, jl, kl));
+                                rq = r(i, j, k) - (dt6 / h[t]) * (ut(i + ti, j + tj, k + tk) + ut(i, j, k)) *
+                                                      (st(i + ti, j + tj, k + tk) - st(i, j, k));
+                            }
+                            if (I == domlo[d]) {
+                                int bclo = bc_lo[d];
+                                if (bclo == ext_dir) {
+                                    lq = scal(il, jl, kl, comp);
+                                    rq = scal(il, jl, kl, comp);
+                                } else if (bclo == foextrap || bclo == hoextrap) {
+                                    if (is_vel && comp == d) rq = mn(rq, 0.0);
+                                    lq = rq;
+                                } else if (bclo == reflect_even) {
+                                    lq = rq;
+                                } else if (bclo == reflect_odd) {
+                                    lq = 0.0;
+                                    rq = 0.0;
+                                }
+                            } else if (I == domhi[d] + 1) {
+                                int bchi = bc_hi[d];
+                                if (bchi == ext_dir) {
+                                    lq = scal(i, j, k, comp);
+                                    rq = scal(i, j, k, comp);
+                                } else if (bchi == foextrap || bchi == hoextrap) {
+                                    if (is_vel && comp == d) lq = mx(lq, 0.0);
+                                    rq = lq;
+                                } else if (bchi == reflect_even) {
+                                    rq = lq;
+                                } else if (bchi == reflect_odd) {
+                                    lq = 0.0;
+                                    rq = 0.0;
+                                }
+                            }
+                            out(i, j, k) = (ud(i, j, k) > 0.0) ? lq : rq;
+                            out(i, j, k) = (fab(ud(i, j, k)) > rel_eps) ? out(i, j, k) : 0.5 * (lq + rq);
+                        }
+                    }
+                // MakeEdgeScalEdges (:1361-1667)
+                for (int d = 0; d < 3; ++d) {
+                    const Box xbx = nodal(L.ba[b], d);
+                    const int di = d == 0, dj = d == 1, dk = d == 2;
+                    const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+                    const int a1i = t1 == 0, a1j = t1 == 1, a1k = t1 == 2;
+                    const int a2i = t2 == 0, a2j = t2 == 1, a2k = t2 == 2;
+                    const Arr& l = sl[d][b];
+                    const Arr& r = sr[d][b];
+                    const Arr& q1 = simh2[t1][t2][b];  // simhyz for d = x
+                    const Arr& q2 = simh2[t2][t1][b];  // simhzy for d = x
+                    const Arr& u1 = *uu[t1];
+                    const Arr& u2 = *uu[t2];
+                    const Arr& ud = *uu[d];
+                    const Arr& f = force[b];
+                    const Arr& se = sedge[d][b];
+                    MO_FOR3(xbx) {
+                        const int I = d == 0 ? i : (d == 1 ? j : k);
+                        const int il = i - di, jl = j - dj, kl = k - dk;
+                        double fl = f(il, jl, kl, comp);
+                        double fr = f(i, j, k, comp);
+                        double lq, rq;
+                        if (is_conservative) {
+                            lq = l(i, j, k) -
+                                 (dt2 / h[t1]) * (q1(il + a1i, jl + a1j, kl + a1k) * u1(il + a1i, jl + a1j, kl + a1k) -
+                                                  q1(il, jl, kl) * u1(il, jl, kl)) -
+                                 (dt2 / h[t2]) * (q2(il + a2i, jl + a2j, kl + a2k) * u2(il + a2i, jl + a2j, kl + a2k) -
+                                                  q2(il, jl, kl) * u2(il, jl, kl)) -
+                                 (dt2 / h[d]) * scal(il, jl, kl, comp) * (ud(i, j, k) - ud(il, jl, kl)) + dt2 * fl;
+                            rq = r(i, j, k) -
+                                 (dt2 / h[t1]) * (q1(i + a1i, j + a1j, k + a1k) * u1(i + a1i, j + a1j, k + a1k) -
+                                                  q1(i, j, k) * u1(i, j, k)) -
+                                 (dt2 / h[t2]) * (q2(i + a2i, j + a2j, k + a2k) * u2(i + a2i, j + a2j, k + a2k) -
+                                                  q2(i, j, k) * u2(i, j, k)) -
+                                 (dt2 / h[d]) * scal(i, j, k, comp) * (ud(i + di, j + dj, k + dk) - ud(i, j, k)) +
+                                 dt2 * fr;
+                        } else {
+                            lq = l(i, j, k) -
+                                 (dt4 / h[t1]) * (u1(il + a1i, jl + a1j, kl + a1k) + u1(il, jl, kl)) *
+                                     (q1(il + a1i, jl + a1j, kl + a1k) - q1(il, jl, kl)) -
+                                 (dt4 / h[t2]) * (u2(il + a2i, jl + a2j, kl + a2k) + u2(il, jl, kl)) *
+                                     (q2(il + a2i, jl + a2j, kl + a2k) - q2(il, jl, kl)) +
+                                 dt2 * fl;
+                            rq = r(i, j, k) -
+                                 (dt4 / h[t1]) * (u1(i + a1i, j + a1j, k + a1k) + u1(i, j, k)) *
+                                     (q1(i + a1i, j + a1j, k + a1k) - q1(i, j, k)) -
+                                 (dt4 / h[t2]) * (u2(i + a2i, j + a2j, k + a2k) + u2(i, j, k)) *
+                                     (q2(i + a2i, j + a2j, k + a2k) - q2(i, j, k)) +
+                                 dt2 * fr;
+                        }
+                        double v = (ud(i, j, k) > 0.0) ? lq : rq;
+                        v = (fab(ud(i, j, k)) > rel_eps) ? v : 0.5 * (lq + rq);
+                        if (I == domlo[d]) {
+                            int bclo = bc_lo[d];
+                            if (bclo == ext_dir) v = scal(il, jl, kl, comp);
+                            else if (bclo == foextrap || bclo == hoextrap) v = (is_vel && comp == d) ? mn(rq, 0.0) : rq;
+                            else if (bclo == reflect_even) v = rq;
+                            else if (bclo == reflect_odd) v = 0.0;
+                        } else if (I == domhi[d] + 1) {
+                            int bchi = bc_hi[d];
+                            if (bchi == ext_dir) v = scal(i, j, k, comp);
+                            else if (bchi == foextrap || bchi == hoextrap) v = (is_vel && comp == d) ? mx(lq, 0.0) : lq;
+                            else if (bchi == reflect_even) v = lq;
+                            else if (bchi == reflect_odd) v = 0.0;
+                        }
+                        se(i, j, k, comp) = v;
+                    }
+                }
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------ forces
+    // Maestro::ModifyScalForce, planar 3-D (Source/MaestroForce.cpp:261-467)
+    void ModifyScalForce(MF& scal_force, MF& state, MF* umac, const std::vector<double>& s0_edge, MF& s0_cart,
+                         int comp, int fullform) {
+        MF s0_edge_cart;
+        s0_edge_cart.define(L.ba, 1, 1);
+        Put1dArrayOnCart(s0_edge, s0_edge_cart, false, false, &bcs_f, 0, false);
+        const double* dx = L.dx;
+        for (int b = 0; b < nb; ++b) {
+            const Arr scal = state[b].comp(comp);
+            const Arr& um = umac[0][b];
+            const Arr& vm = umac[1][b];
+            const Arr& wm = umac[2][b];
+            const Arr& s0a = s0_cart[b];
+            const Arr& s0e = s0_edge_cart[b];
+            const Arr& w0a = w0_cart[b];
+            const Arr force = scal_force[b].comp(comp);
+            MO_FOR3(L.ba[b]) {
+                double divu = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
+                              (wm(i, j, k + 1) - wm(i, j, k)) / dx[2];
+                divu += (w0a(i, j, k + 1, 2) - w0a(i, j, k, 2)) / dx[2];
+                if (fullform == 1) {
+                    force(i, j, k) -= scal(i, j, k) * divu;
+                } else {
+                    double divs0u = s0a(i, j, k) * ((um(i + 1, j, k) - um(i, j, k)) / dx[0] +
+                                                    (vm(i, j + 1, k) - vm(i, j, k)) / dx[1]) +
+                                    (wm(i, j, k + 1) * s0e(i, j, k + 1) - wm(i, j, k) * s0e(i, j, k)) / dx[2];
+                    force(i, j, k) += -(scal(i, j, k) - s0a(i, j, k)) * divu - divs0u;
+                }
+            }
+        }
+        FillPatch(L, scal_force, comp, 1, 0, bcs_f, false);
+    }
+
+    // Maestro::MakeRhoHForce, planar 3-D (Source/MaestroForce.cpp:469-679)
+    void MakeRhoHForce(MF& scal_force, int is_prediction, MF* umac, int add_thermal, int which_step) {
+        std::vector<double> r0(nr), pp0(nr);
+        for (int r = 0; r < nr; ++r) {
+            r0[r] = which_step == 1 ? rho0_old[r] : 0.5 * (rho0_old[r] + rho0_new[r]);
+            pp0[r] = which_step == 1 ? p0_old[r] : 0.5 * (p0_old[r] + p0_new[r]);
+        }
+        MF p0_cart, psi_cart, grav_cart, rho0_cart;
+        p0_cart.define(L.ba, 1, 1, -1, 0.0);
+        psi_cart.define(L.ba, 1, 1, -1, 0.0);
+        grav_cart.define(L.ba, 1, 1, -1, 0.0);
+        rho0_cart.define(L.ba, 1, 1, -1, 0.0);
+        Put1dArrayOnCart(pp0, p0_cart, false, false, &bcs_f, 0, false);
+        Put1dArrayOnCart(psi, psi_cart, false, false, &bcs_f, 0, false);
+        Put1dArrayOnCart(r0, rho0_cart, false, false, &bcs_s, Rho, false);
+        Put1dArrayOnCart(grav_cell, grav_cart, false, false, &bcs_f, 0, false);  // MakeGravCell, planar constant
+        const int domhi = L.dom.hi[2];
+        const int cutoff = P.base_cutoff_density_coord;
+        const bool psi_in = (is_prediction == 1 && P.enthalpy_pred_type == 2) ||
+                            (is_prediction == 1 && P.enthalpy_pred_type == 0) || (is_prediction == 0);
+        for (int b = 0; b < nb; ++b) {
+            const Arr& wm = umac[2][b];
+            const Arr& p0c = p0_cart[b];
+            const Arr& th = thermal[b];
+            const Arr& ps = psi_cart[b];
+            const Arr& gc = grav_cart[b];
+            const Arr& rc = rho0_cart[b];
+            const Arr rf = scal_force[b].comp(RhoH);
+            MO_FOR3(L.ba[b]) {
+                double gradp0 = 0.0;
+                if (k < cutoff) {
+                    gradp0 = rc(i, j, k) * gc(i, j, k);
+                } else if (k == domhi) {
+                    gradp0 = (p0c(i, j, k) - p0c(i, j - 1, k)) / L.dx[2];
+                } else {
+                    gradp0 = (p0c(i, j + 1, k) - p0c(i, j, k)) / L.dx[2];
+                }
+                double veladv = 0.5 * (wm(i, j, k) + wm(i, j, k + 1));
+                rf(i, j, k) = veladv * gradp0;
+                if (psi_in) rf(i, j, k) += ps(i, j, k);
+                if (add_thermal == 1) rf(i, j, k) += th(i, j, k);
+            }
+        }
+        FillPatch(L, scal_force, RhoH, 1, 0, bcs_f, false);
+    }
+
+    // ------------------------------------------------------------------ conversions
+    // Maestro::PutInPertForm (Source/MaestroConvert.cpp:6-34)
+    void PutInPertForm(MF& scal, const std::vector<double>& s0, int comp, int bccomp, const std::vector<BCRec>& bcs,
+                       bool flag) {
+        for (int b = 0; b < nb; ++b) {
+            const Arr& a = scal[b];
+            MO_FOR3(L.ba[b]) {
+                const double s0c = s0[k];
+                if (flag) a(i, j, k, comp) = a(i, j, k, comp) - s0c;
+                else a(i, j, k, comp) = a(i, j, k, comp) + s0c;
+            }
+        }
+        FillPatch(L, scal, comp, 1, bccomp, bcs, false, comp);
+    }
+
+    // Maestro::ConvertRhoXToX (Source/MaestroConvert.cpp:64-91)
+    void ConvertRhoXToX(MF& scal, bool flag) {
+        for (int b = 0; b < nb; ++b) {
+            const Arr& a = scal[b];
+            for (int comp = FirstSpec; comp < FirstSpec + nspec; ++comp)
+                MO_FOR3(L.ba[b]) {
+                    if (flag) a(i, j, k, comp) = a(i, j, k, comp) / a(i, j, k, Rho);
+                    else a(i, j, k, comp) = a(i, j, k, comp) * a(i, j, k, Rho);
+                }
+        }
+        if (flag) FillPatch(L, scal, FirstSpec, nspec, 0, bcs_f, false, FirstSpec);
+        else FillPatch(L, scal, FirstSpec, nspec, FirstSpec, bcs_s, false, FirstSpec);
+    }
+
+    // ------------------------------------------------------------------ fluxes
+    // Maestro::MakeRhoXFlux, planar 3-D (Source/MaestroMakeFlux.cpp:18-465)
+    void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<double>& r0_old,
+                      const std::vector<double>& r0e_old, const std::vector<double>& r0_new,
+                      const std::vector<double>& r0e_new, int start_comp, int num_comp) {
+        const int spt = P.species_pred_type;
+        for (int d = 0; d < 3; ++d) sflux[d].setVal(0.0, Rho, 1, 0);
+        for (int b = 0; b < nb; ++b) {
+            for (int d = 0; d < 3; ++d) {
+                const Arr& f = sflux[d][b];
+                const Arr& e = sedge[d][b];
+                const Arr& u = umac[d][b];
+                const Arr& eta = etarhoflux[b];
+                MO_FOR3(nodal(L.ba[b], d)) {
+                    for (int comp = start_comp; comp < num_comp + start_comp; ++comp) {
+                        double rho0_edge = d < 2 ? 0.5 * (r0_old[k] + r0_new[k]) : 0.5 * (r0e_old[k] + r0e_new[k]);
+                        if (spt == 1) {
+                            f(i, j, k, comp) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, comp);
+                        } else if (spt == 2) {
+                            f(i, j, k, comp) = u(i, j, k) * e(i, j, k, comp);
+                        } else if (spt == 3) {
+                            f(i, j, k, comp) = u(i, j, k) * e(i, j, k, Rho) * e(i, j, k, comp);
+                        }
+                        if (d == 2 && P.evolve_base_state && !P.use_exact_base_state) {
+                            if (comp >= FirstSpec && comp <= FirstSpec + nspec - 1) eta(i, j, k) += f(i, j, k, comp);
+                            if (comp == FirstSpec + nspec - 1) eta(i, j, k) -= w0[k] * rho0_predicted_edge[k];
+                        }
+                        f(i, j, k, Rho) += f(i, j, k, comp);
+                    }
+                }
+            }
+        }
+    }
+
+    // Maestro::MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:467-1067)
+    void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<double>& rh0_old,
+                      const std::vector<double>& rh0e_old, const std::vector<double>& rh0_new,
+                      const std::vector<double>& rh0e_new) {
+        const int ept = P.enthalpy_pred_type;
+        for (int b = 0; b < nb; ++b)
+            for (int d = 0; d < 3; ++d) {
+                const Arr& f = sflux[d][b];
+                const Arr& e = sedge[d][b];
+                const Arr& u = umac[d][b];
+                MO_FOR3(nodal(L.ba[b], d)) {
+                    if (ept == 0) {
+                        f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, RhoH);
+                    } else if (ept == 1) {
+                        if (d < 2) {
+                            double rhoh0_edge = 0.5 * (rh0_old[k] + rh0_new[k]);
+                            f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
+                        } else {
+                            double rhoh0_edge = 0.5 * (rh0e_old[k] + rh0e_new[k]);
+                            f(i, j, k, RhoH) = u(i, j, k) * (e(i, j, k, RhoH) + rhoh0_edge);
+                        }
+                    }
+                }
+            }
+    }
+
+    // ------------------------------------------------------------------ UpdateScal
+    // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297), one level
+    void UpdateScal(MF& sold, MF& snew, MF* sflux, MF& force, int start_comp, int num_comp) {
+        const double* dx = L.dx;
+        const double dt_loc = dt;
+        for (int b = 0; b < nb; ++b) {
+            const Arr& so = sold[b];
+            const Arr& sn = snew[b];
+            const Arr& fx = sflux[0][b];
+            const Arr& fy = sflux[1][b];
+            const Arr& fz = sflux[2][b];
+            const Arr& fo = force[b];
+            if (start_comp == RhoH) {
+                MO_FOR3(L.ba[b]) {
+                    double divterm = ((fx(i + 1, j, k, RhoH) - fx(i, j, k, RhoH)) / dx[0] +
+                                      (fy(i, j + 1, k, RhoH) - fy(i, j, k, RhoH)) / dx[1] +
+                                      (fz(i, j, k + 1, RhoH) - fz(i, j, k, RhoH)) / dx[2]);
+                    sn(i, j, k, RhoH) = so(i, j, k, RhoH) + dt_loc * (-divterm + fo(i, j, k, RhoH));
+                    if (P.do_eos_h_above_cutoff && sn(i, j, k, Rho) <= P.base_cutoff_density)
+                        throw std::runtime_error("UpdateScal: cell at or below base_cutoff_density needs the EOS");
+                }
+            } else {
+                for (int n = 0; n < nspec; ++n) {
+                    const int comp = FirstSpec + n;
+                    MO_FOR3(L.ba[b]) {
+                        double divterm = (fx(i + 1, j, k, comp) - fx(i, j, k, comp)) / dx[0];
+                        divterm += (fy(i, j + 1, k, comp) - fy(i, j, k, comp)) / dx[1];
+                        divterm += (fz(i, j, k + 1, comp) - fz(i, j, k, comp)) / dx[2];
+                        sn(i, j, k, comp) = so(i, j, k, comp) + dt_loc * (-divterm + fo(i, j, k, comp));
+                    }
+                }
+                MO_FOR3(L.ba[b]) {
+                    sn(i, j, k, Rho) = so(i, j, k, Rho);
+                    bool has_negative_species = false;
+                    for (int comp = start_comp; comp < start_comp + nspec; ++comp) {
+                        sn(i, j, k, Rho) += sn(i, j, k, comp) - so(i, j, k, comp);
+                        if (sn(i, j, k, comp) < 0.0) has_negative_species = true;
+                    }
+                    if (sn(i, j, k, Rho) < 0.5 * P.base_cutoff_density) {
+                        for (int comp = start_comp; comp < start_comp + nspec; ++comp)
+                            sn(i, j, k, comp) *= 0.5 * P.base_cutoff_density / sn(i, j, k, Rho);
+                        sn(i, j, k, Rho) = 0.5 * P.base_cutoff_density;
+                    }
+                    if (has_negative_species) {
+                        for (int comp = start_comp; comp < start_comp + nspec; ++comp) {
+                            if (sn(i, j, k, comp) < 0.0) {
+                                double delta = -sn(i, j, k, comp);
+                                double sumX = 0.0;
+                                for (int comp2 = start_comp; comp2 < start_comp + nspec; ++comp2)
+                                    if (comp2 != comp && sn(i, j, k, comp2) >= 0.0) sumX += sn(i, j, k, comp2);
+                                for (int comp2 = start_comp; comp2 < start_comp + nspec; ++comp2)
+                                    if (comp2 != comp && sn(i, j, k, comp2) >= 0.0) {
+                                        double frac = sn(i, j, k, comp2) / sumX;
+                                        sn(i, j, k, comp2) -= frac * delta;
+                                    }
+                                sn(i, j, k, comp) = 0.0;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        (void)num_comp;
+        FillPatch(L, snew, start_comp, num_comp, start_comp, bcs_s, false, start_comp);
+        if (start_comp == FirstSpec) FillPatch(L, snew, Rho, 1, Rho, bcs_s, false, Rho);
+    }
+
+    // ------------------------------------------------------------------ drivers
+    // Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243)
+    void DensityAdvance(MF& scalold, MF& scalnew, MF* sedge, MF* sflux, MF& scal_force, MF& etarhoflux, MF* umac) {
+        std::vector<double> rho0_edge_old, rho0_edge_new;
+        CelltoEdge(rho0_old, rho0_edge_old);
+        CelltoEdge(rho0_new, rho0_edge_new);
+        scal_force.setVal(0.0);
+        MF rho0_old_cart;
+        rho0_old_cart.define(L.ba, 1, 1, -1, 0.0);
+        Put1dArrayOnCart(rho0_old, rho0_old_cart, false, false, &bcs_s, Rho, false);
+        Addw0(umac, -1.0);
+        if (P.species_pred_type == 1) ModifyScalForce(scal_force, scalold, umac, rho0_edge_old, rho0_old_cart, Rho, 0);
+        else if (P.species_pred_type == 3) ModifyScalForce(scal_force, scalold, umac, rho0_edge_old, rho0_old_cart, Rho, 1);
+        Addw0(umac, 1.0);
+        if (P.species_pred_type == 1 || P.species_pred_type == 3) ConvertRhoXToX(scalold, true);
+        if (P.species_pred_type == 1) PutInPertForm(scalold, rho0_old, Rho, 0, bcs_f, true);
+        if (P.species_pred_type == 1 || P.species_pred_type == 3)
+            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, FirstSpec, FirstSpec, nspec, false);
+        else
+            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, FirstSpec, FirstSpec, nspec, true);
+        if (P.species_pred_type == 1 || P.species_pred_type == 3) {
+            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, Rho, Rho, 1, false);
+        } else {
+            for (int d = 0; d < 3; ++d)
+                for (int b = 0; b < nb; ++b) {
+                    const Arr& e = sedge[d][b];
+                    MO_FOR3(nodal(L.ba[b], d)) {
+                        e(i, j, k, Rho) = e(i, j, k, FirstSpec);
+                        for (int ispec = 1; ispec < nspec; ++ispec) e(i, j, k, Rho) += e(i, j, k, FirstSpec + ispec);
+                    }
+                }
+        }
+        if (P.species_pred_type == 1) PutInPertForm(scalold, rho0_old, Rho, Rho, bcs_s, false);
+        if (P.species_pred_type == 1 || P.species_pred_type == 3) ConvertRhoXToX(scalold, false);
+        MakeRhoXFlux(sflux, etarhoflux, sedge, umac, rho0_old, rho0_edge_old, rho0_old, rho0_edge_old, FirstSpec,
+                     nspec);
+        scal_force.setVal(0.0);
+        UpdateScal(scalold, scalnew, sflux, scal_force, FirstSpec, nspec);
+    }
+
+    // Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352)
+    void EnthalpyAdvance(MF& scalold, MF& scalnew, MF* sedge, MF* sflux, MF& scal_force, MF* umac) {
+        std::vector<double> rho0_edge_old, rho0_edge_new, rhoh0_edge_old, rhoh0_edge_new;
+        CelltoEdge(rho0_old, rho0_edge_old);
+        CelltoEdge(rho0_new, rho0_edge_new);
+        CelltoEdge(rhoh0_old, rhoh0_edge_old);
+        CelltoEdge(rhoh0_new, rhoh0_edge_new);
+        scal_force.setVal(0.0);
+        MF rhoh0_old_cart;
+        rhoh0_old_cart.define(L.ba, 1, 1, -1, 0.0);
+        Addw0(umac, -1.0);
+        if (P.enthalpy_pred_type == 1) {
+            MakeRhoHForce(scal_force, 1, umac, 1, 1);
+            Put1dArrayOnCart(rhoh0_old, rhoh0_old_cart, false, false, &bcs_s, RhoH, false);
+            ModifyScalForce(scal_force, scalold, umac, rhoh0_edge_old, rhoh0_old_cart, RhoH, 0);
+        } else {
+            MakeRhoHForce(scal_force, 1, umac, 1, 1);
+        }
+        Addw0(umac, 1.0);
+        if (P.enthalpy_pred_type == 1) PutInPertForm(scalold, rhoh0_old, RhoH, 0, bcs_f, true);
+        MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, RhoH, RhoH, 1, P.enthalpy_pred_type == 0);
+        if (P.enthalpy_pred_type == 1) PutInPertForm(scalold, rhoh0_old, RhoH, RhoH, bcs_s, false);
+        MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_old, rhoh0_edge_old);
+        scal_force.setVal(0.0, RhoH, 1, 1);
+        Addw0(umac, -1.0);
+        MakeRhoHForce(scal_force, 0, umac, 0, 1);
+        Addw0(umac, 1.0);
+        UpdateScal(scalold, scalnew, sflux, scal_force, RhoH, 1);
+    }
+};
+
+// ---------------------------------------------------------------------- flat I/O
+static long ncell_of(const Box& d) {
+    return (long)(d.hi[0] - d.lo[0] + 1) * (d.hi[1] - d.lo[1] + 1) * (d.hi[2] - d.lo[2] + 1);
+}
+static void face_ext(const Box& dom, int d, long ext[3]) {
+    for (int e = 0; e < 3; ++e) ext[e] = dom.hi[e] - dom.lo[e] + 1 + (e == d ? 1 : 0);
+}
+// scatter domain-flat cell data [nc][ncell] into the valid region of an MF
+static void scatter_cells(const Box& dom, const double* src, MF& mf, int c0, int nc) {
+    long nx = dom.hi[0] - dom.lo[0] + 1, ny = dom.hi[1] - dom.lo[1] + 1, N = ncell_of(dom);
+    for (int b = 0; b < mf.size(); ++b)
+        for (int n = 0; n < nc; ++n) MO_FOR3(mf.ba[b]) {
+                long idx = (i - dom.lo[0]) + nx * ((j - dom.lo[1]) + ny * (long)(k - dom.lo[2]));
+                mf[b](i, j, k, c0 + n) = src[(long)n * N + idx];
+            }
+}
+static void gather_cells(const Box& dom, const MF& mf, int c0, int nc, double* dst) {
+    long nx = dom.hi[0] - dom.lo[0] + 1, ny = dom.hi[1] - dom.lo[1] + 1, N = ncell_of(dom);
+    for (int b = 0; b < mf.size(); ++b)
+        for (int n = 0; n < nc; ++n) MO_FOR3(mf.ba[b]) {
+                long idx = (i - dom.lo[0]) + nx * ((j - dom.lo[1]) + ny * (long)(k - dom.lo[2]));
+                dst[(long)n * N + idx] = mf[b](i, j, k, c0 + n);
+            }
+}
+static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, double* dst) {
+    long ext[3];
+    face_ext(dom, d, ext);
+    long N = ext[0] * ext[1] * ext[2];
+    for (int b = 0; b < mf.size(); ++b) {
+        Box vb = nodal(mf.ba[b], d);
+        for (int n = 0; n < nc; ++n) MO_FOR3(vb) {
+                long idx = (i - dom.lo[0]) + ext[0] * ((j - dom.lo[1]) + ext[1] * (long)(k - dom.lo[2]));
+                dst[(long)n * N + idx] = mf[b](i, j, k, c0 + n);
+            }
+    }
+}
+
+static int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out) {
+    Stage S;
+    S.P = *p;
+    S.nspec = p->nspec;
+    S.nscal = 4 + p->nspec;
+    for (int d = 0; d < 3; ++d) {
+        S.L.dom.lo[d] = p->dom_lo[d];
+        S.L.dom.hi[d] = p->dom_hi[d];
+        S.L.per[d] = (p->phys_bc_lo[d] == interior);
+        if ((p->phys_bc_lo[d] == interior) != (p->phys_bc_hi[d] == interior))
+            throw std::runtime_error("periodic direction needs interior on both sides");
+        S.L.dx[d] = p->dx[d];
+    }
+    if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
+    if (p->use_exact_base_state) throw std::runtime_error("use_exact_base_state is spherical-only");
+    if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
+        throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
+    if (!(p->species_pred_type >= 1 && p->species_pred_type <= 3))
+        throw std::runtime_error("species_pred_type must be 1, 2 or 3");
+    for (int b = 0; b < nboxes; ++b) {
+        Box bx;
+        for (int d = 0; d < 3; ++d) {
+            bx.lo[d] = boxes[6 * b + d];
+            bx.hi[d] = boxes[6 * b + 3 + d];
+        }
+        S.L.ba.push_back(bx);
+    }
+    S.nb = nboxes;
+    S.nr = p->dom_hi[2] - p->dom_lo[2] + 1;
+    S.ng_s = p->ppm_type == 2 ? 4 : 3;
+    S.ng_adv = p->ppm_type == 2 ? 4 : 3;
+    S.dt = p->dt;
+    S.rel_eps = p->rel_eps;
+    S.pc = PPMCtx{p->ppm_type, p->dt, p->rel_eps, {p->dx[0], p->dx[1], p->dx[2]}, S.L.dom};
+    S.BCSetup();
+    const int nr = S.nr;
+    auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
+    S.rho0_old = vec(in->rho0_old, nr);
+    S.rho0_new = vec(in->rho0_new, nr);
+    S.rhoh0_old = vec(in->rhoh0_old, nr);
+    S.rhoh0_new = vec(in->rhoh0_new, nr);
+    S.p0_old = vec(in->p0_old, nr);
+    S.p0_new = vec(in->p0_new, nr);
+    S.psi = vec(in->psi, nr);
+    S.grav_cell = vec(in->grav_cell, nr);
+    S.w0_force = vec(in->w0_force, nr);
+    S.w0 = vec(in->w0, nr + 1);
+    S.rho0_predicted_edge = vec(in->rho0_predicted_edge, nr + 1);
+    const Box& dom = S.L.dom;
+
+    // w0_cart: Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1) (Source/MaestroAdvance.cpp:326)
+    S.w0_cart.define(S.L.ba, 3, 2, -1, 0.0);
+    S.Put1dArrayOnCart(S.w0, S.w0_cart, true, true, &S.bcs_u, 0, true);
+    MF w0_force_cart;
+    w0_force_cart.define(S.L.ba, 3, 1, -1, 0.0);
+    if (p->evolve_base_state) S.Put1dArrayOnCart(S.w0_force, w0_force_cart, false, true, &S.bcs_f, 0, false);
+
+    MF uold, sold, snew;
+    uold.define(S.L.ba, 3, S.ng_s, -1, 0.0);
+    sold.define(S.L.ba, S.nscal, S.ng_s, -1, 0.0);
+    snew.define(S.L.ba, S.nscal, S.ng_s, -1, 0.0);
+    S.gpi.define(S.L.ba, 3, 0, -1, 0.0);
+    S.thermal.define(S.L.ba, 1, 1, -1, 0.0);
+    scatter_cells(dom, in->uold, uold, 0, 3);
+    scatter_cells(dom, in->sold, sold, 0, S.nscal);
+    scatter_cells(dom, in->gpi, S.gpi, 0, 3);
+    if (in->thermal) scatter_cells(dom, in->thermal, S.thermal, 0, 1);
+
+    MF umac[3], utrans[3], sedge[3], sflux[3], etarhoflux, scal_force, vel_force;
+    for (int d = 0; d < 3; ++d) {
+        umac[d].define(S.L.ba, 1, 1, d, 0.0);
+        sedge[d].define(S.L.ba, S.nscal, 0, d, 0.0);
+        sflux[d].define(S.L.ba, S.nscal, 0, d, 0.0);
+    }
+    etarhoflux.define(S.L.ba, 1, 0, 2, 0.0);
+    scal_force.define(S.L.ba, S.nscal, 1, -1, 0.0);
+
+    // sold ghost cells as the previous step's UpdateScal leaves them
+    FillPatch(S.L, sold, 0, S.nscal, 0, S.bcs_s, false, 0);
+
+    // STEP 3: AdvancePremac (MacProj skipped)
+    S.AdvancePremac(uold, sold, umac, w0_force_cart, utrans, vel_force);
+    if (out->utrans[0])
+        for (int d = 0; d < 3; ++d) gather_faces(dom, utrans[d], d, 0, 1, out->utrans[d]);
+    if (out->umac_vp[0])
+        for (int d = 0; d < 3; ++d) gather_faces(dom, umac[d], d, 0, 1, out->umac_vp[d]);
+    if (out->vel_force) gather_cells(dom, vel_force, 0, 3, out->vel_force);
+    // STEP 4 (Source/MaestroAdvance.cpp:436-548)
+    S.Addw0(umac, 1.0);
+    S.DensityAdvance(sold, snew, sedge, sflux, scal_force, etarhoflux, umac);
+    S.Addw0(umac, -1.0);
+    S.Addw0(umac, 1.0);
+    S.EnthalpyAdvance(sold, snew, sedge, sflux, scal_force, umac);
+    S.Addw0(umac, -1.0);
+
+    if (out->umac_end[0])
+        for (int d = 0; d < 3; ++d) gather_faces(dom, umac[d], d, 0, 1, out->umac_end[d]);
+    for (int d = 0; d < 3; ++d) {
+        if (out->sedge[d]) gather_faces(dom, sedge[d], d, 0, S.nscal, out->sedge[d]);
+        if (out->sflux[d]) gather_faces(dom, sflux[d], d, 0, S.nscal, out->sflux[d]);
+    }
+    if (out->snew) gather_cells(dom, snew, 0, S.nscal, out->snew);
+    if (out->sold_end) gather_cells(dom, sold, 0, S.nscal, out->sold_end);
+    if (out->etarhoflux) gather_faces(dom, etarhoflux, 2, 0, 1, out->etarhoflux);
+    return 0;
+}
+
+}  // namespace mo
+
+extern "C" {
+
+int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
+                 int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    try {
+        return mo::run_stage(p, nboxes, boxes, in, out);
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+
+int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {
+    std::vector<double> c(s0_cell, s0_cell + nr), e;
+    mo::Stage::CelltoEdge(c, e);
+    std::memcpy(s0_edge, e.data(), sizeof(double) * (nr + 1));
+    return 0;
+}
+
+const char* mo_last_error(void) { return mo::g_err.c_str(); }
+}

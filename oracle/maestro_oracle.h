@@ -1,0 +1,87 @@
+/* Test infrastructure only: C entry points of the CPU oracle for the MAESTROeX
+ * scalar-advection stage.  Loaded by tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / --impl reference legs of bench.py as the checker; the product library
+ * never links or calls it.
+ *
+ * Parity status: unpinned (the reference cannot be built: AMReX and Microphysics are
+ * empty submodules; the reference stores no stage-level golden outputs).  The oracle is a
+ * line-by-line restatement of the reference functions, each citing its file:line.
+ *
+ * All field arrays are single-level, domain-sized, Fortran ordered (i fastest), one
+ * contiguous block per component.  Face arrays in direction d have extent n_d + 1 in d.
+ */
+#ifndef MAESTRO_ORACLE_H
+#define MAESTRO_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same field layout as madv_params in include/maestro_adv.h. */
+typedef struct {
+    int nspec;
+    int ppm_type;           /* 0, 1, 2 */
+    int slope_order;        /* 0, 2, 4 (ppm_type 0 only) */
+    int species_pred_type;  /* 1 rho' & X, 2 rhoX, 3 rho & X */
+    int enthalpy_pred_type; /* 0 rhoh, 1 rhoh' */
+    int ppm_trace_forces;   /* must be 0 */
+    int evolve_base_state;
+    int use_exact_base_state;
+    int phys_bc_lo[3];
+    int phys_bc_hi[3];
+    int dom_lo[3];
+    int dom_hi[3];
+    double dx[3];
+    double dt;
+    double rel_eps;
+    double base_cutoff_density;
+    double buoyancy_cutoff_factor;
+    int do_eos_h_above_cutoff;
+    int base_cutoff_density_coord;
+} mo_params;
+
+typedef struct {
+    const double* uold;      /* [3][ncell] */
+    const double* sold;      /* [nscal][ncell], nscal = 4 + nspec */
+    const double* gpi;       /* [3][ncell] */
+    const double* thermal;   /* [ncell] (may be NULL => 0) */
+    const double* rho0_old;  /* [nr] */
+    const double* rho0_new;
+    const double* rhoh0_old;
+    const double* rhoh0_new;
+    const double* p0_old;
+    const double* p0_new;
+    const double* psi;
+    const double* grav_cell;
+    const double* w0_force;            /* [nr] */
+    const double* w0;                  /* [nr+1] */
+    const double* rho0_predicted_edge; /* [nr+1] */
+} mo_inputs;
+
+typedef struct {
+    double* utrans[3];   /* after MakeUtrans (before w0 is added), valid faces */
+    double* umac_vp[3];  /* VelPred output, valid faces */
+    double* umac_end[3]; /* umac at the end of the stage (after the Addw0 sequence) */
+    double* vel_force;   /* [3][ncell] */
+    double* sedge[3];    /* [nscal][faces_d] */
+    double* sflux[3];    /* [nscal][faces_d] */
+    double* snew;        /* [nscal][ncell] */
+    double* sold_end;    /* [nscal][ncell]: sold after the in-place conversions */
+    double* etarhoflux;  /* [z faces] */
+} mo_outputs;
+
+/* Runs AdvancePremac -> Addw0 -> DensityAdvance(1) -> EnthalpyAdvance(1) as
+ * AdvanceTimeStep does (MAC projection skipped).  boxes: nboxes*6 ints
+ * (lo0 lo1 lo2 hi0 hi1 hi2).  Returns 0, or a negative code with mo_last_error() set. */
+int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                 mo_outputs* out, int nthreads);
+
+/* 1-D CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), single level. */
+int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge);
+
+const char* mo_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,106 @@
+"""Test infrastructure only: ctypes binding of the CPU oracle (the checker).
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs.  The
+product library never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBS = {}
+
+
+class MoInputs(C.Structure):
+    _fields_ = [(name, C.POINTER(C.c_double)) for name in (
+        "uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+        "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge")]
+
+
+class MoOutputs(C.Structure):
+    _fields_ = [
+        ("utrans", C.POINTER(C.c_double) * 3),
+        ("umac_vp", C.POINTER(C.c_double) * 3),
+        ("umac_end", C.POINTER(C.c_double) * 3),
+        ("vel_force", C.POINTER(C.c_double)),
+        ("sedge", C.POINTER(C.c_double) * 3),
+        ("sflux", C.POINTER(C.c_double) * 3),
+        ("snew", C.POINTER(C.c_double)),
+        ("sold_end", C.POINTER(C.c_double)),
+        ("etarhoflux", C.POINTER(C.c_double)),
+    ]
+
+
+def build():
+    """Compile the oracle shared libraries with the committed Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib(checked=False):
+    name = "libmaestro_oracle_chk.so" if checked else "libmaestro_oracle.so"
+    if name not in _LIBS:
+        path = os.path.join(HERE, name)
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.mo_run_stage.restype = C.c_int
+        L.mo_last_error.restype = C.c_char_p
+        _LIBS[name] = L
+    return _LIBS[name]
+
+
+def _p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def run_stage(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_end", "vel_force",
+                                                      "sedge", "sflux", "snew", "sold_end",
+                                                      "etarhoflux")):
+    """Run AdvancePremac + DensityAdvance + EnthalpyAdvance on the CPU; returns numpy arrays."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    n = cfg["n"]
+    nscal = 4 + cfg["nspec"]
+    keep = []
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    inp = MoInputs()
+    for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                 "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+        setattr(inp, name, arr(cfg[name]))
+    out = MoOutputs()
+    res = {}
+    fshape = [(n[2], n[1], n[0] + 1), (n[2], n[1] + 1, n[0]), (n[2] + 1, n[1], n[0])]
+    for key in ("utrans", "umac_vp", "umac_end"):
+        if key in want:
+            res[key] = [np.full(fshape[d], np.nan) for d in range(3)]
+            for d in range(3):
+                getattr(out, key)[d] = _p(res[key][d])
+    for key in ("sedge", "sflux"):
+        if key in want:
+            res[key] = [np.full((nscal,) + fshape[d], np.nan) for d in range(3)]
+            for d in range(3):
+                getattr(out, key)[d] = _p(res[key][d])
+    cshape = (n[2], n[1], n[0])
+    if "vel_force" in want:
+        res["vel_force"] = np.full((3,) + cshape, np.nan)
+        out.vel_force = _p(res["vel_force"])
+    for key in ("snew", "sold_end"):
+        if key in want:
+            res[key] = np.full((nscal,) + cshape, np.nan)
+            setattr(out, key, _p(res[key]))
+    if "etarhoflux" in want:
+        res["etarhoflux"] = np.full(fshape[2], np.nan)
+        out.etarhoflux = _p(res["etarhoflux"])
+    boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    rc = lib(checked).mo_run_stage(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
+                                   C.byref(inp), C.byref(out), nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
+    return res
