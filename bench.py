@@ -1,0 +1,281 @@
+"""Benchmark of the scalar-advection stage (MakeUtrans, VelPred, MakeEdgeScal, fluxes,
+UpdateScal; MAC projection skipped) on the 3-D single-level workload: 256^3 cells in 64
+boxes of 64^3, NumSpec = 13, ppm_type 1, w0 != 0 (seeded synthetic atmosphere).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``value`` is advected cell-updates per second over all GPUs with the
+inputs resident in HBM; ``e2e`` is the same metric through the public API with host
+buffers copied in and the result copied out every step.  ``--impl reference`` times the
+CPU restatement of the reference stage (the oracle) on this host's cores.  With torchrun
+(N > 1) every rank advances its own independent copy of the workload (replicas: the stage
+is single-GPU) and the value is the total over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "advected cell-updates/s (FP64, <=1e-12 rel) batched vs per-box; %HBM; adj/fwd"
+UNIT = "cell-updates/s"
+HBM_PEAK_FALLBACK = 6792.7
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        self.tmp.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.tmp.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.tmp.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample_config(nspec):
+    """Bounded CPU sample with the workload's box shape: 128^3 in 8 boxes of 64^3."""
+    from maestroex_gb300 import configs
+    return configs.planar_config(n=(128, 128, 128), nspec=nspec, ppm_type=1, max_grid=64,
+                                 seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
+
+
+def run_cpu_baseline(steps, warmup, nthreads=0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    cfg = cpu_sample_config(13)
+    ncell = int(np.prod(cfg["n"]))
+    want = ("snew",)
+    for _ in range(warmup):
+        pyoracle.run_stage(cfg, nthreads=nthreads, want=want)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pyoracle.run_stage(cfg, nthreads=nthreads, want=want)
+    dt = (time.perf_counter() - t0) / steps
+    cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    return {"value": ncell / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "oracle on 128^3 cells in 8 boxes of 64^3, NumSpec 13, ppm_type 1 (same box shape "
+                      f"and per-cell work as the GPU workload), {steps} timed of {steps + warmup} runs",
+            "s_per_sample": dt}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--box", type=int, default=64)
+    ap.add_argument("--nspec", type=int, default=13)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-per-box", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = run_cpu_baseline(max(args.steps, 1), min(warmup, 1))
+        cfg_desc = {"workload": f"3-D single level {args.n}^3 in boxes of {args.box}^3, NumSpec {args.nspec}, "
+                                "ppm_type 1, w0 != 0 (CPU restatement timed on a bounded sample)"}
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * cb["s_per_sample"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": cfg_desc,
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from maestroex_gb300 import build, capi, configs
+    from maestroex_gb300.stage import MultiFab, StageBuffers, make_stage
+    if rank == 0 or ws == 1:
+        build.build_library()
+    if ws > 1:
+        dist.barrier()
+
+    cfg = configs.planar_config(n=(args.n,) * 3, nspec=args.nspec, ppm_type=1, max_grid=args.box,
+                                seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
+    ncell = args.n ** 3
+    st = make_stage(cfg)
+    buf = StageBuffers(cfg).load(cfg)
+    snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
+
+    def reset():
+        # the stage mutates sold in place (conversions); restore the inputs on the device
+        for name, ts in snap.items():
+            for dst, src in zip(getattr(buf, name).fabs, ts):
+                dst.copy_(src)
+
+    def step(mode):
+        st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                         thermal=buf.thermal, mode=mode)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(mode, steps, warm):
+        for _ in range(warm):
+            reset()
+            step(mode)
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(steps):
+            reset()  # not timed
+            torch.cuda.synchronize()
+            ev0.record()
+            step(mode)
+            ev1.record()
+            torch.cuda.synchronize()
+            total += ev0.elapsed_time(ev1)
+        barrier()
+        ms = total / steps
+        if ws > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms_graph = timed(capi.MODE_GRAPH, args.steps, warmup)
+    clocks = sampler.stop()
+    launches = st.launch_count()
+    ms_batched = timed(capi.MODE_BATCHED, max(1, args.steps // 2), 1)
+    ms_perbox = None if args.no_per_box else timed(capi.MODE_PER_BOX, max(1, args.steps // 2), 1)
+
+    # end to end: host (pinned) buffers in, stage, result out, every step
+    host = {}
+    for name in ("uold", "sold", "gpi"):
+        mf = getattr(buf, name)
+        host[name] = [t.detach().cpu().pin_memory() for t in mf.fabs]
+    host_out = [t.detach().cpu().pin_memory() for t in buf.snew.fabs]
+    h2d = sum(t.numel() * 8 for v in host.values() for t in v)
+    d2h = sum(t.numel() * 8 for t in host_out)
+    e2e_ms = 0.0
+    for it in range(warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for name, hs in host.items():
+            for dst, src in zip(getattr(buf, name).fabs, hs):
+                dst.copy_(src, non_blocking=True)
+        step(capi.MODE_GRAPH)
+        for dst, src in zip(host_out, buf.snew.fabs):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        if it >= warmup:
+            e2e_ms += (time.perf_counter() - t0) * 1e3
+    e2e_ms /= args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    peaks, peak_kind = measured_peaks()
+    value = ws * ncell / (ms_graph * 1e-3)
+    b_cell = 8 * (2 * args.nspec + 16)
+    hbm_gbs = ncell * b_cell / (ms_graph * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": warmup,
+        "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"3-D single level {args.n}^3 in {len(cfg['boxes'])} boxes of {args.box}^3, "
+                               f"NumSpec {args.nspec}, ppm_type 1, w0 != 0, x/y periodic, z slipwall/outflow",
+                   "mode": "batched kernels replayed as one CUDA graph",
+                   "l2": "inputs (state 2.4 GB) larger than the 129 MB L2; state reset between steps",
+                   "replicas": ws},
+        "clocks": clocks,
+        "e2e": {"value": ws * ncell / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches * args.steps,
+        "per_box": {"value": ws * ncell / (ms_perbox * 1e-3) if ms_perbox else None,
+                    "ms_per_step": ms_perbox},
+        "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
+        "stage_hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": peaks.get("hbm_gbs", HBM_PEAK_FALLBACK),
+                      "frac": hbm_gbs / peaks.get("hbm_gbs", HBM_PEAK_FALLBACK), "peak_kind": peak_kind,
+                      "bytes_per_cell": b_cell},
+    }
+    if not args.no_cpu_baseline:
+        cb = run_cpu_baseline(1, 0)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

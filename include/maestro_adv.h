@@ -1,0 +1,162 @@
+/* maestro_adv.h -- C ABI of the GB300 scalar-advection stage for MAESTROeX.
+ *
+ * Drop-in boundary for the Maestro member functions of the scalar-advection stage
+ * (declarations in Source/Maestro.H of the reference):
+ *   AdvancePremac   Source/Maestro.H:189   (MakeUtrans :1172, MakeVelForce, Addw0, VelPred :1711)
+ *   DensityAdvance  Source/Maestro.H:499   (MakeEdgeScal :913, MakeRhoXFlux :230, UpdateScal :306)
+ *   EnthalpyAdvance Source/Maestro.H:566   (MakeEdgeScal, MakeRhoHFlux :270, UpdateScal)
+ *   Addw0           Source/MaestroFill3dData.cpp:357
+ *
+ * A MultiFab is passed as a list of FABs (one per box, in BoxArray order), each a device
+ * pointer to Fortran-ordered storage (i fastest, then j, k, component) covering the
+ * FAB's index box, ghost cells included -- the layout of amrex::FArrayBox::dataPtr()
+ * with box() and nComp().  The caller owns every buffer; the library never frees them.
+ * Scratch memory is owned by the context.
+ *
+ * Every entry point returns MADV_OK (0) or a negative error code; none aborts.  All work
+ * is ordered on the stream passed in (cudaStream_t as void*; NULL = legacy default
+ * stream).  A context is single-stream and not thread-safe; separate contexts are
+ * independent.
+ */
+#ifndef MAESTRO_ADV_H
+#define MAESTRO_ADV_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MADV_OK = 0,
+    MADV_ERR_PARAM = -1,       /* invalid or inconsistent parameter */
+    MADV_ERR_LAYOUT = -2,      /* bad box list / FAB descriptor */
+    MADV_ERR_UNSUPPORTED = -3, /* option the library does not implement */
+    MADV_ERR_CUDA = -4,        /* CUDA runtime error (see madv_last_error) */
+    MADV_ERR_STATE = -5,       /* call order (layout / base state not set) */
+    MADV_ERR_EOS = -6          /* a cell fell to base_cutoff_density: needs the EOS */
+};
+
+/* AMReX PhysBCType values (Maestro inputs lo_bc / hi_bc). */
+enum { MADV_INTERIOR = 0, MADV_INFLOW = 1, MADV_OUTFLOW = 2, MADV_SYMMETRY = 3,
+       MADV_SLIPWALL = 4, MADV_NOSLIPWALL = 5 };
+
+/* Stage parameters: the Maestro runtime parameters and member state the stage reads. */
+typedef struct {
+    int nspec;                  /* NumSpec; state has 4 + nspec components */
+    int ppm_type;               /* 0 (slopes), 1, 2 */
+    int slope_order;            /* 0, 2, 4 (ppm_type 0) */
+    int species_pred_type;      /* 1 rho'&X, 2 rhoX, 3 rho&X */
+    int enthalpy_pred_type;     /* 0 rhoh, 1 rhoh' */
+    int ppm_trace_forces;       /* must be 0 */
+    int evolve_base_state;
+    int use_exact_base_state;   /* must be 0 (planar) */
+    int phys_bc_lo[3];
+    int phys_bc_hi[3];
+    int dom_lo[3];              /* level-0 domain box */
+    int dom_hi[3];
+    double dx[3];
+    double dt;
+    double rel_eps;
+    double base_cutoff_density;
+    double buoyancy_cutoff_factor;
+    int do_eos_h_above_cutoff;
+    int base_cutoff_density_coord;
+} madv_params;
+
+typedef struct {
+    int lo[3];
+    int hi[3];
+} madv_box;
+
+typedef struct {
+    double* p;   /* device pointer to element (lo) of component 0 */
+    int lo[3];   /* index box covered by the storage (ghosts / nodal extent included) */
+    int hi[3];
+    int ncomp;
+} madv_fab;
+
+typedef struct {
+    int nfab;            /* must equal the number of boxes of the layout */
+    const madv_fab* fab; /* host array of nfab descriptors */
+} madv_multifab;
+
+/* 1-D radial base state of one level (host arrays, nr = dom_hi[2]-dom_lo[2]+1), the
+ * BaseState<Real> members the stage reads.  Copied into the context. */
+typedef struct {
+    const double* rho0_old;            /* [nr] */
+    const double* rho0_new;            /* [nr] */
+    const double* rhoh0_old;           /* [nr] */
+    const double* rhoh0_new;           /* [nr] */
+    const double* p0_old;              /* [nr] */
+    const double* p0_new;              /* [nr] */
+    const double* psi;                 /* [nr] */
+    const double* grav_cell;           /* [nr] */
+    const double* w0_force;            /* [nr] */
+    const double* w0;                  /* [nr+1] edge centred */
+    const double* rho0_predicted_edge; /* [nr+1] */
+} madv_base_state;
+
+typedef struct madv_ctx madv_ctx;
+
+/* Context: parameters are copied; replaces the Maestro member state of the stage. */
+int madv_ctx_create(const madv_params* params, madv_ctx** ctx);
+void madv_ctx_destroy(madv_ctx* ctx);
+/* New dt / rel_eps for the next step (Maestro::EstDt, Source/MaestroDt.cpp:481-483). */
+int madv_set_dt(madv_ctx* ctx, double dt, double rel_eps);
+
+/* One level: boxes in BoxArray order.  Allocates the context's scratch. */
+int madv_set_layout(madv_ctx* ctx, int nboxes, const madv_box* boxes);
+int madv_set_base_state(madv_ctx* ctx, const madv_base_state* bs);
+
+/* Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84), one level.
+ * uold: 3 comps, sold: 4+nspec comps (only Rho is read), gpi: 3 comps (valid region read).
+ * umac[3]: face MultiFabs with >= 1 ghost, written on the valid faces (VelPred output).
+ * utrans[3] (may be NULL): receives the transverse velocities (with w0 added). */
+int madv_advance_premac(madv_ctx* ctx, const madv_multifab* uold, const madv_multifab* sold,
+                        const madv_multifab* gpi, const madv_multifab* umac,
+                        const madv_multifab* utrans, void* stream);
+
+/* Maestro::Addw0, planar (Source/MaestroFill3dData.cpp:357-462): wmac += mult*w0 and
+ * refill of the face ghosts. */
+int madv_addw0(madv_ctx* ctx, const madv_multifab* umac, double mult, void* stream);
+
+/* Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243).
+ * sold is converted and restored in place exactly as the reference does; snew receives
+ * rho and rhoX.  umac must hold the full velocity (w0 added), ghosts filled.
+ * sedge/sflux (may be NULL) receive the edge states / fluxes; etarhoflux may be NULL. */
+int madv_density_advance(madv_ctx* ctx, int which_step, const madv_multifab* sold,
+                         const madv_multifab* snew, const madv_multifab* sedge,
+                         const madv_multifab* sflux, const madv_multifab* etarhoflux,
+                         const madv_multifab* umac, void* stream);
+
+/* Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352).
+ * thermal may be NULL (zero). */
+int madv_enthalpy_advance(madv_ctx* ctx, int which_step, const madv_multifab* sold,
+                          const madv_multifab* snew, const madv_multifab* sedge,
+                          const madv_multifab* sflux, const madv_multifab* umac,
+                          const madv_multifab* thermal, void* stream);
+
+/* The whole stage as Maestro::AdvanceTimeStep runs it with the MAC projection
+ * skipped (Source/MaestroAdvance.cpp:359, 448-455, 541-548): AdvancePremac, Addw0(+1),
+ * DensityAdvance, Addw0(-1), Addw0(+1), EnthalpyAdvance, Addw0(-1).
+ * mode: MADV_MODE_BATCHED runs every kernel once over all boxes;
+ *       MADV_MODE_PER_BOX launches every kernel once per box (the AMReX MFIter form);
+ *       MADV_MODE_GRAPH replays a CUDA graph of the batched form (captured on first use
+ *       for the given buffers). */
+enum { MADV_MODE_BATCHED = 0, MADV_MODE_PER_BOX = 1, MADV_MODE_GRAPH = 2 };
+int madv_stage_forward(madv_ctx* ctx, int mode, const madv_multifab* uold,
+                       const madv_multifab* sold, const madv_multifab* gpi,
+                       const madv_multifab* thermal, const madv_multifab* snew,
+                       const madv_multifab* umac, const madv_multifab* sedge,
+                       const madv_multifab* sflux, const madv_multifab* etarhoflux,
+                       void* stream);
+
+/* Number of kernel launches issued by the last madv_* call (for launch accounting). */
+long madv_last_launch_count(const madv_ctx* ctx);
+
+const char* madv_last_error(void);
+const char* madv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

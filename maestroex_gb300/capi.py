@@ -1,0 +1,89 @@
+"""ctypes binding of the C ABI declared in include/maestro_adv.h (libmaestro_adv.so).
+
+The shared library is built in-tree by ``maestroex_gb300.build.build_library()``; importing
+this module never falls back to anything else: if the library is missing the load fails
+loudly.
+"""
+import ctypes as C
+import os
+
+from .params import MadvParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmaestro_adv.so")
+
+MADV_OK = 0
+MODE_BATCHED, MODE_PER_BOX, MODE_GRAPH = 0, 1, 2
+
+ERRORS = {
+    -1: "MADV_ERR_PARAM", -2: "MADV_ERR_LAYOUT", -3: "MADV_ERR_UNSUPPORTED",
+    -4: "MADV_ERR_CUDA", -5: "MADV_ERR_STATE", -6: "MADV_ERR_EOS",
+}
+
+EXPORTED = [
+    "madv_ctx_create", "madv_ctx_destroy", "madv_set_dt", "madv_set_layout",
+    "madv_set_base_state", "madv_advance_premac", "madv_addw0", "madv_density_advance",
+    "madv_enthalpy_advance", "madv_stage_forward", "madv_last_launch_count",
+    "madv_last_error", "madv_version",
+]
+
+
+class MadvBox(C.Structure):
+    _fields_ = [("lo", C.c_int * 3), ("hi", C.c_int * 3)]
+
+
+class MadvFab(C.Structure):
+    _fields_ = [("p", C.c_void_p), ("lo", C.c_int * 3), ("hi", C.c_int * 3), ("ncomp", C.c_int)]
+
+
+class MadvMultiFab(C.Structure):
+    _fields_ = [("nfab", C.c_int), ("fab", C.POINTER(MadvFab))]
+
+
+class MadvBaseState(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_double)) for n in (
+        "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new", "p0_old", "p0_new", "psi", "grav_cell",
+        "w0_force", "w0", "rho0_predicted_edge")]
+
+
+class MadvError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: run maestroex_gb300.build.build_library() first")
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        L.madv_ctx_create.argtypes = [P(MadvParams), P(C.c_void_p)]
+        L.madv_ctx_destroy.argtypes = [C.c_void_p]
+        L.madv_ctx_destroy.restype = None
+        L.madv_set_dt.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.madv_set_layout.argtypes = [C.c_void_p, C.c_int, P(MadvBox)]
+        L.madv_set_base_state.argtypes = [C.c_void_p, P(MadvBaseState)]
+        MF = P(MadvMultiFab)
+        L.madv_advance_premac.argtypes = [C.c_void_p, MF, MF, MF, MF, MF, C.c_void_p]
+        L.madv_addw0.argtypes = [C.c_void_p, MF, C.c_double, C.c_void_p]
+        L.madv_density_advance.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, C.c_void_p]
+        L.madv_enthalpy_advance.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, C.c_void_p]
+        L.madv_stage_forward.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
+                                         C.c_void_p]
+        L.madv_last_launch_count.argtypes = [C.c_void_p]
+        L.madv_last_launch_count.restype = C.c_long
+        L.madv_last_error.restype = C.c_char_p
+        L.madv_version.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != MADV_OK:
+        raise MadvError(rc, lib().madv_last_error().decode())
+    return rc

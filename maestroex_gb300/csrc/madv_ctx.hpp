@@ -1,0 +1,155 @@
+// Host-side context of the scalar-advection stage library (one AMR level).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <array>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/maestro_adv.h"
+#include "madv_core.cuh"
+
+namespace madv {
+
+struct HBox {
+    int lo[3];
+    int hi[3];
+};
+
+// Internal fields of a level.  The working copies of the caller's state (sold, snew,
+// umac, ...) live here too: the entry points copy the caller's FABs in and out, so the
+// kernels see one fixed layout.
+enum FieldId {
+    F_SOLD, F_SNEW, F_GPI, F_THERMAL, F_W0CART, F_W0FCART, F_UTILDE, F_UFULL,
+    F_UTRANS0, F_UTRANS1, F_UTRANS2, F_UMAC0, F_UMAC1, F_UMAC2,
+    F_VELFORCE, F_SCALFORCE,
+    F_SEDGE0, F_SEDGE1, F_SEDGE2, F_SFLUX0, F_SFLUX1, F_SFLUX2, F_ETA,
+    F_RHO0CART, F_RHOH0CART, F_S0ECART, F_P0CART, F_PSICART, F_GRAVCART,
+    F_FACE0, F_FACE1, F_FACE2,     // PPM interface values, per direction
+    F_IPC0, F_IPC1, F_IPC2,        // Ip of traced component c (3 directional comps)
+    F_IMC0, F_IMC1, F_IMC2,
+    F_SL0, F_SL1, F_SL2,           // left/right predictor states and upwind state per
+    F_SR0, F_SR1, F_SR2,           // face direction (3 comps for velocity, 1 for scalars)
+    F_SIMH0, F_SIMH1, F_SIMH2,
+    F_Q01, F_Q02, F_Q10, F_Q12, F_Q20, F_Q21,  // transverse states [d][t] / [c][d]
+    F_DIVU, F_SLOPE,
+    F_USER,                        // first slot of per-call views of caller FABs
+    NF_INTERNAL = F_USER
+};
+constexpr int N_USER_SLOTS = 64;
+constexpr int NF_TOTAL = F_USER + N_USER_SLOTS;
+
+// transverse-state field for the ordered pair (a, b), a != b
+#define Q_FIELD(a, b) (F_Q01 + 2 * (a) + ((b) > (a) ? (b)-1 : (b)))
+
+struct FieldSpec {
+    int ncomp = 0, ng = 0, nodal = -1;
+};
+
+struct Field {
+    FieldSpec spec;
+    double* base = nullptr;
+    size_t bytes = 0;
+};
+
+struct RegionTable {
+    RegionBox* d = nullptr;
+    std::vector<RegionBox> h;  // region pieces (one per box, two for boundary slabs)
+    long total = 0;
+};
+
+struct CopyDesc {
+    int dst_b, src_b;
+    int lo[3];
+    int n[3];
+    int shift[3];
+    int pad;
+    long start;
+};
+static_assert(sizeof(CopyDesc) == 56, "CopyDesc layout");
+
+struct CopyTable {
+    CopyDesc* d = nullptr;
+    std::vector<CopyDesc> h;
+    long total = 0;
+};
+
+struct Ctx {
+    madv_params P{};
+    int nspec = 0, nscal = 0, ng_s = 3, ng_adv = 3, nr = 0;
+    bool per[3] = {false, false, false};
+    std::vector<HBox> ba;
+    int nb = 0;
+    bool have_layout = false, have_base = false;
+    BCRecD bcs_s[MAX_SCAL], bcs_u[3], bcs_f[MAX_SCAL];
+    BCRecD* d_bcs = nullptr;  // [0,nscal): bcs_s, [nscal, nscal+3): bcs_u, then bcs_f
+    // 1-D base state on the device
+    std::map<std::string, double*> d1;
+    std::map<std::string, std::vector<double>> h1;
+    Field F[NF_INTERNAL];
+    std::vector<FabView> hviews;  // NF_TOTAL * nb
+    FabView* dviews = nullptr;
+    FabView* hviews_pinned = nullptr;
+    std::map<std::array<int, 8>, RegionTable> regions;
+    std::map<std::array<int, 3>, CopyTable> copies;
+    cudaStream_t stream = nullptr;
+    int per_box = 0;      // launch mode: 0 batched, 1 one launch per box
+    bool dry = false;     // build region / copy tables only, launch nothing
+    long launches = 0;
+    int* d_flag = nullptr;  // device error flag (EOS cutoff)
+    // graph mode
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<const void*> graph_key;
+    long graph_launches = 0;
+
+    double* b1(const char* name) { return d1.at(name); }
+    const FabView* V() const { return dviews; }
+};
+
+// Region of each box: the valid cell box grown by glo (low side) / ghi (high side), with
+// `nodal` marking a face-centred index space (hi[nodal] + 1 before growing).
+// `slab` >= 0 selects, for the physical-boundary fill, only cells outside the domain in
+// direction slab (both sides).
+const RegionTable& region(Ctx& c, int glo0, int glo1, int glo2, int ghi0, int ghi1, int ghi2,
+                          int nodal = -1, int slab = -1);
+const CopyTable& copy_table(Ctx& c, int ng, int nodal);
+
+void set_error(const std::string& s);
+bool cuda_ok(cudaError_t e, const char* what);
+
+// ---- kernel launch wrappers (madv_kernels.cu) ----
+void fill_boundary(Ctx& c, int fid, int c0, int nc);
+void phys_fill(Ctx& c, int fid, int c0, int nc, const BCRecD* bcs_dev, int bc_c0, int is_vel,
+               int state_c0);
+void fill_patch(Ctx& c, int fid, int c0, int nc, int which_bcs, int bc_c0, int is_vel, int state_c0);
+void fill_face_ghosts(Ctx& c, int f0);  // FillBoundary + FillUmacGhost of 3 face fields f0..f0+2
+void addw0(Ctx& c, int f0, double mult);
+void set_val(Ctx& c, int fid, double v, int c0, int nc, int ngrow);
+void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow);
+void add_fab(Ctx& c, int dst, int src, int nc, int ngrow);
+void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge);
+void make_utrans(Ctx& c);
+void make_vel_force(Ctx& c);
+void vel_pred(Ctx& c);
+void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative);
+void modify_scal_force(Ctx& c, int comp, const double* d_s0_edge, int s0cart_fid, int fullform);
+void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal, int which_step);
+void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int bccomp, int which_bcs, int flag);
+void convert_rhox_to_x(Ctx& c, int flag);
+void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
+                    const double* r0e_new);
+void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
+                    const double* rh0e_new);
+void sum_species_edges(Ctx& c);
+void update_scal(Ctx& c, int start_comp);
+
+enum { BCS_S = 0, BCS_U = 1, BCS_F = 2 };
+inline const BCRecD* bcs_dev(const Ctx& c, int which) {
+    return which == BCS_S ? c.d_bcs : (which == BCS_U ? c.d_bcs + c.nscal : c.d_bcs + c.nscal + 3);
+}
+inline const BCRecD* bcs_host(const Ctx& c, int which) {
+    return which == BCS_S ? c.bcs_s : (which == BCS_U ? c.bcs_u : c.bcs_f);
+}
+
+}  // namespace madv

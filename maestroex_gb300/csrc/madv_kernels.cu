@@ -1,0 +1,1431 @@
+// Kernels of the GB300 scalar-advection stage (3-D, plane-parallel base state, one level).
+//
+// Each reference ParallelFor of the stage becomes one launch over all boxes of the level
+// (or one launch per box in the per-box mode).  The arithmetic of every element follows
+// the reference expression for expression (same operands, same order, IEEE binary64,
+// no FMA contraction: the library is built with --fmad=false), so results match the
+// reference algorithm bit for bit.  What changes is the amount of FP64 work: GB300 issues
+// FP64 at a small fraction of its FP32 rate, so every intermediate of the stage is
+// computed once and stored, where the reference recomputes it:
+//   * PPM: the limited interface value of each face is computed once per face (the
+//     reference evaluates four van Leer slopes and two interface values per cell and
+//     direction, and in MakeUtrans sweeps all three directions where one is used);
+//   * constant quotients such as (dt/6)/dy are formed once on the host, where the
+//     reference forms them per element (same IEEE operations, same values).
+#include <cstdio>
+
+#include "madv_ctx.hpp"
+
+namespace madv {
+
+#define KARGS const RegionBox *__restrict__ R, int ne, long g0, long g1, const FabView *__restrict__ V, int nb
+#define VW(f) V[(f) * nb + b]
+
+static constexpr int TPB = 256;
+
+// One launch over every box (batched), or one launch per region piece (per-box mode, the
+// MFIter + ParallelFor form of the reference).  Kernel arguments after the region are
+// (V, nb, ...).
+template <typename Kern, typename... Args>
+static void launch(Ctx& c, const RegionTable& rt, int gy, Kern kern, const FabView* V, Args... args) {
+    if (rt.total == 0 || c.dry) return;
+    const int ne = (int)rt.h.size();
+    if (!c.per_box) {
+        dim3 grid((unsigned)((rt.total + TPB - 1) / TPB), gy);
+        kern<<<grid, TPB, 0, c.stream>>>(rt.d, ne, 0L, rt.total, V, c.nb, args...);
+        c.launches++;
+    } else {
+        for (int e = 0; e < ne; ++e) {
+            long s0 = rt.h[e].start;
+            long s1 = (e + 1 < ne) ? rt.h[e + 1].start : rt.total;
+            if (s1 <= s0) continue;
+            dim3 grid((unsigned)((s1 - s0 + TPB - 1) / TPB), gy);
+            kern<<<grid, TPB, 0, c.stream>>>(rt.d, ne, s0, s1, V, c.nb, args...);
+            c.launches++;
+        }
+    }
+}
+
+// Region helpers: the valid box grown by g, and face boxes.
+static const RegionTable& rg_grow(Ctx& c, int g, int nodal = -1) { return region(c, g, g, g, g, g, g, nodal); }
+
+// ============================================================ elementwise utilities
+__global__ void k_set_val(KARGS, int f, double v, int c0, int nc) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView a = VW(f);
+    for (int n = c0; n < c0 + nc; ++n) at(a, i, j, k, n) = v;
+}
+
+void set_val(Ctx& c, int fid, double v, int c0, int nc, int ngrow) {
+    launch(c, rg_grow(c, ngrow, c.F[fid].spec.nodal), 1, k_set_val, c.V(), fid, v, c0, nc);
+}
+
+__global__ void k_copy(KARGS, int fd, int dc0, int fs, int sc0, int nc, int add) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView d = VW(fd), s = VW(fs);
+    for (int n = 0; n < nc; ++n) {
+        if (add) at(d, i, j, k, dc0 + n) += at(s, i, j, k, sc0 + n);
+        else at(d, i, j, k, dc0 + n) = at(s, i, j, k, sc0 + n);
+    }
+}
+
+static int nodal_of(const Ctx& c, int fid) { return fid < NF_INTERNAL ? c.F[fid].spec.nodal : -1; }
+
+void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow) {
+    int nd = dst < NF_INTERNAL ? nodal_of(c, dst) : nodal_of(c, src);
+    launch(c, rg_grow(c, ngrow, nd), 1, k_copy, c.V(), dst, dc0, src, sc0, nc, 0);
+}
+
+void add_fab(Ctx& c, int dst, int src, int nc, int ngrow) {
+    launch(c, rg_grow(c, ngrow, nodal_of(c, dst)), 1, k_copy, c.V(), dst, 0, src, 0, nc, 1);
+}
+
+// Put1dArrayOnCart, planar (Source/MaestroFill3dData.cpp:79-93): valid cells only.
+__global__ void k_put1d(KARGS, int f, const double* __restrict__ s0, int outcomp, int edge) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const int r = k;
+    at(VW(f), i, j, k, outcomp) = edge ? 0.5 * (s0[r] + s0[r + 1]) : s0[r];
+}
+
+void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge) {
+    launch(c, rg_grow(c, 0), 1, k_put1d, c.V(), fid, d_s0, outcomp, edge);
+}
+
+// ============================================================ ghost fills
+__global__ void k_fill_boundary(const CopyDesc* __restrict__ D, int nd, long total, const FabView* __restrict__ V,
+                                int nb, int f, int c0, int nc) {
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= total) return;
+    int lo = 0, hi = nd - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (D[mid].start <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    const CopyDesc& cd = D[lo];
+    long l = gid - cd.start;
+    const long nx = cd.n[0], ny = cd.n[1];
+    const long q = l / nx;
+    const int i = cd.lo[0] + (int)(l - q * nx);
+    const long q2 = q / ny;
+    const int j = cd.lo[1] + (int)(q - q2 * ny);
+    const int k = cd.lo[2] + (int)q2;
+    const FabView dst = V[f * nb + cd.dst_b];
+    const FabView src = V[f * nb + cd.src_b];
+    for (int n = c0; n < c0 + nc; ++n)
+        at(dst, i, j, k, n) = at(src, i - cd.shift[0], j - cd.shift[1], k - cd.shift[2], n);
+}
+
+void fill_boundary(Ctx& c, int fid, int c0, int nc) {
+    const FieldSpec& s = c.F[fid].spec;
+    const CopyTable& ct = copy_table(c, s.ng, s.nodal);
+    if (ct.total == 0 || c.dry) return;
+    unsigned grid = (unsigned)((ct.total + TPB - 1) / TPB);
+    k_fill_boundary<<<grid, TPB, 0, c.stream>>>(ct.d, (int)ct.h.size(), ct.total, c.V(), c.nb, fid, c0, nc);
+    c.launches++;
+}
+
+// Physical-boundary fill of direction d (both sides) for a cell-centred field.  The
+// definitions of the BC types match the oracle's restatement of fab_filcc (foextrap,
+// hoextrap = quadratic face extrapolation in the first ghost, reflect_even/odd,
+// ext_dir = 0 for velocities).
+__global__ void k_phys_fill(KARGS, int f, int c0, int nc, const BCRecD* __restrict__ bcs, int bc_c0, int is_vel,
+                            int state_c0, int d, int domlo, int domhi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView q = VW(f);
+    const int idx[3] = {i, j, k};
+    const int m = idx[d];
+    const int side = m < domlo ? 0 : 1;
+    auto A = [&](int p, int n) -> double {
+        int i2 = i, j2 = j, k2 = k;
+        if (d == 0) i2 = p;
+        else if (d == 1) j2 = p;
+        else k2 = p;
+        return at(q, i2, j2, k2, n);
+    };
+    for (int n = c0; n < c0 + nc; ++n) {
+        const BCRecD bc = bcs[bc_c0 + n - c0];
+        const int t = side == 0 ? bc.lo[d] : bc.hi[d];
+        double v;
+        if (t == BC_INT_DIR) continue;
+        if (t == BC_FOEXTRAP) {
+            v = A(side == 0 ? domlo : domhi, n);
+        } else if (t == BC_HOEXTRAP) {
+            if (side == 0) {
+                if (m < domlo - 1) v = A(domlo, n);
+                else if (domlo + 2 <= domhi) v = 0.125 * (15. * A(domlo, n) - 10. * A(domlo + 1, n) + 3. * A(domlo + 2, n));
+                else v = 0.5 * (3. * A(domlo, n) - A(domlo + 1, n));
+            } else {
+                if (m > domhi + 1) v = A(domhi, n);
+                else if (domhi - 2 >= domlo) v = 0.125 * (15. * A(domhi, n) - 10. * A(domhi - 1, n) + 3. * A(domhi - 2, n));
+                else v = 0.5 * (3. * A(domhi, n) - A(domhi - 1, n));
+            }
+        } else if (t == BC_REFLECT_EVEN) {
+            v = A(side == 0 ? 2 * domlo - 1 - m : 2 * domhi + 1 - m, n);
+        } else if (t == BC_REFLECT_ODD) {
+            v = -A(side == 0 ? 2 * domlo - 1 - m : 2 * domhi + 1 - m, n);
+        } else {  // ext_dir: zero for velocities and Pi; scalars are rejected on the host
+            v = 0.0;
+        }
+        (void)is_vel;
+        (void)state_c0;
+        at(q, i, j, k, n) = v;
+    }
+}
+
+void phys_fill(Ctx& c, int fid, int c0, int nc, const BCRecD* bcs_d, int bc_c0, int is_vel, int state_c0) {
+    const FieldSpec& s = c.F[fid].spec;
+    for (int d = 0; d < 3; ++d) {
+        if (c.per[d]) continue;
+        const RegionTable& rt = region(c, s.ng, s.ng, s.ng, s.ng, s.ng, s.ng, s.nodal, d);
+        launch(c, rt, 1, k_phys_fill, c.V(), fid, c0, nc, bcs_d, bc_c0, is_vel, state_c0, d, c.P.dom_lo[d],
+               c.P.dom_hi[d]);
+    }
+}
+
+void fill_patch(Ctx& c, int fid, int c0, int nc, int which_bcs, int bc_c0, int is_vel, int state_c0) {
+    fill_boundary(c, fid, c0, nc);
+    phys_fill(c, fid, c0, nc, bcs_dev(c, which_bcs), bc_c0, is_vel, state_c0);
+}
+
+// FillUmacGhost (Source/MaestroFillData.cpp:176-453): ghost faces behind physical
+// boundaries, one face direction dd per launch (x, then y, then z, as the reference).
+__global__ void k_umac_ghost(KARGS, int f0, int dd, int bclo, int bchi, int dlo, int dhi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const int I = dd == 0 ? i : (dd == 1 ? j : k);
+    if (I != dlo - 1 && I != dhi + 2) return;
+    const int di = dd == 0, dj = dd == 1, dk = dd == 2;
+    const FabView q[3] = {VW(f0), VW(f0 + 1), VW(f0 + 2)};
+    if (I == dlo - 1) {
+        switch (bclo) {
+            case PB_INFLOW:
+                for (int cc = 0; cc < 3; ++cc) at(q[cc], i, j, k) = cc == dd ? at(q[dd], i + di, j + dj, k + dk) : 0.0;
+                break;
+            case PB_SLIPWALL:
+            case PB_NOSLIPWALL:
+                for (int cc = 0; cc < 3; ++cc) at(q[cc], i, j, k) = 0.0;
+                break;
+            case PB_OUTFLOW:
+                for (int cc = 0; cc < 3; ++cc) at(q[cc], i, j, k) = at(q[cc], i + di, j + dj, k + dk);
+                break;
+            case PB_SYMMETRY:
+                for (int cc = 0; cc < 3; ++cc)
+                    at(q[cc], i, j, k) = cc == dd ? -at(q[dd], i + 2 * di, j + 2 * dj, k + 2 * dk)
+                                                  : at(q[cc], i + di, j + dj, k + dk);
+                break;
+            default: break;
+        }
+    } else {
+        switch (bchi) {
+            case PB_INFLOW:
+                for (int cc = 0; cc < 3; ++cc) {
+                    if (cc == dd) at(q[dd], i, j, k) = at(q[dd], i - di, j - dj, k - dk);
+                    else at(q[cc], i - di, j - dj, k - dk) = 0.0;
+                }
+                break;
+            case PB_SLIPWALL:
+            case PB_NOSLIPWALL:
+                for (int cc = 0; cc < 3; ++cc) {
+                    if (cc == dd) at(q[dd], i, j, k) = 0.0;
+                    else at(q[cc], i - di, j - dj, k - dk) = 0.0;
+                }
+                break;
+            case PB_OUTFLOW:
+                for (int cc = 0; cc < 3; ++cc) {
+                    if (cc == dd) at(q[dd], i, j, k) = at(q[dd], i - di, j - dj, k - dk);
+                    else at(q[cc], i - di, j - dj, k - dk) = at(q[cc], i - 2 * di, j - 2 * dj, k - 2 * dk);
+                }
+                break;
+            case PB_SYMMETRY:
+                for (int cc = 0; cc < 3; ++cc) {
+                    if (cc == dd) at(q[dd], i, j, k) = -at(q[dd], i - 2 * di, j - 2 * dj, k - 2 * dk);
+                    else at(q[cc], i - di, j - dj, k - dk) = at(q[cc], i - 2 * di, j - 2 * dj, k - 2 * dk);
+                }
+                break;
+            default: break;
+        }
+    }
+}
+
+void fill_face_ghosts(Ctx& c, int f0) {
+    for (int d = 0; d < 3; ++d) fill_boundary(c, f0 + d, 0, 1);
+    for (int dd = 0; dd < 3; ++dd) {
+        if (c.per[dd]) continue;
+        const RegionTable& rt = region(c, 1, 1, 1, 1, 1, 1, dd);
+        launch(c, rt, 1, k_umac_ghost, c.V(), f0, dd, c.P.phys_bc_lo[dd], c.P.phys_bc_hi[dd], c.P.dom_lo[dd],
+               c.P.dom_hi[dd]);
+    }
+}
+
+// Addw0, planar (Source/MaestroFill3dData.cpp:381-393)
+__global__ void k_addw0(KARGS, int f, const double* __restrict__ w0, double mult) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    at(VW(f), i, j, k) += mult * w0[k];
+}
+
+void addw0(Ctx& c, int f0, double mult) {
+    launch(c, region(c, 1, 1, 0, 1, 1, 0, 2), 1, k_addw0, c.V(), f0 + 2, (const double*)c.b1("w0"), mult);
+    fill_face_ghosts(c, f0);
+}
+
+// ============================================================ PPM
+// S(m): the field at cell (index + m) along direction D.
+#define SHIFT_S(s, sc) [&](int m) -> double { return at(s, i + m * di, j + m * dj, k + m * dk, sc); }
+
+// Limited interface value of the face between cells f-1 and f along D (Maestro::PPM,
+// Source/MaestroPPM.cpp: ppm_type 1 :37-111, ppm_type 2 :257-335; the boundary
+// stencils of :131-205 / :443-700 are the values the reference assigns to the faces
+// next to an ext_dir/hoextrap boundary).
+template <int D, int PPMT>
+__global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext, int domlo, int domhi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const FabView s = VW(fs);
+    auto S = SHIFT_S(s, sc);
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    double v;
+    if (lo_ext && I == domlo) {
+        v = S(-1);
+    } else if (hi_ext && I == domhi + 1) {
+        v = S(0);
+    } else if (lo_ext && I == domlo + 1) {
+        v = -0.2 * S(-2) + 0.75 * S(-1) + 0.5 * S(0) - 0.05 * S(1);
+        v = mx(v, mn(S(0), S(-1)));
+        v = mn(v, mx(S(0), S(-1)));
+    } else if (hi_ext && I == domhi) {
+        v = -0.2 * S(1) + 0.75 * S(0) + 0.5 * S(-1) - 0.05 * S(-2);
+        v = mx(v, mn(S(-1), S(0)));
+        v = mn(v, mx(S(-1), S(0)));
+    } else if (PPMT == 1) {
+        double dvl = 0.0, dvr = 0.0;
+        double dsc = 0.5 * (S(0) - S(-2));
+        double dsl = 2.0 * (S(-1) - S(-2));
+        double dsr = 2.0 * (S(0) - S(-1));
+        if (dsl * dsr > 0.0) dvl = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
+        dsc = 0.5 * (S(1) - S(-1));
+        dsl = 2.0 * (S(0) - S(-1));
+        dsr = 2.0 * (S(1) - S(0));
+        if (dsl * dsr > 0.0) dvr = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
+        v = 0.5 * (S(0) + S(-1)) - (dvr - dvl) / 6.0;
+        v = mx(v, mn(S(0), S(-1)));
+        v = mn(v, mx(S(0), S(-1)));
+    } else {
+        const double C = 1.25;
+        v = (7.0 / 12.0) * (S(-1) + S(0)) - (1.0 / 12.0) * (S(-2) + S(1));
+        if ((v - S(-1)) * (S(0) - v) < 0.0) {
+            double D2 = 3.0 * (S(-1) - 2.0 * v + S(0));
+            double D2L = S(-2) - 2.0 * S(-1) + S(0);
+            double D2R = S(-1) - 2.0 * S(0) + S(1);
+            double sgn = copysign(1.0, D2);
+            double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
+            v = 0.5 * (S(-1) + S(0)) - D2LIM / 6.0;
+        }
+    }
+    at(VW(ff), i, j, k) = v;
+}
+
+// Interior fourth-order limited face value (ppm_type 2), face between cells c+m-1 and c+m.
+template <int D>
+__device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, int i, int j, int k, int m) {
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    auto S = SHIFT_S(s, sc);
+    const double C = 1.25;
+    double se = (7.0 / 12.0) * (S(m - 1) + S(m)) - (1.0 / 12.0) * (S(m - 2) + S(m + 1));
+    if ((se - S(m - 1)) * (S(m) - se) < 0.0) {
+        double D2 = 3.0 * (S(m - 1) - 2.0 * se + S(m));
+        double D2L = S(m - 2) - 2.0 * S(m - 1) + S(m);
+        double D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
+        double sgn = copysign(1.0, D2);
+        double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
+        se = 0.5 * (S(m - 1) + S(m)) - D2LIM / 6.0;
+    }
+    return se;
+}
+
+// Per-cell limiting and characteristic tracing (Source/MaestroPPM.cpp: quadratic
+// limiter :117-128, Colella-2008 limiter :337-434, tracing :209-251 / :706-770).
+template <int D, int PPMT, int UMAC>
+__global__ void k_ppm_cell(KARGS, int fs, int sc, int ff, int fu, int uc, int fip, int fim, int lo_ext, int hi_ext,
+                           int domlo, int domhi, double dt, double rel_eps, double dxd) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const FabView s = VW(fs);
+    const FabView F = VW(ff);
+    auto S = SHIFT_S(s, sc);
+    auto Fc = [&](int m) -> double { return at(F, i + m * di, j + m * dj, k + m * dk); };
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const double s0 = S(0);
+    double sm, sp;
+    if (PPMT == 1) {
+        sm = Fc(0);
+        sp = Fc(1);
+        const bool special = (lo_ext && I == domlo) || (hi_ext && I == domhi);
+        if (!special) {
+            if ((sp - s0) * (s0 - sm) <= 0.0) {
+                sp = s0;
+                sm = s0;
+            } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
+                sp = 3.0 * s0 - 2.0 * sm;
+            } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
+                sm = 3.0 * s0 - 2.0 * sp;
+            }
+        }
+    } else {
+        const double C = 1.25;
+        double sedgel = Fc(-1), sedge = Fc(0), sedger = Fc(1), sedgerr = Fc(2);
+        if (D == 0 && hi_ext && I == domhi - 1) sedgerr = ppm2_face_regular<D>(s, sc, i, j, k, 2);
+        if (lo_ext && I == domlo) {
+            sm = sedge;
+            sp = sedger;
+        } else if (hi_ext && I == domhi) {
+            sp = sedger;
+            sm = sedge;
+        } else {
+            const double bigm_tol = (D == 0 && lo_ext && (I == domlo + 1 || I == domlo + 2)) ? 1.e10 : 1.e-10;
+            double alphap = sedger - s0;
+            double alpham = sedge - s0;
+            const bool bigp = fabs(alphap) > 2.0 * fabs(alpham);
+            const bool bigm = fabs(alpham) > 2.0 * fabs(alphap);
+            bool extremum = false;
+            if (alpham * alphap >= 0.0) {
+                extremum = true;
+            } else if (bigp || bigm) {
+                double dafacem = sedge - sedgel;
+                double dafacep = sedgerr - sedger;
+                double dabarm = s0 - S(-1);
+                double dabarp = S(1) - s0;
+                double dafacemin = mn(fabs(dafacem), fabs(dafacep));
+                double dabarmin = mn(fabs(dabarm), fabs(dabarp));
+                double dachkm, dachkp;
+                if (dafacemin >= dabarmin) {
+                    dachkm = dafacem;
+                    dachkp = dafacep;
+                } else {
+                    dachkm = dabarm;
+                    dachkp = dabarp;
+                }
+                extremum = (dachkm * dachkp <= 0.0);
+            }
+            if (extremum) {
+                double D2 = 6.0 * (alpham + alphap);
+                double D2L = S(-2) - 2.0 * S(-1) + s0;
+                double D2R = s0 - 2.0 * S(1) + S(2);
+                double D2C = S(-1) - 2.0 * s0 + S(1);
+                double sgn = copysign(1.0, D2);
+                double D2LIM = mx(mn(sgn * D2, mn(C * sgn * D2L, mn(C * sgn * D2R, C * sgn * D2C))), 0.0);
+                double D2ABS = mx(fabs(D2), 1.e-10);
+                alpham = alpham * D2LIM / D2ABS;
+                alphap = alphap * D2LIM / D2ABS;
+            } else {
+                if (bigp) {
+                    double sgn = copysign(1.0, alpham);
+                    double amax = -alphap * alphap / (4.0 * (alpham + alphap));
+                    double delam = S(-1) - s0;
+                    if (sgn * amax >= sgn * delam) {
+                        if (sgn * (delam - alpham) >= 1.e-10) {
+                            alphap = -2.0 * delam - 2.0 * sgn * sqrt(delam * delam - delam * alpham);
+                        } else {
+                            alphap = -2.0 * alpham;
+                        }
+                    }
+                }
+                if (bigm) {
+                    double sgn = copysign(1.0, alphap);
+                    double amax = -alpham * alpham / (4.0 * (alpham + alphap));
+                    double delap = S(1) - s0;
+                    if (sgn * amax >= sgn * delap) {
+                        if (sgn * (delap - alphap) >= bigm_tol) {
+                            alpham = (-2.0 * delap - 2.0 * sgn * sqrt(delap * delap - delap * alphap));
+                        } else {
+                            alpham = -2.0 * alphap;
+                        }
+                    }
+                }
+            }
+            sm = s0 + alpham;
+            sp = s0 + alphap;
+        }
+    }
+    const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
+    const FabView u = VW(fu);
+    const double up = UMAC ? at(u, i + di, j + dj, k + dk, uc) : at(u, i, j, k, uc);
+    const double um = at(u, i, j, k, uc);
+    double ip = s0, im = s0;
+    if (up > rel_eps) {
+        const double sigma = fabs(up) * dt / dxd;
+        ip = sp - 0.5 * sigma * (sp - sm - (1.0 - 2.0 / 3.0 * sigma) * s6);
+    }
+    if (um < -rel_eps) {
+        const double sigma = fabs(um) * dt / dxd;
+        im = sm + 0.5 * sigma * (sp - sm + (1.0 - 2.0 / 3.0 * sigma) * s6);
+    }
+    at(VW(fip), i, j, k, D) = ip;
+    at(VW(fim), i, j, k, D) = im;
+}
+
+// Limited slopes for ppm_type 0 (Maestro::Slopex/y/z, Source/MaestroSlopes.cpp:6-600).
+template <int D>
+__global__ void k_slope(KARGS, int fs, int sc, int fout, int oc, int ncomp, const BCRecD* __restrict__ bcs, int bc_c0,
+                        int slope_order, int ilo, int ihi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const FabView s = VW(fs);
+    const FabView o = VW(fout);
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    for (int n = 0; n < ncomp; ++n) {
+        auto S = SHIFT_S(s, sc + n);
+        const int bclo = bcs[bc_c0 + n].lo[D], bchi = bcs[bc_c0 + n].hi[D];
+        const bool lo_ext = (bclo == BC_EXT_DIR || bclo == BC_HOEXTRAP);
+        const bool hi_ext = (bchi == BC_EXT_DIR || bchi == BC_HOEXTRAP);
+        double out = 0.0;
+        if (slope_order == 2) {
+            double del = 0.5 * (S(1) - S(-1));
+            double dpls = 2.0 * (S(1) - S(0));
+            double dmin = 2.0 * (S(0) - S(-1));
+            double slim = mn(fabs(dpls), fabs(dmin));
+            slim = dpls * dmin > 0.0 ? slim : 0.0;
+            double sflag = copysign(1.0, del);
+            out = sflag * mn(slim, fabs(del));
+            if (lo_ext) {
+                if (I == ilo - 1) {
+                    out = 0.0;
+                } else if (I == ilo) {
+                    del = (S(1) + 3.0 * S(0) - 4.0 * S(-1)) / 3.0;
+                    dpls = 2.0 * (S(1) - S(0));
+                    dmin = 2.0 * (S(0) - S(-1));
+                    slim = mn(fabs(dpls), fabs(dmin));
+                    slim = dpls * dmin > 0.0 ? slim : 0.0;
+                    sflag = copysign(1.0, del);
+                    out = sflag * mn(slim, fabs(del));
+                }
+            }
+            if (hi_ext) {
+                if (I == ihi + 1) {
+                    out = 0.0;
+                } else if (I == ihi) {
+                    del = -(S(-1) + 3.0 * S(0) - 4.0 * S(1)) / 3.0;
+                    dpls = 2.0 * (S(0) - S(-1));
+                    dmin = 2.0 * (S(1) - S(0));
+                    slim = mn(fabs(dpls), fabs(dmin));
+                    slim = dpls * dmin > 0.0 ? slim : 0.0;
+                    sflag = copysign(1.0, del);
+                    out = sflag * mn(slim, fabs(del));
+                }
+            }
+        } else if (slope_order == 4) {
+            double dcen = 0.5 * (S(0) - S(-2));
+            double dmin = 2.0 * (S(-1) - S(-2));
+            double dpls = 2.0 * (S(0) - S(-1));
+            double dlim = mn(fabs(dmin), fabs(dpls));
+            dlim = dpls * dmin > 0.0 ? dlim : 0.0;
+            double dflag = copysign(1.0, dcen);
+            double dxl = dflag * mn(dlim, fabs(dcen));
+            dcen = 0.5 * (S(2) - S(0));
+            dmin = 2.0 * (S(1) - S(0));
+            dpls = 2.0 * (S(2) - S(1));
+            dlim = mn(fabs(dmin), fabs(dpls));
+            dlim = dpls * dmin > 0.0 ? dlim : 0.0;
+            dflag = copysign(1.0, dcen);
+            double dxr = dflag * mn(dlim, fabs(dcen));
+            dcen = 0.5 * (S(1) - S(-1));
+            dmin = 2.0 * (S(0) - S(-1));
+            dpls = 2.0 * (S(1) - S(0));
+            dlim = mn(fabs(dmin), fabs(dpls));
+            dlim = dpls * dmin > 0.0 ? dlim : 0.0;
+            dflag = copysign(1.0, dcen);
+            double ds = 4.0 / 3.0 * dcen - (dxr + dxl) / 6.0;
+            out = dflag * mn(fabs(ds), dlim);
+            // the x sweep tests the centred dlim where y and z test the one-sided slim
+            if (lo_ext) {
+                if (I == ilo - 1) {
+                    out = 0.0;
+                } else if (I == ilo) {
+                    double del = -16.0 / 15.0 * S(-1) + 0.5 * S(0) + 2.0 / 3.0 * S(1) - 0.1 * S(2);
+                    dmin = 2.0 * (S(0) - S(-1));
+                    dpls = 2.0 * (S(1) - S(0));
+                    double slim = mn(fabs(dpls), fabs(dmin));
+                    slim = dpls * dmin > 0.0 ? (D == 0 ? dlim : slim) : 0.0;
+                    double sflag = copysign(1.0, del);
+                    out = sflag * mn(slim, fabs(del));
+                } else if (I == ilo + 1) {
+                    double del = -16.0 / 15.0 * S(-2) + 0.5 * S(-1) + 2.0 / 3.0 * S(0) - 0.1 * S(1);
+                    dmin = 2.0 * (S(-1) - S(-2));
+                    dpls = 2.0 * (S(0) - S(-1));
+                    double slim = mn(fabs(dpls), fabs(dmin));
+                    slim = dpls * dmin > 0.0 ? (D == 0 ? dlim : slim) : 0.0;
+                    double sflag = copysign(1.0, del);
+                    dxl = sflag * mn(slim, fabs(del));
+                    ds = 4.0 / 3.0 * dcen - (dxr + dxl) / 6.0;
+                    out = dflag * mn(fabs(ds), dlim);
+                }
+            }
+            if (hi_ext) {
+                if (I == ihi + 1) {
+                    out = 0.0;
+                } else if (I == ihi) {
+                    double del = -(-16.0 / 15.0 * S(1) + 0.5 * S(0) + 2.0 / 3.0 * S(-1) - 0.1 * S(-2));
+                    dmin = 2.0 * (S(0) - S(-1));
+                    dpls = 2.0 * (S(1) - S(0));
+                    double slim = mn(fabs(dpls), fabs(dmin));
+                    slim = dpls * dmin > 0.0 ? (D == 0 ? dlim : slim) : 0.0;
+                    double sflag = copysign(1.0, del);
+                    out = sflag * mn(slim, fabs(del));
+                } else if (I == ihi - 1) {
+                    double del = -(-16.0 / 15.0 * S(2) + 0.5 * S(1) + 2.0 / 3.0 * S(0) - 0.1 * S(-1));
+                    dmin = 2.0 * (S(1) - S(0));
+                    dpls = 2.0 * (S(2) - S(1));
+                    double slim = mn(fabs(dpls), fabs(dmin));
+                    slim = dpls * dmin > 0.0 ? (D == 0 ? dlim : slim) : 0.0;
+                    double sflag = copysign(1.0, del);
+                    dxr = sflag * mn(slim, fabs(del));
+                    ds = 4.0 / 3.0 * dcen - (dxl + dxr) / 6.0;
+                    out = dflag * mn(fabs(ds), dlim);
+                }
+            }
+        }
+        at(o, i, j, k, oc + n) = out;
+    }
+}
+
+static bool ext_like(int t) { return t == BC_EXT_DIR || t == BC_HOEXTRAP; }
+
+// PPM of component sc of field fs in direction D into fip/fim comp D over the box grown
+// by one cell.  fu/uc: tracing velocity (face field if umac, else cell field comp uc).
+template <int D>
+static void ppm_dir(Ctx& c, int fs, int sc, const BCRecD& bc, int fu, int uc, int umac, int fip, int fim) {
+    const int lo_ext = ext_like(bc.lo[D]), hi_ext = ext_like(bc.hi[D]);
+    const int dlo = c.P.dom_lo[D], dhi = c.P.dom_hi[D];
+    const int gf = c.P.ppm_type == 2 ? 2 : 1;
+    int glo[3] = {1, 1, 1}, ghi[3] = {1, 1, 1};
+    glo[D] = gf;
+    ghi[D] = gf;
+    const RegionTable& rf = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], D);
+    const int ff = F_FACE0 + D;
+    if (c.P.ppm_type == 1)
+        launch(c, rf, 1, k_ppm_face<D, 1>, c.V(), fs, sc, ff, lo_ext, hi_ext, dlo, dhi);
+    else
+        launch(c, rf, 1, k_ppm_face<D, 2>, c.V(), fs, sc, ff, lo_ext, hi_ext, dlo, dhi);
+    const RegionTable& rc = rg_grow(c, 1);
+    const double dt = c.P.dt, re = c.P.rel_eps, dxd = c.P.dx[D];
+    if (c.P.ppm_type == 1) {
+        if (umac) launch(c, rc, 1, k_ppm_cell<D, 1, 1>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
+        else launch(c, rc, 1, k_ppm_cell<D, 1, 0>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
+    } else {
+        if (umac) launch(c, rc, 1, k_ppm_cell<D, 2, 1>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
+        else launch(c, rc, 1, k_ppm_cell<D, 2, 0>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
+    }
+}
+
+static void ppm_any(Ctx& c, int d, int fs, int sc, const BCRecD& bc, int fu, int uc, int umac, int fip, int fim) {
+    if (d == 0) ppm_dir<0>(c, fs, sc, bc, fu, uc, umac, fip, fim);
+    else if (d == 1) ppm_dir<1>(c, fs, sc, bc, fu, uc, umac, fip, fim);
+    else ppm_dir<2>(c, fs, sc, bc, fu, uc, umac, fip, fim);
+}
+
+static void slope_any(Ctx& c, int d, int fs, int sc, int fout, int oc, int ncomp, const BCRecD* bcs_d, int bc_c0) {
+    const RegionTable& rc = rg_grow(c, 1);
+    const int lo = c.P.dom_lo[d], hi = c.P.dom_hi[d], so = c.P.slope_order;
+    if (d == 0) launch(c, rc, 1, k_slope<0>, c.V(), fs, sc, fout, oc, ncomp, bcs_d, bc_c0, so, lo, hi);
+    else if (d == 1) launch(c, rc, 1, k_slope<1>, c.V(), fs, sc, fout, oc, ncomp, bcs_d, bc_c0, so, lo, hi);
+    else launch(c, rc, 1, k_slope<2>, c.V(), fs, sc, fout, oc, ncomp, bcs_d, bc_c0, so, lo, hi);
+}
+
+// ============================================================ MakeUtrans
+// Face kernel of Maestro::MakeUtrans, 3-D (Source/MaestroMakeUtrans.cpp:304-387, 419-502,
+// 535-627).  Planar: the z solve tests the full velocity w + w0_cart.
+template <int D>
+__global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const FabView ut = VW(F_UTILDE);
+    double l, r;
+    if (ppm_type == 0) {
+        const FabView uf = VW(F_UFULL);
+        const FabView sl = VW(F_SLOPE);
+        l = at(ut, i - di, j - dj, k - dk, D) + (0.5 - dt2dx * mx(0.0, at(uf, i - di, j - dj, k - dk, D))) * at(sl, i - di, j - dj, k - dk, 0);
+        r = at(ut, i, j, k, D) - (0.5 + dt2dx * mn(0.0, at(uf, i, j, k, D))) * at(sl, i, j, k, 0);
+    } else {
+        l = at(VW(F_IPC0), i - di, j - dj, k - dk, D);
+        r = at(VW(F_IMC0), i, j, k, D);
+    }
+    if (I == domlo) {
+        switch (bclo) {
+            case PB_INFLOW: l = at(ut, i - di, j - dj, k - dk, D); r = l; break;
+            case PB_SLIPWALL: case PB_NOSLIPWALL: case PB_SYMMETRY: l = 0.0; r = 0.0; break;
+            case PB_OUTFLOW: l = mn(r, 0.0); r = l; break;
+            default: break;
+        }
+    } else if (I == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW: l = at(ut, i + di, j + dj, k + dk, D); r = l; break;
+            case PB_SLIPWALL: case PB_NOSLIPWALL: case PB_SYMMETRY: l = 0.0; r = 0.0; break;
+            case PB_OUTFLOW: l = mx(l, 0.0); r = l; break;
+            default: break;
+        }
+    }
+    double v;
+    if (D < 2) {
+        const bool test = (l <= 0.0 && r >= 0.0) || (fabs(l + r) < rel_eps);
+        v = 0.5 * (l + r) > 0.0 ? l : r;
+        v = test ? 0.0 : v;
+    } else {
+        const double w0c = at(VW(F_W0CART), i, j, k, 2);
+        const bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fabs(l + r + 2.0 * w0c) < rel_eps);
+        v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+        v = test ? 0.0 : v;
+    }
+    at(VW(F_UTRANS0 + D), i, j, k) = v;
+}
+
+void make_utrans(Ctx& c) {
+    const double dt2 = 0.5 * c.P.dt;
+    for (int d = 0; d < 3; ++d) {
+        if (c.P.ppm_type == 0) {
+            slope_any(c, d, F_UTILDE, d, F_SLOPE, 0, 1, bcs_dev(c, BCS_U), d);
+        } else {
+            ppm_any(c, d, F_UTILDE, d, c.bcs_u[d], F_UFULL, d, 0, F_IPC0, F_IMC0);
+        }
+        const RegionTable& rt = rg_grow(c, 0, d);
+        const double dt2dx = dt2 / c.P.dx[d];
+        const int bl = c.P.phys_bc_lo[d], bh = c.P.phys_bc_hi[d], dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
+        if (d == 0) launch(c, rt, 1, k_utrans<0>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+        else if (d == 1) launch(c, rt, 1, k_utrans<1>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+        else launch(c, rt, 1, k_utrans<2>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+    }
+    fill_face_ghosts(c, F_UTRANS0);
+}
+
+// ============================================================ MakeVelForce
+// Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:100-126)
+__global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, double two_dz) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView gpi = VW(F_GPI), rho = VW(F_SOLD), vf = VW(F_VELFORCE);
+    const double r = at(rho, i, j, k, RHO);
+    double rhopert = r - at(VW(F_RHO0CART), i, j, k);
+    if (r < cutoff_rho) rhopert = 0.0;
+    for (int dim = 0; dim < 2; ++dim) at(vf, i, j, k, dim) = -at(gpi, i, j, k, dim) / r;
+    double f2 = (rhopert * at(VW(F_GRAVCART), i, j, k, 2) - at(gpi, i, j, k, 2)) / r - at(VW(F_W0FCART), i, j, k, 2);
+    if (k <= -1 || k >= domhi) {
+    } else {
+        const FabView we = VW(F_UTRANS2), w0 = VW(F_W0CART);
+        f2 -= (at(we, i, j, k + 1) + at(we, i, j, k)) * (at(w0, i, j, k + 1, 2) - at(w0, i, j, k, 2)) / two_dz;
+    }
+    at(vf, i, j, k, 2) = f2;
+}
+
+void make_vel_force(Ctx& c) {
+    // grav_cart (vector, bcs_f) and rho0_cart (rho0_old, bcs_s Rho)
+    set_val(c, F_GRAVCART, 0.0, 0, 3, 1);
+    put1d(c, F_GRAVCART, c.b1("grav_cell"), 2, 0);
+    fill_patch(c, F_GRAVCART, 0, 3, BCS_F, 0, 0, -1);
+    set_val(c, F_RHO0CART, 0.0, 0, 1, 1);
+    put1d(c, F_RHO0CART, c.b1("rho0_old"), 0, 0);
+    fill_patch(c, F_RHO0CART, 0, 1, BCS_S, RHO, 0, RHO);
+    set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
+    launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
+           c.P.dom_hi[2], 2.0 * c.P.dx[2]);
+    fill_patch(c, F_VELFORCE, 0, 3, BCS_U, 0, 1, -1);
+}
+
+// ============================================================ VelPred
+// VelPredInterface, 3-D (Source/MaestroVelPred.cpp:735-1128): predictor states of all
+// three velocity components on D-faces, and their upwind values.
+template <int D>
+__global__ void k_vp_interface(KARGS, int ppm_type, double dt2, double hd, int bclo, int bchi, int domlo, int domhi,
+                               double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView ut = VW(F_UTILDE);
+    double l[3], r[3];
+    if (ppm_type == 0) {
+        const FabView uf = VW(F_UFULL);
+        const FabView sl = D == 0 ? VW(F_IPC0) : (D == 1 ? VW(F_IMC1) : VW(F_IMC2));
+        const double maxu = 0.5 - dt2 * mx(0.0, at(uf, il, jl, kl, D)) / hd;
+        const double minu = 0.5 + dt2 * mn(0.0, at(uf, i, j, k, D)) / hd;
+        for (int n = 0; n < 3; ++n) {
+            l[n] = at(ut, il, jl, kl, n) + maxu * at(sl, il, jl, kl, n);
+            r[n] = at(ut, i, j, k, n) - minu * at(sl, i, j, k, n);
+        }
+    } else {
+        const FabView ip[3] = {VW(F_IPC0), VW(F_IPC1), VW(F_IPC2)};
+        const FabView im[3] = {VW(F_IMC0), VW(F_IMC1), VW(F_IMC2)};
+        for (int n = 0; n < 3; ++n) {
+            l[n] = at(ip[n], il, jl, kl, D);
+            r[n] = at(im[n], i, j, k, D);
+        }
+    }
+    if (I == domlo) {
+        switch (bclo) {
+            case PB_INFLOW:
+                for (int n = 0; n < 3; ++n) { l[n] = at(ut, il, jl, kl, n); r[n] = l[n]; }
+                break;
+            case PB_SLIPWALL: case PB_SYMMETRY:
+                for (int n = 0; n < 3; ++n) {
+                    if (n == D) { l[n] = 0.0; r[n] = 0.0; }
+                    else l[n] = r[n];
+                }
+                break;
+            case PB_NOSLIPWALL:
+                for (int n = 0; n < 3; ++n) { l[n] = 0.0; r[n] = 0.0; }
+                break;
+            case PB_OUTFLOW:
+                r[D] = mn(r[D], 0.0);
+                for (int n = 0; n < 3; ++n) l[n] = r[n];
+                break;
+            default: break;
+        }
+    } else if (I == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW:
+                for (int n = 0; n < 3; ++n) { l[n] = at(ut, i, j, k, n); r[n] = l[n]; }
+                break;
+            case PB_SLIPWALL: case PB_SYMMETRY:
+                for (int n = 0; n < 3; ++n) {
+                    if (n == D) { l[n] = 0.0; r[n] = 0.0; }
+                    else r[n] = l[n];
+                }
+                break;
+            case PB_NOSLIPWALL:
+                for (int n = 0; n < 3; ++n) { l[n] = 0.0; r[n] = 0.0; }
+                break;
+            case PB_OUTFLOW:
+                l[D] = mx(l[D], 0.0);
+                for (int n = 0; n < 3; ++n) r[n] = l[n];
+                break;
+            default: break;
+        }
+    }
+    const FabView L = VW(F_SL0 + D), Rr = VW(F_SR0 + D), M = VW(F_SIMH0 + D);
+    const double tr = at(VW(F_UTRANS0 + D), i, j, k);
+    for (int n = 0; n < 3; ++n) {
+        at(L, i, j, k, n) = l[n];
+        at(Rr, i, j, k, n) = r[n];
+        if (n == D) continue;
+        const double v = tr > 0.0 ? l[n] : r[n];
+        at(M, i, j, k, n) = fabs(tr) < rel_eps ? 0.5 * (l[n] + r[n]) : v;
+    }
+}
+
+// VelPredTransverse (Source/MaestroVelPred.cpp:1130-1595): component C on D-faces
+// corrected in the third direction T.
+template <int C, int D>
+__global__ void k_vp_transverse(KARGS, double dt6h, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int T = 3 - C - D;
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView L = VW(F_SL0 + D), Rr = VW(F_SR0 + D), trt = VW(F_UTRANS0 + T), imt = VW(F_SIMH0 + T);
+    double lq = at(L, i, j, k, C) - dt6h * (at(trt, il + ti, jl + tj, kl + tk) + at(trt, il, jl, kl)) *
+                                        (at(imt, il + ti, jl + tj, kl + tk, C) - at(imt, il, jl, kl, C));
+    double rq = at(Rr, i, j, k, C) - dt6h * (at(trt, i + ti, j + tj, k + tk) + at(trt, i, j, k)) *
+                                         (at(imt, i + ti, j + tj, k + tk, C) - at(imt, i, j, k, C));
+    const FabView ut = VW(F_UTILDE);
+    if (I == domlo) {
+        switch (bclo) {
+            case PB_INFLOW: lq = at(ut, il, jl, kl, C); rq = lq; break;
+            case PB_SLIPWALL: case PB_SYMMETRY: case PB_OUTFLOW: lq = rq; break;
+            case PB_NOSLIPWALL: lq = 0.0; rq = 0.0; break;
+            default: break;
+        }
+    } else if (I == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW: lq = at(ut, i, j, k, C); rq = lq; break;
+            case PB_SLIPWALL: case PB_SYMMETRY: case PB_OUTFLOW: rq = lq; break;
+            case PB_NOSLIPWALL: lq = 0.0; rq = 0.0; break;
+            default: break;
+        }
+    }
+    const double trd = at(VW(F_UTRANS0 + D), i, j, k);
+    const double v = trd > 0.0 ? lq : rq;
+    at(VW(Q_FIELD(C, D)), i, j, k) = fabs(trd) < rel_eps ? 0.5 * (lq + rq) : v;
+}
+
+// VelPredVelocities (Source/MaestroVelPred.cpp:1597-1915)
+template <int D>
+__global__ void k_vp_velocities(KARGS, double dt2, double dt4h1, double dt4h2, int bclo, int bchi, int domlo,
+                                int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    constexpr int a1i = T1 == 0, a1j = T1 == 1, a1k = T1 == 2;
+    constexpr int a2i = T2 == 0, a2j = T2 == 1, a2k = T2 == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView tr1 = VW(F_UTRANS0 + T1), tr2 = VW(F_UTRANS0 + T2);
+    const FabView q1 = VW(Q_FIELD(D, T1)), q2 = VW(Q_FIELD(D, T2));
+    const FabView f = VW(F_VELFORCE);
+    const double fl = at(f, il, jl, kl, D);
+    const double fr = at(f, i, j, k, D);
+    const double ml = at(VW(F_SL0 + D), i, j, k, D) -
+                      dt4h1 * (at(tr1, il + a1i, jl + a1j, kl + a1k) + at(tr1, il, jl, kl)) *
+                          (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
+                      dt4h2 * (at(tr2, il + a2i, jl + a2j, kl + a2k) + at(tr2, il, jl, kl)) *
+                          (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
+                      dt2 * fl;
+    const double mr = at(VW(F_SR0 + D), i, j, k, D) -
+                      dt4h1 * (at(tr1, i + a1i, j + a1j, k + a1k) + at(tr1, i, j, k)) *
+                          (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
+                      dt4h2 * (at(tr2, i + a2i, j + a2j, k + a2k) + at(tr2, i, j, k)) *
+                          (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
+                      dt2 * fr;
+    double v;
+    if (D < 2) {
+        const bool test = (ml <= 0.0 && mr >= 0.0) || (fabs(ml + mr) < rel_eps);
+        v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+        v = test ? 0.0 : v;
+    } else {
+        const double w0c = at(VW(F_W0CART), i, j, k, 2);
+        const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fabs(ml + mr + 2.0 * w0c) < rel_eps);
+        v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+        v = test ? 0.0 : v;
+    }
+    const FabView ut = VW(F_UTILDE);
+    if (I == domlo) {
+        switch (bclo) {
+            case PB_INFLOW: v = at(ut, il, jl, kl, D); break;
+            case PB_SLIPWALL: case PB_SYMMETRY: case PB_NOSLIPWALL: v = 0.0; break;
+            case PB_OUTFLOW: v = mn(mr, 0.0); break;
+            default: break;
+        }
+    } else if (I == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW: v = at(ut, i, j, k, D); break;
+            case PB_SLIPWALL: case PB_SYMMETRY: case PB_NOSLIPWALL: v = 0.0; break;
+            case PB_OUTFLOW: v = mx(ml, 0.0); break;
+            default: break;
+        }
+    }
+    at(VW(F_UMAC0 + D), i, j, k) = v;
+}
+
+template <int C, int D>
+static void vp_transverse_launch(Ctx& c, double dt6) {
+    constexpr int T = 3 - C - D;
+    int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
+    glo[C] = 1;
+    ghi[C] = 1;
+    ghi[D] = 1;
+    const RegionTable& rt = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1);
+    launch(c, rt, 1, k_vp_transverse<C, D>, c.V(), dt6 / c.P.dx[T], c.P.phys_bc_lo[D], c.P.phys_bc_hi[D],
+           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+}
+
+template <int D>
+static void vp_interface_launch(Ctx& c) {
+    int glo[3] = {1, 1, 1};
+    glo[D] = 0;
+    const RegionTable& rt = region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1);
+    launch(c, rt, 1, k_vp_interface<D>, c.V(), c.P.ppm_type, 0.5 * c.P.dt, c.P.dx[D], c.P.phys_bc_lo[D],
+           c.P.phys_bc_hi[D], c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+}
+
+template <int D>
+static void vp_velocities_launch(Ctx& c) {
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    const double dt4 = 0.25 * c.P.dt;
+    launch(c, rg_grow(c, 0, D), 1, k_vp_velocities<D>, c.V(), 0.5 * c.P.dt, dt4 / c.P.dx[T1], dt4 / c.P.dx[T2],
+           c.P.phys_bc_lo[D], c.P.phys_bc_hi[D], c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+}
+
+void vel_pred(Ctx& c) {
+    if (c.P.ppm_type == 0) {
+        slope_any(c, 0, F_UTILDE, 0, F_IPC0, 0, 3, bcs_dev(c, BCS_U), 0);  // slopex -> Ipu
+        slope_any(c, 1, F_UTILDE, 0, F_IMC1, 0, 3, bcs_dev(c, BCS_U), 0);  // slopey -> Imv
+        slope_any(c, 2, F_UTILDE, 0, F_IMC2, 0, 3, bcs_dev(c, BCS_U), 0);  // slopez -> Imw
+    } else {
+        for (int cc = 0; cc < 3; ++cc)
+            for (int d = 0; d < 3; ++d) ppm_any(c, d, F_UTILDE, cc, c.bcs_u[cc], F_UFULL, d, 0, F_IPC0 + cc, F_IMC0 + cc);
+    }
+    vp_interface_launch<0>(c);
+    vp_interface_launch<1>(c);
+    vp_interface_launch<2>(c);
+    const double dt6 = c.P.dt / 6.0;
+    vp_transverse_launch<0, 1>(c, dt6);
+    vp_transverse_launch<0, 2>(c, dt6);
+    vp_transverse_launch<1, 0>(c, dt6);
+    vp_transverse_launch<1, 2>(c, dt6);
+    vp_transverse_launch<2, 0>(c, dt6);
+    vp_transverse_launch<2, 1>(c, dt6);
+    vp_velocities_launch<0>(c);
+    vp_velocities_launch<1>(c);
+    vp_velocities_launch<2>(c);
+}
+
+// ============================================================ MakeEdgeScal
+// MakeDivU (Source/MaestroMakeEdgeScalars.cpp:648-660)
+__global__ void k_divu(KARGS, double dx0) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView u = VW(F_UMAC0), v = VW(F_UMAC1), w = VW(F_UMAC2);
+    double d = at(u, i + 1, j, k) - at(u, i, j, k) + at(v, i, j + 1, k) - at(v, i, j, k) + at(w, i, j, k + 1) -
+               at(w, i, j, k);
+    d /= dx0;
+    at(VW(F_DIVU), i, j, k) = d;
+}
+
+// MakeEdgeScalPredictor, 3-D (Source/MaestroMakeEdgeScalars.cpp:662-863)
+template <int D>
+__global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double hd, int bclo, int bchi, int domlo,
+                               int domhi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView sc = VW(F_SOLD);
+    const double ud = at(VW(F_UMAC0 + D), i, j, k);
+    double l, r;
+    if (ppm_type == 0) {
+        const FabView sl = VW(F_SLOPE);
+        l = at(sc, il, jl, kl, comp) + 0.5 * (1.0 - dt * ud / hd) * at(sl, il, jl, kl, D);
+        r = at(sc, i, j, k, comp) - 0.5 * (1.0 + dt * ud / hd) * at(sl, i, j, k, D);
+    } else {
+        l = at(VW(F_IPC0), il, jl, kl, D);
+        r = at(VW(F_IMC0), i, j, k, D);
+    }
+    if (I == domlo) {
+        if (bclo == BC_EXT_DIR) {
+            l = at(sc, il, jl, kl, comp);
+            r = l;
+        } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
+            l = r;
+        } else if (bclo == BC_REFLECT_ODD) {
+            l = 0.0;
+            r = 0.0;
+        }
+    } else if (I == domhi + 1) {
+        if (bchi == BC_EXT_DIR) {
+            l = at(sc, i, j, k, comp);
+            r = l;
+        } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
+            r = l;
+        } else if (bchi == BC_REFLECT_ODD) {
+            l = 0.0;
+            r = 0.0;
+        }
+    }
+    double sm = (ud > 0.0) ? l : r;
+    sm = (fabs(ud) > 0.0) ? sm : 0.5 * (l + r);
+    at(VW(F_SL0 + D), i, j, k) = l;
+    at(VW(F_SR0 + D), i, j, k) = r;
+    at(VW(F_SIMH0 + D), i, j, k) = sm;
+}
+
+// MakeEdgeScalTransverse, 3-D (Source/MaestroMakeEdgeScalars.cpp:865-1359): D-faces
+// corrected in direction T.
+template <int D, int T>
+__global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double dt3h, double dt6h, int bclo, int bchi,
+                                int domlo, int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView st = VW(F_SIMH0 + T), ut = VW(F_UMAC0 + T), sc = VW(F_SOLD);
+    double lq, rq;
+    if (is_cons) {
+        const FabView dv = VW(F_DIVU);
+        lq = at(VW(F_SL0 + D), i, j, k) -
+             dt3h * (at(st, il + ti, jl + tj, kl + tk) * at(ut, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl) * at(ut, il, jl, kl)) -
+             dt3 * at(sc, il, jl, kl, comp) * at(dv, il, jl, kl) +
+             dt3h * at(sc, il, jl, kl, comp) * (at(ut, il + ti, jl + tj, kl + tk) - at(ut, il, jl, kl));
+        rq = at(VW(F_SR0 + D), i, j, k) -
+             dt3h * (at(st, i + ti, j + tj, k + tk) * at(ut, i + ti, j + tj, k + tk) - at(st, i, j, k) * at(ut, i, j, k)) -
+             dt3 * at(sc, i, j, k, comp) * at(dv, i, j, k) +
+             dt3h * at(sc, i, j, k, comp) * (at(ut, i + ti, j + tj, k + tk) - at(ut, i, j, k));
+    } else {
+        lq = at(VW(F_SL0 + D), i, j, k) - dt6h * (at(ut, il + ti, jl + tj, kl + tk) + at(ut, il, jl, kl)) *
+                                               (at(st, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl));
+        rq = at(VW(F_SR0 + D), i, j, k) - dt6h * (at(ut, i + ti, j + tj, k + tk) + at(ut, i, j, k)) *
+                                               (at(st, i + ti, j + tj, k + tk) - at(st, i, j, k));
+    }
+    if (I == domlo) {
+        if (bclo == BC_EXT_DIR) {
+            lq = at(sc, il, jl, kl, comp);
+            rq = lq;
+        } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
+            lq = rq;
+        } else if (bclo == BC_REFLECT_ODD) {
+            lq = 0.0;
+            rq = 0.0;
+        }
+    } else if (I == domhi + 1) {
+        if (bchi == BC_EXT_DIR) {
+            lq = at(sc, i, j, k, comp);
+            rq = lq;
+        } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
+            rq = lq;
+        } else if (bchi == BC_REFLECT_ODD) {
+            lq = 0.0;
+            rq = 0.0;
+        }
+    }
+    const double ud = at(VW(F_UMAC0 + D), i, j, k);
+    double v = (ud > 0.0) ? lq : rq;
+    v = (fabs(ud) > rel_eps) ? v : 0.5 * (lq + rq);
+    at(VW(Q_FIELD(D, T)), i, j, k) = v;
+}
+
+// MakeEdgeScalEdges, 3-D (Source/MaestroMakeEdgeScalars.cpp:1361-1667)
+template <int D>
+__global__ void k_es_edges(KARGS, int comp, int is_cons, double dt2, double dt2h1, double dt2h2, double dt2hd,
+                           double dt4h1, double dt4h2, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    constexpr int a1i = T1 == 0, a1j = T1 == 1, a1k = T1 == 2;
+    constexpr int a2i = T2 == 0, a2j = T2 == 1, a2k = T2 == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView q1 = VW(Q_FIELD(T1, T2)), q2 = VW(Q_FIELD(T2, T1));
+    const FabView u1 = VW(F_UMAC0 + T1), u2 = VW(F_UMAC0 + T2), udf = VW(F_UMAC0 + D);
+    const FabView sc = VW(F_SOLD), f = VW(F_SCALFORCE);
+    const double fl = at(f, il, jl, kl, comp);
+    const double fr = at(f, i, j, k, comp);
+    double lq, rq;
+    if (is_cons) {
+        lq = at(VW(F_SL0 + D), i, j, k) -
+             dt2h1 * (at(q1, il + a1i, jl + a1j, kl + a1k) * at(u1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl) * at(u1, il, jl, kl)) -
+             dt2h2 * (at(q2, il + a2i, jl + a2j, kl + a2k) * at(u2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl) * at(u2, il, jl, kl)) -
+             dt2hd * at(sc, il, jl, kl, comp) * (at(udf, i, j, k) - at(udf, il, jl, kl)) + dt2 * fl;
+        rq = at(VW(F_SR0 + D), i, j, k) -
+             dt2h1 * (at(q1, i + a1i, j + a1j, k + a1k) * at(u1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k) * at(u1, i, j, k)) -
+             dt2h2 * (at(q2, i + a2i, j + a2j, k + a2k) * at(u2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k) * at(u2, i, j, k)) -
+             dt2hd * at(sc, i, j, k, comp) * (at(udf, i + di, j + dj, k + dk) - at(udf, i, j, k)) + dt2 * fr;
+    } else {
+        lq = at(VW(F_SL0 + D), i, j, k) -
+             dt4h1 * (at(u1, il + a1i, jl + a1j, kl + a1k) + at(u1, il, jl, kl)) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
+             dt4h2 * (at(u2, il + a2i, jl + a2j, kl + a2k) + at(u2, il, jl, kl)) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
+             dt2 * fl;
+        rq = at(VW(F_SR0 + D), i, j, k) -
+             dt4h1 * (at(u1, i + a1i, j + a1j, k + a1k) + at(u1, i, j, k)) * (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
+             dt4h2 * (at(u2, i + a2i, j + a2j, k + a2k) + at(u2, i, j, k)) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
+             dt2 * fr;
+    }
+    const double ud = at(udf, i, j, k);
+    double v = (ud > 0.0) ? lq : rq;
+    v = (fabs(ud) > rel_eps) ? v : 0.5 * (lq + rq);
+    if (I == domlo) {
+        if (bclo == BC_EXT_DIR) v = at(sc, il, jl, kl, comp);
+        else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) v = rq;
+        else if (bclo == BC_REFLECT_ODD) v = 0.0;
+    } else if (I == domhi + 1) {
+        if (bchi == BC_EXT_DIR) v = at(sc, i, j, k, comp);
+        else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) v = lq;
+        else if (bchi == BC_REFLECT_ODD) v = 0.0;
+    }
+    at(VW(F_SEDGE0 + D), i, j, k, comp) = v;
+}
+
+template <int D>
+static void es_predictor_launch(Ctx& c, int comp, const BCRecD& bc) {
+    int glo[3] = {1, 1, 1};
+    glo[D] = 0;
+    const RegionTable& rt = region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1);
+    launch(c, rt, 1, k_es_predictor<D>, c.V(), comp, c.P.ppm_type, c.P.dt, c.P.dx[D], bc.lo[D], bc.hi[D],
+           c.P.dom_lo[D], c.P.dom_hi[D]);
+}
+
+template <int D, int T>
+static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons) {
+    constexpr int O = 3 - D - T;
+    int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
+    glo[O] = 1;
+    ghi[O] = 1;
+    ghi[D] = 1;
+    const RegionTable& rt = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1);
+    const double dt3 = c.P.dt / 3.0, dt6 = c.P.dt / 6.0;
+    launch(c, rt, 1, k_es_transverse<D, T>, c.V(), comp, is_cons, dt3, dt3 / c.P.dx[T], dt6 / c.P.dx[T], bc.lo[D],
+           bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+}
+
+template <int D>
+static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons) {
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    const double dt2 = 0.5 * c.P.dt, dt4 = 0.25 * c.P.dt;
+    launch(c, rg_grow(c, 0, D), 1, k_es_edges<D>, c.V(), comp, is_cons, dt2, dt2 / c.P.dx[T1], dt2 / c.P.dx[T2],
+           dt2 / c.P.dx[D], dt4 / c.P.dx[T1], dt4 / c.P.dx[T2], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
+           c.P.rel_eps);
+}
+
+void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons) {
+    const BCRecD* bh = bcs_host(c, which_bcs);
+    if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), c.P.dx[0]);
+    for (int comp = start_comp; comp < start_comp + num_comp; ++comp) {
+        const BCRecD& bc = bh[comp];  // start_bccomp == start_scomp at every call site
+        if (c.P.ppm_type == 0) {
+            for (int d = 0; d < 3; ++d) slope_any(c, d, F_SOLD, comp, F_SLOPE, d, 1, bcs_dev(c, which_bcs), comp);
+        } else {
+            for (int d = 0; d < 3; ++d) ppm_any(c, d, F_SOLD, comp, bc, F_UMAC0 + d, 0, 1, F_IPC0, F_IMC0);
+        }
+        es_predictor_launch<0>(c, comp, bc);
+        es_predictor_launch<1>(c, comp, bc);
+        es_predictor_launch<2>(c, comp, bc);
+        es_transverse_launch<0, 1>(c, comp, bc, is_cons);
+        es_transverse_launch<0, 2>(c, comp, bc, is_cons);
+        es_transverse_launch<1, 0>(c, comp, bc, is_cons);
+        es_transverse_launch<1, 2>(c, comp, bc, is_cons);
+        es_transverse_launch<2, 0>(c, comp, bc, is_cons);
+        es_transverse_launch<2, 1>(c, comp, bc, is_cons);
+        es_edges_launch<0>(c, comp, bc, is_cons);
+        es_edges_launch<1>(c, comp, bc, is_cons);
+        es_edges_launch<2>(c, comp, bc, is_cons);
+    }
+}
+
+// ============================================================ forces
+// ModifyScalForce, planar 3-D (Source/MaestroForce.cpp:413-441)
+__global__ void k_modify_scal_force(KARGS, int comp, int s0cart, int fullform, double dx0, double dx1, double dx2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
+    const FabView s0a = VW(s0cart), s0e = VW(F_S0ECART), w0a = VW(F_W0CART);
+    const double scal = at(VW(F_SOLD), i, j, k, comp);
+    double divu = (at(um, i + 1, j, k) - at(um, i, j, k)) / dx0 + (at(vm, i, j + 1, k) - at(vm, i, j, k)) / dx1 +
+                  (at(wm, i, j, k + 1) - at(wm, i, j, k)) / dx2;
+    divu += (at(w0a, i, j, k + 1, 2) - at(w0a, i, j, k, 2)) / dx2;
+    double& force = at(VW(F_SCALFORCE), i, j, k, comp);
+    if (fullform == 1) {
+        force -= scal * divu;
+    } else {
+        const double s0 = at(s0a, i, j, k);
+        const double divs0u =
+            s0 * ((at(um, i + 1, j, k) - at(um, i, j, k)) / dx0 + (at(vm, i, j + 1, k) - at(vm, i, j, k)) / dx1) +
+            (at(wm, i, j, k + 1) * at(s0e, i, j, k + 1) - at(wm, i, j, k) * at(s0e, i, j, k)) / dx2;
+        force += -(scal - s0) * divu - divs0u;
+    }
+}
+
+void modify_scal_force(Ctx& c, int comp, const double* d_s0_edge, int s0cart_fid, int fullform) {
+    set_val(c, F_S0ECART, 0.0, 0, 1, 1);
+    put1d(c, F_S0ECART, d_s0_edge, 0, 0);
+    fill_patch(c, F_S0ECART, 0, 1, BCS_F, 0, 0, -1);
+    launch(c, rg_grow(c, 0), 1, k_modify_scal_force, c.V(), comp, s0cart_fid, fullform, c.P.dx[0], c.P.dx[1],
+           c.P.dx[2]);
+    fill_patch(c, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
+}
+
+// MakeRhoHForce, planar 3-D (Source/MaestroForce.cpp:602-627)
+__global__ void k_rhoh_force(KARGS, int cutoff, int domhi, double dz, int psi_in, int add_thermal) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView p0c = VW(F_P0CART);
+    double gradp0 = 0.0;
+    if (k < cutoff) {
+        gradp0 = at(VW(F_RHO0CART), i, j, k) * at(VW(F_GRAVCART), i, j, k, 2);
+    } else if (k == domhi) {
+        gradp0 = (at(p0c, i, j, k) - at(p0c, i, j - 1, k)) / dz;
+    } else {
+        gradp0 = (at(p0c, i, j + 1, k) - at(p0c, i, j, k)) / dz;
+    }
+    const FabView wm = VW(F_UMAC2);
+    const double veladv = 0.5 * (at(wm, i, j, k) + at(wm, i, j, k + 1));
+    double f = veladv * gradp0;
+    if (psi_in) f += at(VW(F_PSICART), i, j, k);
+    if (add_thermal == 1) f += at(VW(F_THERMAL), i, j, k);
+    at(VW(F_SCALFORCE), i, j, k, RHOH) = f;
+}
+
+void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal, int which_step) {
+    // which_step 1: rho0 = rho0_old, p0 = p0_old (which_step 2 averages old and new)
+    (void)which_step;
+    const char* r0 = "rho0_old";
+    const char* p0 = "p0_old";
+    set_val(c, F_P0CART, 0.0, 0, 1, 1);
+    put1d(c, F_P0CART, c.b1(p0), 0, 0);
+    fill_patch(c, F_P0CART, 0, 1, BCS_F, 0, 0, -1);
+    set_val(c, F_PSICART, 0.0, 0, 1, 1);
+    put1d(c, F_PSICART, c.b1("psi"), 0, 0);
+    fill_patch(c, F_PSICART, 0, 1, BCS_F, 0, 0, -1);
+    set_val(c, F_RHO0CART, 0.0, 0, 1, 1);
+    put1d(c, F_RHO0CART, c.b1(r0), 0, 0);
+    fill_patch(c, F_RHO0CART, 0, 1, BCS_S, RHO, 0, RHO);
+    set_val(c, F_GRAVCART, 0.0, 0, 3, 1);
+    put1d(c, F_GRAVCART, c.b1("grav_cell"), 2, 0);
+    fill_patch(c, F_GRAVCART, 0, 3, BCS_F, 0, 0, -1);
+    const int ept = c.P.enthalpy_pred_type;
+    const int psi_in = (is_prediction == 1 && ept == 2) || (is_prediction == 1 && ept == 0) || (is_prediction == 0);
+    launch(c, rg_grow(c, 0), 1, k_rhoh_force, c.V(), c.P.base_cutoff_density_coord, c.P.dom_hi[2], c.P.dx[2], psi_in,
+           add_thermal);
+    fill_patch(c, F_SCALFORCE, RHOH, 1, BCS_F, 0, 0, RHOH);
+}
+
+// ============================================================ conversions
+// PutInPertForm (Source/MaestroConvert.cpp:6-34), valid region
+__global__ void k_pert(KARGS, int comp, const double* __restrict__ s0, int flag) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    double& a = at(VW(F_SOLD), i, j, k, comp);
+    a = flag ? a - s0[k] : a + s0[k];
+}
+
+void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int bccomp, int which_bcs, int flag) {
+    launch(c, rg_grow(c, 0), 1, k_pert, c.V(), comp, d_s0, flag);
+    fill_patch(c, F_SOLD, comp, 1, which_bcs, bccomp, 0, comp);
+}
+
+// ConvertRhoXToX (Source/MaestroConvert.cpp:64-91), valid region
+__global__ void k_rhox_to_x(KARGS, int nspec, int flag) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView s = VW(F_SOLD);
+    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+        if (flag) at(s, i, j, k, comp) = at(s, i, j, k, comp) / at(s, i, j, k, RHO);
+        else at(s, i, j, k, comp) = at(s, i, j, k, comp) * at(s, i, j, k, RHO);
+    }
+}
+
+void convert_rhox_to_x(Ctx& c, int flag) {
+    launch(c, rg_grow(c, 0), 1, k_rhox_to_x, c.V(), c.nspec, flag);
+    if (flag) fill_patch(c, F_SOLD, FIRSTSPEC, c.nspec, BCS_F, 0, 0, FIRSTSPEC);
+    else fill_patch(c, F_SOLD, FIRSTSPEC, c.nspec, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
+}
+
+// ============================================================ fluxes
+// MakeRhoXFlux, planar 3-D (Source/MaestroMakeFlux.cpp:189-306)
+template <int D>
+__global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double* __restrict__ r0o,
+                            const double* __restrict__ r0n, const double* __restrict__ w0,
+                            const double* __restrict__ r0pe) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView fl = VW(F_SFLUX0 + D), e = VW(F_SEDGE0 + D);
+    const double u = at(VW(F_UMAC0 + D), i, j, k);
+    double frho = 0.0;
+    double eta = 0.0;
+    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+        const double rho0_edge = 0.5 * (r0o[k] + r0n[k]);
+        double f = 0.0;
+        if (spt == 1) f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, comp);
+        else if (spt == 2) f = u * at(e, i, j, k, comp);
+        else f = u * at(e, i, j, k, RHO) * at(e, i, j, k, comp);
+        at(fl, i, j, k, comp) = f;
+        if (D == 2 && do_eta) {
+            eta += f;
+            if (comp == FIRSTSPEC + nspec - 1) eta -= w0[k] * r0pe[k];
+        }
+        frho += f;
+    }
+    at(fl, i, j, k, RHO) = frho;
+    if (D == 2 && do_eta) at(VW(F_ETA), i, j, k) += eta;
+}
+
+void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new, const double* r0e_new) {
+    const int do_eta = c.P.evolve_base_state && !c.P.use_exact_base_state;
+    const double* w0 = c.b1("w0");
+    const double* rpe = c.b1("rho0_predicted_edge");
+    launch(c, rg_grow(c, 0, 0), 1, k_rhox_flux<0>, c.V(), c.nspec, c.P.species_pred_type, 0, r0_old, r0_new, w0, rpe);
+    launch(c, rg_grow(c, 0, 1), 1, k_rhox_flux<1>, c.V(), c.nspec, c.P.species_pred_type, 0, r0_old, r0_new, w0, rpe);
+    launch(c, rg_grow(c, 0, 2), 1, k_rhox_flux<2>, c.V(), c.nspec, c.P.species_pred_type, do_eta, r0e_old, r0e_new,
+           w0, rpe);
+}
+
+// MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:673-786)
+template <int D>
+__global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const double* __restrict__ bb) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView e = VW(F_SEDGE0 + D);
+    const double u = at(VW(F_UMAC0 + D), i, j, k);
+    double f;
+    if (ept == 0) {
+        f = u * at(e, i, j, k, RHOH);
+    } else {
+        const double rhoh0_edge = 0.5 * (a[k] + bb[k]);
+        f = D < 2 ? u * (rhoh0_edge + at(e, i, j, k, RHOH)) : u * (at(e, i, j, k, RHOH) + rhoh0_edge);
+    }
+    at(VW(F_SFLUX0 + D), i, j, k, RHOH) = f;
+}
+
+void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
+                    const double* rh0e_new) {
+    const int ept = c.P.enthalpy_pred_type;
+    launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux<0>, c.V(), ept, rh0_old, rh0_new);
+    launch(c, rg_grow(c, 0, 1), 1, k_rhoh_flux<1>, c.V(), ept, rh0_old, rh0_new);
+    launch(c, rg_grow(c, 0, 2), 1, k_rhoh_flux<2>, c.V(), ept, rh0e_old, rh0e_new);
+}
+
+// species_pred_type 2: rho edge state = sum of the (rho X) edge states
+template <int D>
+__global__ void k_sum_species(KARGS, int nspec) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView e = VW(F_SEDGE0 + D);
+    double s = at(e, i, j, k, FIRSTSPEC);
+    for (int n = 1; n < nspec; ++n) s += at(e, i, j, k, FIRSTSPEC + n);
+    at(e, i, j, k, RHO) = s;
+}
+
+void sum_species_edges(Ctx& c) {
+    launch(c, rg_grow(c, 0, 0), 1, k_sum_species<0>, c.V(), c.nspec);
+    launch(c, rg_grow(c, 0, 1), 1, k_sum_species<1>, c.V(), c.nspec);
+    launch(c, rg_grow(c, 0, 2), 1, k_sum_species<2>, c.V(), c.nspec);
+}
+
+// ============================================================ UpdateScal
+// Source/MaestroAdvection.cpp:117-251.  The species update and the density / floor /
+// negative-species pass of the reference are two ParallelFors over the same cells; they
+// are one kernel here with the same per-cell order of operations.
+__global__ void k_update_rhox(KARGS, int nspec, double dt, double dx0, double dx1, double dx2, double half_cutoff) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fz = VW(F_SFLUX2),
+                  fo = VW(F_SCALFORCE);
+    for (int n = 0; n < nspec; ++n) {
+        const int comp = FIRSTSPEC + n;
+        double divterm = (at(fx, i + 1, j, k, comp) - at(fx, i, j, k, comp)) / dx0;
+        divterm += (at(fy, i, j + 1, k, comp) - at(fy, i, j, k, comp)) / dx1;
+        divterm += (at(fz, i, j, k + 1, comp) - at(fz, i, j, k, comp)) / dx2;
+        at(sn, i, j, k, comp) = at(so, i, j, k, comp) + dt * (-divterm + at(fo, i, j, k, comp));
+    }
+    double rho = at(so, i, j, k, RHO);
+    bool neg = false;
+    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+        rho += at(sn, i, j, k, comp) - at(so, i, j, k, comp);
+        if (at(sn, i, j, k, comp) < 0.0) neg = true;
+    }
+    if (rho < half_cutoff) {
+        for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) at(sn, i, j, k, comp) *= half_cutoff / rho;
+        rho = half_cutoff;
+    }
+    at(sn, i, j, k, RHO) = rho;
+    if (neg) {
+        for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+            if (at(sn, i, j, k, comp) < 0.0) {
+                const double delta = -at(sn, i, j, k, comp);
+                double sumX = 0.0;
+                for (int c2 = FIRSTSPEC; c2 < FIRSTSPEC + nspec; ++c2)
+                    if (c2 != comp && at(sn, i, j, k, c2) >= 0.0) sumX += at(sn, i, j, k, c2);
+                for (int c2 = FIRSTSPEC; c2 < FIRSTSPEC + nspec; ++c2)
+                    if (c2 != comp && at(sn, i, j, k, c2) >= 0.0) {
+                        const double frac = at(sn, i, j, k, c2) / sumX;
+                        at(sn, i, j, k, c2) -= frac * delta;
+                    }
+                at(sn, i, j, k, comp) = 0.0;
+            }
+        }
+    }
+}
+
+__global__ void k_update_rhoh(KARGS, double dt, double dx0, double dx1, double dx2, int eos_check, double cutoff,
+                              int* flag) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fz = VW(F_SFLUX2),
+                  fo = VW(F_SCALFORCE);
+    const double divterm = ((at(fx, i + 1, j, k, RHOH) - at(fx, i, j, k, RHOH)) / dx0 +
+                            (at(fy, i, j + 1, k, RHOH) - at(fy, i, j, k, RHOH)) / dx1 +
+                            (at(fz, i, j, k + 1, RHOH) - at(fz, i, j, k, RHOH)) / dx2);
+    at(sn, i, j, k, RHOH) = at(so, i, j, k, RHOH) + dt * (-divterm + at(fo, i, j, k, RHOH));
+    if (eos_check && at(sn, i, j, k, RHO) <= cutoff) atomicOr(flag, 1);
+}
+
+void update_scal(Ctx& c, int start_comp) {
+    const RegionTable& rt = rg_grow(c, 0);
+    if (start_comp == RHOH) {
+        launch(c, rt, 1, k_update_rhoh, c.V(), c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2], c.P.do_eos_h_above_cutoff,
+               c.P.base_cutoff_density, c.d_flag);
+        fill_patch(c, F_SNEW, RHOH, 1, BCS_S, RHOH, 0, RHOH);
+    } else {
+        launch(c, rt, 1, k_update_rhox, c.V(), c.nspec, c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2],
+               0.5 * c.P.base_cutoff_density);
+        fill_patch(c, F_SNEW, FIRSTSPEC, c.nspec, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
+        fill_patch(c, F_SNEW, RHO, 1, BCS_S, RHO, 0, RHO);
+    }
+}
+
+}  // namespace madv

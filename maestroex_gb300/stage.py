@@ -1,0 +1,232 @@
+"""Host-side mirror of the Maestro member functions of the scalar-advection stage.
+
+``ScalarAdvectionStage`` plays the role the ``Maestro`` object plays for these functions
+in the reference (Source/Maestro.H): it owns the stage state (parameters, box layout,
+1-D base state) and exposes AdvancePremac, Addw0, DensityAdvance, EnthalpyAdvance and the
+whole stage with the reference's argument meaning, over ``MultiFab`` objects whose FABs
+live in device memory.  All compute goes through the C ABI of libmaestro_adv.so.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import capi
+from .capi import MadvBaseState, MadvBox, MadvFab, MadvMultiFab, check, lib
+
+
+class MultiFab:
+    """Per-box FABs (torch float64, Fortran order, ghost cells included) on one device.
+
+    ``nodal`` = -1 for cell data, d for faces normal to direction d.
+    """
+
+    def __init__(self, boxes, ncomp, ngrow, nodal=-1, device="cuda", fill=0.0):
+        self.boxes = [tuple(int(v) for v in b) for b in boxes]
+        self.ncomp, self.ng, self.nodal = ncomp, ngrow, nodal
+        self.fabs, self.los, self.his = [], [], []
+        for b in self.boxes:
+            lo = [b[0] - ngrow, b[1] - ngrow, b[2] - ngrow]
+            hi = [b[3] + ngrow, b[4] + ngrow, b[5] + ngrow]
+            if nodal >= 0:
+                hi[nodal] += 1
+            shape = (ncomp, hi[2] - lo[2] + 1, hi[1] - lo[1] + 1, hi[0] - lo[0] + 1)
+            self.fabs.append(torch.full(shape, fill, dtype=torch.float64, device=device))
+            self.los.append(lo)
+            self.his.append(hi)
+        self._desc = None
+
+    def desc(self):
+        if self._desc is None:
+            arr = (MadvFab * len(self.fabs))()
+            for b, t in enumerate(self.fabs):
+                arr[b].p = t.data_ptr()
+                for d in range(3):
+                    arr[b].lo[d] = self.los[b][d]
+                    arr[b].hi[d] = self.his[b][d]
+                arr[b].ncomp = self.ncomp
+            mf = MadvMultiFab(len(self.fabs), arr)
+            self._desc = (mf, arr)
+        return self._desc[0]
+
+    def _slices(self, b, grow=0):
+        bx = self.boxes[b]
+        lo, hi = list(bx[:3]), list(bx[3:])
+        if self.nodal >= 0:
+            hi[self.nodal] += 1
+        fs, ds = [], []
+        for d in (2, 1, 0):
+            a, z = lo[d] - grow, hi[d] + grow
+            fs.append(slice(a - self.los[b][d], z - self.los[b][d] + 1))
+            ds.append(slice(a, z + 1))
+        return tuple(fs), tuple(ds)
+
+    def from_domain(self, arr, c0=0):
+        """Copy a domain-sized array [nc, nz(+1), ny(+1), nx(+1)] into the valid regions."""
+        t = arr if torch.is_tensor(arr) else torch.from_numpy(np.ascontiguousarray(arr))
+        t = t.to(self.fabs[0].device)
+        nc = t.shape[0]
+        for b, f in enumerate(self.fabs):
+            fs, ds = self._slices(b)
+            f[(slice(c0, c0 + nc),) + fs] = t[(slice(None),) + ds]
+        return self
+
+    def to_domain(self, domain_n, comps=None):
+        """Gather the valid regions into a domain-sized tensor."""
+        comps = list(range(self.ncomp)) if comps is None else list(comps)
+        n = list(domain_n)
+        if self.nodal >= 0:
+            n[self.nodal] += 1
+        out = torch.full((len(comps), n[2], n[1], n[0]), float("nan"), dtype=torch.float64,
+                         device=self.fabs[0].device)
+        for b, f in enumerate(self.fabs):
+            fs, ds = self._slices(b)
+            out[(slice(None),) + ds] = f[(comps,) + fs]
+        return out
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ref(mf):
+    return C.byref(mf.desc()) if mf is not None else None
+
+
+def _ref3(mfs):
+    """Three face MultiFabs as a contiguous madv_multifab[3]."""
+    if mfs is None:
+        return None
+    arr = (MadvMultiFab * 3)(*[m.desc() for m in mfs])
+    _ref3.keep.append(arr)
+    if len(_ref3.keep) > 64:
+        del _ref3.keep[:32]
+    return C.cast(arr, C.POINTER(MadvMultiFab))
+
+
+_ref3.keep = []
+
+
+class ScalarAdvectionStage:
+    def __init__(self, params):
+        self.params = params
+        self.ctx = C.c_void_p()
+        check(lib().madv_ctx_create(C.byref(params), C.byref(self.ctx)))
+        self.nscal = 4 + params.nspec
+
+    def close(self):
+        if self.ctx:
+            lib().madv_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_layout(self, boxes):
+        arr = (MadvBox * len(boxes))()
+        for b, bx in enumerate(boxes):
+            for d in range(3):
+                arr[b].lo[d] = int(bx[d])
+                arr[b].hi[d] = int(bx[3 + d])
+        self.boxes = [tuple(b) for b in boxes]
+        check(lib().madv_set_layout(self.ctx, len(boxes), arr))
+
+    def set_base_state(self, rho0_old, rho0_new, rhoh0_old, rhoh0_new, p0_old, p0_new, psi, grav_cell,
+                       w0_force, w0, rho0_predicted_edge):
+        keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (
+            rho0_old, rho0_new, rhoh0_old, rhoh0_new, p0_old, p0_new, psi, grav_cell, w0_force, w0,
+            rho0_predicted_edge)]
+        bs = MadvBaseState(*[_dptr(a) for a in keep])
+        check(lib().madv_set_base_state(self.ctx, C.byref(bs)))
+
+    def set_dt(self, dt, rel_eps):
+        check(lib().madv_set_dt(self.ctx, dt, rel_eps))
+
+    def stage_forward(self, uold, sold, gpi, snew, umac, sedge=None, sflux=None, etarhoflux=None,
+                      thermal=None, mode=capi.MODE_BATCHED, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_stage_forward(self.ctx, mode, _ref(uold), _ref(sold), _ref(gpi), _ref(thermal),
+                                       _ref(snew), _ref3(umac), _ref3(sedge), _ref3(sflux),
+                                       _ref(etarhoflux), C.c_void_p(s)))
+
+    def advance_premac(self, uold, sold, gpi, umac, utrans=None, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_advance_premac(self.ctx, _ref(uold), _ref(sold), _ref(gpi), _ref3(umac),
+                                        _ref3(utrans), C.c_void_p(s)))
+
+    def addw0(self, umac, mult, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_addw0(self.ctx, _ref3(umac), float(mult), C.c_void_p(s)))
+
+    def density_advance(self, sold, snew, sedge, sflux, etarhoflux, umac, which_step=1, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_density_advance(self.ctx, which_step, _ref(sold), _ref(snew), _ref3(sedge),
+                                         _ref3(sflux), _ref(etarhoflux), _ref3(umac), C.c_void_p(s)))
+
+    def enthalpy_advance(self, sold, snew, sedge, sflux, umac, thermal=None, which_step=1, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_enthalpy_advance(self.ctx, which_step, _ref(sold), _ref(snew), _ref3(sedge),
+                                          _ref3(sflux), _ref3(umac), _ref(thermal), C.c_void_p(s)))
+
+    def launch_count(self):
+        return lib().madv_last_launch_count(self.ctx)
+
+
+class StageBuffers:
+    """The caller-side MultiFabs of one stage configuration (as AdvanceTimeStep owns them)."""
+
+    def __init__(self, cfg, device="cuda"):
+        boxes = cfg["boxes"]
+        nscal = 4 + cfg["nspec"]
+        ng = 4 if cfg["ppm_type"] == 2 else 3
+        self.n = cfg["n"]
+        self.uold = MultiFab(boxes, 3, ng, device=device)
+        self.sold = MultiFab(boxes, nscal, ng, device=device)
+        self.gpi = MultiFab(boxes, 3, 0, device=device)
+        self.thermal = MultiFab(boxes, 1, 1, device=device)
+        self.snew = MultiFab(boxes, nscal, ng, device=device)
+        self.umac = [MultiFab(boxes, 1, 1, nodal=d, device=device) for d in range(3)]
+        self.sedge = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(3)]
+        self.sflux = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(3)]
+        self.eta = MultiFab(boxes, 1, 0, nodal=2, device=device)
+
+    def load(self, cfg):
+        self.uold.from_domain(cfg["uold"])
+        self.sold.from_domain(cfg["sold"])
+        self.gpi.from_domain(cfg["gpi"])
+        self.thermal.from_domain(cfg["thermal"])
+        return self
+
+
+def make_stage(cfg):
+    from .params import make_params
+    st = ScalarAdvectionStage(make_params(cfg))
+    st.set_layout(cfg["boxes"])
+    st.set_base_state(cfg["rho0_old"], cfg["rho0_new"], cfg["rhoh0_old"], cfg["rhoh0_new"],
+                      cfg["p0_old"], cfg["p0_new"], cfg["psi"], cfg["grav_cell"], cfg["w0_force"],
+                      cfg["w0"], cfg["rho0_predicted_edge"])
+    return st
+
+
+def run_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
+    """Run the whole stage on the GPU for a config dict; returns domain arrays (numpy)."""
+    st = make_stage(cfg)
+    buf = StageBuffers(cfg, device).load(cfg)
+    st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                     thermal=buf.thermal, mode=mode)
+    torch.cuda.synchronize()
+    n = cfg["n"]
+    res = dict(
+        umac_end=[buf.umac[d].to_domain(n)[0].cpu().numpy() for d in range(3)],
+        sedge=[buf.sedge[d].to_domain(n).cpu().numpy() for d in range(3)],
+        sflux=[buf.sflux[d].to_domain(n).cpu().numpy() for d in range(3)],
+        snew=buf.snew.to_domain(n).cpu().numpy(),
+        sold_end=buf.sold.to_domain(n).cpu().numpy(),
+        etarhoflux=buf.eta.to_domain(n)[0].cpu().numpy(),
+        launches=st.launch_count(),
+    )
+    st.close()
+    return res

@@ -1,0 +1,174 @@
+"""GPU parity: the CUDA stage against the CPU oracle on the same seeded inputs.
+
+Bar: every output component within 1e-12 of the oracle, relative to the component's
+max-norm (the error definition of the benchmark).  The library evaluates the reference
+expressions in the same order without FMA contraction, so in practice the results are
+bitwise equal; the tests record that too.
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from maestroex_gb300 import capi, configs
+from maestroex_gb300.params import (FIRSTSPEC, INTERIOR, NOSLIPWALL, OUTFLOW, RHO, RHOH, SLIPWALL,
+                                    SYMMETRY)
+from helpers import per_comp_rel_err, rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from maestroex_gb300 import build
+    build.build_library()
+
+
+def compare(cfg, res_gpu, res_ref, label=""):
+    nspec = cfg["nspec"]
+    comps = [RHO, RHOH] + list(range(FIRSTSPEC, FIRSTSPEC + nspec))
+    worst = 0.0
+    bitwise = True
+    for d in range(3):
+        e = rel_err(res_gpu["umac_end"][d], res_ref["umac_end"][d])
+        assert e <= TOL, f"{label} umac[{d}] rel err {e}"
+        worst = max(worst, e)
+        bitwise &= np.array_equal(res_gpu["umac_end"][d], res_ref["umac_end"][d])
+        for key in ("sedge", "sflux"):
+            for c in comps:
+                e = rel_err(res_gpu[key][d][c], res_ref[key][d][c])
+                assert e <= TOL, f"{label} {key}[{d}] comp {c} rel err {e}"
+                worst = max(worst, e)
+                bitwise &= np.array_equal(res_gpu[key][d][c], res_ref[key][d][c])
+    for key in ("snew", "sold_end"):
+        for c in comps:
+            e = rel_err(res_gpu[key][c], res_ref[key][c])
+            assert e <= TOL, f"{label} {key} comp {c} rel err {e}"
+            worst = max(worst, e)
+            bitwise &= np.array_equal(res_gpu[key][c], res_ref[key][c])
+    e = rel_err(res_gpu["etarhoflux"], res_ref["etarhoflux"])
+    assert e <= TOL, f"{label} etarhoflux rel err {e}"
+    return worst, bitwise
+
+
+def run_both(cfg, mode=capi.MODE_BATCHED):
+    from maestroex_gb300.stage import run_stage_gpu
+    ref = pyoracle.run_stage(cfg, checked=False)
+    gpu = run_stage_gpu(cfg, mode=mode)
+    return gpu, ref
+
+
+@pytest.mark.parametrize("ppm_type", [1, 2, 0])
+def test_stage_planar_default_bcs(ppm_type):
+    cfg = configs.planar_config(n=(32, 32, 32), nspec=3, ppm_type=ppm_type, max_grid=16, seed=101 + ppm_type)
+    gpu, ref = run_both(cfg)
+    worst, bitwise = compare(cfg, gpu, ref, f"ppm{ppm_type}")
+    assert bitwise, f"not bitwise (worst rel err {worst})"
+
+
+BC_CASES = [
+    ((SYMMETRY, SLIPWALL, SLIPWALL), (OUTFLOW, NOSLIPWALL, OUTFLOW)),
+    ((OUTFLOW, INTERIOR, NOSLIPWALL), (SYMMETRY, INTERIOR, SLIPWALL)),
+    ((SLIPWALL, OUTFLOW, SYMMETRY), (SLIPWALL, SYMMETRY, SYMMETRY)),
+]
+
+
+@pytest.mark.parametrize("ppm_type", [1, 2])
+@pytest.mark.parametrize("case", range(len(BC_CASES)))
+def test_stage_boundary_conditions(ppm_type, case):
+    lo, hi = BC_CASES[case]
+    cfg = configs.planar_config(n=(24, 16, 24), nspec=2, ppm_type=ppm_type, max_grid=(8, 16, 12), bc_lo=lo,
+                                bc_hi=hi, seed=200 + case, cfl=0.5)
+    gpu, ref = run_both(cfg)
+    compare(cfg, gpu, ref, f"bc{case} ppm{ppm_type}")
+
+
+@pytest.mark.parametrize("slope_order", [2, 4, 0])
+def test_stage_slopes(slope_order):
+    cfg = configs.planar_config(n=(16, 16, 24), nspec=2, ppm_type=0, slope_order=slope_order, max_grid=8,
+                                bc_lo=(SLIPWALL, INTERIOR, SLIPWALL), bc_hi=(OUTFLOW, INTERIOR, OUTFLOW),
+                                seed=300 + slope_order)
+    gpu, ref = run_both(cfg)
+    compare(cfg, gpu, ref, f"slope{slope_order}")
+
+
+@pytest.mark.parametrize("spt,ept", [(2, 1), (3, 1), (1, 0), (2, 0)])
+def test_stage_prediction_types(spt, ept):
+    cfg = configs.planar_config(n=(16, 24, 16), nspec=3, ppm_type=1, max_grid=8, species_pred_type=spt,
+                                enthalpy_pred_type=ept, seed=400 + 10 * spt + ept)
+    gpu, ref = run_both(cfg)
+    compare(cfg, gpu, ref, f"spt{spt} ept{ept}")
+
+
+def test_uneven_boxes():
+    rng = np.random.default_rng(5)
+    boxes = configs.uneven_boxes((48, 32, 40), [8, 16, 24], rng)
+    cfg = configs.planar_config(n=(48, 32, 40), nspec=2, ppm_type=2, boxes=boxes, seed=501)
+    gpu, ref = run_both(cfg)
+    compare(cfg, gpu, ref, "uneven")
+
+
+@pytest.mark.parametrize("mode", [capi.MODE_PER_BOX, capi.MODE_GRAPH])
+def test_launch_modes_identical(mode):
+    from maestroex_gb300.stage import run_stage_gpu
+    cfg = configs.planar_config(n=(32, 16, 16), nspec=2, ppm_type=1, max_grid=8, seed=601)
+    a = run_stage_gpu(cfg, mode=capi.MODE_BATCHED)
+    b = run_stage_gpu(cfg, mode=mode)
+    for key in ("snew", "sold_end"):
+        assert np.array_equal(a[key], b[key])
+    for d in range(3):
+        assert np.array_equal(a["sedge"][d], b["sedge"][d])
+        assert np.array_equal(a["umac_end"][d], b["umac_end"][d])
+    assert b["launches"] > 0
+
+
+def test_decomposition_independent():
+    from maestroex_gb300.stage import run_stage_gpu
+    one = configs.planar_config(n=(32, 32, 16), nspec=2, ppm_type=2, boxes=[(0, 0, 0, 31, 31, 15)], seed=701)
+    many = dict(one)
+    many["boxes"] = configs.tile_boxes((32, 32, 16), (8, 16, 8))
+    a = run_stage_gpu(one)
+    b = run_stage_gpu(many)
+    assert np.array_equal(a["snew"], b["snew"])
+    for d in range(3):
+        assert np.array_equal(a["sflux"][d], b["sflux"][d])
+
+
+def test_maestro_entry_points_match_stage():
+    """AdvancePremac -> Addw0 -> DensityAdvance -> Addw0 x2 -> EnthalpyAdvance -> Addw0 through
+    the individual entry points equals the whole-stage call."""
+    import torch
+    from maestroex_gb300.stage import StageBuffers, make_stage, run_stage_gpu
+    cfg = configs.planar_config(n=(16, 16, 32), nspec=3, ppm_type=1, max_grid=16, seed=801)
+    whole = run_stage_gpu(cfg)
+    st = make_stage(cfg)
+    b = StageBuffers(cfg).load(cfg)
+    st.advance_premac(b.uold, b.sold, b.gpi, b.umac)
+    st.addw0(b.umac, 1.0)
+    st.density_advance(b.sold, b.snew, b.sedge, b.sflux, b.eta, b.umac)
+    st.addw0(b.umac, -1.0)
+    st.addw0(b.umac, 1.0)
+    st.enthalpy_advance(b.sold, b.snew, b.sedge, b.sflux, b.umac, thermal=b.thermal)
+    st.addw0(b.umac, -1.0)
+    torch.cuda.synchronize()
+    n = cfg["n"]
+    assert np.array_equal(b.snew.to_domain(n).cpu().numpy()[[0, 1, 4, 5, 6]], whole["snew"][[0, 1, 4, 5, 6]])
+    for d in range(3):
+        assert np.array_equal(b.sflux[d].to_domain(n).cpu().numpy(), whole["sflux"][d])
+        assert np.array_equal(b.umac[d].to_domain(n)[0].cpu().numpy(), whole["umac_end"][d])
+    st.close()
+
+
+def test_rejects_bad_layout_and_params():
+    from maestroex_gb300.params import make_params
+    from maestroex_gb300.stage import ScalarAdvectionStage
+    cfg = configs.planar_config(n=(16, 16, 16), nspec=2, max_grid=8)
+    st = ScalarAdvectionStage(make_params(cfg))
+    with pytest.raises(capi.MadvError) as e:
+        st.set_layout([(0, 0, 0, 7, 7, 7)])  # does not cover the domain
+    assert e.value.code == -2
+    p = make_params(cfg)
+    p.ppm_trace_forces = 1
+    with pytest.raises(capi.MadvError) as e:
+        ScalarAdvectionStage(p)
+    assert e.value.code == -3
