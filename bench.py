@@ -131,6 +131,8 @@ def main():
     ap.add_argument("--nspec", type=int, default=13)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-box", action="store_true")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="run one batched stage and exit (the command ncu captures)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     warmup = max(args.warmup, 3)
@@ -178,6 +180,12 @@ def main():
     def step(mode):
         st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
                          thermal=buf.thermal, mode=mode)
+
+    if args.profile_once:
+        step(capi.MODE_BATCHED)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_once": True, "launches": st.launch_count()}))
+        return
 
     def barrier():
         if ws > 1:
@@ -242,10 +250,25 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
 
+    # per-kernel device time of one batched stage (CUDA events around every launch)
+    import ctypes as C
+    L = capi.lib()
+    reset()
+    capi.check(L.madv_profile(st.ctx, 1))
+    step(capi.MODE_BATCHED)
+    rep = C.create_string_buffer(1 << 20)
+    capi.check(L.madv_profile_report(st.ctx, rep, len(rep)))
+    capi.check(L.madv_profile(st.ctx, 0))
+    kern = json.loads(rep.value.decode())
+    tf = C.c_double(0.0)
+    capi.check(L.madv_probe_fp64_peak(C.byref(tf), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
     if rank != 0:
         dist.destroy_process_group()
         return
     peaks, peak_kind = measured_peaks()
+    ktot = sum(v[1] for v in kern.values())
+    top = sorted(kern.items(), key=lambda kv: -kv[1][1])[:8]
     value = ws * ncell / (ms_graph * 1e-3)
     b_cell = 8 * (2 * args.nspec + 16)
     hbm_gbs = ncell * b_cell / (ms_graph * 1e-3) / 1e9
@@ -265,6 +288,9 @@ def main():
         "per_box": {"value": ws * ncell / (ms_perbox * 1e-3) if ms_perbox else None,
                     "ms_per_step": ms_perbox},
         "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
+        "fp64_peak_tflops_probe": tf.value,
+        "kernels_top": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / ktot, 4)}
+                        for k, v in top},
         "stage_hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": peaks.get("hbm_gbs", HBM_PEAK_FALLBACK),
                       "frac": hbm_gbs / peaks.get("hbm_gbs", HBM_PEAK_FALLBACK), "peak_kind": peak_kind,
                       "bytes_per_cell": b_cell},

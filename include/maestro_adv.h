@@ -153,6 +153,17 @@ int madv_stage_forward(madv_ctx* ctx, int mode, const madv_multifab* uold,
 /* Number of kernel launches issued by the last madv_* call (for launch accounting). */
 long madv_last_launch_count(const madv_ctx* ctx);
 
+/* Per-kernel timing, the counterpart of the reference's BL_PROFILE_VAR regions
+ * (TinyProfiler): when enabled, CUDA events bracket every batched-mode launch.
+ * madv_profile_report synchronises the device and writes a JSON object
+ * {"kernel name": [launches, total_ms], ...} into buf. */
+int madv_profile(madv_ctx* ctx, int enable);
+int madv_profile_report(madv_ctx* ctx, char* buf, int len);
+
+/* FP64 FMA issue-rate probe of the current device (TFLOP/s, 2 flops per FMA): the
+ * ceiling of the FP64-bound stage kernels.  No counterpart in the reference. */
+int madv_probe_fp64_peak(double* tflops, void* stream);
+
 const char* madv_last_error(void);
 const char* madv_version(void);
 

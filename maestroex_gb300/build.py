@@ -1,9 +1,10 @@
 """In-tree build of libmaestro_adv.so for sm_103a (no cmake, no pip install).
 
 Each CUDA translation unit is compiled in parallel, then linked into one shared library
-next to this file.  ``--fmad=false`` keeps every floating-point expression as written
-(no FMA contraction), which is what makes the results bit-identical to the reference
-algorithm evaluated in IEEE binary64.
+next to this file.  ``--fmad=false`` (device code) and ``-ffp-contract=off`` (host code: the 1-D base-state
+edges are formed on the host, and Arm compilers contract a*b+c into an FMA by default)
+keep every floating-point expression as written, which is what makes the results
+bit-identical to the reference algorithm evaluated in IEEE binary64.
 """
 import os
 import shutil
@@ -13,9 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmaestro_adv.so")
-SOURCES = ["madv_kernels.cu", "madv_ctx.cu"]
+SOURCES = ["madv_kernels.cu", "madv_ctx.cu", "madv_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC"]
+FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
 
 
 def nvcc():

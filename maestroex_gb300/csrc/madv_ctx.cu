@@ -484,6 +484,15 @@ static int finish(Ctx& c) {
 
 using namespace madv;
 
+cudaEvent_t Ctx::next_event() {
+    if (ev_next == ev_pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ev_pool.push_back(e);
+    }
+    return ev_pool[ev_next++];
+}
+
 struct madv_ctx {
     Ctx c;
 };
@@ -580,6 +589,7 @@ void madv_ctx_destroy(madv_ctx* h) {
     Ctx& c = h->c;
     free_layout(c);
     for (auto& kv : c.d1) cudaFree(kv.second);
+    for (auto e : c.ev_pool) cudaEventDestroy(e);
     if (c.d_bcs) cudaFree(c.d_bcs);
     if (c.d_flag) cudaFree(c.d_flag);
     delete h;
@@ -910,5 +920,41 @@ int madv_enthalpy_advance(madv_ctx* h, int which_step, const madv_multifab* sold
 }
 
 long madv_last_launch_count(const madv_ctx* h) { return h ? h->c.launches : -1; }
+
+int madv_profile(madv_ctx* h, int enable) {
+    if (!h) return MADV_ERR_PARAM;
+    h->c.profiling = enable != 0;
+    h->c.prof.clear();
+    h->c.ev_next = 0;
+    return MADV_OK;
+}
+
+int madv_profile_report(madv_ctx* h, char* buf, int len) {
+    if (!h || !buf || len <= 0) return MADV_ERR_PARAM;
+    Ctx& c = h->c;
+    if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) return MADV_ERR_CUDA;
+    std::map<std::string, std::pair<long, double>> agg;
+    for (auto& r : c.prof) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.e0, r.e1);
+        const char* name = nullptr;
+        if (cudaFuncGetName(&name, r.fn) != cudaSuccess || !name) name = "?";
+        auto& a = agg[name];
+        a.first += 1;
+        a.second += ms;
+    }
+    std::string js = "{";
+    bool first = true;
+    for (auto& kv : agg) {
+        char tmp[512];
+        std::snprintf(tmp, sizeof(tmp), "%s\"%s\": [%ld, %.6f]", first ? "" : ", ", kv.first.c_str(), kv.second.first,
+                      kv.second.second);
+        js += tmp;
+        first = false;
+    }
+    js += "}";
+    std::snprintf(buf, (size_t)len, "%s", js.c_str());
+    return (int)js.size() < len ? MADV_OK : MADV_ERR_PARAM;
+}
 
 }  // extern "C"

@@ -96,6 +96,16 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     int per_box = 0;      // launch mode: 0 batched, 1 one launch per box
     bool dry = false;     // build region / copy tables only, launch nothing
+    // per-kernel timing (madv_profile): events around every launch
+    bool profiling = false;
+    struct ProfRec {
+        const void* fn;
+        cudaEvent_t e0, e1;
+    };
+    std::vector<ProfRec> prof;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_next = 0;
+    cudaEvent_t next_event();
     long launches = 0;
     int* d_flag = nullptr;  // device error flag (EOS cutoff)
     // graph mode

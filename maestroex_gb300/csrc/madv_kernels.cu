@@ -32,7 +32,17 @@ static void launch(Ctx& c, const RegionTable& rt, int gy, Kern kern, const FabVi
     const int ne = (int)rt.h.size();
     if (!c.per_box) {
         dim3 grid((unsigned)((rt.total + TPB - 1) / TPB), gy);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (c.profiling) {
+            e0 = c.next_event();
+            e1 = c.next_event();
+            cudaEventRecord(e0, c.stream);
+        }
         kern<<<grid, TPB, 0, c.stream>>>(rt.d, ne, 0L, rt.total, V, c.nb, args...);
+        if (c.profiling) {
+            cudaEventRecord(e1, c.stream);
+            c.prof.push_back({(const void*)kern, e0, e1});
+        }
         c.launches++;
     } else {
         for (int e = 0; e < ne; ++e) {
