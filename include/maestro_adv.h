@@ -164,6 +164,14 @@ int madv_profile_report(madv_ctx* ctx, char* buf, int len);
  * ceiling of the FP64-bound stage kernels.  No counterpart in the reference. */
 int madv_probe_fp64_peak(double* tflops, void* stream);
 
+/* Device self-test of the library's exact arithmetic helpers: n seeded operands a over
+ * the whole double range (zeros, subnormals, [2^-1000, 2^1000], both signs) are divided by
+ * y with the library's division-by-constant sequence and compared bit for bit with IEEE
+ * a / y, and the integer sign/threshold tests are compared with the IEEE comparisons
+ * against `threshold`.  *failures = number of mismatches (0 expected).  No counterpart
+ * in the reference. */
+int madv_selftest_exact(double y, double threshold, long long n, long long* failures, void* stream);
+
 const char* madv_last_error(void);
 const char* madv_version(void);
 

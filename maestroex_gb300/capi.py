@@ -25,6 +25,7 @@ EXPORTED = [
     "madv_set_base_state", "madv_advance_premac", "madv_addw0", "madv_density_advance",
     "madv_enthalpy_advance", "madv_stage_forward", "madv_last_launch_count",
     "madv_last_error", "madv_version", "madv_profile", "madv_profile_report", "madv_probe_fp64_peak",
+    "madv_selftest_exact",
 ]
 
 
@@ -80,6 +81,7 @@ def lib():
         L.madv_profile.argtypes = [C.c_void_p, C.c_int]
         L.madv_profile_report.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
         L.madv_probe_fp64_peak.argtypes = [P(C.c_double), C.c_void_p]
+        L.madv_selftest_exact.argtypes = [C.c_double, C.c_double, C.c_longlong, P(C.c_longlong), C.c_void_p]
         L.madv_last_error.restype = C.c_char_p
         L.madv_version.restype = C.c_char_p
         _lib = L

@@ -230,6 +230,10 @@ static void field_specs(Ctx& c) {
     for (int q = F_Q01; q <= F_Q21; ++q) S(q, 1, 1);
     S(F_DIVU, 1, 1);
     S(F_SLOPE, 3, 1);
+    S(F_DSVL, 1, 2);
+    for (int d = 0; d < 3; ++d) S(F_TRA0 + d, 2, 1, d);
+    S(F_TRC, 6, 1);
+    S(F_TCOEF, 6, 1);
 }
 
 static void free_layout(Ctx& c) {
@@ -362,8 +366,8 @@ static void density_advance(Ctx& c) {
     addw0(c, F_UMAC0, 1.0);
     if (spt == 1 || spt == 3) convert_rhox_to_x(c, 1);
     if (spt == 1) put_in_pert_form(c, c.b1("rho0_old"), RHO, 0, BCS_F, 1);
-    make_edge_scal(c, FIRSTSPEC, c.nspec, BCS_S, spt == 2);
-    if (spt == 1 || spt == 3) make_edge_scal(c, RHO, 1, BCS_S, 0);
+    make_edge_scal(c, FIRSTSPEC, c.nspec, BCS_S, spt == 2, 1);  // no force for X / rho X
+    if (spt == 1 || spt == 3) make_edge_scal(c, RHO, 1, BCS_S, 0, 0);
     else sum_species_edges(c);
     if (spt == 1) put_in_pert_form(c, c.b1("rho0_old"), RHO, RHO, BCS_S, 0);
     if (spt == 1 || spt == 3) convert_rhox_to_x(c, 0);
@@ -386,7 +390,7 @@ static void enthalpy_advance(Ctx& c) {
     }
     addw0(c, F_UMAC0, 1.0);
     if (ept == 1) put_in_pert_form(c, c.b1("rhoh0_old"), RHOH, 0, BCS_F, 1);
-    make_edge_scal(c, RHOH, 1, BCS_S, ept == 0);
+    make_edge_scal(c, RHOH, 1, BCS_S, ept == 0, 0);
     if (ept == 1) put_in_pert_form(c, c.b1("rhoh0_old"), RHOH, RHOH, BCS_S, 0);
     make_rhoh_flux(c, c.b1("rhoh0_old"), c.b1("rhoh0_edge_old"), c.b1("rhoh0_old"), c.b1("rhoh0_edge_old"));
     set_val(c, F_SCALFORCE, 0.0, RHOH, 1, 1);

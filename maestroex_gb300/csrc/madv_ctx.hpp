@@ -34,6 +34,10 @@ enum FieldId {
     F_SIMH0, F_SIMH1, F_SIMH2,
     F_Q01, F_Q02, F_Q10, F_Q12, F_Q20, F_Q21,  // transverse states [d][t] / [c][d]
     F_DIVU, F_SLOPE,
+    F_DSVL,                        // van Leer slope per cell (ppm_type 1), one direction
+    F_TRA0, F_TRA1, F_TRA2,        // tracing coefficients (A, B) per D-face of umac
+    F_TRC,                         // tracing coefficients per cell of ufull (A_d, B_d)
+    F_TCOEF,                       // transverse coefficients per cell (dt6: 0-2, dt4: 3-5)
     F_USER,                        // first slot of per-call views of caller FABs
     NF_INTERNAL = F_USER
 };
@@ -142,7 +146,8 @@ void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge);
 void make_utrans(Ctx& c);
 void make_vel_force(Ctx& c);
 void vel_pred(Ctx& c);
-void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative);
+void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative,
+                    int force_zero);
 void modify_scal_force(Ctx& c, int comp, const double* d_s0_edge, int s0cart_fid, int fullform);
 void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal, int which_step);
 void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int bccomp, int which_bcs, int flag);

@@ -15,6 +15,7 @@
 #include <cstdio>
 
 #include "madv_ctx.hpp"
+#include "madv_exact.cuh"
 
 namespace madv {
 
@@ -282,12 +283,29 @@ void addw0(Ctx& c, int f0, double mult) {
 // S(m): the field at cell (index + m) along direction D.
 #define SHIFT_S(s, sc) [&](int m) -> double { return at(s, i + m * di, j + m * dj, k + m * dk, sc); }
 
+// Van Leer slope of each cell along D (Source/MaestroPPM.cpp:37-73).  The reference
+// evaluates it four times per cell and direction; here once.
+template <int D>
+__global__ void k_dsvl(KARGS, int fs, int sc) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const FabView s = VW(fs);
+    auto S = SHIFT_S(s, sc);
+    const double dsc = 0.5 * (S(1) - S(-1));
+    const double dsl = 2.0 * (S(0) - S(-1));
+    const double dsr = 2.0 * (S(1) - S(0));
+    double v = 0.0;
+    if (dsl * dsr > 0.0) v = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
+    at(VW(F_DSVL), i, j, k) = v;
+}
+
 // Limited interface value of the face between cells f-1 and f along D (Maestro::PPM,
 // Source/MaestroPPM.cpp: ppm_type 1 :37-111, ppm_type 2 :257-335; the boundary
 // stencils of :131-205 / :443-700 are the values the reference assigns to the faces
-// next to an ext_dir/hoextrap boundary).
+// next to an ext_dir/hoextrap boundary).  Computed once per face; the reference computes
+// each face twice (as sp of one cell and sm of the next).
 template <int D, int PPMT>
-__global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext, int domlo, int domhi) {
+__global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext, int domlo, int domhi, RecipC r6) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const FabView s = VW(fs);
@@ -307,16 +325,10 @@ __global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext
         v = mx(v, mn(S(-1), S(0)));
         v = mn(v, mx(S(-1), S(0)));
     } else if (PPMT == 1) {
-        double dvl = 0.0, dvr = 0.0;
-        double dsc = 0.5 * (S(0) - S(-2));
-        double dsl = 2.0 * (S(-1) - S(-2));
-        double dsr = 2.0 * (S(0) - S(-1));
-        if (dsl * dsr > 0.0) dvl = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
-        dsc = 0.5 * (S(1) - S(-1));
-        dsl = 2.0 * (S(0) - S(-1));
-        dsr = 2.0 * (S(1) - S(0));
-        if (dsl * dsr > 0.0) dvr = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
-        v = 0.5 * (S(0) + S(-1)) - (dvr - dvl) / 6.0;
+        const FabView dv = VW(F_DSVL);
+        const double dvl = at(dv, i - di, j - dj, k - dk);
+        const double dvr = at(dv, i, j, k);
+        v = 0.5 * (S(0) + S(-1)) - div_c(dvr - dvl, r6);
         v = mx(v, mn(S(0), S(-1)));
         v = mn(v, mx(S(0), S(-1)));
     } else {
@@ -328,7 +340,7 @@ __global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext
             double D2R = S(-1) - 2.0 * S(0) + S(1);
             double sgn = copysign(1.0, D2);
             double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
-            v = 0.5 * (S(-1) + S(0)) - D2LIM / 6.0;
+            v = 0.5 * (S(-1) + S(0)) - div_c(D2LIM, r6);
         }
     }
     at(VW(ff), i, j, k) = v;
@@ -336,7 +348,8 @@ __global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext
 
 // Interior fourth-order limited face value (ppm_type 2), face between cells c+m-1 and c+m.
 template <int D>
-__device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, int i, int j, int k, int m) {
+__device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, int i, int j, int k, int m,
+                                                    const RecipC& r6) {
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     auto S = SHIFT_S(s, sc);
     const double C = 1.25;
@@ -347,16 +360,43 @@ __device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, in
         double D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
         double sgn = copysign(1.0, D2);
         double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
-        se = 0.5 * (S(m - 1) + S(m)) - D2LIM / 6.0;
+        se = 0.5 * (S(m - 1) + S(m)) - div_c(D2LIM, r6);
     }
     return se;
+}
+
+// Characteristic-tracing coefficients of the reference (Source/MaestroPPM.cpp:209-251):
+// sigma = |u| dt / dx, A = 0.5 sigma, B = 1 - 2/3 sigma.  They depend on the velocity
+// only, so they are formed once per velocity field and direction and shared by every
+// traced component (the reference forms them per component, cell and direction).
+// Face-centred velocity (the is_umac case): one (A, B) per D-face.
+template <int D>
+__global__ void k_trace_face(KARGS, int fu, int fout, double dt, double dxd) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const double sigma = fabs(at(VW(fu), i, j, k)) * dt / dxd;
+    const FabView o = VW(fout);
+    at(o, i, j, k, 0) = 0.5 * sigma;
+    at(o, i, j, k, 1) = 1.0 - 2.0 / 3.0 * sigma;
+}
+
+// Cell-centred velocity (the velocity predictions): (A, B) per cell for each direction d,
+// from component d of the tracing velocity.
+__global__ void k_trace_cell(KARGS, int fu, double dt, double dx0, double dx1, double dx2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView u = VW(fu), o = VW(F_TRC);
+    const double dx[3] = {dx0, dx1, dx2};
+    for (int d = 0; d < 3; ++d) {
+        const double sigma = fabs(at(u, i, j, k, d)) * dt / dx[d];
+        at(o, i, j, k, 2 * d) = 0.5 * sigma;
+        at(o, i, j, k, 2 * d + 1) = 1.0 - 2.0 / 3.0 * sigma;
+    }
 }
 
 // Per-cell limiting and characteristic tracing (Source/MaestroPPM.cpp: quadratic
 // limiter :117-128, Colella-2008 limiter :337-434, tracing :209-251 / :706-770).
 template <int D, int PPMT, int UMAC>
 __global__ void k_ppm_cell(KARGS, int fs, int sc, int ff, int fu, int uc, int fip, int fim, int lo_ext, int hi_ext,
-                           int domlo, int domhi, double dt, double rel_eps, double dxd) {
+                           int domlo, int domhi, long long epsb, RecipC r6) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const FabView s = VW(fs);
@@ -383,7 +423,7 @@ __global__ void k_ppm_cell(KARGS, int fs, int sc, int ff, int fu, int uc, int fi
     } else {
         const double C = 1.25;
         double sedgel = Fc(-1), sedge = Fc(0), sedger = Fc(1), sedgerr = Fc(2);
-        if (D == 0 && hi_ext && I == domhi - 1) sedgerr = ppm2_face_regular<D>(s, sc, i, j, k, 2);
+        if (D == 0 && hi_ext && I == domhi - 1) sedgerr = ppm2_face_regular<D>(s, sc, i, j, k, 2, r6);
         if (lo_ext && I == domlo) {
             sm = sedge;
             sp = sedger;
@@ -458,17 +498,24 @@ __global__ void k_ppm_cell(KARGS, int fs, int sc, int ff, int fu, int uc, int fi
     }
     const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
     const FabView u = VW(fu);
-    const double up = UMAC ? at(u, i + di, j + dj, k + dk, uc) : at(u, i, j, k, uc);
-    const double um = at(u, i, j, k, uc);
+    double up, um, Ap, Bp, Am, Bm;
+    if (UMAC) {
+        const FabView T = VW(F_TRA0 + D);
+        up = at(u, i + di, j + dj, k + dk);
+        um = at(u, i, j, k);
+        Ap = at(T, i + di, j + dj, k + dk, 0);
+        Bp = at(T, i + di, j + dj, k + dk, 1);
+        Am = at(T, i, j, k, 0);
+        Bm = at(T, i, j, k, 1);
+    } else {
+        const FabView T = VW(F_TRC);
+        up = um = at(u, i, j, k, uc);
+        Ap = Am = at(T, i, j, k, 2 * D);
+        Bp = Bm = at(T, i, j, k, 2 * D + 1);
+    }
     double ip = s0, im = s0;
-    if (up > rel_eps) {
-        const double sigma = fabs(up) * dt / dxd;
-        ip = sp - 0.5 * sigma * (sp - sm - (1.0 - 2.0 / 3.0 * sigma) * s6);
-    }
-    if (um < -rel_eps) {
-        const double sigma = fabs(um) * dt / dxd;
-        im = sm + 0.5 * sigma * (sp - sm + (1.0 - 2.0 / 3.0 * sigma) * s6);
-    }
+    if (gt_t(up, epsb)) ip = sp - Ap * (sp - sm - Bp * s6);
+    if (lt_negt(um, epsb)) im = sm + Am * (sp - sm + Bm * s6);
     at(VW(fip), i, j, k, D) = ip;
     at(VW(fim), i, j, k, D) = im;
 }
@@ -597,32 +644,40 @@ __global__ void k_slope(KARGS, int fs, int sc, int fout, int oc, int ncomp, cons
     }
 }
 
+
 static bool ext_like(int t) { return t == BC_EXT_DIR || t == BC_HOEXTRAP; }
 
 // PPM of component sc of field fs in direction D into fip/fim comp D over the box grown
-// by one cell.  fu/uc: tracing velocity (face field if umac, else cell field comp uc).
+// by one cell.  umac: trace with the D-face velocity fu (coefficients F_TRA0+D), else
+// with component uc of the cell velocity fu (coefficients F_TRC).
 template <int D>
 static void ppm_dir(Ctx& c, int fs, int sc, const BCRecD& bc, int fu, int uc, int umac, int fip, int fim) {
     const int lo_ext = ext_like(bc.lo[D]), hi_ext = ext_like(bc.hi[D]);
     const int dlo = c.P.dom_lo[D], dhi = c.P.dom_hi[D];
+    const RecipC r6 = make_recip(6.0);
     const int gf = c.P.ppm_type == 2 ? 2 : 1;
     int glo[3] = {1, 1, 1}, ghi[3] = {1, 1, 1};
+    if (c.P.ppm_type == 1) {
+        glo[D] = 2;
+        ghi[D] = 2;
+        launch(c, region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1), 1, k_dsvl<D>, c.V(), fs, sc);
+    }
     glo[D] = gf;
     ghi[D] = gf;
     const RegionTable& rf = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], D);
     const int ff = F_FACE0 + D;
     if (c.P.ppm_type == 1)
-        launch(c, rf, 1, k_ppm_face<D, 1>, c.V(), fs, sc, ff, lo_ext, hi_ext, dlo, dhi);
+        launch(c, rf, 1, k_ppm_face<D, 1>, c.V(), fs, sc, ff, lo_ext, hi_ext, dlo, dhi, r6);
     else
-        launch(c, rf, 1, k_ppm_face<D, 2>, c.V(), fs, sc, ff, lo_ext, hi_ext, dlo, dhi);
+        launch(c, rf, 1, k_ppm_face<D, 2>, c.V(), fs, sc, ff, lo_ext, hi_ext, dlo, dhi, r6);
     const RegionTable& rc = rg_grow(c, 1);
-    const double dt = c.P.dt, re = c.P.rel_eps, dxd = c.P.dx[D];
+    const long long eb = dbits_host(c.P.rel_eps);
     if (c.P.ppm_type == 1) {
-        if (umac) launch(c, rc, 1, k_ppm_cell<D, 1, 1>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
-        else launch(c, rc, 1, k_ppm_cell<D, 1, 0>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
+        if (umac) launch(c, rc, 1, k_ppm_cell<D, 1, 1>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, eb, r6);
+        else launch(c, rc, 1, k_ppm_cell<D, 1, 0>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, eb, r6);
     } else {
-        if (umac) launch(c, rc, 1, k_ppm_cell<D, 2, 1>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
-        else launch(c, rc, 1, k_ppm_cell<D, 2, 0>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, dt, re, dxd);
+        if (umac) launch(c, rc, 1, k_ppm_cell<D, 2, 1>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, eb, r6);
+        else launch(c, rc, 1, k_ppm_cell<D, 2, 0>, c.V(), fs, sc, ff, fu, uc, fip, fim, lo_ext, hi_ext, dlo, dhi, eb, r6);
     }
 }
 
@@ -630,6 +685,14 @@ static void ppm_any(Ctx& c, int d, int fs, int sc, const BCRecD& bc, int fu, int
     if (d == 0) ppm_dir<0>(c, fs, sc, bc, fu, uc, umac, fip, fim);
     else if (d == 1) ppm_dir<1>(c, fs, sc, bc, fu, uc, umac, fip, fim);
     else ppm_dir<2>(c, fs, sc, bc, fu, uc, umac, fip, fim);
+}
+
+// tracing coefficients of the face velocity fields umac0..2 (or utrans0..2)
+static void trace_coeffs_faces(Ctx& c, int fu0) {
+    // faces lo-1 .. hi+2 along d, cells lo-1 .. hi+1 across
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, 0), 1, k_trace_face<0>, c.V(), fu0, F_TRA0, c.P.dt, c.P.dx[0]);
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, 1), 1, k_trace_face<1>, c.V(), fu0 + 1, F_TRA1, c.P.dt, c.P.dx[1]);
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, 2), 1, k_trace_face<2>, c.V(), fu0 + 2, F_TRA2, c.P.dt, c.P.dx[2]);
 }
 
 static void slope_any(Ctx& c, int d, int fs, int sc, int fout, int oc, int ncomp, const BCRecD* bcs_d, int bc_c0) {
@@ -640,9 +703,38 @@ static void slope_any(Ctx& c, int d, int fs, int sc, int fout, int oc, int ncomp
     else launch(c, rc, 1, k_slope<2>, c.V(), fs, sc, fout, oc, ncomp, bcs_d, bc_c0, so, lo, hi);
 }
 
+// Transverse-correction coefficients of a face velocity field (u0..u2 = three D-face
+// fields): per cell and direction t, (dt/6)/h_t * (u_t(c+e_t) + u_t(c)) and the same with
+// dt/4.  These are the leading products of the reference's transverse expressions, e.g.
+// (dt6/hy)*(vmac(i,j+1,k)+vmac(i,j,k)) (Source/MaestroMakeEdgeScalars.cpp:920-927,
+// Source/MaestroVelPred.cpp:1166-1172), so forming them once keeps every result bitwise.
+__global__ void k_transverse_coeffs(KARGS, int fu0, double dt6h0, double dt6h1, double dt6h2, double dt4h0,
+                                    double dt4h1, double dt4h2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView o = VW(F_TCOEF);
+    const FabView u0 = VW(fu0), u1 = VW(fu0 + 1), u2 = VW(fu0 + 2);
+    const double s0 = at(u0, i + 1, j, k) + at(u0, i, j, k);
+    const double s1 = at(u1, i, j + 1, k) + at(u1, i, j, k);
+    const double s2 = at(u2, i, j, k + 1) + at(u2, i, j, k);
+    at(o, i, j, k, 0) = dt6h0 * s0;
+    at(o, i, j, k, 1) = dt6h1 * s1;
+    at(o, i, j, k, 2) = dt6h2 * s2;
+    at(o, i, j, k, 3) = dt4h0 * s0;
+    at(o, i, j, k, 4) = dt4h1 * s1;
+    at(o, i, j, k, 5) = dt4h2 * s2;
+}
+
+static void transverse_coeffs(Ctx& c, int fu0) {
+    const double dt6 = c.P.dt / 6.0, dt4 = 0.25 * c.P.dt;
+    launch(c, rg_grow(c, 1), 1, k_transverse_coeffs, c.V(), fu0, dt6 / c.P.dx[0], dt6 / c.P.dx[1], dt6 / c.P.dx[2],
+           dt4 / c.P.dx[0], dt4 / c.P.dx[1], dt4 / c.P.dx[2]);
+}
+
 // ============================================================ MakeUtrans
 // Face kernel of Maestro::MakeUtrans, 3-D (Source/MaestroMakeUtrans.cpp:304-387, 419-502,
-// 535-627).  Planar: the z solve tests the full velocity w + w0_cart.
+// 535-627).  Planar: the z solve tests the full velocity w + w0_cart.  The PPM of
+// utilde component D along D (ufull tracing) is the same sweep VelPred needs, so it is
+// stored where VelPred reads it (F_IPC0+D / F_IMC0+D, comp D) and not repeated there.
 template <int D>
 __global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
@@ -656,8 +748,8 @@ __global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, 
         l = at(ut, i - di, j - dj, k - dk, D) + (0.5 - dt2dx * mx(0.0, at(uf, i - di, j - dj, k - dk, D))) * at(sl, i - di, j - dj, k - dk, 0);
         r = at(ut, i, j, k, D) - (0.5 + dt2dx * mn(0.0, at(uf, i, j, k, D))) * at(sl, i, j, k, 0);
     } else {
-        l = at(VW(F_IPC0), i - di, j - dj, k - dk, D);
-        r = at(VW(F_IMC0), i, j, k, D);
+        l = at(VW(F_IPC0 + D), i - di, j - dj, k - dk, D);
+        r = at(VW(F_IMC0 + D), i, j, k, D);
     }
     if (I == domlo) {
         switch (bclo) {
@@ -690,11 +782,13 @@ __global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, 
 
 void make_utrans(Ctx& c) {
     const double dt2 = 0.5 * c.P.dt;
+    if (c.P.ppm_type != 0)
+        launch(c, rg_grow(c, 1), 1, k_trace_cell, c.V(), F_UFULL, c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2]);
     for (int d = 0; d < 3; ++d) {
         if (c.P.ppm_type == 0) {
             slope_any(c, d, F_UTILDE, d, F_SLOPE, 0, 1, bcs_dev(c, BCS_U), d);
         } else {
-            ppm_any(c, d, F_UTILDE, d, c.bcs_u[d], F_UFULL, d, 0, F_IPC0, F_IMC0);
+            ppm_any(c, d, F_UTILDE, d, c.bcs_u[d], F_UFULL, d, 0, F_IPC0 + d, F_IMC0 + d);
         }
         const RegionTable& rt = rg_grow(c, 0, d);
         const double dt2dx = dt2 / c.P.dx[d];
@@ -708,7 +802,7 @@ void make_utrans(Ctx& c) {
 
 // ============================================================ MakeVelForce
 // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:100-126)
-__global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, double two_dz) {
+__global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView gpi = VW(F_GPI), rho = VW(F_SOLD), vf = VW(F_VELFORCE);
     const double r = at(rho, i, j, k, RHO);
@@ -719,7 +813,7 @@ __global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, double two_dz) 
     if (k <= -1 || k >= domhi) {
     } else {
         const FabView we = VW(F_UTRANS2), w0 = VW(F_W0CART);
-        f2 -= (at(we, i, j, k + 1) + at(we, i, j, k)) * (at(w0, i, j, k + 1, 2) - at(w0, i, j, k, 2)) / two_dz;
+        f2 -= div_c((at(we, i, j, k + 1) + at(we, i, j, k)) * (at(w0, i, j, k + 1, 2) - at(w0, i, j, k, 2)), r2dz);
     }
     at(vf, i, j, k, 2) = f2;
 }
@@ -734,7 +828,7 @@ void make_vel_force(Ctx& c) {
     fill_patch(c, F_RHO0CART, 0, 1, BCS_S, RHO, 0, RHO);
     set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
     launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
-           c.P.dom_hi[2], 2.0 * c.P.dx[2]);
+           c.P.dom_hi[2], make_recip(2.0 * c.P.dx[2]));
     fill_patch(c, F_VELFORCE, 0, 3, BCS_U, 0, 1, -1);
 }
 
@@ -743,7 +837,7 @@ void make_vel_force(Ctx& c) {
 // three velocity components on D-faces, and their upwind values.
 template <int D>
 __global__ void k_vp_interface(KARGS, int ppm_type, double dt2, double hd, int bclo, int bchi, int domlo, int domhi,
-                               double rel_eps) {
+                               long long epsb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
@@ -810,30 +904,30 @@ __global__ void k_vp_interface(KARGS, int ppm_type, double dt2, double hd, int b
     }
     const FabView L = VW(F_SL0 + D), Rr = VW(F_SR0 + D), M = VW(F_SIMH0 + D);
     const double tr = at(VW(F_UTRANS0 + D), i, j, k);
+    // reference: v = tr > 0 ? l : r;  v = |tr| < rel_eps ? (l+r)/2 : v
+    const bool avg = !((dbits(tr) & ABS_MASK) >= epsb);
+    const bool left = gt0(tr);
     for (int n = 0; n < 3; ++n) {
         at(L, i, j, k, n) = l[n];
         at(Rr, i, j, k, n) = r[n];
         if (n == D) continue;
-        const double v = tr > 0.0 ? l[n] : r[n];
-        at(M, i, j, k, n) = fabs(tr) < rel_eps ? 0.5 * (l[n] + r[n]) : v;
+        at(M, i, j, k, n) = avg ? 0.5 * (l[n] + r[n]) : (left ? l[n] : r[n]);
     }
 }
 
 // VelPredTransverse (Source/MaestroVelPred.cpp:1130-1595): component C on D-faces
-// corrected in the third direction T.
+// corrected in the third direction T.  F_TCOEF comp T holds (dt6/h_T)*(trans_T sum).
 template <int C, int D>
-__global__ void k_vp_transverse(KARGS, double dt6h, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+__global__ void k_vp_transverse(KARGS, int bclo, int bchi, int domlo, int domhi, long long epsb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int T = 3 - C - D;
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
     const int il = i - di, jl = j - dj, kl = k - dk;
-    const FabView L = VW(F_SL0 + D), Rr = VW(F_SR0 + D), trt = VW(F_UTRANS0 + T), imt = VW(F_SIMH0 + T);
-    double lq = at(L, i, j, k, C) - dt6h * (at(trt, il + ti, jl + tj, kl + tk) + at(trt, il, jl, kl)) *
-                                        (at(imt, il + ti, jl + tj, kl + tk, C) - at(imt, il, jl, kl, C));
-    double rq = at(Rr, i, j, k, C) - dt6h * (at(trt, i + ti, j + tj, k + tk) + at(trt, i, j, k)) *
-                                         (at(imt, i + ti, j + tj, k + tk, C) - at(imt, i, j, k, C));
+    const FabView L = VW(F_SL0 + D), Rr = VW(F_SR0 + D), imt = VW(F_SIMH0 + T), tc = VW(F_TCOEF);
+    double lq = at(L, i, j, k, C) - at(tc, il, jl, kl, T) * (at(imt, il + ti, jl + tj, kl + tk, C) - at(imt, il, jl, kl, C));
+    double rq = at(Rr, i, j, k, C) - at(tc, i, j, k, T) * (at(imt, i + ti, j + tj, k + tk, C) - at(imt, i, j, k, C));
     const FabView ut = VW(F_UTILDE);
     if (I == domlo) {
         switch (bclo) {
@@ -851,14 +945,14 @@ __global__ void k_vp_transverse(KARGS, double dt6h, int bclo, int bchi, int doml
         }
     }
     const double trd = at(VW(F_UTRANS0 + D), i, j, k);
-    const double v = trd > 0.0 ? lq : rq;
-    at(VW(Q_FIELD(C, D)), i, j, k) = fabs(trd) < rel_eps ? 0.5 * (lq + rq) : v;
+    const bool avg = !((dbits(trd) & ABS_MASK) >= epsb);
+    at(VW(Q_FIELD(C, D)), i, j, k) = avg ? 0.5 * (lq + rq) : (gt0(trd) ? lq : rq);
 }
 
-// VelPredVelocities (Source/MaestroVelPred.cpp:1597-1915)
+// VelPredVelocities (Source/MaestroVelPred.cpp:1597-1915).  F_TCOEF comps 3..5 hold
+// (dt4/h_t)*(trans_t sum).
 template <int D>
-__global__ void k_vp_velocities(KARGS, double dt2, double dt4h1, double dt4h2, int bclo, int bchi, int domlo,
-                                int domhi, double rel_eps) {
+__global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -866,22 +960,18 @@ __global__ void k_vp_velocities(KARGS, double dt2, double dt4h1, double dt4h2, i
     constexpr int a2i = T2 == 0, a2j = T2 == 1, a2k = T2 == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
     const int il = i - di, jl = j - dj, kl = k - dk;
-    const FabView tr1 = VW(F_UTRANS0 + T1), tr2 = VW(F_UTRANS0 + T2);
+    const FabView tc = VW(F_TCOEF);
     const FabView q1 = VW(Q_FIELD(D, T1)), q2 = VW(Q_FIELD(D, T2));
     const FabView f = VW(F_VELFORCE);
     const double fl = at(f, il, jl, kl, D);
     const double fr = at(f, i, j, k, D);
     const double ml = at(VW(F_SL0 + D), i, j, k, D) -
-                      dt4h1 * (at(tr1, il + a1i, jl + a1j, kl + a1k) + at(tr1, il, jl, kl)) *
-                          (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
-                      dt4h2 * (at(tr2, il + a2i, jl + a2j, kl + a2k) + at(tr2, il, jl, kl)) *
-                          (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
+                      at(tc, il, jl, kl, 3 + T1) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
+                      at(tc, il, jl, kl, 3 + T2) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
                       dt2 * fl;
     const double mr = at(VW(F_SR0 + D), i, j, k, D) -
-                      dt4h1 * (at(tr1, i + a1i, j + a1j, k + a1k) + at(tr1, i, j, k)) *
-                          (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
-                      dt4h2 * (at(tr2, i + a2i, j + a2j, k + a2k) + at(tr2, i, j, k)) *
-                          (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
+                      at(tc, i, j, k, 3 + T1) * (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
+                      at(tc, i, j, k, 3 + T2) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
                       dt2 * fr;
     double v;
     if (D < 2) {
@@ -914,15 +1004,14 @@ __global__ void k_vp_velocities(KARGS, double dt2, double dt4h1, double dt4h2, i
 }
 
 template <int C, int D>
-static void vp_transverse_launch(Ctx& c, double dt6) {
-    constexpr int T = 3 - C - D;
+static void vp_transverse_launch(Ctx& c) {
     int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
     glo[C] = 1;
     ghi[C] = 1;
     ghi[D] = 1;
     const RegionTable& rt = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1);
-    launch(c, rt, 1, k_vp_transverse<C, D>, c.V(), dt6 / c.P.dx[T], c.P.phys_bc_lo[D], c.P.phys_bc_hi[D],
-           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+    launch(c, rt, 1, k_vp_transverse<C, D>, c.V(), c.P.phys_bc_lo[D], c.P.phys_bc_hi[D], c.P.dom_lo[D],
+           c.P.dom_hi[D], dbits_host(c.P.rel_eps));
 }
 
 template <int D>
@@ -931,15 +1020,13 @@ static void vp_interface_launch(Ctx& c) {
     glo[D] = 0;
     const RegionTable& rt = region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1);
     launch(c, rt, 1, k_vp_interface<D>, c.V(), c.P.ppm_type, 0.5 * c.P.dt, c.P.dx[D], c.P.phys_bc_lo[D],
-           c.P.phys_bc_hi[D], c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+           c.P.phys_bc_hi[D], c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
 }
 
 template <int D>
 static void vp_velocities_launch(Ctx& c) {
-    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
-    const double dt4 = 0.25 * c.P.dt;
-    launch(c, rg_grow(c, 0, D), 1, k_vp_velocities<D>, c.V(), 0.5 * c.P.dt, dt4 / c.P.dx[T1], dt4 / c.P.dx[T2],
-           c.P.phys_bc_lo[D], c.P.phys_bc_hi[D], c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+    launch(c, rg_grow(c, 0, D), 1, k_vp_velocities<D>, c.V(), 0.5 * c.P.dt, c.P.phys_bc_lo[D], c.P.phys_bc_hi[D],
+           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
 }
 
 void vel_pred(Ctx& c) {
@@ -948,19 +1035,21 @@ void vel_pred(Ctx& c) {
         slope_any(c, 1, F_UTILDE, 0, F_IMC1, 0, 3, bcs_dev(c, BCS_U), 0);  // slopey -> Imv
         slope_any(c, 2, F_UTILDE, 0, F_IMC2, 0, 3, bcs_dev(c, BCS_U), 0);  // slopez -> Imw
     } else {
+        // the sweeps of component d along d were done by make_utrans (same inputs)
         for (int cc = 0; cc < 3; ++cc)
-            for (int d = 0; d < 3; ++d) ppm_any(c, d, F_UTILDE, cc, c.bcs_u[cc], F_UFULL, d, 0, F_IPC0 + cc, F_IMC0 + cc);
+            for (int d = 0; d < 3; ++d)
+                if (cc != d) ppm_any(c, d, F_UTILDE, cc, c.bcs_u[cc], F_UFULL, d, 0, F_IPC0 + cc, F_IMC0 + cc);
     }
     vp_interface_launch<0>(c);
     vp_interface_launch<1>(c);
     vp_interface_launch<2>(c);
-    const double dt6 = c.P.dt / 6.0;
-    vp_transverse_launch<0, 1>(c, dt6);
-    vp_transverse_launch<0, 2>(c, dt6);
-    vp_transverse_launch<1, 0>(c, dt6);
-    vp_transverse_launch<1, 2>(c, dt6);
-    vp_transverse_launch<2, 0>(c, dt6);
-    vp_transverse_launch<2, 1>(c, dt6);
+    transverse_coeffs(c, F_UTRANS0);
+    vp_transverse_launch<0, 1>(c);
+    vp_transverse_launch<0, 2>(c);
+    vp_transverse_launch<1, 0>(c);
+    vp_transverse_launch<1, 2>(c);
+    vp_transverse_launch<2, 0>(c);
+    vp_transverse_launch<2, 1>(c);
     vp_velocities_launch<0>(c);
     vp_velocities_launch<1>(c);
     vp_velocities_launch<2>(c);
@@ -968,13 +1057,12 @@ void vel_pred(Ctx& c) {
 
 // ============================================================ MakeEdgeScal
 // MakeDivU (Source/MaestroMakeEdgeScalars.cpp:648-660)
-__global__ void k_divu(KARGS, double dx0) {
+__global__ void k_divu(KARGS, RecipC rdx0) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView u = VW(F_UMAC0), v = VW(F_UMAC1), w = VW(F_UMAC2);
     double d = at(u, i + 1, j, k) - at(u, i, j, k) + at(v, i, j + 1, k) - at(v, i, j, k) + at(w, i, j, k + 1) -
                at(w, i, j, k);
-    d /= dx0;
-    at(VW(F_DIVU), i, j, k) = d;
+    at(VW(F_DIVU), i, j, k) = div_c(d, rdx0);
 }
 
 // MakeEdgeScalPredictor, 3-D (Source/MaestroMakeEdgeScalars.cpp:662-863)
@@ -1017,27 +1105,25 @@ __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double 
             r = 0.0;
         }
     }
-    double sm = (ud > 0.0) ? l : r;
-    sm = (fabs(ud) > 0.0) ? sm : 0.5 * (l + r);
     at(VW(F_SL0 + D), i, j, k) = l;
     at(VW(F_SR0 + D), i, j, k) = r;
-    at(VW(F_SIMH0 + D), i, j, k) = sm;
+    at(VW(F_SIMH0 + D), i, j, k) = upwind(ud, l, r, 0);  // tie test |u| > 0
 }
 
 // MakeEdgeScalTransverse, 3-D (Source/MaestroMakeEdgeScalars.cpp:865-1359): D-faces
-// corrected in direction T.
+// corrected in direction T.  Advective form: F_TCOEF comp T = (dt6/h_T)*(u_T sum).
 template <int D, int T>
-__global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double dt3h, double dt6h, int bclo, int bchi,
-                                int domlo, int domhi, double rel_eps) {
+__global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double dt3h, int bclo, int bchi, int domlo,
+                                int domhi, long long epsb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
     const int il = i - di, jl = j - dj, kl = k - dk;
-    const FabView st = VW(F_SIMH0 + T), ut = VW(F_UMAC0 + T), sc = VW(F_SOLD);
+    const FabView st = VW(F_SIMH0 + T), sc = VW(F_SOLD);
     double lq, rq;
     if (is_cons) {
-        const FabView dv = VW(F_DIVU);
+        const FabView ut = VW(F_UMAC0 + T), dv = VW(F_DIVU);
         lq = at(VW(F_SL0 + D), i, j, k) -
              dt3h * (at(st, il + ti, jl + tj, kl + tk) * at(ut, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl) * at(ut, il, jl, kl)) -
              dt3 * at(sc, il, jl, kl, comp) * at(dv, il, jl, kl) +
@@ -1047,10 +1133,9 @@ __global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double
              dt3 * at(sc, i, j, k, comp) * at(dv, i, j, k) +
              dt3h * at(sc, i, j, k, comp) * (at(ut, i + ti, j + tj, k + tk) - at(ut, i, j, k));
     } else {
-        lq = at(VW(F_SL0 + D), i, j, k) - dt6h * (at(ut, il + ti, jl + tj, kl + tk) + at(ut, il, jl, kl)) *
-                                               (at(st, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl));
-        rq = at(VW(F_SR0 + D), i, j, k) - dt6h * (at(ut, i + ti, j + tj, k + tk) + at(ut, i, j, k)) *
-                                               (at(st, i + ti, j + tj, k + tk) - at(st, i, j, k));
+        const FabView tc = VW(F_TCOEF);
+        lq = at(VW(F_SL0 + D), i, j, k) - at(tc, il, jl, kl, T) * (at(st, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl));
+        rq = at(VW(F_SR0 + D), i, j, k) - at(tc, i, j, k, T) * (at(st, i + ti, j + tj, k + tk) - at(st, i, j, k));
     }
     if (I == domlo) {
         if (bclo == BC_EXT_DIR) {
@@ -1073,16 +1158,15 @@ __global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double
             rq = 0.0;
         }
     }
-    const double ud = at(VW(F_UMAC0 + D), i, j, k);
-    double v = (ud > 0.0) ? lq : rq;
-    v = (fabs(ud) > rel_eps) ? v : 0.5 * (lq + rq);
-    at(VW(Q_FIELD(D, T)), i, j, k) = v;
+    at(VW(Q_FIELD(D, T)), i, j, k) = upwind(at(VW(F_UMAC0 + D), i, j, k), lq, rq, epsb);
 }
 
-// MakeEdgeScalEdges, 3-D (Source/MaestroMakeEdgeScalars.cpp:1361-1667)
+// MakeEdgeScalEdges, 3-D (Source/MaestroMakeEdgeScalars.cpp:1361-1667).  Advective form:
+// F_TCOEF comp 3+t = (dt4/h_t)*(u_t sum).  force_zero: the component's force is
+// identically zero (species), so the + dt/2*force term is skipped.
 template <int D>
-__global__ void k_es_edges(KARGS, int comp, int is_cons, double dt2, double dt2h1, double dt2h2, double dt2hd,
-                           double dt4h1, double dt4h2, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+__global__ void k_es_edges(KARGS, int comp, int is_cons, int force_zero, double dt2, double dt2h1, double dt2h2,
+                           double dt2hd, int bclo, int bchi, int domlo, int domhi, long long epsb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -1091,12 +1175,13 @@ __global__ void k_es_edges(KARGS, int comp, int is_cons, double dt2, double dt2h
     const int I = D == 0 ? i : (D == 1 ? j : k);
     const int il = i - di, jl = j - dj, kl = k - dk;
     const FabView q1 = VW(Q_FIELD(T1, T2)), q2 = VW(Q_FIELD(T2, T1));
-    const FabView u1 = VW(F_UMAC0 + T1), u2 = VW(F_UMAC0 + T2), udf = VW(F_UMAC0 + D);
-    const FabView sc = VW(F_SOLD), f = VW(F_SCALFORCE);
-    const double fl = at(f, il, jl, kl, comp);
-    const double fr = at(f, i, j, k, comp);
+    const FabView udf = VW(F_UMAC0 + D);
+    const FabView sc = VW(F_SOLD);
     double lq, rq;
     if (is_cons) {
+        const FabView u1 = VW(F_UMAC0 + T1), u2 = VW(F_UMAC0 + T2), f = VW(F_SCALFORCE);
+        const double fl = at(f, il, jl, kl, comp);
+        const double fr = at(f, i, j, k, comp);
         lq = at(VW(F_SL0 + D), i, j, k) -
              dt2h1 * (at(q1, il + a1i, jl + a1j, kl + a1k) * at(u1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl) * at(u1, il, jl, kl)) -
              dt2h2 * (at(q2, il + a2i, jl + a2j, kl + a2k) * at(u2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl) * at(u2, il, jl, kl)) -
@@ -1106,18 +1191,20 @@ __global__ void k_es_edges(KARGS, int comp, int is_cons, double dt2, double dt2h
              dt2h2 * (at(q2, i + a2i, j + a2j, k + a2k) * at(u2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k) * at(u2, i, j, k)) -
              dt2hd * at(sc, i, j, k, comp) * (at(udf, i + di, j + dj, k + dk) - at(udf, i, j, k)) + dt2 * fr;
     } else {
+        const FabView tc = VW(F_TCOEF);
         lq = at(VW(F_SL0 + D), i, j, k) -
-             dt4h1 * (at(u1, il + a1i, jl + a1j, kl + a1k) + at(u1, il, jl, kl)) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
-             dt4h2 * (at(u2, il + a2i, jl + a2j, kl + a2k) + at(u2, il, jl, kl)) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
-             dt2 * fl;
+             at(tc, il, jl, kl, 3 + T1) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
+             at(tc, il, jl, kl, 3 + T2) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl));
         rq = at(VW(F_SR0 + D), i, j, k) -
-             dt4h1 * (at(u1, i + a1i, j + a1j, k + a1k) + at(u1, i, j, k)) * (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
-             dt4h2 * (at(u2, i + a2i, j + a2j, k + a2k) + at(u2, i, j, k)) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
-             dt2 * fr;
+             at(tc, i, j, k, 3 + T1) * (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
+             at(tc, i, j, k, 3 + T2) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k));
+        if (!force_zero) {
+            const FabView f = VW(F_SCALFORCE);
+            lq = lq + dt2 * at(f, il, jl, kl, comp);
+            rq = rq + dt2 * at(f, i, j, k, comp);
+        }
     }
-    const double ud = at(udf, i, j, k);
-    double v = (ud > 0.0) ? lq : rq;
-    v = (fabs(ud) > rel_eps) ? v : 0.5 * (lq + rq);
+    double v = upwind(at(udf, i, j, k), lq, rq, epsb);
     if (I == domlo) {
         if (bclo == BC_EXT_DIR) v = at(sc, il, jl, kl, comp);
         else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) v = rq;
@@ -1147,23 +1234,27 @@ static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons
     ghi[O] = 1;
     ghi[D] = 1;
     const RegionTable& rt = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1);
-    const double dt3 = c.P.dt / 3.0, dt6 = c.P.dt / 6.0;
-    launch(c, rt, 1, k_es_transverse<D, T>, c.V(), comp, is_cons, dt3, dt3 / c.P.dx[T], dt6 / c.P.dx[T], bc.lo[D],
-           bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+    const double dt3 = c.P.dt / 3.0;
+    launch(c, rt, 1, k_es_transverse<D, T>, c.V(), comp, is_cons, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
+           c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
 }
 
 template <int D>
-static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons) {
+static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero) {
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
-    const double dt2 = 0.5 * c.P.dt, dt4 = 0.25 * c.P.dt;
-    launch(c, rg_grow(c, 0, D), 1, k_es_edges<D>, c.V(), comp, is_cons, dt2, dt2 / c.P.dx[T1], dt2 / c.P.dx[T2],
-           dt2 / c.P.dx[D], dt4 / c.P.dx[T1], dt4 / c.P.dx[T2], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-           c.P.rel_eps);
+    const double dt2 = 0.5 * c.P.dt;
+    launch(c, rg_grow(c, 0, D), 1, k_es_edges<D>, c.V(), comp, is_cons, force_zero, dt2, dt2 / c.P.dx[T1],
+           dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
+           dbits_host(c.P.rel_eps));
 }
 
-void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons) {
+// force_zero: the components' force is identically zero (DensityAdvance species)
+void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons, int force_zero) {
     const BCRecD* bh = bcs_host(c, which_bcs);
-    if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), c.P.dx[0]);
+    if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), make_recip(c.P.dx[0]));
+    // velocity-only quantities shared by every component of this call
+    if (c.P.ppm_type != 0) trace_coeffs_faces(c, F_UMAC0);
+    if (!is_cons) transverse_coeffs(c, F_UMAC0);
     for (int comp = start_comp; comp < start_comp + num_comp; ++comp) {
         const BCRecD& bc = bh[comp];  // start_bccomp == start_scomp at every call site
         if (c.P.ppm_type == 0) {
@@ -1180,30 +1271,30 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
         es_transverse_launch<1, 2>(c, comp, bc, is_cons);
         es_transverse_launch<2, 0>(c, comp, bc, is_cons);
         es_transverse_launch<2, 1>(c, comp, bc, is_cons);
-        es_edges_launch<0>(c, comp, bc, is_cons);
-        es_edges_launch<1>(c, comp, bc, is_cons);
-        es_edges_launch<2>(c, comp, bc, is_cons);
+        es_edges_launch<0>(c, comp, bc, is_cons, force_zero);
+        es_edges_launch<1>(c, comp, bc, is_cons, force_zero);
+        es_edges_launch<2>(c, comp, bc, is_cons, force_zero);
     }
 }
 
 // ============================================================ forces
 // ModifyScalForce, planar 3-D (Source/MaestroForce.cpp:413-441)
-__global__ void k_modify_scal_force(KARGS, int comp, int s0cart, int fullform, double dx0, double dx1, double dx2) {
+__global__ void k_modify_scal_force(KARGS, int comp, int s0cart, int fullform, RecipC r0, RecipC r1, RecipC r2) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
     const FabView s0a = VW(s0cart), s0e = VW(F_S0ECART), w0a = VW(F_W0CART);
     const double scal = at(VW(F_SOLD), i, j, k, comp);
-    double divu = (at(um, i + 1, j, k) - at(um, i, j, k)) / dx0 + (at(vm, i, j + 1, k) - at(vm, i, j, k)) / dx1 +
-                  (at(wm, i, j, k + 1) - at(wm, i, j, k)) / dx2;
-    divu += (at(w0a, i, j, k + 1, 2) - at(w0a, i, j, k, 2)) / dx2;
+    const double du = div_c(at(um, i + 1, j, k) - at(um, i, j, k), r0);
+    const double dv = div_c(at(vm, i, j + 1, k) - at(vm, i, j, k), r1);
+    double divu = du + dv + div_c(at(wm, i, j, k + 1) - at(wm, i, j, k), r2);
+    divu += div_c(at(w0a, i, j, k + 1, 2) - at(w0a, i, j, k, 2), r2);
     double& force = at(VW(F_SCALFORCE), i, j, k, comp);
     if (fullform == 1) {
         force -= scal * divu;
     } else {
         const double s0 = at(s0a, i, j, k);
         const double divs0u =
-            s0 * ((at(um, i + 1, j, k) - at(um, i, j, k)) / dx0 + (at(vm, i, j + 1, k) - at(vm, i, j, k)) / dx1) +
-            (at(wm, i, j, k + 1) * at(s0e, i, j, k + 1) - at(wm, i, j, k) * at(s0e, i, j, k)) / dx2;
+            s0 * (du + dv) + div_c(at(wm, i, j, k + 1) * at(s0e, i, j, k + 1) - at(wm, i, j, k) * at(s0e, i, j, k), r2);
         force += -(scal - s0) * divu - divs0u;
     }
 }
@@ -1212,22 +1303,22 @@ void modify_scal_force(Ctx& c, int comp, const double* d_s0_edge, int s0cart_fid
     set_val(c, F_S0ECART, 0.0, 0, 1, 1);
     put1d(c, F_S0ECART, d_s0_edge, 0, 0);
     fill_patch(c, F_S0ECART, 0, 1, BCS_F, 0, 0, -1);
-    launch(c, rg_grow(c, 0), 1, k_modify_scal_force, c.V(), comp, s0cart_fid, fullform, c.P.dx[0], c.P.dx[1],
-           c.P.dx[2]);
+    launch(c, rg_grow(c, 0), 1, k_modify_scal_force, c.V(), comp, s0cart_fid, fullform, make_recip(c.P.dx[0]),
+           make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
     fill_patch(c, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
 }
 
 // MakeRhoHForce, planar 3-D (Source/MaestroForce.cpp:602-627)
-__global__ void k_rhoh_force(KARGS, int cutoff, int domhi, double dz, int psi_in, int add_thermal) {
+__global__ void k_rhoh_force(KARGS, int cutoff, int domhi, RecipC rdz, int psi_in, int add_thermal) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView p0c = VW(F_P0CART);
     double gradp0 = 0.0;
     if (k < cutoff) {
         gradp0 = at(VW(F_RHO0CART), i, j, k) * at(VW(F_GRAVCART), i, j, k, 2);
     } else if (k == domhi) {
-        gradp0 = (at(p0c, i, j, k) - at(p0c, i, j - 1, k)) / dz;
+        gradp0 = div_c(at(p0c, i, j, k) - at(p0c, i, j - 1, k), rdz);
     } else {
-        gradp0 = (at(p0c, i, j + 1, k) - at(p0c, i, j, k)) / dz;
+        gradp0 = div_c(at(p0c, i, j + 1, k) - at(p0c, i, j, k), rdz);
     }
     const FabView wm = VW(F_UMAC2);
     const double veladv = 0.5 * (at(wm, i, j, k) + at(wm, i, j, k + 1));
@@ -1256,8 +1347,8 @@ void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal, int which_step)
     fill_patch(c, F_GRAVCART, 0, 3, BCS_F, 0, 0, -1);
     const int ept = c.P.enthalpy_pred_type;
     const int psi_in = (is_prediction == 1 && ept == 2) || (is_prediction == 1 && ept == 0) || (is_prediction == 0);
-    launch(c, rg_grow(c, 0), 1, k_rhoh_force, c.V(), c.P.base_cutoff_density_coord, c.P.dom_hi[2], c.P.dx[2], psi_in,
-           add_thermal);
+    launch(c, rg_grow(c, 0), 1, k_rhoh_force, c.V(), c.P.base_cutoff_density_coord, c.P.dom_hi[2],
+           make_recip(c.P.dx[2]), psi_in, add_thermal);
     fill_patch(c, F_SCALFORCE, RHOH, 1, BCS_F, 0, 0, RHOH);
 }
 
@@ -1372,15 +1463,15 @@ void sum_species_edges(Ctx& c) {
 // Source/MaestroAdvection.cpp:117-251.  The species update and the density / floor /
 // negative-species pass of the reference are two ParallelFors over the same cells; they
 // are one kernel here with the same per-cell order of operations.
-__global__ void k_update_rhox(KARGS, int nspec, double dt, double dx0, double dx1, double dx2, double half_cutoff) {
+__global__ void k_update_rhox(KARGS, int nspec, double dt, RecipC r0, RecipC r1, RecipC r2, double half_cutoff) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fz = VW(F_SFLUX2),
                   fo = VW(F_SCALFORCE);
     for (int n = 0; n < nspec; ++n) {
         const int comp = FIRSTSPEC + n;
-        double divterm = (at(fx, i + 1, j, k, comp) - at(fx, i, j, k, comp)) / dx0;
-        divterm += (at(fy, i, j + 1, k, comp) - at(fy, i, j, k, comp)) / dx1;
-        divterm += (at(fz, i, j, k + 1, comp) - at(fz, i, j, k, comp)) / dx2;
+        double divterm = div_c(at(fx, i + 1, j, k, comp) - at(fx, i, j, k, comp), r0);
+        divterm += div_c(at(fy, i, j + 1, k, comp) - at(fy, i, j, k, comp), r1);
+        divterm += div_c(at(fz, i, j, k + 1, comp) - at(fz, i, j, k, comp), r2);
         at(sn, i, j, k, comp) = at(so, i, j, k, comp) + dt * (-divterm + at(fo, i, j, k, comp));
     }
     double rho = at(so, i, j, k, RHO);
@@ -1412,14 +1503,14 @@ __global__ void k_update_rhox(KARGS, int nspec, double dt, double dx0, double dx
     }
 }
 
-__global__ void k_update_rhoh(KARGS, double dt, double dx0, double dx1, double dx2, int eos_check, double cutoff,
+__global__ void k_update_rhoh(KARGS, double dt, RecipC r0, RecipC r1, RecipC r2, int eos_check, double cutoff,
                               int* flag) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fz = VW(F_SFLUX2),
                   fo = VW(F_SCALFORCE);
-    const double divterm = ((at(fx, i + 1, j, k, RHOH) - at(fx, i, j, k, RHOH)) / dx0 +
-                            (at(fy, i, j + 1, k, RHOH) - at(fy, i, j, k, RHOH)) / dx1 +
-                            (at(fz, i, j, k + 1, RHOH) - at(fz, i, j, k, RHOH)) / dx2);
+    const double divterm = (div_c(at(fx, i + 1, j, k, RHOH) - at(fx, i, j, k, RHOH), r0) +
+                            div_c(at(fy, i, j + 1, k, RHOH) - at(fy, i, j, k, RHOH), r1) +
+                            div_c(at(fz, i, j, k + 1, RHOH) - at(fz, i, j, k, RHOH), r2));
     at(sn, i, j, k, RHOH) = at(so, i, j, k, RHOH) + dt * (-divterm + at(fo, i, j, k, RHOH));
     if (eos_check && at(sn, i, j, k, RHO) <= cutoff) atomicOr(flag, 1);
 }
@@ -1427,12 +1518,12 @@ __global__ void k_update_rhoh(KARGS, double dt, double dx0, double dx1, double d
 void update_scal(Ctx& c, int start_comp) {
     const RegionTable& rt = rg_grow(c, 0);
     if (start_comp == RHOH) {
-        launch(c, rt, 1, k_update_rhoh, c.V(), c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2], c.P.do_eos_h_above_cutoff,
-               c.P.base_cutoff_density, c.d_flag);
+        launch(c, rt, 1, k_update_rhoh, c.V(), c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
+               make_recip(c.P.dx[2]), c.P.do_eos_h_above_cutoff, c.P.base_cutoff_density, c.d_flag);
         fill_patch(c, F_SNEW, RHOH, 1, BCS_S, RHOH, 0, RHOH);
     } else {
-        launch(c, rt, 1, k_update_rhox, c.V(), c.nspec, c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2],
-               0.5 * c.P.base_cutoff_density);
+        launch(c, rt, 1, k_update_rhox, c.V(), c.nspec, c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
+               make_recip(c.P.dx[2]), 0.5 * c.P.base_cutoff_density);
         fill_patch(c, F_SNEW, FIRSTSPEC, c.nspec, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
         fill_patch(c, F_SNEW, RHO, 1, BCS_S, RHO, 0, RHO);
     }

@@ -48,3 +48,73 @@ extern "C" int madv_probe_fp64_peak(double* tflops, void* stream) {
     *tflops = flops / (ms * 1e-3) / 1e12;
     return MADV_OK;
 }
+
+#include "madv_exact.cuh"
+
+namespace madv {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+// Random doubles with exponents spread over [2^-1000, 2^1000], both signs, plus
+// zeros, subnormals and values next to powers of two; each checked bit for bit.
+__global__ void k_selftest(unsigned long long n, unsigned long long seed, RecipC r, double thr,
+                           unsigned long long* fails) {
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const long long tb = dbits(thr);
+    unsigned long long local = 0;
+    for (unsigned long long idx = t; idx < n; idx += stride) {
+        unsigned long long h = mix64(idx * 0x9e3779b97f4a7c15ULL + seed);
+        double a;
+        const int kind = (int)(h & 15);
+        if (kind == 0) {
+            a = (h & 16) ? -0.0 : 0.0;
+        } else if (kind == 1) {
+            a = __longlong_as_double((long long)((h >> 8) & 0x000fffffffffffffULL));  // subnormal
+        } else {
+            const unsigned long long mant = (h >> 12) & 0x000fffffffffffffULL;
+            const unsigned long long ex = 23 + (mix64(h) % 2001);  // 2^-1000 .. 2^1000
+            unsigned long long bits = (ex << 52) | (kind == 2 ? 0ULL : (kind == 3 ? 0x000fffffffffffffULL : mant));
+            if (h & 32) bits |= 0x8000000000000000ULL;
+            a = __longlong_as_double((long long)bits);
+        }
+        const double q = div_c(a, r);
+        const double qi = a / r.y;
+        if (dbits(q) != dbits(qi)) ++local;
+        // integer comparisons against IEEE comparisons
+        if (gt_t(a, tb) != (a > thr)) ++local;
+        if (lt_negt(a, tb) != (a < -thr)) ++local;
+        if (abs_gt_t(a, tb) != (fabs(a) > thr)) ++local;
+        if (gt0(a) != (a > 0.0)) ++local;
+        if (nz(a) != (fabs(a) > 0.0)) ++local;
+    }
+    if (local) atomicAdd(fails, local);
+}
+
+}  // namespace madv
+
+extern "C" int madv_selftest_exact(double y, double threshold, long long n, long long* failures, void* stream) {
+    if (!failures || !(y > 0.0) || !(threshold >= 0.0) || n <= 0) return MADV_ERR_PARAM;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long* d = nullptr;
+    if (cudaMallocAsync(&d, sizeof(*d), s) != cudaSuccess) return MADV_ERR_CUDA;
+    cudaMemsetAsync(d, 0, sizeof(*d), s);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    madv::k_selftest<<<nsm * 8, 256, 0, s>>>((unsigned long long)n, 0x1234567ULL, madv::make_recip(y), threshold, d);
+    unsigned long long h = 0;
+    cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    cudaFreeAsync(d, s);
+    if (cudaGetLastError() != cudaSuccess) return MADV_ERR_CUDA;
+    *failures = (long long)h;
+    return MADV_OK;
+}

@@ -172,3 +172,12 @@ def test_rejects_bad_layout_and_params():
     with pytest.raises(capi.MadvError) as e:
         ScalarAdvectionStage(p)
     assert e.value.code == -3
+
+
+@pytest.mark.parametrize("y,thr", [(6.0, 0.0), (3.0, 1e-3), (390625.0, 6.45e-3), (1e8 / 256 * 2, 12.5),
+                                   (0.1, 1e-300), (7.77e-9, 3.3e5)])
+def test_exact_helpers_match_ieee(y, thr):
+    import ctypes as C
+    nfail = C.c_longlong(-1)
+    capi.check(capi.lib().madv_selftest_exact(y, thr, 1 << 24, C.byref(nfail), None))
+    assert nfail.value == 0
