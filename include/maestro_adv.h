@@ -150,6 +150,19 @@ int madv_stage_forward(madv_ctx* ctx, int mode, const madv_multifab* uold,
                        const madv_multifab* sflux, const madv_multifab* etarhoflux,
                        void* stream);
 
+/* Maestro::PPM (Source/Maestro.H:1396, Source/MaestroPPM.cpp:5-2262) on one box: for
+ * component comp of s, the traced edge states Ip(.,d) and Im(.,d), d = 0..2, over the cell
+ * box bx (the reference passes the box grown by one cell).  u, v, w: the tracing
+ * velocity, face-centred (is_umac = 1: FABs covering the x-, y-, z-faces of bx) or
+ * cell-centred (is_umac = 0).  bc = {lo[0..2], hi[0..2]}: the BCRec bcs[bccomp].
+ * ppm_type (1 or 2), dt, rel_eps, dx and the domain box come from the context.  s must
+ * cover bx grown by 2 (ppm_type 1) or 3 (ppm_type 2) cells; Ip and Im are 3-component
+ * FABs covering bx.  Scratch comes from the context and is grown with cudaMalloc when a
+ * larger box arrives. */
+int madv_ppm(madv_ctx* ctx, const madv_box* bx, const madv_fab* s, int comp, const madv_fab* u,
+             const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
+             const madv_fab* Im, void* stream);
+
 /* Number of kernel launches issued by the last madv_* call (for launch accounting). */
 long madv_last_launch_count(const madv_ctx* ctx);
 

@@ -594,6 +594,7 @@ void madv_ctx_destroy(madv_ctx* h) {
     free_layout(c);
     for (auto& kv : c.d1) cudaFree(kv.second);
     for (auto e : c.ev_pool) cudaEventDestroy(e);
+    if (c.box_scratch) cudaFree(c.box_scratch);
     if (c.d_bcs) cudaFree(c.d_bcs);
     if (c.d_flag) cudaFree(c.d_flag);
     delete h;
@@ -924,6 +925,29 @@ int madv_enthalpy_advance(madv_ctx* h, int which_step, const madv_multifab* sold
 }
 
 long madv_last_launch_count(const madv_ctx* h) { return h ? h->c.launches : -1; }
+
+int madv_ppm(madv_ctx* h, const madv_box* bx, const madv_fab* s, int comp, const madv_fab* u, const madv_fab* v,
+             const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip, const madv_fab* Im, void* stream) {
+    if (!h || !bx) return MADV_ERR_PARAM;
+    Ctx& c = h->c;
+    int n[3];
+    for (int d = 0; d < 3; ++d) {
+        n[d] = bx->hi[d] - bx->lo[d] + 1;
+        if (n[d] <= 0) return MADV_ERR_LAYOUT;
+    }
+    const long need = ppm_box_scratch_doubles(n);
+    if (need > c.box_scratch_n) {
+        if (c.box_scratch) cudaFree(c.box_scratch);
+        c.box_scratch = nullptr;
+        c.box_scratch_n = 0;
+        if (!cuda_ok(cudaMalloc(&c.box_scratch, sizeof(double) * need), "cudaMalloc(madv_ppm scratch)"))
+            return MADV_ERR_CUDA;
+        c.box_scratch_n = need;
+    }
+    c.launches = 0;
+    return ppm_box_run(c.P, bx, s, comp, u, v, w, is_umac, bc, Ip, Im, c.box_scratch, (cudaStream_t)stream,
+                       c.launches);
+}
 
 int madv_profile(madv_ctx* h, int enable) {
     if (!h) return MADV_ERR_PARAM;

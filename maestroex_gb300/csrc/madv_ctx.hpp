@@ -116,6 +116,9 @@ struct Ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<const void*> graph_key;
     long graph_launches = 0;
+    // scratch of the single-box entry points (madv_ppm), grown on demand
+    double* box_scratch = nullptr;
+    long box_scratch_n = 0;
 
     double* b1(const char* name) { return d1.at(name); }
     const FabView* V() const { return dviews; }
@@ -157,6 +160,10 @@ void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const d
 void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
                     const double* rh0e_new);
 void sum_species_edges(Ctx& c);
+long ppm_box_scratch_doubles(const int n[3]);
+int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int comp, const madv_fab* u,
+                const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
+                const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
 
 enum { BCS_S = 0, BCS_U = 1, BCS_F = 2 };

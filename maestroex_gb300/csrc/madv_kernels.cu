@@ -16,6 +16,7 @@
 
 #include "madv_ctx.hpp"
 #include "madv_exact.cuh"
+#include "madv_ppm.cuh"
 
 namespace madv {
 
@@ -280,103 +281,34 @@ void addw0(Ctx& c, int f0, double mult) {
 }
 
 // ============================================================ PPM
-// S(m): the field at cell (index + m) along direction D.
-#define SHIFT_S(s, sc) [&](int m) -> double { return at(s, i + m * di, j + m * dj, k + m * dk, sc); }
-
 // Van Leer slope of each cell along D (Source/MaestroPPM.cpp:37-73).  The reference
 // evaluates it four times per cell and direction; here once.
 template <int D>
 __global__ void k_dsvl(KARGS, int fs, int sc) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
-    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
-    const FabView s = VW(fs);
-    auto S = SHIFT_S(s, sc);
-    const double dsc = 0.5 * (S(1) - S(-1));
-    const double dsl = 2.0 * (S(0) - S(-1));
-    const double dsr = 2.0 * (S(1) - S(0));
-    double v = 0.0;
-    if (dsl * dsr > 0.0) v = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
-    at(VW(F_DSVL), i, j, k) = v;
+    at(VW(F_DSVL), i, j, k) = ppm_dsvl<D>(VW(fs), sc, i, j, k);
 }
 
-// Limited interface value of the face between cells f-1 and f along D (Maestro::PPM,
-// Source/MaestroPPM.cpp: ppm_type 1 :37-111, ppm_type 2 :257-335; the boundary
-// stencils of :131-205 / :443-700 are the values the reference assigns to the faces
-// next to an ext_dir/hoextrap boundary).  Computed once per face; the reference computes
-// each face twice (as sp of one cell and sm of the next).
+// Limited interface value of each face, once per face (the reference computes each face
+// twice, as sp of one cell and sm of the next).
 template <int D, int PPMT>
 __global__ void k_ppm_face(KARGS, int fs, int sc, int ff, int lo_ext, int hi_ext, int domlo, int domhi, RecipC r6) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
-    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
-    const FabView s = VW(fs);
-    auto S = SHIFT_S(s, sc);
-    const int I = D == 0 ? i : (D == 1 ? j : k);
-    double v;
-    if (lo_ext && I == domlo) {
-        v = S(-1);
-    } else if (hi_ext && I == domhi + 1) {
-        v = S(0);
-    } else if (lo_ext && I == domlo + 1) {
-        v = -0.2 * S(-2) + 0.75 * S(-1) + 0.5 * S(0) - 0.05 * S(1);
-        v = mx(v, mn(S(0), S(-1)));
-        v = mn(v, mx(S(0), S(-1)));
-    } else if (hi_ext && I == domhi) {
-        v = -0.2 * S(1) + 0.75 * S(0) + 0.5 * S(-1) - 0.05 * S(-2);
-        v = mx(v, mn(S(-1), S(0)));
-        v = mn(v, mx(S(-1), S(0)));
-    } else if (PPMT == 1) {
-        const FabView dv = VW(F_DSVL);
-        const double dvl = at(dv, i - di, j - dj, k - dk);
-        const double dvr = at(dv, i, j, k);
-        v = 0.5 * (S(0) + S(-1)) - div_c(dvr - dvl, r6);
-        v = mx(v, mn(S(0), S(-1)));
-        v = mn(v, mx(S(0), S(-1)));
-    } else {
-        const double C = 1.25;
-        v = (7.0 / 12.0) * (S(-1) + S(0)) - (1.0 / 12.0) * (S(-2) + S(1));
-        if ((v - S(-1)) * (S(0) - v) < 0.0) {
-            double D2 = 3.0 * (S(-1) - 2.0 * v + S(0));
-            double D2L = S(-2) - 2.0 * S(-1) + S(0);
-            double D2R = S(-1) - 2.0 * S(0) + S(1);
-            double sgn = copysign(1.0, D2);
-            double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
-            v = 0.5 * (S(-1) + S(0)) - div_c(D2LIM, r6);
-        }
-    }
-    at(VW(ff), i, j, k) = v;
+    at(VW(ff), i, j, k) = ppm_face_value<D, PPMT>(VW(fs), sc, VW(F_DSVL), i, j, k, lo_ext, hi_ext, domlo, domhi, r6);
 }
 
-// Interior fourth-order limited face value (ppm_type 2), face between cells c+m-1 and c+m.
-template <int D>
-__device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, int i, int j, int k, int m,
-                                                    const RecipC& r6) {
-    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
-    auto S = SHIFT_S(s, sc);
-    const double C = 1.25;
-    double se = (7.0 / 12.0) * (S(m - 1) + S(m)) - (1.0 / 12.0) * (S(m - 2) + S(m + 1));
-    if ((se - S(m - 1)) * (S(m) - se) < 0.0) {
-        double D2 = 3.0 * (S(m - 1) - 2.0 * se + S(m));
-        double D2L = S(m - 2) - 2.0 * S(m - 1) + S(m);
-        double D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
-        double sgn = copysign(1.0, D2);
-        double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
-        se = 0.5 * (S(m - 1) + S(m)) - div_c(D2LIM, r6);
-    }
-    return se;
-}
-
-// Characteristic-tracing coefficients of the reference (Source/MaestroPPM.cpp:209-251):
-// sigma = |u| dt / dx, A = 0.5 sigma, B = 1 - 2/3 sigma.  They depend on the velocity
-// only, so they are formed once per velocity field and direction and shared by every
-// traced component (the reference forms them per component, cell and direction).
+// Characteristic-tracing coefficients.  They depend on the velocity only, so they are
+// formed once per velocity field and direction and shared by every traced component
+// (the reference forms them per component, cell and direction).
 // Face-centred velocity (the is_umac case): one (A, B) per D-face.
 template <int D>
 __global__ void k_trace_face(KARGS, int fu, int fout, double dt, double dxd) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
-    const double sigma = fabs(at(VW(fu), i, j, k)) * dt / dxd;
+    double A, B;
+    trace_coeffs(at(VW(fu), i, j, k), dt, dxd, A, B);
     const FabView o = VW(fout);
-    at(o, i, j, k, 0) = 0.5 * sigma;
-    at(o, i, j, k, 1) = 1.0 - 2.0 / 3.0 * sigma;
+    at(o, i, j, k, 0) = A;
+    at(o, i, j, k, 1) = B;
 }
 
 // Cell-centred velocity (the velocity predictions): (A, B) per cell for each direction d,
@@ -386,117 +318,22 @@ __global__ void k_trace_cell(KARGS, int fu, double dt, double dx0, double dx1, d
     const FabView u = VW(fu), o = VW(F_TRC);
     const double dx[3] = {dx0, dx1, dx2};
     for (int d = 0; d < 3; ++d) {
-        const double sigma = fabs(at(u, i, j, k, d)) * dt / dx[d];
-        at(o, i, j, k, 2 * d) = 0.5 * sigma;
-        at(o, i, j, k, 2 * d + 1) = 1.0 - 2.0 / 3.0 * sigma;
+        double A, B;
+        trace_coeffs(at(u, i, j, k, d), dt, dx[d], A, B);
+        at(o, i, j, k, 2 * d) = A;
+        at(o, i, j, k, 2 * d + 1) = B;
     }
 }
 
-// Per-cell limiting and characteristic tracing (Source/MaestroPPM.cpp: quadratic
-// limiter :117-128, Colella-2008 limiter :337-434, tracing :209-251 / :706-770).
+// Per-cell limiting and characteristic tracing (Source/MaestroPPM.cpp).
 template <int D, int PPMT, int UMAC>
 __global__ void k_ppm_cell(KARGS, int fs, int sc, int ff, int fu, int uc, int fip, int fim, int lo_ext, int hi_ext,
                            int domlo, int domhi, long long epsb, RecipC r6) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const FabView s = VW(fs);
-    const FabView F = VW(ff);
-    auto S = SHIFT_S(s, sc);
-    auto Fc = [&](int m) -> double { return at(F, i + m * di, j + m * dj, k + m * dk); };
-    const int I = D == 0 ? i : (D == 1 ? j : k);
-    const double s0 = S(0);
     double sm, sp;
-    if (PPMT == 1) {
-        sm = Fc(0);
-        sp = Fc(1);
-        const bool special = (lo_ext && I == domlo) || (hi_ext && I == domhi);
-        if (!special) {
-            if ((sp - s0) * (s0 - sm) <= 0.0) {
-                sp = s0;
-                sm = s0;
-            } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
-                sp = 3.0 * s0 - 2.0 * sm;
-            } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
-                sm = 3.0 * s0 - 2.0 * sp;
-            }
-        }
-    } else {
-        const double C = 1.25;
-        double sedgel = Fc(-1), sedge = Fc(0), sedger = Fc(1), sedgerr = Fc(2);
-        if (D == 0 && hi_ext && I == domhi - 1) sedgerr = ppm2_face_regular<D>(s, sc, i, j, k, 2, r6);
-        if (lo_ext && I == domlo) {
-            sm = sedge;
-            sp = sedger;
-        } else if (hi_ext && I == domhi) {
-            sp = sedger;
-            sm = sedge;
-        } else {
-            const double bigm_tol = (D == 0 && lo_ext && (I == domlo + 1 || I == domlo + 2)) ? 1.e10 : 1.e-10;
-            double alphap = sedger - s0;
-            double alpham = sedge - s0;
-            const bool bigp = fabs(alphap) > 2.0 * fabs(alpham);
-            const bool bigm = fabs(alpham) > 2.0 * fabs(alphap);
-            bool extremum = false;
-            if (alpham * alphap >= 0.0) {
-                extremum = true;
-            } else if (bigp || bigm) {
-                double dafacem = sedge - sedgel;
-                double dafacep = sedgerr - sedger;
-                double dabarm = s0 - S(-1);
-                double dabarp = S(1) - s0;
-                double dafacemin = mn(fabs(dafacem), fabs(dafacep));
-                double dabarmin = mn(fabs(dabarm), fabs(dabarp));
-                double dachkm, dachkp;
-                if (dafacemin >= dabarmin) {
-                    dachkm = dafacem;
-                    dachkp = dafacep;
-                } else {
-                    dachkm = dabarm;
-                    dachkp = dabarp;
-                }
-                extremum = (dachkm * dachkp <= 0.0);
-            }
-            if (extremum) {
-                double D2 = 6.0 * (alpham + alphap);
-                double D2L = S(-2) - 2.0 * S(-1) + s0;
-                double D2R = s0 - 2.0 * S(1) + S(2);
-                double D2C = S(-1) - 2.0 * s0 + S(1);
-                double sgn = copysign(1.0, D2);
-                double D2LIM = mx(mn(sgn * D2, mn(C * sgn * D2L, mn(C * sgn * D2R, C * sgn * D2C))), 0.0);
-                double D2ABS = mx(fabs(D2), 1.e-10);
-                alpham = alpham * D2LIM / D2ABS;
-                alphap = alphap * D2LIM / D2ABS;
-            } else {
-                if (bigp) {
-                    double sgn = copysign(1.0, alpham);
-                    double amax = -alphap * alphap / (4.0 * (alpham + alphap));
-                    double delam = S(-1) - s0;
-                    if (sgn * amax >= sgn * delam) {
-                        if (sgn * (delam - alpham) >= 1.e-10) {
-                            alphap = -2.0 * delam - 2.0 * sgn * sqrt(delam * delam - delam * alpham);
-                        } else {
-                            alphap = -2.0 * alpham;
-                        }
-                    }
-                }
-                if (bigm) {
-                    double sgn = copysign(1.0, alphap);
-                    double amax = -alpham * alpham / (4.0 * (alpham + alphap));
-                    double delap = S(1) - s0;
-                    if (sgn * amax >= sgn * delap) {
-                        if (sgn * (delap - alphap) >= bigm_tol) {
-                            alpham = (-2.0 * delap - 2.0 * sgn * sqrt(delap * delap - delap * alphap));
-                        } else {
-                            alpham = -2.0 * alphap;
-                        }
-                    }
-                }
-            }
-            sm = s0 + alpham;
-            sp = s0 + alphap;
-        }
-    }
-    const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
+    ppm_cell_edges<D, PPMT>(s, sc, VW(ff), VW(F_DSVL), i, j, k, lo_ext, hi_ext, domlo, domhi, r6, sm, sp);
     const FabView u = VW(fu);
     double up, um, Ap, Bp, Am, Bm;
     if (UMAC) {
@@ -513,9 +350,8 @@ __global__ void k_ppm_cell(KARGS, int fs, int sc, int ff, int fu, int uc, int fi
         Ap = Am = at(T, i, j, k, 2 * D);
         Bp = Bm = at(T, i, j, k, 2 * D + 1);
     }
-    double ip = s0, im = s0;
-    if (gt_t(up, epsb)) ip = sp - Ap * (sp - sm - Bp * s6);
-    if (lt_negt(um, epsb)) im = sm + Am * (sp - sm + Bm * s6);
+    double ip, im;
+    ppm_trace(at(s, i, j, k, sc), sm, sp, up, um, Ap, Bp, Am, Bm, epsb, ip, im);
     at(VW(fip), i, j, k, D) = ip;
     at(VW(fim), i, j, k, D) = im;
 }

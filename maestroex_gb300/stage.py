@@ -85,6 +85,18 @@ class MultiFab:
         return out
 
 
+def fab_of_tensor(t, lo):
+    """madv_fab over a contiguous float64 device tensor [nc, nz, ny, nx] starting at cell lo."""
+    assert t.is_contiguous() and t.dtype == torch.float64
+    f = MadvFab()
+    f.p = t.data_ptr()
+    for d in range(3):
+        f.lo[d] = int(lo[d])
+        f.hi[d] = int(lo[d]) + t.shape[3 - d] - 1
+    f.ncomp = t.shape[0]
+    return f
+
+
 def _dptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
@@ -173,6 +185,20 @@ class ScalarAdvectionStage:
 
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
+
+    def ppm(self, bx, s, s_lo, comp, vel, vel_lo, is_umac, bc, Ip, Im, stream=None):
+        """Maestro::PPM on one box through madv_ppm.  s, vel[d], Ip, Im: torch tensors
+        [nc, nz, ny, nx] on the device whose first cell is s_lo / vel_lo[d] / bx lo."""
+        fabs = [fab_of_tensor(s, s_lo)] + [fab_of_tensor(vel[d], vel_lo[d]) for d in range(3)] + \
+               [fab_of_tensor(Ip, bx[:3]), fab_of_tensor(Im, bx[:3])]
+        box = MadvBox()
+        for d in range(3):
+            box.lo[d], box.hi[d] = int(bx[d]), int(bx[3 + d])
+        bcs = (C.c_int * 6)(*bc)
+        st = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_ppm(self.ctx, C.byref(box), C.byref(fabs[0]), comp, C.byref(fabs[1]), C.byref(fabs[2]),
+                             C.byref(fabs[3]), int(is_umac), bcs, C.byref(fabs[4]), C.byref(fabs[5]),
+                             C.c_void_p(st)))
 
 
 class StageBuffers:

@@ -1283,5 +1283,44 @@ int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {
     return 0;
 }
 
+static mo::Arr arr_of(const mo_fab* f) {
+    mo::Arr a;
+    a.p = f->p;
+    for (int d = 0; d < 3; ++d) {
+        a.lo[d] = f->lo[d];
+        a.hi[d] = f->hi[d];
+    }
+    const long nx = f->hi[0] - f->lo[0] + 1, ny = f->hi[1] - f->lo[1] + 1, nz = f->hi[2] - f->lo[2] + 1;
+    a.sj = nx;
+    a.sk = nx * ny;
+    a.sn = nx * ny * nz;
+    a.nc = f->nc;
+    return a;
+}
+
+int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const mo_fab* u, const mo_fab* v,
+           const mo_fab* w, int is_umac, const int* bc, const mo_fab* Ip, const mo_fab* Im) {
+    try {
+        mo::Box dom, b;
+        for (int d = 0; d < 3; ++d) {
+            dom.lo[d] = p->dom_lo[d];
+            dom.hi[d] = p->dom_hi[d];
+            b.lo[d] = bx[d];
+            b.hi[d] = bx[3 + d];
+        }
+        mo::PPMCtx pc{p->ppm_type, p->dt, p->rel_eps, {p->dx[0], p->dx[1], p->dx[2]}, dom};
+        mo::BCRec r;
+        for (int d = 0; d < 3; ++d) {
+            r.lo[d] = bc[d];
+            r.hi[d] = bc[3 + d];
+        }
+        mo::PPM(pc, b, arr_of(s), arr_of(u), arr_of(v), arr_of(w), arr_of(Ip), arr_of(Im), r, is_umac != 0, comp);
+        return 0;
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+
 const char* mo_last_error(void) { return mo::g_err.c_str(); }
 }

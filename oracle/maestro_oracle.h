@@ -76,6 +76,20 @@ typedef struct {
 int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
                  mo_outputs* out, int nthreads);
 
+/* A FAB: data covering the index box [lo, hi] (i fastest), nc components. */
+typedef struct {
+    double* p;
+    int lo[3];
+    int hi[3];
+    int nc;
+} mo_fab;
+
+/* Maestro::PPM (Source/MaestroPPM.cpp:5-2262) over the cell box bx[6] (lo, hi) for
+ * component comp of s, tracing velocity u/v/w (face FABs if is_umac, else cell FABs);
+ * bc = {lo[3], hi[3]}; writes Ip/Im comps 0..2. */
+int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const mo_fab* u, const mo_fab* v,
+           const mo_fab* w, int is_umac, const int* bc, const mo_fab* Ip, const mo_fab* Im);
+
 /* 1-D CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), single level. */
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge);
 

@@ -104,3 +104,41 @@ def run_stage(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_e
     if rc != 0:
         raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
     return res
+
+
+class MoFab(C.Structure):
+    _fields_ = [("p", C.POINTER(C.c_double)), ("lo", C.c_int * 3), ("hi", C.c_int * 3), ("nc", C.c_int)]
+
+
+def fab_of(arr, lo):
+    """mo_fab over a numpy array shaped [nc, nz, ny, nx] whose first cell is `lo`."""
+    a = np.ascontiguousarray(arr)
+    f = MoFab()
+    f.p = a.ctypes.data_as(C.POINTER(C.c_double))
+    for d in range(3):
+        f.lo[d] = lo[d]
+        f.hi[d] = lo[d] + a.shape[3 - d] - 1
+    f.nc = a.shape[0]
+    return f, a
+
+
+def ppm(params, bx, s, s_lo, comp, vel, vel_lo, is_umac, bc, checked=True):
+    """Oracle Maestro::PPM on box bx (lo0,lo1,lo2,hi0,hi1,hi2); returns (Ip, Im) [3, nz, ny, nx]."""
+    n = [bx[3 + d] - bx[d] + 1 for d in range(3)]
+    Ip = np.full((3, n[2], n[1], n[0]), np.nan)
+    Im = np.full((3, n[2], n[1], n[0]), np.nan)
+    keep = []
+    fs, a = fab_of(s, s_lo); keep.append(a)
+    fv = []
+    for d in range(3):
+        f, a = fab_of(vel[d], vel_lo[d]); keep.append(a); fv.append(f)
+    fip, _ = fab_of(Ip, bx[:3])
+    fim, _ = fab_of(Im, bx[:3])
+    bcs = (C.c_int * 6)(*bc)
+    bxa = (C.c_int * 6)(*bx)
+    L = lib(checked)
+    rc = L.mo_ppm(C.byref(params), bxa, C.byref(fs), comp, C.byref(fv[0]), C.byref(fv[1]), C.byref(fv[2]),
+                  int(is_umac), bcs, C.byref(fip), C.byref(fim))
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.mo_last_error().decode())
+    return Ip, Im
