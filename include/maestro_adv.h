@@ -163,6 +163,21 @@ int madv_ppm(madv_ctx* ctx, const madv_box* bx, const madv_fab* s, int comp, con
              const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
              const madv_fab* Im, void* stream);
 
+/* madv_ppm without any device allocation, for callers that cannot call cudaMalloc where
+ * they run PPM -- e.g. an AMReX application whose arena already holds most of the GPU's
+ * memory, or code that must avoid the implicit device synchronisation of cudaMalloc and
+ * cudaFree.  No counterpart in the reference.  Same arguments and results as madv_ppm,
+ * with the parameters taken from `params` instead of a context.  Scratch is one static
+ * device array of MADV_PPM_NOALLOC_MAX_DOUBLES doubles (9.04 MiB) that every GPU loading
+ * the library holds until exit; a box needing more (larger than 66 x 66 x 66 cells) is
+ * rejected with MADV_ERR_LAYOUT.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress) and must come before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race, so keep them on one stream. */
+#define MADV_PPM_NOALLOC_MAX_DOUBLES 1184832
+int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_fab* s, int comp,
+                     const madv_fab* u, const madv_fab* v, const madv_fab* w, int is_umac,
+                     const int* bc, const madv_fab* Ip, const madv_fab* Im, void* stream);
+
 /* Number of kernel launches issued by the last madv_* call (for launch accounting). */
 long madv_last_launch_count(const madv_ctx* ctx);
 

@@ -25,7 +25,7 @@ EXPORTED = [
     "madv_set_base_state", "madv_advance_premac", "madv_addw0", "madv_density_advance",
     "madv_enthalpy_advance", "madv_stage_forward", "madv_last_launch_count",
     "madv_last_error", "madv_version", "madv_profile", "madv_profile_report", "madv_probe_fp64_peak",
-    "madv_selftest_exact", "madv_ppm",
+    "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc",
 ]
 
 
@@ -79,6 +79,8 @@ def lib():
         FAB = P(MadvFab)
         L.madv_ppm.argtypes = [C.c_void_p, P(MadvBox), FAB, C.c_int, FAB, FAB, FAB, C.c_int, P(C.c_int), FAB, FAB,
                                C.c_void_p]
+        L.madv_ppm_noalloc.argtypes = [P(MadvParams), P(MadvBox), FAB, C.c_int, FAB, FAB, FAB, C.c_int, P(C.c_int),
+                                       FAB, FAB, C.c_void_p]
         L.madv_last_launch_count.argtypes = [C.c_void_p]
         L.madv_last_launch_count.restype = C.c_long
         L.madv_profile.argtypes = [C.c_void_p, C.c_int]
