@@ -29,6 +29,18 @@ METRIC = "advected cell-updates/s (FP64, <=1e-12 rel) batched vs per-box; %HBM; 
 UNIT = "cell-updates/s"
 HBM_PEAK_FALLBACK = 6792.7
 
+# Per-cell work of the kernels that bound the stage, counted by ncu on one batched stage of
+# 128^3 cells in 8 boxes of 64^3, NumSpec 13, ppm_type 1 (the counts per valid cell do not
+# depend on how many 64^3 boxes there are; summaries under profiles/):
+#   fp64: FP64 warp instructions (smsp__inst_executed_pipe_fp64.sum) per valid cell, one launch
+#   dram: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per valid cell, one launch
+KERNEL_WORK = {
+    "k_ppm_cell<0,1,1>": {"fp64": 0.9596, "dram": None},
+    "k_ppm_cell<1,1,1>": {"fp64": 0.9595, "dram": None},
+    "k_ppm_cell<2,1,1>": {"fp64": 0.9482, "dram": None},
+}
+STAGE_FP64_PER_CELL = 189.02  # FP64 warp instructions per valid cell, whole stage
+
 
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -36,6 +48,68 @@ def measured_peaks():
         with open(p) as f:
             return json.load(f), "measured"
     return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def demangle(name):
+    """Short form of a madv kernel symbol: _ZN4madv10k_ppm_cellILi1ELi1ELi1EEEv... -> k_ppm_cell<1,1,1>."""
+    import re
+    m = re.match(r"_ZN4madv(\d+)", name)
+    if not m:
+        return name
+    n = int(m.group(1))
+    base = name[m.end():m.end() + n]
+    pos = m.end() + n
+    if name[pos:pos + 1] != "I":
+        return base
+    pos += 1
+    args = []
+    while True:
+        a = re.match(r"Li(n?\d+)E", name[pos:])
+        if not a:
+            break
+        args.append(a.group(1).replace("n", "-"))
+        pos += a.end()
+    return f"{base}<{','.join(args)}>"
+
+
+def roofline(kern, ncell, stage_ms, fp64_tflops_probe, peaks, peak_kind):
+    """FP64-issue roofline of the dominant kernel (by device time in one batched stage).
+
+    achieved = FP64 warp instructions per launch (per-cell count x valid cells) / the
+    kernel's mean launch time (CUDA events around each launch); peak = the FP64 issue rate
+    of the DFMA-chain probe run in this process (1 DFMA = 2 flops, so issue rate = probe
+    TFLOP/s / 2).  Units: 10^12 FP64 lane-instructions per second (warp instructions x 32).
+    """
+    fam = {}
+    for k, (n, ms) in kern.items():
+        d = demangle(k)
+        fam.setdefault(d, [0, 0.0])
+        fam[d][0] += n
+        fam[d][1] += ms
+    top = max(fam.items(), key=lambda kv: kv[1][1])
+    name, (launches, ms) = top
+    issue_peak = fp64_tflops_probe / 2.0  # T lane-instructions/s
+    r = {"bound": "fp64", "kernel": name, "unit": "T FP64 lane-inst/s", "launches": launches,
+         "mean_launch_ms": ms / launches, "peak": issue_peak,
+         "peak_kind": "measured in this run (DFMA-chain probe, %.3f TFLOP/s)" % fp64_tflops_probe}
+    work = KERNEL_WORK.get(name)
+    if work is None:
+        r.update({"achieved": None, "frac": None, "traffic": None,
+                  "note": "no ncu instruction count recorded for this kernel"})
+        return r
+    inst = work["fp64"] * 32 * ncell
+    r["achieved"] = inst / (ms / launches * 1e-3) / 1e12
+    r["frac"] = r["achieved"] / issue_peak
+    r["algorithmic_per_launch"] = {"fp64_lane_inst": inst, "per_valid_cell": work["fp64"] * 32}
+    r["traffic"] = None if work["dram"] is None else work["dram"] * ncell
+    hbm = peaks.get("hbm_gbs", HBM_PEAK_FALLBACK)
+    if work["dram"] is not None:
+        r["hbm"] = {"achieved_gbs": r["traffic"] / (ms / launches * 1e-3) / 1e9, "peak_gbs": hbm,
+                    "peak_kind": peak_kind}
+    st_inst = STAGE_FP64_PER_CELL * 32 * ncell
+    r["stage"] = {"fp64_lane_inst": st_inst, "achieved": st_inst / (stage_ms * 1e-3) / 1e12,
+                  "frac": st_inst / (stage_ms * 1e-3) / 1e12 / issue_peak}
+    return r
 
 
 def dist_env():
@@ -291,6 +365,7 @@ def main():
         "fp64_peak_tflops_probe": tf.value,
         "kernels_top": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / ktot, 4)}
                         for k, v in top},
+        "roofline": roofline(kern, ncell, ms_graph, tf.value, peaks, peak_kind),
         "stage_hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": peaks.get("hbm_gbs", HBM_PEAK_FALLBACK),
                       "frac": hbm_gbs / peaks.get("hbm_gbs", HBM_PEAK_FALLBACK), "peak_kind": peak_kind,
                       "bytes_per_cell": b_cell},
