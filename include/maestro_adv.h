@@ -107,6 +107,20 @@ int madv_set_dt(madv_ctx* ctx, double dt, double rel_eps);
 int madv_set_layout(madv_ctx* ctx, int nboxes, const madv_box* boxes);
 int madv_set_base_state(madv_ctx* ctx, const madv_base_state* bs);
 
+/* An AMR hierarchy of nlev levels (1 or 2, refinement ratio 2), the grids[lev] BoxArrays
+ * of the reference (Source/Maestro.H:1855-2025): nboxes[l] boxes of level l follow those
+ * of level l-1 in `boxes`, in level-l index space.  Level 0 covers the domain; level-1
+ * boxes are coarse-aligned (even lo, odd hi).  Replaces madv_set_layout. */
+int madv_set_layout_levels(madv_ctx* ctx, int nlev, const int* nboxes, const madv_box* boxes);
+
+/* Base state of every level, bs[l] holding level l's arrays (nr_l = nr_0 * 2^l cells),
+ * i.e. the (lev, r) rows of the reference's BaseState arrays (Source/BaseState.H:14-130).
+ * Edge states come from Maestro::CelltoEdge over each level's radial chunks followed by
+ * RestrictBase (Source/MaestroCelltoEdge.cpp:5-58); with two levels the per-level
+ * base_cutoff_density_coord follows BaseStateGeometry::ComputeCutoffCoords
+ * (Source/BaseStateGeometry.cpp:112-210) applied to rho0_old.  Call after the layout. */
+int madv_set_base_state_levels(madv_ctx* ctx, int nlev, const madv_base_state* bs);
+
 /* Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84), one level.
  * uold: 3 comps, sold: 4+nspec comps (only Rho is read), gpi: 3 comps (valid region read).
  * umac[3]: face MultiFabs with >= 1 ghost, written on the valid faces (VelPred output).
@@ -149,6 +163,22 @@ int madv_stage_forward(madv_ctx* ctx, int mode, const madv_multifab* uold,
                        const madv_multifab* umac, const madv_multifab* sedge,
                        const madv_multifab* sflux, const madv_multifab* etarhoflux,
                        void* stream);
+
+/* madv_stage_forward on an AMR hierarchy: the reference's Vector<MultiFab> arguments,
+ * uold[l], sold[l], gpi[l], thermal[l], snew[l], etarhoflux[l] for level l and
+ * umac[3*l + d], sedge[3*l + d], sflux[3*l + d] for its faces (thermal, snew, umac, sedge,
+ * sflux and etarhoflux may be NULL).  Between the per-level computations the levels are
+ * coupled as the reference couples them: AverageDown + FillPatch (cell_cons_interp) after
+ * each cell-centred update (Source/MaestroFillData.cpp:7-154), AverageDownFaces +
+ * FillPatchUedge for the face velocities (:156-174, :455-835), AverageDownFaces of the
+ * fluxes (reflux_type 1, Source/MaestroMakeFlux.cpp:460-462).  In MADV_MODE_BATCHED /
+ * MADV_MODE_GRAPH each kernel covers all boxes of one level per launch. */
+int madv_stage_forward_levels(madv_ctx* ctx, int mode, int nlev, const madv_multifab* uold,
+                              const madv_multifab* sold, const madv_multifab* gpi,
+                              const madv_multifab* thermal, const madv_multifab* snew,
+                              const madv_multifab* umac, const madv_multifab* sedge,
+                              const madv_multifab* sflux, const madv_multifab* etarhoflux,
+                              void* stream);
 
 /* Maestro::PPM (Source/Maestro.H:1396, Source/MaestroPPM.cpp:5-2262) on one box: for
  * component comp of s, the traced edge states Ip(.,d) and Im(.,d), d = 0..2, over the cell

@@ -25,7 +25,8 @@ EXPORTED = [
     "madv_set_base_state", "madv_advance_premac", "madv_addw0", "madv_density_advance",
     "madv_enthalpy_advance", "madv_stage_forward", "madv_last_launch_count",
     "madv_last_error", "madv_version", "madv_profile", "madv_profile_report", "madv_probe_fp64_peak",
-    "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc",
+    "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc", "madv_set_layout_levels",
+    "madv_set_base_state_levels", "madv_stage_forward_levels",
 ]
 
 
@@ -69,6 +70,8 @@ def lib():
         L.madv_set_dt.argtypes = [C.c_void_p, C.c_double, C.c_double]
         L.madv_set_layout.argtypes = [C.c_void_p, C.c_int, P(MadvBox)]
         L.madv_set_base_state.argtypes = [C.c_void_p, P(MadvBaseState)]
+        L.madv_set_layout_levels.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(MadvBox)]
+        L.madv_set_base_state_levels.argtypes = [C.c_void_p, C.c_int, P(MadvBaseState)]
         MF = P(MadvMultiFab)
         L.madv_advance_premac.argtypes = [C.c_void_p, MF, MF, MF, MF, MF, C.c_void_p]
         L.madv_addw0.argtypes = [C.c_void_p, MF, C.c_double, C.c_void_p]
@@ -76,6 +79,8 @@ def lib():
         L.madv_enthalpy_advance.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, C.c_void_p]
         L.madv_stage_forward.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                          C.c_void_p]
+        L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
+                                                C.c_void_p]
         FAB = P(MadvFab)
         L.madv_ppm.argtypes = [C.c_void_p, P(MadvBox), FAB, C.c_int, FAB, FAB, FAB, C.c_int, P(C.c_int), FAB, FAB,
                                C.c_void_p]

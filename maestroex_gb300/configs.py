@@ -201,3 +201,76 @@ def config_c2(n=256, box=64, nspec=13, seed=20261203 + 1):
     """Config 2: 3-D single level, 256^3 in 64 boxes of 64^3, NumSpec 13, ppm_type 1, w0 != 0."""
     return planar_config(n=(n, n, n), nspec=nspec, ppm_type=1, max_grid=box, seed=seed,
                          w0_amp=1.0e4, cfl=0.7)
+
+
+def bubble_boxes(n0, nbubbles=3, cover=0.12, block_edges=(8, 16, 32), rng=None, max_edge=32):
+    """Level-1 boxes (refinement ratio 2, fine index space) around seeded bubble centres.
+
+    The coarse domain is cut along each axis into segments whose lengths come from
+    `block_edges` (coarse cells, clipped to max_edge); every block that contains a cell within
+    radius R of a bubble centre becomes one fine box.  R is chosen so the tagged volume is
+    about `cover` of the domain.  Boxes are coarse-aligned (even lo, odd hi in fine cells).
+    """
+    rng = np.random.default_rng(20261203 + 3) if rng is None else rng
+    n0 = tuple(int(v) for v in n0)
+    centres = [rng.uniform(0.2, 0.8, size=3) * np.array(n0) for _ in range(nbubbles)]
+    R = (cover * n0[0] * n0[1] * n0[2] / nbubbles * 3.0 / (4.0 * math.pi)) ** (1.0 / 3.0)
+    cuts = []
+    for d in range(3):
+        pts, p = [0], 0
+        while p < n0[d]:
+            e = int(min(rng.choice(block_edges), max_edge, n0[d] - p))
+            p += e
+            pts.append(p)
+        cuts.append(pts)
+    z, y, x = np.meshgrid(*[np.arange(n0[d]) + 0.5 for d in (2, 1, 0)], indexing="ij")
+    tag = np.zeros((n0[2], n0[1], n0[0]), bool)
+    for c in centres:
+        tag |= (x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 <= R * R
+    boxes = []
+    for k in range(len(cuts[2]) - 1):
+        for j in range(len(cuts[1]) - 1):
+            for i in range(len(cuts[0]) - 1):
+                lo = (cuts[0][i], cuts[1][j], cuts[2][k])
+                hi = (cuts[0][i + 1], cuts[1][j + 1], cuts[2][k + 1])
+                if tag[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]].any():
+                    boxes.append((2 * lo[0], 2 * lo[1], 2 * lo[2], 2 * hi[0] - 1, 2 * hi[1] - 1, 2 * hi[2] - 1))
+    return boxes
+
+
+def _average_down(fine, coarse, fine_boxes):
+    """Coarse cells under fine boxes become the mean of their 8 children (in place)."""
+    for b in fine_boxes:
+        i0, j0, k0, i1, j1, k1 = b
+        f = fine[..., k0:k1 + 1, j0:j1 + 1, i0:i1 + 1]
+        c = f.reshape(f.shape[:-3] + (f.shape[-3] // 2, 2, f.shape[-2] // 2, 2, f.shape[-1] // 2, 2))
+        c = c.sum(axis=(-1, -3, -5)) * 0.125
+        coarse[..., k0 // 2:(k1 + 1) // 2, j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2] = c
+
+
+LEVEL_KEYS = ("n", "dx", "boxes", "uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old",
+              "rhoh0_new", "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge")
+
+
+def planar_amr_config(n0=(32, 32, 32), nspec=3, ppm_type=2, max_grid=16, fine_boxes=None, level0_boxes=None,
+                      seed=20261203 + 2, nbubbles=3, cover=0.12, **kw):
+    """Two-level plane-parallel configuration (refinement ratio 2).
+
+    Both levels are the same seeded atmosphere evaluated at their own resolution; level-0
+    cells under level 1 hold the average of their children (the state a previous step's
+    AverageDown leaves); dt is the CFL step of the finer level.  Returns the level-0 dict
+    (parameters as for planar_config) with "levels": [level-0 arrays, level-1 arrays].
+    """
+    n0 = tuple(int(v) for v in n0)
+    c0 = planar_config(n=n0, nspec=nspec, ppm_type=ppm_type, max_grid=max_grid, boxes=level0_boxes, seed=seed, **kw)
+    n1 = tuple(2 * v for v in n0)
+    if fine_boxes is None:
+        fine_boxes = bubble_boxes(n0, nbubbles=nbubbles, cover=cover, rng=np.random.default_rng(seed + 100))
+    c1 = planar_config(n=n1, nspec=nspec, ppm_type=ppm_type, max_grid=max_grid, boxes=list(fine_boxes),
+                       seed=seed, **kw)
+    for key in ("sold", "uold", "gpi"):
+        _average_down(c1[key], c0[key], fine_boxes)
+    c0["dt"] = min(c0["dt"], c1["dt"])
+    c0["rel_eps"] = max(c0["rel_eps"], c1["rel_eps"])
+    c0["levels"] = [{k: c0[k] for k in LEVEL_KEYS}, {k: c1[k] for k in LEVEL_KEYS}]
+    return c0

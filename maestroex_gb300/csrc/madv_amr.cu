@@ -1,0 +1,399 @@
+// Coarse-fine operations of a two-level hierarchy (refinement ratio 2): the parts of the
+// reference's multi-level stage that couple the levels.
+//
+//   interp_fill         FillPatchTwoLevels with cell_cons_interp (Source/MaestroFillData.cpp:46-73):
+//                       fine ghost cells inside the domain that no fine box covers
+//   average_down        average_down (Source/MaestroFillData.cpp:145-154)
+//   average_down_faces  average_down_faces (Source/MaestroFillData.cpp:156-174)
+//   uedge_interface     the coarse-fine part of Maestro::FillPatchUedge
+//                       (Source/MaestroFillData.cpp:466-825)
+//
+// The AMReX routines are restated from their published algorithms (the reference's AMReX
+// submodule is empty and unpinned):
+//   * coarse values outside the domain are the coarse level's boundary fill of a FAB that
+//     spans the domain (directions swept x, y, z, the last direction applied wins);
+//   * cell_cons_interp: per coarse cell and direction the central slope 0.5 (u+ - u-), or
+//     (u+ + 3 u0 - 4 u-) / 3 and (4 u+ - 3 u0 - u-) / 3 on an ext_dir / hoextrap domain
+//     face, limited against 2 (u+ - u0) and 2 (u0 - u-) (monotonized central); the fine
+//     value is u0 + xoff sx + yoff sy + zoff sz with offsets of -1/4 and +1/4;
+//   * average_down: the sum of the 8 children (k outer, i inner) times 1/8; faces: the sum
+//     of the 4 fine faces (outer = the higher transverse direction) times 1/4.
+// FillPatchUedge on a ghost face: a face on a coarse face takes the fine valid value if a
+// fine box has it (the box owning the cell above it, else below), else the coarse face
+// (owner of the cell above, else below, else of the nearest domain cell, from its ghost
+// faces); a face between coarse faces takes the linear interpolation between its two
+// neighbours in the face direction at the first fine index of its coarse face in the
+// other two directions.  Ghost faces that are valid in another fine box are overwritten by
+// the FillBoundary that follows, as in the reference.
+//
+// Level lookups use an owner map per level (the box owning each cell of the level's
+// domain, int32): 67 MB for a 256^3 level, 537 MB for a 512^3 level.
+#include "madv_launch.cuh"
+
+namespace madv {
+
+struct LevelGeo {
+    int dlo[3], dhi[3], per[3];
+    long nx, ny;
+    const int* owner;
+};
+
+static LevelGeo geo_of(const Ctx& c) {
+    LevelGeo g{};
+    for (int d = 0; d < 3; ++d) {
+        g.dlo[d] = c.P.dom_lo[d];
+        g.dhi[d] = c.P.dom_hi[d];
+        g.per[d] = c.per[d] ? 1 : 0;
+    }
+    g.nx = c.P.dom_hi[0] - c.P.dom_lo[0] + 1;
+    g.ny = c.P.dom_hi[1] - c.P.dom_lo[1] + 1;
+    g.owner = c.d_owner;
+    return g;
+}
+
+int build_owner(Ctx& c) {
+    const long nx = c.P.dom_hi[0] - c.P.dom_lo[0] + 1, ny = c.P.dom_hi[1] - c.P.dom_lo[1] + 1,
+               nz = c.P.dom_hi[2] - c.P.dom_lo[2] + 1;
+    c.h_owner.assign((size_t)(nx * ny * nz), -1);
+    for (int b = 0; b < c.nb; ++b) {
+        const HBox& x = c.ba[b];
+        for (int k = x.lo[2]; k <= x.hi[2]; ++k)
+            for (int j = x.lo[1]; j <= x.hi[1]; ++j)
+                for (int i = x.lo[0]; i <= x.hi[0]; ++i)
+                    c.h_owner[(size_t)((i - c.P.dom_lo[0]) + nx * ((j - c.P.dom_lo[1]) + ny * (long)(k - c.P.dom_lo[2])))] =
+                        b;
+    }
+    if (c.d_owner) cudaFree(c.d_owner);
+    c.d_owner = nullptr;
+    if (!cuda_ok(cudaMalloc(&c.d_owner, sizeof(int) * c.h_owner.size()), "cudaMalloc(owner)") ||
+        !cuda_ok(cudaMemcpy(c.d_owner, c.h_owner.data(), sizeof(int) * c.h_owner.size(), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(owner)"))
+        return MADV_ERR_CUDA;
+    return MADV_OK;
+}
+
+__device__ __forceinline__ int owner_in(const LevelGeo& g, int i, int j, int k) {
+    if (i < g.dlo[0] || i > g.dhi[0] || j < g.dlo[1] || j > g.dhi[1] || k < g.dlo[2] || k > g.dhi[2]) return -1;
+    return g.owner[(i - g.dlo[0]) + g.nx * ((j - g.dlo[1]) + g.ny * (long)(k - g.dlo[2]))];
+}
+
+__device__ __forceinline__ int wrap(const LevelGeo& g, int d, int m) {
+    if (!g.per[d]) return m;
+    const int len = g.dhi[d] - g.dlo[d] + 1;
+    while (m < g.dlo[d]) m += len;
+    while (m > g.dhi[d]) m -= len;
+    return m;
+}
+
+// Coarse value at a (periodically wrapped) index: valid data, or the boundary fill along
+// the highest direction in which the index lies outside the domain (directions below D may
+// still be outside and are resolved recursively).
+template <int D>
+__device__ double cval(const LevelGeo& g, const FabView* __restrict__ Vc, int nbc, int fid, int n, const BCRecD& bc,
+                       bool velish, int p0, int p1, int p2, int* err) {
+    if constexpr (D < 0) {
+        const int b = owner_in(g, p0, p1, p2);
+        if (b < 0) {
+            atomicOr(err, 2);
+            return 0.0;
+        }
+        return at(Vc[fid * nbc + b], p0, p1, p2, n);
+    } else {
+        const int p[3] = {p0, p1, p2};
+        const int m = p[D], dlo = g.dlo[D], dhi = g.dhi[D];
+        if (m >= dlo && m <= dhi) return cval<D - 1>(g, Vc, nbc, fid, n, bc, velish, p0, p1, p2, err);
+        const bool lo = m < dlo;
+        const int t = lo ? bc.lo[D] : bc.hi[D];
+        auto at_m = [&](int q) {
+            int r[3] = {p0, p1, p2};
+            r[D] = q;
+            return cval<D - 1>(g, Vc, nbc, fid, n, bc, velish, r[0], r[1], r[2], err);
+        };
+        switch (t) {
+            case BC_FOEXTRAP: return at_m(lo ? dlo : dhi);
+            case BC_HOEXTRAP:
+                if (lo)
+                    return m < dlo - 1 ? at_m(dlo) : 0.125 * (15. * at_m(dlo) - 10. * at_m(dlo + 1) + 3. * at_m(dlo + 2));
+                return m > dhi + 1 ? at_m(dhi) : 0.125 * (15. * at_m(dhi) - 10. * at_m(dhi - 1) + 3. * at_m(dhi - 2));
+            case BC_REFLECT_EVEN: return at_m(lo ? 2 * dlo - 1 - m : 2 * dhi + 1 - m);
+            case BC_REFLECT_ODD: return -at_m(lo ? 2 * dlo - 1 - m : 2 * dhi + 1 - m);
+            case BC_EXT_DIR:
+                if (!velish) atomicOr(err, 2);
+                return 0.0;
+            default: atomicOr(err, 2); return 0.0;
+        }
+    }
+}
+
+__device__ __forceinline__ double cv(const LevelGeo& g, const FabView* __restrict__ Vc, int nbc, int fid, int n,
+                                     const BCRecD& bc, bool velish, int a, int b, int c, int* err) {
+    return cval<2>(g, Vc, nbc, fid, n, bc, velish, wrap(g, 0, a), wrap(g, 1, b), wrap(g, 2, c), err);
+}
+
+// cell_cons_interp value of fine cell (i, j, k), component n.
+__device__ double cons_interp(const LevelGeo& gc, const FabView* __restrict__ Vc, int nbc, int fid, int n,
+                              const BCRecD& bc, bool velish, int i, int j, int k, int* err) {
+    const int I[3] = {i >> 1, j >> 1, k >> 1};
+    const int f[3] = {i, j, k};
+    const double u0 = cv(gc, Vc, nbc, fid, n, bc, velish, I[0], I[1], I[2], err);
+    double s[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int pp[3] = {I[0], I[1], I[2]}, pm[3] = {I[0], I[1], I[2]};
+        pp[d] += 1;
+        pm[d] -= 1;
+        const double up = cv(gc, Vc, nbc, fid, n, bc, velish, pp[0], pp[1], pp[2], err);
+        const double dn = cv(gc, Vc, nbc, fid, n, bc, velish, pm[0], pm[1], pm[2], err);
+        double dc = 0.5 * (up - dn);
+        if (!gc.per[d]) {
+            if (I[d] == gc.dlo[d] && (bc.lo[d] == BC_EXT_DIR || bc.lo[d] == BC_HOEXTRAP))
+                dc = (up + 3.0 * u0 - 4.0 * dn) / 3.0;
+            if (I[d] == gc.dhi[d] && (bc.hi[d] == BC_EXT_DIR || bc.hi[d] == BC_HOEXTRAP))
+                dc = (4.0 * up - 3.0 * u0 - dn) / 3.0;
+        }
+        const double df = 2.0 * (up - u0);
+        const double db = 2.0 * (u0 - dn);
+        const double sl = (df * db >= 0.0) ? mn(fabs(df), fabs(db)) : 0.0;
+        s[d] = copysign(1.0, dc) * mn(sl, fabs(dc));
+    }
+    double off[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) off[d] = (f[d] - 2 * I[d]) == 0 ? -0.25 : 0.25;
+    return u0 + off[0] * s[0] + off[1] * s[1] + off[2] * s[2];
+}
+
+// ------------------------------------------------------------------ tables
+// Ghost shell of every box of c: its FAB region (valid box, nodal in `nodal`, grown by ng)
+// minus the valid box, as six disjoint slabs per box.
+static const RegionTable& shell_table(Ctx& c, int ng, int nodal) {
+    std::array<int, 4> key{0, ng, nodal, 0};
+    auto it = c.amr_tables.find(key);
+    if (it != c.amr_tables.end()) return it->second;
+    RegionTable& t = c.amr_tables[key];
+    long start = 0;
+    auto push = [&](int b, const int lo[3], const int hi[3]) {
+        RegionBox r{};
+        for (int d = 0; d < 3; ++d) {
+            r.lo[d] = lo[d];
+            r.n[d] = hi[d] - lo[d] + 1;
+            if (r.n[d] <= 0) return;
+        }
+        r.b = b;
+        r.start = start;
+        start += (long)r.n[0] * r.n[1] * r.n[2];
+        t.h.push_back(r);
+    };
+    for (int b = 0; b < c.nb; ++b) {
+        int vlo[3], vhi[3], glo[3], ghi[3];
+        for (int d = 0; d < 3; ++d) {
+            vlo[d] = c.ba[b].lo[d];
+            vhi[d] = c.ba[b].hi[d] + (d == nodal ? 1 : 0);
+            glo[d] = vlo[d] - ng;
+            ghi[d] = vhi[d] + ng;
+        }
+        // z slabs (full x, y), y slabs (full x, valid z), x slabs (valid y, z)
+        for (int side = 0; side < 2; ++side) {
+            int lo[3] = {glo[0], glo[1], side ? vhi[2] + 1 : glo[2]};
+            int hi[3] = {ghi[0], ghi[1], side ? ghi[2] : vlo[2] - 1};
+            push(b, lo, hi);
+        }
+        for (int side = 0; side < 2; ++side) {
+            int lo[3] = {glo[0], side ? vhi[1] + 1 : glo[1], vlo[2]};
+            int hi[3] = {ghi[0], side ? ghi[1] : vlo[1] - 1, vhi[2]};
+            push(b, lo, hi);
+        }
+        for (int side = 0; side < 2; ++side) {
+            int lo[3] = {side ? vhi[0] + 1 : glo[0], vlo[1], vlo[2]};
+            int hi[3] = {side ? ghi[0] : vlo[0] - 1, vhi[1], vhi[2]};
+            push(b, lo, hi);
+        }
+    }
+    t.total = start;
+    if (!t.h.empty()) {
+        if (cudaMalloc(&t.d, sizeof(RegionBox) * t.h.size()) != cudaSuccess ||
+            cudaMemcpy(t.d, t.h.data(), sizeof(RegionBox) * t.h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            throw Fail{MADV_ERR_CUDA};
+    }
+    return t;
+}
+
+// Coarse cells (nodal = -1) or coarse d-faces under each fine box, split by the coarse box
+// holding them (a face on a coarse box boundary appears once per coarse box).  Stored in
+// the fine level; RegionBox.b = coarse box, RegionBox.pad = fine box.
+static const RegionTable& down_table(Ctx& cf, const Ctx& cc, int nodal) {
+    std::array<int, 4> key{1, nodal, 0, 0};
+    auto it = cf.amr_tables.find(key);
+    if (it != cf.amr_tables.end()) return it->second;
+    RegionTable& t = cf.amr_tables[key];
+    long start = 0;
+    for (int fb = 0; fb < cf.nb; ++fb) {
+        int clo[3], chi[3];
+        for (int d = 0; d < 3; ++d) {
+            clo[d] = cf.ba[fb].lo[d] >> 1;
+            chi[d] = (cf.ba[fb].hi[d] >> 1) + (d == nodal ? 1 : 0);
+        }
+        for (int cb = 0; cb < cc.nb; ++cb) {
+            RegionBox r{};
+            bool empty = false;
+            for (int d = 0; d < 3; ++d) {
+                const int lo = std::max(clo[d], cc.ba[cb].lo[d]);
+                const int hi = std::min(chi[d], cc.ba[cb].hi[d] + (d == nodal ? 1 : 0));
+                if (lo > hi) empty = true;
+                r.lo[d] = lo;
+                r.n[d] = hi - lo + 1;
+            }
+            if (empty) continue;
+            r.b = cb;
+            r.pad = fb;
+            r.start = start;
+            start += (long)r.n[0] * r.n[1] * r.n[2];
+            t.h.push_back(r);
+        }
+    }
+    t.total = start;
+    if (!t.h.empty()) {
+        if (cudaMalloc(&t.d, sizeof(RegionBox) * t.h.size()) != cudaSuccess ||
+            cudaMemcpy(t.d, t.h.data(), sizeof(RegionBox) * t.h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            throw Fail{MADV_ERR_CUDA};
+    }
+    return t;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_interp_fill(KARGS, const FabView* __restrict__ Vc, int nbc, LevelGeo gc, LevelGeo gf, int fid,
+                              int c0, int nc, const BCRecD* __restrict__ bcs, int bc_c0, int is_vel, int state_c0,
+                              int* err) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const int p[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        if (!gf.per[d] && (p[d] < gf.dlo[d] || p[d] > gf.dhi[d])) return;
+    if (owner_in(gf, wrap(gf, 0, i), wrap(gf, 1, j), wrap(gf, 2, k)) >= 0) return;
+    const FabView f = VW(fid);
+    for (int n = c0; n < c0 + nc; ++n) {
+        const BCRecD bc = bcs[bc_c0 + n - c0];
+        const bool velish = is_vel || (state_c0 >= 0 && state_c0 + (n - c0) == PI);
+        at(f, i, j, k, n) = cons_interp(gc, Vc, nbc, fid, n, bc, velish, i, j, k, err);
+    }
+}
+
+void interp_fill(Ctx& cc, Ctx& cf, int fid, int c0, int nc, int which_bcs, int bc_c0, int is_vel, int state_c0) {
+    const RegionTable& rt = shell_table(cf, cf.F[fid].spec.ng, -1);
+    launch(cf, rt, 1, k_interp_fill, cf.V(), cc.V(), cc.nb, geo_of(cc), geo_of(cf), fid, c0, nc,
+           bcs_dev(cf, which_bcs), bc_c0, is_vel, state_c0, cf.d_flag);
+}
+
+__global__ void k_avgdown(KARGS, const FabView* __restrict__ Vf, int nbf, int fid, int comp, int ncomp) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView f = Vf[fid * nbf + R[e_].pad], c = VW(fid);
+    for (int n = comp; n < comp + ncomp; ++n) {
+        double s = 0.0;
+        for (int kr = 0; kr < 2; ++kr)
+            for (int jr = 0; jr < 2; ++jr)
+                for (int ir = 0; ir < 2; ++ir) s += at(f, 2 * i + ir, 2 * j + jr, 2 * k + kr, n);
+        at(c, i, j, k, n) = 0.125 * s;
+    }
+}
+
+void average_down(Ctx& cf, Ctx& cc, int fid, int comp, int ncomp) {
+    const RegionTable& rt = down_table(cf, cc, -1);
+    launch(cc, rt, 1, k_avgdown, cc.V(), cf.V(), cf.nb, fid, comp, ncomp);
+}
+
+template <int D>
+__global__ void k_avgdown_faces(KARGS, const FabView* __restrict__ Vf, int nbf, int fid, int c0, int ncomp) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int t1 = D == 0 ? 1 : 0, t2 = D == 2 ? 1 : 2;
+    const FabView f = Vf[fid * nbf + R[e_].pad], c = VW(fid);
+    for (int n = c0; n < c0 + ncomp; ++n) {
+        double s = 0.0;
+        for (int o = 0; o < 2; ++o)
+            for (int in = 0; in < 2; ++in) {
+                int q[3] = {2 * i, 2 * j, 2 * k};
+                q[t1] += in;
+                q[t2] += o;
+                s += at(f, q[0], q[1], q[2], n);
+            }
+        at(c, i, j, k, n) = s * 0.25;
+    }
+}
+
+void average_down_faces(Ctx& cf, Ctx& cc, int f0, int c0, int ncomp) {
+    for (int d = 0; d < 3; ++d) {
+        const RegionTable& rt = down_table(cf, cc, d);
+        if (d == 0) launch(cc, rt, 1, k_avgdown_faces<0>, cc.V(), cf.V(), cf.nb, f0, c0, ncomp);
+        else if (d == 1) launch(cc, rt, 1, k_avgdown_faces<1>, cc.V(), cf.V(), cf.nb, f0 + 1, c0, ncomp);
+        else launch(cc, rt, 1, k_avgdown_faces<2>, cc.V(), cf.V(), cf.nb, f0 + 2, c0, ncomp);
+    }
+}
+
+template <int D>
+__device__ double uedge_even(const FabView* __restrict__ V, int nb, const FabView* __restrict__ Vc, int nbc,
+                             const LevelGeo& gc, const LevelGeo& gf, int fid, int i, int j, int k, int* err) {
+    int q[3] = {i, j, k};
+    int b = owner_in(gf, i, j, k);
+    if (b < 0) {
+        q[D] -= 1;
+        b = owner_in(gf, q[0], q[1], q[2]);
+    }
+    if (b >= 0) return at(VW(fid), i, j, k);
+    const int P[3] = {i >> 1, j >> 1, k >> 1};
+    int c[3] = {P[0], P[1], P[2]};
+    int cb = owner_in(gc, c[0], c[1], c[2]);
+    if (cb < 0) {
+        c[D] -= 1;
+        cb = owner_in(gc, c[0], c[1], c[2]);
+    }
+    if (cb < 0) {
+#pragma unroll
+        for (int e = 0; e < 3; ++e) c[e] = min(max(P[e], gc.dlo[e]), gc.dhi[e]);
+        cb = owner_in(gc, c[0], c[1], c[2]);
+    }
+    if (cb < 0) {
+        atomicOr(err, 4);
+        return 0.0;
+    }
+    const FabView v = Vc[fid * nbc + cb];
+    const long nx = v.sj, ny = v.sk / v.sj, nz = v.sn / v.sk;
+    if (P[0] < v.lo0 || P[0] >= v.lo0 + nx || P[1] < v.lo1 || P[1] >= v.lo1 + ny || P[2] < v.lo2 ||
+        P[2] >= v.lo2 + nz) {
+        atomicOr(err, 4);
+        return 0.0;
+    }
+    return at(v, P[0], P[1], P[2]);
+}
+
+template <int D>
+__global__ void k_uedge_iface(KARGS, const FabView* __restrict__ Vc, int nbc, LevelGeo gc, LevelGeo gf, int fid,
+                              int* err) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    int q[3] = {i, j, k};
+    double v;
+    if ((q[D] & 1) == 0) {
+        v = uedge_even<D>(V, nb, Vc, nbc, gc, gf, fid, i, j, k, err);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+            if (e != D) q[e] -= (q[e] & 1);
+        int a[3] = {q[0], q[1], q[2]}, c[3] = {q[0], q[1], q[2]};
+        a[D] -= 1;
+        c[D] += 1;
+        const double fa = uedge_even<D>(V, nb, Vc, nbc, gc, gf, fid, a[0], a[1], a[2], err);
+        const double fc = uedge_even<D>(V, nb, Vc, nbc, gc, gf, fid, c[0], c[1], c[2], err);
+        const double df = fc - fa;
+        v = fa + df * 1.0 / 2.0;
+    }
+    at(VW(fid), i, j, k) = v;
+}
+
+void uedge_interface(Ctx& cc, Ctx& cf, int f0) {
+    const LevelGeo gc = geo_of(cc), gf = geo_of(cf);
+    for (int d = 0; d < 3; ++d) {
+        const RegionTable& rt = shell_table(cf, 1, d);
+        if (d == 0) launch(cf, rt, 1, k_uedge_iface<0>, cf.V(), cc.V(), cc.nb, gc, gf, f0, cf.d_flag);
+        else if (d == 1) launch(cf, rt, 1, k_uedge_iface<1>, cf.V(), cc.V(), cc.nb, gc, gf, f0 + 1, cf.d_flag);
+        else launch(cf, rt, 1, k_uedge_iface<2>, cf.V(), cc.V(), cc.nb, gc, gf, f0 + 2, cf.d_flag);
+    }
+}
+
+}  // namespace madv

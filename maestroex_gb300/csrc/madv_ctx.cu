@@ -1,6 +1,7 @@
 // Context, layout, base state and the C ABI of the scalar-advection stage library.
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 
 #include "madv_ctx.hpp"
@@ -20,9 +21,6 @@ bool cuda_ok(cudaError_t e, const char* what) {
         if (!cuda_ok((x), #x)) return MADV_ERR_CUDA; \
     } while (0)
 
-struct Fail {
-    int code;
-};
 
 // ------------------------------------------------------------------ region tables
 static HBox valid_box(const Ctx& c, int b, int nodal) {
@@ -82,8 +80,36 @@ const RegionTable& region(Ctx& c, int glo0, int glo1, int glo2, int ghi0, int gh
     return t;
 }
 
+// a minus b as up to six disjoint boxes appended to out
+static void box_minus(const HBox& a, const HBox& b, std::vector<HBox>& out) {
+    for (int d = 0; d < 3; ++d)
+        if (b.hi[d] < a.lo[d] || b.lo[d] > a.hi[d]) {
+            out.push_back(a);
+            return;
+        }
+    HBox rem = a;
+    for (int d = 0; d < 3; ++d) {
+        if (rem.lo[d] < b.lo[d]) {
+            HBox p = rem;
+            p.hi[d] = b.lo[d] - 1;
+            out.push_back(p);
+            rem.lo[d] = b.lo[d];
+        }
+        if (rem.hi[d] > b.hi[d]) {
+            HBox p = rem;
+            p.lo[d] = b.hi[d] + 1;
+            out.push_back(p);
+            rem.hi[d] = b.hi[d];
+        }
+    }
+}
+
 // FillBoundary copy list: every piece of a box's ghost region that lies in another box's
-// valid region (after the periodic shift), minus the box's own valid region.
+// valid region (after the periodic shift), minus the box's own valid region.  Face data
+// can have one ghost face covered by two sources (a face shared by two boxes, or the two
+// periodic images of a face); the sources are ordered by (source box, z, y, x shift) and
+// the last one wins, as a sequential FillBoundary over that order leaves it.  Destination
+// pieces are made disjoint, so the batched copy has no write conflicts.
 const CopyTable& copy_table(Ctx& c, int ng, int nodal) {
     std::array<int, 3> key{ng, nodal, 0};
     auto it = c.copies.find(key);
@@ -99,6 +125,12 @@ const CopyTable& copy_table(Ctx& c, int ng, int nodal) {
             gb.lo[d] -= ng;
             gb.hi[d] += ng;
         }
+        struct Cand {
+            int src;
+            int shift[3];
+            HBox r;
+        };
+        std::vector<Cand> cands;
         for (int cbx = 0; cbx < c.nb; ++cbx) {
             HBox sv = valid_box(c, cbx, nodal);
             for (int sz = -1; sz <= 1; ++sz)
@@ -117,37 +149,36 @@ const CopyTable& copy_table(Ctx& c, int ng, int nodal) {
                             if (r.lo[d] > r.hi[d]) empty = true;
                         }
                         if (empty) continue;
-                        // subtract the destination's valid box: up to six disjoint pieces
-                        HBox rem = r;
-                        auto emit = [&](const HBox& p) {
-                            CopyDesc cd{};
-                            cd.dst_b = b;
-                            cd.src_b = cbx;
-                            for (int d = 0; d < 3; ++d) {
-                                cd.lo[d] = p.lo[d];
-                                cd.n[d] = p.hi[d] - p.lo[d] + 1;
-                                cd.shift[d] = s[d] * len[d];
-                            }
-                            cd.start = start;
-                            start += (long)cd.n[0] * cd.n[1] * cd.n[2];
-                            t.h.push_back(cd);
-                        };
-                        for (int d = 0; d < 3; ++d) {
-                            if (rem.lo[d] < vb.lo[d]) {
-                                HBox p = rem;
-                                p.hi[d] = std::min(rem.hi[d], vb.lo[d] - 1);
-                                emit(p);
-                                rem.lo[d] = vb.lo[d];
-                            }
-                            if (rem.hi[d] > vb.hi[d]) {
-                                HBox p = rem;
-                                p.lo[d] = std::max(rem.lo[d], vb.hi[d] + 1);
-                                emit(p);
-                                rem.hi[d] = vb.hi[d];
-                            }
-                            if (rem.lo[d] > rem.hi[d]) break;
-                        }
+                        // without the destination's valid box
+                        std::vector<HBox> parts;
+                        box_minus(r, vb, parts);
+                        for (auto& p : parts) cands.push_back({cbx, {s[0] * len[0], s[1] * len[1], s[2] * len[2]}, p});
                     }
+        }
+        // last candidate wins: walk backwards, keep what no later candidate claimed
+        std::vector<HBox> claimed;
+        for (int q = (int)cands.size() - 1; q >= 0; --q) {
+            std::vector<HBox> pieces{cands[q].r};
+            for (const HBox& cl : claimed) {
+                std::vector<HBox> next;
+                for (const HBox& p : pieces) box_minus(p, cl, next);
+                pieces.swap(next);
+                if (pieces.empty()) break;
+            }
+            for (const HBox& p : pieces) {
+                CopyDesc cd{};
+                cd.dst_b = b;
+                cd.src_b = cands[q].src;
+                for (int d = 0; d < 3; ++d) {
+                    cd.lo[d] = p.lo[d];
+                    cd.n[d] = p.hi[d] - p.lo[d] + 1;
+                    cd.shift[d] = cands[q].shift[d];
+                }
+                cd.start = start;
+                start += (long)cd.n[0] * cd.n[1] * cd.n[2];
+                t.h.push_back(cd);
+            }
+            claimed.push_back(cands[q].r);
         }
     }
     t.total = start;
@@ -255,26 +286,31 @@ static void free_layout(Ctx& c) {
     if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
     c.graph_exec = nullptr;
     c.graph_key.clear();
+    for (auto& kv : c.amr_tables)
+        if (kv.second.d) cudaFree(kv.second.d);
+    c.amr_tables.clear();
+    if (c.d_owner) cudaFree(c.d_owner);
+    c.d_owner = nullptr;
+    c.h_owner.clear();
 }
 
-static std::vector<double> cell_to_edge(const std::vector<double>& cc) {
-    // Maestro::CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), one level, one chunk
+// Maestro::CelltoEdge (Source/MaestroCelltoEdge.cpp:17-54) on the edges [lo, hi] of one
+// chunk of a level with nr cells.
+static void cell_to_edge_chunk(const std::vector<double>& cc, std::vector<double>& e, int lo, int hi) {
     const int nr = (int)cc.size();
-    std::vector<double> e(nr + 1);
-    for (int r = 0; r <= nr; ++r) {
+    for (int r = lo; r <= hi; ++r) {
         if (r == 0) e[r] = cc[r];
-        else if (r == 1) e[r] = 0.5 * (cc[r - 1] + cc[r]);
+        else if (r == 1 || r == lo) e[r] = 0.5 * (cc[r - 1] + cc[r]);
         else if (r == nr) e[r] = cc[r - 1];
-        else if (r == nr - 1) e[r] = 0.5 * (cc[r] + cc[r - 1]);
+        else if (r == nr - 1 || r == hi) e[r] = 0.5 * (cc[r] + cc[r - 1]);
         else {
             double tmp = 7.0 / 12.0 * (cc[r] + cc[r - 1]) - 1.0 / 12.0 * (cc[r + 1] + cc[r - 2]);
-            double lo = (cc[r - 1] < cc[r]) ? cc[r - 1] : cc[r];  // min(cc[r], cc[r-1])
-            double hi = (cc[r] < cc[r - 1]) ? cc[r - 1] : cc[r];  // max(cc[r], cc[r-1])
-            double t = (tmp < lo) ? lo : tmp;
-            e[r] = (hi < t) ? hi : t;
+            double lo_ = (cc[r - 1] < cc[r]) ? cc[r - 1] : cc[r];  // min(cc[r], cc[r-1])
+            double hi_ = (cc[r] < cc[r - 1]) ? cc[r - 1] : cc[r];  // max(cc[r], cc[r-1])
+            double t = (tmp < lo_) ? lo_ : tmp;
+            e[r] = (hi_ < t) ? hi_ : t;
         }
     }
-    return e;
 }
 
 // ------------------------------------------------------------------ user FAB binding
@@ -325,87 +361,199 @@ enum {
     U_SFLUX0, U_SFLUX1, U_SFLUX2, U_ETA, U_UTRANS0, U_UTRANS1, U_UTRANS2
 };
 
-// ------------------------------------------------------------------ stage pieces
-static void w0_carts(Ctx& c) {
-    // Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1)  (Source/MaestroAdvance.cpp:326)
-    set_val(c, F_W0CART, 0.0, 0, 3, 2);
-    put1d(c, F_W0CART, c.b1("w0"), 2, 1);
-    fill_patch(c, F_W0CART, 0, 3, BCS_U, 0, 1, -1);
-    // Put1dArrayOnCart(w0_force, w0_force_cart, false, true, bcs_f, 0) (:341), evolve_base_state only
-    set_val(c, F_W0FCART, 0.0, 0, 3, 1);
-    if (c.P.evolve_base_state) {
-        put1d(c, F_W0FCART, c.b1("w0_force"), 2, 0);
-        fill_patch(c, F_W0FCART, 0, 3, BCS_F, 0, 0, -1);
+// ------------------------------------------------------------------ level coupling
+// Maestro::FillPatch over all levels (Source/MaestroFillData.cpp:7-74): level 0 is filled
+// from itself; level l > 0 interpolates its uncovered ghost cells from level l-1 first.
+static void fill_patch_h(Hier& H, int fid, int c0, int nc, int which_bcs, int bc_c0, int is_vel, int state_c0) {
+    for (int l = 0; l < H.n(); ++l) {
+        if (l > 0) interp_fill(H[l - 1], H[l], fid, c0, nc, which_bcs, bc_c0, is_vel, state_c0);
+        fill_patch(H[l], fid, c0, nc, which_bcs, bc_c0, is_vel, state_c0);
     }
+}
+// Maestro::AverageDown (Source/MaestroFillData.cpp:145-154)
+static void average_down_h(Hier& H, int fid, int comp, int ncomp) {
+    for (int l = H.n() - 2; l >= 0; --l) average_down(H[l + 1], H[l], fid, comp, ncomp);
+}
+// Maestro::AverageDownFaces (Source/MaestroFillData.cpp:156-174)
+static void average_down_faces_h(Hier& H, int f0, int c0, int ncomp) {
+    for (int l = H.n() - 2; l >= 0; --l) average_down_faces(H[l + 1], H[l], f0, c0, ncomp);
+}
+// The face-velocity ghost fill closing MakeUtrans and Addw0 (Source/MaestroMakeUtrans.cpp:631-647,
+// Source/MaestroFill3dData.cpp:425-461): one level: FillBoundary + FillUmacGhost;
+// several: AverageDownFaces, then FillPatchUedge (Source/MaestroFillData.cpp:455-835).
+static void sync_faces_h(Hier& H, int f0) {
+    if (H.n() == 1) {
+        fill_face_ghosts(H[0], f0);
+        return;
+    }
+    average_down_faces_h(H, f0, 0, 1);
+    for (int l = 0; l < H.n(); ++l) {
+        if (l > 0) uedge_interface(H[l - 1], H[l], f0);
+        fill_face_ghosts(H[l], f0);
+    }
+}
+// Maestro::Put1dArrayOnCart, planar (Source/MaestroFill3dData.cpp:9-36)
+static void put1d_h(Hier& H, int fid, const char* s0, int outcomp, int nc, int edge, int which_bcs, int bc_c0,
+                    int is_vel, int state_c0) {
+    for (auto* c : H.L) {
+        set_val(*c, fid, 0.0, 0, nc, c->F[fid].spec.ng);
+        put1d(*c, fid, c->b1(s0), outcomp, edge);
+    }
+    average_down_h(H, fid, 0, nc);
+    fill_patch_h(H, fid, 0, nc, which_bcs, bc_c0, is_vel, state_c0);
+}
+// Maestro::Addw0 (Source/MaestroFill3dData.cpp:357-462)
+static void addw0_h(Hier& H, int f0, double mult) {
+    for (auto* c : H.L) addw0(*c, f0, mult);
+    sync_faces_h(H, f0);
+}
+
+// ------------------------------------------------------------------ stage pieces
+static void w0_carts(Hier& H) {
+    // Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1)  (Source/MaestroAdvance.cpp:326)
+    put1d_h(H, F_W0CART, "w0", 2, 3, 1, BCS_U, 0, 1, -1);
+    // Put1dArrayOnCart(w0_force, w0_force_cart, false, true, bcs_f, 0) (:341), evolve_base_state only
+    for (auto* c : H.L) set_val(*c, F_W0FCART, 0.0, 0, 3, 1);
+    if (H[0].P.evolve_base_state) put1d_h(H, F_W0FCART, "w0_force", 2, 3, 0, BCS_F, 0, 0, -1);
+}
+
+// Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-259)
+static void make_vel_force_h(Hier& H) {
+    put1d_h(H, F_GRAVCART, "grav_cell", 2, 3, 0, BCS_F, 0, 0, -1);
+    put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
+    for (auto* c : H.L) make_vel_force(*c);
+    average_down_h(H, F_VELFORCE, 0, 3);
+    fill_patch_h(H, F_VELFORCE, 0, 3, BCS_U, 0, 1, -1);
 }
 
 // Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84) on the internal fields.
-static void advance_premac(Ctx& c) {
-    fill_patch(c, F_UTILDE, 0, 3, BCS_U, 0, 1, -1);
-    set_val(c, F_UFULL, 0.0, 0, 3, c.ng_adv);
-    copy_fab(c, F_UFULL, 0, F_W0CART, 0, 3, 0);
-    fill_patch(c, F_UFULL, 0, 3, BCS_U, 0, 1, -1);
-    add_fab(c, F_UFULL, F_UTILDE, 3, c.ng_adv);
-    for (int d = 0; d < 3; ++d) set_val(c, F_UTRANS0 + d, 0.0, 0, 1, 1);
-    make_utrans(c);
-    make_vel_force(c);
-    addw0(c, F_UTRANS0, 1.0);
-    vel_pred(c);
+static void advance_premac(Hier& H) {
+    const int nga = H[0].ng_adv;
+    fill_patch_h(H, F_UTILDE, 0, 3, BCS_U, 0, 1, -1);
+    for (auto* c : H.L) {
+        set_val(*c, F_UFULL, 0.0, 0, 3, nga);
+        copy_fab(*c, F_UFULL, 0, F_W0CART, 0, 3, 0);
+    }
+    fill_patch_h(H, F_UFULL, 0, 3, BCS_U, 0, 1, -1);
+    for (auto* c : H.L) {
+        add_fab(*c, F_UFULL, F_UTILDE, 3, nga);
+        for (int d = 0; d < 3; ++d) set_val(*c, F_UTRANS0 + d, 0.0, 0, 1, 1);
+    }
+    for (auto* c : H.L) make_utrans(*c);
+    sync_faces_h(H, F_UTRANS0);
+    make_vel_force_h(H);
+    addw0_h(H, F_UTRANS0, 1.0);
+    for (auto* c : H.L) vel_pred(*c);
+    average_down_faces_h(H, F_UMAC0, 0, 1);
+}
+
+// Maestro::ModifyScalForce (Source/MaestroForce.cpp:261-467)
+static void modify_scal_force_h(Hier& H, int comp, const char* s0_edge, int s0cart_fid, int fullform) {
+    put1d_h(H, F_S0ECART, s0_edge, 0, 1, 0, BCS_F, 0, 0, -1);
+    for (auto* c : H.L) modify_scal_force(*c, comp, s0cart_fid, fullform);
+    average_down_h(H, F_SCALFORCE, comp, 1);
+    fill_patch_h(H, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
+}
+
+// Maestro::MakeRhoHForce, which_step 1 (Source/MaestroForce.cpp:469-679)
+static void make_rhoh_force_h(Hier& H, int is_prediction, int add_thermal) {
+    put1d_h(H, F_P0CART, "p0_old", 0, 1, 0, BCS_F, 0, 0, -1);
+    put1d_h(H, F_PSICART, "psi", 0, 1, 0, BCS_F, 0, 0, -1);
+    put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
+    put1d_h(H, F_GRAVCART, "grav_cell", 2, 3, 0, BCS_F, 0, 0, -1);
+    for (auto* c : H.L) make_rhoh_force(*c, is_prediction, add_thermal);
+    average_down_h(H, F_SCALFORCE, RHOH, 1);
+    fill_patch_h(H, F_SCALFORCE, RHOH, 1, BCS_F, 0, 0, RHOH);
+}
+
+// Maestro::PutInPertForm (Source/MaestroConvert.cpp:6-34)
+static void put_in_pert_form_h(Hier& H, const char* s0, int comp, int bccomp, int which_bcs, int flag) {
+    for (auto* c : H.L) put_in_pert_form(*c, c->b1(s0), comp, flag);
+    average_down_h(H, F_SOLD, comp, 1);
+    fill_patch_h(H, F_SOLD, comp, 1, which_bcs, bccomp, 0, comp);
+}
+
+// Maestro::ConvertRhoXToX (Source/MaestroConvert.cpp:64-91)
+static void convert_rhox_to_x_h(Hier& H, int flag) {
+    const int ns = H[0].nspec;
+    for (auto* c : H.L) convert_rhox_to_x(*c, flag);
+    average_down_h(H, F_SOLD, FIRSTSPEC, ns);
+    if (flag) fill_patch_h(H, F_SOLD, FIRSTSPEC, ns, BCS_F, 0, 0, FIRSTSPEC);
+    else fill_patch_h(H, F_SOLD, FIRSTSPEC, ns, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
+}
+
+// Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
+static void update_scal_h(Hier& H, int start_comp) {
+    for (auto* c : H.L) update_scal(*c, start_comp);
+    if (start_comp == RHOH) {
+        average_down_h(H, F_SNEW, RHOH, 1);
+        fill_patch_h(H, F_SNEW, RHOH, 1, BCS_S, RHOH, 0, RHOH);
+    } else {
+        const int ns = H[0].nspec;
+        average_down_h(H, F_SNEW, FIRSTSPEC, ns);
+        fill_patch_h(H, F_SNEW, FIRSTSPEC, ns, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
+        average_down_h(H, F_SNEW, RHO, 1);
+        fill_patch_h(H, F_SNEW, RHO, 1, BCS_S, RHO, 0, RHO);
+    }
 }
 
 // Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243)
-static void density_advance(Ctx& c) {
-    const int spt = c.P.species_pred_type;
-    set_val(c, F_SCALFORCE, 0.0, 0, c.nscal, 1);
-    set_val(c, F_RHO0CART, 0.0, 0, 1, 1);
-    put1d(c, F_RHO0CART, c.b1("rho0_old"), 0, 0);
-    fill_patch(c, F_RHO0CART, 0, 1, BCS_S, RHO, 0, RHO);
-    addw0(c, F_UMAC0, -1.0);
-    if (spt == 1) modify_scal_force(c, RHO, c.b1("rho0_edge_old"), F_RHO0CART, 0);
-    else if (spt == 3) modify_scal_force(c, RHO, c.b1("rho0_edge_old"), F_RHO0CART, 1);
-    addw0(c, F_UMAC0, 1.0);
-    if (spt == 1 || spt == 3) convert_rhox_to_x(c, 1);
-    if (spt == 1) put_in_pert_form(c, c.b1("rho0_old"), RHO, 0, BCS_F, 1);
-    make_edge_scal(c, FIRSTSPEC, c.nspec, BCS_S, spt == 2, 1);  // no force for X / rho X
-    if (spt == 1 || spt == 3) make_edge_scal(c, RHO, 1, BCS_S, 0, 0);
-    else sum_species_edges(c);
-    if (spt == 1) put_in_pert_form(c, c.b1("rho0_old"), RHO, RHO, BCS_S, 0);
-    if (spt == 1 || spt == 3) convert_rhox_to_x(c, 0);
-    make_rhox_flux(c, c.b1("rho0_old"), c.b1("rho0_edge_old"), c.b1("rho0_old"), c.b1("rho0_edge_old"));
-    set_val(c, F_SCALFORCE, 0.0, 0, c.nscal, 1);
-    update_scal(c, FIRSTSPEC);
+static void density_advance(Hier& H) {
+    const int spt = H[0].P.species_pred_type;
+    const int ns = H[0].nspec, nscal = H[0].nscal;
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
+    put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
+    addw0_h(H, F_UMAC0, -1.0);
+    if (spt == 1) modify_scal_force_h(H, RHO, "rho0_edge_old", F_RHO0CART, 0);
+    else if (spt == 3) modify_scal_force_h(H, RHO, "rho0_edge_old", F_RHO0CART, 1);
+    addw0_h(H, F_UMAC0, 1.0);
+    if (spt == 1 || spt == 3) convert_rhox_to_x_h(H, 1);
+    if (spt == 1) put_in_pert_form_h(H, "rho0_old", RHO, 0, BCS_F, 1);
+    for (auto* c : H.L) make_edge_scal(*c, FIRSTSPEC, ns, BCS_S, spt == 2, 1);  // no force for X / rho X
+    if (spt == 1 || spt == 3)
+        for (auto* c : H.L) make_edge_scal(*c, RHO, 1, BCS_S, 0, 0);
+    else
+        for (auto* c : H.L) sum_species_edges(*c);
+    if (spt == 1) put_in_pert_form_h(H, "rho0_old", RHO, RHO, BCS_S, 0);
+    if (spt == 1 || spt == 3) convert_rhox_to_x_h(H, 0);
+    for (auto* c : H.L)
+        make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1("rho0_old"), c->b1("rho0_edge_old"));
+    average_down_faces_h(H, F_SFLUX0, 0, nscal);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
+    update_scal_h(H, FIRSTSPEC);
 }
 
 // Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352)
-static void enthalpy_advance(Ctx& c) {
-    const int ept = c.P.enthalpy_pred_type;
-    set_val(c, F_SCALFORCE, 0.0, 0, c.nscal, 1);
-    addw0(c, F_UMAC0, -1.0);
-    make_rhoh_force(c, 1, 1, 1);
+static void enthalpy_advance(Hier& H) {
+    const int ept = H[0].P.enthalpy_pred_type;
+    const int nscal = H[0].nscal;
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
+    addw0_h(H, F_UMAC0, -1.0);
+    make_rhoh_force_h(H, 1, 1);
     if (ept == 1) {
-        set_val(c, F_RHOH0CART, 0.0, 0, 1, 1);
-        put1d(c, F_RHOH0CART, c.b1("rhoh0_old"), 0, 0);
-        fill_patch(c, F_RHOH0CART, 0, 1, BCS_S, RHOH, 0, RHOH);
-        modify_scal_force(c, RHOH, c.b1("rhoh0_edge_old"), F_RHOH0CART, 0);
+        put1d_h(H, F_RHOH0CART, "rhoh0_old", 0, 1, 0, BCS_S, RHOH, 0, RHOH);
+        modify_scal_force_h(H, RHOH, "rhoh0_edge_old", F_RHOH0CART, 0);
     }
-    addw0(c, F_UMAC0, 1.0);
-    if (ept == 1) put_in_pert_form(c, c.b1("rhoh0_old"), RHOH, 0, BCS_F, 1);
-    make_edge_scal(c, RHOH, 1, BCS_S, ept == 0, 0);
-    if (ept == 1) put_in_pert_form(c, c.b1("rhoh0_old"), RHOH, RHOH, BCS_S, 0);
-    make_rhoh_flux(c, c.b1("rhoh0_old"), c.b1("rhoh0_edge_old"), c.b1("rhoh0_old"), c.b1("rhoh0_edge_old"));
-    set_val(c, F_SCALFORCE, 0.0, RHOH, 1, 1);
-    addw0(c, F_UMAC0, -1.0);
-    make_rhoh_force(c, 0, 0, 1);
-    addw0(c, F_UMAC0, 1.0);
-    update_scal(c, RHOH);
+    addw0_h(H, F_UMAC0, 1.0);
+    if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
+    for (auto* c : H.L) make_edge_scal(*c, RHOH, 1, BCS_S, ept == 0, 0);
+    if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, RHOH, BCS_S, 0);
+    for (auto* c : H.L)
+        make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"));
+    average_down_faces_h(H, F_SFLUX0, 0, nscal);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
+    addw0_h(H, F_UMAC0, -1.0);
+    make_rhoh_force_h(H, 0, 0);
+    addw0_h(H, F_UMAC0, 1.0);
+    update_scal_h(H, RHOH);
 }
 
-static int check_ready_c(Ctx* c) {
-    if (!c) return MADV_ERR_PARAM;
-    if (!c->have_layout || !c->have_base) {
-        set_error("madv_set_layout and madv_set_base_state must be called first");
-        return MADV_ERR_STATE;
-    }
+static int check_ready_h(const Hier& H) {
+    for (auto* c : H.L)
+        if (!c->have_layout || !c->have_base) {
+            set_error("the layout and the base state must be set first");
+            return MADV_ERR_STATE;
+        }
     return MADV_OK;
 }
 
@@ -415,7 +563,6 @@ struct StageIO {
 
 static int bind_stage(Ctx& c, const StageIO& io) {
     int rc;
-    const int ngs = c.ng_s;
     if ((rc = bind(c, U_UOLD, io.uold, 3, -1, 0))) return rc;
     if ((rc = bind(c, U_SOLD, io.sold, c.nscal, -1, 0))) return rc;
     if ((rc = bind(c, U_GPI, io.gpi, 3, -1, 0))) return rc;
@@ -427,61 +574,92 @@ static int bind_stage(Ctx& c, const StageIO& io) {
         if (io.sflux && (rc = bind(c, U_SFLUX0 + d, &io.sflux[d], c.nscal, d, 0))) return rc;
     }
     if ((rc = bind(c, U_ETA, io.eta, 1, 2, 0))) return rc;
-    (void)ngs;
     return upload_user_views(c);
 }
 
-// The whole stage on the internal fields, inputs already bound to user slots.
-static void stage_body(Ctx& c, const StageIO& io) {
-    if (!c.dry) cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream);
-    // inputs
-    set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
-    copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, 0);
-    copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
-    fill_patch(c, F_SOLD, 0, c.nscal, BCS_S, 0, 0, 0);
-    copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, 3, 0);
-    set_val(c, F_THERMAL, 0.0, 0, 1, 1);
-    if (io.thermal) copy_fab(c, F_THERMAL, 0, F_USER + U_THERMAL, 0, 1, 0);
-    set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
-    for (int d = 0; d < 3; ++d) {
-        set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
-        set_val(c, F_SEDGE0 + d, 0.0, 0, c.nscal, 0);
-        set_val(c, F_SFLUX0 + d, 0.0, 0, c.nscal, 0);
+// The whole stage on the internal fields of every level, inputs already bound to the user
+// slots (io[l] for level l).
+static void stage_body(Hier& H, const std::vector<StageIO>& io) {
+    for (int l = 0; l < H.n(); ++l) {
+        Ctx& c = H[l];
+        if (!c.dry) cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream);
+        set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
+        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, 0);
+        copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
     }
-    set_val(c, F_ETA, 0.0, 0, 1, 0);
-    w0_carts(c);
+    fill_patch_h(H, F_SOLD, 0, H[0].nscal, BCS_S, 0, 0, 0);
+    for (int l = 0; l < H.n(); ++l) {
+        Ctx& c = H[l];
+        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, 3, 0);
+        set_val(c, F_THERMAL, 0.0, 0, 1, 1);
+        if (io[l].thermal) copy_fab(c, F_THERMAL, 0, F_USER + U_THERMAL, 0, 1, 0);
+        set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
+        for (int d = 0; d < 3; ++d) {
+            set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
+            set_val(c, F_SEDGE0 + d, 0.0, 0, c.nscal, 0);
+            set_val(c, F_SFLUX0 + d, 0.0, 0, c.nscal, 0);
+        }
+        set_val(c, F_ETA, 0.0, 0, 1, 0);
+    }
+    w0_carts(H);
     // STEP 3 and STEP 4 of Maestro::AdvanceTimeStep (Source/MaestroAdvance.cpp:359-548)
-    advance_premac(c);
-    addw0(c, F_UMAC0, 1.0);
-    density_advance(c);
-    addw0(c, F_UMAC0, -1.0);
-    addw0(c, F_UMAC0, 1.0);
-    enthalpy_advance(c);
-    addw0(c, F_UMAC0, -1.0);
+    advance_premac(H);
+    addw0_h(H, F_UMAC0, 1.0);
+    density_advance(H);
+    addw0_h(H, F_UMAC0, -1.0);
+    addw0_h(H, F_UMAC0, 1.0);
+    enthalpy_advance(H);
+    addw0_h(H, F_UMAC0, -1.0);
     // outputs (valid region)
-    if (io.snew) {
-        copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 2, 0);
-        copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
+    for (int l = 0; l < H.n(); ++l) {
+        Ctx& c = H[l];
+        if (io[l].snew) {
+            copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 2, 0);
+            copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
+        }
+        copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
+        for (int d = 0; d < 3; ++d) {
+            if (io[l].umac) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
+            if (io[l].sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
+            if (io[l].sflux) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);
+        }
+        if (io[l].eta) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
     }
-    copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
-    for (int d = 0; d < 3; ++d) {
-        if (io.umac) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
-        if (io.sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
-        if (io.sflux) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);
-    }
-    if (io.eta) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
 }
 
-static int finish(Ctx& c) {
-    int flag = 0;
-    CK(cudaMemcpyAsync(&flag, c.d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    CK(cudaStreamSynchronize(c.stream));
+static int finish(Hier& H) {
+    std::vector<int> flags(H.n(), 0);
+    for (int l = 0; l < H.n(); ++l)
+        CK(cudaMemcpyAsync(&flags[l], H[l].d_flag, sizeof(int), cudaMemcpyDeviceToHost, H[0].stream));
+    CK(cudaStreamSynchronize(H[0].stream));
     CK(cudaGetLastError());
-    if (flag) {
-        set_error("UpdateScal: a cell reached base_cutoff_density; the EOS reset is not implemented");
-        return MADV_ERR_EOS;
+    for (int f : flags) {
+        if (f & 1) {
+            set_error("UpdateScal: a cell reached base_cutoff_density; the EOS reset is not implemented");
+            return MADV_ERR_EOS;
+        }
+        if (f & 6) {
+            set_error("coarse-fine fill: a coarse cell or face was not available (levels not properly nested)");
+            return MADV_ERR_LAYOUT;
+        }
     }
     return MADV_OK;
+}
+
+static void set_mode(Hier& H, cudaStream_t st, int per_box, bool dry) {
+    for (auto* c : H.L) {
+        c->stream = st;
+        c->per_box = per_box;
+        c->dry = dry;
+    }
+}
+static long total_launches(const Hier& H) {
+    long n = 0;
+    for (auto* c : H.L) n += c->launches;
+    return n;
+}
+static void reset_launches(Hier& H) {
+    for (auto* c : H.L) c->launches = 0;
 }
 
 }  // namespace madv
@@ -498,15 +676,155 @@ cudaEvent_t Ctx::next_event() {
 }
 
 struct madv_ctx {
-    Ctx c;
+    Ctx c;                                   // level 0
+    std::vector<std::unique_ptr<Ctx>> fine;  // levels 1, 2, ...
+    Hier H() {
+        Hier h;
+        h.L.push_back(&c);
+        for (auto& f : fine) h.L.push_back(f.get());
+        return h;
+    }
 };
 
-static int check_ready(madv_ctx* h) { return h ? check_ready_c(&h->c) : MADV_ERR_PARAM; }
+static int init_level(Ctx& c, const madv_params& p, int lev) {
+    c.P = p;
+    c.lev = lev;
+    const int r = 1 << lev;
+    for (int d = 0; d < 3; ++d) {
+        c.P.dx[d] = p.dx[d] / r;
+        c.P.dom_lo[d] = p.dom_lo[d] * r;
+        c.P.dom_hi[d] = (p.dom_hi[d] + 1) * r - 1;
+    }
+    c.nspec = p.nspec;
+    c.nscal = 4 + p.nspec;
+    c.ng_s = c.ng_adv = p.ppm_type == 2 ? 4 : 3;
+    c.nr = c.P.dom_hi[2] - c.P.dom_lo[2] + 1;
+    for (int d = 0; d < 3; ++d) c.per[d] = p.phys_bc_lo[d] == PB_INTERIOR;
+    int rc = bc_setup(c);
+    if (rc) return rc;
+    BCRecD all[2 * MAX_SCAL + 3];
+    for (int k = 0; k < c.nscal; ++k) all[k] = c.bcs_s[k];
+    for (int k = 0; k < 3; ++k) all[c.nscal + k] = c.bcs_u[k];
+    for (int k = 0; k < c.nscal; ++k) all[c.nscal + 3 + k] = c.bcs_f[k];
+    if (!cuda_ok(cudaMalloc(&c.d_bcs, sizeof(BCRecD) * (2 * c.nscal + 3)), "cudaMalloc") ||
+        !cuda_ok(cudaMemcpy(c.d_bcs, all, sizeof(BCRecD) * (2 * c.nscal + 3), cudaMemcpyHostToDevice), "cudaMemcpy") ||
+        !cuda_ok(cudaMalloc(&c.d_flag, sizeof(int)), "cudaMalloc"))
+        return MADV_ERR_CUDA;
+    field_specs(c);
+    return MADV_OK;
+}
+
+static void destroy_level(Ctx& c) {
+    free_layout(c);
+    for (auto& kv : c.d1) cudaFree(kv.second);
+    c.d1.clear();
+    for (auto e : c.ev_pool) cudaEventDestroy(e);
+    c.ev_pool.clear();
+    if (c.box_scratch) cudaFree(c.box_scratch);
+    c.box_scratch = nullptr;
+    if (c.d_bcs) cudaFree(c.d_bcs);
+    c.d_bcs = nullptr;
+    if (c.d_flag) cudaFree(c.d_flag);
+    c.d_flag = nullptr;
+}
+
+// Layout of one level: field allocations and views.  Level 0 must cover the domain; finer
+// levels must be coarse-aligned (even lo, odd hi) and lie inside their domain.
+static int layout_level(Ctx& c, int nboxes, const madv_box* boxes, bool cover) {
+    free_layout(c);
+    c.have_layout = false;
+    c.ba.assign(nboxes, HBox{});
+    long vol = 0;
+    for (int b = 0; b < nboxes; ++b) {
+        for (int d = 0; d < 3; ++d) {
+            c.ba[b].lo[d] = boxes[b].lo[d];
+            c.ba[b].hi[d] = boxes[b].hi[d];
+            if (boxes[b].lo[d] > boxes[b].hi[d] || boxes[b].lo[d] < c.P.dom_lo[d] || boxes[b].hi[d] > c.P.dom_hi[d]) {
+                set_error("level " + std::to_string(c.lev) + " box " + std::to_string(b) +
+                          " is empty or outside the domain");
+                return MADV_ERR_LAYOUT;
+            }
+            if (c.lev > 0 && (((boxes[b].lo[d] & 1) != 0) || ((boxes[b].hi[d] & 1) != 1))) {
+                set_error("level " + std::to_string(c.lev) + " box " + std::to_string(b) +
+                          " is not aligned with the coarser level (even lo, odd hi)");
+                return MADV_ERR_LAYOUT;
+            }
+        }
+        vol += (long)(boxes[b].hi[0] - boxes[b].lo[0] + 1) * (boxes[b].hi[1] - boxes[b].lo[1] + 1) *
+               (boxes[b].hi[2] - boxes[b].lo[2] + 1);
+    }
+    for (int a = 0; a < nboxes; ++a)
+        for (int b = a + 1; b < nboxes; ++b) {
+            bool ov = true;
+            for (int d = 0; d < 3; ++d)
+                if (c.ba[a].hi[d] < c.ba[b].lo[d] || c.ba[b].hi[d] < c.ba[a].lo[d]) ov = false;
+            if (ov) {
+                set_error("boxes " + std::to_string(a) + " and " + std::to_string(b) + " overlap");
+                return MADV_ERR_LAYOUT;
+            }
+        }
+    long dvol = 1;
+    for (int d = 0; d < 3; ++d) dvol *= (c.P.dom_hi[d] - c.P.dom_lo[d] + 1);
+    if (cover && vol != dvol) {
+        set_error("level 0 must cover the domain");
+        return MADV_ERR_LAYOUT;
+    }
+    c.nb = nboxes;
+    try {
+        for (int f = 0; f < NF_INTERNAL; ++f) {
+            const FieldSpec& s = c.F[f].spec;
+            size_t tot = 0;
+            for (int b = 0; b < c.nb; ++b) {
+                HBox v = valid_box(c, b, s.nodal);
+                size_t n = 1;
+                for (int d = 0; d < 3; ++d) n *= (size_t)(v.hi[d] - v.lo[d] + 1 + 2 * s.ng);
+                tot += n * s.ncomp;
+            }
+            c.F[f].bytes = tot * sizeof(double);
+            if (!cuda_ok(cudaMalloc(&c.F[f].base, c.F[f].bytes), "cudaMalloc(field)")) throw Fail{MADV_ERR_CUDA};
+            if (!cuda_ok(cudaMemset(c.F[f].base, 0, c.F[f].bytes), "cudaMemset")) throw Fail{MADV_ERR_CUDA};
+        }
+        if (!cuda_ok(cudaMallocHost(&c.hviews_pinned, sizeof(FabView) * NF_TOTAL * c.nb), "cudaMallocHost"))
+            throw Fail{MADV_ERR_CUDA};
+        std::memset(c.hviews_pinned, 0, sizeof(FabView) * NF_TOTAL * c.nb);
+        for (int f = 0; f < NF_INTERNAL; ++f) {
+            const FieldSpec& s = c.F[f].spec;
+            size_t off = 0;
+            for (int b = 0; b < c.nb; ++b) {
+                HBox v = valid_box(c, b, s.nodal);
+                int lo[3], hi[3];
+                size_t n = 1;
+                for (int d = 0; d < 3; ++d) {
+                    lo[d] = v.lo[d] - s.ng;
+                    hi[d] = v.hi[d] + s.ng;
+                    n *= (size_t)(hi[d] - lo[d] + 1);
+                }
+                c.hviews_pinned[f * c.nb + b] = make_view(c.F[f].base + off, lo, hi);
+                off += n * s.ncomp;
+            }
+        }
+        if (!cuda_ok(cudaMalloc(&c.dviews, sizeof(FabView) * NF_TOTAL * c.nb), "cudaMalloc(views)") ||
+            !cuda_ok(cudaMemcpy(c.dviews, c.hviews_pinned, sizeof(FabView) * NF_TOTAL * c.nb, cudaMemcpyHostToDevice),
+                     "cudaMemcpy(views)"))
+            throw Fail{MADV_ERR_CUDA};
+    } catch (const Fail& f) {
+        free_layout(c);
+        return f.code;
+    }
+    c.have_layout = true;
+    return MADV_OK;
+}
+
+static void drop_graph(madv_ctx* h) {
+    if (h->c.graph_exec) cudaGraphExecDestroy(h->c.graph_exec);
+    h->c.graph_exec = nullptr;
+    h->c.graph_key.clear();
+}
 
 extern "C" {
 
 const char* madv_last_error(void) { return g_err.c_str(); }
-const char* madv_version(void) { return "maestro_adv 0.1 (sm_103a, FP64)"; }
+const char* madv_version(void) { return "maestro_adv 0.2 (sm_103a, FP64, 1-2 AMR levels)"; }
 
 int madv_ctx_create(const madv_params* p, madv_ctx** out) {
     if (!p || !out) return MADV_ERR_PARAM;
@@ -561,255 +879,303 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
         return MADV_ERR_PARAM;
     }
     madv_ctx* h = new madv_ctx();
-    Ctx& c = h->c;
-    c.P = *p;
-    c.nspec = p->nspec;
-    c.nscal = 4 + p->nspec;
-    c.ng_s = c.ng_adv = p->ppm_type == 2 ? 4 : 3;
-    c.nr = p->dom_hi[2] - p->dom_lo[2] + 1;
-    for (int d = 0; d < 3; ++d) c.per[d] = p->phys_bc_lo[d] == PB_INTERIOR;
-    int rc = bc_setup(c);
+    int rc = init_level(h->c, *p, 0);
     if (rc) {
+        destroy_level(h->c);
         delete h;
         return rc;
     }
-    BCRecD all[2 * MAX_SCAL + 3];
-    for (int k = 0; k < c.nscal; ++k) all[k] = c.bcs_s[k];
-    for (int k = 0; k < 3; ++k) all[c.nscal + k] = c.bcs_u[k];
-    for (int k = 0; k < c.nscal; ++k) all[c.nscal + 3 + k] = c.bcs_f[k];
-    if (!cuda_ok(cudaMalloc(&c.d_bcs, sizeof(BCRecD) * (2 * c.nscal + 3)), "cudaMalloc") ||
-        !cuda_ok(cudaMemcpy(c.d_bcs, all, sizeof(BCRecD) * (2 * c.nscal + 3), cudaMemcpyHostToDevice), "cudaMemcpy") ||
-        !cuda_ok(cudaMalloc(&c.d_flag, sizeof(int)), "cudaMalloc")) {
-        delete h;
-        return MADV_ERR_CUDA;
-    }
-    field_specs(c);
     *out = h;
     return MADV_OK;
 }
 
 void madv_ctx_destroy(madv_ctx* h) {
     if (!h) return;
-    Ctx& c = h->c;
-    free_layout(c);
-    for (auto& kv : c.d1) cudaFree(kv.second);
-    for (auto e : c.ev_pool) cudaEventDestroy(e);
-    if (c.box_scratch) cudaFree(c.box_scratch);
-    if (c.d_bcs) cudaFree(c.d_bcs);
-    if (c.d_flag) cudaFree(c.d_flag);
+    for (auto& f : h->fine) destroy_level(*f);
+    destroy_level(h->c);
     delete h;
 }
 
 int madv_set_dt(madv_ctx* h, double dt, double rel_eps) {
     if (!h || !(dt > 0.0) || !(rel_eps >= 0.0)) return MADV_ERR_PARAM;
-    h->c.P.dt = dt;
-    h->c.P.rel_eps = rel_eps;
-    if (h->c.graph_exec) cudaGraphExecDestroy(h->c.graph_exec);
-    h->c.graph_exec = nullptr;
-    h->c.graph_key.clear();
+    Hier H = h->H();
+    for (auto* c : H.L) {
+        c->P.dt = dt;
+        c->P.rel_eps = rel_eps;
+    }
+    drop_graph(h);
+    return MADV_OK;
+}
+
+int madv_set_layout_levels(madv_ctx* h, int nlev, const int* nboxes, const madv_box* boxes) {
+    if (!h || nlev < 1 || !nboxes || !boxes) return MADV_ERR_PARAM;
+    if (nlev > 2) {
+        set_error("at most two levels (refinement ratio 2)");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    for (auto& f : h->fine) destroy_level(*f);
+    h->fine.clear();
+    drop_graph(h);
+    for (int l = 1; l < nlev; ++l) {
+        h->fine.emplace_back(new Ctx());
+        int rc = init_level(*h->fine.back(), h->c.P, l);
+        if (rc) return rc;
+    }
+    Hier H = h->H();
+    int off = 0;
+    for (int l = 0; l < nlev; ++l) {
+        if (nboxes[l] <= 0) {
+            set_error("every level needs at least one box");
+            return MADV_ERR_LAYOUT;
+        }
+        int rc = layout_level(H[l], nboxes[l], boxes + off, l == 0);
+        if (rc) return rc;
+        off += nboxes[l];
+        if (nlev > 1 && (rc = build_owner(H[l]))) return rc;
+        if (nlev > 1) H[l].have_base = false;  // radial chunks depend on the layout
+    }
     return MADV_OK;
 }
 
 int madv_set_layout(madv_ctx* h, int nboxes, const madv_box* boxes) {
     if (!h || nboxes <= 0 || !boxes) return MADV_ERR_PARAM;
-    Ctx& c = h->c;
-    free_layout(c);
-    c.have_layout = false;
-    c.ba.assign(nboxes, HBox{});
-    long vol = 0;
-    for (int b = 0; b < nboxes; ++b) {
-        for (int d = 0; d < 3; ++d) {
-            c.ba[b].lo[d] = boxes[b].lo[d];
-            c.ba[b].hi[d] = boxes[b].hi[d];
-            if (boxes[b].lo[d] > boxes[b].hi[d] || boxes[b].lo[d] < c.P.dom_lo[d] || boxes[b].hi[d] > c.P.dom_hi[d]) {
-                set_error("box " + std::to_string(b) + " is empty or outside the domain");
-                return MADV_ERR_LAYOUT;
-            }
-        }
-        vol += (long)(boxes[b].hi[0] - boxes[b].lo[0] + 1) * (boxes[b].hi[1] - boxes[b].lo[1] + 1) *
-               (boxes[b].hi[2] - boxes[b].lo[2] + 1);
+    return madv_set_layout_levels(h, 1, &nboxes, boxes);
+}
+
+int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl) {
+    if (!h || !bsl) return MADV_ERR_PARAM;
+    Hier H = h->H();
+    if (nlev != H.n()) {
+        set_error("the base state needs one entry per level of the layout");
+        return MADV_ERR_PARAM;
     }
-    for (int a = 0; a < nboxes; ++a)
-        for (int b = a + 1; b < nboxes; ++b) {
-            bool ov = true;
-            for (int d = 0; d < 3; ++d)
-                if (c.ba[a].hi[d] < c.ba[b].lo[d] || c.ba[b].hi[d] < c.ba[a].lo[d]) ov = false;
-            if (ov) {
-                set_error("boxes " + std::to_string(a) + " and " + std::to_string(b) + " overlap");
-                return MADV_ERR_LAYOUT;
-            }
+    for (int l = 0; l < nlev; ++l)
+        if (!H[l].have_layout && nlev > 1) {
+            set_error("madv_set_layout_levels must come first");
+            return MADV_ERR_STATE;
         }
-    long dvol = 1;
-    for (int d = 0; d < 3; ++d) dvol *= (c.P.dom_hi[d] - c.P.dom_lo[d] + 1);
-    if (vol != dvol) {
-        set_error("a single-level layout must cover the domain");
-        return MADV_ERR_LAYOUT;
+    // radial chunks per level (BaseStateGeometry::InitMultiLevel, planar, Source/BaseStateGeometry.cpp:355-382):
+    // rows of level l-1 lying under a level-l box are tagged; each run of tagged rows r0..r1
+    // is the level-l chunk [2 r0, 2 r1 + 1]
+    H[0].chunks.assign(1, {0, H[0].nr - 1});
+    for (int l = 1; l < nlev; ++l) {
+        const int nrc = H[l - 1].nr;
+        std::vector<int> tag(nrc, 0);
+        for (auto& b : H[l].ba)
+            for (int r = b.lo[2]; r <= b.hi[2]; ++r) tag[r / 2] = 1;
+        auto& ch = H[l].chunks;
+        ch.clear();
+        bool in = false;
+        for (int r = 0; r < nrc; ++r) {
+            if (tag[r] && !in) {
+                in = true;
+                ch.push_back({2 * r, 0});
+            } else if (!tag[r] && in) {
+                ch.back()[1] = 2 * r - 1;
+                in = false;
+            }
+            if (in && r == nrc - 1) ch.back()[1] = 2 * r + 1;
+        }
     }
-    c.nb = nboxes;
-    try {
-        for (int f = 0; f < NF_INTERNAL; ++f) {
-            const FieldSpec& s = c.F[f].spec;
-            size_t tot = 0;
-            for (int b = 0; b < c.nb; ++b) {
-                HBox v = valid_box(c, b, s.nodal);
-                size_t n = 1;
-                for (int d = 0; d < 3; ++d) n *= (size_t)(v.hi[d] - v.lo[d] + 1 + 2 * s.ng);
-                tot += n * s.ncomp;
+    for (int l = 0; l < nlev; ++l) {
+        Ctx& c = H[l];
+        const madv_base_state* bs = &bsl[l];
+        const int nr = c.nr;
+        struct Arr1 {
+            const char* name;
+            const double* p;
+            int n;
+        } arrs[] = {{"rho0_old", bs->rho0_old, nr},   {"rho0_new", bs->rho0_new, nr}, {"rhoh0_old", bs->rhoh0_old, nr},
+                    {"rhoh0_new", bs->rhoh0_new, nr}, {"p0_old", bs->p0_old, nr},     {"p0_new", bs->p0_new, nr},
+                    {"psi", bs->psi, nr},             {"grav_cell", bs->grav_cell, nr}, {"w0_force", bs->w0_force, nr},
+                    {"w0", bs->w0, nr + 1},           {"rho0_predicted_edge", bs->rho0_predicted_edge, nr + 1}};
+        for (auto& a : arrs) {
+            if (!a.p) {
+                set_error(std::string("base state array ") + a.name + " is NULL");
+                return MADV_ERR_PARAM;
             }
-            c.F[f].bytes = tot * sizeof(double);
-            if (!cuda_ok(cudaMalloc(&c.F[f].base, c.F[f].bytes), "cudaMalloc(field)")) throw Fail{MADV_ERR_CUDA};
-            if (!cuda_ok(cudaMemset(c.F[f].base, 0, c.F[f].bytes), "cudaMemset")) throw Fail{MADV_ERR_CUDA};
+            c.h1[a.name] = std::vector<double>(a.p, a.p + a.n);
         }
-        if (!cuda_ok(cudaMallocHost(&c.hviews_pinned, sizeof(FabView) * NF_TOTAL * c.nb), "cudaMallocHost"))
-            throw Fail{MADV_ERR_CUDA};
-        std::memset(c.hviews_pinned, 0, sizeof(FabView) * NF_TOTAL * c.nb);
-        for (int f = 0; f < NF_INTERNAL; ++f) {
-            const FieldSpec& s = c.F[f].spec;
-            size_t off = 0;
-            for (int b = 0; b < c.nb; ++b) {
-                HBox v = valid_box(c, b, s.nodal);
-                int lo[3], hi[3];
-                size_t n = 1;
-                for (int d = 0; d < 3; ++d) {
-                    lo[d] = v.lo[d] - s.ng;
-                    hi[d] = v.hi[d] + s.ng;
-                    n *= (size_t)(hi[d] - lo[d] + 1);
-                }
-                c.hviews_pinned[f * c.nb + b] = make_view(c.F[f].base + off, lo, hi);
-                off += n * s.ncomp;
-            }
-        }
-        if (!cuda_ok(cudaMalloc(&c.dviews, sizeof(FabView) * NF_TOTAL * c.nb), "cudaMalloc(views)") ||
-            !cuda_ok(cudaMemcpy(c.dviews, c.hviews_pinned, sizeof(FabView) * NF_TOTAL * c.nb, cudaMemcpyHostToDevice),
-                     "cudaMemcpy(views)"))
-            throw Fail{MADV_ERR_CUDA};
-    } catch (const Fail& f) {
-        free_layout(c);
-        return f.code;
     }
-    c.have_layout = true;
+    // Maestro::CelltoEdge over the chunks of every level, then RestrictBase of the edges
+    // (Source/MaestroCelltoEdge.cpp:17-58, Source/MaestroBaseStateGeometry.cpp:240-262)
+    for (const char* name : {"rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new"}) {
+        const std::string en = std::string(name).replace(std::string(name).find("0_"), 2, "0_edge_");
+        for (int l = 0; l < nlev; ++l) {
+            std::vector<double> e(H[l].nr + 1, 0.0);
+            for (auto& ch : H[l].chunks) cell_to_edge_chunk(H[l].h1[name], e, ch[0], ch[1] + 1);
+            H[l].h1[en] = e;
+        }
+        for (int l = nlev - 1; l >= 1; --l)
+            for (auto& ch : H[l].chunks)
+                for (int j = ch[0]; j <= ch[1] + 1; j += 2) H[l - 1].h1[en][j / 2] = H[l].h1[en][j];
+    }
+    // BaseStateGeometry::ComputeCutoffCoords, base cutoff (Source/BaseStateGeometry.cpp:164-210);
+    // one level keeps the caller's base_cutoff_density_coord
+    if (nlev > 1) {
+        bool found = false;
+        int which = 0;
+        std::vector<int> coord(nlev, 0);
+        for (int n = nlev - 1; n >= 0 && !found; --n)
+            for (auto& ch : H[n].chunks) {
+                if (found) break;
+                for (int r = ch[0]; r <= ch[1]; ++r)
+                    if (H[n].h1["rho0_old"][r] <= H[0].P.base_cutoff_density) {
+                        coord[n] = r;
+                        which = n;
+                        found = true;
+                        break;
+                    }
+            }
+        if (!found) {
+            which = nlev - 1;
+            coord[which] = H[which].nr;
+        }
+        for (int n = which + 1; n < nlev; ++n) coord[n] = 2 * coord[n - 1] + 1;
+        for (int n = which - 1; n >= 0; --n) coord[n] = coord[n + 1] % 2 == 0 ? coord[n + 1] / 2 : coord[n + 1] / 2 + 1;
+        for (int n = 0; n < nlev; ++n) H[n].P.base_cutoff_density_coord = coord[n];
+    }
+    for (int l = 0; l < nlev; ++l) {
+        Ctx& c = H[l];
+        for (auto& kv : c.h1) {
+            double*& d = c.d1[kv.first];
+            if (!d && !cuda_ok(cudaMalloc(&d, sizeof(double) * (c.nr + 1)), "cudaMalloc(base)")) return MADV_ERR_CUDA;
+            if (!cuda_ok(cudaMemcpy(d, kv.second.data(), sizeof(double) * kv.second.size(), cudaMemcpyHostToDevice),
+                         "cudaMemcpy(base)"))
+                return MADV_ERR_CUDA;
+        }
+        c.have_base = true;
+    }
+    drop_graph(h);
     return MADV_OK;
 }
 
 int madv_set_base_state(madv_ctx* h, const madv_base_state* bs) {
     if (!h || !bs) return MADV_ERR_PARAM;
+    if (!h->fine.empty()) {
+        set_error("the layout has several levels: use madv_set_base_state_levels");
+        return MADV_ERR_STATE;
+    }
+    return madv_set_base_state_levels(h, 1, bs);
+}
+
+static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab* uold, const madv_multifab* sold,
+                           const madv_multifab* gpi, const madv_multifab* thermal, const madv_multifab* snew,
+                           const madv_multifab* umac, const madv_multifab* sedge, const madv_multifab* sflux,
+                           const madv_multifab* etarhoflux, void* stream) {
+    Hier H = h->H();
+    if (nlev != H.n()) {
+        set_error("the call passes " + std::to_string(nlev) + " levels, the layout has " + std::to_string(H.n()));
+        return MADV_ERR_PARAM;
+    }
+    int rc = check_ready_h(H);
+    if (rc) return rc;
+    if (!uold || !sold || !gpi) {
+        set_error("uold, sold and gpi are required");
+        return MADV_ERR_PARAM;
+    }
+    if (mode < MADV_MODE_BATCHED || mode > MADV_MODE_GRAPH) return MADV_ERR_PARAM;
+    std::vector<StageIO> io(nlev);
+    for (int l = 0; l < nlev; ++l)
+        io[l] = StageIO{&uold[l], &sold[l], &gpi[l], thermal ? &thermal[l] : nullptr, snew ? &snew[l] : nullptr,
+                        umac ? &umac[3 * l] : nullptr, sedge ? &sedge[3 * l] : nullptr,
+                        sflux ? &sflux[3 * l] : nullptr, etarhoflux ? &etarhoflux[l] : nullptr};
     Ctx& c = h->c;
-    const int nr = c.nr;
-    struct Arr1 {
-        const char* name;
-        const double* p;
-        int n;
-    } arrs[] = {{"rho0_old", bs->rho0_old, nr},   {"rho0_new", bs->rho0_new, nr}, {"rhoh0_old", bs->rhoh0_old, nr},
-                {"rhoh0_new", bs->rhoh0_new, nr}, {"p0_old", bs->p0_old, nr},     {"p0_new", bs->p0_new, nr},
-                {"psi", bs->psi, nr},             {"grav_cell", bs->grav_cell, nr}, {"w0_force", bs->w0_force, nr},
-                {"w0", bs->w0, nr + 1},           {"rho0_predicted_edge", bs->rho0_predicted_edge, nr + 1}};
-    for (auto& a : arrs) {
-        if (!a.p) {
-            set_error(std::string("base state array ") + a.name + " is NULL");
-            return MADV_ERR_PARAM;
+    set_mode(H, (cudaStream_t)stream, 0, false);
+    reset_launches(H);
+    try {
+        for (int l = 0; l < nlev; ++l)
+            if ((rc = bind_stage(H[l], io[l]))) return rc;
+        if (mode == MADV_MODE_GRAPH) {
+            std::vector<const void*> key;
+            for (int l = 0; l < nlev; ++l) {
+                const madv_multifab* all[] = {io[l].uold, io[l].sold, io[l].gpi, io[l].thermal, io[l].snew, io[l].eta};
+                for (auto m : all) {
+                    key.push_back(m);
+                    if (m)
+                        for (int b = 0; b < m->nfab; ++b) key.push_back(m->fab[b].p);
+                }
+                for (auto m3 : {io[l].umac, io[l].sedge, io[l].sflux}) {
+                    key.push_back(m3);
+                    if (m3)
+                        for (int d = 0; d < 3; ++d)
+                            for (int b = 0; b < m3[d].nfab; ++b) key.push_back(m3[d].fab[b].p);
+                }
+            }
+            if (!c.graph_exec || key != c.graph_key) {
+                drop_graph(h);
+                // a dry pass builds every region / copy table (no allocation may happen
+                // while capturing), then the stage is captured
+                set_mode(H, (cudaStream_t)stream, 0, true);
+                stage_body(H, io);
+                cudaStream_t cs;
+                CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+                set_mode(H, cs, 0, false);
+                reset_launches(H);
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+                for (auto* lc : H.L) upload_user_views(*lc);
+                stage_body(H, io);
+                CK(cudaStreamEndCapture(cs, &g));
+                CK(cudaGraphInstantiate(&c.graph_exec, g, 0));
+                cudaGraphDestroy(g);
+                cudaStreamDestroy(cs);
+                set_mode(H, (cudaStream_t)stream, 0, false);
+                c.graph_key = key;
+                c.graph_launches = total_launches(H);
+            }
+            CK(cudaGraphLaunch(c.graph_exec, c.stream));
+            reset_launches(H);
+            c.launches = c.graph_launches;
+            return finish(H);
         }
-        c.h1[a.name] = std::vector<double>(a.p, a.p + a.n);
+        set_mode(H, (cudaStream_t)stream, mode == MADV_MODE_PER_BOX, false);
+        stage_body(H, io);
+        set_mode(H, (cudaStream_t)stream, 0, false);
+        return finish(H);
+    } catch (const Fail& f) {
+        set_mode(H, (cudaStream_t)stream, 0, false);
+        return f.code;
     }
-    c.h1["rho0_edge_old"] = cell_to_edge(c.h1["rho0_old"]);
-    c.h1["rho0_edge_new"] = cell_to_edge(c.h1["rho0_new"]);
-    c.h1["rhoh0_edge_old"] = cell_to_edge(c.h1["rhoh0_old"]);
-    c.h1["rhoh0_edge_new"] = cell_to_edge(c.h1["rhoh0_new"]);
-    for (auto& kv : c.h1) {
-        double*& d = c.d1[kv.first];
-        if (!d && !cuda_ok(cudaMalloc(&d, sizeof(double) * (nr + 1)), "cudaMalloc(base)")) return MADV_ERR_CUDA;
-        if (!cuda_ok(cudaMemcpy(d, kv.second.data(), sizeof(double) * kv.second.size(), cudaMemcpyHostToDevice),
-                     "cudaMemcpy(base)"))
-            return MADV_ERR_CUDA;
-    }
-    c.have_base = true;
-    return MADV_OK;
 }
 
 int madv_stage_forward(madv_ctx* h, int mode, const madv_multifab* uold, const madv_multifab* sold,
                        const madv_multifab* gpi, const madv_multifab* thermal, const madv_multifab* snew,
                        const madv_multifab* umac, const madv_multifab* sedge, const madv_multifab* sflux,
                        const madv_multifab* etarhoflux, void* stream) {
-    int rc = check_ready(h);
-    if (rc) return rc;
-    Ctx& c = h->c;
-    if (!uold || !sold || !gpi) {
-        set_error("uold, sold and gpi are required");
-        return MADV_ERR_PARAM;
-    }
-    if (mode < MADV_MODE_BATCHED || mode > MADV_MODE_GRAPH) return MADV_ERR_PARAM;
-    c.stream = (cudaStream_t)stream;
-    c.launches = 0;
-    StageIO io{uold, sold, gpi, thermal, snew, umac, sedge, sflux, etarhoflux};
-    try {
-        if ((rc = bind_stage(c, io))) return rc;
-        if (mode == MADV_MODE_GRAPH) {
-            std::vector<const void*> key;
-            const madv_multifab* all[] = {uold, sold, gpi, thermal, snew, etarhoflux};
-            for (auto m : all) {
-                key.push_back(m);
-                if (m)
-                    for (int b = 0; b < m->nfab; ++b) key.push_back(m->fab[b].p);
-            }
-            for (auto m3 : {umac, sedge, sflux}) {
-                key.push_back(m3);
-                if (m3)
-                    for (int d = 0; d < 3; ++d)
-                        for (int b = 0; b < m3[d].nfab; ++b) key.push_back(m3[d].fab[b].p);
-            }
-            if (!c.graph_exec || key != c.graph_key) {
-                if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
-                c.graph_exec = nullptr;
-                // a dry pass builds every region / copy table (no allocation may happen
-                // while capturing), then the stage is captured
-                c.per_box = 0;
-                c.dry = true;
-                stage_body(c, io);
-                c.dry = false;
-                cudaStream_t cs;
-                CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-                cudaStream_t user = c.stream;
-                c.stream = cs;
-                c.launches = 0;
-                cudaGraph_t g;
-                CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-                upload_user_views(c);
-                stage_body(c, io);
-                CK(cudaStreamEndCapture(cs, &g));
-                CK(cudaGraphInstantiate(&c.graph_exec, g, 0));
-                cudaGraphDestroy(g);
-                cudaStreamDestroy(cs);
-                c.stream = user;
-                c.graph_key = key;
-                c.graph_launches = c.launches;
-            }
-            CK(cudaGraphLaunch(c.graph_exec, c.stream));
-            c.launches = c.graph_launches;
-            return finish(c);
-        }
-        c.per_box = mode == MADV_MODE_PER_BOX;
-        stage_body(c, io);
-        c.per_box = 0;
-        return finish(c);
-    } catch (const Fail& f) {
-        return f.code;
-    }
+    if (!h) return MADV_ERR_PARAM;
+    return stage_forward_h(h, mode, 1, uold, sold, gpi, thermal, snew, umac, sedge, sflux, etarhoflux, stream);
 }
 
-// ---- Maestro-shaped entry points: the same pieces, with the caller's FABs copied in and
-// out around each call.
-static int begin_call(madv_ctx* h, void* stream) {
-    int rc = check_ready(h);
+int madv_stage_forward_levels(madv_ctx* h, int mode, int nlev, const madv_multifab* uold, const madv_multifab* sold,
+                              const madv_multifab* gpi, const madv_multifab* thermal, const madv_multifab* snew,
+                              const madv_multifab* umac, const madv_multifab* sedge, const madv_multifab* sflux,
+                              const madv_multifab* etarhoflux, void* stream) {
+    if (!h) return MADV_ERR_PARAM;
+    return stage_forward_h(h, mode, nlev, uold, sold, gpi, thermal, snew, umac, sedge, sflux, etarhoflux, stream);
+}
+
+// ---- Maestro-shaped entry points (one level): the same pieces, with the caller's FABs
+// copied in and out around each call.
+static int begin_call(madv_ctx* h, void* stream, Hier& H) {
+    if (!h) return MADV_ERR_PARAM;
+    if (!h->fine.empty()) {
+        set_error("the per-function entry points take one level; use madv_stage_forward_levels");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    H = h->H();
+    int rc = check_ready_h(H);
     if (rc) return rc;
-    h->c.stream = (cudaStream_t)stream;
-    h->c.launches = 0;
-    h->c.per_box = 0;
+    set_mode(H, (cudaStream_t)stream, 0, false);
+    reset_launches(H);
     cudaMemsetAsync(h->c.d_flag, 0, sizeof(int), h->c.stream);
     return MADV_OK;
 }
 
 int madv_advance_premac(madv_ctx* h, const madv_multifab* uold, const madv_multifab* sold, const madv_multifab* gpi,
                         const madv_multifab* umac, const madv_multifab* utrans, void* stream) {
-    int rc = begin_call(h, stream);
+    Hier H;
+    int rc = begin_call(h, stream, H);
     if (rc) return rc;
     Ctx& c = h->c;
     if (!uold || !sold || !gpi || !umac) return MADV_ERR_PARAM;
@@ -827,20 +1193,21 @@ int madv_advance_premac(madv_ctx* h, const madv_multifab* uold, const madv_multi
         copy_fab(c, F_SOLD, RHO, F_USER + U_SOLD, RHO, 1, 0);
         copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, 3, 0);
         for (int d = 0; d < 3; ++d) set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
-        w0_carts(c);
-        advance_premac(c);
+        w0_carts(H);
+        advance_premac(H);
         for (int d = 0; d < 3; ++d) {
             copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
             if (utrans) copy_fab(c, F_USER + U_UTRANS0 + d, 0, F_UTRANS0 + d, 0, 1, 0);
         }
-        return finish(c);
+        return finish(H);
     } catch (const Fail& f) {
         return f.code;
     }
 }
 
 int madv_addw0(madv_ctx* h, const madv_multifab* umac, double mult, void* stream) {
-    int rc = begin_call(h, stream);
+    Hier H;
+    int rc = begin_call(h, stream, H);
     if (rc) return rc;
     Ctx& c = h->c;
     if (!umac) return MADV_ERR_PARAM;
@@ -849,9 +1216,9 @@ int madv_addw0(madv_ctx* h, const madv_multifab* umac, double mult, void* stream
             if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 1))) return rc;
         if ((rc = upload_user_views(c))) return rc;
         for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
-        addw0(c, F_UMAC0, mult);
+        addw0_h(H, F_UMAC0, mult);
         for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
-        return finish(c);
+        return finish(H);
     } catch (const Fail& f) {
         return f.code;
     }
@@ -860,7 +1227,8 @@ int madv_addw0(madv_ctx* h, const madv_multifab* umac, double mult, void* stream
 static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_multifab* sold, const madv_multifab* snew,
                           const madv_multifab* sedge, const madv_multifab* sflux, const madv_multifab* eta,
                           const madv_multifab* umac, const madv_multifab* thermal, void* stream) {
-    int rc = begin_call(h, stream);
+    Hier H;
+    int rc = begin_call(h, stream, H);
     if (rc) return rc;
     Ctx& c = h->c;
     if (which_step != 1) {
@@ -879,7 +1247,7 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
         }
         if ((rc = upload_user_views(c))) return rc;
         copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
-        fill_patch(c, F_SOLD, 0, c.nscal, BCS_S, 0, 0, 0);
+        fill_patch_h(H, F_SOLD, 0, c.nscal, BCS_S, 0, 0, 0);
         copy_fab(c, F_SNEW, 0, F_USER + U_SNEW, 0, c.nscal, 0);
         for (int d = 0; d < 3; ++d) {
             copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
@@ -888,16 +1256,16 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
         }
         set_val(c, F_THERMAL, 0.0, 0, 1, 1);
         if (thermal) copy_fab(c, F_THERMAL, 0, F_USER + U_THERMAL, 0, 1, 0);
-        w0_carts(c);
+        w0_carts(H);
         if (which == 0) {
             set_val(c, F_ETA, 0.0, 0, 1, 0);
             if (eta) copy_fab(c, F_ETA, 0, F_USER + U_ETA, 0, 1, 0);
-            density_advance(c);
+            density_advance(H);
             copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 1, 0);
             copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
             if (eta) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
         } else {
-            enthalpy_advance(c);
+            enthalpy_advance(H);
             copy_fab(c, F_USER + U_SNEW, RHOH, F_SNEW, RHOH, 1, 0);
         }
         copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
@@ -906,7 +1274,7 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
             if (sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
             if (sflux) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);
         }
-        return finish(c);
+        return finish(H);
     } catch (const Fail& f) {
         return f.code;
     }
@@ -924,7 +1292,12 @@ int madv_enthalpy_advance(madv_ctx* h, int which_step, const madv_multifab* sold
     return scalar_advance(h, 1, which_step, sold, snew, sedge, sflux, nullptr, umac, thermal, stream);
 }
 
-long madv_last_launch_count(const madv_ctx* h) { return h ? h->c.launches : -1; }
+long madv_last_launch_count(const madv_ctx* h) {
+    if (!h) return -1;
+    long n = h->c.launches;
+    for (auto& f : h->fine) n += f->launches;
+    return n;
+}
 
 int madv_ppm(madv_ctx* h, const madv_box* bx, const madv_fab* s, int comp, const madv_fab* u, const madv_fab* v,
              const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip, const madv_fab* Im, void* stream) {
@@ -951,18 +1324,23 @@ int madv_ppm(madv_ctx* h, const madv_box* bx, const madv_fab* s, int comp, const
 
 int madv_profile(madv_ctx* h, int enable) {
     if (!h) return MADV_ERR_PARAM;
-    h->c.profiling = enable != 0;
-    h->c.prof.clear();
-    h->c.ev_next = 0;
+    Hier H = h->H();
+    for (auto* c : H.L) {
+        c->profiling = enable != 0;
+        c->prof.clear();
+        c->ev_next = 0;
+    }
     return MADV_OK;
 }
 
 int madv_profile_report(madv_ctx* h, char* buf, int len) {
     if (!h || !buf || len <= 0) return MADV_ERR_PARAM;
-    Ctx& c = h->c;
+    Hier H = h->H();
     if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) return MADV_ERR_CUDA;
     std::map<std::string, std::pair<long, double>> agg;
-    for (auto& r : c.prof) {
+    std::vector<Ctx::ProfRec> recs;
+    for (auto* c : H.L) recs.insert(recs.end(), c->prof.begin(), c->prof.end());
+    for (auto& r : recs) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, r.e0, r.e1);
         const char* name = nullptr;

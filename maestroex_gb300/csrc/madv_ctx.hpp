@@ -1,4 +1,4 @@
-// Host-side context of the scalar-advection stage library (one AMR level).
+// Host-side context of the scalar-advection stage library: one Ctx per AMR level.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -11,6 +11,11 @@
 #include "madv_core.cuh"
 
 namespace madv {
+
+// thrown by table builders when a device allocation fails
+struct Fail {
+    int code;
+};
 
 struct HBox {
     int lo[3];
@@ -80,7 +85,8 @@ struct CopyTable {
 };
 
 struct Ctx {
-    madv_params P{};
+    madv_params P{};  // dx, domain and base_cutoff_density_coord are this level's
+    int lev = 0;
     int nspec = 0, nscal = 0, ng_s = 3, ng_adv = 3, nr = 0;
     bool per[3] = {false, false, false};
     std::vector<HBox> ba;
@@ -120,8 +126,21 @@ struct Ctx {
     double* box_scratch = nullptr;
     long box_scratch_n = 0;
 
+    // coarse-fine data (hierarchies of more than one level)
+    std::vector<int> h_owner;  // box owning each cell of the level's domain, -1 = none
+    int* d_owner = nullptr;
+    std::vector<std::array<int, 2>> chunks;  // radial cell ranges of the level's base state
+    std::map<std::array<int, 4>, RegionTable> amr_tables;
+
     double* b1(const char* name) { return d1.at(name); }
     const FabView* V() const { return dviews; }
+};
+
+// The levels of one hierarchy (level 0 first); every level shares the stream and flags.
+struct Hier {
+    std::vector<Ctx*> L;
+    int n() const { return (int)L.size(); }
+    Ctx& operator[](int l) const { return *L[l]; }
 };
 
 // Region of each box: the valid cell box grown by glo (low side) / ghi (high side), with
@@ -147,13 +166,13 @@ void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow);
 void add_fab(Ctx& c, int dst, int src, int nc, int ngrow);
 void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge);
 void make_utrans(Ctx& c);
-void make_vel_force(Ctx& c);
+void make_vel_force(Ctx& c);  // valid cells; F_GRAVCART / F_RHO0CART filled by the caller
 void vel_pred(Ctx& c);
 void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative,
                     int force_zero);
-void modify_scal_force(Ctx& c, int comp, const double* d_s0_edge, int s0cart_fid, int fullform);
-void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal, int which_step);
-void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int bccomp, int which_bcs, int flag);
+void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform);
+void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal);
+void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag);
 void convert_rhox_to_x(Ctx& c, int flag);
 void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
                     const double* r0e_new);
@@ -165,6 +184,13 @@ int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int
                 const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
                 const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
+
+// ---- coarse-fine operations between level cf and its parent cc (madv_amr.cu)
+int build_owner(Ctx& c);  // owner map of the level's domain (host + device)
+void interp_fill(Ctx& cc, Ctx& cf, int fid, int c0, int nc, int which_bcs, int bc_c0, int is_vel, int state_c0);
+void average_down(Ctx& cf, Ctx& cc, int fid, int comp, int ncomp);
+void average_down_faces(Ctx& cf, Ctx& cc, int f0, int c0, int ncomp);
+void uedge_interface(Ctx& cc, Ctx& cf, int f0);
 
 enum { BCS_S = 0, BCS_U = 1, BCS_F = 2 };
 inline const BCRecD* bcs_dev(const Ctx& c, int which) {

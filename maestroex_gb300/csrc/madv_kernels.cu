@@ -1,4 +1,4 @@
-// Kernels of the GB300 scalar-advection stage (3-D, plane-parallel base state, one level).
+// Kernels of the GB300 scalar-advection stage (3-D, plane-parallel base state), per level.
 //
 // Each reference ParallelFor of the stage becomes one launch over all boxes of the level
 // (or one launch per box in the per-box mode).  The arithmetic of every element follows
@@ -16,50 +16,10 @@
 
 #include "madv_ctx.hpp"
 #include "madv_exact.cuh"
+#include "madv_launch.cuh"
 #include "madv_ppm.cuh"
 
 namespace madv {
-
-#define KARGS const RegionBox *__restrict__ R, int ne, long g0, long g1, const FabView *__restrict__ V, int nb
-#define VW(f) V[(f) * nb + b]
-
-static constexpr int TPB = 256;
-
-// One launch over every box (batched), or one launch per region piece (per-box mode, the
-// MFIter + ParallelFor form of the reference).  Kernel arguments after the region are
-// (V, nb, ...).
-template <typename Kern, typename... Args>
-static void launch(Ctx& c, const RegionTable& rt, int gy, Kern kern, const FabView* V, Args... args) {
-    if (rt.total == 0 || c.dry) return;
-    const int ne = (int)rt.h.size();
-    if (!c.per_box) {
-        dim3 grid((unsigned)((rt.total + TPB - 1) / TPB), gy);
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        if (c.profiling) {
-            e0 = c.next_event();
-            e1 = c.next_event();
-            cudaEventRecord(e0, c.stream);
-        }
-        kern<<<grid, TPB, 0, c.stream>>>(rt.d, ne, 0L, rt.total, V, c.nb, args...);
-        if (c.profiling) {
-            cudaEventRecord(e1, c.stream);
-            c.prof.push_back({(const void*)kern, e0, e1});
-        }
-        c.launches++;
-    } else {
-        for (int e = 0; e < ne; ++e) {
-            long s0 = rt.h[e].start;
-            long s1 = (e + 1 < ne) ? rt.h[e + 1].start : rt.total;
-            if (s1 <= s0) continue;
-            dim3 grid((unsigned)((s1 - s0 + TPB - 1) / TPB), gy);
-            kern<<<grid, TPB, 0, c.stream>>>(rt.d, ne, s0, s1, V, c.nb, args...);
-            c.launches++;
-        }
-    }
-}
-
-// Region helpers: the valid box grown by g, and face boxes.
-static const RegionTable& rg_grow(Ctx& c, int g, int nodal = -1) { return region(c, g, g, g, g, g, g, nodal); }
 
 // ============================================================ elementwise utilities
 __global__ void k_set_val(KARGS, int f, double v, int c0, int nc) {
@@ -277,7 +237,6 @@ __global__ void k_addw0(KARGS, int f, const double* __restrict__ w0, double mult
 
 void addw0(Ctx& c, int f0, double mult) {
     launch(c, region(c, 1, 1, 0, 1, 1, 0, 2), 1, k_addw0, c.V(), f0 + 2, (const double*)c.b1("w0"), mult);
-    fill_face_ghosts(c, f0);
 }
 
 // ============================================================ PPM
@@ -633,7 +592,6 @@ void make_utrans(Ctx& c) {
         else if (d == 1) launch(c, rt, 1, k_utrans<1>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
         else launch(c, rt, 1, k_utrans<2>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
     }
-    fill_face_ghosts(c, F_UTRANS0);
 }
 
 // ============================================================ MakeVelForce
@@ -654,18 +612,11 @@ __global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz) {
     at(vf, i, j, k, 2) = f2;
 }
 
+// valid cells of one level; F_GRAVCART and F_RHO0CART are filled by the caller
 void make_vel_force(Ctx& c) {
-    // grav_cart (vector, bcs_f) and rho0_cart (rho0_old, bcs_s Rho)
-    set_val(c, F_GRAVCART, 0.0, 0, 3, 1);
-    put1d(c, F_GRAVCART, c.b1("grav_cell"), 2, 0);
-    fill_patch(c, F_GRAVCART, 0, 3, BCS_F, 0, 0, -1);
-    set_val(c, F_RHO0CART, 0.0, 0, 1, 1);
-    put1d(c, F_RHO0CART, c.b1("rho0_old"), 0, 0);
-    fill_patch(c, F_RHO0CART, 0, 1, BCS_S, RHO, 0, RHO);
     set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
     launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
            c.P.dom_hi[2], make_recip(2.0 * c.P.dx[2]));
-    fill_patch(c, F_VELFORCE, 0, 3, BCS_U, 0, 1, -1);
 }
 
 // ============================================================ VelPred
@@ -1135,13 +1086,10 @@ __global__ void k_modify_scal_force(KARGS, int comp, int s0cart, int fullform, R
     }
 }
 
-void modify_scal_force(Ctx& c, int comp, const double* d_s0_edge, int s0cart_fid, int fullform) {
-    set_val(c, F_S0ECART, 0.0, 0, 1, 1);
-    put1d(c, F_S0ECART, d_s0_edge, 0, 0);
-    fill_patch(c, F_S0ECART, 0, 1, BCS_F, 0, 0, -1);
+// valid cells of one level; F_S0ECART and the s0 cart field are filled by the caller
+void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform) {
     launch(c, rg_grow(c, 0), 1, k_modify_scal_force, c.V(), comp, s0cart_fid, fullform, make_recip(c.P.dx[0]),
            make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
-    fill_patch(c, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
 }
 
 // MakeRhoHForce, planar 3-D (Source/MaestroForce.cpp:602-627)
@@ -1164,28 +1112,13 @@ __global__ void k_rhoh_force(KARGS, int cutoff, int domhi, RecipC rdz, int psi_i
     at(VW(F_SCALFORCE), i, j, k, RHOH) = f;
 }
 
-void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal, int which_step) {
-    // which_step 1: rho0 = rho0_old, p0 = p0_old (which_step 2 averages old and new)
-    (void)which_step;
-    const char* r0 = "rho0_old";
-    const char* p0 = "p0_old";
-    set_val(c, F_P0CART, 0.0, 0, 1, 1);
-    put1d(c, F_P0CART, c.b1(p0), 0, 0);
-    fill_patch(c, F_P0CART, 0, 1, BCS_F, 0, 0, -1);
-    set_val(c, F_PSICART, 0.0, 0, 1, 1);
-    put1d(c, F_PSICART, c.b1("psi"), 0, 0);
-    fill_patch(c, F_PSICART, 0, 1, BCS_F, 0, 0, -1);
-    set_val(c, F_RHO0CART, 0.0, 0, 1, 1);
-    put1d(c, F_RHO0CART, c.b1(r0), 0, 0);
-    fill_patch(c, F_RHO0CART, 0, 1, BCS_S, RHO, 0, RHO);
-    set_val(c, F_GRAVCART, 0.0, 0, 3, 1);
-    put1d(c, F_GRAVCART, c.b1("grav_cell"), 2, 0);
-    fill_patch(c, F_GRAVCART, 0, 3, BCS_F, 0, 0, -1);
+// valid cells of one level; F_P0CART, F_PSICART, F_RHO0CART and F_GRAVCART are filled by
+// the caller (which_step 1: rho0_old and p0_old)
+void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal) {
     const int ept = c.P.enthalpy_pred_type;
     const int psi_in = (is_prediction == 1 && ept == 2) || (is_prediction == 1 && ept == 0) || (is_prediction == 0);
     launch(c, rg_grow(c, 0), 1, k_rhoh_force, c.V(), c.P.base_cutoff_density_coord, c.P.dom_hi[2],
            make_recip(c.P.dx[2]), psi_in, add_thermal);
-    fill_patch(c, F_SCALFORCE, RHOH, 1, BCS_F, 0, 0, RHOH);
 }
 
 // ============================================================ conversions
@@ -1196,9 +1129,8 @@ __global__ void k_pert(KARGS, int comp, const double* __restrict__ s0, int flag)
     a = flag ? a - s0[k] : a + s0[k];
 }
 
-void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int bccomp, int which_bcs, int flag) {
+void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag) {
     launch(c, rg_grow(c, 0), 1, k_pert, c.V(), comp, d_s0, flag);
-    fill_patch(c, F_SOLD, comp, 1, which_bcs, bccomp, 0, comp);
 }
 
 // ConvertRhoXToX (Source/MaestroConvert.cpp:64-91), valid region
@@ -1213,8 +1145,6 @@ __global__ void k_rhox_to_x(KARGS, int nspec, int flag) {
 
 void convert_rhox_to_x(Ctx& c, int flag) {
     launch(c, rg_grow(c, 0), 1, k_rhox_to_x, c.V(), c.nspec, flag);
-    if (flag) fill_patch(c, F_SOLD, FIRSTSPEC, c.nspec, BCS_F, 0, 0, FIRSTSPEC);
-    else fill_patch(c, F_SOLD, FIRSTSPEC, c.nspec, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
 }
 
 // ============================================================ fluxes
@@ -1356,12 +1286,9 @@ void update_scal(Ctx& c, int start_comp) {
     if (start_comp == RHOH) {
         launch(c, rt, 1, k_update_rhoh, c.V(), c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
                make_recip(c.P.dx[2]), c.P.do_eos_h_above_cutoff, c.P.base_cutoff_density, c.d_flag);
-        fill_patch(c, F_SNEW, RHOH, 1, BCS_S, RHOH, 0, RHOH);
     } else {
         launch(c, rt, 1, k_update_rhox, c.V(), c.nspec, c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
                make_recip(c.P.dx[2]), 0.5 * c.P.base_cutoff_density);
-        fill_patch(c, F_SNEW, FIRSTSPEC, c.nspec, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
-        fill_patch(c, F_SNEW, RHO, 1, BCS_S, RHO, 0, RHO);
     }
 }
 

@@ -154,6 +154,45 @@ class ScalarAdvectionStage:
         bs = MadvBaseState(*[_dptr(a) for a in keep])
         check(lib().madv_set_base_state(self.ctx, C.byref(bs)))
 
+    def set_layout_levels(self, level_boxes):
+        """grids[lev] of an AMR hierarchy (level-l index space, refinement ratio 2)."""
+        allb = [b for boxes in level_boxes for b in boxes]
+        arr = (MadvBox * len(allb))()
+        for b, bx in enumerate(allb):
+            for d in range(3):
+                arr[b].lo[d] = int(bx[d])
+                arr[b].hi[d] = int(bx[3 + d])
+        nb = (C.c_int * len(level_boxes))(*[len(b) for b in level_boxes])
+        self.level_boxes = [[tuple(b) for b in boxes] for boxes in level_boxes]
+        check(lib().madv_set_layout_levels(self.ctx, len(level_boxes), nb, arr))
+
+    def set_base_state_levels(self, levels):
+        """levels[l]: dict with level l's 1-D arrays (rho0_old ... rho0_predicted_edge)."""
+        names = ("rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new", "p0_old", "p0_new", "psi", "grav_cell",
+                 "w0_force", "w0", "rho0_predicted_edge")
+        self._bs_keep = [[np.ascontiguousarray(L[n], dtype=np.float64) for n in names] for L in levels]
+        arr = (MadvBaseState * len(levels))()
+        for l, keep in enumerate(self._bs_keep):
+            arr[l] = MadvBaseState(*[_dptr(a) for a in keep])
+        check(lib().madv_set_base_state_levels(self.ctx, len(levels), arr))
+
+    def stage_forward_levels(self, bufs, mode=capi.MODE_BATCHED, stream=None):
+        """The stage on all levels; bufs[l] holds level l's MultiFabs (StageBuffers)."""
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        nl = len(bufs)
+
+        def cells(name):
+            return (MadvMultiFab * nl)(*[getattr(b, name).desc() for b in bufs])
+
+        def faces(name):
+            return (MadvMultiFab * (3 * nl))(*[getattr(b, name)[d].desc() for b in bufs for d in range(3)])
+
+        args = [cells("uold"), cells("sold"), cells("gpi"), cells("thermal"), cells("snew"), faces("umac"),
+                faces("sedge"), faces("sflux"), cells("eta")]
+        self._fwd_keep = args
+        P = C.POINTER(MadvMultiFab)
+        check(lib().madv_stage_forward_levels(self.ctx, mode, nl, *[C.cast(a, P) for a in args], C.c_void_p(s)))
+
     def set_dt(self, dt, rel_eps):
         check(lib().madv_set_dt(self.ctx, dt, rel_eps))
 
@@ -254,5 +293,46 @@ def run_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
         etarhoflux=buf.eta.to_domain(n)[0].cpu().numpy(),
         launches=st.launch_count(),
     )
+    st.close()
+    return res
+
+
+def make_amr_stage(cfg):
+    """Context for a two-level configuration (configs.planar_amr_config)."""
+    from .params import make_params
+    st = ScalarAdvectionStage(make_params(cfg))
+    st.set_layout_levels([L["boxes"] for L in cfg["levels"]])
+    st.set_base_state_levels(cfg["levels"])
+    return st
+
+
+def amr_buffers(cfg, device="cuda"):
+    """One StageBuffers per level, loaded with the level's input arrays."""
+    out = []
+    for L in cfg["levels"]:
+        c = dict(cfg)
+        c.update(L)
+        out.append(StageBuffers(c, device).load(c))
+    return out
+
+
+def run_amr_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
+    """The stage on every level of cfg["levels"]; returns one dict of domain arrays per level."""
+    st = make_amr_stage(cfg)
+    bufs = amr_buffers(cfg, device)
+    st.stage_forward_levels(bufs, mode=mode)
+    torch.cuda.synchronize()
+    res = []
+    for L, buf in zip(cfg["levels"], bufs):
+        n = L["n"]
+        res.append(dict(
+            umac_end=[buf.umac[d].to_domain(n)[0].cpu().numpy() for d in range(3)],
+            sedge=[buf.sedge[d].to_domain(n).cpu().numpy() for d in range(3)],
+            sflux=[buf.sflux[d].to_domain(n).cpu().numpy() for d in range(3)],
+            snew=buf.snew.to_domain(n).cpu().numpy(),
+            sold_end=buf.sold.to_domain(n).cpu().numpy(),
+            etarhoflux=buf.eta.to_domain(n)[0].cpu().numpy(),
+        ))
+    res[0]["launches"] = st.launch_count()
     st.close()
     return res

@@ -13,7 +13,7 @@
 #include <cstring>
 #include <string>
 
-#include "mo_fill.hpp"
+#include "mo_amr.hpp"
 #include "mo_ppm.hpp"
 
 #ifdef _OPENMP
@@ -24,9 +24,13 @@ namespace mo {
 
 static thread_local std::string g_err;
 
-struct Stage {
+// One AMR level of the stage: the per-level bodies of the reference functions.  The
+// coarse-fine synchronisation the reference runs between them (AverageDown, FillPatch,
+// AverageDownFaces, FillPatchUedge) lives in Stage below.
+struct Lev {
     mo_params P;
     Level L;
+    int lev = 0, cutoff = 0;  // level index, base_cutoff_density_coord(lev)
     int nspec = 0, nscal = 0, nb = 0, nr = 0;
     int ng_s = 3, ng_adv = 3;
     std::vector<BCRec> bcs_s, bcs_u, bcs_f;
@@ -64,10 +68,9 @@ struct Stage {
         }
     }
 
-    // Maestro::Put1dArrayOnCart, planar branch (Source/MaestroFill3dData.cpp:9-93):
-    // valid cells from the 1-D array, then FillPatch of the ghost cells.
-    void Put1dArrayOnCart(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec,
-                          const std::vector<BCRec>* bcs, int bccomp, bool is_vel) {
+    // Maestro::Put1dArrayOnCart, planar branch, one level (Source/MaestroFill3dData.cpp:42-93):
+    // valid cells from the level's 1-D array.
+    void Put1d(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec) {
         const int outcomp = vec ? 2 : 0;
         for (int b = 0; b < nb; ++b) {
             const Arr& a = s0_cart[b];
@@ -76,17 +79,12 @@ struct Stage {
                 a(i, j, k, outcomp) = edge ? 0.5 * (s0[r] + s0[r + 1]) : s0[r];
             }
         }
-        if (s0_cart.ng > 0) {
-            int nc = vec ? 3 : 1;
-            FillPatch(L, s0_cart, 0, nc, bccomp, *bcs, is_vel);
-        }
     }
 
-    // Maestro::CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), one level, one chunk.
-    static void CelltoEdge(const std::vector<double>& c, std::vector<double>& e) {
+    // Maestro::CelltoEdge (Source/MaestroCelltoEdge.cpp:17-54) on one chunk [lo, hi] of
+    // edges of a level with nr_lev cells; edges outside the chunk are left alone.
+    static void CelltoEdgeChunk(const std::vector<double>& c, std::vector<double>& e, int lo, int hi) {
         const int nr_lev = (int)c.size();
-        e.assign(nr_lev + 1, 0.0);
-        const int lo = 0, hi = nr_lev;
         for (int r = lo; r <= hi; ++r) {
             if (r == 0) {
                 e[r] = c[r];
@@ -103,6 +101,11 @@ struct Stage {
                 e[r] = mn(mx(tmp, s0min), s0max);
             }
         }
+    }
+    // one level, one chunk spanning the level
+    static void CelltoEdge(const std::vector<double>& c, std::vector<double>& e) {
+        e.assign(c.size() + 1, 0.0);
+        CelltoEdgeChunk(c, e, 0, (int)c.size());
     }
 
     // ------------------------------------------------------------------ face ghosts
@@ -180,23 +183,17 @@ struct Stage {
         }
     }
 
-    void FillFaceGhosts(MF* um) {
-        for (int d = 0; d < 3; ++d) FillBoundary(L, um[d], 0, 1, um[d].ng);
-        FillUmacGhost(um);
-    }
-
-    // Maestro::Addw0, planar (Source/MaestroFill3dData.cpp:357-462)
+    // Maestro::Addw0, planar, one level (Source/MaestroFill3dData.cpp:365-423)
     void Addw0(MF* uedge, double mult) {
         for (int b = 0; b < nb; ++b) {
             const Arr& wedge = uedge[2][b];
             Box zbx = grow(grow(nodal(L.ba[b], 2), 0, 1), 1, 1);
             MO_FOR3(zbx) { wedge(i, j, k) += mult * w0[k]; }
         }
-        FillFaceGhosts(uedge);
     }
 
     // ------------------------------------------------------------------ MakeUtrans
-    // Maestro::MakeUtrans, 3-D (Source/MaestroMakeUtrans.cpp:6-56, 270-648)
+    // Maestro::MakeUtrans, 3-D, one level (Source/MaestroMakeUtrans.cpp:6-56, 270-628)
     void MakeUtrans(MF& utilde, MF& ufull, MF* utrans) {
         const double dt2 = 0.5 * dt;
         const int* domlo = L.dom.lo;
@@ -264,17 +261,11 @@ struct Stage {
                 }
             }
         }
-        FillFaceGhosts(utrans);
     }
 
     // ------------------------------------------------------------------ MakeVelForce
-    // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-126, 250-259)
-    void MakeVelForce(MF& vel_force, MF* uedge, MF& sold, MF& w0_force_cart) {
-        MF grav_cart, rho0_cart;
-        grav_cart.define(L.ba, 3, 1, -1, 0.0);
-        rho0_cart.define(L.ba, 1, 1, -1, 0.0);
-        Put1dArrayOnCart(rho0_old, rho0_cart, false, false, &bcs_s, Rho, false);
-        Put1dArrayOnCart(grav_cell, grav_cart, false, true, &bcs_f, 0, false);
+    // Maestro::MakeVelForce, planar, one level (Source/MaestroForce.cpp:58-126)
+    void MakeVelForce(MF& vel_force, MF* uedge, MF& sold, MF& w0_force_cart, MF& grav_cart, MF& rho0_cart) {
         vel_force.setVal(0.0);
         const int domhi = L.dom.hi[2];
         for (int b = 0; b < nb; ++b) {
@@ -298,11 +289,10 @@ struct Stage {
                 }
             }
         }
-        FillPatch(L, vel_force, 0, 3, 0, bcs_u, true);
     }
 
     // ------------------------------------------------------------------ VelPred
-    // Maestro::VelPred, 3-D (Source/MaestroVelPred.cpp:5-292, 735-1915)
+    // Maestro::VelPred, 3-D, one level (Source/MaestroVelPred.cpp:5-288, 735-1915)
     void VelPred(MF& utilde, MF& ufull, MF* utrans, MF* umac, MF& force) {
         const double dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt6 = dt / 6.0;
         const int* domlo = L.dom.lo;
@@ -525,31 +515,6 @@ struct Stage {
                 }
             }
         }
-    }
-
-    // ------------------------------------------------------------------ AdvancePremac
-    // Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84)
-    void AdvancePremac(MF& uold, MF& sold, MF* umac, MF& w0_force_cart, MF* utrans, MF& vel_force) {
-        MF utilde, ufull;
-        utilde.define(L.ba, 3, ng_adv, -1, 0.0);
-        for (int b = 0; b < nb; ++b) {
-            MO_FOR3(L.ba[b]) for (int n = 0; n < 3; ++n) utilde[b](i, j, k, n) = uold[b](i, j, k, n);
-        }
-        FillPatch(L, utilde, 0, 3, 0, bcs_u, true);
-        ufull.define(L.ba, 3, ng_adv, -1, 0.0);
-        for (int b = 0; b < nb; ++b) {
-            MO_FOR3(L.ba[b]) for (int n = 0; n < 3; ++n) ufull[b](i, j, k, n) = w0_cart[b](i, j, k, n);
-        }
-        FillPatch(L, ufull, 0, 3, 0, bcs_u, true);
-        for (int b = 0; b < nb; ++b) {
-            MO_FOR3(grow(L.ba[b], ng_adv)) for (int n = 0; n < 3; ++n) ufull[b](i, j, k, n) += utilde[b](i, j, k, n);
-        }
-        for (int d = 0; d < 3; ++d) utrans[d].define(L.ba, 1, 1, d, 0.0);
-        MakeUtrans(utilde, ufull, utrans);
-        vel_force.define(L.ba, 3, 1, -1, 0.0);
-        MakeVelForce(vel_force, utrans, sold, w0_force_cart);
-        Addw0(utrans, 1.0);
-        VelPred(utilde, ufull, utrans, umac, vel_force);
     }
 
     // ------------------------------------------------------------------ MakeEdgeScal
@@ -807,12 +772,9 @@ struct Stage {
     }
 
     // ------------------------------------------------------------------ forces
-    // Maestro::ModifyScalForce, planar 3-D (Source/MaestroForce.cpp:261-467)
-    void ModifyScalForce(MF& scal_force, MF& state, MF* umac, const std::vector<double>& s0_edge, MF& s0_cart,
-                         int comp, int fullform) {
-        MF s0_edge_cart;
-        s0_edge_cart.define(L.ba, 1, 1);
-        Put1dArrayOnCart(s0_edge, s0_edge_cart, false, false, &bcs_f, 0, false);
+    // Maestro::ModifyScalForce, planar 3-D, one level (Source/MaestroForce.cpp:261-453)
+    void ModifyScalForce(MF& scal_force, MF& state, MF* umac, MF& s0_edge_cart, MF& s0_cart, int comp,
+                         int fullform) {
         const double* dx = L.dx;
         for (int b = 0; b < nb; ++b) {
             const Arr scal = state[b].comp(comp);
@@ -837,27 +799,12 @@ struct Stage {
                 }
             }
         }
-        FillPatch(L, scal_force, comp, 1, 0, bcs_f, false);
     }
 
-    // Maestro::MakeRhoHForce, planar 3-D (Source/MaestroForce.cpp:469-679)
-    void MakeRhoHForce(MF& scal_force, int is_prediction, MF* umac, int add_thermal, int which_step) {
-        std::vector<double> r0(nr), pp0(nr);
-        for (int r = 0; r < nr; ++r) {
-            r0[r] = which_step == 1 ? rho0_old[r] : 0.5 * (rho0_old[r] + rho0_new[r]);
-            pp0[r] = which_step == 1 ? p0_old[r] : 0.5 * (p0_old[r] + p0_new[r]);
-        }
-        MF p0_cart, psi_cart, grav_cart, rho0_cart;
-        p0_cart.define(L.ba, 1, 1, -1, 0.0);
-        psi_cart.define(L.ba, 1, 1, -1, 0.0);
-        grav_cart.define(L.ba, 1, 1, -1, 0.0);
-        rho0_cart.define(L.ba, 1, 1, -1, 0.0);
-        Put1dArrayOnCart(pp0, p0_cart, false, false, &bcs_f, 0, false);
-        Put1dArrayOnCart(psi, psi_cart, false, false, &bcs_f, 0, false);
-        Put1dArrayOnCart(r0, rho0_cart, false, false, &bcs_s, Rho, false);
-        Put1dArrayOnCart(grav_cell, grav_cart, false, false, &bcs_f, 0, false);  // MakeGravCell, planar constant
+    // Maestro::MakeRhoHForce, planar 3-D, one level (Source/MaestroForce.cpp:541-674)
+    void MakeRhoHForce(MF& scal_force, int is_prediction, MF* umac, int add_thermal, MF& p0_cart, MF& psi_cart,
+                       MF& grav_cart, MF& rho0_cart) {
         const int domhi = L.dom.hi[2];
-        const int cutoff = P.base_cutoff_density_coord;
         const bool psi_in = (is_prediction == 1 && P.enthalpy_pred_type == 2) ||
                             (is_prediction == 1 && P.enthalpy_pred_type == 0) || (is_prediction == 0);
         for (int b = 0; b < nb; ++b) {
@@ -883,13 +830,11 @@ struct Stage {
                 if (add_thermal == 1) rf(i, j, k) += th(i, j, k);
             }
         }
-        FillPatch(L, scal_force, RhoH, 1, 0, bcs_f, false);
     }
 
     // ------------------------------------------------------------------ conversions
-    // Maestro::PutInPertForm (Source/MaestroConvert.cpp:6-34)
-    void PutInPertForm(MF& scal, const std::vector<double>& s0, int comp, int bccomp, const std::vector<BCRec>& bcs,
-                       bool flag) {
+    // Maestro::PutInPertForm, one level (Source/MaestroConvert.cpp:6-30)
+    void PutInPertForm(MF& scal, const std::vector<double>& s0, int comp, bool flag) {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = scal[b];
             MO_FOR3(L.ba[b]) {
@@ -898,10 +843,9 @@ struct Stage {
                 else a(i, j, k, comp) = a(i, j, k, comp) + s0c;
             }
         }
-        FillPatch(L, scal, comp, 1, bccomp, bcs, false, comp);
     }
 
-    // Maestro::ConvertRhoXToX (Source/MaestroConvert.cpp:64-91)
+    // Maestro::ConvertRhoXToX, one level (Source/MaestroConvert.cpp:64-81)
     void ConvertRhoXToX(MF& scal, bool flag) {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = scal[b];
@@ -911,8 +855,6 @@ struct Stage {
                     else a(i, j, k, comp) = a(i, j, k, comp) * a(i, j, k, Rho);
                 }
         }
-        if (flag) FillPatch(L, scal, FirstSpec, nspec, 0, bcs_f, false, FirstSpec);
-        else FillPatch(L, scal, FirstSpec, nspec, FirstSpec, bcs_s, false, FirstSpec);
     }
 
     // ------------------------------------------------------------------ fluxes
@@ -976,7 +918,7 @@ struct Stage {
     }
 
     // ------------------------------------------------------------------ UpdateScal
-    // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297), one level
+    // Maestro::UpdateScal, one level (Source/MaestroAdvection.cpp:86-256)
     void UpdateScal(MF& sold, MF& snew, MF* sflux, MF& force, int start_comp, int num_comp) {
         const double* dx = L.dx;
         const double dt_loc = dt;
@@ -1038,74 +980,352 @@ struct Stage {
             }
         }
         (void)num_comp;
-        FillPatch(L, snew, start_comp, num_comp, start_comp, bcs_s, false, start_comp);
-        if (start_comp == FirstSpec) FillPatch(L, snew, Rho, 1, Rho, bcs_s, false, Rho);
+    }
+
+};
+
+using VMF = std::vector<MF>;                // one MultiFab per level
+using VF = std::vector<std::array<MF, 3>>;  // face MultiFabs per level
+using BS = std::vector<std::vector<double>>;  // a base-state array per level
+
+// The stage over all levels, with the coarse-fine synchronisation of the reference:
+// AverageDown + FillPatch after every cell-centred update, AverageDownFaces + FillPatchUedge
+// for face velocities, AverageDownFaces for fluxes (reflux_type 1, the default).
+struct Stage {
+    mo_params P;
+    int nlev = 1, nspec = 0, nscal = 0, ng_s = 3, ng_adv = 3;
+    std::vector<Lev> S;
+    std::vector<std::vector<std::array<int, 2>>> chunks;  // per level: radial cell ranges
+
+    const std::vector<BCRec>& bcs_s() const { return S[0].bcs_s; }
+    const std::vector<BCRec>& bcs_u() const { return S[0].bcs_u; }
+    const std::vector<BCRec>& bcs_f() const { return S[0].bcs_f; }
+    BS bs(std::vector<double> Lev::*m) const {
+        BS r(nlev);
+        for (int l = 0; l < nlev; ++l) r[l] = S[l].*m;
+        return r;
+    }
+
+    // ------------------------------------------------------------------ level sync
+    // Maestro::FillPatch over all levels (Source/MaestroFillData.cpp:7-74)
+    void FillPatch(VMF& mf, int c0, int nc, int bccomp, const std::vector<BCRec>& bcs, bool is_vel, int sc0 = -1) {
+        for (int lev = 0; lev < nlev; ++lev) {
+            if (lev == 0) mo::FillPatch(S[0].L, mf[0], c0, nc, bccomp, bcs, is_vel, sc0);
+            else FillPatchTwoLevels(S[lev - 1].L, mf[lev - 1], S[lev].L, mf[lev], c0, nc, bccomp, bcs, is_vel, sc0);
+        }
+    }
+    // Maestro::AverageDown (Source/MaestroFillData.cpp:145-154)
+    void AverageDown(VMF& mf, int comp, int ncomp) {
+        for (int lev = nlev - 2; lev >= 0; --lev)
+            mo::AverageDown(S[lev + 1].L, mf[lev + 1], S[lev].L, mf[lev], comp, ncomp);
+    }
+    // Maestro::AverageDownFaces (Source/MaestroFillData.cpp:156-174)
+    void AverageDownFaces(VF& f) {
+        for (int lev = nlev - 2; lev >= 0; --lev) mo::AverageDownFaces(S[lev + 1].L, f[lev + 1], S[lev].L, f[lev]);
+    }
+    // Maestro::FillPatchUedge (Source/MaestroFillData.cpp:455-835)
+    void FillPatchUedge(VF& u) {
+        for (int lev = 0; lev < nlev; ++lev) {
+            if (lev > 0)
+                for (int d = 0; d < 3; ++d) {
+                    UedgeInterface ui(S[lev - 1].L, S[lev].L, u[lev - 1][d], u[lev][d], d);
+                    ui.apply(u[lev][d]);
+                }
+            for (int d = 0; d < 3; ++d) FillBoundary(S[lev].L, u[lev][d], 0, 1, u[lev][d].ng);
+            S[lev].FillUmacGhost(u[lev].data());
+        }
+    }
+    // the face-velocity ghost fill that closes MakeUtrans and Addw0
+    // (Source/MaestroMakeUtrans.cpp:631-647, Source/MaestroFill3dData.cpp:425-461)
+    void SyncFaces(VF& u) {
+        if (nlev == 1) {
+            for (int d = 0; d < 3; ++d) FillBoundary(S[0].L, u[0][d], 0, 1, u[0][d].ng);
+            S[0].FillUmacGhost(u[0].data());
+        } else {
+            AverageDownFaces(u);
+            FillPatchUedge(u);
+        }
+    }
+
+    // ------------------------------------------------------------------ base state
+    // Maestro::Put1dArrayOnCart, planar (Source/MaestroFill3dData.cpp:9-36)
+    void Put1dArrayOnCart(const BS& s0, VMF& s0_cart, bool edge, bool vec, const std::vector<BCRec>* bcs, int bccomp,
+                          bool is_vel) {
+        for (int lev = 0; lev < nlev; ++lev) S[lev].Put1d(s0[lev], s0_cart[lev], edge, vec);
+        const int nc = vec ? 3 : 1;
+        AverageDown(s0_cart, 0, nc);
+        if (s0_cart[0].ng > 0) FillPatch(s0_cart, 0, nc, bccomp, *bcs, is_vel);
+    }
+    // Maestro::CelltoEdge over the chunks of every level, then RestrictBase of the edges
+    // (Source/MaestroCelltoEdge.cpp:17-58, Source/MaestroBaseStateGeometry.cpp:240-262)
+    void CelltoEdge(const BS& c, BS& e) const {
+        e.assign(nlev, {});
+        for (int n = 0; n < nlev; ++n) {
+            e[n].assign(c[n].size() + 1, 0.0);
+            for (auto& ch : chunks[n]) Lev::CelltoEdgeChunk(c[n], e[n], ch[0], ch[1] + 1);
+        }
+        for (int n = nlev - 1; n >= 1; --n)
+            for (auto& ch : chunks[n])
+                for (int j = ch[0]; j <= ch[1] + 1; j += 2) e[n - 1][j / 2] = e[n][j];
+    }
+    // BaseStateGeometry::InitMultiLevel, planar (Source/BaseStateGeometry.cpp:355-382), with the
+    // radial rows of level n - 1 tagged wherever a level-n box lies above them.
+    void InitChunks() {
+        chunks.assign(nlev, {});
+        chunks[0].push_back({0, S[0].nr - 1});
+        for (int n = 1; n < nlev; ++n) {
+            const int nrc = S[n - 1].nr;
+            std::vector<int> tag(nrc, 0);
+            for (const Box& b : S[n].L.ba)
+                for (int r = b.lo[2]; r <= b.hi[2]; ++r) tag[r / 2] = 1;
+            bool in = false;
+            for (int r = 0; r < nrc; ++r) {
+                if (tag[r] && !in) {
+                    in = true;
+                    chunks[n].push_back({2 * r, 0});
+                } else if (!tag[r] && in) {
+                    chunks[n].back()[1] = 2 * r - 1;
+                    in = false;
+                }
+                if (in && r == nrc - 1) chunks[n].back()[1] = 2 * r + 1;
+            }
+        }
+    }
+    // BaseStateGeometry::ComputeCutoffCoords, base cutoff only (Source/BaseStateGeometry.cpp:164-210)
+    void ComputeCutoffCoords() {
+        bool found = false;
+        int which = 0;
+        std::vector<int> coord(nlev, 0);
+        for (int n = nlev - 1; n >= 0; --n)
+            for (auto& ch : chunks[n]) {
+                if (found) break;
+                for (int r = ch[0]; r <= ch[1]; ++r)
+                    if (S[n].rho0_old[r] <= P.base_cutoff_density) {
+                        coord[n] = r;
+                        which = n;
+                        found = true;
+                        break;
+                    }
+            }
+        if (!found) {
+            which = nlev - 1;
+            coord[which] = S[which].nr;
+        }
+        for (int n = which + 1; n < nlev; ++n) coord[n] = 2 * coord[n - 1] + 1;
+        for (int n = which - 1; n >= 0; --n) coord[n] = coord[n + 1] % 2 == 0 ? coord[n + 1] / 2 : coord[n + 1] / 2 + 1;
+        for (int n = 0; n < nlev; ++n) S[n].cutoff = coord[n];
+    }
+
+    // ------------------------------------------------------------------ AdvancePremac
+    void MakeUtrans(VMF& utilde, VMF& ufull, VF& utrans) {
+        for (int lev = 0; lev < nlev; ++lev) S[lev].MakeUtrans(utilde[lev], ufull[lev], utrans[lev].data());
+        SyncFaces(utrans);
+    }
+    void Addw0(VF& u, double mult) {
+        for (int lev = 0; lev < nlev; ++lev) S[lev].Addw0(u[lev].data(), mult);
+        SyncFaces(u);
+    }
+    // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-259)
+    void MakeVelForce(VMF& vel_force, VF& uedge, VMF& sold, VMF& w0_force_cart) {
+        VMF grav_cart(nlev), rho0_cart(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            grav_cart[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+            rho0_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+        }
+        Put1dArrayOnCart(bs(&Lev::rho0_old), rho0_cart, false, false, &bcs_s(), Rho, false);
+        Put1dArrayOnCart(bs(&Lev::grav_cell), grav_cart, false, true, &bcs_f(), 0, false);
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].MakeVelForce(vel_force[lev], uedge[lev].data(), sold[lev], w0_force_cart[lev], grav_cart[lev],
+                                rho0_cart[lev]);
+        AverageDown(vel_force, 0, 3);
+        FillPatch(vel_force, 0, 3, 0, bcs_u(), true);
+    }
+    void VelPred(VMF& utilde, VMF& ufull, VF& utrans, VF& umac, VMF& force) {
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].VelPred(utilde[lev], ufull[lev], utrans[lev].data(), umac[lev].data(), force[lev]);
+        AverageDownFaces(umac);
+    }
+    // Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84)
+    void AdvancePremac(VMF& uold, VMF& sold, VF& umac, VMF& w0_force_cart, VF& utrans, VMF& vel_force) {
+        VMF utilde(nlev), ufull(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Level& L = S[lev].L;
+            utilde[lev].define(L.ba, 3, ng_adv, -1, 0.0);
+            for (int b = 0; b < (int)L.ba.size(); ++b)
+                MO_FOR3(L.ba[b]) for (int n = 0; n < 3; ++n) utilde[lev][b](i, j, k, n) = uold[lev][b](i, j, k, n);
+        }
+        FillPatch(utilde, 0, 3, 0, bcs_u(), true);
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Level& L = S[lev].L;
+            ufull[lev].define(L.ba, 3, ng_adv, -1, 0.0);
+            for (int b = 0; b < (int)L.ba.size(); ++b)
+                MO_FOR3(L.ba[b]) for (int n = 0; n < 3; ++n) ufull[lev][b](i, j, k, n) = S[lev].w0_cart[b](i, j, k, n);
+        }
+        FillPatch(ufull, 0, 3, 0, bcs_u(), true);
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Level& L = S[lev].L;
+            for (int b = 0; b < (int)L.ba.size(); ++b)
+                MO_FOR3(grow(L.ba[b], ng_adv)) for (int n = 0; n < 3; ++n) ufull[lev][b](i, j, k, n) +=
+                    utilde[lev][b](i, j, k, n);
+            for (int d = 0; d < 3; ++d) utrans[lev][d].define(L.ba, 1, 1, d, 0.0);
+        }
+        MakeUtrans(utilde, ufull, utrans);
+        for (int lev = 0; lev < nlev; ++lev) vel_force[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+        MakeVelForce(vel_force, utrans, sold, w0_force_cart);
+        Addw0(utrans, 1.0);
+        VelPred(utilde, ufull, utrans, umac, vel_force);
+    }
+
+    // ------------------------------------------------------------------ scalars
+    void MakeEdgeScal(VMF& state, VF& sedge, VF& umac, VMF& force, const std::vector<BCRec>& bcs, int start_scomp,
+                      int start_bccomp, int num_comp, bool is_conservative) {
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].MakeEdgeScal(state[lev], sedge[lev].data(), umac[lev].data(), force[lev], bcs, start_scomp,
+                                start_bccomp, num_comp, is_conservative);
+    }
+    // Maestro::ModifyScalForce (Source/MaestroForce.cpp:261-467)
+    void ModifyScalForce(VMF& scal_force, VMF& state, VF& umac, const BS& s0_edge, VMF& s0_cart, int comp,
+                         int fullform) {
+        VMF s0_edge_cart(nlev);
+        for (int lev = 0; lev < nlev; ++lev) s0_edge_cart[lev].define(S[lev].L.ba, 1, 1);
+        Put1dArrayOnCart(s0_edge, s0_edge_cart, false, false, &bcs_f(), 0, false);
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].ModifyScalForce(scal_force[lev], state[lev], umac[lev].data(), s0_edge_cart[lev], s0_cart[lev], comp,
+                                   fullform);
+        AverageDown(scal_force, comp, 1);
+        FillPatch(scal_force, comp, 1, 0, bcs_f(), false);
+    }
+    // Maestro::MakeRhoHForce (Source/MaestroForce.cpp:469-679)
+    void MakeRhoHForce(VMF& scal_force, int is_prediction, VF& umac, int add_thermal, int which_step) {
+        BS r0(nlev), pp0(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Lev& L = S[lev];
+            r0[lev].resize(L.nr);
+            pp0[lev].resize(L.nr);
+            for (int r = 0; r < L.nr; ++r) {
+                r0[lev][r] = which_step == 1 ? L.rho0_old[r] : 0.5 * (L.rho0_old[r] + L.rho0_new[r]);
+                pp0[lev][r] = which_step == 1 ? L.p0_old[r] : 0.5 * (L.p0_old[r] + L.p0_new[r]);
+            }
+        }
+        VMF p0_cart(nlev), psi_cart(nlev), grav_cart(nlev), rho0_cart(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            p0_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+            psi_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+            grav_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+            rho0_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+        }
+        Put1dArrayOnCart(pp0, p0_cart, false, false, &bcs_f(), 0, false);
+        Put1dArrayOnCart(bs(&Lev::psi), psi_cart, false, false, &bcs_f(), 0, false);
+        Put1dArrayOnCart(r0, rho0_cart, false, false, &bcs_s(), Rho, false);
+        Put1dArrayOnCart(bs(&Lev::grav_cell), grav_cart, false, false, &bcs_f(), 0, false);  // MakeGravCell, planar
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].MakeRhoHForce(scal_force[lev], is_prediction, umac[lev].data(), add_thermal, p0_cart[lev],
+                                 psi_cart[lev], grav_cart[lev], rho0_cart[lev]);
+        AverageDown(scal_force, RhoH, 1);
+        FillPatch(scal_force, RhoH, 1, 0, bcs_f(), false);
+    }
+    // Maestro::PutInPertForm (Source/MaestroConvert.cpp:6-34)
+    void PutInPertForm(VMF& scal, const BS& s0, int comp, int bccomp, const std::vector<BCRec>& bcs, bool flag) {
+        for (int lev = 0; lev < nlev; ++lev) S[lev].PutInPertForm(scal[lev], s0[lev], comp, flag);
+        AverageDown(scal, comp, 1);
+        FillPatch(scal, comp, 1, bccomp, bcs, false, comp);
+    }
+    // Maestro::ConvertRhoXToX (Source/MaestroConvert.cpp:64-91)
+    void ConvertRhoXToX(VMF& scal, bool flag) {
+        for (int lev = 0; lev < nlev; ++lev) S[lev].ConvertRhoXToX(scal[lev], flag);
+        AverageDown(scal, FirstSpec, nspec);
+        if (flag) FillPatch(scal, FirstSpec, nspec, 0, bcs_f(), false, FirstSpec);
+        else FillPatch(scal, FirstSpec, nspec, FirstSpec, bcs_s(), false, FirstSpec);
+    }
+    // Maestro::MakeRhoXFlux (Source/MaestroMakeFlux.cpp:18-465)
+    void MakeRhoXFlux(VF& sflux, VMF& eta, VF& sedge, VF& umac, const BS& r0_old, const BS& r0e_old, const BS& r0_new,
+                      const BS& r0e_new, int start_comp, int num_comp) {
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].MakeRhoXFlux(sflux[lev].data(), eta[lev], sedge[lev].data(), umac[lev].data(), r0_old[lev],
+                                r0e_old[lev], r0_new[lev], r0e_new[lev], start_comp, num_comp);
+        AverageDownFaces(sflux);
+    }
+    // Maestro::MakeRhoHFlux (Source/MaestroMakeFlux.cpp:467-1067)
+    void MakeRhoHFlux(VF& sflux, VF& sedge, VF& umac, const BS& rh0_old, const BS& rh0e_old, const BS& rh0_new,
+                      const BS& rh0e_new) {
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].MakeRhoHFlux(sflux[lev].data(), sedge[lev].data(), umac[lev].data(), rh0_old[lev], rh0e_old[lev],
+                                rh0_new[lev], rh0e_new[lev]);
+        AverageDownFaces(sflux);
+    }
+    // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
+    void UpdateScal(VMF& sold, VMF& snew, VF& sflux, VMF& force, int start_comp, int num_comp) {
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].UpdateScal(sold[lev], snew[lev], sflux[lev].data(), force[lev], start_comp, num_comp);
+        AverageDown(snew, start_comp, num_comp);
+        FillPatch(snew, start_comp, num_comp, start_comp, bcs_s(), false, start_comp);
+        if (start_comp == FirstSpec) {
+            AverageDown(snew, Rho, 1);
+            FillPatch(snew, Rho, 1, Rho, bcs_s(), false, Rho);
+        }
     }
 
     // ------------------------------------------------------------------ drivers
     // Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243)
-    void DensityAdvance(MF& scalold, MF& scalnew, MF* sedge, MF* sflux, MF& scal_force, MF& etarhoflux, MF* umac) {
-        std::vector<double> rho0_edge_old, rho0_edge_new;
+    void DensityAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VMF& etarhoflux, VF& umac) {
+        const int spt = P.species_pred_type;
+        const BS rho0_old = bs(&Lev::rho0_old), rho0_new = bs(&Lev::rho0_new);
+        BS rho0_edge_old, rho0_edge_new;
         CelltoEdge(rho0_old, rho0_edge_old);
         CelltoEdge(rho0_new, rho0_edge_new);
-        scal_force.setVal(0.0);
-        MF rho0_old_cart;
-        rho0_old_cart.define(L.ba, 1, 1, -1, 0.0);
-        Put1dArrayOnCart(rho0_old, rho0_old_cart, false, false, &bcs_s, Rho, false);
+        for (auto& f : scal_force) f.setVal(0.0);
+        VMF rho0_old_cart(nlev);
+        for (int lev = 0; lev < nlev; ++lev) rho0_old_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+        Put1dArrayOnCart(rho0_old, rho0_old_cart, false, false, &bcs_s(), Rho, false);
         Addw0(umac, -1.0);
-        if (P.species_pred_type == 1) ModifyScalForce(scal_force, scalold, umac, rho0_edge_old, rho0_old_cart, Rho, 0);
-        else if (P.species_pred_type == 3) ModifyScalForce(scal_force, scalold, umac, rho0_edge_old, rho0_old_cart, Rho, 1);
+        if (spt == 1) ModifyScalForce(scal_force, scalold, umac, rho0_edge_old, rho0_old_cart, Rho, 0);
+        else if (spt == 3) ModifyScalForce(scal_force, scalold, umac, rho0_edge_old, rho0_old_cart, Rho, 1);
         Addw0(umac, 1.0);
-        if (P.species_pred_type == 1 || P.species_pred_type == 3) ConvertRhoXToX(scalold, true);
-        if (P.species_pred_type == 1) PutInPertForm(scalold, rho0_old, Rho, 0, bcs_f, true);
-        if (P.species_pred_type == 1 || P.species_pred_type == 3)
-            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, FirstSpec, FirstSpec, nspec, false);
-        else
-            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, FirstSpec, FirstSpec, nspec, true);
-        if (P.species_pred_type == 1 || P.species_pred_type == 3) {
-            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, Rho, Rho, 1, false);
+        if (spt == 1 || spt == 3) ConvertRhoXToX(scalold, true);
+        if (spt == 1) PutInPertForm(scalold, rho0_old, Rho, 0, bcs_f(), true);
+        MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s(), FirstSpec, FirstSpec, nspec, spt == 2);
+        if (spt == 1 || spt == 3) {
+            MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s(), Rho, Rho, 1, false);
         } else {
-            for (int d = 0; d < 3; ++d)
-                for (int b = 0; b < nb; ++b) {
-                    const Arr& e = sedge[d][b];
-                    MO_FOR3(nodal(L.ba[b], d)) {
-                        e(i, j, k, Rho) = e(i, j, k, FirstSpec);
-                        for (int ispec = 1; ispec < nspec; ++ispec) e(i, j, k, Rho) += e(i, j, k, FirstSpec + ispec);
+            for (int lev = 0; lev < nlev; ++lev)
+                for (int d = 0; d < 3; ++d)
+                    for (int b = 0; b < (int)S[lev].L.ba.size(); ++b) {
+                        const Arr& e = sedge[lev][d][b];
+                        MO_FOR3(nodal(S[lev].L.ba[b], d)) {
+                            e(i, j, k, Rho) = e(i, j, k, FirstSpec);
+                            for (int ispec = 1; ispec < nspec; ++ispec) e(i, j, k, Rho) += e(i, j, k, FirstSpec + ispec);
+                        }
                     }
-                }
         }
-        if (P.species_pred_type == 1) PutInPertForm(scalold, rho0_old, Rho, Rho, bcs_s, false);
-        if (P.species_pred_type == 1 || P.species_pred_type == 3) ConvertRhoXToX(scalold, false);
-        MakeRhoXFlux(sflux, etarhoflux, sedge, umac, rho0_old, rho0_edge_old, rho0_old, rho0_edge_old, FirstSpec,
-                     nspec);
-        scal_force.setVal(0.0);
+        if (spt == 1) PutInPertForm(scalold, rho0_old, Rho, Rho, bcs_s(), false);
+        if (spt == 1 || spt == 3) ConvertRhoXToX(scalold, false);
+        MakeRhoXFlux(sflux, etarhoflux, sedge, umac, rho0_old, rho0_edge_old, rho0_old, rho0_edge_old, FirstSpec, nspec);
+        for (auto& f : scal_force) f.setVal(0.0);
         UpdateScal(scalold, scalnew, sflux, scal_force, FirstSpec, nspec);
     }
 
     // Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352)
-    void EnthalpyAdvance(MF& scalold, MF& scalnew, MF* sedge, MF* sflux, MF& scal_force, MF* umac) {
-        std::vector<double> rho0_edge_old, rho0_edge_new, rhoh0_edge_old, rhoh0_edge_new;
-        CelltoEdge(rho0_old, rho0_edge_old);
-        CelltoEdge(rho0_new, rho0_edge_new);
+    void EnthalpyAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VF& umac) {
+        const int ept = P.enthalpy_pred_type;
+        const BS rhoh0_old = bs(&Lev::rhoh0_old), rhoh0_new = bs(&Lev::rhoh0_new);
+        BS rhoh0_edge_old, rhoh0_edge_new;
         CelltoEdge(rhoh0_old, rhoh0_edge_old);
         CelltoEdge(rhoh0_new, rhoh0_edge_new);
-        scal_force.setVal(0.0);
-        MF rhoh0_old_cart;
-        rhoh0_old_cart.define(L.ba, 1, 1, -1, 0.0);
+        for (auto& f : scal_force) f.setVal(0.0);
+        VMF rhoh0_old_cart(nlev);
+        for (int lev = 0; lev < nlev; ++lev) rhoh0_old_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
         Addw0(umac, -1.0);
-        if (P.enthalpy_pred_type == 1) {
-            MakeRhoHForce(scal_force, 1, umac, 1, 1);
-            Put1dArrayOnCart(rhoh0_old, rhoh0_old_cart, false, false, &bcs_s, RhoH, false);
+        MakeRhoHForce(scal_force, 1, umac, 1, 1);
+        if (ept == 1) {
+            Put1dArrayOnCart(rhoh0_old, rhoh0_old_cart, false, false, &bcs_s(), RhoH, false);
             ModifyScalForce(scal_force, scalold, umac, rhoh0_edge_old, rhoh0_old_cart, RhoH, 0);
-        } else {
-            MakeRhoHForce(scal_force, 1, umac, 1, 1);
         }
         Addw0(umac, 1.0);
-        if (P.enthalpy_pred_type == 1) PutInPertForm(scalold, rhoh0_old, RhoH, 0, bcs_f, true);
-        MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s, RhoH, RhoH, 1, P.enthalpy_pred_type == 0);
-        if (P.enthalpy_pred_type == 1) PutInPertForm(scalold, rhoh0_old, RhoH, RhoH, bcs_s, false);
+        if (ept == 1) PutInPertForm(scalold, rhoh0_old, RhoH, 0, bcs_f(), true);
+        MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s(), RhoH, RhoH, 1, ept == 0);
+        if (ept == 1) PutInPertForm(scalold, rhoh0_old, RhoH, RhoH, bcs_s(), false);
         MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_old, rhoh0_edge_old);
-        scal_force.setVal(0.0, RhoH, 1, 1);
+        for (auto& f : scal_force) f.setVal(0.0, RhoH, 1, 1);
         Addw0(umac, -1.0);
         MakeRhoHForce(scal_force, 0, umac, 0, 1);
         Addw0(umac, 1.0);
@@ -1150,110 +1370,143 @@ static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, do
     }
 }
 
-static int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out) {
-    Stage S;
-    S.P = *p;
-    S.nspec = p->nspec;
-    S.nscal = 4 + p->nspec;
-    for (int d = 0; d < 3; ++d) {
-        S.L.dom.lo[d] = p->dom_lo[d];
-        S.L.dom.hi[d] = p->dom_hi[d];
-        S.L.per[d] = (p->phys_bc_lo[d] == interior);
-        if ((p->phys_bc_lo[d] == interior) != (p->phys_bc_hi[d] == interior))
-            throw std::runtime_error("periodic direction needs interior on both sides");
-        S.L.dx[d] = p->dx[d];
-    }
+static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
+                     mo_outputs* out) {
+    if (nlev < 1 || nlev > 4) throw std::runtime_error("1 to 4 levels");
     if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
     if (p->use_exact_base_state) throw std::runtime_error("use_exact_base_state is spherical-only");
     if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
         throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
     if (!(p->species_pred_type >= 1 && p->species_pred_type <= 3))
         throw std::runtime_error("species_pred_type must be 1, 2 or 3");
-    for (int b = 0; b < nboxes; ++b) {
-        Box bx;
+    Stage H;
+    H.P = *p;
+    H.nlev = nlev;
+    H.nspec = p->nspec;
+    H.nscal = 4 + p->nspec;
+    H.ng_s = H.ng_adv = p->ppm_type == 2 ? 4 : 3;
+    H.S.resize(nlev);
+    int off = 0;
+    for (int lev = 0; lev < nlev; ++lev) {
+        Lev& S = H.S[lev];
+        S.P = *p;
+        S.lev = lev;
+        S.nspec = H.nspec;
+        S.nscal = H.nscal;
+        const int r = 1 << lev;
         for (int d = 0; d < 3; ++d) {
-            bx.lo[d] = boxes[6 * b + d];
-            bx.hi[d] = boxes[6 * b + 3 + d];
+            S.L.dom.lo[d] = p->dom_lo[d] * r;
+            S.L.dom.hi[d] = (p->dom_hi[d] + 1) * r - 1;
+            S.L.per[d] = (p->phys_bc_lo[d] == interior);
+            if ((p->phys_bc_lo[d] == interior) != (p->phys_bc_hi[d] == interior))
+                throw std::runtime_error("periodic direction needs interior on both sides");
+            S.L.dx[d] = p->dx[d] / r;
         }
-        S.L.ba.push_back(bx);
+        for (int b = 0; b < nboxes[lev]; ++b) {
+            Box bx;
+            for (int d = 0; d < 3; ++d) {
+                bx.lo[d] = boxes[6 * (off + b) + d];
+                bx.hi[d] = boxes[6 * (off + b) + 3 + d];
+            }
+            S.L.ba.push_back(bx);
+        }
+        off += nboxes[lev];
+        S.nb = nboxes[lev];
+        S.nr = S.L.dom.hi[2] - S.L.dom.lo[2] + 1;
+        S.ng_s = S.ng_adv = H.ng_s;
+        S.dt = p->dt;
+        S.rel_eps = p->rel_eps;
+        S.pc = PPMCtx{p->ppm_type, p->dt, p->rel_eps, {S.L.dx[0], S.L.dx[1], S.L.dx[2]}, S.L.dom};
+        S.BCSetup();
+        const int nr = S.nr;
+        auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
+        const mo_inputs& I = in[lev];
+        S.rho0_old = vec(I.rho0_old, nr);
+        S.rho0_new = vec(I.rho0_new, nr);
+        S.rhoh0_old = vec(I.rhoh0_old, nr);
+        S.rhoh0_new = vec(I.rhoh0_new, nr);
+        S.p0_old = vec(I.p0_old, nr);
+        S.p0_new = vec(I.p0_new, nr);
+        S.psi = vec(I.psi, nr);
+        S.grav_cell = vec(I.grav_cell, nr);
+        S.w0_force = vec(I.w0_force, nr);
+        S.w0 = vec(I.w0, nr + 1);
+        S.rho0_predicted_edge = vec(I.rho0_predicted_edge, nr + 1);
+        S.cutoff = p->base_cutoff_density_coord;
     }
-    S.nb = nboxes;
-    S.nr = p->dom_hi[2] - p->dom_lo[2] + 1;
-    S.ng_s = p->ppm_type == 2 ? 4 : 3;
-    S.ng_adv = p->ppm_type == 2 ? 4 : 3;
-    S.dt = p->dt;
-    S.rel_eps = p->rel_eps;
-    S.pc = PPMCtx{p->ppm_type, p->dt, p->rel_eps, {p->dx[0], p->dx[1], p->dx[2]}, S.L.dom};
-    S.BCSetup();
-    const int nr = S.nr;
-    auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
-    S.rho0_old = vec(in->rho0_old, nr);
-    S.rho0_new = vec(in->rho0_new, nr);
-    S.rhoh0_old = vec(in->rhoh0_old, nr);
-    S.rhoh0_new = vec(in->rhoh0_new, nr);
-    S.p0_old = vec(in->p0_old, nr);
-    S.p0_new = vec(in->p0_new, nr);
-    S.psi = vec(in->psi, nr);
-    S.grav_cell = vec(in->grav_cell, nr);
-    S.w0_force = vec(in->w0_force, nr);
-    S.w0 = vec(in->w0, nr + 1);
-    S.rho0_predicted_edge = vec(in->rho0_predicted_edge, nr + 1);
-    const Box& dom = S.L.dom;
+    H.InitChunks();
+    if (nlev > 1) H.ComputeCutoffCoords();
+    const int nscal = H.nscal;
 
     // w0_cart: Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1) (Source/MaestroAdvance.cpp:326)
-    S.w0_cart.define(S.L.ba, 3, 2, -1, 0.0);
-    S.Put1dArrayOnCart(S.w0, S.w0_cart, true, true, &S.bcs_u, 0, true);
-    MF w0_force_cart;
-    w0_force_cart.define(S.L.ba, 3, 1, -1, 0.0);
-    if (p->evolve_base_state) S.Put1dArrayOnCart(S.w0_force, w0_force_cart, false, true, &S.bcs_f, 0, false);
-
-    MF uold, sold, snew;
-    uold.define(S.L.ba, 3, S.ng_s, -1, 0.0);
-    sold.define(S.L.ba, S.nscal, S.ng_s, -1, 0.0);
-    snew.define(S.L.ba, S.nscal, S.ng_s, -1, 0.0);
-    S.gpi.define(S.L.ba, 3, 0, -1, 0.0);
-    S.thermal.define(S.L.ba, 1, 1, -1, 0.0);
-    scatter_cells(dom, in->uold, uold, 0, 3);
-    scatter_cells(dom, in->sold, sold, 0, S.nscal);
-    scatter_cells(dom, in->gpi, S.gpi, 0, 3);
-    if (in->thermal) scatter_cells(dom, in->thermal, S.thermal, 0, 1);
-
-    MF umac[3], utrans[3], sedge[3], sflux[3], etarhoflux, scal_force, vel_force;
-    for (int d = 0; d < 3; ++d) {
-        umac[d].define(S.L.ba, 1, 1, d, 0.0);
-        sedge[d].define(S.L.ba, S.nscal, 0, d, 0.0);
-        sflux[d].define(S.L.ba, S.nscal, 0, d, 0.0);
+    {
+        VMF w0c(nlev);
+        for (int lev = 0; lev < nlev; ++lev) w0c[lev].define(H.S[lev].L.ba, 3, 2, -1, 0.0);
+        H.Put1dArrayOnCart(H.bs(&Lev::w0), w0c, true, true, &H.bcs_u(), 0, true);
+        for (int lev = 0; lev < nlev; ++lev) H.S[lev].w0_cart = std::move(w0c[lev]);
     }
-    etarhoflux.define(S.L.ba, 1, 0, 2, 0.0);
-    scal_force.define(S.L.ba, S.nscal, 1, -1, 0.0);
+    VMF w0_force_cart(nlev);
+    for (int lev = 0; lev < nlev; ++lev) w0_force_cart[lev].define(H.S[lev].L.ba, 3, 1, -1, 0.0);
+    if (p->evolve_base_state)
+        H.Put1dArrayOnCart(H.bs(&Lev::w0_force), w0_force_cart, false, true, &H.bcs_f(), 0, false);
+
+    VMF uold(nlev), sold(nlev), snew(nlev), etarhoflux(nlev), scal_force(nlev), vel_force(nlev);
+    VF umac(nlev), utrans(nlev), sedge(nlev), sflux(nlev);
+    for (int lev = 0; lev < nlev; ++lev) {
+        Lev& S = H.S[lev];
+        const Box& dom = S.L.dom;
+        uold[lev].define(S.L.ba, 3, H.ng_s, -1, 0.0);
+        sold[lev].define(S.L.ba, nscal, H.ng_s, -1, 0.0);
+        snew[lev].define(S.L.ba, nscal, H.ng_s, -1, 0.0);
+        S.gpi.define(S.L.ba, 3, 0, -1, 0.0);
+        S.thermal.define(S.L.ba, 1, 1, -1, 0.0);
+        scatter_cells(dom, in[lev].uold, uold[lev], 0, 3);
+        scatter_cells(dom, in[lev].sold, sold[lev], 0, nscal);
+        scatter_cells(dom, in[lev].gpi, S.gpi, 0, 3);
+        if (in[lev].thermal) scatter_cells(dom, in[lev].thermal, S.thermal, 0, 1);
+        for (int d = 0; d < 3; ++d) {
+            umac[lev][d].define(S.L.ba, 1, 1, d, 0.0);
+            sedge[lev][d].define(S.L.ba, nscal, 0, d, 0.0);
+            sflux[lev][d].define(S.L.ba, nscal, 0, d, 0.0);
+        }
+        etarhoflux[lev].define(S.L.ba, 1, 0, 2, 0.0);
+        scal_force[lev].define(S.L.ba, nscal, 1, -1, 0.0);
+    }
 
     // sold ghost cells as the previous step's UpdateScal leaves them
-    FillPatch(S.L, sold, 0, S.nscal, 0, S.bcs_s, false, 0);
+    H.FillPatch(sold, 0, nscal, 0, H.bcs_s(), false, 0);
 
     // STEP 3: AdvancePremac (MacProj skipped)
-    S.AdvancePremac(uold, sold, umac, w0_force_cart, utrans, vel_force);
-    if (out->utrans[0])
-        for (int d = 0; d < 3; ++d) gather_faces(dom, utrans[d], d, 0, 1, out->utrans[d]);
-    if (out->umac_vp[0])
-        for (int d = 0; d < 3; ++d) gather_faces(dom, umac[d], d, 0, 1, out->umac_vp[d]);
-    if (out->vel_force) gather_cells(dom, vel_force, 0, 3, out->vel_force);
-    // STEP 4 (Source/MaestroAdvance.cpp:436-548)
-    S.Addw0(umac, 1.0);
-    S.DensityAdvance(sold, snew, sedge, sflux, scal_force, etarhoflux, umac);
-    S.Addw0(umac, -1.0);
-    S.Addw0(umac, 1.0);
-    S.EnthalpyAdvance(sold, snew, sedge, sflux, scal_force, umac);
-    S.Addw0(umac, -1.0);
-
-    if (out->umac_end[0])
-        for (int d = 0; d < 3; ++d) gather_faces(dom, umac[d], d, 0, 1, out->umac_end[d]);
-    for (int d = 0; d < 3; ++d) {
-        if (out->sedge[d]) gather_faces(dom, sedge[d], d, 0, S.nscal, out->sedge[d]);
-        if (out->sflux[d]) gather_faces(dom, sflux[d], d, 0, S.nscal, out->sflux[d]);
+    H.AdvancePremac(uold, sold, umac, w0_force_cart, utrans, vel_force);
+    for (int lev = 0; lev < nlev; ++lev) {
+        const Box& dom = H.S[lev].L.dom;
+        if (out[lev].utrans[0])
+            for (int d = 0; d < 3; ++d) gather_faces(dom, utrans[lev][d], d, 0, 1, out[lev].utrans[d]);
+        if (out[lev].umac_vp[0])
+            for (int d = 0; d < 3; ++d) gather_faces(dom, umac[lev][d], d, 0, 1, out[lev].umac_vp[d]);
+        if (out[lev].vel_force) gather_cells(dom, vel_force[lev], 0, 3, out[lev].vel_force);
     }
-    if (out->snew) gather_cells(dom, snew, 0, S.nscal, out->snew);
-    if (out->sold_end) gather_cells(dom, sold, 0, S.nscal, out->sold_end);
-    if (out->etarhoflux) gather_faces(dom, etarhoflux, 2, 0, 1, out->etarhoflux);
+    // STEP 4 (Source/MaestroAdvance.cpp:436-548)
+    H.Addw0(umac, 1.0);
+    H.DensityAdvance(sold, snew, sedge, sflux, scal_force, etarhoflux, umac);
+    H.Addw0(umac, -1.0);
+    H.Addw0(umac, 1.0);
+    H.EnthalpyAdvance(sold, snew, sedge, sflux, scal_force, umac);
+    H.Addw0(umac, -1.0);
+
+    for (int lev = 0; lev < nlev; ++lev) {
+        const Box& dom = H.S[lev].L.dom;
+        mo_outputs& o = out[lev];
+        if (o.umac_end[0])
+            for (int d = 0; d < 3; ++d) gather_faces(dom, umac[lev][d], d, 0, 1, o.umac_end[d]);
+        for (int d = 0; d < 3; ++d) {
+            if (o.sedge[d]) gather_faces(dom, sedge[lev][d], d, 0, nscal, o.sedge[d]);
+            if (o.sflux[d]) gather_faces(dom, sflux[lev][d], d, 0, nscal, o.sflux[d]);
+        }
+        if (o.snew) gather_cells(dom, snew[lev], 0, nscal, o.snew);
+        if (o.sold_end) gather_cells(dom, sold[lev], 0, nscal, o.sold_end);
+        if (o.etarhoflux) gather_faces(dom, etarhoflux[lev], 2, 0, 1, o.etarhoflux);
+    }
     return 0;
 }
 
@@ -1261,24 +1514,29 @@ static int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_
 
 extern "C" {
 
-int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
-                 int nthreads) {
+int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
+                        mo_outputs* out, int nthreads) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
     try {
-        return mo::run_stage(p, nboxes, boxes, in, out);
+        return mo::run_stage(p, nlev, nboxes, boxes, in, out);
     } catch (const std::exception& e) {
         mo::g_err = e.what();
         return -1;
     }
 }
 
+int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
+                 int nthreads) {
+    return mo_run_stage_levels(p, 1, &nboxes, boxes, in, out, nthreads);
+}
+
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {
     std::vector<double> c(s0_cell, s0_cell + nr), e;
-    mo::Stage::CelltoEdge(c, e);
+    mo::Lev::CelltoEdge(c, e);
     std::memcpy(s0_edge, e.data(), sizeof(double) * (nr + 1));
     return 0;
 }

@@ -46,6 +46,7 @@ def lib(checked=False):
             build()
         L = C.CDLL(path)
         L.mo_run_stage.restype = C.c_int
+        L.mo_run_stage_levels.restype = C.c_int
         L.mo_last_error.restype = C.c_char_p
         _LIBS[name] = L
     return _LIBS[name]
@@ -101,6 +102,66 @@ def run_stage(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_e
     boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
     rc = lib(checked).mo_run_stage(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
                                    C.byref(inp), C.byref(out), nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
+    return res
+
+
+def run_stage_levels(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_end", "vel_force",
+                                                             "sedge", "sflux", "snew", "sold_end",
+                                                             "etarhoflux")):
+    """The stage on the hierarchy cfg["levels"]; returns one dict of arrays per level
+    (domain-sized at the level's resolution, NaN where the level has no box)."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    levels = cfg["levels"]
+    nlev = len(levels)
+    nscal = 4 + cfg["nspec"]
+    keep = []
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    ins = (MoInputs * nlev)()
+    outs = (MoOutputs * nlev)()
+    res = []
+    for lev, L in enumerate(levels):
+        inp = ins[lev]
+        for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                     "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+            setattr(inp, name, arr(L[name]))
+        n = L["n"]
+        out = outs[lev]
+        r = {}
+        fshape = [(n[2], n[1], n[0] + 1), (n[2], n[1] + 1, n[0]), (n[2] + 1, n[1], n[0])]
+        for key in ("utrans", "umac_vp", "umac_end"):
+            if key in want:
+                r[key] = [np.full(fshape[d], np.nan) for d in range(3)]
+                for d in range(3):
+                    getattr(out, key)[d] = _p(r[key][d])
+        for key in ("sedge", "sflux"):
+            if key in want:
+                r[key] = [np.full((nscal,) + fshape[d], np.nan) for d in range(3)]
+                for d in range(3):
+                    getattr(out, key)[d] = _p(r[key][d])
+        cshape = (n[2], n[1], n[0])
+        if "vel_force" in want:
+            r["vel_force"] = np.full((3,) + cshape, np.nan)
+            out.vel_force = _p(r["vel_force"])
+        for key in ("snew", "sold_end"):
+            if key in want:
+                r[key] = np.full((nscal,) + cshape, np.nan)
+                setattr(out, key, _p(r[key]))
+        if "etarhoflux" in want:
+            r["etarhoflux"] = np.full(fshape[2], np.nan)
+            out.etarhoflux = _p(r["etarhoflux"])
+        res.append(r)
+    nboxes = (C.c_int * nlev)(*[len(L["boxes"]) for L in levels])
+    boxes = np.ascontiguousarray(np.array([b for L in levels for b in L["boxes"]], dtype=np.int32).reshape(-1))
+    rc = lib(checked).mo_run_stage_levels(C.byref(p), nlev, nboxes, boxes.ctypes.data_as(C.POINTER(C.c_int)),
+                                          ins, outs, nthreads)
     if rc != 0:
         raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
     return res

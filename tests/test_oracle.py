@@ -102,3 +102,40 @@ def test_oracle_rejects_scalar_inflow():
     cfg = configs.planar_config(n=(16, 16, 16), nspec=2, max_grid=8, bc_lo=(INTERIOR, INTERIOR, INFLOW))
     with pytest.raises(RuntimeError, match="Dirichlet"):
         pyoracle.run_stage(cfg, checked=True)
+
+
+def test_amr_full_coverage_equals_single_level():
+    """A level 1 covering the whole domain reproduces the single-level stage at its
+    resolution exactly (no coarse data reaches it)."""
+    fb = configs.tile_boxes((32, 32, 32), 16)
+    cfg = configs.planar_amr_config(n0=(16, 16, 16), nspec=2, ppm_type=1, max_grid=8, fine_boxes=fb)
+    two = pyoracle.run_stage_levels(cfg, want=("snew", "sflux"))
+    one_cfg = dict(cfg)
+    one_cfg.update(cfg["levels"][1])
+    one_cfg.pop("levels")
+    one = pyoracle.run_stage(one_cfg, want=("snew", "sflux"))
+    assert np.array_equal(two[1]["snew"], one["snew"])
+    for d in range(3):
+        assert np.array_equal(two[1]["sflux"][d], one["sflux"][d])
+
+
+def test_amr_coarse_cells_are_averages_of_fine():
+    """After UpdateScal the coarse cells under level 1 hold the mean of their 8 children."""
+    rng = np.random.default_rng(5)
+    fine = configs.bubble_boxes((16, 16, 16), nbubbles=1, cover=0.1, block_edges=(4,), max_edge=4, rng=rng)
+    cfg = configs.planar_amr_config(n0=(16, 16, 16), nspec=2, ppm_type=2, max_grid=8, fine_boxes=fine)
+    res = pyoracle.run_stage_levels(cfg, want=("snew",))
+    c, f = res[0]["snew"], res[1]["snew"]
+    for b in fine:
+        i0, j0, k0, i1, j1, k1 = b
+        blk = f[:, k0:k1 + 1, j0:j1 + 1, i0:i1 + 1]
+        s = blk.reshape(blk.shape[0], blk.shape[1] // 2, 2, blk.shape[2] // 2, 2, blk.shape[3] // 2, 2)
+        # k-outer, i-inner summation, then * 1/8
+        acc = np.zeros_like(s[:, :, 0, :, 0, :, 0])
+        for kr in range(2):
+            for jr in range(2):
+                for ir in range(2):
+                    acc = acc + s[:, :, kr, :, jr, :, ir]
+        want = 0.125 * acc
+        got = c[:, k0 // 2:(k1 + 1) // 2, j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2]
+        assert np.array_equal(got[[0, 1, 4, 5]], want[[0, 1, 4, 5]])
