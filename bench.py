@@ -194,6 +194,71 @@ def run_cpu_baseline(steps, warmup, nthreads=0):
             "s_per_sample": dt}
 
 
+def run_amr(args, ws, steps, warmup, barrier):
+    """Two-level AMR workload (config 3): the batched path replayed as a CUDA graph against
+    one launch per box, same inputs, same results (bitwise; checked here)."""
+    import torch
+    from maestroex_gb300 import capi, configs
+    from maestroex_gb300.stage import amr_buffers, make_amr_stage
+    cfg = configs.config_c3(n0=args.amr_n, nspec=args.nspec)
+    st = make_amr_stage(cfg)
+    bufs = amr_buffers(cfg)
+    names = ("uold", "sold", "gpi")
+    snap = [{n: [t.clone() for t in getattr(b, n).fabs] for n in names} for b in bufs]
+
+    def reset():
+        for b, sn in zip(bufs, snap):
+            for n, ts in sn.items():
+                for dst, src in zip(getattr(b, n).fabs, ts):
+                    dst.copy_(src)
+
+    def timed(mode, k, warm):
+        for _ in range(warm):
+            reset()
+            st.stage_forward_levels(bufs, mode=mode)
+        barrier()
+        total = 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(k):
+            reset()
+            torch.cuda.synchronize()
+            e0.record()
+            st.stage_forward_levels(bufs, mode=mode)
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        barrier()
+        return total / k
+
+    ms_graph = timed(capi.MODE_GRAPH, steps, warmup)
+    launches_graph = st.launch_count()
+    out_graph = [torch.cat([f.flatten() for f in b.snew.fabs]) for b in bufs]
+    ms_batched = timed(capi.MODE_BATCHED, steps, 1)
+    ms_perbox = timed(capi.MODE_PER_BOX, steps, 1)
+    launches_perbox = st.launch_count()
+    same = all(torch.equal(a, torch.cat([f.flatten() for f in b.snew.fabs])) for a, b in zip(out_graph, bufs))
+    cells = [int(np.prod(L["n"])) if l == 0 else
+             sum((b[3] - b[0] + 1) * (b[4] - b[1] + 1) * (b[5] - b[2] + 1) for b in L["boxes"])
+             for l, L in enumerate(cfg["levels"])]
+    ncell = sum(cells)
+    st.close()
+    del bufs, snap
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"two-level AMR: level 0 {args.amr_n}^3 in {len(cfg['levels'][0]['boxes'])} uneven boxes "
+                    f"(edges 16-128), level 1 (ratio 2) {len(cfg['levels'][1]['boxes'])} boxes of 16-64 cells "
+                    f"around 3 bubbles ({cells[1] / 8 / cells[0]:.3f} of the domain), NumSpec {args.nspec}, "
+                    "ppm_type 2; level-1 state injected from level 0",
+        "cells_per_level": cells, "unit": UNIT,
+        "graph": {"value": ws * ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": launches_graph},
+        "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
+        "per_box": {"value": ws * ncell / (ms_perbox * 1e-3), "ms_per_step": ms_perbox,
+                    "gpu_launches": launches_perbox},
+        "speedup_graph_vs_per_box": ms_perbox / ms_graph,
+        "identical_results_graph_vs_per_box": bool(same),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -205,6 +270,8 @@ def main():
     ap.add_argument("--nspec", type=int, default=13)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-box", action="store_true")
+    ap.add_argument("--amr-n", type=int, default=256, help="level-0 extent of the two-level AMR workload")
+    ap.add_argument("--no-amr", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
     args = ap.parse_args()
@@ -337,6 +404,12 @@ def main():
     tf = C.c_double(0.0)
     capi.check(L.madv_probe_fp64_peak(C.byref(tf), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
 
+    amr = None
+    if not args.no_amr:
+        del st, buf, snap
+        torch.cuda.empty_cache()
+        amr = run_amr(args, ws, max(1, args.steps // 2), warmup, barrier)
+
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -370,6 +443,8 @@ def main():
                       "frac": hbm_gbs / peaks.get("hbm_gbs", HBM_PEAK_FALLBACK), "peak_kind": peak_kind,
                       "bytes_per_cell": b_cell},
     }
+    if amr is not None:
+        line["amr"] = amr
     if not args.no_cpu_baseline:
         cb = run_cpu_baseline(1, 0)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

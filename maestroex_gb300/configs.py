@@ -32,13 +32,14 @@ def tile_boxes(n, max_grid):
     return boxes
 
 
-def uneven_boxes(n, edges, rng):
-    """Seeded guillotine split of the domain into boxes whose edges come from `edges`."""
+def uneven_boxes(n, edges, rng, p_stop=0.35):
+    """Seeded guillotine split of the domain into boxes whose edges come from `edges`;
+    a piece whose extents are all in `edges` stops splitting with probability p_stop."""
     out = []
 
     def split(lo, hi):
         ext = [hi[d] - lo[d] for d in range(3)]
-        if all(e in edges for e in ext) and rng.random() < 0.35:
+        if all(e in edges for e in ext) and rng.random() < p_stop:
             out.append((lo[0], lo[1], lo[2], hi[0] - 1, hi[1] - 1, hi[2] - 1))
             return
         cands = []
@@ -274,3 +275,40 @@ def planar_amr_config(n0=(32, 32, 32), nspec=3, ppm_type=2, max_grid=16, fine_bo
     c0["rel_eps"] = max(c0["rel_eps"], c1["rel_eps"])
     c0["levels"] = [{k: c0[k] for k in LEVEL_KEYS}, {k: c1[k] for k in LEVEL_KEYS}]
     return c0
+
+
+def config_c3(n0=256, nspec=13, seed=20261203 + 3, cover=0.06, p_stop=0.8):
+    """Config 3: two-level AMR, level 0 = n0^3 in uneven boxes (edges from
+    {16, 32, 48, 64, 96, 128}), level 1 (ratio 2) = boxes of 16-64 fine cells of random
+    aspect around 3 seeded bubbles covering about `cover` of the domain; NumSpec 13,
+    ppm_type 2.  Level-1 state is injected from level 0 (each fine cell takes its parent's
+    value: "inject" levels are filled on the device by stage.amr_buffers); the level-1
+    base state is the same atmosphere on the fine radial grid.  dt is halved for the
+    fine level's CFL condition.
+    """
+    from .basestate import cell_to_edge
+    rng = np.random.default_rng(seed)
+    n = (n0, n0, n0)
+    l0 = uneven_boxes(n, [16, 32, 48, 64, 96, 128], rng, p_stop=p_stop)
+    fine = bubble_boxes(n, nbubbles=3, cover=cover, block_edges=(8, 16, 24, 32), max_edge=32,
+                        rng=np.random.default_rng(seed + 100))
+    cfg = planar_config(n=n, nspec=nspec, ppm_type=2, boxes=l0, seed=seed, w0_amp=1.0e4, cfl=0.7)
+    cfg["dt"] *= 0.5
+    n1 = tuple(2 * v for v in n)
+    dx1 = tuple(L_DOMAIN / v for v in n1)
+    nr1 = n1[2]
+    H = 0.25 * L_DOMAIN
+    r_cc = (np.arange(nr1) + 0.5) * dx1[2]
+    rho0 = 1.0e7 * np.exp(-r_cc / H)
+    w0c = cfg["w0"]
+    w0 = np.zeros(nr1 + 1)
+    w0[0::2] = w0c
+    w0[1::2] = 0.5 * (w0c[:-1] + w0c[1:])
+    lev1 = dict(n=n1, dx=dx1, boxes=fine, inject=True,
+                rho0_old=rho0.copy(), rho0_new=rho0.copy(),
+                rhoh0_old=np.repeat(cfg["rhoh0_old"], 2), rhoh0_new=np.repeat(cfg["rhoh0_new"], 2),
+                p0_old=rho0 * abs(GRAV) * H, p0_new=rho0 * abs(GRAV) * H, psi=np.zeros(nr1),
+                grav_cell=np.full(nr1, GRAV), w0_force=np.zeros(nr1), w0=w0,
+                rho0_predicted_edge=cell_to_edge(rho0))
+    cfg["levels"] = [{k: cfg[k] for k in LEVEL_KEYS}, lev1]
+    return cfg

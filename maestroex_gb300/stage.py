@@ -307,12 +307,29 @@ def make_amr_stage(cfg):
 
 
 def amr_buffers(cfg, device="cuda"):
-    """One StageBuffers per level, loaded with the level's input arrays."""
+    """One StageBuffers per level, loaded with the level's input arrays.  A level marked
+    "inject" has no arrays of its own: each of its cells takes the value of its parent cell
+    on the level below (filled on the device box by box)."""
     out = []
-    for L in cfg["levels"]:
+    for lev, L in enumerate(cfg["levels"]):
         c = dict(cfg)
         c.update(L)
-        out.append(StageBuffers(c, device).load(c))
+        if not L.get("inject"):
+            out.append(StageBuffers(c, device).load(c))
+            continue
+        buf = StageBuffers(c, device)
+        P = cfg["levels"][lev - 1]
+        for name in ("uold", "sold", "gpi", "thermal"):
+            src = torch.from_numpy(np.ascontiguousarray(P[name])).to(device)
+            mf = getattr(buf, name)
+            for b, bx in enumerate(mf.boxes):
+                i0, j0, k0, i1, j1, k1 = bx
+                blk = src[:, k0 // 2:(k1 + 1) // 2, j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2]
+                blk = blk.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2).repeat_interleave(2, dim=3)
+                fs, _ = mf._slices(b)
+                mf.fabs[b][(slice(None),) + fs] = blk
+            del src
+        out.append(buf)
     return out
 
 
