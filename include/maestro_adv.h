@@ -133,7 +133,8 @@ int madv_advance_premac(madv_ctx* ctx, const madv_multifab* uold, const madv_mul
  * refill of the face ghosts. */
 int madv_addw0(madv_ctx* ctx, const madv_multifab* umac, double mult, void* stream);
 
-/* Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243).
+/* Maestro::DensityAdvance (Source/MaestroDensityAdvance.cpp:6-243), which_step 1
+ * (predictor) or 2 (corrector: old/new base-state averages in the fluxes).
  * sold is converted and restored in place exactly as the reference does; snew receives
  * rho and rhoX.  umac must hold the full velocity (w0 added), ghosts filled.
  * sedge/sflux (may be NULL) receive the edge states / fluxes; etarhoflux may be NULL. */
@@ -142,7 +143,8 @@ int madv_density_advance(madv_ctx* ctx, int which_step, const madv_multifab* sol
                          const madv_multifab* sflux, const madv_multifab* etarhoflux,
                          const madv_multifab* umac, void* stream);
 
-/* Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352).
+/* Maestro::EnthalpyAdvance (Source/MaestroEnthalpyAdvance.cpp:6-352), which_step 1 or 2
+ * (2 averages the old and new base state in the fluxes and the final MakeRhoHForce).
  * thermal may be NULL (zero). */
 int madv_enthalpy_advance(madv_ctx* ctx, int which_step, const madv_multifab* sold,
                           const madv_multifab* snew, const madv_multifab* sedge,

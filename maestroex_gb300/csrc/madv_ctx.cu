@@ -455,11 +455,12 @@ static void modify_scal_force_h(Hier& H, int comp, const char* s0_edge, int s0ca
     fill_patch_h(H, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
 }
 
-// Maestro::MakeRhoHForce, which_step 1 (Source/MaestroForce.cpp:469-679)
-static void make_rhoh_force_h(Hier& H, int is_prediction, int add_thermal) {
-    put1d_h(H, F_P0CART, "p0_old", 0, 1, 0, BCS_F, 0, 0, -1);
+// Maestro::MakeRhoHForce (Source/MaestroForce.cpp:469-679): which_step 1 uses rho0_old and
+// p0_old, which_step 2 their old/new averages (:493-499)
+static void make_rhoh_force_h(Hier& H, int is_prediction, int add_thermal, int which_step) {
+    put1d_h(H, F_P0CART, which_step == 1 ? "p0_old" : "p0_avg", 0, 1, 0, BCS_F, 0, 0, -1);
     put1d_h(H, F_PSICART, "psi", 0, 1, 0, BCS_F, 0, 0, -1);
-    put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
+    put1d_h(H, F_RHO0CART, which_step == 1 ? "rho0_old" : "rho0_avg", 0, 1, 0, BCS_S, RHO, 0, RHO);
     put1d_h(H, F_GRAVCART, "grav_cell", 2, 3, 0, BCS_F, 0, 0, -1);
     for (auto* c : H.L) make_rhoh_force(*c, is_prediction, add_thermal);
     average_down_h(H, F_SCALFORCE, RHOH, 1);
@@ -497,8 +498,9 @@ static void update_scal_h(Hier& H, int start_comp) {
     }
 }
 
-// Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243)
-static void density_advance(Hier& H) {
+// Maestro::DensityAdvance (Source/MaestroDensityAdvance.cpp:6-243); which_step 2 passes the
+// new base state to the fluxes (:186-219)
+static void density_advance(Hier& H, int which_step) {
     const int spt = H[0].P.species_pred_type;
     const int ns = H[0].nspec, nscal = H[0].nscal;
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
@@ -516,20 +518,22 @@ static void density_advance(Hier& H) {
         for (auto* c : H.L) sum_species_edges(*c);
     if (spt == 1) put_in_pert_form_h(H, "rho0_old", RHO, RHO, BCS_S, 0);
     if (spt == 1 || spt == 3) convert_rhox_to_x_h(H, 0);
-    for (auto* c : H.L)
-        make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1("rho0_old"), c->b1("rho0_edge_old"));
+    const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
+    const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
+    for (auto* c : H.L) make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
     average_down_faces_h(H, F_SFLUX0, 0, nscal);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
     update_scal_h(H, FIRSTSPEC);
 }
 
-// Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352)
-static void enthalpy_advance(Hier& H) {
+// Maestro::EnthalpyAdvance (Source/MaestroEnthalpyAdvance.cpp:6-352); which_step 2 averages
+// the old and new base state in the fluxes (:234-317) and the final MakeRhoHForce (:336)
+static void enthalpy_advance(Hier& H, int which_step) {
     const int ept = H[0].P.enthalpy_pred_type;
     const int nscal = H[0].nscal;
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
     addw0_h(H, F_UMAC0, -1.0);
-    make_rhoh_force_h(H, 1, 1);
+    make_rhoh_force_h(H, 1, 1, 1);
     if (ept == 1) {
         put1d_h(H, F_RHOH0CART, "rhoh0_old", 0, 1, 0, BCS_S, RHOH, 0, RHOH);
         modify_scal_force_h(H, RHOH, "rhoh0_edge_old", F_RHOH0CART, 0);
@@ -538,12 +542,13 @@ static void enthalpy_advance(Hier& H) {
     if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
     for (auto* c : H.L) make_edge_scal(*c, RHOH, 1, BCS_S, ept == 0, 0);
     if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, RHOH, BCS_S, 0);
-    for (auto* c : H.L)
-        make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"));
+    const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
+    const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
+    for (auto* c : H.L) make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en));
     average_down_faces_h(H, F_SFLUX0, 0, nscal);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
     addw0_h(H, F_UMAC0, -1.0);
-    make_rhoh_force_h(H, 0, 0);
+    make_rhoh_force_h(H, 0, 0, which_step);
     addw0_h(H, F_UMAC0, 1.0);
     update_scal_h(H, RHOH);
 }
@@ -605,10 +610,10 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
     // STEP 3 and STEP 4 of Maestro::AdvanceTimeStep (Source/MaestroAdvance.cpp:359-548)
     advance_premac(H);
     addw0_h(H, F_UMAC0, 1.0);
-    density_advance(H);
+    density_advance(H, 1);
     addw0_h(H, F_UMAC0, -1.0);
     addw0_h(H, F_UMAC0, 1.0);
-    enthalpy_advance(H);
+    enthalpy_advance(H, 1);
     addw0_h(H, F_UMAC0, -1.0);
     // outputs (valid region)
     for (int l = 0; l < H.n(); ++l) {
@@ -997,6 +1002,17 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
             c.h1[a.name] = std::vector<double>(a.p, a.p + a.n);
         }
     }
+    // which_step 2 averages of MakeRhoHForce: 0.5 * (old + new) (Source/MaestroForce.cpp:496-497)
+    for (int l = 0; l < nlev; ++l) {
+        Ctx& c = H[l];
+        std::vector<double> ra(c.nr), pa(c.nr);
+        for (int r = 0; r < c.nr; ++r) {
+            ra[r] = 0.5 * (c.h1["rho0_old"][r] + c.h1["rho0_new"][r]);
+            pa[r] = 0.5 * (c.h1["p0_old"][r] + c.h1["p0_new"][r]);
+        }
+        c.h1["rho0_avg"] = ra;
+        c.h1["p0_avg"] = pa;
+    }
     // Maestro::CelltoEdge over the chunks of every level, then RestrictBase of the edges
     // (Source/MaestroCelltoEdge.cpp:17-58, Source/MaestroBaseStateGeometry.cpp:240-262)
     for (const char* name : {"rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new"}) {
@@ -1231,9 +1247,9 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
     int rc = begin_call(h, stream, H);
     if (rc) return rc;
     Ctx& c = h->c;
-    if (which_step != 1) {
-        set_error("only which_step 1 (the predictor) is implemented");
-        return MADV_ERR_UNSUPPORTED;
+    if (which_step != 1 && which_step != 2) {
+        set_error("which_step must be 1 (predictor) or 2 (corrector)");
+        return MADV_ERR_PARAM;
     }
     if (!sold || !snew || !umac) return MADV_ERR_PARAM;
     try {
@@ -1260,12 +1276,12 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
         if (which == 0) {
             set_val(c, F_ETA, 0.0, 0, 1, 0);
             if (eta) copy_fab(c, F_ETA, 0, F_USER + U_ETA, 0, 1, 0);
-            density_advance(H);
+            density_advance(H, which_step);
             copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 1, 0);
             copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
             if (eta) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
         } else {
-            enthalpy_advance(H);
+            enthalpy_advance(H, which_step);
             copy_fab(c, F_USER + U_SNEW, RHOH, F_SNEW, RHOH, 1, 0);
         }
         copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);

@@ -1266,8 +1266,10 @@ struct Stage {
     }
 
     // ------------------------------------------------------------------ drivers
-    // Maestro::DensityAdvance, which_step 1 (Source/MaestroDensityAdvance.cpp:6-243)
-    void DensityAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VMF& etarhoflux, VF& umac) {
+    // Maestro::DensityAdvance (Source/MaestroDensityAdvance.cpp:6-243); which_step 2 passes the
+    // new base state to the flux for the old/new averages (:186-219)
+    void DensityAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VMF& etarhoflux, VF& umac,
+                        int which_step) {
         const int spt = P.species_pred_type;
         const BS rho0_old = bs(&Lev::rho0_old), rho0_new = bs(&Lev::rho0_new);
         BS rho0_edge_old, rho0_edge_new;
@@ -1299,13 +1301,19 @@ struct Stage {
         }
         if (spt == 1) PutInPertForm(scalold, rho0_old, Rho, Rho, bcs_s(), false);
         if (spt == 1 || spt == 3) ConvertRhoXToX(scalold, false);
-        MakeRhoXFlux(sflux, etarhoflux, sedge, umac, rho0_old, rho0_edge_old, rho0_old, rho0_edge_old, FirstSpec, nspec);
+        if (which_step == 1)
+            MakeRhoXFlux(sflux, etarhoflux, sedge, umac, rho0_old, rho0_edge_old, rho0_old, rho0_edge_old, FirstSpec,
+                         nspec);
+        else
+            MakeRhoXFlux(sflux, etarhoflux, sedge, umac, rho0_old, rho0_edge_old, rho0_new, rho0_edge_new, FirstSpec,
+                         nspec);
         for (auto& f : scal_force) f.setVal(0.0);
         UpdateScal(scalold, scalnew, sflux, scal_force, FirstSpec, nspec);
     }
 
-    // Maestro::EnthalpyAdvance, which_step 1 (Source/MaestroEnthalpyAdvance.cpp:6-352)
-    void EnthalpyAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VF& umac) {
+    // Maestro::EnthalpyAdvance (Source/MaestroEnthalpyAdvance.cpp:6-352); which_step 2 averages
+    // the old and new base state in the flux (:234-317) and in the final MakeRhoHForce (:336)
+    void EnthalpyAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VF& umac, int which_step) {
         const int ept = P.enthalpy_pred_type;
         const BS rhoh0_old = bs(&Lev::rhoh0_old), rhoh0_new = bs(&Lev::rhoh0_new);
         BS rhoh0_edge_old, rhoh0_edge_new;
@@ -1324,10 +1332,11 @@ struct Stage {
         if (ept == 1) PutInPertForm(scalold, rhoh0_old, RhoH, 0, bcs_f(), true);
         MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s(), RhoH, RhoH, 1, ept == 0);
         if (ept == 1) PutInPertForm(scalold, rhoh0_old, RhoH, RhoH, bcs_s(), false);
-        MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_old, rhoh0_edge_old);
+        if (which_step == 1) MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_old, rhoh0_edge_old);
+        else MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_new, rhoh0_edge_new);
         for (auto& f : scal_force) f.setVal(0.0, RhoH, 1, 1);
         Addw0(umac, -1.0);
-        MakeRhoHForce(scal_force, 0, umac, 0, 1);
+        MakeRhoHForce(scal_force, 0, umac, 0, which_step);
         Addw0(umac, 1.0);
         UpdateScal(scalold, scalnew, sflux, scal_force, RhoH, 1);
     }
@@ -1371,7 +1380,8 @@ static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, do
 }
 
 static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
-                     mo_outputs* out) {
+                     mo_outputs* out, int which_step) {
+    if (which_step != 1 && which_step != 2) throw std::runtime_error("which_step must be 1 or 2");
     if (nlev < 1 || nlev > 4) throw std::runtime_error("1 to 4 levels");
     if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
     if (p->use_exact_base_state) throw std::runtime_error("use_exact_base_state is spherical-only");
@@ -1488,10 +1498,10 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
     }
     // STEP 4 (Source/MaestroAdvance.cpp:436-548)
     H.Addw0(umac, 1.0);
-    H.DensityAdvance(sold, snew, sedge, sflux, scal_force, etarhoflux, umac);
+    H.DensityAdvance(sold, snew, sedge, sflux, scal_force, etarhoflux, umac, which_step);
     H.Addw0(umac, -1.0);
     H.Addw0(umac, 1.0);
-    H.EnthalpyAdvance(sold, snew, sedge, sflux, scal_force, umac);
+    H.EnthalpyAdvance(sold, snew, sedge, sflux, scal_force, umac, which_step);
     H.Addw0(umac, -1.0);
 
     for (int lev = 0; lev < nlev; ++lev) {
@@ -1515,14 +1525,14 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
 extern "C" {
 
 int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
-                        mo_outputs* out, int nthreads) {
+                        mo_outputs* out, int which_step, int nthreads) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
     try {
-        return mo::run_stage(p, nlev, nboxes, boxes, in, out);
+        return mo::run_stage(p, nlev, nboxes, boxes, in, out, which_step);
     } catch (const std::exception& e) {
         mo::g_err = e.what();
         return -1;
@@ -1531,7 +1541,7 @@ int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const i
 
 int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
                  int nthreads) {
-    return mo_run_stage_levels(p, 1, &nboxes, boxes, in, out, nthreads);
+    return mo_run_stage_levels(p, 1, &nboxes, boxes, in, out, 1, nthreads);
 }
 
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {

@@ -80,9 +80,11 @@ int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inpu
  * domain and cell size of level 0 refined 2^l times; nboxes[l] boxes of level l follow
  * those of level l-1 in `boxes` (level-l index space).  in[l] / out[l] hold level l's
  * domain-sized field arrays (only cells and faces of the level's boxes are read or
- * written) and its base state (nr_l = nr_0 * 2^l cells).  nlev = 1 is mo_run_stage. */
+ * written) and its base state (nr_l = nr_0 * 2^l cells).  which_step 1 runs
+ * DensityAdvance / EnthalpyAdvance as the predictor, 2 as the corrector.  nlev = 1,
+ * which_step 1 is mo_run_stage. */
 int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const int* boxes,
-                        const mo_inputs* in, mo_outputs* out, int nthreads);
+                        const mo_inputs* in, mo_outputs* out, int which_step, int nthreads);
 
 /* A FAB: data covering the index box [lo, hi] (i fastest), nc components. */
 typedef struct {

@@ -109,7 +109,7 @@ def run_stage(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_e
 
 def run_stage_levels(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_end", "vel_force",
                                                              "sedge", "sflux", "snew", "sold_end",
-                                                             "etarhoflux")):
+                                                             "etarhoflux"), which_step=1):
     """The stage on the hierarchy cfg["levels"]; returns one dict of arrays per level
     (domain-sized at the level's resolution, NaN where the level has no box)."""
     from maestroex_gb300.params import make_params
@@ -161,7 +161,7 @@ def run_stage_levels(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", 
     nboxes = (C.c_int * nlev)(*[len(L["boxes"]) for L in levels])
     boxes = np.ascontiguousarray(np.array([b for L in levels for b in L["boxes"]], dtype=np.int32).reshape(-1))
     rc = lib(checked).mo_run_stage_levels(C.byref(p), nlev, nboxes, boxes.ctypes.data_as(C.POINTER(C.c_int)),
-                                          ins, outs, nthreads)
+                                          ins, outs, which_step, nthreads)
     if rc != 0:
         raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
     return res

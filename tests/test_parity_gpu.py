@@ -159,6 +159,40 @@ def test_maestro_entry_points_match_stage():
     st.close()
 
 
+def test_corrector_which_step_2_matches_oracle():
+    """DensityAdvance / EnthalpyAdvance with which_step 2 (old/new base-state averages in
+    the fluxes and in the final MakeRhoHForce) through the entry points, against the oracle."""
+    import torch
+    from maestroex_gb300.stage import StageBuffers, make_stage
+    cfg = configs.planar_config(n=(16, 16, 32), nspec=2, ppm_type=1, max_grid=16, seed=802)
+    z = np.linspace(0.0, 1.0, cfg["n"][2])
+    cfg["rho0_new"] = cfg["rho0_old"] * (1.0 + 1e-3 * np.sin(3.0 * z))
+    cfg["rhoh0_new"] = cfg["rhoh0_old"] * (1.0 - 2e-3 * np.cos(2.0 * z))
+    cfg["p0_new"] = cfg["p0_old"] * (1.0 + 5e-4 * z)
+    c = dict(cfg)
+    c["levels"] = [{k: cfg[k] for k in configs.LEVEL_KEYS}]
+    ref = pyoracle.run_stage_levels(c, which_step=2)[0]
+    st = make_stage(cfg)
+    b = StageBuffers(cfg).load(cfg)
+    st.advance_premac(b.uold, b.sold, b.gpi, b.umac)
+    st.addw0(b.umac, 1.0)
+    st.density_advance(b.sold, b.snew, b.sedge, b.sflux, b.eta, b.umac, which_step=2)
+    st.addw0(b.umac, -1.0)
+    st.addw0(b.umac, 1.0)
+    st.enthalpy_advance(b.sold, b.snew, b.sedge, b.sflux, b.umac, thermal=b.thermal, which_step=2)
+    st.addw0(b.umac, -1.0)
+    torch.cuda.synchronize()
+    n = cfg["n"]
+    comps = [RHO, RHOH, FIRSTSPEC, FIRSTSPEC + 1]
+    snew = b.snew.to_domain(n).cpu().numpy()
+    for cc in comps:
+        assert rel_err(snew[cc], ref["snew"][cc]) <= TOL
+        for d in range(3):
+            assert rel_err(b.sflux[d].to_domain(n).cpu().numpy()[cc], ref["sflux"][d][cc]) <= TOL
+    assert rel_err(b.eta.to_domain(n)[0].cpu().numpy(), ref["etarhoflux"]) <= TOL
+    st.close()
+
+
 def test_rejects_bad_layout_and_params():
     from maestroex_gb300.params import make_params
     from maestroex_gb300.stage import ScalarAdvectionStage
