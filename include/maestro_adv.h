@@ -60,6 +60,8 @@ typedef struct {
     double buoyancy_cutoff_factor;
     int do_eos_h_above_cutoff;
     int base_cutoff_density_coord;
+    int dim;                    /* 3 (0 means 3) or 2: the AMREX_SPACEDIM == 2 form, y radial,
+                                   boxes and domain with z = [0, 0], 2 velocity components */
 } madv_params;
 
 typedef struct {

@@ -312,3 +312,107 @@ def config_c3(n0=256, nspec=13, seed=20261203 + 3, cover=0.06, p_stop=0.8):
                 rho0_predicted_edge=cell_to_edge(rho0))
     cfg["levels"] = [{k: cfg[k] for k in LEVEL_KEYS}, lev1]
     return cfg
+
+
+def planar_config_2d(n=(64, 64), nspec=3, ppm_type=1, bc_lo=(INTERIOR, SLIPWALL), bc_hi=(INTERIOR, OUTFLOW),
+                     max_grid=None, boxes=None, seed=20261203, rho_pert=0.0, w0_amp=0.0, cfl=0.7, gpi_amp=0.0,
+                     species_pred_type=1, enthalpy_pred_type=1, slope_order=4, evolve_base_state=1):
+    """2-D plane-parallel configuration (y radial): rho0(y) = 1e7 exp(-y/H), H = L/4,
+    p0 = rho0 |g| H; NumSpec mass fractions from 6 seeded Gaussian bumps each;
+    rho h = rho (1e17 + 1e16 G) with G a unit-RMS sum of 8 Fourier modes; rhoh0 = the
+    horizontal mean of rho h; divergence-free velocity from a seeded streamfunction of 8
+    modes (evaluated at nodes, differenced to faces, averaged to cells) scaled to Mach 0.01;
+    w0 = 0 unless w0_amp is given.  Arrays are [ncomp, 1, ny, nx]; boxes carry k = 0.
+    """
+    rng = np.random.default_rng(seed)
+    nx, ny = int(n[0]), int(n[1])
+    dx = (L_DOMAIN / nx, L_DOMAIN / ny, 1.0)
+    periodic = [bc_lo[d] == INTERIOR for d in range(2)]
+    H = 0.25 * L_DOMAIN
+    x = (np.arange(nx) + 0.5) * dx[0]
+    y = (np.arange(ny) + 0.5) * dx[1]
+    rho0 = 1.0e7 * np.exp(-y / H)
+    p0 = rho0 * abs(GRAV) * H
+    X = np.zeros((nspec, ny, nx))
+    for s in range(nspec):
+        for _ in range(6):
+            w = rng.uniform(0.05, 0.2) * L_DOMAIN
+            c = rng.uniform(0, L_DOMAIN, size=2)
+            A = rng.uniform(0.2, 1.0)
+            gx = _gauss1d(c[0], w, L_DOMAIN, periodic[0], dx[0], nx)
+            gy = _gauss1d(c[1], w, L_DOMAIN, periodic[1], dx[1], ny)
+            X[s] += A * gy[:, None] * gx[None, :]
+    X = np.maximum(X, 1.0e-10)
+    X /= X.sum(axis=0, keepdims=True)
+
+    def smooth():
+        f = np.zeros((ny, nx))
+        for _ in range(8):
+            kx, ky = rng.integers(1, 5, size=2)
+            px, py = rng.uniform(0, 2 * math.pi, size=2)
+            f += rng.normal() * np.cos(2 * math.pi * ky * y / L_DOMAIN + py)[:, None] * \
+                np.cos(2 * math.pi * kx * x / L_DOMAIN + px)[None, :]
+        return f / math.sqrt(float(np.mean(f * f)))
+
+    rho = rho0[:, None] * (1.0 + rho_pert * smooth()) if rho_pert else np.repeat(rho0[:, None], nx, axis=1)
+    h = 1.0e17 + 1.0e16 * smooth()
+    rhoh = rho * h
+    rhoh0 = rhoh.mean(axis=1)
+    nscal = 4 + nspec
+    sold = np.zeros((nscal, 1, ny, nx))
+    sold[RHO, 0] = rho
+    sold[RHOH, 0] = rhoh
+    sold[TEMP, 0] = 1.0e8
+    sold[FIRSTSPEC:, 0] = rho[None] * X
+    # streamfunction at nodes; u = dpsi/dy on x faces, v = -dpsi/dx on y faces
+    xn = np.arange(nx + 1) * dx[0]
+    yn = np.arange(ny + 1) * dx[1]
+    psi = np.zeros((ny + 1, nx + 1))
+    for _ in range(8):
+        km, lm = rng.integers(1, 5, size=2)
+        phi = rng.uniform(0, 2 * math.pi)
+        a = rng.normal()
+        psi += a * np.sin(math.pi * km * yn / L_DOMAIN)[:, None] * np.cos(2 * math.pi * lm * xn / L_DOMAIN + phi)[None, :]
+    uf = (psi[1:, :] - psi[:-1, :]) / dx[1]          # x faces (ny, nx+1)
+    vf = -(psi[:, 1:] - psi[:, :-1]) / dx[0]         # y faces (ny+1, nx)
+    u = np.zeros((3, 1, ny, nx))
+    u[0, 0] = 0.5 * (uf[:, 1:] + uf[:, :-1])
+    u[1, 0] = 0.5 * (vf[1:, :] + vf[:-1, :])
+    cs = math.sqrt(5.0 / 3.0 * abs(GRAV) * H)
+    u *= 0.01 * cs / np.abs(u).max()
+    u = u[:2]
+    r_edge = np.arange(ny + 1) * dx[1]
+    w0 = np.zeros(ny + 1)
+    if w0_amp:
+        for m in range(1, 5):
+            w0 += rng.normal() * np.sin(m * math.pi * r_edge / L_DOMAIN)
+        w0 *= w0_amp / np.abs(w0).max()
+        w0[0] = 0.0
+    gpi = np.zeros((2, 1, ny, nx))
+    if gpi_amp:
+        for d in range(2):
+            gpi[d, 0] = gpi_amp * abs(GRAV) * rho0[:, None] * smooth()
+    umax_d = [float(np.abs(u[0]).max()), max(float(np.abs(u[1]).max()), float(np.abs(u[1]).max() + np.abs(w0).max()))]
+    umax = max(umax_d)
+    dt = cfl * min(dx[d] / umax_d[d] for d in range(2))
+    if boxes is None:
+        mg = max_grid or max(nx, ny)
+        boxes = [(b[0], b[1], 0, b[3], b[4], 0) for b in tile_boxes((nx, ny, 1), (mg, mg, 1))]
+    from .basestate import cell_to_edge
+    return dict(
+        dim=2, n=(nx, ny, 1), dx=dx, nspec=nspec, ppm_type=ppm_type, slope_order=slope_order,
+        bc_lo=(bc_lo[0], bc_lo[1], INTERIOR), bc_hi=(bc_hi[0], bc_hi[1], INTERIOR),
+        species_pred_type=species_pred_type, enthalpy_pred_type=enthalpy_pred_type,
+        evolve_base_state=evolve_base_state, dt=dt, rel_eps=1.0e-8 * umax, base_cutoff_density=1.0e3,
+        buoyancy_cutoff_factor=5.0, boxes=boxes, seed=seed,
+        uold=np.ascontiguousarray(u), sold=np.ascontiguousarray(sold), gpi=gpi, thermal=np.zeros((1, 1, ny, nx)),
+        rho0_old=rho0.copy(), rho0_new=rho0.copy(), rhoh0_old=rhoh0.copy(), rhoh0_new=rhoh0.copy(),
+        p0_old=p0.copy(), p0_new=p0.copy(), psi=np.zeros(ny), grav_cell=np.full(ny, GRAV),
+        w0_force=np.zeros(ny), w0=w0, rho0_predicted_edge=cell_to_edge(rho0),
+    )
+
+
+def config_c1(n=256, nspec=3, seed=20261203):
+    """Config 1: 2-D single level, one n x n box, NumSpec 3, ppm_type 1, w0 = 0, x periodic,
+    y slipwall (lo) / outflow (hi)."""
+    return planar_config_2d(n=(n, n), nspec=nspec, ppm_type=1, seed=seed)

@@ -30,6 +30,7 @@ static HBox valid_box(const Ctx& c, int b, int nodal) {
 }
 
 const RegionTable& region(Ctx& c, int glo0, int glo1, int glo2, int ghi0, int ghi1, int ghi2, int nodal, int slab) {
+    if (c.ndim == 2) glo2 = ghi2 = 0;
     std::array<int, 8> key{glo0, glo1, glo2, ghi0, ghi1, ghi2, nodal, slab};
     auto it = c.regions.find(key);
     if (it != c.regions.end()) return it->second;
@@ -121,7 +122,7 @@ const CopyTable& copy_table(Ctx& c, int ng, int nodal) {
     for (int b = 0; b < c.nb; ++b) {
         HBox vb = valid_box(c, b, nodal);
         HBox gb = vb;
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             gb.lo[d] -= ng;
             gb.hi[d] += ng;
         }
@@ -133,7 +134,8 @@ const CopyTable& copy_table(Ctx& c, int ng, int nodal) {
         std::vector<Cand> cands;
         for (int cbx = 0; cbx < c.nb; ++cbx) {
             HBox sv = valid_box(c, cbx, nodal);
-            for (int sz = -1; sz <= 1; ++sz)
+            const int zs = c.ndim == 2 ? 0 : 1;
+            for (int sz = -zs; sz <= zs; ++sz)
                 for (int sy = -1; sy <= 1; ++sy)
                     for (int sx = -1; sx <= 1; ++sx) {
                         int s[3] = {sx, sy, sz};
@@ -251,7 +253,7 @@ static void field_specs(Ctx& c) {
     }
     S(F_VELFORCE, 3, 1);
     S(F_SCALFORCE, c.nscal, 1);
-    S(F_ETA, 1, 0, 2);
+    S(F_ETA, 1, 0, c.ndim - 1);
     S(F_RHO0CART, 1, 1);
     S(F_RHOH0CART, 1, 1);
     S(F_S0ECART, 1, 1);
@@ -410,33 +412,35 @@ static void addw0_h(Hier& H, int f0, double mult) {
 
 // ------------------------------------------------------------------ stage pieces
 static void w0_carts(Hier& H) {
+    const int nd = H[0].ndim;
     // Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1)  (Source/MaestroAdvance.cpp:326)
-    put1d_h(H, F_W0CART, "w0", 2, 3, 1, BCS_U, 0, 1, -1);
+    put1d_h(H, F_W0CART, "w0", nd - 1, nd, 1, BCS_U, 0, 1, -1);
     // Put1dArrayOnCart(w0_force, w0_force_cart, false, true, bcs_f, 0) (:341), evolve_base_state only
     for (auto* c : H.L) set_val(*c, F_W0FCART, 0.0, 0, 3, 1);
-    if (H[0].P.evolve_base_state) put1d_h(H, F_W0FCART, "w0_force", 2, 3, 0, BCS_F, 0, 0, -1);
+    if (H[0].P.evolve_base_state) put1d_h(H, F_W0FCART, "w0_force", nd - 1, nd, 0, BCS_F, 0, 0, -1);
 }
 
 // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-259)
 static void make_vel_force_h(Hier& H) {
-    put1d_h(H, F_GRAVCART, "grav_cell", 2, 3, 0, BCS_F, 0, 0, -1);
+    const int nd = H[0].ndim;
+    put1d_h(H, F_GRAVCART, "grav_cell", nd - 1, nd, 0, BCS_F, 0, 0, -1);
     put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
     for (auto* c : H.L) make_vel_force(*c);
-    average_down_h(H, F_VELFORCE, 0, 3);
-    fill_patch_h(H, F_VELFORCE, 0, 3, BCS_U, 0, 1, -1);
+    average_down_h(H, F_VELFORCE, 0, nd);
+    fill_patch_h(H, F_VELFORCE, 0, nd, BCS_U, 0, 1, -1);
 }
 
 // Maestro::AdvancePremac (Source/MaestroAdvection.cpp:7-84) on the internal fields.
 static void advance_premac(Hier& H) {
-    const int nga = H[0].ng_adv;
-    fill_patch_h(H, F_UTILDE, 0, 3, BCS_U, 0, 1, -1);
+    const int nga = H[0].ng_adv, nd = H[0].ndim;
+    fill_patch_h(H, F_UTILDE, 0, nd, BCS_U, 0, 1, -1);
     for (auto* c : H.L) {
         set_val(*c, F_UFULL, 0.0, 0, 3, nga);
-        copy_fab(*c, F_UFULL, 0, F_W0CART, 0, 3, 0);
+        copy_fab(*c, F_UFULL, 0, F_W0CART, 0, nd, 0);
     }
-    fill_patch_h(H, F_UFULL, 0, 3, BCS_U, 0, 1, -1);
+    fill_patch_h(H, F_UFULL, 0, nd, BCS_U, 0, 1, -1);
     for (auto* c : H.L) {
-        add_fab(*c, F_UFULL, F_UTILDE, 3, nga);
+        add_fab(*c, F_UFULL, F_UTILDE, nd, nga);
         for (int d = 0; d < 3; ++d) set_val(*c, F_UTRANS0 + d, 0.0, 0, 1, 1);
     }
     for (auto* c : H.L) make_utrans(*c);
@@ -461,7 +465,7 @@ static void make_rhoh_force_h(Hier& H, int is_prediction, int add_thermal, int w
     put1d_h(H, F_P0CART, which_step == 1 ? "p0_old" : "p0_avg", 0, 1, 0, BCS_F, 0, 0, -1);
     put1d_h(H, F_PSICART, "psi", 0, 1, 0, BCS_F, 0, 0, -1);
     put1d_h(H, F_RHO0CART, which_step == 1 ? "rho0_old" : "rho0_avg", 0, 1, 0, BCS_S, RHO, 0, RHO);
-    put1d_h(H, F_GRAVCART, "grav_cell", 2, 3, 0, BCS_F, 0, 0, -1);
+    put1d_h(H, F_GRAVCART, "grav_cell", H[0].ndim - 1, H[0].ndim, 0, BCS_F, 0, 0, -1);
     for (auto* c : H.L) make_rhoh_force(*c, is_prediction, add_thermal);
     average_down_h(H, F_SCALFORCE, RHOH, 1);
     fill_patch_h(H, F_SCALFORCE, RHOH, 1, BCS_F, 0, 0, RHOH);
@@ -568,17 +572,17 @@ struct StageIO {
 
 static int bind_stage(Ctx& c, const StageIO& io) {
     int rc;
-    if ((rc = bind(c, U_UOLD, io.uold, 3, -1, 0))) return rc;
+    if ((rc = bind(c, U_UOLD, io.uold, c.ndim, -1, 0))) return rc;
     if ((rc = bind(c, U_SOLD, io.sold, c.nscal, -1, 0))) return rc;
-    if ((rc = bind(c, U_GPI, io.gpi, 3, -1, 0))) return rc;
+    if ((rc = bind(c, U_GPI, io.gpi, c.ndim, -1, 0))) return rc;
     if ((rc = bind(c, U_THERMAL, io.thermal, 1, -1, 0))) return rc;
     if ((rc = bind(c, U_SNEW, io.snew, c.nscal, -1, 0))) return rc;
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < c.ndim; ++d) {
         if (io.umac && (rc = bind(c, U_UMAC0 + d, &io.umac[d], 1, d, 0))) return rc;
         if (io.sedge && (rc = bind(c, U_SEDGE0 + d, &io.sedge[d], c.nscal, d, 0))) return rc;
         if (io.sflux && (rc = bind(c, U_SFLUX0 + d, &io.sflux[d], c.nscal, d, 0))) return rc;
     }
-    if ((rc = bind(c, U_ETA, io.eta, 1, 2, 0))) return rc;
+    if ((rc = bind(c, U_ETA, io.eta, 1, c.ndim - 1, 0))) return rc;
     return upload_user_views(c);
 }
 
@@ -589,13 +593,13 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
         Ctx& c = H[l];
         if (!c.dry) cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream);
         set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
-        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, 0);
+        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, c.ndim, 0);
         copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
     }
     fill_patch_h(H, F_SOLD, 0, H[0].nscal, BCS_S, 0, 0, 0);
     for (int l = 0; l < H.n(); ++l) {
         Ctx& c = H[l];
-        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, 3, 0);
+        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, c.ndim, 0);
         set_val(c, F_THERMAL, 0.0, 0, 1, 1);
         if (io[l].thermal) copy_fab(c, F_THERMAL, 0, F_USER + U_THERMAL, 0, 1, 0);
         set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
@@ -623,7 +627,7 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
             copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
         }
         copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             if (io[l].umac) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
             if (io[l].sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
             if (io[l].sflux) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);
@@ -700,11 +704,16 @@ static int init_level(Ctx& c, const madv_params& p, int lev) {
         c.P.dom_lo[d] = p.dom_lo[d] * r;
         c.P.dom_hi[d] = (p.dom_hi[d] + 1) * r - 1;
     }
+    c.ndim = p.dim == 2 ? 2 : 3;
+    if (c.ndim == 2) {
+        c.P.dom_lo[2] = c.P.dom_hi[2] = 0;
+        c.P.phys_bc_lo[2] = c.P.phys_bc_hi[2] = PB_INTERIOR;
+    }
     c.nspec = p.nspec;
     c.nscal = 4 + p.nspec;
     c.ng_s = c.ng_adv = p.ppm_type == 2 ? 4 : 3;
-    c.nr = c.P.dom_hi[2] - c.P.dom_lo[2] + 1;
-    for (int d = 0; d < 3; ++d) c.per[d] = p.phys_bc_lo[d] == PB_INTERIOR;
+    c.nr = c.P.dom_hi[c.ndim - 1] - c.P.dom_lo[c.ndim - 1] + 1;
+    for (int d = 0; d < 3; ++d) c.per[d] = c.P.phys_bc_lo[d] == PB_INTERIOR;
     int rc = bc_setup(c);
     if (rc) return rc;
     BCRecD all[2 * MAX_SCAL + 3];
@@ -855,7 +864,16 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
         set_error("dt must be > 0 and rel_eps >= 0");
         return MADV_ERR_PARAM;
     }
-    for (int d = 0; d < 3; ++d) {
+    const int nd = p->dim == 2 ? 2 : 3;
+    if (p->dim != 0 && p->dim != 2 && p->dim != 3) {
+        set_error("dim must be 2 or 3");
+        return MADV_ERR_PARAM;
+    }
+    if (nd == 2 && (p->dom_lo[2] != 0 || p->dom_hi[2] != 0)) {
+        set_error("a 2-D domain has z = [0, 0]");
+        return MADV_ERR_PARAM;
+    }
+    for (int d = 0; d < nd; ++d) {
         const int lo = p->phys_bc_lo[d], hi = p->phys_bc_hi[d];
         if (lo < 0 || lo > 5 || hi < 0 || hi > 5) {
             set_error("invalid phys_bc");
@@ -879,8 +897,8 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
             return MADV_ERR_PARAM;
         }
     }
-    if (p->dom_lo[2] != 0) {
-        set_error("the radial (z) domain must start at 0");
+    if (p->dom_lo[nd - 1] != 0) {
+        set_error("the radial domain (z, or y in 2-D) must start at 0");
         return MADV_ERR_PARAM;
     }
     madv_ctx* h = new madv_ctx();
@@ -914,8 +932,8 @@ int madv_set_dt(madv_ctx* h, double dt, double rel_eps) {
 
 int madv_set_layout_levels(madv_ctx* h, int nlev, const int* nboxes, const madv_box* boxes) {
     if (!h || nlev < 1 || !nboxes || !boxes) return MADV_ERR_PARAM;
-    if (nlev > 2) {
-        set_error("at most two levels (refinement ratio 2)");
+    if (nlev > 2 || (nlev > 1 && h->c.ndim == 2)) {
+        set_error("at most two levels (refinement ratio 2), one in 2-D");
         return MADV_ERR_UNSUPPORTED;
     }
     for (auto& f : h->fine) destroy_level(*f);
@@ -1114,7 +1132,7 @@ static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab*
                 for (auto m3 : {io[l].umac, io[l].sedge, io[l].sflux}) {
                     key.push_back(m3);
                     if (m3)
-                        for (int d = 0; d < 3; ++d)
+                        for (int d = 0; d < H[l].ndim; ++d)
                             for (int b = 0; b < m3[d].nfab; ++b) key.push_back(m3[d].fab[b].p);
                 }
             }
@@ -1196,22 +1214,22 @@ int madv_advance_premac(madv_ctx* h, const madv_multifab* uold, const madv_multi
     Ctx& c = h->c;
     if (!uold || !sold || !gpi || !umac) return MADV_ERR_PARAM;
     try {
-        if ((rc = bind(c, U_UOLD, uold, 3, -1, 0)) || (rc = bind(c, U_SOLD, sold, 1, -1, 0)) ||
-            (rc = bind(c, U_GPI, gpi, 3, -1, 0)))
+        if ((rc = bind(c, U_UOLD, uold, c.ndim, -1, 0)) || (rc = bind(c, U_SOLD, sold, 1, -1, 0)) ||
+            (rc = bind(c, U_GPI, gpi, c.ndim, -1, 0)))
             return rc;
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 0))) return rc;
             if (utrans && (rc = bind(c, U_UTRANS0 + d, &utrans[d], 1, d, 0))) return rc;
         }
         if ((rc = upload_user_views(c))) return rc;
         set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
-        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, 0);
+        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, c.ndim, 0);
         copy_fab(c, F_SOLD, RHO, F_USER + U_SOLD, RHO, 1, 0);
-        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, 3, 0);
-        for (int d = 0; d < 3; ++d) set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
+        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, c.ndim, 0);
+        for (int d = 0; d < c.ndim; ++d) set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
         w0_carts(H);
         advance_premac(H);
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
             if (utrans) copy_fab(c, F_USER + U_UTRANS0 + d, 0, F_UTRANS0 + d, 0, 1, 0);
         }
@@ -1228,12 +1246,12 @@ int madv_addw0(madv_ctx* h, const madv_multifab* umac, double mult, void* stream
     Ctx& c = h->c;
     if (!umac) return MADV_ERR_PARAM;
     try {
-        for (int d = 0; d < 3; ++d)
+        for (int d = 0; d < c.ndim; ++d)
             if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 1))) return rc;
         if ((rc = upload_user_views(c))) return rc;
-        for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
+        for (int d = 0; d < c.ndim; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
         addw0_h(H, F_UMAC0, mult);
-        for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
+        for (int d = 0; d < c.ndim; ++d) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
         return finish(H);
     } catch (const Fail& f) {
         return f.code;
@@ -1254,9 +1272,9 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
     if (!sold || !snew || !umac) return MADV_ERR_PARAM;
     try {
         if ((rc = bind(c, U_SOLD, sold, c.nscal, -1, 0)) || (rc = bind(c, U_SNEW, snew, c.nscal, -1, 0)) ||
-            (rc = bind(c, U_ETA, eta, 1, 2, 0)) || (rc = bind(c, U_THERMAL, thermal, 1, -1, 0)))
+            (rc = bind(c, U_ETA, eta, 1, c.ndim - 1, 0)) || (rc = bind(c, U_THERMAL, thermal, 1, -1, 0)))
             return rc;
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 1))) return rc;
             if (sedge && (rc = bind(c, U_SEDGE0 + d, &sedge[d], c.nscal, d, 0))) return rc;
             if (sflux && (rc = bind(c, U_SFLUX0 + d, &sflux[d], c.nscal, d, 0))) return rc;
@@ -1265,7 +1283,7 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
         copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
         fill_patch_h(H, F_SOLD, 0, c.nscal, BCS_S, 0, 0, 0);
         copy_fab(c, F_SNEW, 0, F_USER + U_SNEW, 0, c.nscal, 0);
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
             if (sedge) copy_fab(c, F_SEDGE0 + d, 0, F_USER + U_SEDGE0 + d, 0, c.nscal, 0);
             if (sflux) copy_fab(c, F_SFLUX0 + d, 0, F_USER + U_SFLUX0 + d, 0, c.nscal, 0);
@@ -1285,7 +1303,7 @@ static int scalar_advance(madv_ctx* h, int which, int which_step, const madv_mul
             copy_fab(c, F_USER + U_SNEW, RHOH, F_SNEW, RHOH, 1, 0);
         }
         copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
-        for (int d = 0; d < 3; ++d) {
+        for (int d = 0; d < c.ndim; ++d) {
             copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
             if (sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
             if (sflux) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);

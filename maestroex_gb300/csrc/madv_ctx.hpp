@@ -87,6 +87,7 @@ struct CopyTable {
 struct Ctx {
     madv_params P{};  // dx, domain and base_cutoff_density_coord are this level's
     int lev = 0;
+    int ndim = 3;     // 2: the 2-D form (y radial, k = 0 only, regions never grow in z)
     int nspec = 0, nscal = 0, ng_s = 3, ng_adv = 3, nr = 0;
     bool per[3] = {false, false, false};
     std::vector<HBox> ba;
@@ -184,6 +185,23 @@ int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int
                 const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
                 const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
+
+// ---- 2-D forms (madv_kernels.cu), reached through the wrappers above when c.ndim == 2
+void put1d_2d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge);
+void addw0_2d(Ctx& c, int f0, double mult);
+void make_utrans_2d_entry(Ctx& c);
+void make_vel_force_2d(Ctx& c);
+void vel_pred_2d_entry(Ctx& c);
+void make_edge_scal_2d_entry(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons);
+void modify_scal_force_2d(Ctx& c, int comp, int s0cart_fid, int fullform);
+void make_rhoh_force_2d(Ctx& c, int is_prediction, int add_thermal);
+void put_in_pert_form_2d(Ctx& c, const double* d_s0, int comp, int flag);
+void make_rhox_flux_2d(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
+                       const double* r0e_new);
+void make_rhoh_flux_2d(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
+                       const double* rh0e_new);
+void sum_species_edges_2d(Ctx& c);
+void update_scal_2d(Ctx& c, int start_comp);
 
 // ---- coarse-fine operations between level cf and its parent cc (madv_amr.cu)
 int build_owner(Ctx& c);  // owner map of the level's domain (host + device)

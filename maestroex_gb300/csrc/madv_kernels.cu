@@ -60,6 +60,7 @@ __global__ void k_put1d(KARGS, int f, const double* __restrict__ s0, int outcomp
 }
 
 void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge) {
+    if (c.ndim == 2) return put1d_2d(c, fid, d_s0, outcomp, edge);
     launch(c, rg_grow(c, 0), 1, k_put1d, c.V(), fid, d_s0, outcomp, edge);
 }
 
@@ -236,6 +237,7 @@ __global__ void k_addw0(KARGS, int f, const double* __restrict__ w0, double mult
 }
 
 void addw0(Ctx& c, int f0, double mult) {
+    if (c.ndim == 2) return addw0_2d(c, f0, mult);
     launch(c, region(c, 1, 1, 0, 1, 1, 0, 2), 1, k_addw0, c.V(), f0 + 2, (const double*)c.b1("w0"), mult);
 }
 
@@ -576,6 +578,7 @@ __global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, 
 }
 
 void make_utrans(Ctx& c) {
+    if (c.ndim == 2) return make_utrans_2d_entry(c);
     const double dt2 = 0.5 * c.P.dt;
     if (c.P.ppm_type != 0)
         launch(c, rg_grow(c, 1), 1, k_trace_cell, c.V(), F_UFULL, c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2]);
@@ -614,6 +617,7 @@ __global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz) {
 
 // valid cells of one level; F_GRAVCART and F_RHO0CART are filled by the caller
 void make_vel_force(Ctx& c) {
+    if (c.ndim == 2) return make_vel_force_2d(c);
     set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
     launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
            c.P.dom_hi[2], make_recip(2.0 * c.P.dx[2]));
@@ -817,6 +821,7 @@ static void vp_velocities_launch(Ctx& c) {
 }
 
 void vel_pred(Ctx& c) {
+    if (c.ndim == 2) return vel_pred_2d_entry(c);
     if (c.P.ppm_type == 0) {
         slope_any(c, 0, F_UTILDE, 0, F_IPC0, 0, 3, bcs_dev(c, BCS_U), 0);  // slopex -> Ipu
         slope_any(c, 1, F_UTILDE, 0, F_IMC1, 0, 3, bcs_dev(c, BCS_U), 0);  // slopey -> Imv
@@ -1037,6 +1042,7 @@ static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int
 
 // force_zero: the components' force is identically zero (DensityAdvance species)
 void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons, int force_zero) {
+    if (c.ndim == 2) return make_edge_scal_2d_entry(c, start_comp, num_comp, which_bcs, is_cons);
     const BCRecD* bh = bcs_host(c, which_bcs);
     if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), make_recip(c.P.dx[0]));
     // velocity-only quantities shared by every component of this call
@@ -1088,6 +1094,7 @@ __global__ void k_modify_scal_force(KARGS, int comp, int s0cart, int fullform, R
 
 // valid cells of one level; F_S0ECART and the s0 cart field are filled by the caller
 void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform) {
+    if (c.ndim == 2) return modify_scal_force_2d(c, comp, s0cart_fid, fullform);
     launch(c, rg_grow(c, 0), 1, k_modify_scal_force, c.V(), comp, s0cart_fid, fullform, make_recip(c.P.dx[0]),
            make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
 }
@@ -1115,6 +1122,7 @@ __global__ void k_rhoh_force(KARGS, int cutoff, int domhi, RecipC rdz, int psi_i
 // valid cells of one level; F_P0CART, F_PSICART, F_RHO0CART and F_GRAVCART are filled by
 // the caller (which_step 1: rho0_old and p0_old)
 void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal) {
+    if (c.ndim == 2) return make_rhoh_force_2d(c, is_prediction, add_thermal);
     const int ept = c.P.enthalpy_pred_type;
     const int psi_in = (is_prediction == 1 && ept == 2) || (is_prediction == 1 && ept == 0) || (is_prediction == 0);
     launch(c, rg_grow(c, 0), 1, k_rhoh_force, c.V(), c.P.base_cutoff_density_coord, c.P.dom_hi[2],
@@ -1130,6 +1138,7 @@ __global__ void k_pert(KARGS, int comp, const double* __restrict__ s0, int flag)
 }
 
 void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag) {
+    if (c.ndim == 2) return put_in_pert_form_2d(c, d_s0, comp, flag);
     launch(c, rg_grow(c, 0), 1, k_pert, c.V(), comp, d_s0, flag);
 }
 
@@ -1176,6 +1185,7 @@ __global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double*
 }
 
 void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new, const double* r0e_new) {
+    if (c.ndim == 2) return make_rhox_flux_2d(c, r0_old, r0e_old, r0_new, r0e_new);
     const int do_eta = c.P.evolve_base_state && !c.P.use_exact_base_state;
     const double* w0 = c.b1("w0");
     const double* rpe = c.b1("rho0_predicted_edge");
@@ -1203,6 +1213,7 @@ __global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const 
 
 void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
                     const double* rh0e_new) {
+    if (c.ndim == 2) return make_rhoh_flux_2d(c, rh0_old, rh0e_old, rh0_new, rh0e_new);
     const int ept = c.P.enthalpy_pred_type;
     launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux<0>, c.V(), ept, rh0_old, rh0_new);
     launch(c, rg_grow(c, 0, 1), 1, k_rhoh_flux<1>, c.V(), ept, rh0_old, rh0_new);
@@ -1220,6 +1231,7 @@ __global__ void k_sum_species(KARGS, int nspec) {
 }
 
 void sum_species_edges(Ctx& c) {
+    if (c.ndim == 2) return sum_species_edges_2d(c);
     launch(c, rg_grow(c, 0, 0), 1, k_sum_species<0>, c.V(), c.nspec);
     launch(c, rg_grow(c, 0, 1), 1, k_sum_species<1>, c.V(), c.nspec);
     launch(c, rg_grow(c, 0, 2), 1, k_sum_species<2>, c.V(), c.nspec);
@@ -1282,6 +1294,7 @@ __global__ void k_update_rhoh(KARGS, double dt, RecipC r0, RecipC r1, RecipC r2,
 }
 
 void update_scal(Ctx& c, int start_comp) {
+    if (c.ndim == 2) return update_scal_2d(c, start_comp);
     const RegionTable& rt = rg_grow(c, 0);
     if (start_comp == RHOH) {
         launch(c, rt, 1, k_update_rhoh, c.V(), c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
@@ -1290,6 +1303,571 @@ void update_scal(Ctx& c, int start_comp) {
         launch(c, rt, 1, k_update_rhox, c.V(), c.nspec, c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
                make_recip(c.P.dx[2]), 0.5 * c.P.base_cutoff_density);
     }
+}
+
+}  // namespace madv
+
+// ============================================================ 2-D (AMREX_SPACEDIM == 2)
+// The 2-D form of the stage: y is radial (base-state index r = j), boxes and the domain
+// have k = 0 only, two velocity components.  Regions of a 2-D context never grow in z.
+// PPM, the limited slopes, the fills and the x-face transverse velocity are the 3-D
+// kernels run in x and y; the kernels below restate the 2-D branches of the reference
+// (their expressions and quirks differ from 3-D), with plain IEEE division.
+namespace madv {
+
+static const RegionTable& rg2(Ctx& c, int g, int nodal = -1) { return region(c, g, g, 0, g, g, 0, nodal); }
+
+// Put1dArrayOnCart, planar 2-D (Source/MaestroFill3dData.cpp:79-93): r = j
+__global__ void k_put1d_2d(KARGS, int f, const double* __restrict__ s0, int outcomp, int edge) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    at(VW(f), i, j, k, outcomp) = edge ? 0.5 * (s0[j] + s0[j + 1]) : s0[j];
+}
+
+// Addw0, planar 2-D (Source/MaestroFill3dData.cpp:380-386): vedge += mult * w0(j)
+__global__ void k_addw0_2d(KARGS, int f, const double* __restrict__ w0, double mult) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    at(VW(f), i, j, k) += mult * w0[j];
+}
+
+// MakeUtrans, 2-D y faces (Source/MaestroMakeUtrans.cpp:161-266): the lo-side wall case
+// sets vry = 0 twice and leaves vly; the solve tests v + w0_cart.
+__global__ void k_utrans_2dy(KARGS, int ppm_type, double dt2dy, int bclo, int bchi, int domlo, int domhi,
+                             double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView ut = VW(F_UTILDE);
+    double l, r;
+    if (ppm_type == 0) {
+        const FabView uf = VW(F_UFULL), sl = VW(F_SLOPE);
+        l = at(ut, i, j - 1, k, 1) + (0.5 - dt2dy * mx(0.0, at(uf, i, j - 1, k, 1))) * at(sl, i, j - 1, k, 0);
+        r = at(ut, i, j, k, 1) - (0.5 + dt2dy * mn(0.0, at(uf, i, j, k, 1))) * at(sl, i, j, k, 0);
+    } else {
+        l = at(VW(F_IPC0 + 1), i, j - 1, k, 1);
+        r = at(VW(F_IMC0 + 1), i, j, k, 1);
+    }
+    if (j == domlo) {
+        switch (bclo) {
+            case PB_INFLOW: l = at(ut, i, j - 1, k, 1); r = l; break;
+            case PB_SLIPWALL: case PB_NOSLIPWALL: case PB_SYMMETRY: r = 0.0; break;
+            case PB_OUTFLOW: l = mn(r, 0.0); r = l; break;
+            default: break;
+        }
+    } else if (j == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW: l = at(ut, i, j, k, 1); r = l; break;
+            case PB_SLIPWALL: case PB_NOSLIPWALL: case PB_SYMMETRY: l = 0.0; r = 0.0; break;
+            case PB_OUTFLOW: l = mx(l, 0.0); r = l; break;
+            default: break;
+        }
+    }
+    const double w0c = at(VW(F_W0CART), i, j, k, 1);
+    const bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fabs(l + r + 2.0 * w0c) < rel_eps);
+    double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+    at(VW(F_UTRANS1), i, j, k) = test ? 0.0 : v;
+}
+
+static void make_utrans_2d(Ctx& c) {
+    const double dt2 = 0.5 * c.P.dt;
+    if (c.P.ppm_type != 0)
+        launch(c, rg2(c, 1), 1, k_trace_cell, c.V(), F_UFULL, c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2]);
+    for (int d = 0; d < 2; ++d) {
+        if (c.P.ppm_type == 0) slope_any(c, d, F_UTILDE, d, F_SLOPE, 0, 1, bcs_dev(c, BCS_U), d);
+        else ppm_any(c, d, F_UTILDE, d, c.bcs_u[d], F_UFULL, d, 0, F_IPC0 + d, F_IMC0 + d);
+        const RegionTable& rt = rg2(c, 0, d);
+        const double dt2dx = dt2 / c.P.dx[d];
+        const int bl = c.P.phys_bc_lo[d], bh = c.P.phys_bc_hi[d], dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
+        if (d == 0) launch(c, rt, 1, k_utrans<0>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+        else launch(c, rt, 1, k_utrans_2dy, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+    }
+}
+
+// MakeVelForce, planar 2-D (Source/MaestroForce.cpp:100-137)
+__global__ void k_vel_force_2d(KARGS, double cutoff_rho, int domhi, double dy) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView gpi = VW(F_GPI), rho = VW(F_SOLD), vf = VW(F_VELFORCE);
+    const double r = at(rho, i, j, k, RHO);
+    double rhopert = r - at(VW(F_RHO0CART), i, j, k);
+    if (r < cutoff_rho) rhopert = 0.0;
+    at(vf, i, j, k, 0) = -at(gpi, i, j, k, 0) / r;
+    double f1 = (rhopert * at(VW(F_GRAVCART), i, j, k, 1) - at(gpi, i, j, k, 1)) / r - at(VW(F_W0FCART), i, j, k, 1);
+    if (j <= -1 || j >= domhi) {
+    } else {
+        const FabView ve = VW(F_UTRANS1), w0 = VW(F_W0CART);
+        f1 -= (at(ve, i, j + 1, k) + at(ve, i, j, k)) * (at(w0, i, j + 1, k, 1) - at(w0, i, j, k, 1)) / (2.0 * dy);
+    }
+    at(vf, i, j, k, 1) = f1;
+}
+
+// VelPredInterface, 2-D (Source/MaestroVelPred.cpp:296-537).  D = 0: ulx/urx/uimhx into
+// F_SL0/F_SR0/F_SIMH0; D = 1: uly/ury/uimhy into F_SL1/F_SR1/F_SIMH1.
+template <int D>
+__global__ void k_vp_interface_2d(KARGS, int ppm_type, double dt2h, int bclo, int bchi, int domlo, int domhi,
+                                  double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1;
+    constexpr int T = 1 - D;  // the transverse component upwinded into uimh
+    const int I = D == 0 ? i : j;
+    const FabView ut = VW(F_UTILDE), uf = VW(F_UFULL);
+    const FabView l = VW(F_SL0 + D), r = VW(F_SR0 + D);
+    double L[2], Rr[2];
+    if (ppm_type == 0) {
+        const double maxu = mx(0.0, at(uf, i - di, j - dj, k, D));
+        const double minu = mn(0.0, at(uf, i, j, k, D));
+        const FabView sl = D == 0 ? VW(F_IPC0) : VW(F_IMC1);
+        for (int n = 0; n < 2; ++n) {
+            L[n] = at(ut, i - di, j - dj, k, n) + (0.5 - dt2h * maxu) * at(sl, i - di, j - dj, k, n);
+            Rr[n] = at(ut, i, j, k, n) - (0.5 + dt2h * minu) * at(sl, i, j, k, n);
+        }
+    } else {
+        for (int n = 0; n < 2; ++n) {
+            L[n] = at(VW(F_IPC0 + n), i - di, j - dj, k, D);
+            Rr[n] = at(VW(F_IMC0 + n), i, j, k, D);
+        }
+    }
+    if (I == domlo) {
+        switch (bclo) {
+            case PB_INFLOW:
+                for (int n = 0; n < 2; ++n) L[n] = Rr[n] = at(ut, i - di, j - dj, k, n);
+                break;
+            case PB_SLIPWALL: case PB_SYMMETRY:
+                if (D == 0) {
+                    L[0] = 0.0;
+                    Rr[0] = 0.0;
+                    L[1] = Rr[1];
+                } else {
+                    L[0] = Rr[0];
+                    L[1] = 0.0;
+                    Rr[1] = 0.0;
+                }
+                break;
+            case PB_NOSLIPWALL:
+                for (int n = 0; n < 2; ++n) L[n] = Rr[n] = 0.0;
+                break;
+            case PB_OUTFLOW:
+                if (D == 0) {
+                    Rr[0] = mn(Rr[0], 0.0);
+                    for (int n = 0; n < 2; ++n) Rr[n] = L[n];
+                } else {
+                    Rr[1] = mn(Rr[1], 0.0);
+                    for (int n = 0; n < 2; ++n) L[n] = Rr[n];
+                }
+                break;
+            default: break;
+        }
+    } else if (I == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW:
+                for (int n = 0; n < 2; ++n) L[n] = Rr[n] = at(ut, i, j, k, n);
+                break;
+            case PB_SLIPWALL: case PB_SYMMETRY:
+                if (D == 0) {
+                    L[0] = 0.0;
+                    Rr[0] = 0.0;
+                    Rr[1] = L[1];
+                } else {
+                    Rr[0] = L[0];
+                    L[1] = 0.0;
+                    Rr[1] = 0.0;
+                }
+                break;
+            case PB_NOSLIPWALL:
+                for (int n = 0; n < 2; ++n) L[n] = Rr[n] = 0.0;
+                break;
+            case PB_OUTFLOW:
+                L[D] = mx(L[D], 0.0);
+                for (int n = 0; n < 2; ++n) Rr[n] = L[n];
+                break;
+            default: break;
+        }
+    }
+    for (int n = 0; n < 2; ++n) {
+        at(l, i, j, k, n) = L[n];
+        at(r, i, j, k, n) = Rr[n];
+    }
+    const double tr = at(VW(F_UTRANS0 + D), i, j, k);
+    const double v = tr > 0.0 ? L[T] : Rr[T];
+    at(VW(F_SIMH0 + D), i, j, k, T) = fabs(tr) < rel_eps ? 0.5 * (L[T] + Rr[T]) : v;
+}
+
+// VelPredVelocities, 2-D (Source/MaestroVelPred.cpp:539-727)
+template <int D>
+__global__ void k_vp_velocities_2d(KARGS, double dt2, double dt4h, int bclo, int bchi, int domlo, int domhi,
+                                   double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1;
+    constexpr int T = 1 - D;
+    constexpr int ti = T == 0, tj = T == 1;
+    const int I = D == 0 ? i : j;
+    const int il = i - di, jl = j - dj;
+    const FabView f = VW(F_VELFORCE), ttr = VW(F_UTRANS0 + T), q = VW(F_SIMH0 + T);
+    const double fl = at(f, il, jl, k, D), fr = at(f, i, j, k, D);
+    const double ml = at(VW(F_SL0 + D), i, j, k, D) -
+                      dt4h * (at(ttr, il + ti, jl + tj, k) + at(ttr, il, jl, k)) *
+                          (at(q, il + ti, jl + tj, k, D) - at(q, il, jl, k, D)) +
+                      dt2 * fl;
+    const double mr = at(VW(F_SR0 + D), i, j, k, D) -
+                      dt4h * (at(ttr, i + ti, j + tj, k) + at(ttr, i, j, k)) *
+                          (at(q, i + ti, j + tj, k, D) - at(q, i, j, k, D)) +
+                      dt2 * fr;
+    double v;
+    if (D == 0) {
+        v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+        v = (ml <= 0.0 && mr >= 0.0) || (fabs(ml + mr) < rel_eps) ? 0.0 : v;
+    } else {
+        const double w0c = at(VW(F_W0CART), i, j, k, 1);
+        const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fabs(ml + mr + 2.0 * w0c) < rel_eps);
+        v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+        v = test ? 0.0 : v;
+    }
+    const FabView ut = VW(F_UTILDE);
+    if (I == domlo) {
+        switch (bclo) {
+            case PB_INFLOW: v = at(ut, il, jl, k, D); break;
+            case PB_SLIPWALL: case PB_NOSLIPWALL: case PB_SYMMETRY: v = 0.0; break;
+            case PB_OUTFLOW: v = mn(mr, 0.0); break;
+            default: break;
+        }
+    } else if (I == domhi + 1) {
+        switch (bchi) {
+            case PB_INFLOW: v = at(ut, i, j, k, D); break;
+            case PB_SLIPWALL: case PB_NOSLIPWALL: case PB_SYMMETRY: v = 0.0; break;
+            case PB_OUTFLOW: v = mx(ml, 0.0); break;
+            default: break;
+        }
+    }
+    at(VW(F_UMAC0 + D), i, j, k) = v;
+}
+
+static void vel_pred_2d(Ctx& c) {
+    if (c.P.ppm_type == 0) {
+        slope_any(c, 0, F_UTILDE, 0, F_IPC0, 0, 2, bcs_dev(c, BCS_U), 0);  // slopex -> Ipu
+        slope_any(c, 1, F_UTILDE, 0, F_IMC1, 0, 2, bcs_dev(c, BCS_U), 0);  // slopey -> Imv
+    } else {
+        // component d along d was traced by make_utrans (same inputs)
+        ppm_any(c, 1, F_UTILDE, 0, c.bcs_u[0], F_UFULL, 1, 0, F_IPC0, F_IMC0);
+        ppm_any(c, 0, F_UTILDE, 1, c.bcs_u[1], F_UFULL, 0, 0, F_IPC0 + 1, F_IMC0 + 1);
+    }
+    const double dt2 = 0.5 * c.P.dt, dt4 = 0.25 * c.P.dt;
+    for (int d = 0; d < 2; ++d) {
+        const RegionTable& rm = region(c, d == 0 ? 0 : 1, d == 1 ? 0 : 1, 0, 1, 1, 0, -1);  // growLo(obx, d, -1)
+        const int bl = c.P.phys_bc_lo[d], bh = c.P.phys_bc_hi[d], dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
+        if (d == 0)
+            launch(c, rm, 1, k_vp_interface_2d<0>, c.V(), c.P.ppm_type, dt2 / c.P.dx[0], bl, bh, dl, dh, c.P.rel_eps);
+        else
+            launch(c, rm, 1, k_vp_interface_2d<1>, c.V(), c.P.ppm_type, dt2 / c.P.dx[1], bl, bh, dl, dh, c.P.rel_eps);
+    }
+    for (int d = 0; d < 2; ++d) {
+        const int bl = c.P.phys_bc_lo[d], bh = c.P.phys_bc_hi[d], dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
+        const double dt4h = dt4 / c.P.dx[1 - d];
+        if (d == 0) launch(c, rg2(c, 0, 0), 1, k_vp_velocities_2d<0>, c.V(), dt2, dt4h, bl, bh, dl, dh, c.P.rel_eps);
+        else launch(c, rg2(c, 0, 1), 1, k_vp_velocities_2d<1>, c.V(), dt2, dt4h, bl, bh, dl, dh, c.P.rel_eps);
+    }
+}
+
+// MakeEdgeScalPredictor, 2-D (Source/MaestroMakeEdgeScalars.cpp:306-452)
+template <int D>
+__global__ void k_es_predictor_2d(KARGS, int comp, int ppm_type, double dt2, double hd, int bclo, int bchi, int domlo,
+                                  int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1;
+    const int I = D == 0 ? i : j;
+    const FabView s = VW(F_SOLD), ud = VW(F_UMAC0 + D);
+    const double u = at(ud, i, j, k);
+    double l, r;
+    if (ppm_type == 0) {
+        const FabView sl = VW(F_SLOPE);
+        l = at(s, i - di, j - dj, k, comp) + (0.5 - dt2 * u / hd) * at(sl, i - di, j - dj, k, D);
+        r = at(s, i, j, k, comp) - (0.5 + dt2 * u / hd) * at(sl, i, j, k, D);
+    } else {
+        l = at(VW(F_IPC0), i - di, j - dj, k, D);
+        r = at(VW(F_IMC0), i, j, k, D);
+    }
+    if (I == domlo) {
+        if (bclo == BC_EXT_DIR) {
+            l = r = at(s, i - di, j - dj, k, comp);
+        } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
+            l = r;
+        } else if (bclo == BC_REFLECT_ODD) {
+            l = r = 0.0;
+        }
+    } else if (I == domhi + 1) {
+        if (bchi == BC_EXT_DIR) {
+            l = r = at(s, i, j, k, comp);
+        } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
+            r = l;
+        } else if (bchi == BC_REFLECT_ODD) {
+            l = r = 0.0;
+        }
+    }
+    at(VW(F_SL0 + D), i, j, k) = l;
+    at(VW(F_SR0 + D), i, j, k) = r;
+    double sm = (u > 0.0) ? l : r;
+    at(VW(F_SIMH0 + D), i, j, k) = (fabs(u) > rel_eps) ? sm : 0.5 * (l + r);
+}
+
+// MakeEdgeScalEdges, 2-D (Source/MaestroMakeEdgeScalars.cpp:454-644)
+template <int D>
+__global__ void k_es_edges_2d(KARGS, int comp, int is_cons, double dt2, double dt4, double hd, double ht, int bclo,
+                              int bchi, int domlo, int domhi, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1;
+    constexpr int T = 1 - D;
+    constexpr int ti = T == 0, tj = T == 1;
+    const int I = D == 0 ? i : j;
+    const int il = i - di, jl = j - dj;
+    const FabView s = VW(F_SOLD), ud = VW(F_UMAC0 + D), ut = VW(F_UMAC0 + T), st = VW(F_SIMH0 + T);
+    const FabView f = VW(F_SCALFORCE);
+    const double fl = at(f, il, jl, k, comp), fr = at(f, i, j, k, comp);
+    const double l = at(VW(F_SL0 + D), i, j, k), r = at(VW(F_SR0 + D), i, j, k);
+    double lq, rq;
+    if (is_cons) {
+        lq = l - (dt2 / ht) * (at(st, il + ti, jl + tj, k) * at(ut, il + ti, jl + tj, k) - at(st, il, jl, k) * at(ut, il, jl, k)) -
+             (dt2 / hd) * at(s, il, jl, k, comp) * (at(ud, i, j, k) - at(ud, il, jl, k)) + dt2 * fl;
+        rq = r - (dt2 / ht) * (at(st, i + ti, j + tj, k) * at(ut, i + ti, j + tj, k) - at(st, i, j, k) * at(ut, i, j, k)) -
+             (dt2 / hd) * at(s, i, j, k, comp) * (at(ud, i + di, j + dj, k) - at(ud, i, j, k)) + dt2 * fr;
+    } else {
+        lq = l - (dt4 / ht) * (at(ut, il + ti, jl + tj, k) + at(ut, il, jl, k)) *
+                     (at(st, il + ti, jl + tj, k) - at(st, il, jl, k)) +
+             dt2 * fl;
+        rq = r - (dt4 / ht) * (at(ut, i + ti, j + tj, k) + at(ut, i, j, k)) * (at(st, i + ti, j + tj, k) - at(st, i, j, k)) +
+             dt2 * fr;
+    }
+    const double u = at(ud, i, j, k);
+    double v = (u > 0.0) ? lq : rq;
+    v = (fabs(u) > rel_eps) ? v : 0.5 * (lq + rq);
+    if (I == domlo) {
+        if (bclo == BC_EXT_DIR) v = at(s, il, jl, k, comp);
+        else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) v = rq;
+        else if (bclo == BC_REFLECT_ODD) v = 0.0;
+    } else if (I == domhi + 1) {
+        if (bchi == BC_EXT_DIR) v = at(s, i, j, k, comp);
+        else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) v = lq;
+        else if (bchi == BC_REFLECT_ODD) v = 0.0;
+    }
+    at(VW(F_SEDGE0 + D), i, j, k, comp) = v;
+}
+
+static void make_edge_scal_2d(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons) {
+    const BCRecD* bh = bcs_host(c, which_bcs);
+    const double dt2 = 0.5 * c.P.dt, dt4 = 0.25 * c.P.dt;
+    if (c.P.ppm_type != 0) {
+        launch(c, region(c, 1, 1, 0, 1, 1, 0, 0), 1, k_trace_face<0>, c.V(), F_UMAC0, F_TRA0, c.P.dt, c.P.dx[0]);
+        launch(c, region(c, 1, 1, 0, 1, 1, 0, 1), 1, k_trace_face<1>, c.V(), F_UMAC1, F_TRA1, c.P.dt, c.P.dx[1]);
+    }
+    for (int comp = start_comp; comp < start_comp + num_comp; ++comp) {
+        const BCRecD& bc = bh[comp];
+        if (c.P.ppm_type == 0) {
+            for (int d = 0; d < 2; ++d) slope_any(c, d, F_SOLD, comp, F_SLOPE, d, 1, bcs_dev(c, which_bcs), comp);
+        } else {
+            for (int d = 0; d < 2; ++d) ppm_any(c, d, F_SOLD, comp, bc, F_UMAC0 + d, 0, 1, F_IPC0, F_IMC0);
+        }
+        for (int d = 0; d < 2; ++d) {
+            const RegionTable& rm = region(c, d == 0 ? 0 : 1, d == 1 ? 0 : 1, 0, 1, 1, 0, -1);
+            const int dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
+            if (d == 0)
+                launch(c, rm, 1, k_es_predictor_2d<0>, c.V(), comp, c.P.ppm_type, dt2, c.P.dx[0], bc.lo[0], bc.hi[0], dl,
+                       dh, c.P.rel_eps);
+            else
+                launch(c, rm, 1, k_es_predictor_2d<1>, c.V(), comp, c.P.ppm_type, dt2, c.P.dx[1], bc.lo[1], bc.hi[1], dl,
+                       dh, c.P.rel_eps);
+        }
+        for (int d = 0; d < 2; ++d) {
+            const int dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
+            if (d == 0)
+                launch(c, rg2(c, 0, 0), 1, k_es_edges_2d<0>, c.V(), comp, is_cons, dt2, dt4, c.P.dx[0], c.P.dx[1],
+                       bc.lo[0], bc.hi[0], dl, dh, c.P.rel_eps);
+            else
+                launch(c, rg2(c, 0, 1), 1, k_es_edges_2d<1>, c.V(), comp, is_cons, dt2, dt4, c.P.dx[1], c.P.dx[0],
+                       bc.lo[1], bc.hi[1], dl, dh, c.P.rel_eps);
+        }
+    }
+}
+
+// ModifyScalForce, planar 2-D (Source/MaestroForce.cpp:419-447)
+__global__ void k_modify_scal_force_2d(KARGS, int comp, int s0cart, int fullform, double dx0, double dx1) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView um = VW(F_UMAC0), vm = VW(F_UMAC1), s0a = VW(s0cart), s0e = VW(F_S0ECART), w0a = VW(F_W0CART);
+    const double scal = at(VW(F_SOLD), i, j, k, comp);
+    double divu = (at(um, i + 1, j, k) - at(um, i, j, k)) / dx0 + (at(vm, i, j + 1, k) - at(vm, i, j, k)) / dx1;
+    divu += (at(w0a, i, j + 1, k, 1) - at(w0a, i, j, k, 1)) / dx1;
+    double& force = at(VW(F_SCALFORCE), i, j, k, comp);
+    if (fullform == 1) {
+        force -= scal * divu;
+    } else {
+        const double s0 = at(s0a, i, j, k);
+        const double divs0u = s0 * (at(um, i + 1, j, k) - at(um, i, j, k)) / dx0 +
+                              (at(vm, i, j + 1, k) * at(s0e, i, j + 1, k) - at(vm, i, j, k) * at(s0e, i, j, k)) / dx1;
+        force += -(scal - s0) * divu - divs0u;
+    }
+}
+
+// MakeRhoHForce, planar 2-D (Source/MaestroForce.cpp:586-603)
+__global__ void k_rhoh_force_2d(KARGS, int cutoff, int domhi, double dy, int psi_in, int add_thermal) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView p0c = VW(F_P0CART);
+    double gradp0;
+    if (j < cutoff) gradp0 = at(VW(F_RHO0CART), i, j, k) * at(VW(F_GRAVCART), i, j, k, 1);
+    else if (j == domhi) gradp0 = (at(p0c, i, j, k) - at(p0c, i, j - 1, k)) / dy;
+    else gradp0 = (at(p0c, i, j + 1, k) - at(p0c, i, j, k)) / dy;
+    const FabView vm = VW(F_UMAC1);
+    const double veladv = 0.5 * (at(vm, i, j, k) + at(vm, i, j + 1, k));
+    double f = veladv * gradp0;
+    if (psi_in) f += at(VW(F_PSICART), i, j, k);
+    if (add_thermal == 1) f += at(VW(F_THERMAL), i, j, k);
+    at(VW(F_SCALFORCE), i, j, k, RHOH) = f;
+}
+
+// PutInPertForm, 2-D (r = j)
+__global__ void k_pert_2d(KARGS, int comp, const double* __restrict__ s0, int flag) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    double& a = at(VW(F_SOLD), i, j, k, comp);
+    a = flag ? a - s0[j] : a + s0[j];
+}
+
+// MakeRhoXFlux, 2-D (Source/MaestroMakeFlux.cpp:101-182)
+template <int D>
+__global__ void k_rhox_flux_2d(KARGS, int nspec, int spt, int do_eta, const double* __restrict__ r0o,
+                               const double* __restrict__ r0n, const double* __restrict__ w0,
+                               const double* __restrict__ r0pe) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView fl = VW(F_SFLUX0 + D), e = VW(F_SEDGE0 + D);
+    const double u = at(VW(F_UMAC0 + D), i, j, k);
+    double frho = 0.0, eta = 0.0;
+    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+        const double rho0_edge = 0.5 * (r0o[j] + r0n[j]);
+        double f;
+        if (spt == 1) f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, comp);
+        else if (spt == 2) f = u * at(e, i, j, k, comp);
+        else f = u * at(e, i, j, k, RHO) * at(e, i, j, k, comp);
+        at(fl, i, j, k, comp) = f;
+        if (D == 1 && do_eta) {
+            eta += f;
+            if (comp == FIRSTSPEC + nspec - 1) eta -= w0[j] * r0pe[j];
+        }
+        frho += f;
+    }
+    at(fl, i, j, k, RHO) = frho;
+    if (D == 1 && do_eta) at(VW(F_ETA), i, j, k) += eta;
+}
+
+// MakeRhoHFlux, 2-D (Source/MaestroMakeFlux.cpp:597-662)
+template <int D>
+__global__ void k_rhoh_flux_2d(KARGS, int ept, const double* __restrict__ a, const double* __restrict__ bb) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView e = VW(F_SEDGE0 + D);
+    const double u = at(VW(F_UMAC0 + D), i, j, k);
+    double f;
+    if (ept == 0) {
+        f = u * at(e, i, j, k, RHOH);
+    } else {
+        const double rhoh0_edge = 0.5 * (a[j] + bb[j]);
+        f = D == 0 ? u * (rhoh0_edge + at(e, i, j, k, RHOH)) : u * (at(e, i, j, k, RHOH) + rhoh0_edge);
+    }
+    at(VW(F_SFLUX0 + D), i, j, k, RHOH) = f;
+}
+
+// UpdateScal, 2-D (Source/MaestroAdvection.cpp:117-251)
+__global__ void k_update_rhox_2d(KARGS, int nspec, double dt, double dx0, double dx1, double half_cutoff) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fo = VW(F_SCALFORCE);
+    for (int n = 0; n < nspec; ++n) {
+        const int comp = FIRSTSPEC + n;
+        double divterm = (at(fx, i + 1, j, k, comp) - at(fx, i, j, k, comp)) / dx0;
+        divterm += (at(fy, i, j + 1, k, comp) - at(fy, i, j, k, comp)) / dx1;
+        at(sn, i, j, k, comp) = at(so, i, j, k, comp) + dt * (-divterm + at(fo, i, j, k, comp));
+    }
+    double rho = at(so, i, j, k, RHO);
+    bool neg = false;
+    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+        rho += at(sn, i, j, k, comp) - at(so, i, j, k, comp);
+        if (at(sn, i, j, k, comp) < 0.0) neg = true;
+    }
+    if (rho < half_cutoff) {
+        for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) at(sn, i, j, k, comp) *= half_cutoff / rho;
+        rho = half_cutoff;
+    }
+    at(sn, i, j, k, RHO) = rho;
+    if (neg) {
+        for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+            if (at(sn, i, j, k, comp) < 0.0) {
+                const double delta = -at(sn, i, j, k, comp);
+                double sumX = 0.0;
+                for (int c2 = FIRSTSPEC; c2 < FIRSTSPEC + nspec; ++c2)
+                    if (c2 != comp && at(sn, i, j, k, c2) >= 0.0) sumX += at(sn, i, j, k, c2);
+                for (int c2 = FIRSTSPEC; c2 < FIRSTSPEC + nspec; ++c2)
+                    if (c2 != comp && at(sn, i, j, k, c2) >= 0.0) {
+                        const double frac = at(sn, i, j, k, c2) / sumX;
+                        at(sn, i, j, k, c2) -= frac * delta;
+                    }
+                at(sn, i, j, k, comp) = 0.0;
+            }
+        }
+    }
+}
+
+__global__ void k_update_rhoh_2d(KARGS, double dt, double dx0, double dx1, int eos_check, double cutoff, int* flag) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fo = VW(F_SCALFORCE);
+    const double divterm = ((at(fx, i + 1, j, k, RHOH) - at(fx, i, j, k, RHOH)) / dx0 +
+                            (at(fy, i, j + 1, k, RHOH) - at(fy, i, j, k, RHOH)) / dx1);
+    at(sn, i, j, k, RHOH) = at(so, i, j, k, RHOH) + dt * (-divterm + at(fo, i, j, k, RHOH));
+    if (eos_check && at(sn, i, j, k, RHO) <= cutoff) atomicOr(flag, 1);
+}
+
+// ---- wrappers (dispatched to by the 3-D entry points when c.ndim == 2)
+void put1d_2d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge) {
+    launch(c, rg2(c, 0), 1, k_put1d_2d, c.V(), fid, d_s0, outcomp, edge);
+}
+void addw0_2d(Ctx& c, int f0, double mult) {
+    launch(c, region(c, 1, 0, 0, 1, 0, 0, 1), 1, k_addw0_2d, c.V(), f0 + 1, (const double*)c.b1("w0"), mult);
+}
+void make_vel_force_2d(Ctx& c) {
+    set_val(c, F_VELFORCE, 0.0, 0, 2, 1);
+    launch(c, rg2(c, 0), 1, k_vel_force_2d, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
+           c.P.dom_hi[1], c.P.dx[1]);
+}
+void modify_scal_force_2d(Ctx& c, int comp, int s0cart_fid, int fullform) {
+    launch(c, rg2(c, 0), 1, k_modify_scal_force_2d, c.V(), comp, s0cart_fid, fullform, c.P.dx[0], c.P.dx[1]);
+}
+void make_rhoh_force_2d(Ctx& c, int is_prediction, int add_thermal) {
+    const int ept = c.P.enthalpy_pred_type;
+    const int psi_in = (is_prediction == 1 && ept == 2) || (is_prediction == 1 && ept == 0) || (is_prediction == 0);
+    launch(c, rg2(c, 0), 1, k_rhoh_force_2d, c.V(), c.P.base_cutoff_density_coord, c.P.dom_hi[1], c.P.dx[1], psi_in,
+           add_thermal);
+}
+void put_in_pert_form_2d(Ctx& c, const double* d_s0, int comp, int flag) {
+    launch(c, rg2(c, 0), 1, k_pert_2d, c.V(), comp, d_s0, flag);
+}
+void make_rhox_flux_2d(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
+                       const double* r0e_new) {
+    const int do_eta = c.P.evolve_base_state && !c.P.use_exact_base_state;
+    const double* w0 = c.b1("w0");
+    const double* rpe = c.b1("rho0_predicted_edge");
+    launch(c, rg2(c, 0, 0), 1, k_rhox_flux_2d<0>, c.V(), c.nspec, c.P.species_pred_type, 0, r0_old, r0_new, w0, rpe);
+    launch(c, rg2(c, 0, 1), 1, k_rhox_flux_2d<1>, c.V(), c.nspec, c.P.species_pred_type, do_eta, r0e_old, r0e_new,
+           w0, rpe);
+}
+void make_rhoh_flux_2d(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
+                       const double* rh0e_new) {
+    const int ept = c.P.enthalpy_pred_type;
+    launch(c, rg2(c, 0, 0), 1, k_rhoh_flux_2d<0>, c.V(), ept, rh0_old, rh0_new);
+    launch(c, rg2(c, 0, 1), 1, k_rhoh_flux_2d<1>, c.V(), ept, rh0e_old, rh0e_new);
+}
+void sum_species_edges_2d(Ctx& c) {
+    launch(c, rg2(c, 0, 0), 1, k_sum_species<0>, c.V(), c.nspec);
+    launch(c, rg2(c, 0, 1), 1, k_sum_species<1>, c.V(), c.nspec);
+}
+void update_scal_2d(Ctx& c, int start_comp) {
+    const RegionTable& rt = rg2(c, 0);
+    if (start_comp == RHOH)
+        launch(c, rt, 1, k_update_rhoh_2d, c.V(), c.P.dt, c.P.dx[0], c.P.dx[1], c.P.do_eos_h_above_cutoff,
+               c.P.base_cutoff_density, c.d_flag);
+    else
+        launch(c, rt, 1, k_update_rhox_2d, c.V(), c.nspec, c.P.dt, c.P.dx[0], c.P.dx[1], 0.5 * c.P.base_cutoff_density);
+}
+void make_utrans_2d_entry(Ctx& c) { make_utrans_2d(c); }
+void vel_pred_2d_entry(Ctx& c) { vel_pred_2d(c); }
+void make_edge_scal_2d_entry(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons) {
+    make_edge_scal_2d(c, start_comp, num_comp, which_bcs, is_cons);
 }
 
 }  // namespace madv

@@ -37,6 +37,7 @@ class MadvParams(C.Structure):
         ("buoyancy_cutoff_factor", C.c_double),
         ("do_eos_h_above_cutoff", C.c_int),
         ("base_cutoff_density_coord", C.c_int),
+        ("dim", C.c_int),
     ]
 
 
@@ -62,5 +63,6 @@ def make_params(cfg):
     p.base_cutoff_density = cfg["base_cutoff_density"]
     p.buoyancy_cutoff_factor = cfg.get("buoyancy_cutoff_factor", 5.0)
     p.do_eos_h_above_cutoff = cfg.get("do_eos_h_above_cutoff", 1)
-    p.base_cutoff_density_coord = cfg["n"][2]
+    p.dim = cfg.get("dim", 3)
+    p.base_cutoff_density_coord = cfg["n"][p.dim - 1]
     return p

@@ -109,7 +109,7 @@ def _ref3(mfs):
     """Three face MultiFabs as a contiguous madv_multifab[3]."""
     if mfs is None:
         return None
-    arr = (MadvMultiFab * 3)(*[m.desc() for m in mfs])
+    arr = (MadvMultiFab * 3)(*[m.desc() for m in mfs][:3])
     _ref3.keep.append(arr)
     if len(_ref3.keep) > 64:
         del _ref3.keep[:32]
@@ -247,16 +247,18 @@ class StageBuffers:
         boxes = cfg["boxes"]
         nscal = 4 + cfg["nspec"]
         ng = 4 if cfg["ppm_type"] == 2 else 3
+        nd = cfg.get("dim", 3)
         self.n = cfg["n"]
-        self.uold = MultiFab(boxes, 3, ng, device=device)
+        self.nd = nd
+        self.uold = MultiFab(boxes, nd, ng, device=device)
         self.sold = MultiFab(boxes, nscal, ng, device=device)
-        self.gpi = MultiFab(boxes, 3, 0, device=device)
+        self.gpi = MultiFab(boxes, nd, 0, device=device)
         self.thermal = MultiFab(boxes, 1, 1, device=device)
         self.snew = MultiFab(boxes, nscal, ng, device=device)
-        self.umac = [MultiFab(boxes, 1, 1, nodal=d, device=device) for d in range(3)]
-        self.sedge = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(3)]
-        self.sflux = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(3)]
-        self.eta = MultiFab(boxes, 1, 0, nodal=2, device=device)
+        self.umac = [MultiFab(boxes, 1, 1, nodal=d, device=device) for d in range(nd)]
+        self.sedge = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(nd)]
+        self.sflux = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(nd)]
+        self.eta = MultiFab(boxes, 1, 0, nodal=nd - 1, device=device)
 
     def load(self, cfg):
         self.uold.from_domain(cfg["uold"])
@@ -284,10 +286,11 @@ def run_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
                      thermal=buf.thermal, mode=mode)
     torch.cuda.synchronize()
     n = cfg["n"]
+    nd = buf.nd
     res = dict(
-        umac_end=[buf.umac[d].to_domain(n)[0].cpu().numpy() for d in range(3)],
-        sedge=[buf.sedge[d].to_domain(n).cpu().numpy() for d in range(3)],
-        sflux=[buf.sflux[d].to_domain(n).cpu().numpy() for d in range(3)],
+        umac_end=[buf.umac[d].to_domain(n)[0].cpu().numpy() for d in range(nd)],
+        sedge=[buf.sedge[d].to_domain(n).cpu().numpy() for d in range(nd)],
+        sflux=[buf.sflux[d].to_domain(n).cpu().numpy() for d in range(nd)],
         snew=buf.snew.to_domain(n).cpu().numpy(),
         sold_end=buf.sold.to_domain(n).cpu().numpy(),
         etarhoflux=buf.eta.to_domain(n)[0].cpu().numpy(),

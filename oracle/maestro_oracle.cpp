@@ -109,15 +109,16 @@ struct Lev {
     }
 
     // ------------------------------------------------------------------ face ghosts
-    // Maestro::FillUmacGhost (Source/MaestroFillData.cpp:176-453), one level.
-    void FillUmacGhost(MF* um) {
+    // Maestro::FillUmacGhost (Source/MaestroFillData.cpp:176-453), one level; nd = 2 for
+    // the 2-D form (no w faces).
+    void FillUmacGhost(MF* um, int nd = 3) {
         const int* dlo = L.dom.lo;
         const int* dhi = L.dom.hi;
         for (int b = 0; b < nb; ++b) {
             const Arr& umac = um[0][b];
             const Arr& vmac = um[1][b];
-            const Arr& wmac = um[2][b];
-            for (int dd = 0; dd < 3; ++dd) {
+            const Arr& wmac = nd == 3 ? um[2][b] : um[1][b];
+            for (int dd = 0; dd < nd; ++dd) {
                 Box gb = grow(nodal(L.ba[b], dd), 1);
                 const int bclo = P.phys_bc_lo[dd], bchi = P.phys_bc_hi[dd];
                 MO_FOR3(gb) {
@@ -129,19 +130,19 @@ struct Lev {
                     if (I == dlo[dd] - 1) {
                         switch (bclo) {
                             case inflow:
-                                for (int c = 0; c < 3; ++c)
+                                for (int c = 0; c < nd; ++c)
                                     (*comp[c])(i, j, k) = c == dd ? qn(i + di, j + dj, k + dk) : 0.0;
                                 break;
                             case slipwall:
                             case noslipwall:
-                                for (int c = 0; c < 3; ++c) (*comp[c])(i, j, k) = 0.0;
+                                for (int c = 0; c < nd; ++c) (*comp[c])(i, j, k) = 0.0;
                                 break;
                             case outflow:
-                                for (int c = 0; c < 3; ++c)
+                                for (int c = 0; c < nd; ++c)
                                     (*comp[c])(i, j, k) = (*comp[c])(i + di, j + dj, k + dk);
                                 break;
                             case symmetry:
-                                for (int c = 0; c < 3; ++c)
+                                for (int c = 0; c < nd; ++c)
                                     (*comp[c])(i, j, k) = c == dd ? -qn(i + 2 * di, j + 2 * dj, k + 2 * dk)
                                                                   : (*comp[c])(i + di, j + dj, k + dk);
                                 break;
@@ -151,26 +152,26 @@ struct Lev {
                     if (I == dhi[dd] + 2) {
                         switch (bchi) {
                             case inflow:
-                                for (int c = 0; c < 3; ++c) {
+                                for (int c = 0; c < nd; ++c) {
                                     if (c == dd) qn(i, j, k) = qn(i - di, j - dj, k - dk);
                                     else (*comp[c])(i - di, j - dj, k - dk) = 0.0;
                                 }
                                 break;
                             case slipwall:
                             case noslipwall:
-                                for (int c = 0; c < 3; ++c) {
+                                for (int c = 0; c < nd; ++c) {
                                     if (c == dd) qn(i, j, k) = 0.0;
                                     else (*comp[c])(i - di, j - dj, k - dk) = 0.0;
                                 }
                                 break;
                             case outflow:
-                                for (int c = 0; c < 3; ++c) {
+                                for (int c = 0; c < nd; ++c) {
                                     if (c == dd) qn(i, j, k) = qn(i - di, j - dj, k - dk);
                                     else (*comp[c])(i - di, j - dj, k - dk) = (*comp[c])(i - 2 * di, j - 2 * dj, k - 2 * dk);
                                 }
                                 break;
                             case symmetry:
-                                for (int c = 0; c < 3; ++c) {
+                                for (int c = 0; c < nd; ++c) {
                                     if (c == dd) qn(i, j, k) = -qn(i - 2 * di, j - 2 * dj, k - 2 * dk);
                                     else (*comp[c])(i - di, j - dj, k - dk) = (*comp[c])(i - 2 * di, j - 2 * dj, k - 2 * dk);
                                 }
@@ -1342,6 +1343,10 @@ struct Stage {
     }
 };
 
+}  // namespace mo
+#include "mo_stage2d.hpp"
+namespace mo {
+
 // ---------------------------------------------------------------------- flat I/O
 static long ncell_of(const Box& d) {
     return (long)(d.hi[0] - d.lo[0] + 1) * (d.hi[1] - d.lo[1] + 1) * (d.hi[2] - d.lo[2] + 1);
@@ -1520,6 +1525,112 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
     return 0;
 }
 
+// The 2-D stage (AdvancePremac, DensityAdvance, EnthalpyAdvance with the Addw0 calls of
+// AdvanceTimeStep) on one level; domain arrays are [nc][ny][nx].
+static int run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
+                        int which_step) {
+    if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
+    if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
+        throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
+    Stage2D T;
+    Lev& S = T.S;
+    S.P = *p;
+    S.P.phys_bc_lo[2] = S.P.phys_bc_hi[2] = interior;
+    S.nspec = T.nspec = p->nspec;
+    S.nscal = T.nscal = 4 + p->nspec;
+    for (int d = 0; d < 2; ++d) {
+        S.L.dom.lo[d] = p->dom_lo[d];
+        S.L.dom.hi[d] = p->dom_hi[d];
+        S.L.per[d] = (p->phys_bc_lo[d] == interior);
+        if ((p->phys_bc_lo[d] == interior) != (p->phys_bc_hi[d] == interior))
+            throw std::runtime_error("periodic direction needs interior on both sides");
+        S.L.dx[d] = p->dx[d];
+    }
+    S.L.dom.lo[2] = S.L.dom.hi[2] = 0;
+    S.L.per[2] = true;
+    S.L.dx[2] = 1.0;
+    for (int b = 0; b < nboxes; ++b) {
+        Box bx;
+        for (int d = 0; d < 3; ++d) {
+            bx.lo[d] = d < 2 ? boxes[6 * b + d] : 0;
+            bx.hi[d] = d < 2 ? boxes[6 * b + 3 + d] : 0;
+        }
+        S.L.ba.push_back(bx);
+    }
+    S.nb = T.nb = nboxes;
+    S.nr = p->dom_hi[1] - p->dom_lo[1] + 1;
+    S.ng_s = S.ng_adv = T.ng_s = T.ng_adv = p->ppm_type == 2 ? 4 : 3;
+    S.dt = T.dt = p->dt;
+    S.rel_eps = T.rel_eps = p->rel_eps;
+    S.pc = PPMCtx{p->ppm_type, p->dt, p->rel_eps, {p->dx[0], p->dx[1], 1.0}, S.L.dom};
+    S.BCSetup();
+    S.cutoff = p->base_cutoff_density_coord;
+    const int nr = S.nr;
+    auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
+    S.rho0_old = vec(in->rho0_old, nr);
+    S.rho0_new = vec(in->rho0_new, nr);
+    S.rhoh0_old = vec(in->rhoh0_old, nr);
+    S.rhoh0_new = vec(in->rhoh0_new, nr);
+    S.p0_old = vec(in->p0_old, nr);
+    S.p0_new = vec(in->p0_new, nr);
+    S.psi = vec(in->psi, nr);
+    S.grav_cell = vec(in->grav_cell, nr);
+    S.w0_force = vec(in->w0_force, nr);
+    S.w0 = vec(in->w0, nr + 1);
+    S.rho0_predicted_edge = vec(in->rho0_predicted_edge, nr + 1);
+    const Box& dom = S.L.dom;
+    const int nscal = T.nscal;
+
+    S.w0_cart.define(S.L.ba, 2, 2, -1, 0.0);
+    T.Put1dArrayOnCart(S.w0, S.w0_cart, true, true, &S.bcs_u, 0, true);
+    MF w0_force_cart;
+    w0_force_cart.define(S.L.ba, 2, 1, -1, 0.0);
+    if (p->evolve_base_state) T.Put1dArrayOnCart(S.w0_force, w0_force_cart, false, true, &S.bcs_f, 0, false);
+
+    MF uold, sold, snew;
+    uold.define(S.L.ba, 2, T.ng_s, -1, 0.0);
+    sold.define(S.L.ba, nscal, T.ng_s, -1, 0.0);
+    snew.define(S.L.ba, nscal, T.ng_s, -1, 0.0);
+    S.gpi.define(S.L.ba, 2, 0, -1, 0.0);
+    S.thermal.define(S.L.ba, 1, 1, -1, 0.0);
+    scatter_cells(dom, in->uold, uold, 0, 2);
+    scatter_cells(dom, in->sold, sold, 0, nscal);
+    scatter_cells(dom, in->gpi, S.gpi, 0, 2);
+    if (in->thermal) scatter_cells(dom, in->thermal, S.thermal, 0, 1);
+    MF umac[2], utrans[2], sedge[2], sflux[2], etarhoflux, scal_force, vel_force;
+    for (int d = 0; d < 2; ++d) {
+        umac[d].define(S.L.ba, 1, 1, d, 0.0);
+        sedge[d].define(S.L.ba, nscal, 0, d, 0.0);
+        sflux[d].define(S.L.ba, nscal, 0, d, 0.0);
+    }
+    etarhoflux.define(S.L.ba, 1, 0, 1, 0.0);
+    scal_force.define(S.L.ba, nscal, 1, -1, 0.0);
+
+    FillPatch(S.L, sold, 0, nscal, 0, S.bcs_s, false, 0);
+    T.AdvancePremac(uold, sold, umac, w0_force_cart, utrans, vel_force);
+    if (out->utrans[0])
+        for (int d = 0; d < 2; ++d) gather_faces(dom, utrans[d], d, 0, 1, out->utrans[d]);
+    if (out->umac_vp[0])
+        for (int d = 0; d < 2; ++d) gather_faces(dom, umac[d], d, 0, 1, out->umac_vp[d]);
+    if (out->vel_force) gather_cells(dom, vel_force, 0, 2, out->vel_force);
+    T.Addw0(umac, 1.0);
+    T.DensityAdvance(sold, snew, sedge, sflux, scal_force, etarhoflux, umac, which_step);
+    T.Addw0(umac, -1.0);
+    T.Addw0(umac, 1.0);
+    T.EnthalpyAdvance(sold, snew, sedge, sflux, scal_force, umac, which_step);
+    T.Addw0(umac, -1.0);
+    if (out->umac_end[0])
+        for (int d = 0; d < 2; ++d) gather_faces(dom, umac[d], d, 0, 1, out->umac_end[d]);
+    for (int d = 0; d < 2; ++d) {
+        if (out->sedge[d]) gather_faces(dom, sedge[d], d, 0, nscal, out->sedge[d]);
+        if (out->sflux[d]) gather_faces(dom, sflux[d], d, 0, nscal, out->sflux[d]);
+    }
+    if (out->snew) gather_cells(dom, snew, 0, nscal, out->snew);
+    if (out->sold_end) gather_cells(dom, sold, 0, nscal, out->sold_end);
+    if (out->etarhoflux) gather_faces(dom, etarhoflux, 1, 0, 1, out->etarhoflux);
+    return 0;
+}
+
 }  // namespace mo
 
 extern "C" {
@@ -1533,6 +1644,21 @@ int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const i
 #endif
     try {
         return mo::run_stage(p, nlev, nboxes, boxes, in, out, which_step);
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+
+int mo_run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
+                    int which_step, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    try {
+        return mo::run_stage_2d(p, nboxes, boxes, in, out, which_step);
     } catch (const std::exception& e) {
         mo::g_err = e.what();
         return -1;

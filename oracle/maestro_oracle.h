@@ -38,6 +38,7 @@ typedef struct {
     double buoyancy_cutoff_factor;
     int do_eos_h_above_cutoff;
     int base_cutoff_density_coord;
+    int dim; /* 3 (or 0) / 2 */
 } mo_params;
 
 typedef struct {
@@ -85,6 +86,13 @@ int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inpu
  * which_step 1 is mo_run_stage. */
 int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const int* boxes,
                         const mo_inputs* in, mo_outputs* out, int which_step, int nthreads);
+
+/* The 2-D stage (the reference's AMREX_SPACEDIM == 2 code, y radial) on one level:
+ * domain arrays are [nc][ny][nx] with 2 velocity components, boxes give lo/hi in x and y
+ * (z entries ignored), face arrays utrans/umac/sedge/sflux use indices 0 and 1 and
+ * etarhoflux lives on y faces. */
+int mo_run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                    mo_outputs* out, int which_step, int nthreads);
 
 /* A FAB: data covering the index box [lo, hi] (i fastest), nc components. */
 typedef struct {

@@ -47,6 +47,7 @@ def lib(checked=False):
         L = C.CDLL(path)
         L.mo_run_stage.restype = C.c_int
         L.mo_run_stage_levels.restype = C.c_int
+        L.mo_run_stage_2d.restype = C.c_int
         L.mo_last_error.restype = C.c_char_p
         _LIBS[name] = L
     return _LIBS[name]
@@ -162,6 +163,50 @@ def run_stage_levels(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", 
     boxes = np.ascontiguousarray(np.array([b for L in levels for b in L["boxes"]], dtype=np.int32).reshape(-1))
     rc = lib(checked).mo_run_stage_levels(C.byref(p), nlev, nboxes, boxes.ctypes.data_as(C.POINTER(C.c_int)),
                                           ins, outs, which_step, nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
+    return res
+
+
+def run_stage_2d(cfg, checked=False, nthreads=0, which_step=1):
+    """The 2-D stage (configs.planar_config_2d) on the CPU; arrays shaped like the inputs:
+    cells [nc, 1, ny, nx], x faces [.., 1, ny, nx+1], y faces [.., 1, ny+1, nx]."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    nx, ny = cfg["n"][0], cfg["n"][1]
+    nscal = 4 + cfg["nspec"]
+    keep = []
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    inp = MoInputs()
+    for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                 "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+        setattr(inp, name, arr(cfg[name]))
+    out = MoOutputs()
+    fshape = [(1, ny, nx + 1), (1, ny + 1, nx)]
+    res = {}
+    for key in ("utrans", "umac_vp", "umac_end"):
+        res[key] = [np.full(fshape[d], np.nan) for d in range(2)]
+        for d in range(2):
+            getattr(out, key)[d] = _p(res[key][d])
+    for key in ("sedge", "sflux"):
+        res[key] = [np.full((nscal,) + fshape[d], np.nan) for d in range(2)]
+        for d in range(2):
+            getattr(out, key)[d] = _p(res[key][d])
+    res["vel_force"] = np.full((2, 1, ny, nx), np.nan)
+    out.vel_force = _p(res["vel_force"])
+    for key in ("snew", "sold_end"):
+        res[key] = np.full((nscal, 1, ny, nx), np.nan)
+        setattr(out, key, _p(res[key]))
+    res["etarhoflux"] = np.full(fshape[1], np.nan)
+    out.etarhoflux = _p(res["etarhoflux"])
+    boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    rc = lib(checked).mo_run_stage_2d(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
+                                      C.byref(inp), C.byref(out), which_step, nthreads)
     if rc != 0:
         raise RuntimeError("oracle: " + lib(checked).mo_last_error().decode())
     return res
