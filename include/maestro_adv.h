@@ -212,6 +212,37 @@ int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_f
                      const madv_fab* u, const madv_fab* v, const madv_fab* w, int is_umac,
                      const int* bc, const madv_fab* Ip, const madv_fab* Im, void* stream);
 
+/* Adjoint of the scalar path over several advection steps with the velocity held fixed
+ * (the multi-step form of Exec/unit_tests/test_advect/MaestroEvolve.cpp:140-190, which
+ * re-runs AdvancePremac + DensityAdvance + EnthalpyAdvance on a fixed velocity):
+ *     s_0 = sold0,  s_{n+1} = Stage(uold, s_n)  (n < nsteps),  J = sum weight * s_nsteps
+ * over valid cells and all nscal components.  Stage is madv_stage_forward's computation
+ * (snew's density, enthalpy and species; temperature and pi are carried), with gpi = 0
+ * and thermal = 0.  The reverse sweep transposes each phase with the forward's limiter
+ * and upwind decisions frozen; states are stored every ckpt_interval steps and each
+ * block is recomputed from its stored state, so memory grows with nsteps/ckpt_interval
+ * + ckpt_interval states.  No counterpart in the reference.
+ * Scope: one level, 3-D, periodic in every direction, ppm_type 1, species_pred_type 1,
+ * enthalpy_pred_type 1, and w0 = 0, grav_cell = 0 so that the MAC velocities do not depend
+ * on the state (MADV_ERR_UNSUPPORTED otherwise).  The UpdateScal floor and
+ * negative-species branches are taken as not active. */
+typedef struct {
+    int nsteps;                  /* advection steps (>= 1) */
+    int ckpt_interval;           /* steps between stored states (>= 1) */
+    const madv_multifab* uold;   /* cell velocity, 3 components, held fixed */
+    const madv_multifab* sold0;  /* initial state, nscal components */
+    const madv_multifab* weight; /* J = sum(weight * s_nsteps), nscal components */
+} madv_adj_seed;
+
+typedef struct {
+    const madv_multifab* sfinal; /* out (may be NULL): s_nsteps, nscal components */
+    const madv_multifab* grad_s; /* out (NULL: forward only): dJ/dsold0, nscal components */
+    double J;                    /* out */
+    long long device_bytes;      /* out: device memory the call allocated (freed on return) */
+} madv_adj_result;
+
+int madv_stage_adjoint(madv_ctx* ctx, const madv_adj_seed* seed, madv_adj_result* res, void* stream);
+
 /* Number of kernel launches issued by the last madv_* call (for launch accounting). */
 long madv_last_launch_count(const madv_ctx* ctx);
 

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmaestro_adv.so")
-SOURCES = ["madv_kernels.cu", "madv_ctx.cu", "madv_probe.cu", "madv_box.cu", "madv_noalloc.cu", "madv_amr.cu"]
+SOURCES = ["madv_kernels.cu", "madv_ctx.cu", "madv_probe.cu", "madv_box.cu", "madv_noalloc.cu", "madv_amr.cu", "madv_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
 
@@ -28,6 +28,7 @@ def build_library(force=False, verbose=False):
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".hpp"))]
     deps.append(os.path.join(HERE, "..", "include", "maestro_adv.h"))
+    deps.append(os.path.abspath(__file__))  # the source list and flags
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):

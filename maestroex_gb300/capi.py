@@ -26,7 +26,7 @@ EXPORTED = [
     "madv_enthalpy_advance", "madv_stage_forward", "madv_last_launch_count",
     "madv_last_error", "madv_version", "madv_profile", "madv_profile_report", "madv_probe_fp64_peak",
     "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc", "madv_set_layout_levels",
-    "madv_set_base_state_levels", "madv_stage_forward_levels",
+    "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
 ]
 
 
@@ -46,6 +46,16 @@ class MadvBaseState(C.Structure):
     _fields_ = [(n, C.POINTER(C.c_double)) for n in (
         "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new", "p0_old", "p0_new", "psi", "grav_cell",
         "w0_force", "w0", "rho0_predicted_edge")]
+
+
+class MadvAdjSeed(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("ckpt_interval", C.c_int), ("uold", C.POINTER(MadvMultiFab)),
+                ("sold0", C.POINTER(MadvMultiFab)), ("weight", C.POINTER(MadvMultiFab))]
+
+
+class MadvAdjResult(C.Structure):
+    _fields_ = [("sfinal", C.POINTER(MadvMultiFab)), ("grad_s", C.POINTER(MadvMultiFab)), ("J", C.c_double),
+                ("device_bytes", C.c_longlong)]
 
 
 class MadvError(RuntimeError):
@@ -81,6 +91,7 @@ def lib():
                                          C.c_void_p]
         L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                                 C.c_void_p]
+        L.madv_stage_adjoint.argtypes = [C.c_void_p, P(MadvAdjSeed), P(MadvAdjResult), C.c_void_p]
         FAB = P(MadvFab)
         L.madv_ppm.argtypes = [C.c_void_p, P(MadvBox), FAB, C.c_int, FAB, FAB, FAB, C.c_int, P(C.c_int), FAB, FAB,
                                C.c_void_p]

@@ -1,4 +1,6 @@
 // Context, layout, base state and the C ABI of the scalar-advection stage library.
+#include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -568,6 +570,7 @@ static int check_ready_h(const Hier& H) {
 
 struct StageIO {
     const madv_multifab *uold, *sold, *gpi, *thermal, *snew, *umac, *sedge, *sflux, *eta;
+    int sold_out = 1;  // copy the converted-and-restored sold back to the caller
 };
 
 static int bind_stage(Ctx& c, const StageIO& io) {
@@ -599,7 +602,8 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
     fill_patch_h(H, F_SOLD, 0, H[0].nscal, BCS_S, 0, 0, 0);
     for (int l = 0; l < H.n(); ++l) {
         Ctx& c = H[l];
-        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, c.ndim, 0);
+        if (io[l].gpi) copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, c.ndim, 0);
+        else set_val(c, F_GPI, 0.0, 0, 3, 0);
         set_val(c, F_THERMAL, 0.0, 0, 1, 1);
         if (io[l].thermal) copy_fab(c, F_THERMAL, 0, F_USER + U_THERMAL, 0, 1, 0);
         set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
@@ -626,7 +630,7 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
             copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 2, 0);
             copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
         }
-        copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
+        if (io[l].sold_out) copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
         for (int d = 0; d < c.ndim; ++d) {
             if (io[l].umac) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
             if (io[l].sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
@@ -833,6 +837,64 @@ static void drop_graph(madv_ctx* h) {
     if (h->c.graph_exec) cudaGraphExecDestroy(h->c.graph_exec);
     h->c.graph_exec = nullptr;
     h->c.graph_key.clear();
+}
+
+// ------------------------------------------------------------------ adjoint driver
+// Device storage of the reverse sweep, freed when the call returns.
+struct AdjWork {
+    std::vector<double*> owned;
+    size_t bytes = 0;
+    ~AdjWork() {
+        for (auto p : owned) cudaFree(p);
+    }
+    double* alloc(size_t b) {
+        double* p = nullptr;
+        if (!cuda_ok(cudaMalloc(&p, b), "cudaMalloc(adjoint)")) throw Fail{MADV_ERR_CUDA};
+        if (!cuda_ok(cudaMemset(p, 0, b), "cudaMemset(adjoint)")) throw Fail{MADV_ERR_CUDA};
+        owned.push_back(p);
+        bytes += b;
+        return p;
+    }
+};
+
+// doubles of one FAB per box (nc components, ng ghost cells, nodal direction or -1)
+static size_t fab_doubles(const Ctx& c, int nc, int ng, int nodal) {
+    size_t tot = 0;
+    for (int b = 0; b < c.nb; ++b) {
+        HBox v = valid_box(c, b, nodal);
+        size_t n = 1;
+        for (int d = 0; d < 3; ++d) n *= (size_t)(v.hi[d] - v.lo[d] + 1 + 2 * ng);
+        tot += n * nc;
+    }
+    return tot;
+}
+
+// user slot `slot` over FABs laid end to end at p; fabs (optional) receives the
+// madv_fab descriptors of the same storage
+static void bind_raw(Ctx& c, int slot, double* p, int nc, int ng, int nodal, std::vector<madv_fab>* fabs = nullptr) {
+    size_t off = 0;
+    if (fabs) fabs->resize(c.nb);
+    for (int b = 0; b < c.nb; ++b) {
+        HBox v = valid_box(c, b, nodal);
+        int lo[3], hi[3];
+        size_t n = 1;
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = v.lo[d] - ng;
+            hi[d] = v.hi[d] + ng;
+            n *= (size_t)(hi[d] - lo[d] + 1);
+        }
+        c.hviews_pinned[(F_USER + slot) * c.nb + b] = make_view(p + off, lo, hi);
+        if (fabs) {
+            madv_fab& f = (*fabs)[b];
+            f.p = p + off;
+            for (int d = 0; d < 3; ++d) {
+                f.lo[d] = lo[d];
+                f.hi[d] = hi[d];
+            }
+            f.ncomp = nc;
+        }
+        off += n * nc;
+    }
 }
 
 extern "C" {
@@ -1395,6 +1457,168 @@ int madv_profile_report(madv_ctx* h, char* buf, int len) {
     js += "}";
     std::snprintf(buf, (size_t)len, "%s", js.c_str());
     return (int)js.size() < len ? MADV_OK : MADV_ERR_PARAM;
+}
+
+// Multi-step forward s_{n+1} = Stage(uold, s_n) with the velocity held fixed, J = <weight,
+// s_N>, and the reverse sweep dJ/ds_0.  States are stored every ckpt_interval steps; each
+// block of steps is recomputed from its stored state (keeping the block's states and
+// edge states), then reversed step by step.  The last block's states are kept by the
+// first forward pass.
+static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* res, void* stream) {
+    Hier H;
+    int rc = begin_call(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!sd || !res || !sd->uold || !sd->sold0 || !sd->weight || sd->nsteps < 1 || sd->ckpt_interval < 1) {
+        set_error("madv_stage_adjoint: uold, sold0, weight, nsteps >= 1 and ckpt_interval >= 1 are required");
+        return MADV_ERR_PARAM;
+    }
+    if (c.ndim != 3 || !c.per[0] || !c.per[1] || !c.per[2] || c.P.ppm_type != 1 || c.P.species_pred_type != 1 ||
+        c.P.enthalpy_pred_type != 1) {
+        set_error("the adjoint covers 3-D periodic domains with ppm_type 1, species_pred_type 1 and "
+                  "enthalpy_pred_type 1");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    for (const char* nm : {"w0", "grav_cell"})
+        for (double v : c.h1.at(nm))
+            if (v != 0.0) {
+                set_error("the adjoint needs w0 = 0 and grav_cell = 0 (MAC velocities independent of the state)");
+                return MADV_ERR_UNSUPPORTED;
+            }
+    const int ns = c.nscal, K = sd->ckpt_interval, N = sd->nsteps;
+    const int nck = (N + K - 1) / K;
+    const int last0 = (nck - 1) * K;  // first step of the last block
+    const bool rev = res->grad_s != nullptr;
+    const cudaMemcpyKind DD = cudaMemcpyDeviceToDevice;
+    AdjWork W;
+    const size_t st_b = fab_doubles(c, ns, 0, -1) * sizeof(double);
+    double* wsold = W.alloc(st_b);
+    double* wsnew = W.alloc(st_b);
+    std::vector<madv_fab> fo, fn;
+    bind_raw(c, A_WSOLD, wsold, ns, 0, -1, &fo);
+    bind_raw(c, A_WSNEW, wsnew, ns, 0, -1, &fn);
+    const madv_multifab mso{c.nb, fo.data()}, msn{c.nb, fn.data()};
+    StageIO io{sd->uold, &mso, nullptr, nullptr, &msn, nullptr, nullptr, nullptr, nullptr};
+    io.sold_out = 0;
+    std::vector<StageIO> ios{io};
+    if ((rc = bind_stage(c, io))) return rc;
+    if ((rc = bind(c, A_SOLD0, sd->sold0, ns, -1, 0)) || (rc = bind(c, A_WEIGHT, sd->weight, ns, -1, 0)) ||
+        (rc = bind(c, A_SFIN, res->sfinal, ns, -1, 0)) || (rc = bind(c, A_GRADS, res->grad_s, ns, -1, 0)))
+        return rc;
+    std::vector<double*> ck, bst;
+    std::vector<std::array<double*, 3>> bed;
+    double *asold = nullptr, *scr = nullptr, *dir = nullptr;
+    size_t scr_b = 0, dir_b = 0;
+    if (rev) {
+        for (int j = 0; j < nck; ++j) ck.push_back(W.alloc(st_b));
+        for (int j = 0; j < std::min(K, N); ++j) {
+            bst.push_back(W.alloc(st_b));
+            std::array<double*, 3> e;
+            for (int d = 0; d < 3; ++d) e[d] = W.alloc(c.F[F_SEDGE0 + d].bytes);
+            bed.push_back(e);
+        }
+        asold = W.alloc(st_b);
+        bind_raw(c, A_ASOLD, asold, ns, 0, -1);
+        bind_raw(c, A_ASNEW, W.alloc(st_b), ns, 0, -1);
+        for (int d = 0; d < 3; ++d) bind_raw(c, A_AEDGE0 + d, W.alloc(fab_doubles(c, ns, 0, d) * 8), ns, 0, d);
+        // per-component scratch in one block: A_AS, A_AFORCE, A_ASL0 .. A_AQ21
+        const size_t n_as = fab_doubles(c, 1, c.ng_s, -1), n_f = fab_doubles(c, 1, 1, -1),
+                     n_2 = fab_doubles(c, 1, 2, -1);
+        scr_b = (n_as + n_f + 15 * n_2) * sizeof(double);
+        scr = W.alloc(scr_b);
+        bind_raw(c, A_AS, scr, 1, c.ng_s, -1);
+        bind_raw(c, A_AFORCE, scr + n_as, 1, 1, -1);
+        for (int s = A_ASL0; s <= A_AQ21; ++s) bind_raw(c, s, scr + n_as + n_f + (size_t)(s - A_ASL0) * n_2, 1, 2, -1);
+        dir_b = 3 * n_2 * sizeof(double);
+        dir = W.alloc(dir_b);
+        for (int s = A_ASM; s <= A_ADSVL; ++s) bind_raw(c, s, dir + (size_t)(s - A_ASM) * n_2, 1, 2, -1);
+    }
+    double* dJ = W.alloc(sizeof(double));
+    double* dpart = W.alloc(sizeof(double) * (size_t)adj_dot_parts(c));
+    if ((rc = upload_user_views(c))) return rc;
+
+    auto fwd_step = [&]() {
+        stage_body(H, ios);
+        copy_fab(c, F_USER + A_WSOLD, RHO, F_USER + A_WSNEW, RHO, 2, 0);
+        copy_fab(c, F_USER + A_WSOLD, FIRSTSPEC, F_USER + A_WSNEW, FIRSTSPEC, c.nspec, 0);
+    };
+    auto keep_step = [&](int slot) {  // state and edge states of the step about to run / just run
+        cudaMemcpyAsync(bst[slot], wsold, st_b, DD, c.stream);
+    };
+    auto keep_edges = [&](int slot) {
+        for (int d = 0; d < 3; ++d)
+            cudaMemcpyAsync(bed[slot][d], c.F[F_SEDGE0 + d].base, c.F[F_SEDGE0 + d].bytes, DD, c.stream);
+    };
+    auto rev_step = [&]() {
+        // the step's traced fields (X, rho', rhoh') as the forward formed them
+        copy_fab(c, F_SOLD, 0, F_USER + A_WSOLD, 0, ns, 0);
+        fill_patch_h(H, F_SOLD, 0, ns, BCS_S, 0, 0, 0);
+        convert_rhox_to_x_h(H, 1);
+        put_in_pert_form_h(H, "rho0_old", RHO, 0, BCS_F, 1);
+        put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
+        edge_scal_coeffs(c);
+        adj_update(c);
+        adj_flux(c, c.b1("rho0_old"), c.b1("rho0_edge_old"));
+        for (int comp = 0; comp < ns; ++comp) {
+            if (comp == TEMP || comp == PI) continue;
+            cudaMemsetAsync(scr, 0, scr_b, c.stream);
+            adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b);
+            adj_fill_boundary(c, A_AS, c.ng_s);
+            if (comp >= FIRSTSPEC) {
+                adj_convert_x(c, comp);
+            } else {
+                adj_fill_boundary(c, A_AFORCE, 1);
+                adj_pert_force(c, comp);
+            }
+        }
+        copy_fab(c, F_USER + A_ASNEW, 0, F_USER + A_ASOLD, 0, ns, 0);
+        cudaMemsetAsync(asold, 0, st_b, c.stream);
+    };
+
+    copy_fab(c, F_USER + A_WSOLD, 0, F_USER + A_SOLD0, 0, ns, 0);
+    for (int n = 0; n < N; ++n) {
+        if (rev && n % K == 0) CK(cudaMemcpyAsync(ck[n / K], wsold, st_b, DD, c.stream));
+        if (rev && n >= last0) keep_step(n - last0);
+        fwd_step();
+        if (rev && n >= last0) keep_edges(n - last0);
+    }
+    adj_dot(c, A_WEIGHT, A_WSOLD, ns, dpart, dJ);
+    if (res->sfinal) copy_fab(c, F_USER + A_SFIN, 0, F_USER + A_WSOLD, 0, ns, 0);
+    if (rev) {
+        copy_fab(c, F_USER + A_ASNEW, 0, F_USER + A_WEIGHT, 0, ns, 0);
+        for (int bk = nck - 1; bk >= 0; --bk) {
+            const int n0 = bk * K, n1 = std::min(N, n0 + K);
+            if (bk != nck - 1) {
+                CK(cudaMemcpyAsync(wsold, ck[bk], st_b, DD, c.stream));
+                for (int n = n0; n < n1; ++n) {
+                    keep_step(n - n0);
+                    fwd_step();
+                    keep_edges(n - n0);
+                }
+            }
+            for (int n = n1 - 1; n >= n0; --n) {
+                CK(cudaMemcpyAsync(wsold, bst[n - n0], st_b, DD, c.stream));
+                for (int d = 0; d < 3; ++d)
+                    CK(cudaMemcpyAsync(c.F[F_SEDGE0 + d].base, bed[n - n0][d], c.F[F_SEDGE0 + d].bytes, DD, c.stream));
+                rev_step();
+            }
+        }
+        copy_fab(c, F_USER + A_GRADS, 0, F_USER + A_ASNEW, 0, ns, 0);
+    }
+    double Jh = 0.0;
+    CK(cudaMemcpyAsync(&Jh, dJ, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    rc = finish(H);
+    res->J = Jh;
+    res->device_bytes = (long long)W.bytes;
+    return rc;
+}
+
+int madv_stage_adjoint(madv_ctx* h, const madv_adj_seed* seed, madv_adj_result* res, void* stream) {
+    try {
+        return stage_adjoint(h, seed, res, stream);
+    } catch (const Fail& f) {
+        return f.code;
+    }
 }
 
 }  // extern "C"

@@ -210,6 +210,30 @@ void average_down(Ctx& cf, Ctx& cc, int fid, int comp, int ncomp);
 void average_down_faces(Ctx& cf, Ctx& cc, int f0, int c0, int ncomp);
 void uedge_interface(Ctx& cc, Ctx& cf, int f0);
 
+// ---- reverse sweep (madv_adjoint.cu).  User slots bound by the adjoint driver: working
+// state (A_WSOLD / A_WSNEW), state adjoints (A_ASOLD / A_ASNEW), edge-state adjoints, the
+// per-component scratch of the MakeEdgeScal transpose, and the caller's FABs.
+enum {
+    A_WSOLD = 20, A_WSNEW, A_ASOLD, A_ASNEW, A_AS, A_AFORCE,
+    A_AEDGE0, A_AEDGE1, A_AEDGE2,
+    A_ASL0, A_ASL1, A_ASL2, A_ASR0, A_ASR1, A_ASR2, A_ASIMH0, A_ASIMH1, A_ASIMH2,
+    A_AQ01, A_AQ02, A_AQ10, A_AQ12, A_AQ20, A_AQ21,
+    A_ASM, A_ASP, A_ADSVL,
+    A_WEIGHT, A_SOLD0, A_GRADS, A_SFIN,
+    A_END
+};
+static_assert(A_END <= N_USER_SLOTS, "user slots");
+void ppm_faces(Ctx& c, int d, int fs, int sc);  // van Leer slopes + interface values (madv_kernels.cu)
+void edge_scal_coeffs(Ctx& c);                  // tracing / transverse coefficients of F_UMAC0..2
+void adj_update(Ctx& c);
+void adj_flux(Ctx& c, const double* r0, const double* r0e);
+void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes);
+void adj_fill_boundary(Ctx& c, int slot, int ng);
+void adj_convert_x(Ctx& c, int comp);
+void adj_pert_force(Ctx& c, int comp);
+long adj_dot_parts(Ctx& c);
+void adj_dot(Ctx& c, int slot_a, int slot_b, int nc, double* part, double* d_out);
+
 enum { BCS_S = 0, BCS_U = 1, BCS_F = 2 };
 inline const BCRecD* bcs_dev(const Ctx& c, int which) {
     return which == BCS_S ? c.d_bcs : (which == BCS_U ? c.d_bcs + c.nscal : c.d_bcs + c.nscal + 3);

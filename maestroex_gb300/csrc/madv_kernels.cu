@@ -13,6 +13,7 @@
 //   * constant quotients such as (dt/6)/dy are formed once on the host, where the
 //     reference forms them per element (same IEEE operations, same values).
 #include <cstdio>
+#include <type_traits>
 
 #include "madv_ctx.hpp"
 #include "madv_exact.cuh"
@@ -484,6 +485,24 @@ static void ppm_any(Ctx& c, int d, int fs, int sc, const BCRecD& bc, int fu, int
     else ppm_dir<2>(c, fs, sc, bc, fu, uc, umac, fip, fim);
 }
 
+// The first two launches of the ppm_type 1 sweep of ppm_dir (van Leer slopes into F_DSVL,
+// interface values into F_FACE0+d) for component sc of field fs, interior form: the
+// reverse sweep reads them to recover the forward's limiter decisions.
+void ppm_faces(Ctx& c, int d, int fs, int sc) {
+    const RecipC r6 = make_recip(6.0);
+    auto one = [&](auto dir) {
+        constexpr int D = decltype(dir)::value;
+        int glo[3] = {1, 1, 1};
+        glo[D] = 2;
+        launch(c, region(c, glo[0], glo[1], glo[2], glo[0], glo[1], glo[2], -1), 1, k_dsvl<D>, c.V(), fs, sc);
+        launch(c, region(c, 1, 1, 1, 1, 1, 1, D), 1, k_ppm_face<D, 1>, c.V(), fs, sc, F_FACE0 + D, 0, 0,
+               c.P.dom_lo[D], c.P.dom_hi[D], r6);
+    };
+    if (d == 0) one(std::integral_constant<int, 0>{});
+    else if (d == 1) one(std::integral_constant<int, 1>{});
+    else one(std::integral_constant<int, 2>{});
+}
+
 // tracing coefficients of the face velocity fields umac0..2 (or utrans0..2)
 static void trace_coeffs_faces(Ctx& c, int fu0) {
     // faces lo-1 .. hi+2 along d, cells lo-1 .. hi+1 across
@@ -525,6 +544,11 @@ static void transverse_coeffs(Ctx& c, int fu0) {
     const double dt6 = c.P.dt / 6.0, dt4 = 0.25 * c.P.dt;
     launch(c, rg_grow(c, 1), 1, k_transverse_coeffs, c.V(), fu0, dt6 / c.P.dx[0], dt6 / c.P.dx[1], dt6 / c.P.dx[2],
            dt4 / c.P.dx[0], dt4 / c.P.dx[1], dt4 / c.P.dx[2]);
+}
+
+void edge_scal_coeffs(Ctx& c) {
+    trace_coeffs_faces(c, F_UMAC0);
+    transverse_coeffs(c, F_UMAC0);
 }
 
 // ============================================================ MakeUtrans

@@ -1,0 +1,142 @@
+"""Adjoint of the multi-step scalar path (madv_stage_adjoint): the gradient of
+J = <weight, s_nsteps> with respect to the initial state against central finite
+differences of the same GPU forward, with the states differenced before the weights are
+applied (J itself is ~1e25 at these magnitudes)."""
+import numpy as np
+import pytest
+import torch
+
+from maestroex_gb300 import configs
+from maestroex_gb300.capi import MadvError
+from maestroex_gb300.params import FIRSTSPEC, PI, RHO, RHOH, TEMP
+from maestroex_gb300.stage import MultiFab, make_stage
+
+pytestmark = pytest.mark.gpu
+
+
+class Case:
+    def __init__(self, n=(32, 32, 32), max_grid=16, nspec=3, nsteps=4, ckpt=2, seed=20261203 + 4):
+        self.cfg = cfg = configs.adjoint_config(n=n, max_grid=max_grid, nspec=nspec, seed=seed)
+        self.n, self.boxes, self.nscal = cfg["n"], cfg["boxes"], 4 + nspec
+        self.nsteps, self.ckpt = nsteps, ckpt
+        self.st = make_stage(cfg)
+        self.uold = MultiFab(self.boxes, 3, 0).from_domain(cfg["uold"])
+        self.sold = MultiFab(self.boxes, self.nscal, 0).from_domain(cfg["sold"])
+        rng = np.random.default_rng(seed + 1)
+        shape = (n[2], n[1], n[0])
+        w = np.zeros((self.nscal,) + shape)
+        w[RHOH] = rng.normal(size=shape)
+        w[FIRSTSPEC:] = rng.normal(size=(nspec,) + shape)
+        self.w = w
+        self.weight = MultiFab(self.boxes, self.nscal, 0).from_domain(w)
+
+    def adjoint(self):
+        grad = MultiFab(self.boxes, self.nscal, 0, fill=float("nan"))
+        sfin = MultiFab(self.boxes, self.nscal, 0)
+        J, nbytes = self.st.stage_adjoint(self.uold, self.sold, self.weight, self.nsteps, self.ckpt, grad_s=grad,
+                                          sfinal=sfin)
+        torch.cuda.synchronize()
+        return J, grad, sfin, nbytes
+
+    def final(self, s0):
+        sfin = MultiFab(self.boxes, self.nscal, 0)
+        self.st.stage_adjoint(self.uold, s0, self.weight, self.nsteps, self.ckpt, sfinal=sfin)
+        return sfin
+
+    def locate(self, i, j, k):
+        for b, bx in enumerate(self.boxes):
+            if bx[0] <= i <= bx[3] and bx[1] <= j <= bx[4] and bx[2] <= k <= bx[5]:
+                return b, (k - bx[2], j - bx[1], i - bx[0])
+        raise AssertionError("cell outside the layout")
+
+    def perturbed(self, comp, cell, h):
+        s = MultiFab(self.boxes, self.nscal, 0)
+        for a, b in zip(s.fabs, self.sold.fabs):
+            a.copy_(b)
+        bi, loc = self.locate(*cell)
+        s.fabs[bi][(comp,) + loc] += h
+        return s
+
+    def dJ(self, a, b):
+        return sum(float((w * (x - y)).sum()) for w, x, y in zip(self.weight.fabs, a.fabs, b.fabs))
+
+
+def test_adjoint_matches_central_differences():
+    """Central differences with h = 1e-6 |x| (and h/2 to detect a limiter switch inside
+    [x - h, x + h]) at random cells of every differentiated component: density, enthalpy
+    and the species, 4 steps with a stored state every 2.  |x| is floored at a tenth of
+    the component's RMS, so that h stays above the rounding of the differenced states."""
+    case = Case()
+    J, grad, _, _ = case.adjoint()
+    G = grad.to_domain(case.n).cpu().numpy()
+    S = case.cfg["sold"]
+    rng = np.random.default_rng(99)
+    comps = [RHO, RHOH] + list(range(FIRSTSPEC, case.nscal))
+    rms = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
+    worst, checked, kinks = 0.0, 0, 0
+    for t in range(60):
+        comp = comps[t % len(comps)]
+        cell = tuple(int(v) for v in rng.integers(0, case.n[0], size=3))
+        i, j, k = cell
+        x = max(abs(S[comp, k, j, i]), 0.1 * rms[comp])
+        fd = []
+        for rel in (1e-6, 0.5e-6):
+            h = rel * x
+            sp, sm = case.perturbed(comp, cell, h), case.perturbed(comp, cell, -h)
+            fd.append(case.dJ(case.final(sp), case.final(sm)) / (2.0 * h))
+        scale = max(abs(fd[0]), abs(fd[1]))
+        if abs(fd[0] - fd[1]) > 1e-7 * scale:
+            kinks += 1
+            continue
+        g = G[comp, k, j, i]
+        err = abs(g - fd[0]) / max(scale, abs(g), 1e-300)
+        worst = max(worst, err)
+        checked += 1
+    assert np.isfinite(J)
+    assert checked >= 40, (checked, kinks)
+    assert worst <= 1e-6, worst
+
+
+def test_adjoint_carried_components_and_determinism():
+    """Temperature and pi are carried unchanged, so their gradient is the weight; two runs
+    give the same J bit for bit and gradients equal to atomic-summation rounding."""
+    case = Case(n=(32, 32, 32), max_grid=16, nsteps=3, ckpt=2)
+    case.w[TEMP] = 1.0
+    case.w[PI] = -2.0
+    case.weight.from_domain(case.w)
+    J1, g1, s1, nbytes = case.adjoint()
+    J2, g2, s2, _ = case.adjoint()
+    G1 = g1.to_domain(case.n).cpu().numpy()
+    G2 = g2.to_domain(case.n).cpu().numpy()
+    assert J1 == J2
+    assert np.array_equal(s1.to_domain(case.n).cpu().numpy(), s2.to_domain(case.n).cpu().numpy())
+    assert np.all(G1[TEMP] == 1.0) and np.all(G1[PI] == -2.0)
+    assert np.all(np.isfinite(G1))
+    scale = np.abs(G1).max(axis=(1, 2, 3), keepdims=True)
+    assert np.abs(G1 - G2).max() <= 1e-12 * scale.max()
+    assert nbytes > 0
+
+
+def test_adjoint_forward_matches_stage_forward_steps():
+    """The adjoint's forward is the stage: one step of it equals madv_stage_forward's snew
+    (density, enthalpy, species) bit for bit."""
+    from maestroex_gb300.stage import run_stage_gpu
+    case = Case(nsteps=1, ckpt=1)
+    sf = case.final(case.sold).to_domain(case.n).cpu().numpy()
+    cfg = dict(case.cfg)
+    cfg["gpi"] = np.zeros_like(cfg["gpi"])
+    ref = run_stage_gpu(cfg)["snew"]
+    for comp in [RHO, RHOH] + list(range(FIRSTSPEC, case.nscal)):
+        assert np.array_equal(sf[comp], ref[comp]), comp
+
+
+def test_adjoint_rejects_unsupported_configurations():
+    cfg = configs.planar_config(n=(16, 16, 16), max_grid=16, w0_amp=0.0)
+    st = make_stage(cfg)
+    boxes, nscal = cfg["boxes"], 4 + cfg["nspec"]
+    u = MultiFab(boxes, 3, 0)
+    s = MultiFab(boxes, nscal, 0).from_domain(cfg["sold"])
+    g = MultiFab(boxes, nscal, 0)
+    with pytest.raises(MadvError) as e:
+        st.stage_adjoint(u, s, s, 2, 1, grad_s=g)
+    assert e.value.code == -3
