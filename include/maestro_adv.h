@@ -218,7 +218,9 @@ int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_f
  *     s_0 = sold0,  s_{n+1} = Stage(uold, s_n)  (n < nsteps),  J = sum weight * s_nsteps
  * over valid cells and all nscal components.  Stage is madv_stage_forward's computation
  * (snew's density, enthalpy and species; temperature and pi are carried), with gpi = 0
- * and thermal = 0.  The reverse sweep transposes each phase with the forward's limiter
+ * and thermal = 0.  The velocity is held fixed, so dJ/duold sums the MAC-velocity
+ * adjoints of all steps through one transposed AdvancePremac (VelPred, MakeUtrans).
+ * The reverse sweep transposes each phase with the forward's limiter
  * and upwind decisions frozen; states are stored every ckpt_interval steps and each
  * block is recomputed from its stored state, so memory grows with nsteps/ckpt_interval
  * + ckpt_interval states.  No counterpart in the reference.
@@ -236,7 +238,9 @@ typedef struct {
 
 typedef struct {
     const madv_multifab* sfinal; /* out (may be NULL): s_nsteps, nscal components */
-    const madv_multifab* grad_s; /* out (NULL: forward only): dJ/dsold0, nscal components */
+    const madv_multifab* grad_s; /* out (may be NULL): dJ/dsold0, nscal components */
+    const madv_multifab* grad_u; /* out (may be NULL): dJ/duold, 3 components; both NULL:
+                                    forward only */
     double J;                    /* out */
     long long device_bytes;      /* out: device memory the call allocated (freed on return) */
 } madv_adj_result;

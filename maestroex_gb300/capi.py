@@ -54,8 +54,8 @@ class MadvAdjSeed(C.Structure):
 
 
 class MadvAdjResult(C.Structure):
-    _fields_ = [("sfinal", C.POINTER(MadvMultiFab)), ("grad_s", C.POINTER(MadvMultiFab)), ("J", C.c_double),
-                ("device_bytes", C.c_longlong)]
+    _fields_ = [("sfinal", C.POINTER(MadvMultiFab)), ("grad_s", C.POINTER(MadvMultiFab)),
+                ("grad_u", C.POINTER(MadvMultiFab)), ("J", C.c_double), ("device_bytes", C.c_longlong)]
 
 
 class MadvError(RuntimeError):

@@ -1,8 +1,9 @@
-// Reverse (adjoint) sweep of the scalar path of the advection stage: the transposes of
+// Reverse (adjoint) sweep of the advection stage on a fixed velocity: the transposes of
 // UpdateScal, MakeRhoXFlux / MakeRhoHFlux (species_pred_type 1, enthalpy_pred_type 1),
 // MakeEdgeScal with PPM ppm_type 1 (van Leer slopes, interface values, cell-edge limiter,
 // characteristic tracing, predictor, transverse and edge corrections), the pointwise
-// conversions of DensityAdvance / EnthalpyAdvance and FillBoundary.
+// conversions and forces of DensityAdvance / EnthalpyAdvance and FillBoundary; and, for
+// the gradient with respect to the cell velocity, of VelPred and MakeUtrans.
 //
 // Every limiter, clamp and upwind decision is recomputed from the forward inputs with the
 // forward's own expressions (the same compile flags, so the same bits), i.e. the
@@ -12,18 +13,20 @@
 // wherever a transpose reads one cell past the forward region).
 //
 // Scope: 3-D, one level, periodic domain, MAC velocities independent of the state
-// (no buoyancy or pressure-gradient force, w0 = 0).  The forward kernels this mirrors
-// are in madv_kernels.cu (k_update_rhox / k_update_rhoh, k_rhox_flux / k_rhoh_flux,
-// k_es_edges, k_es_transverse, k_es_predictor, k_ppm_cell, k_ppm_face, k_dsvl,
-// k_rhox_to_x, k_pert, k_modify_scal_force, k_fill_boundary).
+// (grav_cell = 0, no pressure gradient, w0 = 0), so the velocity force is zero.  With
+// grav_cell = 0 the gradp0 of MakeRhoHForce is zero (below the cutoff it is rho0 g; above
+// it the reference differences the planar p0 across j, Source/MaestroForce.cpp:606-614),
+// so the rhoh forces' veladv term has no derivative.  The forward kernels mirrored here
+// are in madv_kernels.cu.
 #include "madv_launch.cuh"
 #include "madv_ppm.cuh"
 
 namespace madv {
 
 #define AW(s) VW(F_USER + (s))
+#define AQ_SLOT(a, b) (A_AQ01 + 2 * (a) + ((b) > (a) ? (b)-1 : (b)))
 
-// Weights of the reference's upwinding  v = (u > 0) ? l : r  for |u| > t, (l + r)/2 otherwise.
+// Weights of the scalar upwinding  v = (u > 0) ? l : r  for |u| > t, (l + r)/2 otherwise.
 __device__ __forceinline__ void upwind_w(double u, long long tb, double& wl, double& wr) {
     const long long ub = dbits(u);
     if ((ub & ABS_MASK) > tb) {
@@ -33,6 +36,33 @@ __device__ __forceinline__ void upwind_w(double u, long long tb, double& wl, dou
         wl = 0.5;
         wr = 0.5;
     }
+}
+
+// Weights of VelPred's upwinding by the transverse velocity: (l + r)/2 for |tr| < rel_eps.
+__device__ __forceinline__ void upwind_w_vp(double tr, long long tb, double& wl, double& wr) {
+    if ((dbits(tr) & ABS_MASK) >= tb) {
+        wl = gt0(tr) ? 1.0 : 0.0;
+        wr = 1.0 - wl;
+    } else {
+        wl = 0.5;
+        wr = 0.5;
+    }
+}
+
+// The Riemann selection of MakeUtrans / VelPredVelocities (w0c = w0_cart on z-faces):
+// 0 (the value 0), 1 (l) or 2 (r).
+__device__ __forceinline__ int riemann_pick(double l, double r, double w0c, bool zdir, double rel_eps) {
+    bool test;
+    double v;
+    if (!zdir) {
+        test = (l <= 0.0 && r >= 0.0) || (fabs(l + r) < rel_eps);
+        v = 0.5 * (l + r);
+    } else {
+        test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fabs(l + r + 2.0 * w0c) < rel_eps);
+        v = 0.5 * (l + r) + w0c;
+    }
+    if (test) return 0;
+    return v > 0.0 ? 1 : 2;
 }
 
 // ------------------------------------------------------------------ UpdateScal^T
@@ -59,11 +89,13 @@ __global__ void k_adj_update(KARGS, int nspec) {
 
 // Flux transposes on the valid D-faces of each box.  The update of a box reads only its
 // own face fluxes, so the flux adjoint of face f is dt/h (a(f) - a(f-1)) over the cells
-// f, f-1 that lie in the box.  Then, with F_X = u (rho0_edge + rho'_e) X_e and
-// F_h = u (rhoh0_edge + rhoh'_e): the edge-state adjoints go to A_AEDGE0+D.
+// f, f-1 that lie in the box.  With F_X = u (rho0_edge + rho'_e) X_e and
+// F_h = u (rhoh0_edge + rhoh'_e): edge-state adjoints to A_AEDGE0+D, and (want_u) the
+// face-velocity adjoint to A_AUMAC0+D.
 template <int D>
 __global__ void k_adj_flux(KARGS, int nspec, double dtdx, const double* __restrict__ r0a,
-                           const double* __restrict__ r0b) {
+                           const double* __restrict__ r0b, const double* __restrict__ h0a,
+                           const double* __restrict__ h0b, int want_u) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const RegionBox& rr = R[e_];
@@ -78,24 +110,31 @@ __global__ void k_adj_flux(KARGS, int nspec, double dtdx, const double* __restri
         if (cell_lo) a -= at(an, i - di, j - dj, k - dk, comp);
         return dtdx * a;
     };
-    const double r0e = 0.5 * (r0a[k] + r0b[k]);
-    const double cx = u * (r0e + at(e, i, j, k, RHO));
-    double arho = 0.0;
+    const double erho = 0.5 * (r0a[k] + r0b[k]) + at(e, i, j, k, RHO);
+    const double cx = u * erho;
+    double arho = 0.0, gu = 0.0;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
         const double fb = fbar(comp);
+        const double ex = at(e, i, j, k, comp);
         at(ae, i, j, k, comp) = cx * fb;
-        arho += u * at(e, i, j, k, comp) * fb;
+        arho += u * ex * fb;
+        gu += erho * ex * fb;
     }
     at(ae, i, j, k, RHO) = arho;
-    at(ae, i, j, k, RHOH) = u * fbar(RHOH);
+    const double fh = fbar(RHOH);
+    at(ae, i, j, k, RHOH) = u * fh;
+    if (want_u) {
+        gu += (0.5 * (h0a[k] + h0b[k]) + at(e, i, j, k, RHOH)) * fh;
+        at(AW(A_AUMAC0 + D), i, j, k) += gu;
+    }
 }
 
 // ------------------------------------------------------------------ MakeEdgeScal^T
-#define AQ_SLOT(a, b) (A_AQ01 + 2 * (a) + ((b) > (a) ? (b)-1 : (b)))
-
-// k_es_edges (advective form) transposed: valid D-faces.
+// k_es_edges (advective form) transposed: valid D-faces.  want_u: the adjoint of the
+// transverse coefficients (F_TCOEF comps 3+t) into A_ATCOEF, from the forward transverse
+// states of this component (F_Q fields).
 template <int D>
-__global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long long epsb) {
+__global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long long epsb, int want_u) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -126,11 +165,18 @@ __global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long
         atomicAdd(&at(af, il, jl, kl), dt2 * la);
         atomicAdd(&at(af, i, j, k), dt2 * ra);
     }
+    if (want_u) {
+        const FabView atc = AW(A_ATCOEF), f1 = VW(Q_FIELD(T1, T2)), f2 = VW(Q_FIELD(T2, T1));
+        atomicAdd(&at(atc, il, jl, kl, 3 + T1), -la * (at(f1, il + a1i, jl + a1j, kl + a1k) - at(f1, il, jl, kl)));
+        atomicAdd(&at(atc, il, jl, kl, 3 + T2), -la * (at(f2, il + a2i, jl + a2j, kl + a2k) - at(f2, il, jl, kl)));
+        atomicAdd(&at(atc, i, j, k, 3 + T1), -ra * (at(f1, i + a1i, j + a1j, k + a1k) - at(f1, i, j, k)));
+        atomicAdd(&at(atc, i, j, k, 3 + T2), -ra * (at(f2, i + a2i, j + a2j, k + a2k) - at(f2, i, j, k)));
+    }
 }
 
 // k_es_transverse (advective form) transposed: D-faces corrected in direction T.
 template <int D, int T>
-__global__ void k_adj_es_transverse(KARGS, long long epsb) {
+__global__ void k_adj_es_transverse(KARGS, long long epsb, int want_u) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
@@ -147,6 +193,11 @@ __global__ void k_adj_es_transverse(KARGS, long long epsb) {
     atomicAdd(&at(sh, il, jl, kl), cl);
     atomicAdd(&at(sh, i + ti, j + tj, k + tk), -cr);
     atomicAdd(&at(sh, i, j, k), cr);
+    if (want_u) {
+        const FabView atc = AW(A_ATCOEF), s = VW(F_SIMH0 + T);
+        atomicAdd(&at(atc, il, jl, kl, T), -la * (at(s, il + ti, jl + tj, kl + tk) - at(s, il, jl, kl)));
+        atomicAdd(&at(atc, i, j, k, T), -ra * (at(s, i + ti, j + tj, k + tk) - at(s, i, j, k)));
+    }
 }
 
 // k_es_predictor (ppm_type 1) transposed: simh = upwind(u, l, r, 0).
@@ -160,48 +211,77 @@ __global__ void k_adj_es_predictor(KARGS) {
     at(AW(A_ASR0 + D), i, j, k) += wr * sb;
 }
 
-// k_ppm_cell<D, 1, 1> transposed (cells of the box grown by one): the predictor reads
+// k_ppm_cell<D, 1, UMAC> transposed (cells of the box grown by one).  The predictors read
 // l(face f) = Ip(cell f-1) and r(face f) = Im(cell f), so Ip / Im of a cell take the
-// adjoints of its high / low face.  Tracing is linear in (s0, sm, sp) for the frozen
-// upwind tests; the quadratic limiter (Source/MaestroPPM.cpp:117-128) is piecewise
-// linear in (s0, interface values).  Interface adjoints go to A_ASM (low face) and A_ASP
-// (high face) per cell, gathered per face by k_adj_ppm_face.
-template <int D>
-__global__ void k_adj_ppm_cell(KARGS, int fs, int sc, long long epsb) {
+// adjoints of its high / low face, component lc of A_ASL0+D / A_ASR0+D.  Tracing is
+// linear in (s0, sm, sp) for the frozen upwind tests; the quadratic limiter
+// (Source/MaestroPPM.cpp:117-128) is piecewise linear in (s0, interface values).
+// Interface adjoints go to A_ASM (low face) and A_ASP (high face) per cell, gathered per
+// face by k_adj_ppm_face; the cell adjoint to slot ts, component tcomp.
+// want_u: the tracing coefficients A = |u| dt/(2h), B = 1 - (2/3)|u| dt/h depend on the
+// tracing velocity: UMAC = 1, the D-faces of F_UMAC0+D (adjoint atomically into
+// A_AUMAC0+D); UMAC = 0, component D of the cell velocity F_UFULL = F_UTILDE + w0_cart
+// (adjoint into ts, component D).
+template <int D, int UMAC>
+__global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp, long long epsb, double dtdx,
+                               int want_u) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
-    const double ipb = at(AW(A_ASL0 + D), i + di, j + dj, k + dk);
-    const double imb = at(AW(A_ASR0 + D), i, j, k);
-    const FabView s = VW(fs), F = VW(F_FACE0 + D), T = VW(F_TRA0 + D), u = VW(F_UMAC0 + D);
+    const double ipb = at(AW(A_ASL0 + D), i + di, j + dj, k + dk, lc);
+    const double imb = at(AW(A_ASR0 + D), i, j, k, lc);
+    if (ipb == 0.0 && imb == 0.0) return;  // A_ASM / A_ASP were cleared
+    const FabView s = VW(fs), F = VW(F_FACE0 + D);
     const double s0 = at(s, i, j, k, sc);
     double sm = at(F, i, j, k), sp = at(F, i + di, j + dj, k + dk);
     int cs = 3;
     if ((sp - s0) * (s0 - sm) <= 0.0) {
+        sp = s0;
+        sm = s0;
         cs = 0;
     } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
+        sp = 3.0 * s0 - 2.0 * sm;
         cs = 1;
     } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
+        sm = 3.0 * s0 - 2.0 * sp;
         cs = 2;
     }
-    double bs0 = 0.0, bsm = 0.0, bsp = 0.0;
-    if (gt_t(at(u, i + di, j + dj, k + dk), epsb)) {
-        const double A = at(T, i + di, j + dj, k + dk, 0), B = at(T, i + di, j + dj, k + dk, 1);
-        bsp += (1.0 - A - 3.0 * A * B) * ipb;
-        bsm += (A - 3.0 * A * B) * ipb;
-        bs0 += 6.0 * A * B * ipb;
+    double up, um, Ap, Bp, Am, Bm;
+    if (UMAC) {
+        const FabView T = VW(F_TRA0 + D), u = VW(F_UMAC0 + D);
+        up = at(u, i + di, j + dj, k + dk);
+        um = at(u, i, j, k);
+        Ap = at(T, i + di, j + dj, k + dk, 0);
+        Bp = at(T, i + di, j + dj, k + dk, 1);
+        Am = at(T, i, j, k, 0);
+        Bm = at(T, i, j, k, 1);
+    } else {
+        const FabView T = VW(F_TRC);
+        up = um = at(VW(F_UFULL), i, j, k, D);
+        Ap = Am = at(T, i, j, k, 2 * D);
+        Bp = Bm = at(T, i, j, k, 2 * D + 1);
+    }
+    const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
+    double bs0 = 0.0, bsm = 0.0, bsp = 0.0, gup = 0.0, gum = 0.0;
+    if (gt_t(up, epsb)) {
+        bsp += (1.0 - Ap - 3.0 * Ap * Bp) * ipb;
+        bsm += (Ap - 3.0 * Ap * Bp) * ipb;
+        bs0 += 6.0 * Ap * Bp * ipb;
+        // d ip/dA = -(sp - sm - B s6), d ip/dB = A s6
+        gup = copysign(dtdx, up) * (-0.5 * (sp - sm - Bp * s6) - (2.0 / 3.0) * Ap * s6) * ipb;
     } else {
         bs0 += ipb;
     }
-    if (lt_negt(at(u, i, j, k), epsb)) {
-        const double A = at(T, i, j, k, 0), B = at(T, i, j, k, 1);
-        bsm += (1.0 - A - 3.0 * A * B) * imb;
-        bsp += (A - 3.0 * A * B) * imb;
-        bs0 += 6.0 * A * B * imb;
+    if (lt_negt(um, epsb)) {
+        bsm += (1.0 - Am - 3.0 * Am * Bm) * imb;
+        bsp += (Am - 3.0 * Am * Bm) * imb;
+        bs0 += 6.0 * Am * Bm * imb;
+        // d im/dA = sp - sm + B s6, d im/dB = A s6
+        gum = copysign(dtdx, um) * (0.5 * (sp - sm + Bm * s6) - (2.0 / 3.0) * Am * s6) * imb;
     } else {
         bs0 += imb;
     }
     double fm = 0.0, fp = 0.0;
-    if (cs == 0) {  // sm = sp = s0
+    if (cs == 0) {
         bs0 += bsm + bsp;
     } else if (cs == 1) {  // sp = 3 s0 - 2 sm
         bs0 += 3.0 * bsp;
@@ -215,18 +295,29 @@ __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, long long epsb) {
     }
     at(AW(A_ASM), i, j, k) = fm;
     at(AW(A_ASP), i, j, k) = fp;
-    at(AW(A_AS), i, j, k) += bs0;
+    const FabView t = AW(ts);
+    at(t, i, j, k, tcomp) += bs0;
+    if (want_u) {
+        if (UMAC) {
+            const FabView au = AW(A_AUMAC0 + D);
+            if (gup != 0.0) atomicAdd(&at(au, i + di, j + dj, k + dk), gup);
+            if (gum != 0.0) atomicAdd(&at(au, i, j, k), gum);
+        } else {
+            at(t, i, j, k, D) += gup + gum;
+        }
+    }
 }
 
 // k_ppm_face<D, 1> transposed (Source/MaestroPPM.cpp:37-111 interior form):
 // v = min(max(v0, min(s0, s-1)), max(s0, s-1)), v0 = (s0 + s-1)/2 - (dv(f) - dv(f-1))/6.
+// Cell adjoints to slot ts, component tcomp.
 template <int D>
-__global__ void k_adj_ppm_face(KARGS, int fs, int sc, RecipC r6) {
+__global__ void k_adj_ppm_face(KARGS, int fs, int sc, int ts, int tcomp, RecipC r6) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const double fb = at(AW(A_ASM), i, j, k) + at(AW(A_ASP), i - di, j - dj, k - dk);
     if (fb == 0.0) return;
-    const FabView s = VW(fs), dv = VW(F_DSVL), as = AW(A_AS);
+    const FabView s = VW(fs), dv = VW(F_DSVL), as = AW(ts);
     const double sl = at(s, i - di, j - dj, k - dk, sc), s0 = at(s, i, j, k, sc);
     const double v0 = 0.5 * (s0 + sl) - div_c(at(dv, i, j, k) - at(dv, i - di, j - dj, k - dk), r6);
     // mn(a, b) = (b < a) ? b : a and mx(a, b) = (a < b) ? b : a, as in the forward
@@ -239,27 +330,27 @@ __global__ void k_adj_ppm_face(KARGS, int fs, int sc, RecipC r6) {
     }
     if (hi < v) src = (s0 < sl) ? 2 : 1;
     if (src == 0) {
-        atomicAdd(&at(as, i, j, k), 0.5 * fb);
-        atomicAdd(&at(as, i - di, j - dj, k - dk), 0.5 * fb);
+        atomicAdd(&at(as, i, j, k, tcomp), 0.5 * fb);
+        atomicAdd(&at(as, i - di, j - dj, k - dk, tcomp), 0.5 * fb);
         const FabView ad = AW(A_ADSVL);
         atomicAdd(&at(ad, i, j, k), -fb / 6.0);
         atomicAdd(&at(ad, i - di, j - dj, k - dk), fb / 6.0);
     } else if (src == 1) {
-        atomicAdd(&at(as, i, j, k), fb);
+        atomicAdd(&at(as, i, j, k, tcomp), fb);
     } else {
-        atomicAdd(&at(as, i - di, j - dj, k - dk), fb);
+        atomicAdd(&at(as, i - di, j - dj, k - dk, tcomp), fb);
     }
 }
 
 // k_dsvl<D> transposed (Source/MaestroPPM.cpp:37-73):
 // dv = sign(dsc) min(|dsc|, |dsl|, |dsr|) where dsl dsr > 0, else 0.
 template <int D>
-__global__ void k_adj_dsvl(KARGS, int fs, int sc) {
+__global__ void k_adj_dsvl(KARGS, int fs, int sc, int ts, int tcomp) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const double g = at(AW(A_ADSVL), i, j, k);
     if (g == 0.0) return;
-    const FabView s = VW(fs), as = AW(A_AS);
+    const FabView s = VW(fs), as = AW(ts);
     auto S = SHIFT_S(s, sc);
     const double dsc = 0.5 * (S(1) - S(-1));
     const double dsl = 2.0 * (S(0) - S(-1));
@@ -268,7 +359,7 @@ __global__ void k_adj_dsvl(KARGS, int fs, int sc) {
     const double ac = fabs(dsc), al = fabs(dsl), ar = fabs(dsr);
     const bool inner_r = ar < al;  // mn(|dsl|, |dsr|)
     const double inner = inner_r ? ar : al;
-    auto add = [&](int m, double v) { atomicAdd(&at(as, i + m * di, j + m * dj, k + m * dk), v); };
+    auto add = [&](int m, double v) { atomicAdd(&at(as, i + m * di, j + m * dj, k + m * dk, tcomp), v); };
     if (inner < ac) {  // dv = sign(dsc) |dsl| or sign(dsc) |dsr|
         const double sg = copysign(1.0, dsc);
         if (inner_r) {
@@ -286,10 +377,10 @@ __global__ void k_adj_dsvl(KARGS, int fs, int sc) {
     }
 }
 
-// FillBoundary transposed: every ghost cell was copied from one valid cell, so its
-// adjoint is added to that cell and cleared.
+// FillBoundary transposed: every ghost cell (or face) was copied from one valid one, so
+// its adjoint is added there and cleared.
 __global__ void k_adj_fill_boundary(const CopyDesc* __restrict__ D, int nd, long total, const FabView* __restrict__ V,
-                                    int nb, int f) {
+                                    int nb, int f, int nc) {
     const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= total) return;
     int lo = 0, hi = nd - 1;
@@ -306,10 +397,13 @@ __global__ void k_adj_fill_boundary(const CopyDesc* __restrict__ D, int nd, long
     const long q2 = q / ny;
     const int j = cd.lo[1] + (int)(q - q2 * ny);
     const int k = cd.lo[2] + (int)q2;
-    double& g = at(V[f * nb + cd.dst_b], i, j, k);
-    const double v = g;
-    if (v != 0.0) atomicAdd(&at(V[f * nb + cd.src_b], i - cd.shift[0], j - cd.shift[1], k - cd.shift[2]), v);
-    g = 0.0;
+    const FabView dst = V[f * nb + cd.dst_b], src = V[f * nb + cd.src_b];
+    for (int n = 0; n < nc; ++n) {
+        double& g = at(dst, i, j, k, n);
+        const double v = g;
+        if (v != 0.0) atomicAdd(&at(src, i - cd.shift[0], j - cd.shift[1], k - cd.shift[2], n), v);
+        g = 0.0;
+    }
 }
 
 // ConvertRhoXToX transposed (valid cells): X = rhoX / rho.
@@ -323,15 +417,155 @@ __global__ void k_adj_x(KARGS, int comp) {
     at(ao, i, j, k, RHO) -= a * x / rho;
 }
 
-// PutInPertForm transposed (s' = s - s0) together with the state term of the traced
-// force, ModifyScalForce fullform 0: f = ... - (s - s0) divu - div(s0 u) (valid cells).
-__global__ void k_adj_pert(KARGS, int comp, RecipC r0, RecipC r1, RecipC r2) {
+// PutInPertForm transposed (s' = s - s0) together with the traced force of
+// ModifyScalForce, fullform 0 (Source/MaestroForce.cpp:413-441, valid cells):
+// f = ... - (s - s0) divu - [s0 (du + dv) + (w(k+1) s0e(k+1) - w(k) s0e(k))/dz].
+// want_u: the force's face-velocity adjoint, d f/du(i+1) = -s/dx, d f/dw(k+1) =
+// -(s - s0 + s0e(k+1))/dz, ...  (atomically into A_AUMAC0..2).  s0e(k) is the edge value
+// the forward read from its Cartesian copy: above the top cell that is the ghost cell
+// FillPatch filled, in a periodic domain the image of the bottom edge.
+__global__ void k_adj_pert(KARGS, int comp, const double* __restrict__ s0a, const double* __restrict__ s0e,
+                           RecipC r0, RecipC r1, RecipC r2, int domlo, int domhi, int want_u) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
     const double du = div_c(at(um, i + 1, j, k) - at(um, i, j, k), r0);
     const double dv = div_c(at(vm, i, j + 1, k) - at(vm, i, j, k), r1);
     const double divu = du + dv + div_c(at(wm, i, j, k + 1) - at(wm, i, j, k), r2);
-    at(AW(A_ASOLD), i, j, k, comp) += at(AW(A_AS), i, j, k) - divu * at(AW(A_AFORCE), i, j, k);
+    const double fb = at(AW(A_AFORCE), i, j, k);
+    at(AW(A_ASOLD), i, j, k, comp) += at(AW(A_AS), i, j, k) - divu * fb;
+    if (want_u && fb != 0.0) {
+        const double s = at(AW(A_WSOLD), i, j, k, comp), s0 = s0a[k];
+        const double gx = s * fb / r0.y, gy = s * fb / r1.y;
+        atomicAdd(&at(AW(A_AUMAC0), i + 1, j, k), -gx);
+        atomicAdd(&at(AW(A_AUMAC0), i, j, k), gx);
+        atomicAdd(&at(AW(A_AUMAC1), i, j + 1, k), -gy);
+        atomicAdd(&at(AW(A_AUMAC1), i, j, k), gy);
+        const int kp = k + 1 > domhi ? domlo : k + 1;
+        atomicAdd(&at(AW(A_AUMAC2), i, j, k + 1), -(s - s0 + s0e[kp]) * fb / r2.y);
+        atomicAdd(&at(AW(A_AUMAC2), i, j, k), (s - s0 + s0e[k]) * fb / r2.y);
+    }
+}
+
+// Transverse coefficients transposed (k_transverse_coeffs: per cell c and direction t,
+// dt6/h_t (u_t(c+e_t) + u_t(c)) and dt4/h_t (...)), gathered per t-face from the two
+// cells that read it: the adjoints of F_TCOEF are in A_ATCOEF, the face-velocity adjoint
+// is added to slot ts + T.
+template <int T>
+__global__ void k_adj_tcoef(KARGS, int ts, double dt6h, double dt4h) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
+    const FabView a = AW(A_ATCOEF);
+    const double g = dt6h * (at(a, i, j, k, T) + at(a, i - ti, j - tj, k - tk, T)) +
+                     dt4h * (at(a, i, j, k, 3 + T) + at(a, i - ti, j - tj, k - tk, 3 + T));
+    at(AW(ts + T), i, j, k) += g;
+}
+
+// ------------------------------------------------------------------ VelPred^T, MakeUtrans^T
+// k_vp_velocities transposed (valid D-faces): umac = Riemann(ml, mr) with
+// ml = SL_D(D) - tc(3+T1) dq1 - tc(3+T2) dq2 + dt/2 f (the force is state- and
+// velocity-independent here).
+template <int D>
+__global__ void k_adj_vp_velocities(KARGS, double dt2, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    constexpr int a1i = T1 == 0, a1j = T1 == 1, a1k = T1 == 2;
+    constexpr int a2i = T2 == 0, a2j = T2 == 1, a2k = T2 == 2;
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const double vb = at(AW(A_AUMAC0 + D), i, j, k);
+    if (vb == 0.0) return;
+    const FabView tc = VW(F_TCOEF);
+    const FabView q1 = VW(Q_FIELD(D, T1)), q2 = VW(Q_FIELD(D, T2));
+    const FabView f = VW(F_VELFORCE);
+    const double dq1l = at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl);
+    const double dq2l = at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl);
+    const double dq1r = at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k);
+    const double dq2r = at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k);
+    const double ml = at(VW(F_SL0 + D), i, j, k, D) - at(tc, il, jl, kl, 3 + T1) * dq1l -
+                      at(tc, il, jl, kl, 3 + T2) * dq2l + dt2 * at(f, il, jl, kl, D);
+    const double mr = at(VW(F_SR0 + D), i, j, k, D) - at(tc, i, j, k, 3 + T1) * dq1r -
+                      at(tc, i, j, k, 3 + T2) * dq2r + dt2 * at(f, i, j, k, D);
+    const double w0c = D == 2 ? at(VW(F_W0CART), i, j, k, 2) : 0.0;
+    const int pick = riemann_pick(ml, mr, w0c, D == 2, rel_eps);
+    if (pick == 0) return;
+    const FabView qa1 = AW(AQ_SLOT(D, T1)), qa2 = AW(AQ_SLOT(D, T2)), atc = AW(A_ATCOEF);
+    if (pick == 1) {
+        at(AW(A_ASL0 + D), i, j, k, D) += vb;
+        double c1 = at(tc, il, jl, kl, 3 + T1) * vb, c2 = at(tc, il, jl, kl, 3 + T2) * vb;
+        atomicAdd(&at(qa1, il + a1i, jl + a1j, kl + a1k), -c1);
+        atomicAdd(&at(qa1, il, jl, kl), c1);
+        atomicAdd(&at(qa2, il + a2i, jl + a2j, kl + a2k), -c2);
+        atomicAdd(&at(qa2, il, jl, kl), c2);
+        atomicAdd(&at(atc, il, jl, kl, 3 + T1), -vb * dq1l);
+        atomicAdd(&at(atc, il, jl, kl, 3 + T2), -vb * dq2l);
+    } else {
+        at(AW(A_ASR0 + D), i, j, k, D) += vb;
+        double c1 = at(tc, i, j, k, 3 + T1) * vb, c2 = at(tc, i, j, k, 3 + T2) * vb;
+        atomicAdd(&at(qa1, i + a1i, j + a1j, k + a1k), -c1);
+        atomicAdd(&at(qa1, i, j, k), c1);
+        atomicAdd(&at(qa2, i + a2i, j + a2j, k + a2k), -c2);
+        atomicAdd(&at(qa2, i, j, k), c2);
+        atomicAdd(&at(atc, i, j, k, 3 + T1), -vb * dq1r);
+        atomicAdd(&at(atc, i, j, k, 3 + T2), -vb * dq2r);
+    }
+}
+
+// k_vp_transverse<C, D> transposed: component C on D-faces corrected in T = 3 - C - D,
+// upwinded by utrans_D.
+template <int C, int D>
+__global__ void k_adj_vp_transverse(KARGS, long long epsb) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int T = 3 - C - D;
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const double qb = at(AW(AQ_SLOT(C, D)), i, j, k);
+    if (qb == 0.0) return;
+    double wl, wr;
+    upwind_w_vp(at(VW(F_UTRANS0 + D), i, j, k), epsb, wl, wr);
+    const double la = wl * qb, ra = wr * qb;
+    at(AW(A_ASL0 + D), i, j, k, C) += la;
+    at(AW(A_ASR0 + D), i, j, k, C) += ra;
+    const FabView tc = VW(F_TCOEF), s = VW(F_SIMH0 + T), sh = AW(A_ASIMH0 + T), atc = AW(A_ATCOEF);
+    const double cl = at(tc, il, jl, kl, T) * la, cr = at(tc, i, j, k, T) * ra;
+    atomicAdd(&at(sh, il + ti, jl + tj, kl + tk, C), -cl);
+    atomicAdd(&at(sh, il, jl, kl, C), cl);
+    atomicAdd(&at(sh, i + ti, j + tj, k + tk, C), -cr);
+    atomicAdd(&at(sh, i, j, k, C), cr);
+    atomicAdd(&at(atc, il, jl, kl, T), -la * (at(s, il + ti, jl + tj, kl + tk, C) - at(s, il, jl, kl, C)));
+    atomicAdd(&at(atc, i, j, k, T), -ra * (at(s, i + ti, j + tj, k + tk, C) - at(s, i, j, k, C)));
+}
+
+// k_utrans<D> transposed (valid D-faces, ppm_type 1): utrans = Riemann(Ip(il), Im(i)) of
+// the D component traced along D; its adjoint joins VelPred's at SL_D / SR_D comp D.
+template <int D>
+__global__ void k_adj_utrans(KARGS, double rel_eps) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const double vb = at(AW(A_AUTRANS0 + D), i, j, k);
+    if (vb == 0.0) return;
+    const double l = at(VW(F_IPC0 + D), i - di, j - dj, k - dk, D);
+    const double r = at(VW(F_IMC0 + D), i, j, k, D);
+    const double w0c = D == 2 ? at(VW(F_W0CART), i, j, k, 2) : 0.0;
+    const int pick = riemann_pick(l, r, w0c, D == 2, rel_eps);
+    if (pick == 1) at(AW(A_ASL0 + D), i, j, k, D) += vb;
+    else if (pick == 2) at(AW(A_ASR0 + D), i, j, k, D) += vb;
+}
+
+// k_vp_interface<D> transposed (ppm_type 1): simh_D(n) = upwind by utrans_D of
+// (Ip_n(il), Im_n(i)) for n != D.
+template <int D>
+__global__ void k_adj_vp_interface(KARGS, long long epsb) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    double wl, wr;
+    upwind_w_vp(at(VW(F_UTRANS0 + D), i, j, k), epsb, wl, wr);
+    const FabView sh = AW(A_ASIMH0 + D), L = AW(A_ASL0 + D), Rr = AW(A_ASR0 + D);
+    for (int n = 0; n < 3; ++n) {
+        if (n == D) continue;
+        const double sb = at(sh, i, j, k, n);
+        at(L, i, j, k, n) += wl * sb;
+        at(Rr, i, j, k, n) += wr * sb;
+    }
 }
 
 // sum over the region of sum_n A(n) B(n): one partial sum per block, then a fixed-order
@@ -374,20 +608,24 @@ __global__ void k_sum_parts(const double* __restrict__ part, long n, double* __r
 // ------------------------------------------------------------------ host wrappers
 void adj_update(Ctx& c) { launch(c, rg_grow(c, 0), 1, k_adj_update, c.V(), c.nspec); }
 
-void adj_flux(Ctx& c, const double* r0, const double* r0e) {
-    launch(c, rg_grow(c, 0, 0), 1, k_adj_flux<0>, c.V(), c.nspec, c.P.dt / c.P.dx[0], r0, r0);
-    launch(c, rg_grow(c, 0, 1), 1, k_adj_flux<1>, c.V(), c.nspec, c.P.dt / c.P.dx[1], r0, r0);
-    launch(c, rg_grow(c, 0, 2), 1, k_adj_flux<2>, c.V(), c.nspec, c.P.dt / c.P.dx[2], r0e, r0e);
+void adj_flux(Ctx& c, int want_u) {
+    const double *r0 = c.b1("rho0_old"), *r0e = c.b1("rho0_edge_old");
+    const double *h0 = c.b1("rhoh0_old"), *h0e = c.b1("rhoh0_edge_old");
+    const int ns = c.nspec;
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_flux<0>, c.V(), ns, c.P.dt / c.P.dx[0], r0, r0, h0, h0, want_u);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_flux<1>, c.V(), ns, c.P.dt / c.P.dx[1], r0, r0, h0, h0, want_u);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_flux<2>, c.V(), ns, c.P.dt / c.P.dx[2], r0e, r0e, h0e, h0e, want_u);
 }
 
 template <int D, int T>
-static void adj_transverse_launch(Ctx& c, long long eb) {
+static void adj_transverse_launch(Ctx& c, long long eb, int want_u) {
     constexpr int O = 3 - D - T;
     int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
     glo[O] = 1;
     ghi[O] = 1;
     ghi[D] = 1;
-    launch(c, region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1), 1, k_adj_es_transverse<D, T>, c.V(), eb);
+    launch(c, region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1), 1, k_adj_es_transverse<D, T>, c.V(), eb,
+           want_u);
 }
 
 template <int D>
@@ -397,55 +635,118 @@ static void adj_predictor_launch(Ctx& c) {
     launch(c, region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1), 1, k_adj_es_predictor<D>, c.V());
 }
 
-template <int D>
-static void adj_ppm_launch(Ctx& c, int fs, int comp, long long eb, double* dir, size_t dir_bytes) {
-    ppm_faces(c, D, fs, comp);
+// PPM^T of component sc of field fs along D (ppm_type 1, interior form): adjoints of
+// Ip / Im from component lc of A_ASL0+D / A_ASR0+D, cell adjoints into slot ts comp tc.
+template <int D, int UMAC>
+static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, double* dir, size_t dir_bytes,
+                          int want_u) {
+    ppm_faces(c, D, fs, sc);
     if (!c.dry) cudaMemsetAsync(dir, 0, dir_bytes, c.stream);
+    const long long eb = dbits_host(c.P.rel_eps);
     const RecipC r6 = make_recip(6.0);
-    launch(c, rg_grow(c, 1), 1, k_adj_ppm_cell<D>, c.V(), fs, comp, eb);
+    launch(c, rg_grow(c, 1), 1, k_adj_ppm_cell<D, UMAC>, c.V(), fs, sc, lc, ts, tc, eb, c.P.dt / c.P.dx[D], want_u);
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, D), 1, k_adj_ppm_face<D>, c.V(), fs, sc, ts, tc, r6);
     int glo[3] = {1, 1, 1};
-    glo[D] = 1;
-    launch(c, region(c, glo[0], glo[1], glo[2], glo[0], glo[1], glo[2], D), 1, k_adj_ppm_face<D>, c.V(), fs, comp, r6);
     glo[D] = 2;
-    launch(c, region(c, glo[0], glo[1], glo[2], glo[0], glo[1], glo[2], -1), 1, k_adj_dsvl<D>, c.V(), fs, comp);
+    launch(c, region(c, glo[0], glo[1], glo[2], glo[0], glo[1], glo[2], -1), 1, k_adj_dsvl<D>, c.V(), fs, sc, ts, tc);
 }
 
 // MakeEdgeScal^T of component comp of field fs (advective form, ppm_type 1): from the
 // edge-state adjoints A_AEDGE0..2 (comp) into A_AS (and A_AFORCE unless force_zero).
-// dir: the storage of A_ASM / A_ASP / A_ADSVL, cleared before each direction.
-void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes) {
+// dir: the storage of A_ASM / A_ASP / A_ADSVL, cleared before each direction.  want_u
+// also accumulates the face-velocity adjoints (A_AUMAC0..2, A_ATCOEF); it needs the
+// forward F_Q / F_SIMH fields of this component.
+void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes, int want_u) {
     const long long eb = dbits_host(c.P.rel_eps);
     const double dt2 = 0.5 * c.P.dt;
-    launch(c, rg_grow(c, 0, 0), 1, k_adj_es_edges<0>, c.V(), comp, force_zero, dt2, eb);
-    launch(c, rg_grow(c, 0, 1), 1, k_adj_es_edges<1>, c.V(), comp, force_zero, dt2, eb);
-    launch(c, rg_grow(c, 0, 2), 1, k_adj_es_edges<2>, c.V(), comp, force_zero, dt2, eb);
-    adj_transverse_launch<0, 1>(c, eb);
-    adj_transverse_launch<0, 2>(c, eb);
-    adj_transverse_launch<1, 0>(c, eb);
-    adj_transverse_launch<1, 2>(c, eb);
-    adj_transverse_launch<2, 0>(c, eb);
-    adj_transverse_launch<2, 1>(c, eb);
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_es_edges<0>, c.V(), comp, force_zero, dt2, eb, want_u);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_es_edges<1>, c.V(), comp, force_zero, dt2, eb, want_u);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_es_edges<2>, c.V(), comp, force_zero, dt2, eb, want_u);
+    adj_transverse_launch<0, 1>(c, eb, want_u);
+    adj_transverse_launch<0, 2>(c, eb, want_u);
+    adj_transverse_launch<1, 0>(c, eb, want_u);
+    adj_transverse_launch<1, 2>(c, eb, want_u);
+    adj_transverse_launch<2, 0>(c, eb, want_u);
+    adj_transverse_launch<2, 1>(c, eb, want_u);
     adj_predictor_launch<0>(c);
     adj_predictor_launch<1>(c);
     adj_predictor_launch<2>(c);
-    adj_ppm_launch<0>(c, fs, comp, eb, dir, dir_bytes);
-    adj_ppm_launch<1>(c, fs, comp, eb, dir, dir_bytes);
-    adj_ppm_launch<2>(c, fs, comp, eb, dir, dir_bytes);
+    adj_ppm_launch<0, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u);
+    adj_ppm_launch<1, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u);
+    adj_ppm_launch<2, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u);
 }
 
-void adj_fill_boundary(Ctx& c, int slot, int ng) {
-    const CopyTable& ct = copy_table(c, ng, -1);
+void adj_fill_boundary(Ctx& c, int slot, int nc, int ng, int nodal) {
+    const CopyTable& ct = copy_table(c, ng, nodal);
     if (ct.total == 0 || c.dry) return;
     unsigned grid = (unsigned)((ct.total + TPB - 1) / TPB);
-    k_adj_fill_boundary<<<grid, TPB, 0, c.stream>>>(ct.d, (int)ct.h.size(), ct.total, c.V(), c.nb, F_USER + slot);
+    k_adj_fill_boundary<<<grid, TPB, 0, c.stream>>>(ct.d, (int)ct.h.size(), ct.total, c.V(), c.nb, F_USER + slot, nc);
     c.launches++;
 }
 
 void adj_convert_x(Ctx& c, int comp) { launch(c, rg_grow(c, 0), 1, k_adj_x, c.V(), comp); }
 
-void adj_pert_force(Ctx& c, int comp) {
-    launch(c, rg_grow(c, 0), 1, k_adj_pert, c.V(), comp, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
-           make_recip(c.P.dx[2]));
+void adj_pert_force(Ctx& c, int comp, int want_u) {
+    const double* s0 = c.b1(comp == RHO ? "rho0_old" : "rhoh0_old");
+    const double* s0e = c.b1(comp == RHO ? "rho0_edge_old" : "rhoh0_edge_old");
+    launch(c, rg_grow(c, 0), 1, k_adj_pert, c.V(), comp, s0, s0e, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
+           make_recip(c.P.dx[2]), c.P.dom_lo[2], c.P.dom_hi[2], want_u);
+}
+
+// F_TCOEF^T into face slots ts .. ts+2 (A_AUMAC0 or A_AUTRANS0)
+void adj_tcoef(Ctx& c, int ts) {
+    const double dt6 = c.P.dt / 6.0, dt4 = 0.25 * c.P.dt;
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, 0), 1, k_adj_tcoef<0>, c.V(), ts, dt6 / c.P.dx[0], dt4 / c.P.dx[0]);
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, 1), 1, k_adj_tcoef<1>, c.V(), ts, dt6 / c.P.dx[1], dt4 / c.P.dx[1]);
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, 2), 1, k_adj_tcoef<2>, c.V(), ts, dt6 / c.P.dx[2], dt4 / c.P.dx[2]);
+}
+
+template <int C, int D>
+static void adj_vp_transverse_launch(Ctx& c, long long eb) {
+    int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
+    glo[C] = 1;
+    ghi[C] = 1;
+    ghi[D] = 1;
+    launch(c, region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1), 1, k_adj_vp_transverse<C, D>, c.V(), eb);
+}
+
+template <int D>
+static void adj_vp_interface_launch(Ctx& c, long long eb) {
+    int glo[3] = {1, 1, 1};
+    glo[D] = 0;
+    launch(c, region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1), 1, k_adj_vp_interface<D>, c.V(), eb);
+}
+
+// VelPred^T then MakeUtrans^T (ppm_type 1): from the MAC-velocity adjoints A_AUMAC0..2
+// (valid faces) into the cell-velocity adjoint A_AUT (3 components, with ghost cells).
+// The forward fields of AdvancePremac (F_UTILDE, F_UFULL, F_TRC, F_IPC / F_IMC, F_UTRANS,
+// F_TCOEF of utrans, F_SL / F_SR / F_SIMH, F_Q) must be current.  A_ATCOEF, A_AUTRANS,
+// A_AUT and the per-direction scratch must be zero.
+void adj_vel_pred(Ctx& c, double* dir, size_t dir_bytes) {
+    const long long eb = dbits_host(c.P.rel_eps);
+    const double dt2 = 0.5 * c.P.dt, re = c.P.rel_eps;
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_vp_velocities<0>, c.V(), dt2, re);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_vp_velocities<1>, c.V(), dt2, re);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_vp_velocities<2>, c.V(), dt2, re);
+    adj_vp_transverse_launch<0, 1>(c, eb);
+    adj_vp_transverse_launch<0, 2>(c, eb);
+    adj_vp_transverse_launch<1, 0>(c, eb);
+    adj_vp_transverse_launch<1, 2>(c, eb);
+    adj_vp_transverse_launch<2, 0>(c, eb);
+    adj_vp_transverse_launch<2, 1>(c, eb);
+    adj_tcoef(c, A_AUTRANS0);
+    for (int d = 0; d < 3; ++d) adj_fill_boundary(c, A_AUTRANS0 + d, 1, 1, d);
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_utrans<0>, c.V(), re);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_utrans<1>, c.V(), re);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_utrans<2>, c.V(), re);
+    adj_vp_interface_launch<0>(c, eb);
+    adj_vp_interface_launch<1>(c, eb);
+    adj_vp_interface_launch<2>(c, eb);
+    for (int cc = 0; cc < 3; ++cc) {
+        adj_ppm_launch<0, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1);
+        adj_ppm_launch<1, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1);
+        adj_ppm_launch<2, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1);
+    }
 }
 
 long adj_dot_parts(Ctx& c) { return (rg_grow(c, 0).total + TPB - 1) / TPB; }

@@ -1488,7 +1488,8 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     const int ns = c.nscal, K = sd->ckpt_interval, N = sd->nsteps;
     const int nck = (N + K - 1) / K;
     const int last0 = (nck - 1) * K;  // first step of the last block
-    const bool rev = res->grad_s != nullptr;
+    const bool want_u = res->grad_u != nullptr;
+    const bool rev = res->grad_s != nullptr || want_u;
     const cudaMemcpyKind DD = cudaMemcpyDeviceToDevice;
     AdjWork W;
     const size_t st_b = fab_doubles(c, ns, 0, -1) * sizeof(double);
@@ -1503,12 +1504,13 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     std::vector<StageIO> ios{io};
     if ((rc = bind_stage(c, io))) return rc;
     if ((rc = bind(c, A_SOLD0, sd->sold0, ns, -1, 0)) || (rc = bind(c, A_WEIGHT, sd->weight, ns, -1, 0)) ||
-        (rc = bind(c, A_SFIN, res->sfinal, ns, -1, 0)) || (rc = bind(c, A_GRADS, res->grad_s, ns, -1, 0)))
+        (rc = bind(c, A_SFIN, res->sfinal, ns, -1, 0)) || (rc = bind(c, A_GRADS, res->grad_s, ns, -1, 0)) ||
+        (rc = bind(c, A_GRADU, res->grad_u, 3, -1, 0)))
         return rc;
     std::vector<double*> ck, bst;
     std::vector<std::array<double*, 3>> bed;
-    double *asold = nullptr, *scr = nullptr, *dir = nullptr;
-    size_t scr_b = 0, dir_b = 0;
+    double *asold = nullptr, *scr = nullptr, *dir = nullptr, *atc = nullptr;
+    size_t scr_b = 0, dir_b = 0, atc_b = 0;
     if (rev) {
         for (int j = 0; j < nck; ++j) ck.push_back(W.alloc(st_b));
         for (int j = 0; j < std::min(K, N); ++j) {
@@ -1521,17 +1523,30 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         bind_raw(c, A_ASOLD, asold, ns, 0, -1);
         bind_raw(c, A_ASNEW, W.alloc(st_b), ns, 0, -1);
         for (int d = 0; d < 3; ++d) bind_raw(c, A_AEDGE0 + d, W.alloc(fab_doubles(c, ns, 0, d) * 8), ns, 0, d);
-        // per-component scratch in one block: A_AS, A_AFORCE, A_ASL0 .. A_AQ21
+        // per-component scratch in one block: A_AS, A_AFORCE, A_ASL0 .. A_ASIMH2 (three
+        // components, for the velocity transpose), A_AQ01 .. A_AQ21
         const size_t n_as = fab_doubles(c, 1, c.ng_s, -1), n_f = fab_doubles(c, 1, 1, -1),
                      n_2 = fab_doubles(c, 1, 2, -1);
-        scr_b = (n_as + n_f + 15 * n_2) * sizeof(double);
+        scr_b = (n_as + n_f + 33 * n_2) * sizeof(double);
         scr = W.alloc(scr_b);
         bind_raw(c, A_AS, scr, 1, c.ng_s, -1);
         bind_raw(c, A_AFORCE, scr + n_as, 1, 1, -1);
-        for (int s = A_ASL0; s <= A_AQ21; ++s) bind_raw(c, s, scr + n_as + n_f + (size_t)(s - A_ASL0) * n_2, 1, 2, -1);
+        double* p = scr + n_as + n_f;
+        for (int s = A_ASL0; s <= A_ASIMH2; ++s, p += 3 * n_2) bind_raw(c, s, p, 3, 2, -1);
+        for (int s = A_AQ01; s <= A_AQ21; ++s, p += n_2) bind_raw(c, s, p, 1, 2, -1);
         dir_b = 3 * n_2 * sizeof(double);
         dir = W.alloc(dir_b);
         for (int s = A_ASM; s <= A_ADSVL; ++s) bind_raw(c, s, dir + (size_t)(s - A_ASM) * n_2, 1, 2, -1);
+        if (want_u) {
+            for (int d = 0; d < 3; ++d) {
+                bind_raw(c, A_AUMAC0 + d, W.alloc(fab_doubles(c, 1, 1, d) * 8), 1, 1, d);
+                bind_raw(c, A_AUTRANS0 + d, W.alloc(fab_doubles(c, 1, 1, d) * 8), 1, 1, d);
+            }
+            atc_b = fab_doubles(c, 6, 2, -1) * 8;
+            atc = W.alloc(atc_b);
+            bind_raw(c, A_ATCOEF, atc, 6, 2, -1);
+            bind_raw(c, A_AUT, W.alloc(fab_doubles(c, 3, c.ng_adv, -1) * 8), 3, c.ng_adv, -1);
+        }
     }
     double* dJ = W.alloc(sizeof(double));
     double* dpart = W.alloc(sizeof(double) * (size_t)adj_dot_parts(c));
@@ -1558,17 +1573,19 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
         edge_scal_coeffs(c);
         adj_update(c);
-        adj_flux(c, c.b1("rho0_old"), c.b1("rho0_edge_old"));
+        adj_flux(c, want_u);
         for (int comp = 0; comp < ns; ++comp) {
             if (comp == TEMP || comp == PI) continue;
+            // the velocity adjoint needs this component's transverse states (F_Q, F_SIMH)
+            if (want_u) make_edge_scal(c, comp, 1, BCS_S, 0, comp >= FIRSTSPEC);
             cudaMemsetAsync(scr, 0, scr_b, c.stream);
-            adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b);
-            adj_fill_boundary(c, A_AS, c.ng_s);
+            adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b, want_u);
+            adj_fill_boundary(c, A_AS, 1, c.ng_s, -1);
             if (comp >= FIRSTSPEC) {
                 adj_convert_x(c, comp);
             } else {
-                adj_fill_boundary(c, A_AFORCE, 1);
-                adj_pert_force(c, comp);
+                adj_fill_boundary(c, A_AFORCE, 1, 1, -1);
+                adj_pert_force(c, comp, want_u);
             }
         }
         copy_fab(c, F_USER + A_ASNEW, 0, F_USER + A_ASOLD, 0, ns, 0);
@@ -1603,7 +1620,24 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
                 rev_step();
             }
         }
-        copy_fab(c, F_USER + A_GRADS, 0, F_USER + A_ASNEW, 0, ns, 0);
+        if (res->grad_s) copy_fab(c, F_USER + A_GRADS, 0, F_USER + A_ASNEW, 0, ns, 0);
+        if (want_u) {
+            // MAC-velocity adjoint of every step: the transverse coefficients, then the
+            // ghost faces back to the valid faces they were copied from
+            adj_tcoef(c, A_AUMAC0);
+            for (int d = 0; d < 3; ++d) adj_fill_boundary(c, A_AUMAC0 + d, 1, 1, d);
+            // AdvancePremac's fields (identical in every step), then its transpose
+            copy_fab(c, F_SOLD, 0, F_USER + A_WSOLD, 0, ns, 0);
+            fill_patch_h(H, F_SOLD, 0, ns, BCS_S, 0, 0, 0);
+            set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
+            copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, 0);
+            advance_premac(H);
+            CK(cudaMemsetAsync(atc, 0, atc_b, c.stream));
+            CK(cudaMemsetAsync(scr, 0, scr_b, c.stream));
+            adj_vel_pred(c, dir, dir_b);
+            adj_fill_boundary(c, A_AUT, 3, c.ng_adv, -1);
+            copy_fab(c, F_USER + A_GRADU, 0, F_USER + A_AUT, 0, 3, 0);
+        }
     }
     double Jh = 0.0;
     CK(cudaMemcpyAsync(&Jh, dJ, sizeof(double), cudaMemcpyDeviceToHost, c.stream));

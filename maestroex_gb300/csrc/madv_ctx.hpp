@@ -220,17 +220,20 @@ enum {
     A_AQ01, A_AQ02, A_AQ10, A_AQ12, A_AQ20, A_AQ21,
     A_ASM, A_ASP, A_ADSVL,
     A_WEIGHT, A_SOLD0, A_GRADS, A_SFIN,
+    A_AUMAC0, A_AUMAC1, A_AUMAC2, A_ATCOEF, A_AUTRANS0, A_AUTRANS1, A_AUTRANS2, A_AUT, A_GRADU,
     A_END
 };
 static_assert(A_END <= N_USER_SLOTS, "user slots");
 void ppm_faces(Ctx& c, int d, int fs, int sc);  // van Leer slopes + interface values (madv_kernels.cu)
 void edge_scal_coeffs(Ctx& c);                  // tracing / transverse coefficients of F_UMAC0..2
 void adj_update(Ctx& c);
-void adj_flux(Ctx& c, const double* r0, const double* r0e);
-void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes);
-void adj_fill_boundary(Ctx& c, int slot, int ng);
+void adj_flux(Ctx& c, int want_u);
+void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes, int want_u);
+void adj_fill_boundary(Ctx& c, int slot, int nc, int ng, int nodal);
 void adj_convert_x(Ctx& c, int comp);
-void adj_pert_force(Ctx& c, int comp);
+void adj_pert_force(Ctx& c, int comp, int want_u);
+void adj_tcoef(Ctx& c, int ts);
+void adj_vel_pred(Ctx& c, double* dir, size_t dir_bytes);
 long adj_dot_parts(Ctx& c);
 void adj_dot(Ctx& c, int slot_a, int slot_b, int nc, double* part, double* d_out);
 

@@ -225,16 +225,18 @@ class ScalarAdvectionStage:
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
 
-    def stage_adjoint(self, uold, sold0, weight, nsteps, ckpt_interval, grad_s=None, sfinal=None, stream=None):
+    def stage_adjoint(self, uold, sold0, weight, nsteps, ckpt_interval, grad_s=None, sfinal=None, grad_u=None,
+                      stream=None):
         """madv_stage_adjoint: nsteps fixed-velocity steps from sold0, J = <weight, s_nsteps>,
-        dJ/dsold0 into grad_s (None: forward only) and s_nsteps into sfinal.
-        Returns (J, device bytes the call allocated)."""
+        dJ/dsold0 into grad_s, dJ/duold into grad_u (both None: forward only) and s_nsteps
+        into sfinal.  Returns (J, device bytes the call allocated)."""
         P = C.POINTER(capi.MadvMultiFab)
         seed = capi.MadvAdjSeed(int(nsteps), int(ckpt_interval), C.pointer(uold.desc()), C.pointer(sold0.desc()),
                                 C.pointer(weight.desc()))
         res = capi.MadvAdjResult()
         res.sfinal = C.pointer(sfinal.desc()) if sfinal is not None else P()
         res.grad_s = C.pointer(grad_s.desc()) if grad_s is not None else P()
+        res.grad_u = C.pointer(grad_u.desc()) if grad_u is not None else P()
         s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
         check(lib().madv_stage_adjoint(self.ctx, C.byref(seed), C.byref(res), C.c_void_p(s)))
         return res.J, res.device_bytes
