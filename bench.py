@@ -259,6 +259,158 @@ def run_amr(args, ws, steps, warmup, barrier):
     }
 
 
+def run_adjoint(args, barrier):
+    """Multi-step adjoint workload: 128^3 in 8 boxes of 64^3, NumSpec 3, ppm_type 1, 16 steps
+    at CFL 0.5 with the velocity held fixed, J = sum(w rhoX + v rhoh) with w, v ~ N(0, 1),
+    stored states every 4 steps.  Times the forward alone, the adjoint for dJ/d(state) and
+    the adjoint for dJ/d(state, velocity) (each call runs its own forward), and checks a
+    few gradient entries against central differences (h = 1e-6 max(|x|, rms/10)) of the
+    same forward."""
+    import torch
+    from maestroex_gb300 import configs
+    from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
+    from maestroex_gb300.stage import MultiFab, make_stage
+    n, nsteps, ckpt = args.adj_n, 16, 4
+    cfg = configs.adjoint_config(n=(n, n, n), max_grid=min(64, n), nspec=3)
+    st = make_stage(cfg)
+    boxes, nscal = cfg["boxes"], 4 + cfg["nspec"]
+    u = MultiFab(boxes, 3, 0).from_domain(cfg["uold"])
+    s0 = MultiFab(boxes, nscal, 0).from_domain(cfg["sold"])
+    rng = np.random.default_rng(20261203 + 40)
+    w = np.zeros_like(cfg["sold"])
+    w[RHOH] = rng.normal(size=w[RHOH].shape)
+    w[FIRSTSPEC:] = rng.normal(size=w[FIRSTSPEC:].shape)
+    wt = MultiFab(boxes, nscal, 0).from_domain(w)
+    gs, gu, sf = MultiFab(boxes, nscal, 0), MultiFab(boxes, 3, 0), MultiFab(boxes, nscal, 0)
+
+    def call(kind, uu=None, ss=None):
+        return st.stage_adjoint(u if uu is None else uu, s0 if ss is None else ss, wt, nsteps, ckpt,
+                                grad_s=gs if kind != "fwd" else None, grad_u=gu if kind == "full" else None,
+                                sfinal=sf)
+
+    def timed(kind, reps):
+        call(kind)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record()
+            J, nbytes = call(kind)
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps, J, nbytes
+
+    reps = max(1, args.steps // 2)
+    ms_fwd, J, _ = timed("fwd", reps)
+    ms_state, _, bytes_state = timed("state", reps)
+    ms_full, J_full, bytes_full = timed("full", reps)
+    call("full")
+    G = gs.to_domain(cfg["n"]).cpu().numpy()
+    GU = gu.to_domain(cfg["n"]).cpu().numpy()
+    S, U = cfg["sold"], cfg["uold"]
+
+    def perturbed(src, comp, cell, h):
+        m = MultiFab(boxes, src.ncomp, 0)
+        for a, b in zip(m.fabs, src.fabs):
+            a.copy_(b)
+        i, j, k = cell
+        for bi, bx in enumerate(boxes):
+            if bx[0] <= i <= bx[3] and bx[1] <= j <= bx[4] and bx[2] <= k <= bx[5]:
+                m.fabs[bi][comp, k - bx[2], j - bx[1], i - bx[0]] += h
+        return m
+
+    def final(uu, ss):
+        out = MultiFab(boxes, nscal, 0)
+        st.stage_adjoint(uu, ss, wt, nsteps, ckpt, sfinal=out)
+        return out
+
+    def dJ(a, b):
+        return sum(float((x * (p - q)).sum()) for x, p, q in zip(wt.fabs, a.fabs, b.fabs))
+
+    checks, worst, kinks = [], 0.0, 0
+    rms_s = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
+    rms_u = np.sqrt((U ** 2).mean(axis=(1, 2, 3)))
+    for t, (field, comp) in enumerate([("s", RHOH), ("s", FIRSTSPEC), ("s", FIRSTSPEC + 2), ("s", RHO),
+                                       ("u", 0), ("u", 1), ("u", 2), ("u", 2)]):
+        cell = tuple(int(v) for v in rng.integers(0, n, size=3))
+        i, j, k = cell
+        X, R, G_ = (S, rms_s, G) if field == "s" else (U, rms_u, GU)
+        x = max(abs(X[comp, k, j, i]), 0.1 * R[comp])
+        fd = []
+        for rel in (1e-6, 0.5e-6):
+            h = rel * x
+            if field == "s":
+                a, b = final(u, perturbed(s0, comp, cell, h)), final(u, perturbed(s0, comp, cell, -h))
+            else:
+                a, b = final(perturbed(u, comp, cell, h), s0), final(perturbed(u, comp, cell, -h), s0)
+            fd.append(dJ(a, b) / (2 * h))
+        scale = max(abs(fd[0]), abs(fd[1]))
+        if abs(fd[0] - fd[1]) > 1e-5 * scale:
+            kinks += 1
+            continue
+        err = abs(G_[comp, k, j, i] - fd[0]) / max(scale, 1e-300)
+        worst = max(worst, err)
+        checks.append(err)
+    st.close()
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"3-D single level {n}^3 in {len(boxes)} boxes of {min(64, n)}^3, NumSpec 3, ppm_type 1, "
+                    f"periodic, {nsteps} steps at CFL 0.5 with the velocity held fixed, stored states every {ckpt} "
+                    "steps; J = sum(w rhoX + v rhoh_final), w, v ~ N(0,1)",
+        "fwd_ms": ms_fwd, "adj_state_ms": ms_state, "adj_state_velocity_ms": ms_full,
+        "adj_over_fwd_state": ms_state / ms_fwd, "adj_over_fwd_state_velocity": ms_full / ms_fwd,
+        "device_bytes_state": bytes_state, "device_bytes_state_velocity": bytes_full,
+        "J": J_full,
+        "fd_check": {"entries": len(checks), "skipped_limiter_switch": kinks, "worst_rel_err": worst,
+                     "h": "1e-6 max(|x|, rms/10); entries whose h and h/2 differences disagree by more than 1e-5 "
+                           "(a limiter switch inside [x - h, x + h]) are skipped"},
+    }
+
+
+def run_2d(args, barrier):
+    """2-D workload: one 256 x 256 box, NumSpec 3, ppm_type 1 (the reference's 2-D build),
+    graph-replayed stage."""
+    import torch
+    from maestroex_gb300 import capi, configs
+    from maestroex_gb300.stage import StageBuffers, make_stage
+    cfg = configs.config_c1(n=256)
+    st = make_stage(cfg)
+    buf = StageBuffers(cfg).load(cfg)
+    snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
+
+    def step():
+        for name, ts in snap.items():
+            for dst, src in zip(getattr(buf, name).fabs, ts):
+                dst.copy_(src)
+        st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                         thermal=buf.thermal, mode=capi.MODE_GRAPH)
+
+    for _ in range(3):
+        step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tot, reps = 0.0, max(3, args.steps)
+    for _ in range(reps):
+        for name, ts in snap.items():
+            for dst, src in zip(getattr(buf, name).fabs, ts):
+                dst.copy_(src)
+        torch.cuda.synchronize()
+        e0.record()
+        st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                         thermal=buf.thermal, mode=capi.MODE_GRAPH)
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    ms = tot / reps
+    launches = st.launch_count()
+    st.close()
+    return {"workload": "2-D single level 256 x 256 (one box), NumSpec 3, ppm_type 1, x periodic, "
+                        "y slipwall / outflow", "value": 256 * 256 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+            "gpu_launches": launches}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -272,6 +424,9 @@ def main():
     ap.add_argument("--no-per-box", action="store_true")
     ap.add_argument("--amr-n", type=int, default=256, help="level-0 extent of the two-level AMR workload")
     ap.add_argument("--no-amr", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=128, help="extent of the multi-step adjoint workload")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-2d", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
     args = ap.parse_args()
@@ -409,6 +564,8 @@ def main():
         del st, buf, snap
         torch.cuda.empty_cache()
         amr = run_amr(args, ws, max(1, args.steps // 2), warmup, barrier)
+    adj = None if args.no_adjoint else run_adjoint(args, barrier)
+    two_d = None if args.no_2d else run_2d(args, barrier)
 
     if rank != 0:
         dist.destroy_process_group()
@@ -445,6 +602,10 @@ def main():
     }
     if amr is not None:
         line["amr"] = amr
+    if adj is not None:
+        line["adjoint"] = adj
+    if two_d is not None:
+        line["two_d"] = two_d
     if not args.no_cpu_baseline:
         cb = run_cpu_baseline(1, 0)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -1548,6 +1548,28 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
             bind_raw(c, A_AUT, W.alloc(fab_doubles(c, 3, c.ng_adv, -1) * 8), 3, c.ng_adv, -1);
         }
     }
+    // with the velocity gradient: the transverse states of every traced component of the
+    // block's steps (F_Q01..F_Q21, F_SIMH0..2), kept as the forward forms them
+    static const int TAPE_F[9] = {F_Q01, F_Q02, F_Q10, F_Q12, F_Q20, F_Q21, F_SIMH0, F_SIMH1, F_SIMH2};
+    std::vector<std::vector<std::array<double*, 9>>> tape;
+    if (want_u) {
+        tape.resize(std::min(K, N));
+        for (auto& t : tape) {
+            t.resize(ns);
+            for (int comp = 0; comp < ns; ++comp) {
+                if (comp == TEMP || comp == PI) continue;
+                for (int f = 0; f < 9; ++f) t[comp][f] = W.alloc(c.F[TAPE_F[f]].bytes);
+            }
+        }
+    }
+    auto tape_on = [&](int slot) {
+        if (!want_u) return;
+        c.edge_tape = [&, slot](int comp) {
+            for (int f = 0; f < 9; ++f)
+                cudaMemcpyAsync(tape[slot][comp][f], c.F[TAPE_F[f]].base, c.F[TAPE_F[f]].bytes, DD, c.stream);
+        };
+    };
+    auto tape_off = [&]() { c.edge_tape = nullptr; };
     double* dJ = W.alloc(sizeof(double));
     double* dpart = W.alloc(sizeof(double) * (size_t)adj_dot_parts(c));
     if ((rc = upload_user_views(c))) return rc;
@@ -1564,7 +1586,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         for (int d = 0; d < 3; ++d)
             cudaMemcpyAsync(bed[slot][d], c.F[F_SEDGE0 + d].base, c.F[F_SEDGE0 + d].bytes, DD, c.stream);
     };
-    auto rev_step = [&]() {
+    auto rev_step = [&](int slot) {
         // the step's traced fields (X, rho', rhoh') as the forward formed them
         copy_fab(c, F_SOLD, 0, F_USER + A_WSOLD, 0, ns, 0);
         fill_patch_h(H, F_SOLD, 0, ns, BCS_S, 0, 0, 0);
@@ -1577,7 +1599,9 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         for (int comp = 0; comp < ns; ++comp) {
             if (comp == TEMP || comp == PI) continue;
             // the velocity adjoint needs this component's transverse states (F_Q, F_SIMH)
-            if (want_u) make_edge_scal(c, comp, 1, BCS_S, 0, comp >= FIRSTSPEC);
+            if (want_u)
+                for (int f = 0; f < 9; ++f)
+                    cudaMemcpyAsync(c.F[TAPE_F[f]].base, tape[slot][comp][f], c.F[TAPE_F[f]].bytes, DD, c.stream);
             cudaMemsetAsync(scr, 0, scr_b, c.stream);
             adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b, want_u);
             adj_fill_boundary(c, A_AS, 1, c.ng_s, -1);
@@ -1595,8 +1619,12 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     copy_fab(c, F_USER + A_WSOLD, 0, F_USER + A_SOLD0, 0, ns, 0);
     for (int n = 0; n < N; ++n) {
         if (rev && n % K == 0) CK(cudaMemcpyAsync(ck[n / K], wsold, st_b, DD, c.stream));
-        if (rev && n >= last0) keep_step(n - last0);
+        if (rev && n >= last0) {
+            keep_step(n - last0);
+            tape_on(n - last0);
+        }
         fwd_step();
+        tape_off();
         if (rev && n >= last0) keep_edges(n - last0);
     }
     adj_dot(c, A_WEIGHT, A_WSOLD, ns, dpart, dJ);
@@ -1609,7 +1637,9 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
                 CK(cudaMemcpyAsync(wsold, ck[bk], st_b, DD, c.stream));
                 for (int n = n0; n < n1; ++n) {
                     keep_step(n - n0);
+                    tape_on(n - n0);
                     fwd_step();
+                    tape_off();
                     keep_edges(n - n0);
                 }
             }
@@ -1617,7 +1647,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
                 CK(cudaMemcpyAsync(wsold, bst[n - n0], st_b, DD, c.stream));
                 for (int d = 0; d < 3; ++d)
                     CK(cudaMemcpyAsync(c.F[F_SEDGE0 + d].base, bed[n - n0][d], c.F[F_SEDGE0 + d].bytes, DD, c.stream));
-                rev_step();
+                rev_step(n - n0);
             }
         }
         if (res->grad_s) copy_fab(c, F_USER + A_GRADS, 0, F_USER + A_ASNEW, 0, ns, 0);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -123,6 +124,9 @@ struct Ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<const void*> graph_key;
     long graph_launches = 0;
+    // called after each component of MakeEdgeScal (3-D): the adjoint keeps that
+    // component's transverse states (F_Q*, F_SIMH*) for its reverse sweep
+    std::function<void(int)> edge_tape;
     // scratch of the single-box entry points (madv_ppm), grown on demand
     double* box_scratch = nullptr;
     long box_scratch_n = 0;

@@ -1091,6 +1091,7 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
         es_edges_launch<0>(c, comp, bc, is_cons, force_zero);
         es_edges_launch<1>(c, comp, bc, is_cons, force_zero);
         es_edges_launch<2>(c, comp, bc, is_cons, force_zero);
+        if (c.edge_tape) c.edge_tape(comp);
     }
 }
 
