@@ -637,10 +637,11 @@ static void adj_predictor_launch(Ctx& c) {
 
 // PPM^T of component sc of field fs along D (ppm_type 1, interior form): adjoints of
 // Ip / Im from component lc of A_ASL0+D / A_ASR0+D, cell adjoints into slot ts comp tc.
+// faces: recompute the interface values F_FACE0+D (0: they hold the forward's already).
 template <int D, int UMAC>
 static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, double* dir, size_t dir_bytes,
-                          int want_u) {
-    ppm_faces(c, D, fs, sc);
+                          int want_u, int faces) {
+    ppm_faces(c, D, fs, sc, faces);
     if (!c.dry) cudaMemsetAsync(dir, 0, dir_bytes, c.stream);
     const long long eb = dbits_host(c.P.rel_eps);
     const RecipC r6 = make_recip(6.0);
@@ -655,7 +656,8 @@ static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, doubl
 // edge-state adjoints A_AEDGE0..2 (comp) into A_AS (and A_AFORCE unless force_zero).
 // dir: the storage of A_ASM / A_ASP / A_ADSVL, cleared before each direction.  want_u
 // also accumulates the face-velocity adjoints (A_AUMAC0..2, A_ATCOEF); it needs the
-// forward F_Q / F_SIMH fields of this component.
+// forward F_Q / F_SIMH fields of this component.  F_FACE0..2 must hold this component's
+// forward interface values.
 void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes, int want_u) {
     const long long eb = dbits_host(c.P.rel_eps);
     const double dt2 = 0.5 * c.P.dt;
@@ -671,9 +673,9 @@ void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t
     adj_predictor_launch<0>(c);
     adj_predictor_launch<1>(c);
     adj_predictor_launch<2>(c);
-    adj_ppm_launch<0, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u);
-    adj_ppm_launch<1, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u);
-    adj_ppm_launch<2, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u);
+    adj_ppm_launch<0, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
+    adj_ppm_launch<1, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
+    adj_ppm_launch<2, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
 }
 
 void adj_fill_boundary(Ctx& c, int slot, int nc, int ng, int nodal) {
@@ -743,9 +745,9 @@ void adj_vel_pred(Ctx& c, double* dir, size_t dir_bytes) {
     adj_vp_interface_launch<1>(c, eb);
     adj_vp_interface_launch<2>(c, eb);
     for (int cc = 0; cc < 3; ++cc) {
-        adj_ppm_launch<0, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1);
-        adj_ppm_launch<1, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1);
-        adj_ppm_launch<2, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1);
+        adj_ppm_launch<0, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1);
+        adj_ppm_launch<1, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1);
+        adj_ppm_launch<2, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1);
     }
 }
 

@@ -1510,7 +1510,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     std::vector<double*> ck, bst;
     std::vector<std::array<double*, 3>> bed;
     double *asold = nullptr, *scr = nullptr, *dir = nullptr, *atc = nullptr;
-    size_t scr_b = 0, dir_b = 0, atc_b = 0;
+    size_t scr_b = 0, dir_b = 0, atc_b = 0, n_2 = 0;
     if (rev) {
         for (int j = 0; j < nck; ++j) ck.push_back(W.alloc(st_b));
         for (int j = 0; j < std::min(K, N); ++j) {
@@ -1523,17 +1523,17 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         bind_raw(c, A_ASOLD, asold, ns, 0, -1);
         bind_raw(c, A_ASNEW, W.alloc(st_b), ns, 0, -1);
         for (int d = 0; d < 3; ++d) bind_raw(c, A_AEDGE0 + d, W.alloc(fab_doubles(c, ns, 0, d) * 8), ns, 0, d);
-        // per-component scratch in one block: A_AS, A_AFORCE, A_ASL0 .. A_ASIMH2 (three
-        // components, for the velocity transpose), A_AQ01 .. A_AQ21
-        const size_t n_as = fab_doubles(c, 1, c.ng_s, -1), n_f = fab_doubles(c, 1, 1, -1),
-                     n_2 = fab_doubles(c, 1, 2, -1);
-        scr_b = (n_as + n_f + 33 * n_2) * sizeof(double);
+        // per-component scratch in one block, cleared per component: A_AS, A_AFORCE,
+        // A_ASL0 .. A_ASIMH2, A_AQ01 .. A_AQ21 (one component each; the velocity transpose
+        // rebinds A_ASL0 .. A_ASIMH2 to three-component storage)
+        const size_t n_as = fab_doubles(c, 1, c.ng_s, -1), n_f = fab_doubles(c, 1, 1, -1);
+        n_2 = fab_doubles(c, 1, 2, -1);
+        scr_b = (n_as + n_f + 15 * n_2) * sizeof(double);
         scr = W.alloc(scr_b);
         bind_raw(c, A_AS, scr, 1, c.ng_s, -1);
         bind_raw(c, A_AFORCE, scr + n_as, 1, 1, -1);
         double* p = scr + n_as + n_f;
-        for (int s = A_ASL0; s <= A_ASIMH2; ++s, p += 3 * n_2) bind_raw(c, s, p, 3, 2, -1);
-        for (int s = A_AQ01; s <= A_AQ21; ++s, p += n_2) bind_raw(c, s, p, 1, 2, -1);
+        for (int s = A_ASL0; s <= A_AQ21; ++s, p += n_2) bind_raw(c, s, p, 1, 2, -1);
         dir_b = 3 * n_2 * sizeof(double);
         dir = W.alloc(dir_b);
         for (int s = A_ASM; s <= A_ADSVL; ++s) bind_raw(c, s, dir + (size_t)(s - A_ASM) * n_2, 1, 2, -1);
@@ -1548,31 +1548,69 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
             bind_raw(c, A_AUT, W.alloc(fab_doubles(c, 3, c.ng_adv, -1) * 8), 3, c.ng_adv, -1);
         }
     }
-    // with the velocity gradient: the transverse states of every traced component of the
-    // block's steps (F_Q01..F_Q21, F_SIMH0..2), kept as the forward forms them
-    static const int TAPE_F[9] = {F_Q01, F_Q02, F_Q10, F_Q12, F_Q20, F_Q21, F_SIMH0, F_SIMH1, F_SIMH2};
-    std::vector<std::vector<std::array<double*, 9>>> tape;
-    if (want_u) {
+    // the forward's PPM interface values of every traced component of the block's steps
+    // (F_FACE0..2) and, with the velocity gradient, its transverse states (F_Q01..F_Q21,
+    // F_SIMH0..2), kept as the forward forms them
+    static const int TAPE_F[12] = {F_FACE0, F_FACE1, F_FACE2, F_Q01, F_Q02, F_Q10,
+                                   F_Q12,   F_Q20,   F_Q21,   F_SIMH0, F_SIMH1, F_SIMH2};
+    const int ntape = want_u ? 12 : 3;
+    std::vector<std::vector<std::array<double*, 12>>> tape;
+    if (rev) {
         tape.resize(std::min(K, N));
         for (auto& t : tape) {
             t.resize(ns);
             for (int comp = 0; comp < ns; ++comp) {
                 if (comp == TEMP || comp == PI) continue;
-                for (int f = 0; f < 9; ++f) t[comp][f] = W.alloc(c.F[TAPE_F[f]].bytes);
+                for (int f = 0; f < ntape; ++f) t[comp][f] = W.alloc(c.F[TAPE_F[f]].bytes);
             }
         }
     }
+    // Device view tables, one per (block step, component): the level's table with the taped
+    // fields pointing at that step's and component's storage (same layout as the field).
+    // Kernels take the table at launch, so the forward writes the taped fields straight
+    // into the tape and the reverse reads them from there: nothing is copied.
+    FabView* const base_views = c.dviews;
+    struct ViewsGuard {
+        Ctx& c;
+        FabView* v;
+        ~ViewsGuard() {
+            c.dviews = v;
+            c.edge_tape_begin = nullptr;
+            c.edge_tape = nullptr;
+        }
+    } views_guard{c, base_views};
+    std::vector<std::vector<FabView*>> vt(tape.size(), std::vector<FabView*>(ns, nullptr));
     auto tape_on = [&](int slot) {
-        if (!want_u) return;
-        c.edge_tape = [&, slot](int comp) {
-            for (int f = 0; f < 9; ++f)
-                cudaMemcpyAsync(tape[slot][comp][f], c.F[TAPE_F[f]].base, c.F[TAPE_F[f]].bytes, DD, c.stream);
-        };
+        if (!rev) return;
+        c.edge_tape_begin = [&, slot](int comp) { c.dviews = vt[slot][comp]; };
+        c.edge_tape = [&](int) { c.dviews = base_views; };
     };
-    auto tape_off = [&]() { c.edge_tape = nullptr; };
+    auto tape_off = [&]() {
+        c.edge_tape_begin = nullptr;
+        c.edge_tape = nullptr;
+    };
     double* dJ = W.alloc(sizeof(double));
     double* dpart = W.alloc(sizeof(double) * (size_t)adj_dot_parts(c));
     if ((rc = upload_user_views(c))) return rc;
+    if (rev) {
+        const size_t nv = (size_t)NF_TOTAL * c.nb;
+        std::vector<FabView> h(nv);
+        for (size_t sl = 0; sl < tape.size(); ++sl)
+            for (int comp = 0; comp < ns; ++comp) {
+                if (comp == TEMP || comp == PI) continue;
+                std::memcpy(h.data(), c.hviews_pinned, nv * sizeof(FabView));
+                for (int f = 0; f < ntape; ++f) {
+                    const int fid = TAPE_F[f];
+                    for (int b = 0; b < c.nb; ++b) {
+                        FabView& v = h[(size_t)fid * c.nb + b];
+                        v.p = tape[sl][comp][f] + (v.p - c.F[fid].base);
+                    }
+                }
+                FabView* d = reinterpret_cast<FabView*>(W.alloc(nv * sizeof(FabView)));
+                CK(cudaMemcpy(d, h.data(), nv * sizeof(FabView), cudaMemcpyHostToDevice));
+                vt[sl][comp] = d;
+            }
+    }
 
     auto fwd_step = [&]() {
         stage_body(H, ios);
@@ -1598,12 +1636,12 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         adj_flux(c, want_u);
         for (int comp = 0; comp < ns; ++comp) {
             if (comp == TEMP || comp == PI) continue;
-            // the velocity adjoint needs this component's transverse states (F_Q, F_SIMH)
-            if (want_u)
-                for (int f = 0; f < 9; ++f)
-                    cudaMemcpyAsync(c.F[TAPE_F[f]].base, tape[slot][comp][f], c.F[TAPE_F[f]].bytes, DD, c.stream);
             cudaMemsetAsync(scr, 0, scr_b, c.stream);
+            // this component's interface values (and for the velocity adjoint its
+            // transverse states) as the forward formed them, read from the tape
+            c.dviews = vt[slot][comp];
             adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b, want_u);
+            c.dviews = base_views;
             adj_fill_boundary(c, A_AS, 1, c.ng_s, -1);
             if (comp >= FIRSTSPEC) {
                 adj_convert_x(c, comp);
@@ -1664,6 +1702,11 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
             advance_premac(H);
             CK(cudaMemsetAsync(atc, 0, atc_b, c.stream));
             CK(cudaMemsetAsync(scr, 0, scr_b, c.stream));
+            // three-component predictor / transverse adjoints of the velocity
+            double* vs = W.alloc(27 * n_2 * sizeof(double));
+            CK(cudaStreamSynchronize(c.stream));  // no launch in flight reads the views
+            for (int s = A_ASL0; s <= A_ASIMH2; ++s) bind_raw(c, s, vs + (size_t)(s - A_ASL0) * 3 * n_2, 3, 2, -1);
+            if ((rc = upload_user_views(c))) return rc;
             adj_vel_pred(c, dir, dir_b);
             adj_fill_boundary(c, A_AUT, 3, c.ng_adv, -1);
             copy_fab(c, F_USER + A_GRADU, 0, F_USER + A_AUT, 0, 3, 0);

@@ -124,9 +124,10 @@ struct Ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<const void*> graph_key;
     long graph_launches = 0;
-    // called after each component of MakeEdgeScal (3-D): the adjoint keeps that
-    // component's transverse states (F_Q*, F_SIMH*) for its reverse sweep
-    std::function<void(int)> edge_tape;
+    // called before / after each component of MakeEdgeScal (3-D): the adjoint points the
+    // component's PPM and transverse scratch (F_FACE*, F_Q*, F_SIMH*) at its own storage
+    // there, to keep them for the reverse sweep
+    std::function<void(int)> edge_tape_begin, edge_tape;
     // scratch of the single-box entry points (madv_ppm), grown on demand
     double* box_scratch = nullptr;
     long box_scratch_n = 0;
@@ -228,7 +229,7 @@ enum {
     A_END
 };
 static_assert(A_END <= N_USER_SLOTS, "user slots");
-void ppm_faces(Ctx& c, int d, int fs, int sc);  // van Leer slopes + interface values (madv_kernels.cu)
+void ppm_faces(Ctx& c, int d, int fs, int sc, int faces);  // van Leer slopes (+ interface values)
 void edge_scal_coeffs(Ctx& c);                  // tracing / transverse coefficients of F_UMAC0..2
 void adj_update(Ctx& c);
 void adj_flux(Ctx& c, int want_u);

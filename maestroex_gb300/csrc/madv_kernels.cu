@@ -486,17 +486,18 @@ static void ppm_any(Ctx& c, int d, int fs, int sc, const BCRecD& bc, int fu, int
 }
 
 // The first two launches of the ppm_type 1 sweep of ppm_dir (van Leer slopes into F_DSVL,
-// interface values into F_FACE0+d) for component sc of field fs, interior form: the
-// reverse sweep reads them to recover the forward's limiter decisions.
-void ppm_faces(Ctx& c, int d, int fs, int sc) {
+// and with `faces` the interface values into F_FACE0+d) for component sc of field fs,
+// interior form: the reverse sweep reads them to recover the forward's limiter decisions.
+void ppm_faces(Ctx& c, int d, int fs, int sc, int faces) {
     const RecipC r6 = make_recip(6.0);
     auto one = [&](auto dir) {
         constexpr int D = decltype(dir)::value;
         int glo[3] = {1, 1, 1};
         glo[D] = 2;
         launch(c, region(c, glo[0], glo[1], glo[2], glo[0], glo[1], glo[2], -1), 1, k_dsvl<D>, c.V(), fs, sc);
-        launch(c, region(c, 1, 1, 1, 1, 1, 1, D), 1, k_ppm_face<D, 1>, c.V(), fs, sc, F_FACE0 + D, 0, 0,
-               c.P.dom_lo[D], c.P.dom_hi[D], r6);
+        if (faces)
+            launch(c, region(c, 1, 1, 1, 1, 1, 1, D), 1, k_ppm_face<D, 1>, c.V(), fs, sc, F_FACE0 + D, 0, 0,
+                   c.P.dom_lo[D], c.P.dom_hi[D], r6);
     };
     if (d == 0) one(std::integral_constant<int, 0>{});
     else if (d == 1) one(std::integral_constant<int, 1>{});
@@ -1073,6 +1074,7 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
     if (c.P.ppm_type != 0) trace_coeffs_faces(c, F_UMAC0);
     if (!is_cons) transverse_coeffs(c, F_UMAC0);
     for (int comp = start_comp; comp < start_comp + num_comp; ++comp) {
+        if (c.edge_tape_begin) c.edge_tape_begin(comp);
         const BCRecD& bc = bh[comp];  // start_bccomp == start_scomp at every call site
         if (c.P.ppm_type == 0) {
             for (int d = 0; d < 3; ++d) slope_any(c, d, F_SOLD, comp, F_SLOPE, d, 1, bcs_dev(c, which_bcs), comp);
