@@ -36,7 +36,7 @@ HBM_PEAK_FALLBACK = 6792.7
 #   dram: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per valid cell, one launch
 KERNEL_WORK = {
     "k_ppm_cell<0,1,1>": {"fp64": 0.9596, "dram": None},
-    "k_ppm_cell<1,1,1>": {"fp64": 0.9595, "dram": None},
+    "k_ppm_cell<1,1,1>": {"fp64": 0.9595, "dram": 51.3},
     "k_ppm_cell<2,1,1>": {"fp64": 0.9482, "dram": None},
 }
 STAGE_FP64_PER_CELL = 189.02  # FP64 warp instructions per valid cell, whole stage
@@ -270,7 +270,7 @@ def run_adjoint(args, barrier):
     from maestroex_gb300 import configs
     from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
     from maestroex_gb300.stage import MultiFab, make_stage
-    n, nsteps, ckpt = args.adj_n, 16, 4
+    n, nsteps, ckpt = args.adj_n, args.adj_steps, args.adj_ckpt
     cfg = configs.adjoint_config(n=(n, n, n), max_grid=min(64, n), nspec=3)
     st = make_stage(cfg)
     boxes, nscal = cfg["boxes"], 4 + cfg["nspec"]
@@ -282,6 +282,13 @@ def run_adjoint(args, barrier):
     w[FIRSTSPEC:] = rng.normal(size=w[FIRSTSPEC:].shape)
     wt = MultiFab(boxes, nscal, 0).from_domain(w)
     gs, gu, sf = MultiFab(boxes, nscal, 0), MultiFab(boxes, 3, 0), MultiFab(boxes, nscal, 0)
+
+    if args.profile_adjoint:
+        call_kw = dict(grad_s=gs, grad_u=gu)
+        st.stage_adjoint(u, s0, wt, nsteps, ckpt, **call_kw)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_adjoint": True, "launches": st.launch_count()}))
+        return None
 
     def call(kind, uu=None, ss=None):
         return st.stage_adjoint(u if uu is None else uu, s0 if ss is None else ss, wt, nsteps, ckpt,
@@ -425,7 +432,11 @@ def main():
     ap.add_argument("--amr-n", type=int, default=256, help="level-0 extent of the two-level AMR workload")
     ap.add_argument("--no-amr", action="store_true")
     ap.add_argument("--adj-n", type=int, default=128, help="extent of the multi-step adjoint workload")
+    ap.add_argument("--adj-steps", type=int, default=16)
+    ap.add_argument("--adj-ckpt", type=int, default=4)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="run one adjoint call (state and velocity gradients) and exit (the command ncu captures)")
     ap.add_argument("--no-2d", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
@@ -459,6 +470,10 @@ def main():
         build.build_library()
     if ws > 1:
         dist.barrier()
+
+    if args.profile_adjoint:
+        run_adjoint(args, lambda: torch.cuda.synchronize())
+        return
 
     cfg = configs.planar_config(n=(args.n,) * 3, nspec=args.nspec, ppm_type=1, max_grid=args.box,
                                 seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
