@@ -412,10 +412,21 @@ def run_2d(args, barrier):
         tot += e0.elapsed_time(e1)
     ms = tot / reps
     launches = st.launch_count()
+    gpu = buf.snew.to_domain(cfg["n"]).cpu().numpy()
     st.close()
+    # the oracle on the same inputs: its time on this host (one box: one thread) and the
+    # largest relative difference of the updated density, enthalpy and species
+    from oracle import pyoracle
+    t0 = time.perf_counter()
+    ref = pyoracle.run_stage_2d(cfg, nthreads=1)["snew"]
+    t_or = time.perf_counter() - t0
+    comps = [0, 1] + list(range(4, 4 + cfg["nspec"]))
+    err = max(float(np.abs(gpu[c] - ref[c]).max() / np.abs(ref[c]).max()) for c in comps)
     return {"workload": "2-D single level 256 x 256 (one box), NumSpec 3, ppm_type 1, x periodic, "
                         "y slipwall / outflow", "value": 256 * 256 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
-            "gpu_launches": launches}
+            "gpu_launches": launches, "max_rel_err_vs_oracle": err,
+            "cpu_oracle": {"value": 256 * 256 / t_or, "unit": UNIT, "cores": 1, "kind": "port",
+                           "sample": "the whole 256 x 256 stage, once"}}
 
 
 def main():
