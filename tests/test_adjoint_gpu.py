@@ -142,6 +142,47 @@ def test_velocity_adjoint_matches_central_differences():
     assert worst <= 1e-6, worst
 
 
+class StageSteps(torch.autograd.Function):
+    """The multi-step stage as a torch function of (sold0, uold), domain-sized tensors; its
+    backward is madv_stage_adjoint with the incoming gradient as the weight.  Used only in
+    this gradient-check harness."""
+
+    @staticmethod
+    def forward(ctx, s0, u, case):
+        ctx.case = case
+        sm = MultiFab(case.boxes, case.nscal, 0).from_domain(s0)
+        um = MultiFab(case.boxes, 3, 0).from_domain(u)
+        ctx.mf = (sm, um)
+        out = MultiFab(case.boxes, case.nscal, 0)
+        case.st.stage_adjoint(um, sm, case.weight, case.nsteps, case.ckpt, sfinal=out)
+        return out.to_domain(case.n)
+
+    @staticmethod
+    def backward(ctx, g):
+        case = ctx.case
+        sm, um = ctx.mf
+        w = MultiFab(case.boxes, case.nscal, 0).from_domain(g.contiguous())
+        gs = MultiFab(case.boxes, case.nscal, 0)
+        gu = MultiFab(case.boxes, 3, 0)
+        case.st.stage_adjoint(um, sm, w, case.nsteps, case.ckpt, grad_s=gs, grad_u=gu)
+        return gs.to_domain(case.n), gu.to_domain(case.n), None
+
+
+def test_autograd_wrapper_matches_the_c_abi_adjoint():
+    """torch.autograd through StageSteps gives the gradients of the direct call."""
+    case = Case(nsteps=2, ckpt=1)
+    s0 = torch.from_numpy(case.cfg["sold"]).cuda().requires_grad_(True)
+    u = torch.from_numpy(case.cfg["uold"]).cuda().requires_grad_(True)
+    w = torch.from_numpy(case.w).cuda()
+    J = (w * StageSteps.apply(s0, u, case)).sum()
+    gs, gu = torch.autograd.grad(J, (s0, u))
+    _, grad, _, _, gud = case.adjoint(want_u=True)
+    G, GU = grad.to_domain(case.n), gud.to_domain(case.n)
+    for a, b in ((gs, G), (gu, GU)):
+        scale = b.abs().amax(dim=(1, 2, 3), keepdim=True).clamp_min(1e-300)
+        assert float(((a - b).abs() / scale).max()) <= 1e-12
+
+
 def test_adjoint_carried_components_and_determinism():
     """Temperature and pi are carried unchanged, so their gradient is the weight; two runs
     give the same J bit for bit and gradients equal to atomic-summation rounding."""
