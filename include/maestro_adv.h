@@ -48,7 +48,7 @@ typedef struct {
     int enthalpy_pred_type;     /* 0 rhoh, 1 rhoh' */
     int ppm_trace_forces;       /* must be 0 */
     int evolve_base_state;
-    int use_exact_base_state;   /* must be 0 (planar) */
+    int use_exact_base_state;   /* planar: 0; spherical: 1 */
     int phys_bc_lo[3];
     int phys_bc_hi[3];
     int dom_lo[3];              /* level-0 domain box */
@@ -62,6 +62,11 @@ typedef struct {
     int base_cutoff_density_coord;
     int dim;                    /* 3 (0 means 3) or 2: the AMREX_SPACEDIM == 2 form, y radial,
                                    boxes and domain with z = [0, 0], 2 velocity components */
+    int spherical;              /* 1: full-star spherical geometry (3-D, one level, with
+                                   use_exact_base_state = 1: the irregular radial grid
+                                   r_cc(i) = sqrt(0.75 + 2i) dx, nr = nr_irreg + 1) */
+    double prob_lo[3];          /* physical domain (the star's centre is its midpoint) */
+    double prob_hi[3];
 } madv_params;
 
 typedef struct {

@@ -216,6 +216,116 @@ def adjoint_config(n=(128, 128, 128), max_grid=64, nspec=3, seed=20261203 + 4, c
     return cfg
 
 
+def lane_emden(n_poly=1.5, h=1.0e-4):
+    """theta(xi) of the Lane-Emden equation theta'' + 2 theta'/xi + theta^n = 0 (RK4 from the
+    series start), integrated to the first zero xi_1; returns (xi, theta) arrays."""
+    xi = [h]
+    th = [1.0 - h * h / 6.0]
+    dth = -h / 3.0
+
+    def f(x, t, dt):
+        return dt, -2.0 * dt / x - max(t, 0.0) ** n_poly
+
+    x, t = h, th[0]
+    while t > 0.0:
+        k1 = f(x, t, dth)
+        k2 = f(x + h / 2, t + h / 2 * k1[0], dth + h / 2 * k1[1])
+        k3 = f(x + h / 2, t + h / 2 * k2[0], dth + h / 2 * k2[1])
+        k4 = f(x + h, t + h * k3[0], dth + h * k3[1])
+        t += h / 6 * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0])
+        dth += h / 6 * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1])
+        x += h
+        xi.append(x)
+        th.append(t)
+    return np.array(xi), np.maximum(np.array(th), 0.0)
+
+
+def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20261203 + 5, cfl=0.5,
+                     rho_c=2.0e9, w0_amp=1.0e5, u_amp=1.0e6, L=5.0e8, pert=1.0e-9):
+    """Full-star spherical configuration with the exact base state: an n^3 Cartesian domain
+    [0, L]^3 with the star at its centre, outflow on every face; an n = 1.5 polytrope of
+    central density rho_c and radius 0.9 L/2 (Lane-Emden, integrated here) on the irregular
+    radial grid r_cc(i) = sqrt(0.75 + 2i) dx, with a constant ambient density 1e-5 rho_c
+    outside; w0 on the radial edges a seeded smooth profile of amplitude w0_amp, zero at
+    the centre and outside the star; a seeded smooth velocity of amplitude u_amp tapered to
+    zero at 0.8 of the radius; density and enthalpy perturbed by `pert` (relative);
+    base_cutoff_density half the ambient density, so the buoyancy cutoff (5x) covers the
+    ambient."""
+    rng = np.random.default_rng(seed)
+    n3 = (n, n, n)
+    dx = L / n
+    nr_irreg = int((3.0 * (n / 2 - 0.5) * (n / 2 - 0.5) - 0.75) / 2.0)
+    nr = nr_irreg + 1
+    r_cc = np.sqrt(0.75 + 2.0 * np.arange(nr)) * dx
+    r_edge = np.concatenate([[0.0], np.sqrt(0.75 + 2.0 * (np.arange(nr) + 0.5)) * dx])
+    npoly, gamma = 1.5, 5.0 / 3.0
+    xi, theta = lane_emden(npoly)
+    R = 0.9 * 0.5 * L
+    a = R / xi[-1]
+    G = 6.674e-8
+    K = 4.0 * math.pi * G * a * a * rho_c ** (1.0 - 1.0 / npoly) / (npoly + 1.0)
+    th_r = np.interp(r_cc / a, xi, theta, right=0.0)
+    rho_floor = 1.0e-5 * rho_c
+    rho0 = np.maximum(rho_c * th_r ** npoly, rho_floor)
+    p0 = K * rho0 ** (1.0 + 1.0 / npoly)
+    rhoh0 = gamma / (gamma - 1.0) * p0
+    # gravity from the enclosed mass of the shells between the radial edges
+    shell = 4.0 / 3.0 * math.pi * (r_edge[1:] ** 3 - r_edge[:-1] ** 3)
+    menc = np.cumsum(rho0 * shell) - 0.5 * rho0 * shell
+    grav = -G * menc / r_cc ** 2
+    w0 = np.zeros(nr + 1)
+    inside = r_edge < R
+    for m in range(1, 4):
+        w0[inside] += rng.normal() * np.sin(m * math.pi * r_edge[inside] / R)
+    w0 *= w0_amp / max(np.abs(w0).max(), 1e-300)
+    w0[0] = 0.0
+
+    # cell -> radial index, as Maestro::InitBaseStateMapSphr (round half away from zero)
+    c = (np.arange(n) + 0.5) * dx - 0.5 * L
+    X3, Y3, Z3 = c[None, None, :], c[None, :, None], c[:, None, None]
+    r2 = X3 * X3 + Y3 * Y3 + Z3 * Z3
+    idx = np.floor(r2 / (2.0 * dx * dx) - 0.375 + 0.5).astype(np.int64)
+    shape = (n, n, n)
+    periodic = [False, False, False]
+    rho = rho0[idx] * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
+    X = np.zeros((nspec,) + shape)
+    for sp in range(nspec):
+        X[sp] = 1.0 + 0.5 * _smooth_field(rng, n3, (L / n,) * 3, periodic)
+    X = np.maximum(X, 0.05)
+    X /= X.sum(axis=0, keepdims=True)
+    h = (rhoh0 / rho0)[idx] * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
+    nscal = 4 + nspec
+    sold = np.zeros((nscal,) + shape)
+    sold[RHO] = rho
+    sold[RHOH] = rho * h
+    sold[TEMP] = 1.0e8
+    sold[FIRSTSPEC:] = rho[None] * X
+    # the velocity lives inside the star: a smooth seeded field tapered to zero at 0.8 R
+    taper = np.maximum(0.0, 1.0 - r2 / (0.8 * R) ** 2) ** 2
+    u = np.zeros((3,) + shape)
+    for d in range(3):
+        u[d] = u_amp * taper * _smooth_field(rng, n3, (L / n,) * 3, periodic)
+    umax = max(float(np.abs(u).max()), 1.0) + w0_amp
+    # Maestro::EstDt: the advective limit and the force limit sqrt(2 dx / |f|) with the
+    # buoyancy (rho - rho0) g / rho of the seeded perturbation (Source/MaestroDt.cpp:150-225)
+    fmax = float(np.abs(grav).max()) * float(np.abs(rho / rho0[idx] - 1.0).max())
+    dt = cfl * min(dx / umax, math.sqrt(2.0 * dx / max(fmax, 1e-300)))
+    if boxes is None:
+        boxes = tile_boxes(n3, max_grid)
+    from .basestate import cell_to_edge
+    return dict(
+        n=n3, dx=(dx, dx, dx), nspec=nspec, ppm_type=ppm_type, slope_order=4, bc_lo=(OUTFLOW,) * 3,
+        bc_hi=(OUTFLOW,) * 3, species_pred_type=1, enthalpy_pred_type=1, evolve_base_state=1,
+        use_exact_base_state=1, spherical=1, prob_lo=(0.0, 0.0, 0.0), prob_hi=(L, L, L), nr=nr,
+        dt=dt, rel_eps=1.0e-8 * umax, base_cutoff_density=0.5 * rho_floor, buoyancy_cutoff_factor=5.0,
+        boxes=boxes, seed=seed, uold=np.ascontiguousarray(u), sold=np.ascontiguousarray(sold),
+        gpi=np.zeros((3,) + shape), thermal=np.zeros((1,) + shape),
+        rho0_old=rho0.copy(), rho0_new=rho0.copy(), rhoh0_old=rhoh0.copy(), rhoh0_new=rhoh0.copy(),
+        p0_old=p0.copy(), p0_new=p0.copy(), psi=np.zeros(nr), grav_cell=grav, w0_force=np.zeros(nr), w0=w0,
+        rho0_predicted_edge=cell_to_edge(rho0),
+    )
+
+
 def bubble_boxes(n0, nbubbles=3, cover=0.12, block_edges=(8, 16, 32), rng=None, max_edge=32):
     """Level-1 boxes (refinement ratio 2, fine index space) around seeded bubble centres.
 

@@ -38,6 +38,9 @@ class MadvParams(C.Structure):
         ("do_eos_h_above_cutoff", C.c_int),
         ("base_cutoff_density_coord", C.c_int),
         ("dim", C.c_int),
+        ("spherical", C.c_int),
+        ("prob_lo", C.c_double * 3),
+        ("prob_hi", C.c_double * 3),
     ]
 
 
@@ -51,7 +54,7 @@ def make_params(cfg):
     p.enthalpy_pred_type = cfg.get("enthalpy_pred_type", 1)
     p.ppm_trace_forces = 0
     p.evolve_base_state = cfg.get("evolve_base_state", 1)
-    p.use_exact_base_state = 0
+    p.use_exact_base_state = cfg.get("use_exact_base_state", 0)
     for d in range(3):
         p.phys_bc_lo[d] = cfg["bc_lo"][d]
         p.phys_bc_hi[d] = cfg["bc_hi"][d]
@@ -65,4 +68,11 @@ def make_params(cfg):
     p.do_eos_h_above_cutoff = cfg.get("do_eos_h_above_cutoff", 1)
     p.dim = cfg.get("dim", 3)
     p.base_cutoff_density_coord = cfg["n"][p.dim - 1]
+    p.spherical = cfg.get("spherical", 0)
+    lo = cfg.get("prob_lo", (0.0, 0.0, 0.0))
+    for d in range(3):
+        p.prob_lo[d] = lo[d]
+        p.prob_hi[d] = cfg.get("prob_hi", tuple(lo[e] + cfg["n"][e] * cfg["dx"][e] for e in range(3)))[d]
+    if p.spherical:
+        p.base_cutoff_density_coord = cfg["nr"]
     return p

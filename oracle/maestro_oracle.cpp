@@ -41,6 +41,84 @@ struct Lev {
     PPMCtx pc;
     double dt = 0, rel_eps = 0;
 
+    // ------------------------------------------------------------------ spherical
+    // Full-star geometry with the exact base state: centre, radii of the irregular radial
+    // grid (Source/BaseStateGeometry.cpp:86-96) and w0 on faces (MakeW0mac).
+    double center[3] = {0.0, 0.0, 0.0};
+    std::vector<double> r_cc_loc, r_edge_loc;
+    MF w0mac[3];
+
+    void InitSphr() {
+        for (int d = 0; d < 3; ++d) center[d] = 0.5 * (P.prob_lo[d] + P.prob_hi[d]);
+        const double dxf = L.dx[0];
+        // one radius past the last cell: Put1dArrayOnCart reads r_cc_loc(nr_fine) for the
+        // outermost cells (Source/MaestroFill3dData.cpp:115-118, past its array); the
+        // same formula continued
+        r_cc_loc.assign(nr + 1, 0.0);
+        for (int i = 0; i <= nr; ++i) r_cc_loc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
+        r_edge_loc.assign(nr + 1, 0.0);
+        for (int i = 0; i < nr; ++i) r_edge_loc[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
+    }
+    // cell centre relative to the star's centre (Source/MaestroFill3dData.cpp:103-110)
+    void sph_xyz(int i, int j, int k, double& x, double& y, double& z) const {
+        x = P.prob_lo[0] + (double(i) + 0.5) * L.dx[0] - center[0];
+        y = P.prob_lo[1] + (double(j) + 0.5) * L.dx[1] - center[1];
+        z = P.prob_lo[2] + (double(k) + 0.5) * L.dx[2] - center[2];
+    }
+    // Maestro::InitBaseStateMapSphr (Source/MaestroBaseStateGeometry.cpp:17-35)
+    int cc_to_r(int i, int j, int k) const {
+        double x, y, z;
+        sph_xyz(i, j, k, x, y, z);
+        const double index = (x * x + y * y + z * z) / (2.0 * L.dx[0] * L.dx[0]) - 0.375;
+        return (int)std::round(index);
+    }
+    // Put1dArrayOnCart, spherical, exact base state (Source/MaestroFill3dData.cpp:94-192):
+    // edge-centred input with w0_interp_type 2 (linear), cell-centred input injected
+    void Put1dSphr(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec) {
+        for (int b = 0; b < nb; ++b) {
+            const Arr& a = s0_cart[b];
+            MO_FOR3(L.ba[b]) {
+                double x, y, z;
+                sph_xyz(i, j, k, x, y, z);
+                const double radius = std::sqrt(x * x + y * y + z * z);
+                const int index = cc_to_r(i, j, k);
+                double v;
+                if (edge) {
+                    double rfac;
+                    if (index < nr) {
+                        rfac = (radius - r_edge_loc[index + 1]) / (r_cc_loc[index + 1] - r_cc_loc[index]);
+                    } else {
+                        rfac = (radius - r_edge_loc[index + 1]) / (r_cc_loc[index] - r_cc_loc[index - 1]);
+                    }
+                    if (index < nr) v = rfac * s0[index + 1] + (1.0 - rfac) * s0[index];
+                    else v = s0[nr];
+                } else {
+                    v = s0[index];
+                }
+                if (vec) {
+                    a(i, j, k, 0) = v * x / radius;
+                    a(i, j, k, 1) = v * y / radius;
+                    a(i, j, k, 2) = v * z / radius;
+                } else {
+                    a(i, j, k, 0) = v;
+                }
+            }
+        }
+    }
+    // Maestro::MakeW0mac, w0mac_interp_type 1 (Source/MaestroFill3dData.cpp:464-569): the
+    // face average of w0_cart over the nodal boxes grown by one
+    void MakeW0mac() {
+        for (int d = 0; d < 3; ++d) {
+            w0mac[d].define(L.ba, 1, 1, d, 0.0);
+            const int di = d == 0, dj = d == 1, dk = d == 2;
+            for (int b = 0; b < nb; ++b) {
+                const Arr& wc = w0_cart[b];
+                const Arr& o = w0mac[d][b];
+                MO_FOR3(grow(nodal(L.ba[b], d), 1)) { o(i, j, k) = 0.5 * (wc(i - di, j - dj, k - dk, d) + wc(i, j, k, d)); }
+            }
+        }
+    }
+
     // ------------------------------------------------------------------ setup
     // Maestro::BCSetup (Source/MaestroSetup.cpp:276-500)
     void BCSetup() {
@@ -186,6 +264,15 @@ struct Lev {
 
     // Maestro::Addw0, planar, one level (Source/MaestroFill3dData.cpp:365-423)
     void Addw0(MF* uedge, double mult) {
+        if (P.spherical) {  // Source/MaestroFill3dData.cpp:395-419: valid faces += mult w0mac
+            for (int b = 0; b < nb; ++b)
+                for (int d = 0; d < 3; ++d) {
+                    const Arr& e = uedge[d][b];
+                    const Arr& w = w0mac[d][b];
+                    MO_FOR3(nodal(L.ba[b], d)) { e(i, j, k) += mult * w(i, j, k); }
+                }
+            return;
+        }
         for (int b = 0; b < nb; ++b) {
             const Arr& wedge = uedge[2][b];
             Box zbx = grow(grow(nodal(L.ba[b], 2), 0, 1), 1, 1);
@@ -249,7 +336,12 @@ struct Lev {
                             default: break;
                         }
                     }
-                    if (d < 2) {
+                    if (P.spherical) {  // Source/MaestroMakeUtrans.cpp:368-377: with w0mac
+                        const double w0c = w0mac[d][b](i, j, k);
+                        bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fab(l + r + 2.0 * w0c) < rel_eps);
+                        double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+                        tr(i, j, k) = test ? 0.0 : v;
+                    } else if (d < 2) {
                         bool test = (l <= 0.0 && r >= 0.0) || (fab(l + r) < rel_eps);
                         double v = 0.5 * (l + r) > 0.0 ? l : r;
                         tr(i, j, k) = test ? 0.0 : v;
@@ -268,6 +360,38 @@ struct Lev {
     // Maestro::MakeVelForce, planar, one level (Source/MaestroForce.cpp:58-126)
     void MakeVelForce(MF& vel_force, MF* uedge, MF& sold, MF& w0_force_cart, MF& grav_cart, MF& rho0_cart) {
         vel_force.setVal(0.0);
+        if (P.spherical) {
+            // Source/MaestroForce.cpp:151-252; the exact base state has gradw0 = 0
+            // (:30-41), so the utilde term subtracts Ut.e_r * 0 * e_r
+            const double gradw0 = 0.0;
+            for (int b = 0; b < nb; ++b) {
+                const Arr& gpi_arr = gpi[b];
+                const Arr& rho_arr = sold[b];
+                const Arr& ue = uedge[0][b];
+                const Arr& ve = uedge[1][b];
+                const Arr& we = uedge[2][b];
+                const Arr& w0f = w0_force_cart[b];
+                const Arr& grav = grav_cart[b];
+                const Arr& r0 = rho0_cart[b];
+                const Arr& vf = vel_force[b];
+                MO_FOR3(L.ba[b]) {
+                    double x, y, z;
+                    sph_xyz(i, j, k, x, y, z);
+                    const double inv_radius = 1.0 / std::sqrt(x * x + y * y + z * z);  // MakeNormal
+                    const double nrm[3] = {x * inv_radius, y * inv_radius, z * inv_radius};
+                    double rhopert = rho_arr(i, j, k) - r0(i, j, k);
+                    if (rho_arr(i, j, k) < (P.buoyancy_cutoff_factor * P.base_cutoff_density)) rhopert = 0.0;
+                    for (int dim = 0; dim < 3; ++dim)
+                        vf(i, j, k, dim) =
+                            (rhopert * grav(i, j, k, dim) - gpi_arr(i, j, k, dim)) / rho_arr(i, j, k) - w0f(i, j, k, dim);
+                    const double ut_dot_er = 0.5 * (ue(i, j, k) + ue(i + 1, j, k)) * nrm[0] +
+                                             0.5 * (ve(i, j, k) + ve(i, j + 1, k)) * nrm[1] +
+                                             0.5 * (we(i, j, k) + we(i, j, k + 1)) * nrm[2];
+                    for (int dim = 0; dim < 3; ++dim) vf(i, j, k, dim) -= ut_dot_er * gradw0 * nrm[dim];
+                }
+            }
+            return;
+        }
         const int domhi = L.dom.hi[2];
         for (int b = 0; b < nb; ++b) {
             const Arr& gpi_arr = gpi[b];
@@ -488,7 +612,12 @@ struct Lev {
                                 (dt4 / h[t2]) * (tr2(i + a2i, j + a2j, k + a2k) + tr2(i, j, k)) *
                                     (q2(i + a2i, j + a2j, k + a2k) - q2(i, j, k)) +
                                 dt2 * fr;
-                    if (d < 2) {
+                    if (P.spherical) {  // Source/MaestroVelPred.cpp:1664-1673: with w0mac
+                        const double w0c = w0mac[d][b](i, j, k);
+                        bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fab(ml + mr + 2.0 * w0c) < rel_eps);
+                        double v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+                        out(i, j, k) = test ? 0.0 : v;
+                    } else if (d < 2) {
                         bool test = (ml <= 0.0 && mr >= 0.0) || (fab(ml + mr) < rel_eps);
                         double v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
                         out(i, j, k) = test ? 0.0 : v;
@@ -777,6 +906,40 @@ struct Lev {
     void ModifyScalForce(MF& scal_force, MF& state, MF* umac, MF& s0_edge_cart, MF& s0_cart, int comp,
                          int fullform) {
         const double* dx = L.dx;
+        if (P.spherical) {
+            // Source/MaestroForce.cpp:335-412; divu_cart = Put1dArrayOnCart(divw0) = 0 with
+            // the exact base state (:283-302)
+            const int* domlo = L.dom.lo;
+            const int* domhi = L.dom.hi;
+            for (int b = 0; b < nb; ++b) {
+                const Arr scal = state[b].comp(comp);
+                const Arr& um = umac[0][b];
+                const Arr& vm = umac[1][b];
+                const Arr& wm = umac[2][b];
+                const Arr& s0a = s0_cart[b];
+                const Arr force = scal_force[b].comp(comp);
+                MO_FOR3(L.ba[b]) {
+                    const double divu_c = 0.0;
+                    double divumac = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
+                                     (wm(i, j, k + 1) - wm(i, j, k)) / dx[2];
+                    if (fullform == 1) {
+                        force(i, j, k) -= scal(i, j, k) * (divumac + divu_c);
+                    } else {
+                        const double s0x_hi = i < domhi[0] ? 0.5 * (s0a(i, j, k) + s0a(i + 1, j, k)) : s0a(i, j, k);
+                        const double s0x_lo = i > domlo[0] ? 0.5 * (s0a(i, j, k) + s0a(i - 1, j, k)) : s0a(i, j, k);
+                        const double s0y_hi = j < domhi[1] ? 0.5 * (s0a(i, j, k) + s0a(i, j + 1, k)) : s0a(i, j, k);
+                        const double s0y_lo = j > domlo[1] ? 0.5 * (s0a(i, j, k) + s0a(i, j - 1, k)) : s0a(i, j, k);
+                        const double s0z_hi = k < domhi[2] ? 0.5 * (s0a(i, j, k) + s0a(i, j, k + 1)) : s0a(i, j, k);
+                        const double s0z_lo = k > domlo[2] ? 0.5 * (s0a(i, j, k) + s0a(i, j, k - 1)) : s0a(i, j, k);
+                        double divs0u = (um(i + 1, j, k) * s0x_hi - um(i, j, k) * s0x_lo) / dx[0] +
+                                        (vm(i, j + 1, k) * s0y_hi - vm(i, j, k) * s0y_lo) / dx[1] +
+                                        (wm(i, j, k + 1) * s0z_hi - wm(i, j, k) * s0z_lo) / dx[2];
+                        force(i, j, k) += -divs0u - (scal(i, j, k) - s0a(i, j, k)) * (divumac + divu_c);
+                    }
+                }
+            }
+            return;
+        }
         for (int b = 0; b < nb; ++b) {
             const Arr scal = state[b].comp(comp);
             const Arr& um = umac[0][b];
@@ -804,10 +967,37 @@ struct Lev {
 
     // Maestro::MakeRhoHForce, planar 3-D, one level (Source/MaestroForce.cpp:541-674)
     void MakeRhoHForce(MF& scal_force, int is_prediction, MF* umac, int add_thermal, MF& p0_cart, MF& psi_cart,
-                       MF& grav_cart, MF& rho0_cart) {
+                       MF& grav_cart, MF& rho0_cart, MF* p0mac = nullptr) {
         const int domhi = L.dom.hi[2];
         const bool psi_in = (is_prediction == 1 && P.enthalpy_pred_type == 2) ||
                             (is_prediction == 1 && P.enthalpy_pred_type == 0) || (is_prediction == 0);
+        if (P.spherical) {  // Source/MaestroForce.cpp:637-670: u grad p0 = div(u p0) - p0 div u
+            const double* dx = L.dx;
+            for (int b = 0; b < nb; ++b) {
+                const Arr& um = umac[0][b];
+                const Arr& vm = umac[1][b];
+                const Arr& wm = umac[2][b];
+                const Arr& px = p0mac[0][b];
+                const Arr& py = p0mac[1][b];
+                const Arr& pz = p0mac[2][b];
+                const Arr& p0c = p0_cart[b];
+                const Arr& th = thermal[b];
+                const Arr& ps = psi_cart[b];
+                const Arr rf = scal_force[b].comp(RhoH);
+                MO_FOR3(L.ba[b]) {
+                    double divup = (um(i + 1, j, k) * px(i + 1, j, k) - um(i, j, k) * px(i, j, k)) / dx[0] +
+                                   (vm(i, j + 1, k) * py(i, j + 1, k) - vm(i, j, k) * py(i, j, k)) / dx[1] +
+                                   (wm(i, j, k + 1) * pz(i, j, k + 1) - wm(i, j, k) * pz(i, j, k)) / dx[2];
+                    double p0divu = ((um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
+                                     (wm(i, j, k + 1) - wm(i, j, k)) / dx[2]) *
+                                    p0c(i, j, k);
+                    rf(i, j, k) = divup - p0divu;
+                    if (psi_in) rf(i, j, k) += ps(i, j, k);
+                    if (add_thermal == 1) rf(i, j, k) += th(i, j, k);
+                }
+            }
+            return;
+        }
         for (int b = 0; b < nb; ++b) {
             const Arr& wm = umac[2][b];
             const Arr& p0c = p0_cart[b];
@@ -839,7 +1029,7 @@ struct Lev {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = scal[b];
             MO_FOR3(L.ba[b]) {
-                const double s0c = s0[k];
+                const double s0c = P.spherical ? s0[cc_to_r(i, j, k)] : s0[k];
                 if (flag) a(i, j, k, comp) = a(i, j, k, comp) - s0c;
                 else a(i, j, k, comp) = a(i, j, k, comp) + s0c;
             }
@@ -862,9 +1052,30 @@ struct Lev {
     // Maestro::MakeRhoXFlux, planar 3-D (Source/MaestroMakeFlux.cpp:18-465)
     void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<double>& r0_old,
                       const std::vector<double>& r0e_old, const std::vector<double>& r0_new,
-                      const std::vector<double>& r0e_new, int start_comp, int num_comp) {
+                      const std::vector<double>& r0e_new, int start_comp, int num_comp, MF* r0mac_old = nullptr,
+                      MF* r0mac_new = nullptr) {
         const int spt = P.species_pred_type;
         for (int d = 0; d < 3; ++d) sflux[d].setVal(0.0, Rho, 1, 0);
+        if (P.spherical) {  // Source/MaestroMakeFlux.cpp:56-71, 306-408
+            for (int b = 0; b < nb; ++b)
+                for (int d = 0; d < 3; ++d) {
+                    const Arr& f = sflux[d][b];
+                    const Arr& e = sedge[d][b];
+                    const Arr& u = umac[d][b];
+                    const Arr& ro = r0mac_old[d][b];
+                    const Arr& rn = r0mac_new[d][b];
+                    MO_FOR3(nodal(L.ba[b], d)) {
+                        const double rho0_edge = 0.5 * ro(i, j, k) + 0.5 * rn(i, j, k);  // MultiFab::LinComb
+                        for (int comp = start_comp; comp < num_comp + start_comp; ++comp) {
+                            if (spt == 1) f(i, j, k, comp) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, comp);
+                            else if (spt == 2) f(i, j, k, comp) = u(i, j, k) * e(i, j, k, comp);
+                            else if (spt == 3) f(i, j, k, comp) = u(i, j, k) * e(i, j, k, Rho) * e(i, j, k, comp);
+                            f(i, j, k, Rho) += f(i, j, k, comp);
+                        }
+                    }
+                }
+            return;
+        }
         for (int b = 0; b < nb; ++b) {
             for (int d = 0; d < 3; ++d) {
                 const Arr& f = sflux[d][b];
@@ -895,8 +1106,23 @@ struct Lev {
     // Maestro::MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:467-1067)
     void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<double>& rh0_old,
                       const std::vector<double>& rh0e_old, const std::vector<double>& rh0_new,
-                      const std::vector<double>& rh0e_new) {
+                      const std::vector<double>& rh0e_new, MF* rh0mac_old = nullptr, MF* rh0mac_new = nullptr) {
         const int ept = P.enthalpy_pred_type;
+        if (P.spherical) {  // exact base state, (rho h)' predicted (Source/MaestroMakeFlux.cpp:540-548, 788-840)
+            for (int b = 0; b < nb; ++b)
+                for (int d = 0; d < 3; ++d) {
+                    const Arr& f = sflux[d][b];
+                    const Arr& e = sedge[d][b];
+                    const Arr& u = umac[d][b];
+                    const Arr& ho = rh0mac_old[d][b];
+                    const Arr& hn = rh0mac_new[d][b];
+                    MO_FOR3(nodal(L.ba[b], d)) {
+                        const double rhoh0_edge = 0.5 * ho(i, j, k) + 0.5 * hn(i, j, k);
+                        f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
+                    }
+                }
+            return;
+        }
         for (int b = 0; b < nb; ++b)
             for (int d = 0; d < 3; ++d) {
                 const Arr& f = sflux[d][b];
@@ -1052,10 +1278,33 @@ struct Stage {
     // Maestro::Put1dArrayOnCart, planar (Source/MaestroFill3dData.cpp:9-36)
     void Put1dArrayOnCart(const BS& s0, VMF& s0_cart, bool edge, bool vec, const std::vector<BCRec>* bcs, int bccomp,
                           bool is_vel) {
-        for (int lev = 0; lev < nlev; ++lev) S[lev].Put1d(s0[lev], s0_cart[lev], edge, vec);
+        for (int lev = 0; lev < nlev; ++lev) {
+            if (P.spherical) S[lev].Put1dSphr(s0[lev], s0_cart[lev], edge, vec);
+            else S[lev].Put1d(s0[lev], s0_cart[lev], edge, vec);
+        }
         const int nc = vec ? 3 : 1;
         AverageDown(s0_cart, 0, nc);
         if (s0_cart[0].ng > 0) FillPatch(s0_cart, 0, nc, bccomp, *bcs, is_vel);
+    }
+    // Maestro::MakeS0mac, exact base state, s0mac_interp_type 1 (Source/MaestroFill3dData.cpp:712-783):
+    // s0 injected into cells (two ghost cells by FillPatch with bcs_f), averaged to the
+    // faces of the nodal boxes grown by one
+    void MakeS0mac(const BS& s0, VF& s0mac) {
+        VMF s0_cart(nlev);
+        for (int lev = 0; lev < nlev; ++lev) s0_cart[lev].define(S[lev].L.ba, 1, 2, -1, 0.0);
+        Put1dArrayOnCart(s0, s0_cart, false, false, &bcs_f(), 0, false);
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Level& L = S[lev].L;
+            for (int d = 0; d < 3; ++d) {
+                s0mac[lev][d].define(L.ba, 1, 1, d, 0.0);
+                const int di = d == 0, dj = d == 1, dk = d == 2;
+                for (int b = 0; b < (int)L.ba.size(); ++b) {
+                    const Arr& c = s0_cart[lev][b];
+                    const Arr& o = s0mac[lev][d][b];
+                    MO_FOR3(grow(nodal(L.ba[b], d), 1)) { o(i, j, k) = 0.5 * (c(i - di, j - dj, k - dk) + c(i, j, k)); }
+                }
+            }
+        }
     }
     // Maestro::CelltoEdge over the chunks of every level, then RestrictBase of the edges
     // (Source/MaestroCelltoEdge.cpp:17-58, Source/MaestroBaseStateGeometry.cpp:240-262)
@@ -1189,7 +1438,7 @@ struct Stage {
                          int fullform) {
         VMF s0_edge_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) s0_edge_cart[lev].define(S[lev].L.ba, 1, 1);
-        Put1dArrayOnCart(s0_edge, s0_edge_cart, false, false, &bcs_f(), 0, false);
+        if (!P.spherical) Put1dArrayOnCart(s0_edge, s0_edge_cart, false, false, &bcs_f(), 0, false);
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].ModifyScalForce(scal_force[lev], state[lev], umac[lev].data(), s0_edge_cart[lev], s0_cart[lev], comp,
                                    fullform);
@@ -1216,12 +1465,16 @@ struct Stage {
             rho0_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
         }
         Put1dArrayOnCart(pp0, p0_cart, false, false, &bcs_f(), 0, false);
+        VF p0mac(nlev);
+        if (P.spherical) MakeS0mac(pp0, p0mac);
         Put1dArrayOnCart(bs(&Lev::psi), psi_cart, false, false, &bcs_f(), 0, false);
         Put1dArrayOnCart(r0, rho0_cart, false, false, &bcs_s(), Rho, false);
-        Put1dArrayOnCart(bs(&Lev::grav_cell), grav_cart, false, false, &bcs_f(), 0, false);  // MakeGravCell, planar
+        // MakeGravCell: planar, the constant gravity of grav_cell; the spherical force does
+        // not read it
+        if (!P.spherical) Put1dArrayOnCart(bs(&Lev::grav_cell), grav_cart, false, false, &bcs_f(), 0, false);
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeRhoHForce(scal_force[lev], is_prediction, umac[lev].data(), add_thermal, p0_cart[lev],
-                                 psi_cart[lev], grav_cart[lev], rho0_cart[lev]);
+                                 psi_cart[lev], grav_cart[lev], rho0_cart[lev], p0mac[lev].data());
         AverageDown(scal_force, RhoH, 1);
         FillPatch(scal_force, RhoH, 1, 0, bcs_f(), false);
     }
@@ -1241,17 +1494,28 @@ struct Stage {
     // Maestro::MakeRhoXFlux (Source/MaestroMakeFlux.cpp:18-465)
     void MakeRhoXFlux(VF& sflux, VMF& eta, VF& sedge, VF& umac, const BS& r0_old, const BS& r0e_old, const BS& r0_new,
                       const BS& r0e_new, int start_comp, int num_comp) {
+        VF r0mac_old(nlev), r0mac_new(nlev);
+        if (P.spherical) {  // Source/MaestroDensityAdvance.cpp:167-179, 193-213
+            MakeS0mac(r0_old, r0mac_old);
+            MakeS0mac(r0_new, r0mac_new);
+        }
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeRhoXFlux(sflux[lev].data(), eta[lev], sedge[lev].data(), umac[lev].data(), r0_old[lev],
-                                r0e_old[lev], r0_new[lev], r0e_new[lev], start_comp, num_comp);
+                                r0e_old[lev], r0_new[lev], r0e_new[lev], start_comp, num_comp, r0mac_old[lev].data(),
+                                r0mac_new[lev].data());
         AverageDownFaces(sflux);
     }
     // Maestro::MakeRhoHFlux (Source/MaestroMakeFlux.cpp:467-1067)
     void MakeRhoHFlux(VF& sflux, VF& sedge, VF& umac, const BS& rh0_old, const BS& rh0e_old, const BS& rh0_new,
                       const BS& rh0e_new) {
+        VF h0mac_old(nlev), h0mac_new(nlev);
+        if (P.spherical) {  // exact base state: rhoh0 on faces (Source/MaestroEnthalpyAdvance.cpp:187-220)
+            MakeS0mac(rh0_old, h0mac_old);
+            MakeS0mac(rh0_new, h0mac_new);
+        }
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeRhoHFlux(sflux[lev].data(), sedge[lev].data(), umac[lev].data(), rh0_old[lev], rh0e_old[lev],
-                                rh0_new[lev], rh0e_new[lev]);
+                                rh0_new[lev], rh0e_new[lev], h0mac_old[lev].data(), h0mac_new[lev].data());
         AverageDownFaces(sflux);
     }
     // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
@@ -1273,9 +1537,11 @@ struct Stage {
                         int which_step) {
         const int spt = P.species_pred_type;
         const BS rho0_old = bs(&Lev::rho0_old), rho0_new = bs(&Lev::rho0_new);
-        BS rho0_edge_old, rho0_edge_new;
-        CelltoEdge(rho0_old, rho0_edge_old);
-        CelltoEdge(rho0_new, rho0_edge_new);
+        BS rho0_edge_old(nlev), rho0_edge_new(nlev);
+        if (!P.spherical) {  // spherical: no planar edge state (Source/MaestroDensityAdvance.cpp:22-25)
+            CelltoEdge(rho0_old, rho0_edge_old);
+            CelltoEdge(rho0_new, rho0_edge_new);
+        }
         for (auto& f : scal_force) f.setVal(0.0);
         VMF rho0_old_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) rho0_old_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
@@ -1317,9 +1583,11 @@ struct Stage {
     void EnthalpyAdvance(VMF& scalold, VMF& scalnew, VF& sedge, VF& sflux, VMF& scal_force, VF& umac, int which_step) {
         const int ept = P.enthalpy_pred_type;
         const BS rhoh0_old = bs(&Lev::rhoh0_old), rhoh0_new = bs(&Lev::rhoh0_new);
-        BS rhoh0_edge_old, rhoh0_edge_new;
-        CelltoEdge(rhoh0_old, rhoh0_edge_old);
-        CelltoEdge(rhoh0_new, rhoh0_edge_new);
+        BS rhoh0_edge_old(nlev), rhoh0_edge_new(nlev);
+        if (!P.spherical) {
+            CelltoEdge(rhoh0_old, rhoh0_edge_old);
+            CelltoEdge(rhoh0_new, rhoh0_edge_new);
+        }
         for (auto& f : scal_force) f.setVal(0.0);
         VMF rhoh0_old_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) rhoh0_old_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
@@ -1389,7 +1657,12 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
     if (which_step != 1 && which_step != 2) throw std::runtime_error("which_step must be 1 or 2");
     if (nlev < 1 || nlev > 4) throw std::runtime_error("1 to 4 levels");
     if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
-    if (p->use_exact_base_state) throw std::runtime_error("use_exact_base_state is spherical-only");
+    if (p->use_exact_base_state && !p->spherical) throw std::runtime_error("use_exact_base_state is spherical-only");
+    if (p->spherical) {
+        if (!p->use_exact_base_state) throw std::runtime_error("spherical needs use_exact_base_state = 1");
+        if (nlev != 1) throw std::runtime_error("spherical: one level");
+        if (p->enthalpy_pred_type != 1) throw std::runtime_error("spherical: enthalpy_pred_type 1");
+    }
     if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
         throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
     if (!(p->species_pred_type >= 1 && p->species_pred_type <= 3))
@@ -1428,6 +1701,11 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         off += nboxes[lev];
         S.nb = nboxes[lev];
         S.nr = S.L.dom.hi[2] - S.L.dom.lo[2] + 1;
+        if (p->spherical) {
+            // nr_fine = nr_irreg + 1 (Source/MaestroSetup.cpp:66-82)
+            const double domhi = S.L.dom.hi[0] + 1;
+            S.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
+        }
         S.ng_s = S.ng_adv = H.ng_s;
         S.dt = p->dt;
         S.rel_eps = p->rel_eps;
@@ -1448,6 +1726,7 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         S.w0 = vec(I.w0, nr + 1);
         S.rho0_predicted_edge = vec(I.rho0_predicted_edge, nr + 1);
         S.cutoff = p->base_cutoff_density_coord;
+        if (p->spherical) S.InitSphr();
     }
     H.InitChunks();
     if (nlev > 1) H.ComputeCutoffCoords();
@@ -1459,6 +1738,8 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         for (int lev = 0; lev < nlev; ++lev) w0c[lev].define(H.S[lev].L.ba, 3, 2, -1, 0.0);
         H.Put1dArrayOnCart(H.bs(&Lev::w0), w0c, true, true, &H.bcs_u(), 0, true);
         for (int lev = 0; lev < nlev; ++lev) H.S[lev].w0_cart = std::move(w0c[lev]);
+        if (p->spherical)  // MakeW0mac (Source/MaestroAdvance.cpp:335-338)
+            for (int lev = 0; lev < nlev; ++lev) H.S[lev].MakeW0mac();
     }
     VMF w0_force_cart(nlev);
     for (int lev = 0; lev < nlev; ++lev) w0_force_cart[lev].define(H.S[lev].L.ba, 3, 1, -1, 0.0);

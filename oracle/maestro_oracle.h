@@ -39,6 +39,9 @@ typedef struct {
     int do_eos_h_above_cutoff;
     int base_cutoff_density_coord;
     int dim; /* 3 (or 0) / 2 */
+    int spherical;      /* spherical geometry with the exact (irregular) base state */
+    double prob_lo[3];
+    double prob_hi[3];
 } mo_params;
 
 typedef struct {
