@@ -1,6 +1,7 @@
 // Context, layout, base state and the C ABI of the scalar-advection stage library.
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -269,6 +270,14 @@ static void field_specs(Ctx& c) {
     for (int d = 0; d < 3; ++d) S(F_TRA0 + d, 2, 1, d);
     S(F_TRC, 6, 1);
     S(F_TCOEF, 6, 1);
+    // spherical only (one component each; a planar context allocates them empty)
+    const int ns = c.sph ? 1 : 0;
+    for (int d = 0; d < 3; ++d) {
+        S(F_W0MAC0 + d, ns, 1, d);
+        S(F_S0MAC0 + d, ns, 1, d);
+        S(F_S0MACB0 + d, ns, 1, d);
+    }
+    S(F_S0CART2, ns, 2);
 }
 
 static void free_layout(Ctx& c) {
@@ -401,7 +410,7 @@ static void put1d_h(Hier& H, int fid, const char* s0, int outcomp, int nc, int e
                     int is_vel, int state_c0) {
     for (auto* c : H.L) {
         set_val(*c, fid, 0.0, 0, nc, c->F[fid].spec.ng);
-        put1d(*c, fid, c->b1(s0), outcomp, edge);
+        put1d(*c, fid, c->b1(s0), outcomp, edge, nc == 3);
     }
     average_down_h(H, fid, 0, nc);
     fill_patch_h(H, fid, 0, nc, which_bcs, bc_c0, is_vel, state_c0);
@@ -412,11 +421,21 @@ static void addw0_h(Hier& H, int f0, double mult) {
     sync_faces_h(H, f0);
 }
 
+// Maestro::MakeS0mac, exact base state, s0mac_interp_type 1 (Source/MaestroFill3dData.cpp:712-783):
+// the array injected into cells (two ghosts, FillPatch with bcs_f), averaged to the faces of the
+// nodal boxes grown by one, into dst0 .. dst0 + 2
+static void make_s0mac_h(Hier& H, const char* s0, int dst0) {
+    put1d_h(H, F_S0CART2, s0, 0, 1, 0, BCS_F, 0, 0, -1);
+    for (auto* c : H.L) make_s0mac_faces(*c, dst0);
+}
+
 // ------------------------------------------------------------------ stage pieces
 static void w0_carts(Hier& H) {
     const int nd = H[0].ndim;
     // Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1)  (Source/MaestroAdvance.cpp:326)
     put1d_h(H, F_W0CART, "w0", nd - 1, nd, 1, BCS_U, 0, 1, -1);
+    // MakeW0mac (Source/MaestroAdvance.cpp:335-338)
+    if (H[0].sph) make_w0mac(H[0]);
     // Put1dArrayOnCart(w0_force, w0_force_cart, false, true, bcs_f, 0) (:341), evolve_base_state only
     for (auto* c : H.L) set_val(*c, F_W0FCART, 0.0, 0, 3, 1);
     if (H[0].P.evolve_base_state) put1d_h(H, F_W0FCART, "w0_force", nd - 1, nd, 0, BCS_F, 0, 0, -1);
@@ -455,7 +474,7 @@ static void advance_premac(Hier& H) {
 
 // Maestro::ModifyScalForce (Source/MaestroForce.cpp:261-467)
 static void modify_scal_force_h(Hier& H, int comp, const char* s0_edge, int s0cart_fid, int fullform) {
-    put1d_h(H, F_S0ECART, s0_edge, 0, 1, 0, BCS_F, 0, 0, -1);
+    if (!H[0].sph) put1d_h(H, F_S0ECART, s0_edge, 0, 1, 0, BCS_F, 0, 0, -1);  // planar only (:275-277)
     for (auto* c : H.L) modify_scal_force(*c, comp, s0cart_fid, fullform);
     average_down_h(H, F_SCALFORCE, comp, 1);
     fill_patch_h(H, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
@@ -464,10 +483,13 @@ static void modify_scal_force_h(Hier& H, int comp, const char* s0_edge, int s0ca
 // Maestro::MakeRhoHForce (Source/MaestroForce.cpp:469-679): which_step 1 uses rho0_old and
 // p0_old, which_step 2 their old/new averages (:493-499)
 static void make_rhoh_force_h(Hier& H, int is_prediction, int add_thermal, int which_step) {
-    put1d_h(H, F_P0CART, which_step == 1 ? "p0_old" : "p0_avg", 0, 1, 0, BCS_F, 0, 0, -1);
+    const char* p0n = which_step == 1 ? "p0_old" : "p0_avg";
+    put1d_h(H, F_P0CART, p0n, 0, 1, 0, BCS_F, 0, 0, -1);
+    if (H[0].sph) make_s0mac_h(H, p0n, F_S0MAC0);  // p0mac (Source/MaestroForce.cpp:526-530)
     put1d_h(H, F_PSICART, "psi", 0, 1, 0, BCS_F, 0, 0, -1);
     put1d_h(H, F_RHO0CART, which_step == 1 ? "rho0_old" : "rho0_avg", 0, 1, 0, BCS_S, RHO, 0, RHO);
-    put1d_h(H, F_GRAVCART, "grav_cell", H[0].ndim - 1, H[0].ndim, 0, BCS_F, 0, 0, -1);
+    // the planar force's gravity (MakeGravCell); the spherical force does not read it
+    if (!H[0].sph) put1d_h(H, F_GRAVCART, "grav_cell", H[0].ndim - 1, H[0].ndim, 0, BCS_F, 0, 0, -1);
     for (auto* c : H.L) make_rhoh_force(*c, is_prediction, add_thermal);
     average_down_h(H, F_SCALFORCE, RHOH, 1);
     fill_patch_h(H, F_SCALFORCE, RHOH, 1, BCS_F, 0, 0, RHOH);
@@ -526,6 +548,10 @@ static void density_advance(Hier& H, int which_step) {
     if (spt == 1 || spt == 3) convert_rhox_to_x_h(H, 0);
     const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
     const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
+    if (H[0].sph) {  // rho0 on faces (Source/MaestroDensityAdvance.cpp:167-213)
+        make_s0mac_h(H, "rho0_old", F_S0MAC0);
+        make_s0mac_h(H, r0n, F_S0MACB0);
+    }
     for (auto* c : H.L) make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
     average_down_faces_h(H, F_SFLUX0, 0, nscal);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
@@ -550,6 +576,10 @@ static void enthalpy_advance(Hier& H, int which_step) {
     if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, RHOH, BCS_S, 0);
     const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
     const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
+    if (H[0].sph) {  // rhoh0 on faces, exact base state (Source/MaestroEnthalpyAdvance.cpp:187-220)
+        make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
+        make_s0mac_h(H, rh0n, F_S0MACB0);
+    }
     for (auto* c : H.L) make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en));
     average_down_faces_h(H, F_SFLUX0, 0, nscal);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
@@ -717,6 +747,17 @@ static int init_level(Ctx& c, const madv_params& p, int lev) {
     c.nscal = 4 + p.nspec;
     c.ng_s = c.ng_adv = p.ppm_type == 2 ? 4 : 3;
     c.nr = c.P.dom_hi[c.ndim - 1] - c.P.dom_lo[c.ndim - 1] + 1;
+    c.sph = p.spherical != 0;
+    if (c.sph) {
+        // nr_fine = nr_irreg + 1 (Source/MaestroSetup.cpp:66-82)
+        const double domhi = c.P.dom_hi[0] + 1;
+        c.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
+        for (int d = 0; d < 3; ++d) {
+            c.geo.plo[d] = p.prob_lo[d];
+            c.geo.dx[d] = c.P.dx[d];
+            c.geo.ctr[d] = 0.5 * (p.prob_lo[d] + p.prob_hi[d]);
+        }
+    }
     for (int d = 0; d < 3; ++d) c.per[d] = c.P.phys_bc_lo[d] == PB_INTERIOR;
     int rc = bc_setup(c);
     if (rc) return rc;
@@ -799,6 +840,7 @@ static int layout_level(Ctx& c, int nboxes, const madv_box* boxes, bool cover) {
                 tot += n * s.ncomp;
             }
             c.F[f].bytes = tot * sizeof(double);
+            if (tot == 0) continue;  // a field this context does not use
             if (!cuda_ok(cudaMalloc(&c.F[f].base, c.F[f].bytes), "cudaMalloc(field)")) throw Fail{MADV_ERR_CUDA};
             if (!cuda_ok(cudaMemset(c.F[f].base, 0, c.F[f].bytes), "cudaMemset")) throw Fail{MADV_ERR_CUDA};
         }
@@ -918,8 +960,12 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
         set_error("species_pred_type must be 1..3, enthalpy_pred_type 0 or 1");
         return MADV_ERR_UNSUPPORTED;
     }
-    if (p->ppm_trace_forces != 0 || p->use_exact_base_state != 0) {
-        set_error("ppm_trace_forces and use_exact_base_state must be 0");
+    if (p->spherical && (p->use_exact_base_state != 1 || p->dim == 2 || p->enthalpy_pred_type != 1)) {
+        set_error("spherical geometry needs use_exact_base_state = 1, 3-D and enthalpy_pred_type 1");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    if (p->ppm_trace_forces != 0 || (p->use_exact_base_state != 0 && !p->spherical)) {
+        set_error("ppm_trace_forces must be 0; use_exact_base_state needs spherical geometry");
         return MADV_ERR_UNSUPPORTED;
     }
     if (!(p->dt > 0.0) || !(p->rel_eps >= 0.0)) {
@@ -993,6 +1039,10 @@ int madv_set_dt(madv_ctx* h, double dt, double rel_eps) {
 }
 
 int madv_set_layout_levels(madv_ctx* h, int nlev, const int* nboxes, const madv_box* boxes) {
+    if (h && h->c.sph && nlev > 1) {
+        set_error("spherical geometry: one level");
+        return MADV_ERR_UNSUPPORTED;
+    }
     if (!h || nlev < 1 || !nboxes || !boxes) return MADV_ERR_PARAM;
     if (nlev > 2 || (nlev > 1 && h->c.ndim == 2)) {
         set_error("at most two levels (refinement ratio 2), one in 2-D");
@@ -1081,6 +1131,18 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
             }
             c.h1[a.name] = std::vector<double>(a.p, a.p + a.n);
         }
+    }
+    // spherical: radii of the exact radial grid (Source/BaseStateGeometry.cpp:86-96), r_cc_loc
+    // continued one bin past the last (Put1dArrayOnCart reads r_cc_loc(nr_fine))
+    for (int l = 0; l < nlev; ++l) {
+        Ctx& c = H[l];
+        if (!c.sph) continue;
+        std::vector<double> rc(c.nr + 1), re(c.nr + 1, 0.0);
+        const double dxf = c.P.dx[0];
+        for (int i = 0; i <= c.nr; ++i) rc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
+        for (int i = 0; i < c.nr; ++i) re[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
+        c.h1["r_cc_loc"] = rc;
+        c.h1["r_edge_loc"] = re;
     }
     // which_step 2 averages of MakeRhoHForce: 0.5 * (old + new) (Source/MaestroForce.cpp:496-497)
     for (int l = 0; l < nlev; ++l) {

@@ -18,6 +18,13 @@ struct Fail {
     int code;
 };
 
+// Full-star spherical geometry: cell (i,j,k) sits at prob_lo + (i + 1/2) dx - centre
+// (Source/MaestroFill3dData.cpp:103-110); cells map to the radial bin
+// round(r^2 / (2 dx^2) - 3/8) of the exact base state (Source/MaestroBaseStateGeometry.cpp:24-35).
+struct SphGeo {
+    double plo[3], dx[3], ctr[3];
+};
+
 struct HBox {
     int lo[3];
     int hi[3];
@@ -44,6 +51,10 @@ enum FieldId {
     F_TRA0, F_TRA1, F_TRA2,        // tracing coefficients (A, B) per D-face of umac
     F_TRC,                         // tracing coefficients per cell of ufull (A_d, B_d)
     F_TCOEF,                       // transverse coefficients per cell (dt6: 0-2, dt4: 3-5)
+    F_W0MAC0, F_W0MAC1, F_W0MAC2,  // spherical: w0 on faces (MakeW0mac)
+    F_S0CART2,                     // spherical: a base-state array on cells, two ghosts (MakeS0mac)
+    F_S0MAC0, F_S0MAC1, F_S0MAC2,  // spherical: base state on faces (MakeS0mac), old
+    F_S0MACB0, F_S0MACB1, F_S0MACB2,  //   and new
     F_USER,                        // first slot of per-call views of caller FABs
     NF_INTERNAL = F_USER
 };
@@ -89,6 +100,8 @@ struct Ctx {
     madv_params P{};  // dx, domain and base_cutoff_density_coord are this level's
     int lev = 0;
     int ndim = 3;     // 2: the 2-D form (y radial, k = 0 only, regions never grow in z)
+    bool sph = false; // spherical geometry, exact base state (one level)
+    SphGeo geo{};
     int nspec = 0, nscal = 0, ng_s = 3, ng_adv = 3, nr = 0;
     bool per[3] = {false, false, false};
     std::vector<HBox> ba;
@@ -170,7 +183,7 @@ void addw0(Ctx& c, int f0, double mult);
 void set_val(Ctx& c, int fid, double v, int c0, int nc, int ngrow);
 void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow);
 void add_fab(Ctx& c, int dst, int src, int nc, int ngrow);
-void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge);
+void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec = 0);
 void make_utrans(Ctx& c);
 void make_vel_force(Ctx& c);  // valid cells; F_GRAVCART / F_RHO0CART filled by the caller
 void vel_pred(Ctx& c);
@@ -190,6 +203,18 @@ int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int
                 const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
                 const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
+
+// ---- spherical forms (madv_sphr.cu), reached through the wrappers above when c.sph
+void put1d_sph(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec);
+void make_w0mac(Ctx& c);
+void make_s0mac_faces(Ctx& c, int dst0);  // faces of F_S0CART2 into dst0 .. dst0 + 2
+void addw0_sph(Ctx& c, int f0, double mult);
+void make_vel_force_sph(Ctx& c);
+void modify_scal_force_sph(Ctx& c, int comp, int s0cart_fid, int fullform);
+void make_rhoh_force_sph(Ctx& c, int is_prediction, int add_thermal);
+void put_in_pert_form_sph(Ctx& c, const double* d_s0, int comp, int flag);
+void make_rhox_flux_sph(Ctx& c);
+void make_rhoh_flux_sph(Ctx& c);
 
 // ---- 2-D forms (madv_kernels.cu), reached through the wrappers above when c.ndim == 2
 void put1d_2d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge);

@@ -60,8 +60,9 @@ __global__ void k_put1d(KARGS, int f, const double* __restrict__ s0, int outcomp
     at(VW(f), i, j, k, outcomp) = edge ? 0.5 * (s0[r] + s0[r + 1]) : s0[r];
 }
 
-void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge) {
+void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec) {
     if (c.ndim == 2) return put1d_2d(c, fid, d_s0, outcomp, edge);
+    if (c.sph) return put1d_sph(c, fid, d_s0, outcomp, edge, vec);
     launch(c, rg_grow(c, 0), 1, k_put1d, c.V(), fid, d_s0, outcomp, edge);
 }
 
@@ -238,6 +239,7 @@ __global__ void k_addw0(KARGS, int f, const double* __restrict__ w0, double mult
 }
 
 void addw0(Ctx& c, int f0, double mult) {
+    if (c.sph) return addw0_sph(c, f0, mult);
     if (c.ndim == 2) return addw0_2d(c, f0, mult);
     launch(c, region(c, 1, 1, 0, 1, 1, 0, 2), 1, k_addw0, c.V(), f0 + 2, (const double*)c.b1("w0"), mult);
 }
@@ -558,7 +560,8 @@ void edge_scal_coeffs(Ctx& c) {
 // utilde component D along D (ufull tracing) is the same sweep VelPred needs, so it is
 // stored where VelPred reads it (F_IPC0+D / F_IMC0+D, comp D) and not repeated there.
 template <int D>
-__global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+__global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, int domlo, int domhi, double rel_eps,
+                         int sph) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
@@ -589,12 +592,13 @@ __global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, 
         }
     }
     double v;
-    if (D < 2) {
+    if (D < 2 && !sph) {
         const bool test = (l <= 0.0 && r >= 0.0) || (fabs(l + r) < rel_eps);
         v = 0.5 * (l + r) > 0.0 ? l : r;
         v = test ? 0.0 : v;
     } else {
-        const double w0c = at(VW(F_W0CART), i, j, k, 2);
+        // planar z: the full velocity w + w0_cart; spherical (:368-377): + w0mac in every direction
+        const double w0c = sph ? at(VW(F_W0MAC0 + D), i, j, k) : at(VW(F_W0CART), i, j, k, 2);
         const bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fabs(l + r + 2.0 * w0c) < rel_eps);
         v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
         v = test ? 0.0 : v;
@@ -616,9 +620,10 @@ void make_utrans(Ctx& c) {
         const RegionTable& rt = rg_grow(c, 0, d);
         const double dt2dx = dt2 / c.P.dx[d];
         const int bl = c.P.phys_bc_lo[d], bh = c.P.phys_bc_hi[d], dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
-        if (d == 0) launch(c, rt, 1, k_utrans<0>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
-        else if (d == 1) launch(c, rt, 1, k_utrans<1>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
-        else launch(c, rt, 1, k_utrans<2>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+        const int sph = c.sph;
+        if (d == 0) launch(c, rt, 1, k_utrans<0>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps, sph);
+        else if (d == 1) launch(c, rt, 1, k_utrans<1>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps, sph);
+        else launch(c, rt, 1, k_utrans<2>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps, sph);
     }
 }
 
@@ -642,6 +647,7 @@ __global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz) {
 
 // valid cells of one level; F_GRAVCART and F_RHO0CART are filled by the caller
 void make_vel_force(Ctx& c) {
+    if (c.sph) return make_vel_force_sph(c);
     if (c.ndim == 2) return make_vel_force_2d(c);
     set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
     launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
@@ -768,7 +774,7 @@ __global__ void k_vp_transverse(KARGS, int bclo, int bchi, int domlo, int domhi,
 // VelPredVelocities (Source/MaestroVelPred.cpp:1597-1915).  F_TCOEF comps 3..5 hold
 // (dt4/h_t)*(trans_t sum).
 template <int D>
-__global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo, int domhi, double rel_eps) {
+__global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo, int domhi, double rel_eps, int sph) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -790,12 +796,13 @@ __global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo
                       at(tc, i, j, k, 3 + T2) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
                       dt2 * fr;
     double v;
-    if (D < 2) {
+    if (D < 2 && !sph) {
         const bool test = (ml <= 0.0 && mr >= 0.0) || (fabs(ml + mr) < rel_eps);
         v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
         v = test ? 0.0 : v;
     } else {
-        const double w0c = at(VW(F_W0CART), i, j, k, 2);
+        // spherical (Source/MaestroVelPred.cpp:1664-1673): + w0mac in every direction
+        const double w0c = sph ? at(VW(F_W0MAC0 + D), i, j, k) : at(VW(F_W0CART), i, j, k, 2);
         const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fabs(ml + mr + 2.0 * w0c) < rel_eps);
         v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
         v = test ? 0.0 : v;
@@ -842,7 +849,7 @@ static void vp_interface_launch(Ctx& c) {
 template <int D>
 static void vp_velocities_launch(Ctx& c) {
     launch(c, rg_grow(c, 0, D), 1, k_vp_velocities<D>, c.V(), 0.5 * c.P.dt, c.P.phys_bc_lo[D], c.P.phys_bc_hi[D],
-           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps);
+           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps, (int)c.sph);
 }
 
 void vel_pred(Ctx& c) {
@@ -1121,6 +1128,7 @@ __global__ void k_modify_scal_force(KARGS, int comp, int s0cart, int fullform, R
 
 // valid cells of one level; F_S0ECART and the s0 cart field are filled by the caller
 void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform) {
+    if (c.sph) return modify_scal_force_sph(c, comp, s0cart_fid, fullform);
     if (c.ndim == 2) return modify_scal_force_2d(c, comp, s0cart_fid, fullform);
     launch(c, rg_grow(c, 0), 1, k_modify_scal_force, c.V(), comp, s0cart_fid, fullform, make_recip(c.P.dx[0]),
            make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
@@ -1149,6 +1157,7 @@ __global__ void k_rhoh_force(KARGS, int cutoff, int domhi, RecipC rdz, int psi_i
 // valid cells of one level; F_P0CART, F_PSICART, F_RHO0CART and F_GRAVCART are filled by
 // the caller (which_step 1: rho0_old and p0_old)
 void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal) {
+    if (c.sph) return make_rhoh_force_sph(c, is_prediction, add_thermal);
     if (c.ndim == 2) return make_rhoh_force_2d(c, is_prediction, add_thermal);
     const int ept = c.P.enthalpy_pred_type;
     const int psi_in = (is_prediction == 1 && ept == 2) || (is_prediction == 1 && ept == 0) || (is_prediction == 0);
@@ -1165,6 +1174,7 @@ __global__ void k_pert(KARGS, int comp, const double* __restrict__ s0, int flag)
 }
 
 void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag) {
+    if (c.sph) return put_in_pert_form_sph(c, d_s0, comp, flag);
     if (c.ndim == 2) return put_in_pert_form_2d(c, d_s0, comp, flag);
     launch(c, rg_grow(c, 0), 1, k_pert, c.V(), comp, d_s0, flag);
 }
@@ -1212,6 +1222,7 @@ __global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double*
 }
 
 void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new, const double* r0e_new) {
+    if (c.sph) return make_rhox_flux_sph(c);  // face base state from MakeS0mac (F_S0MAC*, F_S0MACB*)
     if (c.ndim == 2) return make_rhox_flux_2d(c, r0_old, r0e_old, r0_new, r0e_new);
     const int do_eta = c.P.evolve_base_state && !c.P.use_exact_base_state;
     const double* w0 = c.b1("w0");
@@ -1240,6 +1251,7 @@ __global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const 
 
 void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
                     const double* rh0e_new) {
+    if (c.sph) return make_rhoh_flux_sph(c);
     if (c.ndim == 2) return make_rhoh_flux_2d(c, rh0_old, rh0e_old, rh0_new, rh0e_new);
     const int ept = c.P.enthalpy_pred_type;
     launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux<0>, c.V(), ept, rh0_old, rh0_new);
@@ -1402,7 +1414,7 @@ static void make_utrans_2d(Ctx& c) {
         const RegionTable& rt = rg2(c, 0, d);
         const double dt2dx = dt2 / c.P.dx[d];
         const int bl = c.P.phys_bc_lo[d], bh = c.P.phys_bc_hi[d], dl = c.P.dom_lo[d], dh = c.P.dom_hi[d];
-        if (d == 0) launch(c, rt, 1, k_utrans<0>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
+        if (d == 0) launch(c, rt, 1, k_utrans<0>, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps, 0);
         else launch(c, rt, 1, k_utrans_2dy, c.V(), c.P.ppm_type, dt2dx, bl, bh, dl, dh, c.P.rel_eps);
     }
 }

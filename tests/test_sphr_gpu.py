@@ -1,0 +1,48 @@
+"""GPU parity of the spherical stage (full star, exact base state) against the oracle's
+restatement of the reference's spherical branches: every output within 1e-12 of its
+max-norm, in practice bitwise."""
+import numpy as np
+import pytest
+
+import pyoracle
+from maestroex_gb300 import capi, configs
+from maestroex_gb300.configs import uneven_boxes
+from test_parity_gpu import compare
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from maestroex_gb300 import build
+    build.build_library()
+
+
+def run_both(cfg, mode=capi.MODE_BATCHED):
+    from maestroex_gb300.stage import run_stage_gpu
+    return run_stage_gpu(cfg, mode=mode), pyoracle.run_stage(cfg, checked=False)
+
+
+@pytest.mark.parametrize("ppm_type", [1, 2, 0])
+def test_spherical_stage(ppm_type):
+    cfg = configs.spherical_config(n=32, max_grid=16, ppm_type=ppm_type)
+    gpu, ref = run_both(cfg)
+    worst, bitwise = compare(cfg, gpu, ref, f"spherical ppm{ppm_type}")
+    assert bitwise, worst
+
+
+def test_spherical_uneven_boxes_and_graph():
+    rng = np.random.default_rng(11)
+    boxes = uneven_boxes((48, 48, 48), (8, 16, 24), rng)
+    cfg = configs.spherical_config(n=48, boxes=boxes, ppm_type=2, nspec=5)
+    gpu, ref = run_both(cfg, mode=capi.MODE_GRAPH)
+    worst, bitwise = compare(cfg, gpu, ref, "spherical uneven")
+    assert bitwise, worst
+
+
+def test_spherical_rejects_several_levels():
+    from maestroex_gb300.stage import make_stage
+    cfg = configs.spherical_config(n=16, max_grid=16)
+    st = make_stage(cfg)
+    with pytest.raises(capi.MadvError):
+        st.set_layout_levels([cfg["boxes"], [(8, 8, 8, 15, 15, 15)]])
