@@ -376,6 +376,60 @@ def run_adjoint(args, barrier):
     }
 
 
+def run_spherical(args, barrier):
+    """Full-star spherical workload (config 5 geometry, one level): n^3 cells in boxes of 64^3,
+    NumSpec 21, ppm_type 2, exact base state on the irregular radial grid, polytrope star,
+    outflow faces; graph-replayed stage vs one launch per box."""
+    import torch
+    from maestroex_gb300 import capi, configs
+    from maestroex_gb300.stage import StageBuffers, make_stage
+    n = args.sph_n
+    cfg = configs.spherical_config(n=n, max_grid=64, nspec=21, ppm_type=2)
+    st = make_stage(cfg)
+    buf = StageBuffers(cfg).load(cfg)
+    snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
+
+    def reset():
+        for name, ts in snap.items():
+            for dst, src in zip(getattr(buf, name).fabs, ts):
+                dst.copy_(src)
+
+    def timed(mode, reps):
+        for _ in range(2):
+            reset()
+            st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                             thermal=buf.thermal, mode=mode)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for _ in range(reps):
+            reset()
+            torch.cuda.synchronize()
+            e0.record()
+            st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                             thermal=buf.thermal, mode=mode)
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps, st.launch_count()
+
+    reps = max(1, args.steps // 2)
+    ms_graph, l_graph = timed(capi.MODE_GRAPH, reps)
+    out_graph = torch.cat([f.flatten() for f in buf.snew.fabs])
+    ms_box, l_box = timed(capi.MODE_PER_BOX, reps)
+    same = bool(torch.equal(out_graph, torch.cat([f.flatten() for f in buf.snew.fabs])))
+    ncell = n ** 3
+    st.close()
+    del buf, snap
+    torch.cuda.empty_cache()
+    return {"workload": f"spherical full star {n}^3 in {len(cfg['boxes'])} boxes of 64^3, one level, NumSpec 21, "
+                        f"ppm_type 2, exact base state ({cfg['nr']} radial bins), n = 1.5 polytrope, outflow",
+            "unit": UNIT,
+            "graph": {"value": ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": l_graph},
+            "per_box": {"value": ncell / (ms_box * 1e-3), "ms_per_step": ms_box, "gpu_launches": l_box},
+            "identical_results_graph_vs_per_box": same}
+
+
 def run_2d(args, barrier):
     """2-D workload: one 256 x 256 box, NumSpec 3, ppm_type 1 (the reference's 2-D build),
     graph-replayed stage."""
@@ -449,6 +503,8 @@ def main():
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one adjoint call (state and velocity gradients) and exit (the command ncu captures)")
     ap.add_argument("--no-2d", action="store_true")
+    ap.add_argument("--sph-n", type=int, default=256, help="extent of the spherical workload")
+    ap.add_argument("--no-spherical", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
     args = ap.parse_args()
@@ -592,6 +648,7 @@ def main():
         amr = run_amr(args, ws, max(1, args.steps // 2), warmup, barrier)
     adj = None if args.no_adjoint else run_adjoint(args, barrier)
     two_d = None if args.no_2d else run_2d(args, barrier)
+    sph = None if args.no_spherical else run_spherical(args, barrier)
 
     if rank != 0:
         dist.destroy_process_group()
@@ -632,6 +689,8 @@ def main():
         line["adjoint"] = adj
     if two_d is not None:
         line["two_d"] = two_d
+    if sph is not None:
+        line["spherical"] = sph
     if not args.no_cpu_baseline:
         cb = run_cpu_baseline(1, 0)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
