@@ -241,23 +241,26 @@ def lane_emden(n_poly=1.5, h=1.0e-4):
 
 
 def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20261203 + 5, cfl=0.5,
-                     rho_c=2.0e9, w0_amp=1.0e5, u_amp=1.0e6, L=5.0e8, pert=1.0e-9):
+                     rho_c=2.0e9, w0_amp=1.0e5, u_amp=1.0e6, L=5.0e8, pert=1.0e-9, n_base=None):
     """Full-star spherical configuration with the exact base state: an n^3 Cartesian domain
     [0, L]^3 with the star at its centre, outflow on every face; an n = 1.5 polytrope of
     central density rho_c and radius 0.9 L/2 (Lane-Emden, integrated here) on the irregular
     radial grid r_cc(i) = sqrt(0.75 + 2i) dx, with a constant ambient density 1e-5 rho_c
     outside; w0 on the radial edges a seeded smooth profile of amplitude w0_amp, zero at
-    the centre and outside the star; a seeded smooth velocity of amplitude u_amp tapered to
+    the centre and beyond 0.8 of the radius; a seeded smooth velocity of amplitude u_amp tapered to
     zero at 0.8 of the radius; density and enthalpy perturbed by `pert` (relative);
     base_cutoff_density half the ambient density, so the buoyancy cutoff (5x) covers the
-    ambient."""
+    ambient.  n_base: extent of the finest level of a hierarchy, whose cell size sets the
+    radial grid (default n)."""
     rng = np.random.default_rng(seed)
     n3 = (n, n, n)
     dx = L / n
-    nr_irreg = int((3.0 * (n / 2 - 0.5) * (n / 2 - 0.5) - 0.75) / 2.0)
+    nb = n if n_base is None else n_base
+    dxb = L / nb
+    nr_irreg = int((3.0 * (nb / 2 - 0.5) * (nb / 2 - 0.5) - 0.75) / 2.0)
     nr = nr_irreg + 1
-    r_cc = np.sqrt(0.75 + 2.0 * np.arange(nr)) * dx
-    r_edge = np.concatenate([[0.0], np.sqrt(0.75 + 2.0 * (np.arange(nr) + 0.5)) * dx])
+    r_cc = np.sqrt(0.75 + 2.0 * np.arange(nr)) * dxb
+    r_edge = np.concatenate([[0.0], np.sqrt(0.75 + 2.0 * (np.arange(nr) + 0.5)) * dxb])
     npoly, gamma = 1.5, 5.0 / 3.0
     xi, theta = lane_emden(npoly)
     R = 0.9 * 0.5 * L
@@ -274,9 +277,9 @@ def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20
     menc = np.cumsum(rho0 * shell) - 0.5 * rho0 * shell
     grav = -G * menc / r_cc ** 2
     w0 = np.zeros(nr + 1)
-    inside = r_edge < R
+    inside = r_edge < 0.8 * R
     for m in range(1, 4):
-        w0[inside] += rng.normal() * np.sin(m * math.pi * r_edge[inside] / R)
+        w0[inside] += rng.normal() * np.sin(m * math.pi * r_edge[inside] / (0.8 * R))
     w0 *= w0_amp / max(np.abs(w0).max(), 1e-300)
     w0[0] = 0.0
 
@@ -284,7 +287,7 @@ def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20
     c = (np.arange(n) + 0.5) * dx - 0.5 * L
     X3, Y3, Z3 = c[None, None, :], c[None, :, None], c[:, None, None]
     r2 = X3 * X3 + Y3 * Y3 + Z3 * Z3
-    idx = np.floor(r2 / (2.0 * dx * dx) - 0.375 + 0.5).astype(np.int64)
+    idx = np.floor(r2 / (2.0 * dxb * dxb) - 0.375 + 0.5).astype(np.int64)
     shape = (n, n, n)
     periodic = [False, False, False]
     rho = rho0[idx] * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
@@ -324,6 +327,39 @@ def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20
         p0_old=p0.copy(), p0_new=p0.copy(), psi=np.zeros(nr), grav_cell=grav, w0_force=np.zeros(nr), w0=w0,
         rho0_predicted_edge=cell_to_edge(rho0),
     )
+
+
+def spherical_amr_config(n0=32, nspec=3, ppm_type=2, max_grid=16, fine_boxes=None, seed=20261203 + 6,
+                         cover=0.12, inject=False, level0_boxes=None, **kw):
+    """Two-level spherical configuration (refinement ratio 2) on one radial grid set by the
+    fine level.  Level 1: seeded boxes (bubble_boxes) covering about `cover` of the
+    domain.  inject=False: both levels are the same star evaluated at their resolution,
+    level-0 cells under level 1 holding the average of their children; inject=True:
+    level-1 cells take their parent's values (filled on the device by stage.amr_buffers),
+    for sizes whose fine level cannot be evaluated on the whole domain.  dt is the
+    fine level's."""
+    n1 = 2 * n0
+    rng = np.random.default_rng(seed + 100)
+    if fine_boxes is None:
+        fine_boxes = bubble_boxes((n0, n0, n0), nbubbles=3, cover=cover, block_edges=(8, 16, 24, 32), max_edge=32,
+                                  rng=rng)
+    c0 = spherical_config(n=n0, nspec=nspec, ppm_type=ppm_type, max_grid=max_grid, boxes=level0_boxes, seed=seed,
+                          n_base=n1, **kw)
+    if inject:
+        lev1 = dict(n=(n1,) * 3, dx=tuple(v / 2 for v in c0["dx"]), boxes=list(fine_boxes), inject=True)
+        for k in LEVEL_KEYS:
+            if k not in lev1 and k not in ("uold", "sold", "gpi", "thermal"):
+                lev1[k] = c0[k]
+        c0["dt"] *= 0.5
+    else:
+        c1 = spherical_config(n=n1, nspec=nspec, ppm_type=ppm_type, boxes=list(fine_boxes), seed=seed, **kw)
+        for key in ("sold", "uold", "gpi"):
+            _average_down(c1[key], c0[key], fine_boxes)
+        c0["dt"] = min(c0["dt"], c1["dt"])
+        c0["rel_eps"] = max(c0["rel_eps"], c1["rel_eps"])
+        lev1 = {k: c1[k] for k in LEVEL_KEYS}
+    c0["levels"] = [{k: c0[k] for k in LEVEL_KEYS}, lev1]
+    return c0
 
 
 def bubble_boxes(n0, nbubbles=3, cover=0.12, block_edges=(8, 16, 32), rng=None, max_edge=32):

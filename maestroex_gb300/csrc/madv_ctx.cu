@@ -435,7 +435,8 @@ static void w0_carts(Hier& H) {
     // Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1)  (Source/MaestroAdvance.cpp:326)
     put1d_h(H, F_W0CART, "w0", nd - 1, nd, 1, BCS_U, 0, 1, -1);
     // MakeW0mac (Source/MaestroAdvance.cpp:335-338)
-    if (H[0].sph) make_w0mac(H[0]);
+    if (H[0].sph)
+        for (auto* c : H.L) make_w0mac(*c);
     // Put1dArrayOnCart(w0_force, w0_force_cart, false, true, bcs_f, 0) (:341), evolve_base_state only
     for (auto* c : H.L) set_val(*c, F_W0FCART, 0.0, 0, 3, 1);
     if (H[0].P.evolve_base_state) put1d_h(H, F_W0FCART, "w0_force", nd - 1, nd, 0, BCS_F, 0, 0, -1);
@@ -757,6 +758,7 @@ static int init_level(Ctx& c, const madv_params& p, int lev) {
             c.geo.dx[d] = c.P.dx[d];
             c.geo.ctr[d] = 0.5 * (p.prob_lo[d] + p.prob_hi[d]);
         }
+        c.geo.dxf = c.P.dx[0];  // the finest level's, set again with the layout's levels
     }
     for (int d = 0; d < 3; ++d) c.per[d] = c.P.phys_bc_lo[d] == PB_INTERIOR;
     int rc = bc_setup(c);
@@ -1039,10 +1041,6 @@ int madv_set_dt(madv_ctx* h, double dt, double rel_eps) {
 }
 
 int madv_set_layout_levels(madv_ctx* h, int nlev, const int* nboxes, const madv_box* boxes) {
-    if (h && h->c.sph && nlev > 1) {
-        set_error("spherical geometry: one level");
-        return MADV_ERR_UNSUPPORTED;
-    }
     if (!h || nlev < 1 || !nboxes || !boxes) return MADV_ERR_PARAM;
     if (nlev > 2 || (nlev > 1 && h->c.ndim == 2)) {
         set_error("at most two levels (refinement ratio 2), one in 2-D");
@@ -1057,6 +1055,18 @@ int madv_set_layout_levels(madv_ctx* h, int nlev, const int* nboxes, const madv_
         if (rc) return rc;
     }
     Hier H = h->H();
+    if (h->c.sph) {
+        // one radial grid for every level, set by the finest level (Source/MaestroSetup.cpp:60-82,
+        // Source/BaseStateGeometry.cpp:86-96): nr_fine = nr_irreg + 1 and its cell size
+        const Ctx& fl = H[nlev - 1];
+        const double domhi = fl.P.dom_hi[0] + 1;
+        const int nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
+        for (auto* c : H.L) {
+            c->nr = nr;
+            c->geo.dxf = fl.P.dx[0];
+            c->have_base = false;
+        }
+    }
     int off = 0;
     for (int l = 0; l < nlev; ++l) {
         if (nboxes[l] <= 0) {
@@ -1114,7 +1124,8 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
     }
     for (int l = 0; l < nlev; ++l) {
         Ctx& c = H[l];
-        const madv_base_state* bs = &bsl[l];
+        // spherical: one radial base state (max_radial_level = 0) that every level reads
+        const madv_base_state* bs = c.sph ? &bsl[0] : &bsl[l];
         const int nr = c.nr;
         struct Arr1 {
             const char* name;
@@ -1138,7 +1149,7 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
         Ctx& c = H[l];
         if (!c.sph) continue;
         std::vector<double> rc(c.nr + 1), re(c.nr + 1, 0.0);
-        const double dxf = c.P.dx[0];
+        const double dxf = c.geo.dxf;
         for (int i = 0; i <= c.nr; ++i) rc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
         for (int i = 0; i < c.nr; ++i) re[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
         c.h1["r_cc_loc"] = rc;

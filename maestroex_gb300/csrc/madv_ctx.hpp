@@ -18,11 +18,13 @@ struct Fail {
     int code;
 };
 
-// Full-star spherical geometry: cell (i,j,k) sits at prob_lo + (i + 1/2) dx - centre
-// (Source/MaestroFill3dData.cpp:103-110); cells map to the radial bin
-// round(r^2 / (2 dx^2) - 3/8) of the exact base state (Source/MaestroBaseStateGeometry.cpp:24-35).
+// Full-star spherical geometry: cell (i,j,k) of a level sits at prob_lo + (i + 1/2) dx - centre
+// (Source/MaestroFill3dData.cpp:103-110); cells of every level map to the radial bin
+// round(r^2 / (2 dxf^2) - 3/8) of the exact base state, dxf the finest cell size
+// (Source/MaestroBaseStateGeometry.cpp:24-35).
 struct SphGeo {
     double plo[3], dx[3], ctr[3];
+    double dxf;  // cell size of the finest level, which sets the radial grid
 };
 
 struct HBox {

@@ -1,6 +1,7 @@
-// Full-star spherical geometry of the stage with the exact base state (3-D, one level):
-// the irregular radial grid r_cc(i) = sqrt(0.75 + 2i) dx, r_edge(i+1) = sqrt(0.75 +
-// 2(i + 1/2)) dx (Source/BaseStateGeometry.cpp:86-96), the cell-to-bin map, and the
+// Full-star spherical geometry of the stage with the exact base state (3-D, one or two
+// levels sharing one radial grid): r_cc(i) = sqrt(0.75 + 2i) dxf, r_edge(i+1) = sqrt(0.75 +
+// 2(i + 1/2)) dxf with dxf the finest cell size (Source/BaseStateGeometry.cpp:86-96), the
+// cell-to-bin map, and the
 // spherical branches of Put1dArrayOnCart, MakeW0mac, MakeS0mac, Addw0, MakeVelForce,
 // ModifyScalForce, MakeRhoHForce, PutInPertForm, MakeRhoXFlux and MakeRhoHFlux.  The
 // MakeUtrans / VelPred Riemann solves with w0mac are flags of their kernels in
@@ -20,7 +21,7 @@ __device__ __forceinline__ void sph_xyz(const SphGeo& g, int i, int j, int k, do
 __device__ __forceinline__ int sph_bin(const SphGeo& g, int i, int j, int k) {
     double x, y, z;
     sph_xyz(g, i, j, k, x, y, z);
-    const double index = (x * x + y * y + z * z) / (2.0 * g.dx[0] * g.dx[0]) - 0.375;
+    const double index = (x * x + y * y + z * z) / (2.0 * g.dxf * g.dxf) - 0.375;
     return (int)round(index);
 }
 

@@ -45,12 +45,12 @@ struct Lev {
     // Full-star geometry with the exact base state: centre, radii of the irregular radial
     // grid (Source/BaseStateGeometry.cpp:86-96) and w0 on faces (MakeW0mac).
     double center[3] = {0.0, 0.0, 0.0};
+    double dxf = 0.0;  // finest cell size: it sets the radial grid of every level
     std::vector<double> r_cc_loc, r_edge_loc;
     MF w0mac[3];
 
     void InitSphr() {
         for (int d = 0; d < 3; ++d) center[d] = 0.5 * (P.prob_lo[d] + P.prob_hi[d]);
-        const double dxf = L.dx[0];
         // one radius past the last cell: Put1dArrayOnCart reads r_cc_loc(nr_fine) for the
         // outermost cells (Source/MaestroFill3dData.cpp:115-118, past its array); the
         // same formula continued
@@ -69,7 +69,7 @@ struct Lev {
     int cc_to_r(int i, int j, int k) const {
         double x, y, z;
         sph_xyz(i, j, k, x, y, z);
-        const double index = (x * x + y * y + z * z) / (2.0 * L.dx[0] * L.dx[0]) - 0.375;
+        const double index = (x * x + y * y + z * z) / (2.0 * dxf * dxf) - 0.375;
         return (int)std::round(index);
     }
     // Put1dArrayOnCart, spherical, exact base state (Source/MaestroFill3dData.cpp:94-192):
@@ -1660,7 +1660,6 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
     if (p->use_exact_base_state && !p->spherical) throw std::runtime_error("use_exact_base_state is spherical-only");
     if (p->spherical) {
         if (!p->use_exact_base_state) throw std::runtime_error("spherical needs use_exact_base_state = 1");
-        if (nlev != 1) throw std::runtime_error("spherical: one level");
         if (p->enthalpy_pred_type != 1) throw std::runtime_error("spherical: enthalpy_pred_type 1");
     }
     if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
@@ -1702,9 +1701,11 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         S.nb = nboxes[lev];
         S.nr = S.L.dom.hi[2] - S.L.dom.lo[2] + 1;
         if (p->spherical) {
-            // nr_fine = nr_irreg + 1 (Source/MaestroSetup.cpp:66-82)
-            const double domhi = S.L.dom.hi[0] + 1;
+            // nr_fine = nr_irreg + 1 from the finest level (Source/MaestroSetup.cpp:60-82)
+            const int rf = 1 << (nlev - 1);
+            const double domhi = (p->dom_hi[0] + 1) * rf;
             S.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
+            S.dxf = p->dx[0] / rf;
         }
         S.ng_s = S.ng_adv = H.ng_s;
         S.dt = p->dt;
@@ -1713,7 +1714,7 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         S.BCSetup();
         const int nr = S.nr;
         auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
-        const mo_inputs& I = in[lev];
+        const mo_inputs& I = p->spherical ? in[0] : in[lev];  // spherical: one radial base state
         S.rho0_old = vec(I.rho0_old, nr);
         S.rho0_new = vec(I.rho0_new, nr);
         S.rhoh0_old = vec(I.rhoh0_old, nr);

@@ -40,9 +40,16 @@ def test_spherical_uneven_boxes_and_graph():
     assert bitwise, worst
 
 
-def test_spherical_rejects_several_levels():
-    from maestroex_gb300.stage import make_stage
-    cfg = configs.spherical_config(n=16, max_grid=16)
-    st = make_stage(cfg)
-    with pytest.raises(capi.MadvError):
-        st.set_layout_levels([cfg["boxes"], [(8, 8, 8, 15, 15, 15)]])
+@pytest.mark.parametrize("ppm_type", [2, 1])
+def test_spherical_two_levels(ppm_type):
+    """Two levels on one radial grid (the fine level's): every level maps its cells to the
+    fine radial bins; coarse-fine coupling as in the plane-parallel hierarchy."""
+    from maestroex_gb300.stage import run_amr_stage_gpu
+    from test_amr_gpu import compare_levels
+    fine = configs.bubble_boxes((32, 32, 32), nbubbles=3, cover=0.12, block_edges=(4, 8), max_edge=8,
+                                rng=np.random.default_rng(5))
+    cfg = configs.spherical_amr_config(n0=32, max_grid=16, ppm_type=ppm_type, fine_boxes=fine)
+    assert len(fine) > 1
+    gpu = run_amr_stage_gpu(cfg, mode=capi.MODE_GRAPH)
+    ref = pyoracle.run_stage_levels(cfg)
+    assert compare_levels(cfg, gpu, ref, f"spherical 2 levels ppm{ppm_type}")
