@@ -377,28 +377,35 @@ def run_adjoint(args, barrier):
 
 
 def run_spherical(args, barrier):
-    """Full-star spherical workload (config 5 geometry, one level): n^3 cells in boxes of 64^3,
-    NumSpec 21, ppm_type 2, exact base state on the irregular radial grid, polytrope star,
-    outflow faces; graph-replayed stage vs one launch per box."""
+    """Full-star spherical workload (config 5's geometry): two levels, level 0 n^3 in uneven
+    boxes (edges 16-128), level 1 (ratio 2) 16-64-cell boxes around 3 seeded bubbles, NumSpec
+    21, ppm_type 2, exact base state on the fine level's irregular radial grid, polytrope
+    star, outflow faces; the level-1 state injected from level 0.  Graph-replayed stage vs
+    one launch per box, identical results checked."""
     import torch
     from maestroex_gb300 import capi, configs
-    from maestroex_gb300.stage import StageBuffers, make_stage
+    from maestroex_gb300.stage import amr_buffers, make_amr_stage
     n = args.sph_n
-    cfg = configs.spherical_config(n=n, max_grid=64, nspec=21, ppm_type=2)
-    st = make_stage(cfg)
-    buf = StageBuffers(cfg).load(cfg)
-    snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
+    rng = np.random.default_rng(20261203 + 50)
+    l0 = configs.uneven_boxes((n, n, n), [16, 32, 48, 64, 96, 128], rng, p_stop=0.8)
+    fine = configs.bubble_boxes((n, n, n), nbubbles=3, cover=0.06, block_edges=(8, 16, 24, 32), max_edge=32,
+                                rng=np.random.default_rng(20261203 + 51))
+    cfg = configs.spherical_amr_config(n0=n, nspec=21, ppm_type=2, fine_boxes=fine, level0_boxes=l0, inject=True)
+    st = make_amr_stage(cfg)
+    bufs = amr_buffers(cfg)
+    names = ("uold", "sold", "gpi")
+    snap = [{nm: [t.clone() for t in getattr(b, nm).fabs] for nm in names} for b in bufs]
 
     def reset():
-        for name, ts in snap.items():
-            for dst, src in zip(getattr(buf, name).fabs, ts):
-                dst.copy_(src)
+        for b, sn in zip(bufs, snap):
+            for nm, ts in sn.items():
+                for dst, src in zip(getattr(b, nm).fabs, ts):
+                    dst.copy_(src)
 
     def timed(mode, reps):
         for _ in range(2):
             reset()
-            st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
-                             thermal=buf.thermal, mode=mode)
+            st.stage_forward_levels(bufs, mode=mode)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         tot = 0.0
@@ -406,8 +413,7 @@ def run_spherical(args, barrier):
             reset()
             torch.cuda.synchronize()
             e0.record()
-            st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
-                             thermal=buf.thermal, mode=mode)
+            st.stage_forward_levels(bufs, mode=mode)
             e1.record()
             torch.cuda.synchronize()
             tot += e0.elapsed_time(e1)
@@ -415,19 +421,24 @@ def run_spherical(args, barrier):
 
     reps = max(1, args.steps // 2)
     ms_graph, l_graph = timed(capi.MODE_GRAPH, reps)
-    out_graph = torch.cat([f.flatten() for f in buf.snew.fabs])
+    out_graph = [torch.cat([f.flatten() for f in b.snew.fabs]) for b in bufs]
     ms_box, l_box = timed(capi.MODE_PER_BOX, reps)
-    same = bool(torch.equal(out_graph, torch.cat([f.flatten() for f in buf.snew.fabs])))
-    ncell = n ** 3
+    same = all(torch.equal(a, torch.cat([f.flatten() for f in b.snew.fabs])) for a, b in zip(out_graph, bufs))
+    cells = [n ** 3, sum((b[3] - b[0] + 1) * (b[4] - b[1] + 1) * (b[5] - b[2] + 1) for b in fine)]
+    ncell = sum(cells)
     st.close()
-    del buf, snap
+    del bufs, snap
     torch.cuda.empty_cache()
-    return {"workload": f"spherical full star {n}^3 in {len(cfg['boxes'])} boxes of 64^3, one level, NumSpec 21, "
-                        f"ppm_type 2, exact base state ({cfg['nr']} radial bins), n = 1.5 polytrope, outflow",
-            "unit": UNIT,
+    return {"workload": f"spherical full star, two levels: level 0 {n}^3 in {len(l0)} uneven boxes (edges 16-128), "
+                        f"level 1 (ratio 2) {len(fine)} boxes around 3 bubbles ({cells[1] / 8 / cells[0]:.3f} of "
+                        f"the domain), NumSpec 21, ppm_type 2, exact base state ({cfg['nr']} radial bins on the "
+                        "fine grid), n = 1.5 polytrope (rho_c 2e9, radius 0.9 L/2), outflow; level-1 state "
+                        "injected from level 0",
+            "cells_per_level": cells, "unit": UNIT,
             "graph": {"value": ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": l_graph},
             "per_box": {"value": ncell / (ms_box * 1e-3), "ms_per_step": ms_box, "gpu_launches": l_box},
-            "identical_results_graph_vs_per_box": same}
+            "speedup_graph_vs_per_box": ms_box / ms_graph,
+            "identical_results_graph_vs_per_box": bool(same)}
 
 
 def run_2d(args, barrier):

@@ -345,10 +345,40 @@ def amr_buffers(cfg, device="cuda"):
                 i0, j0, k0, i1, j1, k1 = bx
                 blk = src[:, k0 // 2:(k1 + 1) // 2, j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2]
                 blk = blk.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2).repeat_interleave(2, dim=3)
+                if name == "sold" and cfg.get("spherical"):
+                    blk = _sph_rebin(blk, bx, c, P)
                 fs, _ = mf._slices(b)
                 mf.fabs[b][(slice(None),) + fs] = blk
             del src
         out.append(buf)
+    return out
+
+
+def _sph_rebin(blk, bx, fine, coarse):
+    """Spherical injection: a fine cell falls in its own radial bin, so the injected density,
+    species and enthalpy are rescaled by the ratio of the base state of the fine cell's bin to
+    that of its parent's bin (the perturbation relative to the base state is what is
+    injected)."""
+    dev = blk.device
+    L = fine["prob_hi"][0] - fine["prob_lo"][0]
+    dxf = fine["dx"][0]
+
+    def bins(lo, hi, dx, refine):
+        ax = [(torch.arange(lo[d], hi[d] + 1, device=dev, dtype=torch.float64) // refine + 0.5) * dx -
+              0.5 * L for d in range(3)]
+        r2 = ax[2][:, None, None] ** 2 + ax[1][None, :, None] ** 2 + ax[0][None, None, :] ** 2
+        return torch.floor(r2 / (2.0 * dxf * dxf) - 0.375 + 0.5).long()
+
+    lo, hi = bx[:3], bx[3:]
+    bf = bins(lo, hi, dxf, 1)
+    bc = bins(lo, hi, 2.0 * dxf, 2)
+    r0 = torch.from_numpy(np.ascontiguousarray(fine["rho0_old"])).to(dev)
+    h0 = torch.from_numpy(np.ascontiguousarray(fine["rhoh0_old"])).to(dev)
+    out = blk.clone()
+    fr = r0[bf] / r0[bc]
+    out[0] *= fr
+    out[4:] *= fr[None]
+    out[1] *= h0[bf] / h0[bc]
     return out
 
 
