@@ -230,6 +230,8 @@ def run_amr(args, ws, steps, warmup, barrier):
         barrier()
         return total / k
 
+    ms_graph_untuned = timed(capi.MODE_GRAPH, steps, warmup)
+    tuned = st.autotune(lambda: (reset(), st.stage_forward_levels(bufs, mode=capi.MODE_BATCHED)))
     ms_graph = timed(capi.MODE_GRAPH, steps, warmup)
     launches_graph = st.launch_count()
     out_graph = [torch.cat([f.flatten() for f in b.snew.fabs]) for b in bufs]
@@ -250,7 +252,11 @@ def run_amr(args, ws, steps, warmup, barrier):
                     f"around 3 bubbles ({cells[1] / 8 / cells[0]:.3f} of the domain), NumSpec {args.nspec}, "
                     "ppm_type 2; level-1 state injected from level 0",
         "cells_per_level": cells, "unit": UNIT,
-        "graph": {"value": ws * ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": launches_graph},
+        "graph": {"value": ws * ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": launches_graph,
+                  "autotuned": True},
+        "graph_untuned": {"value": ws * ncell / (ms_graph_untuned * 1e-3), "ms_per_step": ms_graph_untuned},
+        "autotuner_choices_per_level": [{str(t): sum(1 for k, v in tuned.items() if k.startswith(f"L{lev} ") and v == t)
+                                         for t in sorted(set(tuned.values()))} for lev in range(2)],
         "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
         "per_box": {"value": ws * ncell / (ms_perbox * 1e-3), "ms_per_step": ms_perbox,
                     "gpu_launches": launches_perbox},
@@ -606,6 +612,9 @@ def main():
 
     sampler = ClockSampler(local)
     sampler.start()
+    ms_graph_untuned = timed(capi.MODE_GRAPH, args.steps, warmup)
+    # launch-shape autotuner (untimed trials of the batched stage), then the graph again
+    tuned = st.autotune(lambda: (reset(), step(capi.MODE_BATCHED)))
     ms_graph = timed(capi.MODE_GRAPH, args.steps, warmup)
     clocks = sampler.stop()
     launches = st.launch_count()
@@ -676,7 +685,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": f"3-D single level {args.n}^3 in {len(cfg['boxes'])} boxes of {args.box}^3, "
                                f"NumSpec {args.nspec}, ppm_type 1, w0 != 0, x/y periodic, z slipwall/outflow",
-                   "mode": "batched kernels replayed as one CUDA graph",
+                   "mode": "batched kernels replayed as one CUDA graph, autotuned threads per block",
                    "l2": "inputs (state 2.4 GB) larger than the 129 MB L2; state reset between steps",
                    "replicas": ws},
         "clocks": clocks,
@@ -686,6 +695,11 @@ def main():
         "per_box": {"value": ws * ncell / (ms_perbox * 1e-3) if ms_perbox else None,
                     "ms_per_step": ms_perbox},
         "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
+        "autotuner": {"untuned_graph": {"value": ws * ncell / (ms_graph_untuned * 1e-3),
+                                        "ms_per_step": ms_graph_untuned},
+                      "threads_per_block_chosen": {str(t): sum(1 for v in tuned.values() if v == t)
+                                                   for t in sorted(set(tuned.values()))},
+                      "speedup": ms_graph_untuned / ms_graph},
         "fp64_peak_tflops_probe": tf.value,
         "kernels_top": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / ktot, 4)}
                         for k, v in top},

@@ -262,6 +262,18 @@ long madv_last_launch_count(const madv_ctx* ctx);
 int madv_profile(madv_ctx* ctx, int enable);
 int madv_profile_report(madv_ctx* ctx, char* buf, int len);
 
+/* Launch-shape autotuner: the threads per block of every stage kernel, chosen per level (the
+ * levels hold a hierarchy's box-size classes) from timed trials of the caller's own stage:
+ *     for each candidate t:  madv_autotune_trial(ctx, t);  run the stage in MADV_MODE_BATCHED;
+ *     madv_autotune_finish(ctx, json, len);
+ * finish picks the fastest candidate per (level, kernel), applies it to later launches and
+ * graphs, and writes the table {"L<level> <kernel symbol>": threads, ...} (a cache for
+ * madv_autotune_apply in a later run).  Kernels are clamped to the block size they can take.
+ * No counterpart in the reference. */
+int madv_autotune_trial(madv_ctx* ctx, int threads);
+int madv_autotune_finish(madv_ctx* ctx, char* json, int len);
+int madv_autotune_apply(madv_ctx* ctx, const char* json);
+
 /* FP64 FMA issue-rate probe of the current device (TFLOP/s, 2 flops per FMA): the
  * ceiling of the FP64-bound stage kernels.  No counterpart in the reference. */
 int madv_probe_fp64_peak(double* tflops, void* stream);

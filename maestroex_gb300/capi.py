@@ -27,6 +27,7 @@ EXPORTED = [
     "madv_last_error", "madv_version", "madv_profile", "madv_profile_report", "madv_probe_fp64_peak",
     "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc", "madv_set_layout_levels",
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
+    "madv_autotune_trial", "madv_autotune_finish", "madv_autotune_apply",
 ]
 
 
@@ -92,6 +93,9 @@ def lib():
         L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                                 C.c_void_p]
         L.madv_stage_adjoint.argtypes = [C.c_void_p, P(MadvAdjSeed), P(MadvAdjResult), C.c_void_p]
+        L.madv_autotune_trial.argtypes = [C.c_void_p, C.c_int]
+        L.madv_autotune_finish.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+        L.madv_autotune_apply.argtypes = [C.c_void_p, C.c_char_p]
         FAB = P(MadvFab)
         L.madv_ppm.argtypes = [C.c_void_p, P(MadvBox), FAB, C.c_int, FAB, FAB, FAB, C.c_int, P(C.c_int), FAB, FAB,
                                C.c_void_p]

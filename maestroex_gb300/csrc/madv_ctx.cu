@@ -3,6 +3,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -709,6 +710,35 @@ static void reset_launches(Hier& H) {
 }  // namespace madv
 
 using namespace madv;
+
+// Threads per block for kernel fn on this level: the autotuner's trial value while it times
+// a candidate, else the chosen value (a loaded table is matched by name at the kernel's first
+// launch), else 256; never more than the kernel can take.
+int Ctx::tpb_of(const void* fn) {
+    auto mx = tpb_max.find(fn);
+    int maxt;
+    if (mx == tpb_max.end()) {
+        cudaFuncAttributes a{};
+        maxt = (cudaFuncGetAttributes(&a, fn) == cudaSuccess && a.maxThreadsPerBlock > 0) ? a.maxThreadsPerBlock : 256;
+        maxt = maxt / 32 * 32;
+        tpb_max[fn] = maxt;
+        if (!tpb_by_name.empty()) {
+            const char* nm = nullptr;
+            if (cudaFuncGetName(&nm, fn) == cudaSuccess && nm) {
+                auto it = tpb_by_name.find("L" + std::to_string(lev) + " " + nm);
+                if (it != tpb_by_name.end()) tpb_choice[fn] = it->second;
+            }
+        }
+    } else {
+        maxt = mx->second;
+    }
+    int t = tpb_trial;
+    if (!t) {
+        auto it = tpb_choice.find(fn);
+        t = it == tpb_choice.end() ? 256 : it->second;
+    }
+    return t > maxt ? maxt : t;
+}
 
 cudaEvent_t Ctx::next_event() {
     if (ev_next == ev_pool.size()) {
@@ -1489,6 +1519,98 @@ int madv_ppm(madv_ctx* h, const madv_box* bx, const madv_fab* s, int comp, const
     c.launches = 0;
     return ppm_box_run(c.P, bx, s, comp, u, v, w, is_umac, bc, Ip, Im, c.box_scratch, (cudaStream_t)stream,
                        c.launches);
+}
+
+// ------------------------------------------------------------------ launch-shape autotuner
+// fold the timed launches of the current trial into the per-kernel totals
+static int tune_collect(Hier& H) {
+    if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) return MADV_ERR_CUDA;
+    for (auto* c : H.L) {
+        if (c->tpb_trial)
+            for (auto& r : c->prof) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, r.e0, r.e1);
+                c->tune_ms[r.fn][c->tpb_trial] += ms;
+            }
+        c->prof.clear();
+        c->ev_next = 0;
+    }
+    return MADV_OK;
+}
+
+int madv_autotune_trial(madv_ctx* h, int threads) {
+    if (!h || threads < 32 || threads > 1024 || threads % 32 != 0) {
+        set_error("threads per block: a multiple of 32 in [32, 1024]");
+        return MADV_ERR_PARAM;
+    }
+    Hier H = h->H();
+    int rc = tune_collect(H);
+    if (rc) return rc;
+    for (auto* c : H.L) {
+        c->tpb_trial = threads;
+        c->profiling = true;
+    }
+    drop_graph(h);
+    return MADV_OK;
+}
+
+static void json_out(const std::string& js, char* buf, int len) {
+    if (buf && len > 0) std::snprintf(buf, (size_t)len, "%s", js.c_str());
+}
+
+int madv_autotune_finish(madv_ctx* h, char* json, int len) {
+    if (!h) return MADV_ERR_PARAM;
+    Hier H = h->H();
+    int rc = tune_collect(H);
+    if (rc) return rc;
+    std::string js = "{";
+    bool first = true;
+    for (auto* c : H.L) {
+        for (auto& kv : c->tune_ms) {
+            int best = 256;
+            double bms = 1e300;
+            for (auto& tv : kv.second)
+                if (tv.second < bms) {
+                    bms = tv.second;
+                    best = tv.first;
+                }
+            c->tpb_choice[kv.first] = best;
+            const char* nm = nullptr;
+            if (cudaFuncGetName(&nm, kv.first) != cudaSuccess || !nm) continue;
+            js += (first ? "\"L" : ", \"L") + std::to_string(c->lev) + " " + nm + "\": " + std::to_string(best);
+            first = false;
+        }
+        c->tune_ms.clear();
+        c->tpb_trial = 0;
+        c->profiling = false;
+    }
+    js += "}";
+    drop_graph(h);
+    json_out(js, json, len);
+    return (int)js.size() < len ? MADV_OK : MADV_ERR_PARAM;
+}
+
+int madv_autotune_apply(madv_ctx* h, const char* json) {
+    if (!h || !json) return MADV_ERR_PARAM;
+    std::map<std::string, int> tab;
+    const char* p = json;
+    while ((p = std::strchr(p, '"'))) {
+        const char* q = std::strchr(p + 1, '"');
+        if (!q) break;
+        std::string key(p + 1, q);
+        const char* colon = std::strchr(q, ':');
+        if (!colon) break;
+        tab[key] = std::atoi(colon + 1);
+        p = colon + 1;
+    }
+    Hier H = h->H();
+    for (auto* c : H.L) {
+        c->tpb_by_name = tab;
+        c->tpb_choice.clear();
+        c->tpb_max.clear();
+    }
+    drop_graph(h);
+    return MADV_OK;
 }
 
 int madv_profile(madv_ctx* h, int enable) {

@@ -134,6 +134,15 @@ struct Ctx {
     size_t ev_next = 0;
     cudaEvent_t next_event();
     long launches = 0;
+    // launch shape: threads per block of each kernel (autotuned per level; 256 by default),
+    // a trial value that overrides them all while the autotuner times a candidate, and the
+    // largest block each kernel can take
+    std::map<const void*, int> tpb_choice;
+    std::map<std::string, int> tpb_by_name;  // a loaded table, resolved at first launch
+    std::map<const void*, int> tpb_max;
+    std::map<const void*, std::map<int, double>> tune_ms;
+    int tpb_trial = 0;
+    int tpb_of(const void* fn);
     int* d_flag = nullptr;  // device error flag (EOS cutoff)
     // graph mode
     cudaGraphExec_t graph_exec = nullptr;

@@ -225,6 +225,22 @@ class ScalarAdvectionStage:
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
 
+    def autotune(self, run_batched, candidates=(64, 128, 256, 512)):
+        """Launch-shape autotuner (madv_autotune_*): run_batched() runs the caller's stage once
+        in MODE_BATCHED; it is timed per kernel for every candidate block size, and the fastest
+        per (level, kernel) is applied.  Returns the chosen table (dict)."""
+        import json
+        for t in candidates:
+            check(lib().madv_autotune_trial(self.ctx, int(t)))
+            run_batched()
+        buf = C.create_string_buffer(1 << 20)
+        check(lib().madv_autotune_finish(self.ctx, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def autotune_apply(self, table):
+        import json
+        check(lib().madv_autotune_apply(self.ctx, json.dumps(table).encode()))
+
     def stage_adjoint(self, uold, sold0, weight, nsteps, ckpt_interval, grad_s=None, sfinal=None, grad_u=None,
                       stream=None):
         """madv_stage_adjoint: nsteps fixed-velocity steps from sold0, J = <weight, s_nsteps>,

@@ -215,3 +215,25 @@ def test_exact_helpers_match_ieee(y, thr):
     nfail = C.c_longlong(-1)
     capi.check(capi.lib().madv_selftest_exact(y, thr, 1 << 24, C.byref(nfail), None))
     assert nfail.value == 0
+
+
+def test_autotuner_keeps_results_and_round_trips():
+    """Block sizes change nothing but speed: the stage after autotuning (graph mode) and a
+    second context given the saved table reproduce the untuned result bit for bit."""
+    from maestroex_gb300.stage import StageBuffers, make_stage
+    cfg = configs.planar_config(n=(32, 32, 32), max_grid=16, seed=20261203 + 9)
+
+    def run(st, mode):
+        buf = StageBuffers(cfg).load(cfg)
+        st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
+                         thermal=buf.thermal, mode=mode)
+        return buf.snew.to_domain(cfg["n"]).cpu().numpy()
+
+    st = make_stage(cfg)
+    ref = run(st, capi.MODE_BATCHED)
+    table = st.autotune(lambda: run(st, capi.MODE_BATCHED), candidates=(64, 512, 128))
+    assert table and all(v in (64, 128, 512) for v in table.values())
+    assert np.array_equal(run(st, capi.MODE_GRAPH), ref, equal_nan=True)
+    st2 = make_stage(cfg)
+    st2.autotune_apply(table)
+    assert np.array_equal(run(st2, capi.MODE_BATCHED), ref, equal_nan=True)
