@@ -225,7 +225,7 @@ class ScalarAdvectionStage:
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
 
-    def autotune(self, run_batched, candidates=(64, 128, 256, 512)):
+    def autotune(self, run_batched, candidates=(32, 64, 128, 256, 512)):
         """Launch-shape autotuner (madv_autotune_*): run_batched() runs the caller's stage once
         in MODE_BATCHED; it is timed per kernel for every candidate block size, and the fastest
         per (level, kernel) is applied.  Returns the chosen table (dict)."""
