@@ -112,6 +112,23 @@ def roofline(kern, ncell, stage_ms, fp64_tflops_probe, peaks, peak_kind):
     return r
 
 
+def max_over_ranks(x, ws, device="cuda"):
+    """The slowest rank's time: every rank times its own replica of the workload, and the
+    job's step time is the maximum (all-reduce MAX over the process group)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(ncell_per_rank, ws, ms):
+    """Whole-job throughput of N replicas: all ranks' cells over the slowest rank's time."""
+    return ws * ncell_per_rank / (ms * 1e-3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -603,12 +620,7 @@ def main():
             torch.cuda.synchronize()
             total += ev0.elapsed_time(ev1)
         barrier()
-        ms = total / steps
-        if ws > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(total / steps, ws)
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -642,11 +654,7 @@ def main():
         torch.cuda.synchronize()
         if it >= warmup:
             e2e_ms += (time.perf_counter() - t0) * 1e3
-    e2e_ms /= args.steps
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms / args.steps, ws)
 
     # per-kernel device time of one batched stage (CUDA events around every launch)
     import ctypes as C
@@ -676,7 +684,7 @@ def main():
     peaks, peak_kind = measured_peaks()
     ktot = sum(v[1] for v in kern.values())
     top = sorted(kern.items(), key=lambda kv: -kv[1][1])[:8]
-    value = ws * ncell / (ms_graph * 1e-3)
+    value = job_value(ncell, ws, ms_graph)
     b_cell = 8 * (2 * args.nspec + 16)
     hbm_gbs = ncell * b_cell / (ms_graph * 1e-3) / 1e9
     line = {
