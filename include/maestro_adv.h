@@ -158,6 +158,55 @@ int madv_enthalpy_advance(madv_ctx* ctx, int which_step, const madv_multifab* so
                           const madv_multifab* sflux, const madv_multifab* umac,
                           const madv_multifab* thermal, void* stream);
 
+/* ---- The member functions inside AdvancePremac / DensityAdvance / EnthalpyAdvance, one
+ * level, 3-D.  Inputs carry the ghost cells the reference's callers fill before the call
+ * (ng_adv = ng_s = 3, or 4 for ppm_type 2); the implicit inputs (dt, rel_eps, BCs, w0 and the
+ * base state) come from the context, as the reference reads them from Maestro members. */
+
+/* Maestro::MakeUtrans (Source/Maestro.H:1172, Source/MaestroMakeUtrans.cpp:6-648).
+ * utilde, ufull: 3 comps, ng_adv ghosts.  utrans[3]: written on the valid faces and, where
+ * the FAB holds it, the ghost face layer the reference fills (FillBoundary + FillUmacGhost).
+ * w0mac (spherical) is built from the context's w0. */
+int madv_make_utrans(madv_ctx* ctx, const madv_multifab* utilde, const madv_multifab* ufull,
+                     const madv_multifab* utrans, void* stream);
+
+/* Maestro::VelPred (Source/Maestro.H:1711, Source/MaestroVelPred.cpp:5-292).
+ * utilde, ufull: ng_adv ghosts; utrans[3]: 1 ghost (w0 already added, as AdvancePremac
+ * passes it); force: 3 comps, 1 ghost.  umac[3] receives the valid faces. */
+int madv_vel_pred(madv_ctx* ctx, const madv_multifab* utilde, const madv_multifab* ufull,
+                  const madv_multifab* utrans, const madv_multifab* umac, const madv_multifab* force,
+                  void* stream);
+
+/* Maestro::MakeEdgeScal (Source/Maestro.H:913, Source/MaestroMakeEdgeScalars.cpp:6-302) for
+ * scalars with bcs_s: is_vel must be 0 and start_bccomp == start_scomp (every scalar call of
+ * the reference).  state: ng_s ghosts; umac[3]: full velocity, 1 ghost; force: 1 ghost.
+ * sedge[3] receives components start_scomp .. start_scomp+num_comp-1 on the valid faces. */
+int madv_make_edge_scal(madv_ctx* ctx, const madv_multifab* state, const madv_multifab* sedge,
+                        const madv_multifab* umac, const madv_multifab* force, int is_vel,
+                        int start_scomp, int start_bccomp, int num_comp, int is_conservative,
+                        void* stream);
+
+/* Maestro::MakeRhoXFlux (Source/Maestro.H:230, Source/MaestroMakeFlux.cpp:18-465) for the
+ * species (start_comp = FirstSpec, num_comp = NumSpec, the reference's only call): sflux[3]
+ * receives Rho and the species; etarhoflux (may be NULL) is accumulated into.  which_step 1
+ * passes rho0_old as the new base state (DensityAdvance's predictor), 2 rho0_new. */
+int madv_make_rhox_flux(madv_ctx* ctx, int which_step, const madv_multifab* sflux,
+                        const madv_multifab* etarhoflux, const madv_multifab* sedge,
+                        const madv_multifab* umac, int start_comp, int num_comp, void* stream);
+
+/* Maestro::MakeRhoHFlux (Source/Maestro.H:270, Source/MaestroMakeFlux.cpp:467-1067): sflux[3]
+ * receives RhoH; which_step as for madv_make_rhox_flux (rhoh0). */
+int madv_make_rhoh_flux(madv_ctx* ctx, int which_step, const madv_multifab* sflux,
+                        const madv_multifab* sedge, const madv_multifab* umac, void* stream);
+
+/* Maestro::UpdateScal (Source/Maestro.H:306, Source/MaestroAdvection.cpp:86-297) for RhoH
+ * (start_comp 1, num_comp 1) or the species (FirstSpec, NumSpec; Rho follows).  stateold,
+ * force: valid region; statenew: the updated components on the valid region and, where
+ * the FAB holds them, the ng_s ghost cells of the closing FillPatch. */
+int madv_update_scal(madv_ctx* ctx, const madv_multifab* stateold, const madv_multifab* statenew,
+                     const madv_multifab* sflux, const madv_multifab* force, int start_comp,
+                     int num_comp, void* stream);
+
 /* The whole stage as Maestro::AdvanceTimeStep runs it with the MAC projection
  * skipped (Source/MaestroAdvance.cpp:359, 448-455, 541-548): AdvancePremac, Addw0(+1),
  * DensityAdvance, Addw0(-1), Addw0(+1), EnthalpyAdvance, Addw0(-1).

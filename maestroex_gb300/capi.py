@@ -28,6 +28,8 @@ EXPORTED = [
     "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc", "madv_set_layout_levels",
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
     "madv_autotune_trial", "madv_autotune_finish", "madv_autotune_apply",
+    "madv_make_utrans", "madv_vel_pred", "madv_make_edge_scal", "madv_make_rhox_flux", "madv_make_rhoh_flux",
+    "madv_update_scal",
 ]
 
 
@@ -88,6 +90,13 @@ def lib():
         L.madv_addw0.argtypes = [C.c_void_p, MF, C.c_double, C.c_void_p]
         L.madv_density_advance.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, C.c_void_p]
         L.madv_enthalpy_advance.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, C.c_void_p]
+        I = C.c_int
+        L.madv_make_utrans.argtypes = [C.c_void_p, MF, MF, MF, C.c_void_p]
+        L.madv_vel_pred.argtypes = [C.c_void_p, MF, MF, MF, MF, MF, C.c_void_p]
+        L.madv_make_edge_scal.argtypes = [C.c_void_p, MF, MF, MF, MF, I, I, I, I, I, C.c_void_p]
+        L.madv_make_rhox_flux.argtypes = [C.c_void_p, I, MF, MF, MF, MF, I, I, C.c_void_p]
+        L.madv_make_rhoh_flux.argtypes = [C.c_void_p, I, MF, MF, MF, C.c_void_p]
+        L.madv_update_scal.argtypes = [C.c_void_p, MF, MF, MF, MF, I, I, C.c_void_p]
         L.madv_stage_forward.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                          C.c_void_p]
         L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,

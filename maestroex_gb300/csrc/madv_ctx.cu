@@ -372,8 +372,19 @@ static int upload_user_views(Ctx& c) {
 
 enum {
     U_UOLD = 0, U_SOLD, U_GPI, U_THERMAL, U_SNEW, U_UMAC0, U_UMAC1, U_UMAC2, U_SEDGE0, U_SEDGE1, U_SEDGE2,
-    U_SFLUX0, U_SFLUX1, U_SFLUX2, U_ETA, U_UTRANS0, U_UTRANS1, U_UTRANS2
+    U_SFLUX0, U_SFLUX1, U_SFLUX2, U_ETA, U_UTRANS0, U_UTRANS1, U_UTRANS2, U_UFULL, U_FORCE
 };
+
+// Ghost width (at most maxg) that every FAB of mf holds around its box
+static int held_ghosts(const Ctx& c, const madv_multifab* mf, int nodal, int maxg) {
+    int g = maxg;
+    for (int b = 0; b < c.nb; ++b) {
+        const madv_fab& f = mf->fab[b];
+        HBox v = valid_box(c, b, nodal);
+        for (int d = 0; d < 3; ++d) g = std::min(g, std::min(v.lo[d] - f.lo[d], f.hi[d] - v.hi[d]));
+    }
+    return std::max(g, 0);
+}
 
 // ------------------------------------------------------------------ level coupling
 // Maestro::FillPatch over all levels (Source/MaestroFillData.cpp:7-74): level 0 is filled
@@ -1489,6 +1500,223 @@ int madv_enthalpy_advance(madv_ctx* h, int which_step, const madv_multifab* sold
                           const madv_multifab* sedge, const madv_multifab* sflux, const madv_multifab* umac,
                           const madv_multifab* thermal, void* stream) {
     return scalar_advance(h, 1, which_step, sold, snew, sedge, sflux, nullptr, umac, thermal, stream);
+}
+
+// ---- the member functions inside AdvancePremac / DensityAdvance / EnthalpyAdvance, one
+// level, 3-D.  Inputs are read with the ghost cells the reference's callers fill before the
+// call; each entry recomputes the implicit inputs it needs from the context (w0_cart, w0mac,
+// the face base state of the spherical fluxes).
+static int begin_member(madv_ctx* h, void* stream, Hier& H) {
+    int rc = begin_call(h, stream, H);
+    if (rc) return rc;
+    if (h->c.ndim != 3) {
+        set_error("the per-member-function entry points are 3-D");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    return MADV_OK;
+}
+
+int madv_make_utrans(madv_ctx* h, const madv_multifab* utilde, const madv_multifab* ufull,
+                     const madv_multifab* utrans, void* stream) {
+    Hier H;
+    int rc = begin_member(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!utilde || !ufull || !utrans) return MADV_ERR_PARAM;
+    try {
+        const int nga = c.ng_adv;
+        if ((rc = bind(c, U_UOLD, utilde, 3, -1, nga)) || (rc = bind(c, U_UFULL, ufull, 3, -1, nga))) return rc;
+        for (int d = 0; d < 3; ++d)
+            if ((rc = bind(c, U_UTRANS0 + d, &utrans[d], 1, d, 0))) return rc;
+        if ((rc = upload_user_views(c))) return rc;
+        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, nga);
+        copy_fab(c, F_UFULL, 0, F_USER + U_UFULL, 0, 3, nga);
+        w0_carts(H);
+        for (int d = 0; d < 3; ++d) set_val(c, F_UTRANS0 + d, 0.0, 0, 1, 1);
+        make_utrans(c);
+        sync_faces_h(H, F_UTRANS0);  // FillBoundary + FillUmacGhost (Source/MaestroMakeUtrans.cpp:630-639)
+        for (int d = 0; d < 3; ++d)
+            copy_fab(c, F_USER + U_UTRANS0 + d, 0, F_UTRANS0 + d, 0, 1, held_ghosts(c, &utrans[d], d, 1));
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+int madv_vel_pred(madv_ctx* h, const madv_multifab* utilde, const madv_multifab* ufull, const madv_multifab* utrans,
+                  const madv_multifab* umac, const madv_multifab* force, void* stream) {
+    Hier H;
+    int rc = begin_member(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!utilde || !ufull || !utrans || !umac || !force) return MADV_ERR_PARAM;
+    try {
+        const int nga = c.ng_adv;
+        if ((rc = bind(c, U_UOLD, utilde, 3, -1, nga)) || (rc = bind(c, U_UFULL, ufull, 3, -1, nga)) ||
+            (rc = bind(c, U_FORCE, force, 3, -1, 1)))
+            return rc;
+        for (int d = 0; d < 3; ++d)
+            if ((rc = bind(c, U_UTRANS0 + d, &utrans[d], 1, d, 1)) || (rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 0)))
+                return rc;
+        if ((rc = upload_user_views(c))) return rc;
+        copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, nga);
+        copy_fab(c, F_UFULL, 0, F_USER + U_UFULL, 0, 3, nga);
+        copy_fab(c, F_VELFORCE, 0, F_USER + U_FORCE, 0, 3, 1);
+        for (int d = 0; d < 3; ++d) {
+            copy_fab(c, F_UTRANS0 + d, 0, F_USER + U_UTRANS0 + d, 0, 1, 1);
+            set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
+        }
+        w0_carts(H);
+        vel_pred_prep(c);
+        vel_pred(c);
+        for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+int madv_make_edge_scal(madv_ctx* h, const madv_multifab* state, const madv_multifab* sedge,
+                        const madv_multifab* umac, const madv_multifab* force, int is_vel, int start_scomp,
+                        int start_bccomp, int num_comp, int is_conservative, void* stream) {
+    Hier H;
+    int rc = begin_member(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!state || !sedge || !umac || !force) return MADV_ERR_PARAM;
+    if (is_vel || start_bccomp != start_scomp) {
+        set_error("MakeEdgeScal: scalars with start_bccomp == start_scomp (velocity edges are not built)");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    if (start_scomp < 0 || num_comp < 1 || start_scomp + num_comp > c.nscal) {
+        set_error("MakeEdgeScal: component range outside the state");
+        return MADV_ERR_PARAM;
+    }
+    try {
+        if ((rc = bind(c, U_SOLD, state, start_scomp + num_comp, -1, c.ng_s)) ||
+            (rc = bind(c, U_FORCE, force, start_scomp + num_comp, -1, 1)))
+            return rc;
+        for (int d = 0; d < 3; ++d)
+            if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 1)) ||
+                (rc = bind(c, U_SEDGE0 + d, &sedge[d], start_scomp + num_comp, d, 0)))
+                return rc;
+        if ((rc = upload_user_views(c))) return rc;
+        copy_fab(c, F_SOLD, start_scomp, F_USER + U_SOLD, start_scomp, num_comp, c.ng_s);
+        copy_fab(c, F_SCALFORCE, start_scomp, F_USER + U_FORCE, start_scomp, num_comp, 1);
+        for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
+        make_edge_scal(c, start_scomp, num_comp, BCS_S, is_conservative != 0, 0);
+        for (int d = 0; d < 3; ++d)
+            copy_fab(c, F_USER + U_SEDGE0 + d, start_scomp, F_SEDGE0 + d, start_scomp, num_comp, 0);
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+// MakeRhoXFlux / MakeRhoHFlux: which_step 1 passes the old base state as the "new" one, as
+// DensityAdvance / EnthalpyAdvance do in the predictor (Source/MaestroDensityAdvance.cpp:186-219)
+static int flux_member(madv_ctx* h, int which, int which_step, const madv_multifab* sflux,
+                       const madv_multifab* etarhoflux, const madv_multifab* sedge, const madv_multifab* umac,
+                       void* stream) {
+    Hier H;
+    int rc = begin_member(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!sflux || !sedge || !umac) return MADV_ERR_PARAM;
+    if (which_step != 1 && which_step != 2) {
+        set_error("which_step must be 1 (predictor) or 2 (corrector)");
+        return MADV_ERR_PARAM;
+    }
+    try {
+        if ((rc = bind(c, U_ETA, etarhoflux, 1, 2, 0))) return rc;
+        for (int d = 0; d < 3; ++d)
+            if ((rc = bind(c, U_SEDGE0 + d, &sedge[d], c.nscal, d, 0)) ||
+                (rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 0)) || (rc = bind(c, U_SFLUX0 + d, &sflux[d], c.nscal, d, 0)))
+                return rc;
+        if ((rc = upload_user_views(c))) return rc;
+        for (int d = 0; d < 3; ++d) {
+            copy_fab(c, F_SEDGE0 + d, 0, F_USER + U_SEDGE0 + d, 0, c.nscal, 0);
+            set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
+            copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 0);
+        }
+        w0_carts(H);
+        if (which == 0) {
+            set_val(c, F_ETA, 0.0, 0, 1, 0);
+            if (etarhoflux) copy_fab(c, F_ETA, 0, F_USER + U_ETA, 0, 1, 0);
+            const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
+            const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
+            if (c.sph) {
+                make_s0mac_h(H, "rho0_old", F_S0MAC0);
+                make_s0mac_h(H, r0n, F_S0MACB0);
+            }
+            make_rhox_flux(c, c.b1("rho0_old"), c.b1("rho0_edge_old"), c.b1(r0n), c.b1(r0en));
+            for (int d = 0; d < 3; ++d) {
+                copy_fab(c, F_USER + U_SFLUX0 + d, RHO, F_SFLUX0 + d, RHO, 1, 0);
+                copy_fab(c, F_USER + U_SFLUX0 + d, FIRSTSPEC, F_SFLUX0 + d, FIRSTSPEC, c.nspec, 0);
+            }
+            if (etarhoflux) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
+        } else {
+            const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
+            const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
+            if (c.sph) {
+                make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
+                make_s0mac_h(H, rh0n, F_S0MACB0);
+            }
+            make_rhoh_flux(c, c.b1("rhoh0_old"), c.b1("rhoh0_edge_old"), c.b1(rh0n), c.b1(rh0en));
+            for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_SFLUX0 + d, RHOH, F_SFLUX0 + d, RHOH, 1, 0);
+        }
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+int madv_make_rhox_flux(madv_ctx* h, int which_step, const madv_multifab* sflux, const madv_multifab* etarhoflux,
+                        const madv_multifab* sedge, const madv_multifab* umac, int start_comp, int num_comp,
+                        void* stream) {
+    if (h && (start_comp != FIRSTSPEC || num_comp != h->c.nspec)) {
+        set_error("MakeRhoXFlux: the species FirstSpec .. FirstSpec+NumSpec-1 (the reference's only call)");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    return flux_member(h, 0, which_step, sflux, etarhoflux, sedge, umac, stream);
+}
+
+int madv_make_rhoh_flux(madv_ctx* h, int which_step, const madv_multifab* sflux, const madv_multifab* sedge,
+                        const madv_multifab* umac, void* stream) {
+    return flux_member(h, 1, which_step, sflux, nullptr, sedge, umac, stream);
+}
+
+int madv_update_scal(madv_ctx* h, const madv_multifab* stateold, const madv_multifab* statenew,
+                     const madv_multifab* sflux, const madv_multifab* force, int start_comp, int num_comp,
+                     void* stream) {
+    Hier H;
+    int rc = begin_member(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!stateold || !statenew || !sflux || !force) return MADV_ERR_PARAM;
+    if (!((start_comp == RHOH && num_comp == 1) || (start_comp == FIRSTSPEC && num_comp == c.nspec))) {
+        set_error("UpdateScal: RhoH, or the species FirstSpec .. FirstSpec+NumSpec-1");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    try {
+        if ((rc = bind(c, U_SOLD, stateold, c.nscal, -1, 0)) || (rc = bind(c, U_SNEW, statenew, c.nscal, -1, 0)) ||
+            (rc = bind(c, U_FORCE, force, c.nscal, -1, 0)))
+            return rc;
+        for (int d = 0; d < 3; ++d)
+            if ((rc = bind(c, U_SFLUX0 + d, &sflux[d], c.nscal, d, 0))) return rc;
+        if ((rc = upload_user_views(c))) return rc;
+        copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
+        copy_fab(c, F_SNEW, 0, F_USER + U_SNEW, 0, c.nscal, 0);
+        copy_fab(c, F_SCALFORCE, 0, F_USER + U_FORCE, 0, c.nscal, 0);
+        for (int d = 0; d < 3; ++d) copy_fab(c, F_SFLUX0 + d, 0, F_USER + U_SFLUX0 + d, 0, c.nscal, 0);
+        update_scal_h(H, start_comp);  // with AverageDown + FillPatch of the updated components
+        const int g = held_ghosts(c, statenew, -1, c.ng_s);
+        copy_fab(c, F_USER + U_SNEW, start_comp, F_SNEW, start_comp, num_comp, g);
+        if (start_comp == FIRSTSPEC) copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 1, g);
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
 }
 
 long madv_last_launch_count(const madv_ctx* h) {

@@ -198,6 +198,7 @@ void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec =
 void make_utrans(Ctx& c);
 void make_vel_force(Ctx& c);  // valid cells; F_GRAVCART / F_RHO0CART filled by the caller
 void vel_pred(Ctx& c);
+void vel_pred_prep(Ctx& c);  // the MakeUtrans work VelPred reuses, for a VelPred call on its own
 void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative,
                     int force_zero);
 void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform);

@@ -1203,7 +1203,8 @@ __global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double*
     const FabView fl = VW(F_SFLUX0 + D), e = VW(F_SEDGE0 + D);
     const double u = at(VW(F_UMAC0 + D), i, j, k);
     double frho = 0.0;
-    double eta = 0.0;
+    // etarhoflux is accumulated into species by species, as the reference does (:170-178)
+    double eta = D == 2 && do_eta ? at(VW(F_ETA), i, j, k) : 0.0;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
         const double rho0_edge = 0.5 * (r0o[k] + r0n[k]);
         double f = 0.0;
@@ -1218,7 +1219,7 @@ __global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double*
         frho += f;
     }
     at(fl, i, j, k, RHO) = frho;
-    if (D == 2 && do_eta) at(VW(F_ETA), i, j, k) += eta;
+    if (D == 2 && do_eta) at(VW(F_ETA), i, j, k) = eta;
 }
 
 void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new, const double* r0e_new) {
@@ -1770,7 +1771,7 @@ __global__ void k_rhox_flux_2d(KARGS, int nspec, int spt, int do_eta, const doub
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView fl = VW(F_SFLUX0 + D), e = VW(F_SEDGE0 + D);
     const double u = at(VW(F_UMAC0 + D), i, j, k);
-    double frho = 0.0, eta = 0.0;
+    double frho = 0.0, eta = D == 1 && do_eta ? at(VW(F_ETA), i, j, k) : 0.0;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
         const double rho0_edge = 0.5 * (r0o[j] + r0n[j]);
         double f;
@@ -1785,7 +1786,7 @@ __global__ void k_rhox_flux_2d(KARGS, int nspec, int spt, int do_eta, const doub
         frho += f;
     }
     at(fl, i, j, k, RHO) = frho;
-    if (D == 1 && do_eta) at(VW(F_ETA), i, j, k) += eta;
+    if (D == 1 && do_eta) at(VW(F_ETA), i, j, k) = eta;
 }
 
 // MakeRhoHFlux, 2-D (Source/MaestroMakeFlux.cpp:597-662)
@@ -1904,6 +1905,16 @@ void update_scal_2d(Ctx& c, int start_comp) {
         launch(c, rt, 1, k_update_rhox_2d, c.V(), c.nspec, c.P.dt, c.P.dx[0], c.P.dx[1], 0.5 * c.P.base_cutoff_density);
 }
 void make_utrans_2d_entry(Ctx& c) { make_utrans_2d(c); }
+
+// What VelPred takes over from MakeUtrans when the two run back to back (ppm_type 1/2): the
+// tracing coefficients of ufull per cell and the PPM sweep of each velocity component along
+// its own direction.  A VelPred call on its own recomputes them from the same inputs.
+void vel_pred_prep(Ctx& c) {
+    if (c.P.ppm_type == 0) return;
+    const RegionTable& rt = c.ndim == 2 ? rg2(c, 1) : rg_grow(c, 1);
+    launch(c, rt, 1, k_trace_cell, c.V(), F_UFULL, c.P.dt, c.P.dx[0], c.P.dx[1], c.P.dx[2]);
+    for (int d = 0; d < c.ndim; ++d) ppm_any(c, d, F_UTILDE, d, c.bcs_u[d], F_UFULL, d, 0, F_IPC0 + d, F_IMC0 + d);
+}
 void vel_pred_2d_entry(Ctx& c) { vel_pred_2d(c); }
 void make_edge_scal_2d_entry(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons) {
     make_edge_scal_2d(c, start_comp, num_comp, which_bcs, is_cons);

@@ -222,6 +222,37 @@ class ScalarAdvectionStage:
         check(lib().madv_enthalpy_advance(self.ctx, which_step, _ref(sold), _ref(snew), _ref3(sedge),
                                           _ref3(sflux), _ref3(umac), _ref(thermal), C.c_void_p(s)))
 
+    # the member functions inside AdvancePremac / DensityAdvance / EnthalpyAdvance (3-D, one level)
+    def make_utrans(self, utilde, ufull, utrans, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_make_utrans(self.ctx, _ref(utilde), _ref(ufull), _ref3(utrans), C.c_void_p(s)))
+
+    def vel_pred(self, utilde, ufull, utrans, umac, force, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_vel_pred(self.ctx, _ref(utilde), _ref(ufull), _ref3(utrans), _ref3(umac), _ref(force),
+                                  C.c_void_p(s)))
+
+    def make_edge_scal(self, state, sedge, umac, force, is_vel, start_scomp, start_bccomp, num_comp,
+                       is_conservative, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_make_edge_scal(self.ctx, _ref(state), _ref3(sedge), _ref3(umac), _ref(force), int(is_vel),
+                                        start_scomp, start_bccomp, num_comp, int(is_conservative), C.c_void_p(s)))
+
+    def make_rhox_flux(self, which_step, sflux, etarhoflux, sedge, umac, start_comp, num_comp, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_make_rhox_flux(self.ctx, which_step, _ref3(sflux), _ref(etarhoflux), _ref3(sedge),
+                                        _ref3(umac), start_comp, num_comp, C.c_void_p(s)))
+
+    def make_rhoh_flux(self, which_step, sflux, sedge, umac, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_make_rhoh_flux(self.ctx, which_step, _ref3(sflux), _ref3(sedge), _ref3(umac),
+                                        C.c_void_p(s)))
+
+    def update_scal(self, stateold, statenew, sflux, force, start_comp, num_comp, stream=None):
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_update_scal(self.ctx, _ref(stateold), _ref(statenew), _ref3(sflux), _ref(force),
+                                     start_comp, num_comp, C.c_void_p(s)))
+
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
 

@@ -1652,9 +1652,9 @@ static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, do
     }
 }
 
-static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
-                     mo_outputs* out, int which_step) {
-    if (which_step != 1 && which_step != 2) throw std::runtime_error("which_step must be 1 or 2");
+// The levels, boundary conditions, base state, w0_cart and (spherical) w0mac of a stage call.
+static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxes, const int* boxes,
+                        const mo_inputs* in) {
     if (nlev < 1 || nlev > 4) throw std::runtime_error("1 to 4 levels");
     if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
     if (p->use_exact_base_state && !p->spherical) throw std::runtime_error("use_exact_base_state is spherical-only");
@@ -1666,7 +1666,6 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
     if (!(p->species_pred_type >= 1 && p->species_pred_type <= 3))
         throw std::runtime_error("species_pred_type must be 1, 2 or 3");
-    Stage H;
     H.P = *p;
     H.nlev = nlev;
     H.nspec = p->nspec;
@@ -1731,17 +1730,22 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
     }
     H.InitChunks();
     if (nlev > 1) H.ComputeCutoffCoords();
-    const int nscal = H.nscal;
 
     // w0_cart: Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1) (Source/MaestroAdvance.cpp:326)
-    {
-        VMF w0c(nlev);
-        for (int lev = 0; lev < nlev; ++lev) w0c[lev].define(H.S[lev].L.ba, 3, 2, -1, 0.0);
-        H.Put1dArrayOnCart(H.bs(&Lev::w0), w0c, true, true, &H.bcs_u(), 0, true);
-        for (int lev = 0; lev < nlev; ++lev) H.S[lev].w0_cart = std::move(w0c[lev]);
-        if (p->spherical)  // MakeW0mac (Source/MaestroAdvance.cpp:335-338)
-            for (int lev = 0; lev < nlev; ++lev) H.S[lev].MakeW0mac();
-    }
+    VMF w0c(nlev);
+    for (int lev = 0; lev < nlev; ++lev) w0c[lev].define(H.S[lev].L.ba, 3, 2, -1, 0.0);
+    H.Put1dArrayOnCart(H.bs(&Lev::w0), w0c, true, true, &H.bcs_u(), 0, true);
+    for (int lev = 0; lev < nlev; ++lev) H.S[lev].w0_cart = std::move(w0c[lev]);
+    if (p->spherical)  // MakeW0mac (Source/MaestroAdvance.cpp:335-338)
+        for (int lev = 0; lev < nlev; ++lev) H.S[lev].MakeW0mac();
+}
+
+static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
+                     mo_outputs* out, int which_step) {
+    if (which_step != 1 && which_step != 2) throw std::runtime_error("which_step must be 1 or 2");
+    Stage H;
+    setup_stage(H, p, nlev, nboxes, boxes, in);
+    const int nscal = H.nscal;
     VMF w0_force_cart(nlev);
     for (int lev = 0; lev < nlev; ++lev) w0_force_cart[lev].define(H.S[lev].L.ba, 3, 1, -1, 0.0);
     if (p->evolve_base_state)
@@ -1915,6 +1919,164 @@ static int run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const 
 
 }  // namespace mo
 
+static mo::Arr arr_of(const mo_fab* f) {
+    mo::Arr a;
+    a.p = f->p;
+    for (int d = 0; d < 3; ++d) {
+        a.lo[d] = f->lo[d];
+        a.hi[d] = f->hi[d];
+    }
+    const long nx = f->hi[0] - f->lo[0] + 1, ny = f->hi[1] - f->lo[1] + 1, nz = f->hi[2] - f->lo[2] + 1;
+    a.sj = nx;
+    a.sk = nx * ny;
+    a.sn = nx * ny * nz;
+    a.nc = f->nc;
+    return a;
+}
+
+// ---------------------------------------------------------------------- one member function
+namespace mo {
+// Argument FABs: args[slot * nboxes + b] is box b's FAB of argument `slot` (p == NULL when
+// the function does not take that argument).
+static Box fab_box(const mo_fab& f) {
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = f.lo[d];
+        b.hi[d] = f.hi[d];
+    }
+    return b;
+}
+static Box intersect(const Box& a, const Box& b) {
+    Box r;
+    for (int d = 0; d < 3; ++d) {
+        r.lo[d] = std::max(a.lo[d], b.lo[d]);
+        r.hi[d] = std::min(a.hi[d], b.hi[d]);
+    }
+    return r;
+}
+// an input MF from the caller's FABs: every FAB must cover the box grown by ng (in_out: the
+// caller's data is copied where it exists, zero elsewhere)
+static void mf_in(MF& mf, const std::vector<Box>& ba, const mo_fab* f, int nc, int ng, int ix, bool in_out = false) {
+    mf.define(ba, nc, ng, ix, 0.0);
+    for (int b = 0; b < mf.size(); ++b) {
+        if (!f[b].p || f[b].nc < nc) throw std::runtime_error("missing argument FAB or too few components");
+        const Box need = mf.fabbox(b), have = fab_box(f[b]);
+        Box r = intersect(need, have);
+        if (!in_out)
+            for (int d = 0; d < 3; ++d)
+                if (have.lo[d] > need.lo[d] || have.hi[d] < need.hi[d])
+                    throw std::runtime_error("argument FAB does not cover its box and ghost cells");
+        const Arr src = arr_of(&f[b]);
+        for (int n = 0; n < nc; ++n) MO_FOR3(r) mf[b](i, j, k, n) = src(i, j, k, n);
+    }
+}
+// components c0 .. c0+nc of an MF back into the caller's FABs, on the valid box grown by ng
+static void mf_out(const MF& mf, const mo_fab* f, int c0, int nc, int ng) {
+    for (int b = 0; b < mf.size(); ++b) {
+        const Box r = intersect(grow(mf.validbox(b), std::min(ng, mf.ng)), fab_box(f[b]));
+        const Arr dst = arr_of(&f[b]);
+        for (int n = c0; n < c0 + nc; ++n) MO_FOR3(r) dst(i, j, k, n) = mf[b](i, j, k, n);
+    }
+}
+
+static int member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
+                  int start_comp, int num_comp, int is_cons, const mo_fab* args) {
+    if (which_step != 1 && which_step != 2) throw std::runtime_error("which_step must be 1 or 2");
+    if (p->dim == 2) throw std::runtime_error("mo_member is 3-D");
+    Stage H;
+    setup_stage(H, p, 1, &nboxes, boxes, base);
+    Lev& S = H.S[0];
+    const std::vector<Box>& ba = S.L.ba;
+    const int nscal = H.nscal, ng_s = H.ng_s, nga = H.ng_adv;
+    auto A = [&](int slot) { return args + (long)slot * nboxes; };
+    VMF m1(1), m2(1), m3(1), m4(1);
+    VF f1(1), f2(1), f3(1);
+    switch (fn) {
+        case MO_MAKE_UTRANS: {  // Maestro::MakeUtrans (Source/MaestroMakeUtrans.cpp:6-648)
+            mf_in(m1[0], ba, A(MO_UTILDE), 3, nga, -1);
+            mf_in(m2[0], ba, A(MO_UFULL), 3, nga, -1);
+            for (int d = 0; d < 3; ++d) f1[0][d].define(ba, 1, 1, d, 0.0);
+            H.MakeUtrans(m1, m2, f1);
+            for (int d = 0; d < 3; ++d) mf_out(f1[0][d], A(MO_UTRANS0 + d), 0, 1, 1);
+            break;
+        }
+        case MO_VEL_PRED: {  // Maestro::VelPred (Source/MaestroVelPred.cpp:5-292)
+            mf_in(m1[0], ba, A(MO_UTILDE), 3, nga, -1);
+            mf_in(m2[0], ba, A(MO_UFULL), 3, nga, -1);
+            mf_in(m3[0], ba, A(MO_FORCE), 3, 1, -1);
+            for (int d = 0; d < 3; ++d) {
+                mf_in(f1[0][d], ba, A(MO_UTRANS0 + d), 1, 1, d);
+                f2[0][d].define(ba, 1, 1, d, 0.0);
+            }
+            H.VelPred(m1, m2, f1, f2, m3);
+            for (int d = 0; d < 3; ++d) mf_out(f2[0][d], A(MO_UMAC0 + d), 0, 1, 0);
+            break;
+        }
+        case MO_MAKE_EDGE_SCAL: {  // Maestro::MakeEdgeScal (Source/MaestroMakeEdgeScalars.cpp:6-302)
+            if (start_comp < 0 || num_comp < 1 || start_comp + num_comp > nscal)
+                throw std::runtime_error("component range outside the state");
+            mf_in(m1[0], ba, A(MO_STATE), nscal, ng_s, -1);
+            mf_in(m2[0], ba, A(MO_FORCE), nscal, 1, -1);
+            for (int d = 0; d < 3; ++d) {
+                mf_in(f1[0][d], ba, A(MO_UMAC0 + d), 1, 1, d);
+                f2[0][d].define(ba, nscal, 0, d, 0.0);
+            }
+            H.MakeEdgeScal(m1, f2, f1, m2, H.bcs_s(), start_comp, start_comp, num_comp, is_cons != 0);
+            for (int d = 0; d < 3; ++d) mf_out(f2[0][d], A(MO_SEDGE0 + d), start_comp, num_comp, 0);
+            break;
+        }
+        case MO_MAKE_RHOX_FLUX:    // Maestro::MakeRhoXFlux (Source/MaestroMakeFlux.cpp:18-465)
+        case MO_MAKE_RHOH_FLUX: {  // Maestro::MakeRhoHFlux (Source/MaestroMakeFlux.cpp:467-1067)
+            const bool x = fn == MO_MAKE_RHOX_FLUX;
+            for (int d = 0; d < 3; ++d) {
+                mf_in(f1[0][d], ba, A(MO_SEDGE0 + d), nscal, 0, d);
+                mf_in(f2[0][d], ba, A(MO_UMAC0 + d), 1, 0, d);
+                f3[0][d].define(ba, nscal, 0, d, 0.0);
+            }
+            const BS s0o = H.bs(x ? &Lev::rho0_old : &Lev::rhoh0_old);
+            const BS s0n = which_step == 1 ? s0o : H.bs(x ? &Lev::rho0_new : &Lev::rhoh0_new);
+            BS s0eo(1), s0en(1);
+            if (!p->spherical) {
+                H.CelltoEdge(s0o, s0eo);
+                H.CelltoEdge(s0n, s0en);
+            }
+            if (x) {
+                if (start_comp != FirstSpec || num_comp != H.nspec)
+                    throw std::runtime_error("MakeRhoXFlux: the species FirstSpec .. FirstSpec+NumSpec-1");
+                if (A(MO_ETA)[0].p) mf_in(m1[0], ba, A(MO_ETA), 1, 0, 2);
+                else m1[0].define(ba, 1, 0, 2, 0.0);
+                H.MakeRhoXFlux(f3, m1, f1, f2, s0o, s0eo, s0n, s0en, start_comp, num_comp);
+                for (int d = 0; d < 3; ++d) {
+                    mf_out(f3[0][d], A(MO_SFLUX0 + d), Rho, 1, 0);
+                    mf_out(f3[0][d], A(MO_SFLUX0 + d), FirstSpec, H.nspec, 0);
+                }
+                if (A(MO_ETA)[0].p) mf_out(m1[0], A(MO_ETA), 0, 1, 0);
+            } else {
+                H.MakeRhoHFlux(f3, f1, f2, s0o, s0eo, s0n, s0en);
+                for (int d = 0; d < 3; ++d) mf_out(f3[0][d], A(MO_SFLUX0 + d), RhoH, 1, 0);
+            }
+            break;
+        }
+        case MO_UPDATE_SCAL: {  // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
+            if (!((start_comp == RhoH && num_comp == 1) || (start_comp == FirstSpec && num_comp == H.nspec)))
+                throw std::runtime_error("UpdateScal: RhoH, or the species");
+            mf_in(m1[0], ba, A(MO_STATE), nscal, 0, -1);
+            mf_in(m2[0], ba, A(MO_SNEW), nscal, ng_s, -1, true);
+            mf_in(m3[0], ba, A(MO_FORCE), nscal, 0, -1);
+            for (int d = 0; d < 3; ++d) mf_in(f1[0][d], ba, A(MO_SFLUX0 + d), nscal, 0, d);
+            H.UpdateScal(m1, m2, f1, m3, start_comp, num_comp);
+            mf_out(m2[0], A(MO_SNEW), start_comp, num_comp, ng_s);
+            if (start_comp == FirstSpec) mf_out(m2[0], A(MO_SNEW), Rho, 1, ng_s);
+            break;
+        }
+        default:
+            throw std::runtime_error("unknown member function");
+    }
+    return 0;
+}
+
+}  // namespace mo
+
 extern "C" {
 
 int mo_run_stage_levels(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
@@ -1959,20 +2121,6 @@ int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {
     return 0;
 }
 
-static mo::Arr arr_of(const mo_fab* f) {
-    mo::Arr a;
-    a.p = f->p;
-    for (int d = 0; d < 3; ++d) {
-        a.lo[d] = f->lo[d];
-        a.hi[d] = f->hi[d];
-    }
-    const long nx = f->hi[0] - f->lo[0] + 1, ny = f->hi[1] - f->lo[1] + 1, nz = f->hi[2] - f->lo[2] + 1;
-    a.sj = nx;
-    a.sk = nx * ny;
-    a.sn = nx * ny * nz;
-    a.nc = f->nc;
-    return a;
-}
 
 int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const mo_fab* u, const mo_fab* v,
            const mo_fab* w, int is_umac, const int* bc, const mo_fab* Ip, const mo_fab* Im) {
@@ -1992,6 +2140,16 @@ int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const m
         }
         mo::PPM(pc, b, arr_of(s), arr_of(u), arr_of(v), arr_of(w), arr_of(Ip), arr_of(Im), r, is_umac != 0, comp);
         return 0;
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+
+int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
+              int start_comp, int num_comp, int is_conservative, const mo_fab* args) {
+    try {
+        return mo::member(p, nboxes, boxes, base, fn, which_step, start_comp, num_comp, is_conservative, args);
     } catch (const std::exception& e) {
         mo::g_err = e.what();
         return -1;

@@ -111,6 +111,26 @@ typedef struct {
 int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const mo_fab* u, const mo_fab* v,
            const mo_fab* w, int is_umac, const int* bc, const mo_fab* Ip, const mo_fab* Im);
 
+/* One Maestro member function of the stage on one 3-D level, on caller FABs that hold
+ * ghost cells as the caller filled them: args[slot * nboxes + b] is box b's FAB of argument
+ * `slot` (p = NULL for arguments the function does not take).  base gives the base state
+ * (only the 1-D arrays are read); which_step 1 passes the old base state as "new" to the
+ * fluxes, 2 the new one.  Outputs are written on the valid region grown by the ghost cells
+ * the reference fills (utrans 1, statenew ng_s), where the caller's FAB has them. */
+enum {
+    MO_UTILDE, MO_UFULL, MO_UTRANS0, MO_UTRANS1, MO_UTRANS2, MO_UMAC0, MO_UMAC1, MO_UMAC2, MO_FORCE, MO_STATE,
+    MO_SNEW, MO_SEDGE0, MO_SEDGE1, MO_SEDGE2, MO_SFLUX0, MO_SFLUX1, MO_SFLUX2, MO_ETA, MO_NSLOT
+};
+enum { MO_MAKE_UTRANS, MO_VEL_PRED, MO_MAKE_EDGE_SCAL, MO_MAKE_RHOX_FLUX, MO_MAKE_RHOH_FLUX, MO_UPDATE_SCAL };
+/*   MO_MAKE_UTRANS    MakeUtrans(utilde, ufull, utrans)
+ *   MO_VEL_PRED       VelPred(utilde, ufull, utrans, umac, force)
+ *   MO_MAKE_EDGE_SCAL MakeEdgeScal(state, sedge, umac, force, bcs_s, start, start, num, is_conservative)
+ *   MO_MAKE_RHOX_FLUX MakeRhoXFlux(sflux, etarhoflux (may be absent), sedge, umac, start, num)
+ *   MO_MAKE_RHOH_FLUX MakeRhoHFlux(sflux, sedge, umac)
+ *   MO_UPDATE_SCAL    UpdateScal(state, snew, sflux, force, start, num) */
+int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
+              int start_comp, int num_comp, int is_conservative, const mo_fab* args);
+
 /* 1-D CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), single level. */
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge);
 

@@ -248,3 +248,46 @@ def ppm(params, bx, s, s_lo, comp, vel, vel_lo, is_umac, bc, checked=True):
     if rc != 0:
         raise RuntimeError("oracle: " + L.mo_last_error().decode())
     return Ip, Im
+
+
+MO_SLOT = dict(utilde=0, ufull=1, utrans=2, umac=5, force=8, state=9, snew=10, sedge=11, sflux=14, eta=17)
+MO_FACE_SLOTS = ("utrans", "umac", "sedge", "sflux")
+MO_NSLOT = 18
+MO_FN = dict(make_utrans=0, vel_pred=1, make_edge_scal=2, make_rhox_flux=3, make_rhoh_flux=4, update_scal=5)
+
+
+def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservative=0, checked=True):
+    """Oracle mo_member: one Maestro member function on caller FABs.  args maps a slot name
+    to the per-box FABs [(array [nc, nz, ny, nx], lo), ...] (three such lists, one per
+    direction, for utrans / umac / sedge / sflux).  Outputs are written into the arrays."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    nb = len(cfg["boxes"])
+    tab = (MoFab * (MO_NSLOT * nb))()
+    keep = []
+    for name, v in args.items():
+        lists = v if name in MO_FACE_SLOTS else [v]
+        for d, fabs in enumerate(lists):
+            assert len(fabs) == nb
+            for b, (a, lo) in enumerate(fabs):
+                assert a.dtype == np.float64 and a.flags.c_contiguous
+                f, _ = fab_of(a, lo)
+                tab[(MO_SLOT[name] + d) * nb + b] = f
+                keep.append(a)
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    inp = MoInputs()
+    for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                 "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+        setattr(inp, name, arr(cfg[name]))
+    boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    L = lib(checked)
+    L.mo_member.restype = C.c_int
+    rc = L.mo_member(C.byref(p), nb, boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp), MO_FN[fn],
+                     which_step, start_comp, num_comp, is_conservative, tab)
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.mo_last_error().decode())

@@ -184,3 +184,50 @@ def test_spherical_star_conserves_mass_and_stays_finite():
     assert sn[0].min() >= 0.99 * so[0].min()
     # the species densities still sum to the density
     assert np.abs(sn[4:].sum(axis=0) - sn[0]).max() <= 1e-10 * sn[0].max()
+
+
+@pytest.mark.parametrize("ppm_type", [1, 2, 0])
+def test_member_functions_keep_uniform_fields(ppm_type):
+    """pyoracle.member (the per-function oracle entry the GPU entry points are checked
+    against): in a periodic domain a uniform velocity gives MakeUtrans / VelPred faces equal
+    to it, MakeEdgeScal of a uniform state with no force gives edge states equal to the state,
+    and UpdateScal with a uniform flux and no force leaves the state unchanged."""
+    from members import MemberInputs, zeros_like
+    cfg = configs.planar_config(n=(16, 16, 16), max_grid=8, ppm_type=ppm_type, bc_lo=(INTERIOR,) * 3,
+                                bc_hi=(INTERIOR,) * 3, w0_amp=0.0)
+    inp = MemberInputs(cfg)
+    u0 = np.array([3.0e5, -2.0e5, 1.5e5])
+    s0 = np.abs(cfg["sold"]).reshape(inp.nscal, -1).mean(axis=1)
+    inp.utilde[...] = u0[:, None, None, None]
+    inp.ufull[...] = u0[:, None, None, None]
+    inp.vel_force[...] = 0.0
+    inp.state[...] = s0[:, None, None, None]
+    inp.scal_force[...] = 0.0
+    for d in range(3):
+        inp.uface[d][...] = u0[d]
+        inp.sflux[d][...] = (s0 * u0[d])[:, None, None, None]
+    g = inp.ng
+    ut, uf = inp.fabs("utilde", g), inp.fabs("ufull", g)
+    utr = [zeros_like(f) for f in inp.fabs("uface", 1)]
+    pyoracle.member(cfg, "make_utrans", {"utilde": ut, "ufull": uf, "utrans": utr})
+    umac = [zeros_like(f) for f in inp.fabs("uface", 0)]
+    pyoracle.member(cfg, "vel_pred", {"utilde": ut, "ufull": uf, "utrans": inp.fabs("uface", 1),
+                                      "force": inp.fabs("vel_force", 1), "umac": umac})
+    for d in range(3):
+        for (a, _), (m, _) in zip(utr[d], umac[d]):
+            assert np.allclose(a, u0[d], rtol=1e-13, atol=0) and np.allclose(m, u0[d], rtol=1e-13, atol=0)
+    se = [zeros_like(f) for f in inp.fabs("sedge", 0)]
+    pyoracle.member(cfg, "make_edge_scal", {"state": inp.fabs("state", g), "umac": inp.fabs("uface", 1),
+                                            "force": inp.fabs("scal_force", 1), "sedge": se},
+                    start_comp=FIRSTSPEC, num_comp=inp.nspec)
+    for d in range(3):
+        for a, _ in se[d]:
+            for c in range(FIRSTSPEC, inp.nscal):
+                assert np.allclose(a[c], s0[c], rtol=1e-13, atol=0)
+    sn = zeros_like(inp.fabs("state", g))
+    for start, num in ((FIRSTSPEC, inp.nspec), (RHOH, 1)):
+        pyoracle.member(cfg, "update_scal", {"state": inp.fabs("state", 0), "snew": sn, "sflux": inp.fabs("sflux", 0),
+                                             "force": inp.fabs("scal_force", 0)}, start_comp=start, num_comp=num)
+    for a, _ in sn:
+        for c in [RHO, RHOH] + list(range(FIRSTSPEC, inp.nscal)):
+            assert np.allclose(a[c], s0[c], rtol=1e-13, atol=0), c
