@@ -34,7 +34,7 @@ struct Lev {
     int nspec = 0, nscal = 0, nb = 0, nr = 0;
     int ng_s = 3, ng_adv = 3;
     std::vector<BCRec> bcs_s, bcs_u, bcs_f;
-    std::vector<double> rho0_old, rho0_new, rhoh0_old, rhoh0_new, p0_old, p0_new, psi, grav_cell,
+    std::vector<real> rho0_old, rho0_new, rhoh0_old, rhoh0_new, p0_old, p0_new, psi, grav_cell,
         w0_force, w0, rho0_predicted_edge;
     MF w0_cart;  // 3 comps, 2 ghosts
     MF gpi, thermal;
@@ -74,7 +74,7 @@ struct Lev {
     }
     // Put1dArrayOnCart, spherical, exact base state (Source/MaestroFill3dData.cpp:94-192):
     // edge-centred input with w0_interp_type 2 (linear), cell-centred input injected
-    void Put1dSphr(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec) {
+    void Put1dSphr(const std::vector<real>& s0, MF& s0_cart, bool edge, bool vec) {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = s0_cart[b];
             MO_FOR3(L.ba[b]) {
@@ -82,7 +82,7 @@ struct Lev {
                 sph_xyz(i, j, k, x, y, z);
                 const double radius = std::sqrt(x * x + y * y + z * z);
                 const int index = cc_to_r(i, j, k);
-                double v;
+                real v;
                 if (edge) {
                     double rfac;
                     if (index < nr) {
@@ -148,7 +148,7 @@ struct Lev {
 
     // Maestro::Put1dArrayOnCart, planar branch, one level (Source/MaestroFill3dData.cpp:42-93):
     // valid cells from the level's 1-D array.
-    void Put1d(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec) {
+    void Put1d(const std::vector<real>& s0, MF& s0_cart, bool edge, bool vec) {
         const int outcomp = vec ? 2 : 0;
         for (int b = 0; b < nb; ++b) {
             const Arr& a = s0_cart[b];
@@ -161,7 +161,7 @@ struct Lev {
 
     // Maestro::CelltoEdge (Source/MaestroCelltoEdge.cpp:17-54) on one chunk [lo, hi] of
     // edges of a level with nr_lev cells; edges outside the chunk are left alone.
-    static void CelltoEdgeChunk(const std::vector<double>& c, std::vector<double>& e, int lo, int hi) {
+    static void CelltoEdgeChunk(const std::vector<real>& c, std::vector<real>& e, int lo, int hi) {
         const int nr_lev = (int)c.size();
         for (int r = lo; r <= hi; ++r) {
             if (r == 0) {
@@ -173,15 +173,15 @@ struct Lev {
             } else if (r == nr_lev - 1 || r == hi) {
                 e[r] = 0.5 * (c[r] + c[r - 1]);
             } else {
-                double tmp = 7.0 / 12.0 * (c[r] + c[r - 1]) - 1.0 / 12.0 * (c[r + 1] + c[r - 2]);
-                double s0min = mn(c[r], c[r - 1]);
-                double s0max = mx(c[r], c[r - 1]);
+                real tmp = 7.0 / 12.0 * (c[r] + c[r - 1]) - 1.0 / 12.0 * (c[r + 1] + c[r - 2]);
+                real s0min = mn(c[r], c[r - 1]);
+                real s0max = mx(c[r], c[r - 1]);
                 e[r] = mn(mx(tmp, s0min), s0max);
             }
         }
     }
     // one level, one chunk spanning the level
-    static void CelltoEdge(const std::vector<double>& c, std::vector<double>& e) {
+    static void CelltoEdge(const std::vector<real>& c, std::vector<real>& e) {
         e.assign(c.size() + 1, 0.0);
         CelltoEdgeChunk(c, e, 0, (int)c.size());
     }
@@ -263,7 +263,7 @@ struct Lev {
     }
 
     // Maestro::Addw0, planar, one level (Source/MaestroFill3dData.cpp:365-423)
-    void Addw0(MF* uedge, double mult) {
+    void Addw0(MF* uedge, real mult) {
         if (P.spherical) {  // Source/MaestroFill3dData.cpp:395-419: valid faces += mult w0mac
             for (int b = 0; b < nb; ++b)
                 for (int d = 0; d < 3; ++d) {
@@ -283,7 +283,7 @@ struct Lev {
     // ------------------------------------------------------------------ MakeUtrans
     // Maestro::MakeUtrans, 3-D, one level (Source/MaestroMakeUtrans.cpp:6-56, 270-628)
     void MakeUtrans(MF& utilde, MF& ufull, MF* utrans) {
-        const double dt2 = 0.5 * dt;
+        const real dt2 = 0.5 * dt;
         const int* domlo = L.dom.lo;
         const int* domhi = L.dom.hi;
         MF Ip, Im;
@@ -311,7 +311,7 @@ struct Lev {
                 const int di = d == 0, dj = d == 1, dk = d == 2;
                 MO_FOR3(xbx) {
                     const int I = d == 0 ? i : (d == 1 ? j : k);
-                    double l = 0.0, r = 0.0;
+                    real l = 0.0, r = 0.0;
                     if (P.ppm_type == 0) {
                         l = ut(i - di, j - dj, k - dk, d) +
                             (0.5 - (dt2 / L.dx[d]) * mx(0.0, uf(i - di, j - dj, k - dk, d))) *
@@ -337,18 +337,18 @@ struct Lev {
                         }
                     }
                     if (P.spherical) {  // Source/MaestroMakeUtrans.cpp:368-377: with w0mac
-                        const double w0c = w0mac[d][b](i, j, k);
+                        const real w0c = w0mac[d][b](i, j, k);
                         bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fab(l + r + 2.0 * w0c) < rel_eps);
-                        double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+                        real v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
                         tr(i, j, k) = test ? 0.0 : v;
                     } else if (d < 2) {
                         bool test = (l <= 0.0 && r >= 0.0) || (fab(l + r) < rel_eps);
-                        double v = 0.5 * (l + r) > 0.0 ? l : r;
+                        real v = 0.5 * (l + r) > 0.0 ? l : r;
                         tr(i, j, k) = test ? 0.0 : v;
                     } else {
-                        const double w0c = w0a(i, j, k, 2);
+                        const real w0c = w0a(i, j, k, 2);
                         bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fab(l + r + 2.0 * w0c) < rel_eps);
-                        double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+                        real v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
                         tr(i, j, k) = test ? 0.0 : v;
                     }
                 }
@@ -363,7 +363,7 @@ struct Lev {
         if (P.spherical) {
             // Source/MaestroForce.cpp:151-252; the exact base state has gradw0 = 0
             // (:30-41), so the utilde term subtracts Ut.e_r * 0 * e_r
-            const double gradw0 = 0.0;
+            const real gradw0 = 0.0;
             for (int b = 0; b < nb; ++b) {
                 const Arr& gpi_arr = gpi[b];
                 const Arr& rho_arr = sold[b];
@@ -379,12 +379,12 @@ struct Lev {
                     sph_xyz(i, j, k, x, y, z);
                     const double inv_radius = 1.0 / std::sqrt(x * x + y * y + z * z);  // MakeNormal
                     const double nrm[3] = {x * inv_radius, y * inv_radius, z * inv_radius};
-                    double rhopert = rho_arr(i, j, k) - r0(i, j, k);
+                    real rhopert = rho_arr(i, j, k) - r0(i, j, k);
                     if (rho_arr(i, j, k) < (P.buoyancy_cutoff_factor * P.base_cutoff_density)) rhopert = 0.0;
                     for (int dim = 0; dim < 3; ++dim)
                         vf(i, j, k, dim) =
                             (rhopert * grav(i, j, k, dim) - gpi_arr(i, j, k, dim)) / rho_arr(i, j, k) - w0f(i, j, k, dim);
-                    const double ut_dot_er = 0.5 * (ue(i, j, k) + ue(i + 1, j, k)) * nrm[0] +
+                    const real ut_dot_er = 0.5 * (ue(i, j, k) + ue(i + 1, j, k)) * nrm[0] +
                                              0.5 * (ve(i, j, k) + ve(i, j + 1, k)) * nrm[1] +
                                              0.5 * (we(i, j, k) + we(i, j, k + 1)) * nrm[2];
                     for (int dim = 0; dim < 3; ++dim) vf(i, j, k, dim) -= ut_dot_er * gradw0 * nrm[dim];
@@ -403,7 +403,7 @@ struct Lev {
             const Arr& r0 = rho0_cart[b];
             const Arr& vf = vel_force[b];
             MO_FOR3(L.ba[b]) {
-                double rhopert = rho_arr(i, j, k) - r0(i, j, k);
+                real rhopert = rho_arr(i, j, k) - r0(i, j, k);
                 if (rho_arr(i, j, k) < (P.buoyancy_cutoff_factor * P.base_cutoff_density)) rhopert = 0.0;
                 for (int dim = 0; dim < 2; ++dim) vf(i, j, k, dim) = -gpi_arr(i, j, k, dim) / rho_arr(i, j, k);
                 vf(i, j, k, 2) = (rhopert * grav(i, j, k, 2) - gpi_arr(i, j, k, 2)) / rho_arr(i, j, k) - w0f(i, j, k, 2);
@@ -419,10 +419,10 @@ struct Lev {
     // ------------------------------------------------------------------ VelPred
     // Maestro::VelPred, 3-D, one level (Source/MaestroVelPred.cpp:5-288, 735-1915)
     void VelPred(MF& utilde, MF& ufull, MF* utrans, MF* umac, MF& force) {
-        const double dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt6 = dt / 6.0;
+        const real dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt6 = dt / 6.0;
         const int* domlo = L.dom.lo;
         const int* domhi = L.dom.hi;
-        const double h[3] = {L.dx[0], L.dx[1], L.dx[2]};
+        const real h[3] = {L.dx[0], L.dx[1], L.dx[2]};
         // Ipu..Imw: per velocity component c, 3 directional comps, 1 ghost
         MF Ipc[3], Imc[3];
         for (int c = 0; c < 3; ++c) {
@@ -469,8 +469,8 @@ struct Lev {
                 MO_FOR3(mbx) {
                     const int I = d == 0 ? i : (d == 1 ? j : k);
                     if (P.ppm_type == 0) {
-                        double maxu = 0.5 - dt2 * mx(0.0, uf(i - di, j - dj, k - dk, d)) / h[d];
-                        double minu = 0.5 + dt2 * mn(0.0, uf(i, j, k, d)) / h[d];
+                        real maxu = 0.5 - dt2 * mx(0.0, uf(i - di, j - dj, k - dk, d)) / h[d];
+                        real minu = 0.5 + dt2 * mn(0.0, uf(i, j, k, d)) / h[d];
                         for (int n = 0; n < 3; ++n) {
                             l(i, j, k, n) = ut(i - di, j - dj, k - dk, n) + maxu * slope(i - di, j - dj, k - dk, n);
                             r(i, j, k, n) = ut(i, j, k, n) - minu * slope(i, j, k, n);
@@ -532,7 +532,7 @@ struct Lev {
                     }
                     for (int n = 0; n < 3; ++n) {
                         if (n == d) continue;
-                        double v = tr(i, j, k) > 0.0 ? l(i, j, k, n) : r(i, j, k, n);
+                        real v = tr(i, j, k) > 0.0 ? l(i, j, k, n) : r(i, j, k, n);
                         im(i, j, k, n) = fab(tr(i, j, k)) < rel_eps ? 0.5 * (l(i, j, k, n) + r(i, j, k, n)) : v;
                     }
                 }
@@ -555,9 +555,9 @@ struct Lev {
                     MO_FOR3(imhbox) {
                         const int I = d == 0 ? i : (d == 1 ? j : k);
                         const int il = i - di, jl = j - dj, kl = k - dk;
-                        double lq = l(i, j, k, c) - (dt6 / h[t]) * (trt(il + ti, jl + tj, kl + tk) + trt(il, jl, kl)) *
+                        real lq = l(i, j, k, c) - (dt6 / h[t]) * (trt(il + ti, jl + tj, kl + tk) + trt(il, jl, kl)) *
                                                         (imt(il + ti, jl + tj, kl + tk, c) - imt(il, jl, kl, c));
-                        double rq = r(i, j, k, c) - (dt6 / h[t]) * (trt(i + ti, j + tj, k + tk) + trt(i, j, k)) *
+                        real rq = r(i, j, k, c) - (dt6 / h[t]) * (trt(i + ti, j + tj, k + tk) + trt(i, j, k)) *
                                                         (imt(i + ti, j + tj, k + tk, c) - imt(i, j, k, c));
                         if (I == domlo[d]) {
                             switch (bclo) {
@@ -574,7 +574,7 @@ struct Lev {
                                 default: break;
                             }
                         }
-                        double v = trd(i, j, k) > 0.0 ? lq : rq;
+                        real v = trd(i, j, k) > 0.0 ? lq : rq;
                         out(i, j, k) = fab(trd(i, j, k)) < rel_eps ? 0.5 * (lq + rq) : v;
                     }
                 }
@@ -598,33 +598,33 @@ struct Lev {
                 MO_FOR3(xbx) {
                     const int I = d == 0 ? i : (d == 1 ? j : k);
                     const int il = i - di, jl = j - dj, kl = k - dk;
-                    double fl = f(il, jl, kl, d);
-                    double fr = f(i, j, k, d);
-                    double ml = l(i, j, k, d) -
+                    real fl = f(il, jl, kl, d);
+                    real fr = f(i, j, k, d);
+                    real ml = l(i, j, k, d) -
                                 (dt4 / h[t1]) * (tr1(il + a1i, jl + a1j, kl + a1k) + tr1(il, jl, kl)) *
                                     (q1(il + a1i, jl + a1j, kl + a1k) - q1(il, jl, kl)) -
                                 (dt4 / h[t2]) * (tr2(il + a2i, jl + a2j, kl + a2k) + tr2(il, jl, kl)) *
                                     (q2(il + a2i, jl + a2j, kl + a2k) - q2(il, jl, kl)) +
                                 dt2 * fl;
-                    double mr = r(i, j, k, d) -
+                    real mr = r(i, j, k, d) -
                                 (dt4 / h[t1]) * (tr1(i + a1i, j + a1j, k + a1k) + tr1(i, j, k)) *
                                     (q1(i + a1i, j + a1j, k + a1k) - q1(i, j, k)) -
                                 (dt4 / h[t2]) * (tr2(i + a2i, j + a2j, k + a2k) + tr2(i, j, k)) *
                                     (q2(i + a2i, j + a2j, k + a2k) - q2(i, j, k)) +
                                 dt2 * fr;
                     if (P.spherical) {  // Source/MaestroVelPred.cpp:1664-1673: with w0mac
-                        const double w0c = w0mac[d][b](i, j, k);
+                        const real w0c = w0mac[d][b](i, j, k);
                         bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fab(ml + mr + 2.0 * w0c) < rel_eps);
-                        double v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+                        real v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
                         out(i, j, k) = test ? 0.0 : v;
                     } else if (d < 2) {
                         bool test = (ml <= 0.0 && mr >= 0.0) || (fab(ml + mr) < rel_eps);
-                        double v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+                        real v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
                         out(i, j, k) = test ? 0.0 : v;
                     } else {
-                        const double w0c = w0a(i, j, k, 2);
+                        const real w0c = w0a(i, j, k, 2);
                         bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fab(ml + mr + 2.0 * w0c) < rel_eps);
-                        double v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+                        real v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
                         out(i, j, k) = test ? 0.0 : v;
                     }
                     if (I == domlo[d]) {
@@ -663,7 +663,7 @@ struct Lev {
         const bool is_vel = false;
         const int* domlo = L.dom.lo;
         const int* domhi = L.dom.hi;
-        const double h[3] = {L.dx[0], L.dx[1], L.dx[2]};
+        const real h[3] = {L.dx[0], L.dx[1], L.dx[2]};
         MF Ip, Im;
         Ip.define(L.ba, 3, 1);
         Im.define(L.ba, 3, 1);
@@ -680,7 +680,7 @@ struct Lev {
         for (int d = 0; d < 3; ++d)
             for (int t = 0; t < 3; ++t)
                 if (d != t) simh2[d][t].define(L.ba, 1, 1, -1, 0.0);
-        const double dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt3 = dt / 3.0, dt6 = dt / 6.0;
+        const real dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt3 = dt / 3.0, dt6 = dt / 6.0;
 
         for (int scomp = start_scomp; scomp < start_scomp + num_comp; ++scomp) {
             const int bccomp = start_bccomp + scomp - start_scomp;
@@ -777,7 +777,7 @@ struct Lev {
                         MO_FOR3(imhbox) {
                             const int I = d == 0 ? i : (d == 1 ? j : k);
                             const int il = i - di, jl = j - dj, kl = k - dk;
-                            double lq, rq;
+                            real lq, rq;
                             if (is_conservative) {
                                 lq = l(i, j, k) -
                                      (dt3 / h[t]) * (st(il + ti, jl + tj, kl + tk) * ut(il + ti, jl + tj, kl + tk) -
@@ -848,9 +848,9 @@ struct Lev {
                     MO_FOR3(xbx) {
                         const int I = d == 0 ? i : (d == 1 ? j : k);
                         const int il = i - di, jl = j - dj, kl = k - dk;
-                        double fl = f(il, jl, kl, comp);
-                        double fr = f(i, j, k, comp);
-                        double lq, rq;
+                        real fl = f(il, jl, kl, comp);
+                        real fr = f(i, j, k, comp);
+                        real lq, rq;
                         if (is_conservative) {
                             lq = l(i, j, k) -
                                  (dt2 / h[t1]) * (q1(il + a1i, jl + a1j, kl + a1k) * u1(il + a1i, jl + a1j, kl + a1k) -
@@ -879,7 +879,7 @@ struct Lev {
                                      (q2(i + a2i, j + a2j, k + a2k) - q2(i, j, k)) +
                                  dt2 * fr;
                         }
-                        double v = (ud(i, j, k) > 0.0) ? lq : rq;
+                        real v = (ud(i, j, k) > 0.0) ? lq : rq;
                         v = (fab(ud(i, j, k)) > rel_eps) ? v : 0.5 * (lq + rq);
                         if (I == domlo[d]) {
                             int bclo = bc_lo[d];
@@ -919,19 +919,19 @@ struct Lev {
                 const Arr& s0a = s0_cart[b];
                 const Arr force = scal_force[b].comp(comp);
                 MO_FOR3(L.ba[b]) {
-                    const double divu_c = 0.0;
-                    double divumac = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
+                    const real divu_c = 0.0;
+                    real divumac = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
                                      (wm(i, j, k + 1) - wm(i, j, k)) / dx[2];
                     if (fullform == 1) {
                         force(i, j, k) -= scal(i, j, k) * (divumac + divu_c);
                     } else {
-                        const double s0x_hi = i < domhi[0] ? 0.5 * (s0a(i, j, k) + s0a(i + 1, j, k)) : s0a(i, j, k);
-                        const double s0x_lo = i > domlo[0] ? 0.5 * (s0a(i, j, k) + s0a(i - 1, j, k)) : s0a(i, j, k);
-                        const double s0y_hi = j < domhi[1] ? 0.5 * (s0a(i, j, k) + s0a(i, j + 1, k)) : s0a(i, j, k);
-                        const double s0y_lo = j > domlo[1] ? 0.5 * (s0a(i, j, k) + s0a(i, j - 1, k)) : s0a(i, j, k);
-                        const double s0z_hi = k < domhi[2] ? 0.5 * (s0a(i, j, k) + s0a(i, j, k + 1)) : s0a(i, j, k);
-                        const double s0z_lo = k > domlo[2] ? 0.5 * (s0a(i, j, k) + s0a(i, j, k - 1)) : s0a(i, j, k);
-                        double divs0u = (um(i + 1, j, k) * s0x_hi - um(i, j, k) * s0x_lo) / dx[0] +
+                        const real s0x_hi = i < domhi[0] ? 0.5 * (s0a(i, j, k) + s0a(i + 1, j, k)) : s0a(i, j, k);
+                        const real s0x_lo = i > domlo[0] ? 0.5 * (s0a(i, j, k) + s0a(i - 1, j, k)) : s0a(i, j, k);
+                        const real s0y_hi = j < domhi[1] ? 0.5 * (s0a(i, j, k) + s0a(i, j + 1, k)) : s0a(i, j, k);
+                        const real s0y_lo = j > domlo[1] ? 0.5 * (s0a(i, j, k) + s0a(i, j - 1, k)) : s0a(i, j, k);
+                        const real s0z_hi = k < domhi[2] ? 0.5 * (s0a(i, j, k) + s0a(i, j, k + 1)) : s0a(i, j, k);
+                        const real s0z_lo = k > domlo[2] ? 0.5 * (s0a(i, j, k) + s0a(i, j, k - 1)) : s0a(i, j, k);
+                        real divs0u = (um(i + 1, j, k) * s0x_hi - um(i, j, k) * s0x_lo) / dx[0] +
                                         (vm(i, j + 1, k) * s0y_hi - vm(i, j, k) * s0y_lo) / dx[1] +
                                         (wm(i, j, k + 1) * s0z_hi - wm(i, j, k) * s0z_lo) / dx[2];
                         force(i, j, k) += -divs0u - (scal(i, j, k) - s0a(i, j, k)) * (divumac + divu_c);
@@ -950,13 +950,13 @@ struct Lev {
             const Arr& w0a = w0_cart[b];
             const Arr force = scal_force[b].comp(comp);
             MO_FOR3(L.ba[b]) {
-                double divu = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
+                real divu = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
                               (wm(i, j, k + 1) - wm(i, j, k)) / dx[2];
                 divu += (w0a(i, j, k + 1, 2) - w0a(i, j, k, 2)) / dx[2];
                 if (fullform == 1) {
                     force(i, j, k) -= scal(i, j, k) * divu;
                 } else {
-                    double divs0u = s0a(i, j, k) * ((um(i + 1, j, k) - um(i, j, k)) / dx[0] +
+                    real divs0u = s0a(i, j, k) * ((um(i + 1, j, k) - um(i, j, k)) / dx[0] +
                                                     (vm(i, j + 1, k) - vm(i, j, k)) / dx[1]) +
                                     (wm(i, j, k + 1) * s0e(i, j, k + 1) - wm(i, j, k) * s0e(i, j, k)) / dx[2];
                     force(i, j, k) += -(scal(i, j, k) - s0a(i, j, k)) * divu - divs0u;
@@ -985,10 +985,10 @@ struct Lev {
                 const Arr& ps = psi_cart[b];
                 const Arr rf = scal_force[b].comp(RhoH);
                 MO_FOR3(L.ba[b]) {
-                    double divup = (um(i + 1, j, k) * px(i + 1, j, k) - um(i, j, k) * px(i, j, k)) / dx[0] +
+                    real divup = (um(i + 1, j, k) * px(i + 1, j, k) - um(i, j, k) * px(i, j, k)) / dx[0] +
                                    (vm(i, j + 1, k) * py(i, j + 1, k) - vm(i, j, k) * py(i, j, k)) / dx[1] +
                                    (wm(i, j, k + 1) * pz(i, j, k + 1) - wm(i, j, k) * pz(i, j, k)) / dx[2];
-                    double p0divu = ((um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
+                    real p0divu = ((um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
                                      (wm(i, j, k + 1) - wm(i, j, k)) / dx[2]) *
                                     p0c(i, j, k);
                     rf(i, j, k) = divup - p0divu;
@@ -1007,7 +1007,7 @@ struct Lev {
             const Arr& rc = rho0_cart[b];
             const Arr rf = scal_force[b].comp(RhoH);
             MO_FOR3(L.ba[b]) {
-                double gradp0 = 0.0;
+                real gradp0 = 0.0;
                 if (k < cutoff) {
                     gradp0 = rc(i, j, k) * gc(i, j, k);
                 } else if (k == domhi) {
@@ -1015,7 +1015,7 @@ struct Lev {
                 } else {
                     gradp0 = (p0c(i, j + 1, k) - p0c(i, j, k)) / L.dx[2];
                 }
-                double veladv = 0.5 * (wm(i, j, k) + wm(i, j, k + 1));
+                real veladv = 0.5 * (wm(i, j, k) + wm(i, j, k + 1));
                 rf(i, j, k) = veladv * gradp0;
                 if (psi_in) rf(i, j, k) += ps(i, j, k);
                 if (add_thermal == 1) rf(i, j, k) += th(i, j, k);
@@ -1025,11 +1025,11 @@ struct Lev {
 
     // ------------------------------------------------------------------ conversions
     // Maestro::PutInPertForm, one level (Source/MaestroConvert.cpp:6-30)
-    void PutInPertForm(MF& scal, const std::vector<double>& s0, int comp, bool flag) {
+    void PutInPertForm(MF& scal, const std::vector<real>& s0, int comp, bool flag) {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = scal[b];
             MO_FOR3(L.ba[b]) {
-                const double s0c = P.spherical ? s0[cc_to_r(i, j, k)] : s0[k];
+                const real s0c = P.spherical ? s0[cc_to_r(i, j, k)] : s0[k];
                 if (flag) a(i, j, k, comp) = a(i, j, k, comp) - s0c;
                 else a(i, j, k, comp) = a(i, j, k, comp) + s0c;
             }
@@ -1050,9 +1050,9 @@ struct Lev {
 
     // ------------------------------------------------------------------ fluxes
     // Maestro::MakeRhoXFlux, planar 3-D (Source/MaestroMakeFlux.cpp:18-465)
-    void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<double>& r0_old,
-                      const std::vector<double>& r0e_old, const std::vector<double>& r0_new,
-                      const std::vector<double>& r0e_new, int start_comp, int num_comp, MF* r0mac_old = nullptr,
+    void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<real>& r0_old,
+                      const std::vector<real>& r0e_old, const std::vector<real>& r0_new,
+                      const std::vector<real>& r0e_new, int start_comp, int num_comp, MF* r0mac_old = nullptr,
                       MF* r0mac_new = nullptr) {
         const int spt = P.species_pred_type;
         for (int d = 0; d < 3; ++d) sflux[d].setVal(0.0, Rho, 1, 0);
@@ -1065,7 +1065,7 @@ struct Lev {
                     const Arr& ro = r0mac_old[d][b];
                     const Arr& rn = r0mac_new[d][b];
                     MO_FOR3(nodal(L.ba[b], d)) {
-                        const double rho0_edge = 0.5 * ro(i, j, k) + 0.5 * rn(i, j, k);  // MultiFab::LinComb
+                        const real rho0_edge = 0.5 * ro(i, j, k) + 0.5 * rn(i, j, k);  // MultiFab::LinComb
                         for (int comp = start_comp; comp < num_comp + start_comp; ++comp) {
                             if (spt == 1) f(i, j, k, comp) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, comp);
                             else if (spt == 2) f(i, j, k, comp) = u(i, j, k) * e(i, j, k, comp);
@@ -1084,7 +1084,7 @@ struct Lev {
                 const Arr& eta = etarhoflux[b];
                 MO_FOR3(nodal(L.ba[b], d)) {
                     for (int comp = start_comp; comp < num_comp + start_comp; ++comp) {
-                        double rho0_edge = d < 2 ? 0.5 * (r0_old[k] + r0_new[k]) : 0.5 * (r0e_old[k] + r0e_new[k]);
+                        real rho0_edge = d < 2 ? 0.5 * (r0_old[k] + r0_new[k]) : 0.5 * (r0e_old[k] + r0e_new[k]);
                         if (spt == 1) {
                             f(i, j, k, comp) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, comp);
                         } else if (spt == 2) {
@@ -1104,9 +1104,9 @@ struct Lev {
     }
 
     // Maestro::MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:467-1067)
-    void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<double>& rh0_old,
-                      const std::vector<double>& rh0e_old, const std::vector<double>& rh0_new,
-                      const std::vector<double>& rh0e_new, MF* rh0mac_old = nullptr, MF* rh0mac_new = nullptr) {
+    void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<real>& rh0_old,
+                      const std::vector<real>& rh0e_old, const std::vector<real>& rh0_new,
+                      const std::vector<real>& rh0e_new, MF* rh0mac_old = nullptr, MF* rh0mac_new = nullptr) {
         const int ept = P.enthalpy_pred_type;
         if (P.spherical) {  // exact base state, (rho h)' predicted (Source/MaestroMakeFlux.cpp:540-548, 788-840)
             for (int b = 0; b < nb; ++b)
@@ -1117,7 +1117,7 @@ struct Lev {
                     const Arr& ho = rh0mac_old[d][b];
                     const Arr& hn = rh0mac_new[d][b];
                     MO_FOR3(nodal(L.ba[b], d)) {
-                        const double rhoh0_edge = 0.5 * ho(i, j, k) + 0.5 * hn(i, j, k);
+                        const real rhoh0_edge = 0.5 * ho(i, j, k) + 0.5 * hn(i, j, k);
                         f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
                     }
                 }
@@ -1133,10 +1133,10 @@ struct Lev {
                         f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, RhoH);
                     } else if (ept == 1) {
                         if (d < 2) {
-                            double rhoh0_edge = 0.5 * (rh0_old[k] + rh0_new[k]);
+                            real rhoh0_edge = 0.5 * (rh0_old[k] + rh0_new[k]);
                             f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
                         } else {
-                            double rhoh0_edge = 0.5 * (rh0e_old[k] + rh0e_new[k]);
+                            real rhoh0_edge = 0.5 * (rh0e_old[k] + rh0e_new[k]);
                             f(i, j, k, RhoH) = u(i, j, k) * (e(i, j, k, RhoH) + rhoh0_edge);
                         }
                     }
@@ -1148,7 +1148,7 @@ struct Lev {
     // Maestro::UpdateScal, one level (Source/MaestroAdvection.cpp:86-256)
     void UpdateScal(MF& sold, MF& snew, MF* sflux, MF& force, int start_comp, int num_comp) {
         const double* dx = L.dx;
-        const double dt_loc = dt;
+        const real dt_loc = dt;
         for (int b = 0; b < nb; ++b) {
             const Arr& so = sold[b];
             const Arr& sn = snew[b];
@@ -1158,7 +1158,7 @@ struct Lev {
             const Arr& fo = force[b];
             if (start_comp == RhoH) {
                 MO_FOR3(L.ba[b]) {
-                    double divterm = ((fx(i + 1, j, k, RhoH) - fx(i, j, k, RhoH)) / dx[0] +
+                    real divterm = ((fx(i + 1, j, k, RhoH) - fx(i, j, k, RhoH)) / dx[0] +
                                       (fy(i, j + 1, k, RhoH) - fy(i, j, k, RhoH)) / dx[1] +
                                       (fz(i, j, k + 1, RhoH) - fz(i, j, k, RhoH)) / dx[2]);
                     sn(i, j, k, RhoH) = so(i, j, k, RhoH) + dt_loc * (-divterm + fo(i, j, k, RhoH));
@@ -1169,7 +1169,7 @@ struct Lev {
                 for (int n = 0; n < nspec; ++n) {
                     const int comp = FirstSpec + n;
                     MO_FOR3(L.ba[b]) {
-                        double divterm = (fx(i + 1, j, k, comp) - fx(i, j, k, comp)) / dx[0];
+                        real divterm = (fx(i + 1, j, k, comp) - fx(i, j, k, comp)) / dx[0];
                         divterm += (fy(i, j + 1, k, comp) - fy(i, j, k, comp)) / dx[1];
                         divterm += (fz(i, j, k + 1, comp) - fz(i, j, k, comp)) / dx[2];
                         sn(i, j, k, comp) = so(i, j, k, comp) + dt_loc * (-divterm + fo(i, j, k, comp));
@@ -1190,13 +1190,13 @@ struct Lev {
                     if (has_negative_species) {
                         for (int comp = start_comp; comp < start_comp + nspec; ++comp) {
                             if (sn(i, j, k, comp) < 0.0) {
-                                double delta = -sn(i, j, k, comp);
-                                double sumX = 0.0;
+                                real delta = -sn(i, j, k, comp);
+                                real sumX = 0.0;
                                 for (int comp2 = start_comp; comp2 < start_comp + nspec; ++comp2)
                                     if (comp2 != comp && sn(i, j, k, comp2) >= 0.0) sumX += sn(i, j, k, comp2);
                                 for (int comp2 = start_comp; comp2 < start_comp + nspec; ++comp2)
                                     if (comp2 != comp && sn(i, j, k, comp2) >= 0.0) {
-                                        double frac = sn(i, j, k, comp2) / sumX;
+                                        real frac = sn(i, j, k, comp2) / sumX;
                                         sn(i, j, k, comp2) -= frac * delta;
                                     }
                                 sn(i, j, k, comp) = 0.0;
@@ -1213,7 +1213,7 @@ struct Lev {
 
 using VMF = std::vector<MF>;                // one MultiFab per level
 using VF = std::vector<std::array<MF, 3>>;  // face MultiFabs per level
-using BS = std::vector<std::vector<double>>;  // a base-state array per level
+using BS = std::vector<std::vector<real>>;  // a base-state array per level
 
 // The stage over all levels, with the coarse-fine synchronisation of the reference:
 // AverageDown + FillPatch after every cell-centred update, AverageDownFaces + FillPatchUedge
@@ -1227,7 +1227,7 @@ struct Stage {
     const std::vector<BCRec>& bcs_s() const { return S[0].bcs_s; }
     const std::vector<BCRec>& bcs_u() const { return S[0].bcs_u; }
     const std::vector<BCRec>& bcs_f() const { return S[0].bcs_f; }
-    BS bs(std::vector<double> Lev::*m) const {
+    BS bs(std::vector<real> Lev::*m) const {
         BS r(nlev);
         for (int l = 0; l < nlev; ++l) r[l] = S[l].*m;
         return r;
@@ -1371,7 +1371,7 @@ struct Stage {
         for (int lev = 0; lev < nlev; ++lev) S[lev].MakeUtrans(utilde[lev], ufull[lev], utrans[lev].data());
         SyncFaces(utrans);
     }
-    void Addw0(VF& u, double mult) {
+    void Addw0(VF& u, real mult) {
         for (int lev = 0; lev < nlev; ++lev) S[lev].Addw0(u[lev].data(), mult);
         SyncFaces(u);
     }
@@ -1631,12 +1631,24 @@ static void scatter_cells(const Box& dom, const double* src, MF& mf, int c0, int
                 mf[b](i, j, k, c0 + n) = src[(long)n * N + idx];
             }
 }
-static void gather_cells(const Box& dom, const MF& mf, int c0, int nc, double* dst) {
+#ifdef MO_TANGENT
+// the directional derivative of scattered cell data (its values already in place)
+static void seed_cells(const Box& dom, const double* dsrc, MF& mf, int c0, int nc) {
     long nx = dom.hi[0] - dom.lo[0] + 1, ny = dom.hi[1] - dom.lo[1] + 1, N = ncell_of(dom);
     for (int b = 0; b < mf.size(); ++b)
         for (int n = 0; n < nc; ++n) MO_FOR3(mf.ba[b]) {
                 long idx = (i - dom.lo[0]) + nx * ((j - dom.lo[1]) + ny * (long)(k - dom.lo[2]));
-                dst[(long)n * N + idx] = mf[b](i, j, k, c0 + n);
+                mf[b](i, j, k, c0 + n).d = dsrc[(long)n * N + idx];
+            }
+}
+#endif
+static void gather_cells(const Box& dom, const MF& mf, int c0, int nc, double* dst, bool tangent = false) {
+    long nx = dom.hi[0] - dom.lo[0] + 1, ny = dom.hi[1] - dom.lo[1] + 1, N = ncell_of(dom);
+    for (int b = 0; b < mf.size(); ++b)
+        for (int n = 0; n < nc; ++n) MO_FOR3(mf.ba[b]) {
+                long idx = (i - dom.lo[0]) + nx * ((j - dom.lo[1]) + ny * (long)(k - dom.lo[2]));
+                const real& x = mf[b](i, j, k, c0 + n);
+                dst[(long)n * N + idx] = tangent ? tangent_of(x) : value_of(x);
             }
 }
 static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, double* dst) {
@@ -1647,7 +1659,7 @@ static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, do
         Box vb = nodal(mf.ba[b], d);
         for (int n = 0; n < nc; ++n) MO_FOR3(vb) {
                 long idx = (i - dom.lo[0]) + ext[0] * ((j - dom.lo[1]) + ext[1] * (long)(k - dom.lo[2]));
-                dst[(long)n * N + idx] = mf[b](i, j, k, c0 + n);
+                dst[(long)n * N + idx] = value_of(mf[b](i, j, k, c0 + n));
             }
     }
 }
@@ -1712,7 +1724,7 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
         S.pc = PPMCtx{p->ppm_type, p->dt, p->rel_eps, {S.L.dx[0], S.L.dx[1], S.L.dx[2]}, S.L.dom};
         S.BCSetup();
         const int nr = S.nr;
-        auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
+        auto vec = [](const double* a, int n) { return std::vector<real>(a, a + n); };
         const mo_inputs& I = p->spherical ? in[0] : in[lev];  // spherical: one radial base state
         S.rho0_old = vec(I.rho0_old, nr);
         S.rho0_new = vec(I.rho0_new, nr);
@@ -1740,8 +1752,16 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
         for (int lev = 0; lev < nlev; ++lev) H.S[lev].MakeW0mac();
 }
 
+// Tangent seeds of one level (tangent build): derivatives of uold and sold, and where the
+// derivative of snew goes; all [nc][ncell] like the values.
+struct TangentIO {
+    const double* duold;
+    const double* dsold;
+    double* dsnew;
+};
+
 static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in,
-                     mo_outputs* out, int which_step) {
+                     mo_outputs* out, int which_step, const TangentIO* tl = nullptr) {
     if (which_step != 1 && which_step != 2) throw std::runtime_error("which_step must be 1 or 2");
     Stage H;
     setup_stage(H, p, nlev, nboxes, boxes, in);
@@ -1763,6 +1783,14 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         S.thermal.define(S.L.ba, 1, 1, -1, 0.0);
         scatter_cells(dom, in[lev].uold, uold[lev], 0, 3);
         scatter_cells(dom, in[lev].sold, sold[lev], 0, nscal);
+#ifdef MO_TANGENT
+        if (tl) {
+            seed_cells(dom, tl[lev].duold, uold[lev], 0, 3);
+            seed_cells(dom, tl[lev].dsold, sold[lev], 0, nscal);
+        }
+#else
+        if (tl) throw std::runtime_error("tangent seeds need the tangent build");
+#endif
         scatter_cells(dom, in[lev].gpi, S.gpi, 0, 3);
         if (in[lev].thermal) scatter_cells(dom, in[lev].thermal, S.thermal, 0, 1);
         for (int d = 0; d < 3; ++d) {
@@ -1805,6 +1833,7 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
             if (o.sflux[d]) gather_faces(dom, sflux[lev][d], d, 0, nscal, o.sflux[d]);
         }
         if (o.snew) gather_cells(dom, snew[lev], 0, nscal, o.snew);
+        if (tl) gather_cells(dom, snew[lev], 0, nscal, tl[lev].dsnew, true);
         if (o.sold_end) gather_cells(dom, sold[lev], 0, nscal, o.sold_end);
         if (o.etarhoflux) gather_faces(dom, etarhoflux[lev], 2, 0, 1, o.etarhoflux);
     }
@@ -1852,7 +1881,7 @@ static int run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const 
     S.BCSetup();
     S.cutoff = p->base_cutoff_density_coord;
     const int nr = S.nr;
-    auto vec = [](const double* a, int n) { return std::vector<double>(a, a + n); };
+    auto vec = [](const double* a, int n) { return std::vector<real>(a, a + n); };
     S.rho0_old = vec(in->rho0_old, nr);
     S.rho0_new = vec(in->rho0_new, nr);
     S.rhoh0_old = vec(in->rhoh0_old, nr);
@@ -1919,6 +1948,7 @@ static int run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const 
 
 }  // namespace mo
 
+#ifndef MO_TANGENT  // the FAB-based entries read and write plain doubles
 static mo::Arr arr_of(const mo_fab* f) {
     mo::Arr a;
     a.p = f->p;
@@ -2076,6 +2106,7 @@ static int member(const mo_params* p, int nboxes, const int* boxes, const mo_inp
 }
 
 }  // namespace mo
+#endif
 
 extern "C" {
 
@@ -2115,13 +2146,14 @@ int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inpu
 }
 
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {
-    std::vector<double> c(s0_cell, s0_cell + nr), e;
+    std::vector<mo::real> c(s0_cell, s0_cell + nr), e;
     mo::Lev::CelltoEdge(c, e);
-    std::memcpy(s0_edge, e.data(), sizeof(double) * (nr + 1));
+    for (int r = 0; r <= nr; ++r) s0_edge[r] = mo::value_of(e[r]);
     return 0;
 }
 
 
+#ifndef MO_TANGENT
 int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const mo_fab* u, const mo_fab* v,
            const mo_fab* w, int is_umac, const int* bc, const mo_fab* Ip, const mo_fab* Im) {
     try {
@@ -2155,6 +2187,24 @@ int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
         return -1;
     }
 }
+
+#else
+int mo_run_stage_tl(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, const double* duold,
+                    const double* dsold, mo_outputs* out, double* dsnew, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    try {
+        const mo::TangentIO t{duold, dsold, dsnew};
+        return mo::run_stage(p, 1, &nboxes, boxes, in, out, 1, &t);
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+#endif
 
 const char* mo_last_error(void) { return mo::g_err.c_str(); }
 }

@@ -131,6 +131,14 @@ enum { MO_MAKE_UTRANS, MO_VEL_PRED, MO_MAKE_EDGE_SCAL, MO_MAKE_RHOX_FLUX, MO_MAK
 int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
               int start_comp, int num_comp, int is_conservative, const mo_fab* args);
 
+/* Tangent build only (libmaestro_oracle_tl.so, compiled with MO_TANGENT): mo_run_stage with
+ * the directional derivatives duold [3][ncell] and dsold [nscal][ncell] of its inputs;
+ * dsnew [nscal][ncell] receives the derivative of snew along them (the tangent-linear model
+ * of the stage, branches decided by the forward values; out receives the values, bitwise
+ * those of mo_run_stage).  mo_ppm and mo_member are not in the tangent build. */
+int mo_run_stage_tl(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, const double* duold,
+                    const double* dsold, mo_outputs* out, double* dsnew, int nthreads);
+
 /* 1-D CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), single level. */
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge);
 

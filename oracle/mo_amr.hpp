@@ -58,7 +58,7 @@ struct Owner {
 inline int floordiv2(int a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); }
 
 // Coarse value of component n at (I,J,K), extended by the BC fill of a domain-wide FAB.
-inline double coarse_value(const Level& Lc, const Owner& oc, const MF& cmf, int n, const BCRec& bc, bool velish,
+inline real coarse_value(const Level& Lc, const Owner& oc, const MF& cmf, int n, const BCRec& bc, bool velish,
                            int I, int J, int K) {
     int p[3] = {I, J, K};
     for (int d = 0; d < 3; ++d)
@@ -100,32 +100,32 @@ inline double coarse_value(const Level& Lc, const Owner& oc, const MF& cmf, int 
 }
 
 // cell_cons_interp value of fine cell (i,j,k) (restated as described at the top).
-inline double cons_interp(const Level& Lc, const Owner& oc, const MF& cmf, int n, const BCRec& bc, bool velish, int i,
+inline real cons_interp(const Level& Lc, const Owner& oc, const MF& cmf, int n, const BCRec& bc, bool velish, int i,
                           int j, int k) {
     const int I[3] = {floordiv2(i), floordiv2(j), floordiv2(k)};
     const int f[3] = {i, j, k};
     auto cv = [&](int a, int b, int c) { return coarse_value(Lc, oc, cmf, n, bc, velish, a, b, c); };
-    const double u0 = cv(I[0], I[1], I[2]);
-    double s[3];
+    const real u0 = cv(I[0], I[1], I[2]);
+    real s[3];
     for (int d = 0; d < 3; ++d) {
         int pp[3] = {I[0], I[1], I[2]}, pm[3] = {I[0], I[1], I[2]};
         pp[d] += 1;
         pm[d] -= 1;
-        const double up = cv(pp[0], pp[1], pp[2]);
-        const double dn = cv(pm[0], pm[1], pm[2]);
-        double dc = 0.5 * (up - dn);
+        const real up = cv(pp[0], pp[1], pp[2]);
+        const real dn = cv(pm[0], pm[1], pm[2]);
+        real dc = 0.5 * (up - dn);
         if (!Lc.per[d]) {
             if (I[d] == Lc.dom.lo[d] && (bc.lo[d] == ext_dir || bc.lo[d] == hoextrap))
                 dc = (up + 3.0 * u0 - 4.0 * dn) / 3.0;
             if (I[d] == Lc.dom.hi[d] && (bc.hi[d] == ext_dir || bc.hi[d] == hoextrap))
                 dc = (4.0 * up - 3.0 * u0 - dn) / 3.0;
         }
-        const double df = 2.0 * (up - u0);
-        const double db = 2.0 * (u0 - dn);
-        double sl = (df * db >= 0.0) ? mn(fab(df), fab(db)) : 0.0;
+        const real df = 2.0 * (up - u0);
+        const real db = 2.0 * (u0 - dn);
+        real sl = (df * db >= 0.0) ? mn(fab(df), fab(db)) : 0.0;
         s[d] = cps(1.0, dc) * mn(sl, fab(dc));
     }
-    double off[3];
+    real off[3];
     for (int d = 0; d < 3; ++d) off[d] = (f[d] - 2 * I[d]) == 0 ? -0.25 : 0.25;
     return u0 + off[0] * s[0] + off[1] * s[1] + off[2] * s[2];
 }
@@ -168,7 +168,7 @@ inline void FillPatchTwoLevels(const Level& Lc, const MF& cmf, const Level& Lf, 
 inline void AverageDown(const Level& Lf, const MF& fmf, const Level& Lc, MF& cmf, int comp, int ncomp) {
     Owner oc;
     oc.build(Lc);
-    const double volfrac = 1.0 / 8.0;
+    const real volfrac = 1.0 / 8.0;
     for (int b = 0; b < fmf.size(); ++b) {
         const Box& fb = Lf.ba[b];
         Box cb;
@@ -178,7 +178,7 @@ inline void AverageDown(const Level& Lf, const MF& fmf, const Level& Lc, MF& cmf
         }
         const Arr& f = fmf[b];
         for (int n = comp; n < comp + ncomp; ++n) MO_FOR3(cb) {
-                double c = 0.0;
+                real c = 0.0;
                 for (int kr = 0; kr < 2; ++kr)
                     for (int jr = 0; jr < 2; ++jr)
                         for (int ir = 0; ir < 2; ++ir) c += f(2 * i + ir, 2 * j + jr, 2 * k + kr, n);
@@ -194,7 +194,7 @@ inline void AverageDown(const Level& Lf, const MF& fmf, const Level& Lc, MF& cmf
 // fine faces on it (summed over the two transverse offsets, outer = higher direction),
 // written to every coarse box whose faces include it.
 inline void AverageDownFaces(const Level& Lf, const std::array<MF, 3>& ff, const Level& Lc, std::array<MF, 3>& cf) {
-    const double facInv = 1.0 / 4.0;
+    const real facInv = 1.0 / 4.0;
     for (int d = 0; d < 3; ++d) {
         const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;  // inner, outer transverse
         for (int b = 0; b < ff[d].size(); ++b) {
@@ -207,7 +207,7 @@ inline void AverageDownFaces(const Level& Lf, const std::array<MF, 3>& ff, const
             cb = nodal(cb, d);
             const Arr& f = ff[d][b];
             for (int n = 0; n < ff[d].nc; ++n) MO_FOR3(cb) {
-                    double c = 0.0;
+                    real c = 0.0;
                     for (int o = 0; o < 2; ++o)
                         for (int in = 0; in < 2; ++in) {
                             int q[3] = {2 * i, 2 * j, 2 * k};
@@ -215,7 +215,7 @@ inline void AverageDownFaces(const Level& Lf, const std::array<MF, 3>& ff, const
                             q[t2] += o;
                             c += f(q[0], q[1], q[2], n);
                         }
-                    const double v = c * facInv;
+                    const real v = c * facInv;
                     for (int cbx = 0; cbx < cf[d].size(); ++cbx)
                         if (contains(nodal(Lc.ba[cbx], d), i, j, k)) cf[d][cbx](i, j, k, n) = v;
                 }
@@ -255,7 +255,7 @@ struct UedgeInterface {
             return -1;
         return o.id[o.idx(i, j, k)];
     }
-    double coarse_face(int I, int J, int K) const {
+    real coarse_face(int I, int J, int K) const {
         int q[3] = {I, J, K};
         int b = owner_in(oc, I, J, K);
         if (b < 0) {
@@ -272,7 +272,7 @@ struct UedgeInterface {
         return cu[b](I, J, K);
     }
     // value of a coarse-aligned face
-    double even_value(int i, int j, int k) const {
+    real even_value(int i, int j, int k) const {
         int q[3] = {i, j, k};
         int b = owner_in(of, i, j, k);
         if (b < 0) {
@@ -282,7 +282,7 @@ struct UedgeInterface {
         if (b >= 0) return fu[b](i, j, k);
         return coarse_face(floordiv2(i), floordiv2(j), floordiv2(k));
     }
-    double value(int i, int j, int k) const {
+    real value(int i, int j, int k) const {
         int q[3] = {i, j, k};
         if ((q[d] & 1) == 0) return even_value(i, j, k);
         for (int e = 0; e < 3; ++e)
@@ -290,9 +290,9 @@ struct UedgeInterface {
         int a[3] = {q[0], q[1], q[2]}, c[3] = {q[0], q[1], q[2]};
         a[d] -= 1;
         c[d] += 1;
-        const double fa = even_value(a[0], a[1], a[2]);
-        const double fc = even_value(c[0], c[1], c[2]);
-        const double df = fc - fa;
+        const real fa = even_value(a[0], a[1], a[2]);
+        const real fc = even_value(c[0], c[1], c[2]);
+        const real df = fc - fa;
         return fa + df * 1.0 / 2.0;
     }
     void apply(MF& fout) const {

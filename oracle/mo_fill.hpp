@@ -96,12 +96,12 @@ inline void PhysFill(const Level& L, MF& mf, int c0, int nc, int ngf, const std:
                     MO_FOR3(r) {
                         int idx[3] = {i, j, k};
                         int m = idx[d];
-                        auto at = [&](int p) -> double {
+                        auto at = [&](int p) -> real {
                             int id2[3] = {i, j, k};
                             id2[d] = p;
                             return q(id2[0], id2[1], id2[2], n);
                         };
-                        double v;
+                        real v;
                         if (t == foextrap) {
                             v = at(side == 0 ? dlo : dhi);
                         } else if (t == hoextrap) {

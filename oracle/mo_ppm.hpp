@@ -31,8 +31,8 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
                     const Arr& Im, int d, int bclo, int bchi, bool is_umac) {
     const int di = d == 0, dj = d == 1, dk = d == 2;
     const int domlo = c.dom.lo[d], domhi = c.dom.hi[d];
-    const double dt_local = c.dt, rel_eps_local = c.rel_eps, dxd = c.dx[d];
-    const double C = 1.25;
+    const real dt_local = c.dt, rel_eps_local = c.rel_eps, dxd = c.dx[d];
+    const real C = 1.25;
     const bool lo_bigm_quirk = (d == 0);       // 1.e10 in the x lo re-limit
     const bool hi_sedgerr_reset = (d != 0);    // y/z reset sedgerr at domhi-1
     const bool lo_sedge_reset = (d == 1);      // y resets sedge at domlo
@@ -41,14 +41,14 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
 
     MO_FOR3(bx) {
         const int I = d == 0 ? i : (d == 1 ? j : k);
-        auto S = [&](int m) -> double { return s(i + m * di, j + m * dj, k + m * dk, n); };
-        double sm, sp;
+        auto S = [&](int m) -> real { return s(i + m * di, j + m * dj, k + m * dk, n); };
+        real sm, sp;
         if (c.ppm_type == 1) {
             // van Leer slopes (:37-73)
-            double dsvl_l = 0.0, dsvl_r = 0.0;
-            double dsc = 0.5 * (S(0) - S(-2));
-            double dsl = 2.0 * (S(-1) - S(-2));
-            double dsr = 2.0 * (S(0) - S(-1));
+            real dsvl_l = 0.0, dsvl_r = 0.0;
+            real dsc = 0.5 * (S(0) - S(-2));
+            real dsl = 2.0 * (S(-1) - S(-2));
+            real dsr = 2.0 * (S(0) - S(-1));
             if (dsl * dsr > 0.0) dsvl_l = cps(1.0, dsc) * mn(fab(dsc), mn(fab(dsl), fab(dsr)));
             dsc = 0.5 * (S(1) - S(-1));
             dsl = 2.0 * (S(0) - S(-1));
@@ -71,7 +71,7 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
             sp = 0.5 * (S(1) + S(0)) - (dsvl_r - dsvl_l) / 6.0;
             sp = mx(sp, mn(S(1), S(0)));
             sp = mn(sp, mx(S(1), S(0)));
-            const double sedgel = sp, sedger = sm;
+            const real sedgel = sp, sedger = sm;
             auto quadlim = [&]() {  // (:117-128)
                 if ((sp - S(0)) * (S(0) - sm) <= 0.0) {
                     sp = S(0);
@@ -117,26 +117,26 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
             }
         } else {
             // ppm_type 2 (:255-640): limited 4th-order face values around the cell
-            auto face = [&](int m) -> double {  // face between cells m-1 and m
-                double se = (7.0 / 12.0) * (S(m - 1) + S(m)) - (1.0 / 12.0) * (S(m - 2) + S(m + 1));
+            auto face = [&](int m) -> real {  // face between cells m-1 and m
+                real se = (7.0 / 12.0) * (S(m - 1) + S(m)) - (1.0 / 12.0) * (S(m - 2) + S(m + 1));
                 if ((se - S(m - 1)) * (S(m) - se) < 0.0) {
-                    double D2 = 3.0 * (S(m - 1) - 2.0 * se + S(m));
-                    double D2L = S(m - 2) - 2.0 * S(m - 1) + S(m);
-                    double D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
-                    double sgn = cps(1.0, D2);
-                    double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
+                    real D2 = 3.0 * (S(m - 1) - 2.0 * se + S(m));
+                    real D2L = S(m - 2) - 2.0 * S(m - 1) + S(m);
+                    real D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
+                    real sgn = cps(1.0, D2);
+                    real D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
                     se = 0.5 * (S(m - 1) + S(m)) - D2LIM / 6.0;
                 }
                 return se;
             };
-            double sedgel = face(-1);
-            double sedge = face(0);
-            double sedger = face(1);
-            double sedgerr = face(2);
-            double alphap, alpham;
+            real sedgel = face(-1);
+            real sedge = face(0);
+            real sedger = face(1);
+            real sedgerr = face(2);
+            real alphap, alpham;
             bool bigp, bigm, extremum;
             // Colella 2008 limiter (:337-434); bigm_tol differs only in the x lo re-limit
-            auto limiter = [&](double bigm_tol) {
+            auto limiter = [&](real bigm_tol) {
                 alphap = sedger - S(0);
                 alpham = sedge - S(0);
                 bigp = fab(alphap) > 2.0 * fab(alpham);
@@ -145,13 +145,13 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
                 if (alpham * alphap >= 0.0) {
                     extremum = true;
                 } else if (bigp || bigm) {
-                    double dafacem = sedge - sedgel;
-                    double dafacep = sedgerr - sedger;
-                    double dabarm = S(0) - S(-1);
-                    double dabarp = S(1) - S(0);
-                    double dafacemin = mn(fab(dafacem), fab(dafacep));
-                    double dabarmin = mn(fab(dabarm), fab(dabarp));
-                    double dachkm = 0.0, dachkp = 0.0;
+                    real dafacem = sedge - sedgel;
+                    real dafacep = sedgerr - sedger;
+                    real dabarm = S(0) - S(-1);
+                    real dabarp = S(1) - S(0);
+                    real dafacemin = mn(fab(dafacem), fab(dafacep));
+                    real dabarmin = mn(fab(dabarm), fab(dabarp));
+                    real dachkm = 0.0, dachkp = 0.0;
                     if (dafacemin >= dabarmin) {
                         dachkm = dafacem;
                         dachkp = dafacep;
@@ -162,35 +162,35 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
                     extremum = (dachkm * dachkp <= 0.0);
                 }
                 if (extremum) {
-                    double D2 = 6.0 * (alpham + alphap);
-                    double D2L = S(-2) - 2.0 * S(-1) + S(0);
-                    double D2R = S(0) - 2.0 * S(1) + S(2);
-                    double D2C = S(-1) - 2.0 * S(0) + S(1);
-                    double sgn = cps(1.0, D2);
-                    double D2LIM = mx(mn(sgn * D2, mn(C * sgn * D2L, mn(C * sgn * D2R, C * sgn * D2C))), 0.0);
-                    double D2ABS = mx(fab(D2), 1.e-10);
+                    real D2 = 6.0 * (alpham + alphap);
+                    real D2L = S(-2) - 2.0 * S(-1) + S(0);
+                    real D2R = S(0) - 2.0 * S(1) + S(2);
+                    real D2C = S(-1) - 2.0 * S(0) + S(1);
+                    real sgn = cps(1.0, D2);
+                    real D2LIM = mx(mn(sgn * D2, mn(C * sgn * D2L, mn(C * sgn * D2R, C * sgn * D2C))), 0.0);
+                    real D2ABS = mx(fab(D2), 1.e-10);
                     alpham = alpham * D2LIM / D2ABS;
                     alphap = alphap * D2LIM / D2ABS;
                 } else {
                     if (bigp) {
-                        double sgn = cps(1.0, alpham);
-                        double amax = -alphap * alphap / (4.0 * (alpham + alphap));
-                        double delam = S(-1) - S(0);
+                        real sgn = cps(1.0, alpham);
+                        real amax = -alphap * alphap / (4.0 * (alpham + alphap));
+                        real delam = S(-1) - S(0);
                         if (sgn * amax >= sgn * delam) {
                             if (sgn * (delam - alpham) >= 1.e-10) {
-                                alphap = -2.0 * delam - 2.0 * sgn * std::sqrt(delam * delam - delam * alpham);
+                                alphap = -2.0 * delam - 2.0 * sgn * sqrt_r(delam * delam - delam * alpham);
                             } else {
                                 alphap = -2.0 * alpham;
                             }
                         }
                     }
                     if (bigm) {
-                        double sgn = cps(1.0, alphap);
-                        double amax = -alpham * alpham / (4.0 * (alpham + alphap));
-                        double delap = S(1) - S(0);
+                        real sgn = cps(1.0, alphap);
+                        real amax = -alpham * alpham / (4.0 * (alpham + alphap));
+                        real delap = S(1) - S(0);
                         if (sgn * amax >= sgn * delap) {
                             if (sgn * (delap - alphap) >= bigm_tol) {
-                                alpham = (-2.0 * delap - 2.0 * sgn * std::sqrt(delap * delap - delap * alphap));
+                                alpham = (-2.0 * delap - 2.0 * sgn * sqrt_r(delap * delap - delap * alphap));
                             } else {
                                 alpham = -2.0 * alphap;
                             }
@@ -240,16 +240,16 @@ inline void PPM_dir(const PPMCtx& c, const Box& bx, const Arr& s, int n, const A
             }
         }
         // characteristic tracing (:209-251, :706-770)
-        double s6 = 6.0 * S(0) - 3.0 * (sm + sp);
+        real s6 = 6.0 * S(0) - 3.0 * (sm + sp);
         const int ii = i + di, jj = j + dj, kk = k + dk;
-        double up = is_umac ? u(ii, jj, kk) : u(i, j, k);
-        double sigma = fab(up) * dt_local / dxd;
+        real up = is_umac ? u(ii, jj, kk) : u(i, j, k);
+        real sigma = fab(up) * dt_local / dxd;
         if (up > rel_eps_local) {
             Ip(i, j, k, d) = sp - 0.5 * sigma * (sp - sm - (1.0 - 2.0 / 3.0 * sigma) * s6);
         } else {
             Ip(i, j, k, d) = S(0);
         }
-        double um = u(i, j, k);
+        real um = u(i, j, k);
         sigma = fab(um) * dt_local / dxd;
         if (um < -rel_eps_local) {
             Im(i, j, k, d) = sm + 0.5 * sigma * (sp - sm + (1.0 - 2.0 / 3.0 * sigma) * s6);
@@ -280,17 +280,17 @@ inline void Slope_dir(int slope_order, const Box& dom, const Box& bx, const Arr&
         const bool hi_ext = (bchi == ext_dir || bchi == hoextrap);
         MO_FOR3(bx) {
             const int I = d == 0 ? i : (d == 1 ? j : k);
-            auto S = [&](int m) -> double { return s(i + m * di, j + m * dj, k + m * dk, n); };
-            double& out = slope(i, j, k, n);
+            auto S = [&](int m) -> real { return s(i + m * di, j + m * dj, k + m * dk, n); };
+            real& out = slope(i, j, k, n);
             if (slope_order == 0) {
                 out = 0.0;
             } else if (slope_order == 2) {
-                double del = 0.5 * (S(1) - S(-1));
-                double dpls = 2.0 * (S(1) - S(0));
-                double dmin = 2.0 * (S(0) - S(-1));
-                double slim = mn(fab(dpls), fab(dmin));
+                real del = 0.5 * (S(1) - S(-1));
+                real dpls = 2.0 * (S(1) - S(0));
+                real dmin = 2.0 * (S(0) - S(-1));
+                real slim = mn(fab(dpls), fab(dmin));
                 slim = dpls * dmin > 0.0 ? slim : 0.0;
-                double sflag = cps(1.0, del);
+                real sflag = cps(1.0, del);
                 out = sflag * mn(slim, fab(del));
                 if (lo_ext) {
                     if (I == ilo - 1) {
@@ -319,46 +319,46 @@ inline void Slope_dir(int slope_order, const Box& dom, const Box& bx, const Arr&
                     }
                 }
             } else if (slope_order == 4) {
-                double dcen = 0.5 * (S(0) - S(-2));
-                double dmin = 2.0 * (S(-1) - S(-2));
-                double dpls = 2.0 * (S(0) - S(-1));
-                double dlim = mn(fab(dmin), fab(dpls));
+                real dcen = 0.5 * (S(0) - S(-2));
+                real dmin = 2.0 * (S(-1) - S(-2));
+                real dpls = 2.0 * (S(0) - S(-1));
+                real dlim = mn(fab(dmin), fab(dpls));
                 dlim = dpls * dmin > 0.0 ? dlim : 0.0;
-                double dflag = cps(1.0, dcen);
-                double dxl = dflag * mn(dlim, fab(dcen));
+                real dflag = cps(1.0, dcen);
+                real dxl = dflag * mn(dlim, fab(dcen));
                 dcen = 0.5 * (S(2) - S(0));
                 dmin = 2.0 * (S(1) - S(0));
                 dpls = 2.0 * (S(2) - S(1));
                 dlim = mn(fab(dmin), fab(dpls));
                 dlim = dpls * dmin > 0.0 ? dlim : 0.0;
                 dflag = cps(1.0, dcen);
-                double dxr = dflag * mn(dlim, fab(dcen));
+                real dxr = dflag * mn(dlim, fab(dcen));
                 dcen = 0.5 * (S(1) - S(-1));
                 dmin = 2.0 * (S(0) - S(-1));
                 dpls = 2.0 * (S(1) - S(0));
                 dlim = mn(fab(dmin), fab(dpls));
                 dlim = dpls * dmin > 0.0 ? dlim : 0.0;
                 dflag = cps(1.0, dcen);
-                double ds = 4.0 / 3.0 * dcen - (dxr + dxl) / 6.0;
+                real ds = 4.0 / 3.0 * dcen - (dxr + dxl) / 6.0;
                 out = dflag * mn(fab(ds), dlim);
                 if (lo_ext) {
                     if (I == ilo - 1) {
                         out = 0.0;
                     } else if (I == ilo) {
-                        double del = -16.0 / 15.0 * S(-1) + 0.5 * S(0) + 2.0 / 3.0 * S(1) - 0.1 * S(2);
+                        real del = -16.0 / 15.0 * S(-1) + 0.5 * S(0) + 2.0 / 3.0 * S(1) - 0.1 * S(2);
                         dmin = 2.0 * (S(0) - S(-1));
                         dpls = 2.0 * (S(1) - S(0));
-                        double slim = mn(fab(dpls), fab(dmin));
+                        real slim = mn(fab(dpls), fab(dmin));
                         slim = dpls * dmin > 0.0 ? (x_dlim_quirk ? dlim : slim) : 0.0;
-                        double sflag = cps(1.0, del);
+                        real sflag = cps(1.0, del);
                         out = sflag * mn(slim, fab(del));
                     } else if (I == ilo + 1) {
-                        double del = -16.0 / 15.0 * S(-2) + 0.5 * S(-1) + 2.0 / 3.0 * S(0) - 0.1 * S(1);
+                        real del = -16.0 / 15.0 * S(-2) + 0.5 * S(-1) + 2.0 / 3.0 * S(0) - 0.1 * S(1);
                         dmin = 2.0 * (S(-1) - S(-2));
                         dpls = 2.0 * (S(0) - S(-1));
-                        double slim = mn(fab(dpls), fab(dmin));
+                        real slim = mn(fab(dpls), fab(dmin));
                         slim = dpls * dmin > 0.0 ? (x_dlim_quirk ? dlim : slim) : 0.0;
-                        double sflag = cps(1.0, del);
+                        real sflag = cps(1.0, del);
                         dxl = sflag * mn(slim, fab(del));
                         ds = 4.0 / 3.0 * dcen - (dxr + dxl) / 6.0;
                         out = dflag * mn(fab(ds), dlim);
@@ -368,20 +368,20 @@ inline void Slope_dir(int slope_order, const Box& dom, const Box& bx, const Arr&
                     if (I == ihi + 1) {
                         out = 0.0;
                     } else if (I == ihi) {
-                        double del = -(-16.0 / 15.0 * S(1) + 0.5 * S(0) + 2.0 / 3.0 * S(-1) - 0.1 * S(-2));
+                        real del = -(-16.0 / 15.0 * S(1) + 0.5 * S(0) + 2.0 / 3.0 * S(-1) - 0.1 * S(-2));
                         dmin = 2.0 * (S(0) - S(-1));
                         dpls = 2.0 * (S(1) - S(0));
-                        double slim = mn(fab(dpls), fab(dmin));
+                        real slim = mn(fab(dpls), fab(dmin));
                         slim = dpls * dmin > 0.0 ? (x_dlim_quirk ? dlim : slim) : 0.0;
-                        double sflag = cps(1.0, del);
+                        real sflag = cps(1.0, del);
                         out = sflag * mn(slim, fab(del));
                     } else if (I == ihi - 1) {
-                        double del = -(-16.0 / 15.0 * S(2) + 0.5 * S(1) + 2.0 / 3.0 * S(0) - 0.1 * S(-1));
+                        real del = -(-16.0 / 15.0 * S(2) + 0.5 * S(1) + 2.0 / 3.0 * S(0) - 0.1 * S(-1));
                         dmin = 2.0 * (S(1) - S(0));
                         dpls = 2.0 * (S(2) - S(1));
-                        double slim = mn(fab(dpls), fab(dmin));
+                        real slim = mn(fab(dpls), fab(dmin));
                         slim = dpls * dmin > 0.0 ? (x_dlim_quirk ? dlim : slim) : 0.0;
-                        double sflag = cps(1.0, del);
+                        real sflag = cps(1.0, del);
                         dxr = sflag * mn(slim, fab(del));
                         ds = 4.0 / 3.0 * dcen - (dxl + dxr) / 6.0;
                         out = dflag * mn(fab(ds), dlim);

@@ -33,7 +33,7 @@ struct Stage2D {
     const Level& L() const { return S.L; }
 
     // Put1dArrayOnCart, planar 2-D (Source/MaestroFill3dData.cpp:79-93, r = j)
-    void Put1dArrayOnCart(const std::vector<double>& s0, MF& s0_cart, bool edge, bool vec,
+    void Put1dArrayOnCart(const std::vector<real>& s0, MF& s0_cart, bool edge, bool vec,
                           const std::vector<BCRec>* bcs, int bccomp, bool is_vel) {
         const int outcomp = vec ? 1 : 0;
         for (int b = 0; b < nb; ++b) {
@@ -52,7 +52,7 @@ struct Stage2D {
     }
 
     // Addw0, planar 2-D (Source/MaestroFill3dData.cpp:380-386)
-    void Addw0(MF* uedge, double mult) {
+    void Addw0(MF* uedge, real mult) {
         for (int b = 0; b < nb; ++b) {
             const Arr& vedge = uedge[1][b];
             Box ybx = grow(nodal(L().ba[b], 1), 0, 1);
@@ -63,7 +63,7 @@ struct Stage2D {
 
     // MakeUtrans, 2-D (Source/MaestroMakeUtrans.cpp:57-268)
     void MakeUtrans(MF& utilde, MF& ufull, MF* utrans) {
-        const double dt2 = 0.5 * dt;
+        const real dt2 = 0.5 * dt;
         const int* domlo = L().dom.lo;
         const int* domhi = L().dom.hi;
         MF Ip, Im;
@@ -90,7 +90,7 @@ struct Stage2D {
                 const int di = d == 0, dj = d == 1;
                 MO_FOR3(xbx) {
                     const int I = d == 0 ? i : j;
-                    double l = 0.0, r = 0.0;
+                    real l = 0.0, r = 0.0;
                     if (S.P.ppm_type == 0) {
                         l = ut(i - di, j - dj, k, d) +
                             (0.5 - (dt2 / L().dx[d]) * mx(0.0, uf(i - di, j - dj, k, d))) * Ipa(i - di, j - dj, k, 0);
@@ -119,12 +119,12 @@ struct Stage2D {
                     }
                     if (d == 0) {
                         bool test = (l <= 0.0 && r >= 0.0) || (fab(l + r) < rel_eps);
-                        double v = 0.5 * (l + r) > 0.0 ? l : r;
+                        real v = 0.5 * (l + r) > 0.0 ? l : r;
                         tr(i, j, k) = test ? 0.0 : v;
                     } else {
-                        const double w0c = w0a(i, j, k, 1);
+                        const real w0c = w0a(i, j, k, 1);
                         bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fab(l + r + 2.0 * w0c) < rel_eps);
-                        double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+                        real v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
                         tr(i, j, k) = test ? 0.0 : v;
                     }
                 }
@@ -152,7 +152,7 @@ struct Stage2D {
             const Arr& r0 = rho0_cart[b];
             const Arr& vf = vel_force[b];
             MO_FOR3(L().ba[b]) {
-                double rhopert = rho_arr(i, j, k) - r0(i, j, k);
+                real rhopert = rho_arr(i, j, k) - r0(i, j, k);
                 if (rho_arr(i, j, k) < (S.P.buoyancy_cutoff_factor * S.P.base_cutoff_density)) rhopert = 0.0;
                 vf(i, j, k, 0) = -gpi_arr(i, j, k, 0) / rho_arr(i, j, k);
                 vf(i, j, k, 1) = (rhopert * grav(i, j, k, 1) - gpi_arr(i, j, k, 1)) / rho_arr(i, j, k) - w0f(i, j, k, 1);
@@ -168,10 +168,10 @@ struct Stage2D {
 
     // VelPred, 2-D (Source/MaestroVelPred.cpp:80-160, 294-727)
     void VelPred(MF& utilde, MF& ufull, MF* utrans, MF* umac, MF& force) {
-        const double dt2 = 0.5 * dt, dt4 = 0.25 * dt;
+        const real dt2 = 0.5 * dt, dt4 = 0.25 * dt;
         const int* domlo = L().dom.lo;
         const int* domhi = L().dom.hi;
-        const double hx = L().dx[0], hy = L().dx[1];
+        const real hx = L().dx[0], hy = L().dx[1];
         MF Ipu, Imu, Ipv, Imv;
         Ipu.define(L().ba, 2, 1);
         Imu.define(L().ba, 2, 1);
@@ -202,8 +202,8 @@ struct Stage2D {
                 const int bclo = S.P.phys_bc_lo[0], bchi = S.P.phys_bc_hi[0];
                 MO_FOR3(mxbx) {
                     if (S.P.ppm_type == 0) {
-                        const double maxu = mx(0.0, uf(i - 1, j, k, 0));
-                        const double minu = mn(0.0, uf(i, j, k, 0));
+                        const real maxu = mx(0.0, uf(i - 1, j, k, 0));
+                        const real minu = mn(0.0, uf(i, j, k, 0));
                         for (int n = 0; n < 2; ++n) {
                             l(i, j, k, n) = ut(i - 1, j, k, n) + (0.5 - (dt2 / hx) * maxu) * Ipu[b](i - 1, j, k, n);
                             r(i, j, k, n) = ut(i, j, k, n) - (0.5 + (dt2 / hx) * minu) * Ipu[b](i, j, k, n);
@@ -253,7 +253,7 @@ struct Stage2D {
                             default: break;
                         }
                     }
-                    double v = tr(i, j, k) > 0.0 ? l(i, j, k, 1) : r(i, j, k, 1);
+                    real v = tr(i, j, k) > 0.0 ? l(i, j, k, 1) : r(i, j, k, 1);
                     im(i, j, k, 1) = fab(tr(i, j, k)) < rel_eps ? 0.5 * (l(i, j, k, 1) + r(i, j, k, 1)) : v;
                 }
             }
@@ -264,8 +264,8 @@ struct Stage2D {
                 const int bclo = S.P.phys_bc_lo[1], bchi = S.P.phys_bc_hi[1];
                 MO_FOR3(mybx) {
                     if (S.P.ppm_type == 0) {
-                        const double maxu = mx(0.0, uf(i, j - 1, k, 1));
-                        const double minu = mn(0.0, uf(i, j, k, 1));
+                        const real maxu = mx(0.0, uf(i, j - 1, k, 1));
+                        const real minu = mn(0.0, uf(i, j, k, 1));
                         for (int n = 0; n < 2; ++n) {
                             l(i, j, k, n) = ut(i, j - 1, k, n) + (0.5 - (dt2 / hy) * maxu) * Imv[b](i, j - 1, k, n);
                             r(i, j, k, n) = ut(i, j, k, n) - (0.5 + (dt2 / hy) * minu) * Imv[b](i, j, k, n);
@@ -315,7 +315,7 @@ struct Stage2D {
                             default: break;
                         }
                     }
-                    double v = tr(i, j, k) > 0.0 ? l(i, j, k, 0) : r(i, j, k, 0);
+                    real v = tr(i, j, k) > 0.0 ? l(i, j, k, 0) : r(i, j, k, 0);
                     im(i, j, k, 0) = fab(tr(i, j, k)) < rel_eps ? 0.5 * (l(i, j, k, 0) + r(i, j, k, 0)) : v;
                 }
             }
@@ -326,16 +326,16 @@ struct Stage2D {
                 const Arr& out = umac[0][b];
                 const int bclo = S.P.phys_bc_lo[0], bchi = S.P.phys_bc_hi[0];
                 MO_FOR3(xbx) {
-                    const double fl = f(i - 1, j, k, 0), fr = f(i, j, k, 0);
-                    const double ml = l(i, j, k, 0) -
+                    const real fl = f(i - 1, j, k, 0), fr = f(i, j, k, 0);
+                    const real ml = l(i, j, k, 0) -
                                       (dt4 / hy) * (vtr(i - 1, j + 1, k) + vtr(i - 1, j, k)) *
                                           (qy(i - 1, j + 1, k, 0) - qy(i - 1, j, k, 0)) +
                                       dt2 * fl;
-                    const double mr = r(i, j, k, 0) -
+                    const real mr = r(i, j, k, 0) -
                                       (dt4 / hy) * (vtr(i, j + 1, k) + vtr(i, j, k)) *
                                           (qy(i, j + 1, k, 0) - qy(i, j, k, 0)) +
                                       dt2 * fr;
-                    double v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+                    real v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
                     v = (ml <= 0.0 && mr >= 0.0) || (fab(ml + mr) < rel_eps) ? 0.0 : v;
                     if (i == domlo[0]) {
                         switch (bclo) {
@@ -362,18 +362,18 @@ struct Stage2D {
                 const Arr& w0a = S.w0_cart[b];
                 const int bclo = S.P.phys_bc_lo[1], bchi = S.P.phys_bc_hi[1];
                 MO_FOR3(ybx) {
-                    const double fl = f(i, j - 1, k, 1), fr = f(i, j, k, 1);
-                    const double ml = l(i, j, k, 1) -
+                    const real fl = f(i, j - 1, k, 1), fr = f(i, j, k, 1);
+                    const real ml = l(i, j, k, 1) -
                                       (dt4 / hx) * (utr(i + 1, j - 1, k) + utr(i, j - 1, k)) *
                                           (qx(i + 1, j - 1, k, 1) - qx(i, j - 1, k, 1)) +
                                       dt2 * fl;
-                    const double mr = r(i, j, k, 1) -
+                    const real mr = r(i, j, k, 1) -
                                       (dt4 / hx) * (utr(i + 1, j, k) + utr(i, j, k)) *
                                           (qx(i + 1, j, k, 1) - qx(i, j, k, 1)) +
                                       dt2 * fr;
-                    const double w0c = w0a(i, j, k, 1);
+                    const real w0c = w0a(i, j, k, 1);
                     const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fab(ml + mr + 2.0 * w0c) < rel_eps);
-                    double v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+                    real v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
                     v = test ? 0.0 : v;
                     if (j == domlo[1]) {
                         switch (bclo) {
@@ -422,8 +422,8 @@ struct Stage2D {
                       int start_bccomp, int num_comp, bool is_conservative) {
         const int* domlo = L().dom.lo;
         const int* domhi = L().dom.hi;
-        const double hx = L().dx[0], hy = L().dx[1];
-        const double dt2 = 0.5 * dt, dt4 = 0.25 * dt;
+        const real hx = L().dx[0], hy = L().dx[1];
+        const real dt2 = 0.5 * dt, dt4 = 0.25 * dt;
         MF Ip, Im, slx, srx, sly, sry, simhx, simhy;
         Ip.define(L().ba, 2, 1);
         Im.define(L().ba, 2, 1);
@@ -457,7 +457,7 @@ struct Stage2D {
                     const Arr& sm = d == 0 ? simhx[b] : simhy[b];
                     const Arr& ud = d == 0 ? um : vm;
                     const Arr& slope = d == 0 ? Ip[b] : Im[b];
-                    const double h = d == 0 ? hx : hy;
+                    const real h = d == 0 ? hx : hy;
                     MO_FOR3(mbx) {
                         const int I = d == 0 ? i : j;
                         if (S.P.ppm_type == 0) {
@@ -504,14 +504,14 @@ struct Stage2D {
                     const Arr& st = d == 0 ? simhy[b] : simhx[b];
                     const Arr& ut = d == 0 ? vm : um;
                     const Arr& ud = d == 0 ? um : vm;
-                    const double ht = d == 0 ? hy : hx, hd = d == 0 ? hx : hy;
+                    const real ht = d == 0 ? hy : hx, hd = d == 0 ? hx : hy;
                     const Arr& f = force[b];
                     const Arr& se = sedge[d][b];
                     MO_FOR3(xbx) {
                         const int I = d == 0 ? i : j;
                         const int il = i - di, jl = j - dj;
-                        const double fl = f(il, jl, k, comp), fr = f(i, j, k, comp);
-                        double lq, rq;
+                        const real fl = f(il, jl, k, comp), fr = f(i, j, k, comp);
+                        real lq, rq;
                         if (is_conservative) {
                             lq = l(i, j, k) -
                                  (dt2 / ht) * (st(il + ti, jl + tj, k) * ut(il + ti, jl + tj, k) -
@@ -529,7 +529,7 @@ struct Stage2D {
                                  (dt4 / ht) * (ut(i + ti, j + tj, k) + ut(i, j, k)) * (st(i + ti, j + tj, k) - st(i, j, k)) +
                                  dt2 * fr;
                         }
-                        double v = (ud(i, j, k) > 0.0) ? lq : rq;
+                        real v = (ud(i, j, k) > 0.0) ? lq : rq;
                         v = (fab(ud(i, j, k)) > rel_eps) ? v : 0.5 * (lq + rq);
                         if (I == domlo[d]) {
                             const int t = bc_lo[d];
@@ -550,7 +550,7 @@ struct Stage2D {
     }
 
     // ModifyScalForce, planar 2-D (Source/MaestroForce.cpp:261-467)
-    void ModifyScalForce(MF& scal_force, MF& state, MF* umac, const std::vector<double>& s0_edge, MF& s0_cart,
+    void ModifyScalForce(MF& scal_force, MF& state, MF* umac, const std::vector<real>& s0_edge, MF& s0_cart,
                          int comp, int fullform) {
         MF s0_edge_cart;
         s0_edge_cart.define(L().ba, 1, 1);
@@ -565,12 +565,12 @@ struct Stage2D {
             const Arr& w0a = S.w0_cart[b];
             const Arr force = scal_force[b].comp(comp);
             MO_FOR3(L().ba[b]) {
-                double divu = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1];
+                real divu = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1];
                 divu += (w0a(i, j + 1, k, 1) - w0a(i, j, k, 1)) / dx[1];
                 if (fullform == 1) {
                     force(i, j, k) -= scal(i, j, k) * divu;
                 } else {
-                    double divs0u = s0a(i, j, k) * (um(i + 1, j, k) - um(i, j, k)) / dx[0] +
+                    real divs0u = s0a(i, j, k) * (um(i + 1, j, k) - um(i, j, k)) / dx[0] +
                                     (vm(i, j + 1, k) * s0e(i, j + 1, k) - vm(i, j, k) * s0e(i, j, k)) / dx[1];
                     force(i, j, k) += -(scal(i, j, k) - s0a(i, j, k)) * divu - divs0u;
                 }
@@ -582,7 +582,7 @@ struct Stage2D {
     // MakeRhoHForce, planar 2-D (Source/MaestroForce.cpp:469-679)
     void MakeRhoHForce(MF& scal_force, int is_prediction, MF* umac, int add_thermal, int which_step) {
         const int nr = S.nr;
-        std::vector<double> r0(nr), pp0(nr);
+        std::vector<real> r0(nr), pp0(nr);
         for (int r = 0; r < nr; ++r) {
             r0[r] = which_step == 1 ? S.rho0_old[r] : 0.5 * (S.rho0_old[r] + S.rho0_new[r]);
             pp0[r] = which_step == 1 ? S.p0_old[r] : 0.5 * (S.p0_old[r] + S.p0_new[r]);
@@ -606,11 +606,11 @@ struct Stage2D {
             const Arr& rc = rho0_cart[b];
             const Arr rf = scal_force[b].comp(RhoH);
             MO_FOR3(L().ba[b]) {
-                double gradp0 = 0.0;
+                real gradp0 = 0.0;
                 if (j < cutoff) gradp0 = rc(i, j, k) * gc(i, j, k);
                 else if (j == domhi) gradp0 = (p0c(i, j, k) - p0c(i, j - 1, k)) / L().dx[1];
                 else gradp0 = (p0c(i, j + 1, k) - p0c(i, j, k)) / L().dx[1];
-                double veladv = 0.5 * (vm(i, j, k) + vm(i, j + 1, k));
+                real veladv = 0.5 * (vm(i, j, k) + vm(i, j + 1, k));
                 rf(i, j, k) = veladv * gradp0;
                 if (psi_in) rf(i, j, k) += ps(i, j, k);
                 if (add_thermal == 1) rf(i, j, k) += th(i, j, k);
@@ -620,12 +620,12 @@ struct Stage2D {
     }
 
     // PutInPertForm, 2-D (r = j)
-    void PutInPertForm(MF& scal, const std::vector<double>& s0, int comp, int bccomp, const std::vector<BCRec>& bcs,
+    void PutInPertForm(MF& scal, const std::vector<real>& s0, int comp, int bccomp, const std::vector<BCRec>& bcs,
                        bool flag) {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = scal[b];
             MO_FOR3(L().ba[b]) {
-                const double s0c = s0[j];
+                const real s0c = s0[j];
                 if (flag) a(i, j, k, comp) = a(i, j, k, comp) - s0c;
                 else a(i, j, k, comp) = a(i, j, k, comp) + s0c;
             }
@@ -640,9 +640,9 @@ struct Stage2D {
     }
 
     // MakeRhoXFlux, 2-D (Source/MaestroMakeFlux.cpp:101-182)
-    void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<double>& r0_old,
-                      const std::vector<double>& r0e_old, const std::vector<double>& r0_new,
-                      const std::vector<double>& r0e_new, int start_comp, int num_comp) {
+    void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<real>& r0_old,
+                      const std::vector<real>& r0e_old, const std::vector<real>& r0_new,
+                      const std::vector<real>& r0e_new, int start_comp, int num_comp) {
         const int spt = S.P.species_pred_type;
         for (int d = 0; d < 2; ++d) sflux[d].setVal(0.0, Rho, 1, 0);
         for (int b = 0; b < nb; ++b)
@@ -653,7 +653,7 @@ struct Stage2D {
                 const Arr& eta = etarhoflux[b];
                 MO_FOR3(nodal(L().ba[b], d)) {
                     for (int comp = start_comp; comp < num_comp + start_comp; ++comp) {
-                        double rho0_edge = d == 0 ? 0.5 * (r0_old[j] + r0_new[j]) : 0.5 * (r0e_old[j] + r0e_new[j]);
+                        real rho0_edge = d == 0 ? 0.5 * (r0_old[j] + r0_new[j]) : 0.5 * (r0e_old[j] + r0e_new[j]);
                         if (spt == 1) f(i, j, k, comp) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, comp);
                         else if (spt == 2) f(i, j, k, comp) = u(i, j, k) * e(i, j, k, comp);
                         else f(i, j, k, comp) = u(i, j, k) * e(i, j, k, Rho) * e(i, j, k, comp);
@@ -668,9 +668,9 @@ struct Stage2D {
     }
 
     // MakeRhoHFlux, 2-D (Source/MaestroMakeFlux.cpp:597-662)
-    void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<double>& rh0_old,
-                      const std::vector<double>& rh0e_old, const std::vector<double>& rh0_new,
-                      const std::vector<double>& rh0e_new) {
+    void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<real>& rh0_old,
+                      const std::vector<real>& rh0e_old, const std::vector<real>& rh0_new,
+                      const std::vector<real>& rh0e_new) {
         const int ept = S.P.enthalpy_pred_type;
         for (int b = 0; b < nb; ++b)
             for (int d = 0; d < 2; ++d) {
@@ -681,10 +681,10 @@ struct Stage2D {
                     if (ept == 0) {
                         f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, RhoH);
                     } else if (d == 0) {
-                        double rhoh0_edge = 0.5 * (rh0_old[j] + rh0_new[j]);
+                        real rhoh0_edge = 0.5 * (rh0_old[j] + rh0_new[j]);
                         f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
                     } else {
-                        double rhoh0_edge = 0.5 * (rh0e_old[j] + rh0e_new[j]);
+                        real rhoh0_edge = 0.5 * (rh0e_old[j] + rh0e_new[j]);
                         f(i, j, k, RhoH) = u(i, j, k) * (e(i, j, k, RhoH) + rhoh0_edge);
                     }
                 }
@@ -702,7 +702,7 @@ struct Stage2D {
             const Arr& fo = force[b];
             if (start_comp == RhoH) {
                 MO_FOR3(L().ba[b]) {
-                    double divterm = ((fx(i + 1, j, k, RhoH) - fx(i, j, k, RhoH)) / dx[0] +
+                    real divterm = ((fx(i + 1, j, k, RhoH) - fx(i, j, k, RhoH)) / dx[0] +
                                       (fy(i, j + 1, k, RhoH) - fy(i, j, k, RhoH)) / dx[1]);
                     sn(i, j, k, RhoH) = so(i, j, k, RhoH) + dt * (-divterm + fo(i, j, k, RhoH));
                     if (S.P.do_eos_h_above_cutoff && sn(i, j, k, Rho) <= S.P.base_cutoff_density)
@@ -712,7 +712,7 @@ struct Stage2D {
                 for (int n = 0; n < nspec; ++n) {
                     const int comp = FirstSpec + n;
                     MO_FOR3(L().ba[b]) {
-                        double divterm = (fx(i + 1, j, k, comp) - fx(i, j, k, comp)) / dx[0];
+                        real divterm = (fx(i + 1, j, k, comp) - fx(i, j, k, comp)) / dx[0];
                         divterm += (fy(i, j + 1, k, comp) - fy(i, j, k, comp)) / dx[1];
                         sn(i, j, k, comp) = so(i, j, k, comp) + dt * (-divterm + fo(i, j, k, comp));
                     }
@@ -732,13 +732,13 @@ struct Stage2D {
                     if (has_negative_species) {
                         for (int comp = start_comp; comp < start_comp + nspec; ++comp) {
                             if (sn(i, j, k, comp) < 0.0) {
-                                double delta = -sn(i, j, k, comp);
-                                double sumX = 0.0;
+                                real delta = -sn(i, j, k, comp);
+                                real sumX = 0.0;
                                 for (int comp2 = start_comp; comp2 < start_comp + nspec; ++comp2)
                                     if (comp2 != comp && sn(i, j, k, comp2) >= 0.0) sumX += sn(i, j, k, comp2);
                                 for (int comp2 = start_comp; comp2 < start_comp + nspec; ++comp2)
                                     if (comp2 != comp && sn(i, j, k, comp2) >= 0.0) {
-                                        double frac = sn(i, j, k, comp2) / sumX;
+                                        real frac = sn(i, j, k, comp2) / sumX;
                                         sn(i, j, k, comp2) -= frac * delta;
                                     }
                                 sn(i, j, k, comp) = 0.0;
@@ -756,7 +756,7 @@ struct Stage2D {
     void DensityAdvance(MF& scalold, MF& scalnew, MF* sedge, MF* sflux, MF& scal_force, MF& etarhoflux, MF* umac,
                         int which_step) {
         const int spt = S.P.species_pred_type;
-        std::vector<double> rho0_edge_old, rho0_edge_new;
+        std::vector<real> rho0_edge_old, rho0_edge_new;
         Lev::CelltoEdge(S.rho0_old, rho0_edge_old);
         Lev::CelltoEdge(S.rho0_new, rho0_edge_new);
         scal_force.setVal(0.0);
@@ -797,7 +797,7 @@ struct Stage2D {
     // EnthalpyAdvance, 2-D (Source/MaestroEnthalpyAdvance.cpp:6-352)
     void EnthalpyAdvance(MF& scalold, MF& scalnew, MF* sedge, MF* sflux, MF& scal_force, MF* umac, int which_step) {
         const int ept = S.P.enthalpy_pred_type;
-        std::vector<double> rhoh0_edge_old, rhoh0_edge_new;
+        std::vector<real> rhoh0_edge_old, rhoh0_edge_new;
         Lev::CelltoEdge(S.rhoh0_old, rhoh0_edge_old);
         Lev::CelltoEdge(S.rhoh0_new, rhoh0_edge_new);
         scal_force.setVal(0.0);

@@ -17,7 +17,24 @@
 #include <string>
 #include <vector>
 
+#ifdef MO_TANGENT
+#include "mo_dual.hpp"
+#endif
+
 namespace mo {
+
+// The oracle's arithmetic type: double, or (tangent build) a value with its directional
+// derivative.  Geometry, indices and parameters are plain numbers in either build.
+#ifdef MO_TANGENT
+using real = Dual;
+#else
+using real = double;
+inline double value_of(double a) { return a; }
+inline double tangent_of(double) { return 0.0; }
+#endif
+inline double fabs_r(double a) { return std::fabs(a); }
+inline double copysign_r(double a, double b) { return std::copysign(a, b); }
+inline double sqrt_r(double a) { return std::sqrt(a); }
 
 // Reference state indices (Source/param/_variables:9-15, NumAux = 0).
 enum { Rho = 0, RhoH = 1, Temp = 2, Pi = 3, FirstSpec = 4 };
@@ -27,10 +44,10 @@ enum { reflect_odd = -1, int_dir = 0, reflect_even = 1, foextrap = 2, ext_dir = 
 enum { interior = 0, inflow = 1, outflow = 2, symmetry = 3, slipwall = 4, noslipwall = 5 };
 
 // amrex::min / amrex::max (std::min / std::max semantics: first argument wins ties).
-inline double mn(double a, double b) { return (b < a) ? b : a; }
-inline double mx(double a, double b) { return (a < b) ? b : a; }
-inline double cps(double a, double b) { return std::copysign(a, b); }
-inline double fab(double a) { return std::fabs(a); }
+inline real mn(real a, real b) { return (b < a) ? b : a; }
+inline real mx(real a, real b) { return (a < b) ? b : a; }
+inline real cps(real a, real b) { return copysign_r(a, b); }
+inline real fab(real a) { return fabs_r(a); }
 
 struct Box {
     int lo[3];
@@ -58,12 +75,12 @@ inline bool contains(const Box& b, int i, int j, int k) {
 
 // Array4-like view: (i,j,k,n) with i fastest.
 struct Arr {
-    double* p = nullptr;
+    real* p = nullptr;
     int lo[3] = {0, 0, 0};
     int hi[3] = {-1, -1, -1};
     long sj = 0, sk = 0, sn = 0;
     int nc = 0;
-    inline double& operator()(int i, int j, int k, int n = 0) const {
+    inline real& operator()(int i, int j, int k, int n = 0) const {
 #ifdef MO_BOUNDS
         if (i < lo[0] || i > hi[0] || j < lo[1] || j > hi[1] || k < lo[2] || k > hi[2] || n < 0 ||
             n >= nc)
@@ -85,10 +102,10 @@ struct Arr {
 struct MF {
     std::vector<Box> ba;
     int nc = 0, ng = 0, ix = -1;
-    std::vector<std::vector<double>> store;
+    std::vector<std::vector<real>> store;
     std::vector<Arr> a;
     void define(const std::vector<Box>& ba_, int nc_, int ng_, int ix_ = -1,
-                double init = std::nan("")) {
+                real init = std::nan("")) {
         ba = ba_;
         nc = nc_;
         ng = ng_;
@@ -112,10 +129,10 @@ struct MF {
     Box fabbox(int b) const { return grow(validbox(b), ng); }
     int size() const { return (int)ba.size(); }
     const Arr& operator[](int b) const { return a[b]; }
-    void setVal(double v) {
+    void setVal(real v) {
         for (auto& s : store) std::fill(s.begin(), s.end(), v);
     }
-    void setVal(double v, int c0, int ncomp, int ngr) {
+    void setVal(real v, int c0, int ncomp, int ngr) {
         for (int b = 0; b < size(); ++b) {
             Box bx = grow(validbox(b), ngr);
             const Arr& f = a[b];

@@ -291,3 +291,66 @@ def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservativ
                      which_step, start_comp, num_comp, is_conservative, tab)
     if rc != 0:
         raise RuntimeError("oracle: " + L.mo_last_error().decode())
+
+
+def lib_tl():
+    """The tangent-linear build of the oracle (libmaestro_oracle_tl.so)."""
+    name = "libmaestro_oracle_tl.so"
+    if name not in _LIBS:
+        path = os.path.join(HERE, name)
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.mo_run_stage_tl.restype = C.c_int
+        L.mo_last_error.restype = C.c_char_p
+        _LIBS[name] = L
+    return _LIBS[name]
+
+
+def run_stage_tl(cfg, duold, dsold, nthreads=0):
+    """The stage and its tangent-linear model on one level: returns (snew, dsnew), dsnew the
+    derivative of snew along (duold, dsold) (domain arrays shaped like uold / sold)."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    n = cfg["n"]
+    nscal = 4 + cfg["nspec"]
+    keep = []
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    inp = MoInputs()
+    for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                 "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+        setattr(inp, name, arr(cfg[name]))
+    out = MoOutputs()
+    snew = np.full((nscal, n[2], n[1], n[0]), np.nan)
+    dsnew = np.full_like(snew, np.nan)
+    out.snew = _p(snew)
+    boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    L = lib_tl()
+    rc = L.mo_run_stage_tl(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp),
+                           arr(duold), arr(dsold), C.byref(out), _p(dsnew), nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.mo_last_error().decode())
+    return snew, dsnew
+
+
+def steps_tl(cfg, s0, ds0, u, du, nsteps, nthreads=0):
+    """nsteps of the stage on a fixed velocity u (dt and rel_eps of cfg), the state carried
+    as the multi-step adjoint carries it (Rho, RhoH and the species from snew; Temp and Pi
+    unchanged), with its tangent along (du, ds0): returns (s_final, ds_final)."""
+    from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
+    comps = [RHO, RHOH] + list(range(FIRSTSPEC, s0.shape[0]))
+    s, ds = s0.copy(), ds0.copy()
+    c = dict(cfg)
+    c["uold"] = u
+    for _ in range(nsteps):
+        c["sold"] = s
+        snew, dsnew = run_stage_tl(c, du, ds, nthreads)
+        s, ds = s.copy(), ds.copy()
+        s[comps] = snew[comps]
+        ds[comps] = dsnew[comps]
+    return s, ds

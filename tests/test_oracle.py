@@ -231,3 +231,41 @@ def test_member_functions_keep_uniform_fields(ppm_type):
     for a, _ in sn:
         for c in [RHO, RHOH] + list(range(FIRSTSPEC, inp.nscal)):
             assert np.allclose(a[c], s0[c], rtol=1e-13, atol=0), c
+
+
+def test_tangent_linear_build_matches_finite_differences():
+    """The oracle's tangent-linear build (libmaestro_oracle_tl.so, the second reference of the
+    GPU adjoint): its values equal the plain oracle's bit for bit, and its derivative along a
+    single-cell direction equals central differences of two stage steps (h = 1e-6 |x|, with
+    the h/2 check that skips a limiter switch inside [x - h, x + h])."""
+    cfg = configs.adjoint_config(n=(16, 16, 16), max_grid=8, nspec=3)
+    S, U = cfg["sold"], cfg["uold"]
+    comps = [RHO, RHOH] + list(range(FIRSTSPEC, S.shape[0]))
+    snew, dsnew = pyoracle.run_stage_tl(cfg, np.zeros_like(U), np.zeros_like(S))
+    assert np.array_equal(snew[comps], pyoracle.run_stage(cfg)["snew"][comps])
+    assert np.all(dsnew[comps] == 0.0)
+    rng = np.random.default_rng(3)
+    w = rng.standard_normal(S.shape)
+    checked, worst = 0, 0.0
+    for t in range(8):
+        comp = comps[t % len(comps)]
+        i, j, k = (int(v) for v in rng.integers(0, 16, 3))
+        dS = np.zeros_like(S)
+        dS[comp, k, j, i] = 1.0
+        _, ds = pyoracle.steps_tl(cfg, S, dS, U, np.zeros_like(U), 2)
+        tl = float((w[comps] * ds[comps]).sum())
+        fd = []
+        for rel in (1e-6, 0.5e-6):
+            h = rel * max(abs(S[comp, k, j, i]), 0.1 * np.sqrt((S[comp] ** 2).mean()))
+            sp, sm = S.copy(), S.copy()
+            sp[comp, k, j, i] += h
+            sm[comp, k, j, i] -= h
+            a, _ = pyoracle.steps_tl(cfg, sp, np.zeros_like(S), U, np.zeros_like(U), 2)
+            b, _ = pyoracle.steps_tl(cfg, sm, np.zeros_like(S), U, np.zeros_like(U), 2)
+            fd.append(float((w[comps] * (a[comps] - b[comps])).sum()) / (2.0 * h))
+        if abs(fd[0] - fd[1]) > 1e-5 * max(abs(fd[0]), abs(fd[1])):
+            continue
+        worst = max(worst, abs(tl - fd[0]) / max(abs(fd[0]), 1e-300))
+        checked += 1
+    assert checked >= 5
+    assert worst <= 1e-6, worst
