@@ -756,7 +756,7 @@ def main():
     if sph is not None:
         line["spherical"] = sph
     if not args.no_cpu_baseline:
-        cb = run_cpu_baseline(1, 0)
+        cb = run_cpu_baseline(1, 1)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
     if ws > 1:
