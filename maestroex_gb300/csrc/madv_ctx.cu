@@ -297,6 +297,10 @@ static void free_layout(Ctx& c) {
     c.dviews = nullptr;
     if (c.hviews_pinned) cudaFreeHost(c.hviews_pinned);
     c.hviews_pinned = nullptr;
+    if (c.dviews_alias) cudaFree(c.dviews_alias);
+    c.dviews_alias = nullptr;
+    if (c.hviews_alias) cudaFreeHost(c.hviews_alias);
+    c.hviews_alias = nullptr;
     if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
     c.graph_exec = nullptr;
     c.graph_key.clear();
@@ -614,7 +618,78 @@ static int check_ready_h(const Hier& H) {
 struct StageIO {
     const madv_multifab *uold, *sold, *gpi, *thermal, *snew, *umac, *sedge, *sflux, *eta;
     int sold_out = 1;  // copy the converted-and-restored sold back to the caller
+    int alias = 0;     // AL_* fields worked in the caller's FABs directly (no copies)
 };
+enum { AL_SOLD = 1, AL_SNEW = 2, AL_UMAC = 4, AL_SEDGE = 8, AL_SFLUX = 16 };
+
+// A caller FAB can stand in for field fid when it has the field's index box (valid box grown
+// by the field's ghost width) and at least its components: views of both then address the
+// same elements.
+static bool can_alias(const Ctx& c, int fid, const madv_multifab* mf) {
+    if (!mf || mf->nfab != c.nb || !mf->fab) return false;
+    const FieldSpec& s = c.F[fid].spec;
+    for (int b = 0; b < c.nb; ++b) {
+        const madv_fab& f = mf->fab[b];
+        if (!f.p || f.ncomp < s.ncomp) return false;
+        const HBox v = valid_box(c, b, s.nodal);
+        for (int d = 0; d < 3; ++d)
+            if (f.lo[d] != v.lo[d] - s.ng || f.hi[d] != v.hi[d] + s.ng) return false;
+    }
+    return true;
+}
+
+// Decide which stage fields work in the caller's FABs (sold and snew, the MAC velocities,
+// edge states and fluxes: the largest copies of the stage) and point c.dviews at a table
+// with those views replaced.  The caller's FABs must be distinct from each other.
+// Returns the table to restore afterwards.
+static FabView* alias_fields(Ctx& c, StageIO& io) {
+    FabView* base = c.dviews;
+    io.alias = 0;
+    std::vector<const double*> ptrs;
+    auto add = [&](const madv_multifab* m, int n) {
+        for (int k = 0; m && k < n; ++k)
+            for (int b = 0; b < m[k].nfab; ++b) ptrs.push_back(m[k].fab[b].p);
+    };
+    add(io.uold, 1), add(io.sold, 1), add(io.gpi, 1), add(io.thermal, 1), add(io.snew, 1), add(io.eta, 1);
+    add(io.umac, c.ndim), add(io.sedge, c.ndim), add(io.sflux, c.ndim);
+    std::vector<const double*> sorted = ptrs;
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return base;
+    auto all = [&](int f0, const madv_multifab* m) {
+        if (!m) return false;
+        for (int d = 0; d < c.ndim; ++d)
+            if (!can_alias(c, f0 + d, &m[d])) return false;
+        return true;
+    };
+    if (io.sold_out && can_alias(c, F_SOLD, io.sold)) io.alias |= AL_SOLD;
+    if (can_alias(c, F_SNEW, io.snew)) io.alias |= AL_SNEW;
+    if (all(F_UMAC0, io.umac)) io.alias |= AL_UMAC;
+    if (all(F_SEDGE0, io.sedge)) io.alias |= AL_SEDGE;
+    if (all(F_SFLUX0, io.sflux)) io.alias |= AL_SFLUX;
+    if (!io.alias) return base;
+    const size_t nv = (size_t)NF_TOTAL * c.nb;
+    if (!c.dviews_alias) {
+        if (!cuda_ok(cudaMalloc(&c.dviews_alias, sizeof(FabView) * nv), "cudaMalloc(views)") ||
+            !cuda_ok(cudaMallocHost(&c.hviews_alias, sizeof(FabView) * nv), "cudaMallocHost(views)"))
+            throw Fail{MADV_ERR_CUDA};
+    }
+    std::memcpy(c.hviews_alias, c.hviews_pinned, sizeof(FabView) * nv);
+    auto swap = [&](int fid, int slot) {
+        for (int b = 0; b < c.nb; ++b) c.hviews_alias[fid * c.nb + b] = c.hviews_pinned[(F_USER + slot) * c.nb + b];
+    };
+    if (io.alias & AL_SOLD) swap(F_SOLD, U_SOLD);
+    if (io.alias & AL_SNEW) swap(F_SNEW, U_SNEW);
+    for (int d = 0; d < c.ndim; ++d) {
+        if (io.alias & AL_UMAC) swap(F_UMAC0 + d, U_UMAC0 + d);
+        if (io.alias & AL_SEDGE) swap(F_SEDGE0 + d, U_SEDGE0 + d);
+        if (io.alias & AL_SFLUX) swap(F_SFLUX0 + d, U_SFLUX0 + d);
+    }
+    if (!cuda_ok(cudaMemcpyAsync(c.dviews_alias, c.hviews_alias, sizeof(FabView) * nv, cudaMemcpyHostToDevice, c.stream),
+                 "cudaMemcpyAsync(views)"))
+        throw Fail{MADV_ERR_CUDA};
+    c.dviews = c.dviews_alias;
+    return base;
+}
 
 static int bind_stage(Ctx& c, const StageIO& io) {
     int rc;
@@ -640,7 +715,7 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
         if (!c.dry) cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream);
         set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
         copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, c.ndim, 0);
-        copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
+        if (!(io[l].alias & AL_SOLD)) copy_fab(c, F_SOLD, 0, F_USER + U_SOLD, 0, c.nscal, 0);
     }
     fill_patch_h(H, F_SOLD, 0, H[0].nscal, BCS_S, 0, 0, 0);
     for (int l = 0; l < H.n(); ++l) {
@@ -649,11 +724,16 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
         else set_val(c, F_GPI, 0.0, 0, 3, 0);
         set_val(c, F_THERMAL, 0.0, 0, 1, 1);
         if (io[l].thermal) copy_fab(c, F_THERMAL, 0, F_USER + U_THERMAL, 0, 1, 0);
-        set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
+        const int al = io[l].alias;
+        if (!(al & AL_SNEW)) set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
         for (int d = 0; d < 3; ++d) {
             set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
-            set_val(c, F_SEDGE0 + d, 0.0, 0, c.nscal, 0);
-            set_val(c, F_SFLUX0 + d, 0.0, 0, c.nscal, 0);
+            // (Source/MaestroAdvance.cpp:190-191); in a caller's FAB only Temp and Pi are not
+            // overwritten by the stage
+            if (al & AL_SEDGE) set_val(c, F_SEDGE0 + d, 0.0, TEMP, 2, 0);
+            else set_val(c, F_SEDGE0 + d, 0.0, 0, c.nscal, 0);
+            if (al & AL_SFLUX) set_val(c, F_SFLUX0 + d, 0.0, TEMP, 2, 0);
+            else set_val(c, F_SFLUX0 + d, 0.0, 0, c.nscal, 0);
         }
         set_val(c, F_ETA, 0.0, 0, 1, 0);
     }
@@ -669,15 +749,16 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
     // outputs (valid region)
     for (int l = 0; l < H.n(); ++l) {
         Ctx& c = H[l];
-        if (io[l].snew) {
+        const int al = io[l].alias;
+        if (io[l].snew && !(al & AL_SNEW)) {
             copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 2, 0);
             copy_fab(c, F_USER + U_SNEW, FIRSTSPEC, F_SNEW, FIRSTSPEC, c.nspec, 0);
         }
-        if (io[l].sold_out) copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
+        if (io[l].sold_out && !(al & AL_SOLD)) copy_fab(c, F_USER + U_SOLD, 0, F_SOLD, 0, c.nscal, 0);
         for (int d = 0; d < c.ndim; ++d) {
-            if (io[l].umac) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
-            if (io[l].sedge) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
-            if (io[l].sflux) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);
+            if (io[l].umac && !(al & AL_UMAC)) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 0);
+            if (io[l].sedge && !(al & AL_SEDGE)) copy_fab(c, F_USER + U_SEDGE0 + d, 0, F_SEDGE0 + d, 0, c.nscal, 0);
+            if (io[l].sflux && !(al & AL_SFLUX)) copy_fab(c, F_USER + U_SFLUX0 + d, 0, F_SFLUX0 + d, 0, c.nscal, 0);
         }
         if (io[l].eta) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
     }
@@ -1293,12 +1374,25 @@ static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab*
     Ctx& c = h->c;
     set_mode(H, (cudaStream_t)stream, 0, false);
     reset_launches(H);
+    // restores every level's view table on every way out
+    std::vector<FabView*> base_views(nlev, nullptr);
+    struct Restore {
+        Hier& H;
+        std::vector<FabView*>& v;
+        ~Restore() {
+            for (int l = 0; l < (int)v.size(); ++l)
+                if (v[l]) H[l].dviews = v[l];
+        }
+    } restore{H, base_views};
     try {
         for (int l = 0; l < nlev; ++l)
             if ((rc = bind_stage(H[l], io[l]))) return rc;
+        // caller FABs laid out as the stage's fields are worked in directly (no copies)
+        for (int l = 0; l < nlev; ++l) base_views[l] = alias_fields(H[l], io[l]);
         if (mode == MADV_MODE_GRAPH) {
             std::vector<const void*> key;
             for (int l = 0; l < nlev; ++l) {
+                key.push_back((const void*)(intptr_t)io[l].alias);
                 const madv_multifab* all[] = {io[l].uold, io[l].sold, io[l].gpi, io[l].thermal, io[l].snew, io[l].eta};
                 for (auto m : all) {
                     key.push_back(m);

@@ -118,6 +118,10 @@ struct Ctx {
     std::vector<FabView> hviews;  // NF_TOTAL * nb
     FabView* dviews = nullptr;
     FabView* hviews_pinned = nullptr;
+    // the table of a stage call that works in caller FABs laid out as its fields
+    // (built from hviews_pinned with those fields' views replaced; allocated on first use)
+    FabView* dviews_alias = nullptr;
+    FabView* hviews_alias = nullptr;
     std::map<std::array<int, 8>, RegionTable> regions;
     std::map<std::array<int, 3>, CopyTable> copies;
     cudaStream_t stream = nullptr;
