@@ -51,6 +51,30 @@ __device__ __forceinline__ double upwind(double u, double l, double r, long long
     return 0.5 * (l + r);
 }
 
+// 3. Scaling by 2 and by 1/2 as a step of the exponent field: exact, and equal to the FP
+//    multiply, whenever x and the result are normal numbers; zeros, subnormals, infinities
+//    and results that would leave the normal range take the multiply.
+__device__ __forceinline__ double twice(double x) {
+    const long long b = dbits(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    return (e >= 1 && e <= 2045) ? __longlong_as_double(b + (1LL << 52)) : 2.0 * x;
+}
+__device__ __forceinline__ double half(double x) {
+    const long long b = dbits(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    return (e >= 2 && e <= 2046) ? __longlong_as_double(b - (1LL << 52)) : 0.5 * x;
+}
+
+// 4. The sign of a product, x*y > 0, without the multiply: x and y non-zero with equal signs,
+//    unless the product could round to zero (|x*y| <= 2^-1075 is only possible when the
+//    biased exponents sum to 971 or less), where the multiply decides.
+__device__ __forceinline__ bool prod_gt0(double x, double y) {
+    const long long bx = dbits(x), by = dbits(y);
+    const long long ax = bx & ABS_MASK, ay = by & ABS_MASK;
+    if ((int)(ax >> 52) + (int)(ay >> 52) <= 971) return x * y > 0.0;
+    return (bx ^ by) >= 0;  // both exponents are then non-zero, so neither is a zero
+}
+
 struct RecipC {
     double y, zh, zl;
 };

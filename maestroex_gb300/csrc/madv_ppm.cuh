@@ -16,12 +16,17 @@ template <int D>
 __device__ __forceinline__ double ppm_dsvl(const FabView& s, int sc, int i, int j, int k) {
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     auto S = SHIFT_S(s, sc);
-    const double dsc = 0.5 * (S(1) - S(-1));
-    const double dsl = 2.0 * (S(0) - S(-1));
-    const double dsr = 2.0 * (S(1) - S(0));
-    double v = 0.0;
-    if (dsl * dsr > 0.0) v = copysign(1.0, dsc) * mn(fabs(dsc), mn(fabs(dsl), fabs(dsr)));
-    return v;
+    const double dsc = half(S(1) - S(-1));
+    const double dsl = twice(S(0) - S(-1));
+    const double dsr = twice(S(1) - S(0));
+    // reference: if (dsl*dsr > 0) dsvl = copysign(1,dsc) * min(|dsc|, min(|dsl|, |dsr|)).
+    // The minimum of non-negative (finite) doubles is the minimum of their bit patterns, and
+    // copysign(1, dsc) * m with m >= 0 is m with the sign of dsc.
+    if (!prod_gt0(dsl, dsr)) return 0.0;
+    long long m = dbits(dsc) & ABS_MASK;
+    m = min(m, dbits(dsl) & ABS_MASK);
+    m = min(m, dbits(dsr) & ABS_MASK);
+    return __longlong_as_double(m | (dbits(dsc) & SIGN_BIT));
 }
 
 // Interior fourth-order limited face value (ppm_type 2), face between cells c+m-1 and c+m.
