@@ -77,7 +77,8 @@ __device__ __forceinline__ void region_ijk(const RegionBox& r, long l, int& i, i
     int i, j, k;                                                          \
     region_ijk((R)[e_], gid_ - (R)[e_].start, i, j, k)
 
-// amrex::min / amrex::max (std::min / std::max semantics).
+// amrex::min / amrex::max (std::min / std::max semantics).  (An integer-key form measured
+// slower: the FP64 min/max instruction is not the costly part of the FP64 pipe.)
 __device__ __forceinline__ double mn(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double mx(double a, double b) { return (a < b) ? b : a; }
 

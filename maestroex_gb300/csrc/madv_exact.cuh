@@ -65,14 +65,15 @@ __device__ __forceinline__ double half(double x) {
     return (e >= 2 && e <= 2046) ? __longlong_as_double(b - (1LL << 52)) : 0.5 * x;
 }
 
-// 4. The sign of a product, x*y > 0, without the multiply: x and y non-zero with equal signs,
-//    unless the product could round to zero (|x*y| <= 2^-1075 is only possible when the
-//    biased exponents sum to 971 or less), where the multiply decides.
+// 4. The sign of a product, x*y > 0, without the multiply: for normal x and y whose biased
+//    exponents sum to more than 971, |x*y| >= 2^-1074 cannot round to zero, and the product
+//    is positive exactly when the signs agree.  Zeros, subnormals and smaller exponent sums
+//    take the multiply.
 __device__ __forceinline__ bool prod_gt0(double x, double y) {
     const long long bx = dbits(x), by = dbits(y);
-    const long long ax = bx & ABS_MASK, ay = by & ABS_MASK;
-    if ((int)(ax >> 52) + (int)(ay >> 52) <= 971) return x * y > 0.0;
-    return (bx ^ by) >= 0;  // both exponents are then non-zero, so neither is a zero
+    const int ex = (int)((bx & ABS_MASK) >> 52), ey = (int)((by & ABS_MASK) >> 52);
+    if (ex == 0 || ey == 0 || ex + ey <= 971) return x * y > 0.0;
+    return (bx ^ by) >= 0;
 }
 
 struct RecipC {

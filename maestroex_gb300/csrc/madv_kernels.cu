@@ -936,9 +936,9 @@ __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double 
 
 // MakeEdgeScalTransverse, 3-D (Source/MaestroMakeEdgeScalars.cpp:865-1359): D-faces
 // corrected in direction T.  Advective form: F_TCOEF comp T = (dt6/h_T)*(u_T sum).
-template <int D, int T>
-__global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double dt3h, int bclo, int bchi, int domlo,
-                                int domhi, long long epsb) {
+template <int D, int T, bool CONS>
+__global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bclo, int bchi, int domlo, int domhi,
+                                long long epsb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
@@ -946,7 +946,7 @@ __global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double
     const int il = i - di, jl = j - dj, kl = k - dk;
     const FabView st = VW(F_SIMH0 + T), sc = VW(F_SOLD);
     double lq, rq;
-    if (is_cons) {
+    if (CONS) {
         const FabView ut = VW(F_UMAC0 + T), dv = VW(F_DIVU);
         lq = at(VW(F_SL0 + D), i, j, k) -
              dt3h * (at(st, il + ti, jl + tj, kl + tk) * at(ut, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl) * at(ut, il, jl, kl)) -
@@ -988,9 +988,9 @@ __global__ void k_es_transverse(KARGS, int comp, int is_cons, double dt3, double
 // MakeEdgeScalEdges, 3-D (Source/MaestroMakeEdgeScalars.cpp:1361-1667).  Advective form:
 // F_TCOEF comp 3+t = (dt4/h_t)*(u_t sum).  force_zero: the component's force is
 // identically zero (species), so the + dt/2*force term is skipped.
-template <int D>
-__global__ void k_es_edges(KARGS, int comp, int is_cons, int force_zero, double dt2, double dt2h1, double dt2h2,
-                           double dt2hd, int bclo, int bchi, int domlo, int domhi, long long epsb) {
+template <int D, bool CONS>
+__global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double dt2h1, double dt2h2, double dt2hd,
+                           int bclo, int bchi, int domlo, int domhi, long long epsb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -1002,7 +1002,7 @@ __global__ void k_es_edges(KARGS, int comp, int is_cons, int force_zero, double 
     const FabView udf = VW(F_UMAC0 + D);
     const FabView sc = VW(F_SOLD);
     double lq, rq;
-    if (is_cons) {
+    if (CONS) {
         const FabView u1 = VW(F_UMAC0 + T1), u2 = VW(F_UMAC0 + T2), f = VW(F_SCALFORCE);
         const double fl = at(f, il, jl, kl, comp);
         const double fr = at(f, i, j, k, comp);
@@ -1059,17 +1059,26 @@ static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons
     ghi[D] = 1;
     const RegionTable& rt = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1);
     const double dt3 = c.P.dt / 3.0;
-    launch(c, rt, 1, k_es_transverse<D, T>, c.V(), comp, is_cons, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
-           c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
+    if (is_cons)
+        launch(c, rt, 1, k_es_transverse<D, T, true>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
+               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
+    else
+        launch(c, rt, 1, k_es_transverse<D, T, false>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
+               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
 }
 
 template <int D>
 static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero) {
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
     const double dt2 = 0.5 * c.P.dt;
-    launch(c, rg_grow(c, 0, D), 1, k_es_edges<D>, c.V(), comp, is_cons, force_zero, dt2, dt2 / c.P.dx[T1],
-           dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-           dbits_host(c.P.rel_eps));
+    if (is_cons)
+        launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, true>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
+               dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
+               dbits_host(c.P.rel_eps));
+    else
+        launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, false>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
+               dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
+               dbits_host(c.P.rel_eps));
 }
 
 // force_zero: the components' force is identically zero (DensityAdvance species)

@@ -74,7 +74,7 @@ __device__ __forceinline__ double ppm_face_value(const FabView& s, int sc, const
     } else if (PPMT == 1) {
         const double dvl = at(dv, i - di, j - dj, k - dk);
         const double dvr = at(dv, i, j, k);
-        v = 0.5 * (S(0) + S(-1)) - div_c(dvr - dvl, r6);
+        v = half(S(0) + S(-1)) - div_c(dvr - dvl, r6);
         v = mx(v, mn(S(0), S(-1)));
         v = mn(v, mx(S(0), S(-1)));
     } else {
@@ -125,13 +125,16 @@ __device__ __forceinline__ void ppm_cell_edges(const FabView& s, int sc, const F
         sp = Fc(1);
         const bool special = (lo_ext && I == domlo) || (hi_ext && I == domhi);
         if (!special) {
-            if ((sp - s0) * (s0 - sm) <= 0.0) {
+            // reference: (sp-s0)*(s0-sm) <= 0;  |sp-s0| >= 2|sm-s0|;  |sm-s0| >= 2|sp-s0|.
+            // sm-s0 = -(s0-sm) exactly; non-negative doubles compare like their bit patterns.
+            const double a = sp - s0, q = s0 - sm;
+            if (!prod_gt0(a, q)) {
                 sp = s0;
                 sm = s0;
-            } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
-                sp = 3.0 * s0 - 2.0 * sm;
-            } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
-                sm = 3.0 * s0 - 2.0 * sp;
+            } else if ((dbits(a) & ABS_MASK) >= (dbits(twice(q)) & ABS_MASK)) {
+                sp = 3.0 * s0 - twice(sm);
+            } else if ((dbits(q) & ABS_MASK) >= (dbits(twice(a)) & ABS_MASK)) {
+                sm = 3.0 * s0 - twice(sp);
             }
         }
     } else {
