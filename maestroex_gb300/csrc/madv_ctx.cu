@@ -571,7 +571,9 @@ static void density_advance(Hier& H, int which_step) {
     }
     for (auto* c : H.L) make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
     average_down_faces_h(H, F_SFLUX0, 0, nscal);
-    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
+    // scal_force.setVal(0) before UpdateScal (Source/MaestroDensityAdvance.cpp:229-231): of
+    // the components read from here on, only Rho has been written since the zeroing above
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHO, 1, 1);
     update_scal_h(H, FIRSTSPEC);
 }
 
@@ -580,7 +582,8 @@ static void density_advance(Hier& H, int which_step) {
 static void enthalpy_advance(Hier& H, int which_step) {
     const int ept = H[0].P.enthalpy_pred_type;
     const int nscal = H[0].nscal;
-    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
+    // scal_force.setVal(0) (Source/MaestroEnthalpyAdvance.cpp:51); the enthalpy half reads RhoH only
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
     addw0_h(H, F_UMAC0, -1.0);
     make_rhoh_force_h(H, 1, 1, 1);
     if (ept == 1) {

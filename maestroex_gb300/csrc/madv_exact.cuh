@@ -35,6 +35,8 @@ __host__ inline long long dbits_host(double x) {
 
 // x > 0.0
 __device__ __forceinline__ bool gt0(double x) { return dbits(x) > 0; }
+// x < 0.0 (-0 is not below 0): the pattern of -x is positive
+__device__ __forceinline__ bool lt0(double x) { return (dbits(x) ^ SIGN_BIT) > 0; }
 // |x| > 0.0
 __device__ __forceinline__ bool nz(double x) { return (dbits(x) & ABS_MASK) != 0; }
 // x > t, with tb = bits(t), t >= +0
@@ -51,29 +53,54 @@ __device__ __forceinline__ double upwind(double u, double l, double r, long long
     return 0.5 * (l + r);
 }
 
-// 3. Scaling by 2 and by 1/2 as a step of the exponent field: exact, and equal to the FP
-//    multiply, whenever x and the result are normal numbers; zeros, subnormals, infinities
-//    and results that would leave the normal range take the multiply.
+// 3. Scaling by 2 and by 1/2 on the bit pattern, equal to the FP multiply (round to nearest
+//    even) for every input: a normal result is an exponent step; a zero or subnormal x has
+//    |x| = a * 2^-1074 with a its magnitude bits (exponent field 1 included), so 2x is the
+//    pattern 2a and x/2 the pattern RN(a/2); 2x past the largest finite double is infinity.
+//    Infinities and NaNs pass through.  No FP64 instruction is issued.
 __device__ __forceinline__ double twice(double x) {
-    const long long b = dbits(x);
-    const int e = (int)((b >> 52) & 0x7ff);
-    return (e >= 1 && e <= 2045) ? __longlong_as_double(b + (1LL << 52)) : 2.0 * x;
+    const long long b = dbits(x), a = b & ABS_MASK, sg = b & SIGN_BIT;
+    long long r;
+    if (a < (1LL << 52)) r = sg | (a << 1);                  // zero or subnormal
+    else if (a < (0x7feLL << 52)) r = b + (1LL << 52);       // normal result
+    else if (a < (0x7ffLL << 52)) r = sg | (0x7ffLL << 52);  // overflow
+    else r = b;                                              // infinity, NaN
+    return __longlong_as_double(r);
 }
 __device__ __forceinline__ double half(double x) {
-    const long long b = dbits(x);
-    const int e = (int)((b >> 52) & 0x7ff);
-    return (e >= 2 && e <= 2046) ? __longlong_as_double(b - (1LL << 52)) : 0.5 * x;
+    const long long b = dbits(x), a = b & ABS_MASK, sg = b & SIGN_BIT;
+    long long r;
+    if (a >= (0x7ffLL << 52)) r = b;                              // infinity, NaN
+    else if (a >= (2LL << 52)) r = b - (1LL << 52);               // normal result
+    else r = sg | ((a >> 1) + (a & (a >> 1) & 1));                // subnormal result, ties to even
+    return __longlong_as_double(r);
 }
 
-// 4. The sign of a product, x*y > 0, without the multiply: for normal x and y whose biased
-//    exponents sum to more than 971, |x*y| >= 2^-1074 cannot round to zero, and the product
-//    is positive exactly when the signs agree.  Zeros, subnormals and smaller exponent sums
-//    take the multiply.
+// 4. The sign of a product, x*y > 0, without the multiply: the operands are non-zero with
+//    equal signs and the product does not round to zero.  With M the 53-bit significand (the
+//    magnitude bits of a subnormal, exponent field taken as 1) and E the exponent field,
+//    |x*y| = Mx*My * 2^(Ex+Ey-2150), which rounds to zero exactly when it is <= 2^-1075,
+//    i.e. Mx*My <= 2^(1075-Ex-Ey).  Normal operands with Ex+Ey >= 972 never do (the common
+//    case, decided by the signs alone); the rest compare the 106-bit significand product.
+//    Operands are not NaN.
 __device__ __forceinline__ bool prod_gt0(double x, double y) {
     const long long bx = dbits(x), by = dbits(y);
-    const int ex = (int)((bx & ABS_MASK) >> 52), ey = (int)((by & ABS_MASK) >> 52);
-    if (ex == 0 || ey == 0 || ex + ey <= 971) return x * y > 0.0;
-    return (bx ^ by) >= 0;
+    const long long ax = bx & ABS_MASK, ay = by & ABS_MASK;
+    if ((bx ^ by) < 0 || ax == 0 || ay == 0) return false;
+    const int ex = (int)(ax >> 52), ey = (int)(ay >> 52);
+    if (ex >= 1 && ey >= 1 && ex + ey >= 972) return true;
+    if (ex == 0x7ff || ey == 0x7ff) return true;  // an infinity times a non-zero
+    const unsigned long long mx = ex ? (unsigned long long)((ax & 0x000fffffffffffffLL) | (1LL << 52)) : ax;
+    const unsigned long long my = ey ? (unsigned long long)((ay & 0x000fffffffffffffLL) | (1LL << 52)) : ay;
+    const int k = 1075 - (ex ? ex : 1) - (ey ? ey : 1);
+    if (k < 0) return true;
+    if (k >= 106) return false;
+    const unsigned long long lo = mx * my, hi = __umul64hi(mx, my);
+    if (k >= 64) {
+        const unsigned long long t = 1ULL << (k - 64);
+        return hi > t || (hi == t && lo != 0);
+    }
+    return hi != 0 || lo > (1ULL << k);
 }
 
 struct RecipC {

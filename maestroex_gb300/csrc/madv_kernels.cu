@@ -1305,7 +1305,7 @@ __global__ void k_update_rhox(KARGS, int nspec, double dt, RecipC r0, RecipC r1,
     bool neg = false;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
         rho += at(sn, i, j, k, comp) - at(so, i, j, k, comp);
-        if (at(sn, i, j, k, comp) < 0.0) neg = true;
+        if (lt0(at(sn, i, j, k, comp))) neg = true;
     }
     if (rho < half_cutoff) {
         for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) at(sn, i, j, k, comp) *= half_cutoff / rho;

@@ -93,7 +93,26 @@ __global__ void k_selftest(unsigned long long n, unsigned long long seed, RecipC
         if (lt_negt(a, tb) != (a < -thr)) ++local;
         if (abs_gt_t(a, tb) != (fabs(a) > thr)) ++local;
         if (gt0(a) != (a > 0.0)) ++local;
+        if (lt0(a) != (a < 0.0)) ++local;
         if (nz(a) != (fabs(a) > 0.0)) ++local;
+        // bit-pattern scaling and product signs against the FP instructions, with operands
+        // pushed to the ends of the exponent range every few draws
+        const unsigned long long h2 = mix64(h ^ 0x5851f42d4c957f2dULL);
+        double e = a;
+        if ((h2 & 7) == 0) {  // near overflow / near the smallest normals
+            const long long eb = (h2 & 8) ? (2040 + (long long)((h2 >> 4) % 7)) : (long long)((h2 >> 4) % 4);
+            e = __longlong_as_double((dbits(a) & ~(0x7ffLL << 52)) | (eb << 52));
+        }
+        if (dbits(twice(e)) != dbits(2.0 * e)) ++local;
+        if (dbits(half(e)) != dbits(0.5 * e)) ++local;
+        // y with an exponent that puts Ex + Ey around the underflow limit of the product
+        const long long ex = (dbits(e) >> 52) & 0x7ff;
+        long long ey = (long long)((h2 >> 8) % 2047);
+        if (h2 & 16) ey = 960 - ex + (long long)((h2 >> 20) % 24);
+        if (ey < 0) ey = 0;
+        if (ey > 2046) ey = 2046;
+        const double yv = __longlong_as_double((long long)((h2 & 0x800fffffffffffffULL) | ((unsigned long long)ey << 52)));
+        if (prod_gt0(e, yv) != (e * yv > 0.0)) ++local;
     }
     if (local) atomicAdd(fails, local);
 }
