@@ -35,11 +35,21 @@ HBM_PEAK_FALLBACK = 6792.7
 #   fp64: FP64 warp instructions (smsp__inst_executed_pipe_fp64.sum) per valid cell, one launch
 #   dram: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per valid cell, one launch
 KERNEL_WORK = {
-    "k_ppm_cell<0,1,1>": {"fp64": 0.9596, "dram": None},
-    "k_ppm_cell<1,1,1>": {"fp64": 0.9595, "dram": 51.3},
-    "k_ppm_cell<2,1,1>": {"fp64": 0.9482, "dram": None},
+    "k_ppm_cell<0,1,1>": {"fp64": 0.6581, "dram": 50.5},
+    "k_ppm_cell<1,1,1>": {"fp64": 0.6467, "dram": 50.6},
+    "k_ppm_cell<2,1,1>": {"fp64": 0.6483, "dram": 52.5},
+    "k_ppm_cell<0,1,0>": {"fp64": 0.7031, "dram": 50.7},
+    "k_ppm_cell<1,1,0>": {"fp64": 0.6740, "dram": 51.1},
+    "k_ppm_cell<2,1,0>": {"fp64": 0.6500, "dram": 51.3},
+    "k_update_rhox": {"fp64": 9.0, "dram": 674.7},
+    "k_ppm_face<0,1>": {"fp64": 0.4189, "dram": None},
+    "k_ppm_face<1,1>": {"fp64": 0.4188, "dram": None},
+    "k_ppm_face<2,1>": {"fp64": 0.4286, "dram": None},
+    "k_es_edges<0,0>": {"fp64": 0.4613, "dram": None},
+    "k_es_edges<1,0>": {"fp64": 0.4613, "dram": None},
+    "k_es_edges<2,0>": {"fp64": 0.4613, "dram": None},
 }
-STAGE_FP64_PER_CELL = 189.02  # FP64 warp instructions per valid cell, whole stage
+STAGE_FP64_PER_CELL = 157.04  # FP64 warp instructions per valid cell, whole stage
 
 
 def measured_peaks():
@@ -64,7 +74,7 @@ def demangle(name):
     pos += 1
     args = []
     while True:
-        a = re.match(r"Li(n?\d+)E", name[pos:])
+        a = re.match(r"L[ib](n?\d+)E", name[pos:])
         if not a:
             break
         args.append(a.group(1).replace("n", "-"))
@@ -73,39 +83,49 @@ def demangle(name):
 
 
 def roofline(kern, ncell, stage_ms, fp64_tflops_probe, peaks, peak_kind):
-    """FP64-issue roofline of the dominant kernel (by device time in one batched stage).
+    """FP64-issue roofline of the dominant kernel: the kernel (all its template instances:
+    directions, PPM type, face or cell tracing velocity) with the most device time in one
+    batched stage.
 
-    achieved = FP64 warp instructions per launch (per-cell count x valid cells) / the
-    kernel's mean launch time (CUDA events around each launch); peak = the FP64 issue rate
-    of the DFMA-chain probe run in this process (1 DFMA = 2 flops, so issue rate = probe
+    achieved = FP64 warp instructions of its launches (per-cell counts x valid cells, from
+    ncu) / their summed launch time (CUDA events around each launch); peak = the FP64 issue
+    rate of the DFMA-chain probe run in this process (1 DFMA = 2 flops, so issue rate = probe
     TFLOP/s / 2).  Units: 10^12 FP64 lane-instructions per second (warp instructions x 32).
     """
+    inst_of = {}
     fam = {}
     for k, (n, ms) in kern.items():
         d = demangle(k)
-        fam.setdefault(d, [0, 0.0])
-        fam[d][0] += n
-        fam[d][1] += ms
-    top = max(fam.items(), key=lambda kv: kv[1][1])
-    name, (launches, ms) = top
+        inst_of.setdefault(d, [0, 0.0])
+        inst_of[d][0] += n
+        inst_of[d][1] += ms
+        base = d.split("<")[0]
+        fam.setdefault(base, {})[d] = inst_of[d]
+    name, members = max(fam.items(), key=lambda kv: sum(v[1] for v in kv[1].values()))
+    launches = sum(v[0] for v in members.values())
+    ms = sum(v[1] for v in members.values())
     issue_peak = fp64_tflops_probe / 2.0  # T lane-instructions/s
-    r = {"bound": "fp64", "kernel": name, "unit": "T FP64 lane-inst/s", "launches": launches,
-         "mean_launch_ms": ms / launches, "peak": issue_peak,
+    r = {"bound": "fp64", "kernel": name, "instances": sorted(members), "unit": "T FP64 lane-inst/s",
+         "launches": launches, "mean_launch_ms": ms / launches, "peak": issue_peak,
          "peak_kind": "measured in this run (DFMA-chain probe, %.3f TFLOP/s)" % fp64_tflops_probe}
-    work = KERNEL_WORK.get(name)
-    if work is None:
+    if any(m not in KERNEL_WORK for m in members):
         r.update({"achieved": None, "frac": None, "traffic": None,
-                  "note": "no ncu instruction count recorded for this kernel"})
+                  "note": "no ncu instruction count recorded for " +
+                          ", ".join(m for m in members if m not in KERNEL_WORK)})
         return r
-    inst = work["fp64"] * 32 * ncell
-    r["achieved"] = inst / (ms / launches * 1e-3) / 1e12
+    inst = sum(KERNEL_WORK[m]["fp64"] * 32 * ncell * v[0] for m, v in members.items())
+    r["achieved"] = inst / (ms * 1e-3) / 1e12
     r["frac"] = r["achieved"] / issue_peak
-    r["algorithmic_per_launch"] = {"fp64_lane_inst": inst, "per_valid_cell": work["fp64"] * 32}
-    r["traffic"] = None if work["dram"] is None else work["dram"] * ncell
-    hbm = peaks.get("hbm_gbs", HBM_PEAK_FALLBACK)
-    if work["dram"] is not None:
+    r["algorithmic_per_launch"] = {"fp64_lane_inst": inst / launches,
+                                   "per_valid_cell": inst / launches / ncell}
+    dram = [KERNEL_WORK[m]["dram"] for m in members]
+    if all(x is not None for x in dram):
+        r["traffic"] = sum(KERNEL_WORK[m]["dram"] * ncell * v[0] for m, v in members.items()) / launches
+        hbm = peaks.get("hbm_gbs", HBM_PEAK_FALLBACK)
         r["hbm"] = {"achieved_gbs": r["traffic"] / (ms / launches * 1e-3) / 1e9, "peak_gbs": hbm,
                     "peak_kind": peak_kind}
+    else:
+        r["traffic"] = None
     st_inst = STAGE_FP64_PER_CELL * 32 * ncell
     r["stage"] = {"fp64_lane_inst": st_inst, "achieved": st_inst / (stage_ms * 1e-3) / 1e12,
                   "frac": st_inst / (stage_ms * 1e-3) / 1e12 / issue_peak}
