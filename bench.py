@@ -220,14 +220,16 @@ def run_cpu_baseline(steps, warmup, nthreads=0):
     want = ("snew",)
     for _ in range(warmup):
         pyoracle.run_stage(cfg, nthreads=nthreads, want=want)
-    t0 = time.perf_counter()
+    times = []
     for _ in range(steps):
+        t0 = time.perf_counter()
         pyoracle.run_stage(cfg, nthreads=nthreads, want=want)
-    dt = (time.perf_counter() - t0) / steps
+        times.append(time.perf_counter() - t0)
+    dt = float(np.median(times))
     cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
     return {"value": ncell / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": "oracle on 128^3 cells in 8 boxes of 64^3, NumSpec 13, ppm_type 1 (same box shape "
-                      f"and per-cell work as the GPU workload), {steps} timed of {steps + warmup} runs",
+                      f"and per-cell work as the GPU workload), median of {steps} timed runs after {warmup}",
             "s_per_sample": dt}
 
 
@@ -776,7 +778,7 @@ def main():
     if sph is not None:
         line["spherical"] = sph
     if not args.no_cpu_baseline:
-        cb = run_cpu_baseline(1, 1)
+        cb = run_cpu_baseline(3, 1, nthreads=os.cpu_count() or 1)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
     if ws > 1:

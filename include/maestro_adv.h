@@ -199,6 +199,23 @@ int madv_make_rhox_flux(madv_ctx* ctx, int which_step, const madv_multifab* sflu
 int madv_make_rhoh_flux(madv_ctx* ctx, int which_step, const madv_multifab* sflux,
                         const madv_multifab* sedge, const madv_multifab* umac, void* stream);
 
+/* Maestro::VelocityAdvance (Source/Maestro.H:1689, Source/MaestroVelocityAdvance.cpp:5-82) with
+ * UpdateVel (Source/MaestroAdvection.cpp:299-526), one level, 3-D: the velocity edge states
+ * (MakeEdgeScal with is_vel, bcs_u) from the MAC velocity plus w0, and unew = uold - dt
+ * (Utilde.grad)Utilde + dt force - dt (w0.grad)Utilde, times the sponge.
+ * uold: 3 comps, valid region read (its ghost cells are filled with bcs_u, as the previous
+ * UpdateVel's FillPatch leaves them); sold: Rho of the first MakeVelForce (rho0_old);
+ * rhohalf: 1 comp, the density of the second (rho0_nph = (rho0_old + rho0_new) / 2); the
+ * gravity of both is the context's grav_cell.  gpi: 3 comps.  umac[3]: the projected MAC
+ * velocity without w0, valid faces read (ghost faces filled as MacProj leaves them).
+ * sponge: 1 comp or NULL (do_sponge = 0).  unew: 3 comps, written on the valid region and
+ * the ghost cells of the closing FillPatch it holds; uedge[3] (may be NULL): the velocity
+ * edge states, 3 comps on the valid faces. */
+int madv_velocity_advance(madv_ctx* ctx, const madv_multifab* uold, const madv_multifab* sold,
+                          const madv_multifab* rhohalf, const madv_multifab* gpi,
+                          const madv_multifab* umac, const madv_multifab* sponge,
+                          const madv_multifab* unew, const madv_multifab* uedge, void* stream);
+
 /* Maestro::UpdateScal (Source/Maestro.H:306, Source/MaestroAdvection.cpp:86-297) for RhoH
  * (start_comp 1, num_comp 1) or the species (FirstSpec, NumSpec; Rho follows).  stateold,
  * force: valid region; statenew: the updated components on the valid region and, where

@@ -376,8 +376,10 @@ static int upload_user_views(Ctx& c) {
 
 enum {
     U_UOLD = 0, U_SOLD, U_GPI, U_THERMAL, U_SNEW, U_UMAC0, U_UMAC1, U_UMAC2, U_SEDGE0, U_SEDGE1, U_SEDGE2,
-    U_SFLUX0, U_SFLUX1, U_SFLUX2, U_ETA, U_UTRANS0, U_UTRANS1, U_UTRANS2, U_UFULL, U_FORCE
+    U_SFLUX0, U_SFLUX1, U_SFLUX2, U_ETA, U_UTRANS0, U_UTRANS1, U_UTRANS2, U_UFULL, U_FORCE,
+    U_RHOHALF, U_SPONGE, U_UEDGE0, U_UEDGE1, U_UEDGE2
 };
+static_assert(U_UEDGE2 < A_WSOLD, "user slots of the entry points and of the adjoint");
 
 // Ghost width (at most maxg) that every FAB of mf holds around its box
 static int held_ghosts(const Ctx& c, const madv_multifab* mf, int nodal, int maxg) {
@@ -459,11 +461,13 @@ static void w0_carts(Hier& H) {
 }
 
 // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-259)
-static void make_vel_force_h(Hier& H) {
+// fe: the face velocity of the utilde force term (utrans in AdvancePremac, umac in
+// VelocityAdvance); rho0: the base-state density of the buoyancy
+static void make_vel_force_h(Hier& H, int fe = F_UTRANS0, const char* rho0 = "rho0_old") {
     const int nd = H[0].ndim;
     put1d_h(H, F_GRAVCART, "grav_cell", nd - 1, nd, 0, BCS_F, 0, 0, -1);
-    put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
-    for (auto* c : H.L) make_vel_force(*c);
+    put1d_h(H, F_RHO0CART, rho0, 0, 1, 0, BCS_S, RHO, 0, RHO);
+    for (auto* c : H.L) make_vel_force(*c, fe);
     average_down_h(H, F_VELFORCE, 0, nd);
     fill_patch_h(H, F_VELFORCE, 0, nd, BCS_U, 0, 1, -1);
 }
@@ -1810,6 +1814,66 @@ int madv_update_scal(madv_ctx* h, const madv_multifab* stateold, const madv_mult
         const int g = held_ghosts(c, statenew, -1, c.ng_s);
         copy_fab(c, F_USER + U_SNEW, start_comp, F_SNEW, start_comp, num_comp, g);
         if (start_comp == FIRSTSPEC) copy_fab(c, F_USER + U_SNEW, RHO, F_SNEW, RHO, 1, g);
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+// Maestro::VelocityAdvance (Source/MaestroVelocityAdvance.cpp:5-82) with UpdateVel
+// (Source/MaestroAdvection.cpp:299-526), one level, 3-D.  The velocity edge states are
+// MakeEdgeScal with is_vel on the internal state field (components 0-2 hold uold) and the
+// updated velocity goes through F_SNEW components 0-2, both scratch of this call.
+int madv_velocity_advance(madv_ctx* h, const madv_multifab* uold, const madv_multifab* sold,
+                          const madv_multifab* rhohalf, const madv_multifab* gpi, const madv_multifab* umac,
+                          const madv_multifab* sponge, const madv_multifab* unew, const madv_multifab* uedge,
+                          void* stream) {
+    Hier H;
+    int rc = begin_member(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!uold || !sold || !rhohalf || !gpi || !umac || !unew) return MADV_ERR_PARAM;
+    if (c.P.ppm_trace_forces) {
+        set_error("VelocityAdvance: ppm_trace_forces = 1 is not supported");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    try {
+        if ((rc = bind(c, U_UOLD, uold, 3, -1, 0)) || (rc = bind(c, U_SOLD, sold, 1, -1, 0)) ||
+            (rc = bind(c, U_RHOHALF, rhohalf, 1, -1, 0)) || (rc = bind(c, U_GPI, gpi, 3, -1, 0)) ||
+            (rc = bind(c, U_SPONGE, sponge, 1, -1, 0)) || (rc = bind(c, U_SNEW, unew, 3, -1, 0)))
+            return rc;
+        for (int d = 0; d < 3; ++d) {
+            if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 0))) return rc;
+            if (uedge && (rc = bind(c, U_UEDGE0 + d, &uedge[d], 3, d, 0))) return rc;
+        }
+        if ((rc = upload_user_views(c))) return rc;
+        copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, 3, 0);
+        for (int d = 0; d < 3; ++d) {
+            set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
+            copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 0);
+        }
+        sync_faces_h(H, F_UMAC0);  // the ghost faces as MacProj leaves them (FillUmacGhost)
+        w0_carts(H);
+        // MakeVelForce(vel_force, umac, sold, rho0_old, grav_cell_old, w0_force_cart, 1)
+        copy_fab(c, F_SOLD, RHO, F_USER + U_SOLD, RHO, 1, 0);
+        make_vel_force_h(H, F_UMAC0, "rho0_old");
+        addw0_h(H, F_UMAC0, 1.0);
+        // MakeEdgeScal(uold, uedge, umac, vel_force, true, bcs_u, AMREX_SPACEDIM, 0, 0, AMREX_SPACEDIM, false)
+        copy_fab(c, F_SOLD, 0, F_USER + U_UOLD, 0, 3, 0);
+        fill_patch_h(H, F_SOLD, 0, 3, BCS_U, 0, 1, -1);
+        copy_fab(c, F_SCALFORCE, 0, F_VELFORCE, 0, 3, 1);
+        for (int d = 0; d < 3; ++d) set_val(c, F_SEDGE0 + d, 0.0, 0, 3, 0);
+        make_edge_scal(c, 0, 3, BCS_U, 0, 0, 1);
+        addw0_h(H, F_UMAC0, -1.0);
+        // MakeVelForce(vel_force, umac, rhohalf, rho0_nph, grav_cell_nph, w0_force_cart, 1)
+        copy_fab(c, F_SOLD, RHO, F_USER + U_RHOHALF, 0, 1, 0);
+        make_vel_force_h(H, F_UMAC0, "rho0_avg");
+        update_vel(c, F_USER + U_UOLD, sponge ? F_USER + U_SPONGE : -1);
+        average_down_h(H, F_SNEW, 0, 3);
+        fill_patch_h(H, F_SNEW, 0, 3, BCS_U, 0, 1, -1);
+        copy_fab(c, F_USER + U_SNEW, 0, F_SNEW, 0, 3, held_ghosts(c, unew, -1, c.ng_s));
+        if (uedge)
+            for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UEDGE0 + d, 0, F_SEDGE0 + d, 0, 3, 0);
         return finish(H);
     } catch (const Fail& f) {
         return f.code;

@@ -60,7 +60,7 @@ enum FieldId {
     F_USER,                        // first slot of per-call views of caller FABs
     NF_INTERNAL = F_USER
 };
-constexpr int N_USER_SLOTS = 64;
+constexpr int N_USER_SLOTS = 72;
 constexpr int NF_TOTAL = F_USER + N_USER_SLOTS;
 
 // transverse-state field for the ordered pair (a, b), a != b
@@ -200,11 +200,12 @@ void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow);
 void add_fab(Ctx& c, int dst, int src, int nc, int ngrow);
 void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec = 0);
 void make_utrans(Ctx& c);
-void make_vel_force(Ctx& c);  // valid cells; F_GRAVCART / F_RHO0CART filled by the caller
+// valid cells; face velocity fe .. fe+2; F_GRAVCART / F_RHO0CART filled by the caller
+void make_vel_force(Ctx& c, int fe = F_UTRANS0);
 void vel_pred(Ctx& c);
 void vel_pred_prep(Ctx& c);  // the MakeUtrans work VelPred reuses, for a VelPred call on its own
 void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative,
-                    int force_zero);
+                    int force_zero, int is_vel = 0);
 void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform);
 void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal);
 void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag);
@@ -219,13 +220,14 @@ int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int
                 const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
                 const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
+void update_vel(Ctx& c, int fu, int fsponge);  // UpdateVel into F_SNEW comps 0-2; fsponge -1: no sponge
 
 // ---- spherical forms (madv_sphr.cu), reached through the wrappers above when c.sph
 void put1d_sph(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec);
 void make_w0mac(Ctx& c);
 void make_s0mac_faces(Ctx& c, int dst0);  // faces of F_S0CART2 into dst0 .. dst0 + 2
 void addw0_sph(Ctx& c, int f0, double mult);
-void make_vel_force_sph(Ctx& c);
+void make_vel_force_sph(Ctx& c, int fe);
 void modify_scal_force_sph(Ctx& c, int comp, int s0cart_fid, int fullform);
 void make_rhoh_force_sph(Ctx& c, int is_prediction, int add_thermal);
 void put_in_pert_form_sph(Ctx& c, const double* d_s0, int comp, int flag);
@@ -260,7 +262,7 @@ void uedge_interface(Ctx& cc, Ctx& cf, int f0);
 // state (A_WSOLD / A_WSNEW), state adjoints (A_ASOLD / A_ASNEW), edge-state adjoints, the
 // per-component scratch of the MakeEdgeScal transpose, and the caller's FABs.
 enum {
-    A_WSOLD = 20, A_WSNEW, A_ASOLD, A_ASNEW, A_AS, A_AFORCE,
+    A_WSOLD = 28, A_WSNEW, A_ASOLD, A_ASNEW, A_AS, A_AFORCE,
     A_AEDGE0, A_AEDGE1, A_AEDGE2,
     A_ASL0, A_ASL1, A_ASL2, A_ASR0, A_ASR1, A_ASR2, A_ASIMH0, A_ASIMH1, A_ASIMH2,
     A_AQ01, A_AQ02, A_AQ10, A_AQ12, A_AQ20, A_AQ21,

@@ -629,7 +629,7 @@ void make_utrans(Ctx& c) {
 
 // ============================================================ MakeVelForce
 // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:100-126)
-__global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz) {
+__global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz, int fe) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView gpi = VW(F_GPI), rho = VW(F_SOLD), vf = VW(F_VELFORCE);
     const double r = at(rho, i, j, k, RHO);
@@ -639,19 +639,19 @@ __global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz) {
     double f2 = (rhopert * at(VW(F_GRAVCART), i, j, k, 2) - at(gpi, i, j, k, 2)) / r - at(VW(F_W0FCART), i, j, k, 2);
     if (k <= -1 || k >= domhi) {
     } else {
-        const FabView we = VW(F_UTRANS2), w0 = VW(F_W0CART);
+        const FabView we = VW(fe + 2), w0 = VW(F_W0CART);
         f2 -= div_c((at(we, i, j, k + 1) + at(we, i, j, k)) * (at(w0, i, j, k + 1, 2) - at(w0, i, j, k, 2)), r2dz);
     }
     at(vf, i, j, k, 2) = f2;
 }
 
 // valid cells of one level; F_GRAVCART and F_RHO0CART are filled by the caller
-void make_vel_force(Ctx& c) {
-    if (c.sph) return make_vel_force_sph(c);
+void make_vel_force(Ctx& c, int fe) {
+    if (c.sph) return make_vel_force_sph(c, fe);
     if (c.ndim == 2) return make_vel_force_2d(c);
     set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
     launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
-           c.P.dom_hi[2], make_recip(2.0 * c.P.dx[2]));
+           c.P.dom_hi[2], make_recip(2.0 * c.P.dx[2]), fe);
 }
 
 // ============================================================ VelPred
@@ -892,7 +892,7 @@ __global__ void k_divu(KARGS, RecipC rdx0) {
 // MakeEdgeScalPredictor, 3-D (Source/MaestroMakeEdgeScalars.cpp:662-863)
 template <int D>
 __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double hd, int bclo, int bchi, int domlo,
-                               int domhi) {
+                               int domhi, int vclamp) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
@@ -913,6 +913,7 @@ __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double 
             l = at(sc, il, jl, kl, comp);
             r = l;
         } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
+            if (vclamp && bclo != BC_REFLECT_EVEN) r = mn(r, 0.0);  // is_vel, comp == D
             l = r;
         } else if (bclo == BC_REFLECT_ODD) {
             l = 0.0;
@@ -923,6 +924,7 @@ __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double 
             l = at(sc, i, j, k, comp);
             r = l;
         } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
+            if (vclamp && bchi != BC_REFLECT_EVEN) l = mx(l, 0.0);
             r = l;
         } else if (bchi == BC_REFLECT_ODD) {
             l = 0.0;
@@ -938,7 +940,7 @@ __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double 
 // corrected in direction T.  Advective form: F_TCOEF comp T = (dt6/h_T)*(u_T sum).
 template <int D, int T, bool CONS>
 __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bclo, int bchi, int domlo, int domhi,
-                                long long epsb) {
+                                long long epsb, int vclamp) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
@@ -966,6 +968,7 @@ __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bc
             lq = at(sc, il, jl, kl, comp);
             rq = lq;
         } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
+            if (vclamp && bclo != BC_REFLECT_EVEN) rq = mn(rq, 0.0);
             lq = rq;
         } else if (bclo == BC_REFLECT_ODD) {
             lq = 0.0;
@@ -976,6 +979,7 @@ __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bc
             lq = at(sc, i, j, k, comp);
             rq = lq;
         } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
+            if (vclamp && bchi != BC_REFLECT_EVEN) lq = mx(lq, 0.0);
             rq = lq;
         } else if (bchi == BC_REFLECT_ODD) {
             lq = 0.0;
@@ -990,7 +994,7 @@ __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bc
 // identically zero (species), so the + dt/2*force term is skipped.
 template <int D, bool CONS>
 __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double dt2h1, double dt2h2, double dt2hd,
-                           int bclo, int bchi, int domlo, int domhi, long long epsb) {
+                           int bclo, int bchi, int domlo, int domhi, long long epsb, int vclamp) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -1031,27 +1035,31 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
     double v = upwind(at(udf, i, j, k), lq, rq, epsb);
     if (I == domlo) {
         if (bclo == BC_EXT_DIR) v = at(sc, il, jl, kl, comp);
-        else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) v = rq;
+        else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP) v = vclamp ? mn(rq, 0.0) : rq;
+        else if (bclo == BC_REFLECT_EVEN) v = rq;
         else if (bclo == BC_REFLECT_ODD) v = 0.0;
     } else if (I == domhi + 1) {
         if (bchi == BC_EXT_DIR) v = at(sc, i, j, k, comp);
-        else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) v = lq;
+        else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP) v = vclamp ? mx(lq, 0.0) : lq;
+        else if (bchi == BC_REFLECT_EVEN) v = lq;
         else if (bchi == BC_REFLECT_ODD) v = 0.0;
     }
     at(VW(F_SEDGE0 + D), i, j, k, comp) = v;
 }
 
+// vclamp: velocity edge states (is_vel) of the component normal to the faces, whose
+// outflow-boundary values are clamped to outflow (Source/MaestroMakeEdgeScalars.cpp:715, 732)
 template <int D>
-static void es_predictor_launch(Ctx& c, int comp, const BCRecD& bc) {
+static void es_predictor_launch(Ctx& c, int comp, const BCRecD& bc, int vclamp) {
     int glo[3] = {1, 1, 1};
     glo[D] = 0;
     const RegionTable& rt = region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1);
     launch(c, rt, 1, k_es_predictor<D>, c.V(), comp, c.P.ppm_type, c.P.dt, c.P.dx[D], bc.lo[D], bc.hi[D],
-           c.P.dom_lo[D], c.P.dom_hi[D]);
+           c.P.dom_lo[D], c.P.dom_hi[D], vclamp);
 }
 
 template <int D, int T>
-static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons) {
+static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int vclamp) {
     constexpr int O = 3 - D - T;
     int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
     glo[O] = 1;
@@ -1061,28 +1069,28 @@ static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons
     const double dt3 = c.P.dt / 3.0;
     if (is_cons)
         launch(c, rt, 1, k_es_transverse<D, T, true>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
-               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
+               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps), vclamp);
     else
         launch(c, rt, 1, k_es_transverse<D, T, false>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
-               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps));
+               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps), vclamp);
 }
 
 template <int D>
-static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero) {
+static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp) {
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
     const double dt2 = 0.5 * c.P.dt;
     if (is_cons)
         launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, true>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-               dbits_host(c.P.rel_eps));
+               dbits_host(c.P.rel_eps), vclamp);
     else
         launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, false>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-               dbits_host(c.P.rel_eps));
+               dbits_host(c.P.rel_eps), vclamp);
 }
 
 // force_zero: the components' force is identically zero (DensityAdvance species)
-void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons, int force_zero) {
+void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons, int force_zero, int is_vel) {
     if (c.ndim == 2) return make_edge_scal_2d_entry(c, start_comp, num_comp, which_bcs, is_cons);
     const BCRecD* bh = bcs_host(c, which_bcs);
     if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), make_recip(c.P.dx[0]));
@@ -1097,18 +1105,19 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
         } else {
             for (int d = 0; d < 3; ++d) ppm_any(c, d, F_SOLD, comp, bc, F_UMAC0 + d, 0, 1, F_IPC0, F_IMC0);
         }
-        es_predictor_launch<0>(c, comp, bc);
-        es_predictor_launch<1>(c, comp, bc);
-        es_predictor_launch<2>(c, comp, bc);
-        es_transverse_launch<0, 1>(c, comp, bc, is_cons);
-        es_transverse_launch<0, 2>(c, comp, bc, is_cons);
-        es_transverse_launch<1, 0>(c, comp, bc, is_cons);
-        es_transverse_launch<1, 2>(c, comp, bc, is_cons);
-        es_transverse_launch<2, 0>(c, comp, bc, is_cons);
-        es_transverse_launch<2, 1>(c, comp, bc, is_cons);
-        es_edges_launch<0>(c, comp, bc, is_cons, force_zero);
-        es_edges_launch<1>(c, comp, bc, is_cons, force_zero);
-        es_edges_launch<2>(c, comp, bc, is_cons, force_zero);
+        const int v0 = is_vel && comp == 0, v1 = is_vel && comp == 1, v2 = is_vel && comp == 2;
+        es_predictor_launch<0>(c, comp, bc, v0);
+        es_predictor_launch<1>(c, comp, bc, v1);
+        es_predictor_launch<2>(c, comp, bc, v2);
+        es_transverse_launch<0, 1>(c, comp, bc, is_cons, v0);
+        es_transverse_launch<0, 2>(c, comp, bc, is_cons, v0);
+        es_transverse_launch<1, 0>(c, comp, bc, is_cons, v1);
+        es_transverse_launch<1, 2>(c, comp, bc, is_cons, v1);
+        es_transverse_launch<2, 0>(c, comp, bc, is_cons, v2);
+        es_transverse_launch<2, 1>(c, comp, bc, is_cons, v2);
+        es_edges_launch<0>(c, comp, bc, is_cons, force_zero, v0);
+        es_edges_launch<1>(c, comp, bc, is_cons, force_zero, v1);
+        es_edges_launch<2>(c, comp, bc, is_cons, force_zero, v2);
         if (c.edge_tape) c.edge_tape(comp);
     }
 }
@@ -1340,6 +1349,55 @@ __global__ void k_update_rhoh(KARGS, double dt, RecipC r0, RecipC r1, RecipC r2,
                             div_c(at(fz, i, j, k + 1, RHOH) - at(fz, i, j, k, RHOH), r2));
     at(sn, i, j, k, RHOH) = at(so, i, j, k, RHOH) + dt * (-divterm + at(fo, i, j, k, RHOH));
     if (eos_check && at(sn, i, j, k, RHO) <= cutoff) atomicOr(flag, 1);
+}
+
+// Maestro::UpdateVel, 3-D (Source/MaestroAdvection.cpp:299-526): unew = uold - dt (Utilde.grad)
+// Utilde + dt force, minus dt (w0.grad) Utilde (planar: w0bar from w0_cart of cells k and k+1;
+// spherical: w0mac averaged to the cell, every direction), times the sponge where given.
+// uold: field fu; MAC velocity without w0: F_UMAC*; edge states: F_SEDGE* comps 0-2; force:
+// F_VELFORCE; output F_SNEW comps 0-2.
+__global__ void k_update_vel(KARGS, int fu, int fsp, int sph, double dt, RecipC r0, RecipC r1, RecipC r2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView uo = VW(fu), un = VW(F_SNEW), um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
+    const FabView ex = VW(F_SEDGE0), ey = VW(F_SEDGE1), ez = VW(F_SEDGE2), f = VW(F_VELFORCE);
+    const double ubar = 0.5 * (at(um, i, j, k) + at(um, i + 1, j, k));
+    const double vbar = 0.5 * (at(vm, i, j, k) + at(vm, i, j + 1, k));
+    const double wbar = 0.5 * (at(wm, i, j, k) + at(wm, i, j, k + 1));
+    double v[3];
+    for (int n = 0; n < 3; ++n) {
+        const double ugrad = div_c(ubar * (at(ex, i + 1, j, k, n) - at(ex, i, j, k, n)), r0) +
+                             div_c(vbar * (at(ey, i, j + 1, k, n) - at(ey, i, j, k, n)), r1) +
+                             div_c(wbar * (at(ez, i, j, k + 1, n) - at(ez, i, j, k, n)), r2);
+        v[n] = at(uo, i, j, k, n) - dt * ugrad + dt * at(f, i, j, k, n);
+    }
+    if (!sph) {
+        const FabView w0c = VW(F_W0CART);
+        const double w0bar = 0.5 * (at(w0c, i, j, k, 2) + at(w0c, i, j, k + 1, 2));
+        for (int n = 0; n < 3; ++n) {
+            v[n] -= div_c(dt * w0bar * (at(ez, i, j, k + 1, n) - at(ez, i, j, k, n)), r2);
+            if (fsp >= 0) v[n] *= at(VW(fsp), i, j, k);
+        }
+    } else {
+        const FabView wx = VW(F_W0MAC0), wy = VW(F_W0MAC1), wz = VW(F_W0MAC2);
+        double w0r[3];
+        for (int n = 0; n < 3; ++n) {
+            const double gx = div_c(at(ex, i + 1, j, k, n) - at(ex, i, j, k, n), r0);
+            const double gy = div_c(at(ey, i, j + 1, k, n) - at(ey, i, j, k, n), r1);
+            const double gz = div_c(at(ez, i, j, k + 1, n) - at(ez, i, j, k, n), r2);
+            w0r[n] = gx * 0.5 * (at(wx, i, j, k) + at(wx, i + 1, j, k)) +
+                     gy * 0.5 * (at(wy, i, j, k) + at(wy, i, j + 1, k)) +
+                     gz * 0.5 * (at(wz, i, j, k) + at(wz, i, j, k + 1));
+        }
+        for (int n = 0; n < 3; ++n) v[n] -= dt * w0r[n];
+        if (fsp >= 0)
+            for (int n = 0; n < 3; ++n) v[n] *= at(VW(fsp), i, j, k);
+    }
+    for (int n = 0; n < 3; ++n) at(un, i, j, k, n) = v[n];
+}
+
+void update_vel(Ctx& c, int fu, int fsponge) {
+    launch(c, rg_grow(c, 0), 1, k_update_vel, c.V(), fu, fsponge, (int)c.sph, c.P.dt, make_recip(c.P.dx[0]),
+           make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
 }
 
 void update_scal(Ctx& c, int start_comp) {

@@ -97,7 +97,7 @@ void addw0_sph(Ctx& c, int f0, double mult) {
 
 // MakeVelForce, spherical (Source/MaestroForce.cpp:151-252; MakeNormal :1190-1227).  The
 // exact base state has gradw0 = 0 (:30-41): the utilde term subtracts Ut.e_r * 0 * e_r.
-__global__ void k_vel_force_sph(KARGS, double cutoff_rho, SphGeo g) {
+__global__ void k_vel_force_sph(KARGS, double cutoff_rho, SphGeo g, int fe) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const double gradw0 = 0.0;
     double x, y, z;
@@ -110,16 +110,17 @@ __global__ void k_vel_force_sph(KARGS, double cutoff_rho, SphGeo g) {
     if (r < cutoff_rho) rhopert = 0.0;
     for (int dim = 0; dim < 3; ++dim)
         at(vf, i, j, k, dim) = (rhopert * at(grav, i, j, k, dim) - at(gpi, i, j, k, dim)) / r - at(w0f, i, j, k, dim);
-    const FabView ue = VW(F_UTRANS0), ve = VW(F_UTRANS1), we = VW(F_UTRANS2);
+    const FabView ue = VW(fe), ve = VW(fe + 1), we = VW(fe + 2);
     const double ut_dot_er = 0.5 * (at(ue, i, j, k) + at(ue, i + 1, j, k)) * nrm[0] +
                              0.5 * (at(ve, i, j, k) + at(ve, i, j + 1, k)) * nrm[1] +
                              0.5 * (at(we, i, j, k) + at(we, i, j, k + 1)) * nrm[2];
     for (int dim = 0; dim < 3; ++dim) at(vf, i, j, k, dim) -= ut_dot_er * gradw0 * nrm[dim];
 }
 
-void make_vel_force_sph(Ctx& c) {
+void make_vel_force_sph(Ctx& c, int fe) {
     set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
-    launch(c, rg_grow(c, 0), 1, k_vel_force_sph, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density, c.geo);
+    launch(c, rg_grow(c, 0), 1, k_vel_force_sph, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density, c.geo,
+           fe);
 }
 
 // ModifyScalForce, spherical (Source/MaestroForce.cpp:335-412); divu_cart is

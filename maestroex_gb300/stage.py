@@ -253,6 +253,13 @@ class ScalarAdvectionStage:
         check(lib().madv_update_scal(self.ctx, _ref(stateold), _ref(statenew), _ref3(sflux), _ref(force),
                                      start_comp, num_comp, C.c_void_p(s)))
 
+    def velocity_advance(self, uold, sold, rhohalf, gpi, umac, unew, uedge=None, sponge=None, stream=None):
+        """Maestro::VelocityAdvance + UpdateVel (3-D, one level): unew (and the velocity edge
+        states uedge) from uold, the projected MAC velocity umac (without w0) and rhohalf."""
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib().madv_velocity_advance(self.ctx, _ref(uold), _ref(sold), _ref(rhohalf), _ref(gpi), _ref3(umac),
+                                          _ref(sponge), _ref(unew), _ref3(uedge), C.c_void_p(s)))
+
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
 

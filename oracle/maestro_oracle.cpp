@@ -659,8 +659,7 @@ struct Lev {
     // Maestro::MakeEdgeScal, 3-D, is_vel = false (Source/MaestroMakeEdgeScalars.cpp:6-302,
     // 662-1667).  BC overrides of the is_vel branches are kept for completeness.
     void MakeEdgeScal(MF& state, MF* sedge, MF* umac, MF& force, const std::vector<BCRec>& bcs, int start_scomp,
-                      int start_bccomp, int num_comp, bool is_conservative) {
-        const bool is_vel = false;
+                      int start_bccomp, int num_comp, bool is_conservative, bool is_vel = false) {
         const int* domlo = L.dom.lo;
         const int* domhi = L.dom.hi;
         const real h[3] = {L.dx[0], L.dx[1], L.dx[2]};
@@ -1146,6 +1145,50 @@ struct Lev {
 
     // ------------------------------------------------------------------ UpdateScal
     // Maestro::UpdateScal, one level (Source/MaestroAdvection.cpp:86-256)
+    // Maestro::UpdateVel (Source/MaestroAdvection.cpp:299-526): unew = uold - dt (U.grad)U
+    // + dt force, minus the w0 advection term, times the sponge where one is given
+    void UpdateVel(MF& uold, MF& unew, MF* umac, MF* uedge, MF& force, MF* sponge) {
+        const double* dx = L.dx;
+        const real dt_loc = dt;
+        for (int b = 0; b < nb; ++b) {
+            const Arr &uo = uold[b], &un = unew[b], &um = umac[0][b], &vm = umac[1][b], &wm = umac[2][b];
+            const Arr &ex = uedge[0][b], &ey = uedge[1][b], &ez = uedge[2][b], &f = force[b];
+            MO_FOR3(L.ba[b]) {
+                const real ubar = 0.5 * (um(i, j, k) + um(i + 1, j, k));
+                const real vbar = 0.5 * (vm(i, j, k) + vm(i, j + 1, k));
+                const real wbar = 0.5 * (wm(i, j, k) + wm(i, j, k + 1));
+                real ugrad[3];
+                for (int n = 0; n < 3; ++n)
+                    ugrad[n] = ubar * (ex(i + 1, j, k, n) - ex(i, j, k, n)) / dx[0] +
+                               vbar * (ey(i, j + 1, k, n) - ey(i, j, k, n)) / dx[1] +
+                               wbar * (ez(i, j, k + 1, n) - ez(i, j, k, n)) / dx[2];
+                for (int n = 0; n < 3; ++n) un(i, j, k, n) = uo(i, j, k, n) - dt_loc * ugrad[n] + dt_loc * f(i, j, k, n);
+                if (!P.spherical) {
+                    const Arr& w0c = w0_cart[b];
+                    const real w0bar = 0.5 * (w0c(i, j, k, 2) + w0c(i, j, k + 1, 2));
+                    for (int n = 0; n < 3; ++n) {
+                        un(i, j, k, n) -= dt_loc * w0bar * (ez(i, j, k + 1, n) - ez(i, j, k, n)) / dx[2];
+                        if (sponge) un(i, j, k, n) *= (*sponge)[b](i, j, k);
+                    }
+                } else {
+                    const Arr &w0x = w0mac[0][b], &w0y = w0mac[1][b], &w0z = w0mac[2][b];
+                    real w0r[3];
+                    for (int n = 0; n < 3; ++n) {
+                        const real gx = (ex(i + 1, j, k, n) - ex(i, j, k, n)) / dx[0];
+                        const real gy = (ey(i, j + 1, k, n) - ey(i, j, k, n)) / dx[1];
+                        const real gz = (ez(i, j, k + 1, n) - ez(i, j, k, n)) / dx[2];
+                        w0r[n] = gx * 0.5 * (w0x(i, j, k) + w0x(i + 1, j, k)) +
+                                 gy * 0.5 * (w0y(i, j, k) + w0y(i, j + 1, k)) +
+                                 gz * 0.5 * (w0z(i, j, k) + w0z(i, j, k + 1));
+                    }
+                    for (int n = 0; n < 3; ++n) un(i, j, k, n) -= dt_loc * w0r[n];
+                    if (sponge)
+                        for (int n = 0; n < 3; ++n) un(i, j, k, n) *= (*sponge)[b](i, j, k);
+                }
+            }
+        }
+    }
+
     void UpdateScal(MF& sold, MF& snew, MF* sflux, MF& force, int start_comp, int num_comp) {
         const double* dx = L.dx;
         const real dt_loc = dt;
@@ -1376,13 +1419,13 @@ struct Stage {
         SyncFaces(u);
     }
     // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-259)
-    void MakeVelForce(VMF& vel_force, VF& uedge, VMF& sold, VMF& w0_force_cart) {
+    void MakeVelForce(VMF& vel_force, VF& uedge, VMF& sold, VMF& w0_force_cart, const BS* rho0 = nullptr) {
         VMF grav_cart(nlev), rho0_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) {
             grav_cart[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
             rho0_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
         }
-        Put1dArrayOnCart(bs(&Lev::rho0_old), rho0_cart, false, false, &bcs_s(), Rho, false);
+        Put1dArrayOnCart(rho0 ? *rho0 : bs(&Lev::rho0_old), rho0_cart, false, false, &bcs_s(), Rho, false);
         Put1dArrayOnCart(bs(&Lev::grav_cell), grav_cart, false, true, &bcs_f(), 0, false);
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeVelForce(vel_force[lev], uedge[lev].data(), sold[lev], w0_force_cart[lev], grav_cart[lev],
@@ -1428,10 +1471,12 @@ struct Stage {
 
     // ------------------------------------------------------------------ scalars
     void MakeEdgeScal(VMF& state, VF& sedge, VF& umac, VMF& force, const std::vector<BCRec>& bcs, int start_scomp,
-                      int start_bccomp, int num_comp, bool is_conservative) {
+                      int start_bccomp, int num_comp, bool is_conservative, bool is_vel = false) {
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeEdgeScal(state[lev], sedge[lev].data(), umac[lev].data(), force[lev], bcs, start_scomp,
-                                start_bccomp, num_comp, is_conservative);
+                                start_bccomp, num_comp, is_conservative, is_vel);
+        // edge restriction of velocity edge states (Source/MaestroMakeEdgeScalars.cpp:294-301)
+        if (is_vel && nlev > 1) AverageDownFaces(sedge);
     }
     // Maestro::ModifyScalForce (Source/MaestroForce.cpp:261-467)
     void ModifyScalForce(VMF& scal_force, VMF& state, VF& umac, const BS& s0_edge, VMF& s0_cart, int comp,
@@ -1608,6 +1653,34 @@ struct Stage {
         MakeRhoHForce(scal_force, 0, umac, 0, which_step);
         Addw0(umac, 1.0);
         UpdateScal(scalold, scalnew, sflux, scal_force, RhoH, 1);
+    }
+
+    // Maestro::VelocityAdvance (Source/MaestroVelocityAdvance.cpp:5-82) and UpdateVel
+    // (Source/MaestroAdvection.cpp:299-526, with its AverageDown + FillPatch): umac holds the
+    // projected MAC velocity without w0, its ghost faces filled; uold its ghost cells
+    void VelocityAdvance(VMF& uold, VMF& sold, VMF& rhohalf, VF& umac, VMF& w0_force_cart, VMF& unew, VF& uedge,
+                         VMF* sponge) {
+        VMF vel_force(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            vel_force[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+            for (int d = 0; d < 3; ++d) uedge[lev][d].define(S[lev].L.ba, 3, 0, d, 0.0);
+        }
+        MakeVelForce(vel_force, umac, sold, w0_force_cart);
+        Addw0(umac, 1.0);
+        MakeEdgeScal(uold, uedge, umac, vel_force, bcs_u(), 0, 0, 3, false, true);
+        Addw0(umac, -1.0);
+        BS rho0_nph(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Lev& L = S[lev];
+            rho0_nph[lev].resize(L.nr);
+            for (int r = 0; r < L.nr; ++r) rho0_nph[lev][r] = 0.5 * (L.rho0_old[r] + L.rho0_new[r]);
+        }
+        MakeVelForce(vel_force, umac, rhohalf, w0_force_cart, &rho0_nph);
+        for (int lev = 0; lev < nlev; ++lev)
+            S[lev].UpdateVel(uold[lev], unew[lev], umac[lev].data(), uedge[lev].data(), vel_force[lev],
+                             sponge ? &(*sponge)[lev] : nullptr);
+        AverageDown(unew, 0, 3);
+        FillPatch(unew, 0, 3, 0, bcs_u(), true);
     }
 };
 
@@ -1837,6 +1910,50 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
         if (o.sold_end) gather_cells(dom, sold[lev], 0, nscal, o.sold_end);
         if (o.etarhoflux) gather_faces(dom, etarhoflux[lev], 2, 0, 1, o.etarhoflux);
     }
+    return 0;
+}
+
+// AdvancePremac for the MAC velocity (the projection skipped; its ghost faces filled as
+// MacProj leaves them), then VelocityAdvance on the state's velocity.
+static int run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                                const double* rhohalf, const double* sponge, double* unew_out, double* const* uedge_out,
+                                double* const* umac_out) {
+    if (p->dim == 2) throw std::runtime_error("VelocityAdvance: 3-D");
+    Stage H;
+    setup_stage(H, p, 1, &nboxes, boxes, in);
+    Lev& S = H.S[0];
+    const Box& dom = S.L.dom;
+    const int nscal = H.nscal;
+    VMF w0_force_cart(1), uold(1), sold(1), vel_force(1), rh(1), unew(1), sp(1);
+    VF umac(1), utrans(1), uedge(1);
+    w0_force_cart[0].define(S.L.ba, 3, 1, -1, 0.0);
+    if (p->evolve_base_state)
+        H.Put1dArrayOnCart(H.bs(&Lev::w0_force), w0_force_cart, false, true, &H.bcs_f(), 0, false);
+    uold[0].define(S.L.ba, 3, H.ng_s, -1, 0.0);
+    sold[0].define(S.L.ba, nscal, H.ng_s, -1, 0.0);
+    S.gpi.define(S.L.ba, 3, 0, -1, 0.0);
+    S.thermal.define(S.L.ba, 1, 1, -1, 0.0);
+    scatter_cells(dom, in->uold, uold[0], 0, 3);
+    scatter_cells(dom, in->sold, sold[0], 0, nscal);
+    scatter_cells(dom, in->gpi, S.gpi, 0, 3);
+    for (int d = 0; d < 3; ++d) umac[0][d].define(S.L.ba, 1, 1, d, 0.0);
+    H.FillPatch(sold, 0, nscal, 0, H.bcs_s(), false, 0);
+    H.AdvancePremac(uold, sold, umac, w0_force_cart, utrans, vel_force);
+    H.SyncFaces(umac);
+    for (int d = 0; d < 3; ++d)
+        if (umac_out && umac_out[d]) gather_faces(dom, umac[0][d], d, 0, 1, umac_out[d]);
+    H.FillPatch(uold, 0, 3, 0, H.bcs_u(), true);
+    rh[0].define(S.L.ba, 1, 1, -1, 0.0);
+    scatter_cells(dom, rhohalf, rh[0], 0, 1);
+    if (sponge) {
+        sp[0].define(S.L.ba, 1, 0, -1, 0.0);
+        scatter_cells(dom, sponge, sp[0], 0, 1);
+    }
+    unew[0].define(S.L.ba, 3, H.ng_s, -1, 0.0);
+    H.VelocityAdvance(uold, sold, rh, umac, w0_force_cart, unew, uedge, sponge ? &sp : nullptr);
+    gather_cells(dom, unew[0], 0, 3, unew_out);
+    for (int d = 0; d < 3; ++d)
+        if (uedge_out && uedge_out[d]) gather_faces(dom, uedge[0][d], d, 0, 3, uedge_out[d]);
     return 0;
 }
 
@@ -2143,6 +2260,22 @@ int mo_run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const mo_i
 int mo_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
                  int nthreads) {
     return mo_run_stage_levels(p, 1, &nboxes, boxes, in, out, 1, nthreads);
+}
+
+int mo_run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                            const double* rhohalf, const double* sponge, double* unew, double* const* uedge,
+                            double* const* umac, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    try {
+        return mo::run_velocity_advance(p, nboxes, boxes, in, rhohalf, sponge, unew, uedge, umac);
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
 }
 
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge) {

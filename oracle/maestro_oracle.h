@@ -139,6 +139,18 @@ int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
 int mo_run_stage_tl(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, const double* duold,
                     const double* dsold, mo_outputs* out, double* dsnew, int nthreads);
 
+/* AdvancePremac for the MAC velocity (MAC projection skipped; its ghost faces filled by
+ * FillBoundary + FillUmacGhost as MacProj leaves them), then Maestro::VelocityAdvance
+ * (Source/MaestroVelocityAdvance.cpp:5-82) with UpdateVel (Source/MaestroAdvection.cpp:
+ * 299-526) on one 3-D level: uold gets its ghost cells by FillPatch with bcs_u.  rhohalf
+ * [ncell] is the half-time density of the second MakeVelForce (with rho0_nph = (rho0_old +
+ * rho0_new) / 2 and grav_cell); sponge [ncell] may be NULL (do_sponge = 0).  Writes unew
+ * [3][ncell], uedge[d] [3][faces_d] (may be NULL) and the MAC velocity VelocityAdvance was
+ * given, umac[d] (may be NULL). */
+int mo_run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                            const double* rhohalf, const double* sponge, double* unew, double* const* uedge,
+                            double* const* umac, int nthreads);
+
 /* 1-D CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), single level. */
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge);
 

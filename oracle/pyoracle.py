@@ -354,3 +354,37 @@ def steps_tl(cfg, s0, ds0, u, du, nsteps, nthreads=0):
         s[comps] = snew[comps]
         ds[comps] = dsnew[comps]
     return s, ds
+
+
+def run_velocity_advance(cfg, rhohalf, sponge=None, nthreads=0, checked=False):
+    """AdvancePremac (MAC projection skipped) then VelocityAdvance + UpdateVel on the CPU:
+    returns dict(unew [3, nz, ny, nx], uedge [3 arrays 3 x faces], umac [3 face arrays])."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    n = cfg["n"]
+    keep = []
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    inp = MoInputs()
+    for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                 "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+        setattr(inp, name, arr(cfg[name]))
+    fshape = [(n[2], n[1], n[0] + 1), (n[2], n[1] + 1, n[0]), (n[2] + 1, n[1], n[0])]
+    unew = np.full((3, n[2], n[1], n[0]), np.nan)
+    uedge = [np.full((3,) + fshape[d], np.nan) for d in range(3)]
+    umac = [np.full(fshape[d], np.nan) for d in range(3)]
+    ue = (C.POINTER(C.c_double) * 3)(*[_p(a) for a in uedge])
+    um = (C.POINTER(C.c_double) * 3)(*[_p(a) for a in umac])
+    boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    L = lib(checked)
+    L.mo_run_velocity_advance.restype = C.c_int
+    rc = L.mo_run_velocity_advance(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
+                                   C.byref(inp), arr(rhohalf), arr(sponge) if sponge is not None else None,
+                                   _p(unew), ue, um, nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.mo_last_error().decode())
+    return dict(unew=unew, uedge=uedge, umac=umac)

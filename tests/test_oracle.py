@@ -269,3 +269,23 @@ def test_tangent_linear_build_matches_finite_differences():
         checked += 1
     assert checked >= 5
     assert worst <= 1e-6, worst
+
+
+@pytest.mark.parametrize("ppm_type", [1, 2])
+def test_velocity_advance_keeps_uniform_flow(ppm_type):
+    """pyoracle.run_velocity_advance (VelocityAdvance + UpdateVel): in a periodic domain with
+    no gravity, pressure gradient or w0, a uniform velocity stays uniform and the velocity
+    edge states equal it; with a sponge factor s the new velocity is s times the old."""
+    cfg = configs.planar_config(n=(16, 16, 16), max_grid=8, ppm_type=ppm_type, bc_lo=(INTERIOR,) * 3,
+                                bc_hi=(INTERIOR,) * 3, w0_amp=0.0, gpi_amp=0.0, rho_pert=0.0)
+    cfg["grav_cell"] = np.zeros_like(cfg["grav_cell"])
+    u0 = np.array([3.0e5, -2.0e5, 1.5e5])
+    cfg["uold"] = np.broadcast_to(u0[:, None, None, None], cfg["uold"].shape).copy()
+    rhohalf = cfg["sold"][RHO]
+    r = pyoracle.run_velocity_advance(cfg, rhohalf, checked=True)
+    for d in range(3):
+        assert np.allclose(r["unew"][d], u0[d], rtol=1e-13, atol=0)
+        assert np.allclose(r["uedge"][d][d], u0[d], rtol=1e-13, atol=0)
+    sp = np.full(rhohalf.shape, 0.5)
+    r2 = pyoracle.run_velocity_advance(cfg, rhohalf, sponge=sp)
+    assert np.array_equal(r2["unew"], 0.5 * r["unew"])
