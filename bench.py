@@ -486,6 +486,52 @@ def run_spherical(args, barrier):
             "identical_results_graph_vs_per_box": bool(same)}
 
 
+def run_velocity(args, barrier):
+    """VelocityAdvance + UpdateVel on the bench workload (256^3 in 64 boxes of 64^3, w0 != 0):
+    the MAC velocity from AdvancePremac, then madv_velocity_advance timed with CUDA events
+    (one launch sequence over all boxes per call; inputs are not modified by the call)."""
+    import torch
+    from maestroex_gb300 import configs
+    from maestroex_gb300.params import RHO
+    from maestroex_gb300.stage import MultiFab, StageBuffers, make_stage
+    cfg = configs.planar_config(n=(args.n,) * 3, nspec=args.nspec, ppm_type=1, max_grid=args.box,
+                                seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
+    st = make_stage(cfg)
+    buf = StageBuffers(cfg).load(cfg)
+    boxes = cfg["boxes"]
+    umac = [MultiFab(boxes, 1, 1, nodal=d) for d in range(3)]
+    st.advance_premac(buf.uold, buf.sold, buf.gpi, umac)
+    rh = MultiFab(boxes, 1, 0)
+    for t, s in zip(rh.fabs, buf.sold.fabs):
+        g = buf.sold.ng
+        t.copy_(s[RHO:RHO + 1, g:-g, g:-g, g:-g])
+    unew = MultiFab(boxes, 3, buf.sold.ng)
+    uedge = [MultiFab(boxes, 3, 0, nodal=d) for d in range(3)]
+
+    def call():
+        st.velocity_advance(buf.uold, buf.sold, rh, buf.gpi, umac, unew, uedge)
+
+    for _ in range(3):
+        call()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, args.steps)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    launches = st.launch_count()
+    st.close()
+    ncell = args.n ** 3
+    return {"workload": f"VelocityAdvance + UpdateVel, {args.n}^3 in boxes of {args.box}^3, ppm_type 1, w0 != 0, "
+                        "x/y periodic, z slipwall / outflow (velocity edge states with the outflow clamp)",
+            "value": ncell / (ms * 1e-3), "unit": UNIT, "ms_per_call": ms, "gpu_launches": launches,
+            "mode": "batched launches (one per kernel over all boxes)"}
+
+
 def run_2d(args, barrier):
     """2-D workload: one 256 x 256 box, NumSpec 3, ppm_type 1 (the reference's 2-D build),
     graph-replayed stage."""
@@ -559,6 +605,7 @@ def main():
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one adjoint call (state and velocity gradients) and exit (the command ncu captures)")
     ap.add_argument("--no-2d", action="store_true")
+    ap.add_argument("--no-velocity", action="store_true")
     ap.add_argument("--sph-n", type=int, default=256, help="extent of the spherical workload")
     ap.add_argument("--no-spherical", action="store_true")
     ap.add_argument("--profile-once", action="store_true",
@@ -727,6 +774,7 @@ def main():
         amr = run_amr(args, ws, max(1, args.steps // 2), warmup, barrier)
     adj = None if args.no_adjoint else run_adjoint(args, barrier)
     two_d = None if args.no_2d else run_2d(args, barrier)
+    vel = None if args.no_velocity else run_velocity(args, barrier)
     sph = None if args.no_spherical else run_spherical(args, barrier)
 
     if rank != 0:
@@ -775,6 +823,8 @@ def main():
         line["adjoint"] = adj
     if two_d is not None:
         line["two_d"] = two_d
+    if vel is not None:
+        line["velocity_advance"] = vel
     if sph is not None:
         line["spherical"] = sph
     if not args.no_cpu_baseline:

@@ -233,16 +233,17 @@ __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp,
     const FabView s = VW(fs), F = VW(F_FACE0 + D);
     const double s0 = at(s, i, j, k, sc);
     double sm = at(F, i, j, k), sp = at(F, i + di, j + dj, k + dk);
-    int cs = 3;
-    if ((sp - s0) * (s0 - sm) <= 0.0) {
+    int cs = 3;  // the forward limiter's case, decided as k_ppm_cell decides it
+    const double a = sp - s0, q = s0 - sm;
+    if (!prod_gt0(a, q)) {
         sp = s0;
         sm = s0;
         cs = 0;
-    } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
-        sp = 3.0 * s0 - 2.0 * sm;
+    } else if ((dbits(a) & ABS_MASK) >= (dbits(twice(q)) & ABS_MASK)) {
+        sp = 3.0 * s0 - twice(sm);
         cs = 1;
-    } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
-        sm = 3.0 * s0 - 2.0 * sp;
+    } else if ((dbits(q) & ABS_MASK) >= (dbits(twice(a)) & ABS_MASK)) {
+        sm = 3.0 * s0 - twice(sp);
         cs = 2;
     }
     double up, um, Ap, Bp, Am, Bm;
@@ -261,22 +262,28 @@ __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp,
         Bp = Bm = at(T, i, j, k, 2 * D + 1);
     }
     const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
+    const double dpm = sp - sm;
     double bs0 = 0.0, bsm = 0.0, bsp = 0.0, gup = 0.0, gum = 0.0;
+    // ip = sp - A (sp - sm - B s6): d/dsp = 1 - A - 3AB, d/dsm = A - 3AB, d/ds0 = 6AB, with
+    // t = A ipb and w = 3AB ipb (the adjoint is not held to the forward's rounding)
     if (gt_t(up, epsb)) {
-        bsp += (1.0 - Ap - 3.0 * Ap * Bp) * ipb;
-        bsm += (Ap - 3.0 * Ap * Bp) * ipb;
-        bs0 += 6.0 * Ap * Bp * ipb;
-        // d ip/dA = -(sp - sm - B s6), d ip/dB = A s6
-        gup = copysign(dtdx, up) * (-0.5 * (sp - sm - Bp * s6) - (2.0 / 3.0) * Ap * s6) * ipb;
+        const double t = Ap * ipb, w = 3.0 * (Bp * t);
+        bsp += (ipb - t) - w;
+        bsm += t - w;
+        bs0 += twice(w);
+        // d ip/dA = -(sp - sm - B s6), d ip/dB = A s6; dA/du = sign(u) dt/dx / 2, dB/du = -(2/3) sign(u) dt/dx
+        if (want_u) gup = copysign(dtdx, up) * ipb * (half(Bp * s6 - dpm) - (2.0 / 3.0) * Ap * s6);
     } else {
         bs0 += ipb;
     }
+    // im = sm + A (sp - sm + B s6): d/dsm = 1 - A - 3AB, d/dsp = A - 3AB, d/ds0 = 6AB
     if (lt_negt(um, epsb)) {
-        bsm += (1.0 - Am - 3.0 * Am * Bm) * imb;
-        bsp += (Am - 3.0 * Am * Bm) * imb;
-        bs0 += 6.0 * Am * Bm * imb;
+        const double t = Am * imb, w = 3.0 * (Bm * t);
+        bsm += (imb - t) - w;
+        bsp += t - w;
+        bs0 += twice(w);
         // d im/dA = sp - sm + B s6, d im/dB = A s6
-        gum = copysign(dtdx, um) * (0.5 * (sp - sm + Bm * s6) - (2.0 / 3.0) * Am * s6) * imb;
+        if (want_u) gum = copysign(dtdx, um) * imb * (half(dpm + Bm * s6) - (2.0 / 3.0) * Am * s6);
     } else {
         bs0 += imb;
     }
@@ -319,7 +326,7 @@ __global__ void k_adj_ppm_face(KARGS, int fs, int sc, int ts, int tcomp, RecipC 
     if (fb == 0.0) return;
     const FabView s = VW(fs), dv = VW(F_DSVL), as = AW(ts);
     const double sl = at(s, i - di, j - dj, k - dk, sc), s0 = at(s, i, j, k, sc);
-    const double v0 = 0.5 * (s0 + sl) - div_c(at(dv, i, j, k) - at(dv, i - di, j - dj, k - dk), r6);
+    const double v0 = half(s0 + sl) - div_c(at(dv, i, j, k) - at(dv, i - di, j - dj, k - dk), r6);
     // mn(a, b) = (b < a) ? b : a and mx(a, b) = (a < b) ? b : a, as in the forward
     const double lo = mn(s0, sl), hi = mx(s0, sl);
     int src = 0;  // 0: v0, 1: s0, 2: s-1
@@ -333,8 +340,9 @@ __global__ void k_adj_ppm_face(KARGS, int fs, int sc, int ts, int tcomp, RecipC 
         atomicAdd(&at(as, i, j, k, tcomp), 0.5 * fb);
         atomicAdd(&at(as, i - di, j - dj, k - dk, tcomp), 0.5 * fb);
         const FabView ad = AW(A_ADSVL);
-        atomicAdd(&at(ad, i, j, k), -fb / 6.0);
-        atomicAdd(&at(ad, i - di, j - dj, k - dk), fb / 6.0);
+        const double f6 = div_c(fb, r6);
+        atomicAdd(&at(ad, i, j, k), -f6);
+        atomicAdd(&at(ad, i - di, j - dj, k - dk), f6);
     } else if (src == 1) {
         atomicAdd(&at(as, i, j, k, tcomp), fb);
     } else {
@@ -352,28 +360,29 @@ __global__ void k_adj_dsvl(KARGS, int fs, int sc, int ts, int tcomp) {
     if (g == 0.0) return;
     const FabView s = VW(fs), as = AW(ts);
     auto S = SHIFT_S(s, sc);
-    const double dsc = 0.5 * (S(1) - S(-1));
-    const double dsl = 2.0 * (S(0) - S(-1));
-    const double dsr = 2.0 * (S(1) - S(0));
-    if (!(dsl * dsr > 0.0)) return;
-    const double ac = fabs(dsc), al = fabs(dsl), ar = fabs(dsr);
+    // the forward's decisions, taken as k_dsvl takes them (bit-pattern scaling, product sign,
+    // minimum of the magnitudes' bit patterns)
+    const double dsc = half(S(1) - S(-1));
+    const double dsl = twice(S(0) - S(-1));
+    const double dsr = twice(S(1) - S(0));
+    if (!prod_gt0(dsl, dsr)) return;
+    const long long ac = dbits(dsc) & ABS_MASK, al = dbits(dsl) & ABS_MASK, ar = dbits(dsr) & ABS_MASK;
     const bool inner_r = ar < al;  // mn(|dsl|, |dsr|)
-    const double inner = inner_r ? ar : al;
+    const long long inner = inner_r ? ar : al;
     auto add = [&](int m, double v) { atomicAdd(&at(as, i + m * di, j + m * dj, k + m * dk, tcomp), v); };
-    if (inner < ac) {  // dv = sign(dsc) |dsl| or sign(dsc) |dsr|
-        const double sg = copysign(1.0, dsc);
+    if (inner < ac) {  // dv = sign(dsc) |dsl| or sign(dsc) |dsr|: weight +-2 g
+        const long long sg = (dbits(dsc) ^ dbits(inner_r ? dsr : dsl)) & SIGN_BIT;
+        const double w = __longlong_as_double(dbits(twice(g)) ^ sg);
         if (inner_r) {
-            const double w = 2.0 * sg * copysign(1.0, dsr) * g;
             add(1, w);
             add(0, -w);
         } else {
-            const double w = 2.0 * sg * copysign(1.0, dsl) * g;
             add(0, w);
             add(-1, -w);
         }
     } else {  // dv = dsc
-        add(1, 0.5 * g);
-        add(-1, -0.5 * g);
+        add(1, half(g));
+        add(-1, -half(g));
     }
 }
 
@@ -413,8 +422,9 @@ __global__ void k_adj_x(KARGS, int comp) {
     const FabView ao = AW(A_ASOLD);
     const double rho = at(AW(A_WSOLD), i, j, k, RHO);
     const double x = at(VW(F_SOLD), i, j, k, comp);
-    at(ao, i, j, k, comp) += a / rho;
-    at(ao, i, j, k, RHO) -= a * x / rho;
+    const double ar = a / rho;  // d(rhoX / rho): one division for both partials
+    at(ao, i, j, k, comp) += ar;
+    at(ao, i, j, k, RHO) -= ar * x;
 }
 
 // PutInPertForm transposed (s' = s - s0) together with the traced force of
