@@ -216,6 +216,34 @@ int madv_velocity_advance(madv_ctx* ctx, const madv_multifab* uold, const madv_m
                           const madv_multifab* umac, const madv_multifab* sponge,
                           const madv_multifab* unew, const madv_multifab* uedge, void* stream);
 
+/* Runtime parameters of EstDt (Source/param/_cpp_parameters: cfl, drdxfac, max_dt,
+ * fixed_dt, small_dt). */
+typedef struct {
+    double cfl;      /* 0.5 by default */
+    int drdxfac;     /* spherical radial spacing = finest dx / drdxfac (1 by default) */
+    double max_dt;   /* 1e33 */
+    double fixed_dt; /* -1: not fixed */
+    double small_dt; /* 1e-10: a smaller estimate is an error, as the reference aborts */
+} madv_dt_params;
+
+typedef struct {
+    double dt;          /* after the max_dt / fixed_dt limits */
+    double dt_estimate; /* before them */
+    double umax;        /* the largest speed; rel_eps = 1e-8 umax */
+    double rel_eps;
+} madv_dt_result;
+
+/* Maestro::EstDt (Source/Maestro.H:530, Source/MaestroDt.cpp:11-225 planar, :301-384 spherical,
+ * :440-483), 3-D, over nlev levels: dt = cfl min(dx / max|u_d|, dr / max|w0|) (the radial speed
+ * with the cell-centred w0), limited by sqrt(2 dx / max|f_d|) with vel_force from
+ * MakeVelForce at zero MAC velocity and w0_force; rel_eps = 1e-8 umax.  uold, gpi: ndim comps,
+ * sold: Rho, valid regions read.  Bit for bit the reference's values.  The divU and dS/dt
+ * constraints of EstDt (:226-300) need S_cc, dSdt and gamma1bar from the reactions / EOS
+ * part of the step and are left to the caller (min with this dt). */
+int madv_est_dt(madv_ctx* ctx, int nlev, const madv_multifab* uold, const madv_multifab* sold,
+                const madv_multifab* gpi, const madv_dt_params* params, madv_dt_result* result,
+                void* stream);
+
 /* Maestro::UpdateScal (Source/Maestro.H:306, Source/MaestroAdvection.cpp:86-297) for RhoH
  * (start_comp 1, num_comp 1) or the species (FirstSpec, NumSpec; Rho follows).  stateold,
  * force: valid region; statenew: the updated components on the valid region and, where

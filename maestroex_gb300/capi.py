@@ -29,8 +29,17 @@ EXPORTED = [
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
     "madv_autotune_trial", "madv_autotune_finish", "madv_autotune_apply",
     "madv_make_utrans", "madv_vel_pred", "madv_make_edge_scal", "madv_make_rhox_flux", "madv_make_rhoh_flux",
-    "madv_update_scal", "madv_velocity_advance",
+    "madv_update_scal", "madv_velocity_advance", "madv_est_dt",
 ]
+
+
+class MadvDtParams(C.Structure):
+    _fields_ = [("cfl", C.c_double), ("drdxfac", C.c_int), ("max_dt", C.c_double), ("fixed_dt", C.c_double),
+                ("small_dt", C.c_double)]
+
+
+class MadvDtResult(C.Structure):
+    _fields_ = [("dt", C.c_double), ("dt_estimate", C.c_double), ("umax", C.c_double), ("rel_eps", C.c_double)]
 
 
 class MadvBox(C.Structure):
@@ -98,6 +107,7 @@ def lib():
         L.madv_make_rhoh_flux.argtypes = [C.c_void_p, I, MF, MF, MF, C.c_void_p]
         L.madv_update_scal.argtypes = [C.c_void_p, MF, MF, MF, MF, I, I, C.c_void_p]
         L.madv_velocity_advance.argtypes = [C.c_void_p, MF, MF, MF, MF, MF, MF, MF, MF, C.c_void_p]
+        L.madv_est_dt.argtypes = [C.c_void_p, I, MF, MF, MF, P(MadvDtParams), P(MadvDtResult), C.c_void_p]
         L.madv_stage_forward.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                          C.c_void_p]
         L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,

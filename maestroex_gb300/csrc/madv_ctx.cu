@@ -915,6 +915,8 @@ static void destroy_level(Ctx& c) {
     if (c.d_bcs) cudaFree(c.d_bcs);
     c.d_bcs = nullptr;
     if (c.d_flag) cudaFree(c.d_flag);
+    if (c.d_red) cudaFree(c.d_red);
+    c.d_red = nullptr;
     c.d_flag = nullptr;
 }
 
@@ -1875,6 +1877,99 @@ int madv_velocity_advance(madv_ctx* h, const madv_multifab* uold, const madv_mul
         if (uedge)
             for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UEDGE0 + d, 0, F_SEDGE0 + d, 0, 3, 0);
         return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+// Maestro::EstDt (Source/MaestroDt.cpp:11-225 planar, :301-384 spherical, :440-483): the
+// advective and force constraints and rel_eps on every level.  The per-level maxima are exact
+// (k_dt_maxima), and the reference's per-box minima of monotone functions of per-box maxima
+// equal the same functions of the level maxima, so dt and umax match it bit for bit.
+int madv_est_dt(madv_ctx* h, int nlev, const madv_multifab* uold, const madv_multifab* sold,
+                const madv_multifab* gpi, const madv_dt_params* prm, madv_dt_result* res, void* stream) {
+    if (!h || !uold || !sold || !gpi || !prm || !res) return MADV_ERR_PARAM;
+    Hier H = h->H();
+    if (nlev != H.n()) {
+        set_error("the call passes " + std::to_string(nlev) + " levels, the layout has " + std::to_string(H.n()));
+        return MADV_ERR_PARAM;
+    }
+    int rc = check_ready_h(H);
+    if (rc) return rc;
+    if (!(prm->cfl > 0.0) || prm->drdxfac < 1) {
+        set_error("EstDt: cfl > 0 and drdxfac >= 1");
+        return MADV_ERR_PARAM;
+    }
+    if (H[0].ndim != 3) {
+        set_error("EstDt: 3-D");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    set_mode(H, (cudaStream_t)stream, 0, false);
+    reset_launches(H);
+    try {
+        const int nd = H[0].ndim;
+        for (int l = 0; l < nlev; ++l) {
+            Ctx& c = H[l];
+            if ((rc = bind(c, U_UOLD, &uold[l], nd, -1, 0)) || (rc = bind(c, U_SOLD, &sold[l], 1, -1, 0)) ||
+                (rc = bind(c, U_GPI, &gpi[l], nd, -1, 0)) || (rc = upload_user_views(c)))
+                return rc;
+            if (!c.d_red && !cuda_ok(cudaMalloc(&c.d_red, 7 * sizeof(unsigned long long)), "cudaMalloc(EstDt)"))
+                return MADV_ERR_CUDA;
+            cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream);
+            set_val(c, F_UTILDE, 0.0, 0, 3, 0);
+            copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, nd, 0);
+            copy_fab(c, F_SOLD, RHO, F_USER + U_SOLD, RHO, 1, 0);
+            set_val(c, F_GPI, 0.0, 0, 3, 0);
+            copy_fab(c, F_GPI, 0, F_USER + U_GPI, 0, nd, 0);
+            for (int d = 0; d < 3; ++d) set_val(c, F_UTRANS0 + d, 0.0, 0, 1, 1);  // umac_dummy (:24-37)
+        }
+        w0_carts(H);
+        // MakeVelForce(vel_force, umac_dummy, sold, rho0_old, grav_cell_old, w0_force_cart_dummy, 0)
+        for (auto* c : H.L) set_val(*c, F_W0FCART, 0.0, 0, 3, 1);
+        make_vel_force_h(H);
+        std::vector<std::array<unsigned long long, 7>> mx(nlev);
+        for (int l = 0; l < nlev; ++l) {
+            Ctx& c = H[l];
+            CK(cudaMemsetAsync(c.d_red, 0, 7 * sizeof(unsigned long long), c.stream));
+            dt_maxima(c);
+            CK(cudaMemcpyAsync(mx[l].data(), c.d_red, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               c.stream));
+        }
+        if ((rc = finish(H))) return rc;
+        auto val = [](unsigned long long b) {
+            double v;
+            std::memcpy(&v, &b, sizeof(v));
+            return v;
+        };
+        const double eps = 1.e-8;
+        double dt = 1.e20, umax = 0.0;
+        for (int l = 0; l < nlev; ++l) {
+            const Ctx& c = H[l];
+            const double spd[3] = {val(mx[l][0]), val(mx[l][1]), val(mx[l][2])}, spdr = val(mx[l][3]);
+            const double f[3] = {val(mx[l][4]), val(mx[l][5]), val(mx[l][6])};
+            double dt_temp = 1.e99;
+            umax = std::max(umax, std::max(spd[0], std::max(spd[1], std::max(spd[2], spdr))));
+            for (int d = 0; d < nd; ++d)
+                if (spd[d] > eps) dt_temp = std::min(dt_temp, c.P.dx[d] / spd[d]);
+            // radial spacing: dx of the radial direction, or base_geom.dr(0) = finest dx / drdxfac
+            const double dr = c.sph ? c.geo.dxf / prm->drdxfac : c.P.dx[nd - 1];
+            if (spdr > eps) dt_temp = std::min(dt_temp, dr / spdr);
+            dt_temp *= prm->cfl;
+            for (int d = 0; d < nd; ++d)
+                if (f[d] > eps) dt_temp = std::min(dt_temp, std::sqrt(2.0 * c.P.dx[d] / f[d]));
+            dt = std::min(dt, std::min(1.e50, dt_temp));
+        }
+        res->dt_estimate = dt;
+        if (dt < prm->small_dt) {
+            set_error("EstDt: dt < small_dt");
+            return MADV_ERR_PARAM;
+        }
+        if (dt > prm->max_dt) dt = prm->max_dt;
+        if (prm->fixed_dt != -1.0) dt = prm->fixed_dt;
+        res->dt = dt;
+        res->umax = umax;
+        res->rel_eps = umax * 1.e-8;
+        return MADV_OK;
     } catch (const Fail& f) {
         return f.code;
     }

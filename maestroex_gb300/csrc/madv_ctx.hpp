@@ -148,6 +148,7 @@ struct Ctx {
     int tpb_trial = 0;
     int tpb_of(const void* fn);
     int* d_flag = nullptr;  // device error flag (EOS cutoff)
+    unsigned long long* d_red = nullptr;  // EstDt maxima (allocated on first use)
     // graph mode
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<const void*> graph_key;
@@ -221,6 +222,8 @@ int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int
                 const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
 void update_vel(Ctx& c, int fu, int fsponge);  // UpdateVel into F_SNEW comps 0-2; fsponge -1: no sponge
+// EstDt maxima of a level into c.d_red[0..6] (spdx, spdy, spdz, spdr, fx, fy, fz as bit patterns)
+void dt_maxima(Ctx& c);
 
 // ---- spherical forms (madv_sphr.cu), reached through the wrappers above when c.sph
 void put1d_sph(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec);

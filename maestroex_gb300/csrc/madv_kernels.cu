@@ -1400,6 +1400,46 @@ void update_vel(Ctx& c, int fu, int fsponge) {
            make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
 }
 
+// EstDt (Source/MaestroDt.cpp:128-225 planar, :301-384 spherical): maxima over a level's
+// valid cells of |u| per direction (the radial one with the cell-centred w0 added; the
+// spherical w0mac of EstDt is zero with the exact base state), of |w0_cart| (radial
+// component; component 0 in spherical geometry, as the reference reads it) and of
+// |vel_force| per direction.  The magnitudes' bit patterns order like their values, so the
+// maxima are exact: warp maxima by shuffles, then one atomicMax per warp and quantity.
+__global__ void k_dt_maxima(KARGS, int sph, int nd, unsigned long long* out) {
+    const long gid = g0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long m[7] = {0ULL, 0ULL, 0ULL, 0ULL, 0ULL, 0ULL, 0ULL};
+    if (gid < g1) {
+        const int e = find_box(R, ne, gid);
+        const int b = R[e].b;
+        int i, j, k;
+        region_ijk(R[e], gid - R[e].start, i, j, k);
+        const FabView u = VW(F_UTILDE), w0c = VW(F_W0CART), f = VW(F_VELFORCE);
+        for (int d = 0; d < nd; ++d) {
+            double v = at(u, i, j, k, d);
+            if (!sph && d == nd - 1) v = v + 0.5 * (at(w0c, i, j, k, d) + at(w0c, i, j + (d == 1), k + (d == 2), d));
+            m[d] = (unsigned long long)(dbits(v) & ABS_MASK);
+            m[4 + d] = (unsigned long long)(dbits(at(f, i, j, k, d)) & ABS_MASK);
+        }
+        m[3] = (unsigned long long)(dbits(at(w0c, i, j, k, sph ? 0 : nd - 1)) & ABS_MASK);
+    }
+    for (int q = 0; q < 7; ++q) {
+        unsigned long long v = m[q];
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+            v = o > v ? o : v;
+        }
+        m[q] = v;
+    }
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 7; ++q)
+            if (m[q]) atomicMax(out + q, m[q]);
+}
+
+void dt_maxima(Ctx& c) {
+    launch(c, rg_grow(c, 0), 1, k_dt_maxima, c.V(), (int)c.sph, c.ndim, c.d_red);
+}
+
 void update_scal(Ctx& c, int start_comp) {
     if (c.ndim == 2) return update_scal_2d(c, start_comp);
     const RegionTable& rt = rg_grow(c, 0);

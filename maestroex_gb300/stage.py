@@ -253,6 +253,21 @@ class ScalarAdvectionStage:
         check(lib().madv_update_scal(self.ctx, _ref(stateold), _ref(statenew), _ref3(sflux), _ref(force),
                                      start_comp, num_comp, C.c_void_p(s)))
 
+    def est_dt(self, uold, sold, gpi, cfl=0.5, drdxfac=1, max_dt=1.0e33, fixed_dt=-1.0, small_dt=1.0e-10,
+               stream=None):
+        """Maestro::EstDt (advective and force constraints): returns (dt, dt_estimate, umax,
+        rel_eps).  uold / sold / gpi: one MultiFab, or a list with one per level."""
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        lv = [uold, sold, gpi]
+        if not isinstance(uold, (list, tuple)):
+            lv = [[uold], [sold], [gpi]]
+        nl = len(lv[0])
+        arrs = [(capi.MadvMultiFab * nl)(*[m.desc() for m in mfs]) for mfs in lv]
+        prm = capi.MadvDtParams(cfl, drdxfac, max_dt, fixed_dt, small_dt)
+        res = capi.MadvDtResult()
+        check(lib().madv_est_dt(self.ctx, nl, arrs[0], arrs[1], arrs[2], C.byref(prm), C.byref(res), C.c_void_p(s)))
+        return res.dt, res.dt_estimate, res.umax, res.rel_eps
+
     def velocity_advance(self, uold, sold, rhohalf, gpi, umac, unew, uedge=None, sponge=None, stream=None):
         """Maestro::VelocityAdvance + UpdateVel (3-D, one level): unew (and the velocity edge
         states uedge) from uold, the projected MAC velocity umac (without w0) and rhohalf."""

@@ -1682,6 +1682,60 @@ struct Stage {
         AverageDown(unew, 0, 3);
         FillPatch(unew, 0, 3, 0, bcs_u(), true);
     }
+
+    // Maestro::EstDt (Source/MaestroDt.cpp:11-225 planar, :301-384 spherical; the divU and
+    // dS/dt constraints :226-300, :385-438 are not restated: they need S_cc, dSdt and
+    // gamma1bar from the reactions / EOS part of the step), evaluated box by box as the
+    // reference does.  vel_force: MakeVelForce with a zero MAC velocity and w0_force
+    // (:14-81); the spherical w0mac is zero with the exact base state (:44-64).  Returns dt
+    // before the max_dt / fixed_dt / small_dt clamps; umax before the 1e-8 of rel_eps.
+    void EstDt(VMF& uold, VMF& sold, double cfl, int drdxfac, double& dt, double& umax) {
+        VMF vel_force(nlev), w0f(nlev);
+        VF umac0(nlev);
+        for (int lev = 0; lev < nlev; ++lev) {
+            vel_force[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+            w0f[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+            for (int d = 0; d < 3; ++d) umac0[lev][d].define(S[lev].L.ba, 1, 1, d, 0.0);
+        }
+        MakeVelForce(vel_force, umac0, sold, w0f);
+        dt = 1.e20;
+        umax = 0.0;
+        const int nd = P.dim == 2 ? 2 : 3;
+        for (int lev = 0; lev < nlev; ++lev) {
+            const Lev& L = S[lev];
+            const double* dx = L.L.dx;
+            double dt_lev = 1.e50, umax_lev = 0.0;
+            for (int b = 0; b < L.nb; ++b) {
+                const Arr &u = uold[lev][b], &w0c = L.w0_cart[b], &f = vel_force[lev][b];
+                double spd[3] = {0.0, 0.0, 0.0}, spdr = 0.0, fm[3] = {0.0, 0.0, 0.0};
+                MO_FOR3(L.L.ba[b]) {
+                    for (int d = 0; d < nd; ++d) {
+                        real v = u(i, j, k, d);
+                        if (!P.spherical && d == nd - 1)
+                            v = u(i, j, k, d) + 0.5 * (w0c(i, j, k, d) + w0c(i, j + (d == 1), k + (d == 2), d));
+                        if (P.spherical) v = u(i, j, k, d) + 0.5 * (0.0 + 0.0);  // w0mac = 0
+                        spd[d] = std::max(spd[d], std::fabs(value_of(v)));
+                        fm[d] = std::max(fm[d], std::fabs(value_of(f(i, j, k, d))));
+                    }
+                    spdr = std::max(spdr, std::fabs(value_of(w0c(i, j, k, P.spherical ? 0 : nd - 1))));
+                }
+                const double eps = 1.e-8;
+                double dt_temp = 1.e99;
+                const double umax_grid = std::max(spd[0], std::max(spd[1], std::max(spd[2], spdr)));
+                for (int d = 0; d < nd; ++d)
+                    if (spd[d] > eps) dt_temp = std::min(dt_temp, dx[d] / spd[d]);
+                const double dr = P.spherical ? (L.dxf / drdxfac) : dx[nd - 1];
+                if (spdr > eps) dt_temp = std::min(dt_temp, dr / spdr);
+                dt_temp *= cfl;
+                for (int d = 0; d < nd; ++d)
+                    if (fm[d] > eps) dt_temp = std::min(dt_temp, std::sqrt(2.0 * dx[d] / fm[d]));
+                dt_lev = std::min(dt_lev, dt_temp);
+                umax_lev = std::max(umax_lev, umax_grid);
+            }
+            umax = std::max(umax, umax_lev);
+            dt = std::min(dt, dt_lev);
+        }
+    }
 };
 
 }  // namespace mo
@@ -1954,6 +2008,26 @@ static int run_velocity_advance(const mo_params* p, int nboxes, const int* boxes
     gather_cells(dom, unew[0], 0, 3, unew_out);
     for (int d = 0; d < 3; ++d)
         if (uedge_out && uedge_out[d]) gather_faces(dom, uedge[0][d], d, 0, 3, uedge_out[d]);
+    return 0;
+}
+
+static int est_dt(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in, double cfl,
+                  int drdxfac, double* dt, double* umax) {
+    if (p->dim == 2) throw std::runtime_error("EstDt: 3-D");
+    Stage H;
+    setup_stage(H, p, nlev, nboxes, boxes, in);
+    VMF uold(nlev), sold(nlev);
+    for (int lev = 0; lev < nlev; ++lev) {
+        Lev& S = H.S[lev];
+        const Box& dom = S.L.dom;
+        uold[lev].define(S.L.ba, 3, 0, -1, 0.0);
+        sold[lev].define(S.L.ba, H.nscal, 1, -1, 0.0);
+        S.gpi.define(S.L.ba, 3, 0, -1, 0.0);
+        scatter_cells(dom, in[lev].uold, uold[lev], 0, p->dim == 2 ? 2 : 3);
+        scatter_cells(dom, in[lev].sold, sold[lev], 0, H.nscal);
+        scatter_cells(dom, in[lev].gpi, S.gpi, 0, p->dim == 2 ? 2 : 3);
+    }
+    H.EstDt(uold, sold, cfl, drdxfac, *dt, *umax);
     return 0;
 }
 
@@ -2272,6 +2346,16 @@ int mo_run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, co
 #endif
     try {
         return mo::run_velocity_advance(p, nboxes, boxes, in, rhohalf, sponge, unew, uedge, umac);
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+
+int mo_est_dt(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in, double cfl,
+              int drdxfac, double* dt, double* umax) {
+    try {
+        return mo::est_dt(p, nlev, nboxes, boxes, in, cfl, drdxfac, dt, umax);
     } catch (const std::exception& e) {
         mo::g_err = e.what();
         return -1;

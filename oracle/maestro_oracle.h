@@ -151,6 +151,15 @@ int mo_run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, co
                             const double* rhohalf, const double* sponge, double* unew, double* const* uedge,
                             double* const* umac, int nthreads);
 
+/* Maestro::EstDt (Source/MaestroDt.cpp:11-225, spherical :301-384) on an nlev hierarchy
+ * laid out as for mo_run_stage_levels: the advective (|u|, with the cell-centred w0 on the
+ * radial direction, and |w0|) and force (MakeVelForce with zero MAC velocity and w0_force)
+ * constraints, cfl and drdxfac (spherical dr = finest dx / drdxfac) as the runtime
+ * parameters.  dt: before max_dt / fixed_dt / small_dt; umax: rel_eps = 1e-8 umax.  The
+ * divU and dS/dt constraints are not included. */
+int mo_est_dt(const mo_params* p, int nlev, const int* nboxes, const int* boxes, const mo_inputs* in, double cfl,
+              int drdxfac, double* dt, double* umax);
+
 /* 1-D CelltoEdge (Source/MaestroCelltoEdge.cpp:5-55), single level. */
 int mo_cell_to_edge(const double* s0_cell, int nr, double* s0_edge);
 

@@ -388,3 +388,34 @@ def run_velocity_advance(cfg, rhohalf, sponge=None, nthreads=0, checked=False):
     if rc != 0:
         raise RuntimeError("oracle: " + L.mo_last_error().decode())
     return dict(unew=unew, uedge=uedge, umac=umac)
+
+
+def est_dt(cfg, cfl=0.5, drdxfac=1):
+    """Oracle EstDt (advective + force constraints) on cfg's single level or cfg["levels"]:
+    returns (dt before the max_dt / fixed_dt limits, umax)."""
+    from maestroex_gb300.params import make_params
+    p = make_params(cfg)
+    levels = cfg["levels"] if "levels" in cfg else [cfg]
+    nlev = len(levels)
+    keep = []
+
+    def arr(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return _p(a)
+
+    ins = (MoInputs * nlev)()
+    for lev, Lv in enumerate(levels):
+        for name in ("uold", "sold", "gpi", "thermal", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new",
+                     "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
+            setattr(ins[lev], name, arr(Lv[name] if name in Lv else cfg[name]))
+    nboxes = (C.c_int * nlev)(*[len(Lv["boxes"]) for Lv in levels])
+    boxes = np.ascontiguousarray(np.array([b for Lv in levels for b in Lv["boxes"]], dtype=np.int32).reshape(-1))
+    dt, umax = C.c_double(0.0), C.c_double(0.0)
+    L = lib()
+    L.mo_est_dt.restype = C.c_int
+    rc = L.mo_est_dt(C.byref(p), nlev, nboxes, boxes.ctypes.data_as(C.POINTER(C.c_int)), ins, C.c_double(cfl),
+                     int(drdxfac), C.byref(dt), C.byref(umax))
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.mo_last_error().decode())
+    return dt.value, umax.value
