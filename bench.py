@@ -234,12 +234,12 @@ def run_cpu_baseline(steps, warmup, nthreads=0):
 
 
 def run_amr(args, ws, steps, warmup, barrier):
-    """Two-level AMR workload (config 3): the batched path replayed as a CUDA graph against
+    """Two-level AMR workload: the batched path replayed as a CUDA graph against
     one launch per box, same inputs, same results (bitwise; checked here)."""
     import torch
     from maestroex_gb300 import capi, configs
     from maestroex_gb300.stage import amr_buffers, make_amr_stage
-    cfg = configs.config_c3(n0=args.amr_n, nspec=args.nspec)
+    cfg = configs.workload_amr(n0=args.amr_n, nspec=args.nspec)
     st = make_amr_stage(cfg)
     bufs = amr_buffers(cfg)
     names = ("uold", "sold", "gpi")
@@ -422,7 +422,7 @@ def run_adjoint(args, barrier):
 
 
 def run_spherical(args, barrier):
-    """Full-star spherical workload (config 5's geometry): two levels, level 0 n^3 in uneven
+    """Full-star spherical workload: two levels, level 0 n^3 in uneven
     boxes (edges 16-128), level 1 (ratio 2) 16-64-cell boxes around 3 seeded bubbles, NumSpec
     21, ppm_type 2, exact base state on the fine level's irregular radial grid, polytrope
     star, outflow faces; the level-1 state injected from level 0.  Graph-replayed stage vs
@@ -538,7 +538,7 @@ def run_2d(args, barrier):
     import torch
     from maestroex_gb300 import capi, configs
     from maestroex_gb300.stage import StageBuffers, make_stage
-    cfg = configs.config_c1(n=256)
+    cfg = configs.workload_2d(n=256)
     st = make_stage(cfg)
     buf = StageBuffers(cfg).load(cfg)
     snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}

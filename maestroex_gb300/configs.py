@@ -198,8 +198,8 @@ def planar_config(n=(32, 32, 32), nspec=3, ppm_type=1, bc_lo=(INTERIOR, INTERIOR
     return cfg
 
 
-def config_c2(n=256, box=64, nspec=13, seed=20261203 + 1):
-    """Config 2: 3-D single level, 256^3 in 64 boxes of 64^3, NumSpec 13, ppm_type 1, w0 != 0."""
+def workload_planar(n=256, box=64, nspec=13, seed=20261203 + 1):
+    """3-D single level, 256^3 in 64 boxes of 64^3, NumSpec 13, ppm_type 1, w0 != 0 (the bench workload)."""
     return planar_config(n=(n, n, n), nspec=nspec, ppm_type=1, max_grid=box, seed=seed,
                          w0_amp=1.0e4, cfl=0.7)
 
@@ -435,8 +435,8 @@ def planar_amr_config(n0=(32, 32, 32), nspec=3, ppm_type=2, max_grid=16, fine_bo
     return c0
 
 
-def config_c3(n0=256, nspec=13, seed=20261203 + 3, cover=0.06, p_stop=0.8):
-    """Config 3: two-level AMR, level 0 = n0^3 in uneven boxes (edges from
+def workload_amr(n0=256, nspec=13, seed=20261203 + 3, cover=0.06, p_stop=0.8):
+    """Two-level AMR, level 0 = n0^3 in uneven boxes (edges from
     {16, 32, 48, 64, 96, 128}), level 1 (ratio 2) = boxes of 16-64 fine cells of random
     aspect around 3 seeded bubbles covering about `cover` of the domain; NumSpec 13,
     ppm_type 2.  Level-1 state is injected from level 0 (each fine cell takes its parent's
@@ -570,7 +570,7 @@ def planar_config_2d(n=(64, 64), nspec=3, ppm_type=1, bc_lo=(INTERIOR, SLIPWALL)
     )
 
 
-def config_c1(n=256, nspec=3, seed=20261203):
-    """Config 1: 2-D single level, one n x n box, NumSpec 3, ppm_type 1, w0 = 0, x periodic,
+def workload_2d(n=256, nspec=3, seed=20261203):
+    """2-D single level, one n x n box, NumSpec 3, ppm_type 1, w0 = 0, x periodic,
     y slipwall (lo) / outflow (hi)."""
     return planar_config_2d(n=(n, n), nspec=nspec, ppm_type=1, seed=seed)

@@ -37,7 +37,9 @@ __device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, in
     auto S = SHIFT_S(s, sc);
     const double C = 1.25;
     double se = (7.0 / 12.0) * (S(m - 1) + S(m)) - (1.0 / 12.0) * (S(m - 2) + S(m + 1));
-    if ((se - S(m - 1)) * (S(m) - se) < 0.0) {
+    // reference: (se - s(m-1)) * (s(m) - se) < 0, i.e. the product of (se - s(m-1)) and
+    // -(s(m) - se) = se - s(m) (exact) is positive
+    if (prod_gt0(se - S(m - 1), se - S(m))) {
         double D2 = 3.0 * (S(m - 1) - 2.0 * se + S(m));
         double D2L = S(m - 2) - 2.0 * S(m - 1) + S(m);
         double D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
@@ -151,10 +153,12 @@ __device__ __forceinline__ void ppm_cell_edges(const FabView& s, int sc, const F
             const double bigm_tol = (D == 0 && lo_ext && (I == domlo + 1 || I == domlo + 2)) ? 1.e10 : 1.e-10;
             double alphap = sedger - s0;
             double alpham = sedge - s0;
-            const bool bigp = fabs(alphap) > 2.0 * fabs(alpham);
-            const bool bigm = fabs(alpham) > 2.0 * fabs(alphap);
+            // |alphap| > 2|alpham| and |alpham| > 2|alphap| on magnitudes' bit patterns;
+            // alpham * alphap >= 0 is "not (alpham * -alphap > 0)"
+            const bool bigp = (dbits(alphap) & ABS_MASK) > (dbits(twice(alpham)) & ABS_MASK);
+            const bool bigm = (dbits(alpham) & ABS_MASK) > (dbits(twice(alphap)) & ABS_MASK);
             bool extremum = false;
-            if (alpham * alphap >= 0.0) {
+            if (!prod_gt0(alpham, -alphap)) {
                 extremum = true;
             } else if (bigp || bigm) {
                 double dafacem = sedge - sedgel;
@@ -171,7 +175,7 @@ __device__ __forceinline__ void ppm_cell_edges(const FabView& s, int sc, const F
                     dachkm = dabarm;
                     dachkp = dabarp;
                 }
-                extremum = (dachkm * dachkp <= 0.0);
+                extremum = !prod_gt0(dachkm, dachkp);
             }
             if (extremum) {
                 double D2 = 6.0 * (alpham + alphap);

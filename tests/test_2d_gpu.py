@@ -75,8 +75,8 @@ def test_2d_prediction_types_and_modes():
     assert np.array_equal(g["snew"], gpu["snew"])
 
 
-def test_config1_one_256_box():
-    """Config 1: 2-D, one 256 x 256 box, NumSpec 3, ppm_type 1, w0 = 0."""
-    cfg = configs.config_c1(n=256)
+def test_one_256_box():
+    """2-D, one 256 x 256 box, NumSpec 3, ppm_type 1, w0 = 0."""
+    cfg = configs.workload_2d(n=256)
     gpu, ref = run_both(cfg)
-    assert compare_2d(cfg, gpu, ref, "c1")
+    assert compare_2d(cfg, gpu, ref, "256 x 256")

@@ -171,7 +171,7 @@ def test_2d_mass_conserved_between_walls():
 
 
 def test_spherical_star_conserves_mass_and_stays_finite():
-    """Spherical, exact base state (config 5's geometry at 32^3 in 8 boxes): nothing reaches the
+    """Spherical, exact base state (a full star at 32^3 in 8 boxes): nothing reaches the
     outflow faces, so the update conserves the total density to rounding; the ambient
     stays at its floor and every updated field is finite."""
     from maestroex_gb300 import configs
