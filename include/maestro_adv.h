@@ -67,6 +67,8 @@ typedef struct {
                                    r_cc(i) = sqrt(0.75 + 2i) dx, nr = nr_irreg + 1) */
     double prob_lo[3];          /* physical domain (the star's centre is its midpoint) */
     double prob_hi[3];
+    int reflux_type;            /* coarse-fine flux synchronisation: 1 (or 0) AverageDownFaces
+                                   of the fluxes, 2 FluxRegister reflux of the coarse state */
 } madv_params;
 
 typedef struct {

@@ -7,6 +7,8 @@
 //   average_down_faces  average_down_faces (Source/MaestroFillData.cpp:156-174)
 //   uedge_interface     the coarse-fine part of Maestro::FillPatchUedge
 //                       (Source/MaestroFillData.cpp:466-825)
+//   flux register       FluxRegister CrseInit / FineAdd / Reflux of reflux_type 2
+//                       (Source/MaestroMakeFlux.cpp:412-456, Source/MaestroAdvection.cpp:258-276)
 //
 // The AMReX routines are restated from their published algorithms (the reference's AMReX
 // submodule is empty and unpinned):
@@ -18,6 +20,15 @@
 //     value is u0 + xoff sx + yoff sy + zoff sz with offsets of -1/4 and +1/4;
 //   * average_down: the sum of the 8 children (k outer, i inner) times 1/8; faces: the sum
 //     of the 4 fine faces (outer = the higher transverse direction) times 1/4.
+//   * FluxRegister: one register face per coarse face of each coarsened fine box's six
+//     sides (orientations x-lo, y-lo, z-lo, x-hi, y-hi, z-hi).  CrseInit sets it to
+//     mult * (coarse flux of the face, read from the box owning the coarse cell inside the
+//     fine box); FineAdd adds mult * each of its 4 fine faces in turn (outer = the higher
+//     transverse direction); Reflux adds -reg / vol (lo side) or +reg / vol (hi side) to the
+//     coarse cell outside the face (periodic images wrapped, cells outside the domain
+//     skipped), the orientations one after the other.  With CrseInit's mult = -dt * (coarse
+//     face area) and FineAdd's dt * (fine face area), reg = dt A_c (<F_fine> - F_coarse),
+//     the flux mismatch the outside coarse cell's update takes back.
 // FillPatchUedge on a ghost face: a face on a coarse face takes the fine valid value if a
 // fine box has it (the box owning the cell above it, else below), else the coarse face
 // (owner of the cell above, else below, else of the nearest domain cell, from its ghost
@@ -325,6 +336,160 @@ void average_down_faces(Ctx& cf, Ctx& cc, int f0, int c0, int ncomp) {
         else if (d == 1) launch(cc, rt, 1, k_avgdown_faces<1>, cc.V(), cf.V(), cf.nb, f0 + 1, c0, ncomp);
         else launch(cc, rt, 1, k_avgdown_faces<2>, cc.V(), cf.V(), cf.nb, f0 + 2, c0, ncomp);
     }
+}
+
+// ---- flux register (reflux_type 2)
+// register faces of orientation o of every fine box: coarse face planes, box index in .b
+static const RegionTable& reg_table(Ctx& cf, int o) {
+    std::array<int, 4> key{2, o, 0, 0};
+    auto it = cf.amr_tables.find(key);
+    if (it != cf.amr_tables.end()) return it->second;
+    RegionTable& t = cf.amr_tables[key];
+    const int D = o % 3, side = o / 3;
+    long start = 0;
+    for (int fb = 0; fb < cf.nb; ++fb) {
+        RegionBox r{};
+        for (int d = 0; d < 3; ++d) {
+            const int lo = cf.ba[fb].lo[d] >> 1, hi = cf.ba[fb].hi[d] >> 1;
+            r.lo[d] = lo;
+            r.n[d] = hi - lo + 1;
+        }
+        if (side == 1) r.lo[D] += r.n[D];  // the hi face: coarsened hi + 1
+        r.n[D] = 1;
+        r.b = fb;
+        r.pad = o;
+        r.start = start;
+        start += (long)r.n[0] * r.n[1] * r.n[2];
+        t.h.push_back(r);
+    }
+    t.total = start;
+    if (!cuda_ok(cudaMalloc(&t.d, sizeof(RegionBox) * t.h.size()), "cudaMalloc(register table)") ||
+        !cuda_ok(cudaMemcpy(t.d, t.h.data(), sizeof(RegionBox) * t.h.size(), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(register table)"))
+        throw Fail{MADV_ERR_CUDA};
+    return t;
+}
+
+// register storage of a fine level: [orientation][face][component], allocated on first use
+static double* reg_storage(Ctx& cf, long off[7]) {
+    off[0] = 0;
+    for (int o = 0; o < 6; ++o) off[o + 1] = off[o] + reg_table(cf, o).total;
+    if (!cf.d_reg) {
+        if (!cuda_ok(cudaMalloc(&cf.d_reg, sizeof(double) * (size_t)off[6] * cf.nscal), "cudaMalloc(register)"))
+            throw Fail{MADV_ERR_CUDA};
+        cudaMemset(cf.d_reg, 0, sizeof(double) * (size_t)off[6] * cf.nscal);
+    }
+    return cf.d_reg;
+}
+
+// CrseInit: reg = mult * coarse flux on the face (the coarse box owning the inside cell)
+template <int D, int SIDE>
+__global__ void k_fr_crse_init(KARGS, const FabView* __restrict__ Vc, int nbc, LevelGeo gc, int ff, double* reg,
+                               long off, int nscal, int c0, int nc, double mult, int* err) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    int q[3] = {i, j, k};
+    if (SIDE == 1) q[D] -= 1;  // the inside cell of a hi face
+    const int cb = owner_in(gc, q[0], q[1], q[2]);
+    if (cb < 0) {
+        atomicOr(err, 4);
+        return;
+    }
+    const FabView fl = Vc[(ff + D) * nbc + cb];
+    double* r = reg + (off + gid_) * nscal;
+    for (int n = c0; n < c0 + nc; ++n) r[n] = mult * at(fl, i, j, k, n);
+}
+
+// FineAdd: reg += mult * each fine face of the coarse face, in turn
+template <int D>
+__global__ void k_fr_fine_add(KARGS, int ff, double* reg, long off, int nscal, int c0, int nc, double mult) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int t1 = D == 0 ? 1 : 0, t2 = D == 2 ? 1 : 2;
+    const FabView fl = VW(ff + D);
+    double* r = reg + (off + gid_) * nscal;
+    for (int n = c0; n < c0 + nc; ++n) {
+        double v = r[n];
+        for (int o = 0; o < 2; ++o)
+            for (int in = 0; in < 2; ++in) {
+                int q[3] = {2 * i, 2 * j, 2 * k};
+                q[t1] += in;
+                q[t2] += o;
+                v = v + mult * at(fl, q[0], q[1], q[2], n);
+            }
+        r[n] = v;
+    }
+}
+
+// Reflux: the coarse cell outside the face takes -reg/vol (lo side) or +reg/vol (hi side)
+template <int D, int SIDE>
+__global__ void k_fr_reflux(KARGS, const FabView* __restrict__ Vc, int nbc, LevelGeo gc, int fs, const double* reg,
+                            long off, int nscal, int c0, int nc, double vol) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    int q[3] = {i, j, k};
+    if (SIDE == 0) q[D] -= 1;
+    q[D] = wrap(gc, D, q[D]);
+    const int cb = owner_in(gc, q[0], q[1], q[2]);
+    if (cb < 0) return;  // outside the domain, or no coarse box there
+    const FabView sn = Vc[fs * nbc + cb];
+    const double* r = reg + (off + gid_) * nscal;
+    for (int n = c0; n < c0 + nc; ++n) {
+        if (SIDE == 0) at(sn, q[0], q[1], q[2], n) = at(sn, q[0], q[1], q[2], n) - r[n] / vol;
+        else at(sn, q[0], q[1], q[2], n) = at(sn, q[0], q[1], q[2], n) + r[n] / vol;
+    }
+}
+
+template <int D, int SIDE>
+static void fr_crse_init_o(Ctx& cf, Ctx& cc, double* reg, long off, int c0, int nc, double mult) {
+    launch(cf, reg_table(cf, D + 3 * SIDE), 1, k_fr_crse_init<D, SIDE>, cf.V(), cc.V(), cc.nb, geo_of(cc), F_SFLUX0,
+           reg, off, cf.nscal, c0, nc, mult, cf.d_flag);
+}
+template <int D>
+static void fr_fine_add_o(Ctx& cf, int o, double* reg, long off, int c0, int nc, double mult) {
+    launch(cf, reg_table(cf, o), 1, k_fr_fine_add<D>, cf.V(), F_SFLUX0, reg, off, cf.nscal, c0, nc, mult);
+}
+template <int D, int SIDE>
+static void fr_reflux_o(Ctx& cf, Ctx& cc, const double* reg, long off, int c0, int nc, double vol) {
+    launch(cf, reg_table(cf, D + 3 * SIDE), 1, k_fr_reflux<D, SIDE>, cf.V(), cc.V(), cc.nb, geo_of(cc), F_SNEW,
+           reg, off, cf.nscal, c0, nc, vol);
+}
+
+// FluxRegister::CrseInit of the coarse level's fluxes, components c0 .. c0+nc-1, mult =
+// -dt * coarse face area (Source/MaestroMakeFlux.cpp:430-439)
+void flux_reg_crse_init(Ctx& cf, Ctx& cc, int c0, int nc, double dt) {
+    long off[7];
+    double* reg = reg_storage(cf, off);
+    const double area[3] = {cc.P.dx[1] * cc.P.dx[2], cc.P.dx[0] * cc.P.dx[2], cc.P.dx[0] * cc.P.dx[1]};
+    fr_crse_init_o<0, 0>(cf, cc, reg, off[0], c0, nc, -1.0 * dt * area[0]);
+    fr_crse_init_o<0, 1>(cf, cc, reg, off[3], c0, nc, -1.0 * dt * area[0]);
+    fr_crse_init_o<1, 0>(cf, cc, reg, off[1], c0, nc, -1.0 * dt * area[1]);
+    fr_crse_init_o<1, 1>(cf, cc, reg, off[4], c0, nc, -1.0 * dt * area[1]);
+    fr_crse_init_o<2, 0>(cf, cc, reg, off[2], c0, nc, -1.0 * dt * area[2]);
+    fr_crse_init_o<2, 1>(cf, cc, reg, off[5], c0, nc, -1.0 * dt * area[2]);
+}
+
+// FluxRegister::FineAdd of the fine level's fluxes, mult = dt * fine face area (:441-450)
+void flux_reg_fine_add(Ctx& cf, int c0, int nc, double dt) {
+    long off[7];
+    double* reg = reg_storage(cf, off);
+    const double area[3] = {cf.P.dx[1] * cf.P.dx[2], cf.P.dx[0] * cf.P.dx[2], cf.P.dx[0] * cf.P.dx[1]};
+    for (int side = 0; side < 2; ++side) {
+        fr_fine_add_o<0>(cf, 0 + 3 * side, reg, off[0 + 3 * side], c0, nc, 1.0 * dt * area[0]);
+        fr_fine_add_o<1>(cf, 1 + 3 * side, reg, off[1 + 3 * side], c0, nc, 1.0 * dt * area[1]);
+        fr_fine_add_o<2>(cf, 2 + 3 * side, reg, off[2 + 3 * side], c0, nc, 1.0 * dt * area[2]);
+    }
+}
+
+// FluxRegister::Reflux into the coarse level's new state (Source/MaestroAdvection.cpp:259-276),
+// the orientations in turn
+void flux_reg_reflux(Ctx& cf, Ctx& cc, int c0, int nc) {
+    long off[7];
+    const double* reg = reg_storage(cf, off);
+    const double vol = cc.P.dx[0] * cc.P.dx[1] * cc.P.dx[2];
+    fr_reflux_o<0, 0>(cf, cc, reg, off[0], c0, nc, vol);
+    fr_reflux_o<1, 0>(cf, cc, reg, off[1], c0, nc, vol);
+    fr_reflux_o<2, 0>(cf, cc, reg, off[2], c0, nc, vol);
+    fr_reflux_o<0, 1>(cf, cc, reg, off[3], c0, nc, vol);
+    fr_reflux_o<1, 1>(cf, cc, reg, off[4], c0, nc, vol);
+    fr_reflux_o<2, 1>(cf, cc, reg, off[5], c0, nc, vol);
 }
 
 template <int D>

@@ -535,6 +535,17 @@ static void convert_rhox_to_x_h(Hier& H, int flag) {
 // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
 static void update_scal_h(Hier& H, int start_comp) {
     for (auto* c : H.L) update_scal(*c, start_comp);
+    // reflux_type 2: the coarse cells next to each finer level take back the flux mismatch,
+    // the finest pair first (Source/MaestroAdvection.cpp:258-276)
+    if (H[0].P.reflux_type == 2)
+        for (int l = H.n() - 2; l >= 0; --l) {
+            if (start_comp == RHOH) {
+                flux_reg_reflux(H[l + 1], H[l], RHOH, 1);
+            } else {
+                flux_reg_reflux(H[l + 1], H[l], FIRSTSPEC, H[0].nspec);
+                flux_reg_reflux(H[l + 1], H[l], RHO, 1);
+            }
+        }
     if (start_comp == RHOH) {
         average_down_h(H, F_SNEW, RHOH, 1);
         fill_patch_h(H, F_SNEW, RHOH, 1, BCS_S, RHOH, 0, RHOH);
@@ -544,6 +555,27 @@ static void update_scal_h(Hier& H, int start_comp) {
         fill_patch_h(H, F_SNEW, FIRSTSPEC, ns, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
         average_down_h(H, F_SNEW, RHO, 1);
         fill_patch_h(H, F_SNEW, RHO, 1, BCS_S, RHO, 0, RHO);
+    }
+}
+
+// the fluxes across levels: reflux_type 1 averages the fine fluxes down onto the coarse faces
+// (Source/MaestroMakeFlux.cpp:460-462); reflux_type 2 records the flux mismatch of the
+// updated components (and Rho with the species) in the flux registers (:420-456)
+static void flux_sync_h(Hier& H, int c0, int nc) {
+    if (H[0].P.reflux_type != 2) {
+        average_down_faces_h(H, F_SFLUX0, 0, H[0].nscal);
+        return;
+    }
+    const double dt = H[0].P.dt;
+    for (int l = 0; l < H.n(); ++l) {
+        if (l + 1 < H.n()) {
+            flux_reg_crse_init(H[l + 1], H[l], c0, nc, dt);
+            if (c0 == FIRSTSPEC) flux_reg_crse_init(H[l + 1], H[l], RHO, 1, dt);
+        }
+        if (l > 0) {
+            flux_reg_fine_add(H[l], c0, nc, dt);
+            if (c0 == FIRSTSPEC) flux_reg_fine_add(H[l], RHO, 1, dt);
+        }
     }
 }
 
@@ -574,7 +606,7 @@ static void density_advance(Hier& H, int which_step) {
         make_s0mac_h(H, r0n, F_S0MACB0);
     }
     for (auto* c : H.L) make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
-    average_down_faces_h(H, F_SFLUX0, 0, nscal);
+    flux_sync_h(H, FIRSTSPEC, ns);
     // scal_force.setVal(0) before UpdateScal (Source/MaestroDensityAdvance.cpp:229-231): of
     // the components read from here on, only Rho has been written since the zeroing above
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHO, 1, 1);
@@ -605,7 +637,7 @@ static void enthalpy_advance(Hier& H, int which_step) {
         make_s0mac_h(H, rh0n, F_S0MACB0);
     }
     for (auto* c : H.L) make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en));
-    average_down_faces_h(H, F_SFLUX0, 0, nscal);
+    flux_sync_h(H, RHOH, 1);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
     addw0_h(H, F_UMAC0, -1.0);
     make_rhoh_force_h(H, 0, 0, which_step);
@@ -917,6 +949,8 @@ static void destroy_level(Ctx& c) {
     if (c.d_flag) cudaFree(c.d_flag);
     if (c.d_red) cudaFree(c.d_red);
     c.d_red = nullptr;
+    if (c.d_reg) cudaFree(c.d_reg);
+    c.d_reg = nullptr;
     c.d_flag = nullptr;
 }
 
@@ -1099,6 +1133,10 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
     }
     if (p->ppm_trace_forces != 0 || (p->use_exact_base_state != 0 && !p->spherical)) {
         set_error("ppm_trace_forces must be 0; use_exact_base_state needs spherical geometry");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    if (p->reflux_type < 0 || p->reflux_type > 2 || (p->reflux_type == 2 && p->dim == 2)) {
+        set_error("reflux_type must be 1 (or 0) or 2; 2 is built for 3-D");
         return MADV_ERR_UNSUPPORTED;
     }
     if (!(p->dt > 0.0) || !(p->rel_eps >= 0.0)) {

@@ -149,6 +149,7 @@ struct Ctx {
     int tpb_of(const void* fn);
     int* d_flag = nullptr;  // device error flag (EOS cutoff)
     unsigned long long* d_red = nullptr;  // EstDt maxima (allocated on first use)
+    double* d_reg = nullptr;  // flux register of this (fine) level with the level below (reflux_type 2)
     // graph mode
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<const void*> graph_key;
@@ -260,6 +261,9 @@ void interp_fill(Ctx& cc, Ctx& cf, int fid, int c0, int nc, int which_bcs, int b
 void average_down(Ctx& cf, Ctx& cc, int fid, int comp, int ncomp);
 void average_down_faces(Ctx& cf, Ctx& cc, int f0, int c0, int ncomp);
 void uedge_interface(Ctx& cc, Ctx& cf, int f0);
+void flux_reg_crse_init(Ctx& cf, Ctx& cc, int c0, int nc, double dt);
+void flux_reg_fine_add(Ctx& cf, int c0, int nc, double dt);
+void flux_reg_reflux(Ctx& cf, Ctx& cc, int c0, int nc);
 
 // ---- reverse sweep (madv_adjoint.cu).  User slots bound by the adjoint driver: working
 // state (A_WSOLD / A_WSNEW), state adjoints (A_ASOLD / A_ASNEW), edge-state adjoints, the

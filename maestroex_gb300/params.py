@@ -41,6 +41,7 @@ class MadvParams(C.Structure):
         ("spherical", C.c_int),
         ("prob_lo", C.c_double * 3),
         ("prob_hi", C.c_double * 3),
+        ("reflux_type", C.c_int),
     ]
 
 
@@ -75,4 +76,5 @@ def make_params(cfg):
         p.prob_hi[d] = cfg.get("prob_hi", tuple(lo[e] + cfg["n"][e] * cfg["dx"][e] for e in range(3)))[d]
     if p.spherical:
         p.base_cutoff_density_coord = cfg["nr"]
+    p.reflux_type = cfg.get("reflux_type", 1)
     return p

@@ -1409,6 +1409,137 @@ struct Stage {
         for (int n = 0; n < nlev; ++n) S[n].cutoff = coord[n];
     }
 
+    // ------------------------------------------------------------------ FluxRegister
+    // reflux_type 2 (Source/MaestroMakeFlux.cpp:412-456, Source/MaestroAdvection.cpp:258-276),
+    // AMReX FluxRegister restated: level l >= 1 holds, per fine box and orientation (x-lo,
+    // y-lo, z-lo, x-hi, y-hi, z-hi), one register value per coarse face of the coarsened
+    // box's side and component.  CrseInit sets mult * coarse flux (read from the coarse box
+    // owning the inside cell), FineAdd adds mult * each of the 4 fine faces in turn (outer =
+    // the higher transverse direction), Reflux adds -reg/vol (lo) or +reg/vol (hi) to the
+    // coarse cell outside the face, orientation by orientation.
+    std::vector<std::vector<std::array<std::vector<real>, 6>>> freg;  // [lev][box][orientation]
+    Box RegFaces(int lev, int b, int o) const {
+        const int D = o % 3;
+        Box f;
+        for (int d = 0; d < 3; ++d) {
+            f.lo[d] = S[lev].L.ba[b].lo[d] >> 1;
+            f.hi[d] = S[lev].L.ba[b].hi[d] >> 1;
+        }
+        if (o >= 3) f.lo[D] = f.hi[D] + 1;
+        f.hi[D] = f.lo[D];
+        return f;
+    }
+    std::vector<real>& Reg(int lev, int b, int o) {
+        if (freg.size() != (size_t)nlev) freg.assign(nlev, {});
+        if (freg[lev].size() != S[lev].L.ba.size()) freg[lev].assign(S[lev].L.ba.size(), {});
+        std::vector<real>& r = freg[lev][b][o];
+        const Box f = RegFaces(lev, b, o);
+        const size_t n = (size_t)(f.hi[0] - f.lo[0] + 1) * (f.hi[1] - f.lo[1] + 1) * (f.hi[2] - f.lo[2] + 1) * nscal;
+        if (r.size() != n) r.assign(n, 0.0);
+        return r;
+    }
+    static long FaceIdx(const Box& f, int i, int j, int k) {
+        const long nx = f.hi[0] - f.lo[0] + 1, ny = f.hi[1] - f.lo[1] + 1;
+        return (i - f.lo[0]) + nx * ((j - f.lo[1]) + ny * (long)(k - f.lo[2]));
+    }
+    void CrseInit(int levf, VF& sflux, int c0, int nc) {
+        const int levc = levf - 1;
+        const double* dx = S[levc].L.dx;
+        const double area[3] = {dx[1] * dx[2], dx[0] * dx[2], dx[0] * dx[1]};
+        Owner oc;
+        oc.build(S[levc].L);
+        for (int b = 0; b < (int)S[levf].L.ba.size(); ++b)
+            for (int o = 0; o < 6; ++o) {
+                const int D = o % 3;
+                const double mult = -1.0 * dt_ * area[D];
+                std::vector<real>& r = Reg(levf, b, o);
+                const Box f = RegFaces(levf, b, o);
+                MO_FOR3(f) {
+                    int q[3] = {i, j, k};
+                    if (o >= 3) q[D] -= 1;
+                    const int cb = oc.at(S[levc].L, q[0], q[1], q[2]);
+                    if (cb < 0) throw std::runtime_error("CrseInit: a coarse cell under the fine level has no box");
+                    for (int n = c0; n < c0 + nc; ++n)
+                        r[FaceIdx(f, i, j, k) * nscal + n] = mult * sflux[levc][D][cb](i, j, k, n);
+                }
+            }
+    }
+    void FineAdd(int levf, VF& sflux, int c0, int nc) {
+        const double* dx = S[levf].L.dx;
+        const double area[3] = {dx[1] * dx[2], dx[0] * dx[2], dx[0] * dx[1]};
+        for (int b = 0; b < (int)S[levf].L.ba.size(); ++b)
+            for (int o = 0; o < 6; ++o) {
+                const int D = o % 3, t1 = D == 0 ? 1 : 0, t2 = D == 2 ? 1 : 2;
+                const double mult = 1.0 * dt_ * area[D];
+                std::vector<real>& r = Reg(levf, b, o);
+                const Box f = RegFaces(levf, b, o);
+                const Arr& fl = sflux[levf][D][b];
+                MO_FOR3(f) {
+                    for (int n = c0; n < c0 + nc; ++n) {
+                        real v = r[FaceIdx(f, i, j, k) * nscal + n];
+                        for (int oo = 0; oo < 2; ++oo)
+                            for (int in = 0; in < 2; ++in) {
+                                int q[3] = {2 * i, 2 * j, 2 * k};
+                                q[t1] += in;
+                                q[t2] += oo;
+                                v = v + mult * fl(q[0], q[1], q[2], n);
+                            }
+                        r[FaceIdx(f, i, j, k) * nscal + n] = v;
+                    }
+                }
+            }
+    }
+    void Reflux(int levf, VMF& snew, int c0, int nc) {
+        const int levc = levf - 1;
+        const Level& Lc = S[levc].L;
+        const double vol = Lc.dx[0] * Lc.dx[1] * Lc.dx[2];
+        Owner oc;
+        oc.build(Lc);
+        for (int o = 0; o < 6; ++o)
+            for (int b = 0; b < (int)S[levf].L.ba.size(); ++b) {
+                const int D = o % 3;
+                std::vector<real>& r = Reg(levf, b, o);
+                const Box f = RegFaces(levf, b, o);
+                MO_FOR3(f) {
+                    int q[3] = {i, j, k};
+                    if (o < 3) q[D] -= 1;
+                    const int len = Lc.dom.hi[D] - Lc.dom.lo[D] + 1;
+                    if (Lc.per[D]) {
+                        if (q[D] < Lc.dom.lo[D]) q[D] += len;
+                        if (q[D] > Lc.dom.hi[D]) q[D] -= len;
+                    }
+                    const int cb = oc.at(Lc, q[0], q[1], q[2]);
+                    if (cb < 0) continue;
+                    const Arr& sn = snew[levc][cb];
+                    for (int n = c0; n < c0 + nc; ++n) {
+                        const real g = r[FaceIdx(f, i, j, k) * nscal + n];
+                        if (o < 3) sn(q[0], q[1], q[2], n) = sn(q[0], q[1], q[2], n) - g / vol;
+                        else sn(q[0], q[1], q[2], n) = sn(q[0], q[1], q[2], n) + g / vol;
+                    }
+                }
+            }
+    }
+    double dt_ = 0.0;
+    // the fluxes across levels: reflux_type 1 AverageDownFaces (Source/MaestroMakeFlux.cpp:460-462),
+    // 2 the registers of the updated components (and Rho with the species)
+    void FluxSync(VF& sflux, int c0, int nc) {
+        if (P.reflux_type != 2) {
+            AverageDownFaces(sflux);
+            return;
+        }
+        dt_ = P.dt;
+        for (int lev = 0; lev < nlev; ++lev) {
+            if (lev + 1 < nlev) {
+                CrseInit(lev + 1, sflux, c0, nc);
+                if (c0 == FirstSpec) CrseInit(lev + 1, sflux, Rho, 1);
+            }
+            if (lev > 0) {
+                FineAdd(lev, sflux, c0, nc);
+                if (c0 == FirstSpec) FineAdd(lev, sflux, Rho, 1);
+            }
+        }
+    }
+
     // ------------------------------------------------------------------ AdvancePremac
     void MakeUtrans(VMF& utilde, VMF& ufull, VF& utrans) {
         for (int lev = 0; lev < nlev; ++lev) S[lev].MakeUtrans(utilde[lev], ufull[lev], utrans[lev].data());
@@ -1548,7 +1679,7 @@ struct Stage {
             S[lev].MakeRhoXFlux(sflux[lev].data(), eta[lev], sedge[lev].data(), umac[lev].data(), r0_old[lev],
                                 r0e_old[lev], r0_new[lev], r0e_new[lev], start_comp, num_comp, r0mac_old[lev].data(),
                                 r0mac_new[lev].data());
-        AverageDownFaces(sflux);
+        FluxSync(sflux, start_comp, num_comp);
     }
     // Maestro::MakeRhoHFlux (Source/MaestroMakeFlux.cpp:467-1067)
     void MakeRhoHFlux(VF& sflux, VF& sedge, VF& umac, const BS& rh0_old, const BS& rh0e_old, const BS& rh0_new,
@@ -1561,12 +1692,17 @@ struct Stage {
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeRhoHFlux(sflux[lev].data(), sedge[lev].data(), umac[lev].data(), rh0_old[lev], rh0e_old[lev],
                                 rh0_new[lev], rh0e_new[lev], h0mac_old[lev].data(), h0mac_new[lev].data());
-        AverageDownFaces(sflux);
+        FluxSync(sflux, RhoH, 1);
     }
     // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
     void UpdateScal(VMF& sold, VMF& snew, VF& sflux, VMF& force, int start_comp, int num_comp) {
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].UpdateScal(sold[lev], snew[lev], sflux[lev].data(), force[lev], start_comp, num_comp);
+        if (P.reflux_type == 2)
+            for (int lev = nlev - 2; lev >= 0; --lev) {
+                Reflux(lev + 1, snew, start_comp, num_comp);
+                if (start_comp == FirstSpec) Reflux(lev + 1, snew, Rho, 1);
+            }
         AverageDown(snew, start_comp, num_comp);
         FillPatch(snew, start_comp, num_comp, start_comp, bcs_s(), false, start_comp);
         if (start_comp == FirstSpec) {

@@ -42,6 +42,7 @@ typedef struct {
     int spherical;      /* spherical geometry with the exact (irregular) base state */
     double prob_lo[3];
     double prob_hi[3];
+    int reflux_type; /* 1 (or 0): AverageDownFaces of the fluxes; 2: FluxRegister reflux */
 } mo_params;
 
 typedef struct {
