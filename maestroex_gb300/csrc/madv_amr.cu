@@ -39,6 +39,7 @@
 //
 // Level lookups use an owner map per level (the box owning each cell of the level's
 // domain, int32): 67 MB for a 256^3 level, 537 MB for a 512^3 level.
+#include "madv_exact.cuh"
 #include "madv_launch.cuh"
 
 namespace madv {
@@ -138,44 +139,17 @@ __device__ double cval(const LevelGeo& g, const FabView* __restrict__ Vc, int nb
 
 __device__ __forceinline__ double cv(const LevelGeo& g, const FabView* __restrict__ Vc, int nbc, int fid, int n,
                                      const BCRecD& bc, bool velish, int a, int b, int c, int* err) {
-    return cval<2>(g, Vc, nbc, fid, n, bc, velish, wrap(g, 0, a), wrap(g, 1, b), wrap(g, 2, c), err);
-}
-
-// cell_cons_interp value of fine cell (i, j, k), component n.
-__device__ double cons_interp(const LevelGeo& gc, const FabView* __restrict__ Vc, int nbc, int fid, int n,
-                              const BCRecD& bc, bool velish, int i, int j, int k, int* err) {
-    const int I[3] = {i >> 1, j >> 1, k >> 1};
-    const int f[3] = {i, j, k};
-    const double u0 = cv(gc, Vc, nbc, fid, n, bc, velish, I[0], I[1], I[2], err);
-    double s[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        int pp[3] = {I[0], I[1], I[2]}, pm[3] = {I[0], I[1], I[2]};
-        pp[d] += 1;
-        pm[d] -= 1;
-        const double up = cv(gc, Vc, nbc, fid, n, bc, velish, pp[0], pp[1], pp[2], err);
-        const double dn = cv(gc, Vc, nbc, fid, n, bc, velish, pm[0], pm[1], pm[2], err);
-        double dc = 0.5 * (up - dn);
-        if (!gc.per[d]) {
-            if (I[d] == gc.dlo[d] && (bc.lo[d] == BC_EXT_DIR || bc.lo[d] == BC_HOEXTRAP))
-                dc = (up + 3.0 * u0 - 4.0 * dn) / 3.0;
-            if (I[d] == gc.dhi[d] && (bc.hi[d] == BC_EXT_DIR || bc.hi[d] == BC_HOEXTRAP))
-                dc = (4.0 * up - 3.0 * u0 - dn) / 3.0;
-        }
-        const double df = 2.0 * (up - u0);
-        const double db = 2.0 * (u0 - dn);
-        const double sl = (df * db >= 0.0) ? mn(fabs(df), fabs(db)) : 0.0;
-        s[d] = copysign(1.0, dc) * mn(sl, fabs(dc));
+    const int p0 = wrap(g, 0, a), p1 = wrap(g, 1, b), p2 = wrap(g, 2, c);
+    // a cell of the domain: its owner's value (what cval reaches through its recursion)
+    if (p0 >= g.dlo[0] && p0 <= g.dhi[0] && p1 >= g.dlo[1] && p1 <= g.dhi[1] && p2 >= g.dlo[2] && p2 <= g.dhi[2]) {
+        const int ob = g.owner[(p0 - g.dlo[0]) + g.nx * ((p1 - g.dlo[1]) + g.ny * (long)(p2 - g.dlo[2]))];
+        if (ob >= 0) return at(Vc[fid * nbc + ob], p0, p1, p2, n);
+        atomicOr(err, 2);
+        return 0.0;
     }
-    double off[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) off[d] = (f[d] - 2 * I[d]) == 0 ? -0.25 : 0.25;
-    return u0 + off[0] * s[0] + off[1] * s[1] + off[2] * s[2];
+    return cval<2>(g, Vc, nbc, fid, n, bc, velish, p0, p1, p2, err);
 }
 
-// ------------------------------------------------------------------ tables
-// Ghost shell of every box of c: its FAB region (valid box, nodal in `nodal`, grown by ng)
-// minus the valid box, as six disjoint slabs per box.
 static const RegionTable& shell_table(Ctx& c, int ng, int nodal) {
     std::array<int, 4> key{0, ng, nodal, 0};
     auto it = c.amr_tables.find(key);
@@ -271,6 +245,44 @@ static const RegionTable& down_table(Ctx& cf, const Ctx& cc, int nodal) {
 }
 
 // ------------------------------------------------------------------ kernels
+// cell_cons_interp value of fine cell (i, j, k), component n.  The exact bit-pattern forms
+// of 2x, x/2, |x|, the product sign and copysign(1, dc) * m of madv_exact.cuh replace the FP
+// instructions of the literal expressions.  (Resolving the 7 coarse neighbours once for all
+// components was tried: it costs registers, and the kernel ran slower.)
+__device__ double cons_interp(const LevelGeo& gc, const FabView* __restrict__ Vc, int nbc, int fid, int n,
+                              const BCRecD& bc, bool velish, int i, int j, int k, int* err) {
+    const int I[3] = {i >> 1, j >> 1, k >> 1};
+    const int f[3] = {i, j, k};
+    const double u0 = cv(gc, Vc, nbc, fid, n, bc, velish, I[0], I[1], I[2], err);
+    double s[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int pp[3] = {I[0], I[1], I[2]}, pm[3] = {I[0], I[1], I[2]};
+        pp[d] += 1;
+        pm[d] -= 1;
+        const double up = cv(gc, Vc, nbc, fid, n, bc, velish, pp[0], pp[1], pp[2], err);
+        const double dn = cv(gc, Vc, nbc, fid, n, bc, velish, pm[0], pm[1], pm[2], err);
+        double dc = half(up - dn);
+        if (!gc.per[d]) {
+            if (I[d] == gc.dlo[d] && (bc.lo[d] == BC_EXT_DIR || bc.lo[d] == BC_HOEXTRAP))
+                dc = (up + 3.0 * u0 - 4.0 * dn) / 3.0;
+            if (I[d] == gc.dhi[d] && (bc.hi[d] == BC_EXT_DIR || bc.hi[d] == BC_HOEXTRAP))
+                dc = (4.0 * up - 3.0 * u0 - dn) / 3.0;
+        }
+        const double df = twice(up - u0);
+        const double db = twice(u0 - dn);
+        // sl = (df * db >= 0) ? min(|df|, |db|) : 0;  s = copysign(1, dc) * min(sl, |dc|)
+        long long sl = 0;
+        if (!prod_gt0(df, -db)) sl = min(dbits(df) & ABS_MASK, dbits(db) & ABS_MASK);
+        const long long m = min(sl, dbits(dc) & ABS_MASK);
+        s[d] = __longlong_as_double(m | (dbits(dc) & SIGN_BIT));
+    }
+    double off[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) off[d] = (f[d] - 2 * I[d]) == 0 ? -0.25 : 0.25;
+    return u0 + off[0] * s[0] + off[1] * s[1] + off[2] * s[2];
+}
+
 __global__ void k_interp_fill(KARGS, const FabView* __restrict__ Vc, int nbc, LevelGeo gc, LevelGeo gf, int fid,
                               int c0, int nc, const BCRecD* __restrict__ bcs, int bc_c0, int is_vel, int state_c0,
                               int* err) {
