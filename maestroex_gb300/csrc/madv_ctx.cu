@@ -645,11 +645,70 @@ static void enthalpy_advance(Hier& H, int which_step) {
     update_scal_h(H, RHOH);
 }
 
-static int check_ready_h(const Hier& H) {
+// The stage's working copies of the caller's sold, snew, umac, sedge and sflux: a call that
+// hands over FABs laid out as these fields works in them directly, so their storage is
+// allocated at the first call that does not (at 256^3 with NumSpec 13 they are 60% of a
+// level's fields).
+static bool deferrable(int f) {
+    return f == F_SOLD || f == F_SNEW || (f >= F_UMAC0 && f <= F_UMAC2) || (f >= F_SEDGE0 && f <= F_SEDGE2) ||
+           (f >= F_SFLUX0 && f <= F_SFLUX2);
+}
+
+// host views of field f: one FAB per box (valid box grown by the field's ghost width), laid
+// end to end from the field's base
+static void field_views(Ctx& c, int f) {
+    const FieldSpec& s = c.F[f].spec;
+    size_t off = 0;
+    for (int b = 0; b < c.nb; ++b) {
+        HBox v = valid_box(c, b, s.nodal);
+        int lo[3], hi[3];
+        size_t n = 1;
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = v.lo[d] - s.ng;
+            hi[d] = v.hi[d] + s.ng;
+            n *= (size_t)(hi[d] - lo[d] + 1);
+        }
+        c.hviews_pinned[f * c.nb + b] = make_view(c.F[f].base + off, lo, hi);
+        off += n * s.ncomp;
+    }
+}
+
+// allocates, zeroes and enters in the base view table a deferred field; on failure the
+// field stays deferred with empty views
+static void materialize(Ctx& c, int f) {
+    Field& F = c.F[f];
+    if (!F.deferred) return;
+    if (!cuda_ok(cudaMalloc(&F.base, F.bytes), "cudaMalloc(field)")) {
+        F.base = nullptr;
+        throw Fail{MADV_ERR_CUDA};
+    }
+    field_views(c, f);
+    const size_t v0 = (size_t)f * c.nb;
+    if (!cuda_ok(cudaMemset(F.base, 0, F.bytes), "cudaMemset") ||
+        !cuda_ok(cudaMemcpy(c.dviews + v0, c.hviews_pinned + v0, sizeof(FabView) * c.nb, cudaMemcpyHostToDevice),
+                 "cudaMemcpy(views)") ||
+        !cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) {
+        cudaFree(F.base);
+        F.base = nullptr;
+        std::memset(c.hviews_pinned + v0, 0, sizeof(FabView) * c.nb);
+        throw Fail{MADV_ERR_CUDA};
+    }
+    F.deferred = false;
+}
+
+// every_field: allocate the deferred fields too (every entry point but the stage, which
+// allocates those its caller does not hand over)
+static int check_ready_h(const Hier& H, bool every_field = true) {
     for (auto* c : H.L)
         if (!c->have_layout || !c->have_base) {
             set_error("the layout and the base state must be set first");
             return MADV_ERR_STATE;
+        }
+    if (every_field) try {
+            for (auto* c : H.L)
+                for (int f = 0; f < NF_INTERNAL; ++f) materialize(*c, f);
+        } catch (const Fail& f) {
+            return f.code;
         }
     return MADV_OK;
 }
@@ -693,18 +752,29 @@ static FabView* alias_fields(Ctx& c, StageIO& io) {
     add(io.umac, c.ndim), add(io.sedge, c.ndim), add(io.sflux, c.ndim);
     std::vector<const double*> sorted = ptrs;
     std::sort(sorted.begin(), sorted.end());
-    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return base;
+    const bool distinct = std::adjacent_find(sorted.begin(), sorted.end()) == sorted.end();
     auto all = [&](int f0, const madv_multifab* m) {
         if (!m) return false;
         for (int d = 0; d < c.ndim; ++d)
             if (!can_alias(c, f0 + d, &m[d])) return false;
         return true;
     };
-    if (io.sold_out && can_alias(c, F_SOLD, io.sold)) io.alias |= AL_SOLD;
-    if (can_alias(c, F_SNEW, io.snew)) io.alias |= AL_SNEW;
-    if (all(F_UMAC0, io.umac)) io.alias |= AL_UMAC;
-    if (all(F_SEDGE0, io.sedge)) io.alias |= AL_SEDGE;
-    if (all(F_SFLUX0, io.sflux)) io.alias |= AL_SFLUX;
+    if (distinct) {
+        if (io.sold_out && can_alias(c, F_SOLD, io.sold)) io.alias |= AL_SOLD;
+        if (can_alias(c, F_SNEW, io.snew)) io.alias |= AL_SNEW;
+        if (all(F_UMAC0, io.umac)) io.alias |= AL_UMAC;
+        if (all(F_SEDGE0, io.sedge)) io.alias |= AL_SEDGE;
+        if (all(F_SFLUX0, io.sflux)) io.alias |= AL_SFLUX;
+    }
+    // the fields this call does not work in the caller's FABs need their own storage
+    if (!(io.alias & AL_SOLD)) materialize(c, F_SOLD);
+    if (!(io.alias & AL_SNEW)) materialize(c, F_SNEW);
+    for (int d = 0; d < 3; ++d) {
+        const bool in_call = d < c.ndim;
+        if (!(in_call && (io.alias & AL_UMAC))) materialize(c, F_UMAC0 + d);
+        if (!(in_call && (io.alias & AL_SEDGE))) materialize(c, F_SEDGE0 + d);
+        if (!(in_call && (io.alias & AL_SFLUX))) materialize(c, F_SFLUX0 + d);
+    }
     if (!io.alias) return base;
     const size_t nv = (size_t)NF_TOTAL * c.nb;
     if (!c.dviews_alias) {
@@ -1007,29 +1077,20 @@ static int layout_level(Ctx& c, int nboxes, const madv_box* boxes, bool cover) {
                 tot += n * s.ncomp;
             }
             c.F[f].bytes = tot * sizeof(double);
+            c.F[f].deferred = false;
             if (tot == 0) continue;  // a field this context does not use
+            if (deferrable(f)) {
+                c.F[f].deferred = true;
+                continue;
+            }
             if (!cuda_ok(cudaMalloc(&c.F[f].base, c.F[f].bytes), "cudaMalloc(field)")) throw Fail{MADV_ERR_CUDA};
             if (!cuda_ok(cudaMemset(c.F[f].base, 0, c.F[f].bytes), "cudaMemset")) throw Fail{MADV_ERR_CUDA};
         }
         if (!cuda_ok(cudaMallocHost(&c.hviews_pinned, sizeof(FabView) * NF_TOTAL * c.nb), "cudaMallocHost"))
             throw Fail{MADV_ERR_CUDA};
         std::memset(c.hviews_pinned, 0, sizeof(FabView) * NF_TOTAL * c.nb);
-        for (int f = 0; f < NF_INTERNAL; ++f) {
-            const FieldSpec& s = c.F[f].spec;
-            size_t off = 0;
-            for (int b = 0; b < c.nb; ++b) {
-                HBox v = valid_box(c, b, s.nodal);
-                int lo[3], hi[3];
-                size_t n = 1;
-                for (int d = 0; d < 3; ++d) {
-                    lo[d] = v.lo[d] - s.ng;
-                    hi[d] = v.hi[d] + s.ng;
-                    n *= (size_t)(hi[d] - lo[d] + 1);
-                }
-                c.hviews_pinned[f * c.nb + b] = make_view(c.F[f].base + off, lo, hi);
-                off += n * s.ncomp;
-            }
-        }
+        for (int f = 0; f < NF_INTERNAL; ++f)
+            if (!c.F[f].deferred) field_views(c, f);
         if (!cuda_ok(cudaMalloc(&c.dviews, sizeof(FabView) * NF_TOTAL * c.nb), "cudaMalloc(views)") ||
             !cuda_ok(cudaMemcpy(c.dviews, c.hviews_pinned, sizeof(FabView) * NF_TOTAL * c.nb, cudaMemcpyHostToDevice),
                      "cudaMemcpy(views)"))
@@ -1406,7 +1467,7 @@ static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab*
         set_error("the call passes " + std::to_string(nlev) + " levels, the layout has " + std::to_string(H.n()));
         return MADV_ERR_PARAM;
     }
-    int rc = check_ready_h(H);
+    int rc = check_ready_h(H, false);
     if (rc) return rc;
     if (!uold || !sold || !gpi) {
         set_error("uold, sold and gpi are required");

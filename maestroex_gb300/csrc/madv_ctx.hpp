@@ -74,6 +74,7 @@ struct Field {
     FieldSpec spec;
     double* base = nullptr;
     size_t bytes = 0;
+    bool deferred = false;  // storage not allocated yet: its views are empty
 };
 
 struct RegionTable {

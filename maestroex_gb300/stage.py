@@ -64,11 +64,10 @@ class MultiFab:
     def from_domain(self, arr, c0=0):
         """Copy a domain-sized array [nc, nz(+1), ny(+1), nx(+1)] into the valid regions."""
         t = arr if torch.is_tensor(arr) else torch.from_numpy(np.ascontiguousarray(arr))
-        t = t.to(self.fabs[0].device)
         nc = t.shape[0]
-        for b, f in enumerate(self.fabs):
+        for b, f in enumerate(self.fabs):  # box by box: no domain-sized copy on the device
             fs, ds = self._slices(b)
-            f[(slice(c0, c0 + nc),) + fs] = t[(slice(None),) + ds]
+            f[(slice(c0, c0 + nc),) + fs] = t[(slice(None),) + ds].to(f.device)
         return self
 
     def to_domain(self, domain_n, comps=None):
@@ -408,11 +407,11 @@ def amr_buffers(cfg, device="cuda"):
         buf = StageBuffers(c, device)
         P = cfg["levels"][lev - 1]
         for name in ("uold", "sold", "gpi", "thermal"):
-            src = torch.from_numpy(np.ascontiguousarray(P[name])).to(device)
+            src = torch.from_numpy(np.ascontiguousarray(P[name]))  # host: only parent blocks travel
             mf = getattr(buf, name)
             for b, bx in enumerate(mf.boxes):
                 i0, j0, k0, i1, j1, k1 = bx
-                blk = src[:, k0 // 2:(k1 + 1) // 2, j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2]
+                blk = src[:, k0 // 2:(k1 + 1) // 2, j0 // 2:(j1 + 1) // 2, i0 // 2:(i1 + 1) // 2].to(device)
                 blk = blk.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2).repeat_interleave(2, dim=3)
                 if name == "sold" and cfg.get("spherical"):
                     blk = _sph_rebin(blk, bx, c, P)

@@ -275,3 +275,37 @@ def test_caller_layouts_work_in_place_or_through_copies(mode):
             x, y = getattr(a, name)[d].to_domain(n), getattr(b, name)[d].to_domain(n)
             assert torch.equal(x, y), (name, d)
             assert torch.all(x[TEMP:PI + 1] == 0.0)
+
+
+def test_working_copies_allocated_at_first_use():
+    """A context whose stage calls work in the caller's FABs never allocates its own copies
+    of sold, snew, umac, sedge and sflux; the first entry point that needs them (EstDt here)
+    allocates them, and the stage's results stay the same bit for bit."""
+    import torch
+    from maestroex_gb300.stage import StageBuffers, make_stage
+    cfg = configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=1, seed=20261203 + 12)
+    st = make_stage(cfg)
+    a = StageBuffers(cfg).load(cfg)
+
+    def run():
+        a.load(cfg)
+        st.stage_forward(a.uold, a.sold, a.gpi, a.snew, a.umac, a.sedge, a.sflux, a.eta, thermal=a.thermal,
+                         mode=capi.MODE_GRAPH)
+        torch.cuda.synchronize()
+        return [t.clone() for t in a.snew.fabs] + [t.clone() for m in a.sflux for t in m.fabs]
+
+    first = run()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    a.load(cfg)
+    st.est_dt(a.uold, a.sold, a.gpi)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    nscal, g = 4 + cfg["nspec"], a.sold.ng
+    cells = sum((b[3] - b[0] + 1 + 2 * g) * (b[4] - b[1] + 1 + 2 * g) * (b[5] - b[2] + 1 + 2 * g)
+                for b in cfg["boxes"])
+    faces = sum((b[3] - b[0] + 2) * (b[4] - b[1] + 1) * (b[5] - b[2] + 1) for b in cfg["boxes"])
+    deferred = 8 * (2 * nscal * cells + 3 * 2 * nscal * faces)
+    assert free0 - free1 >= 0.9 * deferred, (free0 - free1, deferred)
+    second = run()
+    assert all(torch.equal(x, y) for x, y in zip(first, second))
