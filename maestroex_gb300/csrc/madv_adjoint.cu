@@ -12,8 +12,10 @@
 // adjoint FABs, which have the forward FABs' index spaces (and zero-filled margins
 // wherever a transpose reads one cell past the forward region).
 //
-// Scope: 3-D, one level, periodic domain, MAC velocities independent of the state
-// (grav_cell = 0, no pressure gradient, w0 = 0), so the velocity force is zero.  With
+// Scope: 3-D, one level, MAC velocities independent of the state
+// (grav_cell = 0, no pressure gradient, w0 = 0), so the velocity force is zero.  Periodic
+// domains; and for the state gradient alone also physical boundaries whose scalar BCs are
+// foextrap, reflect_even or reflect_odd (outflow, slip and no-slip walls, symmetry).  With
 // grav_cell = 0 the gradp0 of MakeRhoHForce is zero (below the cutoff it is rho0 g; above
 // it the reference differences the planar p0 across j, Source/MaestroForce.cpp:606-614),
 // so the rhoh forces' veladv term has no derivative.  The forward kernels mirrored here
@@ -46,6 +48,21 @@ __device__ __forceinline__ void upwind_w_vp(double tr, long long tb, double& wl,
     } else {
         wl = 0.5;
         wr = 0.5;
+    }
+}
+
+// The edge and transverse states of a scalar on a domain face with a physical boundary:
+// foextrap and reflect_even take the inside state (r on the low face, l on the high face),
+// reflect_odd gives zero (3-D blocks of Source/MaestroMakeEdgeScalars.cpp: predictor
+// :711-860, transverse :934-1340, edges :1456-1660).  ext_dir and hoextrap scalars are
+// rejected on the host.
+__device__ __forceinline__ void boundary_w(int I, int bclo, int bchi, int domlo, int domhi, double& wl, double& wr) {
+    if (I == domlo && bclo != BC_INT_DIR) {
+        wl = 0.0;
+        wr = bclo == BC_REFLECT_ODD ? 0.0 : 1.0;
+    } else if (I == domhi + 1 && bchi != BC_INT_DIR) {
+        wr = 0.0;
+        wl = bchi == BC_REFLECT_ODD ? 0.0 : 1.0;
     }
 }
 
@@ -134,7 +151,8 @@ __global__ void k_adj_flux(KARGS, int nspec, double dtdx, const double* __restri
 // transverse coefficients (F_TCOEF comps 3+t) into A_ATCOEF, from the forward transverse
 // states of this component (F_Q fields).
 template <int D>
-__global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long long epsb, int want_u) {
+__global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long long epsb, int want_u, int bclo,
+                               int bchi, int domlo, int domhi) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -144,6 +162,7 @@ __global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long
     const double ab = at(AW(A_AEDGE0 + D), i, j, k, comp);
     double wl, wr;
     upwind_w(at(VW(F_UMAC0 + D), i, j, k), epsb, wl, wr);
+    boundary_w(D == 0 ? i : (D == 1 ? j : k), bclo, bchi, domlo, domhi, wl, wr);
     const double la = wl * ab, ra = wr * ab;
     at(AW(A_ASL0 + D), i, j, k) += la;
     at(AW(A_ASR0 + D), i, j, k) += ra;
@@ -176,7 +195,7 @@ __global__ void k_adj_es_edges(KARGS, int comp, int force_zero, double dt2, long
 
 // k_es_transverse (advective form) transposed: D-faces corrected in direction T.
 template <int D, int T>
-__global__ void k_adj_es_transverse(KARGS, long long epsb, int want_u) {
+__global__ void k_adj_es_transverse(KARGS, long long epsb, int want_u, int bclo, int bchi, int domlo, int domhi) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
@@ -184,6 +203,7 @@ __global__ void k_adj_es_transverse(KARGS, long long epsb, int want_u) {
     const double qb = at(AW(AQ_SLOT(D, T)), i, j, k);
     double wl, wr;
     upwind_w(at(VW(F_UMAC0 + D), i, j, k), epsb, wl, wr);
+    boundary_w(D == 0 ? i : (D == 1 ? j : k), bclo, bchi, domlo, domhi, wl, wr);
     const double la = wl * qb, ra = wr * qb;
     at(AW(A_ASL0 + D), i, j, k) += la;
     at(AW(A_ASR0 + D), i, j, k) += ra;
@@ -200,15 +220,31 @@ __global__ void k_adj_es_transverse(KARGS, long long epsb, int want_u) {
     }
 }
 
-// k_es_predictor (ppm_type 1) transposed: simh = upwind(u, l, r, 0).
+// k_es_predictor (ppm_type 1) transposed: simh = upwind(u, l, r, 0).  On a domain face
+// with a physical boundary the forward set l, r and simh all to the inside state (r on the
+// low face, l on the high face; zero for reflect_odd), so that state takes all three
+// adjoints and the outside one none.
 template <int D>
-__global__ void k_adj_es_predictor(KARGS) {
+__global__ void k_adj_es_predictor(KARGS, int bclo, int bchi, int domlo, int domhi) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const double sb = at(AW(A_ASIMH0 + D), i, j, k);
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    double& la = at(AW(A_ASL0 + D), i, j, k);
+    double& ra = at(AW(A_ASR0 + D), i, j, k);
+    if (I == domlo && bclo != BC_INT_DIR) {
+        ra = bclo == BC_REFLECT_ODD ? 0.0 : ra + la + sb;
+        la = 0.0;
+        return;
+    }
+    if (I == domhi + 1 && bchi != BC_INT_DIR) {
+        la = bchi == BC_REFLECT_ODD ? 0.0 : la + ra + sb;
+        ra = 0.0;
+        return;
+    }
     double wl, wr;
     upwind_w(at(VW(F_UMAC0 + D), i, j, k), 0, wl, wr);
-    at(AW(A_ASL0 + D), i, j, k) += wl * sb;
-    at(AW(A_ASR0 + D), i, j, k) += wr * sb;
+    la += wl * sb;
+    ra += wr * sb;
 }
 
 // k_ppm_cell<D, 1, UMAC> transposed (cells of the box grown by one).  The predictors read
@@ -413,6 +449,38 @@ __global__ void k_adj_fill_boundary(const CopyDesc* __restrict__ D, int nd, long
         if (v != 0.0) atomicAdd(&at(src, i - cd.shift[0], j - cd.shift[1], k - cd.shift[2], n), v);
         g = 0.0;
     }
+}
+
+// FillPatch's physical-boundary fill of direction d (k_phys_fill) transposed, component n
+// of adjoint slot s: each ghost cell outside the domain in d hands its adjoint to the cell
+// it was copied from (foextrap: the boundary cell; reflect_even / odd: the mirror cell,
+// negated for odd) and is cleared, since the fill overwrote it.  The cells written are
+// inside the domain in d and the cells read outside, so one pass has no read-write
+// overlap; several ghost cells feeding one cell add atomically.  Run d = 2, 1, 0 (the
+// reverse of the forward's order: a corner filled by a later direction from a ghost cell of
+// an earlier one passes its adjoint on through that ghost cell), then FillBoundary^T.
+__global__ void k_adj_phys_fill(KARGS, int s, int n, BCRecD bc, int d, int domlo, int domhi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView q = AW(s);
+    const int m = d == 0 ? i : (d == 1 ? j : k);
+    const int side = m < domlo ? 0 : 1;
+    const int t = side == 0 ? bc.lo[d] : bc.hi[d];
+    if (t == BC_INT_DIR) return;
+    double& g = at(q, i, j, k, n);
+    const double a = g;
+    g = 0.0;
+    int p;
+    double w = 1.0;
+    if (t == BC_FOEXTRAP) {
+        p = side == 0 ? domlo : domhi;
+    } else if (t == BC_REFLECT_EVEN || t == BC_REFLECT_ODD) {
+        p = side == 0 ? 2 * domlo - 1 - m : 2 * domhi + 1 - m;
+        if (t == BC_REFLECT_ODD) w = -1.0;
+    } else {  // ext_dir: the ghost value does not depend on the state
+        return;
+    }
+    const int i2 = d == 0 ? p : i, j2 = d == 1 ? p : j, k2 = d == 2 ? p : k;
+    atomicAdd(&at(q, i2, j2, k2, n), w * a);
 }
 
 // ConvertRhoXToX transposed (valid cells): X = rhoX / rho.
@@ -628,21 +696,22 @@ void adj_flux(Ctx& c, int want_u) {
 }
 
 template <int D, int T>
-static void adj_transverse_launch(Ctx& c, long long eb, int want_u) {
+static void adj_transverse_launch(Ctx& c, long long eb, int want_u, const BCRecD& bc) {
     constexpr int O = 3 - D - T;
     int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
     glo[O] = 1;
     ghi[O] = 1;
     ghi[D] = 1;
     launch(c, region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1), 1, k_adj_es_transverse<D, T>, c.V(), eb,
-           want_u);
+           want_u, bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D]);
 }
 
 template <int D>
-static void adj_predictor_launch(Ctx& c) {
+static void adj_predictor_launch(Ctx& c, const BCRecD& bc) {
     int glo[3] = {1, 1, 1};
     glo[D] = 0;
-    launch(c, region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1), 1, k_adj_es_predictor<D>, c.V());
+    launch(c, region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1), 1, k_adj_es_predictor<D>, c.V(), bc.lo[D], bc.hi[D],
+           c.P.dom_lo[D], c.P.dom_hi[D]);
 }
 
 // PPM^T of component sc of field fs along D (ppm_type 1, interior form): adjoints of
@@ -671,18 +740,23 @@ static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, doubl
 void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes, int want_u) {
     const long long eb = dbits_host(c.P.rel_eps);
     const double dt2 = 0.5 * c.P.dt;
-    launch(c, rg_grow(c, 0, 0), 1, k_adj_es_edges<0>, c.V(), comp, force_zero, dt2, eb, want_u);
-    launch(c, rg_grow(c, 0, 1), 1, k_adj_es_edges<1>, c.V(), comp, force_zero, dt2, eb, want_u);
-    launch(c, rg_grow(c, 0, 2), 1, k_adj_es_edges<2>, c.V(), comp, force_zero, dt2, eb, want_u);
-    adj_transverse_launch<0, 1>(c, eb, want_u);
-    adj_transverse_launch<0, 2>(c, eb, want_u);
-    adj_transverse_launch<1, 0>(c, eb, want_u);
-    adj_transverse_launch<1, 2>(c, eb, want_u);
-    adj_transverse_launch<2, 0>(c, eb, want_u);
-    adj_transverse_launch<2, 1>(c, eb, want_u);
-    adj_predictor_launch<0>(c);
-    adj_predictor_launch<1>(c);
-    adj_predictor_launch<2>(c);
+    const BCRecD& bc = bcs_host(c, BCS_S)[comp];  // the forward's edge-state BCs of comp
+    const int *lo = c.P.dom_lo, *hi = c.P.dom_hi;
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_es_edges<0>, c.V(), comp, force_zero, dt2, eb, want_u, bc.lo[0], bc.hi[0],
+           lo[0], hi[0]);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_es_edges<1>, c.V(), comp, force_zero, dt2, eb, want_u, bc.lo[1], bc.hi[1],
+           lo[1], hi[1]);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_es_edges<2>, c.V(), comp, force_zero, dt2, eb, want_u, bc.lo[2], bc.hi[2],
+           lo[2], hi[2]);
+    adj_transverse_launch<0, 1>(c, eb, want_u, bc);
+    adj_transverse_launch<0, 2>(c, eb, want_u, bc);
+    adj_transverse_launch<1, 0>(c, eb, want_u, bc);
+    adj_transverse_launch<1, 2>(c, eb, want_u, bc);
+    adj_transverse_launch<2, 0>(c, eb, want_u, bc);
+    adj_transverse_launch<2, 1>(c, eb, want_u, bc);
+    adj_predictor_launch<0>(c, bc);
+    adj_predictor_launch<1>(c, bc);
+    adj_predictor_launch<2>(c, bc);
     adj_ppm_launch<0, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
     adj_ppm_launch<1, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
     adj_ppm_launch<2, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
@@ -694,6 +768,16 @@ void adj_fill_boundary(Ctx& c, int slot, int nc, int ng, int nodal) {
     unsigned grid = (unsigned)((ct.total + TPB - 1) / TPB);
     k_adj_fill_boundary<<<grid, TPB, 0, c.stream>>>(ct.d, (int)ct.h.size(), ct.total, c.V(), c.nb, F_USER + slot, nc);
     c.launches++;
+}
+
+// PhysBC^T of component n of adjoint slot `slot` (cell-centred, ng ghost cells) under the
+// BCs bc, the transpose of phys_fill: every non-periodic direction, last one first
+void adj_phys_fill(Ctx& c, int slot, int n, int ng, const BCRecD& bc) {
+    for (int d = 2; d >= 0; --d) {
+        if (c.per[d] || d >= c.ndim) continue;
+        launch(c, region(c, ng, ng, ng, ng, ng, ng, -1, d), 1, k_adj_phys_fill, c.V(), slot, n, bc, d,
+               c.P.dom_lo[d], c.P.dom_hi[d]);
+    }
 }
 
 void adj_convert_x(Ctx& c, int comp) { launch(c, rg_grow(c, 0), 1, k_adj_x, c.V(), comp); }

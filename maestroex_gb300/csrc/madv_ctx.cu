@@ -2251,12 +2251,21 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         set_error("madv_stage_adjoint: uold, sold0, weight, nsteps >= 1 and ckpt_interval >= 1 are required");
         return MADV_ERR_PARAM;
     }
-    if (c.ndim != 3 || !c.per[0] || !c.per[1] || !c.per[2] || c.P.ppm_type != 1 || c.P.species_pred_type != 1 ||
-        c.P.enthalpy_pred_type != 1) {
-        set_error("the adjoint covers 3-D periodic domains with ppm_type 1, species_pred_type 1 and "
-                  "enthalpy_pred_type 1");
+    if (c.ndim != 3 || c.P.ppm_type != 1 || c.P.species_pred_type != 1 || c.P.enthalpy_pred_type != 1) {
+        set_error("the adjoint covers 3-D domains with ppm_type 1, species_pred_type 1 and enthalpy_pred_type 1");
         return MADV_ERR_UNSUPPORTED;
     }
+    // physical boundaries: outflow and symmetry, whose scalar BCs (foextrap, reflect_even)
+    // fill ghost cells by copies; the velocity gradient needs a periodic domain
+    for (int d = 0; d < 3; ++d)
+        for (int pb : {c.P.phys_bc_lo[d], c.P.phys_bc_hi[d]}) {
+            if (pb == PB_INTERIOR) continue;
+            if ((pb != PB_OUTFLOW && pb != PB_SYMMETRY) || res->grad_u) {
+                set_error("the adjoint covers periodic, outflow and symmetry boundaries (the velocity gradient "
+                          "periodic ones only)");
+                return MADV_ERR_UNSUPPORTED;
+            }
+        }
     for (const char* nm : {"w0", "grav_cell"})
         for (double v : c.h1.at(nm))
             if (v != 0.0) {
@@ -2420,10 +2429,15 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
             c.dviews = vt[slot][comp];
             adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b, want_u);
             c.dviews = base_views;
+            // the traced field's and the force's FillPatch (BCS_F, the BC entries the
+            // forward's fills read), transposed
+            const BCRecD* bf = bcs_host(c, BCS_F);
+            adj_phys_fill(c, A_AS, 0, c.ng_s, bf[comp >= FIRSTSPEC ? comp - FIRSTSPEC : 0]);
             adj_fill_boundary(c, A_AS, 1, c.ng_s, -1);
             if (comp >= FIRSTSPEC) {
                 adj_convert_x(c, comp);
             } else {
+                adj_phys_fill(c, A_AFORCE, 0, 1, bf[0]);
                 adj_fill_boundary(c, A_AFORCE, 1, 1, -1);
                 adj_pert_force(c, comp, want_u);
             }

@@ -286,6 +286,7 @@ void adj_update(Ctx& c);
 void adj_flux(Ctx& c, int want_u);
 void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t dir_bytes, int want_u);
 void adj_fill_boundary(Ctx& c, int slot, int nc, int ng, int nodal);
+void adj_phys_fill(Ctx& c, int slot, int n, int ng, const BCRecD& bc);
 void adj_convert_x(Ctx& c, int comp);
 void adj_pert_force(Ctx& c, int comp, int want_u);
 void adj_tcoef(Ctx& c, int ts);

@@ -233,12 +233,16 @@ def test_member_functions_keep_uniform_fields(ppm_type):
             assert np.allclose(a[c], s0[c], rtol=1e-13, atol=0), c
 
 
-def test_tangent_linear_build_matches_finite_differences():
+@pytest.mark.parametrize("bc", ["periodic", "outflow_symmetry"])
+def test_tangent_linear_build_matches_finite_differences(bc):
     """The oracle's tangent-linear build (libmaestro_oracle_tl.so, the second reference of the
     GPU adjoint): its values equal the plain oracle's bit for bit, and its derivative along a
     single-cell direction equals central differences of two stage steps (h = 1e-6 |x|, with
-    the h/2 check that skips a limiter switch inside [x - h, x + h])."""
-    cfg = configs.adjoint_config(n=(16, 16, 16), max_grid=8, nspec=3)
+    the h/2 check that skips a limiter switch inside [x - h, x + h]).  With physical
+    boundaries the cells are drawn from the two layers next to the domain faces."""
+    from maestroex_gb300.params import INTERIOR, OUTFLOW, SYMMETRY
+    kw = {} if bc == "periodic" else dict(bc_lo=(SYMMETRY, INTERIOR, OUTFLOW), bc_hi=(OUTFLOW, INTERIOR, SYMMETRY))
+    cfg = configs.adjoint_config(n=(16, 16, 16), max_grid=8, nspec=3, **kw)
     S, U = cfg["sold"], cfg["uold"]
     comps = [RHO, RHOH] + list(range(FIRSTSPEC, S.shape[0]))
     snew, dsnew = pyoracle.run_stage_tl(cfg, np.zeros_like(U), np.zeros_like(S))
@@ -250,6 +254,8 @@ def test_tangent_linear_build_matches_finite_differences():
     for t in range(8):
         comp = comps[t % len(comps)]
         i, j, k = (int(v) for v in rng.integers(0, 16, 3))
+        if bc != "periodic":
+            i, k = (int(rng.choice([0, 1, 14, 15])) for _ in range(2))
         dS = np.zeros_like(S)
         dS[comp, k, j, i] = 1.0
         _, ds = pyoracle.steps_tl(cfg, S, dS, U, np.zeros_like(U), 2)
