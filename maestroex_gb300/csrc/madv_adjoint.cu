@@ -12,7 +12,7 @@
 // adjoint FABs, which have the forward FABs' index spaces (and zero-filled margins
 // wherever a transpose reads one cell past the forward region).
 //
-// Scope: 3-D, one level, MAC velocities independent of the state
+// Scope: 3-D, one level, plane-parallel or spherical, MAC velocities independent of the state
 // (grav_cell = 0, no pressure gradient, w0 = 0), so the velocity force is zero.  Periodic
 // domains; and for the state gradient alone also physical boundaries whose scalar BCs are
 // foextrap, reflect_even or reflect_odd (outflow, slip and no-slip walls, symmetry).  With
@@ -112,7 +112,7 @@ __global__ void k_adj_update(KARGS, int nspec) {
 template <int D>
 __global__ void k_adj_flux(KARGS, int nspec, double dtdx, const double* __restrict__ r0a,
                            const double* __restrict__ r0b, const double* __restrict__ h0a,
-                           const double* __restrict__ h0b, int want_u) {
+                           const double* __restrict__ h0b, int want_u, int sph) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const RegionBox& rr = R[e_];
@@ -127,7 +127,11 @@ __global__ void k_adj_flux(KARGS, int nspec, double dtdx, const double* __restri
         if (cell_lo) a -= at(an, i - di, j - dj, k - dk, comp);
         return dtdx * a;
     };
-    const double erho = 0.5 * (r0a[k] + r0b[k]) + at(e, i, j, k, RHO);
+    // rho0_edge: planar, the old and new edge base state of row k; spherical, MakeS0mac's
+    // face values of the two (F_S0MAC*, F_S0MACB*), combined as k_rhox_flux_sph does
+    const double r0f = sph ? 0.5 * at(VW(F_S0MAC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACB0 + D), i, j, k)
+                           : 0.5 * (r0a[k] + r0b[k]);
+    const double erho = r0f + at(e, i, j, k, RHO);
     const double cx = u * erho;
     double arho = 0.0, gu = 0.0;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
@@ -690,9 +694,10 @@ void adj_flux(Ctx& c, int want_u) {
     const double *r0 = c.b1("rho0_old"), *r0e = c.b1("rho0_edge_old");
     const double *h0 = c.b1("rhoh0_old"), *h0e = c.b1("rhoh0_edge_old");
     const int ns = c.nspec;
-    launch(c, rg_grow(c, 0, 0), 1, k_adj_flux<0>, c.V(), ns, c.P.dt / c.P.dx[0], r0, r0, h0, h0, want_u);
-    launch(c, rg_grow(c, 0, 1), 1, k_adj_flux<1>, c.V(), ns, c.P.dt / c.P.dx[1], r0, r0, h0, h0, want_u);
-    launch(c, rg_grow(c, 0, 2), 1, k_adj_flux<2>, c.V(), ns, c.P.dt / c.P.dx[2], r0e, r0e, h0e, h0e, want_u);
+    const int sph = c.sph ? 1 : 0;
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_flux<0>, c.V(), ns, c.P.dt / c.P.dx[0], r0, r0, h0, h0, want_u, sph);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_flux<1>, c.V(), ns, c.P.dt / c.P.dx[1], r0, r0, h0, h0, want_u, sph);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_flux<2>, c.V(), ns, c.P.dt / c.P.dx[2], r0e, r0e, h0e, h0e, want_u, sph);
 }
 
 template <int D, int T>

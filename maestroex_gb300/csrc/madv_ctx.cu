@@ -2419,6 +2419,12 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         put_in_pert_form_h(H, "rho0_old", RHO, 0, BCS_F, 1);
         put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
         edge_scal_coeffs(c);
+        // spherical: the face base state of the density fluxes (which_step 1: rho0_old for
+        // both of MakeRhoXFlux's old and new)
+        if (c.sph) {
+            make_s0mac_h(H, "rho0_old", F_S0MAC0);
+            make_s0mac_h(H, "rho0_old", F_S0MACB0);
+        }
         adj_update(c);
         adj_flux(c, want_u);
         for (int comp = 0; comp < ns; ++comp) {

@@ -15,9 +15,12 @@ pytestmark = pytest.mark.gpu
 
 
 class Case:
-    def __init__(self, n=(32, 32, 32), max_grid=16, nspec=3, nsteps=4, ckpt=2, seed=20261203 + 4, bc=None):
+    def __init__(self, n=(32, 32, 32), max_grid=16, nspec=3, nsteps=4, ckpt=2, seed=20261203 + 4, bc=None, cfg=None):
         kw = {} if bc is None else dict(bc_lo=bc[0], bc_hi=bc[1])
-        self.cfg = cfg = configs.adjoint_config(n=n, max_grid=max_grid, nspec=nspec, seed=seed, **kw)
+        if cfg is None:
+            cfg = configs.adjoint_config(n=n, max_grid=max_grid, nspec=nspec, seed=seed, **kw)
+        self.cfg = cfg
+        n, nspec = cfg["n"], cfg["nspec"]
         self.n, self.boxes, self.nscal = cfg["n"], cfg["boxes"], 4 + nspec
         self.nsteps, self.ckpt = nsteps, ckpt
         self.st = make_stage(cfg)
@@ -266,6 +269,40 @@ NON_PERIODIC = {
     "outflow": ((OUTFLOW,) * 3, (OUTFLOW,) * 3),
     "mixed": ((SYMMETRY, INTERIOR, OUTFLOW), (OUTFLOW, INTERIOR, SYMMETRY)),
 }
+
+
+def spherical_adjoint_config(n=32, nspec=3, max_grid=16):
+    """Full-star spherical configuration (exact base state, outflow on every face) with a
+    state-independent MAC velocity: w0 = 0, no gravity, ppm_type 1."""
+    cfg = configs.spherical_config(n=n, nspec=nspec, ppm_type=1, max_grid=max_grid, w0_amp=0.0)
+    cfg["grav_cell"] = np.zeros_like(cfg["grav_cell"])
+    return cfg
+
+
+def tl_dot(case, G, vs):
+    import pyoracle
+    S, U = case.cfg["sold"], case.cfg["uold"]
+    _, ds = pyoracle.steps_tl(case.cfg, S, vs, U, np.zeros_like(U), case.nsteps)
+    return float((case.w * ds).sum()), float((G * vs).sum()), float(np.abs(G * vs).sum())
+
+
+def test_spherical_adjoint_matches_cpu_tangent_linear_model():
+    """Spherical geometry (32^3 full star in 8 boxes, outflow faces): the density fluxes'
+    face base state of MakeS0mac in the flux transpose; the rest of the transposes are the
+    plane-parallel ones.  Dot-product check against the oracle's tangent-linear build over
+    every cell, and over the cells of the star's ambient/surface shell alone."""
+    case = Case(cfg=spherical_adjoint_config())
+    J, grad, _, _ = case.adjoint()
+    G = grad.to_domain(case.n).cpu().numpy()
+    S = case.cfg["sold"]
+    rng = np.random.default_rng(2028)
+    vs = rng.standard_normal(S.shape) * np.sqrt((S ** 2).mean(axis=(1, 2, 3), keepdims=True))
+    tl, adj, scale = tl_dot(case, G, vs)
+    print(f"spherical: tangent-linear {tl:.15e}, adjoint {adj:.15e}, diff / sum|terms| {abs(tl - adj) / scale:.2e}")
+    assert abs(tl - adj) <= 1e-10 * scale
+    shell = (S[RHO] < 1e-3 * S[RHO].max())[None]
+    tl, adj, scale = tl_dot(case, G, vs * shell)
+    assert abs(tl - adj) <= 1e-10 * scale
 
 
 @pytest.mark.parametrize("bc", sorted(NON_PERIODIC))
