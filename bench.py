@@ -421,6 +421,99 @@ def run_adjoint(args, barrier):
     }
 
 
+def run_spherical_adjoint(args, barrier):
+    """Spherical multi-step adjoint: a full star on one level, n^3 in boxes of 64^3, NumSpec
+    21, ppm_type 1, outflow faces, the velocity held fixed and independent of the state
+    (w0 = 0, no gravity), 8 steps with the state stored every 4.  Times the forward alone and
+    the adjoint for dJ/d(state) (which runs its own forward), and checks three gradient
+    entries inside the star against central differences of the same forward."""
+    import torch
+    from maestroex_gb300 import configs
+    from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
+    from maestroex_gb300.stage import MultiFab, make_stage
+    n, nsteps, ckpt = args.sph_adj_n, 8, 4
+    cfg = configs.spherical_config(n=n, nspec=21, ppm_type=1, max_grid=min(64, n), w0_amp=0.0)
+    cfg["grav_cell"] = np.zeros_like(cfg["grav_cell"])
+    st = make_stage(cfg)
+    boxes, nscal = cfg["boxes"], 4 + cfg["nspec"]
+    u = MultiFab(boxes, 3, 0).from_domain(cfg["uold"])
+    s0 = MultiFab(boxes, nscal, 0).from_domain(cfg["sold"])
+    rng = np.random.default_rng(20261203 + 60)
+    w = np.zeros_like(cfg["sold"])
+    w[RHOH] = rng.normal(size=w[RHOH].shape)
+    w[FIRSTSPEC:] = rng.normal(size=w[FIRSTSPEC:].shape)
+    wt = MultiFab(boxes, nscal, 0).from_domain(w)
+    gs, sf = MultiFab(boxes, nscal, 0), MultiFab(boxes, nscal, 0)
+
+    def call(grad):
+        return st.stage_adjoint(u, s0, wt, nsteps, ckpt, grad_s=gs if grad else None, sfinal=sf)
+
+    def timed(grad, reps):
+        call(grad)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record()
+            J, nbytes = call(grad)
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps, J, nbytes
+
+    reps = max(1, args.steps // 2)
+    ms_fwd, _, _ = timed(False, reps)
+    ms_adj, J, nbytes = timed(True, reps)
+    G = gs.to_domain(cfg["n"]).cpu().numpy()
+    S = cfg["sold"]
+
+    def final(ss):
+        out = MultiFab(boxes, nscal, 0)
+        st.stage_adjoint(u, ss, wt, nsteps, ckpt, sfinal=out)
+        return out
+
+    def perturbed(comp, cell, h):
+        m = MultiFab(boxes, nscal, 0)
+        for a, b in zip(m.fabs, s0.fabs):
+            a.copy_(b)
+        i, j, k = cell
+        for bi, bx in enumerate(boxes):
+            if bx[0] <= i <= bx[3] and bx[1] <= j <= bx[4] and bx[2] <= k <= bx[5]:
+                m.fabs[bi][comp, k - bx[2], j - bx[1], i - bx[0]] += h
+        return m
+
+    checks, worst, kinks = [], 0.0, 0
+    rms = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
+    for comp in (RHOH, FIRSTSPEC, RHO):
+        # a cell inside the star, within a quarter radius of the centre
+        cell = tuple(int(v) for v in n // 2 + rng.integers(-n // 10, n // 10 + 1, size=3))
+        i, j, k = cell
+        x = max(abs(S[comp, k, j, i]), 0.1 * rms[comp])
+        fd = []
+        for rel in (1e-6, 0.5e-6):
+            h = rel * x
+            a, b = final(perturbed(comp, cell, h)), final(perturbed(comp, cell, -h))
+            fd.append(sum(float((x_ * (p - q)).sum()) for x_, p, q in zip(wt.fabs, a.fabs, b.fabs)) / (2 * h))
+        scale = max(abs(fd[0]), abs(fd[1]))
+        if abs(fd[0] - fd[1]) > 1e-5 * scale:
+            kinks += 1
+            continue
+        err = abs(G[comp, k, j, i] - fd[0]) / max(scale, 1e-300)
+        worst = max(worst, err)
+        checks.append(err)
+    st.close()
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"spherical full star, one level {n}^3 in {len(boxes)} boxes of {min(64, n)}^3, NumSpec 21, "
+                    f"ppm_type 1, outflow, exact base state, w0 = 0 and no gravity (the velocity held fixed), "
+                    f"{nsteps} steps, stored states every {ckpt}; J = sum(w rhoX + v rhoh_final), w, v ~ N(0,1)",
+        "fwd_ms": ms_fwd, "adj_state_ms": ms_adj, "adj_over_fwd_state": ms_adj / ms_fwd, "device_bytes": nbytes,
+        "J": J,
+        "fd_check": {"entries": len(checks), "skipped_limiter_switch": kinks, "worst_rel_err": worst},
+    }
+
+
 def run_spherical(args, barrier):
     """Full-star spherical workload: two levels, level 0 n^3 in uneven
     boxes (edges 16-128), level 1 (ratio 2) 16-64-cell boxes around 3 seeded bubbles, NumSpec
@@ -612,6 +705,8 @@ def main():
     ap.add_argument("--sph-cover", type=float, default=0.06,
                     help="bubble radius parameter of the spherical workload's level 1 (0.06: about 11%% of the domain)")
     ap.add_argument("--no-spherical", action="store_true")
+    ap.add_argument("--no-sph-adjoint", action="store_true")
+    ap.add_argument("--sph-adj-n", type=int, default=128, help="extent of the spherical adjoint workload")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
     args = ap.parse_args()
@@ -782,6 +877,7 @@ def main():
     two_d = None if args.no_2d else run_2d(args, barrier)
     vel = None if args.no_velocity else run_velocity(args, barrier)
     sph = None if args.no_spherical else run_spherical(args, barrier)
+    sph_adj = None if args.no_sph_adjoint else run_spherical_adjoint(args, barrier)
 
     if rank != 0:
         dist.destroy_process_group()
@@ -833,6 +929,8 @@ def main():
         line["velocity_advance"] = vel
     if sph is not None:
         line["spherical"] = sph
+    if sph_adj is not None:
+        line["spherical_adjoint"] = sph_adj
     if not args.no_cpu_baseline:
         cb = run_cpu_baseline(3, 1, nthreads=os.cpu_count() or 1)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
