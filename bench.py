@@ -425,7 +425,7 @@ def run_spherical_adjoint(args, barrier):
     """Spherical multi-step adjoint: a full star on one level, n^3 in boxes of 64^3, NumSpec
     21, ppm_type 1, outflow faces, the velocity held fixed and independent of the state
     (w0 = 0, no gravity), 8 steps with the state stored every 4.  Times the forward alone and
-    the adjoint for dJ/d(state) (which runs its own forward), and checks three gradient
+    the adjoint for dJ/d(state) (which runs its own forward), and checks eight gradient
     entries inside the star against central differences of the same forward."""
     import torch
     from maestroex_gb300 import configs
@@ -485,9 +485,9 @@ def run_spherical_adjoint(args, barrier):
 
     checks, worst, kinks = [], 0.0, 0
     rms = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
-    for comp in (RHOH, FIRSTSPEC, RHO):
-        # a cell inside the star, within a quarter radius of the centre
-        cell = tuple(int(v) for v in n // 2 + rng.integers(-n // 10, n // 10 + 1, size=3))
+    for comp in (RHOH, FIRSTSPEC, RHO, RHOH, FIRSTSPEC + 5, RHO, FIRSTSPEC + 11, RHOH):
+        # a cell inside the star, within about half its radius of the centre
+        cell = tuple(int(v) for v in n // 2 + rng.integers(-n // 5, n // 5 + 1, size=3))
         i, j, k = cell
         x = max(abs(S[comp, k, j, i]), 0.1 * rms[comp])
         fd = []

@@ -13,7 +13,8 @@
 // wherever a transpose reads one cell past the forward region).
 //
 // Scope: 3-D, one level, plane-parallel or spherical, MAC velocities independent of the state
-// (grav_cell = 0, no pressure gradient, w0 = 0), so the velocity force is zero.  Periodic
+// (grav_cell = 0, no pressure gradient), so the velocity force has no state term; w0 may be
+// non-zero for the state gradient (the gradient with respect to the velocity needs w0 = 0).  Periodic
 // domains; and for the state gradient alone also physical boundaries whose scalar BCs are
 // foextrap, reflect_even or reflect_odd (outflow, slip and no-slip walls, symmetry).  With
 // grav_cell = 0 the gradp0 of MakeRhoHForce is zero (below the cutoff it is rho0 g; above
@@ -507,12 +508,22 @@ __global__ void k_adj_x(KARGS, int comp) {
 // the forward read from its Cartesian copy: above the top cell that is the ghost cell
 // FillPatch filled, in a periodic domain the image of the bottom edge.
 __global__ void k_adj_pert(KARGS, int comp, const double* __restrict__ s0a, const double* __restrict__ s0e,
-                           RecipC r0, RecipC r1, RecipC r2, int domlo, int domhi, int want_u) {
+                           RecipC r0, RecipC r1, RecipC r2, int domlo, int domhi, int want_u,
+                           const double* __restrict__ w0, int sph) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
-    const double du = div_c(at(um, i + 1, j, k) - at(um, i, j, k), r0);
-    const double dv = div_c(at(vm, i, j + 1, k) - at(vm, i, j, k), r1);
-    const double divu = du + dv + div_c(at(wm, i, j, k + 1) - at(wm, i, j, k), r2);
+    // ModifyScalForce runs between Addw0(-1) and Addw0(+1): its umac is the MAC velocity
+    // without w0 (planar: w0 on the z faces; spherical: w0mac on every face)
+    auto U = [&](const FabView& f, int d, int a, int bb, int cc) {
+        const double v = at(f, a, bb, cc);
+        if (sph) return v + -1.0 * at(VW(F_W0MAC0 + d), a, bb, cc);
+        return d == 2 ? v + -1.0 * w0[cc] : v;
+    };
+    const double du = div_c(U(um, 0, i + 1, j, k) - U(um, 0, i, j, k), r0);
+    const double dv = div_c(U(vm, 1, i, j + 1, k) - U(vm, 1, i, j, k), r1);
+    double divu = du + dv + div_c(U(wm, 2, i, j, k + 1) - U(wm, 2, i, j, k), r2);
+    // planar: ModifyScalForce adds the divergence of w0_cart (Source/MaestroForce.cpp:413-441)
+    if (!sph) divu += div_c(at(VW(F_W0CART), i, j, k + 1, 2) - at(VW(F_W0CART), i, j, k, 2), r2);
     const double fb = at(AW(A_AFORCE), i, j, k);
     at(AW(A_ASOLD), i, j, k, comp) += at(AW(A_AS), i, j, k) - divu * fb;
     if (want_u && fb != 0.0) {
@@ -791,7 +802,7 @@ void adj_pert_force(Ctx& c, int comp, int want_u) {
     const double* s0 = c.b1(comp == RHO ? "rho0_old" : "rhoh0_old");
     const double* s0e = c.b1(comp == RHO ? "rho0_edge_old" : "rhoh0_edge_old");
     launch(c, rg_grow(c, 0), 1, k_adj_pert, c.V(), comp, s0, s0e, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
-           make_recip(c.P.dx[2]), c.P.dom_lo[2], c.P.dom_hi[2], want_u);
+           make_recip(c.P.dx[2]), c.P.dom_lo[2], c.P.dom_hi[2], want_u, c.b1("w0"), c.sph ? 1 : 0);
 }
 
 // F_TCOEF^T into face slots ts .. ts+2 (A_AUMAC0 or A_AUTRANS0)

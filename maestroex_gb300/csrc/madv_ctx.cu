@@ -2266,10 +2266,15 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
                 return MADV_ERR_UNSUPPORTED;
             }
         }
-    for (const char* nm : {"w0", "grav_cell"})
-        for (double v : c.h1.at(nm))
+    for (double v : c.h1.at("grav_cell"))
+        if (v != 0.0) {
+            set_error("the adjoint needs grav_cell = 0 (MAC velocities independent of the state)");
+            return MADV_ERR_UNSUPPORTED;
+        }
+    if (res->grad_u)
+        for (double v : c.h1.at("w0"))
             if (v != 0.0) {
-                set_error("the adjoint needs w0 = 0 and grav_cell = 0 (MAC velocities independent of the state)");
+                set_error("the adjoint's velocity gradient needs w0 = 0");
                 return MADV_ERR_UNSUPPORTED;
             }
     const int ns = c.nscal, K = sd->ckpt_interval, N = sd->nsteps;
@@ -2367,9 +2372,36 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         }
     } views_guard{c, base_views};
     std::vector<std::vector<FabView*>> vt(tape.size(), std::vector<FabView*>(ns, nullptr));
+    // With w0 != 0 the stage ends with umac - w0 in F_UMAC, while the edge states and fluxes
+    // saw umac + w0 (the density and the enthalpy halves each form it once).  The velocity is
+    // the same in every step: the first taped forward step keeps both, and the reverse
+    // steps put them back, so every upwind and tracing decision is the forward's.
+    bool has_w0 = false;
+    for (double v : c.h1.at("w0")) has_w0 |= v != 0.0;
+    std::array<std::array<double*, 3>, 2> umac_keep{};
+    if (rev && has_w0)
+        for (auto& a : umac_keep)
+            for (int d = 0; d < 3; ++d) a[d] = W.alloc(c.F[F_UMAC0 + d].bytes);
+    auto keep_umac = [&](int which) {
+        for (int d = 0; d < 3; ++d)
+            cudaMemcpyAsync(umac_keep[which][d], c.F[F_UMAC0 + d].base, c.F[F_UMAC0 + d].bytes, DD, c.stream);
+    };
+    auto put_umac = [&](int which) {
+        if (!has_w0) return;
+        for (int d = 0; d < 3; ++d)
+            cudaMemcpyAsync(c.F[F_UMAC0 + d].base, umac_keep[which][d], c.F[F_UMAC0 + d].bytes, DD, c.stream);
+        edge_scal_coeffs(c);
+    };
+    bool umac_kept = false;
     auto tape_on = [&](int slot) {
         if (!rev) return;
-        c.edge_tape_begin = [&, slot](int comp) { c.dviews = vt[slot][comp]; };
+        c.edge_tape_begin = [&, slot](int comp) {
+            if (has_w0 && !umac_kept && (comp == FIRSTSPEC || comp == RHOH)) {
+                keep_umac(comp == RHOH ? 1 : 0);
+                umac_kept = comp == RHOH;
+            }
+            c.dviews = vt[slot][comp];
+        };
         c.edge_tape = [&](int) { c.dviews = base_views; };
     };
     auto tape_off = [&]() {
@@ -2419,6 +2451,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         put_in_pert_form_h(H, "rho0_old", RHO, 0, BCS_F, 1);
         put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
         edge_scal_coeffs(c);
+        put_umac(0);  // the density half's MAC velocity (w0 != 0)
         // spherical: the face base state of the density fluxes (which_step 1: rho0_old for
         // both of MakeRhoXFlux's old and new)
         if (c.sph) {
@@ -2430,6 +2463,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         for (int comp = 0; comp < ns; ++comp) {
             if (comp == TEMP || comp == PI) continue;
             cudaMemsetAsync(scr, 0, scr_b, c.stream);
+            if (comp == RHOH) put_umac(1);  // the enthalpy half's (w0 != 0)
             // this component's interface values (and for the velocity adjoint its
             // transverse states) as the forward formed them, read from the tape
             c.dviews = vt[slot][comp];
@@ -2447,6 +2481,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
                 adj_fill_boundary(c, A_AFORCE, 1, 1, -1);
                 adj_pert_force(c, comp, want_u);
             }
+            if (comp == RHOH) put_umac(0);
         }
         copy_fab(c, F_USER + A_ASNEW, 0, F_USER + A_ASOLD, 0, ns, 0);
         cudaMemsetAsync(asold, 0, st_b, c.stream);

@@ -271,10 +271,10 @@ NON_PERIODIC = {
 }
 
 
-def spherical_adjoint_config(n=32, nspec=3, max_grid=16):
+def spherical_adjoint_config(n=32, nspec=3, max_grid=16, w0_amp=0.0):
     """Full-star spherical configuration (exact base state, outflow on every face) with a
-    state-independent MAC velocity: w0 = 0, no gravity, ppm_type 1."""
-    cfg = configs.spherical_config(n=n, nspec=nspec, ppm_type=1, max_grid=max_grid, w0_amp=0.0)
+    state-independent MAC velocity: no gravity, ppm_type 1, w0 of amplitude w0_amp."""
+    cfg = configs.spherical_config(n=n, nspec=nspec, ppm_type=1, max_grid=max_grid, w0_amp=w0_amp)
     cfg["grav_cell"] = np.zeros_like(cfg["grav_cell"])
     return cfg
 
@@ -286,12 +286,14 @@ def tl_dot(case, G, vs):
     return float((case.w * ds).sum()), float((G * vs).sum()), float(np.abs(G * vs).sum())
 
 
-def test_spherical_adjoint_matches_cpu_tangent_linear_model():
+@pytest.mark.parametrize("w0_amp", [0.0, 1.0e5])
+def test_spherical_adjoint_matches_cpu_tangent_linear_model(w0_amp):
     """Spherical geometry (32^3 full star in 8 boxes, outflow faces): the density fluxes'
     face base state of MakeS0mac in the flux transpose; the rest of the transposes are the
-    plane-parallel ones.  Dot-product check against the oracle's tangent-linear build over
-    every cell, and over the cells of the star's ambient/surface shell alone."""
-    case = Case(cfg=spherical_adjoint_config())
+    plane-parallel ones; with w0 != 0 the force transpose takes the MAC velocity without
+    w0mac, as ModifyScalForce does.  Dot-product check against the oracle's tangent-linear
+    build over every cell, and over the cells of the star's ambient/surface shell alone."""
+    case = Case(cfg=spherical_adjoint_config(w0_amp=w0_amp))
     J, grad, _, _ = case.adjoint()
     G = grad.to_domain(case.n).cpu().numpy()
     S = case.cfg["sold"]
@@ -332,3 +334,25 @@ def test_non_periodic_adjoint_matches_cpu_tangent_linear_model(bc):
     _, dsb = pyoracle.steps_tl(case.cfg, S, vb, U, np.zeros_like(U), case.nsteps)
     tlb, adjb = float((case.w * dsb).sum()), float((G * vb).sum())
     assert abs(tlb - adjb) <= 1e-10 * float(np.abs(G * vb).sum())
+
+
+def test_planar_adjoint_with_w0_matches_cpu_tangent_linear_model():
+    """Plane-parallel, w0 != 0 (amplitude 1e4 cm/s): the MAC velocity carries w0 on the z
+    faces in the edge states and fluxes and not in ModifyScalForce.  Dot-product check of the
+    state gradient against the oracle's tangent-linear build; the velocity gradient is
+    rejected with w0 != 0."""
+    cfg = configs.adjoint_config(n=(32, 32, 32), max_grid=16, nspec=3, w0_amp=1.0e4,
+                                 bc_lo=(INTERIOR, INTERIOR, OUTFLOW), bc_hi=(INTERIOR, INTERIOR, OUTFLOW))
+    assert np.abs(cfg["w0"]).max() > 0.0
+    case = Case(cfg=cfg)
+    J, grad, _, _ = case.adjoint()
+    G = grad.to_domain(case.n).cpu().numpy()
+    S = case.cfg["sold"]
+    rng = np.random.default_rng(2029)
+    vs = rng.standard_normal(S.shape) * np.sqrt((S ** 2).mean(axis=(1, 2, 3), keepdims=True))
+    tl, adj, scale = tl_dot(case, G, vs)
+    print(f"planar w0: tangent-linear {tl:.15e}, adjoint {adj:.15e}, diff / sum|terms| {abs(tl - adj) / scale:.2e}")
+    assert abs(tl - adj) <= 1e-10 * scale
+    with pytest.raises(MadvError) as e:
+        case.adjoint(want_u=True)
+    assert e.value.code == -3
