@@ -325,10 +325,12 @@ int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_f
  * and upwind decisions frozen; states are stored every ckpt_interval steps and each
  * block is recomputed from its stored state, so memory grows with nsteps/ckpt_interval
  * + ckpt_interval states.  No counterpart in the reference.
- * Scope: one level, 3-D, periodic in every direction, ppm_type 1, species_pred_type 1,
- * enthalpy_pred_type 1, and w0 = 0, grav_cell = 0 so that the MAC velocities do not depend
- * on the state (MADV_ERR_UNSUPPORTED otherwise).  The UpdateScal floor and
- * negative-species branches are taken as not active. */
+ * Scope: one level, 3-D, plane-parallel or spherical, ppm_type 1, species_pred_type 1,
+ * enthalpy_pred_type 1, and grav_cell = 0 so that the MAC velocities do not depend on the
+ * state.  The state gradient (grad_s) also allows outflow and symmetry boundaries and
+ * w0 != 0.  The velocity gradient (grad_u) needs a periodic domain and w0 = 0.  Anything
+ * else returns MADV_ERR_UNSUPPORTED.  The UpdateScal floor and negative-species branches
+ * are taken as not active. */
 typedef struct {
     int nsteps;                  /* advection steps (>= 1) */
     int ckpt_interval;           /* steps between stored states (>= 1) */
