@@ -327,8 +327,8 @@ int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_f
  * + ckpt_interval states.  No counterpart in the reference.
  * Scope: one level, 3-D, plane-parallel or spherical, ppm_type 1, species_pred_type 1,
  * enthalpy_pred_type 1, and grav_cell = 0 so that the MAC velocities do not depend on the
- * state.  The state gradient (grad_s) also allows outflow and symmetry boundaries and
- * w0 != 0.  The velocity gradient (grad_u) needs a periodic domain and w0 = 0.  Anything
+ * state.  The state gradient (grad_s) also allows outflow, symmetry and wall boundaries
+ * and w0 != 0.  The velocity gradient (grad_u) needs a periodic domain and w0 = 0.  Anything
  * else returns MADV_ERR_UNSUPPORTED.  The UpdateScal floor and negative-species branches
  * are taken as not active. */
 typedef struct {

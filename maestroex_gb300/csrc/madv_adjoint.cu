@@ -15,8 +15,8 @@
 // Scope: 3-D, one level, plane-parallel or spherical, MAC velocities independent of the state
 // (grav_cell = 0, no pressure gradient), so the velocity force has no state term; w0 may be
 // non-zero for the state gradient (the gradient with respect to the velocity needs w0 = 0).  Periodic
-// domains; and for the state gradient alone also physical boundaries whose scalar BCs are
-// foextrap, reflect_even or reflect_odd (outflow, slip and no-slip walls, symmetry).  With
+// domains; and for the state gradient alone also outflow, symmetry and wall boundaries
+// (scalar BCs foextrap, reflect_even, hoextrap: PPM's boundary stencils transposed).  With
 // grav_cell = 0 the gradp0 of MakeRhoHForce is zero (below the cutoff it is rho0 g; above
 // it the reference differences the planar p0 across j, Source/MaestroForce.cpp:606-614),
 // so the rhoh forces' veladv term has no derivative.  The forward kernels mirrored here
@@ -252,6 +252,42 @@ __global__ void k_adj_es_predictor(KARGS, int bclo, int bchi, int domlo, int dom
     ra += wr * sb;
 }
 
+// The interior face value of ppm_type 1 transposed, face f between cells f-1 and f
+// (face = the cell (i,j,k) of index f along D): v = clamp(v0) between the two cells,
+// v0 = (s(f) + s(f-1))/2 - (dv(f) - dv(f-1))/6, the clamp decided as the forward decides it
+// (mn(a, b) = (b < a) ? b : a, mx(a, b) = (a < b) ? b : a).  v0 is formed with the forward's
+// expression: half() for the stored faces, 0.5 * () for the ones a ghost cell recomputes.
+// Adjoint fb to the two cells (slot as, component tc) and the slopes (A_ADSVL).
+template <int D>
+__device__ __forceinline__ void adj_face_regular(const FabView* __restrict__ V, int nb, int b, const FabView& s, int sc,
+                                                 const FabView& dv, const FabView& as, int tc, int i, int j, int k,
+                                                 double fb, const RecipC& r6, bool halved) {
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const double sl = at(s, i - di, j - dj, k - dk, sc), s0 = at(s, i, j, k, sc);
+    const double sum = s0 + sl;
+    const double v0 = (halved ? half(sum) : 0.5 * sum) - div_c(at(dv, i, j, k) - at(dv, i - di, j - dj, k - dk), r6);
+    const double lo = mn(s0, sl), hi = mx(s0, sl);
+    int src = 0;  // 0: v0, 1: s0, 2: s-1
+    double v = v0;
+    if (v < lo) {
+        v = lo;
+        src = (sl < s0) ? 2 : 1;
+    }
+    if (hi < v) src = (s0 < sl) ? 2 : 1;
+    if (src == 0) {
+        atomicAdd(&at(as, i, j, k, tc), 0.5 * fb);
+        atomicAdd(&at(as, i - di, j - dj, k - dk, tc), 0.5 * fb);
+        const FabView ad = AW(A_ADSVL);
+        const double f6 = div_c(fb, r6);
+        atomicAdd(&at(ad, i, j, k), -f6);
+        atomicAdd(&at(ad, i - di, j - dj, k - dk), f6);
+    } else if (src == 1) {
+        atomicAdd(&at(as, i, j, k, tc), fb);
+    } else {
+        atomicAdd(&at(as, i - di, j - dj, k - dk, tc), fb);
+    }
+}
+
 // k_ppm_cell<D, 1, UMAC> transposed (cells of the box grown by one).  The predictors read
 // l(face f) = Ip(cell f-1) and r(face f) = Im(cell f), so Ip / Im of a cell take the
 // adjoints of its high / low face, component lc of A_ASL0+D / A_ASR0+D.  Tracing is
@@ -265,7 +301,7 @@ __global__ void k_adj_es_predictor(KARGS, int bclo, int bchi, int domlo, int dom
 // (adjoint into ts, component D).
 template <int D, int UMAC>
 __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp, long long epsb, double dtdx,
-                               int want_u) {
+                               int want_u, int lo_ext, int hi_ext, int domlo, int domhi, RecipC r6) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const double ipb = at(AW(A_ASL0 + D), i + di, j + dj, k + dk, lc);
@@ -273,10 +309,29 @@ __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp,
     if (ipb == 0.0 && imb == 0.0) return;  // A_ASM / A_ASP were cleared
     const FabView s = VW(fs), F = VW(F_FACE0 + D);
     const double s0 = at(s, i, j, k, sc);
-    double sm = at(F, i, j, k), sp = at(F, i + di, j + dj, k + dk);
+    // Next to an ext_dir / hoextrap boundary (ppm_cell_edges): the first interior cell is
+    // not limited, and a ghost cell beyond the boundary reads the interior interpolants of
+    // the two boundary faces, recomputed, instead of the boundary values stored there.
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const bool outside = (lo_ext && I < domlo) || (hi_ext && I > domhi);
+    auto recomputed = [&](int f) {
+        return outside && ((lo_ext && (f == domlo || f == domlo + 1)) || (hi_ext && (f == domhi || f == domhi + 1)));
+    };
+    auto regular = [&](int ii, int jj, int kk) {
+        const FabView dv = VW(F_DSVL);
+        const double sl = at(s, ii - di, jj - dj, kk - dk, sc), sr = at(s, ii, jj, kk, sc);
+        double v = 0.5 * (sr + sl) - div_c(at(dv, ii, jj, kk) - at(dv, ii - di, jj - dj, kk - dk), r6);
+        v = mx(v, mn(sr, sl));
+        return mn(v, mx(sr, sl));
+    };
+    const bool rm = recomputed(I), rp = recomputed(I + 1);
+    double sm = rm ? regular(i, j, k) : at(F, i, j, k);
+    double sp = rp ? regular(i + di, j + dj, k + dk) : at(F, i + di, j + dj, k + dk);
+    const bool special = (lo_ext && I == domlo) || (hi_ext && I == domhi);
     int cs = 3;  // the forward limiter's case, decided as k_ppm_cell decides it
     const double a = sp - s0, q = s0 - sm;
-    if (!prod_gt0(a, q)) {
+    if (special) {
+    } else if (!prod_gt0(a, q)) {
         sp = s0;
         sm = s0;
         cs = 0;
@@ -341,9 +396,13 @@ __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp,
         fm = bsm;
         fp = bsp;
     }
-    at(AW(A_ASM), i, j, k) = fm;
-    at(AW(A_ASP), i, j, k) = fp;
     const FabView t = AW(ts);
+    // a recomputed face's adjoint goes straight through its interior interpolant; the
+    // stored boundary value's transpose (k_adj_ppm_face) sees none of it
+    if (rm) adj_face_regular<D>(V, nb, b, s, sc, VW(F_DSVL), t, tcomp, i, j, k, fm, r6, false);
+    if (rp) adj_face_regular<D>(V, nb, b, s, sc, VW(F_DSVL), t, tcomp, i + di, j + dj, k + dk, fp, r6, false);
+    at(AW(A_ASM), i, j, k) = rm ? 0.0 : fm;
+    at(AW(A_ASP), i, j, k) = rp ? 0.0 : fp;
     at(t, i, j, k, tcomp) += bs0;
     if (want_u) {
         if (UMAC) {
@@ -359,36 +418,60 @@ __global__ void k_adj_ppm_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp,
 // k_ppm_face<D, 1> transposed (Source/MaestroPPM.cpp:37-111 interior form):
 // v = min(max(v0, min(s0, s-1)), max(s0, s-1)), v0 = (s0 + s-1)/2 - (dv(f) - dv(f-1))/6.
 // Cell adjoints to slot ts, component tcomp.
+// Faces next to an ext_dir / hoextrap boundary (ppm_face_value): the boundary face takes
+// the ghost cell's value, the next one the one-sided cubic
+// -s(-2)/5 + 3 s(-1)/4 + s(0)/2 - s(1)/20 (mirrored on the high side), clamped like the
+// interior interpolant.
 template <int D>
-__global__ void k_adj_ppm_face(KARGS, int fs, int sc, int ts, int tcomp, RecipC r6) {
+__global__ void k_adj_ppm_face(KARGS, int fs, int sc, int ts, int tcomp, RecipC r6, int lo_ext, int hi_ext, int domlo,
+                               int domhi) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const double fb = at(AW(A_ASM), i, j, k) + at(AW(A_ASP), i - di, j - dj, k - dk);
     if (fb == 0.0) return;
-    const FabView s = VW(fs), dv = VW(F_DSVL), as = AW(ts);
-    const double sl = at(s, i - di, j - dj, k - dk, sc), s0 = at(s, i, j, k, sc);
-    const double v0 = half(s0 + sl) - div_c(at(dv, i, j, k) - at(dv, i - di, j - dj, k - dk), r6);
-    // mn(a, b) = (b < a) ? b : a and mx(a, b) = (a < b) ? b : a, as in the forward
-    const double lo = mn(s0, sl), hi = mx(s0, sl);
-    int src = 0;  // 0: v0, 1: s0, 2: s-1
-    double v = v0;
-    if (v < lo) {
-        v = lo;
-        src = (sl < s0) ? 2 : 1;
+    const FabView s = VW(fs), as = AW(ts);
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    auto add = [&](int m, double v) { atomicAdd(&at(as, i + m * di, j + m * dj, k + m * dk, tcomp), v); };
+    if (lo_ext && I == domlo) {
+        add(-1, fb);
+        return;
     }
-    if (hi < v) src = (s0 < sl) ? 2 : 1;
-    if (src == 0) {
-        atomicAdd(&at(as, i, j, k, tcomp), 0.5 * fb);
-        atomicAdd(&at(as, i - di, j - dj, k - dk, tcomp), 0.5 * fb);
-        const FabView ad = AW(A_ADSVL);
-        const double f6 = div_c(fb, r6);
-        atomicAdd(&at(ad, i, j, k), -f6);
-        atomicAdd(&at(ad, i - di, j - dj, k - dk), f6);
-    } else if (src == 1) {
-        atomicAdd(&at(as, i, j, k, tcomp), fb);
-    } else {
-        atomicAdd(&at(as, i - di, j - dj, k - dk, tcomp), fb);
+    if (hi_ext && I == domhi + 1) {
+        add(0, fb);
+        return;
     }
+    const bool cub_lo = lo_ext && I == domlo + 1, cub_hi = hi_ext && I == domhi;
+    if (cub_lo || cub_hi) {
+        auto S = SHIFT_S(s, sc);
+        const double v0 = cub_lo ? -0.2 * S(-2) + 0.75 * S(-1) + 0.5 * S(0) - 0.05 * S(1)
+                                 : -0.2 * S(1) + 0.75 * S(0) + 0.5 * S(-1) - 0.05 * S(-2);
+        const double sl = S(-1), s0 = S(0);
+        const double lo = mn(s0, sl), hi = mx(s0, sl);
+        int src = 0;
+        double v = v0;
+        if (v < lo) {
+            v = lo;
+            src = (sl < s0) ? 2 : 1;
+        }
+        if (hi < v) src = (s0 < sl) ? 2 : 1;
+        if (src == 1) {
+            add(0, fb);
+        } else if (src == 2) {
+            add(-1, fb);
+        } else if (cub_lo) {
+            add(-2, -0.2 * fb);
+            add(-1, 0.75 * fb);
+            add(0, 0.5 * fb);
+            add(1, -0.05 * fb);
+        } else {
+            add(1, -0.2 * fb);
+            add(0, 0.75 * fb);
+            add(-1, 0.5 * fb);
+            add(-2, -0.05 * fb);
+        }
+        return;
+    }
+    adj_face_regular<D>(V, nb, b, s, sc, VW(F_DSVL), as, tcomp, i, j, k, fb, r6, true);
 }
 
 // k_dsvl<D> transposed (Source/MaestroPPM.cpp:37-73):
@@ -735,13 +818,17 @@ static void adj_predictor_launch(Ctx& c, const BCRecD& bc) {
 // faces: recompute the interface values F_FACE0+D (0: they hold the forward's already).
 template <int D, int UMAC>
 static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, double* dir, size_t dir_bytes,
-                          int want_u, int faces) {
+                          int want_u, int faces, const BCRecD& bc) {
     ppm_faces(c, D, fs, sc, faces);
     if (!c.dry) cudaMemsetAsync(dir, 0, dir_bytes, c.stream);
     const long long eb = dbits_host(c.P.rel_eps);
     const RecipC r6 = make_recip(6.0);
-    launch(c, rg_grow(c, 1), 1, k_adj_ppm_cell<D, UMAC>, c.V(), fs, sc, lc, ts, tc, eb, c.P.dt / c.P.dx[D], want_u);
-    launch(c, region(c, 1, 1, 1, 1, 1, 1, D), 1, k_adj_ppm_face<D>, c.V(), fs, sc, ts, tc, r6);
+    // the forward's boundary stencils (ppm_any): ext_dir / hoextrap sides
+    auto ext = [](int t) { return (t == BC_EXT_DIR || t == BC_HOEXTRAP) ? 1 : 0; };
+    const int le = ext(bc.lo[D]), he = ext(bc.hi[D]), dl = c.P.dom_lo[D], dh = c.P.dom_hi[D];
+    launch(c, rg_grow(c, 1), 1, k_adj_ppm_cell<D, UMAC>, c.V(), fs, sc, lc, ts, tc, eb, c.P.dt / c.P.dx[D], want_u,
+           le, he, dl, dh, r6);
+    launch(c, region(c, 1, 1, 1, 1, 1, 1, D), 1, k_adj_ppm_face<D>, c.V(), fs, sc, ts, tc, r6, le, he, dl, dh);
     int glo[3] = {1, 1, 1};
     glo[D] = 2;
     launch(c, region(c, glo[0], glo[1], glo[2], glo[0], glo[1], glo[2], -1), 1, k_adj_dsvl<D>, c.V(), fs, sc, ts, tc);
@@ -773,9 +860,9 @@ void adj_edge_scal(Ctx& c, int fs, int comp, int force_zero, double* dir, size_t
     adj_predictor_launch<0>(c, bc);
     adj_predictor_launch<1>(c, bc);
     adj_predictor_launch<2>(c, bc);
-    adj_ppm_launch<0, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
-    adj_ppm_launch<1, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
-    adj_ppm_launch<2, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0);
+    adj_ppm_launch<0, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0, bc);
+    adj_ppm_launch<1, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0, bc);
+    adj_ppm_launch<2, 1>(c, fs, comp, 0, A_AS, 0, dir, dir_bytes, want_u, 0, bc);
 }
 
 void adj_fill_boundary(Ctx& c, int slot, int nc, int ng, int nodal) {
@@ -855,9 +942,9 @@ void adj_vel_pred(Ctx& c, double* dir, size_t dir_bytes) {
     adj_vp_interface_launch<1>(c, eb);
     adj_vp_interface_launch<2>(c, eb);
     for (int cc = 0; cc < 3; ++cc) {
-        adj_ppm_launch<0, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1);
-        adj_ppm_launch<1, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1);
-        adj_ppm_launch<2, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1);
+        adj_ppm_launch<0, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1, c.bcs_u[cc]);
+        adj_ppm_launch<1, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1, c.bcs_u[cc]);
+        adj_ppm_launch<2, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1, c.bcs_u[cc]);
     }
 }
 

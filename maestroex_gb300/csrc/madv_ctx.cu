@@ -2255,14 +2255,15 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         set_error("the adjoint covers 3-D domains with ppm_type 1, species_pred_type 1 and enthalpy_pred_type 1");
         return MADV_ERR_UNSUPPORTED;
     }
-    // physical boundaries: outflow and symmetry, whose scalar BCs (foextrap, reflect_even)
-    // fill ghost cells by copies; the velocity gradient needs a periodic domain
+    // physical boundaries: outflow, symmetry and walls (the traced fields' ghost cells are
+    // copies, BCS_F; walls' hoextrap scalar BCs select PPM's boundary stencils); inflow's
+    // ext_dir scalars are not covered; the velocity gradient needs a periodic domain
     for (int d = 0; d < 3; ++d)
         for (int pb : {c.P.phys_bc_lo[d], c.P.phys_bc_hi[d]}) {
             if (pb == PB_INTERIOR) continue;
-            if ((pb != PB_OUTFLOW && pb != PB_SYMMETRY) || res->grad_u) {
-                set_error("the adjoint covers periodic, outflow and symmetry boundaries (the velocity gradient "
-                          "periodic ones only)");
+            if (pb == PB_INFLOW || res->grad_u) {
+                set_error("the adjoint covers periodic, outflow, symmetry and wall boundaries (the velocity "
+                          "gradient periodic ones only)");
                 return MADV_ERR_UNSUPPORTED;
             }
         }
