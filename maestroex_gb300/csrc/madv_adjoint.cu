@@ -1,7 +1,8 @@
 // Reverse (adjoint) sweep of the advection stage on a fixed velocity: the transposes of
 // UpdateScal, MakeRhoXFlux / MakeRhoHFlux (species_pred_type 1, enthalpy_pred_type 1),
 // MakeEdgeScal with PPM ppm_type 1 (van Leer slopes, interface values, cell-edge limiter,
-// characteristic tracing, predictor, transverse and edge corrections), the pointwise
+// characteristic tracing, predictor, transverse and edge corrections) and ppm_type 2 (the
+// fourth-order interfaces and the Colella-Sekora limiter, differentiated on their branch), the pointwise
 // conversions and forces of DensityAdvance / EnthalpyAdvance and FillBoundary; and, for
 // the gradient with respect to the cell velocity, of VelPred and MakeUtrans.
 //
@@ -250,6 +251,212 @@ __global__ void k_adj_es_predictor(KARGS, int bclo, int bchi, int domlo, int dom
     upwind_w(at(VW(F_UMAC0 + D), i, j, k), 0, wl, wr);
     la += wl * sb;
     ra += wr * sb;
+}
+
+// ------------------------------------------------------------------ ppm_type 2 transposed
+// A value with one directional derivative.  The value is formed by exactly the forward's
+// double operations (so every decision taken on it is the forward's); the derivative is
+// that of the branch taken.  |x| differentiates as the oracle's tangent build does
+// (sign bit set: -x).
+struct Dv {
+    double v, d;
+};
+__device__ __forceinline__ Dv operator+(Dv a, Dv b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dv operator-(Dv a, Dv b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dv operator-(Dv a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ Dv operator*(Dv a, Dv b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Dv operator*(double a, Dv b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ Dv operator/(Dv a, Dv b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+__device__ __forceinline__ Dv dv_abs(Dv a) { return signbit(a.v) ? -a : a; }
+__device__ __forceinline__ Dv dv_sqrt(Dv a) {
+    const double r = sqrt(a.v);
+    return {r, a.d / (2.0 * r)};
+}
+__device__ __forceinline__ Dv dv_mn(Dv a, Dv b) { return (b.v < a.v) ? b : a; }
+__device__ __forceinline__ Dv dv_mx(Dv a, Dv b) { return (a.v < b.v) ? b : a; }
+
+// The ppm_type 2 edge values of one cell away from ext_dir / hoextrap boundaries
+// (ppm_cell_edges, Colella-Sekora limiter, Source/MaestroPPM.cpp:337-434) on values with a
+// derivative: S[0..4] = s(-2..2), F[0..3] = faces -1..2 of the cell.  Returns whether the
+// limiter changed either edge (otherwise sm = F(0), sp = F(1)).
+__device__ __forceinline__ bool ppm2_edges_dv(const Dv* S, const Dv* F, Dv& sm, Dv& sp) {
+    const double C = 1.25;
+    const Dv s0 = S[2];
+    Dv alphap = F[2] - s0, alpham = F[1] - s0;
+    const bool bigp = (dbits(alphap.v) & ABS_MASK) > (dbits(twice(alpham.v)) & ABS_MASK);
+    const bool bigm = (dbits(alpham.v) & ABS_MASK) > (dbits(twice(alphap.v)) & ABS_MASK);
+    bool extremum = false, changed = false;
+    if (!prod_gt0(alpham.v, -alphap.v)) {
+        extremum = true;
+    } else if (bigp || bigm) {
+        const Dv dafacem = F[1] - F[0], dafacep = F[3] - F[2];
+        const Dv dabarm = s0 - S[1], dabarp = S[3] - s0;
+        const double dafacemin = mn(fabs(dafacem.v), fabs(dafacep.v));
+        const double dabarmin = mn(fabs(dabarm.v), fabs(dabarp.v));
+        const bool face = dafacemin >= dabarmin;
+        extremum = !prod_gt0(face ? dafacem.v : dabarm.v, face ? dafacep.v : dabarp.v);
+    }
+    if (extremum) {
+        const Dv D2 = 6.0 * (alpham + alphap);
+        const Dv D2L = S[0] - 2.0 * S[1] + s0;
+        const Dv D2R = s0 - 2.0 * S[3] + S[4];
+        const Dv D2C = S[1] - 2.0 * s0 + S[3];
+        const double sgn = copysign(1.0, D2.v);
+        const Dv D2LIM = dv_mx(dv_mn(sgn * D2, dv_mn(C * sgn * D2L, dv_mn(C * sgn * D2R, C * sgn * D2C))), Dv{0.0, 0.0});
+        const Dv D2ABS = dv_mx(dv_abs(D2), Dv{1.e-10, 0.0});
+        alpham = alpham * D2LIM / D2ABS;
+        alphap = alphap * D2LIM / D2ABS;
+        changed = true;
+    } else {
+        if (bigp) {
+            const double sgn = copysign(1.0, alpham.v);
+            const double amax = -alphap.v * alphap.v / (4.0 * (alpham.v + alphap.v));
+            const Dv delam = S[1] - s0;
+            if (sgn * amax >= sgn * delam.v) {
+                if (sgn * (delam.v - alpham.v) >= 1.e-10)
+                    alphap = -2.0 * delam - 2.0 * sgn * dv_sqrt(delam * delam - delam * alpham);
+                else
+                    alphap = -2.0 * alpham;
+                changed = true;
+            }
+        }
+        if (bigm) {
+            const double sgn = copysign(1.0, alphap.v);
+            const double amax = -alpham.v * alpham.v / (4.0 * (alpham.v + alphap.v));
+            const Dv delap = S[3] - s0;
+            if (sgn * amax >= sgn * delap.v) {
+                if (sgn * (delap.v - alphap.v) >= 1.e-10)
+                    alpham = -2.0 * delap - 2.0 * sgn * dv_sqrt(delap * delap - delap * alphap);
+                else
+                    alpham = -2.0 * alphap;
+                changed = true;
+            }
+        }
+    }
+    sm = s0 + alpham;
+    sp = s0 + alphap;
+    return changed;
+}
+
+// ppm2_face_regular on values with a derivative, face between cells m-1 and m:
+// S[0..3] = s(m-2 .. m+1).
+__device__ __forceinline__ Dv ppm2_face_dv(const Dv* S, const RecipC& r6) {
+    const double C = 1.25;
+    Dv se = (7.0 / 12.0) * (S[1] + S[2]) - (1.0 / 12.0) * (S[0] + S[3]);
+    if (prod_gt0(se.v - S[1].v, se.v - S[2].v)) {
+        const Dv D2 = 3.0 * (S[1] - 2.0 * se + S[2]);
+        const Dv D2L = S[0] - 2.0 * S[1] + S[2];
+        const Dv D2R = S[1] - 2.0 * S[2] + S[3];
+        const double sgn = copysign(1.0, D2.v);
+        const Dv D2LIM = sgn * dv_mx(dv_mn(C * sgn * D2L, dv_mn(C * sgn * D2R, sgn * D2)), Dv{0.0, 0.0});
+        // div_c(x, 6) is the correctly rounded x / 6: its derivative is d / 6
+        se = 0.5 * (S[1] + S[2]) - Dv{div_c(D2LIM.v, r6), D2LIM.d / 6.0};
+    }
+    return se;
+}
+
+// k_ppm_cell<D, 2, 1> transposed away from ext_dir / hoextrap boundaries (cells of the box
+// grown by one): the tracing as for ppm_type 1, then the limiter's transpose.  Where the
+// limiter left the edges alone, sm = s0 + (F(0) - s0) and sp likewise, so their adjoints go
+// to the two faces; elsewhere the limiter is differentiated along each of its nine inputs
+// (s(-2..2), faces -1..2) on its own branch.  Face adjoints: faces -1, 0 into A_ASM of cells
+// -1, 0 and faces 1, 2 into A_ASP of cells 0, 1 (k_adj_ppm2_face gathers A_ASM(f) +
+// A_ASP(f-1)); cell adjoints to slot ts, component tcomp.
+template <int D>
+__global__ void k_adj_ppm2_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp, long long epsb) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const double ipb = at(AW(A_ASL0 + D), i + di, j + dj, k + dk, lc);
+    const double imb = at(AW(A_ASR0 + D), i, j, k, lc);
+    if (ipb == 0.0 && imb == 0.0) return;
+    const FabView s = VW(fs), F = VW(F_FACE0 + D);
+    Dv Sv[5], Fv[4];
+    for (int m = 0; m < 5; ++m) Sv[m] = Dv{at(s, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, sc), 0.0};
+    for (int m = 0; m < 4; ++m) Fv[m] = Dv{at(F, i + (m - 1) * di, j + (m - 1) * dj, k + (m - 1) * dk), 0.0};
+    Dv smv, spv;
+    const bool changed = ppm2_edges_dv(Sv, Fv, smv, spv);
+    const double s0 = Sv[2].v;
+    const FabView T = VW(F_TRA0 + D), u = VW(F_UMAC0 + D);
+    const double up = at(u, i + di, j + dj, k + dk), um = at(u, i, j, k);
+    const double Ap = at(T, i + di, j + dj, k + dk, 0), Bp = at(T, i + di, j + dj, k + dk, 1);
+    const double Am = at(T, i, j, k, 0), Bm = at(T, i, j, k, 1);
+    (void)smv;
+    (void)spv;
+    double bs0 = 0.0, bsm = 0.0, bsp = 0.0;
+    if (gt_t(up, epsb)) {
+        const double t = Ap * ipb, w = 3.0 * (Bp * t);
+        bsp += (ipb - t) - w;
+        bsm += t - w;
+        bs0 += twice(w);
+    } else {
+        bs0 += ipb;
+    }
+    if (lt_negt(um, epsb)) {
+        const double t = Am * imb, w = 3.0 * (Bm * t);
+        bsm += (imb - t) - w;
+        bsp += t - w;
+        bs0 += twice(w);
+    } else {
+        bs0 += imb;
+    }
+    double gS[5] = {0.0, 0.0, bs0, 0.0, 0.0}, gF[4] = {0.0, 0.0, 0.0, 0.0};
+    if (!changed) {
+        gF[1] = bsm;
+        gF[2] = bsp;
+    } else {
+        for (int q = 0; q < 9; ++q) {
+            Dv* x = q < 5 ? &Sv[q] : &Fv[q - 5];
+            x->d = 1.0;
+            Dv a, c2;
+            ppm2_edges_dv(Sv, Fv, a, c2);
+            x->d = 0.0;
+            const double g = bsm * a.d + bsp * c2.d;
+            if (q < 5) gS[q] += g;
+            else gF[q - 5] += g;
+        }
+    }
+    const FabView as = AW(ts);
+    for (int m = 0; m < 5; ++m)
+        if (gS[m] != 0.0) atomicAdd(&at(as, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, tcomp), gS[m]);
+    const FabView am = AW(A_ASM), ap = AW(A_ASP);
+    if (gF[0] != 0.0) atomicAdd(&at(am, i - di, j - dj, k - dk), gF[0]);
+    if (gF[1] != 0.0) atomicAdd(&at(am, i, j, k), gF[1]);
+    if (gF[2] != 0.0) atomicAdd(&at(ap, i, j, k), gF[2]);
+    if (gF[3] != 0.0) atomicAdd(&at(ap, i + di, j + dj, k + dk), gF[3]);
+}
+
+// k_ppm_face<D, 2> transposed away from ext_dir / hoextrap boundaries, faces lo-2 .. hi+3 of
+// the box along D (the forward's face region): the fourth-order interpolant, or on a limited
+// face its limited form differentiated along each of its four cells.
+template <int D>
+__global__ void k_adj_ppm2_face(KARGS, int fs, int sc, int ts, int tcomp, RecipC r6) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const RegionBox& rr = R[e_];
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    // A_ASM / A_ASP cover cells lo-2 .. hi+2: the last face has no A_ASM entry and the first
+    // no A_ASP entry, and the cell kernel writes none there
+    double fb = 0.0;
+    if (I != rr.lo[D] + rr.n[D] - 1) fb += at(AW(A_ASM), i, j, k);
+    if (I != rr.lo[D]) fb += at(AW(A_ASP), i - di, j - dj, k - dk);
+    if (fb == 0.0) return;
+    const FabView s = VW(fs), as = AW(ts);
+    Dv Sv[4];
+    for (int m = 0; m < 4; ++m) Sv[m] = Dv{at(s, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, sc), 0.0};
+    const double se = (7.0 / 12.0) * (Sv[1].v + Sv[2].v) - (1.0 / 12.0) * (Sv[0].v + Sv[3].v);
+    double g[4];
+    if (!prod_gt0(se - Sv[1].v, se - Sv[2].v)) {
+        g[0] = g[3] = -(1.0 / 12.0) * fb;
+        g[1] = g[2] = (7.0 / 12.0) * fb;
+    } else {
+        for (int q = 0; q < 4; ++q) {
+            Sv[q].d = 1.0;
+            g[q] = fb * ppm2_face_dv(Sv, r6).d;
+            Sv[q].d = 0.0;
+        }
+    }
+    for (int m = 0; m < 4; ++m)
+        if (g[m] != 0.0) atomicAdd(&at(as, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, tcomp), g[m]);
 }
 
 // The interior face value of ppm_type 1 transposed, face f between cells f-1 and f
@@ -819,6 +1026,15 @@ static void adj_predictor_launch(Ctx& c, const BCRecD& bc) {
 template <int D, int UMAC>
 static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, double* dir, size_t dir_bytes,
                           int want_u, int faces, const BCRecD& bc) {
+    if (c.P.ppm_type == 2) {  // scalars (UMAC = 1, no velocity gradient), no ext_dir / hoextrap side
+        if (!c.dry) cudaMemsetAsync(dir, 0, dir_bytes, c.stream);
+        int g[3] = {1, 1, 1};
+        g[D] = 2;
+        launch(c, rg_grow(c, 1), 1, k_adj_ppm2_cell<D>, c.V(), fs, sc, lc, ts, tc, dbits_host(c.P.rel_eps));
+        launch(c, region(c, g[0], g[1], g[2], g[0], g[1], g[2], D), 1, k_adj_ppm2_face<D>, c.V(), fs, sc, ts, tc,
+               make_recip(6.0));
+        return;
+    }
     ppm_faces(c, D, fs, sc, faces);
     if (!c.dry) cudaMemsetAsync(dir, 0, dir_bytes, c.stream);
     const long long eb = dbits_host(c.P.rel_eps);

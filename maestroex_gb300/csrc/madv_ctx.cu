@@ -2251,9 +2251,20 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         set_error("madv_stage_adjoint: uold, sold0, weight, nsteps >= 1 and ckpt_interval >= 1 are required");
         return MADV_ERR_PARAM;
     }
-    if (c.ndim != 3 || c.P.ppm_type != 1 || c.P.species_pred_type != 1 || c.P.enthalpy_pred_type != 1) {
-        set_error("the adjoint covers 3-D domains with ppm_type 1, species_pred_type 1 and enthalpy_pred_type 1");
+    if (c.ndim != 3 || (c.P.ppm_type != 1 && c.P.ppm_type != 2) || c.P.species_pred_type != 1 ||
+        c.P.enthalpy_pred_type != 1) {
+        set_error("the adjoint covers 3-D domains with ppm_type 1 or 2, species_pred_type 1 and enthalpy_pred_type 1");
         return MADV_ERR_UNSUPPORTED;
+    }
+    // ppm_type 2: the state gradient away from walls (their boundary stencils are not transposed)
+    if (c.P.ppm_type == 2) {
+        bool wall = false;
+        for (int d = 0; d < 3; ++d)
+            for (int pb : {c.P.phys_bc_lo[d], c.P.phys_bc_hi[d]}) wall |= pb == PB_SLIPWALL || pb == PB_NOSLIPWALL;
+        if (wall || res->grad_u) {
+            set_error("the ppm_type 2 adjoint covers the state gradient on periodic, outflow and symmetry boundaries");
+            return MADV_ERR_UNSUPPORTED;
+        }
     }
     // physical boundaries: outflow, symmetry and walls (the traced fields' ghost cells are
     // copies, BCS_F; walls' hoextrap scalar BCs select PPM's boundary stencils); inflow's
