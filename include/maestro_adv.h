@@ -325,7 +325,8 @@ int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_f
  * and upwind decisions frozen; states are stored every ckpt_interval steps and each
  * block is recomputed from its stored state, so memory grows with nsteps/ckpt_interval
  * + ckpt_interval states.  No counterpart in the reference.
- * Scope: one level, 3-D, plane-parallel or spherical, ppm_type 1, species_pred_type 1,
+ * Scope: one level, 3-D, plane-parallel or spherical, ppm_type 1 (or 2: state gradient, no
+ * walls), species_pred_type 1,
  * enthalpy_pred_type 1, and grav_cell = 0 so that the MAC velocities do not depend on the
  * state.  The state gradient (grad_s) also allows outflow, symmetry and wall boundaries
  * and w0 != 0.  The velocity gradient (grad_u) needs a periodic domain and w0 = 0.  Anything

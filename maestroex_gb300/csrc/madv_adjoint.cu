@@ -276,66 +276,151 @@ __device__ __forceinline__ Dv dv_mn(Dv a, Dv b) { return (b.v < a.v) ? b : a; }
 __device__ __forceinline__ Dv dv_mx(Dv a, Dv b) { return (a.v < b.v) ? b : a; }
 
 // The ppm_type 2 edge values of one cell away from ext_dir / hoextrap boundaries
-// (ppm_cell_edges, Colella-Sekora limiter, Source/MaestroPPM.cpp:337-434) on values with a
-// derivative: S[0..4] = s(-2..2), F[0..3] = faces -1..2 of the cell.  Returns whether the
-// limiter changed either edge (otherwise sm = F(0), sp = F(1)).
-__device__ __forceinline__ bool ppm2_edges_dv(const Dv* S, const Dv* F, Dv& sm, Dv& sp) {
+// (ppm_cell_edges, Colella-Sekora limiter, Source/MaestroPPM.cpp:337-434) and their
+// transpose: S[0..4] = s(-2..2), F[0..3] = faces -1..2 of the cell.  The forward part
+// repeats the forward's double operations, so every decision is the forward's; the reverse
+// part takes the edge adjoints bsm, bsp of the branch taken and adds the input adjoints to
+// gS, gF.  Returns the edges in sm, sp.
+__device__ __forceinline__ void ppm2_edges_adj(const double* S, const double* F, double bsm, double bsp, double* gS,
+                                               double* gF, double& sm, double& sp) {
     const double C = 1.25;
-    const Dv s0 = S[2];
-    Dv alphap = F[2] - s0, alpham = F[1] - s0;
-    const bool bigp = (dbits(alphap.v) & ABS_MASK) > (dbits(twice(alpham.v)) & ABS_MASK);
-    const bool bigm = (dbits(alpham.v) & ABS_MASK) > (dbits(twice(alphap.v)) & ABS_MASK);
-    bool extremum = false, changed = false;
-    if (!prod_gt0(alpham.v, -alphap.v)) {
+    const double s0 = S[2];
+    const double am0 = F[1] - s0, ap0 = F[2] - s0;
+    double alpham = am0, alphap = ap0;
+    const bool bigp = (dbits(alphap) & ABS_MASK) > (dbits(twice(alpham)) & ABS_MASK);
+    const bool bigm = (dbits(alpham) & ABS_MASK) > (dbits(twice(alphap)) & ABS_MASK);
+    bool extremum = false;
+    if (!prod_gt0(alpham, -alphap)) {
         extremum = true;
     } else if (bigp || bigm) {
-        const Dv dafacem = F[1] - F[0], dafacep = F[3] - F[2];
-        const Dv dabarm = s0 - S[1], dabarp = S[3] - s0;
-        const double dafacemin = mn(fabs(dafacem.v), fabs(dafacep.v));
-        const double dabarmin = mn(fabs(dabarm.v), fabs(dabarp.v));
+        const double dafacem = F[1] - F[0], dafacep = F[3] - F[2];
+        const double dabarm = s0 - S[1], dabarp = S[3] - s0;
+        const double dafacemin = mn(fabs(dafacem), fabs(dafacep));
+        const double dabarmin = mn(fabs(dabarm), fabs(dabarp));
         const bool face = dafacemin >= dabarmin;
-        extremum = !prod_gt0(face ? dafacem.v : dabarm.v, face ? dafacep.v : dabarp.v);
+        extremum = !prod_gt0(face ? dafacem : dabarm, face ? dafacep : dabarp);
     }
+    double gam = 0.0, gap = 0.0;  // adjoints of am0, ap0
+    gS[2] += bsm + bsp;           // sm = s0 + alpham, sp = s0 + alphap
     if (extremum) {
-        const Dv D2 = 6.0 * (alpham + alphap);
-        const Dv D2L = S[0] - 2.0 * S[1] + s0;
-        const Dv D2R = s0 - 2.0 * S[3] + S[4];
-        const Dv D2C = S[1] - 2.0 * s0 + S[3];
-        const double sgn = copysign(1.0, D2.v);
-        const Dv D2LIM = dv_mx(dv_mn(sgn * D2, dv_mn(C * sgn * D2L, dv_mn(C * sgn * D2R, C * sgn * D2C))), Dv{0.0, 0.0});
-        const Dv D2ABS = dv_mx(dv_abs(D2), Dv{1.e-10, 0.0});
+        const double D2 = 6.0 * (alpham + alphap);
+        const double D2L = S[0] - 2.0 * S[1] + s0;
+        const double D2R = s0 - 2.0 * S[3] + S[4];
+        const double D2C = S[1] - 2.0 * s0 + S[3];
+        const double sgn = copysign(1.0, D2);
+        // D2LIM = mx(mn(sgn D2, mn(C sgn D2L, mn(C sgn D2R, C sgn D2C))), 0): which term it is
+        const double cD = sgn * D2, cL = C * sgn * D2L, cR = C * sgn * D2R, cC = C * sgn * D2C;
+        int pick = (cC < cR) ? 3 : 2;  // 0: D2, 1: D2L, 2: D2R, 3: D2C, 4: the constant 0
+        double v = pick == 3 ? cC : cR;
+        if (v < cL) {
+        } else {
+            pick = 1;
+            v = cL;
+        }
+        if (v < cD) {
+        } else {
+            pick = 0;
+            v = cD;
+        }
+        if (v < 0.0) {
+            pick = 4;
+            v = 0.0;
+        }
+        const double D2LIM = v;
+        const bool abs_pick = !(fabs(D2) < 1.e-10);
+        const double D2ABS = abs_pick ? fabs(D2) : 1.e-10;
         alpham = alpham * D2LIM / D2ABS;
         alphap = alphap * D2LIM / D2ABS;
-        changed = true;
+        const double q = bsm * am0 + bsp * ap0;
+        gam += bsm * D2LIM / D2ABS;
+        gap += bsp * D2LIM / D2ABS;
+        const double gL = q / D2ABS;                     // d/dD2LIM
+        double gD2 = 0.0;
+        if (abs_pick) gD2 -= (signbit(D2) ? -1.0 : 1.0) * q * D2LIM / (D2ABS * D2ABS);
+        if (pick == 0) gD2 += gL * sgn;
+        const double gc = gL * C * sgn;                  // d/d(D2L, D2R or D2C)
+        if (pick == 1) {
+            gS[0] += gc;
+            gS[1] -= 2.0 * gc;
+            gS[2] += gc;
+        } else if (pick == 2) {
+            gS[2] += gc;
+            gS[3] -= 2.0 * gc;
+            gS[4] += gc;
+        } else if (pick == 3) {
+            gS[1] += gc;
+            gS[2] -= 2.0 * gc;
+            gS[3] += gc;
+        }
+        gam += 6.0 * gD2;
+        gap += 6.0 * gD2;
     } else {
+        // bigp rewrites alphap from (alpham, delam); bigm then alpham from (alphap, delap)
+        int p_case = 0, m_case = 0;  // 0: unchanged, 1: the square-root form, 2: -2 x the other
+        double p_sq = 0.0, p_sg = 0.0, delam = 0.0, m_sq = 0.0, m_sg = 0.0, delap = 0.0, ap_in = 0.0;
         if (bigp) {
-            const double sgn = copysign(1.0, alpham.v);
-            const double amax = -alphap.v * alphap.v / (4.0 * (alpham.v + alphap.v));
-            const Dv delam = S[1] - s0;
-            if (sgn * amax >= sgn * delam.v) {
-                if (sgn * (delam.v - alpham.v) >= 1.e-10)
-                    alphap = -2.0 * delam - 2.0 * sgn * dv_sqrt(delam * delam - delam * alpham);
-                else
+            const double sgn = copysign(1.0, alpham);
+            const double amax = -alphap * alphap / (4.0 * (alpham + alphap));
+            delam = S[1] - s0;
+            if (sgn * amax >= sgn * delam) {
+                if (sgn * (delam - alpham) >= 1.e-10) {
+                    p_sq = sqrt(delam * delam - delam * alpham);
+                    alphap = -2.0 * delam - 2.0 * sgn * p_sq;
+                    p_case = 1;
+                } else {
                     alphap = -2.0 * alpham;
-                changed = true;
+                    p_case = 2;
+                }
+                p_sg = sgn;
             }
         }
+        ap_in = alphap;
         if (bigm) {
-            const double sgn = copysign(1.0, alphap.v);
-            const double amax = -alpham.v * alpham.v / (4.0 * (alpham.v + alphap.v));
-            const Dv delap = S[3] - s0;
-            if (sgn * amax >= sgn * delap.v) {
-                if (sgn * (delap.v - alphap.v) >= 1.e-10)
-                    alpham = -2.0 * delap - 2.0 * sgn * dv_sqrt(delap * delap - delap * alphap);
-                else
+            const double sgn = copysign(1.0, alphap);
+            const double amax = -alpham * alpham / (4.0 * (alpham + alphap));
+            delap = S[3] - s0;
+            if (sgn * amax >= sgn * delap) {
+                if (sgn * (delap - alphap) >= 1.e-10) {
+                    m_sq = sqrt(delap * delap - delap * alphap);
+                    alpham = -2.0 * delap - 2.0 * sgn * m_sq;
+                    m_case = 1;
+                } else {
                     alpham = -2.0 * alphap;
-                changed = true;
+                    m_case = 2;
+                }
+                m_sg = sgn;
             }
         }
+        double g_am = bsm, g_ap = bsp;  // adjoints of the final alpham, alphap
+        if (m_case == 1) {              // alpham = -2 delap - 2 sg sqrt(delap^2 - delap ap_in)
+            const double gdp = g_am * (-2.0 - m_sg * (2.0 * delap - ap_in) / m_sq);
+            g_ap += g_am * (m_sg * delap / m_sq);
+            gS[3] += gdp;
+            gS[2] -= gdp;
+            g_am = 0.0;
+        } else if (m_case == 2) {
+            g_ap += -2.0 * g_am;
+            g_am = 0.0;
+        }
+        if (p_case == 1) {  // alphap = -2 delam - 2 sg sqrt(delam^2 - delam am0)
+            const double gdm = g_ap * (-2.0 - p_sg * (2.0 * delam - am0) / p_sq);
+            g_am += g_ap * (p_sg * delam / p_sq);
+            gS[1] += gdm;
+            gS[2] -= gdm;
+            g_ap = 0.0;
+        } else if (p_case == 2) {
+            g_am += -2.0 * g_ap;
+            g_ap = 0.0;
+        }
+        gam += g_am;
+        gap += g_ap;
     }
+    // am0 = F(0) - s0, ap0 = F(1) - s0
+    gF[1] += gam;
+    gF[2] += gap;
+    gS[2] -= gam + gap;
     sm = s0 + alpham;
     sp = s0 + alphap;
-    return changed;
 }
 
 // ppm2_face_regular on values with a derivative, face between cells m-1 and m:
@@ -356,10 +441,8 @@ __device__ __forceinline__ Dv ppm2_face_dv(const Dv* S, const RecipC& r6) {
 }
 
 // k_ppm_cell<D, 2, 1> transposed away from ext_dir / hoextrap boundaries (cells of the box
-// grown by one): the tracing as for ppm_type 1, then the limiter's transpose.  Where the
-// limiter left the edges alone, sm = s0 + (F(0) - s0) and sp likewise, so their adjoints go
-// to the two faces; elsewhere the limiter is differentiated along each of its nine inputs
-// (s(-2..2), faces -1..2) on its own branch.  Face adjoints: faces -1, 0 into A_ASM of cells
+// grown by one): the tracing as for ppm_type 1, then the limiter's transpose on the
+// forward's branch (ppm2_edges_adj).  Face adjoints: faces -1, 0 into A_ASM of cells
 // -1, 0 and faces 1, 2 into A_ASP of cells 0, 1 (k_adj_ppm2_face gathers A_ASM(f) +
 // A_ASP(f-1)); cell adjoints to slot ts, component tcomp.
 template <int D>
@@ -370,18 +453,15 @@ __global__ void k_adj_ppm2_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp
     const double imb = at(AW(A_ASR0 + D), i, j, k, lc);
     if (ipb == 0.0 && imb == 0.0) return;
     const FabView s = VW(fs), F = VW(F_FACE0 + D);
-    Dv Sv[5], Fv[4];
-    for (int m = 0; m < 5; ++m) Sv[m] = Dv{at(s, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, sc), 0.0};
-    for (int m = 0; m < 4; ++m) Fv[m] = Dv{at(F, i + (m - 1) * di, j + (m - 1) * dj, k + (m - 1) * dk), 0.0};
-    Dv smv, spv;
-    const bool changed = ppm2_edges_dv(Sv, Fv, smv, spv);
-    const double s0 = Sv[2].v;
+    double Sv[5], Fv[4];
+    for (int m = 0; m < 5; ++m) Sv[m] = at(s, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, sc);
+    for (int m = 0; m < 4; ++m) Fv[m] = at(F, i + (m - 1) * di, j + (m - 1) * dj, k + (m - 1) * dk);
+    // the edges first (the tracing's transpose needs only the branch, not the values: its
+    // weights are the tracing coefficients), then the tracing adjoints into the limiter's
     const FabView T = VW(F_TRA0 + D), u = VW(F_UMAC0 + D);
     const double up = at(u, i + di, j + dj, k + dk), um = at(u, i, j, k);
     const double Ap = at(T, i + di, j + dj, k + dk, 0), Bp = at(T, i + di, j + dj, k + dk, 1);
     const double Am = at(T, i, j, k, 0), Bm = at(T, i, j, k, 1);
-    (void)smv;
-    (void)spv;
     double bs0 = 0.0, bsm = 0.0, bsp = 0.0;
     if (gt_t(up, epsb)) {
         const double t = Ap * ipb, w = 3.0 * (Bp * t);
@@ -400,21 +480,8 @@ __global__ void k_adj_ppm2_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp
         bs0 += imb;
     }
     double gS[5] = {0.0, 0.0, bs0, 0.0, 0.0}, gF[4] = {0.0, 0.0, 0.0, 0.0};
-    if (!changed) {
-        gF[1] = bsm;
-        gF[2] = bsp;
-    } else {
-        for (int q = 0; q < 9; ++q) {
-            Dv* x = q < 5 ? &Sv[q] : &Fv[q - 5];
-            x->d = 1.0;
-            Dv a, c2;
-            ppm2_edges_dv(Sv, Fv, a, c2);
-            x->d = 0.0;
-            const double g = bsm * a.d + bsp * c2.d;
-            if (q < 5) gS[q] += g;
-            else gF[q - 5] += g;
-        }
-    }
+    double sm, sp;
+    ppm2_edges_adj(Sv, Fv, bsm, bsp, gS, gF, sm, sp);
     const FabView as = AW(ts);
     for (int m = 0; m < 5; ++m)
         if (gS[m] != 0.0) atomicAdd(&at(as, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, tcomp), gS[m]);
