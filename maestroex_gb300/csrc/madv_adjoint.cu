@@ -2,9 +2,10 @@
 // UpdateScal, MakeRhoXFlux / MakeRhoHFlux (species_pred_type 1, enthalpy_pred_type 1),
 // MakeEdgeScal with PPM ppm_type 1 (van Leer slopes, interface values, cell-edge limiter,
 // characteristic tracing, predictor, transverse and edge corrections) and ppm_type 2 (the
-// fourth-order interfaces and the Colella-Sekora limiter, differentiated on their branch), the pointwise
-// conversions and forces of DensityAdvance / EnthalpyAdvance and FillBoundary; and, for
-// the gradient with respect to the cell velocity, of VelPred and MakeUtrans.
+// fourth-order interfaces and the Colella-Sekora limiter, on their branch), the pointwise
+// conversions and forces of DensityAdvance / EnthalpyAdvance, FillBoundary and the
+// physical-boundary fill; and, for the gradient with respect to the cell velocity, of
+// VelPred and MakeUtrans.
 //
 // Every limiter, clamp and upwind decision is recomputed from the forward inputs with the
 // forward's own expressions (the same compile flags, so the same bits), i.e. the
@@ -13,11 +14,11 @@
 // adjoint FABs, which have the forward FABs' index spaces (and zero-filled margins
 // wherever a transpose reads one cell past the forward region).
 //
-// Scope: 3-D, one level, plane-parallel or spherical, MAC velocities independent of the state
-// (grav_cell = 0, no pressure gradient), so the velocity force has no state term; w0 may be
-// non-zero for the state gradient (the gradient with respect to the velocity needs w0 = 0).  Periodic
-// domains; and for the state gradient alone also outflow, symmetry and wall boundaries
-// (scalar BCs foextrap, reflect_even, hoextrap: PPM's boundary stencils transposed).  With
+// Scope: 3-D, one level, plane-parallel or spherical, MAC velocities independent of the
+// state (grav_cell = 0, no pressure gradient), so the velocity force has no state term.
+// The state gradient allows w0 != 0 and outflow, symmetry and wall boundaries (scalar BCs
+// foextrap, reflect_even, hoextrap: PPM's boundary stencils transposed; ppm_type 2 without
+// walls); the gradient with respect to the velocity needs a periodic domain and w0 = 0.  With
 // grav_cell = 0 the gradp0 of MakeRhoHForce is zero (below the cutoff it is rho0 g; above
 // it the reference differences the planar p0 across j, Source/MaestroForce.cpp:606-614),
 // so the rhoh forces' veladv term has no derivative.  The forward kernels mirrored here
@@ -256,8 +257,7 @@ __global__ void k_adj_es_predictor(KARGS, int bclo, int bchi, int domlo, int dom
 // ------------------------------------------------------------------ ppm_type 2 transposed
 // A value with one directional derivative.  The value is formed by exactly the forward's
 // double operations (so every decision taken on it is the forward's); the derivative is
-// that of the branch taken.  |x| differentiates as the oracle's tangent build does
-// (sign bit set: -x).
+// that of the branch taken.
 struct Dv {
     double v, d;
 };
@@ -267,11 +267,6 @@ __device__ __forceinline__ Dv operator-(Dv a) { return {-a.v, -a.d}; }
 __device__ __forceinline__ Dv operator*(Dv a, Dv b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
 __device__ __forceinline__ Dv operator*(double a, Dv b) { return {a * b.v, a * b.d}; }
 __device__ __forceinline__ Dv operator/(Dv a, Dv b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
-__device__ __forceinline__ Dv dv_abs(Dv a) { return signbit(a.v) ? -a : a; }
-__device__ __forceinline__ Dv dv_sqrt(Dv a) {
-    const double r = sqrt(a.v);
-    return {r, a.d / (2.0 * r)};
-}
 __device__ __forceinline__ Dv dv_mn(Dv a, Dv b) { return (b.v < a.v) ? b : a; }
 __device__ __forceinline__ Dv dv_mx(Dv a, Dv b) { return (a.v < b.v) ? b : a; }
 
