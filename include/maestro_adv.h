@@ -32,7 +32,8 @@ enum {
     MADV_ERR_UNSUPPORTED = -3, /* option the library does not implement */
     MADV_ERR_CUDA = -4,        /* CUDA runtime error (see madv_last_error) */
     MADV_ERR_STATE = -5,       /* call order (layout / base state not set) */
-    MADV_ERR_EOS = -6          /* a cell fell to base_cutoff_density: needs the EOS */
+    MADV_ERR_EOS = -6,         /* a cell fell to base_cutoff_density: needs the EOS */
+    MADV_ERR_NOCONV = -7       /* an iterative solve did not reach its tolerance */
 };
 
 /* AMReX PhysBCType values (Maestro inputs lo_bc / hi_bc). */
@@ -387,6 +388,27 @@ int madv_selftest_exact(double y, double threshold, long long n, long long* fail
 
 const char* madv_last_error(void);
 const char* madv_version(void);
+
+/* Maestro::MacProj (Source/MaestroMacProj.cpp:11-236, declared at Source/Maestro.H:835),
+ * plane-parallel 3-D, one level.  umac[3] (>= 1 ghost face) enters with Utilde^* and leaves
+ * with Utilde = Utilde^* - (B / beta0) grad phi, B = beta0^2 / rho_face (use_alt_energy_fix),
+ * where phi solves -div(B grad phi) = macrhs - div(beta0 Utilde^*) to
+ * max|residual| <= tol_rel * max|rhs| (the reference's mac_tol_rel: min(eps_mac *
+ * mac_level_factor^finest_level, eps_mac_max) = 1e-10 on one level).  Boundaries: periodic,
+ * outflow Dirichlet phi = 0, other physical faces Neumann (SetMacSolverBCs).  The ghost
+ * faces of umac are refilled (FillBoundary + FillUmacGhost).  rho: the density the
+ * reference fills from sold (predictor) or the sold / snew average (corrector), valid
+ * cells read.  macrhs: beta0 (S - Sbar), valid cells.  beta0: host array [nr].  macphi
+ * (may be NULL) receives phi on the valid cells (mean-free when no face is Dirichlet).
+ * The solve is a cell-centred geometric multigrid on the level's domain (even extents).
+ * Returns MADV_ERR_NOCONV if max_iter V-cycles do not reach the tolerance. */
+typedef struct {
+    int iterations;       /* V-cycles taken */
+    double resid_ratio;   /* final max|residual| / max|rhs| */
+} madv_mac_result;
+int madv_mac_project(madv_ctx* ctx, const madv_multifab* umac, const madv_multifab* macphi,
+                     const madv_multifab* macrhs, const madv_multifab* rho, const double* beta0, double tol_rel,
+                     int max_iter, madv_mac_result* result, void* stream);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,7 @@ MODE_BATCHED, MODE_PER_BOX, MODE_GRAPH = 0, 1, 2
 
 ERRORS = {
     -1: "MADV_ERR_PARAM", -2: "MADV_ERR_LAYOUT", -3: "MADV_ERR_UNSUPPORTED",
-    -4: "MADV_ERR_CUDA", -5: "MADV_ERR_STATE", -6: "MADV_ERR_EOS",
+    -4: "MADV_ERR_CUDA", -5: "MADV_ERR_STATE", -6: "MADV_ERR_EOS", -7: "MADV_ERR_NOCONV",
 }
 
 EXPORTED = [
@@ -29,7 +29,7 @@ EXPORTED = [
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
     "madv_autotune_trial", "madv_autotune_finish", "madv_autotune_apply",
     "madv_make_utrans", "madv_vel_pred", "madv_make_edge_scal", "madv_make_rhox_flux", "madv_make_rhoh_flux",
-    "madv_update_scal", "madv_velocity_advance", "madv_est_dt",
+    "madv_update_scal", "madv_velocity_advance", "madv_est_dt", "madv_mac_project",
 ]
 
 
@@ -40,6 +40,10 @@ class MadvDtParams(C.Structure):
 
 class MadvDtResult(C.Structure):
     _fields_ = [("dt", C.c_double), ("dt_estimate", C.c_double), ("umax", C.c_double), ("rel_eps", C.c_double)]
+
+
+class MadvMacResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("resid_ratio", C.c_double)]
 
 
 class MadvBox(C.Structure):
@@ -108,6 +112,8 @@ def lib():
         L.madv_update_scal.argtypes = [C.c_void_p, MF, MF, MF, MF, I, I, C.c_void_p]
         L.madv_velocity_advance.argtypes = [C.c_void_p, MF, MF, MF, MF, MF, MF, MF, MF, C.c_void_p]
         L.madv_est_dt.argtypes = [C.c_void_p, I, MF, MF, MF, P(MadvDtParams), P(MadvDtResult), C.c_void_p]
+        L.madv_mac_project.argtypes = [C.c_void_p, MF, MF, MF, MF, P(C.c_double), C.c_double, I, P(MadvMacResult),
+                                       C.c_void_p]
         L.madv_stage_forward.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                          C.c_void_p]
         L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,

@@ -1020,6 +1020,7 @@ static void destroy_level(Ctx& c) {
     if (c.d_red) cudaFree(c.d_red);
     c.d_red = nullptr;
     if (c.d_reg) cudaFree(c.d_reg);
+    mac_free(c);
     c.d_reg = nullptr;
     c.d_flag = nullptr;
 }
@@ -1985,6 +1986,51 @@ int madv_velocity_advance(madv_ctx* h, const madv_multifab* uold, const madv_mul
 // advective and force constraints and rel_eps on every level.  The per-level maxima are exact
 // (k_dt_maxima), and the reference's per-box minima of monotone functions of per-box maxima
 // equal the same functions of the level maxima, so dt and umax match it bit for bit.
+// Maestro::MacProj, plane-parallel, one level (Source/MaestroMacProj.cpp:11-236): the
+// caller's umac is copied in with its ghost faces, projected, refilled and copied back
+int madv_mac_project(madv_ctx* h, const madv_multifab* umac, const madv_multifab* macphi, const madv_multifab* macrhs,
+                     const madv_multifab* rho, const double* beta0, double tol_rel, int max_iter,
+                     madv_mac_result* result, void* stream) {
+    Hier H;
+    int rc = begin_call(h, stream, H);
+    if (rc) return rc;
+    Ctx& c = h->c;
+    if (!umac || !macrhs || !rho || !beta0 || !(tol_rel > 0.0) || max_iter < 1) {
+        set_error("madv_mac_project: umac, macrhs, rho, beta0, tol_rel > 0 and max_iter >= 1 are required");
+        return MADV_ERR_PARAM;
+    }
+    if (c.ndim != 3 || c.sph) {
+        set_error("madv_mac_project covers plane-parallel 3-D levels");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    try {
+        for (int d = 0; d < 3; ++d)
+            if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 1))) return rc;
+        if ((rc = bind(c, U_FORCE, macrhs, 1, -1, 0)) || (rc = bind(c, U_RHOHALF, rho, 1, -1, 0)) ||
+            (rc = bind(c, U_SPONGE, macphi, 1, -1, 0)))
+            return rc;
+        if ((rc = upload_user_views(c))) return rc;
+        for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
+        // beta0 on the radial edges: CelltoEdge (Source/MaestroCelltoEdge.cpp:17-54)
+        const int nr = c.P.dom_hi[2] - c.P.dom_lo[2] + 1;
+        std::vector<double> b0(beta0, beta0 + nr), b0e(nr + 1, 0.0);
+        cell_to_edge_chunk(b0, b0e, 0, nr);
+        int it = 0;
+        double ratio = 0.0;
+        rc = mac_project_level(c, U_FORCE, U_RHOHALF, macphi ? U_SPONGE : -1, b0.data(), b0e.data(), tol_rel, max_iter,
+                               &it, &ratio);
+        if (result) {
+            result->iterations = it;
+            result->resid_ratio = ratio;
+        }
+        if (rc) return rc;
+        for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
 int madv_est_dt(madv_ctx* h, int nlev, const madv_multifab* uold, const madv_multifab* sold,
                 const madv_multifab* gpi, const madv_dt_params* prm, madv_dt_result* res, void* stream) {
     if (!h || !uold || !sold || !gpi || !prm || !res) return MADV_ERR_PARAM;

@@ -151,6 +151,7 @@ struct Ctx {
     int* d_flag = nullptr;  // device error flag (EOS cutoff)
     unsigned long long* d_red = nullptr;  // EstDt maxima (allocated on first use)
     double* d_reg = nullptr;  // flux register of this (fine) level with the level below (reflux_type 2)
+    struct MacMG* mac = nullptr;  // MAC-projection multigrid grids of this level (madv_macproj.cu)
     // graph mode
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<const void*> graph_key;
@@ -197,6 +198,9 @@ void phys_fill(Ctx& c, int fid, int c0, int nc, const BCRecD* bcs_dev, int bc_c0
                int state_c0);
 void fill_patch(Ctx& c, int fid, int c0, int nc, int which_bcs, int bc_c0, int is_vel, int state_c0);
 void fill_face_ghosts(Ctx& c, int f0);  // FillBoundary + FillUmacGhost of 3 face fields f0..f0+2
+void mac_free(Ctx& c);
+int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0, const double* beta0_edge,
+                      double tol_rel, int max_iter, int* iters_out, double* ratio_out);
 void addw0(Ctx& c, int f0, double mult);
 void set_val(Ctx& c, int fid, double v, int c0, int nc, int ngrow);
 void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow);

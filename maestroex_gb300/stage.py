@@ -252,6 +252,17 @@ class ScalarAdvectionStage:
         check(lib().madv_update_scal(self.ctx, _ref(stateold), _ref(statenew), _ref3(sflux), _ref(force),
                                      start_comp, num_comp, C.c_void_p(s)))
 
+    def mac_project(self, umac, macrhs, rho, beta0, macphi=None, tol_rel=1.0e-10, max_iter=100, stream=None):
+        """Maestro::MacProj (plane-parallel, one level): umac (3 face MultiFabs, >= 1 ghost)
+        projected in place so that div(beta0 umac) = macrhs; returns (V-cycles, final
+        max|residual| / max|rhs|).  rho, macrhs: cell MultiFabs; beta0: 1-D cell array."""
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        b0 = np.ascontiguousarray(beta0, dtype=np.float64)
+        res = capi.MadvMacResult()
+        check(lib().madv_mac_project(self.ctx, _ref3(umac), _ref(macphi), _ref(macrhs), _ref(rho), _dptr(b0),
+                                     float(tol_rel), int(max_iter), C.byref(res), C.c_void_p(s)))
+        return res.iterations, res.resid_ratio
+
     def est_dt(self, uold, sold, gpi, cfl=0.5, drdxfac=1, max_dt=1.0e33, fixed_dt=-1.0, small_dt=1.0e-10,
                stream=None):
         """Maestro::EstDt (advective and force constraints): returns (dt, dt_estimate, umax,

@@ -334,3 +334,40 @@ def test_flux_register_equals_face_averaging_and_conserves_mass():
             return r[0][key][RHO][~covered].sum() * 8.0 + r[1][key][RHO][fm].sum()
 
         assert abs(mass("snew") - mass("sold_end")) <= 1e-13 * abs(mass("sold_end")), rt
+
+
+@pytest.mark.parametrize("bc", ["outflow_top", "walls"])
+def test_mac_projection_oracle_meets_its_constraint(bc):
+    """oracle/mo_macproj.py (Maestro::MacProj restated and solved to 1e-14): after the
+    projection div(beta0 u) = macrhs (up to the rhs mean when no face is Dirichlet), and the
+    correction is a gradient: u changes by -(B / beta0) grad phi."""
+    import mo_macproj
+    from maestroex_gb300.params import INTERIOR, OUTFLOW, SLIPWALL
+    lo = (INTERIOR, INTERIOR, SLIPWALL)
+    hi = (INTERIOR, INTERIOR, OUTFLOW if bc == "outflow_top" else SLIPWALL)
+    rng = np.random.default_rng(71)
+    nx, ny, nz = 8, 8, 12
+    dx = (1.0, 1.0, 1.0)
+    rho = 1.0 + 0.5 * rng.random((nz, ny, nx))
+    beta0 = np.linspace(2.0, 1.0, nz)
+    umac = [rng.standard_normal((nz, ny, nx + 1)), rng.standard_normal((nz, ny + 1, nx)),
+            rng.standard_normal((nz + 1, ny, nx))]
+    umac[0][..., -1] = umac[0][..., 0]
+    umac[1][:, -1, :] = umac[1][:, 0, :]
+    umac[2][0] = 0.0
+    if bc == "walls":
+        umac[2][-1] = 0.0
+    macrhs = 0.1 * rng.standard_normal((nz, ny, nx))
+    out, phi = mo_macproj.mac_project(umac, macrhs, rho, beta0, dx, lo, hi)
+    b0e = mo_macproj.cell_to_edge(beta0)
+    bz = [beta0[:, None, None], beta0[:, None, None], b0e[:, None, None]]
+    bu = [u * b for u, b in zip(out, bz)]
+    div = (bu[0][:, :, 1:] - bu[0][:, :, :-1]) + (bu[1][:, 1:] - bu[1][:, :-1]) + (bu[2][1:] - bu[2][:-1])
+    bi = [u * b for u, b in zip(umac, bz)]
+    div0 = (bi[0][:, :, 1:] - bi[0][:, :, :-1]) + (bi[1][:, 1:] - bi[1][:, :-1]) + (bi[2][1:] - bi[2][:-1])
+    target = macrhs - (macrhs - div0).mean() if bc == "walls" else macrhs
+    assert np.abs(div - target).max() <= 1e-11 * np.abs(target).max()
+    # interior x faces: the change is -(B / beta0) (phi_i - phi_{i-1}) / dx
+    B = beta0[:, None, None] ** 2 / (0.5 * (rho[:, :, 1:] + rho[:, :, :-1]))
+    du = -(B / beta0[:, None, None]) * (phi[:, :, 1:] - phi[:, :, :-1])
+    assert np.allclose(out[0][:, :, 1:-1] - umac[0][:, :, 1:-1], du, rtol=1e-9, atol=1e-12)
