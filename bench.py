@@ -421,6 +421,73 @@ def run_adjoint(args, barrier):
     }
 
 
+def run_mac_projection(args, barrier):
+    """MAC projection (Maestro::MacProj, plane-parallel, one level) on the headline layout:
+    256^3 in 64 boxes of 64^3, periodic x / y, slip wall below and outflow above (Dirichlet
+    phi = 0 there), the seeded atmosphere's density, beta0 = rho0, a MAC velocity of the
+    workload's magnitude with a seeded perturbation and macrhs = beta0 (S - Sbar) of 1e-3 of
+    it, solved to the reference's tolerance (1e-10 of max|rhs|, max norm).  Times one call:
+    gathers, multigrid V-cycles, correction and ghost refill."""
+    import torch
+    from maestroex_gb300 import configs
+    from maestroex_gb300.params import INTERIOR, OUTFLOW, RHO, SLIPWALL
+    from maestroex_gb300.stage import MultiFab, make_stage
+    n = args.n
+    cfg = configs.planar_config(n=(n, n, n), nspec=2, ppm_type=1, max_grid=min(64, n),
+                                bc_lo=(INTERIOR, INTERIOR, SLIPWALL), bc_hi=(INTERIOR, INTERIOR, OUTFLOW),
+                                rho_pert=1e-3, w0_amp=0.0, seed=20261203 + 80)
+    rng = np.random.default_rng(20261203 + 81)
+    st = make_stage(cfg)
+    boxes = cfg["boxes"]
+    umax = float(np.abs(cfg["uold"]).max())
+    shapes = [(n, n, n + 1), (n, n + 1, n), (n + 1, n, n)]
+    um = [MultiFab(boxes, 1, 1, nodal=d) for d in range(3)]
+    snap = []
+    for d in range(3):
+        u = umax * (0.5 + 0.1 * rng.standard_normal(shapes[d]))
+        if d == 2:
+            u[0] = 0.0  # the wall
+        else:
+            np.moveaxis(u, 2 - d, -1)[..., -1] = np.moveaxis(u, 2 - d, -1)[..., 0]
+        um[d].from_domain(torch.from_numpy(u[None]))
+        snap.append([t.clone() for t in um[d].fabs])
+    beta0 = cfg["rho0_old"]
+    rh = MultiFab(boxes, 1, 0).from_domain(
+        torch.from_numpy((1e-3 * umax / cfg["dx"][0] * beta0[:, None, None] * rng.standard_normal((n, n, n)))[None]))
+    ro = MultiFab(boxes, 1, 0).from_domain(torch.from_numpy(cfg["sold"][RHO][None].copy()))
+    phi = MultiFab(boxes, 1, 0)
+
+    def reset():
+        for d in range(3):
+            for dst, src in zip(um[d].fabs, snap[d]):
+                dst.copy_(src)
+
+    for _ in range(2):
+        reset()
+        st.mac_project(um, rh, ro, beta0, macphi=phi)
+    barrier()
+    reps = max(1, args.steps // 2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tot, it, ratio = 0.0, 0, 0.0
+    for _ in range(reps):
+        reset()
+        torch.cuda.synchronize()
+        e0.record()
+        it, ratio = st.mac_project(um, rh, ro, beta0, macphi=phi)
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    launches = st.launch_count()
+    st.close()
+    del um, snap, rh, ro, phi
+    torch.cuda.empty_cache()
+    ms = tot / reps
+    return {"workload": f"MAC projection, {n}^3 in {len(boxes)} boxes of {min(64, n)}^3, periodic x/y, slip wall "
+                        "below, outflow above, seeded atmosphere density, beta0 = rho0, tolerance 1e-10 of max|rhs|",
+            "ms_per_call": ms, "v_cycles": it, "resid_ratio": ratio, "gpu_launches": launches,
+            "value": n ** 3 / (ms * 1e-3), "unit": "cells/s"}
+
+
 def run_spherical_adjoint(args, barrier):
     """Spherical multi-step adjoint: a full star on one level, n^3 in boxes of 64^3, NumSpec
     21, ppm_type 2, outflow faces, w0 of amplitude 1e5 cm/s, the velocity held fixed and
@@ -710,6 +777,7 @@ def main():
                     help="bubble radius parameter of the spherical workload's level 1 (0.06: about 11%% of the domain)")
     ap.add_argument("--no-spherical", action="store_true")
     ap.add_argument("--no-sph-adjoint", action="store_true")
+    ap.add_argument("--no-mac", action="store_true")
     ap.add_argument("--sph-adj-n", type=int, default=128, help="extent of the spherical adjoint workload")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
@@ -882,6 +950,7 @@ def main():
     vel = None if args.no_velocity else run_velocity(args, barrier)
     sph = None if args.no_spherical else run_spherical(args, barrier)
     sph_adj = None if args.no_sph_adjoint else run_spherical_adjoint(args, barrier)
+    mac = None if args.no_mac else run_mac_projection(args, barrier)
 
     if rank != 0:
         dist.destroy_process_group()
@@ -935,6 +1004,8 @@ def main():
         line["spherical"] = sph
     if sph_adj is not None:
         line["spherical_adjoint"] = sph_adj
+    if mac is not None:
+        line["mac_projection"] = mac
     if not args.no_cpu_baseline:
         cb = run_cpu_baseline(3, 1, nthreads=os.cpu_count() or 1)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
