@@ -205,17 +205,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample_config(nspec):
-    """Bounded CPU sample with the workload's box shape: 128^3 in 8 boxes of 64^3."""
+def cpu_sample_config(nspec, n=128, box=64):
+    """CPU sample with the workload's box shape: n^3 in boxes of box^3 (128^3 in 8 boxes of
+    64^3 for the bounded baseline next to the GPU line; the whole workload for the
+    reference arm)."""
     from maestroex_gb300 import configs
-    return configs.planar_config(n=(128, 128, 128), nspec=nspec, ppm_type=1, max_grid=64,
+    return configs.planar_config(n=(n, n, n), nspec=nspec, ppm_type=1, max_grid=box,
                                  seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
 
 
-def run_cpu_baseline(steps, warmup, nthreads=0):
+def run_cpu_baseline(steps, warmup, nthreads=0, nspec=13, n=128, box=64):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    cfg = cpu_sample_config(13)
+    cfg = cpu_sample_config(nspec, n, box)
     ncell = int(np.prod(cfg["n"]))
     want = ("snew",)
     for _ in range(warmup):
@@ -223,14 +225,77 @@ def run_cpu_baseline(steps, warmup, nthreads=0):
     times = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        pyoracle.run_stage(cfg, nthreads=nthreads, want=want)
+        res = pyoracle.run_stage(cfg, nthreads=nthreads, want=want)
         times.append(time.perf_counter() - t0)
     dt = float(np.median(times))
     cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
     return {"value": ncell / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "oracle on 128^3 cells in 8 boxes of 64^3, NumSpec 13, ppm_type 1 (same box shape "
-                      f"and per-cell work as the GPU workload), median of {steps} timed runs after {warmup}",
-            "s_per_sample": dt}
+            "sample": f"oracle on {n}^3 cells in {len(cfg['boxes'])} boxes of {box}^3, NumSpec {nspec}, ppm_type 1 "
+                      f"(same box shape and per-cell work as the GPU workload), median of {steps} timed runs after "
+                      f"{warmup}",
+            "s_per_sample": dt, "cfg": cfg, "snew": res["snew"]}
+
+
+def state_parity(gpu_levels, ref_levels, nspec):
+    """Largest relative difference of the updated state from the oracle's, per component:
+    max |gpu - ref| over the valid cells of every level divided by the component's max |ref|
+    (the benchmark's error definition), and the pointwise relative difference over the cells
+    where |ref| > 1e-3 max |ref|; `bitwise` when every value is identical."""
+    from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
+    names = {RHO: "rho", RHOH: "rhoh"}
+    names.update({FIRSTSPEC + s: f"rhoX{s + 1}" for s in range(nspec)})
+    per, point, bitwise = {}, 0.0, True
+    for c, name in names.items():
+        g = np.concatenate([np.asarray(x)[c][np.isfinite(np.asarray(r)[c])] for x, r in zip(gpu_levels, ref_levels)])
+        r = np.concatenate([np.asarray(r)[c][np.isfinite(np.asarray(r)[c])] for r in ref_levels])
+        scale = float(np.abs(r).max())
+        d = np.abs(g - r)
+        per[name] = float(d.max() / scale) if scale > 0 else float(d.max())
+        big = np.abs(r) > 1e-3 * scale
+        if big.any():
+            point = max(point, float((d[big] / np.abs(r[big])).max()))
+        bitwise &= bool(np.array_equal(g, r))
+    return {"max_rel_err_vs_oracle": max(per.values()), "pointwise_rel_err": point, "bitwise": bitwise,
+            "per_component": per, "tolerance": 1e-12}
+
+
+def run_parity(headline_ref, args):
+    """The GPU stage against the oracle on the benchmark workloads' shapes: the headline
+    layout (the CPU-baseline sample, whose oracle result is reused), the two-level AMR shape
+    and the spherical two-level shape, each at a size the oracle runs in seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    import torch
+    from maestroex_gb300 import capi, configs
+    from maestroex_gb300.stage import run_amr_stage_gpu, run_stage_gpu
+    out = {}
+    cfg = headline_ref["cfg"]
+    gpu = run_stage_gpu(cfg, mode=capi.MODE_GRAPH)
+    out["headline_layout"] = {"sample": f"{cfg['n'][0]}^3 in {len(cfg['boxes'])} boxes of 64^3, NumSpec "
+                                        f"{cfg['nspec']}, ppm_type 1, w0 != 0 (the CPU-baseline sample), graph mode",
+                              **state_parity([gpu["snew"]], [headline_ref["snew"]], cfg["nspec"])}
+    cfg = configs.two_level_sample(nspec=args.nspec)
+    t0 = time.perf_counter()
+    ref = pyoracle.run_stage_levels(cfg, want=("snew",))
+    t_or = time.perf_counter() - t0
+    gpu = run_amr_stage_gpu(cfg, mode=capi.MODE_GRAPH)
+    l1 = cfg["levels"][1]["boxes"]
+    out["amr"] = {"sample": f"two levels: level 0 64^3 in {len(cfg['levels'][0]['boxes'])} uneven boxes, level 1 "
+                            f"{len(l1)} boxes of 16-32 cells around 3 bubbles, NumSpec {args.nspec}, ppm_type 2, "
+                            "w0 != 0, graph mode", "oracle_s": t_or,
+                  **state_parity([g["snew"] for g in gpu], [r["snew"] for r in ref], args.nspec)}
+    cfg = configs.spherical_two_level_sample()
+    t0 = time.perf_counter()
+    ref = pyoracle.run_stage_levels(cfg, want=("snew",))
+    t_or = time.perf_counter() - t0
+    gpu = run_amr_stage_gpu(cfg, mode=capi.MODE_GRAPH)
+    out["spherical"] = {"sample": f"spherical full star, two levels: level 0 48^3 in "
+                                  f"{len(cfg['levels'][0]['boxes'])} uneven boxes, level 1 "
+                                  f"{len(cfg['levels'][1]['boxes'])} boxes, NumSpec 21, ppm_type 2, w0 1e5, "
+                                  "graph mode", "oracle_s": t_or,
+                        **state_parity([g["snew"] for g in gpu], [r["snew"] for r in ref], 21)}
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_amr(args, ws, steps, warmup, barrier):
@@ -304,13 +369,44 @@ def run_amr(args, ws, steps, warmup, barrier):
     }
 
 
+def fd_check(grad_of, jdiff, draw, want, max_tries, skip_tol=1e-7):
+    """Central-difference check of adjoint gradient entries.
+
+    draw() -> (field, comp, cell, x): a seeded random entry and its magnitude scale;
+    jdiff(field, comp, cell, h) = J(x + h) - J(x - h), the states differenced before the
+    weights are applied; grad_of(field, comp, cell) = the adjoint's entry.  Each entry is
+    differenced with h = 1e-6 x and h/2.  A limiter or upwind switch inside [x - h, x + h]
+    shows as a difference between the two quotients far above their O(h^2) truncation
+    error: such entries are skipped when the quotients differ by more than skip_tol
+    (1e-7, below the 1e-6 pass bar).  The error of an accepted entry is taken against the
+    Richardson extrapolation (4 D(h/2) - D(h)) / 3.  Stops after `want` accepted entries or
+    `max_tries` drawn ones."""
+    errs, skipped, tries = [], 0, 0
+    while len(errs) < want and tries < max_tries:
+        tries += 1
+        field, comp, cell, x = draw()
+        d = [jdiff(field, comp, cell, rel * x) / (2 * rel * x) for rel in (1e-6, 0.5e-6)]
+        scale = max(abs(d[0]), abs(d[1]), 1e-300)
+        if abs(d[0] - d[1]) > skip_tol * scale:
+            skipped += 1
+            continue
+        rich = (4.0 * d[1] - d[0]) / 3.0
+        errs.append(abs(grad_of(field, comp, cell) - rich) / scale)
+    return {"entries": len(errs), "skipped_limiter_switch": skipped,
+            "worst_rel_err": max(errs) if errs else None, "median_rel_err": float(np.median(errs)) if errs else None,
+            "pass_bar": 1e-6, "passed": bool(errs) and max(errs) <= 1e-6,
+            "h": "1e-6 max(|x|, rms/10) and h/2; entries whose two quotients differ by more than "
+                 f"{skip_tol:g} (a limiter switch inside [x - h, x + h]) are skipped; error against the Richardson "
+                 "extrapolation (4 D(h/2) - D(h)) / 3"}
+
+
 def run_adjoint(args, barrier):
     """Multi-step adjoint workload: 128^3 in 8 boxes of 64^3, NumSpec 3, ppm_type 1, 16 steps
     at CFL 0.5 with the velocity held fixed, J = sum(w rhoX + v rhoh) with w, v ~ N(0, 1),
     stored states every 4 steps.  Times the forward alone, the adjoint for dJ/d(state) and
-    the adjoint for dJ/d(state, velocity) (each call runs its own forward), and checks a
-    few gradient entries against central differences (h = 1e-6 max(|x|, rms/10)) of the
-    same forward."""
+    the adjoint for dJ/d(state, velocity) (each call runs its own forward), and checks
+    --fd-entries gradient entries at random cells against central differences of the same
+    forward (fd_check)."""
     import torch
     from maestroex_gb300 import configs
     from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
@@ -381,30 +477,28 @@ def run_adjoint(args, barrier):
     def dJ(a, b):
         return sum(float((x * (p - q)).sum()) for x, p, q in zip(wt.fabs, a.fabs, b.fabs))
 
-    checks, worst, kinks = [], 0.0, 0
     rms_s = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
     rms_u = np.sqrt((U ** 2).mean(axis=(1, 2, 3)))
-    for t, (field, comp) in enumerate([("s", RHOH), ("s", FIRSTSPEC), ("s", FIRSTSPEC + 2), ("s", RHO),
-                                       ("u", 0), ("u", 1), ("u", 2), ("u", 2)]):
+    kinds = [("s", RHOH), ("s", FIRSTSPEC), ("s", FIRSTSPEC + 1), ("s", FIRSTSPEC + 2), ("s", RHO),
+             ("u", 0), ("u", 1), ("u", 2)]
+
+    def draw():
+        field, comp = kinds[int(rng.integers(0, len(kinds)))]
         cell = tuple(int(v) for v in rng.integers(0, n, size=3))
+        X, R = (S, rms_s) if field == "s" else (U, rms_u)
         i, j, k = cell
-        X, R, G_ = (S, rms_s, G) if field == "s" else (U, rms_u, GU)
-        x = max(abs(X[comp, k, j, i]), 0.1 * R[comp])
-        fd = []
-        for rel in (1e-6, 0.5e-6):
-            h = rel * x
-            if field == "s":
-                a, b = final(u, perturbed(s0, comp, cell, h)), final(u, perturbed(s0, comp, cell, -h))
-            else:
-                a, b = final(perturbed(u, comp, cell, h), s0), final(perturbed(u, comp, cell, -h), s0)
-            fd.append(dJ(a, b) / (2 * h))
-        scale = max(abs(fd[0]), abs(fd[1]))
-        if abs(fd[0] - fd[1]) > 1e-5 * scale:
-            kinks += 1
-            continue
-        err = abs(G_[comp, k, j, i] - fd[0]) / max(scale, 1e-300)
-        worst = max(worst, err)
-        checks.append(err)
+        return field, comp, cell, max(abs(X[comp, k, j, i]), 0.1 * R[comp])
+
+    def jdiff(field, comp, cell, h):
+        if field == "s":
+            return dJ(final(u, perturbed(s0, comp, cell, h)), final(u, perturbed(s0, comp, cell, -h)))
+        return dJ(final(perturbed(u, comp, cell, h), s0), final(perturbed(u, comp, cell, -h), s0))
+
+    def grad_of(field, comp, cell):
+        i, j, k = cell
+        return (G if field == "s" else GU)[comp, k, j, i]
+
+    fd = fd_check(grad_of, jdiff, draw, args.fd_entries, 2 * args.fd_entries)
     st.close()
     torch.cuda.empty_cache()
     return {
@@ -415,9 +509,7 @@ def run_adjoint(args, barrier):
         "adj_over_fwd_state": ms_state / ms_fwd, "adj_over_fwd_state_velocity": ms_full / ms_fwd,
         "device_bytes_state": bytes_state, "device_bytes_state_velocity": bytes_full,
         "J": J_full,
-        "fd_check": {"entries": len(checks), "skipped_limiter_switch": kinks, "worst_rel_err": worst,
-                     "h": "1e-6 max(|x|, rms/10); entries whose h and h/2 differences disagree by more than 1e-5 "
-                           "(a limiter switch inside [x - h, x + h]) are skipped"},
+        "fd_check": fd,
     }
 
 
@@ -492,8 +584,9 @@ def run_spherical_adjoint(args, barrier):
     """Spherical multi-step adjoint: a full star on one level, n^3 in boxes of 64^3, NumSpec
     21, ppm_type 2, outflow faces, w0 of amplitude 1e5 cm/s, the velocity held fixed and
     independent of the state (no gravity), 8 steps with the state stored every 4.  Times the forward alone and
-    the adjoint for dJ/d(state) (which runs its own forward), and checks eight gradient
-    entries inside the star against central differences of the same forward."""
+    the adjoint for dJ/d(state) (which runs its own forward), and checks --sph-fd-entries
+    gradient entries inside the star against central differences of the same forward
+    (fd_check)."""
     import torch
     from maestroex_gb300 import configs
     from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
@@ -552,25 +645,25 @@ def run_spherical_adjoint(args, barrier):
                 m.fabs[bi][comp, k - bx[2], j - bx[1], i - bx[0]] += h
         return m
 
-    checks, worst, kinks = [], 0.0, 0
     rms = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
-    for comp in (RHOH, FIRSTSPEC, RHO, RHOH, FIRSTSPEC + 5, RHO, FIRSTSPEC + 11, RHOH):
+    comps = [RHOH, RHO] + [FIRSTSPEC + c for c in range(21)]
+
+    def draw():
+        comp = comps[int(rng.integers(0, len(comps)))]
         # a cell inside the star, within about half its radius of the centre
         cell = tuple(int(v) for v in n // 2 + rng.integers(-n // 5, n // 5 + 1, size=3))
         i, j, k = cell
-        x = max(abs(S[comp, k, j, i]), 0.1 * rms[comp])
-        fd = []
-        for rel in (1e-6, 0.5e-6):
-            h = rel * x
-            a, b = final(perturbed(comp, cell, h)), final(perturbed(comp, cell, -h))
-            fd.append(sum(float((x_ * (p - q)).sum()) for x_, p, q in zip(wt.fabs, a.fabs, b.fabs)) / (2 * h))
-        scale = max(abs(fd[0]), abs(fd[1]))
-        if abs(fd[0] - fd[1]) > 1e-5 * scale:
-            kinks += 1
-            continue
-        err = abs(G[comp, k, j, i] - fd[0]) / max(scale, 1e-300)
-        worst = max(worst, err)
-        checks.append(err)
+        return "s", comp, cell, max(abs(S[comp, k, j, i]), 0.1 * rms[comp])
+
+    def jdiff(field, comp, cell, h):
+        a, b = final(perturbed(comp, cell, h)), final(perturbed(comp, cell, -h))
+        return sum(float((x_ * (p - q)).sum()) for x_, p, q in zip(wt.fabs, a.fabs, b.fabs))
+
+    def grad_of(field, comp, cell):
+        i, j, k = cell
+        return G[comp, k, j, i]
+
+    fd = fd_check(grad_of, jdiff, draw, args.sph_fd_entries, 2 * args.sph_fd_entries)
     st.close()
     torch.cuda.empty_cache()
     return {
@@ -581,7 +674,7 @@ def run_spherical_adjoint(args, barrier):
                     f"{nsteps} steps, stored states every {ckpt}; J = sum(w rhoX + v rhoh_final), w, v ~ N(0,1)",
         "fwd_ms": ms_fwd, "adj_state_ms": ms_adj, "adj_over_fwd_state": ms_adj / ms_fwd, "device_bytes": nbytes,
         "J": J,
-        "fd_check": {"entries": len(checks), "skipped_limiter_switch": kinks, "worst_rel_err": worst},
+        "fd_check": fd,
     }
 
 
@@ -761,6 +854,7 @@ def main():
     ap.add_argument("--box", type=int, default=64)
     ap.add_argument("--nspec", type=int, default=13)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the GPU-vs-oracle parity samples")
     ap.add_argument("--no-per-box", action="store_true")
     ap.add_argument("--amr-n", type=int, default=256, help="level-0 extent of the two-level AMR workload")
     ap.add_argument("--no-amr", action="store_true")
@@ -768,6 +862,9 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=16)
     ap.add_argument("--adj-ckpt", type=int, default=4)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--fd-entries", type=int, default=64, help="central-difference entries of the adjoint leg")
+    ap.add_argument("--sph-fd-entries", type=int, default=64,
+                    help="central-difference entries of the spherical adjoint leg")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="run one adjoint call (state and velocity gradients) and exit (the command ncu captures)")
     ap.add_argument("--no-2d", action="store_true")
@@ -788,9 +885,12 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = run_cpu_baseline(max(args.steps, 1), min(warmup, 1))
-        cfg_desc = {"workload": f"3-D single level {args.n}^3 in boxes of {args.box}^3, NumSpec {args.nspec}, "
-                                "ppm_type 1, w0 != 0 (CPU restatement timed on a bounded sample)"}
+        # the whole workload: one step of the oracle at 256^3 is about 20 s on 16 cores
+        cb = run_cpu_baseline(max(args.steps, 1), 1, nthreads=os.cpu_count() or 1, nspec=args.nspec, n=args.n,
+                              box=args.box)
+        cfg_desc = {"workload": f"3-D single level {args.n}^3 in {len(cb['cfg']['boxes'])} boxes of {args.box}^3, "
+                                f"NumSpec {args.nspec}, ppm_type 1, w0 != 0, x/y periodic, z slipwall/outflow",
+                    "implementation": "CPU restatement of the reference stage (the oracle), OpenMP over boxes"}
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * cb["s_per_sample"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -816,6 +916,7 @@ def main():
         run_adjoint(args, lambda: torch.cuda.synchronize())
         return
 
+    t_start = time.perf_counter()
     cfg = configs.planar_config(n=(args.n,) * 3, nspec=args.nspec, ppm_type=1, max_grid=args.box,
                                 seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
     ncell = args.n ** 3
@@ -942,15 +1043,23 @@ def main():
     st.close()
     del st, buf, snap, sets
     torch.cuda.empty_cache()
-    amr = None
-    if not args.no_amr:
-        amr = run_amr(args, ws, max(1, args.steps // 2), warmup, barrier)
-    adj = None if args.no_adjoint else run_adjoint(args, barrier)
-    two_d = None if args.no_2d else run_2d(args, barrier)
-    vel = None if args.no_velocity else run_velocity(args, barrier)
-    sph = None if args.no_spherical else run_spherical(args, barrier)
-    sph_adj = None if args.no_sph_adjoint else run_spherical_adjoint(args, barrier)
-    mac = None if args.no_mac else run_mac_projection(args, barrier)
+    leg_s = {"headline": time.perf_counter() - t_start}
+
+    def leg(name, skip, fn):
+        if skip:
+            return None
+        t0 = time.perf_counter()
+        r = fn()
+        leg_s[name] = time.perf_counter() - t0
+        return r
+
+    amr = leg("amr", args.no_amr, lambda: run_amr(args, ws, max(1, args.steps // 2), warmup, barrier))
+    adj = leg("adjoint", args.no_adjoint, lambda: run_adjoint(args, barrier))
+    two_d = leg("two_d", args.no_2d, lambda: run_2d(args, barrier))
+    vel = leg("velocity_advance", args.no_velocity, lambda: run_velocity(args, barrier))
+    sph = leg("spherical", args.no_spherical, lambda: run_spherical(args, barrier))
+    sph_adj = leg("spherical_adjoint", args.no_sph_adjoint, lambda: run_spherical_adjoint(args, barrier))
+    mac = leg("mac_projection", args.no_mac, lambda: run_mac_projection(args, barrier))
 
     if rank != 0:
         dist.destroy_process_group()
@@ -1007,8 +1116,16 @@ def main():
     if mac is not None:
         line["mac_projection"] = mac
     if not args.no_cpu_baseline:
-        cb = run_cpu_baseline(3, 1, nthreads=os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        cb = run_cpu_baseline(5, 1, nthreads=os.cpu_count() or 1, nspec=args.nspec)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        c1 = run_cpu_baseline(3, 0, nthreads=1, nspec=args.nspec, n=64, box=64)
+        line["cpu_baseline_1core"] = {k: c1[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if not args.no_parity:
+            line["parity"] = run_parity(cb, args)
+            line["max_rel_err_vs_oracle"] = line["parity"]["headline_layout"]["max_rel_err_vs_oracle"]
+        leg_s["cpu_baseline_and_parity"] = time.perf_counter() - t0
+    line["leg_seconds"] = {k: round(v, 1) for k, v in leg_s.items()}
     print(json.dumps(line))
     if ws > 1:
         dist.destroy_process_group()

@@ -475,6 +475,29 @@ def workload_amr(n0=256, nspec=13, seed=20261203 + 3, cover=0.06, p_stop=0.8):
     return cfg
 
 
+def two_level_sample(nspec=13, n0=64, seed=20261203 + 3, **kw):
+    """The two-level AMR workload's shape at a size the oracle checks in seconds: level 0
+    n0^3 in uneven boxes (edges 16-64), level 1 (ratio 2) in boxes of 16-32 fine cells around
+    3 seeded bubbles (about 14% of the domain at n0 = 64), ppm_type 2, w0 != 0; both levels
+    evaluated at their own resolution (no injection)."""
+    rng = np.random.default_rng(seed)
+    l0 = uneven_boxes((n0,) * 3, [16, 32, 48, 64], rng, p_stop=0.35)
+    fine = bubble_boxes((n0,) * 3, nbubbles=3, cover=0.01, block_edges=(8, 16), max_edge=16,
+                        rng=np.random.default_rng(seed + 100))
+    return planar_amr_config(n0=(n0,) * 3, nspec=nspec, ppm_type=2, fine_boxes=fine, level0_boxes=l0, seed=seed,
+                             w0_amp=1.0e4, cfl=0.7, **kw)
+
+
+def spherical_two_level_sample(nspec=21, n0=48, seed=20261203 + 50):
+    """The spherical workload's shape at a size the oracle checks in seconds: the full star
+    on level 0 n0^3 in uneven boxes (edges 16-48) and a level 1 of 16-32-cell boxes around 3
+    bubbles (about 16% of the domain at n0 = 48), NumSpec 21, ppm_type 2, w0 amplitude 1e5."""
+    l0 = uneven_boxes((n0,) * 3, [16, 32, 48], np.random.default_rng(seed), p_stop=0.35)
+    fine = bubble_boxes((n0,) * 3, nbubbles=3, cover=0.01, block_edges=(8, 16), max_edge=16,
+                        rng=np.random.default_rng(seed + 1))
+    return spherical_amr_config(n0=n0, nspec=nspec, ppm_type=2, fine_boxes=fine, level0_boxes=l0, w0_amp=1.0e5)
+
+
 def planar_config_2d(n=(64, 64), nspec=3, ppm_type=1, bc_lo=(INTERIOR, SLIPWALL), bc_hi=(INTERIOR, OUTFLOW),
                      max_grid=None, boxes=None, seed=20261203, rho_pert=0.0, w0_amp=0.0, cfl=0.7, gpi_amp=0.0,
                      species_pred_type=1, enthalpy_pred_type=1, slope_order=4, evolve_base_state=1):
