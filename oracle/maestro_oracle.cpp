@@ -2531,6 +2531,30 @@ int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const m
     }
 }
 
+int mo_slopes(int slope_order, int d, const int* dom, const int* bx, const mo_fab* s, int ncomp, const int* bcs,
+              const mo_fab* slope) {
+    try {
+        mo::Box D, b;
+        for (int e = 0; e < 3; ++e) {
+            D.lo[e] = dom[e];
+            D.hi[e] = dom[3 + e];
+            b.lo[e] = bx[e];
+            b.hi[e] = bx[3 + e];
+        }
+        std::vector<mo::BCRec> r(ncomp);
+        for (int n = 0; n < ncomp; ++n)
+            for (int e = 0; e < 3; ++e) {
+                r[n].lo[e] = bcs[6 * n + e];
+                r[n].hi[e] = bcs[6 * n + 3 + e];
+            }
+        mo::Slope_dir(slope_order, D, b, arr_of(s), arr_of(slope), ncomp, r, 0, d);
+        return 0;
+    } catch (const std::exception& e) {
+        mo::g_err = e.what();
+        return -1;
+    }
+}
+
 int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
               int start_comp, int num_comp, int is_conservative, const mo_fab* args) {
     try {

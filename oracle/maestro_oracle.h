@@ -112,6 +112,12 @@ typedef struct {
 int mo_ppm(const mo_params* p, const int* bx, const mo_fab* s, int comp, const mo_fab* u, const mo_fab* v,
            const mo_fab* w, int is_umac, const int* bc, const mo_fab* Ip, const mo_fab* Im);
 
+/* Maestro::Slopex/y/z (Source/MaestroSlopes.cpp:6-600) in direction d over the cell box
+ * bx[6] for components 0..ncomp-1 of s into slope, domain dom[6]; bcs[6 n + (0..5)] are
+ * component n's BCTypes (lo[3], hi[3]). */
+int mo_slopes(int slope_order, int d, const int* dom, const int* bx, const mo_fab* s, int ncomp, const int* bcs,
+              const mo_fab* slope);
+
 /* One Maestro member function of the stage on one 3-D level, on caller FABs that hold
  * ghost cells as the caller filled them: args[slot * nboxes + b] is box b's FAB of argument
  * `slot` (p = NULL for arguments the function does not take).  base gives the base state

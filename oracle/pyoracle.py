@@ -250,6 +250,23 @@ def ppm(params, bx, s, s_lo, comp, vel, vel_lo, is_umac, bc, checked=True):
     return Ip, Im
 
 
+def slopes(slope_order, d, dom, bx, s, s_lo, bcs, checked=True):
+    """Oracle Maestro::Slopex/y/z in direction d over bx for every component of s
+    ([nc, nz, ny, nx] at s_lo); bcs: one (lo0, lo1, lo2, hi0, hi1, hi2) per component.
+    Returns the slopes [nc, nz, ny, nx] on bx (NaN where not written)."""
+    n = [bx[3 + e] - bx[e] + 1 for e in range(3)]
+    out = np.full((s.shape[0], n[2], n[1], n[0]), np.nan)
+    keep = []
+    fs, a = fab_of(s, s_lo); keep.append(a)
+    fo, _ = fab_of(out, bx[:3])
+    L = lib(checked)
+    rc = L.mo_slopes(int(slope_order), int(d), (C.c_int * 6)(*dom), (C.c_int * 6)(*bx), C.byref(fs), s.shape[0],
+                     (C.c_int * (6 * len(bcs)))(*[v for b in bcs for v in b]), C.byref(fo))
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.mo_last_error().decode())
+    return out
+
+
 MO_SLOT = dict(utilde=0, ufull=1, utrans=2, umac=5, force=8, state=9, snew=10, sedge=11, sflux=14, eta=17)
 MO_FACE_SLOTS = ("utrans", "umac", "sedge", "sflux")
 MO_NSLOT = 18

@@ -1,0 +1,54 @@
+"""The oracle against golden fixtures written by the reference's own PPM and slope
+functions (tests/golden/make_golden.py): bit for bit.  Runs on every host; the fixtures
+carry the reference's results where its sources are absent."""
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+from maestroex_gb300 import configs
+from maestroex_gb300.params import make_params
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ppm_slopes.npz")
+
+
+def golden():
+    return np.load(GOLDEN)
+
+
+def ppm_fixture(g, c):
+    pre = f"ppm{c}_"
+    m = [int(v) for v in g[pre + "meta"]]
+    ppm_type, is_umac, bc, bx, s_lo, dom_n = m[0], m[1], m[2:8], tuple(m[8:14]), m[14:17], tuple(m[17:20])
+    cfg = configs.planar_config(n=dom_n, nspec=1, ppm_type=ppm_type, max_grid=max(dom_n))
+    p = make_params(cfg)
+    p.dt, p.rel_eps = float(g[pre + "real"][0]), float(g[pre + "real"][1])
+    for d in range(3):
+        p.dx[d] = float(g[pre + "real"][2 + d])
+    vel = [g[pre + f"vel{d}"] for d in range(3)]
+    return p, ppm_type, is_umac, bc, bx, g[pre + "s"], s_lo, vel, g[pre + "Ip"], g[pre + "Im"]
+
+
+def n_fixtures(g, kind):
+    return sum(1 for k in g.files if k.startswith(kind) and k.endswith("_meta"))
+
+
+@pytest.mark.parametrize("c", range(6))
+def test_oracle_ppm_matches_golden(c):
+    g = golden()
+    assert n_fixtures(g, "ppm") == 6
+    p, ppm_type, is_umac, bc, bx, s, s_lo, vel, Ip, Im = ppm_fixture(g, c)
+    a, b = pyoracle.ppm(p, bx, s, s_lo, 1, vel, [bx[:3]] * 3, is_umac, bc)
+    assert np.array_equal(a, Ip) and np.array_equal(b, Im)
+
+
+@pytest.mark.parametrize("c", range(6))
+def test_oracle_slopes_match_golden(c):
+    g = golden()
+    assert n_fixtures(g, "slope") == 6
+    m = [int(v) for v in g[f"slope{c}_meta"]]
+    so, d, dom, bx, lo = m[0], m[1], tuple(m[2:8]), tuple(m[8:14]), m[14:17]
+    bcs = [tuple(int(v) for v in b) for b in g[f"slope{c}_bcs"]]
+    out = pyoracle.slopes(so, d, dom, bx, g[f"slope{c}_s"], lo, bcs)
+    assert np.array_equal(out, g[f"slope{c}_slope"])

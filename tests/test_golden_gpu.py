@@ -1,0 +1,33 @@
+"""The GPU library's PPM (madv_ppm, the drop-in for Maestro::PPM) against golden fixtures
+written by the reference's own PPM (tests/golden/make_golden.py): bit for bit."""
+import numpy as np
+import pytest
+
+from test_golden import golden, ppm_fixture
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from maestroex_gb300 import build
+    build.build_library()
+
+
+@pytest.mark.parametrize("c", range(6))
+def test_madv_ppm_matches_golden(c):
+    import torch
+    from maestroex_gb300.stage import ScalarAdvectionStage
+    p, ppm_type, is_umac, bc, bx, s, s_lo, vel, Ip_ref, Im_ref = ppm_fixture(golden(), c)
+    st = ScalarAdvectionStage(p)
+    dev = torch.device("cuda")
+    ts = torch.from_numpy(np.ascontiguousarray(s)).to(dev)
+    tv = [torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in vel]
+    n = [bx[3 + d] - bx[d] + 1 for d in range(3)]
+    Ip = torch.full((3, n[2], n[1], n[0]), float("nan"), dtype=torch.float64, device=dev)
+    Im = torch.full_like(Ip, float("nan"))
+    st.ppm(bx, ts, s_lo, 1, tv, [bx[:3]] * 3, is_umac, bc, Ip, Im)
+    torch.cuda.synchronize()
+    assert np.array_equal(Ip.cpu().numpy(), Ip_ref)
+    assert np.array_equal(Im.cpu().numpy(), Im_ref)
+    st.close()
