@@ -52,6 +52,15 @@ KERNEL_WORK = {
 STAGE_FP64_PER_CELL = 157.04  # FP64 warp instructions per valid cell, whole stage
 
 
+def jsonable(o):
+    """json.dumps default: numpy scalars and arrays as Python numbers and lists."""
+    if isinstance(o, np.generic):
+        return o.item()
+    if isinstance(o, np.ndarray):
+        return o.tolist()
+    raise TypeError(f"not JSON serialisable: {type(o).__name__}")
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -381,7 +390,7 @@ def fd_check(grad_of, jdiff, draw, want, max_tries, skip_tol=1e-7):
     (1e-7, below the 1e-6 pass bar).  The error of an accepted entry is taken against the
     Richardson extrapolation (4 D(h/2) - D(h)) / 3.  Stops after `want` accepted entries or
     `max_tries` drawn ones."""
-    errs, skipped, tries = [], 0, 0
+    errs, skipped, tries = [], 0, 0  # errors as Python floats
     while len(errs) < want and tries < max_tries:
         tries += 1
         field, comp, cell, x = draw()
@@ -391,10 +400,10 @@ def fd_check(grad_of, jdiff, draw, want, max_tries, skip_tol=1e-7):
             skipped += 1
             continue
         rich = (4.0 * d[1] - d[0]) / 3.0
-        errs.append(abs(grad_of(field, comp, cell) - rich) / scale)
+        errs.append(float(abs(grad_of(field, comp, cell) - rich) / scale))
     return {"entries": len(errs), "skipped_limiter_switch": skipped,
             "worst_rel_err": max(errs) if errs else None, "median_rel_err": float(np.median(errs)) if errs else None,
-            "pass_bar": 1e-6, "passed": bool(errs) and max(errs) <= 1e-6,
+            "pass_bar": 1e-6, "passed": bool(errs) and bool(max(errs) <= 1e-6),
             "h": "1e-6 max(|x|, rms/10) and h/2; entries whose two quotients differ by more than "
                  f"{skip_tol:g} (a limiter switch inside [x - h, x + h]) are skipped; error against the Richardson "
                  "extrapolation (4 D(h/2) - D(h)) / 3"}
@@ -897,7 +906,7 @@ def main():
                 "data": "synthetic", "config": cfg_desc,
                 "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(line, default=jsonable))
         return
 
     import torch
@@ -1051,6 +1060,9 @@ def main():
         t0 = time.perf_counter()
         r = fn()
         leg_s[name] = time.perf_counter() - t0
+        # progress on stderr (the JSON line on stdout comes at the end)
+        print(json.dumps({"leg": name, "seconds": round(leg_s[name], 1), "result": r}, default=jsonable),
+              file=sys.stderr, flush=True)
         return r
 
     amr = leg("amr", args.no_amr, lambda: run_amr(args, ws, max(1, args.steps // 2), warmup, barrier))
@@ -1126,7 +1138,7 @@ def main():
             line["max_rel_err_vs_oracle"] = line["parity"]["headline_layout"]["max_rel_err_vs_oracle"]
         leg_s["cpu_baseline_and_parity"] = time.perf_counter() - t0
     line["leg_seconds"] = {k: round(v, 1) for k, v in leg_s.items()}
-    print(json.dumps(line))
+    print(json.dumps(line, default=jsonable))
     if ws > 1:
         dist.destroy_process_group()
 

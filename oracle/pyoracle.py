@@ -277,6 +277,12 @@ def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservativ
     """Oracle mo_member: one Maestro member function on caller FABs.  args maps a slot name
     to the per-box FABs [(array [nc, nz, ny, nx], lo), ...] (three such lists, one per
     direction, for utrans / umac / sedge / sflux).  Outputs are written into the arrays."""
+    L = lib(checked)
+    member_call(L, L.mo_member, L.mo_last_error, cfg, fn, args, which_step, start_comp, num_comp, is_conservative)
+
+
+def member_call(L, entry, last_error, cfg, fn, args, which_step, start_comp, num_comp, is_conservative):
+    """Calls a C entry with mo_member's arguments (the oracle's, or the reference build's)."""
     from maestroex_gb300.params import make_params
     p = make_params(cfg)
     nb = len(cfg["boxes"])
@@ -302,12 +308,11 @@ def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservativ
                  "p0_old", "p0_new", "psi", "grav_cell", "w0_force", "w0", "rho0_predicted_edge"):
         setattr(inp, name, arr(cfg[name]))
     boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
-    L = lib(checked)
-    L.mo_member.restype = C.c_int
-    rc = L.mo_member(C.byref(p), nb, boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp), MO_FN[fn],
-                     which_step, start_comp, num_comp, is_conservative, tab)
+    entry.restype = C.c_int
+    rc = entry(C.byref(p), nb, boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp), MO_FN[fn],
+               which_step, start_comp, num_comp, is_conservative, tab)
     if rc != 0:
-        raise RuntimeError("oracle: " + L.mo_last_error().decode())
+        raise RuntimeError(last_error().decode())
 
 
 def lib_tl():

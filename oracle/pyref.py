@@ -69,3 +69,11 @@ def slopes(slope_order, d, dom, bx, s, s_lo, bcs):
     _check(lib().ref_slopes(int(slope_order), int(d), (C.c_int * 6)(*dom), (C.c_int * 6)(*bx), C.byref(fs),
                             s.shape[0], (C.c_int * (6 * len(bcs)))(*[v for b in bcs for v in b]), C.byref(fo)))
     return out
+
+
+def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservative=0):
+    """The reference's own member function on caller FABs, same arguments as
+    pyoracle.member (outputs written into the argument arrays, valid cells / faces only)."""
+    L = lib()
+    pyoracle.member_call(L, L.ref_member, L.ref_last_error, cfg, fn, args, which_step, start_comp, num_comp,
+                         is_conservative)

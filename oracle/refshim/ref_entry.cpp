@@ -6,11 +6,69 @@
 #include <string>
 
 #include "Maestro.H"
+#include "maestro_oracle.h"
 
 namespace maestro {
-int ppm_type = 1;
+int reflux_type = 1;
+int maestro_verbose = 0;
+amrex::Real cfl = 0.5;
+amrex::Real init_shrink = 1.0;
+amrex::Real small_dt = 1.e-10;
+amrex::Real max_dt = 1.e33;
+amrex::Real fixed_dt = -1.0;
+bool use_soundspeed_firstdt = false;
+bool use_divu_firstdt = false;
+bool spherical = false;
+bool octant = false;
+bool do_sponge = false;
+amrex::Real anelastic_cutoff_density = -1.0;
+amrex::Real base_cutoff_density = -1.0;
+amrex::Real burning_cutoff_density_lo = -1.0;
+amrex::Real burning_cutoff_density_hi = 1.e100;
+amrex::Real buoyancy_cutoff_factor = 5.0;
+bool evolve_base_state = true;
+bool use_exact_base_state = false;
+bool average_base_state = false;
+bool do_eos_h_above_cutoff = true;
+int enthalpy_pred_type = 1;
+int species_pred_type = 1;
 int slope_order = 4;
+int ppm_type = 1;
+int ppm_trace_forces = 0;
+bool use_centrifugal = true;
+bool use_alt_energy_fix = true;
+int s0_interp_type = 3;
+int w0_interp_type = 2;
+int s0mac_interp_type = 1;
+int w0mac_interp_type = 1;
+int drdxfac = 5;
 }  // namespace maestro
+
+amrex::IntVect Maestro::nodal_flag(1, 1, 1);
+amrex::IntVect Maestro::nodal_flag_x(1, 0, 0);
+amrex::IntVect Maestro::nodal_flag_y(0, 1, 0);
+amrex::IntVect Maestro::nodal_flag_z(0, 0, 1);
+
+// AMReX's fills and averages on one level.  Ghost cells are the caller's business here:
+// every comparison made with this library covers valid cells and faces only, so the
+// stand-ins keep ghost data as it is.  Averaging down has nothing to do on one level.
+void Maestro::FillPatch(Real, amrex::Vector<MF>&, amrex::Vector<MF>&, amrex::Vector<MF>&, int, int, int, int,
+                        const BCs&, int) {
+    if (finest_level > 0) amrex::Abort("stand-in FillPatch: one level only");
+}
+void Maestro::FillPatch(int, Real, MF&, amrex::Vector<MF>&, amrex::Vector<MF>&, int, int, int, int, const BCs&, int) {
+    if (finest_level > 0) amrex::Abort("stand-in FillPatch: one level only");
+}
+void Maestro::AverageDown(amrex::Vector<MF>&, int, int) {
+    if (finest_level > 0) amrex::Abort("stand-in AverageDown: one level only");
+}
+void Maestro::AverageDownFaces(FaceMFs&) {
+    if (finest_level > 0) amrex::Abort("stand-in AverageDownFaces: one level only");
+}
+void Maestro::FillUmacGhost(FaceMFs&, int) {}
+void Maestro::FillPatchUedge(FaceMFs&) {
+    if (finest_level > 0) amrex::Abort("stand-in FillPatchUedge: one level only");
+}
 
 using namespace amrex;
 
@@ -38,6 +96,135 @@ Box box_of(const int* b) {
     }
     return bx;
 }
+void set_params(const mo_params* p) {
+    maestro::ppm_type = p->ppm_type;
+    maestro::slope_order = p->slope_order;
+    maestro::ppm_trace_forces = p->ppm_trace_forces;
+    maestro::spherical = p->spherical;
+    maestro::use_exact_base_state = p->use_exact_base_state;
+    maestro::evolve_base_state = p->evolve_base_state;
+    maestro::species_pred_type = p->species_pred_type;
+    maestro::enthalpy_pred_type = p->enthalpy_pred_type;
+    maestro::reflux_type = p->reflux_type;
+    maestro::base_cutoff_density = p->base_cutoff_density;
+    maestro::buoyancy_cutoff_factor = p->buoyancy_cutoff_factor;
+    maestro::do_eos_h_above_cutoff = p->do_eos_h_above_cutoff;
+}
+
+// phys_bc -> BCType of the velocity, scalar and "first-order extrapolation" components,
+// the table of Maestro::BCSetup (Source/MaestroSetup.cpp:329-500)
+void bc_setup(Maestro& m) {
+    using namespace amrex::BCType;
+    m.bcs_s.assign(Nscal, BCRec());
+    m.bcs_u.assign(AMREX_SPACEDIM, BCRec());
+    m.bcs_f.assign(Nscal, BCRec());
+    for (int side = 0; side < 2; ++side)
+        for (int dir = 0; dir < 3; ++dir) {
+            const int pb = side == 0 ? m.phys_bc.lo(dir) : m.phys_bc.hi(dir);
+            int u, s, t, pi, f;
+            int udir = -999;
+            switch (pb) {
+                case 0: u = s = t = pi = f = int_dir; break;                                  // interior
+                case 1: u = s = t = ext_dir; pi = f = foextrap; break;                         // inflow
+                case 2: u = s = t = foextrap; pi = ext_dir; f = foextrap; break;               // outflow
+                case 3: u = s = t = pi = f = reflect_even; udir = reflect_odd; break;          // symmetry
+                case 4: u = s = t = hoextrap; udir = ext_dir; pi = f = foextrap; break;        // slipwall
+                case 5: u = ext_dir; s = t = hoextrap; pi = f = foextrap; break;               // noslipwall
+                default: amrex::Abort("Invalid phys_bc");
+            }
+            auto set = [&](BCRec& r, int v) { side == 0 ? r.setLo(dir, v) : r.setHi(dir, v); };
+            for (int c = 0; c < AMREX_SPACEDIM; ++c) set(m.bcs_u[c], (c == dir && udir != -999) ? udir : u);
+            set(m.bcs_s[Rho], s);
+            set(m.bcs_s[RhoH], s);
+            for (int c = FirstSpec; c < FirstSpec + NumSpec; ++c) set(m.bcs_s[c], s);
+            set(m.bcs_s[Temp], t);
+            set(m.bcs_s[Pi], pi);
+            for (int c = 0; c < Nscal; ++c) set(m.bcs_f[c], f);
+        }
+}
+
+void setup(Maestro& m, const mo_params* p, int nboxes, const int* boxes) {
+    if (p->dim == 2) amrex::Abort("the reference build here is 3-D");
+    if (p->nspec != NumSpec) amrex::Abort("the reference build has NumSpec " + std::to_string(NumSpec));
+    set_params(p);
+    m.dt = p->dt;
+    m.rel_eps = p->rel_eps;
+    m.finest_level = 0;
+    Geometry g;
+    for (int d = 0; d < 3; ++d) {
+        g.domain.lo[d] = p->dom_lo[d];
+        g.domain.hi[d] = p->dom_hi[d];
+        g.dx_[d] = p->dx[d];
+        g.rb.lo_[d] = p->prob_lo[d];
+        g.rb.hi_[d] = p->prob_hi[d];
+        g.per[d] = p->phys_bc_lo[d] == 0;
+        m.phys_bc.setLo(d, p->phys_bc_lo[d]);
+        m.phys_bc.setHi(d, p->phys_bc_hi[d]);
+    }
+    m.geom.assign(1, g);
+    std::vector<Box> bl;
+    for (int b = 0; b < nboxes; ++b) bl.push_back(box_of(boxes + 6 * b));
+    m.grids.assign(1, BoxArray(bl));
+    m.dmap.assign(1, DistributionMapping());
+    bc_setup(m);
+}
+
+// A MultiFab on ba (typed nodal in direction `nodal` if >= 0) with ng ghosts and nc
+// components holding the caller's FABs where they overlap (NaN elsewhere).
+void mf_from(MultiFab& mf, const BoxArray& ba, const mo_fab* f, int nc, int ng, int nodal) {
+    BoxArray b2 = nodal >= 0 ? convert(ba, IntVect(nodal == 0, nodal == 1, nodal == 2)) : ba;
+    mf.define(b2, DistributionMapping(), nc, ng);
+    for (int i = 0; i < mf.size(); ++i) {
+        const auto dst = mf.array(i);
+        const auto src = arr<Real>(reinterpret_cast<const RefFab*>(&f[i]));
+        const int ncopy = std::min(nc, f[i].nc);
+        ParallelFor(mf.fabs_[i].box, ncopy, [&](int x, int y, int z, int n) {
+            if (src.contains(x, y, z)) dst(x, y, z, n) = src(x, y, z, n);
+        });
+    }
+}
+
+// copies components [c0, c0 + nc) of the valid region of mf into the caller's FABs
+void mf_to(const MultiFab& mf, const mo_fab* f, int c0, int nc) {
+    for (int i = 0; i < mf.size(); ++i) {
+        const auto src = mf.array(i);
+        const auto dst = arr<Real>(reinterpret_cast<const RefFab*>(&f[i]));
+        const Box vb = mf.boxArray()[i];
+        ParallelFor(vb, nc, [&](int x, int y, int z, int n) {
+            if (dst.contains(x, y, z)) dst(x, y, z, c0 + n) = src(x, y, z, c0 + n);
+        });
+    }
+}
+
+int member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
+           int start_comp, int num_comp, int is_cons, const mo_fab* args) {
+    (void)base;
+    (void)which_step;
+    Maestro m;
+    setup(m, p, nboxes, boxes);
+    const BoxArray& ba = m.grids[0];
+    const int ng_s = maestro::ppm_type == 2 ? 4 : 3;
+    auto A = [&](int slot) { return args + (long)slot * nboxes; };
+    Vector<MultiFab> m1(1), m2(1), m3(1);
+    Vector<std::array<MultiFab, AMREX_SPACEDIM>> f1(1), f2(1);
+    switch (fn) {
+        case MO_MAKE_EDGE_SCAL: {
+            mf_from(m1[0], ba, A(MO_STATE), Nscal, ng_s, -1);
+            mf_from(m2[0], ba, A(MO_FORCE), Nscal, 1, -1);
+            for (int d = 0; d < 3; ++d) {
+                mf_from(f1[0][d], ba, A(MO_UMAC0 + d), 1, 1, d);
+                f2[0][d].define(convert(ba, IntVect(d == 0, d == 1, d == 2)), DistributionMapping(), Nscal, 0);
+                f2[0][d].setVal(0.0);
+            }
+            m.MakeEdgeScal(m1, f2, f1, m2, false, m.bcs_s, Nscal, start_comp, start_comp, num_comp, is_cons != 0);
+            for (int d = 0; d < 3; ++d) mf_to(f2[0][d], A(MO_SEDGE0 + d), start_comp, num_comp);
+            return 0;
+        }
+        default:
+            amrex::Abort("member function not in this reference build");
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -86,6 +273,20 @@ int ref_slopes(int slope_order_, int d, const int* dom, const int* bx, const Ref
         if (d == 1) Maestro::Slopey(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         if (d == 2) Maestro::Slopez(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         return 0;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+/* One Maestro member function on one 3-D level, the arguments of mo_member
+ * (oracle/maestro_oracle.h): the same slots, per-box FABs and outputs, run by the
+ * reference's own member function on MultiFabs holding copies of the caller's FABs;
+ * outputs are copied back on the valid cells / faces. */
+int ref_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
+               int start_comp, int num_comp, int is_cons, const mo_fab* args) {
+    try {
+        return member(p, nboxes, boxes, base, fn, which_step, start_comp, num_comp, is_cons, args);
     } catch (const std::exception& e) {
         g_err = e.what();
         return -1;
