@@ -59,8 +59,10 @@ def _p(a):
 
 def run_stage(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_end", "vel_force",
                                                       "sedge", "sflux", "snew", "sold_end",
-                                                      "etarhoflux")):
-    """Run AdvancePremac + DensityAdvance + EnthalpyAdvance on the CPU; returns numpy arrays."""
+                                                      "etarhoflux"), _entry=None):
+    """Run AdvancePremac + DensityAdvance + EnthalpyAdvance on the CPU; returns numpy arrays.
+    _entry: (call, last_error) of another C entry with mo_run_stage's arguments but the
+    thread count (the reference build's, pyref.run_stage)."""
     from maestroex_gb300.params import make_params
     p = make_params(cfg)
     n = cfg["n"]
@@ -101,6 +103,13 @@ def run_stage(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", "umac_e
         res["etarhoflux"] = np.full(fshape[2], np.nan)
         out.etarhoflux = _p(res["etarhoflux"])
     boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    if _entry is not None:
+        call, last_error = _entry
+        rc = call(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp),
+                  C.byref(out))
+        if rc != 0:
+            raise RuntimeError(last_error().decode())
+        return res
     rc = lib(checked).mo_run_stage(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
                                    C.byref(inp), C.byref(out), nthreads)
     if rc != 0:

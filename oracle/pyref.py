@@ -23,20 +23,29 @@ def available():
     return os.path.isdir(os.path.join(REF, "Source"))
 
 
-def lib():
+NUMSPECS = (2, 3, 5, 13)  # the reference's NumSpec is a compile-time constant: one build each
+
+
+def lib(nspec=3):
+    """The reference build for NumSpec = nspec (oracle/_ref/ns<nspec>/libmaestro_ref.so)."""
     if not _LIB:
         if not available():
             raise RuntimeError(f"reference sources not found under {REF}")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF}"], check=True)
-        L = C.CDLL(os.path.join(HERE, "_ref", "libmaestro_ref.so"))
+        _LIB.append({})
+    if nspec not in NUMSPECS:
+        raise ValueError(f"no reference build for NumSpec {nspec} (built: {NUMSPECS})")
+    libs = _LIB[0]
+    if nspec not in libs:
+        L = C.CDLL(os.path.join(HERE, "_ref", f"ns{nspec}", "libmaestro_ref.so"))
         L.ref_last_error.restype = C.c_char_p
-        _LIB.append(L)
-    return _LIB[0]
+        libs[nspec] = L
+    return libs[nspec]
 
 
-def _check(rc):
+def _check(rc, nspec=3):
     if rc != 0:
-        raise RuntimeError("reference: " + lib().ref_last_error().decode())
+        raise RuntimeError("reference: " + lib(nspec).ref_last_error().decode())
 
 
 def ppm(params, bx, s, s_lo, comp, vel, vel_lo, is_umac, bc):
@@ -74,6 +83,13 @@ def slopes(slope_order, d, dom, bx, s, s_lo, bcs):
 def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservative=0):
     """The reference's own member function on caller FABs, same arguments as
     pyoracle.member (outputs written into the argument arrays, valid cells / faces only)."""
-    L = lib()
+    L = lib(cfg["nspec"])
     pyoracle.member_call(L, L.ref_member, L.ref_last_error, cfg, fn, args, which_step, start_comp, num_comp,
                          is_conservative)
+
+
+def run_stage(cfg, want=("umac_vp", "umac_end", "sedge", "sflux", "snew", "sold_end", "etarhoflux")):
+    """The stage of pyoracle.run_stage run by the reference's own AdvancePremac,
+    DensityAdvance and EnthalpyAdvance (utrans and vel_force stay inside AdvancePremac)."""
+    L = lib(cfg["nspec"])
+    return pyoracle.run_stage(cfg, want=want, _entry=(L.ref_run_stage, L.ref_last_error))

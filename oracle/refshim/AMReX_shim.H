@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -36,6 +37,8 @@
 #define BL_PROFILE_VAR_STOP(a)
 #define BL_PROFILE(a)
 #define AMREX_ASSERT(x) ((void)0)
+#define BL_ASSERT(x) ((void)0)
+#define BL_SPACEDIM AMREX_SPACEDIM
 #define AMREX_ALWAYS_ASSERT(x)                                                       \
     do {                                                                             \
         if (!(x)) throw std::runtime_error("assertion failed: " #x);                 \
@@ -325,12 +328,28 @@ class BoxArray {
   public:
     BoxArray() = default;
     explicit BoxArray(std::vector<Box> b) : b_(std::move(b)) {}
+    explicit BoxArray(class BoxList&&);
     int size() const { return (int)b_.size(); }
     const Box& operator[](int i) const { return b_[i]; }
     Box get(int i) const { return b_[i]; }
     bool empty() const { return b_.empty(); }
     void push_back(const Box& b) { b_.push_back(b); }
+    // used by the multi-level branches only (never reached with one level)
+    BoxArray& maxSize(int) { return *this; }
+    BoxArray& coarsen(const IntVect&) { Abort("stand-in BoxArray::coarsen: one level only"); }
+    BoxArray& refine(const IntVect&) { Abort("stand-in BoxArray::refine: one level only"); }
+    BoxArray& surroundingNodes(int d) {
+        for (auto& b : b_) b.surroundingNodes(d);
+        return *this;
+    }
 };
+
+class BoxList {
+  public:
+    std::vector<Box> boxes;
+};
+inline BoxList GetBndryCells(const BoxArray&, int) { Abort("stand-in GetBndryCells: one level only"); }
+inline BoxArray::BoxArray(BoxList&& bl) : b_(std::move(bl.boxes)) {}
 
 // index type flags (1 = nodal in that direction)
 inline BoxArray convert(const BoxArray& ba, const IntVect& typ) {
@@ -350,7 +369,15 @@ class DistributionMapping {
   public:
     DistributionMapping() = default;
     explicit DistributionMapping(const BoxArray&) {}
+    void KnapSackProcessorMap(const std::vector<long>&, int) {}
 };
+
+namespace ParallelDescriptor {
+inline int NProcs() { return 1; }
+inline int MyProc() { return 0; }
+inline int IOProcessorNumber() { return 0; }
+inline bool IOProcessor() { return true; }
+}  // namespace ParallelDescriptor
 
 class Periodicity {
   public:
@@ -473,6 +500,15 @@ class FabArrayOf {
                          nc_);
     }
     Array4<const T> const_array(int i) const { return Array4<const T>(array(i)); }
+    // the FAB's view from component c on (AMReX's array(mfi, start_comp))
+    Array4<T> array(int i, int c) const {
+        Array4<T> a = array(i);
+        a.p += (long)c * a.nstride;
+        a.ncomp -= c;
+        return a;
+    }
+    inline Array4<T> array(const MFIter& mfi, int c) const;
+    inline Array4<const T> const_array(const MFIter& mfi, int c) const;
     inline Array4<T> array(const MFIter& mfi) const;
     inline Array4<const T> const_array(const MFIter& mfi) const;
 
@@ -486,11 +522,74 @@ class FabArrayOf {
         }
     }
     void setVal(Real v, int comp, int ncomp, const IntVect& ng) { setVal(v, comp, ncomp, ng[0]); }
-    // ghost exchange between boxes and physical fills belong to AMReX and are left to the
-    // caller: the stand-in keeps the data as it is (comparisons cover valid regions)
-    void FillBoundary(const Periodicity&) {}
-    void FillBoundary(int, int, const Periodicity&) {}
-    void FillBoundary() {}
+    // Copies into the cells of dst box b grown by dst_ng (skipping b's own valid region when
+    // ghosts_only) the values of every box c's region grown by src_ng of src, also through
+    // the periodic images of src; boxes and shifts are visited in order (box, z, y, x shift)
+    // and a later source overwrites an earlier one.
+    static void copy_regions(FabArrayOf& dst, const FabArrayOf& src, int scomp, int dcomp, int ncomp, int src_ng,
+                             int dst_ng, const Periodicity& per, const Box& dom, bool ghosts_only) {
+        int len[3];
+        for (int d = 0; d < 3; ++d) len[d] = dom.hi[d] - dom.lo[d] + 1;
+        for (int b = 0; b < dst.size(); ++b) {
+            const Box vb = dst.ba_[b];
+            const Box gb = grow(vb, dst_ng);
+            const auto D = dst.array(b);
+            for (int c = 0; c < src.size(); ++c) {
+                const Box sb = grow(src.ba_[c], src_ng);
+                const auto S = src.array(c);
+                for (int sz = -1; sz <= 1; ++sz)
+                    for (int sy = -1; sy <= 1; ++sy)
+                        for (int sx = -1; sx <= 1; ++sx) {
+                            const int sh[3] = {sx, sy, sz};
+                            bool ok = true;
+                            for (int d = 0; d < 3; ++d)
+                                if (sh[d] != 0 && !per.per[d]) ok = false;
+                            if (!ok) continue;
+                            if (ghosts_only && c == b && sx == 0 && sy == 0 && sz == 0) continue;
+                            Box r;
+                            bool empty = false;
+                            for (int d = 0; d < 3; ++d) {
+                                r.lo[d] = std::max(gb.lo[d], sb.lo[d] + sh[d] * len[d]);
+                                r.hi[d] = std::min(gb.hi[d], sb.hi[d] + sh[d] * len[d]);
+                                if (r.lo[d] > r.hi[d]) empty = true;
+                            }
+                            if (empty) continue;
+                            ParallelFor(r, ncomp, [&](int i, int j, int k, int n) {
+                                if (ghosts_only && vb.contains(i, j, k)) return;
+                                D(i, j, k, dcomp + n) =
+                                    S(i - sx * len[0], j - sy * len[1], k - sz * len[2], scomp + n);
+                            });
+                        }
+            }
+        }
+    }
+    // the level's domain (cell-centred) for the periodic images: set by the caller
+    static Box& domain_for_fills() {
+        static Box dom;
+        return dom;
+    }
+    void FillBoundary(int scomp, int ncomp, int ng, const Periodicity& per) {
+        copy_regions(*this, *this, scomp, scomp, ncomp, 0, ng, per, domain_for_fills(), true);
+    }
+    void FillBoundary(int scomp, int ncomp, const IntVect& ng, const Periodicity& per) {
+        FillBoundary(scomp, ncomp, ng[0], per);
+    }
+    void FillBoundary(int scomp, int ncomp, const Periodicity& per) { FillBoundary(scomp, ncomp, ng_, per); }
+    void FillBoundary(const Periodicity& per) { FillBoundary(0, nc_, ng_, per); }
+    void ParallelCopy(const FabArrayOf& src, int scomp, int dcomp, int ncomp, int src_ng, int dst_ng,
+                      const Periodicity& per = Periodicity()) {
+        copy_regions(*this, src, scomp, dcomp, ncomp, src_ng, dst_ng, per, domain_for_fills(), false);
+    }
+    void ParallelCopy(const FabArrayOf& src, int scomp, int dcomp, int ncomp, const IntVect& src_ng,
+                      const IntVect& dst_ng, const Periodicity& per = Periodicity()) {
+        ParallelCopy(src, scomp, dcomp, ncomp, src_ng[0], dst_ng[0], per);
+    }
+    void ParallelCopy(const FabArrayOf& src) { ParallelCopy(src, 0, 0, nc_, 0, 0); }
+    inline class FArrayBox operator[](const MFIter& mfi) const;
+    void clear() {
+        fabs_.clear();
+        ba_ = BoxArray();
+    }
 
     template <class F>
     static void each(MultiFab& dst, int ng, int ncomp, F&& f) {
@@ -581,9 +680,207 @@ template <class T>
 inline Array4<const T> FabArrayOf<T>::const_array(const MFIter& mfi) const {
     return const_array(mfi.index());
 }
+template <class T>
+inline Array4<T> FabArrayOf<T>::array(const MFIter& mfi, int c) const {
+    return array(mfi.index(), c);
+}
+template <class T>
+inline Array4<const T> FabArrayOf<T>::const_array(const MFIter& mfi, int c) const {
+    return Array4<const T>(array(mfi.index(), c));
+}
 using MultiFab = FabArrayOf<Real>;
 using iMultiFab = FabArrayOf<int>;
+
+// one FAB of a MultiFab (a view: box incl. ghosts, components, data)
+class FArrayBox {
+  public:
+    Box box_;
+    int nc_ = 0;
+    Real* p_ = nullptr;
+    const Box& box() const { return box_; }
+    const int* loVect() const { return box_.lo; }
+    const int* hiVect() const { return box_.hi; }
+    int nComp() const { return nc_; }
+    Array4<Real> array(int c = 0) const {
+        Array4<Real> a(p_, Dim3{box_.lo[0], box_.lo[1], box_.lo[2]},
+                       Dim3{box_.hi[0] + 1, box_.hi[1] + 1, box_.hi[2] + 1}, nc_);
+        a.p += (long)c * a.nstride;
+        a.ncomp -= c;
+        return a;
+    }
+};
+template <class T>
+inline FArrayBox FabArrayOf<T>::operator[](const MFIter& mfi) const {
+    FArrayBox f;
+    f.box_ = fabs_[mfi.index()].box;
+    f.nc_ = nc_;
+    f.p_ = fabs_[mfi.index()].p;
+    return f;
+}
+
+// AMReX's generic physical-boundary fill of cell-centred data (fab_filcc) for the cells of
+// bx outside the domain, direction by direction (x, then y, then z, each over the whole of
+// bx in the other directions):
+//   foextrap      the nearest interior value;
+//   hoextrap      the first ghost cell takes the value at the face of the quadratic through
+//                 the first three interior cells, (15 q0 - 10 q1 + 3 q2)/8 (linear,
+//                 (3 q0 - q1)/2, with fewer than three), deeper ghost cells the nearest
+//                 interior value;
+//   reflect_even  the mirror image; reflect_odd the mirror image with its sign changed;
+//   int_dir, ext_dir  left as they are (periodic images; Dirichlet data is the caller's).
+inline void fab_filcc(const Box& bx, const Array4<Real>& q, int ncomp, const Box& dom, const Real*, const Real*,
+                      const BCRec* bcr) {
+    for (int n = 0; n < ncomp; ++n) {
+        const BCRec& bc = bcr[n];
+        for (int d = 0; d < AMREX_SPACEDIM; ++d) {
+            const int dlo = dom.lo[d], dhi = dom.hi[d];
+            for (int side = 0; side < 2; ++side) {
+                const int t = side == 0 ? bc.lo(d) : bc.hi(d);
+                if (t != BCType::foextrap && t != BCType::hoextrap && t != BCType::reflect_even &&
+                    t != BCType::reflect_odd)
+                    continue;
+                Box r = bx;
+                if (side == 0) r.hi[d] = std::min(bx.hi[d], dlo - 1);
+                else r.lo[d] = std::max(bx.lo[d], dhi + 1);
+                if (r.lo[d] > r.hi[d]) continue;
+                ParallelFor(r, [&](int i, int j, int k) {
+                    int idx[3] = {i, j, k};
+                    const int m = idx[d];
+                    auto at = [&](int pnt) {
+                        int id2[3] = {i, j, k};
+                        id2[d] = pnt;
+                        return q(id2[0], id2[1], id2[2], n);
+                    };
+                    Real v;
+                    if (t == BCType::foextrap) {
+                        v = at(side == 0 ? dlo : dhi);
+                    } else if (t == BCType::hoextrap) {
+                        if (side == 0) {
+                            if (m < dlo - 1) v = at(dlo);
+                            else if (dlo + 2 <= std::min(bx.hi[d], dhi))
+                                v = 0.125 * (15. * at(dlo) - 10. * at(dlo + 1) + 3. * at(dlo + 2));
+                            else v = 0.5 * (3. * at(dlo) - at(dlo + 1));
+                        } else {
+                            if (m > dhi + 1) v = at(dhi);
+                            else if (dhi - 2 >= std::max(bx.lo[d], dlo))
+                                v = 0.125 * (15. * at(dhi) - 10. * at(dhi - 1) + 3. * at(dhi - 2));
+                            else v = 0.5 * (3. * at(dhi) - at(dhi - 1));
+                        }
+                    } else if (t == BCType::reflect_even) {
+                        v = at(side == 0 ? 2 * dlo - 1 - m : 2 * dhi + 1 - m);
+                    } else {
+                        v = -at(side == 0 ? 2 * dlo - 1 - m : 2 * dhi + 1 - m);
+                    }
+                    q(i, j, k, n) = v;
+                });
+            }
+        }
+    }
+}
+
+class BndryFuncArray {};
+
+// physical-boundary fill of a MultiFab: the functor runs on every FAB whose box grown by
+// nghost reaches outside the domain (grown in the periodic directions)
+template <class F>
+class PhysBCFunct {
+    Geometry geom_;
+    Vector<BCRec> bcr_;
+    F f_;
+
+  public:
+    PhysBCFunct() = default;
+    void define(const Geometry& g, const Vector<BCRec>& bcr, F f) {
+        geom_ = g;
+        bcr_ = bcr;
+        f_ = f;
+    }
+    void operator()(MultiFab& mf, int dcomp, int ncomp, const IntVect& nghost, Real time, int bccomp) {
+        Box gdom = geom_.Domain();
+        for (int d = 0; d < AMREX_SPACEDIM; ++d)
+            if (geom_.isPeriodic(d)) gdom.grow(d, nghost[d]);
+        for (MFIter mfi(mf); mfi.isValid(); ++mfi) {
+            Box gbx = grow(mfi.validbox(), nghost);
+            Box gd = gdom;
+            for (int d = 0; d < 3; ++d)
+                if (gbx.typ[d]) gd.surroundingNodes(d);
+            bool inside = true;
+            for (int d = 0; d < 3; ++d)
+                if (gbx.lo[d] < gd.lo[d] || gbx.hi[d] > gd.hi[d]) inside = false;
+            if (inside) continue;
+            FArrayBox dest = mf[mfi];
+            f_(gbx, dest, dcomp, ncomp, geom_, time, bcr_, bccomp, dcomp);
+        }
+    }
+};
+
+class Interpolater {};
+extern Interpolater cell_cons_interp;
+
+// FillPatchSingleLevel on one time level: the components come from the valid regions of
+// the source (through the periodic images) into mf's valid and ghost cells, then the
+// physical boundary fill
+template <class BC>
+inline void FillPatchSingleLevel(MultiFab& mf, Real time, const Vector<MultiFab*>& smf, const Vector<Real>&,
+                                 int scomp, int dcomp, int ncomp, const Geometry& geom, BC& physbc, int bccomp) {
+    if (smf.size() != 1) Abort("stand-in FillPatchSingleLevel: one time level");
+    const IntVect ng = mf.nGrowVect();
+    if (smf[0] == &mf && scomp == dcomp) mf.FillBoundary(dcomp, ncomp, ng, geom.periodicity());
+    else mf.ParallelCopy(*smf[0], scomp, dcomp, ncomp, IntVect(0, 0, 0), ng, geom.periodicity());
+    physbc(mf, dcomp, ncomp, ng, time, bccomp);
+}
+template <class... A>
+inline void FillPatchTwoLevels(A&&...) {
+    Abort("stand-in FillPatchTwoLevels: one level only");
+}
+template <class... A>
+inline void InterpFromCoarseLevel(A&&...) {
+    Abort("stand-in InterpFromCoarseLevel: one level only");
+}
+template <class... A>
+inline void average_down_faces(A&&...) {
+    Abort("stand-in average_down_faces: one level only");
+}
 inline bool TilingIfNotGPU() { return false; }
+
+template <class F>
+inline void ParallelFor(long n, F&& f) {
+    for (long i = 0; i < n; ++i) f((int)i);
+}
+template <class F1, class F2>
+inline void ParallelFor(const Box& b1, const Box& b2, F1&& f1, F2&& f2) {
+    ParallelFor(b1, f1);
+    ParallelFor(b2, f2);
+}
+template <class F1, class F2, class F3>
+inline void ParallelFor(const Box& b1, const Box& b2, const Box& b3, F1&& f1, F2&& f2, F3&& f3) {
+    ParallelFor(b1, f1);
+    ParallelFor(b2, f2);
+    ParallelFor(b3, f3);
+}
+
+// coarse-fine flux registers: one level only here, so any use is an error
+class FluxRegister {
+  public:
+    template <class... A>
+    void CrseInit(A&&...) {
+        Abort("stand-in FluxRegister: one level only");
+    }
+    template <class... A>
+    void FineAdd(A&&...) {
+        Abort("stand-in FluxRegister: one level only");
+    }
+    template <class... A>
+    void Reflux(A&&...) {
+        Abort("stand-in FluxRegister: one level only");
+    }
+    void setVal(Real) {}
+};
+
+template <class... A>
+inline void average_down(A&&...) {
+    Abort("stand-in average_down: one level only");
+}
 
 namespace Gpu {
 template <class T>

@@ -27,6 +27,36 @@ constexpr int NumAux = 0;
 constexpr int Rho = 0, RhoH = 1, Temp = 2, Pi = 3, FirstSpec = 4, FirstAux = 4 + NumSpec;
 constexpr int Nscal = 4 + NumSpec;
 
+// the algorithm options of Source/Maestro.H:50-60
+enum species_pred { predict_rhoprime_and_X = 1, predict_rhoX, predict_rho_and_X };
+enum enthalpy_pred {
+    predict_rhoh = 0,
+    predict_rhohprime,
+    predict_h,
+    predict_T_then_rhohprime,
+    predict_T_then_h,
+    predict_hprime,
+    predict_Tprime_then_h
+};
+
+// the equation of state (Microphysics, absent): the stage calls it only below the base
+// cutoff density and for temperature predictions, which the comparisons never reach
+enum eos_input_t { eos_input_rt = 1, eos_input_rh, eos_input_tp, eos_input_rp, eos_input_re, eos_input_ps, eos_input_ph, eos_input_th };
+struct eos_t {
+    amrex::Real rho = 0, T = 0, p = 0, e = 0, h = 0, s = 0, cs = 0, gam1 = 0, cp = 0, cv = 0, dpdr = 0, dedr = 0,
+                dpdT = 0, dedT = 0, dhdr = 0, dhdT = 0;
+    amrex::Real xn[NumSpec > 0 ? NumSpec : 1] = {};
+    amrex::Real aux[1] = {};
+};
+using eos_rh_t = eos_t;
+using eos_rep_t = eos_t;
+using eos_re_t = eos_t;
+using eos_rp_t = eos_t;
+template <class S>
+inline void eos(eos_input_t, S&) {
+    amrex::Abort("equation of state not available in the reference build");
+}
+
 // Source/MaestroFill3dData.cpp:339 (declared in the reference's Maestro.H)
 amrex::Real QuadInterp(const amrex::Real x, const amrex::Real x0, const amrex::Real x1, const amrex::Real x2,
                        const amrex::Real y0, const amrex::Real y1, const amrex::Real y2, const bool limit = true);
@@ -53,7 +83,19 @@ class Maestro {
     amrex::BCRec phys_bc;
     BCs bcs_s, bcs_u, bcs_f;
 
-    // Source/MaestroFillData.cpp (AMReX fills: defined by the stand-in, see ref_entry.cpp)
+    // Source/MaestroBCFill.cpp
+    static void ScalarFill(const A4& scal, const Box& bx, const Box& domainBox, const Real* dx,
+                           const amrex::BCRec bcs, const Real* gridlo, const int comp);
+    static void VelFill(const A4& vel, const Box& bx, const Box& domainBox, const Real* dx, const amrex::BCRec bcs,
+                        const Real* gridlo, const int comp = 0);
+    static void FillExtBC(const A4& q, const Box& bx, const Box& domainBox, const Real* dx, const amrex::BCRec bcs,
+                          const int comp, const bool is_vel = false);
+
+    // Source/MaestroFillData.cpp
+    void FillCoarsePatch(int lev, Real time, MF& mf, amrex::Vector<MF>& mf_old, amrex::Vector<MF>& mf_new,
+                         int srccomp, int destcomp, int ncomp, const BCs& bcs, int variable_type = 0);
+    void GetData(int lev, Real time, amrex::Vector<MF*>& mf, amrex::Vector<Real>& mftime, amrex::Vector<MF>& mf_old,
+                 amrex::Vector<MF>& mf_new) const;
     void FillPatch(Real time, amrex::Vector<MF>& mf, amrex::Vector<MF>& mf_old, amrex::Vector<MF>& mf_new,
                    int srccomp, int destcomp, int ncomp, int startbccomp, const BCs& bcs_in, int variable_type = 0);
     void FillPatch(int lev, Real time, MF& mf, amrex::Vector<MF>& mf_old, amrex::Vector<MF>& mf_new, int srccomp,
@@ -75,6 +117,20 @@ class Maestro {
     Real t_old = 0.0, t_new = 0.0;
     amrex::Vector<MF> sold, snew, uold, unew;
     static amrex::IntVect nodal_flag, nodal_flag_x, nodal_flag_y, nodal_flag_z;
+    static int ng_s;
+    static constexpr Real Gconst = 6.67428e-8;  // Source/Maestro.H:1864
+    int ng_adv = 3;
+    BaseState<Real> rho0_old, rho0_new, rhoh0_old, rhoh0_new, p0_old, p0_new, tempbar, psi, grav_cell_old,
+        grav_cell_new, w0_force, etarho_cc, etarho_ec;
+    amrex::Vector<MF> gpi;
+    amrex::Vector<std::unique_ptr<amrex::FluxRegister>> flux_reg_s;
+    amrex::IntVect refRatio(int) const { return amrex::IntVect(2, 2, 2); }
+
+    // Source/MaestroMakeGrav.cpp, Source/MaestroRhoHT.cpp
+    void MakeGravCell(BaseState<Real>& grav_cell, const BaseState<Real>& rho0_s) const;
+    void MakeGravEdge(BaseState<Real>& grav_edge_state, const BaseState<Real>& rho0_state) const;
+    void HfromRhoTedge(FaceMFs& sedge, const BaseState<Real>& rho0_edge_old, const BaseState<Real>& rhoh0_edge_old,
+                       const BaseState<Real>& rho0_edge_new, const BaseState<Real>& rhoh0_edge_new);
 
     // Source/MaestroFill3dData.cpp
     void Put1dArrayOnCart(const BaseState<Real>& s0, amrex::Vector<MF>& s0_cart, const bool is_input_edge_centered,

@@ -41,6 +41,10 @@ extern int w0_interp_type;
 extern int s0mac_interp_type;
 extern int w0mac_interp_type;
 extern int drdxfac;
+extern amrex::Real grav_const;
+extern amrex::Real planar_invsq_mass;
+extern bool do_planar_invsq_grav;
+extern bool do_2d_planar_octant;
 }  // namespace maestro
 
 #endif

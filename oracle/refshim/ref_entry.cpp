@@ -42,33 +42,25 @@ int w0_interp_type = 2;
 int s0mac_interp_type = 1;
 int w0mac_interp_type = 1;
 int drdxfac = 5;
+amrex::Real grav_const = -1.5e10;
+amrex::Real planar_invsq_mass = 0.0;
+bool do_planar_invsq_grav = false;
+bool do_2d_planar_octant = false;
 }  // namespace maestro
+
+int Maestro::ng_s = 3;
+// needs the equation of state (temperature predictions): not in this build
+void Maestro::HfromRhoTedge(FaceMFs&, const BaseState<Real>&, const BaseState<Real>&, const BaseState<Real>&,
+                            const BaseState<Real>&) {
+    amrex::Abort("HfromRhoTedge needs the equation of state");
+}
 
 amrex::IntVect Maestro::nodal_flag(1, 1, 1);
 amrex::IntVect Maestro::nodal_flag_x(1, 0, 0);
 amrex::IntVect Maestro::nodal_flag_y(0, 1, 0);
 amrex::IntVect Maestro::nodal_flag_z(0, 0, 1);
 
-// AMReX's fills and averages on one level.  Ghost cells are the caller's business here:
-// every comparison made with this library covers valid cells and faces only, so the
-// stand-ins keep ghost data as it is.  Averaging down has nothing to do on one level.
-void Maestro::FillPatch(Real, amrex::Vector<MF>&, amrex::Vector<MF>&, amrex::Vector<MF>&, int, int, int, int,
-                        const BCs&, int) {
-    if (finest_level > 0) amrex::Abort("stand-in FillPatch: one level only");
-}
-void Maestro::FillPatch(int, Real, MF&, amrex::Vector<MF>&, amrex::Vector<MF>&, int, int, int, int, const BCs&, int) {
-    if (finest_level > 0) amrex::Abort("stand-in FillPatch: one level only");
-}
-void Maestro::AverageDown(amrex::Vector<MF>&, int, int) {
-    if (finest_level > 0) amrex::Abort("stand-in AverageDown: one level only");
-}
-void Maestro::AverageDownFaces(FaceMFs&) {
-    if (finest_level > 0) amrex::Abort("stand-in AverageDownFaces: one level only");
-}
-void Maestro::FillUmacGhost(FaceMFs&, int) {}
-void Maestro::FillPatchUedge(FaceMFs&) {
-    if (finest_level > 0) amrex::Abort("stand-in FillPatchUedge: one level only");
-}
+amrex::Interpolater amrex::cell_cons_interp;
 
 using namespace amrex;
 
@@ -143,7 +135,9 @@ void bc_setup(Maestro& m) {
         }
 }
 
-void setup(Maestro& m, const mo_params* p, int nboxes, const int* boxes) {
+void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in);
+
+void setup(Maestro& m, const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in) {
     if (p->dim == 2) amrex::Abort("the reference build here is 3-D");
     if (p->nspec != NumSpec) amrex::Abort("the reference build has NumSpec " + std::to_string(NumSpec));
     set_params(p);
@@ -166,7 +160,178 @@ void setup(Maestro& m, const mo_params* p, int nboxes, const int* boxes) {
     for (int b = 0; b < nboxes; ++b) bl.push_back(box_of(boxes + 6 * b));
     m.grids.assign(1, BoxArray(bl));
     m.dmap.assign(1, DistributionMapping());
+    MultiFab::domain_for_fills() = g.domain;
     bc_setup(m);
+    Maestro::ng_s = maestro::ppm_type == 2 ? 4 : 3;
+    m.ng_adv = Maestro::ng_s;
+    m.t_old = 0.0;
+    m.t_new = p->dt;
+    setup_base_state(m, p, in);
+}
+
+// The radial base state as Maestro::Setup (Source/MaestroSetup.cpp:57-118) sizes it and
+// BaseStateGeometry::Init / InitMultiLevel / ComputeCutoffCoords lay it out, holding the
+// caller's 1-D arrays; spherical geometry also gets the cell normals and the cell-to-bin
+// map (Source/MaestroInit.cpp:71-72, 120-121).
+void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in) {
+    int nr_fine, nr_irreg = 0;
+    Real dr_fine;
+    if (maestro::spherical) {
+        const Real domhi = p->dom_hi[0] + 1;
+        nr_irreg = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0);
+        if (!maestro::use_exact_base_state) amrex::Abort("spherical: the exact base state only");
+        nr_fine = nr_irreg + 1;
+        dr_fine = p->dx[0] / maestro::drdxfac;
+    } else {
+        nr_fine = p->dom_hi[2] + 1;
+        dr_fine = p->dx[2];
+    }
+    // plane-parallel gravity is the constant grav_const (MakeGravCell,
+    // Source/MaestroMakeGrav.cpp); the caller's grav_cell holds it
+    if (!maestro::spherical) maestro::grav_const = in->grav_cell[0];
+    m.base_geom.max_radial_level = 0;
+    m.base_geom.Init(0, nr_fine, dr_fine, nr_irreg, m.geom, 0, m.center);
+    BaseState<int> tags(1, nr_fine);
+    tags.setVal(0);
+    m.base_geom.InitMultiLevel(0, tags.array());
+    auto fill = [&](BaseState<Real>& b, const double* src, int len) {
+        b.resize(1, len);
+        auto a = b.array();
+        for (int r = 0; r < len; ++r) a(0, r) = src ? src[r] : 0.0;
+    };
+    fill(m.rho0_old, in->rho0_old, nr_fine);
+    fill(m.rho0_new, in->rho0_new, nr_fine);
+    fill(m.rhoh0_old, in->rhoh0_old, nr_fine);
+    fill(m.rhoh0_new, in->rhoh0_new, nr_fine);
+    fill(m.p0_old, in->p0_old, nr_fine);
+    fill(m.p0_new, in->p0_new, nr_fine);
+    fill(m.psi, in->psi, nr_fine);
+    fill(m.grav_cell_old, in->grav_cell, nr_fine);
+    fill(m.grav_cell_new, in->grav_cell, nr_fine);
+    fill(m.w0_force, in->w0_force, nr_fine);
+    fill(m.w0, in->w0, nr_fine + 1);
+    fill(m.tempbar, nullptr, nr_fine);
+    fill(m.etarho_cc, nullptr, nr_fine);
+    fill(m.etarho_ec, nullptr, nr_fine + 1);
+    m.base_geom.ComputeCutoffCoords(m.rho0_old.array());
+    if (m.base_geom.base_cutoff_density_coord(0) != p->base_cutoff_density_coord)
+        amrex::Abort("base cutoff coordinate " + std::to_string(m.base_geom.base_cutoff_density_coord(0)) +
+                     " differs from the caller's " + std::to_string(p->base_cutoff_density_coord));
+    const BoxArray& ba = m.grids[0];
+    m.w0_cart.resize(1);
+    m.w0_cart[0].define(ba, DistributionMapping(), AMREX_SPACEDIM, 2);
+    m.w0_cart[0].setVal(0.0);
+    if (maestro::spherical) {
+        m.normal.resize(1);
+        m.normal[0].define(ba, DistributionMapping(), 3, 1);
+        m.cell_cc_to_r.resize(1);
+        m.cell_cc_to_r[0].define(ba, DistributionMapping(), 1, 0);
+        m.MakeNormal();
+        m.MakeCCtoRadii();
+    }
+    m.Put1dArrayOnCart(m.w0, m.w0_cart, true, true, m.bcs_u, 0, 1);
+}
+
+// domain arrays (i fastest, one block per component) <-> valid regions of a MultiFab
+void scatter(const Box& dom, const double* src, MultiFab& mf, int c0, int nc) {
+    const long nx = dom.length(0), ny = dom.length(1), nz = dom.length(2);
+    for (int b = 0; b < mf.size(); ++b) {
+        const auto a = mf.array(b);
+        ParallelFor(mf.boxArray()[b], nc, [&](int i, int j, int k, int n) {
+            a(i, j, k, c0 + n) = src[(((long)n * nz + (k - dom.lo[2])) * ny + (j - dom.lo[1])) * nx + (i - dom.lo[0])];
+        });
+    }
+}
+void gather(const Box& dom, const MultiFab& mf, int c0, int nc, double* dst) {
+    if (!dst) return;
+    Box d = dom;
+    for (int e = 0; e < 3; ++e)
+        if (mf.boxArray()[0].typ[e]) d.surroundingNodes(e);
+    const long nx = d.length(0), ny = d.length(1), nz = d.length(2);
+    for (int b = 0; b < mf.size(); ++b) {
+        const auto a = mf.array(b);
+        ParallelFor(mf.boxArray()[b], nc, [&](int i, int j, int k, int n) {
+            dst[(((long)n * nz + (k - d.lo[2])) * ny + (j - d.lo[1])) * nx + (i - d.lo[0])] = a(i, j, k, c0 + n);
+        });
+    }
+}
+
+BoxArray faces(const BoxArray& ba, int d) { return convert(ba, IntVect(d == 0, d == 1, d == 2)); }
+
+// AdvancePremac -> Addw0 -> DensityAdvance(1) -> Addw0 -> EnthalpyAdvance(1) as the
+// predictor of Maestro::AdvanceTimeStep calls them (Source/MaestroAdvance.cpp:160-210,
+// 290-360, 436-548), the MAC projection skipped
+int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out) {
+    Maestro m;
+    setup(m, p, nboxes, boxes, in);
+    const BoxArray& ba = m.grids[0];
+    const DistributionMapping dm;
+    const Box dom = m.geom[0].Domain();
+    const int ng = Maestro::ng_s;
+    m.uold.resize(1);
+    m.uold[0].define(ba, dm, AMREX_SPACEDIM, ng);
+    m.uold[0].setVal(0.0);
+    scatter(dom, in->uold, m.uold[0], 0, 3);
+    m.sold.resize(1);
+    m.sold[0].define(ba, dm, Nscal, ng);
+    m.sold[0].setVal(0.0);
+    scatter(dom, in->sold, m.sold[0], 0, Nscal);
+    m.snew.resize(1);
+    m.snew[0].define(ba, dm, Nscal, ng);
+    m.snew[0].setVal(0.0);
+    MultiFab::Copy(m.snew[0], m.sold[0], Temp, Temp, 1, ng);
+    m.gpi.resize(1);
+    m.gpi[0].define(ba, dm, AMREX_SPACEDIM, 0);
+    scatter(dom, in->gpi, m.gpi[0], 0, 3);
+    Vector<MultiFab> thermal(1), scal_force(1), etarhoflux(1), w0_force_cart(1);
+    thermal[0].define(ba, dm, 1, 1);
+    thermal[0].setVal(0.0);
+    if (in->thermal) scatter(dom, in->thermal, thermal[0], 0, 1);
+    scal_force[0].define(ba, dm, Nscal, 1);
+    scal_force[0].setVal(0.0);
+    etarhoflux[0].define(faces(ba, 2), dm, 1, 1);
+    etarhoflux[0].setVal(0.0);
+    w0_force_cart[0].define(ba, dm, AMREX_SPACEDIM, 1);
+    w0_force_cart[0].setVal(0.0);
+    Vector<std::array<MultiFab, AMREX_SPACEDIM>> umac(1), sedge(1), sflux(1), w0mac(1);
+    for (int d = 0; d < 3; ++d) {
+        umac[0][d].define(faces(ba, d), dm, 1, 1);
+        sedge[0][d].define(faces(ba, d), dm, Nscal, 0);
+        sflux[0][d].define(faces(ba, d), dm, Nscal, 0);
+        w0mac[0][d].define(faces(ba, d), dm, 1, 1);
+        umac[0][d].setVal(0.0);
+        sedge[0][d].setVal(0.0);
+        sflux[0][d].setVal(0.0);
+        w0mac[0][d].setVal(0.0);
+    }
+    if (maestro::spherical) m.MakeW0mac(w0mac);
+    if (maestro::evolve_base_state) m.Put1dArrayOnCart(m.w0_force, w0_force_cart, false, true, m.bcs_f, 0);
+    BaseState<Real> rho0_predicted_edge(1, m.base_geom.nr_fine + 1);
+    {
+        auto a = rho0_predicted_edge.array();
+        for (int r = 0; r <= m.base_geom.nr_fine; ++r) a(0, r) = in->rho0_predicted_edge[r];
+    }
+    // the old state's ghost cells as the previous step's UpdateScal leaves them
+    m.FillPatch(m.t_old, m.sold, m.sold, m.sold, 0, 0, Nscal, 0, m.bcs_s);
+
+    m.AdvancePremac(umac, w0mac, w0_force_cart);
+    for (int d = 0; d < 3; ++d) gather(dom, umac[0][d], 0, 1, out->umac_vp[d]);
+    m.Addw0(umac, w0mac, 1.);
+    m.DensityAdvance(1, m.sold, m.snew, sedge, sflux, scal_force, etarhoflux, umac, w0mac, rho0_predicted_edge);
+    m.Addw0(umac, w0mac, -1.);
+    m.Addw0(umac, w0mac, 1.);
+    m.EnthalpyAdvance(1, m.sold, m.snew, sedge, sflux, scal_force, umac, w0mac, thermal);
+    m.Addw0(umac, w0mac, -1.);
+
+    for (int d = 0; d < 3; ++d) {
+        gather(dom, umac[0][d], 0, 1, out->umac_end[d]);
+        gather(dom, sedge[0][d], 0, Nscal, out->sedge[d]);
+        gather(dom, sflux[0][d], 0, Nscal, out->sflux[d]);
+    }
+    gather(dom, m.snew[0], 0, Nscal, out->snew);
+    gather(dom, m.sold[0], 0, Nscal, out->sold_end);
+    gather(dom, etarhoflux[0], 0, 1, out->etarhoflux);
+    return 0;
 }
 
 // A MultiFab on ba (typed nodal in direction `nodal` if >= 0) with ng ghosts and nc
@@ -198,12 +363,10 @@ void mf_to(const MultiFab& mf, const mo_fab* f, int c0, int nc) {
 
 int member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
            int start_comp, int num_comp, int is_cons, const mo_fab* args) {
-    (void)base;
-    (void)which_step;
     Maestro m;
-    setup(m, p, nboxes, boxes);
+    setup(m, p, nboxes, boxes, base);
     const BoxArray& ba = m.grids[0];
-    const int ng_s = maestro::ppm_type == 2 ? 4 : 3;
+    const int ng_s = Maestro::ng_s;
     auto A = [&](int slot) { return args + (long)slot * nboxes; };
     Vector<MultiFab> m1(1), m2(1), m3(1);
     Vector<std::array<MultiFab, AMREX_SPACEDIM>> f1(1), f2(1);
@@ -273,6 +436,18 @@ int ref_slopes(int slope_order_, int d, const int* dom, const int* bx, const Ref
         if (d == 1) Maestro::Slopey(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         if (d == 2) Maestro::Slopez(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         return 0;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+/* The stage of mo_run_stage (oracle/maestro_oracle.h) run by the reference's own
+ * AdvancePremac, DensityAdvance and EnthalpyAdvance on one 3-D level; every output but
+ * utrans and vel_force (local to AdvancePremac). */
+int ref_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out) {
+    try {
+        return run_stage(p, nboxes, boxes, in, out);
     } catch (const std::exception& e) {
         g_err = e.what();
         return -1;

@@ -18,7 +18,22 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")]
 
 import pyref  # noqa: E402
+from maestroex_gb300 import configs  # noqa: E402
+from maestroex_gb300.params import FIRSTSPEC, INTERIOR, NOSLIPWALL, OUTFLOW, RHO, RHOH, SLIPWALL, SYMMETRY  # noqa: E402
 from test_reference_pin import field, ppm_inputs  # noqa: E402
+
+# whole-stage fixtures: small single-level configurations (the inputs are stored with the
+# outputs, so that hosts whose random streams differ still read the same values)
+STAGE_FIXTURES = {
+    "planar_ppm1_w0": lambda: configs.planar_config(n=(16, 12, 12), nspec=2, ppm_type=1, max_grid=(8, 12, 12),
+                                                    seed=901, w0_amp=1.0e4),
+    "planar_ppm2_walls": lambda: configs.planar_config(n=(12, 12, 16), nspec=2, ppm_type=2, max_grid=(12, 6, 8),
+                                                       bc_lo=(SYMMETRY, SLIPWALL, NOSLIPWALL),
+                                                       bc_hi=(OUTFLOW, SLIPWALL, OUTFLOW), seed=902, cfl=0.5),
+    "spherical_ppm2": lambda: configs.spherical_config(n=12, nspec=2, ppm_type=2, max_grid=6),
+}
+STAGE_INPUTS = ("uold", "sold", "gpi", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new", "p0_old", "p0_new", "psi",
+                "grav_cell", "w0_force", "w0", "rho0_predicted_edge")
 
 # (ppm_type, is_umac, bc lo[3] hi[3]): every BCType on some face, both tracing velocities
 PPM_FIXTURES = [
@@ -59,6 +74,20 @@ def main():
         out[pre + "slope"] = pyref.slopes(so, d, dom, bx, s, lo, bcs)
     np.savez_compressed(os.path.join(HERE, "ppm_slopes.npz"), **out)
     print(f"wrote {len(PPM_FIXTURES)} PPM and {len(SLOPE_FIXTURES)} slope fixtures")
+
+    out = {}
+    for name, make in STAGE_FIXTURES.items():
+        cfg = make()
+        ref = pyref.run_stage(cfg)
+        comps = [RHO, RHOH] + list(range(FIRSTSPEC, FIRSTSPEC + cfg["nspec"]))
+        for k in STAGE_INPUTS:
+            out[f"{name}_in_{k}"] = cfg[k]
+        out[f"{name}_snew"] = ref["snew"][comps]
+        for d in range(3):
+            out[f"{name}_umac_end{d}"] = ref["umac_end"][d]
+            out[f"{name}_sflux{d}_rho"] = ref["sflux"][d][RHO]
+    np.savez_compressed(os.path.join(HERE, "stage.npz"), **out)
+    print(f"wrote {len(STAGE_FIXTURES)} stage fixtures")
 
 
 if __name__ == "__main__":

@@ -31,3 +31,14 @@ def test_madv_ppm_matches_golden(c):
     assert np.array_equal(Ip.cpu().numpy(), Ip_ref)
     assert np.array_equal(Im.cpu().numpy(), Im_ref)
     st.close()
+
+
+@pytest.mark.parametrize("name", ("planar_ppm1_w0", "planar_ppm2_walls", "spherical_ppm2"))
+def test_gpu_stage_matches_golden(name):
+    """The whole stage on the GPU (graph-replayed batched kernels) against the reference's
+    own stage on the same inputs, bit for bit."""
+    from maestroex_gb300 import capi
+    from maestroex_gb300.stage import run_stage_gpu
+    from test_golden import check_stage, stage_fixture
+    cfg, ref = stage_fixture(name)
+    check_stage(cfg, run_stage_gpu(cfg, mode=capi.MODE_GRAPH), ref, name)
