@@ -387,7 +387,7 @@ def steps_tl(cfg, s0, ds0, u, du, nsteps, nthreads=0):
     return s, ds
 
 
-def run_velocity_advance(cfg, rhohalf, sponge=None, nthreads=0, checked=False):
+def run_velocity_advance(cfg, rhohalf, sponge=None, nthreads=0, checked=False, _entry=None):
     """AdvancePremac (MAC projection skipped) then VelocityAdvance + UpdateVel on the CPU:
     returns dict(unew [3, nz, ny, nx], uedge [3 arrays 3 x faces], umac [3 face arrays])."""
     from maestroex_gb300.params import make_params
@@ -411,11 +411,17 @@ def run_velocity_advance(cfg, rhohalf, sponge=None, nthreads=0, checked=False):
     ue = (C.POINTER(C.c_double) * 3)(*[_p(a) for a in uedge])
     um = (C.POINTER(C.c_double) * 3)(*[_p(a) for a in umac])
     boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    args = (C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp), arr(rhohalf),
+            arr(sponge) if sponge is not None else None, _p(unew), ue, um)
+    if _entry is not None:  # (call, last_error) of the reference build: no thread count
+        call, last_error = _entry
+        call.restype = C.c_int
+        if call(*args) != 0:
+            raise RuntimeError(last_error().decode())
+        return dict(unew=unew, uedge=uedge, umac=umac)
     L = lib(checked)
     L.mo_run_velocity_advance.restype = C.c_int
-    rc = L.mo_run_velocity_advance(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
-                                   C.byref(inp), arr(rhohalf), arr(sponge) if sponge is not None else None,
-                                   _p(unew), ue, um, nthreads)
+    rc = L.mo_run_velocity_advance(*args, nthreads)
     if rc != 0:
         raise RuntimeError("oracle: " + L.mo_last_error().decode())
     return dict(unew=unew, uedge=uedge, umac=umac)

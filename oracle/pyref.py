@@ -93,3 +93,10 @@ def run_stage(cfg, want=("umac_vp", "umac_end", "sedge", "sflux", "snew", "sold_
     DensityAdvance and EnthalpyAdvance (utrans and vel_force stay inside AdvancePremac)."""
     L = lib(cfg["nspec"])
     return pyoracle.run_stage(cfg, want=want, _entry=(L.ref_run_stage, L.ref_last_error))
+
+
+def run_velocity_advance(cfg, rhohalf, sponge=None):
+    """pyoracle.run_velocity_advance run by the reference's own AdvancePremac and
+    VelocityAdvance (unew and umac; uedge stays inside VelocityAdvance)."""
+    L = lib(cfg["nspec"])
+    return pyoracle.run_velocity_advance(cfg, rhohalf, sponge, _entry=(L.ref_run_velocity_advance, L.ref_last_error))

@@ -258,6 +258,65 @@ void gather(const Box& dom, const MultiFab& mf, int c0, int nc, double* dst) {
 
 BoxArray faces(const BoxArray& ba, int d) { return convert(ba, IntVect(d == 0, d == 1, d == 2)); }
 
+int run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                         const double* rhohalf, const double* sponge, double* unew_out, double* const* umac_out) {
+    Maestro m;
+    setup(m, p, nboxes, boxes, in);
+    maestro::do_sponge = sponge != nullptr;
+    const BoxArray& ba = m.grids[0];
+    const DistributionMapping dm;
+    const Box dom = m.geom[0].Domain();
+    const int ng = Maestro::ng_s;
+    m.uold.resize(1);
+    m.uold[0].define(ba, dm, AMREX_SPACEDIM, ng);
+    m.uold[0].setVal(0.0);
+    scatter(dom, in->uold, m.uold[0], 0, 3);
+    m.unew.resize(1);
+    m.unew[0].define(ba, dm, AMREX_SPACEDIM, ng);
+    m.unew[0].setVal(0.0);
+    m.sold.resize(1);
+    m.sold[0].define(ba, dm, Nscal, ng);
+    m.sold[0].setVal(0.0);
+    scatter(dom, in->sold, m.sold[0], 0, Nscal);
+    m.gpi.resize(1);
+    m.gpi[0].define(ba, dm, AMREX_SPACEDIM, 0);
+    scatter(dom, in->gpi, m.gpi[0], 0, 3);
+    Vector<MultiFab> w0_force_cart(1), rh(1), sp(1);
+    w0_force_cart[0].define(ba, dm, AMREX_SPACEDIM, 1);
+    w0_force_cart[0].setVal(0.0);
+    rh[0].define(ba, dm, 1, 1);
+    rh[0].setVal(0.0);
+    scatter(dom, rhohalf, rh[0], 0, 1);
+    // the reference always holds a sponge field (read only with do_sponge)
+    sp[0].define(ba, dm, 1, 0);
+    sp[0].setVal(1.0);
+    if (sponge) scatter(dom, sponge, sp[0], 0, 1);
+    Vector<std::array<MultiFab, AMREX_SPACEDIM>> umac(1), w0mac(1);
+    for (int d = 0; d < 3; ++d) {
+        umac[0][d].define(faces(ba, d), dm, 1, 1);
+        w0mac[0][d].define(faces(ba, d), dm, 1, 1);
+        umac[0][d].setVal(0.0);
+        w0mac[0][d].setVal(0.0);
+    }
+    if (maestro::spherical) m.MakeW0mac(w0mac);
+    if (maestro::evolve_base_state) m.Put1dArrayOnCart(m.w0_force, w0_force_cart, false, true, m.bcs_f, 0);
+    m.FillPatch(m.t_old, m.sold, m.sold, m.sold, 0, 0, Nscal, 0, m.bcs_s);
+    m.AdvancePremac(umac, w0mac, w0_force_cart);
+    m.FillPatchUedge(umac);
+    for (int d = 0; d < 3; ++d) gather(dom, umac[0][d], 0, 1, umac_out ? umac_out[d] : nullptr);
+    m.FillPatch(m.t_old, m.uold, m.uold, m.uold, 0, 0, AMREX_SPACEDIM, 0, m.bcs_u, 1);
+    // rho0_nph = (rho0_old + rho0_new) / 2 and the cell gravity, as the caller passes them
+    BaseState<Real> rho0_nph(1, m.base_geom.nr_fine);
+    {
+        auto a = rho0_nph.array();
+        const auto o = m.rho0_old.array(), n = m.rho0_new.array();
+        for (int r = 0; r < m.base_geom.nr_fine; ++r) a(0, r) = 0.5 * (o(0, r) + n(0, r));
+    }
+    m.VelocityAdvance(rh, umac, w0mac, w0_force_cart, rho0_nph, m.grav_cell_old, sp);
+    gather(dom, m.unew[0], 0, 3, unew_out);
+    return 0;
+}
+
 // AdvancePremac -> Addw0 -> DensityAdvance(1) -> Addw0 -> EnthalpyAdvance(1) as the
 // predictor of Maestro::AdvanceTimeStep calls them (Source/MaestroAdvance.cpp:160-210,
 // 290-360, 436-548), the MAC projection skipped
@@ -436,6 +495,22 @@ int ref_slopes(int slope_order_, int d, const int* dom, const int* bx, const Ref
         if (d == 1) Maestro::Slopey(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         if (d == 2) Maestro::Slopez(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         return 0;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+/* mo_run_velocity_advance (oracle/maestro_oracle.h) run by the reference's own
+ * AdvancePremac, FillPatchUedge (the MAC projection's closing face fill) and
+ * VelocityAdvance with UpdateVel; writes unew and umac (uedge stays inside
+ * VelocityAdvance). */
+int ref_run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
+                             const double* rhohalf, const double* sponge, double* unew_out, double* const* uedge_out,
+                             double* const* umac_out) {
+    (void)uedge_out;
+    try {
+        return run_velocity_advance(p, nboxes, boxes, in, rhohalf, sponge, unew_out, umac_out);
     } catch (const std::exception& e) {
         g_err = e.what();
         return -1;

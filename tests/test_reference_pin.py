@@ -184,3 +184,35 @@ def test_make_edge_scal_member_matches_reference_source(ppm_type, is_cons):
     for d in range(3):
         for b in range(len(cfg["boxes"])):
             assert np.array_equal(outs[0][d][b][0], outs[1][d][b][0]), (d, b)
+
+
+# ------------------------------------------------------------------- VelocityAdvance
+def velocity_cases():
+    from maestroex_gb300.params import OUTFLOW, SLIPWALL
+    return {
+        "planar ppm1": lambda: configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=1),
+        "planar ppm2 outflow": lambda: configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=2,
+                                                             bc_lo=(OUTFLOW, SLIPWALL, SLIPWALL),
+                                                             bc_hi=(OUTFLOW, OUTFLOW, OUTFLOW)),
+        "planar ppm0": lambda: configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=0),
+        "spherical ppm2": lambda: configs.spherical_config(n=32, max_grid=16, ppm_type=2),
+    }
+
+
+VELOCITY_CASES = velocity_cases()
+
+
+@pytest.mark.parametrize("name", list(VELOCITY_CASES))
+@pytest.mark.parametrize("with_sponge", [False, True])
+def test_velocity_advance_matches_reference_source(name, with_sponge):
+    """AdvancePremac, then Maestro::VelocityAdvance with UpdateVel (and the sponge)."""
+    from maestroex_gb300.params import RHO
+    cfg = VELOCITY_CASES[name]()
+    rng = np.random.default_rng(17)
+    rhohalf = cfg["sold"][RHO] * (1.0 + 1e-4 * rng.standard_normal(cfg["sold"][RHO].shape))
+    sponge = rng.uniform(0.5, 1.0, size=rhohalf.shape) if with_sponge else None
+    ours = pyoracle.run_velocity_advance(cfg, rhohalf, sponge, checked=True)
+    ref = pyref.run_velocity_advance(cfg, rhohalf, sponge)
+    for d in range(3):
+        assert np.array_equal(ours["umac"][d], ref["umac"][d]), f"{name}: umac[{d}]"
+        assert np.array_equal(ours["unew"][d], ref["unew"][d]), f"{name}: unew comp {d}"
