@@ -3,9 +3,11 @@
  * cpu_baseline / --impl reference legs of bench.py as the checker; the product library
  * never links or calls it.
  *
- * Parity status: unpinned (the reference cannot be built: AMReX and Microphysics are
- * empty submodules; the reference stores no stage-level golden outputs).  The oracle is a
- * line-by-line restatement of the reference functions, each citing its file:line.
+ * Parity status: pinned.  The oracle is a line-by-line restatement of the reference
+ * functions, each citing its file:line, and is checked bit for bit against the reference's
+ * own stage sources compiled against AMReX stand-ins (refshim/, ref_entry.cpp; entry points
+ * ref_run_stage, ref_run_velocity_advance, ref_ppm, ref_slopes, ref_member with the
+ * arguments of the mo_ functions below).
  *
  * All field arrays are single-level, domain-sized, Fortran ordered (i fastest), one
  * contiguous block per component.  Face arrays in direction d have extent n_d + 1 in d.
