@@ -177,7 +177,7 @@ def run_stage_levels(cfg, checked=False, nthreads=0, want=("utrans", "umac_vp", 
     return res
 
 
-def run_stage_2d(cfg, checked=False, nthreads=0, which_step=1):
+def run_stage_2d(cfg, checked=False, nthreads=0, which_step=1, _entry=None):
     """The 2-D stage (configs.planar_config_2d) on the CPU; arrays shaped like the inputs:
     cells [nc, 1, ny, nx], x faces [.., 1, ny, nx+1], y faces [.., 1, ny+1, nx]."""
     from maestroex_gb300.params import make_params
@@ -214,6 +214,13 @@ def run_stage_2d(cfg, checked=False, nthreads=0, which_step=1):
     res["etarhoflux"] = np.full(fshape[1], np.nan)
     out.etarhoflux = _p(res["etarhoflux"])
     boxes = np.ascontiguousarray(np.array(cfg["boxes"], dtype=np.int32).reshape(-1))
+    if _entry is not None:  # (call, last_error) of the reference's 2-D build (predictor only)
+        call, last_error = _entry
+        call.restype = C.c_int
+        if call(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)), C.byref(inp),
+                C.byref(out)) != 0:
+            raise RuntimeError(last_error().decode())
+        return res
     rc = lib(checked).mo_run_stage_2d(C.byref(p), len(cfg["boxes"]), boxes.ctypes.data_as(C.POINTER(C.c_int)),
                                       C.byref(inp), C.byref(out), which_step, nthreads)
     if rc != 0:

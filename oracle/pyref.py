@@ -24,23 +24,26 @@ def available():
 
 
 NUMSPECS = (2, 3, 5, 13)  # the reference's NumSpec is a compile-time constant: one build each
+NUMSPECS_2D = (2, 3)
 
 
-def lib(nspec=3):
-    """The reference build for NumSpec = nspec (oracle/_ref/ns<nspec>/libmaestro_ref.so)."""
+def lib(nspec=3, dim=3):
+    """The reference build for NumSpec = nspec in dim dimensions
+    (oracle/_ref/ns<nspec>[_2d]/libmaestro_ref.so)."""
     if not _LIB:
         if not available():
             raise RuntimeError(f"reference sources not found under {REF}")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF}"], check=True)
         _LIB.append({})
-    if nspec not in NUMSPECS:
-        raise ValueError(f"no reference build for NumSpec {nspec} (built: {NUMSPECS})")
+    if nspec not in (NUMSPECS if dim == 3 else NUMSPECS_2D):
+        raise ValueError(f"no {dim}-D reference build for NumSpec {nspec}")
     libs = _LIB[0]
-    if nspec not in libs:
-        L = C.CDLL(os.path.join(HERE, "_ref", f"ns{nspec}", "libmaestro_ref.so"))
+    key = (nspec, dim)
+    if key not in libs:
+        L = C.CDLL(os.path.join(HERE, "_ref", f"ns{nspec}" + ("_2d" if dim == 2 else ""), "libmaestro_ref.so"))
         L.ref_last_error.restype = C.c_char_p
-        libs[nspec] = L
-    return libs[nspec]
+        libs[key] = L
+    return libs[key]
 
 
 def _check(rc, nspec=3):
@@ -100,3 +103,9 @@ def run_velocity_advance(cfg, rhohalf, sponge=None):
     VelocityAdvance (unew and umac; uedge stays inside VelocityAdvance)."""
     L = lib(cfg["nspec"])
     return pyoracle.run_velocity_advance(cfg, rhohalf, sponge, _entry=(L.ref_run_velocity_advance, L.ref_last_error))
+
+
+def run_stage_2d(cfg):
+    """pyoracle.run_stage_2d run by the reference's own 2-D stage (AMREX_SPACEDIM 2 build)."""
+    L = lib(cfg["nspec"], dim=2)
+    return pyoracle.run_stage_2d(cfg, _entry=(L.ref_run_stage, L.ref_last_error))

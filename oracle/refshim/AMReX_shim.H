@@ -97,6 +97,7 @@ class IntVect {
     int v[3] = {0, 0, 0};
     IntVect() = default;
     IntVect(int a, int b, int c) : v{a, b, c} {}
+    IntVect(int a, int b) : v{a, b, 0} {}
     int& operator[](int d) { return v[d]; }
     const int& operator[](int d) const { return v[d]; }
     const int* getVect() const { return v; }
@@ -224,14 +225,18 @@ enum physicalBndryTypes : int { interior = 0, inflow, outflow, symmetry, slipwal
 
 class BCRec {
   public:
-    int bc[6] = {0, 0, 0, 0, 0, 0};
+    int bc[2 * AMREX_SPACEDIM] = {};  // lo[dim], hi[dim]; directions beyond dim read int_dir
     BCRec() = default;
     const int* lo() const { return bc; }
-    const int* hi() const { return bc + 3; }
-    int lo(int d) const { return bc[d]; }
-    int hi(int d) const { return bc[3 + d]; }
-    void setLo(int d, int v) { bc[d] = v; }
-    void setHi(int d, int v) { bc[3 + d] = v; }
+    const int* hi() const { return bc + AMREX_SPACEDIM; }
+    int lo(int d) const { return d < AMREX_SPACEDIM ? bc[d] : 0; }
+    int hi(int d) const { return d < AMREX_SPACEDIM ? bc[AMREX_SPACEDIM + d] : 0; }
+    void setLo(int d, int v) {
+        if (d < AMREX_SPACEDIM) bc[d] = v;
+    }
+    void setHi(int d, int v) {
+        if (d < AMREX_SPACEDIM) bc[AMREX_SPACEDIM + d] = v;
+    }
 };
 
 namespace Math {

@@ -11,9 +11,6 @@
 #include <BaseState.H>
 #include <BaseStateGeometry.H>
 
-#if AMREX_SPACEDIM != 3
-#error "the stand-in declares the 3-D member functions only"
-#endif
 
 #include "maestro_params.H"
 using namespace maestro;
@@ -143,14 +140,20 @@ class Maestro {
                           const bool is_input_edge_centered, const bool is_output_a_vector, const BCs& bcs = BCs(),
                           const int sbccomp = 0);
     void Addw0(FaceMFs& u_edge, const FaceMFs& w0mac, const Real& mult);
+#if (AMREX_SPACEDIM == 3)
     void MakeW0mac(FaceMFs& w0mac);
     void MakeS0mac(const BaseState<Real>& s0, FaceMFs& s0mac);
+#endif
     void MakeNormal();
     void PutDataOnFaces(const amrex::Vector<MF>& s_cc, FaceMFs& face, const bool harmonic_avg);
+#if (AMREX_SPACEDIM == 3)
     void MakeCCtoRadii();
+#endif
 
     // Source/MaestroBaseStateGeometry.cpp
+#if (AMREX_SPACEDIM == 3)
     void InitBaseStateMapSphr(const int lev, const amrex::MFIter& mfi, const DX dx_fine, const DX dx_lev);
+#endif
     void ComputeCutoffCoords(const BaseState<Real>& rho0_state) const;
     void RestrictBase(BaseState<Real>& s0, const bool is_cell_centered) const;
     void RestrictBase(const BaseStateArray<Real>& s0, const bool is_cell_centered) const;
@@ -210,6 +213,15 @@ class Maestro {
     // Source/MaestroVelPred.cpp
     void VelPred(amrex::Vector<MF>& utilde, const amrex::Vector<MF>& ufull, const FaceMFs& utrans, FaceMFs& umac,
                  const FaceMFs& w0mac, const amrex::Vector<MF>& force);
+#if (AMREX_SPACEDIM == 2)
+    void VelPredInterface(const amrex::MFIter& mfi, C4 utilde, C4 ufull, C4 utrans, C4 vtrans, C4 Imu, C4 Ipu,
+                          C4 Imv, C4 Ipv, A4 ulx, A4 urx, A4 uimhx, A4 uly, A4 ury, A4 uimhy, const Box& domainBox,
+                          const DX& dx) const;
+    void VelPredVelocities(const amrex::MFIter& mfi, C4 utilde, C4 utrans, C4 vtrans, A4 umac, A4 vmac, C4 Imfx,
+                           C4 Ipfx, C4 Imfy, C4 Ipfy, C4 ulx, C4 urx, C4 uimhx, C4 uly, C4 ury, C4 uimhy, C4 force,
+                           C4 w0_cart_in, const Box& domainBox, const DX& dx) const;
+
+#else
     void VelPredInterface(const amrex::MFIter& mfi, C4 utilde, C4 ufull, C4 utrans, C4 vtrans, C4 wtrans, C4 Imu,
                           C4 Ipu, C4 Imv, C4 Ipv, C4 Imw, C4 Ipw, A4 ulx, A4 urx, A4 uimhx, A4 uly, A4 ury,
                           A4 uimhy, A4 ulz, A4 urz, A4 uimhz, const Box& domainBox, const DX& dx) const;
@@ -221,11 +233,21 @@ class Maestro {
                            C4 Ipfz, C4 ulx, C4 urx, C4 uly, C4 ury, C4 ulz, C4 urz, C4 uimhyz, C4 uimhzy,
                            C4 vimhxz, C4 vimhzx, C4 wimhxy, C4 wimhyx, C4 force, C4 w0_cart_in,
                            const Box& domainBox, const DX& dx) const;
+#endif
 
     // Source/MaestroMakeEdgeScalars.cpp
     void MakeEdgeScal(amrex::Vector<MF>& state, FaceMFs& sedge, FaceMFs& umac, amrex::Vector<MF>& force,
                       const bool is_vel, const BCs& bcs, int nbccomp, int start_scomp, int start_bccomp,
                       int num_comp, const bool is_conservative);
+#if (AMREX_SPACEDIM == 2)
+    void MakeEdgeScalPredictor(const amrex::MFIter& mfi, A4 slx, A4 srx, A4 sly, A4 sry, A4 scal, A4 Ip, A4 Im,
+                               A4 umac, A4 vmac, A4 simhx, A4 simhy, const Box& domainBox, const BCs& bcs,
+                               const DX dx, int comp, int bccomp, bool is_vel) const;
+    void MakeEdgeScalEdges(const amrex::MFIter& mfi, A4 slx, A4 srx, A4 sly, A4 sry, A4 scal, A4 sedgex, A4 sedgey,
+                           A4 force, A4 umac, A4 vmac, A4 Ipf, A4 Imf, A4 simhx, A4 simhy, const Box& domainBox,
+                           const BCs& bcs, const DX dx, int comp, int bccomp, const bool is_vel,
+                           const bool is_conservative) const;
+#else
     static void MakeDivU(const Box& bx, A4 divu, A4 umac, A4 vmac, A4 wmac, const DX dx);
     void MakeEdgeScalPredictor(const amrex::MFIter& mfi, A4 slx, A4 srx, A4 sly, A4 sry, A4 slz, A4 srz, A4 scal,
                                A4 Ip, A4 Im, A4 slopez, A4 umac, A4 vmac, A4 wmac, A4 simhx, A4 simhy, A4 simhz,
@@ -241,6 +263,8 @@ class Maestro {
                            A4 simhxy, A4 simhxz, A4 simhyx, A4 simhyz, A4 simhzx, A4 simhzy, const Box& domainBox,
                            const BCs& bcs, const DX dx, int comp, int bccomp, const bool is_vel,
                            const bool is_conservative) const;
+
+#endif
 
     void PPM(const amrex::Box& bx, amrex::Array4<const amrex::Real> const s,
              amrex::Array4<const amrex::Real> const u, amrex::Array4<const amrex::Real> const v,

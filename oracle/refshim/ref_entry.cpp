@@ -111,7 +111,7 @@ void bc_setup(Maestro& m) {
     m.bcs_u.assign(AMREX_SPACEDIM, BCRec());
     m.bcs_f.assign(Nscal, BCRec());
     for (int side = 0; side < 2; ++side)
-        for (int dir = 0; dir < 3; ++dir) {
+        for (int dir = 0; dir < AMREX_SPACEDIM; ++dir) {
             const int pb = side == 0 ? m.phys_bc.lo(dir) : m.phys_bc.hi(dir);
             int u, s, t, pi, f;
             int udir = -999;
@@ -138,7 +138,8 @@ void bc_setup(Maestro& m) {
 void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in);
 
 void setup(Maestro& m, const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in) {
-    if (p->dim == 2) amrex::Abort("the reference build here is 3-D");
+    if ((p->dim == 2 ? 2 : 3) != AMREX_SPACEDIM)
+        amrex::Abort("this reference build is " + std::to_string(AMREX_SPACEDIM) + "-D");
     if (p->nspec != NumSpec) amrex::Abort("the reference build has NumSpec " + std::to_string(NumSpec));
     set_params(p);
     m.dt = p->dt;
@@ -183,8 +184,8 @@ void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in) {
         nr_fine = nr_irreg + 1;
         dr_fine = p->dx[0] / maestro::drdxfac;
     } else {
-        nr_fine = p->dom_hi[2] + 1;
-        dr_fine = p->dx[2];
+        nr_fine = p->dom_hi[AMREX_SPACEDIM - 1] + 1;
+        dr_fine = p->dx[AMREX_SPACEDIM - 1];
     }
     // plane-parallel gravity is the constant grav_const (MakeGravCell,
     // Source/MaestroMakeGrav.cpp); the caller's grav_cell holds it
@@ -221,6 +222,7 @@ void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in) {
     m.w0_cart.resize(1);
     m.w0_cart[0].define(ba, DistributionMapping(), AMREX_SPACEDIM, 2);
     m.w0_cart[0].setVal(0.0);
+#if (AMREX_SPACEDIM == 3)
     if (maestro::spherical) {
         m.normal.resize(1);
         m.normal[0].define(ba, DistributionMapping(), 3, 1);
@@ -229,6 +231,7 @@ void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in) {
         m.MakeNormal();
         m.MakeCCtoRadii();
     }
+#endif
     m.Put1dArrayOnCart(m.w0, m.w0_cart, true, true, m.bcs_u, 0, 1);
 }
 
@@ -258,6 +261,7 @@ void gather(const Box& dom, const MultiFab& mf, int c0, int nc, double* dst) {
 
 BoxArray faces(const BoxArray& ba, int d) { return convert(ba, IntVect(d == 0, d == 1, d == 2)); }
 
+#if (AMREX_SPACEDIM == 3)
 int run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in,
                          const double* rhohalf, const double* sponge, double* unew_out, double* const* umac_out) {
     Maestro m;
@@ -320,6 +324,8 @@ int run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, const
 // AdvancePremac -> Addw0 -> DensityAdvance(1) -> Addw0 -> EnthalpyAdvance(1) as the
 // predictor of Maestro::AdvanceTimeStep calls them (Source/MaestroAdvance.cpp:160-210,
 // 290-360, 436-548), the MAC projection skipped
+#endif
+
 int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out) {
     Maestro m;
     setup(m, p, nboxes, boxes, in);
@@ -330,7 +336,7 @@ int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
     m.uold.resize(1);
     m.uold[0].define(ba, dm, AMREX_SPACEDIM, ng);
     m.uold[0].setVal(0.0);
-    scatter(dom, in->uold, m.uold[0], 0, 3);
+    scatter(dom, in->uold, m.uold[0], 0, AMREX_SPACEDIM);
     m.sold.resize(1);
     m.sold[0].define(ba, dm, Nscal, ng);
     m.sold[0].setVal(0.0);
@@ -341,19 +347,19 @@ int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
     MultiFab::Copy(m.snew[0], m.sold[0], Temp, Temp, 1, ng);
     m.gpi.resize(1);
     m.gpi[0].define(ba, dm, AMREX_SPACEDIM, 0);
-    scatter(dom, in->gpi, m.gpi[0], 0, 3);
+    scatter(dom, in->gpi, m.gpi[0], 0, AMREX_SPACEDIM);
     Vector<MultiFab> thermal(1), scal_force(1), etarhoflux(1), w0_force_cart(1);
     thermal[0].define(ba, dm, 1, 1);
     thermal[0].setVal(0.0);
     if (in->thermal) scatter(dom, in->thermal, thermal[0], 0, 1);
     scal_force[0].define(ba, dm, Nscal, 1);
     scal_force[0].setVal(0.0);
-    etarhoflux[0].define(faces(ba, 2), dm, 1, 1);
+    etarhoflux[0].define(faces(ba, AMREX_SPACEDIM - 1), dm, 1, 1);
     etarhoflux[0].setVal(0.0);
     w0_force_cart[0].define(ba, dm, AMREX_SPACEDIM, 1);
     w0_force_cart[0].setVal(0.0);
     Vector<std::array<MultiFab, AMREX_SPACEDIM>> umac(1), sedge(1), sflux(1), w0mac(1);
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < AMREX_SPACEDIM; ++d) {
         umac[0][d].define(faces(ba, d), dm, 1, 1);
         sedge[0][d].define(faces(ba, d), dm, Nscal, 0);
         sflux[0][d].define(faces(ba, d), dm, Nscal, 0);
@@ -363,7 +369,9 @@ int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
         sflux[0][d].setVal(0.0);
         w0mac[0][d].setVal(0.0);
     }
+#if (AMREX_SPACEDIM == 3)
     if (maestro::spherical) m.MakeW0mac(w0mac);
+#endif
     if (maestro::evolve_base_state) m.Put1dArrayOnCart(m.w0_force, w0_force_cart, false, true, m.bcs_f, 0);
     BaseState<Real> rho0_predicted_edge(1, m.base_geom.nr_fine + 1);
     {
@@ -374,7 +382,7 @@ int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
     m.FillPatch(m.t_old, m.sold, m.sold, m.sold, 0, 0, Nscal, 0, m.bcs_s);
 
     m.AdvancePremac(umac, w0mac, w0_force_cart);
-    for (int d = 0; d < 3; ++d) gather(dom, umac[0][d], 0, 1, out->umac_vp[d]);
+    for (int d = 0; d < AMREX_SPACEDIM; ++d) gather(dom, umac[0][d], 0, 1, out->umac_vp[d]);
     m.Addw0(umac, w0mac, 1.);
     m.DensityAdvance(1, m.sold, m.snew, sedge, sflux, scal_force, etarhoflux, umac, w0mac, rho0_predicted_edge);
     m.Addw0(umac, w0mac, -1.);
@@ -382,7 +390,7 @@ int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
     m.EnthalpyAdvance(1, m.sold, m.snew, sedge, sflux, scal_force, umac, w0mac, thermal);
     m.Addw0(umac, w0mac, -1.);
 
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < AMREX_SPACEDIM; ++d) {
         gather(dom, umac[0][d], 0, 1, out->umac_end[d]);
         gather(dom, sedge[0][d], 0, Nscal, out->sedge[d]);
         gather(dom, sflux[0][d], 0, Nscal, out->sflux[d]);
@@ -420,6 +428,7 @@ void mf_to(const MultiFab& mf, const mo_fab* f, int c0, int nc) {
     }
 }
 
+#if (AMREX_SPACEDIM == 3)
 int member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
            int start_comp, int num_comp, int is_cons, const mo_fab* args) {
     Maestro m;
@@ -446,6 +455,7 @@ int member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* ba
             amrex::Abort("member function not in this reference build");
     }
 }
+#endif
 
 }  // namespace
 
@@ -468,7 +478,10 @@ int ref_ppm(int ppm_type_, double dt, double rel_eps, const double* dx, const in
         }
         GpuArray<Real, AMREX_SPACEDIM> dxa;
         for (int d = 0; d < AMREX_SPACEDIM; ++d) dxa[d] = dx[d];
-        m.PPM(box_of(bx), arr<const Real>(s), arr<const Real>(u), arr<const Real>(v), arr<const Real>(w),
+        m.PPM(box_of(bx), arr<const Real>(s), arr<const Real>(u), arr<const Real>(v),
+#if (AMREX_SPACEDIM == 3)
+              arr<const Real>(w),
+#endif
               arr<Real>(Ip), arr<Real>(Im), box_of(dom), bcs, dxa, is_umac != 0, comp, comp);
         return 0;
     } catch (const std::exception& e) {
@@ -493,7 +506,9 @@ int ref_slopes(int slope_order_, int d, const int* dom, const int* bx, const Ref
         auto sl = arr<Real>(slope);
         if (d == 0) Maestro::Slopex(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
         if (d == 1) Maestro::Slopey(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
+#if (AMREX_SPACEDIM == 3)
         if (d == 2) Maestro::Slopez(box_of(bx), sa, sl, box_of(dom), bcs, ncomp, 0);
+#endif
         return 0;
     } catch (const std::exception& e) {
         g_err = e.what();
@@ -501,6 +516,7 @@ int ref_slopes(int slope_order_, int d, const int* dom, const int* bx, const Ref
     }
 }
 
+#if (AMREX_SPACEDIM == 3)
 /* mo_run_velocity_advance (oracle/maestro_oracle.h) run by the reference's own
  * AdvancePremac, FillPatchUedge (the MAC projection's closing face fill) and
  * VelocityAdvance with UpdateVel; writes unew and umac (uedge stays inside
@@ -516,6 +532,7 @@ int ref_run_velocity_advance(const mo_params* p, int nboxes, const int* boxes, c
         return -1;
     }
 }
+#endif
 
 /* The stage of mo_run_stage (oracle/maestro_oracle.h) run by the reference's own
  * AdvancePremac, DensityAdvance and EnthalpyAdvance on one 3-D level; every output but
@@ -529,6 +546,7 @@ int ref_run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inp
     }
 }
 
+#if (AMREX_SPACEDIM == 3)
 /* One Maestro member function on one 3-D level, the arguments of mo_member
  * (oracle/maestro_oracle.h): the same slots, per-box FABs and outputs, run by the
  * reference's own member function on MultiFabs holding copies of the caller's FABs;
@@ -542,6 +560,7 @@ int ref_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs
         return -1;
     }
 }
+#endif
 
 const char* ref_last_error(void) { return g_err.c_str(); }
 }

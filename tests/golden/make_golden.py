@@ -31,6 +31,8 @@ STAGE_FIXTURES = {
                                                        bc_lo=(SYMMETRY, SLIPWALL, NOSLIPWALL),
                                                        bc_hi=(OUTFLOW, SLIPWALL, OUTFLOW), seed=902, cfl=0.5),
     "spherical_ppm2": lambda: configs.spherical_config(n=12, nspec=2, ppm_type=2, max_grid=6),
+    "planar_2d_ppm1": lambda: configs.planar_config_2d(n=(32, 32), nspec=2, ppm_type=1, max_grid=16, rho_pert=1e-3,
+                                                       w0_amp=1e4),
 }
 STAGE_INPUTS = ("uold", "sold", "gpi", "rho0_old", "rho0_new", "rhoh0_old", "rhoh0_new", "p0_old", "p0_new", "psi",
                 "grav_cell", "w0_force", "w0", "rho0_predicted_edge")
@@ -78,12 +80,13 @@ def main():
     out = {}
     for name, make in STAGE_FIXTURES.items():
         cfg = make()
-        ref = pyref.run_stage(cfg)
+        nd = 2 if cfg.get("dim") == 2 else 3
+        ref = pyref.run_stage_2d(cfg) if nd == 2 else pyref.run_stage(cfg)
         comps = [RHO, RHOH] + list(range(FIRSTSPEC, FIRSTSPEC + cfg["nspec"]))
         for k in STAGE_INPUTS:
             out[f"{name}_in_{k}"] = cfg[k]
         out[f"{name}_snew"] = ref["snew"][comps]
-        for d in range(3):
+        for d in range(nd):
             out[f"{name}_umac_end{d}"] = ref["umac_end"][d]
             out[f"{name}_sflux{d}_rho"] = ref["sflux"][d][RHO]
     np.savez_compressed(os.path.join(HERE, "stage.npz"), **out)

@@ -33,7 +33,7 @@ def test_madv_ppm_matches_golden(c):
     st.close()
 
 
-@pytest.mark.parametrize("name", ("planar_ppm1_w0", "planar_ppm2_walls", "spherical_ppm2"))
+@pytest.mark.parametrize("name", ("planar_ppm1_w0", "planar_ppm2_walls", "spherical_ppm2", "planar_2d_ppm1"))
 def test_gpu_stage_matches_golden(name):
     """The whole stage on the GPU (graph-replayed batched kernels) against the reference's
     own stage on the same inputs, bit for bit."""

@@ -216,3 +216,41 @@ def test_velocity_advance_matches_reference_source(name, with_sponge):
     for d in range(3):
         assert np.array_equal(ours["umac"][d], ref["umac"][d]), f"{name}: umac[{d}]"
         assert np.array_equal(ours["unew"][d], ref["unew"][d]), f"{name}: unew comp {d}"
+
+
+# --------------------------------------------------------------------------- 2-D stage
+# the reference built with AMREX_SPACEDIM = 2 (its 2-D branches: y radial, two velocity
+# components), the same predictor sequence
+def stage_cases_2d():
+    from maestroex_gb300.params import NOSLIPWALL, OUTFLOW, SLIPWALL, SYMMETRY
+    C = {}
+    for ppm in (1, 2, 0):
+        C[f"2-D ppm{ppm}"] = lambda ppm=ppm: configs.planar_config_2d(n=(48, 64), nspec=3, ppm_type=ppm, max_grid=16,
+                                                                     rho_pert=1e-3, w0_amp=1e4)
+    C["2-D walls ppm2"] = lambda: configs.planar_config_2d(n=(40, 48), nspec=2, ppm_type=2, max_grid=16,
+                                                           bc_lo=(SLIPWALL, NOSLIPWALL), bc_hi=(OUTFLOW, SYMMETRY))
+    C["2-D 256^2 one box (the 2-D workload)"] = lambda: configs.workload_2d(n=256)
+    return C
+
+
+STAGE_CASES_2D = stage_cases_2d()
+
+
+@pytest.mark.parametrize("case", list(STAGE_CASES_2D))
+def test_2d_stage_matches_reference_source(case):
+    from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
+    cfg = STAGE_CASES_2D[case]()
+    a = pyoracle.run_stage_2d(cfg, checked=True)
+    b = pyref.run_stage_2d(cfg)
+    comps = [RHO, RHOH] + list(range(FIRSTSPEC, FIRSTSPEC + cfg["nspec"]))
+    for key in ("umac_vp", "umac_end"):
+        for d in range(2):
+            assert np.array_equal(a[key][d], b[key][d]), f"{case}: {key}[{d}]"
+    for key in ("sedge", "sflux"):
+        for d in range(2):
+            for c in comps:
+                assert np.array_equal(a[key][d][c], b[key][d][c]), f"{case}: {key}[{d}] comp {c}"
+    for key in ("snew", "sold_end"):
+        for c in comps:
+            assert np.array_equal(a[key][c], b[key][c]), f"{case}: {key} comp {c}"
+    assert np.array_equal(a["etarhoflux"], b["etarhoflux"]), f"{case}: etarhoflux"
