@@ -374,6 +374,17 @@ int madv_autotune_trial(madv_ctx* ctx, int threads);
 int madv_autotune_finish(madv_ctx* ctx, char* json, int len);
 int madv_autotune_apply(madv_ctx* ctx, const char* json);
 
+/* Implementation options of a context (no counterpart in the reference; results never
+ * depend on them):
+ *   "staged_ppm"      1 (default): each PPM direction runs as one kernel over tiles of whole
+ *                     pencils staged in shared memory by bulk copies; 0: three launches
+ *                     (slopes, interface values, cell limiter) through global memory.
+ *   "sweep_tile_Da", "sweep_tile_Db" (D = 0, 1, 2): cells of a staged tile across
+ *                     direction D, in the first / second transverse direction (x before y
+ *                     before z); defaults 4 x 2 for D = 0 and 32 x 2 for D = 1, 2.
+ * Returns MADV_ERR_PARAM for an unknown key or a value outside 1..256. */
+int madv_set_option(madv_ctx* ctx, const char* key, int value);
+
 /* FP64 FMA issue-rate probe of the current device (TFLOP/s, 2 flops per FMA): the
  * ceiling of the FP64-bound stage kernels.  No counterpart in the reference. */
 int madv_probe_fp64_peak(double* tflops, void* stream);

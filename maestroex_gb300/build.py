@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmaestro_adv.so")
-SOURCES = ["madv_kernels.cu", "madv_ctx.cu", "madv_probe.cu", "madv_box.cu", "madv_noalloc.cu", "madv_amr.cu", "madv_adjoint.cu", "madv_sphr.cu", "madv_macproj.cu"]
+SOURCES = ["madv_kernels.cu", "madv_ctx.cu", "madv_probe.cu", "madv_box.cu", "madv_noalloc.cu", "madv_amr.cu", "madv_adjoint.cu", "madv_sphr.cu", "madv_macproj.cu", "madv_sweep.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off"]
 

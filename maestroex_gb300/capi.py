@@ -29,7 +29,7 @@ EXPORTED = [
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
     "madv_autotune_trial", "madv_autotune_finish", "madv_autotune_apply",
     "madv_make_utrans", "madv_vel_pred", "madv_make_edge_scal", "madv_make_rhox_flux", "madv_make_rhoh_flux",
-    "madv_update_scal", "madv_velocity_advance", "madv_est_dt", "madv_mac_project",
+    "madv_update_scal", "madv_velocity_advance", "madv_est_dt", "madv_mac_project", "madv_set_option",
 ]
 
 
@@ -130,6 +130,7 @@ def lib():
         L.madv_last_launch_count.argtypes = [C.c_void_p]
         L.madv_last_launch_count.restype = C.c_long
         L.madv_profile.argtypes = [C.c_void_p, C.c_int]
+        L.madv_set_option.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
         L.madv_profile_report.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
         L.madv_probe_fp64_peak.argtypes = [P(C.c_double), C.c_void_p]
         L.madv_selftest_exact.argtypes = [C.c_double, C.c_double, C.c_longlong, P(C.c_longlong), C.c_void_p]

@@ -307,6 +307,7 @@ static void free_layout(Ctx& c) {
     for (auto& kv : c.amr_tables)
         if (kv.second.d) cudaFree(kv.second.d);
     c.amr_tables.clear();
+    sweep_free(c);
     if (c.d_owner) cudaFree(c.d_owner);
     c.d_owner = nullptr;
     c.h_owner.clear();
@@ -887,6 +888,10 @@ static int finish(Hier& H) {
         if (f & 6) {
             set_error("coarse-fine fill: a coarse cell or face was not available (levels not properly nested)");
             return MADV_ERR_LAYOUT;
+        }
+        if (f & 8) {
+            set_error("staged PPM sweep: a shared-memory staging copy did not complete in time");
+            return MADV_ERR_CUDA;
         }
     }
     return MADV_OK;
@@ -2237,6 +2242,32 @@ int madv_autotune_apply(madv_ctx* h, const char* json) {
         c->tpb_by_name = tab;
         c->tpb_choice.clear();
         c->tpb_max.clear();
+    }
+    drop_graph(h);
+    return MADV_OK;
+}
+
+int madv_set_option(madv_ctx* h, const char* key, int value) {
+    if (!h || !key) return MADV_ERR_PARAM;
+    Hier H = h->H();
+    const std::string k(key);
+    if (k == "staged_ppm") {
+        for (auto* c : H.L) c->staged_ppm = value != 0;
+    } else if (k.rfind("sweep_tile_", 0) == 0 && k.size() == 13 && k[11] >= '0' && k[11] <= '2' &&
+               (k[12] == 'a' || k[12] == 'b')) {
+        if (value < 1 || value > 256) return MADV_ERR_PARAM;
+        const int D = k[11] - '0';
+        for (auto* c : H.L) {
+            auto it = c->sweep_shape.find(D);
+            std::array<int, 2> sh = it != c->sweep_shape.end() ? it->second
+                                                             : (D == 0 ? std::array<int, 2>{4, 2}
+                                                                       : std::array<int, 2>{32, 2});
+            sh[k[12] == 'a' ? 0 : 1] = value;
+            c->sweep_shape[D] = sh;
+        }
+    } else {
+        set_error("madv_set_option: unknown option " + k);
+        return MADV_ERR_PARAM;
     }
     drop_graph(h);
     return MADV_OK;

@@ -160,6 +160,10 @@ struct Ctx {
     // component's PPM and transverse scratch (F_FACE*, F_Q*, F_SIMH*) at its own storage
     // there, to keep them for the reverse sweep
     std::function<void(int)> edge_tape_begin, edge_tape;
+    // PPM sweeps: the staged (fused) form (madv_sweep.cu) unless turned off; tile shape
+    // across each direction D (cells in the two transverse directions), default when absent
+    bool staged_ppm = true;
+    std::map<int, std::array<int, 2>> sweep_shape;
     // scratch of the single-box entry points (madv_ppm), grown on demand
     double* box_scratch = nullptr;
     long box_scratch_n = 0;
@@ -191,6 +195,10 @@ const CopyTable& copy_table(Ctx& c, int ng, int nodal);
 
 void set_error(const std::string& s);
 bool cuda_ok(cudaError_t e, const char* what);
+
+// ---- staged PPM sweep (madv_sweep.cu) ----
+bool ppm_sweep(Ctx& c, int D, int fs, int sc, int fu, int uc, int umac, int fip, int fim, int lo_ext, int hi_ext);
+void sweep_free(Ctx& c);
 
 // ---- kernel launch wrappers (madv_kernels.cu) ----
 void fill_boundary(Ctx& c, int fid, int c0, int nc);

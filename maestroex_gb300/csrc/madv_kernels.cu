@@ -453,6 +453,7 @@ static bool ext_like(int t) { return t == BC_EXT_DIR || t == BC_HOEXTRAP; }
 template <int D>
 static void ppm_dir(Ctx& c, int fs, int sc, const BCRecD& bc, int fu, int uc, int umac, int fip, int fim) {
     const int lo_ext = ext_like(bc.lo[D]), hi_ext = ext_like(bc.hi[D]);
+    if (ppm_sweep(c, D, fs, sc, fu, uc, umac, fip, fim, lo_ext, hi_ext)) return;
     const int dlo = c.P.dom_lo[D], dhi = c.P.dom_hi[D];
     const RecipC r6 = make_recip(6.0);
     const int gf = c.P.ppm_type == 2 ? 2 : 1;

@@ -288,6 +288,10 @@ class ScalarAdvectionStage:
     def launch_count(self):
         return lib().madv_last_launch_count(self.ctx)
 
+    def set_option(self, key, value):
+        """madv_set_option: an implementation option (staged PPM sweeps, their tile shape)."""
+        check(lib().madv_set_option(self.ctx, key.encode(), int(value)))
+
     def autotune(self, run_batched, candidates=(32, 64, 128, 256, 512)):
         """Launch-shape autotuner (madv_autotune_*): run_batched() runs the caller's stage once
         in MODE_BATCHED; it is timed per kernel for every candidate block size, and the fastest
