@@ -616,9 +616,35 @@ static void density_advance(Hier& H, int which_step) {
 
 // Maestro::EnthalpyAdvance (Source/MaestroEnthalpyAdvance.cpp:6-352); which_step 2 averages
 // the old and new base state in the fluxes (:234-317) and the final MakeRhoHForce (:336)
+// Maestro::ConvertRhoHToH (Source/MaestroConvert.cpp:93-114)
+static void convert_rhoh_to_h_h(Hier& H, int flag) {
+    for (auto* c : H.L) convert_rhoh_to_h(*c, flag);
+    average_down_h(H, F_SOLD, RHOH, 1);
+    if (flag) fill_patch_h(H, F_SOLD, RHOH, 1, BCS_F, 0, 0, RHOH);
+    else fill_patch_h(H, F_SOLD, RHOH, 1, BCS_S, RHOH, 0, RHOH);
+}
+
+// the fluxes of (rho h): the base state of the enthalpy (and, for the h prediction, of the
+// density) at the old time, with the new one for which_step 2
+static void rhoh_flux_h(Hier& H, int which_step) {
+    const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
+    const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
+    const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
+    const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
+    if (H[0].sph) {  // rhoh0 on faces, exact base state (Source/MaestroEnthalpyAdvance.cpp:187-220)
+        make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
+        make_s0mac_h(H, rh0n, F_S0MACB0);
+    }
+    for (auto* c : H.L)
+        make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en), c->b1("rho0_old"),
+                       c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
+}
+
 static void enthalpy_advance(Hier& H, int which_step) {
     const int ept = H[0].P.enthalpy_pred_type;
     const int nscal = H[0].nscal;
+    // predict_h: (rho h) -> h (Source/MaestroEnthalpyAdvance.cpp:40-43)
+    if (ept == 2) convert_rhoh_to_h_h(H, 1);
     // scal_force.setVal(0) (Source/MaestroEnthalpyAdvance.cpp:51); the enthalpy half reads RhoH only
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
     addw0_h(H, F_UMAC0, -1.0);
@@ -627,17 +653,14 @@ static void enthalpy_advance(Hier& H, int which_step) {
         put1d_h(H, F_RHOH0CART, "rhoh0_old", 0, 1, 0, BCS_S, RHOH, 0, RHOH);
         modify_scal_force_h(H, RHOH, "rhoh0_edge_old", F_RHOH0CART, 0);
     }
+    if (ept == 2)  // the force of h: the (rho h) force over rho (:80-88)
+        for (auto* c : H.L) h_force(*c);
     addw0_h(H, F_UMAC0, 1.0);
     if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
     for (auto* c : H.L) make_edge_scal(*c, RHOH, 1, BCS_S, ept == 0, 0);
     if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, RHOH, BCS_S, 0);
-    const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
-    const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
-    if (H[0].sph) {  // rhoh0 on faces, exact base state (Source/MaestroEnthalpyAdvance.cpp:187-220)
-        make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
-        make_s0mac_h(H, rh0n, F_S0MACB0);
-    }
-    for (auto* c : H.L) make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en));
+    if (ept == 2) convert_rhoh_to_h_h(H, 0);  // h -> (rho h) (:164-167)
+    rhoh_flux_h(H, which_step);
     flux_sync_h(H, RHOH, 1);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
     addw0_h(H, F_UMAC0, -1.0);
@@ -1190,8 +1213,9 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
         return MADV_ERR_PARAM;
     }
     if (p->species_pred_type < 1 || p->species_pred_type > 3 || p->enthalpy_pred_type < 0 ||
-        p->enthalpy_pred_type > 1) {
-        set_error("species_pred_type must be 1..3, enthalpy_pred_type 0 or 1");
+        p->enthalpy_pred_type > 2) {
+        set_error("species_pred_type must be 1..3, enthalpy_pred_type 0, 1 or 2 (3-6 predict the temperature "
+                  "and need the equation of state)");
         return MADV_ERR_UNSUPPORTED;
     }
     if (p->spherical && (p->use_exact_base_state != 1 || p->dim == 2 || p->enthalpy_pred_type != 1)) {
@@ -1864,13 +1888,7 @@ static int flux_member(madv_ctx* h, int which, int which_step, const madv_multif
             }
             if (etarhoflux) copy_fab(c, F_USER + U_ETA, 0, F_ETA, 0, 1, 0);
         } else {
-            const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
-            const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
-            if (c.sph) {
-                make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
-                make_s0mac_h(H, rh0n, F_S0MACB0);
-            }
-            make_rhoh_flux(c, c.b1("rhoh0_old"), c.b1("rhoh0_edge_old"), c.b1(rh0n), c.b1(rh0en));
+            rhoh_flux_h(H, which_step);
             for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_SFLUX0 + d, RHOH, F_SFLUX0 + d, RHOH, 1, 0);
         }
         return finish(H);

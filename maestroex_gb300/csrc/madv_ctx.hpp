@@ -228,7 +228,10 @@ void convert_rhox_to_x(Ctx& c, int flag);
 void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
                     const double* r0e_new);
 void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
-                    const double* rh0e_new);
+                    const double* rh0e_new, const double* r0_old, const double* r0e_old, const double* r0_new,
+                    const double* r0e_new);
+void convert_rhoh_to_h(Ctx& c, int flag);  // valid region
+void h_force(Ctx& c);                      // scal_force(RhoH) /= sold(Rho), valid + 1 ghost
 void sum_species_edges(Ctx& c);
 long ppm_box_scratch_doubles(const int n[3]);
 int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int comp, const madv_fab* u,
@@ -264,7 +267,8 @@ void put_in_pert_form_2d(Ctx& c, const double* d_s0, int comp, int flag);
 void make_rhox_flux_2d(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
                        const double* r0e_new);
 void make_rhoh_flux_2d(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
-                       const double* rh0e_new);
+                       const double* rh0e_new, const double* r0_old, const double* r0e_old, const double* r0_new,
+                       const double* r0e_new);
 void sum_species_edges_2d(Ctx& c);
 void update_scal_2d(Ctx& c, int start_comp);
 

@@ -1254,14 +1254,24 @@ void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const d
 }
 
 // MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:673-786)
+// enthalpy_pred_type 2 (the edge state is h, :673-786 have_h): (rho0 edge + rho') h with
+// species_pred_type 1 (ra, rb: rho0 on the faces' radial positions), rho h otherwise
 template <int D>
-__global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const double* __restrict__ bb) {
+__global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const double* __restrict__ bb, int spt,
+                            const double* __restrict__ ra, const double* __restrict__ rb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView e = VW(F_SEDGE0 + D);
     const double u = at(VW(F_UMAC0 + D), i, j, k);
     double f;
     if (ept == 0) {
         f = u * at(e, i, j, k, RHOH);
+    } else if (ept == 2) {
+        if (spt == 1) {
+            const double rho0_edge = 0.5 * (ra[k] + rb[k]);
+            f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, RHOH);
+        } else {
+            f = u * at(e, i, j, k, RHO) * at(e, i, j, k, RHOH);
+        }
     } else {
         const double rhoh0_edge = 0.5 * (a[k] + bb[k]);
         f = D < 2 ? u * (rhoh0_edge + at(e, i, j, k, RHOH)) : u * (at(e, i, j, k, RHOH) + rhoh0_edge);
@@ -1270,13 +1280,36 @@ __global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const 
 }
 
 void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
-                    const double* rh0e_new) {
+                    const double* rh0e_new, const double* r0_old, const double* r0e_old, const double* r0_new,
+                    const double* r0e_new) {
     if (c.sph) return make_rhoh_flux_sph(c);
-    if (c.ndim == 2) return make_rhoh_flux_2d(c, rh0_old, rh0e_old, rh0_new, rh0e_new);
-    const int ept = c.P.enthalpy_pred_type;
-    launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux<0>, c.V(), ept, rh0_old, rh0_new);
-    launch(c, rg_grow(c, 0, 1), 1, k_rhoh_flux<1>, c.V(), ept, rh0_old, rh0_new);
-    launch(c, rg_grow(c, 0, 2), 1, k_rhoh_flux<2>, c.V(), ept, rh0e_old, rh0e_new);
+    if (c.ndim == 2) return make_rhoh_flux_2d(c, rh0_old, rh0e_old, rh0_new, rh0e_new, r0_old, r0e_old, r0_new, r0e_new);
+    const int ept = c.P.enthalpy_pred_type, spt = c.P.species_pred_type;
+    launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux<0>, c.V(), ept, rh0_old, rh0_new, spt, r0_old, r0_new);
+    launch(c, rg_grow(c, 0, 1), 1, k_rhoh_flux<1>, c.V(), ept, rh0_old, rh0_new, spt, r0_old, r0_new);
+    launch(c, rg_grow(c, 0, 2), 1, k_rhoh_flux<2>, c.V(), ept, rh0e_old, rh0e_new, spt, r0e_old, r0e_new);
+}
+
+// Maestro::ConvertRhoHToH on the valid region (Source/MaestroConvert.cpp:93-105): flag,
+// (rho h) -> h = (rho h) / rho; else h -> h rho
+__global__ void k_rhoh_to_h(KARGS, int flag) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView s = VW(F_SOLD);
+    double& a = at(s, i, j, k, RHOH);
+    a = flag ? a / at(s, i, j, k, RHO) : a * at(s, i, j, k, RHO);
+}
+void convert_rhoh_to_h(Ctx& c, int flag) { launch(c, rg_grow(c, 0), 1, k_rhoh_to_h, c.V(), flag); }
+
+// the prediction force of h: the (rho h) force over rho, valid cells and one ghost cell
+// (MultiFab::Divide, Source/MaestroEnthalpyAdvance.cpp:83-88)
+__global__ void k_h_force(KARGS) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    double& f = at(VW(F_SCALFORCE), i, j, k, RHOH);
+    f = f / at(VW(F_SOLD), i, j, k, RHO);
+}
+void h_force(Ctx& c) {
+    const int gz = c.ndim == 2 ? 0 : 1;
+    launch(c, region(c, 1, 1, gz, 1, 1, gz, -1), 1, k_h_force, c.V());
 }
 
 // species_pred_type 2: rho edge state = sum of the (rho X) edge states
@@ -1899,13 +1932,21 @@ __global__ void k_rhox_flux_2d(KARGS, int nspec, int spt, int do_eta, const doub
 
 // MakeRhoHFlux, 2-D (Source/MaestroMakeFlux.cpp:597-662)
 template <int D>
-__global__ void k_rhoh_flux_2d(KARGS, int ept, const double* __restrict__ a, const double* __restrict__ bb) {
+__global__ void k_rhoh_flux_2d(KARGS, int ept, const double* __restrict__ a, const double* __restrict__ bb, int spt,
+                               const double* __restrict__ ra, const double* __restrict__ rb) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView e = VW(F_SEDGE0 + D);
     const double u = at(VW(F_UMAC0 + D), i, j, k);
     double f;
     if (ept == 0) {
         f = u * at(e, i, j, k, RHOH);
+    } else if (ept == 2) {  // the edge state is h (Source/MaestroMakeFlux.cpp:597-662, have_h)
+        if (spt == 1) {
+            const double rho0_edge = 0.5 * (ra[j] + rb[j]);
+            f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, RHOH);
+        } else {
+            f = u * at(e, i, j, k, RHO) * at(e, i, j, k, RHOH);
+        }
     } else {
         const double rhoh0_edge = 0.5 * (a[j] + bb[j]);
         f = D == 0 ? u * (rhoh0_edge + at(e, i, j, k, RHOH)) : u * (at(e, i, j, k, RHOH) + rhoh0_edge);
@@ -1995,10 +2036,11 @@ void make_rhox_flux_2d(Ctx& c, const double* r0_old, const double* r0e_old, cons
            w0, rpe);
 }
 void make_rhoh_flux_2d(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
-                       const double* rh0e_new) {
-    const int ept = c.P.enthalpy_pred_type;
-    launch(c, rg2(c, 0, 0), 1, k_rhoh_flux_2d<0>, c.V(), ept, rh0_old, rh0_new);
-    launch(c, rg2(c, 0, 1), 1, k_rhoh_flux_2d<1>, c.V(), ept, rh0e_old, rh0e_new);
+                       const double* rh0e_new, const double* r0_old, const double* r0e_old, const double* r0_new,
+                       const double* r0e_new) {
+    const int ept = c.P.enthalpy_pred_type, spt = c.P.species_pred_type;
+    launch(c, rg2(c, 0, 0), 1, k_rhoh_flux_2d<0>, c.V(), ept, rh0_old, rh0_new, spt, r0_old, r0_new);
+    launch(c, rg2(c, 0, 1), 1, k_rhoh_flux_2d<1>, c.V(), ept, rh0e_old, rh0e_new, spt, r0e_old, r0e_new);
 }
 void sum_species_edges_2d(Ctx& c) {
     launch(c, rg2(c, 0, 0), 1, k_sum_species<0>, c.V(), c.nspec);

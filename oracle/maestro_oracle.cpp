@@ -1047,6 +1047,18 @@ struct Lev {
         }
     }
 
+    // Maestro::ConvertRhoHToH, the valid region (Source/MaestroConvert.cpp:93-105):
+    // flag: (rho h) -> h = (rho h) / rho; else h -> rho h
+    void ConvertRhoHToH(MF& scal, bool flag) {
+        for (int b = 0; b < nb; ++b) {
+            const Arr& a = scal[b];
+            MO_FOR3(L.ba[b]) {
+                if (flag) a(i, j, k, RhoH) = a(i, j, k, RhoH) / a(i, j, k, Rho);
+                else a(i, j, k, RhoH) = a(i, j, k, RhoH) * a(i, j, k, Rho);
+            }
+        }
+    }
+
     // ------------------------------------------------------------------ fluxes
     // Maestro::MakeRhoXFlux, planar 3-D (Source/MaestroMakeFlux.cpp:18-465)
     void MakeRhoXFlux(MF* sflux, MF& etarhoflux, MF* sedge, MF* umac, const std::vector<real>& r0_old,
@@ -1105,8 +1117,11 @@ struct Lev {
     // Maestro::MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:467-1067)
     void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<real>& rh0_old,
                       const std::vector<real>& rh0e_old, const std::vector<real>& rh0_new,
-                      const std::vector<real>& rh0e_new, MF* rh0mac_old = nullptr, MF* rh0mac_new = nullptr) {
+                      const std::vector<real>& rh0e_new, MF* rh0mac_old = nullptr, MF* rh0mac_new = nullptr,
+                      const std::vector<real>* r0_old = nullptr, const std::vector<real>* r0e_old = nullptr,
+                      const std::vector<real>* r0_new = nullptr, const std::vector<real>* r0e_new = nullptr) {
         const int ept = P.enthalpy_pred_type;
+        const int spt = P.species_pred_type;
         if (P.spherical) {  // exact base state, (rho h)' predicted (Source/MaestroMakeFlux.cpp:540-548, 788-840)
             for (int b = 0; b < nb; ++b)
                 for (int d = 0; d < 3; ++d) {
@@ -1137,6 +1152,14 @@ struct Lev {
                         } else {
                             real rhoh0_edge = 0.5 * (rh0e_old[k] + rh0e_new[k]);
                             f(i, j, k, RhoH) = u(i, j, k) * (e(i, j, k, RhoH) + rhoh0_edge);
+                        }
+                    } else if (ept == 2) {  // the edge state is h (:673-786, have_h)
+                        if (spt == 1) {  // density edge state rho': x / y faces cell rho0, z faces edge rho0
+                            const real rho0_edge = d < 2 ? 0.5 * ((*r0_old)[k] + (*r0_new)[k])
+                                                         : 0.5 * ((*r0e_old)[k] + (*r0e_new)[k]);
+                            f(i, j, k, RhoH) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, RhoH);
+                        } else {  // density edge state rho
+                            f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, Rho) * e(i, j, k, RhoH);
                         }
                     }
                 }
@@ -1683,7 +1706,8 @@ struct Stage {
     }
     // Maestro::MakeRhoHFlux (Source/MaestroMakeFlux.cpp:467-1067)
     void MakeRhoHFlux(VF& sflux, VF& sedge, VF& umac, const BS& rh0_old, const BS& rh0e_old, const BS& rh0_new,
-                      const BS& rh0e_new) {
+                      const BS& rh0e_new, const BS* r0_old = nullptr, const BS* r0e_old = nullptr,
+                      const BS* r0_new = nullptr, const BS* r0e_new = nullptr) {
         VF h0mac_old(nlev), h0mac_new(nlev);
         if (P.spherical) {  // exact base state: rhoh0 on faces (Source/MaestroEnthalpyAdvance.cpp:187-220)
             MakeS0mac(rh0_old, h0mac_old);
@@ -1691,8 +1715,17 @@ struct Stage {
         }
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeRhoHFlux(sflux[lev].data(), sedge[lev].data(), umac[lev].data(), rh0_old[lev], rh0e_old[lev],
-                                rh0_new[lev], rh0e_new[lev], h0mac_old[lev].data(), h0mac_new[lev].data());
+                                rh0_new[lev], rh0e_new[lev], h0mac_old[lev].data(), h0mac_new[lev].data(),
+                                r0_old ? &(*r0_old)[lev] : nullptr, r0e_old ? &(*r0e_old)[lev] : nullptr,
+                                r0_new ? &(*r0_new)[lev] : nullptr, r0e_new ? &(*r0e_new)[lev] : nullptr);
         FluxSync(sflux, RhoH, 1);
+    }
+    // Maestro::ConvertRhoHToH with its AverageDown and FillPatch (Source/MaestroConvert.cpp:93-114)
+    void ConvertRhoHToH(VMF& scal, bool flag) {
+        for (int lev = 0; lev < nlev; ++lev) S[lev].ConvertRhoHToH(scal[lev], flag);
+        AverageDown(scal, RhoH, 1);
+        if (flag) FillPatch(scal, RhoH, 1, 0, bcs_f(), false, RhoH);
+        else FillPatch(scal, RhoH, 1, RhoH, bcs_s(), false, RhoH);
     }
     // Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
     void UpdateScal(VMF& sold, VMF& snew, VF& sflux, VMF& force, int start_comp, int num_comp) {
@@ -1769,6 +1802,8 @@ struct Stage {
             CelltoEdge(rhoh0_old, rhoh0_edge_old);
             CelltoEdge(rhoh0_new, rhoh0_edge_new);
         }
+        // predict_h: (rho h) -> h (Source/MaestroEnthalpyAdvance.cpp:40-43)
+        if (ept == 2) ConvertRhoHToH(scalold, true);
         for (auto& f : scal_force) f.setVal(0.0);
         VMF rhoh0_old_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) rhoh0_old_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
@@ -1778,12 +1813,30 @@ struct Stage {
             Put1dArrayOnCart(rhoh0_old, rhoh0_old_cart, false, false, &bcs_s(), RhoH, false);
             ModifyScalForce(scal_force, scalold, umac, rhoh0_edge_old, rhoh0_old_cart, RhoH, 0);
         }
+        if (ept == 2)  // the force of h: that of (rho h) over rho, one ghost cell (:80-88)
+            for (int lev = 0; lev < nlev; ++lev)
+                for (int b = 0; b < S[lev].nb; ++b) {
+                    const Arr& f = scal_force[lev][b];
+                    const Arr& so = scalold[lev][b];
+                    MO_FOR3(grow(S[lev].L.ba[b], 1)) f(i, j, k, RhoH) = f(i, j, k, RhoH) / so(i, j, k, Rho);
+                }
         Addw0(umac, 1.0);
         if (ept == 1) PutInPertForm(scalold, rhoh0_old, RhoH, 0, bcs_f(), true);
         MakeEdgeScal(scalold, sedge, umac, scal_force, bcs_s(), RhoH, RhoH, 1, ept == 0);
         if (ept == 1) PutInPertForm(scalold, rhoh0_old, RhoH, RhoH, bcs_s(), false);
-        if (which_step == 1) MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_old, rhoh0_edge_old);
-        else MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_new, rhoh0_edge_new);
+        if (ept == 2) ConvertRhoHToH(scalold, false);  // h -> (rho h) (:164-167)
+        const BS rho0_old = bs(&Lev::rho0_old), rho0_new = bs(&Lev::rho0_new);
+        BS rho0_edge_old(nlev), rho0_edge_new(nlev);
+        if (!P.spherical) {
+            CelltoEdge(rho0_old, rho0_edge_old);
+            CelltoEdge(rho0_new, rho0_edge_new);
+        }
+        if (which_step == 1)
+            MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_old, rhoh0_edge_old, &rho0_old,
+                         &rho0_edge_old, &rho0_old, &rho0_edge_old);
+        else
+            MakeRhoHFlux(sflux, sedge, umac, rhoh0_old, rhoh0_edge_old, rhoh0_new, rhoh0_edge_new, &rho0_old,
+                         &rho0_edge_old, &rho0_new, &rho0_edge_new);
         for (auto& f : scal_force) f.setVal(0.0, RhoH, 1, 1);
         Addw0(umac, -1.0);
         MakeRhoHForce(scal_force, 0, umac, 0, which_step);
@@ -1937,8 +1990,8 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
         if (!p->use_exact_base_state) throw std::runtime_error("spherical needs use_exact_base_state = 1");
         if (p->enthalpy_pred_type != 1) throw std::runtime_error("spherical: enthalpy_pred_type 1");
     }
-    if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
-        throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
+    if (!(p->enthalpy_pred_type >= 0 && p->enthalpy_pred_type <= 2))
+        throw std::runtime_error("enthalpy_pred_type must be 0, 1 or 2");
     if (!(p->species_pred_type >= 1 && p->species_pred_type <= 3))
         throw std::runtime_error("species_pred_type must be 1, 2 or 3");
     H.P = *p;
@@ -2172,8 +2225,8 @@ static int est_dt(const mo_params* p, int nlev, const int* nboxes, const int* bo
 static int run_stage_2d(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* in, mo_outputs* out,
                         int which_step) {
     if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
-    if (!(p->enthalpy_pred_type == 0 || p->enthalpy_pred_type == 1))
-        throw std::runtime_error("enthalpy_pred_type must be 0 or 1");
+    if (!(p->enthalpy_pred_type >= 0 && p->enthalpy_pred_type <= 2))
+        throw std::runtime_error("enthalpy_pred_type must be 0, 1 or 2");
     Stage2D T;
     Lev& S = T.S;
     S.P = *p;

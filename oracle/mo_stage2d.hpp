@@ -633,6 +633,13 @@ struct Stage2D {
         FillPatch(S.L, scal, comp, 1, bccomp, bcs, false, comp);
     }
 
+    // ConvertRhoHToH (Source/MaestroConvert.cpp:93-114), one level
+    void ConvertRhoHToH(MF& scal, bool flag) {
+        S.ConvertRhoHToH(scal, flag);
+        if (flag) FillPatch(S.L, scal, RhoH, 1, 0, S.bcs_f, false, RhoH);
+        else FillPatch(S.L, scal, RhoH, 1, RhoH, S.bcs_s, false, RhoH);
+    }
+
     void ConvertRhoXToX(MF& scal, bool flag) {
         S.ConvertRhoXToX(scal, flag);
         if (flag) FillPatch(S.L, scal, FirstSpec, nspec, 0, S.bcs_f, false, FirstSpec);
@@ -670,8 +677,11 @@ struct Stage2D {
     // MakeRhoHFlux, 2-D (Source/MaestroMakeFlux.cpp:597-662)
     void MakeRhoHFlux(MF* sflux, MF* sedge, MF* umac, const std::vector<real>& rh0_old,
                       const std::vector<real>& rh0e_old, const std::vector<real>& rh0_new,
-                      const std::vector<real>& rh0e_new) {
+                      const std::vector<real>& rh0e_new, const std::vector<real>& r0_old,
+                      const std::vector<real>& r0e_old, const std::vector<real>& r0_new,
+                      const std::vector<real>& r0e_new) {
         const int ept = S.P.enthalpy_pred_type;
+        const int spt = S.P.species_pred_type;
         for (int b = 0; b < nb; ++b)
             for (int d = 0; d < 2; ++d) {
                 const Arr& f = sflux[d][b];
@@ -680,6 +690,13 @@ struct Stage2D {
                 MO_FOR3(nodal(L().ba[b], d)) {
                     if (ept == 0) {
                         f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, RhoH);
+                    } else if (ept == 2) {  // the edge state is h (Source/MaestroMakeFlux.cpp:597-662, have_h)
+                        if (spt == 1) {
+                            const real rho0_edge = d == 0 ? 0.5 * (r0_old[j] + r0_new[j]) : 0.5 * (r0e_old[j] + r0e_new[j]);
+                            f(i, j, k, RhoH) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, RhoH);
+                        } else {
+                            f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, Rho) * e(i, j, k, RhoH);
+                        }
                     } else if (d == 0) {
                         real rhoh0_edge = 0.5 * (rh0_old[j] + rh0_new[j]);
                         f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
@@ -800,6 +817,7 @@ struct Stage2D {
         std::vector<real> rhoh0_edge_old, rhoh0_edge_new;
         Lev::CelltoEdge(S.rhoh0_old, rhoh0_edge_old);
         Lev::CelltoEdge(S.rhoh0_new, rhoh0_edge_new);
+        if (ept == 2) ConvertRhoHToH(scalold, true);  // predict_h (Source/MaestroEnthalpyAdvance.cpp:40-43)
         scal_force.setVal(0.0);
         MF rhoh0_old_cart;
         rhoh0_old_cart.define(L().ba, 1, 1, -1, 0.0);
@@ -809,12 +827,26 @@ struct Stage2D {
             Put1dArrayOnCart(S.rhoh0_old, rhoh0_old_cart, false, false, &S.bcs_s, RhoH, false);
             ModifyScalForce(scal_force, scalold, umac, rhoh0_edge_old, rhoh0_old_cart, RhoH, 0);
         }
+        if (ept == 2)  // the force of h (:80-88)
+            for (int b = 0; b < nb; ++b) {
+                const Arr& f = scal_force[b];
+                const Arr& so = scalold[b];
+                MO_FOR3(g2(L().ba[b], 1)) f(i, j, k, RhoH) = f(i, j, k, RhoH) / so(i, j, k, Rho);
+            }
         Addw0(umac, 1.0);
         if (ept == 1) PutInPertForm(scalold, S.rhoh0_old, RhoH, 0, S.bcs_f, true);
         MakeEdgeScal(scalold, sedge, umac, scal_force, S.bcs_s, RhoH, RhoH, 1, ept == 0);
         if (ept == 1) PutInPertForm(scalold, S.rhoh0_old, RhoH, RhoH, S.bcs_s, false);
-        if (which_step == 1) MakeRhoHFlux(sflux, sedge, umac, S.rhoh0_old, rhoh0_edge_old, S.rhoh0_old, rhoh0_edge_old);
-        else MakeRhoHFlux(sflux, sedge, umac, S.rhoh0_old, rhoh0_edge_old, S.rhoh0_new, rhoh0_edge_new);
+        if (ept == 2) ConvertRhoHToH(scalold, false);
+        std::vector<real> rho0_edge_old, rho0_edge_new;
+        Lev::CelltoEdge(S.rho0_old, rho0_edge_old);
+        Lev::CelltoEdge(S.rho0_new, rho0_edge_new);
+        if (which_step == 1)
+            MakeRhoHFlux(sflux, sedge, umac, S.rhoh0_old, rhoh0_edge_old, S.rhoh0_old, rhoh0_edge_old, S.rho0_old,
+                         rho0_edge_old, S.rho0_old, rho0_edge_old);
+        else
+            MakeRhoHFlux(sflux, sedge, umac, S.rhoh0_old, rhoh0_edge_old, S.rhoh0_new, rhoh0_edge_new, S.rho0_old,
+                         rho0_edge_old, S.rho0_new, rho0_edge_new);
         scal_force.setVal(0.0, RhoH, 1, 1);
         Addw0(umac, -1.0);
         MakeRhoHForce(scal_force, 0, umac, 0, which_step);

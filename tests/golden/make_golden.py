@@ -47,7 +47,7 @@ SLOPE_FIXTURES = [(so, d) for so in (2, 4) for d in range(3)]
 
 
 def main():
-    dom_n = (10, 8, 6)
+    dom_n = (10, 8, 8)
     out = {}
     for c, (ppm_type, is_umac, bc) in enumerate(PPM_FIXTURES):
         bx = (-1, -1, -1, dom_n[0], dom_n[1], dom_n[2])

@@ -80,3 +80,12 @@ def test_one_256_box():
     cfg = configs.workload_2d(n=256)
     gpu, ref = run_both(cfg)
     assert compare_2d(cfg, gpu, ref, "256 x 256")
+
+
+@pytest.mark.parametrize("spt", [1, 2])
+def test_2d_enthalpy_prediction_of_h(spt):
+    """enthalpy_pred_type 2: h = (rho h) / rho predicted, the flux rho h u."""
+    cfg = configs.planar_config_2d(n=(32, 48), nspec=3, ppm_type=1, max_grid=16, rho_pert=1e-3, w0_amp=1e4,
+                                   species_pred_type=spt, enthalpy_pred_type=2, seed=931 + spt)
+    gpu, ref = run_both(cfg)
+    assert compare_2d(cfg, gpu, ref, f"ept2 spt{spt}")

@@ -92,7 +92,7 @@ def test_stage_slopes(slope_order):
     compare(cfg, gpu, ref, f"slope{slope_order}")
 
 
-@pytest.mark.parametrize("spt,ept", [(2, 1), (3, 1), (1, 0), (2, 0)])
+@pytest.mark.parametrize("spt,ept", [(2, 1), (3, 1), (1, 0), (2, 0), (1, 2), (2, 2), (3, 2)])
 def test_stage_prediction_types(spt, ept):
     cfg = configs.planar_config(n=(16, 24, 16), nspec=3, ppm_type=1, max_grid=8, species_pred_type=spt,
                                 enthalpy_pred_type=ept, seed=400 + 10 * spt + ept)

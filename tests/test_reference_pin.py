@@ -118,7 +118,7 @@ def stage_cases():
         C[f"ppm0 slope_order {so}"] = lambda so=so: configs.planar_config(
             n=(16, 16, 24), nspec=2, ppm_type=0, slope_order=so, max_grid=8, bc_lo=(SLIPWALL, INTERIOR, SLIPWALL),
             bc_hi=(OUTFLOW, INTERIOR, OUTFLOW), seed=300 + so)
-    for spt, ept in [(2, 1), (3, 1), (1, 0), (2, 0)]:
+    for spt, ept in [(2, 1), (3, 1), (1, 0), (2, 0), (1, 2), (2, 2), (3, 2)]:
         C[f"species_pred_type {spt} enthalpy_pred_type {ept}"] = lambda spt=spt, ept=ept: configs.planar_config(
             n=(16, 24, 16), nspec=3, ppm_type=1, max_grid=8, species_pred_type=spt, enthalpy_pred_type=ept,
             seed=400 + 10 * spt + ept)
@@ -229,6 +229,10 @@ def stage_cases_2d():
                                                                      rho_pert=1e-3, w0_amp=1e4)
     C["2-D walls ppm2"] = lambda: configs.planar_config_2d(n=(40, 48), nspec=2, ppm_type=2, max_grid=16,
                                                            bc_lo=(SLIPWALL, NOSLIPWALL), bc_hi=(OUTFLOW, SYMMETRY))
+    for spt in (1, 2):
+        C[f"2-D enthalpy_pred_type 2, species_pred_type {spt}"] = lambda spt=spt: configs.planar_config_2d(
+            n=(32, 48), nspec=3, ppm_type=1, max_grid=16, rho_pert=1e-3, w0_amp=1e4, species_pred_type=spt,
+            enthalpy_pred_type=2)
     C["2-D 256^2 one box (the 2-D workload)"] = lambda: configs.workload_2d(n=256)
     return C
 
