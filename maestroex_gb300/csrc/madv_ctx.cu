@@ -255,8 +255,13 @@ static void field_specs(Ctx& c) {
         S(F_SR0 + d, 3, 1);
         S(F_SIMH0 + d, 3, 1);
     }
-    S(F_VELFORCE, 3, 1);
-    S(F_SCALFORCE, c.nscal, 1);
+    // the forces carry ng_s ghost cells when they are traced (Source/MaestroAdvance.cpp:150-155,
+    // Source/MaestroAdvection.cpp:62-67)
+    const int ngf = c.P.ppm_trace_forces ? c.ng_s : 1;
+    S(F_VELFORCE, 3, ngf);
+    S(F_SCALFORCE, c.nscal, ngf);
+    S(F_IPF, c.P.ppm_trace_forces ? 3 : 0, 1);
+    S(F_IMF, c.P.ppm_trace_forces ? 3 : 0, 1);
     S(F_ETA, 1, 0, c.ndim - 1);
     S(F_RHO0CART, 1, 1);
     S(F_RHOH0CART, 1, 1);
@@ -585,7 +590,7 @@ static void flux_sync_h(Hier& H, int c0, int nc) {
 static void density_advance(Hier& H, int which_step) {
     const int spt = H[0].P.species_pred_type;
     const int ns = H[0].nspec, nscal = H[0].nscal;
-    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, 1);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, c->F[F_SCALFORCE].spec.ng);
     put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
     addw0_h(H, F_UMAC0, -1.0);
     if (spt == 1) modify_scal_force_h(H, RHO, "rho0_edge_old", F_RHO0CART, 0);
@@ -610,7 +615,7 @@ static void density_advance(Hier& H, int which_step) {
     flux_sync_h(H, FIRSTSPEC, ns);
     // scal_force.setVal(0) before UpdateScal (Source/MaestroDensityAdvance.cpp:229-231): of
     // the components read from here on, only Rho has been written since the zeroing above
-    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHO, 1, 1);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHO, 1, c->F[F_SCALFORCE].spec.ng);
     update_scal_h(H, FIRSTSPEC);
 }
 
@@ -646,7 +651,7 @@ static void enthalpy_advance(Hier& H, int which_step) {
     // predict_h: (rho h) -> h (Source/MaestroEnthalpyAdvance.cpp:40-43)
     if (ept == 2) convert_rhoh_to_h_h(H, 1);
     // scal_force.setVal(0) (Source/MaestroEnthalpyAdvance.cpp:51); the enthalpy half reads RhoH only
-    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, c->F[F_SCALFORCE].spec.ng);
     addw0_h(H, F_UMAC0, -1.0);
     make_rhoh_force_h(H, 1, 1, 1);
     if (ept == 1) {
@@ -662,7 +667,7 @@ static void enthalpy_advance(Hier& H, int which_step) {
     if (ept == 2) convert_rhoh_to_h_h(H, 0);  // h -> (rho h) (:164-167)
     rhoh_flux_h(H, which_step);
     flux_sync_h(H, RHOH, 1);
-    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, 1);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, c->F[F_SCALFORCE].spec.ng);
     addw0_h(H, F_UMAC0, -1.0);
     make_rhoh_force_h(H, 0, 0, which_step);
     addw0_h(H, F_UMAC0, 1.0);
@@ -1222,8 +1227,10 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
         set_error("spherical geometry needs use_exact_base_state = 1, 3-D and enthalpy_pred_type 1");
         return MADV_ERR_UNSUPPORTED;
     }
-    if (p->ppm_trace_forces != 0 || (p->use_exact_base_state != 0 && !p->spherical)) {
-        set_error("ppm_trace_forces must be 0; use_exact_base_state needs spherical geometry");
+    if ((p->ppm_trace_forces != 0 && (p->ppm_trace_forces != 1 || p->ppm_type == 0 || p->dim == 2)) ||
+        (p->use_exact_base_state != 0 && !p->spherical)) {
+        set_error("ppm_trace_forces = 1 needs ppm_type 1 or 2 in 3-D (with ppm_type 0 the reference reads forces it "
+                  "never traced); use_exact_base_state needs spherical geometry");
         return MADV_ERR_UNSUPPORTED;
     }
     if (p->reflux_type < 0 || p->reflux_type > 2 || (p->reflux_type == 2 && p->dim == 2)) {
@@ -1785,7 +1792,7 @@ int madv_vel_pred(madv_ctx* h, const madv_multifab* utilde, const madv_multifab*
     try {
         const int nga = c.ng_adv;
         if ((rc = bind(c, U_UOLD, utilde, 3, -1, nga)) || (rc = bind(c, U_UFULL, ufull, 3, -1, nga)) ||
-            (rc = bind(c, U_FORCE, force, 3, -1, 1)))
+            (rc = bind(c, U_FORCE, force, 3, -1, c.F[F_VELFORCE].spec.ng)))
             return rc;
         for (int d = 0; d < 3; ++d)
             if ((rc = bind(c, U_UTRANS0 + d, &utrans[d], 1, d, 1)) || (rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 0)))
@@ -1793,7 +1800,7 @@ int madv_vel_pred(madv_ctx* h, const madv_multifab* utilde, const madv_multifab*
         if ((rc = upload_user_views(c))) return rc;
         copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, nga);
         copy_fab(c, F_UFULL, 0, F_USER + U_UFULL, 0, 3, nga);
-        copy_fab(c, F_VELFORCE, 0, F_USER + U_FORCE, 0, 3, 1);
+        copy_fab(c, F_VELFORCE, 0, F_USER + U_FORCE, 0, 3, c.F[F_VELFORCE].spec.ng);
         for (int d = 0; d < 3; ++d) {
             copy_fab(c, F_UTRANS0 + d, 0, F_USER + U_UTRANS0 + d, 0, 1, 1);
             set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
@@ -1826,7 +1833,7 @@ int madv_make_edge_scal(madv_ctx* h, const madv_multifab* state, const madv_mult
     }
     try {
         if ((rc = bind(c, U_SOLD, state, start_scomp + num_comp, -1, c.ng_s)) ||
-            (rc = bind(c, U_FORCE, force, start_scomp + num_comp, -1, 1)))
+            (rc = bind(c, U_FORCE, force, start_scomp + num_comp, -1, c.F[F_SCALFORCE].spec.ng)))
             return rc;
         for (int d = 0; d < 3; ++d)
             if ((rc = bind(c, U_UMAC0 + d, &umac[d], 1, d, 1)) ||
@@ -1834,7 +1841,7 @@ int madv_make_edge_scal(madv_ctx* h, const madv_multifab* state, const madv_mult
                 return rc;
         if ((rc = upload_user_views(c))) return rc;
         copy_fab(c, F_SOLD, start_scomp, F_USER + U_SOLD, start_scomp, num_comp, c.ng_s);
-        copy_fab(c, F_SCALFORCE, start_scomp, F_USER + U_FORCE, start_scomp, num_comp, 1);
+        copy_fab(c, F_SCALFORCE, start_scomp, F_USER + U_FORCE, start_scomp, num_comp, c.F[F_SCALFORCE].spec.ng);
         for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
         make_edge_scal(c, start_scomp, num_comp, BCS_S, is_conservative != 0, 0);
         for (int d = 0; d < 3; ++d)
@@ -1986,7 +1993,7 @@ int madv_velocity_advance(madv_ctx* h, const madv_multifab* uold, const madv_mul
         // MakeEdgeScal(uold, uedge, umac, vel_force, true, bcs_u, AMREX_SPACEDIM, 0, 0, AMREX_SPACEDIM, false)
         copy_fab(c, F_SOLD, 0, F_USER + U_UOLD, 0, 3, 0);
         fill_patch_h(H, F_SOLD, 0, 3, BCS_U, 0, 1, -1);
-        copy_fab(c, F_SCALFORCE, 0, F_VELFORCE, 0, 3, 1);
+        copy_fab(c, F_SCALFORCE, 0, F_VELFORCE, 0, 3, c.F[F_VELFORCE].spec.ng);
         for (int d = 0; d < 3; ++d) set_val(c, F_SEDGE0 + d, 0.0, 0, 3, 0);
         make_edge_scal(c, 0, 3, BCS_U, 0, 0, 1);
         addw0_h(H, F_UMAC0, -1.0);
@@ -2347,8 +2354,9 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         return MADV_ERR_PARAM;
     }
     if (c.ndim != 3 || (c.P.ppm_type != 1 && c.P.ppm_type != 2) || c.P.species_pred_type != 1 ||
-        c.P.enthalpy_pred_type != 1) {
-        set_error("the adjoint covers 3-D domains with ppm_type 1 or 2, species_pred_type 1 and enthalpy_pred_type 1");
+        c.P.enthalpy_pred_type != 1 || c.P.ppm_trace_forces) {
+        set_error("the adjoint covers 3-D domains with ppm_type 1 or 2, species_pred_type 1, enthalpy_pred_type 1 "
+                  "and untraced forces");
         return MADV_ERR_UNSUPPORTED;
     }
     // ppm_type 2: the state gradient away from walls (their boundary stencils are not transposed)

@@ -57,6 +57,7 @@ enum FieldId {
     F_S0CART2,                     // spherical: a base-state array on cells, two ghosts (MakeS0mac)
     F_S0MAC0, F_S0MAC1, F_S0MAC2,  // spherical: base state on faces (MakeS0mac), old
     F_S0MACB0, F_S0MACB1, F_S0MACB2,  //   and new
+    F_IPF, F_IMF,                  // ppm_trace_forces: the traced force, 3 directional comps
     F_USER,                        // first slot of per-call views of caller FABs
     NF_INTERNAL = F_USER
 };

@@ -650,7 +650,7 @@ __global__ void k_vel_force(KARGS, double cutoff_rho, int domhi, RecipC r2dz, in
 void make_vel_force(Ctx& c, int fe) {
     if (c.sph) return make_vel_force_sph(c, fe);
     if (c.ndim == 2) return make_vel_force_2d(c);
-    set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
+    set_val(c, F_VELFORCE, 0.0, 0, 3, c.F[F_VELFORCE].spec.ng);
     launch(c, rg_grow(c, 0), 1, k_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density,
            c.P.dom_hi[2], make_recip(2.0 * c.P.dx[2]), fe);
 }
@@ -775,7 +775,8 @@ __global__ void k_vp_transverse(KARGS, int bclo, int bchi, int domlo, int domhi,
 // VelPredVelocities (Source/MaestroVelPred.cpp:1597-1915).  F_TCOEF comps 3..5 hold
 // (dt4/h_t)*(trans_t sum).
 template <int D>
-__global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo, int domhi, double rel_eps, int sph) {
+__global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo, int domhi, double rel_eps, int sph,
+                                int ptf) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -785,9 +786,10 @@ __global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo
     const int il = i - di, jl = j - dj, kl = k - dk;
     const FabView tc = VW(F_TCOEF);
     const FabView q1 = VW(Q_FIELD(D, T1)), q2 = VW(Q_FIELD(D, T2));
+    // the traced force if ppm_trace_forces = 1 (Source/MaestroVelPred.cpp:1644-1647)
     const FabView f = VW(F_VELFORCE);
-    const double fl = at(f, il, jl, kl, D);
-    const double fr = at(f, i, j, k, D);
+    const double fl = ptf ? at(VW(F_IPF), il, jl, kl, D) : at(f, il, jl, kl, D);
+    const double fr = ptf ? at(VW(F_IMF), i, j, k, D) : at(f, i, j, k, D);
     const double ml = at(VW(F_SL0 + D), i, j, k, D) -
                       at(tc, il, jl, kl, 3 + T1) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
                       at(tc, il, jl, kl, 3 + T2) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
@@ -850,7 +852,7 @@ static void vp_interface_launch(Ctx& c) {
 template <int D>
 static void vp_velocities_launch(Ctx& c) {
     launch(c, rg_grow(c, 0, D), 1, k_vp_velocities<D>, c.V(), 0.5 * c.P.dt, c.P.phys_bc_lo[D], c.P.phys_bc_hi[D],
-           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps, (int)c.sph);
+           c.P.dom_lo[D], c.P.dom_hi[D], c.P.rel_eps, (int)c.sph, c.P.ppm_trace_forces);
 }
 
 void vel_pred(Ctx& c) {
@@ -864,6 +866,10 @@ void vel_pred(Ctx& c) {
         for (int cc = 0; cc < 3; ++cc)
             for (int d = 0; d < 3; ++d)
                 if (cc != d) ppm_any(c, d, F_UTILDE, cc, c.bcs_u[cc], F_UFULL, d, 0, F_IPC0 + cc, F_IMC0 + cc);
+        // ppm_trace_forces: force component d traced along d, the direction VelPredVelocities
+        // reads (Source/MaestroVelPred.cpp:117-137, 203-247)
+        if (c.P.ppm_trace_forces)
+            for (int d = 0; d < 3; ++d) ppm_any(c, d, F_VELFORCE, d, c.bcs_u[d], F_UFULL, d, 0, F_IPF, F_IMF);
     }
     vp_interface_launch<0>(c);
     vp_interface_launch<1>(c);
@@ -995,7 +1001,7 @@ __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bc
 // identically zero (species), so the + dt/2*force term is skipped.
 template <int D, bool CONS>
 __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double dt2h1, double dt2h2, double dt2hd,
-                           int bclo, int bchi, int domlo, int domhi, long long epsb, int vclamp) {
+                           int bclo, int bchi, int domlo, int domhi, long long epsb, int vclamp, int ptf) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -1008,9 +1014,10 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
     const FabView sc = VW(F_SOLD);
     double lq, rq;
     if (CONS) {
+        // the traced force if ppm_trace_forces = 1 (Source/MaestroMakeEdgeScalars.cpp:1405-1408)
         const FabView u1 = VW(F_UMAC0 + T1), u2 = VW(F_UMAC0 + T2), f = VW(F_SCALFORCE);
-        const double fl = at(f, il, jl, kl, comp);
-        const double fr = at(f, i, j, k, comp);
+        const double fl = ptf ? at(VW(F_IPF), il, jl, kl, D) : at(f, il, jl, kl, comp);
+        const double fr = ptf ? at(VW(F_IMF), i, j, k, D) : at(f, i, j, k, comp);
         lq = at(VW(F_SL0 + D), i, j, k) -
              dt2h1 * (at(q1, il + a1i, jl + a1j, kl + a1k) * at(u1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl) * at(u1, il, jl, kl)) -
              dt2h2 * (at(q2, il + a2i, jl + a2j, kl + a2k) * at(u2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl) * at(u2, il, jl, kl)) -
@@ -1029,8 +1036,8 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
              at(tc, i, j, k, 3 + T2) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k));
         if (!force_zero) {
             const FabView f = VW(F_SCALFORCE);
-            lq = lq + dt2 * at(f, il, jl, kl, comp);
-            rq = rq + dt2 * at(f, i, j, k, comp);
+            lq = lq + dt2 * (ptf ? at(VW(F_IPF), il, jl, kl, D) : at(f, il, jl, kl, comp));
+            rq = rq + dt2 * (ptf ? at(VW(F_IMF), i, j, k, D) : at(f, i, j, k, comp));
         }
     }
     double v = upwind(at(udf, i, j, k), lq, rq, epsb);
@@ -1080,14 +1087,15 @@ template <int D>
 static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp) {
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
     const double dt2 = 0.5 * c.P.dt;
+    const int ptf = c.P.ppm_trace_forces;
     if (is_cons)
         launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, true>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-               dbits_host(c.P.rel_eps), vclamp);
+               dbits_host(c.P.rel_eps), vclamp, ptf);
     else
         launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, false>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-               dbits_host(c.P.rel_eps), vclamp);
+               dbits_host(c.P.rel_eps), vclamp, ptf);
 }
 
 // force_zero: the components' force is identically zero (DensityAdvance species)
@@ -1105,6 +1113,10 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
             for (int d = 0; d < 3; ++d) slope_any(c, d, F_SOLD, comp, F_SLOPE, d, 1, bcs_dev(c, which_bcs), comp);
         } else {
             for (int d = 0; d < 3; ++d) ppm_any(c, d, F_SOLD, comp, bc, F_UMAC0 + d, 0, 1, F_IPC0, F_IMC0);
+            // ppm_trace_forces: the component's force traced like it (Source/MaestroMakeEdgeScalars.cpp:
+            // 137-141, 223-227); a force known to be zero traces to zero and is not read
+            if (c.P.ppm_trace_forces && !force_zero)
+                for (int d = 0; d < 3; ++d) ppm_any(c, d, F_SCALFORCE, comp, bc, F_UMAC0 + d, 0, 1, F_IPF, F_IMF);
         }
         const int v0 = is_vel && comp == 0, v1 = is_vel && comp == 1, v2 = is_vel && comp == 2;
         es_predictor_launch<0>(c, comp, bc, v0);

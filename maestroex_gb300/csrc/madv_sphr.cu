@@ -118,7 +118,7 @@ __global__ void k_vel_force_sph(KARGS, double cutoff_rho, SphGeo g, int fe) {
 }
 
 void make_vel_force_sph(Ctx& c, int fe) {
-    set_val(c, F_VELFORCE, 0.0, 0, 3, 1);
+    set_val(c, F_VELFORCE, 0.0, 0, 3, c.F[F_VELFORCE].spec.ng);
     launch(c, rg_grow(c, 0), 1, k_vel_force_sph, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density, c.geo,
            fe);
 }

@@ -53,7 +53,7 @@ def make_params(cfg):
     p.slope_order = cfg.get("slope_order", 4)
     p.species_pred_type = cfg.get("species_pred_type", 1)
     p.enthalpy_pred_type = cfg.get("enthalpy_pred_type", 1)
-    p.ppm_trace_forces = 0
+    p.ppm_trace_forces = cfg.get("ppm_trace_forces", 0)
     p.evolve_base_state = cfg.get("evolve_base_state", 1)
     p.use_exact_base_state = cfg.get("use_exact_base_state", 0)
     for d in range(3):

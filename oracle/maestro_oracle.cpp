@@ -441,6 +441,14 @@ struct Lev {
             for (int d = 0; d < 3; ++d)
                 if (c != d) qimh[c][d].define(L.ba, 1, 1);
         MF& velsrc = (P.ppm_type == 0) ? utilde : ufull;
+        // ppm_trace_forces: the force of each component traced like the component (Ipfx..Imfz)
+        const bool ptf = P.ppm_trace_forces == 1;
+        MF Ipf[3], Imf[3];
+        if (ptf)
+            for (int c = 0; c < 3; ++c) {
+                Ipf[c].define(L.ba, 3, 1);
+                Imf[c].define(L.ba, 3, 1);
+            }
 #pragma omp parallel for schedule(dynamic)
         for (int b = 0; b < nb; ++b) {
             const Box obx = grow(L.ba[b], 1);
@@ -452,9 +460,13 @@ struct Lev {
                 Slope_dir(P.slope_order, L.dom, obx, ut, Imc[1][b], 3, bcs_u, 0, 1);  // slopey -> Imv
                 Slope_dir(P.slope_order, L.dom, obx, ut, Imc[2][b], 3, bcs_u, 0, 2);  // slopez -> Imw
             } else {
-                for (int c = 0; c < 3; ++c)
+                for (int c = 0; c < 3; ++c) {
                     PPM(pc, obx, ut, velsrc[b].comp(0), velsrc[b].comp(1), velsrc[b].comp(2), Ipc[c][b], Imc[c][b],
                         bcs_u[c], false, c);
+                    if (ptf)  // (:117-137, 203-247)
+                        PPM(pc, obx, force[b], velsrc[b].comp(0), velsrc[b].comp(1), velsrc[b].comp(2), Ipf[c][b],
+                            Imf[c][b], bcs_u[c], false, c);
+                }
             }
             // VelPredInterface (:735-1128)
             for (int d = 0; d < 3; ++d) {
@@ -598,8 +610,9 @@ struct Lev {
                 MO_FOR3(xbx) {
                     const int I = d == 0 ? i : (d == 1 ? j : k);
                     const int il = i - di, jl = j - dj, kl = k - dk;
-                    real fl = f(il, jl, kl, d);
-                    real fr = f(i, j, k, d);
+                    // the traced force if ppm_trace_forces = 1 (:581-584, 656-659, 1644-1647)
+                    real fl = ptf ? Ipf[d][b](il, jl, kl, d) : f(il, jl, kl, d);
+                    real fr = ptf ? Imf[d][b](i, j, k, d) : f(i, j, k, d);
                     real ml = l(i, j, k, d) -
                                 (dt4 / h[t1]) * (tr1(il + a1i, jl + a1j, kl + a1k) + tr1(il, jl, kl)) *
                                     (q1(il + a1i, jl + a1j, kl + a1k) - q1(il, jl, kl)) -
@@ -663,9 +676,14 @@ struct Lev {
         const int* domlo = L.dom.lo;
         const int* domhi = L.dom.hi;
         const real h[3] = {L.dx[0], L.dx[1], L.dx[2]};
-        MF Ip, Im;
+        MF Ip, Im, Ipf, Imf;
         Ip.define(L.ba, 3, 1);
         Im.define(L.ba, 3, 1);
+        const bool ptf = P.ppm_trace_forces == 1;
+        if (ptf) {
+            Ipf.define(L.ba, 3, 1);
+            Imf.define(L.ba, 3, 1);
+        }
         MF sl[3], sr[3], simh[3];
         for (int d = 0; d < 3; ++d) {
             sl[d].define(L.ba, 1, 1, -1, 0.0);
@@ -697,6 +715,9 @@ struct Lev {
                     Slope_dir(P.slope_order, L.dom, obx, sc, slopez[b], 1, one, 0, 2);
                 } else {
                     PPM(pc, obx, state[b], umac[0][b], umac[1][b], umac[2][b], Ip[b], Im[b], bcs[bccomp], true, comp);
+                    if (ptf)  // the force traced like the component (:137-141, 223-227)
+                        PPM(pc, obx, force[b], umac[0][b], umac[1][b], umac[2][b], Ipf[b], Imf[b], bcs[bccomp], true,
+                            comp);
                 }
             }
             const int bc_lo[3] = {bcs[bccomp].lo[0], bcs[bccomp].lo[1], bcs[bccomp].lo[2]};
@@ -847,8 +868,9 @@ struct Lev {
                     MO_FOR3(xbx) {
                         const int I = d == 0 ? i : (d == 1 ? j : k);
                         const int il = i - di, jl = j - dj, kl = k - dk;
-                        real fl = f(il, jl, kl, comp);
-                        real fr = f(i, j, k, comp);
+                        // the traced force if ppm_trace_forces = 1 (:1405-1408, 1495-1498, 1585-1588)
+                        real fl = ptf ? Ipf[b](il, jl, kl, d) : f(il, jl, kl, comp);
+                        real fr = ptf ? Imf[b](i, j, k, d) : f(i, j, k, comp);
                         real lq, rq;
                         if (is_conservative) {
                             lq = l(i, j, k) -
@@ -1617,7 +1639,9 @@ struct Stage {
             for (int d = 0; d < 3; ++d) utrans[lev][d].define(L.ba, 1, 1, d, 0.0);
         }
         MakeUtrans(utilde, ufull, utrans);
-        for (int lev = 0; lev < nlev; ++lev) vel_force[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+        // the forces carry ng_s ghost cells when they are traced (Source/MaestroAdvection.cpp:62-67)
+        const int ngf = P.ppm_trace_forces ? ng_s : 1;
+        for (int lev = 0; lev < nlev; ++lev) vel_force[lev].define(S[lev].L.ba, 3, ngf, -1, 0.0);
         MakeVelForce(vel_force, utrans, sold, w0_force_cart);
         Addw0(utrans, 1.0);
         VelPred(utilde, ufull, utrans, umac, vel_force);
@@ -1851,7 +1875,7 @@ struct Stage {
                          VMF* sponge) {
         VMF vel_force(nlev);
         for (int lev = 0; lev < nlev; ++lev) {
-            vel_force[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+            vel_force[lev].define(S[lev].L.ba, 3, P.ppm_trace_forces ? ng_s : 1, -1, 0.0);
             for (int d = 0; d < 3; ++d) uedge[lev][d].define(S[lev].L.ba, 3, 0, d, 0.0);
         }
         MakeVelForce(vel_force, umac, sold, w0_force_cart);
@@ -1882,7 +1906,7 @@ struct Stage {
         VMF vel_force(nlev), w0f(nlev);
         VF umac0(nlev);
         for (int lev = 0; lev < nlev; ++lev) {
-            vel_force[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
+            vel_force[lev].define(S[lev].L.ba, 3, P.ppm_trace_forces ? ng_s : 1, -1, 0.0);
             w0f[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
             for (int d = 0; d < 3; ++d) umac0[lev][d].define(S[lev].L.ba, 1, 1, d, 0.0);
         }
@@ -1984,7 +2008,9 @@ static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, do
 static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxes, const int* boxes,
                         const mo_inputs* in) {
     if (nlev < 1 || nlev > 4) throw std::runtime_error("1 to 4 levels");
-    if (p->ppm_trace_forces != 0) throw std::runtime_error("ppm_trace_forces = 1 is not supported");
+    if (p->ppm_trace_forces != 0 && (p->ppm_type == 0 || p->ppm_trace_forces != 1))
+        throw std::runtime_error("ppm_trace_forces = 1 needs ppm_type 1 or 2 (the reference reads untraced forces "
+                                 "with ppm_type 0)");
     if (p->use_exact_base_state && !p->spherical) throw std::runtime_error("use_exact_base_state is spherical-only");
     if (p->spherical) {
         if (!p->use_exact_base_state) throw std::runtime_error("spherical needs use_exact_base_state = 1");
@@ -2115,7 +2141,7 @@ static int run_stage(const mo_params* p, int nlev, const int* nboxes, const int*
             sflux[lev][d].define(S.L.ba, nscal, 0, d, 0.0);
         }
         etarhoflux[lev].define(S.L.ba, 1, 0, 2, 0.0);
-        scal_force[lev].define(S.L.ba, nscal, 1, -1, 0.0);
+        scal_force[lev].define(S.L.ba, nscal, p->ppm_trace_forces ? H.ng_s : 1, -1, 0.0);
     }
 
     // sold ghost cells as the previous step's UpdateScal leaves them
@@ -2413,7 +2439,7 @@ static int member(const mo_params* p, int nboxes, const int* boxes, const mo_inp
         case MO_VEL_PRED: {  // Maestro::VelPred (Source/MaestroVelPred.cpp:5-292)
             mf_in(m1[0], ba, A(MO_UTILDE), 3, nga, -1);
             mf_in(m2[0], ba, A(MO_UFULL), 3, nga, -1);
-            mf_in(m3[0], ba, A(MO_FORCE), 3, 1, -1);
+            mf_in(m3[0], ba, A(MO_FORCE), 3, p->ppm_trace_forces ? ng_s : 1, -1);
             for (int d = 0; d < 3; ++d) {
                 mf_in(f1[0][d], ba, A(MO_UTRANS0 + d), 1, 1, d);
                 f2[0][d].define(ba, 1, 1, d, 0.0);
@@ -2426,7 +2452,7 @@ static int member(const mo_params* p, int nboxes, const int* boxes, const mo_inp
             if (start_comp < 0 || num_comp < 1 || start_comp + num_comp > nscal)
                 throw std::runtime_error("component range outside the state");
             mf_in(m1[0], ba, A(MO_STATE), nscal, ng_s, -1);
-            mf_in(m2[0], ba, A(MO_FORCE), nscal, 1, -1);
+            mf_in(m2[0], ba, A(MO_FORCE), nscal, p->ppm_trace_forces ? ng_s : 1, -1);
             for (int d = 0; d < 3; ++d) {
                 mf_in(f1[0][d], ba, A(MO_UMAC0 + d), 1, 1, d);
                 f2[0][d].define(ba, nscal, 0, d, 0.0);

@@ -352,7 +352,8 @@ int run_stage(const mo_params* p, int nboxes, const int* boxes, const mo_inputs*
     thermal[0].define(ba, dm, 1, 1);
     thermal[0].setVal(0.0);
     if (in->thermal) scatter(dom, in->thermal, thermal[0], 0, 1);
-    scal_force[0].define(ba, dm, Nscal, 1);
+    // the forces carry ng_s ghost cells when they are traced (Source/MaestroAdvance.cpp:150-155)
+    scal_force[0].define(ba, dm, Nscal, maestro::ppm_trace_forces ? ng : 1);
     scal_force[0].setVal(0.0);
     etarhoflux[0].define(faces(ba, AMREX_SPACEDIM - 1), dm, 1, 1);
     etarhoflux[0].setVal(0.0);

@@ -375,3 +375,32 @@ def test_set_option_rejects_unknown_keys():
 def make_stage_small():
     from maestroex_gb300.stage import make_stage
     return make_stage(configs.planar_config(n=(16, 16, 16), nspec=2, ppm_type=1, max_grid=16, seed=705))
+
+
+def traced(cfg):
+    cfg["ppm_trace_forces"] = 1
+    return cfg
+
+
+TRACED_CASES = {
+    "planar ppm1": lambda: traced(configs.planar_config(n=(32, 32, 32), nspec=3, ppm_type=1, max_grid=16, seed=801,
+                                                        gpi_amp=1e-3, rho_pert=1e-3)),
+    "planar ppm2 walls": lambda: traced(configs.planar_config(n=(24, 16, 24), nspec=2, ppm_type=2,
+                                                              max_grid=(8, 16, 12), bc_lo=(SYMMETRY, SLIPWALL, SLIPWALL),
+                                                              bc_hi=(OUTFLOW, NOSLIPWALL, OUTFLOW), seed=802, cfl=0.5,
+                                                              gpi_amp=1e-3)),
+    "spherical ppm2": lambda: traced(configs.spherical_config(n=32, max_grid=16, ppm_type=2)),
+    "species 2, h predicted": lambda: traced(configs.planar_config(n=(16, 24, 16), nspec=3, ppm_type=1, max_grid=8,
+                                                                   species_pred_type=2, enthalpy_pred_type=2,
+                                                                   seed=803)),
+}
+
+
+@pytest.mark.parametrize("name", list(TRACED_CASES))
+def test_traced_forces_match_oracle(name):
+    """ppm_trace_forces = 1: the velocity and scalar forces traced by PPM (Ipf / Imf) in
+    VelPred and MakeEdgeScal, with ng_s ghost cells on the forces."""
+    cfg = TRACED_CASES[name]()
+    gpu, ref = run_both(cfg, mode=capi.MODE_GRAPH)
+    worst, bitwise = compare(cfg, gpu, ref, f"traced forces, {name}")
+    assert bitwise, worst

@@ -130,6 +130,18 @@ def stage_cases():
     C["NumSpec 13, 32^3 boxes, w0"] = lambda: configs.planar_config(n=(64, 64, 64), nspec=13, ppm_type=1,
                                                                     max_grid=32, seed=7, w0_amp=1e4)
 
+    def traced(cfg):
+        cfg["ppm_trace_forces"] = 1
+        return cfg
+
+    for ppm in (1, 2):
+        C[f"traced forces ppm{ppm}"] = lambda ppm=ppm: traced(configs.planar_config(
+            n=(32, 32, 32), nspec=3, ppm_type=ppm, max_grid=16, seed=101 + ppm, gpi_amp=1e-3, rho_pert=1e-3))
+    C["traced forces, walls"] = lambda: traced(configs.planar_config(
+        n=(24, 16, 24), nspec=2, ppm_type=2, max_grid=(8, 16, 12), bc_lo=(SYMMETRY, SLIPWALL, SLIPWALL),
+        bc_hi=(OUTFLOW, NOSLIPWALL, OUTFLOW), seed=200, cfl=0.5, gpi_amp=1e-3))
+    C["traced forces, spherical"] = lambda: traced(configs.spherical_config(n=32, max_grid=16, ppm_type=2))
+
     def negative_species():
         from test_bench_shapes_gpu import headline_shape, plant_negative_species
         cfg = headline_shape(13, n=(64, 64, 64), seed=20261203 + 21)
@@ -196,6 +208,8 @@ def velocity_cases():
                                                              bc_hi=(OUTFLOW, OUTFLOW, OUTFLOW)),
         "planar ppm0": lambda: configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=0),
         "spherical ppm2": lambda: configs.spherical_config(n=32, max_grid=16, ppm_type=2),
+        "planar ppm2 traced forces": lambda: dict(configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=2,
+                                                                        gpi_amp=1e-3), ppm_trace_forces=1),
     }
 
 

@@ -74,3 +74,13 @@ def test_velocity_advance_matches_oracle(name, with_sponge):
     gpu = run_gpu(cfg, rhohalf, sponge)
     ref = pyoracle.run_velocity_advance(cfg, rhohalf, sponge)
     assert compare(gpu, ref, name), f"{name}: within 1e-12 but not bitwise"
+
+
+def test_velocity_advance_with_traced_forces_matches_oracle():
+    cfg = configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=2, gpi_amp=1e-3)
+    cfg["ppm_trace_forces"] = 1
+    rng = np.random.default_rng(19)
+    rhohalf = cfg["sold"][RHO] * (1.0 + 1e-4 * rng.standard_normal(cfg["sold"][RHO].shape))
+    gpu = run_gpu(cfg, rhohalf)
+    ref = pyoracle.run_velocity_advance(cfg, rhohalf)
+    assert compare(gpu, ref, "traced forces"), "within 1e-12 but not bitwise"
