@@ -1016,8 +1016,9 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
     if (CONS) {
         // the traced force if ppm_trace_forces = 1 (Source/MaestroMakeEdgeScalars.cpp:1405-1408)
         const FabView u1 = VW(F_UMAC0 + T1), u2 = VW(F_UMAC0 + T2), f = VW(F_SCALFORCE);
-        const double fl = ptf ? at(VW(F_IPF), il, jl, kl, D) : at(f, il, jl, kl, comp);
-        const double fr = ptf ? at(VW(F_IMF), i, j, k, D) : at(f, i, j, k, comp);
+        // force_zero: the force is zero (and so is its trace, which is not formed)
+        const double fl = force_zero ? 0.0 : ptf ? at(VW(F_IPF), il, jl, kl, D) : at(f, il, jl, kl, comp);
+        const double fr = force_zero ? 0.0 : ptf ? at(VW(F_IMF), i, j, k, D) : at(f, i, j, k, comp);
         lq = at(VW(F_SL0 + D), i, j, k) -
              dt2h1 * (at(q1, il + a1i, jl + a1j, kl + a1k) * at(u1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl) * at(u1, il, jl, kl)) -
              dt2h2 * (at(q2, il + a2i, jl + a2j, kl + a2k) * at(u2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl) * at(u2, il, jl, kl)) -
