@@ -1965,10 +1965,6 @@ int madv_velocity_advance(madv_ctx* h, const madv_multifab* uold, const madv_mul
     if (rc) return rc;
     Ctx& c = h->c;
     if (!uold || !sold || !rhohalf || !gpi || !umac || !unew) return MADV_ERR_PARAM;
-    if (c.P.ppm_trace_forces) {
-        set_error("VelocityAdvance: ppm_trace_forces = 1 is not supported");
-        return MADV_ERR_UNSUPPORTED;
-    }
     try {
         if ((rc = bind(c, U_UOLD, uold, 3, -1, 0)) || (rc = bind(c, U_SOLD, sold, 1, -1, 0)) ||
             (rc = bind(c, U_RHOHALF, rhohalf, 1, -1, 0)) || (rc = bind(c, U_GPI, gpi, 3, -1, 0)) ||
