@@ -808,6 +808,8 @@ def run_2d(args, barrier):
     from maestroex_gb300.stage import StageBuffers, make_stage
     cfg = configs.workload_2d(n=256)
     st = make_stage(cfg)
+    if args.staged_ppm >= 0:
+        st.set_option("staged_ppm", args.staged_ppm)
     buf = StageBuffers(cfg).load(cfg)
     snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
 
@@ -887,6 +889,8 @@ def main():
     ap.add_argument("--sph-adj-n", type=int, default=128, help="extent of the spherical adjoint workload")
     ap.add_argument("--profile-once", action="store_true",
                     help="run one batched stage and exit (the command ncu captures)")
+    ap.add_argument("--staged-ppm", type=int, default=-1, choices=[-1, 0, 1],
+                    help="PPM form of the headline stage: 1 staged sweeps, 0 three launches, -1 the library default")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     warmup = max(args.warmup, 3)
@@ -930,6 +934,8 @@ def main():
                                 seed=20261203 + 1, w0_amp=1.0e4, cfl=0.7)
     ncell = args.n ** 3
     st = make_stage(cfg)
+    if args.staged_ppm >= 0:
+        st.set_option("staged_ppm", args.staged_ppm)
     buf = StageBuffers(cfg).load(cfg)
     snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
 

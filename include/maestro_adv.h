@@ -376,9 +376,11 @@ int madv_autotune_apply(madv_ctx* ctx, const char* json);
 
 /* Implementation options of a context (no counterpart in the reference; results never
  * depend on them):
- *   "staged_ppm"      1 (default): each PPM direction runs as one kernel over tiles of whole
- *                     pencils staged in shared memory by bulk copies; 0: three launches
- *                     (slopes, interface values, cell limiter) through global memory.
+ *   "staged_ppm"      1: each PPM direction runs as one kernel over tiles of whole pencils
+ *                     staged in shared memory by bulk copies; 0 (default): three launches
+ *                     (slopes, interface values, cell limiter) through global memory, which
+ *                     measure faster on GB300 (the stage is FP64-issue bound, and the fused
+ *                     kernel's registers and shared memory cut its occupancy).
  *   "sweep_tile_Da", "sweep_tile_Db" (D = 0, 1, 2): cells of a staged tile across
  *                     direction D, in the first / second transverse direction (x before y
  *                     before z); defaults 4 x 2 for D = 0 and 32 x 2 for D = 1, 2.

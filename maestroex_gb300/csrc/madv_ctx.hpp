@@ -161,9 +161,9 @@ struct Ctx {
     // component's PPM and transverse scratch (F_FACE*, F_Q*, F_SIMH*) at its own storage
     // there, to keep them for the reverse sweep
     std::function<void(int)> edge_tape_begin, edge_tape;
-    // PPM sweeps: the staged (fused) form (madv_sweep.cu) unless turned off; tile shape
+    // PPM sweeps: the staged (fused) form (madv_sweep.cu) when turned on; tile shape
     // across each direction D (cells in the two transverse directions), default when absent
-    bool staged_ppm = true;
+    bool staged_ppm = false;
     std::map<int, std::array<int, 2>> sweep_shape;
     // scratch of the single-box entry points (madv_ppm), grown on demand
     double* box_scratch = nullptr;

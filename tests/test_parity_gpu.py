@@ -201,11 +201,13 @@ def test_rejects_bad_layout_and_params():
     with pytest.raises(capi.MadvError) as e:
         st.set_layout([(0, 0, 0, 7, 7, 7)])  # does not cover the domain
     assert e.value.code == -2
-    p = make_params(cfg)
-    p.ppm_trace_forces = 1
-    with pytest.raises(capi.MadvError) as e:
-        ScalarAdvectionStage(p)
-    assert e.value.code == -3
+    # traced forces need PPM (with ppm_type 0 the reference reads traces it never formed)
+    for ppm_type, ptf in ((0, 1), (1, 2)):
+        p = make_params(cfg)
+        p.ppm_type, p.ppm_trace_forces = ppm_type, ptf
+        with pytest.raises(capi.MadvError) as e:
+            ScalarAdvectionStage(p)
+        assert e.value.code == -3
 
 
 @pytest.mark.parametrize("y,thr", [(6.0, 0.0), (3.0, 1e-3), (390625.0, 6.45e-3), (1e8 / 256 * 2, 12.5),
