@@ -368,8 +368,11 @@ def run_amr(args, ws, steps, warmup, barrier):
         "graph": {"value": ws * ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": launches_graph,
                   "autotuned": True},
         "graph_untuned": {"value": ws * ncell / (ms_graph_untuned * 1e-3), "ms_per_step": ms_graph_untuned},
-        "autotuner_choices_per_level": [{str(t): sum(1 for k, v in tuned.items() if k.startswith(f"L{lev} ") and v == t)
-                                         for t in sorted(set(tuned.values()))} for lev in range(2)],
+        "autotuner_choices_per_level": [{str(t): sum(1 for k, v in tuned.items()
+                                                     if k.startswith(f"L{lev} ") and not k.endswith("ppm_form") and v == t)
+                                         for t in sorted({v for k, v in tuned.items() if not k.endswith("ppm_form")})}
+                                        for lev in range(2)],
+        "autotuner_ppm_form_per_level": [tuned.get(f"L{lev} ppm_form") for lev in range(2)],
         "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
         "per_box": {"value": ws * ncell / (ms_perbox * 1e-3), "ms_per_step": ms_perbox,
                     "gpu_launches": launches_perbox},
@@ -1108,8 +1111,11 @@ def main():
         "batched_no_graph": {"value": ws * ncell / (ms_batched * 1e-3), "ms_per_step": ms_batched},
         "autotuner": {"untuned_graph": {"value": ws * ncell / (ms_graph_untuned * 1e-3),
                                         "ms_per_step": ms_graph_untuned},
-                      "threads_per_block_chosen": {str(t): sum(1 for v in tuned.values() if v == t)
-                                                   for t in sorted(set(tuned.values()))},
+                      "threads_per_block_chosen": {str(t): sum(1 for k, v in tuned.items()
+                                                               if not k.endswith("ppm_form") and v == t)
+                                                   for t in sorted({v for k, v in tuned.items()
+                                                                    if not k.endswith("ppm_form")})},
+                      "ppm_form_chosen": tuned.get("L0 ppm_form"),
                       "speedup": ms_graph_untuned / ms_graph},
         "fp64_peak_tflops_probe": tf.value,
         "kernels_top": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / ktot, 4)}

@@ -307,8 +307,10 @@ int madv_ppm(madv_ctx* ctx, const madv_box* bx, const madv_fab* s, int comp, con
  * device array of MADV_PPM_NOALLOC_MAX_DOUBLES doubles (9.04 MiB) that every GPU loading
  * the library holds until exit; a box needing more (larger than 66 x 66 x 66 cells) is
  * rejected with MADV_ERR_LAYOUT.  The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress) and must come before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race, so keep them on one stream. */
+ * device address (cudaGetSymbolAddress) and must come before any stream capture; the
+ * address is cached for the process, so do not call this entry point on a device after
+ * cudaDeviceReset.  All calls share the array: calls that overlap on the GPU race, so keep
+ * them on one stream. */
 #define MADV_PPM_NOALLOC_MAX_DOUBLES 1184832
 int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_fab* s, int comp,
                      const madv_fab* u, const madv_fab* v, const madv_fab* w, int is_umac,
@@ -371,6 +373,14 @@ int madv_profile_report(madv_ctx* ctx, char* buf, int len);
  * madv_autotune_apply in a later run).  Kernels are clamped to the block size they can take.
  * No counterpart in the reference. */
 int madv_autotune_trial(madv_ctx* ctx, int threads);
+/* The PPM form, tuned the same way per level: for each form f in [0, MADV_AUTOTUNE_PPM_FORMS):
+ * madv_autotune_ppm_trial(ctx, f); run the stage.  Form 0 is the three-launch PPM (slopes,
+ * interfaces, cell limiter); forms 1-4 the staged sweep kernel with tile shapes (across x;
+ * across y and z) 4x2; 32x2, 8x2; 32x1, 2x2; 16x2 and 4x4; 16x4.  finish keeps the form
+ * whose PPM kernels took the least time on each level ("L<level> ppm_form" in the table).
+ * Results do not depend on the form. */
+#define MADV_AUTOTUNE_PPM_FORMS 5
+int madv_autotune_ppm_trial(madv_ctx* ctx, int form);
 int madv_autotune_finish(madv_ctx* ctx, char* json, int len);
 int madv_autotune_apply(madv_ctx* ctx, const char* json);
 

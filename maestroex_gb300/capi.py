@@ -27,7 +27,7 @@ EXPORTED = [
     "madv_last_error", "madv_version", "madv_profile", "madv_profile_report", "madv_probe_fp64_peak",
     "madv_selftest_exact", "madv_ppm", "madv_ppm_noalloc", "madv_set_layout_levels",
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
-    "madv_autotune_trial", "madv_autotune_finish", "madv_autotune_apply",
+    "madv_autotune_trial", "madv_autotune_ppm_trial", "madv_autotune_finish", "madv_autotune_apply",
     "madv_make_utrans", "madv_vel_pred", "madv_make_edge_scal", "madv_make_rhox_flux", "madv_make_rhoh_flux",
     "madv_update_scal", "madv_velocity_advance", "madv_est_dt", "madv_mac_project", "madv_set_option",
 ]
@@ -120,6 +120,7 @@ def lib():
                                                 C.c_void_p]
         L.madv_stage_adjoint.argtypes = [C.c_void_p, P(MadvAdjSeed), P(MadvAdjResult), C.c_void_p]
         L.madv_autotune_trial.argtypes = [C.c_void_p, C.c_int]
+        L.madv_autotune_ppm_trial.argtypes = [C.c_void_p, C.c_int]
         L.madv_autotune_finish.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
         L.madv_autotune_apply.argtypes = [C.c_void_p, C.c_char_p]
         FAB = P(MadvFab)

@@ -2008,10 +2008,6 @@ int madv_velocity_advance(madv_ctx* h, const madv_multifab* uold, const madv_mul
     }
 }
 
-// Maestro::EstDt (Source/MaestroDt.cpp:11-225 planar, :301-384 spherical, :440-483): the
-// advective and force constraints and rel_eps on every level.  The per-level maxima are exact
-// (k_dt_maxima), and the reference's per-box minima of monotone functions of per-box maxima
-// equal the same functions of the level maxima, so dt and umax match it bit for bit.
 // Maestro::MacProj, plane-parallel, one level (Source/MaestroMacProj.cpp:11-236): the
 // caller's umac is copied in with its ghost faces, projected, refilled and copied back
 int madv_mac_project(madv_ctx* h, const madv_multifab* umac, const madv_multifab* macphi, const madv_multifab* macrhs,
@@ -2057,6 +2053,10 @@ int madv_mac_project(madv_ctx* h, const madv_multifab* umac, const madv_multifab
     }
 }
 
+// Maestro::EstDt (Source/MaestroDt.cpp:11-225 planar, :301-384 spherical, :440-483): the
+// advective and force constraints and rel_eps on every level.  The per-level maxima are exact
+// (k_dt_maxima), and the reference's per-box minima of monotone functions of per-box maxima
+// equal the same functions of the level maxima, so dt and umax match it bit for bit.
 int madv_est_dt(madv_ctx* h, int nlev, const madv_multifab* uold, const madv_multifab* sold,
                 const madv_multifab* gpi, const madv_dt_params* prm, madv_dt_result* res, void* stream) {
     if (!h || !uold || !sold || !gpi || !prm || !res) return MADV_ERR_PARAM;
@@ -2177,15 +2177,48 @@ int madv_ppm(madv_ctx* h, const madv_box* bx, const madv_fab* s, int comp, const
 }
 
 // ------------------------------------------------------------------ launch-shape autotuner
-// fold the timed launches of the current trial into the per-kernel totals
+// The PPM forms the autotuner tries per level: three launches (slopes, interfaces, cell
+// limiter), or the staged sweep kernel with a tile shape across x (D = 0) and across y / z.
+struct PpmForm {
+    int staged;
+    int x_a, x_b, yz_a, yz_b;
+};
+static const PpmForm PPM_FORMS[] = {{0, 0, 0, 0, 0}, {1, 4, 2, 32, 2}, {1, 8, 2, 32, 1}, {1, 2, 2, 16, 2}, {1, 4, 4, 16, 4}};
+constexpr int N_PPM_FORMS = (int)(sizeof(PPM_FORMS) / sizeof(PPM_FORMS[0]));
+
+static void set_ppm_form(Ctx& c, int k) {
+    const PpmForm& f = PPM_FORMS[k];
+    c.staged_ppm = f.staged != 0;
+    c.sweep_shape.clear();
+    if (f.staged) {
+        c.sweep_shape[0] = {f.x_a, f.x_b};
+        c.sweep_shape[1] = {f.yz_a, f.yz_b};
+        c.sweep_shape[2] = {f.yz_a, f.yz_b};
+    }
+}
+
+static bool is_ppm_kernel(Ctx& c, const void* fn) {
+    auto it = c.is_ppm_fn.find(fn);
+    if (it != c.is_ppm_fn.end()) return it->second;
+    const char* nm = nullptr;
+    bool yes = false;
+    if (cudaFuncGetName(&nm, fn) == cudaSuccess && nm)
+        yes = std::strstr(nm, "k_dsvl") || std::strstr(nm, "k_ppm_face") || std::strstr(nm, "k_ppm_cell") ||
+              std::strstr(nm, "k_ppm_sweep");
+    return c.is_ppm_fn[fn] = yes;
+}
+
+// fold the timed launches of the current trial into the per-kernel totals (block-size
+// trials) or the PPM kernels' total (PPM form trials)
 static int tune_collect(Hier& H) {
     if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) return MADV_ERR_CUDA;
     for (auto* c : H.L) {
-        if (c->tpb_trial)
+        if (c->tpb_trial || c->ppm_trial >= 0)
             for (auto& r : c->prof) {
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, r.e0, r.e1);
-                c->tune_ms[r.fn][c->tpb_trial] += ms;
+                if (c->tpb_trial) c->tune_ms[r.fn][c->tpb_trial] += ms;
+                else if (is_ppm_kernel(*c, r.fn)) c->ppm_tune_ms[c->ppm_trial] += ms;
             }
         c->prof.clear();
         c->ev_next = 0;
@@ -2203,6 +2236,25 @@ int madv_autotune_trial(madv_ctx* h, int threads) {
     if (rc) return rc;
     for (auto* c : H.L) {
         c->tpb_trial = threads;
+        c->ppm_trial = -1;
+        c->profiling = true;
+    }
+    drop_graph(h);
+    return MADV_OK;
+}
+
+int madv_autotune_ppm_trial(madv_ctx* h, int form) {
+    if (!h || form < 0 || form >= N_PPM_FORMS) {
+        set_error("madv_autotune_ppm_trial: form must be in [0, MADV_AUTOTUNE_PPM_FORMS)");
+        return MADV_ERR_PARAM;
+    }
+    Hier H = h->H();
+    int rc = tune_collect(H);
+    if (rc) return rc;
+    for (auto* c : H.L) {
+        c->tpb_trial = 0;
+        c->ppm_trial = form;
+        set_ppm_form(*c, form);
         c->profiling = true;
     }
     drop_graph(h);
@@ -2235,8 +2287,25 @@ int madv_autotune_finish(madv_ctx* h, char* json, int len) {
             js += (first ? "\"L" : ", \"L") + std::to_string(c->lev) + " " + nm + "\": " + std::to_string(best);
             first = false;
         }
+        if (!c->ppm_tune_ms.empty()) {  // the fastest PPM form of this level's box sizes
+            int best = 0;
+            double bms = 1e300;
+            for (auto& kv : c->ppm_tune_ms)
+                if (kv.second < bms) {
+                    bms = kv.second;
+                    best = kv.first;
+                }
+            c->ppm_form = best;
+            set_ppm_form(*c, best);
+            js += (first ? "\"L" : ", \"L") + std::to_string(c->lev) + " ppm_form\": " + std::to_string(best);
+            first = false;
+        } else if (c->ppm_trial >= 0) {
+            set_ppm_form(*c, c->ppm_form >= 0 ? c->ppm_form : 0);
+        }
         c->tune_ms.clear();
+        c->ppm_tune_ms.clear();
         c->tpb_trial = 0;
+        c->ppm_trial = -1;
         c->profiling = false;
     }
     js += "}";
@@ -2263,6 +2332,11 @@ int madv_autotune_apply(madv_ctx* h, const char* json) {
         c->tpb_by_name = tab;
         c->tpb_choice.clear();
         c->tpb_max.clear();
+        auto it = tab.find("L" + std::to_string(c->lev) + " ppm_form");
+        if (it != tab.end() && it->second >= 0 && it->second < N_PPM_FORMS) {
+            c->ppm_form = it->second;
+            set_ppm_form(*c, it->second);
+        }
     }
     drop_graph(h);
     return MADV_OK;

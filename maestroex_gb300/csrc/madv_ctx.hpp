@@ -148,6 +148,13 @@ struct Ctx {
     std::map<const void*, int> tpb_max;
     std::map<const void*, std::map<int, double>> tune_ms;
     int tpb_trial = 0;
+    // PPM form trials of the autotuner (madv_autotune_ppm_trial): the candidate being timed
+    // (-1: none), the PPM kernels' device time per candidate, and the per-kernel cache of
+    // "is a PPM kernel" (k_dsvl, k_ppm_face, k_ppm_cell, k_ppm_sweep)
+    int ppm_trial = -1;
+    std::map<int, double> ppm_tune_ms;
+    std::map<const void*, bool> is_ppm_fn;
+    int ppm_form = -1;  // the candidate chosen or loaded (-1: the context's own options)
     int tpb_of(const void* fn);
     int* d_flag = nullptr;  // device error flag (EOS cutoff)
     unsigned long long* d_red = nullptr;  // EstDt maxima (allocated on first use)

@@ -175,8 +175,11 @@ __global__ void k_mg_prolong(MGGrid cg, MGGrid f) {
     f.phi[c] += cg.phi[mg_cell(cg, i / 2, j / 2, k / 2)];
 }
 
-// out[0] = max |x| (bit pattern of a non-negative double), out[1] += sum x
-__global__ void k_mg_norms(const double* __restrict__ x, long n, unsigned long long* out_max, double* out_sum) {
+// out_max = max |x| (bit pattern of a non-negative double); part[block] = the block's sum of
+// x.  Every partial sum is formed in a fixed order (grid-stride per thread, a shuffle tree
+// per warp, warps in order per block), so the sum does not depend on scheduling.
+__global__ void k_mg_norms(const double* __restrict__ x, long n, unsigned long long* out_max, double* part) {
+    __shared__ double ws[32];
     double m = 0.0, s = 0.0;
     for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
         m = fmax(m, fabs(x[c]));
@@ -188,8 +191,21 @@ __global__ void k_mg_norms(const double* __restrict__ x, long n, unsigned long l
     }
     if ((threadIdx.x & 31) == 0) {
         atomicMax(out_max, (unsigned long long)__double_as_longlong(m));
-        atomicAdd(out_sum, s);
+        ws[threadIdx.x >> 5] = s;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += ws[w];
+        part[blockIdx.x] = b;
+    }
+}
+
+// sum of the block partials, in block order (one thread)
+__global__ void k_mg_sum_parts(const double* __restrict__ part, int nb, double* out_sum) {
+    double s = 0.0;
+    for (int q = 0; q < nb; ++q) s += part[q];
+    out_sum[0] = s;
 }
 
 __global__ void k_mg_shift(double* __restrict__ x, long n, const double* __restrict__ sum, double inv_n) {
@@ -282,6 +298,7 @@ struct MacMG {
     int n0[3] = {0, 0, 0};
     unsigned long long* d_max = nullptr;
     double* d_sum = nullptr;
+    double* d_part = nullptr;  // per-block partial sums of k_mg_norms
     double* d_beta = nullptr;  // beta0 [nr], beta0_edge [nr + 1]
 };
 
@@ -290,16 +307,21 @@ void mac_free(Ctx& c) {
     for (double* p : c.mac->mem) cudaFree(p);
     if (c.mac->d_max) cudaFree(c.mac->d_max);
     if (c.mac->d_sum) cudaFree(c.mac->d_sum);
+    if (c.mac->d_part) cudaFree(c.mac->d_part);
     if (c.mac->d_beta) cudaFree(c.mac->d_beta);
     delete c.mac;
     c.mac = nullptr;
 }
 
+// blocks of the norm / sum kernel: a fixed grid for every array size, so the order of the
+// partial sums is fixed too
+constexpr long NORM_BLOCKS = 152L * 8;
+
 static dim3 blocks_of(long n) { return dim3((unsigned)((n + TPB - 1) / TPB)); }
 
 static long ncell(const MGGrid& g) { return (long)g.n[0] * g.n[1] * g.n[2]; }
 
-// Builds (once per domain) grids coarsened by 2 while every extent stays even and >= 2.
+// Builds (once per domain) grids coarsened by 2 in every direction (rule below).
 static int mac_hierarchy(Ctx& c, const int n0[3], int nr) {
     if (c.mac && c.mac->n0[0] == n0[0] && c.mac->n0[1] == n0[1] && c.mac->n0[2] == n0[2]) return MADV_OK;
     mac_free(c);
@@ -331,8 +353,14 @@ static int mac_hierarchy(Ctx& c, const int n0[3], int nr) {
             return MADV_ERR_CUDA;
         }
         M.lev.push_back(g);
+        // coarsen while every extent halves to >= 2 cells.  A periodic extent must halve to an
+        // even one, so that the red-black colouring stays consistent across the wrap, and so
+        // must x, whose rows the smoother splits into two colours of n[0] / 2 cells
         bool more = true;
-        for (int d = 0; d < 3; ++d) more = more && n[d] % 4 == 0;
+        for (int d = 0; d < 3; ++d) {
+            const bool even_needed = d == 0 || c.P.phys_bc_lo[d] == MADV_INTERIOR;
+            more = more && n[d] % 2 == 0 && n[d] / 2 >= 2 && (!even_needed || (n[d] / 2) % 2 == 0);
+        }
         if (!more) break;
         for (int d = 0; d < 3; ++d) {
             n[d] /= 2;
@@ -341,6 +369,7 @@ static int mac_hierarchy(Ctx& c, const int n0[3], int nr) {
     }
     if (cudaMalloc(&M.d_max, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&M.d_sum, sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&M.d_part, sizeof(double) * NORM_BLOCKS) != cudaSuccess ||
         cudaMalloc(&M.d_beta, sizeof(double) * (2 * nr + 1)) != cudaSuccess) {
         set_error("cudaMalloc(MAC multigrid)");
         mac_free(c);
@@ -387,10 +416,10 @@ static void mg_vcycle(Ctx& c, const MGBC& bc, int l) {
 static int mg_norms(Ctx& c, const double* x, long n, double& amax, double* sum_out, bool device_sum_only = false) {
     MacMG& M = *c.mac;
     MP_CK(cudaMemsetAsync(M.d_max, 0, sizeof(unsigned long long), c.stream));
-    MP_CK(cudaMemsetAsync(M.d_sum, 0, sizeof(double), c.stream));
-    const unsigned nb = (unsigned)std::min<long>((n + TPB - 1) / TPB, 152L * 8);
-    k_mg_norms<<<nb, TPB, 0, c.stream>>>(x, n, M.d_max, M.d_sum);
-    c.launches++;
+    const unsigned nb = (unsigned)std::min<long>((n + TPB - 1) / TPB, NORM_BLOCKS);
+    k_mg_norms<<<nb, TPB, 0, c.stream>>>(x, n, M.d_max, M.d_part);
+    k_mg_sum_parts<<<1, 1, 0, c.stream>>>(M.d_part, (int)nb, M.d_sum);
+    c.launches += 2;
     if (device_sum_only) return MADV_OK;
     unsigned long long bits = 0;
     double s = 0.0;

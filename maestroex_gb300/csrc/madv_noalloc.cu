@@ -15,7 +15,10 @@
 //
 // Host code cannot use the array's name as a device address.  The first call on each
 // device, with that device current, looks the address up with cudaGetSymbolAddress and
-// caches it; make that first call on a device before any stream capture.
+// caches it; make that first call on a device before any stream capture.  The cached
+// address belongs to the device's primary context: a process that resets a device
+// (cudaDeviceReset) or otherwise destroys its primary context must not call this entry
+// point on that device afterwards, because the cache would still hold the old address.
 //
 // Nothing in the array has to start at zero: every element a call reads was written
 // earlier in the same call.  All calls share the array and it keeps the last call's

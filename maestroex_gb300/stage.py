@@ -292,13 +292,18 @@ class ScalarAdvectionStage:
         """madv_set_option: an implementation option (staged PPM sweeps, their tile shape)."""
         check(lib().madv_set_option(self.ctx, key.encode(), int(value)))
 
-    def autotune(self, run_batched, candidates=(32, 64, 128, 256, 512)):
+    def autotune(self, run_batched, candidates=(32, 64, 128, 256, 512), ppm_forms=range(5)):
         """Launch-shape autotuner (madv_autotune_*): run_batched() runs the caller's stage once
         in MODE_BATCHED; it is timed per kernel for every candidate block size, and the fastest
-        per (level, kernel) is applied.  Returns the chosen table (dict)."""
+        per (level, kernel) is applied; then per level the fastest PPM form (three launches or
+        the staged sweep with one of its tile shapes) among ppm_forms.  Returns the chosen
+        table (dict)."""
         import json
         for t in candidates:
             check(lib().madv_autotune_trial(self.ctx, int(t)))
+            run_batched()
+        for f in ppm_forms:
+            check(lib().madv_autotune_ppm_trial(self.ctx, int(f)))
             run_batched()
         buf = C.create_string_buffer(1 << 20)
         check(lib().madv_autotune_finish(self.ctx, buf, len(buf)))

@@ -117,3 +117,48 @@ def test_mac_projection_rejects_spherical_and_odd_domains():
     with pytest.raises(capi.MadvError) as e:
         st.mac_project(um, cell, cell, np.ones(31))
     assert e.value.code == -3
+
+
+@pytest.mark.parametrize("case", ["walls_z", "periodic_xy_outflow_z"])
+def test_mac_projection_on_extents_that_are_not_powers_of_two(case):
+    """40 x 40 x 60 cells: the multigrid coarsens to 10 x 10 x 15 (x and the periodic y stay
+    even, z goes odd) and still converges in a few V-cycles."""
+    bc = CASES[case]
+    cfg, umac, rho, beta0, macrhs = inputs(bc, n=(40, 40, 60), max_grid=20)
+    gpu, gphi, it, ratio = run_gpu(cfg, umac, rho, beta0, macrhs)
+    ref, rphi = mo_macproj.mac_project(umac, macrhs, rho, beta0, cfg["dx"], bc[0], bc[1])
+    umax = max(float(np.abs(r).max()) for r in ref)
+    err = max(float(np.abs(g - r).max()) for g, r in zip(gpu, ref)) / umax
+    assert ratio <= 1e-12 and 1 <= it <= 40, (it, ratio)
+    assert err <= 1e-8
+
+
+def test_mac_projection_removes_an_analytic_gradient():
+    """A closed form, independent of the oracle's restatement: with constant rho and beta0 on
+    a periodic box, u* = grad psi (face differences of psi = cos(2 pi x / Lx) + sin(4 pi y /
+    Ly) cos(2 pi z / Lz)) is removed entirely, and phi = (rho / beta0) psi up to a constant."""
+    bc = CASES["all_periodic"]
+    cfg, umac, rho, beta0, macrhs = inputs(bc, n=(32, 24, 16), max_grid=16)
+    nx, ny, nz = cfg["n"]
+    dx = cfg["dx"]
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    z = (np.arange(nz) + 0.5) / nz
+    psi = (np.cos(2 * np.pi * x)[None, None, :] + np.sin(4 * np.pi * y)[None, :, None] *
+           np.cos(2 * np.pi * z)[:, None, None])
+    psi = psi * float(np.abs(cfg["uold"]).max()) * dx[0]
+
+    def grad(p, d):  # face differences, periodic: face 0 and face n carry the same value
+        ax = 2 - d
+        g = (p - np.roll(p, 1, axis=ax)) / dx[d]
+        return np.concatenate([g, np.take(g, [0], axis=ax)], axis=ax)
+
+    ustar = [grad(psi, d) for d in range(3)]
+    rho_c, beta_c = 2.5e7, 3.0e7
+    rho = np.full((nz, ny, nx), rho_c)
+    beta0 = np.full(nz, beta_c)
+    gpu, gphi, it, ratio = run_gpu(cfg, ustar, rho, beta0, np.zeros((nz, ny, nx)))
+    umax = max(float(np.abs(u).max()) for u in ustar)
+    assert max(float(np.abs(u).max()) for u in gpu) <= 1e-8 * umax
+    want = rho_c / beta_c * psi
+    assert float(np.abs((gphi - gphi.mean()) - (want - want.mean())).max()) <= 1e-8 * float(np.abs(want).max())

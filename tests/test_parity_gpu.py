@@ -220,8 +220,9 @@ def test_exact_helpers_match_ieee(y, thr):
 
 
 def test_autotuner_keeps_results_and_round_trips():
-    """Block sizes change nothing but speed: the stage after autotuning (graph mode) and a
-    second context given the saved table reproduce the untuned result bit for bit."""
+    """Block sizes and the PPM form change nothing but speed: the stage after autotuning
+    (graph mode) and a second context given the saved table reproduce the untuned result
+    bit for bit."""
     from maestroex_gb300.stage import StageBuffers, make_stage
     cfg = configs.planar_config(n=(32, 32, 32), max_grid=16, seed=20261203 + 9)
 
@@ -234,7 +235,8 @@ def test_autotuner_keeps_results_and_round_trips():
     st = make_stage(cfg)
     ref = run(st, capi.MODE_BATCHED)
     table = st.autotune(lambda: run(st, capi.MODE_BATCHED), candidates=(64, 512, 128))
-    assert table and all(v in (64, 128, 512) for v in table.values())
+    assert table and all(v in (64, 128, 512) for k, v in table.items() if not k.endswith("ppm_form"))
+    assert table["L0 ppm_form"] in range(5)  # the PPM form chosen for the level
     assert np.array_equal(run(st, capi.MODE_GRAPH), ref, equal_nan=True)
     st2 = make_stage(cfg)
     st2.autotune_apply(table)
