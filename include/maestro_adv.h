@@ -70,6 +70,16 @@ typedef struct {
     double prob_hi[3];
     int reflux_type;            /* coarse-fine flux synchronisation: 1 (or 0) AverageDownFaces
                                    of the fluxes, 2 FluxRegister reflux of the coarse state */
+    int drdxfac;                /* spherical, inexact base state: radial bins per cell width
+                                   (0 means 1) */
+    int w0_interp_type;         /* spherical Put1dArrayOnCart of edge-centred w0: 1 constant,
+                                   2 linear (default, 0 means 2), 3 quadratic */
+    int w0mac_interp_type;      /* spherical MakeW0mac: 1 (default, 0 means 1) face average of
+                                   w0_cart, 2 linear, 3 quadratic at the faces, 4 nodes then faces */
+    int s0_interp_type;         /* spherical, inexact base state, Put1dArrayOnCart of cell-centred
+                                   arrays: 1 constant, 2 linear, 3 quadratic (default, 0 means 3) */
+    int s0mac_interp_type;      /* spherical MakeS0mac: 1 (default, 0 means 1) cell values averaged
+                                   to faces; inexact base state also 2 linear, 3 quadratic */
 } madv_params;
 
 typedef struct {

@@ -243,8 +243,28 @@ def lane_emden(n_poly=1.5, h=1.0e-4):
     return np.array(xi), np.maximum(np.array(th), 0.0)
 
 
+def _sph_bins_to_cells(s0, radius, drf, t):
+    """Cell values of a bin-centred radial array on uniform bins of drf, as the reference's
+    Put1dArrayOnCart forms them (s0_interp_type t: 1 constant, 2 linear, 3 quadratic clipped
+    to its three points' range); used to lay the initial state on the base state."""
+    nr = len(s0)
+    rcc = (np.arange(nr) + 0.5) * drf
+    index = (radius / drf).astype(np.int64)
+    if t == 1:
+        return s0[np.minimum(index, nr - 1)]
+    if t == 2:
+        return np.interp(radius, rcc, s0)
+    i = np.clip(index, 1, nr - 2)
+    x0, x1, x2 = rcc[i - 1], rcc[i], rcc[i + 1]
+    y0, y1, y2 = s0[i - 1], s0[i], s0[i + 1]
+    y = (y0 + (y1 - y0) / (x1 - x0) * (radius - x0) +
+         ((y2 - y1) / (x2 - x1) - (y1 - y0) / (x1 - x0)) / (x2 - x0) * (radius - x0) * (radius - x1))
+    return np.clip(y, np.minimum(y0, np.minimum(y1, y2)), np.maximum(y0, np.maximum(y1, y2)))
+
+
 def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20261203 + 5, cfl=0.5,
-                     rho_c=2.0e9, w0_amp=1.0e5, u_amp=1.0e6, L=5.0e8, pert=1.0e-9, n_base=None):
+                     rho_c=2.0e9, w0_amp=1.0e5, u_amp=1.0e6, L=5.0e8, pert=1.0e-9, n_base=None, exact=True,
+                     drdxfac=1, **interp):
     """Full-star spherical configuration with the exact base state: an n^3 Cartesian domain
     [0, L]^3 with the star at its centre, outflow on every face; an n = 1.5 polytrope of
     central density rho_c and radius 0.9 L/2 (Lane-Emden, integrated here) on the irregular
@@ -254,16 +274,26 @@ def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20
     zero at 0.8 of the radius; density and enthalpy perturbed by `pert` (relative);
     base_cutoff_density half the ambient density, so the buoyancy cutoff (5x) covers the
     ambient.  n_base: extent of the finest level of a hierarchy, whose cell size sets the
-    radial grid (default n)."""
+    radial grid (default n).  exact=False: the uniform radial bins of the reference's default
+    (use_exact_base_state = 0), dr = dx_fine / drdxfac, nr = int(max_dist / dr) + 1 with
+    max_dist the centre-to-corner distance; interp: w0_interp_type, w0mac_interp_type,
+    s0_interp_type, s0mac_interp_type (the reference's defaults when absent)."""
     rng = np.random.default_rng(seed)
     n3 = (n, n, n)
     dx = L / n
     nb = n if n_base is None else n_base
     dxb = L / nb
-    nr_irreg = int((3.0 * (nb / 2 - 0.5) * (nb / 2 - 0.5) - 0.75) / 2.0)
-    nr = nr_irreg + 1
-    r_cc = np.sqrt(0.75 + 2.0 * np.arange(nr)) * dxb
-    r_edge = np.concatenate([[0.0], np.sqrt(0.75 + 2.0 * (np.arange(nr) + 0.5)) * dxb])
+    if exact:
+        nr_irreg = int((3.0 * (nb / 2 - 0.5) * (nb / 2 - 0.5) - 0.75) / 2.0)
+        nr = nr_irreg + 1
+        r_cc = np.sqrt(0.75 + 2.0 * np.arange(nr)) * dxb
+        r_edge = np.concatenate([[0.0], np.sqrt(0.75 + 2.0 * (np.arange(nr) + 0.5)) * dxb])
+    else:
+        drf = dxb / drdxfac
+        half = 0.5 * L
+        nr = int(math.sqrt(3.0 * half * half) / drf) + 1
+        r_cc = (np.arange(nr) + 0.5) * drf
+        r_edge = np.arange(nr + 1) * drf
     npoly, gamma = 1.5, 5.0 / 3.0
     xi, theta = lane_emden(npoly)
     R = 0.9 * 0.5 * L
@@ -286,20 +316,32 @@ def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20
     w0 *= w0_amp / max(np.abs(w0).max(), 1e-300)
     w0[0] = 0.0
 
-    # cell -> radial index, as Maestro::InitBaseStateMapSphr (round half away from zero)
+    # cell -> radial index, as Maestro::InitBaseStateMapSphr (round half away from zero), or
+    # the uniform bin of the cell centre
     c = (np.arange(n) + 0.5) * dx - 0.5 * L
     X3, Y3, Z3 = c[None, None, :], c[None, :, None], c[:, None, None]
     r2 = X3 * X3 + Y3 * Y3 + Z3 * Z3
-    idx = np.floor(r2 / (2.0 * dxb * dxb) - 0.375 + 0.5).astype(np.int64)
+    if exact:
+        idx = np.floor(r2 / (2.0 * dxb * dxb) - 0.375 + 0.5).astype(np.int64)
+
+        def on_cells(a):
+            return a[idx]
+    else:
+        # the cells hold the base state as Put1dArrayOnCart interpolates it there, so that
+        # the buoyancy starts at the seeded perturbation
+        t = interp.get("s0_interp_type", 3)
+
+        def on_cells(a):
+            return _sph_bins_to_cells(a, np.sqrt(r2), dxb / drdxfac, t)
     shape = (n, n, n)
     periodic = [False, False, False]
-    rho = rho0[idx] * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
+    rho = on_cells(rho0) * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
     X = np.zeros((nspec,) + shape)
     for sp in range(nspec):
         X[sp] = 1.0 + 0.5 * _smooth_field(rng, n3, (L / n,) * 3, periodic)
     X = np.maximum(X, 0.05)
     X /= X.sum(axis=0, keepdims=True)
-    h = (rhoh0 / rho0)[idx] * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
+    h = on_cells(rhoh0) / on_cells(rho0) * (1.0 + pert * _smooth_field(rng, n3, (L / n,) * 3, periodic))
     nscal = 4 + nspec
     sold = np.zeros((nscal,) + shape)
     sold[RHO] = rho
@@ -314,15 +356,17 @@ def spherical_config(n=64, nspec=3, ppm_type=1, max_grid=32, boxes=None, seed=20
     umax = max(float(np.abs(u).max()), 1.0) + w0_amp
     # Maestro::EstDt: the advective limit and the force limit sqrt(2 dx / |f|) with the
     # buoyancy (rho - rho0) g / rho of the seeded perturbation (Source/MaestroDt.cpp:150-225)
-    fmax = float(np.abs(grav).max()) * float(np.abs(rho / rho0[idx] - 1.0).max())
+    fmax = float(np.abs(grav).max()) * float(np.abs(rho / on_cells(rho0) - 1.0).max())
     dt = cfl * min(dx / umax, math.sqrt(2.0 * dx / max(fmax, 1e-300)))
     if boxes is None:
         boxes = tile_boxes(n3, max_grid)
     from .basestate import cell_to_edge
+    extra = dict(drdxfac=drdxfac, **interp)
     return dict(
         n=n3, dx=(dx, dx, dx), nspec=nspec, ppm_type=ppm_type, slope_order=4, bc_lo=(OUTFLOW,) * 3,
         bc_hi=(OUTFLOW,) * 3, species_pred_type=1, enthalpy_pred_type=1, evolve_base_state=1,
-        use_exact_base_state=1, spherical=1, prob_lo=(0.0, 0.0, 0.0), prob_hi=(L, L, L), nr=nr,
+        use_exact_base_state=1 if exact else 0, spherical=1, prob_lo=(0.0, 0.0, 0.0), prob_hi=(L, L, L), nr=nr,
+        **extra,
         dt=dt, rel_eps=1.0e-8 * umax, base_cutoff_density=0.5 * rho_floor, buoyancy_cutoff_factor=5.0,
         boxes=boxes, seed=seed, uold=np.ascontiguousarray(u), sold=np.ascontiguousarray(sold),
         gpi=np.zeros((3,) + shape), thermal=np.zeros((1,) + shape),

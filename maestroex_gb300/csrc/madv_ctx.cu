@@ -1223,6 +1223,12 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
                   "and need the equation of state)");
         return MADV_ERR_UNSUPPORTED;
     }
+    if (p->spherical && ((p->w0_interp_type != 0 && p->w0_interp_type != 2) ||
+                         (p->w0mac_interp_type != 0 && p->w0mac_interp_type != 1) ||
+                         (p->s0mac_interp_type != 0 && p->s0mac_interp_type != 1))) {
+        set_error("spherical: w0_interp_type 2, w0mac_interp_type 1 and s0mac_interp_type 1 are built");
+        return MADV_ERR_UNSUPPORTED;
+    }
     if (p->spherical && (p->use_exact_base_state != 1 || p->dim == 2 || p->enthalpy_pred_type != 1)) {
         set_error("spherical geometry needs use_exact_base_state = 1, 3-D and enthalpy_pred_type 1");
         return MADV_ERR_UNSUPPORTED;

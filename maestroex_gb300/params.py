@@ -42,6 +42,11 @@ class MadvParams(C.Structure):
         ("prob_lo", C.c_double * 3),
         ("prob_hi", C.c_double * 3),
         ("reflux_type", C.c_int),
+        ("drdxfac", C.c_int),
+        ("w0_interp_type", C.c_int),
+        ("w0mac_interp_type", C.c_int),
+        ("s0_interp_type", C.c_int),
+        ("s0mac_interp_type", C.c_int),
     ]
 
 
@@ -77,4 +82,11 @@ def make_params(cfg):
     if p.spherical:
         p.base_cutoff_density_coord = cfg["nr"]
     p.reflux_type = cfg.get("reflux_type", 1)
+    # spherical radial interpolation (Source/param/_cpp_parameters: drdxfac :116,
+    # s0_interp_type :527, w0_interp_type :533, s0mac_interp_type :539, w0mac_interp_type :546)
+    p.drdxfac = cfg.get("drdxfac", 1)
+    p.w0_interp_type = cfg.get("w0_interp_type", 2)
+    p.w0mac_interp_type = cfg.get("w0mac_interp_type", 1)
+    p.s0_interp_type = cfg.get("s0_interp_type", 3)
+    p.s0mac_interp_type = cfg.get("s0mac_interp_type", 1)
     return p

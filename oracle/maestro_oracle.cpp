@@ -3,9 +3,9 @@
 // AdvancePremac -> DensityAdvance -> EnthalpyAdvance call chain so that the GPU library
 // can be checked against it; it is never linked into or called by the product.
 //
-// Parity status: unpinned (see maestro_oracle.h).
+// Parity status: pinned (see maestro_oracle.h).
 //
-// Build: -O2 -ffp-contract=off (no FMA contraction), no fast-math, so every expression is
+// Build: -O3 -ffp-contract=off (no FMA contraction), no fast-math, so every expression is
 // evaluated in the reference's operation order with IEEE binary64 rounding.
 #include "maestro_oracle.h"
 
@@ -42,22 +42,92 @@ struct Lev {
     double dt = 0, rel_eps = 0;
 
     // ------------------------------------------------------------------ spherical
-    // Full-star geometry with the exact base state: centre, radii of the irregular radial
-    // grid (Source/BaseStateGeometry.cpp:86-96) and w0 on faces (MakeW0mac).
+    // Full-star geometry: centre, the radii of the radial grid (Source/BaseStateGeometry.cpp:
+    // 86-104) -- the exact (irregular) grid, or uniform bins of drf = dxf / drdxfac -- and w0 on
+    // faces (MakeW0mac).
     double center[3] = {0.0, 0.0, 0.0};
     double dxf = 0.0;  // finest cell size: it sets the radial grid of every level
+    double drf = 0.0;  // base_geom.dr_fine = dxf / drdxfac (Source/MaestroSetup.cpp:68)
     std::vector<double> r_cc_loc, r_edge_loc;
     MF w0mac[3];
 
     void InitSphr() {
         for (int d = 0; d < 3; ++d) center[d] = 0.5 * (P.prob_lo[d] + P.prob_hi[d]);
+        drf = dxf / (P.drdxfac > 0 ? P.drdxfac : 1);
         // one radius past the last cell: Put1dArrayOnCart reads r_cc_loc(nr_fine) for the
         // outermost cells (Source/MaestroFill3dData.cpp:115-118, past its array); the
         // same formula continued
         r_cc_loc.assign(nr + 1, 0.0);
-        for (int i = 0; i <= nr; ++i) r_cc_loc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
         r_edge_loc.assign(nr + 1, 0.0);
-        for (int i = 0; i < nr; ++i) r_edge_loc[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
+        if (P.use_exact_base_state) {
+            for (int i = 0; i <= nr; ++i) r_cc_loc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
+            for (int i = 0; i < nr; ++i) r_edge_loc[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
+        } else {
+            for (int i = 0; i <= nr; ++i) r_cc_loc[i] = (double(i) + 0.5) * drf;
+            for (int i = 0; i <= nr; ++i) r_edge_loc[i] = double(i) * drf;
+        }
+    }
+    // Put1dArrayOnCart's value of a cell-centred array at cell (i, j, k)
+    real sph_cell_at(const std::vector<real>& s0, int i, int j, int k) const {
+        if (P.use_exact_base_state) return s0[cc_to_r(i, j, k)];
+        double x, y, z;
+        sph_xyz(i, j, k, x, y, z);
+        return sph_cell_value(s0, std::sqrt(x * x + y * y + z * z), s0_interp());
+    }
+    int w0_interp() const { return P.w0_interp_type ? P.w0_interp_type : 2; }
+    int w0mac_interp() const { return P.w0mac_interp_type ? P.w0mac_interp_type : 1; }
+    int s0_interp() const { return P.s0_interp_type ? P.s0_interp_type : 3; }
+    // QuadInterp with its limiter on, the default of its declaration (Source/Maestro.H:65-68,
+    // Source/MaestroFill3dData.cpp:338-355): the quadratic through three points, clipped to
+    // the range of their values
+    static real QuadInterp(real x, real x0, real x1, real x2, real y0, real y1, real y2) {
+        real y = y0 + (y1 - y0) / (x1 - x0) * (x - x0) +
+                 ((y2 - y1) / (x2 - x1) - (y1 - y0) / (x1 - x0)) / (x2 - x0) * (x - x0) * (x - x1);
+        const real m12 = y1 > y2 ? y1 : y2, mx = y0 > m12 ? y0 : m12;
+        const real n12 = y1 < y2 ? y1 : y2, mn = y0 < n12 ? y0 : n12;
+        if (y > mx) y = mx;
+        if (y < mn) y = mn;
+        return y;
+    }
+    // Put1dArrayOnCart's value of an edge-centred array at radius `radius`: index is the
+    // cell's bin (cc_to_r with the exact grid, int(radius / drf) with uniform bins) and rfac
+    // its fraction (Source/MaestroFill3dData.cpp:111-159, 207-256)
+    real sph_edge_value(const std::vector<real>& s0, double radius, int index) const {
+        double rfac;
+        if (P.use_exact_base_state) {
+            if (index < nr) rfac = (radius - r_edge_loc[index + 1]) / (r_cc_loc[index + 1] - r_cc_loc[index]);
+            else rfac = (radius - r_edge_loc[index + 1]) / (r_cc_loc[index] - r_cc_loc[index - 1]);
+        } else {
+            rfac = (radius - double(index) * drf) / drf;
+        }
+        const int t = w0_interp();
+        if (t == 1) return rfac > 0.5 ? s0[index + 1] : s0[index];
+        if (t == 2) return index < nr ? rfac * s0[index + 1] + (1.0 - rfac) * s0[index] : s0[nr];
+        if (index <= 0) index = 0;
+        else if (index >= nr - 1) index = nr - 2;
+        else if (radius - r_edge_loc[index] < r_edge_loc[index + 1]) index--;
+        return QuadInterp(radius, r_edge_loc[index], r_edge_loc[index + 1], r_edge_loc[index + 2], s0[index],
+                          s0[index + 1], s0[index + 2]);
+    }
+    // Put1dArrayOnCart's value of a cell-centred array, uniform bins, s0_interp_type
+    // (Source/MaestroFill3dData.cpp:259-320); an index past the last bin takes the last value
+    // whichever way the reference's comparison (which reads past its radii there) goes
+    real sph_cell_value(const std::vector<real>& s0, double radius, int t) const {
+        int index = int(radius / drf);
+        if (t == 1) return s0[index];
+        if (t == 2) {
+            if (index > nr - 1) return s0[nr - 1];
+            if (radius >= r_cc_loc[index]) {
+                if (index >= nr - 1) return s0[nr - 1];
+                return s0[index + 1] * (radius - r_cc_loc[index]) / drf + s0[index] * (r_cc_loc[index + 1] - radius) / drf;
+            }
+            if (index == 0) return s0[index];
+            return s0[index] * (radius - r_cc_loc[index - 1]) / drf + s0[index - 1] * (r_cc_loc[index] - radius) / drf;
+        }
+        if (index == 0) index = 1;
+        else if (index >= nr - 1) index = nr - 2;
+        return QuadInterp(radius, r_cc_loc[index - 1], r_cc_loc[index], r_cc_loc[index + 1], s0[index - 1], s0[index],
+                          s0[index + 1]);
     }
     // cell centre relative to the star's centre (Source/MaestroFill3dData.cpp:103-110)
     void sph_xyz(int i, int j, int k, double& x, double& y, double& z) const {
@@ -72,8 +142,9 @@ struct Lev {
         const double index = (x * x + y * y + z * z) / (2.0 * dxf * dxf) - 0.375;
         return (int)std::round(index);
     }
-    // Put1dArrayOnCart, spherical, exact base state (Source/MaestroFill3dData.cpp:94-192):
-    // edge-centred input with w0_interp_type 2 (linear), cell-centred input injected
+    // Put1dArrayOnCart, spherical (Source/MaestroFill3dData.cpp:94-336): an edge-centred
+    // input with w0_interp_type, a cell-centred one injected (exact grid) or interpolated
+    // with s0_interp_type (uniform bins); vector output = value times the radial unit vector
     void Put1dSphr(const std::vector<real>& s0, MF& s0_cart, bool edge, bool vec) {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = s0_cart[b];
@@ -81,20 +152,10 @@ struct Lev {
                 double x, y, z;
                 sph_xyz(i, j, k, x, y, z);
                 const double radius = std::sqrt(x * x + y * y + z * z);
-                const int index = cc_to_r(i, j, k);
+                const int index = P.use_exact_base_state ? cc_to_r(i, j, k) : int(radius / drf);
                 real v;
-                if (edge) {
-                    double rfac;
-                    if (index < nr) {
-                        rfac = (radius - r_edge_loc[index + 1]) / (r_cc_loc[index + 1] - r_cc_loc[index]);
-                    } else {
-                        rfac = (radius - r_edge_loc[index + 1]) / (r_cc_loc[index] - r_cc_loc[index - 1]);
-                    }
-                    if (index < nr) v = rfac * s0[index + 1] + (1.0 - rfac) * s0[index];
-                    else v = s0[nr];
-                } else {
-                    v = s0[index];
-                }
+                if (edge) v = sph_edge_value(s0, radius, index);
+                else v = P.use_exact_base_state ? s0[index] : sph_cell_value(s0, radius, s0_interp());
                 if (vec) {
                     a(i, j, k, 0) = v * x / radius;
                     a(i, j, k, 1) = v * y / radius;
@@ -105,16 +166,80 @@ struct Lev {
             }
         }
     }
-    // Maestro::MakeW0mac, w0mac_interp_type 1 (Source/MaestroFill3dData.cpp:464-569): the
-    // face average of w0_cart over the nodal boxes grown by one
+    // w0 interpolated linearly in uniform bins of drf at radius `radius` (MakeW0mac types 2, 4)
+    real w0_linear(double radius) const {
+        const int index = int(radius / drf);
+        const double rfac = (radius - double(index) * drf) / drf;
+        return index < nr ? rfac * w0[index + 1] + (1.0 - rfac) * w0[index] : w0[nr];
+    }
+    // Maestro::MakeW0mac (Source/MaestroFill3dData.cpp:464-710) over the nodal boxes grown by
+    // one: w0mac_interp_type 1 averages w0_cart to the faces; 2 / 3 interpolate w0 at the
+    // face centres (linear in uniform bins / quadratic in r_edge_loc); 4 interpolates it at
+    // the nodes (grown by one) and averages their four values on each face
     void MakeW0mac() {
+        const int t = w0mac_interp();
+        MF w0_nodal;
+        if (t == 4) {
+            // node (i,j,k) kept at cell (i,j,k): two ghost cells hold the nodes of the box grown by one
+            w0_nodal.define(L.ba, 3, 2, -1, 0.0);
+            for (int b = 0; b < nb; ++b) {
+                Box nb1 = grow(L.ba[b], 1);
+                for (int d = 0; d < 3; ++d) nb1.hi[d] += 1;
+                const Arr& o = w0_nodal[b];
+                MO_FOR3(nb1) {
+                    const double x = P.prob_lo[0] + double(i) * L.dx[0] - center[0];
+                    const double y = P.prob_lo[1] + double(j) * L.dx[1] - center[1];
+                    const double z = P.prob_lo[2] + double(k) * L.dx[2] - center[2];
+                    const double radius = std::sqrt(x * x + y * y + z * z);
+                    const real v = w0_linear(radius);
+                    if (radius == 0.0) {
+                        for (int n = 0; n < 3; ++n) o(i, j, k, n) = v;
+                    } else {
+                        o(i, j, k, 0) = v * x / radius;
+                        o(i, j, k, 1) = v * y / radius;
+                        o(i, j, k, 2) = v * z / radius;
+                    }
+                }
+            }
+        }
         for (int d = 0; d < 3; ++d) {
             w0mac[d].define(L.ba, 1, 1, d, 0.0);
             const int di = d == 0, dj = d == 1, dk = d == 2;
             for (int b = 0; b < nb; ++b) {
                 const Arr& wc = w0_cart[b];
                 const Arr& o = w0mac[d][b];
-                MO_FOR3(grow(nodal(L.ba[b], d), 1)) { o(i, j, k) = 0.5 * (wc(i - di, j - dj, k - dk, d) + wc(i, j, k, d)); }
+                MO_FOR3(grow(nodal(L.ba[b], d), 1)) {
+                    if (t == 1) {
+                        o(i, j, k) = 0.5 * (wc(i - di, j - dj, k - dk, d) + wc(i, j, k, d));
+                    } else if (t == 2 || t == 3) {
+                        const double x = P.prob_lo[0] + (double(i) + (di ? 0.0 : 0.5)) * L.dx[0] - center[0];
+                        const double y = P.prob_lo[1] + (double(j) + (dj ? 0.0 : 0.5)) * L.dx[1] - center[1];
+                        const double z = P.prob_lo[2] + (double(k) + (dk ? 0.0 : 0.5)) * L.dx[2] - center[2];
+                        const double radius = std::sqrt(x * x + y * y + z * z);
+                        real v;
+                        if (t == 2) {
+                            v = w0_linear(radius);
+                        } else {
+                            int index = int(radius / drf);
+                            if (index <= 0) index = 0;
+                            else if (index >= nr - 1) index = nr - 2;
+                            else if (radius - r_edge_loc[index] < r_edge_loc[index + 1]) index--;
+                            v = QuadInterp(radius, r_edge_loc[index], r_edge_loc[index + 1], r_edge_loc[index + 2],
+                                           w0[index], w0[index + 1], w0[index + 2]);
+                        }
+                        o(i, j, k) = v * (d == 0 ? x : d == 1 ? y : z) / radius;
+                    } else {
+                        const Arr& wn = w0_nodal[b];
+                        // the four nodes of the face: the two transverse directions, low / high
+                        const int T1 = d == 0 ? 1 : 0, T2 = d == 2 ? 1 : 2;
+                        int a1[3] = {0, 0, 0}, a2[3] = {0, 0, 0};
+                        a1[T1] = 1;
+                        a2[T2] = 1;
+                        o(i, j, k) = 0.25 * (wn(i, j, k, d) + wn(i + a1[0], j + a1[1], k + a1[2], d) +
+                                             wn(i + a2[0], j + a2[1], k + a2[2], d) +
+                                             wn(i + a1[0] + a2[0], j + a1[1] + a2[1], k + a1[2] + a2[2], d));
+                    }
+                }
             }
         }
     }
@@ -358,12 +483,12 @@ struct Lev {
 
     // ------------------------------------------------------------------ MakeVelForce
     // Maestro::MakeVelForce, planar, one level (Source/MaestroForce.cpp:58-126)
-    void MakeVelForce(MF& vel_force, MF* uedge, MF& sold, MF& w0_force_cart, MF& grav_cart, MF& rho0_cart) {
+    void MakeVelForce(MF& vel_force, MF* uedge, MF& sold, MF& w0_force_cart, MF& grav_cart, MF& rho0_cart,
+                      const MF* gradw0_cart = nullptr) {
         vel_force.setVal(0.0);
         if (P.spherical) {
-            // Source/MaestroForce.cpp:151-252; the exact base state has gradw0 = 0
-            // (:30-41), so the utilde term subtracts Ut.e_r * 0 * e_r
-            const real gradw0 = 0.0;
+            // Source/MaestroForce.cpp:151-252; gradw0_cart holds dw0/dr of the uniform bins; the
+            // exact base state has gradw0 = 0 (:30-41), so the utilde term subtracts Ut.e_r * 0 * e_r
             for (int b = 0; b < nb; ++b) {
                 const Arr& gpi_arr = gpi[b];
                 const Arr& rho_arr = sold[b];
@@ -387,6 +512,7 @@ struct Lev {
                     const real ut_dot_er = 0.5 * (ue(i, j, k) + ue(i + 1, j, k)) * nrm[0] +
                                              0.5 * (ve(i, j, k) + ve(i, j + 1, k)) * nrm[1] +
                                              0.5 * (we(i, j, k) + we(i, j, k + 1)) * nrm[2];
+                    const real gradw0 = gradw0_cart ? (*gradw0_cart)[b](i, j, k) : real(0.0);
                     for (int dim = 0; dim < 3; ++dim) vf(i, j, k, dim) -= ut_dot_er * gradw0 * nrm[dim];
                 }
             }
@@ -925,11 +1051,11 @@ struct Lev {
     // ------------------------------------------------------------------ forces
     // Maestro::ModifyScalForce, planar 3-D, one level (Source/MaestroForce.cpp:261-453)
     void ModifyScalForce(MF& scal_force, MF& state, MF* umac, MF& s0_edge_cart, MF& s0_cart, int comp,
-                         int fullform) {
+                         int fullform, const MF* divu_cart = nullptr) {
         const double* dx = L.dx;
         if (P.spherical) {
-            // Source/MaestroForce.cpp:335-412; divu_cart = Put1dArrayOnCart(divw0) = 0 with
-            // the exact base state (:283-302)
+            // Source/MaestroForce.cpp:335-412; divu_cart = Put1dArrayOnCart(divw0), which is 0
+            // with the exact base state (:283-302)
             const int* domlo = L.dom.lo;
             const int* domhi = L.dom.hi;
             for (int b = 0; b < nb; ++b) {
@@ -940,7 +1066,7 @@ struct Lev {
                 const Arr& s0a = s0_cart[b];
                 const Arr force = scal_force[b].comp(comp);
                 MO_FOR3(L.ba[b]) {
-                    const real divu_c = 0.0;
+                    const real divu_c = divu_cart ? (*divu_cart)[b](i, j, k) : real(0.0);
                     real divumac = (um(i + 1, j, k) - um(i, j, k)) / dx[0] + (vm(i, j + 1, k) - vm(i, j, k)) / dx[1] +
                                      (wm(i, j, k + 1) - wm(i, j, k)) / dx[2];
                     if (fullform == 1) {
@@ -1050,7 +1176,7 @@ struct Lev {
         for (int b = 0; b < nb; ++b) {
             const Arr& a = scal[b];
             MO_FOR3(L.ba[b]) {
-                const real s0c = P.spherical ? s0[cc_to_r(i, j, k)] : s0[k];
+                const real s0c = P.spherical ? sph_cell_at(s0, i, j, k) : s0[k];
                 if (flag) a(i, j, k, comp) = a(i, j, k, comp) - s0c;
                 else a(i, j, k, comp) = a(i, j, k, comp) + s0c;
             }
@@ -1141,10 +1267,12 @@ struct Lev {
                       const std::vector<real>& rh0e_old, const std::vector<real>& rh0_new,
                       const std::vector<real>& rh0e_new, MF* rh0mac_old = nullptr, MF* rh0mac_new = nullptr,
                       const std::vector<real>* r0_old = nullptr, const std::vector<real>* r0e_old = nullptr,
-                      const std::vector<real>* r0_new = nullptr, const std::vector<real>* r0e_new = nullptr) {
+                      const std::vector<real>* r0_new = nullptr, const std::vector<real>* r0e_new = nullptr,
+                      MF* r0mac_old = nullptr, MF* r0mac_new = nullptr) {
         const int ept = P.enthalpy_pred_type;
         const int spt = P.species_pred_type;
-        if (P.spherical) {  // exact base state, (rho h)' predicted (Source/MaestroMakeFlux.cpp:540-548, 788-840)
+        if (P.spherical && P.use_exact_base_state) {
+            // exact base state, (rho h)' predicted (Source/MaestroMakeFlux.cpp:540-548, 788-840)
             for (int b = 0; b < nb; ++b)
                 for (int d = 0; d < 3; ++d) {
                     const Arr& f = sflux[d][b];
@@ -1155,6 +1283,27 @@ struct Lev {
                     MO_FOR3(nodal(L.ba[b], d)) {
                         const real rhoh0_edge = 0.5 * ho(i, j, k) + 0.5 * hn(i, j, k);
                         f(i, j, k, RhoH) = u(i, j, k) * (rhoh0_edge + e(i, j, k, RhoH));
+                    }
+                }
+            return;
+        }
+        if (P.spherical) {
+            // uniform bins (Source/MaestroMakeFlux.cpp:549-575, 846-1000): rhoh predicted, or
+            // (rho h)' with (rho h)_0 on the faces as rho0mac * h0mac; rh0mac_old / _new carry
+            // h0mac here, r0mac_old / _new rho0mac
+            for (int b = 0; b < nb; ++b)
+                for (int d = 0; d < 3; ++d) {
+                    const Arr& f = sflux[d][b];
+                    const Arr& e = sedge[d][b];
+                    const Arr& u = umac[d][b];
+                    MO_FOR3(nodal(L.ba[b], d)) {
+                        if (ept == 0) {
+                            f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, RhoH);
+                        } else {
+                            const real rho0_edge = 0.5 * r0mac_old[d][b](i, j, k) + 0.5 * r0mac_new[d][b](i, j, k);
+                            const real h0_edge = 0.5 * rh0mac_old[d][b](i, j, k) + 0.5 * rh0mac_new[d][b](i, j, k);
+                            f(i, j, k, RhoH) = u(i, j, k) * (rho0_edge * h0_edge + e(i, j, k, RhoH));
+                        }
                     }
                 }
             return;
@@ -1374,22 +1523,34 @@ struct Stage {
         AverageDown(s0_cart, 0, nc);
         if (s0_cart[0].ng > 0) FillPatch(s0_cart, 0, nc, bccomp, *bcs, is_vel);
     }
-    // Maestro::MakeS0mac, exact base state, s0mac_interp_type 1 (Source/MaestroFill3dData.cpp:712-783):
-    // s0 injected into cells (two ghost cells by FillPatch with bcs_f), averaged to the
-    // faces of the nodal boxes grown by one
+    // Maestro::MakeS0mac (Source/MaestroFill3dData.cpp:712-1188) over the nodal boxes grown by
+    // one: s0mac_interp_type 1 puts s0 on the cells (two ghost cells, FillPatch with bcs_f) and
+    // averages them to the faces; with uniform bins, 2 / 3 interpolate s0 at the face centres
+    // (linear / quadratic in r_cc_loc, as Put1dArrayOnCart does at the cell centres)
     void MakeS0mac(const BS& s0, VF& s0mac) {
+        const int t = P.s0mac_interp_type ? P.s0mac_interp_type : 1;
         VMF s0_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) s0_cart[lev].define(S[lev].L.ba, 1, 2, -1, 0.0);
-        Put1dArrayOnCart(s0, s0_cart, false, false, &bcs_f(), 0, false);
+        if (t == 1) Put1dArrayOnCart(s0, s0_cart, false, false, &bcs_f(), 0, false);
         for (int lev = 0; lev < nlev; ++lev) {
-            const Level& L = S[lev].L;
+            const Lev& V = S[lev];
+            const Level& L = V.L;
             for (int d = 0; d < 3; ++d) {
                 s0mac[lev][d].define(L.ba, 1, 1, d, 0.0);
                 const int di = d == 0, dj = d == 1, dk = d == 2;
                 for (int b = 0; b < (int)L.ba.size(); ++b) {
                     const Arr& c = s0_cart[lev][b];
                     const Arr& o = s0mac[lev][d][b];
-                    MO_FOR3(grow(nodal(L.ba[b], d), 1)) { o(i, j, k) = 0.5 * (c(i - di, j - dj, k - dk) + c(i, j, k)); }
+                    MO_FOR3(grow(nodal(L.ba[b], d), 1)) {
+                        if (t == 1) {
+                            o(i, j, k) = 0.5 * (c(i - di, j - dj, k - dk) + c(i, j, k));
+                        } else {
+                            const double x = P.prob_lo[0] + (double(i) + (di ? 0.0 : 0.5)) * L.dx[0] - V.center[0];
+                            const double y = P.prob_lo[1] + (double(j) + (dj ? 0.0 : 0.5)) * L.dx[1] - V.center[1];
+                            const double z = P.prob_lo[2] + (double(k) + (dk ? 0.0 : 0.5)) * L.dx[2] - V.center[2];
+                            o(i, j, k) = V.sph_cell_value(s0[lev], std::sqrt(x * x + y * y + z * z), t);
+                        }
+                    }
                 }
             }
         }
@@ -1596,16 +1757,28 @@ struct Stage {
     }
     // Maestro::MakeVelForce, planar (Source/MaestroForce.cpp:6-259)
     void MakeVelForce(VMF& vel_force, VF& uedge, VMF& sold, VMF& w0_force_cart, const BS* rho0 = nullptr) {
-        VMF grav_cart(nlev), rho0_cart(nlev);
+        VMF grav_cart(nlev), rho0_cart(nlev), gradw0_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) {
             grav_cart[lev].define(S[lev].L.ba, 3, 1, -1, 0.0);
             rho0_cart[lev].define(S[lev].L.ba, 1, 1, -1, 0.0);
+        }
+        // gradw0 = (w0(r+1) - w0(r)) / dr of the uniform bins, on the cells (Source/MaestroForce.cpp:36-50)
+        const bool grad = P.spherical && !P.use_exact_base_state;
+        if (grad) {
+            BS gradw0(nlev);
+            for (int lev = 0; lev < nlev; ++lev) {
+                const Lev& L = S[lev];
+                gradw0[lev].assign(L.nr, 0.0);
+                for (int r = 0; r < L.nr; ++r) gradw0[lev][r] = (L.w0[r + 1] - L.w0[r]) / L.drf;
+                gradw0_cart[lev].define(L.L.ba, 1, 1, -1, 0.0);
+            }
+            Put1dArrayOnCart(gradw0, gradw0_cart, false, false, &bcs_u(), 0, true);
         }
         Put1dArrayOnCart(rho0 ? *rho0 : bs(&Lev::rho0_old), rho0_cart, false, false, &bcs_s(), Rho, false);
         Put1dArrayOnCart(bs(&Lev::grav_cell), grav_cart, false, true, &bcs_f(), 0, false);
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeVelForce(vel_force[lev], uedge[lev].data(), sold[lev], w0_force_cart[lev], grav_cart[lev],
-                                rho0_cart[lev]);
+                                rho0_cart[lev], grad ? &gradw0_cart[lev] : nullptr);
         AverageDown(vel_force, 0, 3);
         FillPatch(vel_force, 0, 3, 0, bcs_u(), true);
     }
@@ -1662,9 +1835,27 @@ struct Stage {
         VMF s0_edge_cart(nlev);
         for (int lev = 0; lev < nlev; ++lev) s0_edge_cart[lev].define(S[lev].L.ba, 1, 1);
         if (!P.spherical) Put1dArrayOnCart(s0_edge, s0_edge_cart, false, false, &bcs_f(), 0, false);
+        // uniform bins: div(w0) of the shells on the cells (Source/MaestroForce.cpp:283-305)
+        const bool divw = P.spherical && !P.use_exact_base_state;
+        VMF divu_cart(nlev);
+        if (divw) {
+            BS divw0(nlev);
+            for (int lev = 0; lev < nlev; ++lev) {
+                const Lev& L = S[lev];
+                divw0[lev].assign(L.nr, 0.0);
+                const auto& re = L.r_edge_loc;
+                const auto& rc = L.r_cc_loc;
+                for (int r = 0; r < L.nr - 1; ++r) {
+                    const double dr_loc = re[r + 1] - re[r];
+                    divw0[lev][r] = (re[r + 1] * re[r + 1] * L.w0[r + 1] - re[r] * re[r] * L.w0[r]) / (dr_loc * rc[r] * rc[r]);
+                }
+                divu_cart[lev].define(L.L.ba, 1, 0, -1, 0.0);
+            }
+            Put1dArrayOnCart(divw0, divu_cart, false, false, &bcs_u(), 0, false);
+        }
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].ModifyScalForce(scal_force[lev], state[lev], umac[lev].data(), s0_edge_cart[lev], s0_cart[lev], comp,
-                                   fullform);
+                                   fullform, divw ? &divu_cart[lev] : nullptr);
         AverageDown(scal_force, comp, 1);
         FillPatch(scal_force, comp, 1, 0, bcs_f(), false);
     }
@@ -1732,16 +1923,31 @@ struct Stage {
     void MakeRhoHFlux(VF& sflux, VF& sedge, VF& umac, const BS& rh0_old, const BS& rh0e_old, const BS& rh0_new,
                       const BS& rh0e_new, const BS* r0_old = nullptr, const BS* r0e_old = nullptr,
                       const BS* r0_new = nullptr, const BS* r0e_new = nullptr) {
-        VF h0mac_old(nlev), h0mac_new(nlev);
-        if (P.spherical) {  // exact base state: rhoh0 on faces (Source/MaestroEnthalpyAdvance.cpp:187-220)
+        VF h0mac_old(nlev), h0mac_new(nlev), r0mac_old(nlev), r0mac_new(nlev);
+        if (P.spherical && P.use_exact_base_state) {  // rhoh0 on faces (Source/MaestroEnthalpyAdvance.cpp:187-220)
             MakeS0mac(rh0_old, h0mac_old);
             MakeS0mac(rh0_new, h0mac_new);
+        } else if (P.spherical) {  // rho0 and h0 = rhoh0 / rho0 on faces (:194-220, 251-300)
+            BS h0o(nlev), h0n(nlev);
+            for (int lev = 0; lev < nlev; ++lev) {
+                h0o[lev].resize(rh0_old[lev].size());
+                h0n[lev].resize(rh0_new[lev].size());
+                for (size_t r = 0; r < h0o[lev].size(); ++r) {
+                    h0o[lev][r] = rh0_old[lev][r] / (*r0_old)[lev][r];
+                    h0n[lev][r] = rh0_new[lev][r] / (*r0_new)[lev][r];
+                }
+            }
+            MakeS0mac(*r0_old, r0mac_old);
+            MakeS0mac(*r0_new, r0mac_new);
+            MakeS0mac(h0o, h0mac_old);
+            MakeS0mac(h0n, h0mac_new);
         }
         for (int lev = 0; lev < nlev; ++lev)
             S[lev].MakeRhoHFlux(sflux[lev].data(), sedge[lev].data(), umac[lev].data(), rh0_old[lev], rh0e_old[lev],
                                 rh0_new[lev], rh0e_new[lev], h0mac_old[lev].data(), h0mac_new[lev].data(),
                                 r0_old ? &(*r0_old)[lev] : nullptr, r0e_old ? &(*r0e_old)[lev] : nullptr,
-                                r0_new ? &(*r0_new)[lev] : nullptr, r0e_new ? &(*r0e_new)[lev] : nullptr);
+                                r0_new ? &(*r0_new)[lev] : nullptr, r0e_new ? &(*r0e_new)[lev] : nullptr,
+                                r0mac_old[lev].data(), r0mac_new[lev].data());
         FluxSync(sflux, RhoH, 1);
     }
     // Maestro::ConvertRhoHToH with its AverageDown and FillPatch (Source/MaestroConvert.cpp:93-114)
@@ -2004,6 +2210,17 @@ static void gather_faces(const Box& dom, const MF& mf, int d, int c0, int nc, do
     }
 }
 
+// nr_fine of spherical geometry with uniform radial bins (Source/MaestroSetup.cpp:83-95)
+static int mo_sph_nr_fine(const mo_params* p, int nlev) {
+    const double dxf = p->dx[0] / (1 << (nlev - 1));
+    const double drf = dxf / (p->drdxfac > 0 ? p->drdxfac : 1);
+    const double lenx = 0.5 * (p->prob_hi[0] - p->prob_lo[0]);
+    const double leny = 0.5 * (p->prob_hi[1] - p->prob_lo[1]);
+    const double lenz = 0.5 * (p->prob_hi[2] - p->prob_lo[2]);
+    const double max_dist = std::sqrt(lenx * lenx + leny * leny + lenz * lenz);
+    return int(max_dist / drf) + 1;
+}
+
 // The levels, boundary conditions, base state, w0_cart and (spherical) w0mac of a stage call.
 static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxes, const int* boxes,
                         const mo_inputs* in) {
@@ -2013,8 +2230,17 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
                                  "with ppm_type 0)");
     if (p->use_exact_base_state && !p->spherical) throw std::runtime_error("use_exact_base_state is spherical-only");
     if (p->spherical) {
-        if (!p->use_exact_base_state) throw std::runtime_error("spherical needs use_exact_base_state = 1");
-        if (p->enthalpy_pred_type != 1) throw std::runtime_error("spherical: enthalpy_pred_type 1");
+        if (p->use_exact_base_state && p->enthalpy_pred_type != 1)
+            throw std::runtime_error("spherical with the exact base state: enthalpy_pred_type 1");
+        if (!p->use_exact_base_state && p->enthalpy_pred_type > 1)
+            throw std::runtime_error("spherical with uniform radial bins: enthalpy_pred_type 0 or 1");
+        if (p->use_exact_base_state && p->s0mac_interp_type > 1)
+            throw std::runtime_error("exact base state: s0mac_interp_type 1 (types 2 and 3 index the irregular grid "
+                                     "past its end, Source/MaestroFill3dData.cpp:786-790)");
+        if (p->w0_interp_type < 0 || p->w0_interp_type > 3 || p->w0mac_interp_type < 0 || p->w0mac_interp_type > 4 ||
+            p->s0_interp_type < 0 || p->s0_interp_type > 3 || p->s0mac_interp_type < 0 || p->s0mac_interp_type > 3 ||
+            p->drdxfac < 0)
+            throw std::runtime_error("interpolation type out of range");
     }
     if (!(p->enthalpy_pred_type >= 0 && p->enthalpy_pred_type <= 2))
         throw std::runtime_error("enthalpy_pred_type must be 0, 1 or 2");
@@ -2054,11 +2280,16 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
         S.nb = nboxes[lev];
         S.nr = S.L.dom.hi[2] - S.L.dom.lo[2] + 1;
         if (p->spherical) {
-            // nr_fine = nr_irreg + 1 from the finest level (Source/MaestroSetup.cpp:60-82)
+            // nr_fine from the finest level (Source/MaestroSetup.cpp:60-96): nr_irreg + 1 for the
+            // exact base state, else int(max_dist / dr_fine) + 1 with dr_fine = dx_fine / drdxfac
             const int rf = 1 << (nlev - 1);
-            const double domhi = (p->dom_hi[0] + 1) * rf;
-            S.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
             S.dxf = p->dx[0] / rf;
+            if (p->use_exact_base_state) {
+                const double domhi = (p->dom_hi[0] + 1) * rf;
+                S.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
+            } else {
+                S.nr = mo_sph_nr_fine(p, nlev);
+            }
         }
         S.ng_s = S.ng_adv = H.ng_s;
         S.dt = p->dt;

@@ -45,6 +45,11 @@ typedef struct {
     double prob_lo[3];
     double prob_hi[3];
     int reflux_type; /* 1 (or 0): AverageDownFaces of the fluxes; 2: FluxRegister reflux */
+    int drdxfac;           /* spherical, inexact base state (0 means 1) */
+    int w0_interp_type;    /* 1, 2 (0 means 2), 3 */
+    int w0mac_interp_type; /* 1 (0 means 1), 2, 3, 4 */
+    int s0_interp_type;    /* 1, 2, 3 (0 means 3) */
+    int s0mac_interp_type; /* 1 (0 means 1), 2, 3 */
 } mo_params;
 
 typedef struct {

@@ -101,6 +101,11 @@ void set_params(const mo_params* p) {
     maestro::base_cutoff_density = p->base_cutoff_density;
     maestro::buoyancy_cutoff_factor = p->buoyancy_cutoff_factor;
     maestro::do_eos_h_above_cutoff = p->do_eos_h_above_cutoff;
+    maestro::drdxfac = p->drdxfac > 0 ? p->drdxfac : 1;
+    maestro::w0_interp_type = p->w0_interp_type ? p->w0_interp_type : 2;
+    maestro::w0mac_interp_type = p->w0mac_interp_type ? p->w0mac_interp_type : 1;
+    maestro::s0_interp_type = p->s0_interp_type ? p->s0_interp_type : 3;
+    maestro::s0mac_interp_type = p->s0mac_interp_type ? p->s0mac_interp_type : 1;
 }
 
 // phys_bc -> BCType of the velocity, scalar and "first-order extrapolation" components,
@@ -180,9 +185,16 @@ void setup_base_state(Maestro& m, const mo_params* p, const mo_inputs* in) {
     if (maestro::spherical) {
         const Real domhi = p->dom_hi[0] + 1;
         nr_irreg = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0);
-        if (!maestro::use_exact_base_state) amrex::Abort("spherical: the exact base state only");
-        nr_fine = nr_irreg + 1;
         dr_fine = p->dx[0] / maestro::drdxfac;
+        if (maestro::use_exact_base_state) {
+            nr_fine = nr_irreg + 1;
+        } else {
+            const double lenx = 0.5 * (p->prob_hi[0] - p->prob_lo[0]);
+            const double leny = 0.5 * (p->prob_hi[1] - p->prob_lo[1]);
+            const double lenz = 0.5 * (p->prob_hi[2] - p->prob_lo[2]);
+            const double max_dist = std::sqrt(lenx * lenx + leny * leny + lenz * lenz);
+            nr_fine = int(max_dist / dr_fine) + 1;
+        }
     } else {
         nr_fine = p->dom_hi[AMREX_SPACEDIM - 1] + 1;
         dr_fine = p->dx[AMREX_SPACEDIM - 1];

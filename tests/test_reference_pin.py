@@ -141,6 +141,22 @@ def stage_cases():
         n=(24, 16, 24), nspec=2, ppm_type=2, max_grid=(8, 16, 12), bc_lo=(SYMMETRY, SLIPWALL, SLIPWALL),
         bc_hi=(OUTFLOW, NOSLIPWALL, OUTFLOW), seed=200, cfl=0.5, gpi_amp=1e-3))
     C["traced forces, spherical"] = lambda: traced(configs.spherical_config(n=32, max_grid=16, ppm_type=2))
+    # spherical with uniform radial bins (use_exact_base_state = 0, the reference's default):
+    # every interpolation type of Put1dArrayOnCart, MakeW0mac and MakeS0mac, drdxfac, rhoh
+    inexact = {"uniform bins": {}, "uniform bins, rhoh predicted": {"enthalpy_pred_type": 0},
+               "uniform bins, w0 constant, s0 linear": {"w0_interp_type": 1, "s0_interp_type": 2},
+               "uniform bins, w0 quadratic, s0 constant": {"w0_interp_type": 3, "s0_interp_type": 1},
+               "uniform bins, w0mac linear, s0mac linear": {"w0mac_interp_type": 2, "s0mac_interp_type": 2},
+               "uniform bins, w0mac quadratic, s0mac quadratic": {"w0mac_interp_type": 3, "s0mac_interp_type": 3},
+               "uniform bins, w0mac nodal, drdxfac 5": {"w0mac_interp_type": 4, "drdxfac": 5}}
+    for name, kw in inexact.items():
+        ept = kw.pop("enthalpy_pred_type", 1)
+        for ppm in (1, 2):
+            C[f"spherical {name} ppm{ppm}"] = lambda kw=kw, ept=ept, ppm=ppm: dict(
+                configs.spherical_config(n=16, max_grid=8, ppm_type=ppm, exact=False, **kw), enthalpy_pred_type=ept)
+    for name, kw in {"w0 constant": {"w0_interp_type": 1}, "w0 quadratic": {"w0_interp_type": 3},
+                     "w0mac nodal": {"w0mac_interp_type": 4}, "w0mac quadratic": {"w0mac_interp_type": 3}}.items():
+        C[f"spherical exact grid, {name}"] = lambda kw=kw: configs.spherical_config(n=16, max_grid=8, ppm_type=1, **kw)
 
     def negative_species():
         from test_bench_shapes_gpu import headline_shape, plant_negative_species
@@ -208,6 +224,9 @@ def velocity_cases():
                                                              bc_hi=(OUTFLOW, OUTFLOW, OUTFLOW)),
         "planar ppm0": lambda: configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=0),
         "spherical ppm2": lambda: configs.spherical_config(n=32, max_grid=16, ppm_type=2),
+        "spherical uniform bins ppm2": lambda: configs.spherical_config(n=16, max_grid=8, ppm_type=2, exact=False),
+        "spherical uniform bins, w0mac nodal, s0 linear": lambda: configs.spherical_config(
+            n=16, max_grid=8, ppm_type=1, exact=False, w0mac_interp_type=4, s0_interp_type=2),
         "planar ppm2 traced forces": lambda: dict(configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=2,
                                                                         gpi_amp=1e-3), ppm_trace_forces=1),
     }
