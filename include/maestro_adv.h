@@ -49,7 +49,8 @@ typedef struct {
     int enthalpy_pred_type;     /* 0 rhoh, 1 rhoh', 2 h (3-D planar and 2-D; spherical: 1) */
     int ppm_trace_forces;       /* 0, or 1 (ppm_type 1/2, 3-D): forces traced by PPM */
     int evolve_base_state;
-    int use_exact_base_state;   /* planar: 0; spherical: 1 */
+    int use_exact_base_state;   /* planar: 0; spherical: 1 the exact (irregular) radial grid,
+                                   0 uniform radial bins of dx_fine / drdxfac */
     int phys_bc_lo[3];
     int phys_bc_hi[3];
     int dom_lo[3];              /* level-0 domain box */
@@ -63,9 +64,11 @@ typedef struct {
     int base_cutoff_density_coord;
     int dim;                    /* 3 (0 means 3) or 2: the AMREX_SPACEDIM == 2 form, y radial,
                                    boxes and domain with z = [0, 0], 2 velocity components */
-    int spherical;              /* 1: full-star spherical geometry (3-D, one level, with
+    int spherical;              /* 1: full-star spherical geometry (3-D, one or two levels):
                                    use_exact_base_state = 1: the irregular radial grid
-                                   r_cc(i) = sqrt(0.75 + 2i) dx, nr = nr_irreg + 1) */
+                                   r_cc(i) = sqrt(0.75 + 2i) dx, nr = nr_irreg + 1; 0: r_cc(i) =
+                                   (i + 1/2) dr, dr = dx / drdxfac, nr = int(max_dist / dr) + 1
+                                   with max_dist the centre-to-corner distance; dx the finest */
     double prob_lo[3];          /* physical domain (the star's centre is its midpoint) */
     double prob_hi[3];
     int reflux_type;            /* coarse-fine flux synchronisation: 1 (or 0) AverageDownFaces

@@ -284,6 +284,15 @@ static void field_specs(Ctx& c) {
         S(F_S0MACB0 + d, ns, 1, d);
     }
     S(F_S0CART2, ns, 2);
+    const int nu = c.sph && !c.P.use_exact_base_state ? 1 : 0;  // uniform radial bins only
+    for (int d = 0; d < 3; ++d) {
+        S(F_S0MACC0 + d, nu, 1, d);
+        S(F_S0MACD0 + d, nu, 1, d);
+    }
+    S(F_GRADW0, nu, 1);
+    S(F_DIVW0, nu, 0);
+    // nodes of the box grown by one, node (i,j,k) at cell (i,j,k): two ghost cells
+    S(F_W0NODAL, c.sph && c.geo.w0maci == 4 ? 3 : 0, 2);
 }
 
 static void free_layout(Ctx& c) {
@@ -445,10 +454,15 @@ static void addw0_h(Hier& H, int f0, double mult) {
     sync_faces_h(H, f0);
 }
 
-// Maestro::MakeS0mac, exact base state, s0mac_interp_type 1 (Source/MaestroFill3dData.cpp:712-783):
-// the array injected into cells (two ghosts, FillPatch with bcs_f), averaged to the faces of the
-// nodal boxes grown by one, into dst0 .. dst0 + 2
+// Maestro::MakeS0mac (Source/MaestroFill3dData.cpp:712-1188) into dst0 .. dst0 + 2 over the
+// nodal boxes grown by one: s0mac_interp_type 1 puts the array on the cells (two ghosts,
+// FillPatch with bcs_f) and averages it to the faces; 2 / 3 (uniform bins) interpolate it at the
+// face centres
 static void make_s0mac_h(Hier& H, const char* s0, int dst0) {
+    if (H[0].geo.s0maci != 1) {
+        for (auto* c : H.L) make_s0mac_interp(*c, c->b1(s0), dst0);
+        return;
+    }
     put1d_h(H, F_S0CART2, s0, 0, 1, 0, BCS_F, 0, 0, -1);
     for (auto* c : H.L) make_s0mac_faces(*c, dst0);
 }
@@ -471,6 +485,8 @@ static void w0_carts(Hier& H) {
 // VelocityAdvance); rho0: the base-state density of the buoyancy
 static void make_vel_force_h(Hier& H, int fe = F_UTRANS0, const char* rho0 = "rho0_old") {
     const int nd = H[0].ndim;
+    // spherical, uniform bins: dw0/dr on the cells (Source/MaestroForce.cpp:36-52)
+    if (H[0].sph && !H[0].geo.exact) put1d_h(H, F_GRADW0, "gradw0", 0, 1, 0, BCS_U, 0, 1, -1);
     put1d_h(H, F_GRAVCART, "grav_cell", nd - 1, nd, 0, BCS_F, 0, 0, -1);
     put1d_h(H, F_RHO0CART, rho0, 0, 1, 0, BCS_S, RHO, 0, RHO);
     for (auto* c : H.L) make_vel_force(*c, fe);
@@ -502,6 +518,8 @@ static void advance_premac(Hier& H) {
 // Maestro::ModifyScalForce (Source/MaestroForce.cpp:261-467)
 static void modify_scal_force_h(Hier& H, int comp, const char* s0_edge, int s0cart_fid, int fullform) {
     if (!H[0].sph) put1d_h(H, F_S0ECART, s0_edge, 0, 1, 0, BCS_F, 0, 0, -1);  // planar only (:275-277)
+    // spherical, uniform bins: div w0 on the cells (:283-305)
+    if (H[0].sph && !H[0].geo.exact) put1d_h(H, F_DIVW0, "divw0", 0, 1, 0, BCS_U, 0, 0, -1);
     for (auto* c : H.L) modify_scal_force(*c, comp, s0cart_fid, fullform);
     average_down_h(H, F_SCALFORCE, comp, 1);
     fill_patch_h(H, F_SCALFORCE, comp, 1, BCS_F, 0, 0, comp);
@@ -636,9 +654,14 @@ static void rhoh_flux_h(Hier& H, int which_step) {
     const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
     const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
     const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
-    if (H[0].sph) {  // rhoh0 on faces, exact base state (Source/MaestroEnthalpyAdvance.cpp:187-220)
+    if (H[0].sph && H[0].geo.exact) {  // rhoh0 on faces (Source/MaestroEnthalpyAdvance.cpp:187-220)
         make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
         make_s0mac_h(H, rh0n, F_S0MACB0);
+    } else if (H[0].sph) {  // uniform bins: rho0 and h0 = rhoh0 / rho0 on faces (:194-220, 251-300)
+        make_s0mac_h(H, "rho0_old", F_S0MACC0);
+        make_s0mac_h(H, r0n, F_S0MACD0);
+        make_s0mac_h(H, "h0_old", F_S0MAC0);
+        make_s0mac_h(H, which_step == 1 ? "h0_old" : "h0_new", F_S0MACB0);
     }
     for (auto* c : H.L)
         make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en), c->b1("rho0_old"),
@@ -994,6 +1017,25 @@ struct madv_ctx {
     }
 };
 
+// The spherical radial grid from the finest level (Source/MaestroSetup.cpp:60-96): its cell
+// size dxf and x extent nfine cells; dr_fine = dxf / drdxfac; nr_fine = nr_irreg + 1 for the
+// exact base state, else int(max_dist / dr_fine) + 1 with max_dist the centre-to-corner distance
+static void sph_radial_grid(Ctx& c, double dxf, int nfine) {
+    c.geo.dxf = dxf;
+    c.geo.drf = dxf / (c.P.drdxfac > 0 ? c.P.drdxfac : 1);
+    if (c.geo.exact) {
+        const double domhi = nfine;
+        c.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
+    } else {
+        const double lenx = 0.5 * (c.P.prob_hi[0] - c.P.prob_lo[0]);
+        const double leny = 0.5 * (c.P.prob_hi[1] - c.P.prob_lo[1]);
+        const double lenz = 0.5 * (c.P.prob_hi[2] - c.P.prob_lo[2]);
+        const double max_dist = std::sqrt(lenx * lenx + leny * leny + lenz * lenz);
+        c.nr = int(max_dist / c.geo.drf) + 1;
+    }
+    c.geo.nr = c.nr;
+}
+
 static int init_level(Ctx& c, const madv_params& p, int lev) {
     c.P = p;
     c.lev = lev;
@@ -1014,15 +1056,17 @@ static int init_level(Ctx& c, const madv_params& p, int lev) {
     c.nr = c.P.dom_hi[c.ndim - 1] - c.P.dom_lo[c.ndim - 1] + 1;
     c.sph = p.spherical != 0;
     if (c.sph) {
-        // nr_fine = nr_irreg + 1 (Source/MaestroSetup.cpp:66-82)
-        const double domhi = c.P.dom_hi[0] + 1;
-        c.nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
         for (int d = 0; d < 3; ++d) {
             c.geo.plo[d] = p.prob_lo[d];
             c.geo.dx[d] = c.P.dx[d];
             c.geo.ctr[d] = 0.5 * (p.prob_lo[d] + p.prob_hi[d]);
         }
-        c.geo.dxf = c.P.dx[0];  // the finest level's, set again with the layout's levels
+        c.geo.exact = p.use_exact_base_state != 0;
+        c.geo.w0i = p.w0_interp_type ? p.w0_interp_type : 2;
+        c.geo.w0maci = p.w0mac_interp_type ? p.w0mac_interp_type : 1;
+        c.geo.s0i = p.s0_interp_type ? p.s0_interp_type : 3;
+        c.geo.s0maci = p.s0mac_interp_type ? p.s0mac_interp_type : 1;
+        sph_radial_grid(c, c.P.dx[0], c.P.dom_hi[0] - c.P.dom_lo[0] + 1);  // set again with the layout's levels
     }
     for (int d = 0; d < 3; ++d) c.per[d] = c.P.phys_bc_lo[d] == PB_INTERIOR;
     int rc = bc_setup(c);
@@ -1223,14 +1267,21 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
                   "and need the equation of state)");
         return MADV_ERR_UNSUPPORTED;
     }
-    if (p->spherical && ((p->w0_interp_type != 0 && p->w0_interp_type != 2) ||
-                         (p->w0mac_interp_type != 0 && p->w0mac_interp_type != 1) ||
-                         (p->s0mac_interp_type != 0 && p->s0mac_interp_type != 1))) {
-        set_error("spherical: w0_interp_type 2, w0mac_interp_type 1 and s0mac_interp_type 1 are built");
+    if (p->spherical && (p->w0_interp_type < 0 || p->w0_interp_type > 3 || p->w0mac_interp_type < 0 ||
+                         p->w0mac_interp_type > 4 || p->s0_interp_type < 0 || p->s0_interp_type > 3 ||
+                         p->s0mac_interp_type < 0 || p->s0mac_interp_type > 3 || p->drdxfac < 0)) {
+        set_error("spherical: w0_interp_type 1-3, w0mac_interp_type 1-4, s0_interp_type 1-3, s0mac_interp_type 1-3, "
+                  "drdxfac >= 1 (0: the default)");
+        return MADV_ERR_PARAM;
+    }
+    if (p->spherical && p->use_exact_base_state && p->s0mac_interp_type > 1) {
+        set_error("spherical with the exact base state: s0mac_interp_type 1 (the reference's types 2 and 3 index the "
+                  "irregular radial grid with the uniform-grid formula and read past its end)");
         return MADV_ERR_UNSUPPORTED;
     }
-    if (p->spherical && (p->use_exact_base_state != 1 || p->dim == 2 || p->enthalpy_pred_type != 1)) {
-        set_error("spherical geometry needs use_exact_base_state = 1, 3-D and enthalpy_pred_type 1");
+    if (p->spherical && (p->dim == 2 || (p->use_exact_base_state && p->enthalpy_pred_type != 1) ||
+                         (!p->use_exact_base_state && p->enthalpy_pred_type > 1))) {
+        set_error("spherical geometry needs 3-D and enthalpy_pred_type 1 (uniform radial bins: 0 or 1)");
         return MADV_ERR_UNSUPPORTED;
     }
     if ((p->ppm_trace_forces != 0 && (p->ppm_trace_forces != 1 || p->ppm_type == 0 || p->dim == 2)) ||
@@ -1329,14 +1380,11 @@ int madv_set_layout_levels(madv_ctx* h, int nlev, const int* nboxes, const madv_
     }
     Hier H = h->H();
     if (h->c.sph) {
-        // one radial grid for every level, set by the finest level (Source/MaestroSetup.cpp:60-82,
-        // Source/BaseStateGeometry.cpp:86-96): nr_fine = nr_irreg + 1 and its cell size
+        // one radial grid for every level, set by the finest level's cell size
+        // (Source/MaestroSetup.cpp:60-96, Source/BaseStateGeometry.cpp:86-104)
         const Ctx& fl = H[nlev - 1];
-        const double domhi = fl.P.dom_hi[0] + 1;
-        const int nr = int((3.0 * (domhi / 2 - 0.5) * (domhi / 2 - 0.5) - 0.75) / 2.0) + 1;
         for (auto* c : H.L) {
-            c->nr = nr;
-            c->geo.dxf = fl.P.dx[0];
+            sph_radial_grid(*c, fl.P.dx[0], fl.P.dom_hi[0] - fl.P.dom_lo[0] + 1);
             c->have_base = false;
         }
     }
@@ -1416,17 +1464,42 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
             c.h1[a.name] = std::vector<double>(a.p, a.p + a.n);
         }
     }
-    // spherical: radii of the exact radial grid (Source/BaseStateGeometry.cpp:86-96), r_cc_loc
-    // continued one bin past the last (Put1dArrayOnCart reads r_cc_loc(nr_fine))
+    // spherical: radii of the radial grid (Source/BaseStateGeometry.cpp:86-104), the exact one
+    // or uniform bins of drf; r_cc_loc continued one bin past the last (Put1dArrayOnCart reads
+    // r_cc_loc(nr_fine) with the exact grid)
     for (int l = 0; l < nlev; ++l) {
         Ctx& c = H[l];
         if (!c.sph) continue;
         std::vector<double> rc(c.nr + 1), re(c.nr + 1, 0.0);
-        const double dxf = c.geo.dxf;
-        for (int i = 0; i <= c.nr; ++i) rc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
-        for (int i = 0; i < c.nr; ++i) re[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
+        const double dxf = c.geo.dxf, drf = c.geo.drf;
+        if (c.geo.exact) {
+            for (int i = 0; i <= c.nr; ++i) rc[i] = std::sqrt(0.75 + 2.0 * double(i)) * dxf;
+            for (int i = 0; i < c.nr; ++i) re[i + 1] = std::sqrt(0.75 + 2.0 * (double(i) + 0.5)) * dxf;
+        } else {
+            for (int i = 0; i <= c.nr; ++i) rc[i] = (double(i) + 0.5) * drf;
+            for (int i = 0; i <= c.nr; ++i) re[i] = double(i) * drf;
+        }
         c.h1["r_cc_loc"] = rc;
         c.h1["r_edge_loc"] = re;
+        if (!c.geo.exact) {
+            // dw0/dr on the bins (Source/MaestroForce.cpp:36-50), div w0 of the shells
+            // (:283-297, the last bin 0) and h0 = rhoh0 / rho0 (Source/MaestroEnthalpyAdvance.cpp:194)
+            const auto& w0 = c.h1["w0"];
+            std::vector<double> g(c.nr), dv(c.nr, 0.0), ho(c.nr), hn(c.nr);
+            for (int r = 0; r < c.nr; ++r) g[r] = (w0[r + 1] - w0[r]) / drf;
+            for (int r = 0; r < c.nr - 1; ++r) {
+                const double dr_loc = re[r + 1] - re[r];
+                dv[r] = (re[r + 1] * re[r + 1] * w0[r + 1] - re[r] * re[r] * w0[r]) / (dr_loc * rc[r] * rc[r]);
+            }
+            for (int r = 0; r < c.nr; ++r) {
+                ho[r] = c.h1["rhoh0_old"][r] / c.h1["rho0_old"][r];
+                hn[r] = c.h1["rhoh0_new"][r] / c.h1["rho0_new"][r];
+            }
+            c.h1["gradw0"] = g;
+            c.h1["divw0"] = dv;
+            c.h1["h0_old"] = ho;
+            c.h1["h0_new"] = hn;
+        }
     }
     // which_step 2 averages of MakeRhoHForce: 0.5 * (old + new) (Source/MaestroForce.cpp:496-497)
     for (int l = 0; l < nlev; ++l) {
@@ -2077,8 +2150,9 @@ int madv_est_dt(madv_ctx* h, int nlev, const madv_multifab* uold, const madv_mul
         set_error("EstDt: cfl > 0 and drdxfac >= 1");
         return MADV_ERR_PARAM;
     }
-    if (H[0].ndim != 3) {
-        set_error("EstDt: 3-D");
+    if (H[0].ndim != 3 || (H[0].sph && !H[0].geo.exact)) {
+        set_error("EstDt: 3-D, planar or spherical with the exact base state (uniform radial bins put w0 on the "
+                  "faces, Source/MaestroDt.cpp:44-64, which this entry does not)");
         return MADV_ERR_UNSUPPORTED;
     }
     set_mode(H, (cudaStream_t)stream, 0, false);
@@ -2430,9 +2504,10 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         return MADV_ERR_PARAM;
     }
     if (c.ndim != 3 || (c.P.ppm_type != 1 && c.P.ppm_type != 2) || c.P.species_pred_type != 1 ||
-        c.P.enthalpy_pred_type != 1 || c.P.ppm_trace_forces) {
+        c.P.enthalpy_pred_type != 1 || c.P.ppm_trace_forces || (c.sph && !c.geo.exact) ||
+        (c.sph && (c.geo.w0i != 2 || c.geo.w0maci != 1))) {
         set_error("the adjoint covers 3-D domains with ppm_type 1 or 2, species_pred_type 1, enthalpy_pred_type 1 "
-                  "and untraced forces");
+                  "and untraced forces; spherical with the exact base state and the default interpolation");
         return MADV_ERR_UNSUPPORTED;
     }
     // ppm_type 2: the state gradient away from walls (their boundary stencils are not transposed)

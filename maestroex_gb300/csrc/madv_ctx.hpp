@@ -19,12 +19,18 @@ struct Fail {
 };
 
 // Full-star spherical geometry: cell (i,j,k) of a level sits at prob_lo + (i + 1/2) dx - centre
-// (Source/MaestroFill3dData.cpp:103-110); cells of every level map to the radial bin
-// round(r^2 / (2 dxf^2) - 3/8) of the exact base state, dxf the finest cell size
-// (Source/MaestroBaseStateGeometry.cpp:24-35).
+// (Source/MaestroFill3dData.cpp:103-110); with the exact base state, cells of every level map
+// to the radial bin round(r^2 / (2 dxf^2) - 3/8), dxf the finest cell size
+// (Source/MaestroBaseStateGeometry.cpp:24-35); with uniform bins (use_exact_base_state = 0)
+// to int(r / drf), drf = dxf / drdxfac, and the radial arrays are interpolated
+// (Source/MaestroFill3dData.cpp:193-336).
 struct SphGeo {
     double plo[3], dx[3], ctr[3];
     double dxf;  // cell size of the finest level, which sets the radial grid
+    double drf;  // base_geom.dr_fine
+    int exact;   // use_exact_base_state
+    int nr;      // nr_fine
+    int w0i, w0maci, s0i, s0maci;  // w0_interp_type, w0mac_interp_type, s0_interp_type, s0mac_interp_type
 };
 
 struct HBox {
@@ -57,6 +63,11 @@ enum FieldId {
     F_S0CART2,                     // spherical: a base-state array on cells, two ghosts (MakeS0mac)
     F_S0MAC0, F_S0MAC1, F_S0MAC2,  // spherical: base state on faces (MakeS0mac), old
     F_S0MACB0, F_S0MACB1, F_S0MACB2,  //   and new
+    F_S0MACC0, F_S0MACC1, F_S0MACC2,  // spherical, uniform bins: rho0 on faces, old
+    F_S0MACD0, F_S0MACD1, F_S0MACD2,  //   and new (h0 on faces goes into F_S0MAC*, F_S0MACB*)
+    F_W0NODAL,                     // spherical, w0mac_interp_type 4: w0 at the nodes (3 comps)
+    F_GRADW0,                      // spherical, uniform bins: dw0/dr on cells (MakeVelForce)
+    F_DIVW0,                       // spherical, uniform bins: div w0 on cells (ModifyScalForce)
     F_IPF, F_IMF,                  // ppm_trace_forces: the traced force, 3 directional comps
     F_USER,                        // first slot of per-call views of caller FABs
     NF_INTERNAL = F_USER
@@ -254,6 +265,7 @@ void dt_maxima(Ctx& c);
 void put1d_sph(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec);
 void make_w0mac(Ctx& c);
 void make_s0mac_faces(Ctx& c, int dst0);  // faces of F_S0CART2 into dst0 .. dst0 + 2
+void make_s0mac_interp(Ctx& c, const double* d_s0, int dst0);  // s0mac_interp_type 2, 3 (uniform bins)
 void addw0_sph(Ctx& c, int f0, double mult);
 void make_vel_force_sph(Ctx& c, int fe);
 void modify_scal_force_sph(Ctx& c, int comp, int s0cart_fid, int fullform);

@@ -53,3 +53,61 @@ def test_spherical_two_levels(ppm_type):
     gpu = run_amr_stage_gpu(cfg, mode=capi.MODE_GRAPH)
     ref = pyoracle.run_stage_levels(cfg)
     assert compare_levels(cfg, gpu, ref, f"spherical 2 levels ppm{ppm_type}")
+
+
+# uniform radial bins (use_exact_base_state = 0, the reference's default): every interpolation
+# type of Put1dArrayOnCart, MakeW0mac and MakeS0mac, drdxfac, and (rho h) predicted
+UNIFORM_CASES = {
+    "defaults": {},
+    "rhoh predicted": {"enthalpy_pred_type": 0},
+    "w0 constant, s0 linear": {"w0_interp_type": 1, "s0_interp_type": 2},
+    "w0 quadratic, s0 constant": {"w0_interp_type": 3, "s0_interp_type": 1},
+    "w0mac linear, s0mac linear": {"w0mac_interp_type": 2, "s0mac_interp_type": 2},
+    "w0mac quadratic, s0mac quadratic": {"w0mac_interp_type": 3, "s0mac_interp_type": 3},
+    "w0mac nodal, drdxfac 5": {"w0mac_interp_type": 4, "drdxfac": 5},
+}
+
+
+@pytest.mark.parametrize("ppm_type", [1, 2])
+@pytest.mark.parametrize("name", list(UNIFORM_CASES))
+def test_spherical_uniform_bins(name, ppm_type):
+    kw = dict(UNIFORM_CASES[name])
+    ept = kw.pop("enthalpy_pred_type", 1)
+    cfg = configs.spherical_config(n=32, max_grid=16, ppm_type=ppm_type, exact=False, **kw)
+    cfg["enthalpy_pred_type"] = ept
+    gpu, ref = run_both(cfg, mode=capi.MODE_GRAPH)
+    worst, bitwise = compare(cfg, gpu, ref, f"spherical uniform bins, {name}, ppm{ppm_type}")
+    assert bitwise, worst
+
+
+@pytest.mark.parametrize("kw", [{"w0_interp_type": 3}, {"w0mac_interp_type": 4}, {"w0mac_interp_type": 2}])
+def test_spherical_exact_grid_interpolation_types(kw):
+    """The exact grid with the uniform-bin w0mac types (they index w0 by r / dr_fine, as the
+    reference does whatever the grid) and the quadratic w0."""
+    cfg = configs.spherical_config(n=16, max_grid=8, ppm_type=1, **kw)
+    gpu, ref = run_both(cfg)
+    worst, bitwise = compare(cfg, gpu, ref, f"spherical exact grid {kw}")
+    assert bitwise, worst
+
+
+def test_spherical_uniform_bins_two_levels():
+    from maestroex_gb300.stage import run_amr_stage_gpu
+    from test_amr_gpu import compare_levels
+    fine = configs.bubble_boxes((32, 32, 32), nbubbles=3, cover=0.12, block_edges=(4, 8), max_edge=8,
+                                rng=np.random.default_rng(5))
+    cfg = configs.spherical_amr_config(n0=32, max_grid=16, ppm_type=2, fine_boxes=fine, exact=False,
+                                       w0mac_interp_type=4)
+    gpu = run_amr_stage_gpu(cfg, mode=capi.MODE_GRAPH)
+    ref = pyoracle.run_stage_levels(cfg)
+    assert compare_levels(cfg, gpu, ref, "spherical uniform bins, 2 levels")
+
+
+def test_spherical_uniform_bins_rejections():
+    from maestroex_gb300.params import make_params
+    from maestroex_gb300.stage import ScalarAdvectionStage
+    for exact, kw in ((True, {"s0mac_interp_type": 2}), (False, {"enthalpy_pred_type": 2}),
+                      (False, {"w0mac_interp_type": 5})):
+        cfg = configs.spherical_config(n=16, max_grid=16, exact=exact)
+        cfg.update(kw)
+        with pytest.raises(capi.MadvError):
+            ScalarAdvectionStage(make_params(cfg))

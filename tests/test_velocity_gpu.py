@@ -61,6 +61,9 @@ CASES = {
                                                          bc_hi=(OUTFLOW, OUTFLOW, OUTFLOW)),
     "planar ppm0": lambda: configs.planar_config(n=(32, 32, 32), max_grid=16, ppm_type=0),
     "spherical ppm2": lambda: configs.spherical_config(n=32, max_grid=16, ppm_type=2),
+    "spherical uniform bins ppm2": lambda: configs.spherical_config(n=32, max_grid=16, ppm_type=2, exact=False),
+    "spherical uniform bins, w0mac nodal, s0 linear": lambda: configs.spherical_config(
+        n=32, max_grid=16, ppm_type=1, exact=False, w0mac_interp_type=4, s0_interp_type=2),
 }
 
 
