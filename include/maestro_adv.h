@@ -426,7 +426,8 @@ const char* madv_last_error(void);
 const char* madv_version(void);
 
 /* Maestro::MacProj (Source/MaestroMacProj.cpp:11-236, declared at Source/Maestro.H:835),
- * plane-parallel 3-D, one level.  umac[3] (>= 1 ghost face) enters with Utilde^* and leaves
+ * 3-D, one level, plane-parallel or spherical (beta0 on the faces from MakeS0mac, :41-44).
+ * umac[3] (>= 1 ghost face) enters with Utilde^* and leaves
  * with Utilde = Utilde^* - (B / beta0) grad phi, B = beta0^2 / rho_face (use_alt_energy_fix),
  * where phi solves -div(B grad phi) = macrhs - div(beta0 Utilde^*) to
  * max|residual| <= tol_rel * max|rhs| (the reference's mac_tol_rel: min(eps_mac *
@@ -434,7 +435,8 @@ const char* madv_version(void);
  * outflow Dirichlet phi = 0, other physical faces Neumann (SetMacSolverBCs).  The ghost
  * faces of umac are refilled (FillBoundary + FillUmacGhost).  rho: the density the
  * reference fills from sold (predictor) or the sold / snew average (corrector), valid
- * cells read.  macrhs: beta0 (S - Sbar), valid cells.  beta0: host array [nr].  macphi
+ * cells read.  macrhs: beta0 (S - Sbar), valid cells.  beta0: host array [nr] (spherical:
+ * the radial bins of the base state).  macphi
  * (may be NULL) receives phi on the valid cells (mean-free when no face is Dirichlet).
  * The solve is a cell-centred geometric multigrid on the level's domain (even extents).
  * Returns MADV_ERR_NOCONV if max_iter V-cycles do not reach the tolerance. */

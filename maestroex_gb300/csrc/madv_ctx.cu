@@ -2100,8 +2100,8 @@ int madv_mac_project(madv_ctx* h, const madv_multifab* umac, const madv_multifab
         set_error("madv_mac_project: umac, macrhs, rho, beta0, tol_rel > 0 and max_iter >= 1 are required");
         return MADV_ERR_PARAM;
     }
-    if (c.ndim != 3 || c.sph) {
-        set_error("madv_mac_project covers plane-parallel 3-D levels");
+    if (c.ndim != 3 || H.n() != 1) {
+        set_error("madv_mac_project covers one 3-D level, plane-parallel or spherical");
         return MADV_ERR_UNSUPPORTED;
     }
     try {
@@ -2112,10 +2112,23 @@ int madv_mac_project(madv_ctx* h, const madv_multifab* umac, const madv_multifab
             return rc;
         if ((rc = upload_user_views(c))) return rc;
         for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
-        // beta0 on the radial edges: CelltoEdge (Source/MaestroCelltoEdge.cpp:17-54)
+        if (c.sph) {  // beta0 on the faces: MakeS0mac (Source/MaestroMacProj.cpp:41-44) into F_S0MAC*
+            std::vector<double>& b = c.h1["beta0_mac"];
+            b.assign(beta0, beta0 + c.nr);
+            double*& d = c.d1["beta0_mac"];
+            if (!d && !cuda_ok(cudaMalloc(&d, sizeof(double) * (c.nr + 1)), "cudaMalloc(beta0)")) return MADV_ERR_CUDA;
+            if (!cuda_ok(cudaMemcpyAsync(d, b.data(), sizeof(double) * c.nr, cudaMemcpyHostToDevice, c.stream),
+                         "cudaMemcpyAsync(beta0)"))
+                return MADV_ERR_CUDA;
+            make_s0mac_h(H, "beta0_mac", F_S0MAC0);
+        }
+        // plane-parallel: beta0 on the radial edges, CelltoEdge (Source/MaestroCelltoEdge.cpp:17-54)
         const int nr = c.P.dom_hi[2] - c.P.dom_lo[2] + 1;
-        std::vector<double> b0(beta0, beta0 + nr), b0e(nr + 1, 0.0);
-        cell_to_edge_chunk(b0, b0e, 0, nr);
+        std::vector<double> b0(nr, 0.0), b0e(nr + 1, 0.0);  // spherical: unused (beta0 is on the faces)
+        if (!c.sph) {
+            b0.assign(beta0, beta0 + nr);
+            cell_to_edge_chunk(b0, b0e, 0, nr);
+        }
         int it = 0;
         double ratio = 0.0;
         rc = mac_project_level(c, U_FORCE, U_RHOHALF, macphi ? U_SPONGE : -1, b0.data(), b0e.data(), tol_rel, max_iter,

@@ -213,21 +213,43 @@ __global__ void k_mg_shift(double* __restrict__ x, long n, const double* __restr
     if (c < n) x[c] -= sum[0] * inv_n;
 }
 
+// beta0 on the faces: plane-parallel, beta0(k) on x / y faces and beta0_edge(k) on z faces;
+// spherical, one value per face of the domain (MakeS0mac of beta0, gathered from the boxes)
+struct MPBeta {
+    const double* b0;
+    const double* b0e;
+    const double* f[3];
+    int sph;
+};
+template <int D>
+__device__ __forceinline__ double mp_beta(const MPBeta& be, const MGGrid& g, int a0, int a1, int a2) {
+    if (be.sph) return be.f[D][mg_face<D>(g, a0, a1, a2)];
+    return D == 2 ? be.b0e[a2] : be.b0[a2];
+}
+
+// spherical: the beta0 faces of the boxes (F_S0MAC*) into the domain's face arrays; a face
+// two boxes share holds the same value in both
+template <int D>
+__global__ void k_mp_beta_faces(KARGS, MGGrid g, double* __restrict__ out, int l0, int l1, int l2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    out[mg_face<D>(g, i - l0, j - l1, k - l2)] = at(VW(F_S0MAC0 + D), i, j, k);
+}
+
 // ---- the level's FABs <-> the multigrid's arrays (domain cell (i,j,k) at i - lo0, ...)
 // Valid cells: rho into g.res (read by the coefficient kernels), the solver rhs
-// macrhs - div(beta0 umac) (ComputeMACSolverRHS after MultFacesByBeta0: x/y faces times
-// beta0(k), z faces times beta0_edge(k)), phi = 0.
-__global__ void k_mp_gather(KARGS, MGGrid g, int srhs, int srho, const double* __restrict__ b0,
-                            const double* __restrict__ b0e, double dx0, double dx1, double dx2, int l0, int l1, int l2) {
+// macrhs - div(beta0 umac) (ComputeMACSolverRHS after MultFacesByBeta0 or, spherical, the
+// product with beta0mac), phi = 0.
+__global__ void k_mp_gather(KARGS, MGGrid g, int srhs, int srho, MPBeta be, double dx0, double dx1, double dx2, int l0,
+                            int l1, int l2) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView u = VW(F_UMAC0), v = VW(F_UMAC1), w = VW(F_UMAC2);
-    const int kr = k - l2;
-    const double bz = b0[kr];
-    const long c = mg_cell(g, i - l0, j - l1, kr);
+    const int a0 = i - l0, a1 = j - l1, kr = k - l2;
+    const long c = mg_cell(g, a0, a1, kr);
     g.res[c] = at(VW(F_USER + srho), i, j, k);
-    g.rhs[c] = at(VW(F_USER + srhs), i, j, k) - ((at(u, i + 1, j, k) * bz - at(u, i, j, k) * bz) / dx0 +
-                                                 (at(v, i, j + 1, k) * bz - at(v, i, j, k) * bz) / dx1 +
-                                                 (at(w, i, j, k + 1) * b0e[kr + 1] - at(w, i, j, k) * b0e[kr]) / dx2);
+    g.rhs[c] = at(VW(F_USER + srhs), i, j, k) -
+               ((at(u, i + 1, j, k) * mp_beta<0>(be, g, a0 + 1, a1, kr) - at(u, i, j, k) * mp_beta<0>(be, g, a0, a1, kr)) / dx0 +
+                (at(v, i, j + 1, k) * mp_beta<1>(be, g, a0, a1 + 1, kr) - at(v, i, j, k) * mp_beta<1>(be, g, a0, a1, kr)) / dx1 +
+                (at(w, i, j, k + 1) * mp_beta<2>(be, g, a0, a1, kr + 1) - at(w, i, j, k) * mp_beta<2>(be, g, a0, a1, kr)) / dx2);
     g.phi[c] = 0.0;
 }
 
@@ -235,7 +257,7 @@ __global__ void k_mp_gather(KARGS, MGGrid g, int srhs, int srho, const double* _
 // g.res; across a physical face the ghost cell is the inside cell (foextrap / reflect_even;
 // only outflow's Dirichlet faces read it)
 template <int D>
-__global__ void k_mp_bcoef(MGGrid g, MGBC bc, const double* __restrict__ b0, const double* __restrict__ b0e) {
+__global__ void k_mp_bcoef(MGGrid g, MGBC bc, MPBeta be) {
     int nf[3] = {g.n[0], g.n[1], g.n[2]};
     nf[D] += 1;
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -251,7 +273,7 @@ __global__ void k_mp_bcoef(MGGrid g, MGBC bc, const double* __restrict__ b0, con
     if (m == n) r[D] = bc.hi[D] == MG_PER ? 0 : n - 1;
     const double face = 0.5 * (g.res[mg_cell(g, l[0], l[1], l[2])] + g.res[mg_cell(g, r[0], r[1], r[2])]);
     double Bv = 1.0 / face;
-    const double beta = D == 2 ? b0e[a[2]] : b0[a[2]];
+    const double beta = mp_beta<D>(be, g, a[0], a[1], a[2]);
     Bv *= beta;
     Bv *= beta;
     g.B[D][c] = Bv;
@@ -260,8 +282,7 @@ __global__ void k_mp_bcoef(MGGrid g, MGBC bc, const double* __restrict__ b0, con
 // Valid D-faces of every box: beta0 umac += -B grad phi, then umac /= beta0 (getFluxes with
 // maxorder 2: a Dirichlet face sees the ghost 2 phi_b - phi_0, phi_b = 0)
 template <int D>
-__global__ void k_mp_correct(KARGS, MGGrid g, MGBC bc, const double* __restrict__ b0, const double* __restrict__ b0e,
-                             double inv_h, int l0, int l1, int l2) {
+__global__ void k_mp_correct(KARGS, MGGrid g, MGBC bc, MPBeta be, double inv_h, int l0, int l1, int l2) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     int a[3] = {i - l0, j - l1, k - l2};
     const int m = a[D], n = g.n[D];
@@ -281,7 +302,7 @@ __global__ void k_mp_correct(KARGS, MGGrid g, MGBC bc, const double* __restrict_
         else grad = 0.0;
     }
     const double flux = -B * grad;
-    const double beta = D == 2 ? b0e[a[2]] : b0[a[2]];
+    const double beta = mp_beta<D>(be, g, a[0], a[1], a[2]);
     double& u = at(VW(F_UMAC0 + D), i, j, k);
     u = (u * beta + flux) / beta;
 }
@@ -289,6 +310,53 @@ __global__ void k_mp_correct(KARGS, MGGrid g, MGBC bc, const double* __restrict_
 __global__ void k_mp_phi_out(KARGS, MGGrid g, int sphi, int l0, int l1, int l2) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     at(VW(F_USER + sphi), i, j, k) = g.phi[mg_cell(g, i - l0, j - l1, k - l2)];
+}
+
+// ---- conjugate gradients preconditioned by one V-cycle (used where the coefficients jump by
+// orders of magnitude: spherical geometry, B ~ rho0 from the core to the ambient)
+// q = A p (p read through a copy of the grid whose phi is p)
+__global__ void k_pcg_apply(MGGrid g, MGBC bc, const double* __restrict__ p, double* __restrict__ q) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)g.n[0] * g.n[1] * g.n[2]) return;
+    int i, j, k;
+    mg_ijk(g, c, i, j, k);
+    MGGrid gp = g;
+    gp.phi = const_cast<double*>(p);
+    double off, diag;
+    mg_apply(gp, bc, i, j, k, off, diag);
+    q[c] = diag * p[c] - off;
+}
+
+// part[block] = the block's sum of x * y, in a fixed order (as k_mg_norms)
+__global__ void k_pcg_dot(const double* __restrict__ x, const double* __restrict__ y, long n, double* part) {
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x)
+        s += x[c] * y[c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += ws[w];
+        part[blockIdx.x] = b;
+    }
+}
+
+// x += a p, r -= a q
+__global__ void k_pcg_step(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                           const double* __restrict__ q, double a, long n) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    x[c] += a * p[c];
+    r[c] -= a * q[c];
+}
+
+// p = z + b p
+__global__ void k_pcg_dir(double* __restrict__ p, const double* __restrict__ z, double b, long n) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    p[c] = z[c] + b * p[c];
 }
 
 // ---- the hierarchy and the solve
@@ -300,6 +368,8 @@ struct MacMG {
     double* d_sum = nullptr;
     double* d_part = nullptr;  // per-block partial sums of k_mg_norms
     double* d_beta = nullptr;  // beta0 [nr], beta0_edge [nr + 1]
+    double* d_bface[3] = {nullptr, nullptr, nullptr};  // spherical: beta0 on the domain's faces
+    double* pcg = nullptr;  // spherical: x, r, p, q, z of the PCG, one block of ncell each
 };
 
 void mac_free(Ctx& c) {
@@ -309,6 +379,9 @@ void mac_free(Ctx& c) {
     if (c.mac->d_sum) cudaFree(c.mac->d_sum);
     if (c.mac->d_part) cudaFree(c.mac->d_part);
     if (c.mac->d_beta) cudaFree(c.mac->d_beta);
+    for (double* p : c.mac->d_bface)
+        if (p) cudaFree(p);
+    if (c.mac->pcg) cudaFree(c.mac->pcg);
     delete c.mac;
     c.mac = nullptr;
 }
@@ -370,7 +443,11 @@ static int mac_hierarchy(Ctx& c, const int n0[3], int nr) {
     if (cudaMalloc(&M.d_max, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&M.d_sum, sizeof(double)) != cudaSuccess ||
         cudaMalloc(&M.d_part, sizeof(double) * NORM_BLOCKS) != cudaSuccess ||
-        cudaMalloc(&M.d_beta, sizeof(double) * (2 * nr + 1)) != cudaSuccess) {
+        cudaMalloc(&M.d_beta, sizeof(double) * (2 * nr + 1)) != cudaSuccess ||
+        (c.sph && (cudaMalloc(&M.d_bface[0], sizeof(double) * (n0[0] + 1) * n0[1] * n0[2]) != cudaSuccess ||
+                   cudaMalloc(&M.d_bface[1], sizeof(double) * n0[0] * (n0[1] + 1) * n0[2]) != cudaSuccess ||
+                   cudaMalloc(&M.d_bface[2], sizeof(double) * n0[0] * n0[1] * (n0[2] + 1)) != cudaSuccess ||
+                   cudaMalloc(&M.pcg, sizeof(double) * 5 * (size_t)n0[0] * n0[1] * n0[2]) != cudaSuccess))) {
         set_error("cudaMalloc(MAC multigrid)");
         mac_free(c);
         return MADV_ERR_CUDA;
@@ -434,6 +511,73 @@ static int mg_norms(Ctx& c, const double* x, long n, double& amax, double* sum_o
 // MacProj on one plane-parallel level.  The caller has bound macrhs (slot srhs), rho
 // (slot srho) and macphi (slot sphi, may be < 0) and copied umac (valid faces and one
 // ghost) into F_UMAC0..2; umac is corrected there and its ghost faces refilled.
+// sum over the blocks of k_pcg_dot, read back (the stream is synchronised)
+static int pcg_dot(Ctx& c, const double* x, const double* y, long n, double& out) {
+    MacMG& M = *c.mac;
+    const unsigned nb = (unsigned)std::min<long>((n + TPB - 1) / TPB, NORM_BLOCKS);
+    k_pcg_dot<<<nb, TPB, 0, c.stream>>>(x, y, n, M.d_part);
+    k_mg_sum_parts<<<1, 1, 0, c.stream>>>(M.d_part, (int)nb, M.d_sum);
+    c.launches += 2;
+    MP_CK(cudaMemcpyAsync(&out, M.d_sum, sizeof(out), cudaMemcpyDeviceToHost, c.stream));
+    MP_CK(cudaStreamSynchronize(c.stream));
+    return MADV_OK;
+}
+
+// Conjugate gradients on A phi = rhs of the finest grid, preconditioned by one V-cycle
+// (symmetric: the post-smoothing runs the colours in reverse), from phi = 0, until
+// max|r| <= target; the flexible (Polak-Ribiere) update tolerates the fixed-sweep coarsest
+// solve.  phi ends in g.phi.  Every dot product is summed in a fixed order.
+static int mac_pcg(Ctx& c, const MGBC& bc, double target, int max_iter, int& it, double& res_max) {
+    MacMG& M = *c.mac;
+    MGGrid& g = M.lev[0];
+    const long n = ncell(g);
+    double *x = M.pcg, *r = x + n, *p = r + n, *q = p + n, *z = q + n;
+    int rc;
+    MP_CK(cudaMemsetAsync(x, 0, sizeof(double) * n, c.stream));
+    MP_CK(cudaMemcpyAsync(r, g.rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+    auto precondition = [&]() -> int {  // z = V-cycle(r) from zero
+        MP_CK(cudaMemcpyAsync(g.rhs, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+        MP_CK(cudaMemsetAsync(g.phi, 0, sizeof(double) * n, c.stream));
+        mg_vcycle(c, bc, 0);
+        MP_CK(cudaMemcpyAsync(z, g.phi, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+        return MADV_OK;
+    };
+    it = 0;
+    if ((rc = mg_norms(c, r, n, res_max, nullptr))) return rc;
+    if (res_max <= target) {
+        MP_CK(cudaMemsetAsync(g.phi, 0, sizeof(double) * n, c.stream));
+        return MADV_OK;
+    }
+    if ((rc = precondition())) return rc;
+    MP_CK(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+    double rz = 0.0;
+    if ((rc = pcg_dot(c, r, z, n, rz))) return rc;
+    while (it < max_iter) {
+        k_pcg_apply<<<blocks_of(n), TPB, 0, c.stream>>>(g, bc, p, q);
+        c.launches++;
+        double pq = 0.0;
+        if ((rc = pcg_dot(c, p, q, n, pq))) return rc;
+        if (!(pq > 0.0)) break;  // exact solution reached, or not positive definite
+        const double a = rz / pq;
+        k_pcg_step<<<blocks_of(n), TPB, 0, c.stream>>>(x, r, p, q, a, n);
+        c.launches++;
+        ++it;
+        if ((rc = mg_norms(c, r, n, res_max, nullptr))) return rc;
+        if (res_max <= target) break;
+        // z_old into q (free until the next apply), then z = M^-1 r; beta = r.(z - z_old) / rz
+        MP_CK(cudaMemcpyAsync(q, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+        if ((rc = precondition())) return rc;
+        double rz_new = 0.0, rzo = 0.0;
+        if ((rc = pcg_dot(c, r, z, n, rz_new)) || (rc = pcg_dot(c, r, q, n, rzo))) return rc;
+        const double b = (rz_new - rzo) / rz;
+        rz = rz_new;
+        k_pcg_dir<<<blocks_of(n), TPB, 0, c.stream>>>(p, z, b, n);
+        c.launches++;
+    }
+    MP_CK(cudaMemcpyAsync(g.phi, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+    return MADV_OK;
+}
+
 int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0, const double* beta0_edge,
                       double tol_rel, int max_iter, int* iters_out, double* ratio_out) {
     int n0[3], l[3];
@@ -459,16 +603,22 @@ int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0,
     int rc = mac_hierarchy(c, n0, nr);
     if (rc) return rc;
     MacMG& M = *c.mac;
-    MP_CK(cudaMemcpyAsync(M.d_beta, beta0, sizeof(double) * nr, cudaMemcpyHostToDevice, c.stream));
-    MP_CK(cudaMemcpyAsync(M.d_beta + nr, beta0_edge, sizeof(double) * (nr + 1), cudaMemcpyHostToDevice, c.stream));
-    const double *b0 = M.d_beta, *b0e = M.d_beta + nr;
     const MGGrid& g = M.lev[0];
-    launch(c, rg_grow(c, 0), 1, k_mp_gather, c.V(), g, srhs, srho, b0, b0e, c.P.dx[0], c.P.dx[1], c.P.dx[2], l[0],
-           l[1], l[2]);
+    MPBeta be{M.d_beta, M.d_beta + nr, {M.d_bface[0], M.d_bface[1], M.d_bface[2]}, c.sph ? 1 : 0};
+    if (c.sph) {  // beta0mac (F_S0MAC*, made by the caller) onto the domain's faces
+        launch(c, rg_grow(c, 0, 0), 1, k_mp_beta_faces<0>, c.V(), g, M.d_bface[0], l[0], l[1], l[2]);
+        launch(c, rg_grow(c, 0, 1), 1, k_mp_beta_faces<1>, c.V(), g, M.d_bface[1], l[0], l[1], l[2]);
+        launch(c, rg_grow(c, 0, 2), 1, k_mp_beta_faces<2>, c.V(), g, M.d_bface[2], l[0], l[1], l[2]);
+    } else {
+        MP_CK(cudaMemcpyAsync(M.d_beta, beta0, sizeof(double) * nr, cudaMemcpyHostToDevice, c.stream));
+        MP_CK(cudaMemcpyAsync(M.d_beta + nr, beta0_edge, sizeof(double) * (nr + 1), cudaMemcpyHostToDevice, c.stream));
+    }
+    launch(c, rg_grow(c, 0), 1, k_mp_gather, c.V(), g, srhs, srho, be, c.P.dx[0], c.P.dx[1], c.P.dx[2], l[0], l[1],
+           l[2]);
     auto faces = [&](long n, int d) { return n / g.n[d] * (g.n[d] + 1); };
-    k_mp_bcoef<0><<<blocks_of(faces(ncell(g), 0)), TPB, 0, c.stream>>>(g, bc, b0, b0e);
-    k_mp_bcoef<1><<<blocks_of(faces(ncell(g), 1)), TPB, 0, c.stream>>>(g, bc, b0, b0e);
-    k_mp_bcoef<2><<<blocks_of(faces(ncell(g), 2)), TPB, 0, c.stream>>>(g, bc, b0, b0e);
+    k_mp_bcoef<0><<<blocks_of(faces(ncell(g), 0)), TPB, 0, c.stream>>>(g, bc, be);
+    k_mp_bcoef<1><<<blocks_of(faces(ncell(g), 1)), TPB, 0, c.stream>>>(g, bc, be);
+    k_mp_bcoef<2><<<blocks_of(faces(ncell(g), 2)), TPB, 0, c.stream>>>(g, bc, be);
     c.launches += 3;
     for (size_t q = 1; q < M.lev.size(); ++q) {
         const MGGrid &f = M.lev[q - 1], &cg = M.lev[q];
@@ -490,13 +640,17 @@ int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0,
     const double target = tol_rel * rhs_max;
     int it = 0;
     double res_max = 0.0;
-    while (true) {
-        k_mg_resid<<<blocks_of(n), TPB, 0, c.stream>>>(g, bc);
-        c.launches++;
-        if ((rc = mg_norms(c, g.res, n, res_max, nullptr))) return rc;
-        if (res_max <= target || it >= max_iter) break;
-        mg_vcycle(c, bc, 0);
-        ++it;
+    if (!c.sph) {  // V-cycles on the residual equation until the reference's stopping test holds
+        while (true) {
+            k_mg_resid<<<blocks_of(n), TPB, 0, c.stream>>>(g, bc);
+            c.launches++;
+            if ((rc = mg_norms(c, g.res, n, res_max, nullptr))) return rc;
+            if (res_max <= target || it >= max_iter) break;
+            mg_vcycle(c, bc, 0);
+            ++it;
+        }
+    } else if ((rc = mac_pcg(c, bc, target, max_iter, it, res_max))) {
+        return rc;
     }
     if (iters_out) *iters_out = it;
     if (ratio_out) *ratio_out = rhs_max > 0.0 ? res_max / rhs_max : 0.0;
@@ -511,9 +665,9 @@ int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0,
         k_mg_shift<<<blocks_of(n), TPB, 0, c.stream>>>(g.phi, n, M.d_sum, 1.0 / (double)n);
         c.launches++;
     }
-    launch(c, rg_grow(c, 0, 0), 1, k_mp_correct<0>, c.V(), g, bc, b0, b0e, 1.0 / c.P.dx[0], l[0], l[1], l[2]);
-    launch(c, rg_grow(c, 0, 1), 1, k_mp_correct<1>, c.V(), g, bc, b0, b0e, 1.0 / c.P.dx[1], l[0], l[1], l[2]);
-    launch(c, rg_grow(c, 0, 2), 1, k_mp_correct<2>, c.V(), g, bc, b0, b0e, 1.0 / c.P.dx[2], l[0], l[1], l[2]);
+    launch(c, rg_grow(c, 0, 0), 1, k_mp_correct<0>, c.V(), g, bc, be, 1.0 / c.P.dx[0], l[0], l[1], l[2]);
+    launch(c, rg_grow(c, 0, 1), 1, k_mp_correct<1>, c.V(), g, bc, be, 1.0 / c.P.dx[1], l[0], l[1], l[2]);
+    launch(c, rg_grow(c, 0, 2), 1, k_mp_correct<2>, c.V(), g, bc, be, 1.0 / c.P.dx[2], l[0], l[1], l[2]);
     if (sphi >= 0) launch(c, rg_grow(c, 0), 1, k_mp_phi_out, c.V(), g, sphi, l[0], l[1], l[2]);
     fill_face_ghosts(c, F_UMAC0);
     return MADV_OK;

@@ -253,9 +253,10 @@ class ScalarAdvectionStage:
                                      start_comp, num_comp, C.c_void_p(s)))
 
     def mac_project(self, umac, macrhs, rho, beta0, macphi=None, tol_rel=1.0e-10, max_iter=100, stream=None):
-        """Maestro::MacProj (plane-parallel, one level): umac (3 face MultiFabs, >= 1 ghost)
-        projected in place so that div(beta0 umac) = macrhs; returns (V-cycles, final
-        max|residual| / max|rhs|).  rho, macrhs: cell MultiFabs; beta0: 1-D cell array."""
+        """Maestro::MacProj (one level, plane-parallel or spherical): umac (3 face MultiFabs,
+        >= 1 ghost) projected in place so that div(beta0 umac) = macrhs; returns (V-cycles,
+        final max|residual| / max|rhs|).  rho, macrhs: cell MultiFabs; beta0: 1-D cell array
+        (spherical: on the radial bins)."""
         s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
         b0 = np.ascontiguousarray(beta0, dtype=np.float64)
         res = capi.MadvMacResult()

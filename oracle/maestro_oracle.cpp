@@ -2692,6 +2692,12 @@ static int member(const mo_params* p, int nboxes, const int* boxes, const mo_inp
             for (int d = 0; d < 3; ++d) mf_out(f2[0][d], A(MO_SEDGE0 + d), start_comp, num_comp, 0);
             break;
         }
+        case MO_MAKE_S0MAC: {  // Maestro::MakeS0mac of rho0_old (Source/MaestroFill3dData.cpp:712-1188)
+            if (!p->spherical) throw std::runtime_error("MakeS0mac is spherical-only");
+            H.MakeS0mac(H.bs(&Lev::rho0_old), f1);
+            for (int d = 0; d < 3; ++d) mf_out(f1[0][d], A(MO_UMAC0 + d), 0, 1, 1);
+            break;
+        }
         case MO_MAKE_RHOX_FLUX:    // Maestro::MakeRhoXFlux (Source/MaestroMakeFlux.cpp:18-465)
         case MO_MAKE_RHOH_FLUX: {  // Maestro::MakeRhoHFlux (Source/MaestroMakeFlux.cpp:467-1067)
             const bool x = fn == MO_MAKE_RHOX_FLUX;

@@ -135,13 +135,16 @@ enum {
     MO_UTILDE, MO_UFULL, MO_UTRANS0, MO_UTRANS1, MO_UTRANS2, MO_UMAC0, MO_UMAC1, MO_UMAC2, MO_FORCE, MO_STATE,
     MO_SNEW, MO_SEDGE0, MO_SEDGE1, MO_SEDGE2, MO_SFLUX0, MO_SFLUX1, MO_SFLUX2, MO_ETA, MO_NSLOT
 };
-enum { MO_MAKE_UTRANS, MO_VEL_PRED, MO_MAKE_EDGE_SCAL, MO_MAKE_RHOX_FLUX, MO_MAKE_RHOH_FLUX, MO_UPDATE_SCAL };
+enum { MO_MAKE_UTRANS, MO_VEL_PRED, MO_MAKE_EDGE_SCAL, MO_MAKE_RHOX_FLUX, MO_MAKE_RHOH_FLUX, MO_UPDATE_SCAL,
+       MO_MAKE_S0MAC };
 /*   MO_MAKE_UTRANS    MakeUtrans(utilde, ufull, utrans)
  *   MO_VEL_PRED       VelPred(utilde, ufull, utrans, umac, force)
  *   MO_MAKE_EDGE_SCAL MakeEdgeScal(state, sedge, umac, force, bcs_s, start, start, num, is_conservative)
  *   MO_MAKE_RHOX_FLUX MakeRhoXFlux(sflux, etarhoflux (may be absent), sedge, umac, start, num)
  *   MO_MAKE_RHOH_FLUX MakeRhoHFlux(sflux, sedge, umac)
- *   MO_UPDATE_SCAL    UpdateScal(state, snew, sflux, force, start, num) */
+ *   MO_UPDATE_SCAL    UpdateScal(state, snew, sflux, force, start, num)
+ *   MO_MAKE_S0MAC     MakeS0mac(rho0_old, umac): spherical, the base state's rho0_old on the
+ *                     faces (one ghost face) */
 int mo_member(const mo_params* p, int nboxes, const int* boxes, const mo_inputs* base, int fn, int which_step,
               int start_comp, int num_comp, int is_conservative, const mo_fab* args);
 

@@ -1,5 +1,5 @@
-"""Test infrastructure only: the CPU oracle of Maestro::MacProj, plane-parallel 3-D, one
-level (Source/MaestroMacProj.cpp:11-236, MultFacesByBeta0 :238-329, ComputeMACSolverRHS
+"""Test infrastructure only: the CPU oracle of Maestro::MacProj, 3-D, one level,
+plane-parallel or spherical (Source/MaestroMacProj.cpp:11-236, MultFacesByBeta0 :238-329, ComputeMACSolverRHS
 :331-372, SetMacSolverBCs :424-453).  Nothing in the product library uses this file; the
 tests compare the GPU projection with it.
 
@@ -41,14 +41,14 @@ def cell_to_edge(cc):
     return e
 
 
-def mac_project(umac, macrhs, rho, beta0, dx, bc_lo, bc_hi):
+def mac_project(umac, macrhs, rho, beta0, dx, bc_lo, bc_hi, beta_faces=None):
     """umac: [x faces (nz, ny, nx+1), y faces (nz, ny+1, nx), z faces (nz+1, ny, nx)];
     macrhs, rho: (nz, ny, nx); beta0: (nz,).  bc_lo / bc_hi: PhysBCType per direction
-    (x, y, z).  Returns (projected umac, phi)."""
+    (x, y, z).  beta_faces: spherical geometry, beta0 on the faces (MakeS0mac of beta0,
+    Source/MaestroMacProj.cpp:41-44), three arrays shaped like umac, used in place of beta0
+    and its CelltoEdge.  Returns (projected umac, phi)."""
     nz, ny, nx = rho.shape
     n = (nx, ny, nz)
-    b0 = np.asarray(beta0, dtype=np.float64)
-    b0e = cell_to_edge(b0)
     per = [bc_lo[d] == INTERIOR for d in range(3)]
     kind = []  # per direction: (lo, hi) in {"per", "dir", "neu"}
     for d in range(3):
@@ -56,8 +56,14 @@ def mac_project(umac, macrhs, rho, beta0, dx, bc_lo, bc_hi):
             kind.append(("per", "per"))
         else:
             kind.append(tuple("dir" if b == OUTFLOW else "neu" for b in (bc_lo[d], bc_hi[d])))
-    # beta0 on the faces: x, y faces beta0(k), z faces beta0_edge(k)
-    bz = [b0[:, None, None], b0[:, None, None], b0e[:, None, None]]
+    # beta0 on the faces: plane-parallel, x and y faces beta0(k), z faces beta0_edge(k);
+    # spherical, the given face arrays
+    if beta_faces is None:
+        b0 = np.asarray(beta0, dtype=np.float64)
+        b0e = cell_to_edge(b0)
+        bz = [b0[:, None, None], b0[:, None, None], b0e[:, None, None]]
+    else:
+        bz = [np.asarray(b, dtype=np.float64) for b in beta_faces]
     bu = [umac[d] * bz[d] for d in range(3)]
     rhs = macrhs - ((bu[0][:, :, 1:] - bu[0][:, :, :-1]) / dx[0] + (bu[1][:, 1:, :] - bu[1][:, :-1, :]) / dx[1] +
                     (bu[2][1:, :, :] - bu[2][:-1, :, :]) / dx[2])

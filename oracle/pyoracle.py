@@ -286,7 +286,8 @@ def slopes(slope_order, d, dom, bx, s, s_lo, bcs, checked=True):
 MO_SLOT = dict(utilde=0, ufull=1, utrans=2, umac=5, force=8, state=9, snew=10, sedge=11, sflux=14, eta=17)
 MO_FACE_SLOTS = ("utrans", "umac", "sedge", "sflux")
 MO_NSLOT = 18
-MO_FN = dict(make_utrans=0, vel_pred=1, make_edge_scal=2, make_rhox_flux=3, make_rhoh_flux=4, update_scal=5)
+MO_FN = dict(make_utrans=0, vel_pred=1, make_edge_scal=2, make_rhox_flux=3, make_rhoh_flux=4, update_scal=5,
+             make_s0mac=6)
 
 
 def member(cfg, fn, args, which_step=1, start_comp=0, num_comp=0, is_conservative=0, checked=True):
