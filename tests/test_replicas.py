@@ -1,7 +1,8 @@
 """The multi-GPU form of bench.py is N independent replicas of the single-GPU stage (the
-stage has no cross-GPU exchange built): the host logic that combines the ranks -- the
-slowest rank's time and the whole-job throughput -- checked with two gloo processes on
-the CPU."""
+library's phases exchange no halos across GPUs; the box-sharding layer is
+maestroex_gb300/partition.py, tests/test_partition.py): the host logic that combines the
+ranks -- the slowest rank's time and the whole-job throughput -- checked with two gloo
+processes on the CPU."""
 import os
 import sys
 
