@@ -46,7 +46,7 @@ typedef struct {
     int ppm_type;               /* 0 (slopes), 1, 2 */
     int slope_order;            /* 0, 2, 4 (ppm_type 0) */
     int species_pred_type;      /* 1 rho'&X, 2 rhoX, 3 rho&X */
-    int enthalpy_pred_type;     /* 0 rhoh, 1 rhoh', 2 h (3-D planar and 2-D; spherical: 1) */
+    int enthalpy_pred_type;     /* 0 rhoh, 1 rhoh', 2 h (spherical with the exact base state: 1) */
     int ppm_trace_forces;       /* 0, or 1 (ppm_type 1/2, 3-D): forces traced by PPM */
     int evolve_base_state;
     int use_exact_base_state;   /* planar: 0; spherical: 1 the exact (irregular) radial grid,

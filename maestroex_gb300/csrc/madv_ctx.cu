@@ -1279,9 +1279,9 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
                   "irregular radial grid with the uniform-grid formula and read past its end)");
         return MADV_ERR_UNSUPPORTED;
     }
-    if (p->spherical && (p->dim == 2 || (p->use_exact_base_state && p->enthalpy_pred_type != 1) ||
-                         (!p->use_exact_base_state && p->enthalpy_pred_type > 1))) {
-        set_error("spherical geometry needs 3-D and enthalpy_pred_type 1 (uniform radial bins: 0 or 1)");
+    if (p->spherical && (p->dim == 2 || (p->use_exact_base_state && p->enthalpy_pred_type != 1))) {
+        set_error("spherical geometry needs 3-D, and enthalpy_pred_type 1 with the exact base state (the reference "
+                  "supports neither (rho h) nor h there, Source/MaestroMakeFlux.cpp:791-796)");
         return MADV_ERR_UNSUPPORTED;
     }
     if ((p->ppm_trace_forces != 0 && (p->ppm_trace_forces != 1 || p->ppm_type == 0 || p->dim == 2)) ||

@@ -396,10 +396,11 @@ void make_rhox_flux_sph(Ctx& c) {
 
 // MakeRhoHFlux, spherical (Source/MaestroMakeFlux.cpp:540-575, 788-1000).  Exact base state,
 // (rho h)' predicted: rhoh0 on the faces in F_S0MAC* (old) and F_S0MACB* (new).  Uniform bins:
-// (rho h) predicted (ept 0), or (rho h)' with (rho h)_0 on the faces as rho0mac * h0mac, rho0 in
-// F_S0MACC* / F_S0MACD*, h0 in F_S0MAC* / F_S0MACB*; each the LinComb 0.5 old + 0.5 new.
+// (rho h) predicted (ept 0); h predicted (ept 2), times rho0mac + rho' (species_pred_type 1) or
+// rho; or (rho h)' with (rho h)_0 on the faces as rho0mac * h0mac, rho0 in F_S0MACC* /
+// F_S0MACD*, h0 in F_S0MAC* / F_S0MACB*; each the LinComb 0.5 old + 0.5 new.
 template <int D>
-__global__ void k_rhoh_flux_sph(KARGS, int exact, int ept) {
+__global__ void k_rhoh_flux_sph(KARGS, int exact, int ept, int spt) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const double u = at(VW(F_UMAC0 + D), i, j, k), e = at(VW(F_SEDGE0 + D), i, j, k, RHOH);
     double f;
@@ -408,6 +409,10 @@ __global__ void k_rhoh_flux_sph(KARGS, int exact, int ept) {
         f = u * (rhoh0_edge + e);
     } else if (ept == 0) {
         f = u * e;
+    } else if (ept == 2) {
+        const double rho0_edge = 0.5 * at(VW(F_S0MACC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACD0 + D), i, j, k);
+        const double r = at(VW(F_SEDGE0 + D), i, j, k, RHO);
+        f = spt == 1 ? u * (rho0_edge + r) * e : u * r * e;
     } else {
         const double rho0_edge = 0.5 * at(VW(F_S0MACC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACD0 + D), i, j, k);
         const double h0_edge = 0.5 * at(VW(F_S0MAC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACB0 + D), i, j, k);
@@ -417,10 +422,10 @@ __global__ void k_rhoh_flux_sph(KARGS, int exact, int ept) {
 }
 
 void make_rhoh_flux_sph(Ctx& c) {
-    const int ex = c.geo.exact, ept = c.P.enthalpy_pred_type;
-    launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux_sph<0>, c.V(), ex, ept);
-    launch(c, rg_grow(c, 0, 1), 1, k_rhoh_flux_sph<1>, c.V(), ex, ept);
-    launch(c, rg_grow(c, 0, 2), 1, k_rhoh_flux_sph<2>, c.V(), ex, ept);
+    const int ex = c.geo.exact, ept = c.P.enthalpy_pred_type, spt = c.P.species_pred_type;
+    launch(c, rg_grow(c, 0, 0), 1, k_rhoh_flux_sph<0>, c.V(), ex, ept, spt);
+    launch(c, rg_grow(c, 0, 1), 1, k_rhoh_flux_sph<1>, c.V(), ex, ept, spt);
+    launch(c, rg_grow(c, 0, 2), 1, k_rhoh_flux_sph<2>, c.V(), ex, ept, spt);
 }
 
 }  // namespace madv

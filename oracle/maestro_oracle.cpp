@@ -1288,9 +1288,9 @@ struct Lev {
             return;
         }
         if (P.spherical) {
-            // uniform bins (Source/MaestroMakeFlux.cpp:549-575, 846-1000): rhoh predicted, or
-            // (rho h)' with (rho h)_0 on the faces as rho0mac * h0mac; rh0mac_old / _new carry
-            // h0mac here, r0mac_old / _new rho0mac
+            // uniform bins (Source/MaestroMakeFlux.cpp:549-575, 846-1000): rhoh predicted; h
+            // predicted, times (rho0mac + rho') or rho; or (rho h)' with (rho h)_0 on the faces as
+            // rho0mac * h0mac; rh0mac_old / _new carry h0mac here, r0mac_old / _new rho0mac
             for (int b = 0; b < nb; ++b)
                 for (int d = 0; d < 3; ++d) {
                     const Arr& f = sflux[d][b];
@@ -1299,6 +1299,10 @@ struct Lev {
                     MO_FOR3(nodal(L.ba[b], d)) {
                         if (ept == 0) {
                             f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, RhoH);
+                        } else if (ept == 2) {
+                            const real rho0_edge = 0.5 * r0mac_old[d][b](i, j, k) + 0.5 * r0mac_new[d][b](i, j, k);
+                            if (spt == 1) f(i, j, k, RhoH) = u(i, j, k) * (rho0_edge + e(i, j, k, Rho)) * e(i, j, k, RhoH);
+                            else f(i, j, k, RhoH) = u(i, j, k) * e(i, j, k, Rho) * e(i, j, k, RhoH);
                         } else {
                             const real rho0_edge = 0.5 * r0mac_old[d][b](i, j, k) + 0.5 * r0mac_new[d][b](i, j, k);
                             const real h0_edge = 0.5 * rh0mac_old[d][b](i, j, k) + 0.5 * rh0mac_new[d][b](i, j, k);
@@ -2232,8 +2236,8 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
     if (p->spherical) {
         if (p->use_exact_base_state && p->enthalpy_pred_type != 1)
             throw std::runtime_error("spherical with the exact base state: enthalpy_pred_type 1");
-        if (!p->use_exact_base_state && p->enthalpy_pred_type > 1)
-            throw std::runtime_error("spherical with uniform radial bins: enthalpy_pred_type 0 or 1");
+        if (!p->use_exact_base_state && p->enthalpy_pred_type > 2)
+            throw std::runtime_error("spherical with uniform radial bins: enthalpy_pred_type 0, 1 or 2");
         if (p->use_exact_base_state && p->s0mac_interp_type > 1)
             throw std::runtime_error("exact base state: s0mac_interp_type 1 (types 2 and 3 index the irregular grid "
                                      "past its end, Source/MaestroFill3dData.cpp:786-790)");

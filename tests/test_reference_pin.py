@@ -148,12 +148,16 @@ def stage_cases():
                "uniform bins, w0 quadratic, s0 constant": {"w0_interp_type": 3, "s0_interp_type": 1},
                "uniform bins, w0mac linear, s0mac linear": {"w0mac_interp_type": 2, "s0mac_interp_type": 2},
                "uniform bins, w0mac quadratic, s0mac quadratic": {"w0mac_interp_type": 3, "s0mac_interp_type": 3},
-               "uniform bins, w0mac nodal, drdxfac 5": {"w0mac_interp_type": 4, "drdxfac": 5}}
+               "uniform bins, w0mac nodal, drdxfac 5": {"w0mac_interp_type": 4, "drdxfac": 5},
+               "uniform bins, h predicted": {"enthalpy_pred_type": 2},
+               "uniform bins, h predicted, rhoX": {"enthalpy_pred_type": 2, "species_pred_type": 2}}
     for name, kw in inexact.items():
         ept = kw.pop("enthalpy_pred_type", 1)
+        spt = kw.pop("species_pred_type", 1)
         for ppm in (1, 2):
-            C[f"spherical {name} ppm{ppm}"] = lambda kw=kw, ept=ept, ppm=ppm: dict(
-                configs.spherical_config(n=16, max_grid=8, ppm_type=ppm, exact=False, **kw), enthalpy_pred_type=ept)
+            C[f"spherical {name} ppm{ppm}"] = lambda kw=kw, ept=ept, spt=spt, ppm=ppm: dict(
+                configs.spherical_config(n=16, max_grid=8, ppm_type=ppm, exact=False, **kw), enthalpy_pred_type=ept,
+                species_pred_type=spt)
     for name, kw in {"w0 constant": {"w0_interp_type": 1}, "w0 quadratic": {"w0_interp_type": 3},
                      "w0mac nodal": {"w0mac_interp_type": 4}, "w0mac quadratic": {"w0mac_interp_type": 3}}.items():
         C[f"spherical exact grid, {name}"] = lambda kw=kw: configs.spherical_config(n=16, max_grid=8, ppm_type=1, **kw)

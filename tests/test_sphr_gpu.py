@@ -65,6 +65,8 @@ UNIFORM_CASES = {
     "w0mac linear, s0mac linear": {"w0mac_interp_type": 2, "s0mac_interp_type": 2},
     "w0mac quadratic, s0mac quadratic": {"w0mac_interp_type": 3, "s0mac_interp_type": 3},
     "w0mac nodal, drdxfac 5": {"w0mac_interp_type": 4, "drdxfac": 5},
+    "h predicted": {"enthalpy_pred_type": 2},
+    "h predicted, rhoX": {"enthalpy_pred_type": 2, "species_pred_type": 2},
 }
 
 
@@ -73,8 +75,9 @@ UNIFORM_CASES = {
 def test_spherical_uniform_bins(name, ppm_type):
     kw = dict(UNIFORM_CASES[name])
     ept = kw.pop("enthalpy_pred_type", 1)
+    spt = kw.pop("species_pred_type", 1)
     cfg = configs.spherical_config(n=32, max_grid=16, ppm_type=ppm_type, exact=False, **kw)
-    cfg["enthalpy_pred_type"] = ept
+    cfg["enthalpy_pred_type"], cfg["species_pred_type"] = ept, spt
     gpu, ref = run_both(cfg, mode=capi.MODE_GRAPH)
     worst, bitwise = compare(cfg, gpu, ref, f"spherical uniform bins, {name}, ppm{ppm_type}")
     assert bitwise, worst
@@ -105,7 +108,7 @@ def test_spherical_uniform_bins_two_levels():
 def test_spherical_uniform_bins_rejections():
     from maestroex_gb300.params import make_params
     from maestroex_gb300.stage import ScalarAdvectionStage
-    for exact, kw in ((True, {"s0mac_interp_type": 2}), (False, {"enthalpy_pred_type": 2}),
+    for exact, kw in ((True, {"s0mac_interp_type": 2}), (True, {"enthalpy_pred_type": 2}),
                       (False, {"w0mac_interp_type": 5})):
         cfg = configs.spherical_config(n=16, max_grid=16, exact=exact)
         cfg.update(kw)
