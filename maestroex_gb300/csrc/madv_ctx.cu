@@ -2163,10 +2163,13 @@ int madv_est_dt(madv_ctx* h, int nlev, const madv_multifab* uold, const madv_mul
         set_error("EstDt: cfl > 0 and drdxfac >= 1");
         return MADV_ERR_PARAM;
     }
-    if (H[0].ndim != 3 || (H[0].sph && !H[0].geo.exact)) {
-        set_error("EstDt: 3-D, planar or spherical with the exact base state (uniform radial bins put w0 on the "
-                  "faces, Source/MaestroDt.cpp:44-64, which this entry does not)");
+    if (H[0].ndim != 3) {
+        set_error("EstDt: 3-D");
         return MADV_ERR_UNSUPPORTED;
+    }
+    if (H[0].sph && !H[0].geo.exact && prm->drdxfac != (H[0].P.drdxfac > 0 ? H[0].P.drdxfac : 1)) {
+        set_error("EstDt: drdxfac must be the radial grid's (madv_params.drdxfac)");
+        return MADV_ERR_PARAM;
     }
     set_mode(H, (cudaStream_t)stream, 0, false);
     reset_launches(H);

@@ -1453,7 +1453,9 @@ void update_vel(Ctx& c, int fu, int fsponge) {
 // component; component 0 in spherical geometry, as the reference reads it) and of
 // |vel_force| per direction.  The magnitudes' bit patterns order like their values, so the
 // maxima are exact: warp maxima by shuffles, then one atomicMax per warp and quantity.
-__global__ void k_dt_maxima(KARGS, int sph, int nd, unsigned long long* out) {
+// w0m: spherical with uniform bins and an evolving base state, the face w0mac averaged to the
+// cell (Source/MaestroDt.cpp:313-334); other spherical cases add 0.5 (0 + 0)
+__global__ void k_dt_maxima(KARGS, int sph, int nd, int w0m, unsigned long long* out) {
     const long gid = g0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long m[7] = {0ULL, 0ULL, 0ULL, 0ULL, 0ULL, 0ULL, 0ULL};
     if (gid < g1) {
@@ -1465,6 +1467,12 @@ __global__ void k_dt_maxima(KARGS, int sph, int nd, unsigned long long* out) {
         for (int d = 0; d < nd; ++d) {
             double v = at(u, i, j, k, d);
             if (!sph && d == nd - 1) v = v + 0.5 * (at(w0c, i, j, k, d) + at(w0c, i, j + (d == 1), k + (d == 2), d));
+            if (sph && w0m) {
+                const FabView wm = VW(F_W0MAC0 + d);
+                v = v + 0.5 * (at(wm, i, j, k) + at(wm, i + (d == 0), j + (d == 1), k + (d == 2)));
+            } else if (sph) {
+                v = v + 0.5 * (0.0 + 0.0);
+            }
             m[d] = (unsigned long long)(dbits(v) & ABS_MASK);
             m[4 + d] = (unsigned long long)(dbits(at(f, i, j, k, d)) & ABS_MASK);
         }
@@ -1484,7 +1492,8 @@ __global__ void k_dt_maxima(KARGS, int sph, int nd, unsigned long long* out) {
 }
 
 void dt_maxima(Ctx& c) {
-    launch(c, rg_grow(c, 0), 1, k_dt_maxima, c.V(), (int)c.sph, c.ndim, c.d_red);
+    const int w0m = c.sph && !c.geo.exact && c.P.evolve_base_state;
+    launch(c, rg_grow(c, 0), 1, k_dt_maxima, c.V(), (int)c.sph, c.ndim, w0m, c.d_red);
 }
 
 void update_scal(Ctx& c, int start_comp) {

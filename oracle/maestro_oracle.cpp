@@ -2131,12 +2131,19 @@ struct Stage {
             for (int b = 0; b < L.nb; ++b) {
                 const Arr &u = uold[lev][b], &w0c = L.w0_cart[b], &f = vel_force[lev][b];
                 double spd[3] = {0.0, 0.0, 0.0}, spdr = 0.0, fm[3] = {0.0, 0.0, 0.0};
+                // spherical: w0mac from MakeW0mac with uniform bins and an evolving base
+                // state, else 0 (Source/MaestroDt.cpp:42-64, 313-334)
+                const bool w0m = P.spherical && !P.use_exact_base_state && P.evolve_base_state;
                 MO_FOR3(L.L.ba[b]) {
                     for (int d = 0; d < nd; ++d) {
                         real v = u(i, j, k, d);
                         if (!P.spherical && d == nd - 1)
                             v = u(i, j, k, d) + 0.5 * (w0c(i, j, k, d) + w0c(i, j + (d == 1), k + (d == 2), d));
-                        if (P.spherical) v = u(i, j, k, d) + 0.5 * (0.0 + 0.0);  // w0mac = 0
+                        if (P.spherical && w0m)
+                            v = u(i, j, k, d) + 0.5 * (L.w0mac[d][b](i, j, k) +
+                                                       L.w0mac[d][b](i + (d == 0), j + (d == 1), k + (d == 2)));
+                        else if (P.spherical)
+                            v = u(i, j, k, d) + 0.5 * (0.0 + 0.0);
                         spd[d] = std::max(spd[d], std::fabs(value_of(v)));
                         fm[d] = std::max(fm[d], std::fabs(value_of(f(i, j, k, d))));
                     }

@@ -52,3 +52,18 @@ def test_est_dt_two_levels_and_limits():
     assert st.est_dt(*lv, fixed_dt=123.0)[0] == 123.0
     with pytest.raises(MadvError):
         st.est_dt(*lv, small_dt=2.0 * dt)
+
+
+@pytest.mark.parametrize("kw", [{}, {"w0mac_interp_type": 4, "drdxfac": 2}])
+def test_est_dt_spherical_uniform_bins(kw):
+    """Uniform radial bins with an evolving base state: the velocity limit adds w0mac
+    (MakeW0mac) averaged to the cells; the radial spacing is the bins' dr."""
+    cfg = configs.spherical_config(n=32, max_grid=16, ppm_type=1, exact=False, **kw)
+    st = make_stage(cfg)
+    buf = StageBuffers(cfg).load(cfg)
+    f = kw.get("drdxfac", 1)
+    dt, dt_est, umax, rel_eps = st.est_dt(buf.uold, buf.sold, buf.gpi, cfl=0.7, drdxfac=f)
+    rdt, rumax = pyoracle.est_dt(cfg, cfl=0.7, drdxfac=f)
+    assert dt == rdt and umax == rumax
+    with pytest.raises(MadvError):  # the radial grid's drdxfac only
+        st.est_dt(buf.uold, buf.sold, buf.gpi, cfl=0.7, drdxfac=f + 1)
