@@ -36,6 +36,9 @@ struct MGGrid {
     int n[3];
     double ih2[3];  // 1 / h_d^2
     double *phi, *rhs, *res, *B[3];
+    // the operator's weights, formed once per solve (k_mg_prep): W_d = B_d / h_d^2 on every
+    // face, and per cell the diagonal and its reciprocal (0 where the diagonal is 0)
+    double *W[3], *diag, *idiag;
 };
 struct MGBC {
     int lo[3], hi[3];
@@ -106,7 +109,56 @@ __device__ __forceinline__ void mg_apply(const MGGrid& g, const MGBC& bc, int i,
 #undef MG_TERM
 }
 
-// Gauss-Seidel on the cells of one colour ((i + j + k) % 2 == color)
+// sum_f W_f phi_nb over the faces of cell (i,j,k) with a neighbour (interior and periodic
+// faces), in mg_apply's order, from the stored weights
+__device__ __forceinline__ double mg_off(const MGGrid& g, const MGBC& bc, const double* __restrict__ phi, int i,
+                                         int j, int k) {
+    double off = 0.0;
+    const int idx[3] = {i, j, k};
+#pragma unroll
+    for (int D = 0; D < 3; ++D)
+#pragma unroll
+        for (int hi = 0; hi < 2; ++hi) {
+            const int m = idx[D], n = g.n[D];
+            const bool edge = hi ? (m == n - 1) : (m == 0);
+            int b[3] = {i, j, k};
+            if (!edge) {
+                b[D] = hi ? m + 1 : m - 1;
+            } else if ((hi ? bc.hi[D] : bc.lo[D]) == MG_PER) {
+                b[D] = hi ? 0 : n - 1;
+            } else {
+                continue;
+            }
+            int a[3] = {i, j, k};
+            a[D] = hi ? m + 1 : m;
+            const long f = D == 0 ? mg_face<0>(g, a[0], a[1], a[2])
+                                  : (D == 1 ? mg_face<1>(g, a[0], a[1], a[2]) : mg_face<2>(g, a[0], a[1], a[2]));
+            off += g.W[D][f] * phi[mg_cell(g, b[0], b[1], b[2])];
+        }
+    return off;
+}
+
+// W_d = B_d / h_d^2 on the faces of direction D
+template <int D>
+__global__ void k_mg_prep_w(MGGrid g) {
+    long nf = (long)g.n[0] * g.n[1] * g.n[2] / g.n[D] * (g.n[D] + 1);
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nf) g.W[D][c] = g.B[D][c] * g.ih2[D];
+}
+
+// the diagonal of every cell (mg_apply's sum, Dirichlet faces doubled) and its reciprocal
+__global__ void k_mg_prep_diag(MGGrid g, MGBC bc) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)g.n[0] * g.n[1] * g.n[2]) return;
+    int i, j, k;
+    mg_ijk(g, c, i, j, k);
+    double off, diag;
+    mg_apply(g, bc, i, j, k, off, diag);
+    g.diag[c] = diag;
+    g.idiag[c] = diag > 0.0 ? 1.0 / diag : 0.0;
+}
+
+// Gauss-Seidel on the cells of one colour ((i + j + k) % 2 == color), from the stored weights
 __global__ void k_mg_smooth(MGGrid g, MGBC bc, int color) {
     const long half = (long)g.n[0] * g.n[1] * g.n[2] / 2;
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -115,10 +167,9 @@ __global__ void k_mg_smooth(MGGrid g, MGBC bc, int color) {
     const long row = t / (g.n[0] / 2);
     const int jj = (int)(row % g.n[1]), kk = (int)(row / g.n[1]);
     const int ii = 2 * (int)(t % (g.n[0] / 2)) + ((jj + kk + color) & 1);
-    double off, diag;
-    mg_apply(g, bc, ii, jj, kk, off, diag);
     const long c = mg_cell(g, ii, jj, kk);
-    if (diag > 0.0) g.phi[c] = (g.rhs[c] + off) / diag;
+    const double id = g.idiag[c];
+    if (id > 0.0) g.phi[c] = (g.rhs[c] + mg_off(g, bc, g.phi, ii, jj, kk)) * id;
 }
 
 // res = rhs - A phi
@@ -127,9 +178,7 @@ __global__ void k_mg_resid(MGGrid g, MGBC bc) {
     if (c >= (long)g.n[0] * g.n[1] * g.n[2]) return;
     int i, j, k;
     mg_ijk(g, c, i, j, k);
-    double off, diag;
-    mg_apply(g, bc, i, j, k, off, diag);
-    g.res[c] = g.rhs[c] - (diag * g.phi[c] - off);
+    g.res[c] = g.rhs[c] - (g.diag[c] * g.phi[c] - mg_off(g, bc, g.phi, i, j, k));
 }
 
 // coarse rhs = mean of the 8 fine residuals; coarse phi = 0
@@ -320,11 +369,7 @@ __global__ void k_pcg_apply(MGGrid g, MGBC bc, const double* __restrict__ p, dou
     if (c >= (long)g.n[0] * g.n[1] * g.n[2]) return;
     int i, j, k;
     mg_ijk(g, c, i, j, k);
-    MGGrid gp = g;
-    gp.phi = const_cast<double*>(p);
-    double off, diag;
-    mg_apply(gp, bc, i, j, k, off, diag);
-    q[c] = diag * p[c] - off;
+    q[c] = g.diag[c] * p[c] - mg_off(g, bc, p, i, j, k);
 }
 
 // part[block] = the block's sum of x * y, in a fixed order (as k_mg_norms)
@@ -419,8 +464,14 @@ static int mac_hierarchy(Ctx& c, const int n0[3], int nr) {
         g.phi = alloc(nc);
         g.rhs = alloc(nc);
         g.res = alloc(nc);
-        for (int d = 0; d < 3; ++d) g.B[d] = alloc(nc / n[d] * (n[d] + 1));
-        if (!g.phi || !g.rhs || !g.res || !g.B[0] || !g.B[1] || !g.B[2]) {
+        g.diag = alloc(nc);
+        g.idiag = alloc(nc);
+        for (int d = 0; d < 3; ++d) {
+            g.B[d] = alloc(nc / n[d] * (n[d] + 1));
+            g.W[d] = alloc(nc / n[d] * (n[d] + 1));
+        }
+        if (!g.phi || !g.rhs || !g.res || !g.diag || !g.idiag || !g.B[0] || !g.B[1] || !g.B[2] || !g.W[0] || !g.W[1] ||
+            !g.W[2]) {
             set_error("cudaMalloc(MAC multigrid)");
             mac_free(c);
             return MADV_ERR_CUDA;
@@ -627,6 +678,14 @@ int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0,
         k_mg_coarsen_b<1><<<blocks_of(nc / cg.n[1] * (cg.n[1] + 1)), TPB, 0, c.stream>>>(f, cg);
         k_mg_coarsen_b<2><<<blocks_of(nc / cg.n[2] * (cg.n[2] + 1)), TPB, 0, c.stream>>>(f, cg);
         c.launches += 3;
+    }
+    for (const MGGrid& q : M.lev) {  // the weights and diagonals every sweep reads
+        const long nc = ncell(q);
+        k_mg_prep_w<0><<<blocks_of(nc / q.n[0] * (q.n[0] + 1)), TPB, 0, c.stream>>>(q);
+        k_mg_prep_w<1><<<blocks_of(nc / q.n[1] * (q.n[1] + 1)), TPB, 0, c.stream>>>(q);
+        k_mg_prep_w<2><<<blocks_of(nc / q.n[2] * (q.n[2] + 1)), TPB, 0, c.stream>>>(q);
+        k_mg_prep_diag<<<blocks_of(nc), TPB, 0, c.stream>>>(q, bc);
+        c.launches += 4;
     }
     const long n = ncell(g);
     if (!dirichlet) {  // singular: the rhs made mean-free
