@@ -1287,7 +1287,8 @@ int madv_ctx_create(const madv_params* p, madv_ctx** out) {
     if ((p->ppm_trace_forces != 0 && (p->ppm_trace_forces != 1 || p->ppm_type == 0 || p->dim == 2)) ||
         (p->use_exact_base_state != 0 && !p->spherical)) {
         set_error("ppm_trace_forces = 1 needs ppm_type 1 or 2 in 3-D (with ppm_type 0 the reference reads forces it "
-                  "never traced); use_exact_base_state needs spherical geometry");
+                  "never traced; its 2-D VelPred reads force traces it never writes); use_exact_base_state needs "
+                  "spherical geometry");
         return MADV_ERR_UNSUPPORTED;
     }
     if (p->reflux_type < 0 || p->reflux_type > 2 || (p->reflux_type == 2 && p->dim == 2)) {
