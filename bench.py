@@ -861,7 +861,7 @@ def run_2d(args, barrier):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
@@ -992,13 +992,23 @@ def main():
     ms_batched = timed(capi.MODE_BATCHED, max(1, args.steps // 2), 1)
     ms_perbox = None if args.no_per_box else timed(capi.MODE_PER_BOX, max(1, args.steps // 2), 1)
 
-    # end to end through the public API: every step copies its inputs (uold, sold, gpi) from
-    # pinned host memory and its result (snew) back.  Two device buffer sets pipeline the
-    # steps: step n+1's inputs travel on one copy stream while step n computes, and step n's
-    # result travels back on another while step n+1 computes.
-    host = {name: [t.cpu().pin_memory() for t in ts] for name, ts in snap.items()}
+    # end to end through the public API: every step copies its inputs (uold, sold, gpi: the
+    # valid cells of every box, which is all the stage reads of them) from pinned host memory
+    # and its result (snew's valid cells) back.  Two device buffer sets pipeline the steps:
+    # step n+1's inputs travel on one copy stream while step n computes, and step n's result
+    # travels back on another while step n+1 computes; each box's valid cells cross the bus
+    # as one contiguous block, unpacked into (or packed from) the FAB on the device.
+    def valid(mf, b):
+        fs, _ = mf._slices(b)
+        return mf.fabs[b][(slice(None),) + fs]
+
+    host = {name: [snap[name][b][(slice(None),) + getattr(buf, name)._slices(b)[0]].cpu().contiguous().pin_memory()
+                   for b in range(len(cfg["boxes"]))] for name in ("uold", "sold", "gpi")}
     sets = [buf, StageBuffers(cfg).load(cfg)]
-    host_out = [[t.detach().cpu().pin_memory() for t in b.snew.fabs] for b in sets]
+    stage_in = {name: [torch.empty_like(t, device="cuda") for t in ts] for name, ts in host.items()}
+    nb = len(cfg["boxes"])
+    host_out = [[valid(b.snew, q).cpu().contiguous().pin_memory() for q in range(nb)] for b in sets]
+    stage_out = [torch.empty_like(t, device="cuda") for t in host_out[0]]
     h2d = sum(t.numel() * 8 for v in host.values() for t in v)
     d2h = sum(t.numel() * 8 for t in host_out[0])
     comp = torch.cuda.current_stream()
@@ -1012,8 +1022,10 @@ def main():
         with torch.cuda.stream(s_in):
             s_in.wait_event(ev_out[k % 2])  # this set's previous result has left the device
             for name, hs in host.items():
-                for dst, src in zip(getattr(bk, name).fabs, hs):
-                    dst.copy_(src, non_blocking=True)
+                mf = getattr(bk, name)
+                for q, (tmp, src) in enumerate(zip(stage_in[name], hs)):
+                    tmp.copy_(src, non_blocking=True)
+                    valid(mf, q).copy_(tmp)
             ev_in[k % 2].record(s_in)
 
     def compute_and_copy_out(k):
@@ -1024,8 +1036,9 @@ def main():
         ev_done[k % 2].record(comp)
         with torch.cuda.stream(s_out):
             s_out.wait_event(ev_done[k % 2])
-            for dst, src in zip(host_out[k % 2], bk.snew.fabs):
-                dst.copy_(src, non_blocking=True)
+            for q, (dst, tmp) in enumerate(zip(host_out[k % 2], stage_out)):
+                tmp.copy_(valid(bk.snew, q))
+                dst.copy_(tmp, non_blocking=True)
             ev_out[k % 2].record(s_out)
 
     def pipeline(n0, n):
@@ -1103,7 +1116,8 @@ def main():
         "clocks": clocks,
         "e2e": {"value": ws * ncell / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "mode": "madv_stage_forward (batched) per step on pinned host inputs, copies pipelined against "
+                "mode": "madv_stage_forward (batched) per step; the valid cells of uold, sold, gpi copied in from "
+                        "pinned host memory and snew's copied out, each box one contiguous block, pipelined against "
                         "the neighbouring steps' compute on two copy streams"},
         "gpu_launches": launches * args.steps,
         "per_box": {"value": ws * ncell / (ms_perbox * 1e-3) if ms_perbox else None,
