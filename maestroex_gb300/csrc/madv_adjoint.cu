@@ -14,7 +14,7 @@
 // adjoint FABs, which have the forward FABs' index spaces (and zero-filled margins
 // wherever a transpose reads one cell past the forward region).
 //
-// Scope: 3-D, one level, plane-parallel or spherical, MAC velocities independent of the
+// Scope: 3-D, one level, plane-parallel or spherical (either radial grid), MAC velocities independent of the
 // state (grav_cell = 0, no pressure gradient), so the velocity force has no state term.
 // The state gradient allows w0 != 0 and outflow, symmetry and wall boundaries (scalar BCs
 // foextrap, reflect_even, hoextrap: PPM's boundary stencils transposed; ppm_type 2 without
@@ -874,8 +874,10 @@ __global__ void k_adj_pert(KARGS, int comp, const double* __restrict__ s0a, cons
     const double du = div_c(U(um, 0, i + 1, j, k) - U(um, 0, i, j, k), r0);
     const double dv = div_c(U(vm, 1, i, j + 1, k) - U(vm, 1, i, j, k), r1);
     double divu = du + dv + div_c(U(wm, 2, i, j, k + 1) - U(wm, 2, i, j, k), r2);
-    // planar: ModifyScalForce adds the divergence of w0_cart (Source/MaestroForce.cpp:413-441)
+    // planar: ModifyScalForce adds the divergence of w0_cart (Source/MaestroForce.cpp:413-441);
+    // spherical on uniform bins, div w0 of the shells on the cells (:283-305; sph == 2)
     if (!sph) divu += div_c(at(VW(F_W0CART), i, j, k + 1, 2) - at(VW(F_W0CART), i, j, k, 2), r2);
+    if (sph == 2) divu = divu + at(VW(F_DIVW0), i, j, k);
     const double fb = at(AW(A_AFORCE), i, j, k);
     at(AW(A_ASOLD), i, j, k, comp) += at(AW(A_AS), i, j, k) - divu * fb;
     if (want_u && fb != 0.0) {
@@ -1167,7 +1169,8 @@ void adj_pert_force(Ctx& c, int comp, int want_u) {
     const double* s0 = c.b1(comp == RHO ? "rho0_old" : "rhoh0_old");
     const double* s0e = c.b1(comp == RHO ? "rho0_edge_old" : "rhoh0_edge_old");
     launch(c, rg_grow(c, 0), 1, k_adj_pert, c.V(), comp, s0, s0e, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
-           make_recip(c.P.dx[2]), c.P.dom_lo[2], c.P.dom_hi[2], want_u, c.b1("w0"), c.sph ? 1 : 0);
+           make_recip(c.P.dx[2]), c.P.dom_lo[2], c.P.dom_hi[2], want_u, c.b1("w0"),
+           c.sph ? (c.geo.exact ? 1 : 2) : 0);
 }
 
 // F_TCOEF^T into face slots ts .. ts+2 (A_AUMAC0 or A_AUTRANS0)

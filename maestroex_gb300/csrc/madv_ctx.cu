@@ -2521,10 +2521,9 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         return MADV_ERR_PARAM;
     }
     if (c.ndim != 3 || (c.P.ppm_type != 1 && c.P.ppm_type != 2) || c.P.species_pred_type != 1 ||
-        c.P.enthalpy_pred_type != 1 || c.P.ppm_trace_forces || (c.sph && !c.geo.exact) ||
-        (c.sph && (c.geo.w0i != 2 || c.geo.w0maci != 1))) {
+        c.P.enthalpy_pred_type != 1 || c.P.ppm_trace_forces) {
         set_error("the adjoint covers 3-D domains with ppm_type 1 or 2, species_pred_type 1, enthalpy_pred_type 1 "
-                  "and untraced forces; spherical with the exact base state and the default interpolation");
+                  "and untraced forces");
         return MADV_ERR_UNSUPPORTED;
     }
     // ppm_type 2: the state gradient away from walls (their boundary stencils are not transposed)
