@@ -690,12 +690,13 @@ def run_spherical_adjoint(args, barrier):
     }
 
 
-def run_spherical(args, barrier):
+def run_spherical(args, barrier, exact=True):
     """Full-star spherical workload: two levels, level 0 n^3 in uneven
     boxes (edges 16-128), level 1 (ratio 2) 16-64-cell boxes around 3 seeded bubbles, NumSpec
     21, ppm_type 2, exact base state on the fine level's irregular radial grid, polytrope
     star, outflow faces; the level-1 state injected from level 0.  Graph-replayed stage vs
-    one launch per box, identical results checked."""
+    one launch per box, identical results checked.  exact=False: the same on uniform radial
+    bins with the reference's default interpolation types (graph mode only)."""
     import torch
     from maestroex_gb300 import capi, configs
     from maestroex_gb300.stage import amr_buffers, make_amr_stage
@@ -704,7 +705,8 @@ def run_spherical(args, barrier):
     l0 = configs.uneven_boxes((n, n, n), [16, 32, 48, 64, 96, 128], rng, p_stop=0.8)
     fine = configs.bubble_boxes((n, n, n), nbubbles=3, cover=args.sph_cover, block_edges=(8, 16, 24, 32),
                                 max_edge=32, rng=np.random.default_rng(20261203 + 51))
-    cfg = configs.spherical_amr_config(n0=n, nspec=21, ppm_type=2, fine_boxes=fine, level0_boxes=l0, inject=True)
+    cfg = configs.spherical_amr_config(n0=n, nspec=21, ppm_type=2, fine_boxes=fine, level0_boxes=l0, inject=True,
+                                       exact=exact)
     st = make_amr_stage(cfg)
     bufs = amr_buffers(cfg)
     names = ("uold", "sold", "gpi")
@@ -737,24 +739,27 @@ def run_spherical(args, barrier):
 
     reps = max(1, args.steps // 2)
     ms_graph, l_graph = timed(capi.MODE_GRAPH, reps)
-    out_graph = [[f.cpu() for f in b.snew.fabs] for b in bufs]
-    ms_box, l_box = timed(capi.MODE_PER_BOX, reps)
-    same = all(torch.equal(a, f.cpu()) for og, b in zip(out_graph, bufs) for a, f in zip(og, b.snew.fabs))
     cells = [n ** 3, sum((b[3] - b[0] + 1) * (b[4] - b[1] + 1) * (b[5] - b[2] + 1) for b in fine)]
     ncell = sum(cells)
+    grid = (f"exact base state ({cfg['nr']} radial bins on the fine grid)" if exact else
+            f"uniform radial bins ({cfg['nr']} of dx_fine), w0 linear, s0 quadratic, w0mac / s0mac face averages")
+    res = {"workload": f"spherical full star, two levels: level 0 {n}^3 in {len(l0)} uneven boxes (edges 16-128), "
+                       f"level 1 (ratio 2) {len(fine)} boxes around 3 bubbles ({cells[1] / 8 / cells[0]:.3f} of "
+                       f"the domain), NumSpec 21, ppm_type 2, {grid}, n = 1.5 polytrope (rho_c 2e9, radius "
+                       "0.9 L/2), outflow; level-1 state injected from level 0",
+           "cells_per_level": cells, "unit": UNIT,
+           "graph": {"value": ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": l_graph}}
+    if exact:
+        out_graph = [[f.cpu() for f in b.snew.fabs] for b in bufs]
+        ms_box, l_box = timed(capi.MODE_PER_BOX, reps)
+        same = all(torch.equal(a, f.cpu()) for og, b in zip(out_graph, bufs) for a, f in zip(og, b.snew.fabs))
+        res.update({"per_box": {"value": ncell / (ms_box * 1e-3), "ms_per_step": ms_box, "gpu_launches": l_box},
+                    "speedup_graph_vs_per_box": ms_box / ms_graph,
+                    "identical_results_graph_vs_per_box": bool(same)})
     st.close()
     del bufs, snap
     torch.cuda.empty_cache()
-    return {"workload": f"spherical full star, two levels: level 0 {n}^3 in {len(l0)} uneven boxes (edges 16-128), "
-                        f"level 1 (ratio 2) {len(fine)} boxes around 3 bubbles ({cells[1] / 8 / cells[0]:.3f} of "
-                        f"the domain), NumSpec 21, ppm_type 2, exact base state ({cfg['nr']} radial bins on the "
-                        "fine grid), n = 1.5 polytrope (rho_c 2e9, radius 0.9 L/2), outflow; level-1 state "
-                        "injected from level 0",
-            "cells_per_level": cells, "unit": UNIT,
-            "graph": {"value": ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": l_graph},
-            "per_box": {"value": ncell / (ms_box * 1e-3), "ms_per_step": ms_box, "gpu_launches": l_box},
-            "speedup_graph_vs_per_box": ms_box / ms_graph,
-            "identical_results_graph_vs_per_box": bool(same)}
+    return res
 
 
 def run_velocity(args, barrier):
@@ -1092,6 +1097,7 @@ def main():
     two_d = leg("two_d", args.no_2d, lambda: run_2d(args, barrier))
     vel = leg("velocity_advance", args.no_velocity, lambda: run_velocity(args, barrier))
     sph = leg("spherical", args.no_spherical, lambda: run_spherical(args, barrier))
+    sph_u = leg("spherical_uniform_bins", args.no_spherical, lambda: run_spherical(args, barrier, exact=False))
     sph_adj = leg("spherical_adjoint", args.no_sph_adjoint, lambda: run_spherical_adjoint(args, barrier))
     mac = leg("mac_projection", args.no_mac, lambda: run_mac_projection(args, barrier))
 
@@ -1149,6 +1155,8 @@ def main():
         line["velocity_advance"] = vel
     if sph is not None:
         line["spherical"] = sph
+    if sph_u is not None:
+        line["spherical_uniform_bins"] = sph_u
     if sph_adj is not None:
         line["spherical_adjoint"] = sph_adj
     if mac is not None:

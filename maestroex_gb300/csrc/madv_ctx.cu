@@ -1423,9 +1423,15 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
         }
     // radial chunks per level (BaseStateGeometry::InitMultiLevel, planar, Source/BaseStateGeometry.cpp:355-382):
     // rows of level l-1 lying under a level-l box are tagged; each run of tagged rows r0..r1
-    // is the level-l chunk [2 r0, 2 r1 + 1]
+    // is the level-l chunk [2 r0, 2 r1 + 1].  Spherical: one radial level (max_radial_level 0,
+    // Source/MaestroSetup.cpp:65) that every level reads whole, so one chunk of all nr bins
+    const bool sph = H[0].sph;
     H[0].chunks.assign(1, {0, H[0].nr - 1});
     for (int l = 1; l < nlev; ++l) {
+        if (sph) {
+            H[l].chunks.assign(1, {0, H[l].nr - 1});
+            continue;
+        }
         const int nrc = H[l - 1].nr;
         std::vector<int> tag(nrc, 0);
         for (auto& b : H[l].ba)
@@ -1522,13 +1528,14 @@ int madv_set_base_state_levels(madv_ctx* h, int nlev, const madv_base_state* bsl
             for (auto& ch : H[l].chunks) cell_to_edge_chunk(H[l].h1[name], e, ch[0], ch[1] + 1);
             H[l].h1[en] = e;
         }
-        for (int l = nlev - 1; l >= 1; --l)
+        for (int l = nlev - 1; l >= 1 && !sph; --l)
             for (auto& ch : H[l].chunks)
                 for (int j = ch[0]; j <= ch[1] + 1; j += 2) H[l - 1].h1[en][j / 2] = H[l].h1[en][j];
     }
     // BaseStateGeometry::ComputeCutoffCoords, base cutoff (Source/BaseStateGeometry.cpp:164-210);
-    // one level keeps the caller's base_cutoff_density_coord
-    if (nlev > 1) {
+    // one level, and spherical geometry (one radial level; no spherical kernel reads the
+    // coordinate), keep the caller's base_cutoff_density_coord
+    if (nlev > 1 && !sph) {
         bool found = false;
         int which = 0;
         std::vector<int> coord(nlev, 0);

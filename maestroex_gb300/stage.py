@@ -444,30 +444,55 @@ def amr_buffers(cfg, device="cuda"):
 
 
 def _sph_rebin(blk, bx, fine, coarse):
-    """Spherical injection: a fine cell falls in its own radial bin, so the injected density,
-    species and enthalpy are rescaled by the ratio of the base state of the fine cell's bin to
-    that of its parent's bin (the perturbation relative to the base state is what is
-    injected)."""
+    """Spherical injection: the injected density, species and enthalpy are rescaled by the
+    ratio of the base state at the fine cell's centre to that at its parent's centre (the
+    perturbation relative to the base state is what is injected).  The base state at a cell
+    is its radial bin's value on the exact grid, and on uniform bins the Put1dArrayOnCart
+    interpolation of s0_interp_type the state was laid on."""
     dev = blk.device
     L = fine["prob_hi"][0] - fine["prob_lo"][0]
     dxf = fine["dx"][0]
+    exact = fine.get("use_exact_base_state", 1)
+    drf = dxf / fine.get("drdxfac", 1)
+    t = fine.get("s0_interp_type", 3)
 
-    def bins(lo, hi, dx, refine):
+    def radius2(lo, hi, dx, refine):
         ax = [(torch.arange(lo[d], hi[d] + 1, device=dev, dtype=torch.float64) // refine + 0.5) * dx -
               0.5 * L for d in range(3)]
-        r2 = ax[2][:, None, None] ** 2 + ax[1][None, :, None] ** 2 + ax[0][None, None, :] ** 2
-        return torch.floor(r2 / (2.0 * dxf * dxf) - 0.375 + 0.5).long()
+        return ax[2][:, None, None] ** 2 + ax[1][None, :, None] ** 2 + ax[0][None, None, :] ** 2
+
+    def on_cells(s0, r2):
+        if exact:  # the exact grid's bin of the cell centre
+            return s0[torch.floor(r2 / (2.0 * dxf * dxf) - 0.375 + 0.5).long()]
+        nr = s0.numel()
+        r = torch.sqrt(r2)
+        index = (r / drf).long()
+        if t == 1:
+            return s0[torch.clamp(index, max=nr - 1)]
+        rcc = (torch.arange(nr, device=dev, dtype=torch.float64) + 0.5) * drf
+        if t == 2:  # linear between the two nearest bin centres, constant past the ends
+            i = torch.clamp(torch.searchsorted(rcc, r) - 1, 0, nr - 2)
+            x0, x1 = rcc[i], rcc[i + 1]
+            w = torch.clamp((r - x0) / (x1 - x0), 0.0, 1.0)
+            return s0[i] + w * (s0[i + 1] - s0[i])
+        i = torch.clamp(index, 1, nr - 2)  # quadratic through three bins, clipped to their range
+        x0, x1, x2 = rcc[i - 1], rcc[i], rcc[i + 1]
+        y0, y1, y2 = s0[i - 1], s0[i], s0[i + 1]
+        y = (y0 + (y1 - y0) / (x1 - x0) * (r - x0) +
+             ((y2 - y1) / (x2 - x1) - (y1 - y0) / (x1 - x0)) / (x2 - x0) * (r - x0) * (r - x1))
+        return torch.minimum(torch.maximum(y, torch.minimum(y0, torch.minimum(y1, y2))),
+                             torch.maximum(y0, torch.maximum(y1, y2)))
 
     lo, hi = bx[:3], bx[3:]
-    bf = bins(lo, hi, dxf, 1)
-    bc = bins(lo, hi, 2.0 * dxf, 2)
+    rf2 = radius2(lo, hi, dxf, 1)
+    rc2 = radius2(lo, hi, 2.0 * dxf, 2)
     r0 = torch.from_numpy(np.ascontiguousarray(fine["rho0_old"])).to(dev)
     h0 = torch.from_numpy(np.ascontiguousarray(fine["rhoh0_old"])).to(dev)
     out = blk.clone()
-    fr = r0[bf] / r0[bc]
+    fr = on_cells(r0, rf2) / on_cells(r0, rc2)
     out[0] *= fr
     out[4:] *= fr[None]
-    out[1] *= h0[bf] / h0[bc]
+    out[1] *= on_cells(h0, rf2) / on_cells(h0, rc2)
     return out
 
 

@@ -1572,11 +1572,16 @@ struct Stage {
                 for (int j = ch[0]; j <= ch[1] + 1; j += 2) e[n - 1][j / 2] = e[n][j];
     }
     // BaseStateGeometry::InitMultiLevel, planar (Source/BaseStateGeometry.cpp:355-382), with the
-    // radial rows of level n - 1 tagged wherever a level-n box lies above them.
+    // radial rows of level n - 1 tagged wherever a level-n box lies above them.  Spherical: one
+    // radial level (max_radial_level 0, Source/MaestroSetup.cpp:65), read whole by every level.
     void InitChunks() {
         chunks.assign(nlev, {});
         chunks[0].push_back({0, S[0].nr - 1});
         for (int n = 1; n < nlev; ++n) {
+            if (P.spherical) {
+                chunks[n].push_back({0, S[n].nr - 1});
+                continue;
+            }
             const int nrc = S[n - 1].nr;
             std::vector<int> tag(nrc, 0);
             for (const Box& b : S[n].L.ba)
@@ -2325,7 +2330,7 @@ static void setup_stage(Stage& H, const mo_params* p, int nlev, const int* nboxe
         if (p->spherical) S.InitSphr();
     }
     H.InitChunks();
-    if (nlev > 1) H.ComputeCutoffCoords();
+    if (nlev > 1 && !p->spherical) H.ComputeCutoffCoords();  // spherical: no kernel reads it
 
     // w0_cart: Put1dArrayOnCart(w0, w0_cart, true, true, bcs_u, 0, 1) (Source/MaestroAdvance.cpp:326)
     VMF w0c(nlev);

@@ -93,13 +93,20 @@ def test_spherical_exact_grid_interpolation_types(kw):
     assert bitwise, worst
 
 
-def test_spherical_uniform_bins_two_levels():
+@pytest.mark.parametrize("corner", [False, True])
+def test_spherical_uniform_bins_two_levels(corner):
+    """corner: one more level-1 box in the domain's top corner, whose rows (fine z up to 63)
+    lie past the 56 radial bins -- the one radial level is read whole on every level, not in
+    the plane-parallel chunks the fine rows would give."""
     from maestroex_gb300.stage import run_amr_stage_gpu
     from test_amr_gpu import compare_levels
     fine = configs.bubble_boxes((32, 32, 32), nbubbles=3, cover=0.12, block_edges=(4, 8), max_edge=8,
                                 rng=np.random.default_rng(5))
+    if corner:
+        fine = fine + [(56, 56, 56, 63, 63, 63)]
     cfg = configs.spherical_amr_config(n0=32, max_grid=16, ppm_type=2, fine_boxes=fine, exact=False,
                                        w0mac_interp_type=4)
+    assert cfg["nr"] < 64
     gpu = run_amr_stage_gpu(cfg, mode=capi.MODE_GRAPH)
     ref = pyoracle.run_stage_levels(cfg)
     assert compare_levels(cfg, gpu, ref, "spherical uniform bins, 2 levels")
