@@ -315,7 +315,7 @@ def run_amr(args, ws, steps, warmup, barrier):
     from maestroex_gb300.stage import amr_buffers, make_amr_stage
     cfg = configs.workload_amr(n0=args.amr_n, nspec=args.nspec)
     st = make_amr_stage(cfg)
-    bufs = amr_buffers(cfg)
+    bufs = amr_buffers(cfg, edges=edges)
     names = ("uold", "sold", "gpi")
     snap = [{n: [t.clone() for t in getattr(b, n).fabs] for n in names} for b in bufs]
 
@@ -690,17 +690,20 @@ def run_spherical_adjoint(args, barrier):
     }
 
 
-def run_spherical(args, barrier, exact=True):
+def run_spherical(args, barrier, exact=True, n=None):
     """Full-star spherical workload: two levels, level 0 n^3 in uneven
     boxes (edges 16-128), level 1 (ratio 2) 16-64-cell boxes around 3 seeded bubbles, NumSpec
     21, ppm_type 2, exact base state on the fine level's irregular radial grid, polytrope
-    star, outflow faces; the level-1 state injected from level 0.  Graph-replayed stage vs
-    one launch per box, identical results checked.  exact=False: the same on uniform radial
-    bins with the reference's default interpolation types (graph mode only)."""
+    star, outflow faces; the level-1 state injected from level 0.  The caller holds no
+    edge-state or flux MultiFabs (the library streams the species) unless --sph-edges.
+    Graph-replayed stage timed; one step launched per box checked identical.  exact=False:
+    the same on uniform radial bins with the reference's default interpolation types (graph
+    mode only)."""
     import torch
     from maestroex_gb300 import capi, configs
     from maestroex_gb300.stage import amr_buffers, make_amr_stage
-    n = args.sph_n
+    n = n or args.sph_n
+    edges = args.sph_edges
     rng = np.random.default_rng(20261203 + 50)
     l0 = configs.uneven_boxes((n, n, n), [16, 32, 48, 64, 96, 128], rng, p_stop=0.8)
     fine = configs.bubble_boxes((n, n, n), nbubbles=3, cover=args.sph_cover, block_edges=(8, 16, 24, 32),
@@ -708,7 +711,7 @@ def run_spherical(args, barrier, exact=True):
     cfg = configs.spherical_amr_config(n0=n, nspec=21, ppm_type=2, fine_boxes=fine, level0_boxes=l0, inject=True,
                                        exact=exact)
     st = make_amr_stage(cfg)
-    bufs = amr_buffers(cfg)
+    bufs = amr_buffers(cfg, edges=edges)
     names = ("uold", "sold", "gpi")
     # the inputs every repetition starts from, kept in pinned host memory (HBM holds the
     # stage's buffers)
@@ -720,8 +723,8 @@ def run_spherical(args, barrier, exact=True):
                 for dst, src in zip(getattr(b, nm).fabs, ts):
                     dst.copy_(src, non_blocking=True)
 
-    def timed(mode, reps):
-        for _ in range(2):
+    def timed(mode, reps, warm=2):
+        for _ in range(warm):
             reset()
             st.stage_forward_levels(bufs, mode=mode)
         barrier()
@@ -739,19 +742,22 @@ def run_spherical(args, barrier, exact=True):
 
     reps = max(1, args.steps // 2)
     ms_graph, l_graph = timed(capi.MODE_GRAPH, reps)
+    free, total = torch.cuda.mem_get_info()
     cells = [n ** 3, sum((b[3] - b[0] + 1) * (b[4] - b[1] + 1) * (b[5] - b[2] + 1) for b in fine)]
     ncell = sum(cells)
     grid = (f"exact base state ({cfg['nr']} radial bins on the fine grid)" if exact else
             f"uniform radial bins ({cfg['nr']} of dx_fine), w0 linear, s0 quadratic, w0mac / s0mac face averages")
+    held = ("edge states and fluxes returned" if edges else
+            "no edge-state or flux MultiFabs: the species streamed through the library's slots")
     res = {"workload": f"spherical full star, two levels: level 0 {n}^3 in {len(l0)} uneven boxes (edges 16-128), "
                        f"level 1 (ratio 2) {len(fine)} boxes around 3 bubbles ({cells[1] / 8 / cells[0]:.3f} of "
                        f"the domain), NumSpec 21, ppm_type 2, {grid}, n = 1.5 polytrope (rho_c 2e9, radius "
-                       "0.9 L/2), outflow; level-1 state injected from level 0",
-           "cells_per_level": cells, "unit": UNIT,
+                       f"0.9 L/2), outflow; level-1 state injected from level 0; {held}",
+           "cells_per_level": cells, "unit": UNIT, "device_gb_in_use": (total - free) / 1e9,
            "graph": {"value": ncell / (ms_graph * 1e-3), "ms_per_step": ms_graph, "gpu_launches": l_graph}}
     if exact:
         out_graph = [[f.cpu() for f in b.snew.fabs] for b in bufs]
-        ms_box, l_box = timed(capi.MODE_PER_BOX, reps)
+        ms_box, l_box = timed(capi.MODE_PER_BOX, 1, 1)
         same = all(torch.equal(a, f.cpu()) for og, b in zip(out_graph, bufs) for a, f in zip(og, b.snew.fabs))
         res.update({"per_box": {"value": ncell / (ms_box * 1e-3), "ms_per_step": ms_box, "gpu_launches": l_box},
                     "speedup_graph_vs_per_box": ms_box / ms_graph,
@@ -888,9 +894,12 @@ def main():
                     help="run one adjoint call (state and velocity gradients) and exit (the command ncu captures)")
     ap.add_argument("--no-2d", action="store_true")
     ap.add_argument("--no-velocity", action="store_true")
-    ap.add_argument("--sph-n", type=int, default=256, help="extent of the spherical workload")
+    ap.add_argument("--sph-n", type=int, default=384, help="extent of the spherical workload")
+    ap.add_argument("--sph-u-n", type=int, default=256, help="extent of the spherical workload on uniform bins")
     ap.add_argument("--sph-cover", type=float, default=0.06,
                     help="bubble radius parameter of the spherical workload's level 1 (0.06: about 11%% of the domain)")
+    ap.add_argument("--sph-edges", action="store_true",
+                    help="spherical legs: hold edge-state and flux MultiFabs (384^3 then exceeds HBM)")
     ap.add_argument("--no-spherical", action="store_true")
     ap.add_argument("--no-sph-adjoint", action="store_true")
     ap.add_argument("--no-mac", action="store_true")
@@ -1097,7 +1106,8 @@ def main():
     two_d = leg("two_d", args.no_2d, lambda: run_2d(args, barrier))
     vel = leg("velocity_advance", args.no_velocity, lambda: run_velocity(args, barrier))
     sph = leg("spherical", args.no_spherical, lambda: run_spherical(args, barrier))
-    sph_u = leg("spherical_uniform_bins", args.no_spherical, lambda: run_spherical(args, barrier, exact=False))
+    sph_u = leg("spherical_uniform_bins", args.no_spherical,
+                lambda: run_spherical(args, barrier, exact=False, n=args.sph_u_n))
     sph_adj = leg("spherical_adjoint", args.no_sph_adjoint, lambda: run_spherical_adjoint(args, barrier))
     mac = leg("mac_projection", args.no_mac, lambda: run_mac_projection(args, barrier))
 

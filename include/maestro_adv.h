@@ -274,7 +274,13 @@ int madv_update_scal(madv_ctx* ctx, const madv_multifab* stateold, const madv_mu
  * mode: MADV_MODE_BATCHED runs every kernel once over all boxes;
  *       MADV_MODE_PER_BOX launches every kernel once per box (the AMReX MFIter form);
  *       MADV_MODE_GRAPH replays a CUDA graph of the batched form (captured on first use
- *       for the given buffers). */
+ *       for the given buffers).
+ * sedge and sflux both NULL (3-D): the caller wants neither the edge states nor the fluxes
+ * (the reference's AdvanceTimeStep reads neither after the stage: etarhoflux and the flux
+ * registers carry what it needs).  The species are then streamed: each species' edge
+ * states, fluxes and update pass through slots of three components (Rho, RhoH, the species
+ * in flight), so the context holds 6 face-centred doubles per cell instead of 2 nscal.
+ * The new state, the MAC velocities and etarhoflux are the full stage's bit for bit. */
 enum { MADV_MODE_BATCHED = 0, MADV_MODE_PER_BOX = 1, MADV_MODE_GRAPH = 2 };
 int madv_stage_forward(madv_ctx* ctx, int mode, const madv_multifab* uold,
                        const madv_multifab* sold, const madv_multifab* gpi,

@@ -397,7 +397,7 @@ static double* reg_storage(Ctx& cf, long off[7]) {
 // CrseInit: reg = mult * coarse flux on the face (the coarse box owning the inside cell)
 template <int D, int SIDE>
 __global__ void k_fr_crse_init(KARGS, const FabView* __restrict__ Vc, int nbc, LevelGeo gc, int ff, double* reg,
-                               long off, int nscal, int c0, int nc, double mult, int* err) {
+                               long off, int nscal, int c0, int nc, double mult, int slot, int* err) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     int q[3] = {i, j, k};
     if (SIDE == 1) q[D] -= 1;  // the inside cell of a hi face
@@ -408,12 +408,13 @@ __global__ void k_fr_crse_init(KARGS, const FabView* __restrict__ Vc, int nbc, L
     }
     const FabView fl = Vc[(ff + D) * nbc + cb];
     double* r = reg + (off + gid_) * nscal;
-    for (int n = c0; n < c0 + nc; ++n) r[n] = mult * at(fl, i, j, k, n);
+    for (int n = c0; n < c0 + nc; ++n) r[n] = mult * at(fl, i, j, k, slot >= 0 ? slot : n);
 }
 
 // FineAdd: reg += mult * each fine face of the coarse face, in turn
 template <int D>
-__global__ void k_fr_fine_add(KARGS, int ff, double* reg, long off, int nscal, int c0, int nc, double mult) {
+__global__ void k_fr_fine_add(KARGS, int ff, double* reg, long off, int nscal, int c0, int nc, double mult,
+                              int slot) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int t1 = D == 0 ? 1 : 0, t2 = D == 2 ? 1 : 2;
     const FabView fl = VW(ff + D);
@@ -425,7 +426,7 @@ __global__ void k_fr_fine_add(KARGS, int ff, double* reg, long off, int nscal, i
                 int q[3] = {2 * i, 2 * j, 2 * k};
                 q[t1] += in;
                 q[t2] += o;
-                v = v + mult * at(fl, q[0], q[1], q[2], n);
+                v = v + mult * at(fl, q[0], q[1], q[2], slot >= 0 ? slot : n);
             }
         r[n] = v;
     }
@@ -450,13 +451,13 @@ __global__ void k_fr_reflux(KARGS, const FabView* __restrict__ Vc, int nbc, Leve
 }
 
 template <int D, int SIDE>
-static void fr_crse_init_o(Ctx& cf, Ctx& cc, double* reg, long off, int c0, int nc, double mult) {
+static void fr_crse_init_o(Ctx& cf, Ctx& cc, double* reg, long off, int c0, int nc, double mult, int slot) {
     launch(cf, reg_table(cf, D + 3 * SIDE), 1, k_fr_crse_init<D, SIDE>, cf.V(), cc.V(), cc.nb, geo_of(cc), F_SFLUX0,
-           reg, off, cf.nscal, c0, nc, mult, cf.d_flag);
+           reg, off, cf.nscal, c0, nc, mult, slot, cf.d_flag);
 }
 template <int D>
-static void fr_fine_add_o(Ctx& cf, int o, double* reg, long off, int c0, int nc, double mult) {
-    launch(cf, reg_table(cf, o), 1, k_fr_fine_add<D>, cf.V(), F_SFLUX0, reg, off, cf.nscal, c0, nc, mult);
+static void fr_fine_add_o(Ctx& cf, int o, double* reg, long off, int c0, int nc, double mult, int slot) {
+    launch(cf, reg_table(cf, o), 1, k_fr_fine_add<D>, cf.V(), F_SFLUX0, reg, off, cf.nscal, c0, nc, mult, slot);
 }
 template <int D, int SIDE>
 static void fr_reflux_o(Ctx& cf, Ctx& cc, const double* reg, long off, int c0, int nc, double vol) {
@@ -466,27 +467,27 @@ static void fr_reflux_o(Ctx& cf, Ctx& cc, const double* reg, long off, int c0, i
 
 // FluxRegister::CrseInit of the coarse level's fluxes, components c0 .. c0+nc-1, mult =
 // -dt * coarse face area (Source/MaestroMakeFlux.cpp:430-439)
-void flux_reg_crse_init(Ctx& cf, Ctx& cc, int c0, int nc, double dt) {
+void flux_reg_crse_init(Ctx& cf, Ctx& cc, int c0, int nc, double dt, int slot) {
     long off[7];
     double* reg = reg_storage(cf, off);
     const double area[3] = {cc.P.dx[1] * cc.P.dx[2], cc.P.dx[0] * cc.P.dx[2], cc.P.dx[0] * cc.P.dx[1]};
-    fr_crse_init_o<0, 0>(cf, cc, reg, off[0], c0, nc, -1.0 * dt * area[0]);
-    fr_crse_init_o<0, 1>(cf, cc, reg, off[3], c0, nc, -1.0 * dt * area[0]);
-    fr_crse_init_o<1, 0>(cf, cc, reg, off[1], c0, nc, -1.0 * dt * area[1]);
-    fr_crse_init_o<1, 1>(cf, cc, reg, off[4], c0, nc, -1.0 * dt * area[1]);
-    fr_crse_init_o<2, 0>(cf, cc, reg, off[2], c0, nc, -1.0 * dt * area[2]);
-    fr_crse_init_o<2, 1>(cf, cc, reg, off[5], c0, nc, -1.0 * dt * area[2]);
+    fr_crse_init_o<0, 0>(cf, cc, reg, off[0], c0, nc, -1.0 * dt * area[0], slot);
+    fr_crse_init_o<0, 1>(cf, cc, reg, off[3], c0, nc, -1.0 * dt * area[0], slot);
+    fr_crse_init_o<1, 0>(cf, cc, reg, off[1], c0, nc, -1.0 * dt * area[1], slot);
+    fr_crse_init_o<1, 1>(cf, cc, reg, off[4], c0, nc, -1.0 * dt * area[1], slot);
+    fr_crse_init_o<2, 0>(cf, cc, reg, off[2], c0, nc, -1.0 * dt * area[2], slot);
+    fr_crse_init_o<2, 1>(cf, cc, reg, off[5], c0, nc, -1.0 * dt * area[2], slot);
 }
 
 // FluxRegister::FineAdd of the fine level's fluxes, mult = dt * fine face area (:441-450)
-void flux_reg_fine_add(Ctx& cf, int c0, int nc, double dt) {
+void flux_reg_fine_add(Ctx& cf, int c0, int nc, double dt, int slot) {
     long off[7];
     double* reg = reg_storage(cf, off);
     const double area[3] = {cf.P.dx[1] * cf.P.dx[2], cf.P.dx[0] * cf.P.dx[2], cf.P.dx[0] * cf.P.dx[1]};
     for (int side = 0; side < 2; ++side) {
-        fr_fine_add_o<0>(cf, 0 + 3 * side, reg, off[0 + 3 * side], c0, nc, 1.0 * dt * area[0]);
-        fr_fine_add_o<1>(cf, 1 + 3 * side, reg, off[1 + 3 * side], c0, nc, 1.0 * dt * area[1]);
-        fr_fine_add_o<2>(cf, 2 + 3 * side, reg, off[2 + 3 * side], c0, nc, 1.0 * dt * area[2]);
+        fr_fine_add_o<0>(cf, 0 + 3 * side, reg, off[0 + 3 * side], c0, nc, 1.0 * dt * area[0], slot);
+        fr_fine_add_o<1>(cf, 1 + 3 * side, reg, off[1 + 3 * side], c0, nc, 1.0 * dt * area[1], slot);
+        fr_fine_add_o<2>(cf, 2 + 3 * side, reg, off[2 + 3 * side], c0, nc, 1.0 * dt * area[2], slot);
     }
 }
 

@@ -293,6 +293,12 @@ static void field_specs(Ctx& c) {
     S(F_DIVW0, nu, 0);
     // nodes of the box grown by one, node (i,j,k) at cell (i,j,k): two ghost cells
     S(F_W0NODAL, c.sph && c.geo.w0maci == 4 ? 3 : 0, 2);
+    // species streaming (a stage call that returns no edge states or fluxes): Rho, RhoH and
+    // the species in flight, in place of the nscal components of F_SEDGE* / F_SFLUX*
+    for (int d = 0; d < 3; ++d) {
+        S(F_SEDGES0 + d, c.ndim == 3 ? 3 : 0, 0, d);
+        S(F_SFLUXS0 + d, c.ndim == 3 ? 3 : 0, 0, d);
+    }
 }
 
 static void free_layout(Ctx& c) {
@@ -556,9 +562,14 @@ static void convert_rhox_to_x_h(Hier& H, int flag) {
     else fill_patch_h(H, F_SOLD, FIRSTSPEC, ns, BCS_S, FIRSTSPEC, 0, FIRSTSPEC);
 }
 
-// Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297)
+// Maestro::UpdateScal (Source/MaestroAdvection.cpp:86-297): the update on every level, then
+// the levels' synchronisation
+static void update_scal_sync_h(Hier& H, int start_comp);
 static void update_scal_h(Hier& H, int start_comp) {
     for (auto* c : H.L) update_scal(*c, start_comp);
+    update_scal_sync_h(H, start_comp);
+}
+static void update_scal_sync_h(Hier& H, int start_comp) {
     // reflux_type 2: the coarse cells next to each finer level take back the flux mismatch,
     // the finest pair first (Source/MaestroAdvection.cpp:258-276)
     if (H[0].P.reflux_type == 2)
@@ -585,9 +596,11 @@ static void update_scal_h(Hier& H, int start_comp) {
 // the fluxes across levels: reflux_type 1 averages the fine fluxes down onto the coarse faces
 // (Source/MaestroMakeFlux.cpp:460-462); reflux_type 2 records the flux mismatch of the
 // updated components (and Rho with the species) in the flux registers (:420-456)
-static void flux_sync_h(Hier& H, int c0, int nc) {
+// (stream: species streaming, whose flux slots hold Rho and RhoH at their own components)
+static void flux_sync_h(Hier& H, int c0, int nc, bool stream = false) {
     if (H[0].P.reflux_type != 2) {
-        average_down_faces_h(H, F_SFLUX0, 0, H[0].nscal);
+        if (stream) average_down_faces_h(H, F_SFLUX0, c0, nc);
+        else average_down_faces_h(H, F_SFLUX0, 0, H[0].nscal);
         return;
     }
     const double dt = H[0].P.dt;
@@ -603,9 +616,80 @@ static void flux_sync_h(Hier& H, int c0, int nc) {
     }
 }
 
+// one component's flux across the levels, read from F_SFLUX* component `slot` (-1: comp)
+static void flux_sync_one_h(Hier& H, int comp, int slot) {
+    if (H[0].P.reflux_type != 2) {
+        average_down_faces_h(H, F_SFLUX0, slot >= 0 ? slot : comp, 1);
+        return;
+    }
+    const double dt = H[0].P.dt;
+    for (int l = 0; l < H.n(); ++l) {
+        if (l + 1 < H.n()) flux_reg_crse_init(H[l + 1], H[l], comp, 1, dt, slot);
+        if (l > 0) flux_reg_fine_add(H[l], comp, 1, dt, slot);
+    }
+}
+
+// DensityAdvance with the species streamed: a stage call that returns no edge states and no
+// fluxes holds one species' edge states and fluxes at a time (component SLOT of the slot
+// fields) instead of all of them.  Each species' values and every sum are those of
+// density_advance below, in the same order:
+// * the species are independent of each other up to UpdateScal's density sum and
+//   negative-species fix, so each runs edge state -> back to rho X -> flux -> coarse-fine
+//   flux sync -> update before the next; the Rho flux and etarhoflux, sums over the species
+//   in component order, carry over from species to species;
+// * the edge state of rho (species_pred_type 1, 3) reads only the density and its force, so
+//   it is formed first, while the density is in perturbational form, and the density goes
+//   back before the species do (converting X back to rho X reads the full density);
+// * the closing pass (density from the species' changes, floor, negative-species fix) and
+//   the reflux follow the last species, as in UpdateScal.
+static void density_advance_streamed(Hier& H, int which_step) {
+    constexpr int SLOT = 2;
+    const int spt = H[0].P.species_pred_type;
+    const int ns = H[0].nspec, nscal = H[0].nscal;
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, c->F[F_SCALFORCE].spec.ng);
+    put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
+    addw0_h(H, F_UMAC0, -1.0);
+    if (spt == 1) modify_scal_force_h(H, RHO, "rho0_edge_old", F_RHO0CART, 0);
+    else if (spt == 3) modify_scal_force_h(H, RHO, "rho0_edge_old", F_RHO0CART, 1);
+    addw0_h(H, F_UMAC0, 1.0);
+    if (spt == 1 || spt == 3) convert_rhox_to_x_h(H, 1);
+    if (spt == 1) put_in_pert_form_h(H, "rho0_old", RHO, 0, BCS_F, 1);
+    const int cons = spt == 2;  // the species' form; rho's edge state is advective
+    for (auto* c : H.L) edge_scal_setup(*c, cons);
+    if (spt == 1 || spt == 3)
+        for (auto* c : H.L) make_edge_scal(*c, RHO, 1, BCS_S, 0, 0, 0, -1, false);
+    if (spt == 1) put_in_pert_form_h(H, "rho0_old", RHO, RHO, BCS_S, 0);
+    const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
+    const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
+    if (H[0].sph) {  // rho0 on faces (Source/MaestroDensityAdvance.cpp:167-213)
+        make_s0mac_h(H, "rho0_old", F_S0MAC0);
+        make_s0mac_h(H, r0n, F_S0MACB0);
+    }
+    for (int n = 0; n < ns; ++n) {
+        const int comp = FIRSTSPEC + n;
+        for (auto* c : H.L) make_edge_scal(*c, comp, 1, BCS_S, cons, 1, 0, SLOT, false);  // no force for X / rho X
+        if (spt == 2)
+            for (auto* c : H.L) sum_species_edge_step(*c, SLOT, n == 0);
+        if (spt == 1 || spt == 3) {  // X -> rho X (Maestro::ConvertRhoXToX, flag false)
+            for (auto* c : H.L) convert_rhox_to_x(*c, 0, comp, 1);
+            average_down_h(H, F_SOLD, comp, 1);
+            fill_patch_h(H, F_SOLD, comp, 1, BCS_S, comp, 0, comp);
+        }
+        for (auto* c : H.L)
+            make_rhox_flux(*c, c->b1("rho0_old"), c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en), comp, 1, SLOT);
+        flux_sync_one_h(H, comp, SLOT);
+        for (auto* c : H.L) update_species(*c, comp, SLOT);
+    }
+    flux_sync_one_h(H, RHO, -1);
+    for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHO, 1, c->F[F_SCALFORCE].spec.ng);
+    for (auto* c : H.L) update_rhox_fix(*c);
+    update_scal_sync_h(H, FIRSTSPEC);
+}
+
 // Maestro::DensityAdvance (Source/MaestroDensityAdvance.cpp:6-243); which_step 2 passes the
 // new base state to the fluxes (:186-219)
-static void density_advance(Hier& H, int which_step) {
+static void density_advance(Hier& H, int which_step, bool stream = false) {
+    if (stream) return density_advance_streamed(H, which_step);
     const int spt = H[0].P.species_pred_type;
     const int ns = H[0].nspec, nscal = H[0].nscal;
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, 0, nscal, c->F[F_SCALFORCE].spec.ng);
@@ -668,7 +752,7 @@ static void rhoh_flux_h(Hier& H, int which_step) {
                        c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
 }
 
-static void enthalpy_advance(Hier& H, int which_step) {
+static void enthalpy_advance(Hier& H, int which_step, bool stream = false) {
     const int ept = H[0].P.enthalpy_pred_type;
     const int nscal = H[0].nscal;
     // predict_h: (rho h) -> h (Source/MaestroEnthalpyAdvance.cpp:40-43)
@@ -689,7 +773,7 @@ static void enthalpy_advance(Hier& H, int which_step) {
     if (ept == 1) put_in_pert_form_h(H, "rhoh0_old", RHOH, RHOH, BCS_S, 0);
     if (ept == 2) convert_rhoh_to_h_h(H, 0);  // h -> (rho h) (:164-167)
     rhoh_flux_h(H, which_step);
-    flux_sync_h(H, RHOH, 1);
+    flux_sync_h(H, RHOH, 1, stream);
     for (auto* c : H.L) set_val(*c, F_SCALFORCE, 0.0, RHOH, 1, c->F[F_SCALFORCE].spec.ng);
     addw0_h(H, F_UMAC0, -1.0);
     make_rhoh_force_h(H, 0, 0, which_step);
@@ -701,9 +785,10 @@ static void enthalpy_advance(Hier& H, int which_step) {
 // hands over FABs laid out as these fields works in them directly, so their storage is
 // allocated at the first call that does not (at 256^3 with NumSpec 13 they are 60% of a
 // level's fields).
+static bool stream_slot(int f) { return f >= F_SEDGES0 && f <= F_SFLUXS2; }
 static bool deferrable(int f) {
     return f == F_SOLD || f == F_SNEW || (f >= F_UMAC0 && f <= F_UMAC2) || (f >= F_SEDGE0 && f <= F_SEDGE2) ||
-           (f >= F_SFLUX0 && f <= F_SFLUX2);
+           (f >= F_SFLUX0 && f <= F_SFLUX2) || stream_slot(f);
 }
 
 // host views of field f: one FAB per box (valid box grown by the field's ghost width), laid
@@ -749,7 +834,7 @@ static void materialize(Ctx& c, int f) {
 }
 
 // every_field: allocate the deferred fields too (every entry point but the stage, which
-// allocates those its caller does not hand over)
+// allocates those its caller does not hand over); the streaming slots only the stage uses
 static int check_ready_h(const Hier& H, bool every_field = true) {
     for (auto* c : H.L)
         if (!c->have_layout || !c->have_base) {
@@ -758,7 +843,8 @@ static int check_ready_h(const Hier& H, bool every_field = true) {
         }
     if (every_field) try {
             for (auto* c : H.L)
-                for (int f = 0; f < NF_INTERNAL; ++f) materialize(*c, f);
+                for (int f = 0; f < NF_INTERNAL; ++f)
+                    if (!stream_slot(f)) materialize(*c, f);
         } catch (const Fail& f) {
             return f.code;
         }
@@ -769,8 +855,9 @@ struct StageIO {
     const madv_multifab *uold, *sold, *gpi, *thermal, *snew, *umac, *sedge, *sflux, *eta;
     int sold_out = 1;  // copy the converted-and-restored sold back to the caller
     int alias = 0;     // AL_* fields worked in the caller's FABs directly (no copies)
+    int stream = 0;    // species streaming: the species' edge states and fluxes pass through slots
 };
-enum { AL_SOLD = 1, AL_SNEW = 2, AL_UMAC = 4, AL_SEDGE = 8, AL_SFLUX = 16 };
+enum { AL_SOLD = 1, AL_SNEW = 2, AL_UMAC = 4, AL_SEDGE = 8, AL_SFLUX = 16, AL_STREAM = 32 };
 
 // A caller FAB can stand in for field fid when it has the field's index box (valid box grown
 // by the field's ghost width) and at least its components: views of both then address the
@@ -818,12 +905,18 @@ static FabView* alias_fields(Ctx& c, StageIO& io) {
         if (all(F_SEDGE0, io.sedge)) io.alias |= AL_SEDGE;
         if (all(F_SFLUX0, io.sflux)) io.alias |= AL_SFLUX;
     }
+    if (io.stream) io.alias |= AL_STREAM;
     // the fields this call does not work in the caller's FABs need their own storage
     if (!(io.alias & AL_SOLD)) materialize(c, F_SOLD);
     if (!(io.alias & AL_SNEW)) materialize(c, F_SNEW);
     for (int d = 0; d < 3; ++d) {
         const bool in_call = d < c.ndim;
         if (!(in_call && (io.alias & AL_UMAC))) materialize(c, F_UMAC0 + d);
+        if (io.alias & AL_STREAM) {
+            materialize(c, F_SEDGES0 + d);
+            materialize(c, F_SFLUXS0 + d);
+            continue;
+        }
         if (!(in_call && (io.alias & AL_SEDGE))) materialize(c, F_SEDGE0 + d);
         if (!(in_call && (io.alias & AL_SFLUX))) materialize(c, F_SFLUX0 + d);
     }
@@ -844,6 +937,11 @@ static FabView* alias_fields(Ctx& c, StageIO& io) {
         if (io.alias & AL_UMAC) swap(F_UMAC0 + d, U_UMAC0 + d);
         if (io.alias & AL_SEDGE) swap(F_SEDGE0 + d, U_SEDGE0 + d);
         if (io.alias & AL_SFLUX) swap(F_SFLUX0 + d, U_SFLUX0 + d);
+        if (io.alias & AL_STREAM)  // the slots stand in for the edge states and fluxes
+            for (int b = 0; b < c.nb; ++b) {
+                c.hviews_alias[(F_SEDGE0 + d) * c.nb + b] = c.hviews_pinned[(F_SEDGES0 + d) * c.nb + b];
+                c.hviews_alias[(F_SFLUX0 + d) * c.nb + b] = c.hviews_pinned[(F_SFLUXS0 + d) * c.nb + b];
+            }
     }
     if (!cuda_ok(cudaMemcpyAsync(c.dviews_alias, c.hviews_alias, sizeof(FabView) * nv, cudaMemcpyHostToDevice, c.stream),
                  "cudaMemcpyAsync(views)"))
@@ -889,6 +987,11 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
         if (!(al & AL_SNEW)) set_val(c, F_SNEW, 0.0, 0, c.nscal, c.ng_s);
         for (int d = 0; d < 3; ++d) {
             set_val(c, F_UMAC0 + d, 0.0, 0, 1, 1);
+            if (al & AL_STREAM) {  // the three slots
+                set_val(c, F_SEDGE0 + d, 0.0, 0, 3, 0);
+                set_val(c, F_SFLUX0 + d, 0.0, 0, 3, 0);
+                continue;
+            }
             // (Source/MaestroAdvance.cpp:190-191); in a caller's FAB only Temp and Pi are not
             // overwritten by the stage
             if (al & AL_SEDGE) set_val(c, F_SEDGE0 + d, 0.0, TEMP, 2, 0);
@@ -900,12 +1003,13 @@ static void stage_body(Hier& H, const std::vector<StageIO>& io) {
     }
     w0_carts(H);
     // STEP 3 and STEP 4 of Maestro::AdvanceTimeStep (Source/MaestroAdvance.cpp:359-548)
+    const bool stream = io[0].stream;
     advance_premac(H);
     addw0_h(H, F_UMAC0, 1.0);
-    density_advance(H, 1);
+    density_advance(H, 1, stream);
     addw0_h(H, F_UMAC0, -1.0);
     addw0_h(H, F_UMAC0, 1.0);
-    enthalpy_advance(H, 1);
+    enthalpy_advance(H, 1, stream);
     addw0_h(H, F_UMAC0, -1.0);
     // outputs (valid region)
     for (int l = 0; l < H.n(); ++l) {
@@ -1599,10 +1703,13 @@ static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab*
     }
     if (mode < MADV_MODE_BATCHED || mode > MADV_MODE_GRAPH) return MADV_ERR_PARAM;
     std::vector<StageIO> io(nlev);
-    for (int l = 0; l < nlev; ++l)
+    for (int l = 0; l < nlev; ++l) {
         io[l] = StageIO{&uold[l], &sold[l], &gpi[l], thermal ? &thermal[l] : nullptr, snew ? &snew[l] : nullptr,
                         umac ? &umac[3 * l] : nullptr, sedge ? &sedge[3 * l] : nullptr,
                         sflux ? &sflux[3 * l] : nullptr, etarhoflux ? &etarhoflux[l] : nullptr};
+        // no edge states and no fluxes returned (3-D): the species are streamed
+        io[l].stream = !sedge && !sflux && H[l].ndim == 3;
+    }
     Ctx& c = h->c;
     set_mode(H, (cudaStream_t)stream, 0, false);
     reset_launches(H);

@@ -69,6 +69,8 @@ enum FieldId {
     F_GRADW0,                      // spherical, uniform bins: dw0/dr on cells (MakeVelForce)
     F_DIVW0,                       // spherical, uniform bins: div w0 on cells (ModifyScalForce)
     F_IPF, F_IMF,                  // ppm_trace_forces: the traced force, 3 directional comps
+    F_SEDGES0, F_SEDGES1, F_SEDGES2,  // species streaming: edge-state slots (Rho, RhoH, one species)
+    F_SFLUXS0, F_SFLUXS1, F_SFLUXS2,  //   and flux slots, standing in for F_SEDGE* / F_SFLUX*
     F_USER,                        // first slot of per-call views of caller FABs
     NF_INTERNAL = F_USER
 };
@@ -238,14 +240,20 @@ void make_utrans(Ctx& c);
 void make_vel_force(Ctx& c, int fe = F_UTRANS0);
 void vel_pred(Ctx& c);
 void vel_pred_prep(Ctx& c);  // the MakeUtrans work VelPred reuses, for a VelPred call on its own
+// slot >= 0: the edge state of every component goes to component `slot` of F_SEDGE* (species
+// streaming); setup = false: the velocity-only coefficients are already in place
 void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_conservative,
-                    int force_zero, int is_vel = 0);
+                    int force_zero, int is_vel = 0, int slot = -1, bool setup = true);
+void edge_scal_setup(Ctx& c, int is_conservative);
 void modify_scal_force(Ctx& c, int comp, int s0cart_fid, int fullform);
 void make_rhoh_force(Ctx& c, int is_prediction, int add_thermal);
 void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag);
-void convert_rhox_to_x(Ctx& c, int flag);
+void convert_rhox_to_x(Ctx& c, int flag, int c0 = FIRSTSPEC, int nc = -1);  // nc -1: every species
+// species c0 .. c0+nc-1 (nc -1: every species); slot >= 0: their edge state and flux in component
+// `slot` of F_SEDGE* / F_SFLUX* (one species per call), the Rho flux and etarhoflux accumulated
 void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new,
-                    const double* r0e_new);
+                    const double* r0e_new, int c0 = FIRSTSPEC, int nc = -1, int slot = -1);
+void sum_species_edge_step(Ctx& c, int slot, int first);  // species_pred_type 2, streamed
 void make_rhoh_flux(Ctx& c, const double* rh0_old, const double* rh0e_old, const double* rh0_new,
                     const double* rh0e_new, const double* r0_old, const double* r0e_old, const double* r0_new,
                     const double* r0e_new);
@@ -257,6 +265,10 @@ int ppm_box_run(const madv_params& P, const madv_box* bx, const madv_fab* s, int
                 const madv_fab* v, const madv_fab* w, int is_umac, const int* bc, const madv_fab* Ip,
                 const madv_fab* Im, double* scratch, cudaStream_t st, long& launches);
 void update_scal(Ctx& c, int start_comp);
+// UpdateScal of the species split for streaming: one species from its flux in F_SFLUX* comp
+// `slot`, then the density, floor and negative-species pass over all of them
+void update_species(Ctx& c, int comp, int slot);
+void update_rhox_fix(Ctx& c);
 void update_vel(Ctx& c, int fu, int fsponge);  // UpdateVel into F_SNEW comps 0-2; fsponge -1: no sponge
 // EstDt maxima of a level into c.d_red[0..6] (spdx, spdy, spdz, spdr, fx, fy, fz as bit patterns)
 void dt_maxima(Ctx& c);
@@ -271,7 +283,7 @@ void make_vel_force_sph(Ctx& c, int fe);
 void modify_scal_force_sph(Ctx& c, int comp, int s0cart_fid, int fullform);
 void make_rhoh_force_sph(Ctx& c, int is_prediction, int add_thermal);
 void put_in_pert_form_sph(Ctx& c, const double* d_s0, int comp, int flag);
-void make_rhox_flux_sph(Ctx& c);
+void make_rhox_flux_sph(Ctx& c, int c0, int nc, int slot);
 void make_rhoh_flux_sph(Ctx& c);
 
 // ---- 2-D forms (madv_kernels.cu), reached through the wrappers above when c.ndim == 2
@@ -298,8 +310,9 @@ void interp_fill(Ctx& cc, Ctx& cf, int fid, int c0, int nc, int which_bcs, int b
 void average_down(Ctx& cf, Ctx& cc, int fid, int comp, int ncomp);
 void average_down_faces(Ctx& cf, Ctx& cc, int f0, int c0, int ncomp);
 void uedge_interface(Ctx& cc, Ctx& cf, int f0);
-void flux_reg_crse_init(Ctx& cf, Ctx& cc, int c0, int nc, double dt);
-void flux_reg_fine_add(Ctx& cf, int c0, int nc, double dt);
+// slot >= 0: the flux of component c0 (nc 1) is read from F_SFLUX* component `slot`
+void flux_reg_crse_init(Ctx& cf, Ctx& cc, int c0, int nc, double dt, int slot = -1);
+void flux_reg_fine_add(Ctx& cf, int c0, int nc, double dt, int slot = -1);
 void flux_reg_reflux(Ctx& cf, Ctx& cc, int c0, int nc);
 
 // ---- reverse sweep (madv_adjoint.cu).  User slots bound by the adjoint driver: working

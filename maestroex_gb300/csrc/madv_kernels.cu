@@ -1001,7 +1001,7 @@ __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bc
 // identically zero (species), so the + dt/2*force term is skipped.
 template <int D, bool CONS>
 __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double dt2h1, double dt2h2, double dt2hd,
-                           int bclo, int bchi, int domlo, int domhi, long long epsb, int vclamp, int ptf) {
+                           int bclo, int bchi, int domlo, int domhi, long long epsb, int vclamp, int ptf, int oc) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
@@ -1053,7 +1053,7 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
         else if (bchi == BC_REFLECT_EVEN) v = lq;
         else if (bchi == BC_REFLECT_ODD) v = 0.0;
     }
-    at(VW(F_SEDGE0 + D), i, j, k, comp) = v;
+    at(VW(F_SEDGE0 + D), i, j, k, oc) = v;
 }
 
 // vclamp: velocity edge states (is_vel) of the component normal to the faces, whose
@@ -1085,28 +1085,33 @@ static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons
 }
 
 template <int D>
-static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp) {
+static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp, int oc) {
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
     const double dt2 = 0.5 * c.P.dt;
     const int ptf = c.P.ppm_trace_forces;
     if (is_cons)
         launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, true>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-               dbits_host(c.P.rel_eps), vclamp, ptf);
+               dbits_host(c.P.rel_eps), vclamp, ptf, oc);
     else
         launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, false>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
-               dbits_host(c.P.rel_eps), vclamp, ptf);
+               dbits_host(c.P.rel_eps), vclamp, ptf, oc);
+}
+
+// velocity-only quantities shared by every component of a MakeEdgeScal call
+void edge_scal_setup(Ctx& c, int is_cons) {
+    if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), make_recip(c.P.dx[0]));
+    if (c.P.ppm_type != 0) trace_coeffs_faces(c, F_UMAC0);
+    if (!is_cons) transverse_coeffs(c, F_UMAC0);
 }
 
 // force_zero: the components' force is identically zero (DensityAdvance species)
-void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons, int force_zero, int is_vel) {
+void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_cons, int force_zero, int is_vel,
+                    int slot, bool setup) {
     if (c.ndim == 2) return make_edge_scal_2d_entry(c, start_comp, num_comp, which_bcs, is_cons);
     const BCRecD* bh = bcs_host(c, which_bcs);
-    if (is_cons) launch(c, rg_grow(c, 1), 1, k_divu, c.V(), make_recip(c.P.dx[0]));
-    // velocity-only quantities shared by every component of this call
-    if (c.P.ppm_type != 0) trace_coeffs_faces(c, F_UMAC0);
-    if (!is_cons) transverse_coeffs(c, F_UMAC0);
+    if (setup) edge_scal_setup(c, is_cons);
     for (int comp = start_comp; comp < start_comp + num_comp; ++comp) {
         if (c.edge_tape_begin) c.edge_tape_begin(comp);
         const BCRecD& bc = bh[comp];  // start_bccomp == start_scomp at every call site
@@ -1129,9 +1134,10 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
         es_transverse_launch<1, 2>(c, comp, bc, is_cons, v1);
         es_transverse_launch<2, 0>(c, comp, bc, is_cons, v2);
         es_transverse_launch<2, 1>(c, comp, bc, is_cons, v2);
-        es_edges_launch<0>(c, comp, bc, is_cons, force_zero, v0);
-        es_edges_launch<1>(c, comp, bc, is_cons, force_zero, v1);
-        es_edges_launch<2>(c, comp, bc, is_cons, force_zero, v2);
+        const int oc = slot >= 0 ? slot : comp;
+        es_edges_launch<0>(c, comp, bc, is_cons, force_zero, v0, oc);
+        es_edges_launch<1>(c, comp, bc, is_cons, force_zero, v1, oc);
+        es_edges_launch<2>(c, comp, bc, is_cons, force_zero, v2, oc);
         if (c.edge_tape) c.edge_tape(comp);
     }
 }
@@ -1212,38 +1218,42 @@ void put_in_pert_form(Ctx& c, const double* d_s0, int comp, int flag) {
 }
 
 // ConvertRhoXToX (Source/MaestroConvert.cpp:64-91), valid region
-__global__ void k_rhox_to_x(KARGS, int nspec, int flag) {
+__global__ void k_rhox_to_x(KARGS, int c0, int nc, int flag) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView s = VW(F_SOLD);
-    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+    for (int comp = c0; comp < c0 + nc; ++comp) {
         if (flag) at(s, i, j, k, comp) = at(s, i, j, k, comp) / at(s, i, j, k, RHO);
         else at(s, i, j, k, comp) = at(s, i, j, k, comp) * at(s, i, j, k, RHO);
     }
 }
 
-void convert_rhox_to_x(Ctx& c, int flag) {
-    launch(c, rg_grow(c, 0), 1, k_rhox_to_x, c.V(), c.nspec, flag);
+void convert_rhox_to_x(Ctx& c, int flag, int c0, int nc) {
+    launch(c, rg_grow(c, 0), 1, k_rhox_to_x, c.V(), c0, nc < 0 ? c.nspec : nc, flag);
 }
 
 // ============================================================ fluxes
 // MakeRhoXFlux, planar 3-D (Source/MaestroMakeFlux.cpp:189-306)
+// Species c0 .. c0+nc-1 of nspec; slot >= 0: the one species' edge state and flux are in
+// component `slot`.  The Rho flux (the species fluxes summed in order from 0) and etarhoflux
+// carry over between calls, so species streamed one call at a time sum in the same order.
 template <int D>
-__global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double* __restrict__ r0o,
-                            const double* __restrict__ r0n, const double* __restrict__ w0,
-                            const double* __restrict__ r0pe) {
+__global__ void k_rhox_flux(KARGS, int c0, int nc, int nspec, int slot, int spt, int do_eta,
+                            const double* __restrict__ r0o, const double* __restrict__ r0n,
+                            const double* __restrict__ w0, const double* __restrict__ r0pe) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView fl = VW(F_SFLUX0 + D), e = VW(F_SEDGE0 + D);
     const double u = at(VW(F_UMAC0 + D), i, j, k);
-    double frho = 0.0;
+    double frho = c0 == FIRSTSPEC ? 0.0 : at(fl, i, j, k, RHO);
     // etarhoflux is accumulated into species by species, as the reference does (:170-178)
     double eta = D == 2 && do_eta ? at(VW(F_ETA), i, j, k) : 0.0;
-    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+    for (int comp = c0; comp < c0 + nc; ++comp) {
+        const int ec = slot >= 0 ? slot : comp;
         const double rho0_edge = 0.5 * (r0o[k] + r0n[k]);
         double f = 0.0;
-        if (spt == 1) f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, comp);
-        else if (spt == 2) f = u * at(e, i, j, k, comp);
-        else f = u * at(e, i, j, k, RHO) * at(e, i, j, k, comp);
-        at(fl, i, j, k, comp) = f;
+        if (spt == 1) f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, ec);
+        else if (spt == 2) f = u * at(e, i, j, k, ec);
+        else f = u * at(e, i, j, k, RHO) * at(e, i, j, k, ec);
+        at(fl, i, j, k, ec) = f;
         if (D == 2 && do_eta) {
             eta += f;
             if (comp == FIRSTSPEC + nspec - 1) eta -= w0[k] * r0pe[k];
@@ -1254,16 +1264,18 @@ __global__ void k_rhox_flux(KARGS, int nspec, int spt, int do_eta, const double*
     if (D == 2 && do_eta) at(VW(F_ETA), i, j, k) = eta;
 }
 
-void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new, const double* r0e_new) {
-    if (c.sph) return make_rhox_flux_sph(c);  // face base state from MakeS0mac (F_S0MAC*, F_S0MACB*)
+void make_rhox_flux(Ctx& c, const double* r0_old, const double* r0e_old, const double* r0_new, const double* r0e_new,
+                    int c0, int nc, int slot) {
+    if (nc < 0) nc = c.nspec;
+    if (c.sph) return make_rhox_flux_sph(c, c0, nc, slot);  // face base state from MakeS0mac (F_S0MAC*, F_S0MACB*)
     if (c.ndim == 2) return make_rhox_flux_2d(c, r0_old, r0e_old, r0_new, r0e_new);
     const int do_eta = c.P.evolve_base_state && !c.P.use_exact_base_state;
     const double* w0 = c.b1("w0");
     const double* rpe = c.b1("rho0_predicted_edge");
-    launch(c, rg_grow(c, 0, 0), 1, k_rhox_flux<0>, c.V(), c.nspec, c.P.species_pred_type, 0, r0_old, r0_new, w0, rpe);
-    launch(c, rg_grow(c, 0, 1), 1, k_rhox_flux<1>, c.V(), c.nspec, c.P.species_pred_type, 0, r0_old, r0_new, w0, rpe);
-    launch(c, rg_grow(c, 0, 2), 1, k_rhox_flux<2>, c.V(), c.nspec, c.P.species_pred_type, do_eta, r0e_old, r0e_new,
-           w0, rpe);
+    const int ns = c.nspec, spt = c.P.species_pred_type;
+    launch(c, rg_grow(c, 0, 0), 1, k_rhox_flux<0>, c.V(), c0, nc, ns, slot, spt, 0, r0_old, r0_new, w0, rpe);
+    launch(c, rg_grow(c, 0, 1), 1, k_rhox_flux<1>, c.V(), c0, nc, ns, slot, spt, 0, r0_old, r0_new, w0, rpe);
+    launch(c, rg_grow(c, 0, 2), 1, k_rhox_flux<2>, c.V(), c0, nc, ns, slot, spt, do_eta, r0e_old, r0e_new, w0, rpe);
 }
 
 // MakeRhoHFlux, planar 3-D (Source/MaestroMakeFlux.cpp:673-786)
@@ -1335,6 +1347,20 @@ __global__ void k_sum_species(KARGS, int nspec) {
     at(e, i, j, k, RHO) = s;
 }
 
+// the same sum, one species at a time from edge-state component `slot`
+template <int D>
+__global__ void k_sum_species_step(KARGS, int slot, int first) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView e = VW(F_SEDGE0 + D);
+    at(e, i, j, k, RHO) = first ? at(e, i, j, k, slot) : at(e, i, j, k, RHO) + at(e, i, j, k, slot);
+}
+
+void sum_species_edge_step(Ctx& c, int slot, int first) {
+    launch(c, rg_grow(c, 0, 0), 1, k_sum_species_step<0>, c.V(), slot, first);
+    launch(c, rg_grow(c, 0, 1), 1, k_sum_species_step<1>, c.V(), slot, first);
+    launch(c, rg_grow(c, 0, 2), 1, k_sum_species_step<2>, c.V(), slot, first);
+}
+
 void sum_species_edges(Ctx& c) {
     if (c.ndim == 2) return sum_species_edges_2d(c);
     launch(c, rg_grow(c, 0, 0), 1, k_sum_species<0>, c.V(), c.nspec);
@@ -1346,17 +1372,22 @@ void sum_species_edges(Ctx& c) {
 // Source/MaestroAdvection.cpp:117-251.  The species update and the density / floor /
 // negative-species pass of the reference are two ParallelFors over the same cells; they
 // are one kernel here with the same per-cell order of operations.
-__global__ void k_update_rhox(KARGS, int nspec, double dt, RecipC r0, RecipC r1, RecipC r2, double half_cutoff) {
-    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+// the new (rho X) of one species from its flux in component fc of F_SFLUX*
+__device__ __forceinline__ void update_species_cell(const FabView* __restrict__ V, int nb, int b, int comp, int fc,
+                                                    double dt, const RecipC& r0, const RecipC& r1, const RecipC& r2,
+                                                    int i, int j, int k) {
     const FabView so = VW(F_SOLD), sn = VW(F_SNEW), fx = VW(F_SFLUX0), fy = VW(F_SFLUX1), fz = VW(F_SFLUX2),
                   fo = VW(F_SCALFORCE);
-    for (int n = 0; n < nspec; ++n) {
-        const int comp = FIRSTSPEC + n;
-        double divterm = div_c(at(fx, i + 1, j, k, comp) - at(fx, i, j, k, comp), r0);
-        divterm += div_c(at(fy, i, j + 1, k, comp) - at(fy, i, j, k, comp), r1);
-        divterm += div_c(at(fz, i, j, k + 1, comp) - at(fz, i, j, k, comp), r2);
-        at(sn, i, j, k, comp) = at(so, i, j, k, comp) + dt * (-divterm + at(fo, i, j, k, comp));
-    }
+    double divterm = div_c(at(fx, i + 1, j, k, fc) - at(fx, i, j, k, fc), r0);
+    divterm += div_c(at(fy, i, j + 1, k, fc) - at(fy, i, j, k, fc), r1);
+    divterm += div_c(at(fz, i, j, k + 1, fc) - at(fz, i, j, k, fc), r2);
+    at(sn, i, j, k, comp) = at(so, i, j, k, comp) + dt * (-divterm + at(fo, i, j, k, comp));
+}
+
+// rho from the species' changes, the density floor and the negative-species fix
+__device__ __forceinline__ void rhox_fix_cell(const FabView* __restrict__ V, int nb, int b, int nspec,
+                                              double half_cutoff, int i, int j, int k) {
+    const FabView so = VW(F_SOLD), sn = VW(F_SNEW);
     double rho = at(so, i, j, k, RHO);
     bool neg = false;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
@@ -1384,6 +1415,22 @@ __global__ void k_update_rhox(KARGS, int nspec, double dt, RecipC r0, RecipC r1,
             }
         }
     }
+}
+
+__global__ void k_update_rhox(KARGS, int nspec, double dt, RecipC r0, RecipC r1, RecipC r2, double half_cutoff) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    for (int n = 0; n < nspec; ++n) update_species_cell(V, nb, b, FIRSTSPEC + n, FIRSTSPEC + n, dt, r0, r1, r2, i, j, k);
+    rhox_fix_cell(V, nb, b, nspec, half_cutoff, i, j, k);
+}
+
+__global__ void k_update_species(KARGS, int comp, int fc, double dt, RecipC r0, RecipC r1, RecipC r2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    update_species_cell(V, nb, b, comp, fc, dt, r0, r1, r2, i, j, k);
+}
+
+__global__ void k_update_rhox_fix(KARGS, int nspec, double half_cutoff) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    rhox_fix_cell(V, nb, b, nspec, half_cutoff, i, j, k);
 }
 
 __global__ void k_update_rhoh(KARGS, double dt, RecipC r0, RecipC r1, RecipC r2, int eos_check, double cutoff,
@@ -1506,6 +1553,15 @@ void update_scal(Ctx& c, int start_comp) {
         launch(c, rt, 1, k_update_rhox, c.V(), c.nspec, c.P.dt, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
                make_recip(c.P.dx[2]), 0.5 * c.P.base_cutoff_density);
     }
+}
+
+void update_species(Ctx& c, int comp, int slot) {
+    launch(c, rg_grow(c, 0), 1, k_update_species, c.V(), comp, slot, c.P.dt, make_recip(c.P.dx[0]),
+           make_recip(c.P.dx[1]), make_recip(c.P.dx[2]));
+}
+
+void update_rhox_fix(Ctx& c) {
+    launch(c, rg_grow(c, 0), 1, k_update_rhox_fix, c.V(), c.nspec, 0.5 * c.P.base_cutoff_density);
 }
 
 }  // namespace madv

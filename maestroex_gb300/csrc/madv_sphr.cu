@@ -369,29 +369,32 @@ void put_in_pert_form_sph(Ctx& c, const double* d_s0, int comp, int flag) {
 
 // MakeRhoXFlux, spherical (Source/MaestroMakeFlux.cpp:56-71, 306-408): the face base state is
 // the LinComb 0.5 old + 0.5 new of MakeS0mac (F_S0MAC*, F_S0MACB*)
+// species c0 .. c0+nc-1; slot >= 0: the one species' edge state and flux in component `slot`,
+// the Rho flux carried over between calls (as in the plane-parallel kernel)
 template <int D>
-__global__ void k_rhox_flux_sph(KARGS, int nspec, int spt) {
+__global__ void k_rhox_flux_sph(KARGS, int c0, int nc, int slot, int spt) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView fl = VW(F_SEDGE0 + D), sf = VW(F_SFLUX0 + D);
     const double u = at(VW(F_UMAC0 + D), i, j, k);
     const double rho0_edge = 0.5 * at(VW(F_S0MAC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACB0 + D), i, j, k);
-    double frho = 0.0;
-    for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
+    double frho = c0 == FIRSTSPEC ? 0.0 : at(sf, i, j, k, RHO);
+    for (int comp = c0; comp < c0 + nc; ++comp) {
+        const int ec = slot >= 0 ? slot : comp;
         double f = 0.0;
-        if (spt == 1) f = u * (rho0_edge + at(fl, i, j, k, RHO)) * at(fl, i, j, k, comp);
-        else if (spt == 2) f = u * at(fl, i, j, k, comp);
-        else f = u * at(fl, i, j, k, RHO) * at(fl, i, j, k, comp);
-        at(sf, i, j, k, comp) = f;
+        if (spt == 1) f = u * (rho0_edge + at(fl, i, j, k, RHO)) * at(fl, i, j, k, ec);
+        else if (spt == 2) f = u * at(fl, i, j, k, ec);
+        else f = u * at(fl, i, j, k, RHO) * at(fl, i, j, k, ec);
+        at(sf, i, j, k, ec) = f;
         frho += f;
     }
     at(sf, i, j, k, RHO) = frho;
 }
 
-void make_rhox_flux_sph(Ctx& c) {
-    const int ns = c.nspec, spt = c.P.species_pred_type;
-    launch(c, rg_grow(c, 0, 0), 1, k_rhox_flux_sph<0>, c.V(), ns, spt);
-    launch(c, rg_grow(c, 0, 1), 1, k_rhox_flux_sph<1>, c.V(), ns, spt);
-    launch(c, rg_grow(c, 0, 2), 1, k_rhox_flux_sph<2>, c.V(), ns, spt);
+void make_rhox_flux_sph(Ctx& c, int c0, int nc, int slot) {
+    const int spt = c.P.species_pred_type;
+    launch(c, rg_grow(c, 0, 0), 1, k_rhox_flux_sph<0>, c.V(), c0, nc, slot, spt);
+    launch(c, rg_grow(c, 0, 1), 1, k_rhox_flux_sph<1>, c.V(), c0, nc, slot, spt);
+    launch(c, rg_grow(c, 0, 2), 1, k_rhox_flux_sph<2>, c.V(), c0, nc, slot, spt);
 }
 
 // MakeRhoHFlux, spherical (Source/MaestroMakeFlux.cpp:540-575, 788-1000).  Exact base state,

@@ -21,19 +21,29 @@ class MultiFab:
     ``nodal`` = -1 for cell data, d for faces normal to direction d.
     """
 
+    ALIGN = 32  # doubles: every FAB starts on a 256-byte boundary
+
     def __init__(self, boxes, ncomp, ngrow, nodal=-1, device="cuda", fill=0.0):
         self.boxes = [tuple(int(v) for v in b) for b in boxes]
         self.ncomp, self.ng, self.nodal = ncomp, ngrow, nodal
         self.fabs, self.los, self.his = [], [], []
+        shapes, offs, tot = [], [], 0
         for b in self.boxes:
             lo = [b[0] - ngrow, b[1] - ngrow, b[2] - ngrow]
             hi = [b[3] + ngrow, b[4] + ngrow, b[5] + ngrow]
             if nodal >= 0:
                 hi[nodal] += 1
             shape = (ncomp, hi[2] - lo[2] + 1, hi[1] - lo[1] + 1, hi[0] - lo[0] + 1)
-            self.fabs.append(torch.full(shape, fill, dtype=torch.float64, device=device))
+            shapes.append(shape)
+            offs.append(tot)
+            tot += -(-int(np.prod(shape)) // self.ALIGN) * self.ALIGN
             self.los.append(lo)
             self.his.append(hi)
+        # one allocation for the whole MultiFab (thousands of per-box allocations would each
+        # round up in the caching allocator), FABs as views into it
+        self.data = torch.full((max(tot, 1),), fill, dtype=torch.float64, device=device)
+        for shape, o in zip(shapes, offs):
+            self.fabs.append(self.data[o:o + int(np.prod(shape))].view(shape))
         self._desc = None
 
     def desc(self):
@@ -176,7 +186,9 @@ class ScalarAdvectionStage:
         check(lib().madv_set_base_state_levels(self.ctx, len(levels), arr))
 
     def stage_forward_levels(self, bufs, mode=capi.MODE_BATCHED, stream=None):
-        """The stage on all levels; bufs[l] holds level l's MultiFabs (StageBuffers)."""
+        """The stage on all levels; bufs[l] holds level l's MultiFabs (StageBuffers).  Buffers
+        without edge states and fluxes (StageBuffers(edges=False)) ask for neither: the library
+        then streams the species through slots of its own."""
         s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
         nl = len(bufs)
 
@@ -184,6 +196,8 @@ class ScalarAdvectionStage:
             return (MadvMultiFab * nl)(*[getattr(b, name).desc() for b in bufs])
 
         def faces(name):
+            if getattr(bufs[0], name) is None:
+                return None
             return (MadvMultiFab * (3 * nl))(*[getattr(b, name)[d].desc() for b in bufs for d in range(3)])
 
         args = [cells("uold"), cells("sold"), cells("gpi"), cells("thermal"), cells("snew"), faces("umac"),
@@ -346,9 +360,10 @@ class ScalarAdvectionStage:
 
 
 class StageBuffers:
-    """The caller-side MultiFabs of one stage configuration (as AdvanceTimeStep owns them)."""
+    """The caller-side MultiFabs of one stage configuration (as AdvanceTimeStep owns them).
+    edges=False: no edge-state and flux MultiFabs (a caller that needs neither after the stage)."""
 
-    def __init__(self, cfg, device="cuda"):
+    def __init__(self, cfg, device="cuda", edges=True):
         boxes = cfg["boxes"]
         nscal = 4 + cfg["nspec"]
         ng = 4 if cfg["ppm_type"] == 2 else 3
@@ -361,8 +376,8 @@ class StageBuffers:
         self.thermal = MultiFab(boxes, 1, 1, device=device)
         self.snew = MultiFab(boxes, nscal, ng, device=device)
         self.umac = [MultiFab(boxes, 1, 1, nodal=d, device=device) for d in range(nd)]
-        self.sedge = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(nd)]
-        self.sflux = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(nd)]
+        self.sedge = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(nd)] if edges else None
+        self.sflux = [MultiFab(boxes, nscal, 0, nodal=d, device=device) for d in range(nd)] if edges else None
         self.eta = MultiFab(boxes, 1, 0, nodal=nd - 1, device=device)
 
     def load(self, cfg):
@@ -383,10 +398,11 @@ def make_stage(cfg):
     return st
 
 
-def run_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
-    """Run the whole stage on the GPU for a config dict; returns domain arrays (numpy)."""
+def run_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda", edges=True):
+    """Run the whole stage on the GPU for a config dict; returns domain arrays (numpy).
+    edges=False: no edge states or fluxes asked for (3-D: the species are streamed)."""
     st = make_stage(cfg)
-    buf = StageBuffers(cfg, device).load(cfg)
+    buf = StageBuffers(cfg, device, edges).load(cfg)
     st.stage_forward(buf.uold, buf.sold, buf.gpi, buf.snew, buf.umac, buf.sedge, buf.sflux, buf.eta,
                      thermal=buf.thermal, mode=mode)
     torch.cuda.synchronize()
@@ -394,13 +410,14 @@ def run_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
     nd = buf.nd
     res = dict(
         umac_end=[buf.umac[d].to_domain(n)[0].cpu().numpy() for d in range(nd)],
-        sedge=[buf.sedge[d].to_domain(n).cpu().numpy() for d in range(nd)],
-        sflux=[buf.sflux[d].to_domain(n).cpu().numpy() for d in range(nd)],
         snew=buf.snew.to_domain(n).cpu().numpy(),
         sold_end=buf.sold.to_domain(n).cpu().numpy(),
         etarhoflux=buf.eta.to_domain(n)[0].cpu().numpy(),
         launches=st.launch_count(),
     )
+    if edges:
+        res["sedge"] = [buf.sedge[d].to_domain(n).cpu().numpy() for d in range(nd)]
+        res["sflux"] = [buf.sflux[d].to_domain(n).cpu().numpy() for d in range(nd)]
     st.close()
     return res
 
@@ -414,18 +431,19 @@ def make_amr_stage(cfg):
     return st
 
 
-def amr_buffers(cfg, device="cuda"):
+def amr_buffers(cfg, device="cuda", edges=True):
     """One StageBuffers per level, loaded with the level's input arrays.  A level marked
     "inject" has no arrays of its own: each of its cells takes the value of its parent cell
-    on the level below (filled on the device box by box)."""
+    on the level below (filled on the device box by box).  edges=False: no edge-state and
+    flux MultiFabs."""
     out = []
     for lev, L in enumerate(cfg["levels"]):
         c = dict(cfg)
         c.update(L)
         if not L.get("inject"):
-            out.append(StageBuffers(c, device).load(c))
+            out.append(StageBuffers(c, device, edges).load(c))
             continue
-        buf = StageBuffers(c, device)
+        buf = StageBuffers(c, device, edges)
         P = cfg["levels"][lev - 1]
         for name in ("uold", "sold", "gpi", "thermal"):
             src = torch.from_numpy(np.ascontiguousarray(P[name]))  # host: only parent blocks travel
@@ -496,23 +514,26 @@ def _sph_rebin(blk, bx, fine, coarse):
     return out
 
 
-def run_amr_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda"):
-    """The stage on every level of cfg["levels"]; returns one dict of domain arrays per level."""
+def run_amr_stage_gpu(cfg, mode=capi.MODE_BATCHED, device="cuda", edges=True):
+    """The stage on every level of cfg["levels"]; returns one dict of domain arrays per level
+    (edges=False: species streamed, no edge states or fluxes returned)."""
     st = make_amr_stage(cfg)
-    bufs = amr_buffers(cfg, device)
+    bufs = amr_buffers(cfg, device, edges)
     st.stage_forward_levels(bufs, mode=mode)
     torch.cuda.synchronize()
     res = []
     for L, buf in zip(cfg["levels"], bufs):
         n = L["n"]
-        res.append(dict(
+        r = dict(
             umac_end=[buf.umac[d].to_domain(n)[0].cpu().numpy() for d in range(3)],
-            sedge=[buf.sedge[d].to_domain(n).cpu().numpy() for d in range(3)],
-            sflux=[buf.sflux[d].to_domain(n).cpu().numpy() for d in range(3)],
             snew=buf.snew.to_domain(n).cpu().numpy(),
             sold_end=buf.sold.to_domain(n).cpu().numpy(),
             etarhoflux=buf.eta.to_domain(n)[0].cpu().numpy(),
-        ))
+        )
+        if edges:
+            r["sedge"] = [buf.sedge[d].to_domain(n).cpu().numpy() for d in range(3)]
+            r["sflux"] = [buf.sflux[d].to_domain(n).cpu().numpy() for d in range(3)]
+        res.append(r)
     res[0]["launches"] = st.launch_count()
     st.close()
     return res
