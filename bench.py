@@ -315,7 +315,9 @@ def run_amr(args, ws, steps, warmup, barrier):
     from maestroex_gb300.stage import amr_buffers, make_amr_stage
     cfg = configs.workload_amr(n0=args.amr_n, nspec=args.nspec)
     st = make_amr_stage(cfg)
-    bufs = amr_buffers(cfg, edges=edges)
+    if args.component_streams >= 0:
+        st.set_option("component_streams", args.component_streams)
+    bufs = amr_buffers(cfg)
     names = ("uold", "sold", "gpi")
     snap = [{n: [t.clone() for t in getattr(b, n).fabs] for n in names} for b in bufs]
 
@@ -908,6 +910,9 @@ def main():
                     help="run one batched stage and exit (the command ncu captures)")
     ap.add_argument("--staged-ppm", type=int, default=-1, choices=[-1, 0, 1],
                     help="PPM form of the headline stage: 1 staged sweeps, 0 three launches, -1 the library default")
+    ap.add_argument("--component-streams", type=int, default=-1, choices=[-1, 0, 1],
+                    help="headline and AMR stages: 1 MakeEdgeScal components alternate between two streams, "
+                         "0 one stream, -1 the library default")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     warmup = max(args.warmup, 3)
@@ -953,6 +958,8 @@ def main():
     st = make_stage(cfg)
     if args.staged_ppm >= 0:
         st.set_option("staged_ppm", args.staged_ppm)
+    if args.component_streams >= 0:
+        st.set_option("component_streams", args.component_streams)
     buf = StageBuffers(cfg).load(cfg)
     snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
 

@@ -413,6 +413,12 @@ int madv_autotune_apply(madv_ctx* ctx, const char* json);
  *   "sweep_tile_Da", "sweep_tile_Db" (D = 0, 1, 2): cells of a staged tile across
  *                     direction D, in the first / second transverse direction (x before y
  *                     before z); defaults 4 x 2 for D = 0 and 32 x 2 for D = 1, 2.
+ *   "component_streams" 1: in a stage call (3-D, not per box, not while madv_profile
+ *                     times launches) the components of each MakeEdgeScal alternate between
+ *                     the caller's stream and a second one, which works in its own copy of
+ *                     the per-component scratch (allocated at first use: about 46 doubles per
+ *                     cell); 0 (default): one stream -- the stage is FP64-issue bound and
+ *                     the overlap measures 0.5% on GB300.
  * Returns MADV_ERR_PARAM for an unknown key or a value outside 1..256. */
 int madv_set_option(madv_ctx* ctx, const char* key, int value);
 

@@ -328,6 +328,13 @@ static void free_layout(Ctx& c) {
         if (kv.second.d) cudaFree(kv.second.d);
     c.amr_tables.clear();
     sweep_free(c);
+    for (auto& kv : c.side_scratch) cudaFree(kv.second);
+    c.side_scratch.clear();
+    if (c.dviews_side) cudaFree(c.dviews_side);
+    c.dviews_side = nullptr;
+    if (c.hviews_side) cudaFreeHost(c.hviews_side);
+    c.hviews_side = nullptr;
+    c.side_mirror = nullptr;
     if (c.d_owner) cudaFree(c.d_owner);
     c.d_owner = nullptr;
     c.h_owner.clear();
@@ -950,6 +957,51 @@ static FabView* alias_fields(Ctx& c, StageIO& io) {
     return base;
 }
 
+// The per-component scratch of MakeEdgeScal (3-D): what one component's chain writes
+// before its edge state (PPM, slopes, predictor, transverse states, traced force)
+static const int SIDE_SCRATCH[] = {F_DSVL, F_FACE0, F_FACE1, F_FACE2, F_IPC0, F_IMC0, F_SLOPE, F_SL0, F_SL1,
+                                   F_SL2,  F_SR0,   F_SR1,   F_SR2,   F_SIMH0, F_SIMH1, F_SIMH2, F_Q01, F_Q02,
+                                   F_Q10,  F_Q12,   F_Q20,   F_Q21,   F_IPF,  F_IMF};
+
+// component streams: the side stream's view table, a copy of the current one (c.dviews,
+// whose host image is `host`) with the per-component scratch moved to the side's copies
+// (allocated and zeroed at first use); uploaded on the level's stream
+static void side_views(Ctx& c, const FabView* host) {
+    c.side_mirror = nullptr;
+    if (!c.comp_streams || c.ndim != 3) return;
+    if (!c.side) {
+        if (!cuda_ok(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking), "cudaStreamCreate") ||
+            !cuda_ok(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming), "cudaEventCreate") ||
+            !cuda_ok(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming), "cudaEventCreate"))
+            throw Fail{MADV_ERR_CUDA};
+    }
+    const size_t nv = (size_t)NF_TOTAL * c.nb;
+    if (!c.dviews_side) {
+        if (!cuda_ok(cudaMalloc(&c.dviews_side, sizeof(FabView) * nv), "cudaMalloc(views)") ||
+            !cuda_ok(cudaMallocHost(&c.hviews_side, sizeof(FabView) * nv), "cudaMallocHost(views)"))
+            throw Fail{MADV_ERR_CUDA};
+    }
+    std::memcpy(c.hviews_side, host, sizeof(FabView) * nv);
+    for (int f : SIDE_SCRATCH) {
+        const Field& F = c.F[f];
+        if (!F.base || F.bytes == 0) continue;
+        double*& dup = c.side_scratch[f];
+        if (!dup) {
+            if (!cuda_ok(cudaMalloc(&dup, F.bytes), "cudaMalloc(side scratch)") ||
+                !cuda_ok(cudaMemset(dup, 0, F.bytes), "cudaMemset"))
+                throw Fail{MADV_ERR_CUDA};
+        }
+        for (int b = 0; b < c.nb; ++b) {
+            FabView& v = c.hviews_side[(size_t)f * c.nb + b];
+            v.p = dup + (v.p - F.base);
+        }
+    }
+    if (!cuda_ok(cudaMemcpyAsync(c.dviews_side, c.hviews_side, sizeof(FabView) * nv, cudaMemcpyHostToDevice, c.stream),
+                 "cudaMemcpyAsync(views)"))
+        throw Fail{MADV_ERR_CUDA};
+    c.side_mirror = c.dviews;
+}
+
 static int bind_stage(Ctx& c, const StageIO& io) {
     int rc;
     if ((rc = bind(c, U_UOLD, io.uold, c.ndim, -1, 0))) return rc;
@@ -1193,6 +1245,11 @@ static void destroy_level(Ctx& c) {
     c.d1.clear();
     for (auto e : c.ev_pool) cudaEventDestroy(e);
     c.ev_pool.clear();
+    if (c.side) cudaStreamDestroy(c.side);
+    if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+    if (c.ev_join) cudaEventDestroy(c.ev_join);
+    c.side = nullptr;
+    c.ev_fork = c.ev_join = nullptr;
     if (c.box_scratch) cudaFree(c.box_scratch);
     c.box_scratch = nullptr;
     if (c.d_bcs) cudaFree(c.d_bcs);
@@ -1719,8 +1776,10 @@ static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab*
         Hier& H;
         std::vector<FabView*>& v;
         ~Restore() {
-            for (int l = 0; l < (int)v.size(); ++l)
+            for (int l = 0; l < (int)v.size(); ++l) {
                 if (v[l]) H[l].dviews = v[l];
+                H[l].side_mirror = nullptr;
+            }
         }
     } restore{H, base_views};
     try {
@@ -1728,6 +1787,8 @@ static int stage_forward_h(madv_ctx* h, int mode, int nlev, const madv_multifab*
             if ((rc = bind_stage(H[l], io[l]))) return rc;
         // caller FABs laid out as the stage's fields are worked in directly (no copies)
         for (int l = 0; l < nlev; ++l) base_views[l] = alias_fields(H[l], io[l]);
+        for (int l = 0; l < nlev; ++l)
+            side_views(H[l], H[l].dviews == H[l].dviews_alias ? H[l].hviews_alias : H[l].hviews_pinned);
         if (mode == MADV_MODE_GRAPH) {
             std::vector<const void*> key;
             for (int l = 0; l < nlev; ++l) {
@@ -2559,6 +2620,8 @@ int madv_set_option(madv_ctx* h, const char* key, int value) {
     const std::string k(key);
     if (k == "staged_ppm") {
         for (auto* c : H.L) c->staged_ppm = value != 0;
+    } else if (k == "component_streams") {
+        for (auto* c : H.L) c->comp_streams = value != 0;
     } else if (k.rfind("sweep_tile_", 0) == 0 && k.size() == 13 && k[11] >= '0' && k[11] <= '2' &&
                (k[12] == 'a' || k[12] == 'b')) {
         if (value < 1 || value > 256) return MADV_ERR_PARAM;

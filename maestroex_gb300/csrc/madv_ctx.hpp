@@ -185,6 +185,18 @@ struct Ctx {
     // across each direction D (cells in the two transverse directions), default when absent
     bool staged_ppm = false;
     std::map<int, std::array<int, 2>> sweep_shape;
+    // component streams (option "component_streams"): the components of a MakeEdgeScal call
+    // alternate between the level's stream and `side`, the side's components working in
+    // copies of the per-component scratch fields (views in dviews_side, a copy of the table
+    // side_mirror with those fields moved); built per stage call, used while dviews ==
+    // side_mirror
+    bool comp_streams = false;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    std::map<int, double*> side_scratch;
+    FabView* dviews_side = nullptr;
+    FabView* hviews_side = nullptr;
+    const FabView* side_mirror = nullptr;
     // scratch of the single-box entry points (madv_ppm), grown on demand
     double* box_scratch = nullptr;
     long box_scratch_n = 0;

@@ -1112,7 +1112,22 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
     if (c.ndim == 2) return make_edge_scal_2d_entry(c, start_comp, num_comp, which_bcs, is_cons);
     const BCRecD* bh = bcs_host(c, which_bcs);
     if (setup) edge_scal_setup(c, is_cons);
+    // component streams: every other component on the side stream, in its own scratch
+    // (components are independent: each reads the state, the velocities and the shared
+    // coefficients formed above, and writes only its scratch and its edge state)
+    // (not while per-launch timing runs: the autotuner's trials time each kernel alone)
+    const bool two = c.comp_streams && c.side_mirror && c.side_mirror == c.dviews && !c.per_box &&
+                     !c.edge_tape_begin && !c.staged_ppm && !c.profiling && num_comp > 1;
+    cudaStream_t main_stream = c.stream;
+    FabView* main_views = c.dviews;
+    if (two && !c.dry) {
+        cudaEventRecord(c.ev_fork, main_stream);
+        cudaStreamWaitEvent(c.side, c.ev_fork, 0);
+    }
     for (int comp = start_comp; comp < start_comp + num_comp; ++comp) {
+        const bool alt = two && ((comp - start_comp) & 1);
+        c.stream = alt ? c.side : main_stream;
+        c.dviews = alt ? c.dviews_side : main_views;
         if (c.edge_tape_begin) c.edge_tape_begin(comp);
         const BCRecD& bc = bh[comp];  // start_bccomp == start_scomp at every call site
         if (c.P.ppm_type == 0) {
@@ -1139,6 +1154,12 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
         es_edges_launch<1>(c, comp, bc, is_cons, force_zero, v1, oc);
         es_edges_launch<2>(c, comp, bc, is_cons, force_zero, v2, oc);
         if (c.edge_tape) c.edge_tape(comp);
+    }
+    c.stream = main_stream;
+    c.dviews = main_views;
+    if (two && !c.dry) {
+        cudaEventRecord(c.ev_join, c.side);
+        cudaStreamWaitEvent(main_stream, c.ev_join, 0);
     }
 }
 
