@@ -205,17 +205,19 @@ def workload_planar(n=256, box=64, nspec=13, seed=20261203 + 1):
 
 
 def adjoint_config(n=(128, 128, 128), max_grid=64, nspec=3, seed=20261203 + 4, cfl=0.5, bc_lo=(INTERIOR,) * 3,
-                   bc_hi=(INTERIOR,) * 3, w0_amp=0.0, ppm_type=1):
+                   bc_hi=(INTERIOR,) * 3, w0_amp=0.0, ppm_type=1, gravity=False):
     """3-D single-level configuration of the multi-step adjoint (periodic unless bc_lo /
-    bc_hi say otherwise): the velocity is held fixed and does not depend on the state
-    (grav_cell = 0, gpi = 0; w0 of amplitude w0_amp, default 0), ppm_type 1 (or 2),
-    species_pred_type 1, enthalpy_pred_type 1;
-    dt from CFL 0.5.  The density perturbation rho - rho0 is 1% of rho0, so that a
-    perturbation of 1e-6 rho is small against it."""
+    bc_hi say otherwise): the cell velocity is held fixed (gpi = 0; w0 of amplitude w0_amp,
+    default 0), ppm_type 1 (or 2), species_pred_type 1, enthalpy_pred_type 1; dt from CFL
+    0.5.  gravity=False: grav_cell = 0, so the MAC velocity does not depend on the state;
+    True: the constant gravity of planar_config, the MAC velocity taking the buoyancy of the
+    density through MakeVelForce.  The density perturbation rho - rho0 is 1% of rho0, so
+    that a perturbation of 1e-6 rho is small against it."""
     cfg = planar_config(n=n, nspec=nspec, ppm_type=ppm_type, bc_lo=bc_lo, bc_hi=bc_hi,
                         max_grid=max_grid, seed=seed, w0_amp=w0_amp, cfl=cfl, gpi_amp=0.0, evolve_base_state=0,
                         rho_pert=1.0e-2)
-    cfg["grav_cell"] = np.zeros_like(cfg["grav_cell"])
+    if not gravity:
+        cfg["grav_cell"] = np.zeros_like(cfg["grav_cell"])
     return cfg
 
 

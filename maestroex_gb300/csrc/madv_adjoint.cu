@@ -148,9 +148,30 @@ __global__ void k_adj_flux(KARGS, int nspec, double dtdx, const double* __restri
     const double fh = fbar(RHOH);
     at(ae, i, j, k, RHOH) = u * fh;
     if (want_u) {
-        gu += (0.5 * (h0a[k] + h0b[k]) + at(e, i, j, k, RHOH)) * fh;
+        // spherical: the (rho h) term reads MakeS0mac's faces (k_adj_flux_rhoh_u_sph)
+        if (!sph) gu += (0.5 * (h0a[k] + h0b[k]) + at(e, i, j, k, RHOH)) * fh;
         at(AW(A_AUMAC0 + D), i, j, k) += gu;
     }
+}
+
+// The (rho h) flux's face-velocity adjoint, spherical (k_rhoh_flux_sph, enthalpy_pred_type 1):
+// F_h = u (rhoh0_face + rhoh'_e) with rhoh0_face the LinComb of F_S0MAC* and F_S0MACB*
+// (exact base state), or rho0_face h0_face (uniform bins: rho0 in F_S0MACC* / F_S0MACD*).
+template <int D>
+__global__ void k_adj_flux_rhoh_u_sph(KARGS, double dtdx, int exact) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const RegionBox& rr = R[e_];
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const FabView an = AW(A_ASNEW);
+    double a = 0.0;
+    if (I < rr.lo[D] + rr.n[D] - 1) a += at(an, i, j, k, RHOH);
+    if (I > rr.lo[D]) a -= at(an, i - di, j - dj, k - dk, RHOH);
+    if (a == 0.0) return;
+    const double h0f = 0.5 * at(VW(F_S0MAC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACB0 + D), i, j, k);
+    const double base =
+        exact ? h0f : (0.5 * at(VW(F_S0MACC0 + D), i, j, k) + 0.5 * at(VW(F_S0MACD0 + D), i, j, k)) * h0f;
+    at(AW(A_AUMAC0 + D), i, j, k) += (base + at(VW(F_SEDGE0 + D), i, j, k, RHOH)) * (dtdx * a);
 }
 
 // ------------------------------------------------------------------ MakeEdgeScal^T
@@ -440,8 +461,11 @@ __device__ __forceinline__ Dv ppm2_face_dv(const Dv* S, const RecipC& r6) {
 // forward's branch (ppm2_edges_adj).  Face adjoints: faces -1, 0 into A_ASM of cells
 // -1, 0 and faces 1, 2 into A_ASP of cells 0, 1 (k_adj_ppm2_face gathers A_ASM(f) +
 // A_ASP(f-1)); cell adjoints to slot ts, component tcomp.
+// want_u: the tracing coefficients' velocity adjoint into A_AUMAC0+D, as for ppm_type 1
+// (the tracing is the same function of the limited edges sm, sp and s6).
 template <int D>
-__global__ void k_adj_ppm2_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp, long long epsb) {
+__global__ void k_adj_ppm2_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp, long long epsb, double dtdx,
+                                int want_u) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const double ipb = at(AW(A_ASL0 + D), i + di, j + dj, k + dk, lc);
@@ -477,6 +501,15 @@ __global__ void k_adj_ppm2_cell(KARGS, int fs, int sc, int lc, int ts, int tcomp
     double gS[5] = {0.0, 0.0, bs0, 0.0, 0.0}, gF[4] = {0.0, 0.0, 0.0, 0.0};
     double sm, sp;
     ppm2_edges_adj(Sv, Fv, bsm, bsp, gS, gF, sm, sp);
+    if (want_u) {  // d ip/dA = -(sp - sm - B s6), d ip/dB = A s6; d im/dA = sp - sm + B s6, d im/dB = A s6
+        const double s6 = 6.0 * Sv[2] - 3.0 * (sm + sp), dpm = sp - sm;
+        const FabView au = AW(A_AUMAC0 + D);
+        if (gt_t(up, epsb))
+            atomicAdd(&at(au, i + di, j + dj, k + dk),
+                      copysign(dtdx, up) * ipb * (half(Bp * s6 - dpm) - (2.0 / 3.0) * Ap * s6));
+        if (lt_negt(um, epsb))
+            atomicAdd(&at(au, i, j, k), copysign(dtdx, um) * imb * (half(dpm + Bm * s6) - (2.0 / 3.0) * Am * s6));
+    }
     const FabView as = AW(ts);
     for (int m = 0; m < 5; ++m)
         if (gS[m] != 0.0) atomicAdd(&at(as, i + (m - 2) * di, j + (m - 2) * dj, k + (m - 2) * dk, tcomp), gS[m]);
@@ -858,10 +891,11 @@ __global__ void k_adj_x(KARGS, int comp) {
 // want_u: the force's face-velocity adjoint, d f/du(i+1) = -s/dx, d f/dw(k+1) =
 // -(s - s0 + s0e(k+1))/dz, ...  (atomically into A_AUMAC0..2).  s0e(k) is the edge value
 // the forward read from its Cartesian copy: above the top cell that is the ghost cell
-// FillPatch filled, in a periodic domain the image of the bottom edge.
+// FillPatch filled (BCS_F): in a periodic domain the image of the bottom edge, else (first-
+// order extrapolation, or the even reflection of symmetry) the top cell's own.
 __global__ void k_adj_pert(KARGS, int comp, const double* __restrict__ s0a, const double* __restrict__ s0e,
                            RecipC r0, RecipC r1, RecipC r2, int domlo, int domhi, int want_u,
-                           const double* __restrict__ w0, int sph) {
+                           const double* __restrict__ w0, int sph, int zper) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
     // ModifyScalForce runs between Addw0(-1) and Addw0(+1): its umac is the MAC velocity
@@ -880,14 +914,14 @@ __global__ void k_adj_pert(KARGS, int comp, const double* __restrict__ s0a, cons
     if (sph == 2) divu = divu + at(VW(F_DIVW0), i, j, k);
     const double fb = at(AW(A_AFORCE), i, j, k);
     at(AW(A_ASOLD), i, j, k, comp) += at(AW(A_AS), i, j, k) - divu * fb;
-    if (want_u && fb != 0.0) {
+    if (want_u && fb != 0.0 && !sph) {  // spherical: k_adj_pert_u_sph
         const double s = at(AW(A_WSOLD), i, j, k, comp), s0 = s0a[k];
         const double gx = s * fb / r0.y, gy = s * fb / r1.y;
         atomicAdd(&at(AW(A_AUMAC0), i + 1, j, k), -gx);
         atomicAdd(&at(AW(A_AUMAC0), i, j, k), gx);
         atomicAdd(&at(AW(A_AUMAC1), i, j + 1, k), -gy);
         atomicAdd(&at(AW(A_AUMAC1), i, j, k), gy);
-        const int kp = k + 1 > domhi ? domlo : k + 1;
+        const int kp = k + 1 > domhi ? (zper ? domlo : domhi) : k + 1;
         atomicAdd(&at(AW(A_AUMAC2), i, j, k + 1), -(s - s0 + s0e[kp]) * fb / r2.y);
         atomicAdd(&at(AW(A_AUMAC2), i, j, k), (s - s0 + s0e[k]) * fb / r2.y);
     }
@@ -1090,11 +1124,12 @@ static void adj_predictor_launch(Ctx& c, const BCRecD& bc) {
 template <int D, int UMAC>
 static void adj_ppm_launch(Ctx& c, int fs, int sc, int lc, int ts, int tc, double* dir, size_t dir_bytes,
                           int want_u, int faces, const BCRecD& bc) {
-    if (c.P.ppm_type == 2) {  // scalars (UMAC = 1, no velocity gradient), no ext_dir / hoextrap side
+    if (c.P.ppm_type == 2) {  // scalars (UMAC = 1), no ext_dir / hoextrap side
         if (!c.dry) cudaMemsetAsync(dir, 0, dir_bytes, c.stream);
         int g[3] = {1, 1, 1};
         g[D] = 2;
-        launch(c, rg_grow(c, 1), 1, k_adj_ppm2_cell<D>, c.V(), fs, sc, lc, ts, tc, dbits_host(c.P.rel_eps));
+        launch(c, rg_grow(c, 1), 1, k_adj_ppm2_cell<D>, c.V(), fs, sc, lc, ts, tc, dbits_host(c.P.rel_eps),
+               c.P.dt / c.P.dx[D], want_u);
         launch(c, region(c, g[0], g[1], g[2], g[0], g[1], g[2], D), 1, k_adj_ppm2_face<D>, c.V(), fs, sc, ts, tc,
                make_recip(6.0));
         return;
@@ -1170,7 +1205,7 @@ void adj_pert_force(Ctx& c, int comp, int want_u) {
     const double* s0e = c.b1(comp == RHO ? "rho0_edge_old" : "rhoh0_edge_old");
     launch(c, rg_grow(c, 0), 1, k_adj_pert, c.V(), comp, s0, s0e, make_recip(c.P.dx[0]), make_recip(c.P.dx[1]),
            make_recip(c.P.dx[2]), c.P.dom_lo[2], c.P.dom_hi[2], want_u, c.b1("w0"),
-           c.sph ? (c.geo.exact ? 1 : 2) : 0);
+           c.sph ? (c.geo.exact ? 1 : 2) : 0, c.per[2] ? 1 : 0);
 }
 
 // F_TCOEF^T into face slots ts .. ts+2 (A_AUMAC0 or A_AUTRANS0)
@@ -1227,6 +1262,202 @@ void adj_vel_pred(Ctx& c, double* dir, size_t dir_bytes) {
         adj_ppm_launch<1, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1, c.bcs_u[cc]);
         adj_ppm_launch<2, 0>(c, F_UTILDE, cc, cc, A_AUT, cc, dir, dir_bytes, 1, 1, c.bcs_u[cc]);
     }
+}
+
+// ModifyScalForce's face-velocity adjoint, spherical, fullform 0 (k_modify_scal_force_sph,
+// valid cells): f += -div(s0_face u) - (s - s0) div u, s0_face the average of the two
+// cells' s0 (the cell's own at the domain edge), s0 the Cartesian base state in field s0c.
+__global__ void k_adj_pert_u_sph(KARGS, int comp, int s0c, double dx0, double dx1, double dx2, int lo0, int lo1,
+                                 int lo2, int hi0, int hi1, int hi2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const double fb = at(AW(A_AFORCE), i, j, k);
+    if (fb == 0.0) return;
+    const FabView s0a = VW(s0c);
+    const double s = at(s0a, i, j, k);
+    const double c = at(AW(A_WSOLD), i, j, k, comp) - s;
+    const double sxh = i < hi0 ? 0.5 * (s + at(s0a, i + 1, j, k)) : s;
+    const double sxl = i > lo0 ? 0.5 * (s + at(s0a, i - 1, j, k)) : s;
+    const double syh = j < hi1 ? 0.5 * (s + at(s0a, i, j + 1, k)) : s;
+    const double syl = j > lo1 ? 0.5 * (s + at(s0a, i, j - 1, k)) : s;
+    const double szh = k < hi2 ? 0.5 * (s + at(s0a, i, j, k + 1)) : s;
+    const double szl = k > lo2 ? 0.5 * (s + at(s0a, i, j, k - 1)) : s;
+    atomicAdd(&at(AW(A_AUMAC0), i + 1, j, k), -(sxh + c) * fb / dx0);
+    atomicAdd(&at(AW(A_AUMAC0), i, j, k), (sxl + c) * fb / dx0);
+    atomicAdd(&at(AW(A_AUMAC1), i, j + 1, k), -(syh + c) * fb / dx1);
+    atomicAdd(&at(AW(A_AUMAC1), i, j, k), (syl + c) * fb / dx1);
+    atomicAdd(&at(AW(A_AUMAC2), i, j, k + 1), -(szh + c) * fb / dx2);
+    atomicAdd(&at(AW(A_AUMAC2), i, j, k), (szl + c) * fb / dx2);
+}
+
+// MakeRhoHForce's face-velocity adjoint (valid cells), the force's adjoint being scale times
+// component comp of slot src.  Plane-parallel (k_rhoh_force): f = (w(k) + w(k+1))/2 gradp0,
+// gradp0 as the forward forms it; spherical (k_rhoh_force_sph): f = div(u p0_face) - p0 div u,
+// p0_face in F_S0MAC*.  F_P0CART (and plane-parallel F_RHO0CART, F_GRAVCART) current.
+__global__ void k_adj_rhoh_force_u(KARGS, int src, int comp, double scale, int sph, int cutoff, int domhi, RecipC rdz,
+                                   double dx0, double dx1, double dx2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const double fb = scale * at(AW(src), i, j, k, comp);
+    if (fb == 0.0) return;
+    const FabView p0c = VW(F_P0CART);
+    if (!sph) {
+        double gradp0;
+        if (k < cutoff) gradp0 = at(VW(F_RHO0CART), i, j, k) * at(VW(F_GRAVCART), i, j, k, 2);
+        else if (k == domhi) gradp0 = div_c(at(p0c, i, j, k) - at(p0c, i, j - 1, k), rdz);
+        else gradp0 = div_c(at(p0c, i, j + 1, k) - at(p0c, i, j, k), rdz);
+        const double g = 0.5 * gradp0 * fb;
+        atomicAdd(&at(AW(A_AUMAC2), i, j, k), g);
+        atomicAdd(&at(AW(A_AUMAC2), i, j, k + 1), g);
+        return;
+    }
+    const double p0 = at(p0c, i, j, k);
+    const FabView px = VW(F_S0MAC0), py = VW(F_S0MAC1), pz = VW(F_S0MAC2);
+    atomicAdd(&at(AW(A_AUMAC0), i + 1, j, k), (at(px, i + 1, j, k) - p0) * fb / dx0);
+    atomicAdd(&at(AW(A_AUMAC0), i, j, k), -(at(px, i, j, k) - p0) * fb / dx0);
+    atomicAdd(&at(AW(A_AUMAC1), i, j + 1, k), (at(py, i, j + 1, k) - p0) * fb / dx1);
+    atomicAdd(&at(AW(A_AUMAC1), i, j, k), -(at(py, i, j, k) - p0) * fb / dx1);
+    atomicAdd(&at(AW(A_AUMAC2), i, j, k + 1), (at(pz, i, j, k + 1) - p0) * fb / dx2);
+    atomicAdd(&at(AW(A_AUMAC2), i, j, k), -(at(pz, i, j, k) - p0) * fb / dx2);
+}
+
+void adj_flux_rhoh_u_sph(Ctx& c) {
+    const int ex = c.geo.exact ? 1 : 0;
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_flux_rhoh_u_sph<0>, c.V(), c.P.dt / c.P.dx[0], ex);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_flux_rhoh_u_sph<1>, c.V(), c.P.dt / c.P.dx[1], ex);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_flux_rhoh_u_sph<2>, c.V(), c.P.dt / c.P.dx[2], ex);
+}
+
+void adj_pert_u_sph(Ctx& c, int comp, int s0c) {
+    launch(c, rg_grow(c, 0), 1, k_adj_pert_u_sph, c.V(), comp, s0c, c.P.dx[0], c.P.dx[1], c.P.dx[2], c.P.dom_lo[0],
+           c.P.dom_lo[1], c.P.dom_lo[2], c.P.dom_hi[0], c.P.dom_hi[1], c.P.dom_hi[2]);
+}
+
+void adj_rhoh_force_u(Ctx& c, int src, int comp, double scale) {
+    launch(c, rg_grow(c, 0), 1, k_adj_rhoh_force_u, c.V(), src, comp, scale, c.sph ? 1 : 0,
+           c.P.base_cutoff_density_coord, c.P.dom_hi[2], make_recip(c.P.dx[2]), c.P.dx[0], c.P.dx[1], c.P.dx[2]);
+}
+
+// ------------------------------------------------------------------ buoyancy
+// k_umac_ghost transposed (one face direction dd): a ghost face the forward set to w times
+// a source face passes w times its adjoint to the source and keeps none; one set to zero
+// keeps none.  Every ghost and every source belongs to one thread of the launch.
+__global__ void k_adj_umac_ghost(KARGS, int dd, int bclo, int bchi, int dlo, int dhi) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const int I = dd == 0 ? i : (dd == 1 ? j : k);
+    if (I != dlo - 1 && I != dhi + 2) return;
+    const int di = dd == 0, dj = dd == 1, dk = dd == 2;
+    const FabView q[3] = {AW(A_AUMAC0), AW(A_AUMAC1), AW(A_AUMAC2)};
+    auto move = [&](const FabView& f, int s, int t, double w) {  // ghost at offset s, source at t (in dd)
+        double& g = at(f, i + s * di, j + s * dj, k + s * dk);
+        const double a = g;
+        g = 0.0;
+        if (w != 0.0) at(f, i + t * di, j + t * dj, k + t * dk) += w * a;
+    };
+    if (I == dlo - 1) {
+        for (int cc = 0; cc < 3; ++cc) switch (bclo) {
+                case PB_INFLOW: move(q[cc], 0, 1, cc == dd ? 1.0 : 0.0); break;
+                case PB_SLIPWALL:
+                case PB_NOSLIPWALL: move(q[cc], 0, 0, 0.0); break;
+                case PB_OUTFLOW: move(q[cc], 0, 1, 1.0); break;
+                case PB_SYMMETRY: cc == dd ? move(q[dd], 0, 2, -1.0) : move(q[cc], 0, 1, 1.0); break;
+                default: break;
+            }
+    } else {
+        for (int cc = 0; cc < 3; ++cc) switch (bchi) {
+                case PB_INFLOW: cc == dd ? move(q[dd], 0, -1, 1.0) : move(q[cc], -1, -1, 0.0); break;
+                case PB_SLIPWALL:
+                case PB_NOSLIPWALL: cc == dd ? move(q[dd], 0, 0, 0.0) : move(q[cc], -1, -1, 0.0); break;
+                case PB_OUTFLOW: cc == dd ? move(q[dd], 0, -1, 1.0) : move(q[cc], -1, -2, 1.0); break;
+                case PB_SYMMETRY: cc == dd ? move(q[dd], 0, -2, -1.0) : move(q[cc], -1, -2, 1.0); break;
+                default: break;
+            }
+    }
+}
+
+// k_vp_velocities<D> (untraced forces) transposed with respect to the force: the face value
+// is the left state ml (which carries + dt/2 f of cell il), the right state mr (+ dt/2 f of
+// cell i) or zero, decided as the forward decides it, boundary faces included (outflow:
+// min(mr, 0) on the low side, max(ml, 0) on the high side); valid faces.
+template <int D>
+__global__ void k_adj_vp_force(KARGS, double dt2, int bclo, int bchi, int domlo, int domhi, double rel_eps, int sph) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const double vb = at(AW(A_AUMAC0 + D), i, j, k);
+    if (vb == 0.0) return;
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    constexpr int a1i = T1 == 0, a1j = T1 == 1, a1k = T1 == 2;
+    constexpr int a2i = T2 == 0, a2j = T2 == 1, a2k = T2 == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    const int il = i - di, jl = j - dj, kl = k - dk;
+    const FabView tc = VW(F_TCOEF), f = VW(F_VELFORCE);
+    const FabView q1 = VW(Q_FIELD(D, T1)), q2 = VW(Q_FIELD(D, T2));
+    const double ml = at(VW(F_SL0 + D), i, j, k, D) -
+                      at(tc, il, jl, kl, 3 + T1) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
+                      at(tc, il, jl, kl, 3 + T2) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl)) +
+                      dt2 * at(f, il, jl, kl, D);
+    const double mr = at(VW(F_SR0 + D), i, j, k, D) -
+                      at(tc, i, j, k, 3 + T1) * (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
+                      at(tc, i, j, k, 3 + T2) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k)) +
+                      dt2 * at(f, i, j, k, D);
+    int side;  // 0: zero, 1: ml, 2: mr
+    if (D < 2 && !sph) {
+        const bool test = (ml <= 0.0 && mr >= 0.0) || (fabs(ml + mr) < rel_eps);
+        side = test ? 0 : (0.5 * (ml + mr) > 0.0 ? 1 : 2);
+    } else {
+        const double w0c = sph ? at(VW(F_W0MAC0 + D), i, j, k) : at(VW(F_W0CART), i, j, k, 2);
+        const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fabs(ml + mr + 2.0 * w0c) < rel_eps);
+        side = test ? 0 : (0.5 * (ml + mr) + w0c > 0.0 ? 1 : 2);
+    }
+    if (I == domlo) {
+        if (bclo == PB_OUTFLOW) side = mr < 0.0 ? 2 : 0;
+        else if (bclo != PB_INTERIOR) side = 0;
+    } else if (I == domhi + 1) {
+        if (bchi == PB_OUTFLOW) side = ml > 0.0 ? 1 : 0;
+        else if (bchi != PB_INTERIOR) side = 0;
+    }
+    const FabView af = AW(A_AVELF);
+    if (side == 1) atomicAdd(&at(af, il, jl, kl, D), dt2 * vb);
+    else if (side == 2) atomicAdd(&at(af, i, j, k, D), dt2 * vb);
+}
+
+// MakeVelForce transposed with respect to the density (valid cells): f_d = (rho' g_d -
+// gpi_d) / rho + terms free of rho, with rho' = rho - rho0 (0 below the buoyancy cutoff),
+// so df_d/drho = ((rho >= cutoff ? rho0 : 0) g_d + gpi_d) / rho^2.  The plane-parallel
+// gravity has its z component only (F_GRAVCART comps 0, 1 are zero).
+__global__ void k_adj_vel_force(KARGS, double cutoff_rho) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const FabView a = AW(A_AVELF), g = VW(F_GRAVCART), gp = VW(F_GPI);
+    const double r = at(VW(F_SOLD), i, j, k, RHO);
+    const double r0 = r < cutoff_rho ? 0.0 : at(VW(F_RHO0CART), i, j, k);
+    double acc = 0.0;
+    for (int d = 0; d < 3; ++d) acc += at(a, i, j, k, d) * (r0 * at(g, i, j, k, d) + at(gp, i, j, k, d));
+    if (acc != 0.0) at(AW(A_ASOLD), i, j, k, RHO) += acc / (r * r);
+}
+
+// The MAC-velocity adjoint's ghost faces back onto the valid faces: FillUmacGhost^T per
+// non-periodic direction (z, y, x: the reverse of the forward's order), then FillBoundary^T
+void adj_umac_ghosts(Ctx& c) {
+    for (int dd = 2; dd >= 0; --dd) {
+        if (c.per[dd]) continue;
+        launch(c, region(c, 1, 1, 1, 1, 1, 1, dd), 1, k_adj_umac_ghost, c.V(), dd, c.P.phys_bc_lo[dd],
+               c.P.phys_bc_hi[dd], c.P.dom_lo[dd], c.P.dom_hi[dd]);
+    }
+    for (int d = 0; d < 3; ++d) adj_fill_boundary(c, A_AUMAC0 + d, 1, 1, d);
+}
+
+// From the valid-face MAC-velocity adjoints into the density adjoint: VelPred's final states
+// with respect to the force, the force's FillPatch (BCS_U) transposed, MakeVelForce^T.
+// AdvancePremac's forward fields of the step (F_SL*, F_SR*, F_Q*, F_TCOEF of utrans,
+// F_VELFORCE, F_RHO0CART, F_GRAVCART, F_SOLD) must be current; A_AVELF must be zero.
+void adj_vel_force(Ctx& c) {
+    const double dt2 = 0.5 * c.P.dt, re = c.P.rel_eps;
+    const int sph = c.sph ? 1 : 0;
+    const int *lo = c.P.phys_bc_lo, *hi = c.P.phys_bc_hi, *dl = c.P.dom_lo, *dh = c.P.dom_hi;
+    launch(c, rg_grow(c, 0, 0), 1, k_adj_vp_force<0>, c.V(), dt2, lo[0], hi[0], dl[0], dh[0], re, sph);
+    launch(c, rg_grow(c, 0, 1), 1, k_adj_vp_force<1>, c.V(), dt2, lo[1], hi[1], dl[1], dh[1], re, sph);
+    launch(c, rg_grow(c, 0, 2), 1, k_adj_vp_force<2>, c.V(), dt2, lo[2], hi[2], dl[2], dh[2], re, sph);
+    for (int n = 0; n < 3; ++n) adj_phys_fill(c, A_AVELF, n, 1, c.bcs_u[n]);
+    adj_fill_boundary(c, A_AVELF, 3, 1, -1);
+    launch(c, rg_grow(c, 0), 1, k_adj_vel_force, c.V(), c.P.buoyancy_cutoff_factor * c.P.base_cutoff_density);
 }
 
 long adj_dot_parts(Ctx& c) { return (rg_grow(c, 0).total + TPB - 1) / TPB; }

@@ -738,6 +738,22 @@ static void convert_rhoh_to_h_h(Hier& H, int flag) {
     else fill_patch_h(H, F_SOLD, RHOH, 1, BCS_S, RHOH, 0, RHOH);
 }
 
+// spherical: the face base state of the (rho h) fluxes (Source/MaestroEnthalpyAdvance.cpp:
+// 187-220, 251-300): rhoh0 (exact base state), or rho0 and h0 = rhoh0 / rho0 (uniform bins)
+static void rhoh_face_base_h(Hier& H, int which_step) {
+    const char* rh0n = which_step == 1 ? "rhoh0_old" : "rhoh0_new";
+    const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
+    if (H[0].sph && H[0].geo.exact) {
+        make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
+        make_s0mac_h(H, rh0n, F_S0MACB0);
+    } else if (H[0].sph) {
+        make_s0mac_h(H, "rho0_old", F_S0MACC0);
+        make_s0mac_h(H, r0n, F_S0MACD0);
+        make_s0mac_h(H, "h0_old", F_S0MAC0);
+        make_s0mac_h(H, which_step == 1 ? "h0_old" : "h0_new", F_S0MACB0);
+    }
+}
+
 // the fluxes of (rho h): the base state of the enthalpy (and, for the h prediction, of the
 // density) at the old time, with the new one for which_step 2
 static void rhoh_flux_h(Hier& H, int which_step) {
@@ -745,15 +761,7 @@ static void rhoh_flux_h(Hier& H, int which_step) {
     const char* rh0en = which_step == 1 ? "rhoh0_edge_old" : "rhoh0_edge_new";
     const char* r0n = which_step == 1 ? "rho0_old" : "rho0_new";
     const char* r0en = which_step == 1 ? "rho0_edge_old" : "rho0_edge_new";
-    if (H[0].sph && H[0].geo.exact) {  // rhoh0 on faces (Source/MaestroEnthalpyAdvance.cpp:187-220)
-        make_s0mac_h(H, "rhoh0_old", F_S0MAC0);
-        make_s0mac_h(H, rh0n, F_S0MACB0);
-    } else if (H[0].sph) {  // uniform bins: rho0 and h0 = rhoh0 / rho0 on faces (:194-220, 251-300)
-        make_s0mac_h(H, "rho0_old", F_S0MACC0);
-        make_s0mac_h(H, r0n, F_S0MACD0);
-        make_s0mac_h(H, "h0_old", F_S0MAC0);
-        make_s0mac_h(H, which_step == 1 ? "h0_old" : "h0_new", F_S0MACB0);
-    }
+    rhoh_face_base_h(H, which_step);
     for (auto* c : H.L)
         make_rhoh_flux(*c, c->b1("rhoh0_old"), c->b1("rhoh0_edge_old"), c->b1(rh0n), c->b1(rh0en), c->b1("rho0_old"),
                        c->b1("rho0_edge_old"), c->b1(r0n), c->b1(r0en));
@@ -2725,11 +2733,21 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
                 return MADV_ERR_UNSUPPORTED;
             }
         }
-    for (double v : c.h1.at("grav_cell"))
-        if (v != 0.0) {
-            set_error("the adjoint needs grav_cell = 0 (MAC velocities independent of the state)");
+    // buoyancy: with gravity the MAC velocity depends on the density through MakeVelForce, so
+    // every reverse step carries the MAC-velocity adjoint back to the density (state
+    // gradient; the force's ghost fill is transposed for periodic, outflow and symmetry faces)
+    bool buoy = false;
+    for (double v : c.h1.at("grav_cell")) buoy |= v != 0.0;
+    if (buoy) {
+        bool wall = false;
+        for (int d = 0; d < 3; ++d)
+            for (int pb : {c.P.phys_bc_lo[d], c.P.phys_bc_hi[d]}) wall |= pb == PB_SLIPWALL || pb == PB_NOSLIPWALL;
+        if (wall || res->grad_u) {
+            set_error("with gravity the adjoint covers the state gradient on periodic, outflow and symmetry "
+                      "boundaries");
             return MADV_ERR_UNSUPPORTED;
         }
+    }
     if (res->grad_u)
         for (double v : c.h1.at("w0"))
             if (v != 0.0) {
@@ -2741,6 +2759,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     const int last0 = (nck - 1) * K;  // first step of the last block
     const bool want_u = res->grad_u != nullptr;
     const bool rev = res->grad_s != nullptr || want_u;
+    const bool need_u = want_u || (buoy && rev);  // the scalar transposes accumulate the MAC-velocity adjoint
     const cudaMemcpyKind DD = cudaMemcpyDeviceToDevice;
     AdjWork W;
     const size_t st_b = fab_doubles(c, ns, 0, -1) * sizeof(double);
@@ -2760,8 +2779,10 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         return rc;
     std::vector<double*> ck, bst;
     std::vector<std::array<double*, 3>> bed;
-    double *asold = nullptr, *scr = nullptr, *dir = nullptr, *atc = nullptr;
-    size_t scr_b = 0, dir_b = 0, atc_b = 0, n_2 = 0;
+    double *asold = nullptr, *scr = nullptr, *dir = nullptr, *atc = nullptr, *avelf = nullptr;
+    std::array<double*, 3> aumac{};
+    std::array<size_t, 3> aumac_b{};
+    size_t scr_b = 0, dir_b = 0, atc_b = 0, avelf_b = 0, n_2 = 0;
     if (rev) {
         for (int j = 0; j < nck; ++j) ck.push_back(W.alloc(st_b));
         for (int j = 0; j < std::min(K, N); ++j) {
@@ -2788,15 +2809,24 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         dir_b = 3 * n_2 * sizeof(double);
         dir = W.alloc(dir_b);
         for (int s = A_ASM; s <= A_ADSVL; ++s) bind_raw(c, s, dir + (size_t)(s - A_ASM) * n_2, 1, 2, -1);
-        if (want_u) {
+        if (need_u) {
             for (int d = 0; d < 3; ++d) {
-                bind_raw(c, A_AUMAC0 + d, W.alloc(fab_doubles(c, 1, 1, d) * 8), 1, 1, d);
-                bind_raw(c, A_AUTRANS0 + d, W.alloc(fab_doubles(c, 1, 1, d) * 8), 1, 1, d);
+                aumac_b[d] = fab_doubles(c, 1, 1, d) * 8;
+                aumac[d] = W.alloc(aumac_b[d]);
+                bind_raw(c, A_AUMAC0 + d, aumac[d], 1, 1, d);
             }
             atc_b = fab_doubles(c, 6, 2, -1) * 8;
             atc = W.alloc(atc_b);
             bind_raw(c, A_ATCOEF, atc, 6, 2, -1);
+        }
+        if (want_u) {
+            for (int d = 0; d < 3; ++d) bind_raw(c, A_AUTRANS0 + d, W.alloc(fab_doubles(c, 1, 1, d) * 8), 1, 1, d);
             bind_raw(c, A_AUT, W.alloc(fab_doubles(c, 3, c.ng_adv, -1) * 8), 3, c.ng_adv, -1);
+        }
+        if (buoy) {
+            avelf_b = fab_doubles(c, 3, 1, -1) * 8;
+            avelf = W.alloc(avelf_b);
+            bind_raw(c, A_AVELF, avelf, 3, 1, -1);
         }
     }
     // the forward's PPM interface values of every traced component of the block's steps
@@ -2804,7 +2834,7 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     // F_SIMH0..2), kept as the forward forms them
     static const int TAPE_F[12] = {F_FACE0, F_FACE1, F_FACE2, F_Q01, F_Q02, F_Q10,
                                    F_Q12,   F_Q20,   F_Q21,   F_SIMH0, F_SIMH1, F_SIMH2};
-    const int ntape = want_u ? 12 : 3;
+    const int ntape = need_u ? 12 : 3;
     std::vector<std::vector<std::array<double*, 12>>> tape;
     if (rev) {
         tape.resize(std::min(K, N));
@@ -2832,31 +2862,38 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
     } views_guard{c, base_views};
     std::vector<std::vector<FabView*>> vt(tape.size(), std::vector<FabView*>(ns, nullptr));
     // With w0 != 0 the stage ends with umac - w0 in F_UMAC, while the edge states and fluxes
-    // saw umac + w0 (the density and the enthalpy halves each form it once).  The velocity is
-    // the same in every step: the first taped forward step keeps both, and the reverse
-    // steps put them back, so every upwind and tracing decision is the forward's.
+    // saw umac + w0 (the density and the enthalpy halves each form it once).  Without gravity
+    // the velocity is the same in every step: the first taped forward step keeps both, and
+    // the reverse steps put them back, so every upwind and tracing decision is the
+    // forward's.  With gravity the MAC velocity is the step's own: every taped step keeps
+    // its pair.
     bool has_w0 = false;
     for (double v : c.h1.at("w0")) has_w0 |= v != 0.0;
-    std::array<std::array<double*, 3>, 2> umac_keep{};
-    if (rev && has_w0)
-        for (auto& a : umac_keep)
-            for (int d = 0; d < 3; ++d) a[d] = W.alloc(c.F[F_UMAC0 + d].bytes);
-    auto keep_umac = [&](int which) {
+    const bool keep_per_step = buoy;
+    const bool keeps = has_w0 || keep_per_step;
+    std::vector<std::array<std::array<double*, 3>, 2>> umac_keep(keep_per_step ? std::min(K, N) : 1);
+    if (rev && keeps)
+        for (auto& pair : umac_keep)
+            for (auto& a : pair)
+                for (int d = 0; d < 3; ++d) a[d] = W.alloc(c.F[F_UMAC0 + d].bytes);
+    auto keep_umac = [&](int slot, int which) {
+        auto& a = umac_keep[keep_per_step ? slot : 0][which];
         for (int d = 0; d < 3; ++d)
-            cudaMemcpyAsync(umac_keep[which][d], c.F[F_UMAC0 + d].base, c.F[F_UMAC0 + d].bytes, DD, c.stream);
+            cudaMemcpyAsync(a[d], c.F[F_UMAC0 + d].base, c.F[F_UMAC0 + d].bytes, DD, c.stream);
     };
-    auto put_umac = [&](int which) {
-        if (!has_w0) return;
+    auto put_umac = [&](int slot, int which) {
+        if (!keeps) return;
+        auto& a = umac_keep[keep_per_step ? slot : 0][which];
         for (int d = 0; d < 3; ++d)
-            cudaMemcpyAsync(c.F[F_UMAC0 + d].base, umac_keep[which][d], c.F[F_UMAC0 + d].bytes, DD, c.stream);
+            cudaMemcpyAsync(c.F[F_UMAC0 + d].base, a[d], c.F[F_UMAC0 + d].bytes, DD, c.stream);
         edge_scal_coeffs(c);
     };
     bool umac_kept = false;
     auto tape_on = [&](int slot) {
         if (!rev) return;
         c.edge_tape_begin = [&, slot](int comp) {
-            if (has_w0 && !umac_kept && (comp == FIRSTSPEC || comp == RHOH)) {
-                keep_umac(comp == RHOH ? 1 : 0);
+            if (keeps && (keep_per_step || !umac_kept) && (comp == FIRSTSPEC || comp == RHOH)) {
+                keep_umac(slot, comp == RHOH ? 1 : 0);
                 umac_kept = comp == RHOH;
             }
             c.dviews = vt[slot][comp];
@@ -2910,7 +2947,11 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
         put_in_pert_form_h(H, "rho0_old", RHO, 0, BCS_F, 1);
         put_in_pert_form_h(H, "rhoh0_old", RHOH, 0, BCS_F, 1);
         edge_scal_coeffs(c);
-        put_umac(0);  // the density half's MAC velocity (w0 != 0)
+        put_umac(slot, 0);  // the density half's MAC velocity (w0 != 0, or gravity)
+        if (buoy) {  // this step's MAC-velocity adjoint only
+            for (int d = 0; d < 3; ++d) cudaMemsetAsync(aumac[d], 0, aumac_b[d], c.stream);
+            cudaMemsetAsync(atc, 0, atc_b, c.stream);
+        }
         // spherical: the face base state of the density fluxes (which_step 1: rho0_old for
         // both of MakeRhoXFlux's old and new)
         if (c.sph) {
@@ -2918,15 +2959,33 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
             make_s0mac_h(H, "rho0_old", F_S0MACB0);
         }
         adj_update(c);
-        adj_flux(c, want_u);
+        adj_flux(c, need_u);
+        if (need_u) {
+            // the spherical (rho h) flux's face-velocity term, on the faces it was formed with
+            if (c.sph) {
+                rhoh_face_base_h(H, 1);
+                adj_flux_rhoh_u_sph(c);
+            }
+            // MakeRhoHForce's and ModifyScalForce's fields (which_step 1: p0_old, rho0_old,
+            // rhoh0_old), then the final (rho h) force's face-velocity term (rhoh_new = ... + dt f)
+            put1d_h(H, F_P0CART, "p0_old", 0, 1, 0, BCS_F, 0, 0, -1);
+            put1d_h(H, F_RHO0CART, "rho0_old", 0, 1, 0, BCS_S, RHO, 0, RHO);
+            if (c.sph) {
+                make_s0mac_h(H, "p0_old", F_S0MAC0);
+                put1d_h(H, F_RHOH0CART, "rhoh0_old", 0, 1, 0, BCS_S, RHOH, 0, RHOH);
+            } else {
+                put1d_h(H, F_GRAVCART, "grav_cell", c.ndim - 1, c.ndim, 0, BCS_F, 0, 0, -1);
+            }
+            adj_rhoh_force_u(c, A_ASNEW, RHOH, c.P.dt);
+        }
         for (int comp = 0; comp < ns; ++comp) {
             if (comp == TEMP || comp == PI) continue;
             cudaMemsetAsync(scr, 0, scr_b, c.stream);
-            if (comp == RHOH) put_umac(1);  // the enthalpy half's (w0 != 0)
+            if (comp == RHOH) put_umac(slot, 1);  // the enthalpy half's (w0 != 0, or gravity)
             // this component's interface values (and for the velocity adjoint its
             // transverse states) as the forward formed them, read from the tape
             c.dviews = vt[slot][comp];
-            adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b, want_u);
+            adj_edge_scal(c, F_SOLD, comp, comp >= FIRSTSPEC, dir, dir_b, need_u);
             c.dviews = base_views;
             // the traced field's and the force's FillPatch (BCS_F, the BC entries the
             // forward's fills read), transposed
@@ -2938,9 +2997,25 @@ static int stage_adjoint(madv_ctx* h, const madv_adj_seed* sd, madv_adj_result* 
             } else {
                 adj_phys_fill(c, A_AFORCE, 0, 1, bf[0]);
                 adj_fill_boundary(c, A_AFORCE, 1, 1, -1);
-                adj_pert_force(c, comp, want_u);
+                adj_pert_force(c, comp, need_u);
+                if (need_u && c.sph) adj_pert_u_sph(c, comp, comp == RHO ? F_RHO0CART : F_RHOH0CART);
+                if (need_u && comp == RHOH) adj_rhoh_force_u(c, A_AFORCE, 0, 1.0);  // the traced force's
             }
-            if (comp == RHOH) put_umac(0);
+            if (comp == RHOH) put_umac(slot, 0);
+        }
+        if (buoy) {
+            // the step's MAC-velocity adjoint onto its valid faces (transverse coefficients,
+            // then the ghost faces), then through the force into the density: AdvancePremac's
+            // fields of this step recomputed from its state
+            adj_tcoef(c, A_AUMAC0);
+            adj_umac_ghosts(c);
+            copy_fab(c, F_SOLD, 0, F_USER + A_WSOLD, 0, ns, 0);
+            fill_patch_h(H, F_SOLD, 0, ns, BCS_S, 0, 0, 0);
+            set_val(c, F_UTILDE, 0.0, 0, 3, c.ng_adv);
+            copy_fab(c, F_UTILDE, 0, F_USER + U_UOLD, 0, 3, 0);
+            advance_premac(H);
+            cudaMemsetAsync(avelf, 0, avelf_b, c.stream);
+            adj_vel_force(c);
         }
         copy_fab(c, F_USER + A_ASNEW, 0, F_USER + A_ASOLD, 0, ns, 0);
         cudaMemsetAsync(asold, 0, st_b, c.stream);

@@ -338,6 +338,7 @@ enum {
     A_ASM, A_ASP, A_ADSVL,
     A_WEIGHT, A_SOLD0, A_GRADS, A_SFIN,
     A_AUMAC0, A_AUMAC1, A_AUMAC2, A_ATCOEF, A_AUTRANS0, A_AUTRANS1, A_AUTRANS2, A_AUT, A_GRADU,
+    A_AVELF,  // buoyancy: adjoint of MakeVelForce's force (3 components, one ghost cell)
     A_END
 };
 static_assert(A_END <= N_USER_SLOTS, "user slots");
@@ -352,6 +353,18 @@ void adj_convert_x(Ctx& c, int comp);
 void adj_pert_force(Ctx& c, int comp, int want_u);
 void adj_tcoef(Ctx& c, int ts);
 void adj_vel_pred(Ctx& c, double* dir, size_t dir_bytes);
+// buoyancy (a MAC velocity that depends on the density through MakeVelForce): the MAC
+// velocity adjoint's ghost faces (FillUmacGhost^T, then FillBoundary^T), VelPred's final
+// states transposed with respect to the force, the force's FillPatch^T, and MakeVelForce^T
+// into the density adjoint (A_ASOLD)
+void adj_umac_ghosts(Ctx& c);
+void adj_vel_force(Ctx& c);
+// face-velocity terms of the spherical (rho h) flux (F_S0MAC* set as rhoh_flux sets them) and
+// ModifyScalForce (Cartesian base state in field s0c), and of MakeRhoHForce (force adjoint
+// scale * component comp of slot src; F_P0CART and, spherical, p0 faces in F_S0MAC* current)
+void adj_flux_rhoh_u_sph(Ctx& c);
+void adj_pert_u_sph(Ctx& c, int comp, int s0c);
+void adj_rhoh_force_u(Ctx& c, int src, int comp, double scale);
 long adj_dot_parts(Ctx& c);
 void adj_dot(Ctx& c, int slot_a, int slot_b, int nc, double* part, double* d_out);
 

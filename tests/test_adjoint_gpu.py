@@ -411,3 +411,67 @@ def test_spherical_uniform_bins_adjoint_matches_cpu_tangent_linear_model(kw):
     print(f"spherical uniform bins: tangent-linear {tl:.15e}, adjoint {adj:.15e}, "
           f"diff / sum|terms| {abs(tl - adj) / scale:.2e}")
     assert abs(tl - adj) <= 1e-10 * scale
+
+
+# buoyancy: with gravity the MAC velocity depends on the density through MakeVelForce and
+# VelPred's final states, so each reverse step carries its MAC-velocity adjoint (the flux,
+# tracing, transverse and force transposes, the transverse coefficients, the ghost faces)
+# back to the density through the force.  The stage has no MAC projection and these steps
+# no force-limited dt, so at full strength the buoyant kicks drain cells within the four
+# steps: the gravity is scaled down (1e-3 plane-parallel, 1e-5 for the star).  The path
+# still dominates the density's sensitivity (by ~1e17 over the same configuration without
+# gravity), so the density-only dot product checks it.
+BUOYANCY = {
+    "periodic": dict(n=(32, 32, 32)),
+    "outflow": dict(n=(32, 24, 32), seed=20261203 + 40, bc_lo=NON_PERIODIC["outflow"][0],
+                    bc_hi=NON_PERIODIC["outflow"][1]),
+    "mixed": dict(n=(32, 24, 32), seed=20261203 + 40, bc_lo=NON_PERIODIC["mixed"][0], bc_hi=NON_PERIODIC["mixed"][1]),
+}
+
+
+def density_and_state_dots(case, label):
+    J, grad, _, _ = case.adjoint()
+    G = grad.to_domain(case.n).cpu().numpy()
+    S = case.cfg["sold"]
+    rng = np.random.default_rng(2030)
+    vs = rng.standard_normal(S.shape) * np.sqrt((S ** 2).mean(axis=(1, 2, 3), keepdims=True))
+    for part, v in (("state", vs), ("density", vs * (np.arange(S.shape[0]) == RHO)[:, None, None, None])):
+        tl, adj, scale = tl_dot(case, G, v)
+        print(f"{label} {part}: tangent-linear {tl:.15e}, adjoint {adj:.15e}, "
+              f"diff / sum|terms| {abs(tl - adj) / scale:.2e}")
+        assert abs(tl - adj) <= 1e-10 * scale, part
+
+
+@pytest.mark.parametrize("ppm_type,bc", [(1, "periodic"), (1, "outflow"), (1, "mixed"), (2, "periodic"),
+                                         (2, "outflow")])
+def test_buoyancy_adjoint_matches_cpu_tangent_linear_model(ppm_type, bc):
+    """Plane-parallel with gravity: dot-product check of the state gradient against the
+    oracle's tangent-linear build (whose forward recomputes the MAC velocity from the state in
+    every step), over every cell and over the density alone."""
+    cfg = configs.adjoint_config(max_grid=16, nspec=3, ppm_type=ppm_type, gravity=True, **BUOYANCY[bc])
+    cfg["grav_cell"] = cfg["grav_cell"] * 1.0e-3
+    density_and_state_dots(Case(cfg=cfg), f"buoyancy ppm{ppm_type} {bc}")
+
+
+@pytest.mark.parametrize("ppm_type,w0_amp,exact", [(1, 0.0, True), (2, 1.0e5, True), (1, 1.0e5, False)])
+def test_spherical_buoyancy_adjoint_matches_cpu_tangent_linear_model(ppm_type, w0_amp, exact):
+    """The full star with gravity (outflow faces, the force along the radius, w0mac in
+    VelPred's decisions): dot-product check against the oracle's tangent-linear build over
+    every cell and over the density alone."""
+    cfg = configs.spherical_config(n=32, nspec=3, ppm_type=ppm_type, max_grid=16, w0_amp=w0_amp, exact=exact)
+    cfg["grav_cell"] = cfg["grav_cell"] * 1.0e-5
+    density_and_state_dots(Case(cfg=cfg), f"spherical buoyancy ppm{ppm_type} w0 {w0_amp} exact {exact}")
+
+
+def test_buoyancy_adjoint_rejects_walls_and_velocity_gradient():
+    cfg = configs.adjoint_config(n=(16, 16, 16), max_grid=16, gravity=True)
+    case = Case(cfg=cfg, nsteps=2, ckpt=1)
+    with pytest.raises(MadvError) as e:
+        case.adjoint(want_u=True)
+    assert e.value.code == -3
+    walls = NON_PERIODIC["walls"]
+    cfg = configs.adjoint_config(n=(16, 16, 16), max_grid=16, gravity=True, bc_lo=walls[0], bc_hi=walls[1])
+    case = Case(cfg=cfg, nsteps=2, ckpt=1)
+    with pytest.raises(MadvError) as e:
+        case.adjoint()
+    assert e.value.code == -3
