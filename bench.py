@@ -601,61 +601,76 @@ def run_spherical_adjoint(args, barrier):
     (default 1e-3: the MAC velocity takes the density's buoyancy through MakeVelForce, and
     the steps -- no MAC projection, no force-limited dt -- stay above the cutoff density;
     0: no gravity, the MAC velocity independent of the state).  Times the forward alone and
-    the adjoint for dJ/d(state) (which runs its own forward), and checks --sph-fd-entries
-    gradient entries inside the star against central differences of the same forward
-    (fd_check), a third of them density entries."""
+    the adjoint for dJ/d(state) (which runs its own forward) at --sph-adj-n, and checks
+    --sph-fd-entries gradient entries inside the star against central differences of the
+    same forward (fd_check, a third of them density entries) on the same star at
+    --sph-fd-n cells a side (each entry costs four 8-step forwards)."""
     import torch
     from maestroex_gb300 import configs
     from maestroex_gb300.params import FIRSTSPEC, RHO, RHOH
     from maestroex_gb300.stage import MultiFab, make_stage
-    n, nsteps, ckpt = args.sph_adj_n, 8, 4
-    # a smooth 1% perturbation of density and enthalpy, so that the star's symmetry ties no
-    # limiter decision within the finite-difference step
-    cfg = configs.spherical_config(n=n, nspec=21, ppm_type=2, max_grid=min(64, n), w0_amp=1.0e5, pert=1.0e-2)
+    nsteps, ckpt = 8, 4
     gscale = args.sph_adj_gravity
-    cfg["grav_cell"] = cfg["grav_cell"] * gscale
-    st = make_stage(cfg)
-    boxes, nscal = cfg["boxes"], 4 + cfg["nspec"]
-    u = MultiFab(boxes, 3, 0).from_domain(cfg["uold"])
-    s0 = MultiFab(boxes, nscal, 0).from_domain(cfg["sold"])
-    rng = np.random.default_rng(20261203 + 60)
-    w = np.zeros_like(cfg["sold"])
-    w[RHOH] = rng.normal(size=w[RHOH].shape)
-    w[FIRSTSPEC:] = rng.normal(size=w[FIRSTSPEC:].shape)
-    wt = MultiFab(boxes, nscal, 0).from_domain(w)
-    gs, sf = MultiFab(boxes, nscal, 0), MultiFab(boxes, nscal, 0)
 
-    def call(grad):
-        return st.stage_adjoint(u, s0, wt, nsteps, ckpt, grad_s=gs if grad else None, sfinal=sf)
+    def case(n):
+        # a smooth 1% perturbation of density and enthalpy, so that the star's symmetry ties
+        # no limiter decision within the finite-difference step
+        cfg = configs.spherical_config(n=n, nspec=21, ppm_type=2, max_grid=min(64, n), w0_amp=1.0e5, pert=1.0e-2)
+        cfg["grav_cell"] = cfg["grav_cell"] * gscale
+        boxes, nscal = cfg["boxes"], 4 + cfg["nspec"]
+        rng = np.random.default_rng(20261203 + 60)
+        w = np.zeros_like(cfg["sold"])
+        w[RHOH] = rng.normal(size=w[RHOH].shape)
+        w[FIRSTSPEC:] = rng.normal(size=w[FIRSTSPEC:].shape)
+        return dict(cfg=cfg, st=make_stage(cfg), boxes=boxes, nscal=nscal, n=n,
+                    u=MultiFab(boxes, 3, 0).from_domain(cfg["uold"]),
+                    s0=MultiFab(boxes, nscal, 0).from_domain(cfg["sold"]),
+                    wt=MultiFab(boxes, nscal, 0).from_domain(w),
+                    gs=MultiFab(boxes, nscal, 0), sf=MultiFab(boxes, nscal, 0))
 
-    def timed(grad, reps):
-        call(grad)
+    def call(c, grad):
+        return c["st"].stage_adjoint(c["u"], c["s0"], c["wt"], nsteps, ckpt, grad_s=c["gs"] if grad else None,
+                                     sfinal=c["sf"])
+
+    def timed(c, grad, reps):
+        call(c, grad)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         tot = 0.0
         for _ in range(reps):
             torch.cuda.synchronize()
             e0.record()
-            J, nbytes = call(grad)
+            J, nbytes = call(c, grad)
             e1.record()
             torch.cuda.synchronize()
             tot += e0.elapsed_time(e1)
         return tot / reps, J, nbytes
 
+    big = case(args.sph_adj_n)
     reps = max(1, args.steps // 2)
-    ms_fwd, _, _ = timed(False, reps)
-    ms_adj, J, nbytes = timed(True, reps)
-    G = gs.to_domain(cfg["n"]).cpu().numpy()
+    ms_fwd, _, _ = timed(big, False, reps)
+    ms_adj, J, nbytes = timed(big, True, reps)
+    nboxes = len(big["boxes"])
+    big["st"].close()
+    del big
+    torch.cuda.empty_cache()
+
+    c = case(args.sph_fd_n)
+    call(c, True)
+    torch.cuda.synchronize()
+    n, boxes, nscal, cfg = c["n"], c["boxes"], c["nscal"], c["cfg"]
+    G = c["gs"].to_domain(cfg["n"]).cpu().numpy()
     S = cfg["sold"]
+    rng = np.random.default_rng(20261203 + 61)
 
     def final(ss):
         out = MultiFab(boxes, nscal, 0)
-        st.stage_adjoint(u, ss, wt, nsteps, ckpt, sfinal=out)
+        c["st"].stage_adjoint(c["u"], ss, c["wt"], nsteps, ckpt, sfinal=out)
         return out
 
     def perturbed(comp, cell, h):
         m = MultiFab(boxes, nscal, 0)
-        for a, b in zip(m.fabs, s0.fabs):
+        for a, b in zip(m.fabs, c["s0"].fabs):
             a.copy_(b)
         i, j, k = cell
         for bi, bx in enumerate(boxes):
@@ -664,7 +679,7 @@ def run_spherical_adjoint(args, barrier):
         return m
 
     rms = np.sqrt((S ** 2).mean(axis=(1, 2, 3)))
-    comps = [RHOH, RHO] + [FIRSTSPEC + c for c in range(21)]
+    comps = [RHOH, RHO] + [FIRSTSPEC + q for q in range(21)]
 
     def draw():
         comp = RHO if rng.random() < 1.0 / 3.0 else comps[int(rng.integers(0, len(comps)))]
@@ -675,7 +690,7 @@ def run_spherical_adjoint(args, barrier):
 
     def jdiff(field, comp, cell, h):
         a, b = final(perturbed(comp, cell, h)), final(perturbed(comp, cell, -h))
-        return sum(float((x_ * (p - q)).sum()) for x_, p, q in zip(wt.fabs, a.fabs, b.fabs))
+        return sum(float((x_ * (p - q)).sum()) for x_, p, q in zip(c["wt"].fabs, a.fabs, b.fabs))
 
     def grad_of(field, comp, cell):
         i, j, k = cell
@@ -687,10 +702,12 @@ def run_spherical_adjoint(args, barrier):
     # the skip threshold sits at 4e-7, still under the 1e-6 bar
     fd = fd_check(grad_of, jdiff, draw, args.sph_fd_entries, 3 * args.sph_fd_entries,
                   skip_tol=4e-7 if gscale else 1e-7)
-    st.close()
+    fd["grid"] = f"{n}^3 in {len(boxes)} boxes, the same star and steps"
+    c["st"].close()
     torch.cuda.empty_cache()
+    N = args.sph_adj_n
     return {
-        "workload": f"spherical full star, one level {n}^3 in {len(boxes)} boxes of {min(64, n)}^3, NumSpec 21, "
+        "workload": f"spherical full star, one level {N}^3 in {nboxes} boxes of {min(64, N)}^3, NumSpec 21, "
                     f"ppm_type 2, outflow, exact base state, density and enthalpy perturbed by a smooth 1% field, "
                     "w0 amplitude 1e5 cm/s, the cell velocity held fixed, "
                     + (f"the star's gravity scaled by {gscale:g} (buoyancy: the MAC velocity depends on the density)"
@@ -916,6 +933,8 @@ def main():
     ap.add_argument("--no-sph-adjoint", action="store_true")
     ap.add_argument("--no-mac", action="store_true")
     ap.add_argument("--sph-adj-n", type=int, default=128, help="extent of the spherical adjoint workload")
+    ap.add_argument("--sph-fd-n", type=int, default=64,
+                    help="extent of the spherical adjoint's finite-difference check (same star and steps)")
     ap.add_argument("--sph-adj-gravity", type=float, default=1.0e-3,
                     help="spherical adjoint: scale of the star's gravity (0: none)")
     ap.add_argument("--profile-once", action="store_true",
