@@ -348,12 +348,13 @@ int madv_ppm_noalloc(const madv_params* params, const madv_box* bx, const madv_f
  * block is recomputed from its stored state, so memory grows with nsteps/ckpt_interval
  * + ckpt_interval states.  No counterpart in the reference.
  * Scope: one level, 3-D, plane-parallel or spherical, ppm_type 1 (or 2: state gradient, no
- * walls), species_pred_type 1,
- * enthalpy_pred_type 1, and grav_cell = 0 so that the MAC velocities do not depend on the
- * state.  The state gradient (grad_s) also allows outflow, symmetry and wall boundaries
- * and w0 != 0.  The velocity gradient (grad_u) needs a periodic domain and w0 = 0.  Anything
- * else returns MADV_ERR_UNSUPPORTED.  The UpdateScal floor and negative-species branches
- * are taken as not active. */
+ * walls), species_pred_type 1, enthalpy_pred_type 1.  The state gradient (grad_s) also
+ * allows outflow, symmetry and wall boundaries and w0 != 0, and gravity (grav_cell != 0:
+ * the MAC velocity then depends on the density through MakeVelForce and VelPred, and each
+ * reverse step carries its MAC-velocity adjoint back to the density) on periodic, outflow
+ * and symmetry boundaries.  The velocity gradient (grad_u) needs a periodic domain,
+ * w0 = 0 and grav_cell = 0.  Anything else returns MADV_ERR_UNSUPPORTED.  The UpdateScal
+ * floor and negative-species branches are taken as not active. */
 typedef struct {
     int nsteps;                  /* advection steps (>= 1) */
     int ckpt_interval;           /* steps between stored states (>= 1) */
