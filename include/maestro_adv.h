@@ -461,6 +461,25 @@ int madv_mac_project(madv_ctx* ctx, const madv_multifab* umac, const madv_multif
                      const madv_multifab* macrhs, const madv_multifab* rho, const double* beta0, double tol_rel,
                      int max_iter, madv_mac_result* result, void* stream);
 
+/* Maestro::MacProj on an AMR hierarchy (the layout's nlev levels; one level: madv_mac_project),
+ * two plane-parallel 3-D levels: umac[3*nlev] (faces of level l at [3l + d]), macphi[nlev]
+ * (may be NULL), macrhs[nlev], rho[nlev], beta0: host array of every level's rows, level 0's
+ * nr0 then level 1's nr1 = 2 nr0 (the (lev, r) rows of the reference's BaseState); its edges
+ * come from CelltoEdge over each level's radial chunks, level 1's restricted onto level 0.
+ * The composite problem: phi on the level-0 cells no level-1 box covers and on the level-1
+ * cells; a level-1 cell sees across a coarse-fine face the ghost (1/3) phi_fine +
+ * (2/3) phi_parent, and a level-0 cell's flux through that face is the mean of the four fine
+ * fluxes.  (The reference's MLMG interpolates its coarse-fine ghosts in AMReX's own way,
+ * which is not restated here: the two agree to the discretisation error at the coarse-fine
+ * boundary, not to the tolerance.)  Solved to max|residual| <= tol_rel max|rhs| by
+ * conjugate gradients preconditioned with a level-0 V-cycle and level-1 smoothing; then
+ * AverageDownFaces and FillPatchUedge of umac, as the reference ends.  result.iterations
+ * counts conjugate-gradient iterations.  A level-1 face on the coarse-fine boundary takes
+ * the parent coarse cell's rho outside. */
+int madv_mac_project_levels(madv_ctx* ctx, int nlev, const madv_multifab* umac, const madv_multifab* macphi,
+                            const madv_multifab* macrhs, const madv_multifab* rho, const double* beta0,
+                            double tol_rel, int max_iter, madv_mac_result* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

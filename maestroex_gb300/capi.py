@@ -29,7 +29,8 @@ EXPORTED = [
     "madv_set_base_state_levels", "madv_stage_forward_levels", "madv_stage_adjoint",
     "madv_autotune_trial", "madv_autotune_ppm_trial", "madv_autotune_finish", "madv_autotune_apply",
     "madv_make_utrans", "madv_vel_pred", "madv_make_edge_scal", "madv_make_rhox_flux", "madv_make_rhoh_flux",
-    "madv_update_scal", "madv_velocity_advance", "madv_est_dt", "madv_mac_project", "madv_set_option",
+    "madv_update_scal", "madv_velocity_advance", "madv_est_dt", "madv_mac_project", "madv_mac_project_levels",
+    "madv_set_option",
 ]
 
 
@@ -114,6 +115,8 @@ def lib():
         L.madv_est_dt.argtypes = [C.c_void_p, I, MF, MF, MF, P(MadvDtParams), P(MadvDtResult), C.c_void_p]
         L.madv_mac_project.argtypes = [C.c_void_p, MF, MF, MF, MF, P(C.c_double), C.c_double, I, P(MadvMacResult),
                                        C.c_void_p]
+        L.madv_mac_project_levels.argtypes = [C.c_void_p, I, MF, MF, MF, MF, P(C.c_double), C.c_double, I,
+                                              P(MadvMacResult), C.c_void_p]
         L.madv_stage_forward.argtypes = [C.c_void_p, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,
                                          C.c_void_p]
         L.madv_stage_forward_levels.argtypes = [C.c_void_p, C.c_int, C.c_int, MF, MF, MF, MF, MF, MF, MF, MF, MF,

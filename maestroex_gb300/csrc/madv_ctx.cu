@@ -1869,9 +1869,10 @@ int madv_stage_forward_levels(madv_ctx* h, int mode, int nlev, const madv_multif
 
 // ---- Maestro-shaped entry points (one level): the same pieces, with the caller's FABs
 // copied in and out around each call.
-static int begin_call(madv_ctx* h, void* stream, Hier& H) {
+// levels: the entry takes every level of the layout (else it takes one level only)
+static int begin_call(madv_ctx* h, void* stream, Hier& H, bool levels = false) {
     if (!h) return MADV_ERR_PARAM;
-    if (!h->fine.empty()) {
+    if (!h->fine.empty() && !levels) {
         set_error("the per-function entry points take one level; use madv_stage_forward_levels");
         return MADV_ERR_UNSUPPORTED;
     }
@@ -2323,6 +2324,63 @@ int madv_mac_project(madv_ctx* h, const madv_multifab* umac, const madv_multifab
         }
         if (rc) return rc;
         for (int d = 0; d < 3; ++d) copy_fab(c, F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
+        return finish(H);
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+// MacProj on an AMR hierarchy of two plane-parallel levels (Source/MaestroMacProj.cpp:11-236):
+// the composite solve of madv_macproj.cu, then AverageDownFaces and FillPatchUedge of umac.
+int madv_mac_project_levels(madv_ctx* h, int nlev, const madv_multifab* umac, const madv_multifab* macphi,
+                            const madv_multifab* macrhs, const madv_multifab* rho, const double* beta0,
+                            double tol_rel, int max_iter, madv_mac_result* result, void* stream) {
+    Hier H;
+    int rc = begin_call(h, stream, H, true);
+    if (rc) return rc;
+    if (!umac || !macrhs || !rho || !beta0 || !(tol_rel > 0.0) || max_iter < 1 || nlev != H.n()) {
+        set_error("madv_mac_project_levels: one entry per level of the layout; umac, macrhs, rho, beta0, "
+                  "tol_rel > 0 and max_iter >= 1 are required");
+        return MADV_ERR_PARAM;
+    }
+    if (nlev == 1) return madv_mac_project(h, umac, macphi, macrhs, rho, beta0, tol_rel, max_iter, result, stream);
+    if (nlev != 2 || H[0].sph || H[0].ndim != 3) {
+        set_error("madv_mac_project_levels covers one or two 3-D plane-parallel levels");
+        return MADV_ERR_UNSUPPORTED;
+    }
+    try {
+        for (int l = 0; l < 2; ++l) {
+            Ctx& c = H[l];
+            for (int d = 0; d < 3; ++d)
+                if ((rc = bind(c, U_UMAC0 + d, &umac[3 * l + d], 1, d, 1))) return rc;
+            if ((rc = bind(c, U_FORCE, &macrhs[l], 1, -1, 0)) || (rc = bind(c, U_RHOHALF, &rho[l], 1, -1, 0)) ||
+                (rc = bind(c, U_SPONGE, macphi ? &macphi[l] : nullptr, 1, -1, 0)))
+                return rc;
+            if ((rc = upload_user_views(c))) return rc;
+            for (int d = 0; d < 3; ++d) copy_fab(c, F_UMAC0 + d, 0, F_USER + U_UMAC0 + d, 0, 1, 1);
+        }
+        // beta0 on the radial edges of both levels: CelltoEdge over each level's chunks, the
+        // level-1 edges restricted onto level 0 (Source/MaestroCelltoEdge.cpp:17-58,
+        // Source/BaseStateGeometry.cpp:240-262)
+        const int nr0 = H[0].nr, nr1 = H[1].nr;
+        std::vector<double> b0(beta0, beta0 + nr0), b1(beta0 + nr0, beta0 + nr0 + nr1);
+        std::vector<double> e0(nr0 + 1, 0.0), e1(nr1 + 1, 0.0);
+        cell_to_edge_chunk(b0, e0, 0, nr0);
+        for (auto& ch : H[1].chunks) cell_to_edge_chunk(b1, e1, ch[0], ch[1] + 1);
+        for (auto& ch : H[1].chunks)
+            for (int j = ch[0]; j <= ch[1] + 1; j += 2) e0[j / 2] = e1[j];
+        int it = 0;
+        double ratio = 0.0;
+        rc = mac_project_two_levels(H[0], H[1], U_FORCE, U_RHOHALF, macphi ? U_SPONGE : -1, b0.data(), e0.data(),
+                                    b1.data(), e1.data(), tol_rel, max_iter, &it, &ratio);
+        if (result) {
+            result->iterations = it;
+            result->resid_ratio = ratio;
+        }
+        if (rc) return rc;
+        sync_faces_h(H, F_UMAC0);  // AverageDownFaces, FillPatchUedge, the ghost faces
+        for (int l = 0; l < 2; ++l)
+            for (int d = 0; d < 3; ++d) copy_fab(H[l], F_USER + U_UMAC0 + d, 0, F_UMAC0 + d, 0, 1, 1);
         return finish(H);
     } catch (const Fail& f) {
         return f.code;

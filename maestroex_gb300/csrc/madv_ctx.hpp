@@ -242,6 +242,10 @@ void fill_face_ghosts(Ctx& c, int f0);  // FillBoundary + FillUmacGhost of 3 fac
 void mac_free(Ctx& c);
 int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0, const double* beta0_edge,
                       double tol_rel, int max_iter, int* iters_out, double* ratio_out);
+// MacProj on two plane-parallel levels (madv_macproj.cu): level 0 in c, level 1 in f
+int mac_project_two_levels(Ctx& c, Ctx& f, int srhs, int srho, int sphi, const double* b0c, const double* b0ce,
+                           const double* b1, const double* b1e, double tol_rel, int max_iter, int* iters_out,
+                           double* ratio_out);
 void addw0(Ctx& c, int f0, double mult);
 void set_val(Ctx& c, int fid, double v, int c0, int nc, int ngrow);
 void copy_fab(Ctx& c, int dst, int dc0, int src, int sc0, int nc, int ngrow);

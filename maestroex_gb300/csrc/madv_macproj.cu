@@ -415,10 +415,31 @@ struct MacMG {
     double* d_beta = nullptr;  // beta0 [nr], beta0_edge [nr + 1]
     double* d_bface[3] = {nullptr, nullptr, nullptr};  // spherical: beta0 on the domain's faces
     double* pcg = nullptr;  // spherical: x, r, p, q, z of the PCG, one block of ncell each
+    struct MLFine* ml = nullptr;  // two levels: the level-1 grid and the composite solve's arrays
 };
+
+// Two levels (refinement ratio 2): the level-1 domain as one dense grid (its cells off the
+// level-1 boxes unused), the masks, the composite diagonals and the PCG vectors of both levels
+struct MLFine {
+    MGGrid g{};
+    int n1[3] = {0, 0, 0};
+    std::vector<double*> mem;
+    double *mask = nullptr, *cov = nullptr;      // level-1 cells of a box; covered level-0 cells
+    double *cdiag0 = nullptr, *cdiag1 = nullptr;  // the composite operator's diagonals
+    double *v0 = nullptr, *v1 = nullptr;          // x r p q z per level, five blocks each
+    double* beta1 = nullptr;                      // level 1: beta0 [nr1], beta0_edge [nr1 + 1]
+};
+
+static void ml_free(MLFine*& m) {
+    if (!m) return;
+    for (double* p : m->mem) cudaFree(p);
+    delete m;
+    m = nullptr;
+}
 
 void mac_free(Ctx& c) {
     if (!c.mac) return;
+    ml_free(c.mac->ml);
     for (double* p : c.mac->mem) cudaFree(p);
     if (c.mac->d_max) cudaFree(c.mac->d_max);
     if (c.mac->d_sum) cudaFree(c.mac->d_sum);
@@ -729,6 +750,680 @@ int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0,
     launch(c, rg_grow(c, 0, 2), 1, k_mp_correct<2>, c.V(), g, bc, be, 1.0 / c.P.dx[2], l[0], l[1], l[2]);
     if (sphi >= 0) launch(c, rg_grow(c, 0), 1, k_mp_phi_out, c.V(), g, sphi, l[0], l[1], l[2]);
     fill_face_ghosts(c, F_UMAC0);
+    return MADV_OK;
+}
+
+
+// ======================================================================= two levels
+// The composite system (plane-parallel, refinement ratio 2).  Unknowns: phi on the level-0
+// cells no level-1 box covers and on the level-1 cells.  A level-1 cell sees across a
+// coarse-fine face the ghost (1/3) phi_c + (2/3) phi_parent (linear along the normal between
+// its own centre, h1/2 inside, and the coarse centre, h1 outside): face weight (2/3) W1.  A
+// level-0 cell takes across a face shared with a covered cell the mean of the four fine
+// fluxes: weight (1/4)(2/3) B1 / (h0 h1) per fine cell.  With volume weights the operator is
+// symmetric.  MLMG's coarse-fine interpolation is AMReX's and not restated here.
+
+// the neighbour of grid cell a along D on side s (-1 / +1): false outside a non-periodic
+// face (t receives the face's boundary type), else b holds it (wrapped)
+__device__ __forceinline__ bool ml_nb(const MGGrid& g, const MGBC& bc, const int a[3], int D, int s, int b[3], int& t) {
+    b[0] = a[0];
+    b[1] = a[1];
+    b[2] = a[2];
+    b[D] += s;
+    if (b[D] >= 0 && b[D] < g.n[D]) return true;
+    t = s < 0 ? bc.lo[D] : bc.hi[D];
+    if (t != MG_PER) return false;
+    b[D] = s < 0 ? g.n[D] - 1 : 0;
+    return true;
+}
+// face index along D of the s-side face of cell a
+__device__ __forceinline__ long ml_face(const MGGrid& g, const int a[3], int D, int s) {
+    int f[3] = {a[0], a[1], a[2]};
+    if (s > 0) f[D] += 1;
+    return D == 0 ? mg_face<0>(g, f[0], f[1], f[2]) : (D == 1 ? mg_face<1>(g, f[0], f[1], f[2]) : mg_face<2>(g, f[0], f[1], f[2]));
+}
+
+// level-1 cells of the boxes (valid cells of the fine level) into the mask
+__global__ void k_ml_mask(KARGS, MGGrid F, double* mask, int l0, int l1, int l2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    mask[mg_cell(F, i - l0, j - l1, k - l2)] = 1.0;
+}
+// covered level-0 cells: all eight children in the mask
+__global__ void k_ml_cov(MGGrid C, MGGrid F, const double* __restrict__ mask, double* cov) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)C.n[0] * C.n[1] * C.n[2]) return;
+    int I, J, K;
+    mg_ijk(C, c, I, J, K);
+    double m = 1.0;
+    for (int q = 0; q < 8; ++q) m *= mask[mg_cell(F, 2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2))];
+    cov[c] = m;
+}
+
+// valid cells of a level: rho into g.res, macrhs into g.rhs, phi = 0
+__global__ void k_ml_gather_cells(KARGS, MGGrid g, int srhs, int srho, int l0, int l1, int l2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const long c = mg_cell(g, i - l0, j - l1, k - l2);
+    g.res[c] = at(VW(F_USER + srho), i, j, k);
+    g.rhs[c] = at(VW(F_USER + srhs), i, j, k);
+    g.phi[c] = 0.0;
+}
+// valid D-faces of a level: beta0 umac into g.W[D] (scratch until the weights are formed)
+template <int D>
+__global__ void k_ml_gather_faces(KARGS, MGGrid g, MPBeta be, int l0, int l1, int l2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const int a0 = i - l0, a1 = j - l1, a2 = k - l2;
+    g.W[D][mg_face<D>(g, a0, a1, a2)] = at(VW(F_UMAC0 + D), i, j, k) * mp_beta<D>(be, g, a0, a1, a2);
+}
+// a level-1 face belongs to a box when a cell on either side is in the mask (across a
+// periodic face, the wrapped cell)
+template <int D>
+__device__ __forceinline__ bool ml_box_face(const MGGrid& F, const MGBC& bc, const double* __restrict__ mask, int f0,
+                                            int f1, int f2) {
+    const int a[3] = {f0, f1, f2};
+    int l[3] = {f0, f1, f2}, r[3] = {f0, f1, f2};
+    l[D] -= 1;
+    bool in = false;
+    if (a[D] < F.n[D]) in = in || mask[mg_cell(F, r[0], r[1], r[2])] != 0.0;
+    else if (bc.hi[D] == MG_PER) {
+        r[D] = 0;
+        in = in || mask[mg_cell(F, r[0], r[1], r[2])] != 0.0;
+    }
+    if (a[D] > 0) in = in || mask[mg_cell(F, l[0], l[1], l[2])] != 0.0;
+    else if (bc.lo[D] == MG_PER) {
+        l[D] = F.n[D] - 1;
+        in = in || mask[mg_cell(F, l[0], l[1], l[2])] != 0.0;
+    }
+    return in;
+}
+// AverageDownFaces of beta0 umac: a level-0 face whose four level-1 faces belong to boxes
+// takes their mean
+template <int D>
+__global__ void k_ml_avgdown_bu(MGGrid C, MGGrid F, MGBC bc, const double* __restrict__ mask) {
+    constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    int nc[3] = {C.n[0], C.n[1], C.n[2]};
+    nc[D] += 1;
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)nc[0] * nc[1] * nc[2]) return;
+    int a[3];
+    a[0] = (int)(c % nc[0]);
+    a[1] = (int)((c / nc[0]) % nc[1]);
+    a[2] = (int)(c / ((long)nc[0] * nc[1]));
+    double s = 0.0;
+    for (int q = 0; q < 4; ++q) {
+        int b[3] = {2 * a[0], 2 * a[1], 2 * a[2]};
+        b[T1] += q & 1;
+        b[T2] += q >> 1;
+        if (!ml_box_face<D>(F, bc, mask, b[0], b[1], b[2])) return;
+        s += F.W[D][mg_face<D>(F, b[0], b[1], b[2])];
+    }
+    C.W[D][c] = 0.25 * s;
+}
+// rhs -= div(beta0 umac) (faces in g.W), on the cells of weight != 0 (every cell: wt null)
+__global__ void k_ml_rhs(MGGrid g, const double* __restrict__ wt) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)g.n[0] * g.n[1] * g.n[2]) return;
+    if (wt && wt[c] == 0.0) {
+        g.rhs[c] = 0.0;
+        return;
+    }
+    int i, j, k;
+    mg_ijk(g, c, i, j, k);
+    const double h0 = sqrt(1.0 / g.ih2[0]), h1 = sqrt(1.0 / g.ih2[1]), h2 = sqrt(1.0 / g.ih2[2]);
+    g.rhs[c] -= (g.W[0][mg_face<0>(g, i + 1, j, k)] - g.W[0][mg_face<0>(g, i, j, k)]) / h0 +
+                (g.W[1][mg_face<1>(g, i, j + 1, k)] - g.W[1][mg_face<1>(g, i, j, k)]) / h1 +
+                (g.W[2][mg_face<2>(g, i, j, k + 1)] - g.W[2][mg_face<2>(g, i, j, k)]) / h2;
+}
+// level-1 cells off the boxes take their parent's rho (the outside of a coarse-fine face)
+__global__ void k_ml_rho_out(MGGrid F, MGGrid C, const double* __restrict__ mask) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)F.n[0] * F.n[1] * F.n[2]) return;
+    if (mask[c] != 0.0) return;
+    int i, j, k;
+    mg_ijk(F, c, i, j, k);
+    F.res[c] = C.res[mg_cell(C, i / 2, j / 2, k / 2)];
+}
+
+// the weight of the s-side face of level-1 cell a toward a coarse-fine ghost or a fine
+// neighbour; fc receives the neighbour (or the parent, coarse) and its kind
+struct MLTerm {
+    double w;
+    long nb;   // fine neighbour, or parent coarse cell, or -1 (boundary)
+    int coarse;
+};
+__device__ __forceinline__ MLTerm ml_fine_term(const MGGrid& F, const MGGrid& C, const MGBC& bc,
+                                               const double* __restrict__ mask, const int a[3], int D, int s) {
+    const double W = F.W[D][ml_face(F, a, D, s)];
+    int b[3], t = MG_PER;
+    if (!ml_nb(F, bc, a, D, s, b, t)) return MLTerm{t == MG_DIR ? 2.0 * W : 0.0, -1, 0};
+    const long nb = mg_cell(F, b[0], b[1], b[2]);
+    if (mask[nb] != 0.0) return MLTerm{W, nb, 0};
+    return MLTerm{(2.0 / 3.0) * W, mg_cell(C, b[0] / 2, b[1] / 2, b[2] / 2), 1};
+}
+
+// composite diagonal of the level-1 cells
+__global__ void k_ml_cdiag1(MGGrid F, MGGrid C, MGBC bc, const double* __restrict__ mask, double* cd) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)F.n[0] * F.n[1] * F.n[2]) return;
+    if (mask[c] == 0.0) {
+        cd[c] = 0.0;
+        return;
+    }
+    int a[3];
+    mg_ijk(F, c, a[0], a[1], a[2]);
+    double d = 0.0;
+    for (int D = 0; D < 3; ++D)
+        for (int s = -1; s <= 1; s += 2) d += ml_fine_term(F, C, bc, mask, a, D, s).w;
+    cd[c] = d;
+}
+
+// the level-0 side of a coarse-fine face: the four level-1 cells behind it and the weight of
+// each, (1/4)(2/3) B1 / (h0 h1) = W1 / 12 (W1 = B1 / h1^2, h0 = 2 h1)
+__device__ __forceinline__ void ml_cf_cells(const MGGrid& F, const int q[3], int D, int s, long cells[4], double w[4]) {
+    const int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
+    for (int m = 0; m < 4; ++m) {
+        int cc[3] = {2 * q[0], 2 * q[1], 2 * q[2]};
+        cc[D] = s > 0 ? 2 * q[D] : 2 * q[D] + 1;
+        cc[T1] += m & 1;
+        cc[T2] += m >> 1;
+        cells[m] = mg_cell(F, cc[0], cc[1], cc[2]);
+        w[m] = F.W[D][ml_face(F, cc, D, -s)] / 12.0;
+    }
+}
+
+// composite diagonal of the uncovered level-0 cells (0 on covered ones)
+__global__ void k_ml_cdiag0(MGGrid C, MGGrid F, MGBC bc, const double* __restrict__ cov, double* cd) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)C.n[0] * C.n[1] * C.n[2]) return;
+    if (cov[c] != 0.0) {
+        cd[c] = 0.0;
+        return;
+    }
+    int a[3];
+    mg_ijk(C, c, a[0], a[1], a[2]);
+    double d = 0.0;
+    for (int D = 0; D < 3; ++D)
+        for (int s = -1; s <= 1; s += 2) {
+            const double W = C.W[D][ml_face(C, a, D, s)];
+            int q[3], t = MG_PER;
+            if (!ml_nb(C, bc, a, D, s, q, t)) {
+                if (t == MG_DIR) d += 2.0 * W;
+                continue;
+            }
+            if (cov[mg_cell(C, q[0], q[1], q[2])] == 0.0) {
+                d += W;
+                continue;
+            }
+            long cells[4];
+            double w[4];
+            ml_cf_cells(F, q, D, s, cells, w);
+            d += w[0] + w[1] + w[2] + w[3];
+        }
+    cd[c] = d;
+}
+
+// q = A p on both levels (cells outside the unknowns get 0)
+__global__ void k_ml_apply0(MGGrid C, MGGrid F, MGBC bc, const double* __restrict__ cov,
+                            const double* __restrict__ cd, const double* __restrict__ p0,
+                            const double* __restrict__ p1, double* __restrict__ q0) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)C.n[0] * C.n[1] * C.n[2]) return;
+    if (cov[c] != 0.0) {
+        q0[c] = 0.0;
+        return;
+    }
+    int a[3];
+    mg_ijk(C, c, a[0], a[1], a[2]);
+    double off = 0.0;
+    for (int D = 0; D < 3; ++D)
+        for (int s = -1; s <= 1; s += 2) {
+            int q[3], t = MG_PER;
+            if (!ml_nb(C, bc, a, D, s, q, t)) continue;
+            const long nb = mg_cell(C, q[0], q[1], q[2]);
+            if (cov[nb] == 0.0) {
+                off += C.W[D][ml_face(C, a, D, s)] * p0[nb];
+                continue;
+            }
+            long cells[4];
+            double w[4];
+            ml_cf_cells(F, q, D, s, cells, w);
+            for (int m = 0; m < 4; ++m) off += w[m] * p1[cells[m]];
+        }
+    q0[c] = cd[c] * p0[c] - off;
+}
+__global__ void k_ml_apply1(MGGrid F, MGGrid C, MGBC bc, const double* __restrict__ mask,
+                            const double* __restrict__ cd, const double* __restrict__ p1,
+                            const double* __restrict__ p0, double* __restrict__ q1) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)F.n[0] * F.n[1] * F.n[2]) return;
+    if (mask[c] == 0.0) {
+        q1[c] = 0.0;
+        return;
+    }
+    int a[3];
+    mg_ijk(F, c, a[0], a[1], a[2]);
+    double off = 0.0;
+    for (int D = 0; D < 3; ++D)
+        for (int s = -1; s <= 1; s += 2) {
+            const MLTerm t = ml_fine_term(F, C, bc, mask, a, D, s);
+            if (t.nb >= 0) off += t.w * (t.coarse ? p0[t.nb] : p1[t.nb]);
+        }
+    q1[c] = cd[c] * p1[c] - off;
+}
+
+// part[block] = the block's sum over both levels of wt * x * y (weights: 1 on uncovered
+// level-0 cells, 1/8 on level-1 cells of the boxes, 0 elsewhere), in a fixed order;
+// out_max (when given) = max |x| over the unknowns
+__global__ void k_ml_dot(const double* __restrict__ x0, const double* __restrict__ y0, const double* __restrict__ cov,
+                         long n0, const double* __restrict__ x1, const double* __restrict__ y1,
+                         const double* __restrict__ mask, long n1, double* part, unsigned long long* out_max) {
+    __shared__ double ws[32];
+    double s = 0.0, m = 0.0;
+    for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n0 + n1; c += (long)gridDim.x * blockDim.x) {
+        double w, x, y;
+        if (c < n0) {
+            w = 1.0 - cov[c];
+            x = x0[c];
+            y = y0 ? y0[c] : 1.0;
+        } else {
+            w = 0.125 * mask[c - n0];
+            x = x1[c - n0];
+            y = y1 ? y1[c - n0] : 1.0;
+        }
+        if (w != 0.0) {
+            s += w * x * y;
+            m = fmax(m, fabs(x));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ws[threadIdx.x >> 5] = s;
+        if (out_max) atomicMax(out_max, (unsigned long long)__double_as_longlong(m));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += ws[w];
+        part[blockIdx.x] = b;
+    }
+}
+// x -= sum / vol on the unknowns (a mean-free projection of a singular system)
+__global__ void k_ml_shift(double* __restrict__ x0, const double* __restrict__ cov, long n0, double* __restrict__ x1,
+                           const double* __restrict__ mask, long n1, const double* __restrict__ sum, double inv_vol) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n0) {
+        if (cov[c] == 0.0) x0[c] -= sum[0] * inv_vol;
+    } else if (c < n0 + n1) {
+        if (mask[c - n0] != 0.0) x1[c - n0] -= sum[0] * inv_vol;
+    }
+}
+
+// preconditioner: the coarse rhs (uncovered cells: r0; covered: the mean of the children's
+// r1), a level-0 V-cycle, the result prolonged to level 1 and smoothed there
+__global__ void k_ml_restrict(MGGrid C, MGGrid F, const double* __restrict__ cov, const double* __restrict__ r0,
+                              const double* __restrict__ r1) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)C.n[0] * C.n[1] * C.n[2]) return;
+    double v = r0[c];
+    if (cov[c] != 0.0) {
+        int I, J, K;
+        mg_ijk(C, c, I, J, K);
+        double s = 0.0;
+        for (int q = 0; q < 8; ++q) s += r1[mg_cell(F, 2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2))];
+        v = 0.125 * s;
+    }
+    C.rhs[c] = v;
+    C.phi[c] = 0.0;
+}
+__global__ void k_ml_prolong(MGGrid F, MGGrid C, const double* __restrict__ mask, const double* __restrict__ cov,
+                             double* __restrict__ z0, double* __restrict__ z1) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long n0 = (long)C.n[0] * C.n[1] * C.n[2];
+    if (c < n0) z0[c] = cov[c] != 0.0 ? 0.0 : C.phi[c];
+    if (c >= (long)F.n[0] * F.n[1] * F.n[2]) return;
+    int i, j, k;
+    mg_ijk(F, c, i, j, k);
+    z1[c] = mask[c] != 0.0 ? C.phi[mg_cell(C, i / 2, j / 2, k / 2)] : 0.0;
+}
+// Gauss-Seidel on the level-1 cells of one colour for A z = r, the coarse-fine ghosts from z0
+__global__ void k_ml_smooth1(MGGrid F, MGGrid C, MGBC bc, const double* __restrict__ mask,
+                             const double* __restrict__ cd, const double* __restrict__ r1,
+                             const double* __restrict__ z0, double* __restrict__ z1, int color) {
+    const long half = (long)F.n[0] * F.n[1] * F.n[2] / 2;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= half) return;
+    const long row = t / (F.n[0] / 2);
+    const int jj = (int)(row % F.n[1]), kk = (int)(row / F.n[1]);
+    const int ii = 2 * (int)(t % (F.n[0] / 2)) + ((jj + kk + color) & 1);
+    const long c = mg_cell(F, ii, jj, kk);
+    if (mask[c] == 0.0 || cd[c] <= 0.0) return;
+    const int a[3] = {ii, jj, kk};
+    double off = 0.0;
+    for (int D = 0; D < 3; ++D)
+        for (int s = -1; s <= 1; s += 2) {
+            const MLTerm q = ml_fine_term(F, C, bc, mask, a, D, s);
+            if (q.nb >= 0) off += q.w * (q.coarse ? z0[q.nb] : z1[q.nb]);
+        }
+    z1[c] = (r1[c] + off) / cd[c];
+}
+// x += a p, r -= a q on a level
+__global__ void k_ml_step(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                          const double* __restrict__ q, double a, long n) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    x[c] += a * p[c];
+    r[c] -= a * q[c];
+}
+
+// phi of both levels from the solution: level 1 on its cells; level 0 on the uncovered
+// cells, and on the covered ones the mean of the children
+__global__ void k_ml_phi(MGGrid C, MGGrid F, const double* __restrict__ cov, const double* __restrict__ mask,
+                         const double* __restrict__ x0, const double* __restrict__ x1) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long n0 = (long)C.n[0] * C.n[1] * C.n[2], n1 = (long)F.n[0] * F.n[1] * F.n[2];
+    if (c < n1) F.phi[c] = mask[c] != 0.0 ? x1[c] : 0.0;
+    if (c >= n0) return;
+    if (cov[c] == 0.0) {
+        C.phi[c] = x0[c];
+        return;
+    }
+    int I, J, K;
+    mg_ijk(C, c, I, J, K);
+    double s = 0.0;
+    for (int q = 0; q < 8; ++q) s += x1[mg_cell(F, 2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2))];
+    C.phi[c] = 0.125 * s;
+}
+
+// valid D-faces of the level-1 boxes: beta0 umac += -B grad phi, umac /= beta0; a cell off
+// the boxes is the ghost (1/3) phi of the cell across + (2/3) phi of its parent
+template <int D>
+__global__ void k_ml_correct1(KARGS, MGGrid F, MGGrid C, MGBC bc, MPBeta be, const double* __restrict__ mask,
+                              double inv_h, int l0, int l1, int l2) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    const int a[3] = {i - l0, j - l1, k - l2};
+    const double B = F.B[D][mg_face<D>(F, a[0], a[1], a[2])];
+    int r[3] = {a[0], a[1], a[2]};  // the cell on the high side (wrapped)
+    if (r[D] >= F.n[D]) r[D] = 0;
+    auto value = [&](const int q[3], const int other[3]) {
+        const long cq = mg_cell(F, q[0], q[1], q[2]);
+        if (mask[cq] != 0.0) return F.phi[cq];
+        return (1.0 / 3.0) * F.phi[mg_cell(F, other[0], other[1], other[2])] +
+               (2.0 / 3.0) * C.phi[mg_cell(C, q[0] / 2, q[1] / 2, q[2] / 2)];
+    };
+    double grad;
+    if (a[D] == 0 && bc.lo[D] != MG_PER) {
+        grad = bc.lo[D] == MG_DIR ? (F.phi[mg_cell(F, r[0], r[1], r[2])] - (-F.phi[mg_cell(F, r[0], r[1], r[2])])) * inv_h
+                                  : 0.0;
+    } else if (a[D] == F.n[D] && bc.hi[D] != MG_PER) {
+        int q[3] = {a[0], a[1], a[2]};
+        q[D] = F.n[D] - 1;
+        const double v = F.phi[mg_cell(F, q[0], q[1], q[2])];
+        grad = bc.hi[D] == MG_DIR ? ((-v) - v) * inv_h : 0.0;
+    } else {
+        int q[3] = {a[0], a[1], a[2]};  // the low-side cell (wrapped)
+        q[D] = a[D] == 0 ? F.n[D] - 1 : a[D] - 1;
+        grad = (value(r, q) - value(q, r)) * inv_h;
+    }
+    const double beta = mp_beta<D>(be, F, a[0], a[1], a[2]);
+    double& u = at(VW(F_UMAC0 + D), i, j, k);
+    u = (u * beta + -B * grad) / beta;
+}
+
+
+// sum over the unknowns of both levels of wt x y (y null: wt x) and max |x|, read back
+static int ml_dot(Ctx& c, const double* x0, const double* y0, long n0, const double* x1, const double* y1, long n1,
+                  double& sum, double* amax) {
+    MacMG& M = *c.mac;
+    MLFine& L = *M.ml;
+    if (amax) MP_CK(cudaMemsetAsync(M.d_max, 0, sizeof(unsigned long long), c.stream));
+    const unsigned nb = (unsigned)std::min<long>((n0 + n1 + TPB - 1) / TPB, NORM_BLOCKS);
+    k_ml_dot<<<nb, TPB, 0, c.stream>>>(x0, y0, L.cov, n0, x1, y1, L.mask, n1, M.d_part, amax ? M.d_max : nullptr);
+    k_mg_sum_parts<<<1, 1, 0, c.stream>>>(M.d_part, (int)nb, M.d_sum);
+    c.launches += 2;
+    unsigned long long bits = 0;
+    MP_CK(cudaMemcpyAsync(&sum, M.d_sum, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    if (amax) MP_CK(cudaMemcpyAsync(&bits, M.d_max, sizeof(bits), cudaMemcpyDeviceToHost, c.stream));
+    MP_CK(cudaStreamSynchronize(c.stream));
+    if (amax) std::memcpy(amax, &bits, sizeof(double));
+    return MADV_OK;
+}
+
+// MacProj on two plane-parallel levels (the composite system above).  The caller has bound
+// macrhs (slot srhs), rho (srho), macphi (sphi, may be < 0) on both levels and copied umac
+// into F_UMAC0..2 of both; umac is corrected there (level-0 faces under level 1 are left for
+// the caller's AverageDownFaces).  b0c / b0ce: beta0 and its edges of level 0 (nr0, nr0 + 1);
+// b1 / b1e of level 1 (nr1 = 2 nr0).  The solve: conjugate gradients in the volume-weighted
+// inner product, preconditioned by a level-0 V-cycle on the restricted residual, prolonged
+// and smoothed on level 1 (two red-black sweeps), flexible update; every sum in a fixed order.
+int mac_project_two_levels(Ctx& c, Ctx& f, int srhs, int srho, int sphi, const double* b0c, const double* b0ce,
+                           const double* b1, const double* b1e, double tol_rel, int max_iter, int* iters_out,
+                           double* ratio_out) {
+    int n0[3], lo0[3], lo1[3], n1[3];
+    MGBC bc{};
+    bool dirichlet = false;
+    for (int d = 0; d < 3; ++d) {
+        lo0[d] = c.P.dom_lo[d];
+        lo1[d] = f.P.dom_lo[d];
+        n0[d] = c.P.dom_hi[d] - c.P.dom_lo[d] + 1;
+        n1[d] = 2 * n0[d];
+        if (n0[d] % 2 != 0) {
+            set_error("the MAC projection needs even domain extents");
+            return MADV_ERR_UNSUPPORTED;
+        }
+        auto t = [&](int pb) {
+            if (c.per[d]) return (int)MG_PER;
+            if (pb == PB_OUTFLOW) return (int)MG_DIR;
+            return (int)MG_NEU;
+        };
+        bc.lo[d] = t(c.P.phys_bc_lo[d]);
+        bc.hi[d] = t(c.P.phys_bc_hi[d]);
+        dirichlet = dirichlet || bc.lo[d] == MG_DIR || bc.hi[d] == MG_DIR;
+    }
+    const int nr0 = n0[2], nr1 = n1[2];
+    int rc = mac_hierarchy(c, n0, nr0);
+    if (rc) return rc;
+    MacMG& M = *c.mac;
+    if (!M.ml || M.ml->n1[0] != n1[0] || M.ml->n1[1] != n1[1] || M.ml->n1[2] != n1[2]) {
+        ml_free(M.ml);
+        M.ml = new MLFine();
+        MLFine& L = *M.ml;
+        for (int d = 0; d < 3; ++d) L.n1[d] = n1[d];
+        const long c1 = (long)n1[0] * n1[1] * n1[2], c0 = (long)n0[0] * n0[1] * n0[2];
+        auto alloc = [&](long cnt) -> double* {
+            double* p = nullptr;
+            if (cudaMalloc(&p, sizeof(double) * cnt) != cudaSuccess) return nullptr;
+            L.mem.push_back(p);
+            return p;
+        };
+        MGGrid& F = L.g;
+        for (int d = 0; d < 3; ++d) F.n[d] = n1[d];
+        F.phi = alloc(c1);
+        F.rhs = alloc(c1);
+        F.res = alloc(c1);
+        bool ok = F.phi && F.rhs && F.res;
+        for (int d = 0; d < 3; ++d) {
+            F.B[d] = alloc(c1 / n1[d] * (n1[d] + 1));
+            F.W[d] = alloc(c1 / n1[d] * (n1[d] + 1));
+            ok = ok && F.B[d] && F.W[d];
+        }
+        L.mask = alloc(c1);
+        L.cov = alloc(c0);
+        L.cdiag0 = alloc(c0);
+        L.cdiag1 = alloc(c1);
+        L.v0 = alloc(5 * c0);
+        L.v1 = alloc(5 * c1);
+        L.beta1 = alloc(2 * nr1 + 1);
+        ok = ok && L.mask && L.cov && L.cdiag0 && L.cdiag1 && L.v0 && L.v1 && L.beta1;
+        if (!ok) {
+            ml_free(M.ml);
+            set_error("cudaMalloc(two-level MAC projection)");
+            return MADV_ERR_CUDA;
+        }
+    }
+    MLFine& L = *M.ml;
+    MGGrid& C = M.lev[0];
+    MGGrid& F = L.g;
+    for (int d = 0; d < 3; ++d) F.ih2[d] = 1.0 / (f.P.dx[d] * f.P.dx[d]);
+    const long N0 = ncell(C), N1 = ncell(F);
+    MP_CK(cudaMemcpyAsync(M.d_beta, b0c, sizeof(double) * nr0, cudaMemcpyHostToDevice, c.stream));
+    MP_CK(cudaMemcpyAsync(M.d_beta + nr0, b0ce, sizeof(double) * (nr0 + 1), cudaMemcpyHostToDevice, c.stream));
+    MP_CK(cudaMemcpyAsync(L.beta1, b1, sizeof(double) * nr1, cudaMemcpyHostToDevice, c.stream));
+    MP_CK(cudaMemcpyAsync(L.beta1 + nr1, b1e, sizeof(double) * (nr1 + 1), cudaMemcpyHostToDevice, c.stream));
+    const MPBeta be0{M.d_beta, M.d_beta + nr0, {nullptr, nullptr, nullptr}, 0};
+    const MPBeta be1{L.beta1, L.beta1 + nr1, {nullptr, nullptr, nullptr}, 0};
+    // the level-1 cells and the covered level-0 cells
+    MP_CK(cudaMemsetAsync(L.mask, 0, sizeof(double) * N1, c.stream));
+    launch(f, rg_grow(f, 0), 1, k_ml_mask, f.V(), F, L.mask, lo1[0], lo1[1], lo1[2]);
+    k_ml_cov<<<blocks_of(N0), TPB, 0, c.stream>>>(C, F, L.mask, L.cov);
+    // rho, macrhs and beta0 umac of both levels; beta0 umac averaged down; the rhs
+    MP_CK(cudaMemsetAsync(F.res, 0, sizeof(double) * N1, c.stream));
+    MP_CK(cudaMemsetAsync(F.rhs, 0, sizeof(double) * N1, c.stream));
+    MP_CK(cudaMemsetAsync(F.phi, 0, sizeof(double) * N1, c.stream));
+    auto faces = [&](const MGGrid& g, int d) { return ncell(g) / g.n[d] * (g.n[d] + 1); };
+    for (int d = 0; d < 3; ++d) MP_CK(cudaMemsetAsync(F.W[d], 0, sizeof(double) * faces(F, d), c.stream));
+    launch(c, rg_grow(c, 0), 1, k_ml_gather_cells, c.V(), C, srhs, srho, lo0[0], lo0[1], lo0[2]);
+    launch(f, rg_grow(f, 0), 1, k_ml_gather_cells, f.V(), F, srhs, srho, lo1[0], lo1[1], lo1[2]);
+    launch(c, rg_grow(c, 0, 0), 1, k_ml_gather_faces<0>, c.V(), C, be0, lo0[0], lo0[1], lo0[2]);
+    launch(c, rg_grow(c, 0, 1), 1, k_ml_gather_faces<1>, c.V(), C, be0, lo0[0], lo0[1], lo0[2]);
+    launch(c, rg_grow(c, 0, 2), 1, k_ml_gather_faces<2>, c.V(), C, be0, lo0[0], lo0[1], lo0[2]);
+    launch(f, rg_grow(f, 0, 0), 1, k_ml_gather_faces<0>, f.V(), F, be1, lo1[0], lo1[1], lo1[2]);
+    launch(f, rg_grow(f, 0, 1), 1, k_ml_gather_faces<1>, f.V(), F, be1, lo1[0], lo1[1], lo1[2]);
+    launch(f, rg_grow(f, 0, 2), 1, k_ml_gather_faces<2>, f.V(), F, be1, lo1[0], lo1[1], lo1[2]);
+    k_ml_avgdown_bu<0><<<blocks_of(faces(C, 0)), TPB, 0, c.stream>>>(C, F, bc, L.mask);
+    k_ml_avgdown_bu<1><<<blocks_of(faces(C, 1)), TPB, 0, c.stream>>>(C, F, bc, L.mask);
+    k_ml_avgdown_bu<2><<<blocks_of(faces(C, 2)), TPB, 0, c.stream>>>(C, F, bc, L.mask);
+    k_ml_rhs<<<blocks_of(N0), TPB, 0, c.stream>>>(C, nullptr);
+    k_ml_rhs<<<blocks_of(N1), TPB, 0, c.stream>>>(F, L.mask);
+    k_ml_rho_out<<<blocks_of(N1), TPB, 0, c.stream>>>(F, C, L.mask);
+    c.launches += 7;
+    // face coefficients of both levels, the level-0 multigrid (the preconditioner's), weights
+    k_mp_bcoef<0><<<blocks_of(faces(C, 0)), TPB, 0, c.stream>>>(C, bc, be0);
+    k_mp_bcoef<1><<<blocks_of(faces(C, 1)), TPB, 0, c.stream>>>(C, bc, be0);
+    k_mp_bcoef<2><<<blocks_of(faces(C, 2)), TPB, 0, c.stream>>>(C, bc, be0);
+    k_mp_bcoef<0><<<blocks_of(faces(F, 0)), TPB, 0, c.stream>>>(F, bc, be1);
+    k_mp_bcoef<1><<<blocks_of(faces(F, 1)), TPB, 0, c.stream>>>(F, bc, be1);
+    k_mp_bcoef<2><<<blocks_of(faces(F, 2)), TPB, 0, c.stream>>>(F, bc, be1);
+    c.launches += 6;
+    for (size_t q = 1; q < M.lev.size(); ++q) {
+        const MGGrid &fg = M.lev[q - 1], &cg = M.lev[q];
+        k_mg_coarsen_b<0><<<blocks_of(faces(cg, 0)), TPB, 0, c.stream>>>(fg, cg);
+        k_mg_coarsen_b<1><<<blocks_of(faces(cg, 1)), TPB, 0, c.stream>>>(fg, cg);
+        k_mg_coarsen_b<2><<<blocks_of(faces(cg, 2)), TPB, 0, c.stream>>>(fg, cg);
+        c.launches += 3;
+    }
+    for (const MGGrid& q : M.lev) {
+        k_mg_prep_w<0><<<blocks_of(faces(q, 0)), TPB, 0, c.stream>>>(q);
+        k_mg_prep_w<1><<<blocks_of(faces(q, 1)), TPB, 0, c.stream>>>(q);
+        k_mg_prep_w<2><<<blocks_of(faces(q, 2)), TPB, 0, c.stream>>>(q);
+        k_mg_prep_diag<<<blocks_of(ncell(q)), TPB, 0, c.stream>>>(q, bc);
+        c.launches += 4;
+    }
+    k_mg_prep_w<0><<<blocks_of(faces(F, 0)), TPB, 0, c.stream>>>(F);
+    k_mg_prep_w<1><<<blocks_of(faces(F, 1)), TPB, 0, c.stream>>>(F);
+    k_mg_prep_w<2><<<blocks_of(faces(F, 2)), TPB, 0, c.stream>>>(F);
+    k_ml_cdiag0<<<blocks_of(N0), TPB, 0, c.stream>>>(C, F, bc, L.cov, L.cdiag0);
+    k_ml_cdiag1<<<blocks_of(N1), TPB, 0, c.stream>>>(F, C, bc, L.mask, L.cdiag1);
+    c.launches += 5;
+    // conjugate gradients on the composite system
+    double *x0 = L.v0, *r0 = x0 + N0, *p0 = r0 + N0, *q0 = p0 + N0, *z0 = q0 + N0;
+    double *x1 = L.v1, *r1 = x1 + N1, *p1 = r1 + N1, *q1 = p1 + N1, *z1 = q1 + N1;
+    MP_CK(cudaMemsetAsync(x0, 0, sizeof(double) * N0, c.stream));
+    MP_CK(cudaMemsetAsync(x1, 0, sizeof(double) * N1, c.stream));
+    MP_CK(cudaMemcpyAsync(r0, C.rhs, sizeof(double) * N0, cudaMemcpyDeviceToDevice, c.stream));
+    MP_CK(cudaMemcpyAsync(r1, F.rhs, sizeof(double) * N1, cudaMemcpyDeviceToDevice, c.stream));
+    const double inv_vol = 1.0 / (double)N0;  // the composite volume in level-0 cells
+    double sum = 0.0, rhs_max = 0.0;
+    if (!dirichlet) {  // singular: the rhs made mean-free in the volume-weighted sense
+        if ((rc = ml_dot(c, r0, nullptr, N0, r1, nullptr, N1, sum, nullptr))) return rc;
+        k_ml_shift<<<blocks_of(N0 + N1), TPB, 0, c.stream>>>(r0, L.cov, N0, r1, L.mask, N1, M.d_sum, inv_vol);
+        c.launches++;
+    }
+    if ((rc = ml_dot(c, r0, nullptr, N0, r1, nullptr, N1, sum, &rhs_max))) return rc;
+    const double target = tol_rel * rhs_max;
+    auto precondition = [&]() {
+        k_ml_restrict<<<blocks_of(N0), TPB, 0, c.stream>>>(C, F, L.cov, r0, r1);
+        c.launches++;
+        mg_vcycle(c, bc, 0);
+        k_ml_prolong<<<blocks_of(std::max(N0, N1)), TPB, 0, c.stream>>>(F, C, L.mask, L.cov, z0, z1);
+        c.launches++;
+        for (int s = 0; s < 2; ++s) {
+            k_ml_smooth1<<<blocks_of(N1 / 2), TPB, 0, c.stream>>>(F, C, bc, L.mask, L.cdiag1, r1, z0, z1, s);
+            c.launches++;
+        }
+        for (int s = 1; s >= 0; --s) {
+            k_ml_smooth1<<<blocks_of(N1 / 2), TPB, 0, c.stream>>>(F, C, bc, L.mask, L.cdiag1, r1, z0, z1, s);
+            c.launches++;
+        }
+    };
+    auto apply = [&](const double* a0, const double* a1, double* b0, double* b1v) {
+        k_ml_apply0<<<blocks_of(N0), TPB, 0, c.stream>>>(C, F, bc, L.cov, L.cdiag0, a0, a1, b0);
+        k_ml_apply1<<<blocks_of(N1), TPB, 0, c.stream>>>(F, C, bc, L.mask, L.cdiag1, a1, a0, b1v);
+        c.launches += 2;
+    };
+    int it = 0;
+    double res_max = rhs_max;
+    if (res_max > target) {
+        precondition();
+        MP_CK(cudaMemcpyAsync(p0, z0, sizeof(double) * N0, cudaMemcpyDeviceToDevice, c.stream));
+        MP_CK(cudaMemcpyAsync(p1, z1, sizeof(double) * N1, cudaMemcpyDeviceToDevice, c.stream));
+        double rz = 0.0;
+        if ((rc = ml_dot(c, r0, z0, N0, r1, z1, N1, rz, nullptr))) return rc;
+        while (it < max_iter) {
+            apply(p0, p1, q0, q1);
+            double pq = 0.0;
+            if ((rc = ml_dot(c, p0, q0, N0, p1, q1, N1, pq, nullptr))) return rc;
+            if (!(pq > 0.0)) break;
+            const double a = rz / pq;
+            k_ml_step<<<blocks_of(N0), TPB, 0, c.stream>>>(x0, r0, p0, q0, a, N0);
+            k_ml_step<<<blocks_of(N1), TPB, 0, c.stream>>>(x1, r1, p1, q1, a, N1);
+            c.launches += 2;
+            ++it;
+            if ((rc = ml_dot(c, r0, nullptr, N0, r1, nullptr, N1, sum, &res_max))) return rc;
+            if (res_max <= target) break;
+            // z_old into q, z = M^-1 r; flexible (Polak-Ribiere) beta = r.(z - z_old) / rz
+            MP_CK(cudaMemcpyAsync(q0, z0, sizeof(double) * N0, cudaMemcpyDeviceToDevice, c.stream));
+            MP_CK(cudaMemcpyAsync(q1, z1, sizeof(double) * N1, cudaMemcpyDeviceToDevice, c.stream));
+            precondition();
+            double rz_new = 0.0, rzo = 0.0;
+            if ((rc = ml_dot(c, r0, z0, N0, r1, z1, N1, rz_new, nullptr)) ||
+                (rc = ml_dot(c, r0, q0, N0, r1, q1, N1, rzo, nullptr)))
+                return rc;
+            const double bb = (rz_new - rzo) / rz;
+            rz = rz_new;
+            k_pcg_dir<<<blocks_of(N0), TPB, 0, c.stream>>>(p0, z0, bb, N0);
+            k_pcg_dir<<<blocks_of(N1), TPB, 0, c.stream>>>(p1, z1, bb, N1);
+            c.launches += 2;
+        }
+    }
+    if (iters_out) *iters_out = it;
+    if (ratio_out) *ratio_out = rhs_max > 0.0 ? res_max / rhs_max : 0.0;
+    if (res_max > target) {
+        set_error("MAC projection: the composite solve did not reach the tolerance in " + std::to_string(max_iter) +
+                  " iterations");
+        return MADV_ERR_NOCONV;
+    }
+    if (!dirichlet) {  // phi made mean-free (volume-weighted)
+        if ((rc = ml_dot(c, x0, nullptr, N0, x1, nullptr, N1, sum, nullptr))) return rc;
+        k_ml_shift<<<blocks_of(N0 + N1), TPB, 0, c.stream>>>(x0, L.cov, N0, x1, L.mask, N1, M.d_sum, inv_vol);
+        c.launches++;
+    }
+    k_ml_phi<<<blocks_of(std::max(N0, N1)), TPB, 0, c.stream>>>(C, F, L.cov, L.mask, x0, x1);
+    c.launches++;
+    launch(c, rg_grow(c, 0, 0), 1, k_mp_correct<0>, c.V(), C, bc, be0, 1.0 / c.P.dx[0], lo0[0], lo0[1], lo0[2]);
+    launch(c, rg_grow(c, 0, 1), 1, k_mp_correct<1>, c.V(), C, bc, be0, 1.0 / c.P.dx[1], lo0[0], lo0[1], lo0[2]);
+    launch(c, rg_grow(c, 0, 2), 1, k_mp_correct<2>, c.V(), C, bc, be0, 1.0 / c.P.dx[2], lo0[0], lo0[1], lo0[2]);
+    launch(f, rg_grow(f, 0, 0), 1, k_ml_correct1<0>, f.V(), F, C, bc, be1, (const double*)L.mask, 1.0 / f.P.dx[0],
+           lo1[0], lo1[1], lo1[2]);
+    launch(f, rg_grow(f, 0, 1), 1, k_ml_correct1<1>, f.V(), F, C, bc, be1, (const double*)L.mask, 1.0 / f.P.dx[1],
+           lo1[0], lo1[1], lo1[2]);
+    launch(f, rg_grow(f, 0, 2), 1, k_ml_correct1<2>, f.V(), F, C, bc, be1, (const double*)L.mask, 1.0 / f.P.dx[2],
+           lo1[0], lo1[1], lo1[2]);
+    if (sphi >= 0) {
+        launch(c, rg_grow(c, 0), 1, k_mp_phi_out, c.V(), C, sphi, lo0[0], lo0[1], lo0[2]);
+        launch(f, rg_grow(f, 0), 1, k_mp_phi_out, f.V(), F, sphi, lo1[0], lo1[1], lo1[2]);
+    }
     return MADV_OK;
 }
 

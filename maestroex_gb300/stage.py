@@ -278,6 +278,24 @@ class ScalarAdvectionStage:
                                      float(tol_rel), int(max_iter), C.byref(res), C.c_void_p(s)))
         return res.iterations, res.resid_ratio
 
+    def mac_project_levels(self, umac, macrhs, rho, beta0, macphi=None, tol_rel=1.0e-10, max_iter=200, stream=None):
+        """Maestro::MacProj on the layout's levels (two plane-parallel levels: the composite
+        solve): umac[l] (3 face MultiFabs per level, >= 1 ghost) projected in place; macrhs[l],
+        rho[l], macphi[l] per level; beta0[l] the level's radial rows.  Returns (iterations,
+        final max|residual| / max|rhs|)."""
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        nl = len(macrhs)
+        b0 = np.ascontiguousarray(np.concatenate([np.asarray(b, dtype=np.float64) for b in beta0]))
+        faces = (capi.MadvMultiFab * (3 * nl))(*[umac[l][d].desc() for l in range(nl) for d in range(3)])
+        cells = [(capi.MadvMultiFab * nl)(*[m[l].desc() for l in range(nl)]) for m in (macrhs, rho)]
+        phi = None if macphi is None else (capi.MadvMultiFab * nl)(*[macphi[l].desc() for l in range(nl)])
+        res = capi.MadvMacResult()
+        P = C.POINTER(capi.MadvMultiFab)
+        check(lib().madv_mac_project_levels(self.ctx, nl, C.cast(faces, P), None if phi is None else C.cast(phi, P),
+                                            C.cast(cells[0], P), C.cast(cells[1], P), _dptr(b0), float(tol_rel),
+                                            int(max_iter), C.byref(res), C.c_void_p(s)))
+        return res.iterations, res.resid_ratio
+
     def est_dt(self, uold, sold, gpi, cfl=0.5, drdxfac=1, max_dt=1.0e33, fixed_dt=-1.0, small_dt=1.0e-10,
                stream=None):
         """Maestro::EstDt (advective and force constraints): returns (dt, dt_estimate, umax,
