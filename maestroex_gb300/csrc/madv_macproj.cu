@@ -1,4 +1,5 @@
-// Maestro::MacProj, plane-parallel, one level (Source/MaestroMacProj.cpp:11-236).
+// Maestro::MacProj (Source/MaestroMacProj.cpp:11-246): one level, plane-parallel or spherical,
+// and two plane-parallel levels (the composite solve at the end of this file).
 //
 // umac enters holding Utilde^* and leaves with Utilde:
 //   B = beta0^2 / rho_face on the faces (average_cellcenter_to_face of rho, inverted, times
