@@ -317,6 +317,8 @@ def run_amr(args, ws, steps, warmup, barrier):
     st = make_amr_stage(cfg)
     if args.component_streams >= 0:
         st.set_option("component_streams", args.component_streams)
+    if args.es_inline >= 0:
+        st.set_option("es_inline", args.es_inline)
     bufs = amr_buffers(cfg)
     names = ("uold", "sold", "gpi")
     snap = [{n: [t.clone() for t in getattr(b, n).fabs] for n in names} for b in bufs]
@@ -944,6 +946,9 @@ def main():
     ap.add_argument("--component-streams", type=int, default=-1, choices=[-1, 0, 1],
                     help="headline and AMR stages: 1 MakeEdgeScal components alternate between two streams, "
                          "0 one stream, -1 the library default")
+    ap.add_argument("--es-inline", type=int, default=-1, choices=[-1, 0, 1],
+                    help="headline and AMR stages: 1 the edge kernels form the predictor's states from Ip / Im, "
+                         "0 the predictor stores them, -1 the library default")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     warmup = max(args.warmup, 3)
@@ -991,6 +996,8 @@ def main():
         st.set_option("staged_ppm", args.staged_ppm)
     if args.component_streams >= 0:
         st.set_option("component_streams", args.component_streams)
+    if args.es_inline >= 0:
+        st.set_option("es_inline", args.es_inline)
     buf = StageBuffers(cfg).load(cfg)
     snap = {name: [t.clone() for t in getattr(buf, name).fabs] for name in ("uold", "sold", "gpi")}
 

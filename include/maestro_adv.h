@@ -420,6 +420,10 @@ int madv_autotune_apply(madv_ctx* ctx, const char* json);
  *                     the per-component scratch (allocated at first use: about 46 doubles per
  *                     cell); 0 (default): one stream -- the stage is FP64-issue bound and
  *                     the overlap measures 0.5% on GB300.
+ *   "es_inline"       1 (default): with ppm_type 1 / 2, MakeEdgeScal's transverse and edge
+ *                     kernels take the predictor's left / right states straight from the
+ *                     traced Ip / Im, and only the upwind state is stored per face; 0: the
+ *                     predictor stores all three (as the reference's slx / srx / simhx).
  * Returns MADV_ERR_PARAM for an unknown key or a value outside 1..256. */
 int madv_set_option(madv_ctx* ctx, const char* key, int value);
 

@@ -191,6 +191,9 @@ struct Ctx {
     // side_mirror with those fields moved); built per stage call, used while dviews ==
     // side_mirror
     bool comp_streams = false;
+    // option "es_inline": MakeEdgeScal's edge kernels form the predictor's l / r from Ip / Im
+    // and only the upwind state is stored (ppm_type 1 / 2, outside the adjoint's tape)
+    bool es_inline = true;
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::map<int, double*> side_scratch;

@@ -46,12 +46,6 @@ __device__ __forceinline__ bool lt_negt(double x, long long tb) { return (dbits(
 // |x| > t, with tb = bits(t), t >= +0
 __device__ __forceinline__ bool abs_gt_t(double x, long long tb) { return (dbits(x) & ABS_MASK) > tb; }
 
-// Riemann upwinding of the reference:  v = (u > 0) ? l : r;  v = (|u| > t) ? v : (l+r)/2
-__device__ __forceinline__ double upwind(double u, double l, double r, long long tb) {
-    const long long ub = dbits(u);
-    if ((ub & ABS_MASK) > tb) return ub > 0 ? l : r;
-    return 0.5 * (l + r);
-}
 
 // 3. Scaling by 2 and by 1/2 on the bit pattern, equal to the FP multiply (round to nearest
 //    even) for every input: a normal result is an exponent step; a zero or subnormal x has
@@ -74,6 +68,14 @@ __device__ __forceinline__ double half(double x) {
     else if (a >= (2LL << 52)) r = b - (1LL << 52);               // normal result
     else r = sg | ((a >> 1) + (a & (a >> 1) & 1));                // subnormal result, ties to even
     return __longlong_as_double(r);
+}
+
+// Riemann upwinding of the reference:  v = (u > 0) ? l : r;  v = (|u| > t) ? v : (l+r)/2
+// (0.5 * x as half(x): the same bits, no FP64 multiply)
+__device__ __forceinline__ double upwind(double u, double l, double r, long long tb) {
+    const long long ub = dbits(u);
+    if ((ub & ABS_MASK) > tb) return ub > 0 ? l : r;
+    return half(l + r);
 }
 
 // 4. The sign of a product, x*y > 0, without the multiply: the operands are non-zero with

@@ -57,7 +57,7 @@ void add_fab(Ctx& c, int dst, int src, int nc, int ngrow) {
 __global__ void k_put1d(KARGS, int f, const double* __restrict__ s0, int outcomp, int edge) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const int r = k;
-    at(VW(f), i, j, k, outcomp) = edge ? 0.5 * (s0[r] + s0[r + 1]) : s0[r];
+    at(VW(f), i, j, k, outcomp) = edge ? half(s0[r] + s0[r + 1]) : s0[r];
 }
 
 void put1d(Ctx& c, int fid, const double* d_s0, int outcomp, int edge, int vec) {
@@ -129,11 +129,11 @@ __global__ void k_phys_fill(KARGS, int f, int c0, int nc, const BCRecD* __restri
             if (side == 0) {
                 if (m < domlo - 1) v = A(domlo, n);
                 else if (domlo + 2 <= domhi) v = 0.125 * (15. * A(domlo, n) - 10. * A(domlo + 1, n) + 3. * A(domlo + 2, n));
-                else v = 0.5 * (3. * A(domlo, n) - A(domlo + 1, n));
+                else v = half(3. * A(domlo, n) - A(domlo + 1, n));
             } else {
                 if (m > domhi + 1) v = A(domhi, n);
                 else if (domhi - 2 >= domlo) v = 0.125 * (15. * A(domhi, n) - 10. * A(domhi - 1, n) + 3. * A(domhi - 2, n));
-                else v = 0.5 * (3. * A(domhi, n) - A(domhi - 1, n));
+                else v = half(3. * A(domhi, n) - A(domhi - 1, n));
             }
         } else if (t == BC_REFLECT_EVEN) {
             v = A(side == 0 ? 2 * domlo - 1 - m : 2 * domhi + 1 - m, n);
@@ -336,7 +336,7 @@ __global__ void k_slope(KARGS, int fs, int sc, int fout, int oc, int ncomp, cons
         const bool hi_ext = (bchi == BC_EXT_DIR || bchi == BC_HOEXTRAP);
         double out = 0.0;
         if (slope_order == 2) {
-            double del = 0.5 * (S(1) - S(-1));
+            double del = half(S(1) - S(-1));
             double dpls = 2.0 * (S(1) - S(0));
             double dmin = 2.0 * (S(0) - S(-1));
             double slim = mn(fabs(dpls), fabs(dmin));
@@ -370,21 +370,21 @@ __global__ void k_slope(KARGS, int fs, int sc, int fout, int oc, int ncomp, cons
                 }
             }
         } else if (slope_order == 4) {
-            double dcen = 0.5 * (S(0) - S(-2));
+            double dcen = half(S(0) - S(-2));
             double dmin = 2.0 * (S(-1) - S(-2));
             double dpls = 2.0 * (S(0) - S(-1));
             double dlim = mn(fabs(dmin), fabs(dpls));
             dlim = dpls * dmin > 0.0 ? dlim : 0.0;
             double dflag = copysign(1.0, dcen);
             double dxl = dflag * mn(dlim, fabs(dcen));
-            dcen = 0.5 * (S(2) - S(0));
+            dcen = half(S(2) - S(0));
             dmin = 2.0 * (S(1) - S(0));
             dpls = 2.0 * (S(2) - S(1));
             dlim = mn(fabs(dmin), fabs(dpls));
             dlim = dpls * dmin > 0.0 ? dlim : 0.0;
             dflag = copysign(1.0, dcen);
             double dxr = dflag * mn(dlim, fabs(dcen));
-            dcen = 0.5 * (S(1) - S(-1));
+            dcen = half(S(1) - S(-1));
             dmin = 2.0 * (S(0) - S(-1));
             dpls = 2.0 * (S(1) - S(0));
             dlim = mn(fabs(dmin), fabs(dpls));
@@ -595,13 +595,13 @@ __global__ void k_utrans(KARGS, int ppm_type, double dt2dx, int bclo, int bchi, 
     double v;
     if (D < 2 && !sph) {
         const bool test = (l <= 0.0 && r >= 0.0) || (fabs(l + r) < rel_eps);
-        v = 0.5 * (l + r) > 0.0 ? l : r;
+        v = half(l + r) > 0.0 ? l : r;
         v = test ? 0.0 : v;
     } else {
         // planar z: the full velocity w + w0_cart; spherical (:368-377): + w0mac in every direction
         const double w0c = sph ? at(VW(F_W0MAC0 + D), i, j, k) : at(VW(F_W0CART), i, j, k, 2);
         const bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fabs(l + r + 2.0 * w0c) < rel_eps);
-        v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+        v = half(l + r) + w0c > 0.0 ? l : r;
         v = test ? 0.0 : v;
     }
     at(VW(F_UTRANS0 + D), i, j, k) = v;
@@ -734,7 +734,7 @@ __global__ void k_vp_interface(KARGS, int ppm_type, double dt2, double hd, int b
         at(L, i, j, k, n) = l[n];
         at(Rr, i, j, k, n) = r[n];
         if (n == D) continue;
-        at(M, i, j, k, n) = avg ? 0.5 * (l[n] + r[n]) : (left ? l[n] : r[n]);
+        at(M, i, j, k, n) = avg ? half(l[n] + r[n]) : (left ? l[n] : r[n]);
     }
 }
 
@@ -769,7 +769,7 @@ __global__ void k_vp_transverse(KARGS, int bclo, int bchi, int domlo, int domhi,
     }
     const double trd = at(VW(F_UTRANS0 + D), i, j, k);
     const bool avg = !((dbits(trd) & ABS_MASK) >= epsb);
-    at(VW(Q_FIELD(C, D)), i, j, k) = avg ? 0.5 * (lq + rq) : (gt0(trd) ? lq : rq);
+    at(VW(Q_FIELD(C, D)), i, j, k) = avg ? half(lq + rq) : (gt0(trd) ? lq : rq);
 }
 
 // VelPredVelocities (Source/MaestroVelPred.cpp:1597-1915).  F_TCOEF comps 3..5 hold
@@ -801,13 +801,13 @@ __global__ void k_vp_velocities(KARGS, double dt2, int bclo, int bchi, int domlo
     double v;
     if (D < 2 && !sph) {
         const bool test = (ml <= 0.0 && mr >= 0.0) || (fabs(ml + mr) < rel_eps);
-        v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+        v = half(ml + mr) > 0.0 ? ml : mr;
         v = test ? 0.0 : v;
     } else {
         // spherical (Source/MaestroVelPred.cpp:1664-1673): + w0mac in every direction
         const double w0c = sph ? at(VW(F_W0MAC0 + D), i, j, k) : at(VW(F_W0CART), i, j, k, 2);
         const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fabs(ml + mr + 2.0 * w0c) < rel_eps);
-        v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+        v = half(ml + mr) + w0c > 0.0 ? ml : mr;
         v = test ? 0.0 : v;
     }
     const FabView ut = VW(F_UTILDE);
@@ -896,6 +896,55 @@ __global__ void k_divu(KARGS, RecipC rdx0) {
     at(VW(F_DIVU), i, j, k) = div_c(d, rdx0);
 }
 
+// MakeEdgeScalPredictor's boundary rules (Source/MaestroMakeEdgeScalars.cpp:662-863) on the
+// D-face whose index along D is I: l and r replaced on the domain's low and high faces.
+// sc_l / sc_r: the state of the cell below / above the face (ext_dir takes the ghost value).
+__device__ __forceinline__ void es_pred_bc(int I, int bclo, int bchi, int domlo, int domhi, int vclamp, double sc_l,
+                                           double sc_r, double& l, double& r) {
+    if (I == domlo) {
+        if (bclo == BC_EXT_DIR) {
+            l = sc_l;
+            r = l;
+        } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
+            if (vclamp && bclo != BC_REFLECT_EVEN) r = mn(r, 0.0);  // is_vel, comp == D
+            l = r;
+        } else if (bclo == BC_REFLECT_ODD) {
+            l = 0.0;
+            r = 0.0;
+        }
+    } else if (I == domhi + 1) {
+        if (bchi == BC_EXT_DIR) {
+            l = sc_r;
+            r = l;
+        } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
+            if (vclamp && bchi != BC_REFLECT_EVEN) l = mx(l, 0.0);
+            r = l;
+        } else if (bchi == BC_REFLECT_ODD) {
+            l = 0.0;
+            r = 0.0;
+        }
+    }
+}
+
+// The predictor's states of the D-face (i,j,k) with ppm_type 1 / 2 as its consumers use them:
+// Ip of the cell below, Im of the cell above (F_IPC0 / F_IMC0 component D).  On a domain face
+// the consumers' own boundary rules (k_es_transverse, k_es_edges) overwrite both states for
+// ext_dir and reflect_odd, and the outside one (l below, r above) for foextrap, hoextrap and
+// reflect_even, so of the predictor's rules only the velocity clamp of the inside state is
+// left to apply here.  k_es_simh stores the upwind state with every rule.
+template <int D>
+__device__ __forceinline__ void es_pred_lr(const FabView& ip, const FabView& im, int bclo, int bchi, int domlo,
+                                           int domhi, int vclamp, int i, int j, int k, double& l, double& r) {
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    l = at(ip, i - di, j - dj, k - dk, D);
+    r = at(im, i, j, k, D);
+    if (vclamp) {
+        if (I == domlo && (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP)) r = mn(r, 0.0);
+        else if (I == domhi + 1 && (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP)) l = mx(l, 0.0);
+    }
+}
+
 // MakeEdgeScalPredictor, 3-D (Source/MaestroMakeEdgeScalars.cpp:662-863)
 template <int D>
 __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double hd, int bclo, int bchi, int domlo,
@@ -909,66 +958,70 @@ __global__ void k_es_predictor(KARGS, int comp, int ppm_type, double dt, double 
     double l, r;
     if (ppm_type == 0) {
         const FabView sl = VW(F_SLOPE);
-        l = at(sc, il, jl, kl, comp) + 0.5 * (1.0 - dt * ud / hd) * at(sl, il, jl, kl, D);
-        r = at(sc, i, j, k, comp) - 0.5 * (1.0 + dt * ud / hd) * at(sl, i, j, k, D);
+        l = at(sc, il, jl, kl, comp) + half(1.0 - dt * ud / hd) * at(sl, il, jl, kl, D);
+        r = at(sc, i, j, k, comp) - half(1.0 + dt * ud / hd) * at(sl, i, j, k, D);
     } else {
         l = at(VW(F_IPC0), il, jl, kl, D);
         r = at(VW(F_IMC0), i, j, k, D);
     }
-    if (I == domlo) {
-        if (bclo == BC_EXT_DIR) {
-            l = at(sc, il, jl, kl, comp);
-            r = l;
-        } else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) {
-            if (vclamp && bclo != BC_REFLECT_EVEN) r = mn(r, 0.0);  // is_vel, comp == D
-            l = r;
-        } else if (bclo == BC_REFLECT_ODD) {
-            l = 0.0;
-            r = 0.0;
-        }
-    } else if (I == domhi + 1) {
-        if (bchi == BC_EXT_DIR) {
-            l = at(sc, i, j, k, comp);
-            r = l;
-        } else if (bchi == BC_FOEXTRAP || bchi == BC_HOEXTRAP || bchi == BC_REFLECT_EVEN) {
-            if (vclamp && bchi != BC_REFLECT_EVEN) l = mx(l, 0.0);
-            r = l;
-        } else if (bchi == BC_REFLECT_ODD) {
-            l = 0.0;
-            r = 0.0;
-        }
-    }
+    if (I == domlo || I == domhi + 1)
+        es_pred_bc(I, bclo, bchi, domlo, domhi, vclamp, at(sc, il, jl, kl, comp), at(sc, i, j, k, comp), l, r);
     at(VW(F_SL0 + D), i, j, k) = l;
     at(VW(F_SR0 + D), i, j, k) = r;
     at(VW(F_SIMH0 + D), i, j, k) = upwind(ud, l, r, 0);  // tie test |u| > 0
 }
 
+// The predictor's upwind state alone (ppm_type 1 / 2): the transverse kernels read it at
+// neighbouring faces, while the edge states' l and r are formed where they are used.
+template <int D>
+__global__ void k_es_simh(KARGS, int comp, int bclo, int bchi, int domlo, int domhi, int vclamp) {
+    MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    const int I = D == 0 ? i : (D == 1 ? j : k);
+    double l = at(VW(F_IPC0), i - di, j - dj, k - dk, D), r = at(VW(F_IMC0), i, j, k, D);
+    if (I == domlo || I == domhi + 1) {
+        const FabView sc = VW(F_SOLD);
+        es_pred_bc(I, bclo, bchi, domlo, domhi, vclamp, at(sc, i - di, j - dj, k - dk, comp), at(sc, i, j, k, comp), l, r);
+    }
+    at(VW(F_SIMH0 + D), i, j, k) = upwind(at(VW(F_UMAC0 + D), i, j, k), l, r, 0);  // tie test |u| > 0
+}
+
 // MakeEdgeScalTransverse, 3-D (Source/MaestroMakeEdgeScalars.cpp:865-1359): D-faces
 // corrected in direction T.  Advective form: F_TCOEF comp T = (dt6/h_T)*(u_T sum).
-template <int D, int T, bool CONS>
-__global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bclo, int bchi, int domlo, int domhi,
+// INL (ppm_type 1 / 2): the D-face's predictor states l and r are formed here from F_IPC0 /
+// F_IMC0 instead of read from F_SL0 / F_SR0 (the same values: Ip, Im and the boundary rules).
+template <int D, int T, bool CONS, bool INL>
+__global__ void __launch_bounds__(TPB, CONS ? 4 : 6) k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bclo, int bchi, int domlo, int domhi,
                                 long long epsb, int vclamp) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     constexpr int ti = T == 0, tj = T == 1, tk = T == 2;
     const int I = D == 0 ? i : (D == 1 ? j : k);
     const int il = i - di, jl = j - dj, kl = k - dk;
-    const FabView st = VW(F_SIMH0 + T), sc = VW(F_SOLD);
+    const FabView st = VW(F_SIMH0 + T), sc = VW(F_SOLD), ut = VW(F_UMAC0 + T);
+    auto simh = [&](int a, int bb, int cc) -> double { return at(st, a, bb, cc); };
+    double sl, sr;
+    if (INL) {
+        es_pred_lr<D>(VW(F_IPC0), VW(F_IMC0), bclo, bchi, domlo, domhi, vclamp, i, j, k, sl, sr);
+    } else {
+        sl = at(VW(F_SL0 + D), i, j, k);
+        sr = at(VW(F_SR0 + D), i, j, k);
+    }
     double lq, rq;
     if (CONS) {
-        const FabView ut = VW(F_UMAC0 + T), dv = VW(F_DIVU);
-        lq = at(VW(F_SL0 + D), i, j, k) -
-             dt3h * (at(st, il + ti, jl + tj, kl + tk) * at(ut, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl) * at(ut, il, jl, kl)) -
+        const FabView dv = VW(F_DIVU);
+        lq = sl -
+             dt3h * (simh(il + ti, jl + tj, kl + tk) * at(ut, il + ti, jl + tj, kl + tk) - simh(il, jl, kl) * at(ut, il, jl, kl)) -
              dt3 * at(sc, il, jl, kl, comp) * at(dv, il, jl, kl) +
              dt3h * at(sc, il, jl, kl, comp) * (at(ut, il + ti, jl + tj, kl + tk) - at(ut, il, jl, kl));
-        rq = at(VW(F_SR0 + D), i, j, k) -
-             dt3h * (at(st, i + ti, j + tj, k + tk) * at(ut, i + ti, j + tj, k + tk) - at(st, i, j, k) * at(ut, i, j, k)) -
+        rq = sr -
+             dt3h * (simh(i + ti, j + tj, k + tk) * at(ut, i + ti, j + tj, k + tk) - simh(i, j, k) * at(ut, i, j, k)) -
              dt3 * at(sc, i, j, k, comp) * at(dv, i, j, k) +
              dt3h * at(sc, i, j, k, comp) * (at(ut, i + ti, j + tj, k + tk) - at(ut, i, j, k));
     } else {
         const FabView tc = VW(F_TCOEF);
-        lq = at(VW(F_SL0 + D), i, j, k) - at(tc, il, jl, kl, T) * (at(st, il + ti, jl + tj, kl + tk) - at(st, il, jl, kl));
-        rq = at(VW(F_SR0 + D), i, j, k) - at(tc, i, j, k, T) * (at(st, i + ti, j + tj, k + tk) - at(st, i, j, k));
+        lq = sl - at(tc, il, jl, kl, T) * (simh(il + ti, jl + tj, kl + tk) - simh(il, jl, kl));
+        rq = sr - at(tc, i, j, k, T) * (simh(i + ti, j + tj, k + tk) - simh(i, j, k));
     }
     if (I == domlo) {
         if (bclo == BC_EXT_DIR) {
@@ -999,7 +1052,8 @@ __global__ void k_es_transverse(KARGS, int comp, double dt3, double dt3h, int bc
 // MakeEdgeScalEdges, 3-D (Source/MaestroMakeEdgeScalars.cpp:1361-1667).  Advective form:
 // F_TCOEF comp 3+t = (dt4/h_t)*(u_t sum).  force_zero: the component's force is
 // identically zero (species), so the + dt/2*force term is skipped.
-template <int D, bool CONS>
+// INL: the D-face's predictor states formed from F_IPC0 / F_IMC0 (as in k_es_transverse).
+template <int D, bool CONS, bool INL>
 __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double dt2h1, double dt2h2, double dt2hd,
                            int bclo, int bchi, int domlo, int domhi, long long epsb, int vclamp, int ptf, int oc) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
@@ -1012,6 +1066,13 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
     const FabView q1 = VW(Q_FIELD(T1, T2)), q2 = VW(Q_FIELD(T2, T1));
     const FabView udf = VW(F_UMAC0 + D);
     const FabView sc = VW(F_SOLD);
+    double sl, sr;
+    if (INL) {
+        es_pred_lr<D>(VW(F_IPC0), VW(F_IMC0), bclo, bchi, domlo, domhi, vclamp, i, j, k, sl, sr);
+    } else {
+        sl = at(VW(F_SL0 + D), i, j, k);
+        sr = at(VW(F_SR0 + D), i, j, k);
+    }
     double lq, rq;
     if (CONS) {
         // the traced force if ppm_trace_forces = 1 (Source/MaestroMakeEdgeScalars.cpp:1405-1408)
@@ -1019,20 +1080,20 @@ __global__ void k_es_edges(KARGS, int comp, int force_zero, double dt2, double d
         // force_zero: the force is zero (and so is its trace, which is not formed)
         const double fl = force_zero ? 0.0 : ptf ? at(VW(F_IPF), il, jl, kl, D) : at(f, il, jl, kl, comp);
         const double fr = force_zero ? 0.0 : ptf ? at(VW(F_IMF), i, j, k, D) : at(f, i, j, k, comp);
-        lq = at(VW(F_SL0 + D), i, j, k) -
+        lq = sl -
              dt2h1 * (at(q1, il + a1i, jl + a1j, kl + a1k) * at(u1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl) * at(u1, il, jl, kl)) -
              dt2h2 * (at(q2, il + a2i, jl + a2j, kl + a2k) * at(u2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl) * at(u2, il, jl, kl)) -
              dt2hd * at(sc, il, jl, kl, comp) * (at(udf, i, j, k) - at(udf, il, jl, kl)) + dt2 * fl;
-        rq = at(VW(F_SR0 + D), i, j, k) -
+        rq = sr -
              dt2h1 * (at(q1, i + a1i, j + a1j, k + a1k) * at(u1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k) * at(u1, i, j, k)) -
              dt2h2 * (at(q2, i + a2i, j + a2j, k + a2k) * at(u2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k) * at(u2, i, j, k)) -
              dt2hd * at(sc, i, j, k, comp) * (at(udf, i + di, j + dj, k + dk) - at(udf, i, j, k)) + dt2 * fr;
     } else {
         const FabView tc = VW(F_TCOEF);
-        lq = at(VW(F_SL0 + D), i, j, k) -
+        lq = sl -
              at(tc, il, jl, kl, 3 + T1) * (at(q1, il + a1i, jl + a1j, kl + a1k) - at(q1, il, jl, kl)) -
              at(tc, il, jl, kl, 3 + T2) * (at(q2, il + a2i, jl + a2j, kl + a2k) - at(q2, il, jl, kl));
-        rq = at(VW(F_SR0 + D), i, j, k) -
+        rq = sr -
              at(tc, i, j, k, 3 + T1) * (at(q1, i + a1i, j + a1j, k + a1k) - at(q1, i, j, k)) -
              at(tc, i, j, k, 3 + T2) * (at(q2, i + a2i, j + a2j, k + a2k) - at(q2, i, j, k));
         if (!force_zero) {
@@ -1067,36 +1128,59 @@ static void es_predictor_launch(Ctx& c, int comp, const BCRecD& bc, int vclamp) 
            c.P.dom_lo[D], c.P.dom_hi[D], vclamp);
 }
 
+template <int D>
+static void es_simh_launch(Ctx& c, int comp, const BCRecD& bc, int vclamp) {
+    int glo[3] = {1, 1, 1};
+    glo[D] = 0;
+    const RegionTable& rt = region(c, glo[0], glo[1], glo[2], 1, 1, 1, -1);
+    launch(c, rt, 1, k_es_simh<D>, c.V(), comp, bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D], vclamp);
+}
+
+template <int D, int T, bool INL>
+static void es_transverse_launch_t(Ctx& c, const RegionTable& rt, int comp, const BCRecD& bc, int is_cons,
+                                   int vclamp) {
+    const double dt3 = c.P.dt / 3.0;
+    if (is_cons)
+        launch(c, rt, 1, k_es_transverse<D, T, true, INL>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
+               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps), vclamp);
+    else
+        launch(c, rt, 1, k_es_transverse<D, T, false, INL>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
+               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps), vclamp);
+}
+
+// inl: the D-face's predictor states formed in the kernel
 template <int D, int T>
-static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int vclamp) {
+static void es_transverse_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int vclamp, bool inl) {
     constexpr int O = 3 - D - T;
     int glo[3] = {0, 0, 0}, ghi[3] = {0, 0, 0};
     glo[O] = 1;
     ghi[O] = 1;
     ghi[D] = 1;
     const RegionTable& rt = region(c, glo[0], glo[1], glo[2], ghi[0], ghi[1], ghi[2], -1);
-    const double dt3 = c.P.dt / 3.0;
-    if (is_cons)
-        launch(c, rt, 1, k_es_transverse<D, T, true>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
-               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps), vclamp);
-    else
-        launch(c, rt, 1, k_es_transverse<D, T, false>, c.V(), comp, dt3, dt3 / c.P.dx[T], bc.lo[D], bc.hi[D],
-               c.P.dom_lo[D], c.P.dom_hi[D], dbits_host(c.P.rel_eps), vclamp);
+    if (inl) es_transverse_launch_t<D, T, true>(c, rt, comp, bc, is_cons, vclamp);
+    else es_transverse_launch_t<D, T, false>(c, rt, comp, bc, is_cons, vclamp);
 }
 
-template <int D>
-static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp, int oc) {
+template <int D, bool INL>
+static void es_edges_launch_t(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp, int oc) {
     constexpr int T1 = D == 0 ? 1 : 0, T2 = D == 2 ? 1 : 2;
     const double dt2 = 0.5 * c.P.dt;
     const int ptf = c.P.ppm_trace_forces;
     if (is_cons)
-        launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, true>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
+        launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, true, INL>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
                dbits_host(c.P.rel_eps), vclamp, ptf, oc);
     else
-        launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, false>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
+        launch(c, rg_grow(c, 0, D), 1, k_es_edges<D, false, INL>, c.V(), comp, force_zero, dt2, dt2 / c.P.dx[T1],
                dt2 / c.P.dx[T2], dt2 / c.P.dx[D], bc.lo[D], bc.hi[D], c.P.dom_lo[D], c.P.dom_hi[D],
                dbits_host(c.P.rel_eps), vclamp, ptf, oc);
+}
+
+template <int D>
+static void es_edges_launch(Ctx& c, int comp, const BCRecD& bc, int is_cons, int force_zero, int vclamp, int oc,
+                            bool inl) {
+    if (inl) es_edges_launch_t<D, true>(c, comp, bc, is_cons, force_zero, vclamp, oc);
+    else es_edges_launch_t<D, false>(c, comp, bc, is_cons, force_zero, vclamp, oc);
 }
 
 // velocity-only quantities shared by every component of a MakeEdgeScal call
@@ -1140,19 +1224,29 @@ void make_edge_scal(Ctx& c, int start_comp, int num_comp, int which_bcs, int is_
                 for (int d = 0; d < 3; ++d) ppm_any(c, d, F_SCALFORCE, comp, bc, F_UMAC0 + d, 0, 1, F_IPF, F_IMF);
         }
         const int v0 = is_vel && comp == 0, v1 = is_vel && comp == 1, v2 = is_vel && comp == 2;
-        es_predictor_launch<0>(c, comp, bc, v0);
-        es_predictor_launch<1>(c, comp, bc, v1);
-        es_predictor_launch<2>(c, comp, bc, v2);
-        es_transverse_launch<0, 1>(c, comp, bc, is_cons, v0);
-        es_transverse_launch<0, 2>(c, comp, bc, is_cons, v0);
-        es_transverse_launch<1, 0>(c, comp, bc, is_cons, v1);
-        es_transverse_launch<1, 2>(c, comp, bc, is_cons, v1);
-        es_transverse_launch<2, 0>(c, comp, bc, is_cons, v2);
-        es_transverse_launch<2, 1>(c, comp, bc, is_cons, v2);
+        // with PPM the predictor's l and r are Ip / Im passed on: the transverse and edge
+        // kernels form them themselves and only the upwind state is stored (the full
+        // predictor runs where the adjoint's tape keeps its fields)
+        const bool inl = c.es_inline && c.P.ppm_type != 0 && !c.edge_tape_begin;
+        if (inl) {
+            es_simh_launch<0>(c, comp, bc, v0);
+            es_simh_launch<1>(c, comp, bc, v1);
+            es_simh_launch<2>(c, comp, bc, v2);
+        } else {
+            es_predictor_launch<0>(c, comp, bc, v0);
+            es_predictor_launch<1>(c, comp, bc, v1);
+            es_predictor_launch<2>(c, comp, bc, v2);
+        }
+        es_transverse_launch<0, 1>(c, comp, bc, is_cons, v0, inl);
+        es_transverse_launch<0, 2>(c, comp, bc, is_cons, v0, inl);
+        es_transverse_launch<1, 0>(c, comp, bc, is_cons, v1, inl);
+        es_transverse_launch<1, 2>(c, comp, bc, is_cons, v1, inl);
+        es_transverse_launch<2, 0>(c, comp, bc, is_cons, v2, inl);
+        es_transverse_launch<2, 1>(c, comp, bc, is_cons, v2, inl);
         const int oc = slot >= 0 ? slot : comp;
-        es_edges_launch<0>(c, comp, bc, is_cons, force_zero, v0, oc);
-        es_edges_launch<1>(c, comp, bc, is_cons, force_zero, v1, oc);
-        es_edges_launch<2>(c, comp, bc, is_cons, force_zero, v2, oc);
+        es_edges_launch<0>(c, comp, bc, is_cons, force_zero, v0, oc, inl);
+        es_edges_launch<1>(c, comp, bc, is_cons, force_zero, v1, oc, inl);
+        es_edges_launch<2>(c, comp, bc, is_cons, force_zero, v2, oc, inl);
         if (c.edge_tape) c.edge_tape(comp);
     }
     c.stream = main_stream;
@@ -1206,7 +1300,7 @@ __global__ void k_rhoh_force(KARGS, int cutoff, int domhi, RecipC rdz, int psi_i
         gradp0 = div_c(at(p0c, i, j + 1, k) - at(p0c, i, j, k), rdz);
     }
     const FabView wm = VW(F_UMAC2);
-    const double veladv = 0.5 * (at(wm, i, j, k) + at(wm, i, j, k + 1));
+    const double veladv = half(at(wm, i, j, k) + at(wm, i, j, k + 1));
     double f = veladv * gradp0;
     if (psi_in) f += at(VW(F_PSICART), i, j, k);
     if (add_thermal == 1) f += at(VW(F_THERMAL), i, j, k);
@@ -1269,7 +1363,7 @@ __global__ void k_rhox_flux(KARGS, int c0, int nc, int nspec, int slot, int spt,
     double eta = D == 2 && do_eta ? at(VW(F_ETA), i, j, k) : 0.0;
     for (int comp = c0; comp < c0 + nc; ++comp) {
         const int ec = slot >= 0 ? slot : comp;
-        const double rho0_edge = 0.5 * (r0o[k] + r0n[k]);
+        const double rho0_edge = half(r0o[k] + r0n[k]);
         double f = 0.0;
         if (spt == 1) f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, ec);
         else if (spt == 2) f = u * at(e, i, j, k, ec);
@@ -1313,13 +1407,13 @@ __global__ void k_rhoh_flux(KARGS, int ept, const double* __restrict__ a, const 
         f = u * at(e, i, j, k, RHOH);
     } else if (ept == 2) {
         if (spt == 1) {
-            const double rho0_edge = 0.5 * (ra[k] + rb[k]);
+            const double rho0_edge = half(ra[k] + rb[k]);
             f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, RHOH);
         } else {
             f = u * at(e, i, j, k, RHO) * at(e, i, j, k, RHOH);
         }
     } else {
-        const double rhoh0_edge = 0.5 * (a[k] + bb[k]);
+        const double rhoh0_edge = half(a[k] + bb[k]);
         f = D < 2 ? u * (rhoh0_edge + at(e, i, j, k, RHOH)) : u * (at(e, i, j, k, RHOH) + rhoh0_edge);
     }
     at(VW(F_SFLUX0 + D), i, j, k, RHOH) = f;
@@ -1475,9 +1569,9 @@ __global__ void k_update_vel(KARGS, int fu, int fsp, int sph, double dt, RecipC 
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     const FabView uo = VW(fu), un = VW(F_SNEW), um = VW(F_UMAC0), vm = VW(F_UMAC1), wm = VW(F_UMAC2);
     const FabView ex = VW(F_SEDGE0), ey = VW(F_SEDGE1), ez = VW(F_SEDGE2), f = VW(F_VELFORCE);
-    const double ubar = 0.5 * (at(um, i, j, k) + at(um, i + 1, j, k));
-    const double vbar = 0.5 * (at(vm, i, j, k) + at(vm, i, j + 1, k));
-    const double wbar = 0.5 * (at(wm, i, j, k) + at(wm, i, j, k + 1));
+    const double ubar = half(at(um, i, j, k) + at(um, i + 1, j, k));
+    const double vbar = half(at(vm, i, j, k) + at(vm, i, j + 1, k));
+    const double wbar = half(at(wm, i, j, k) + at(wm, i, j, k + 1));
     double v[3];
     for (int n = 0; n < 3; ++n) {
         const double ugrad = div_c(ubar * (at(ex, i + 1, j, k, n) - at(ex, i, j, k, n)), r0) +
@@ -1487,7 +1581,7 @@ __global__ void k_update_vel(KARGS, int fu, int fsp, int sph, double dt, RecipC 
     }
     if (!sph) {
         const FabView w0c = VW(F_W0CART);
-        const double w0bar = 0.5 * (at(w0c, i, j, k, 2) + at(w0c, i, j, k + 1, 2));
+        const double w0bar = half(at(w0c, i, j, k, 2) + at(w0c, i, j, k + 1, 2));
         for (int n = 0; n < 3; ++n) {
             v[n] -= div_c(dt * w0bar * (at(ez, i, j, k + 1, n) - at(ez, i, j, k, n)), r2);
             if (fsp >= 0) v[n] *= at(VW(fsp), i, j, k);
@@ -1534,10 +1628,10 @@ __global__ void k_dt_maxima(KARGS, int sph, int nd, int w0m, unsigned long long*
         const FabView u = VW(F_UTILDE), w0c = VW(F_W0CART), f = VW(F_VELFORCE);
         for (int d = 0; d < nd; ++d) {
             double v = at(u, i, j, k, d);
-            if (!sph && d == nd - 1) v = v + 0.5 * (at(w0c, i, j, k, d) + at(w0c, i, j + (d == 1), k + (d == 2), d));
+            if (!sph && d == nd - 1) v = v + half(at(w0c, i, j, k, d) + at(w0c, i, j + (d == 1), k + (d == 2), d));
             if (sph && w0m) {
                 const FabView wm = VW(F_W0MAC0 + d);
-                v = v + 0.5 * (at(wm, i, j, k) + at(wm, i + (d == 0), j + (d == 1), k + (d == 2)));
+                v = v + half(at(wm, i, j, k) + at(wm, i + (d == 0), j + (d == 1), k + (d == 2)));
             } else if (sph) {
                 v = v + 0.5 * (0.0 + 0.0);
             }
@@ -1600,7 +1694,7 @@ static const RegionTable& rg2(Ctx& c, int g, int nodal = -1) { return region(c, 
 // Put1dArrayOnCart, planar 2-D (Source/MaestroFill3dData.cpp:79-93): r = j
 __global__ void k_put1d_2d(KARGS, int f, const double* __restrict__ s0, int outcomp, int edge) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
-    at(VW(f), i, j, k, outcomp) = edge ? 0.5 * (s0[j] + s0[j + 1]) : s0[j];
+    at(VW(f), i, j, k, outcomp) = edge ? half(s0[j] + s0[j + 1]) : s0[j];
 }
 
 // Addw0, planar 2-D (Source/MaestroFill3dData.cpp:380-386): vedge += mult * w0(j)
@@ -1641,7 +1735,7 @@ __global__ void k_utrans_2dy(KARGS, int ppm_type, double dt2dy, int bclo, int bc
     }
     const double w0c = at(VW(F_W0CART), i, j, k, 1);
     const bool test = (l + w0c <= 0.0 && r + w0c >= 0.0) || (fabs(l + r + 2.0 * w0c) < rel_eps);
-    double v = 0.5 * (l + r) + w0c > 0.0 ? l : r;
+    double v = half(l + r) + w0c > 0.0 ? l : r;
     at(VW(F_UTRANS1), i, j, k) = test ? 0.0 : v;
 }
 
@@ -1765,7 +1859,7 @@ __global__ void k_vp_interface_2d(KARGS, int ppm_type, double dt2h, int bclo, in
     }
     const double tr = at(VW(F_UTRANS0 + D), i, j, k);
     const double v = tr > 0.0 ? L[T] : Rr[T];
-    at(VW(F_SIMH0 + D), i, j, k, T) = fabs(tr) < rel_eps ? 0.5 * (L[T] + Rr[T]) : v;
+    at(VW(F_SIMH0 + D), i, j, k, T) = fabs(tr) < rel_eps ? half(L[T] + Rr[T]) : v;
 }
 
 // VelPredVelocities, 2-D (Source/MaestroVelPred.cpp:539-727)
@@ -1790,12 +1884,12 @@ __global__ void k_vp_velocities_2d(KARGS, double dt2, double dt4h, int bclo, int
                       dt2 * fr;
     double v;
     if (D == 0) {
-        v = 0.5 * (ml + mr) > 0.0 ? ml : mr;
+        v = half(ml + mr) > 0.0 ? ml : mr;
         v = (ml <= 0.0 && mr >= 0.0) || (fabs(ml + mr) < rel_eps) ? 0.0 : v;
     } else {
         const double w0c = at(VW(F_W0CART), i, j, k, 1);
         const bool test = (ml + w0c <= 0.0 && mr + w0c >= 0.0) || (fabs(ml + mr + 2.0 * w0c) < rel_eps);
-        v = 0.5 * (ml + mr) + w0c > 0.0 ? ml : mr;
+        v = half(ml + mr) + w0c > 0.0 ? ml : mr;
         v = test ? 0.0 : v;
     }
     const FabView ut = VW(F_UTILDE);
@@ -1881,7 +1975,7 @@ __global__ void k_es_predictor_2d(KARGS, int comp, int ppm_type, double dt2, dou
     at(VW(F_SL0 + D), i, j, k) = l;
     at(VW(F_SR0 + D), i, j, k) = r;
     double sm = (u > 0.0) ? l : r;
-    at(VW(F_SIMH0 + D), i, j, k) = (fabs(u) > rel_eps) ? sm : 0.5 * (l + r);
+    at(VW(F_SIMH0 + D), i, j, k) = (fabs(u) > rel_eps) ? sm : half(l + r);
 }
 
 // MakeEdgeScalEdges, 2-D (Source/MaestroMakeEdgeScalars.cpp:454-644)
@@ -1913,7 +2007,7 @@ __global__ void k_es_edges_2d(KARGS, int comp, int is_cons, double dt2, double d
     }
     const double u = at(ud, i, j, k);
     double v = (u > 0.0) ? lq : rq;
-    v = (fabs(u) > rel_eps) ? v : 0.5 * (lq + rq);
+    v = (fabs(u) > rel_eps) ? v : half(lq + rq);
     if (I == domlo) {
         if (bclo == BC_EXT_DIR) v = at(s, il, jl, k, comp);
         else if (bclo == BC_FOEXTRAP || bclo == BC_HOEXTRAP || bclo == BC_REFLECT_EVEN) v = rq;
@@ -1989,7 +2083,7 @@ __global__ void k_rhoh_force_2d(KARGS, int cutoff, int domhi, double dy, int psi
     else if (j == domhi) gradp0 = (at(p0c, i, j, k) - at(p0c, i, j - 1, k)) / dy;
     else gradp0 = (at(p0c, i, j + 1, k) - at(p0c, i, j, k)) / dy;
     const FabView vm = VW(F_UMAC1);
-    const double veladv = 0.5 * (at(vm, i, j, k) + at(vm, i, j + 1, k));
+    const double veladv = half(at(vm, i, j, k) + at(vm, i, j + 1, k));
     double f = veladv * gradp0;
     if (psi_in) f += at(VW(F_PSICART), i, j, k);
     if (add_thermal == 1) f += at(VW(F_THERMAL), i, j, k);
@@ -2013,7 +2107,7 @@ __global__ void k_rhox_flux_2d(KARGS, int nspec, int spt, int do_eta, const doub
     const double u = at(VW(F_UMAC0 + D), i, j, k);
     double frho = 0.0, eta = D == 1 && do_eta ? at(VW(F_ETA), i, j, k) : 0.0;
     for (int comp = FIRSTSPEC; comp < FIRSTSPEC + nspec; ++comp) {
-        const double rho0_edge = 0.5 * (r0o[j] + r0n[j]);
+        const double rho0_edge = half(r0o[j] + r0n[j]);
         double f;
         if (spt == 1) f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, comp);
         else if (spt == 2) f = u * at(e, i, j, k, comp);
@@ -2041,13 +2135,13 @@ __global__ void k_rhoh_flux_2d(KARGS, int ept, const double* __restrict__ a, con
         f = u * at(e, i, j, k, RHOH);
     } else if (ept == 2) {  // the edge state is h (Source/MaestroMakeFlux.cpp:597-662, have_h)
         if (spt == 1) {
-            const double rho0_edge = 0.5 * (ra[j] + rb[j]);
+            const double rho0_edge = half(ra[j] + rb[j]);
             f = u * (rho0_edge + at(e, i, j, k, RHO)) * at(e, i, j, k, RHOH);
         } else {
             f = u * at(e, i, j, k, RHO) * at(e, i, j, k, RHOH);
         }
     } else {
-        const double rhoh0_edge = 0.5 * (a[j] + bb[j]);
+        const double rhoh0_edge = half(a[j] + bb[j]);
         f = D == 0 ? u * (rhoh0_edge + at(e, i, j, k, RHOH)) : u * (at(e, i, j, k, RHOH) + rhoh0_edge);
     }
     at(VW(F_SFLUX0 + D), i, j, k, RHOH) = f;

@@ -45,7 +45,7 @@ __device__ __forceinline__ double ppm2_face_regular(const FabView& s, int sc, in
         double D2R = S(m - 1) - 2.0 * S(m) + S(m + 1);
         double sgn = copysign(1.0, D2);
         double D2LIM = sgn * mx(mn(C * sgn * D2L, mn(C * sgn * D2R, sgn * D2)), 0.0);
-        se = 0.5 * (S(m - 1) + S(m)) - div_c(D2LIM, r6);
+        se = half(S(m - 1) + S(m)) - div_c(D2LIM, r6);
     }
     return se;
 }
@@ -115,7 +115,7 @@ __device__ __forceinline__ void ppm_cell_edges(const FabView& s, int sc, const F
             if (PPMT == 2) return ppm2_face_regular<D>(s, sc, i, j, k, m, r6);
             const double dvl = at(dv, i + (m - 1) * di, j + (m - 1) * dj, k + (m - 1) * dk);
             const double dvr = at(dv, i + m * di, j + m * dj, k + m * dk);
-            double v = 0.5 * (S(m) + S(m - 1)) - div_c(dvr - dvl, r6);
+            double v = half(S(m) + S(m - 1)) - div_c(dvr - dvl, r6);
             v = mx(v, mn(S(m), S(m - 1)));
             return mn(v, mx(S(m), S(m - 1)));
         }

@@ -7,6 +7,7 @@
 // MakeUtrans / VelPred Riemann solves with w0mac are flags of their kernels in
 // madv_kernels.cu.  Divisions by dx and radii are IEEE divisions, as the reference writes
 // them; `sqrt` is the correctly rounded square root.
+#include "madv_exact.cuh"
 #include "madv_launch.cuh"
 
 namespace madv {
@@ -135,7 +136,7 @@ __global__ void k_face_avg(KARGS, int src, int sc, int dst) {
     MADV_ELEMENT(R, ne, g0, g1, b, i, j, k);
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
     const FabView s = VW(src);
-    at(VW(dst), i, j, k) = 0.5 * (at(s, i - di, j - dj, k - dk, sc) + at(s, i, j, k, sc));
+    at(VW(dst), i, j, k) = half(at(s, i - di, j - dj, k - dk, sc) + at(s, i, j, k, sc));
 }
 
 static void face_avg(Ctx& c, int src, int comp_is_dir, int dst0) {
@@ -283,9 +284,9 @@ __global__ void k_vel_force_sph(KARGS, double cutoff_rho, SphGeo g, int fe) {
     for (int dim = 0; dim < 3; ++dim)
         at(vf, i, j, k, dim) = (rhopert * at(grav, i, j, k, dim) - at(gpi, i, j, k, dim)) / r - at(w0f, i, j, k, dim);
     const FabView ue = VW(fe), ve = VW(fe + 1), we = VW(fe + 2);
-    const double ut_dot_er = 0.5 * (at(ue, i, j, k) + at(ue, i + 1, j, k)) * nrm[0] +
-                             0.5 * (at(ve, i, j, k) + at(ve, i, j + 1, k)) * nrm[1] +
-                             0.5 * (at(we, i, j, k) + at(we, i, j, k + 1)) * nrm[2];
+    const double ut_dot_er = half(at(ue, i, j, k) + at(ue, i + 1, j, k)) * nrm[0] +
+                             half(at(ve, i, j, k) + at(ve, i, j + 1, k)) * nrm[1] +
+                             half(at(we, i, j, k) + at(we, i, j, k + 1)) * nrm[2];
     for (int dim = 0; dim < 3; ++dim) at(vf, i, j, k, dim) -= ut_dot_er * gradw0 * nrm[dim];
 }
 
@@ -310,12 +311,12 @@ __global__ void k_modify_scal_force_sph(KARGS, int comp, int s0cart, int fullfor
         force -= scal * (divumac + divu_c);
     } else {
         const double s = at(s0a, i, j, k);
-        const double sxh = i < hi0 ? 0.5 * (s + at(s0a, i + 1, j, k)) : s;
-        const double sxl = i > lo0 ? 0.5 * (s + at(s0a, i - 1, j, k)) : s;
-        const double syh = j < hi1 ? 0.5 * (s + at(s0a, i, j + 1, k)) : s;
-        const double syl = j > lo1 ? 0.5 * (s + at(s0a, i, j - 1, k)) : s;
-        const double szh = k < hi2 ? 0.5 * (s + at(s0a, i, j, k + 1)) : s;
-        const double szl = k > lo2 ? 0.5 * (s + at(s0a, i, j, k - 1)) : s;
+        const double sxh = i < hi0 ? half(s + at(s0a, i + 1, j, k)) : s;
+        const double sxl = i > lo0 ? half(s + at(s0a, i - 1, j, k)) : s;
+        const double syh = j < hi1 ? half(s + at(s0a, i, j + 1, k)) : s;
+        const double syl = j > lo1 ? half(s + at(s0a, i, j - 1, k)) : s;
+        const double szh = k < hi2 ? half(s + at(s0a, i, j, k + 1)) : s;
+        const double szl = k > lo2 ? half(s + at(s0a, i, j, k - 1)) : s;
         const double divs0u = (at(um, i + 1, j, k) * sxh - at(um, i, j, k) * sxl) / dx0 +
                               (at(vm, i, j + 1, k) * syh - at(vm, i, j, k) * syl) / dx1 +
                               (at(wm, i, j, k + 1) * szh - at(wm, i, j, k) * szl) / dx2;
