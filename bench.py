@@ -35,21 +35,21 @@ HBM_PEAK_FALLBACK = 6792.7
 #   fp64: FP64 warp instructions (smsp__inst_executed_pipe_fp64.sum) per valid cell, one launch
 #   dram: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per valid cell, one launch
 KERNEL_WORK = {
-    "k_ppm_cell<0,1,1>": {"fp64": 0.6581, "dram": 50.5},
-    "k_ppm_cell<1,1,1>": {"fp64": 0.6467, "dram": 50.6},
-    "k_ppm_cell<2,1,1>": {"fp64": 0.6483, "dram": 52.5},
-    "k_ppm_cell<0,1,0>": {"fp64": 0.7031, "dram": 50.7},
-    "k_ppm_cell<1,1,0>": {"fp64": 0.6740, "dram": 51.1},
-    "k_ppm_cell<2,1,0>": {"fp64": 0.6500, "dram": 51.3},
-    "k_update_rhox": {"fp64": 9.0, "dram": 674.7},
-    "k_ppm_face<0,1>": {"fp64": 0.4189, "dram": None},
-    "k_ppm_face<1,1>": {"fp64": 0.4188, "dram": None},
-    "k_ppm_face<2,1>": {"fp64": 0.4286, "dram": None},
-    "k_es_edges<0,0>": {"fp64": 0.4613, "dram": None},
-    "k_es_edges<1,0>": {"fp64": 0.4613, "dram": None},
-    "k_es_edges<2,0>": {"fp64": 0.4613, "dram": None},
+    "k_ppm_cell<0,1,1>": {"fp64": 0.6582, "dram": 50.7},
+    "k_ppm_cell<1,1,1>": {"fp64": 0.6467, "dram": 51.3},
+    "k_ppm_cell<2,1,1>": {"fp64": 0.6482, "dram": 51.9},
+    "k_ppm_cell<0,1,0>": {"fp64": 0.7034, "dram": 50.4},
+    "k_ppm_cell<1,1,0>": {"fp64": 0.6736, "dram": 50.8},
+    "k_ppm_cell<2,1,0>": {"fp64": 0.6502, "dram": 50.9},
+    "k_update_rhox": {"fp64": 9.0, "dram": 675.0},
+    "k_ppm_face<0,1>": {"fp64": 0.4189, "dram": 18.4},
+    "k_ppm_face<1,1>": {"fp64": 0.4188, "dram": 19.0},
+    "k_ppm_face<2,1>": {"fp64": 0.4287, "dram": 19.0},
+    "k_es_edges<0,0,1>": {"fp64": 0.4433, "dram": 62.4},
+    "k_es_edges<1,0,1>": {"fp64": 0.4191, "dram": 63.7},
+    "k_es_edges<2,0,1>": {"fp64": 0.3989, "dram": 64.0},
 }
-STAGE_FP64_PER_CELL = 157.04  # FP64 warp instructions per valid cell, whole stage
+STAGE_FP64_PER_CELL = 146.50  # FP64 warp instructions per valid cell, whole stage
 
 
 def jsonable(o):
