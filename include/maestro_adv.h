@@ -424,6 +424,11 @@ int madv_autotune_apply(madv_ctx* ctx, const char* json);
  *                     kernels take the predictor's left / right states straight from the
  *                     traced Ip / Im, and only the upwind state is stored per face; 0: the
  *                     predictor stores all three (as the reference's slx / srx / simhx).
+ *   "mg_block_cycle"  1 (default): the MAC projection's multigrid V-cycle, from its first
+ *                     grid of at most 4096 cells down to the coarsest, runs in one thread
+ *                     block with the same per-cell arithmetic (bitwise the same result);
+ *                     0: one launch per smoothing sweep, residual, restriction and
+ *                     prolongation on those grids too.
  * Returns MADV_ERR_PARAM for an unknown key or a value outside 1..256. */
 int madv_set_option(madv_ctx* ctx, const char* key, int value);
 

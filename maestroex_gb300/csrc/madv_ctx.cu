@@ -2690,6 +2690,8 @@ int madv_set_option(madv_ctx* h, const char* key, int value) {
         for (auto* c : H.L) c->comp_streams = value != 0;
     } else if (k == "es_inline") {
         for (auto* c : H.L) c->es_inline = value != 0;
+    } else if (k == "mg_block_cycle") {
+        for (auto* c : H.L) c->mg_block_cycle = value != 0;
     } else if (k.rfind("sweep_tile_", 0) == 0 && k.size() == 13 && k[11] >= '0' && k[11] <= '2' &&
                (k[12] == 'a' || k[12] == 'b')) {
         if (value < 1 || value > 256) return MADV_ERR_PARAM;

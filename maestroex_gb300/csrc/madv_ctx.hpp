@@ -194,6 +194,9 @@ struct Ctx {
     // option "es_inline": MakeEdgeScal's edge kernels form the predictor's l / r from Ip / Im
     // and only the upwind state is stored (ppm_type 1 / 2, outside the adjoint's tape)
     bool es_inline = true;
+    // option "mg_block_cycle": the MAC multigrid's V-cycle from the first grid of at most 4096
+    // cells down runs in one thread block (one launch per cycle instead of ~170)
+    bool mg_block_cycle = true;
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::map<int, double*> side_scratch;

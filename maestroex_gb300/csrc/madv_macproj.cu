@@ -159,7 +159,25 @@ __global__ void k_mg_prep_diag(MGGrid g, MGBC bc) {
     g.idiag[c] = diag > 0.0 ? 1.0 / diag : 0.0;
 }
 
-// Gauss-Seidel on the cells of one colour ((i + j + k) % 2 == color), from the stored weights
+// Gauss-Seidel update of cell (i,j,k), from the stored weights
+__device__ __forceinline__ void mg_smooth_cell(const MGGrid& g, const MGBC& bc, int i, int j, int k) {
+    const long c = mg_cell(g, i, j, k);
+    const double id = g.idiag[c];
+    if (id > 0.0) g.phi[c] = (g.rhs[c] + mg_off(g, bc, g.phi, i, j, k)) * id;
+}
+__device__ __forceinline__ void mg_resid_cell(const MGGrid& g, const MGBC& bc, int i, int j, int k) {
+    const long c = mg_cell(g, i, j, k);
+    g.res[c] = g.rhs[c] - (g.diag[c] * g.phi[c] - mg_off(g, bc, g.phi, i, j, k));
+}
+__device__ __forceinline__ void mg_restrict_cell(const MGGrid& f, const MGGrid& cg, int I, int J, int K) {
+    double s = 0.0;
+    for (int q = 0; q < 8; ++q) s += f.res[mg_cell(f, 2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2))];
+    const long c = mg_cell(cg, I, J, K);
+    cg.rhs[c] = 0.125 * s;
+    cg.phi[c] = 0.0;
+}
+
+// Gauss-Seidel on the cells of one colour ((i + j + k) % 2 == color)
 __global__ void k_mg_smooth(MGGrid g, MGBC bc, int color) {
     const long half = (long)g.n[0] * g.n[1] * g.n[2] / 2;
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -167,10 +185,7 @@ __global__ void k_mg_smooth(MGGrid g, MGBC bc, int color) {
     // the t-th cell of the colour: rows of n[0] cells hold n[0]/2 of each colour
     const long row = t / (g.n[0] / 2);
     const int jj = (int)(row % g.n[1]), kk = (int)(row / g.n[1]);
-    const int ii = 2 * (int)(t % (g.n[0] / 2)) + ((jj + kk + color) & 1);
-    const long c = mg_cell(g, ii, jj, kk);
-    const double id = g.idiag[c];
-    if (id > 0.0) g.phi[c] = (g.rhs[c] + mg_off(g, bc, g.phi, ii, jj, kk)) * id;
+    mg_smooth_cell(g, bc, 2 * (int)(t % (g.n[0] / 2)) + ((jj + kk + color) & 1), jj, kk);
 }
 
 // res = rhs - A phi
@@ -179,7 +194,7 @@ __global__ void k_mg_resid(MGGrid g, MGBC bc) {
     if (c >= (long)g.n[0] * g.n[1] * g.n[2]) return;
     int i, j, k;
     mg_ijk(g, c, i, j, k);
-    g.res[c] = g.rhs[c] - (g.diag[c] * g.phi[c] - mg_off(g, bc, g.phi, i, j, k));
+    mg_resid_cell(g, bc, i, j, k);
 }
 
 // coarse rhs = mean of the 8 fine residuals; coarse phi = 0
@@ -188,10 +203,7 @@ __global__ void k_mg_restrict(MGGrid f, MGGrid cg) {
     if (c >= (long)cg.n[0] * cg.n[1] * cg.n[2]) return;
     int I, J, K;
     mg_ijk(cg, c, I, J, K);
-    double s = 0.0;
-    for (int q = 0; q < 8; ++q) s += f.res[mg_cell(f, 2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2))];
-    cg.rhs[c] = 0.125 * s;
-    cg.phi[c] = 0.0;
+    mg_restrict_cell(f, cg, I, J, K);
 }
 
 // coarse face coefficient = mean of the 4 fine faces it covers
@@ -217,12 +229,73 @@ __global__ void k_mg_coarsen_b(MGGrid f, MGGrid cg) {
 }
 
 // fine phi += coarse phi (piecewise constant)
+__device__ __forceinline__ void mg_prolong_cell(const MGGrid& cg, const MGGrid& f, int i, int j, int k) {
+    f.phi[mg_cell(f, i, j, k)] += cg.phi[mg_cell(cg, i / 2, j / 2, k / 2)];
+}
 __global__ void k_mg_prolong(MGGrid cg, MGGrid f) {
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (long)f.n[0] * f.n[1] * f.n[2]) return;
     int i, j, k;
     mg_ijk(f, c, i, j, k);
-    f.phi[c] += cg.phi[mg_cell(cg, i / 2, j / 2, k / 2)];
+    mg_prolong_cell(cg, f, i, j, k);
+}
+
+// The V-cycle from a grid of at most MG_BLOCK_CELLS cells down, in one thread block: the
+// same per-cell smoothing, residual, restriction and prolongation as the launches of
+// mg_vcycle, in the same order (a colour's update reads only the other colour, so the order
+// within a sweep does not matter), with the block synchronised between steps.  The result
+// is bitwise that of one launch per step; the coarse levels' ~170 launches of a few cells
+// each become one.
+constexpr long MG_BLOCK_CELLS = 4096;
+constexpr int MG_BLOCK_LEVELS = 12;
+constexpr int MG_BLOCK_THREADS = 1024;
+struct MGStack {
+    MGGrid g[MG_BLOCK_LEVELS];
+    int n;
+};
+
+__device__ void mgb_smooth(const MGGrid& g, const MGBC& bc, int color) {
+    const int nh = g.n[0] / 2, tot = nh * g.n[1] * g.n[2];
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        const int row = t / nh, jj = row % g.n[1], kk = row / g.n[1];
+        mg_smooth_cell(g, bc, 2 * (t % nh) + ((jj + kk + color) & 1), jj, kk);
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(MG_BLOCK_THREADS) k_mg_block_cycle(MGStack S, MGBC bc, int nu, int bottom) {
+    const int last = S.n - 1;
+    for (int l = 0; l < last; ++l) {
+        const MGGrid& g = S.g[l];
+        const MGGrid& cg = S.g[l + 1];
+        for (int s = 0; s < nu; ++s) {
+            mgb_smooth(g, bc, 0);
+            mgb_smooth(g, bc, 1);
+        }
+        const int n = g.n[0] * g.n[1] * g.n[2];
+        for (int c = threadIdx.x; c < n; c += blockDim.x)
+            mg_resid_cell(g, bc, c % g.n[0], (c / g.n[0]) % g.n[1], c / (g.n[0] * g.n[1]));
+        __syncthreads();
+        const int nc = cg.n[0] * cg.n[1] * cg.n[2];
+        for (int c = threadIdx.x; c < nc; c += blockDim.x)
+            mg_restrict_cell(g, cg, c % cg.n[0], (c / cg.n[0]) % cg.n[1], c / (cg.n[0] * cg.n[1]));
+        __syncthreads();
+    }
+    for (int s = 0; s < bottom; ++s) {
+        mgb_smooth(S.g[last], bc, 0);
+        mgb_smooth(S.g[last], bc, 1);
+    }
+    for (int l = last - 1; l >= 0; --l) {
+        const MGGrid& g = S.g[l];
+        const int n = g.n[0] * g.n[1] * g.n[2];
+        for (int c = threadIdx.x; c < n; c += blockDim.x)
+            mg_prolong_cell(S.g[l + 1], g, c % g.n[0], (c / g.n[0]) % g.n[1], c / (g.n[0] * g.n[1]));
+        __syncthreads();
+        for (int s = 0; s < nu; ++s) {
+            mgb_smooth(g, bc, 1);
+            mgb_smooth(g, bc, 0);
+        }
+    }
 }
 
 // out_max = max |x| (bit pattern of a non-negative double); part[block] = the block's sum of
@@ -533,11 +606,29 @@ static void mg_smooth(Ctx& c, const MGGrid& g, const MGBC& bc, int color) {
     c.launches++;
 }
 
+static void mg_resid(Ctx& c, const MGGrid& g, const MGBC& bc) {
+    k_mg_resid<<<blocks_of(ncell(g)), TPB, 0, c.stream>>>(g, bc);
+    c.launches++;
+}
+
+static int mg_bottom_sweeps(const MGGrid& g) {  // the coarsest grid: to convergence
+    const int nmax = std::max(g.n[0], std::max(g.n[1], g.n[2]));
+    return std::min(2000, std::max(64, 2 * nmax * nmax));
+}
+
 static void mg_vcycle(Ctx& c, const MGBC& bc, int l) {
     MacMG& M = *c.mac;
     const MGGrid& g = M.lev[l];
-    const int nmax = std::max(g.n[0], std::max(g.n[1], g.n[2]));
-    const int nu = 2, bottom = std::min(2000, std::max(64, 2 * nmax * nmax));  // the coarsest grid: to convergence
+    const int nu = 2, bottom = mg_bottom_sweeps(g);
+    const int nrest = (int)M.lev.size() - l;
+    if (c.mg_block_cycle && ncell(g) <= MG_BLOCK_CELLS && nrest <= MG_BLOCK_LEVELS) {
+        MGStack S{};
+        S.n = nrest;
+        for (int q = 0; q < nrest; ++q) S.g[q] = M.lev[l + q];
+        k_mg_block_cycle<<<1, MG_BLOCK_THREADS, 0, c.stream>>>(S, bc, nu, mg_bottom_sweeps(M.lev.back()));
+        c.launches++;
+        return;
+    }
     if (l + 1 == (int)M.lev.size()) {
         for (int s = 0; s < bottom; ++s) {
             mg_smooth(c, g, bc, 0);
@@ -550,9 +641,9 @@ static void mg_vcycle(Ctx& c, const MGBC& bc, int l) {
         mg_smooth(c, g, bc, 1);
     }
     const MGGrid& cg = M.lev[l + 1];
-    k_mg_resid<<<blocks_of(ncell(g)), TPB, 0, c.stream>>>(g, bc);
+    mg_resid(c, g, bc);
     k_mg_restrict<<<blocks_of(ncell(cg)), TPB, 0, c.stream>>>(g, cg);
-    c.launches += 2;
+    c.launches++;
     mg_vcycle(c, bc, l + 1);
     k_mg_prolong<<<blocks_of(ncell(g)), TPB, 0, c.stream>>>(cg, g);
     c.launches++;
@@ -723,8 +814,7 @@ int mac_project_level(Ctx& c, int srhs, int srho, int sphi, const double* beta0,
     double res_max = 0.0;
     if (!c.sph) {  // V-cycles on the residual equation until the reference's stopping test holds
         while (true) {
-            k_mg_resid<<<blocks_of(n), TPB, 0, c.stream>>>(g, bc);
-            c.launches++;
+            mg_resid(c, g, bc);
             if ((rc = mg_norms(c, g.res, n, res_max, nullptr))) return rc;
             if (res_max <= target || it >= max_iter) break;
             mg_vcycle(c, bc, 0);

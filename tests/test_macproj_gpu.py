@@ -51,8 +51,10 @@ def inputs(bc, n=(32, 32, 48), max_grid=16, seed=20261203 + 70):
     return cfg, umac, rho, beta0, macrhs
 
 
-def run_gpu(cfg, umac, rho, beta0, macrhs, tol=1e-12):
+def run_gpu(cfg, umac, rho, beta0, macrhs, tol=1e-12, options=None):
     st = make_stage(cfg)
+    for k, v in (options or {}).items():
+        st.set_option(k, v)
     boxes = cfg["boxes"]
     um = [MultiFab(boxes, 1, 1, nodal=d) for d in range(3)]
     for d in range(3):
@@ -135,6 +137,22 @@ def test_mac_projection_on_extents_that_are_not_powers_of_two(case):
     err = max(float(np.abs(g - r).max()) for g, r in zip(gpu, ref)) / umax
     assert ratio <= 1e-12 and 1 <= it <= 40, (it, ratio)
     assert err <= 1e-8
+
+
+@pytest.mark.parametrize("case,n", [(c, (64, 64, 48)) for c in sorted(CASES)] +
+                         [("walls_z", (40, 40, 60)), ("periodic_xy_outflow_z", (128, 128, 128))])
+def test_mac_block_cycle_is_bitwise_the_launch_per_step_cycle(case, n):
+    """The V-cycle's coarse grids (<= 4096 cells) in one thread block (option mg_block_cycle,
+    the default) give the same bits as one launch per sweep, residual, restriction and
+    prolongation: the same per-cell arithmetic in the same order."""
+    bc = CASES[case]
+    cfg, umac, rho, beta0, macrhs = inputs(bc, n=n, max_grid=32 if n[0] % 32 == 0 else 20)
+    a = run_gpu(cfg, umac, rho, beta0, macrhs, options={"mg_block_cycle": 1})
+    b = run_gpu(cfg, umac, rho, beta0, macrhs, options={"mg_block_cycle": 0})
+    assert a[2] == b[2] and a[3] == b[3]
+    for x, y in zip(a[0], b[0]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a[1], b[1])
 
 
 def test_mac_projection_removes_an_analytic_gradient():
